@@ -1,0 +1,424 @@
+"""Seeded scene descriptions (``odegpuScene``) and the workload generators.
+
+A :class:`Scene` owns numpy arrays laid out exactly as ``include/odegpu_scene.h``
+describes and exposes them as a ctypes ``odegpuScene`` for libodegpu (and for
+the CPU oracle used by the tests). Generators build the workloads this project
+measures; each uses numpy's PCG64 generator with an explicit seed so every
+consumer sees identical inputs.
+
+Mass properties follow ODE's dMassSetBox / dMassSetSphere formulas
+(ode/src/mass.cpp:118-124, :201-215) evaluated in FP64.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+
+import numpy as np
+
+GEOM_SPHERE, GEOM_BOX, GEOM_CAPSULE, GEOM_PLANE, GEOM_HEIGHTFIELD = 0, 1, 2, 4, 9
+JOINT_BALL, JOINT_HINGE, JOINT_CONTACT, JOINT_HINGE2 = 1, 2, 4, 6
+BODY_GYROSCOPIC, BODY_NO_GRAVITY = 1, 2
+
+CONTACT_MU2 = 0x001
+CONTACT_BOUNCE = 0x004
+CONTACT_SOFT_ERP = 0x008
+CONTACT_SOFT_CFM = 0x010
+CONTACT_APPROX1 = 0x3000
+
+GEOM_NPARAM = 4
+JOINT_NPARAM = 20
+INF = float("inf")
+
+
+class Surface(C.Structure):
+    _fields_ = [("mode", C.c_int)] + [(n, C.c_double) for n in (
+        "mu", "mu2", "bounce", "bounce_vel", "soft_erp", "soft_cfm",
+        "motion1", "motion2", "motionN", "slip1", "slip2")]
+
+
+class WorldParams(C.Structure):
+    _fields_ = [("gravity", C.c_double * 3), ("erp", C.c_double), ("cfm", C.c_double),
+                ("iterations", C.c_int), ("sor_w", C.c_double), ("max_vel", C.c_double),
+                ("min_depth", C.c_double), ("dt", C.c_double), ("max_contacts", C.c_int),
+                ("seed", C.c_uint)]
+
+
+class Heightfield(C.Structure):
+    _fields_ = [("nx", C.c_int), ("nz", C.c_int), ("width", C.c_double), ("depth", C.c_double),
+                ("scale", C.c_double), ("offset", C.c_double), ("thickness", C.c_double),
+                ("wrap", C.c_int), ("heights", C.POINTER(C.c_double)),
+                ("pos", C.c_double * 3), ("R", C.c_double * 9)]
+
+
+_P = C.POINTER
+
+
+class CScene(C.Structure):
+    _fields_ = [
+        ("n_worlds", C.c_int),
+        ("body_off", _P(C.c_int)), ("geom_off", _P(C.c_int)), ("joint_off", _P(C.c_int)),
+        ("world", _P(WorldParams)),
+        ("body_pos", _P(C.c_double)), ("body_q", _P(C.c_double)), ("body_lvel", _P(C.c_double)),
+        ("body_avel", _P(C.c_double)), ("body_mass", _P(C.c_double)), ("body_I", _P(C.c_double)),
+        ("body_flags", _P(C.c_int)),
+        ("geom_type", _P(C.c_int)), ("geom_body", _P(C.c_int)), ("geom_param", _P(C.c_double)),
+        ("geom_surface", _P(C.c_int)),
+        ("surfaces", _P(Surface)), ("n_surfaces", C.c_int),
+        ("heightfields", _P(Heightfield)), ("n_heightfields", C.c_int),
+        ("joint_type", _P(C.c_int)), ("joint_body", _P(C.c_int)), ("joint_anchor", _P(C.c_double)),
+        ("joint_axis1", _P(C.c_double)), ("joint_axis2", _P(C.c_double)),
+        ("joint_param", _P(C.c_double)),
+        ("n_ctrl_steps", C.c_int), ("joint_torque", _P(C.c_double)), ("body_force", _P(C.c_double)),
+    ]
+
+
+def _ptr(a, ctype):
+    if a is None:
+        return C.cast(None, _P(ctype))
+    return a.ctypes.data_as(_P(ctype))
+
+
+def box_mass(density, lx, ly, lz):
+    """dMassSetBox (ode/src/mass.cpp:201-215): mass and diagonal inertia."""
+    m = lx * ly * lz * density
+    return m, np.diag([m / 12.0 * (ly * ly + lz * lz), m / 12.0 * (lx * lx + lz * lz),
+                       m / 12.0 * (lx * lx + ly * ly)])
+
+
+def box_mass_total(m, lx, ly, lz):
+    return m, np.diag([m / 12.0 * (ly * ly + lz * lz), m / 12.0 * (lx * lx + lz * lz),
+                       m / 12.0 * (lx * lx + ly * ly)])
+
+
+def sphere_mass(density, r):
+    """dMassSetSphere (ode/src/mass.cpp:118-124)."""
+    m = (4.0 / 3.0) * math.pi * r * r * r * density
+    return sphere_mass_total(m, r)
+
+
+def sphere_mass_total(m, r):
+    ii = 0.4 * m * r * r
+    return m, np.diag([ii, ii, ii])
+
+
+class SceneBuilder:
+    """Accumulates worlds object by object; :meth:`build` freezes into a Scene."""
+
+    def __init__(self):
+        self.worlds = []
+        self.surfaces = []
+        self.heightfields = []   # (Heightfield kwargs, heights array)
+
+    def add_surface(self, mode, mu, mu2=0.0, bounce=0.0, bounce_vel=0.0, soft_erp=0.0,
+                    soft_cfm=0.0):
+        self.surfaces.append(dict(mode=mode, mu=mu, mu2=mu2, bounce=bounce,
+                                  bounce_vel=bounce_vel, soft_erp=soft_erp, soft_cfm=soft_cfm))
+        return len(self.surfaces) - 1
+
+    def add_heightfield(self, heights, width, depth, scale=1.0, offset=0.0, thickness=1.0,
+                        wrap=0, pos=(0, 0, 0), R=np.eye(3)):
+        h = np.ascontiguousarray(heights, dtype=np.float64)
+        self.heightfields.append((dict(nx=h.shape[1], nz=h.shape[0], width=width, depth=depth,
+                                       scale=scale, offset=offset, thickness=thickness,
+                                       wrap=wrap, pos=tuple(pos),
+                                       R=tuple(np.asarray(R, float).ravel())), h))
+        return len(self.heightfields) - 1
+
+    def new_world(self, gravity=(0, 0, -9.81), erp=0.2, cfm=1e-5, iterations=20, sor_w=1.3,
+                  max_vel=INF, min_depth=0.0, dt=0.01, max_contacts=4, seed=0):
+        w = dict(params=dict(gravity=gravity, erp=erp, cfm=cfm, iterations=iterations,
+                             sor_w=sor_w, max_vel=max_vel, min_depth=min_depth, dt=dt,
+                             max_contacts=max_contacts, seed=seed),
+                 bodies=[], geoms=[], joints=[])
+        self.worlds.append(w)
+        return w
+
+    @staticmethod
+    def add_body(w, pos, mass, I, q=(1, 0, 0, 0), lvel=(0, 0, 0), avel=(0, 0, 0),
+                 flags=BODY_GYROSCOPIC):
+        w["bodies"].append(dict(pos=pos, q=q, lvel=lvel, avel=avel, mass=mass,
+                                I=np.asarray(I, float).reshape(9), flags=flags))
+        return len(w["bodies"]) - 1
+
+    @staticmethod
+    def add_geom(w, gtype, body, param, surface=0):
+        p = list(param) + [0.0] * (GEOM_NPARAM - len(param))
+        w["geoms"].append(dict(type=gtype, body=body, param=p, surface=surface))
+        return len(w["geoms"]) - 1
+
+    @staticmethod
+    def add_joint(w, jtype, b1, b2, anchor=(0, 0, 0), axis1=(1, 0, 0), axis2=(0, 1, 0),
+                  param=None):
+        p = np.zeros(JOINT_NPARAM)
+        if param is not None:
+            p[:len(param)] = param
+        w["joints"].append(dict(type=jtype, b=(b1, b2), anchor=anchor, axis1=axis1,
+                                axis2=axis2, param=p))
+        return len(w["joints"]) - 1
+
+    def build(self):
+        return Scene(self)
+
+
+def limot_params(lostop=-INF, histop=INF, vel=0.0, fmax=0.0, fudge=1.0, bounce=0.0,
+                 cfm=1e-5, stop_erp=0.2, stop_cfm=1e-5):
+    return [lostop, histop, vel, fmax, fudge, bounce, cfm, stop_erp, stop_cfm]
+
+
+class Scene:
+    """Frozen, contiguous arrays + the ctypes view (``self.c``)."""
+
+    def __init__(self, b: SceneBuilder):
+        W = b.worlds
+        self.n_worlds = len(W)
+        nbs = [len(w["bodies"]) for w in W]
+        ngs = [len(w["geoms"]) for w in W]
+        njs = [len(w["joints"]) for w in W]
+        self.body_off = np.concatenate([[0], np.cumsum(nbs)]).astype(np.int32)
+        self.geom_off = np.concatenate([[0], np.cumsum(ngs)]).astype(np.int32)
+        self.joint_off = np.concatenate([[0], np.cumsum(njs)]).astype(np.int32)
+        bodies = [bd for w in W for bd in w["bodies"]]
+        geoms = [g for w in W for g in w["geoms"]]
+        joints = [j for w in W for j in w["joints"]]
+        f64 = np.float64
+
+        def arr(key, objs, width, dtype=f64):
+            if not objs:
+                return np.zeros((1, width) if width else 1, dtype=dtype)
+            return np.ascontiguousarray(np.array([o[key] for o in objs], dtype=dtype))
+
+        self.body_pos = arr("pos", bodies, 3)
+        self.body_q = arr("q", bodies, 4)
+        self.body_lvel = arr("lvel", bodies, 3)
+        self.body_avel = arr("avel", bodies, 3)
+        self.body_mass = arr("mass", bodies, 0)
+        self.body_I = arr("I", bodies, 9)
+        self.body_flags = arr("flags", bodies, 0, np.int32)
+        self.geom_type = arr("type", geoms, 0, np.int32)
+        self.geom_body = arr("body", geoms, 0, np.int32)
+        self.geom_param = arr("param", geoms, GEOM_NPARAM)
+        self.geom_surface = arr("surface", geoms, 0, np.int32)
+        self.joint_type = arr("type", joints, 0, np.int32)
+        self.joint_body = arr("b", joints, 2, np.int32)
+        self.joint_anchor = arr("anchor", joints, 3)
+        self.joint_axis1 = arr("axis1", joints, 3)
+        self.joint_axis2 = arr("axis2", joints, 3)
+        self.joint_param = arr("param", joints, JOINT_NPARAM)
+        self.world_params = (WorldParams * max(1, self.n_worlds))()
+        for i, w in enumerate(W):
+            p = w["params"]
+            wp = self.world_params[i]
+            wp.gravity[:] = list(p["gravity"])
+            for k in ("erp", "cfm", "iterations", "sor_w", "max_vel", "min_depth", "dt",
+                      "max_contacts", "seed"):
+                setattr(wp, k, p[k])
+        surfs = b.surfaces or [dict(mode=0, mu=0.0)]
+        self.surfaces = (Surface * len(surfs))()
+        for i, s in enumerate(surfs):
+            for k, v in s.items():
+                setattr(self.surfaces[i], k, v)
+        self.hf_heights = [h for _, h in b.heightfields]
+        self.heightfields = (Heightfield * max(1, len(b.heightfields)))()
+        for i, (kw, h) in enumerate(b.heightfields):
+            H = self.heightfields[i]
+            for k in ("nx", "nz", "width", "depth", "scale", "offset", "thickness", "wrap"):
+                setattr(H, k, kw[k])
+            H.heights = h.ctypes.data_as(_P(C.c_double))
+            H.pos[:] = list(kw["pos"])
+            H.R[:] = list(kw["R"])
+        self.n_heightfields = len(b.heightfields)
+        self.n_ctrl_steps = 0
+        self.joint_torque = None
+        self.body_force = None
+        self.nb_total = int(self.body_off[-1])
+        self.nj_total = int(self.joint_off[-1])
+        self.ng_total = int(self.geom_off[-1])
+        self._refresh()
+
+    def set_controls(self, joint_torque=None, body_force=None):
+        """Per-step controls: joint_torque [S][nj_total][2], body_force [S][nb_total][6]."""
+        S = 0
+        if joint_torque is not None:
+            self.joint_torque = np.ascontiguousarray(joint_torque, dtype=np.float64)
+            S = self.joint_torque.shape[0]
+        if body_force is not None:
+            self.body_force = np.ascontiguousarray(body_force, dtype=np.float64)
+            S = self.body_force.shape[0]
+        self.n_ctrl_steps = S
+        self._refresh()
+
+    def _refresh(self):
+        c = CScene()
+        c.n_worlds = self.n_worlds
+        c.body_off = _ptr(self.body_off, C.c_int)
+        c.geom_off = _ptr(self.geom_off, C.c_int)
+        c.joint_off = _ptr(self.joint_off, C.c_int)
+        c.world = C.cast(self.world_params, _P(WorldParams))
+        for k in ("body_pos", "body_q", "body_lvel", "body_avel", "body_mass", "body_I",
+                  "geom_param", "joint_anchor", "joint_axis1", "joint_axis2", "joint_param"):
+            setattr(c, k, _ptr(getattr(self, k), C.c_double))
+        for k in ("body_flags", "geom_type", "geom_body", "geom_surface", "joint_type",
+                  "joint_body"):
+            setattr(c, k, _ptr(getattr(self, k), C.c_int))
+        c.surfaces = C.cast(self.surfaces, _P(Surface))
+        c.n_surfaces = len(self.surfaces)
+        c.heightfields = C.cast(self.heightfields, _P(Heightfield))
+        c.n_heightfields = self.n_heightfields
+        c.n_ctrl_steps = self.n_ctrl_steps
+        c.joint_torque = _ptr(self.joint_torque, C.c_double)
+        c.body_force = _ptr(self.body_force, C.c_double)
+        self.c = c
+
+    def world_bodies(self, w):
+        return int(self.body_off[w]), int(self.body_off[w + 1])
+
+    def world_joints(self, w):
+        return int(self.joint_off[w]), int(self.joint_off[w + 1])
+
+
+# --------------------------------------------------------------------------
+# workload generators
+
+def _std_surface(b, mu=0.5):
+    return b.add_surface(CONTACT_APPROX1 | CONTACT_SOFT_ERP | CONTACT_SOFT_CFM, mu,
+                         soft_erp=0.2, soft_cfm=1e-5)
+
+
+def box_drop(seed=0, n_boxes=20, steps_hint=200):
+    """20 boxes, edges U[0.2,1.0] m, density 1000, x,y in U[-3,3], z in U[0.5,5],
+    identity orientation, onto plane z=0; g=-9.81, dt=0.01, 20 iterations, w=1.3,
+    mu=0.5, Approx1|SoftERP|SoftCFM, soft_erp 0.2, soft_cfm 1e-5, <=4 contacts."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    b = SceneBuilder()
+    s = _std_surface(b, 0.5)
+    w = b.new_world(cfm=1e-5, seed=seed & 0xFFFFFFFF)
+    b.add_geom(w, GEOM_PLANE, -1, (0, 0, 1, 0), s)
+    for _ in range(n_boxes):
+        lx, ly, lz = rng.uniform(0.2, 1.0, 3)
+        x, y = rng.uniform(-3, 3, 2)
+        z = rng.uniform(0.5, 5)
+        m, I = box_mass(1000.0, lx, ly, lz)
+        bi = b.add_body(w, (x, y, z), m, I)
+        b.add_geom(w, GEOM_BOX, bi, (lx, ly, lz), s)
+    return b.build()
+
+
+def batched_worlds(n_worlds=4096, seed=1, nmin=4, nmax=64):
+    """Independent worlds of uneven size: N in [4,64] log-uniform bodies per world,
+    each a sphere (r U[0.1,0.5]) or a box (edges U[0.2,1.0]) with p=0.5, density
+    1000, on plane z=0; about 25% of bodies linked into ball-joint chains of 2-6
+    links. Surface and stepping as in box_drop. Bodies are placed with x,y in
+    U[-3,3], z in U[0.5,5]; chain links are laid out along x from their first
+    body, 0.6 m apart, ball anchors midway."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    b = SceneBuilder()
+    s = _std_surface(b, 0.5)
+    lo, hi = math.log(nmin), math.log(nmax + 1)
+    for wi in range(n_worlds):
+        n = int(math.floor(math.exp(rng.uniform(lo, hi))))
+        n = max(nmin, min(nmax, n))
+        w = b.new_world(cfm=1e-5, seed=int(rng.integers(0, 2**32)))
+        b.add_geom(w, GEOM_PLANE, -1, (0, 0, 1, 0), s)
+        # decide chains: pick ~25% of the bodies, group them into chains of 2..6
+        n_chain_bodies = int(round(0.25 * n))
+        chains = []
+        left = n_chain_bodies
+        while left >= 2:
+            L = int(rng.integers(2, 7))
+            L = min(L, left)
+            chains.append(L)
+            left -= L
+        chain_start = {}
+        idx = 0
+        for L in chains:
+            chain_start[idx] = L
+            idx += L
+        i = 0
+        while i < n:
+            L = chain_start.get(i, 1)
+            x0, y0 = rng.uniform(-3, 3, 2)
+            z0 = rng.uniform(0.5, 5)
+            prev = -1
+            for k in range(L):
+                pos = (x0 + 0.6 * k, y0, z0)
+                if rng.uniform() < 0.5:
+                    r = rng.uniform(0.1, 0.5)
+                    m, I = sphere_mass(1000.0, r)
+                    bi = b.add_body(w, pos, m, I)
+                    b.add_geom(w, GEOM_SPHERE, bi, (r,), s)
+                else:
+                    lx, ly, lz = rng.uniform(0.2, 1.0, 3)
+                    m, I = box_mass(1000.0, lx, ly, lz)
+                    bi = b.add_body(w, pos, m, I)
+                    b.add_geom(w, GEOM_BOX, bi, (lx, ly, lz), s)
+                if prev >= 0:
+                    anchor = (x0 + 0.6 * k - 0.3, y0, z0)
+                    b.add_joint(w, JOINT_BALL, prev, bi, anchor=anchor, param=(0.2, 1e-5))
+                prev = bi
+            i += L
+    return b.build()
+
+
+def box_stack(n_worlds=1, height=5, seed=3, spacing=0.0):
+    """Non-chaotic stacks: `height` unit boxes (0.5 m, density 1000) resting
+    exactly on each other on plane z=0, tiny seeded horizontal offsets (<1 mm)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    b = SceneBuilder()
+    s = _std_surface(b, 0.5)
+    for wi in range(n_worlds):
+        w = b.new_world(cfm=1e-5, seed=int(rng.integers(0, 2**32)))
+        b.add_geom(w, GEOM_PLANE, -1, (0, 0, 1, 0), s)
+        L = 0.5
+        for k in range(height):
+            m, I = box_mass(1000.0, L, L, L)
+            dx, dy = rng.uniform(-1e-3, 1e-3, 2)
+            bi = b.add_body(w, (dx + spacing * wi, dy, L / 2 + k * L - 1e-3 * (k + 1)), m, I)
+            b.add_geom(w, GEOM_BOX, bi, (L, L, L), s)
+    return b.build()
+
+
+def hinge_chains(n_worlds=1024, links=8, seed=4, steps=100):
+    """Differentiable batch: each world an 8-link hinge chain of 0.5x0.1x0.1 m,
+    1 kg boxes along x, the first link hinged to the static environment, hinge
+    axes along y, initial joint angles U[-0.5,0.5] rad (applied as a planar
+    rotation about y accumulated down the chain) and joint rates U[-1,1] rad/s;
+    per-step hinge torques U[-2,2] N m; the end link can touch plane z=-2."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    b = SceneBuilder()
+    s = _std_surface(b, 0.5)
+    L = 0.5
+    for wi in range(n_worlds):
+        w = b.new_world(cfm=1e-5, seed=int(rng.integers(0, 2**32)))
+        b.add_geom(w, GEOM_PLANE, -1, (0, 0, 1, -2.0), s)
+        angles = rng.uniform(-0.5, 0.5, links)
+        rates = rng.uniform(-1.0, 1.0, links)
+        theta = 0.0
+        omega = 0.0
+        joint_pt = np.zeros(3)
+        vel_pt = np.zeros(3)
+        prev = -1
+        for k in range(links):
+            theta += angles[k]
+            omega += rates[k]
+            # link direction in the x-z plane after rotating about y by theta
+            d = np.array([math.cos(theta), 0.0, -math.sin(theta)])
+            center = joint_pt + 0.5 * L * d
+            # rotation about y by theta: q = (cos(t/2), 0, sin(t/2), 0)
+            q = (math.cos(theta / 2), 0.0, math.sin(theta / 2), 0.0)
+            wvec = np.array([0.0, omega, 0.0])
+            vcenter = vel_pt + np.cross(wvec, center - joint_pt)
+            m, I = box_mass_total(1.0, L, 0.1, 0.1)
+            bi = b.add_body(w, tuple(center), m, I, q=q, lvel=tuple(vcenter), avel=tuple(wvec))
+            b.add_geom(w, GEOM_BOX, bi, (L, 0.1, 0.1), s)
+            b.add_joint(w, JOINT_HINGE, prev if prev >= 0 else bi, bi if prev >= 0 else -1,
+                        anchor=tuple(joint_pt), axis1=(0, 1, 0),
+                        param=limot_params(cfm=1e-5, stop_erp=0.2, stop_cfm=1e-5))
+            vel_pt = vcenter + np.cross(wvec, joint_pt + L * d - center)
+            joint_pt = joint_pt + L * d
+            prev = bi
+    sc = b.build()
+    tq = np.zeros((steps, sc.nj_total, 2))
+    tq[:, :, 0] = rng.uniform(-2, 2, (steps, sc.nj_total))
+    sc.set_controls(joint_torque=tq)
+    return sc

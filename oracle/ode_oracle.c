@@ -1,0 +1,2081 @@
+/*
+ * ode_oracle.c -- TEST INFRASTRUCTURE ONLY: the oracle. A CPU restatement of
+ * ODE 0.12's primitive narrowphase + dWorldQuickStep step pipeline, written for
+ * this project from the reference's behaviour (not copied), in FP64. Used by
+ * tests/ as the checker, by __graft_entry__.smoke() to check one GPU step and
+ * by bench.py's CPU-baseline leg. The product never links or calls it.
+ *
+ * Pinning: tests/test_oracle_vs_ref.py checks this file against the reference
+ * ODE built from its own sources (oracle/Makefile -> oracle/_ref/) on seeded
+ * scenes; results are required to be bit-identical in FP64 (the arithmetic
+ * below follows the reference's operation order and is compiled without FMA
+ * contraction). Golden vectors from the reference are committed under
+ * tests/golden/ for hosts where the reference sources are absent.
+ */
+#define _GNU_SOURCE
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#include <pthread.h>
+#include "ode_oracle.h"
+
+typedef double real;
+#define R_INF ((real)INFINITY)
+#define R_PI 3.14159265358979323846
+#define R_SQRT1_2 0.70710678118654752440
+
+/* ------------------------------------------------------------------------ */
+/* small vector helpers; each keeps the reference's evaluation order        */
+/* (include/ode/odemath.h:44-225)                                          */
+
+static inline real dot3(const real* a, const real* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+static inline real dot3s(const real* a, const real* b, int sa, int sb) {
+  return a[0] * b[0] + a[sa] * b[sb] + a[2 * sa] * b[2 * sb];
+}
+static inline void cross3(real* r, const real* a, const real* b) {
+  real r0 = a[1] * b[2] - a[2] * b[1];
+  real r1 = a[2] * b[0] - a[0] * b[2];
+  real r2 = a[0] * b[1] - a[1] * b[0];
+  r[0] = r0; r[1] = r1; r[2] = r2;
+}
+/* res = A*b, A is 3x4 row-major (dMultiply0_331) */
+static inline void mul0_331(real* res, const real* A, const real* b) {
+  real r0 = dot3(A, b), r1 = dot3(A + 4, b), r2 = dot3(A + 8, b);
+  res[0] = r0; res[1] = r1; res[2] = r2;
+}
+/* res = A^T*b (dMultiply1_331) */
+static inline void mul1_331(real* res, const real* A, const real* b) {
+  real r0 = dot3s(A, b, 4, 1), r1 = dot3s(A + 1, b, 4, 1), r2 = dot3s(A + 2, b, 4, 1);
+  res[0] = r0; res[1] = r1; res[2] = r2;
+}
+/* res = A*B^T (dMultiply2_333): row i of res is B * (row i of A) */
+static inline void mul2_333(real* res, const real* A, const real* B) {
+  mul0_331(res + 0, B, A + 0);
+  mul0_331(res + 4, B, A + 4);
+  mul0_331(res + 8, B, A + 8);
+}
+/* res = A*B (dMultiply0_333): row i of res is B^T * (row i of A) */
+static inline void mul0_333(real* res, const real* A, const real* B) {
+  mul1_331(res + 0, B, A + 0);
+  mul1_331(res + 4, B, A + 4);
+  mul1_331(res + 8, B, A + 8);
+}
+
+/* _dSafeNormalize3, ode/src/odemath.cpp:42-83 */
+static int safe_normalize3(real* a) {
+  real aa[3];
+  int idx;
+  aa[0] = fabs(a[0]); aa[1] = fabs(a[1]); aa[2] = fabs(a[2]);
+  if (aa[1] > aa[0]) {
+    idx = (aa[2] > aa[1]) ? 2 : 1;
+  } else {
+    if (aa[2] > aa[0]) idx = 2;
+    else {
+      if (aa[0] <= 0) { a[0] = 1; a[1] = 0; a[2] = 0; return 0; }
+      idx = 0;
+    }
+  }
+  a[0] /= aa[idx]; a[1] /= aa[idx]; a[2] /= aa[idx];
+  real l = 1.0 / sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
+  a[0] *= l; a[1] *= l; a[2] *= l;
+  return 1;
+}
+/* _dSafeNormalize4, ode/src/odemath.cpp:119-138 */
+static void normalize4(real* a) {
+  real l = dot3(a, a) + a[3] * a[3];
+  if (l > 0) {
+    l = 1.0 / sqrt(l);
+    a[0] *= l; a[1] *= l; a[2] *= l; a[3] *= l;
+  } else {
+    a[0] = 1; a[1] = 0; a[2] = 0; a[3] = 0;
+  }
+}
+/* dPlaneSpace, ode/src/odemath.cpp:151-178 */
+static void plane_space(const real* n, real* p, real* q) {
+  if (fabs(n[2]) > R_SQRT1_2) {
+    real a = n[1] * n[1] + n[2] * n[2];
+    real k = 1.0 / sqrt(a);
+    p[0] = 0; p[1] = -n[2] * k; p[2] = n[1] * k;
+    q[0] = a * k; q[1] = -n[0] * p[2]; q[2] = n[0] * p[1];
+  } else {
+    real a = n[0] * n[0] + n[1] * n[1];
+    real k = 1.0 / sqrt(a);
+    p[0] = -n[1] * k; p[1] = n[0] * k; p[2] = 0;
+    q[0] = -n[2] * p[1]; q[1] = n[2] * p[0]; q[2] = a * k;
+  }
+}
+/* dRfromQ, ode/src/rotation.cpp:236-255 */
+static void r_from_q(real* R, const real* q) {
+  real qq1 = 2 * q[1] * q[1], qq2 = 2 * q[2] * q[2], qq3 = 2 * q[3] * q[3];
+  R[0] = 1 - qq2 - qq3; R[1] = 2 * (q[1] * q[2] - q[0] * q[3]); R[2] = 2 * (q[1] * q[3] + q[0] * q[2]); R[3] = 0;
+  R[4] = 2 * (q[1] * q[2] + q[0] * q[3]); R[5] = 1 - qq1 - qq3; R[6] = 2 * (q[2] * q[3] - q[0] * q[1]); R[7] = 0;
+  R[8] = 2 * (q[1] * q[3] - q[0] * q[2]); R[9] = 2 * (q[2] * q[3] + q[0] * q[1]); R[10] = 1 - qq1 - qq2; R[11] = 0;
+}
+/* dQMultiply0..3, ode/src/rotation.cpp:191-226 */
+static void qmul1(real* qa, const real* qb, const real* qc) {
+  qa[0] = qb[0] * qc[0] + qb[1] * qc[1] + qb[2] * qc[2] + qb[3] * qc[3];
+  qa[1] = qb[0] * qc[1] - qb[1] * qc[0] - qb[2] * qc[3] + qb[3] * qc[2];
+  qa[2] = qb[0] * qc[2] - qb[2] * qc[0] - qb[3] * qc[1] + qb[1] * qc[3];
+  qa[3] = qb[0] * qc[3] - qb[3] * qc[0] - qb[1] * qc[2] + qb[2] * qc[1];
+}
+static void qmul2(real* qa, const real* qb, const real* qc) {
+  qa[0] = qb[0] * qc[0] + qb[1] * qc[1] + qb[2] * qc[2] + qb[3] * qc[3];
+  qa[1] = -qb[0] * qc[1] + qb[1] * qc[0] - qb[2] * qc[3] + qb[3] * qc[2];
+  qa[2] = -qb[0] * qc[2] + qb[2] * qc[0] - qb[3] * qc[1] + qb[1] * qc[3];
+  qa[3] = -qb[0] * qc[3] + qb[3] * qc[0] - qb[1] * qc[2] + qb[2] * qc[1];
+}
+static void qmul3(real* qa, const real* qb, const real* qc) {
+  qa[0] = qb[0] * qc[0] - qb[1] * qc[1] - qb[2] * qc[2] - qb[3] * qc[3];
+  qa[1] = -qb[0] * qc[1] - qb[1] * qc[0] + qb[2] * qc[3] - qb[3] * qc[2];
+  qa[2] = -qb[0] * qc[2] - qb[2] * qc[0] + qb[3] * qc[1] - qb[1] * qc[3];
+  qa[3] = -qb[0] * qc[3] - qb[3] * qc[0] + qb[1] * qc[2] - qb[2] * qc[1];
+}
+
+/* ------------------------------------------------------------------------ */
+/* RNG: ode/src/misc.cpp:31-117 (32-bit LCG, xor-folded modulus)            */
+
+static _Thread_local unsigned int g_seed = 0;
+
+static unsigned int rand_next(void) {
+  g_seed = (unsigned int)(1664525u * g_seed + 1013904223u);
+  return g_seed;
+}
+static int rand_int(int n) {
+  const unsigned int un = (unsigned int)n;
+  unsigned int r = rand_next();
+  if (un <= 0x10u) {
+    r ^= (r >> 16); r ^= (r >> 8); r ^= (r >> 4);
+    if (un <= 0x2u) { r ^= (r >> 2); r ^= (r >> 1); }
+    else if (un <= 0x4u) { r ^= (r >> 2); }
+  } else if (un <= 0x100u) {
+    r ^= (r >> 16); r ^= (r >> 8);
+  } else if (un <= 0x10000u) {
+    r ^= (r >> 16);
+  }
+  return (int)(r % un);
+}
+void oracle_rand_set_seed(unsigned int s) { g_seed = s; }
+unsigned int oracle_rand_get_seed(void) { return g_seed; }
+int oracle_rand_int(int n) { return rand_int(n); }
+int oracle_test_rand(void) {
+  unsigned int old = g_seed;
+  int ok = 1;
+  g_seed = 0;
+  if (rand_next() != 0x3c6ef35fu || rand_next() != 0x47502932u || rand_next() != 0xd1ccf6e9u ||
+      rand_next() != 0xaaf95334u || rand_next() != 0x6252e503u)
+    ok = 0;
+  g_seed = old;
+  return ok;
+}
+
+/* ------------------------------------------------------------------------ */
+/* 3x3 SPD inverse by Cholesky, as dBodySetMass computes invI               */
+/* (ode/src/ode.cpp:492-509 -> ode/src/matrix.cpp:121-230). A, Ainv: 3x4.   */
+
+static int invert_pd3(const real* A, real* Ainv) {
+  real L[12], recip[3];
+  memcpy(L, A, sizeof(L));
+  for (int i = 0; i < 3; ++i) {
+    for (int j = 0; j < i; ++j) {
+      real sum = L[i * 4 + j];
+      for (int k = 0; k < j; ++k) sum -= L[i * 4 + k] * L[j * 4 + k];
+      L[i * 4 + j] = sum * recip[j];
+    }
+    real sum = L[i * 4 + i];
+    for (int k = 0; k < i; ++k) sum -= L[i * 4 + k] * L[i * 4 + k];
+    if (sum <= 0) return 0;
+    real s = sqrt(sum);
+    L[i * 4 + i] = s;
+    recip[i] = 1.0 / s;
+  }
+  memset(Ainv, 0, 12 * sizeof(real));
+  for (int c = 0; c < 3; ++c) {
+    real x[3] = {0, 0, 0}, y[3];
+    x[c] = 1;
+    for (int r = 0; r < 3; ++r) {
+      real sum = 0;
+      for (int k = 0; k < r; ++k) sum += L[r * 4 + k] * y[k];
+      y[r] = (x[r] - sum) / L[r * 4 + r];
+    }
+    for (int r = 2; r >= 0; --r) {
+      real sum = 0;
+      for (int k = r + 1; k < 3; ++k) sum += L[k * 4 + r] * x[k];
+      x[r] = (y[r] - sum) / L[r * 4 + r];
+    }
+    for (int r = 0; r < 3; ++r) Ainv[r * 4 + c] = x[r];
+  }
+  return 1;
+}
+
+/* ------------------------------------------------------------------------ */
+/* world model                                                              */
+
+typedef struct {
+  real pos[3], q[4], R[12];
+  real lvel[3], avel[3], facc[3], tacc[3];
+  real mass, invMass, I[12], invI[12];
+  int flags;
+  int tag;
+  int* jl; int jl_n, jl_cap, jl_persist;   /* attached joints, attach order */
+} OBody;
+
+typedef struct {
+  real vel, fmax, lostop, histop, fudge, normal_cfm, stop_erp, stop_cfm, bounce;
+  int limit; real limit_err;
+} OLimot;
+
+typedef struct {
+  int type;
+  int b[2];          /* node[0].body, node[1].body after dJointAttach */
+  int reverse;
+  int tag;
+  /* ball / hinge / hinge2 */
+  real anchor1[4], anchor2[4], axis1[4], axis2[4], qrel[4];
+  real erp, cfm;
+  OLimot lm1, lm2;
+  real c0, s0, v1[4], v2[4], susp_erp, susp_cfm;
+  /* contact */
+  odegpuSurface surf;
+  real cpos[3], cnormal[3], cdepth;
+  int the_m;
+  real fb[12];       /* joint feedback f1 t1 f2 t2 */
+} OJoint;
+
+typedef struct {
+  int type, body;
+  real p[4];     /* sphere r / box sides / capsule r,len / plane */
+  int surface;
+  const odegpuHeightfield* hf;
+  real hpos[3], hR[12];
+} OGeom;
+
+typedef struct {
+  const odegpuScene* sc;
+  int w, nb, ng, nj_persist;
+  OBody* body;
+  OGeom* geom;
+  OJoint* joint; int nj, cap_j;
+  real gravity[3], erp, cfm, sor_w, max_vel, min_depth, dt;
+  int iterations, max_contacts;
+  oracleTap* tap;
+} OWorld;
+
+static void body_attach(OBody* b, int j) {
+  if (b->jl_n == b->jl_cap) {
+    b->jl_cap = b->jl_cap ? 2 * b->jl_cap : 8;
+    b->jl = (int*)realloc(b->jl, b->jl_cap * sizeof(int));
+  }
+  b->jl[b->jl_n++] = j;
+}
+
+/* dJointAttach, ode/src/ode.cpp:1348-1399: a missing body1 moves to body2's
+ * slot and sets the reverse flag; the joint is prepended on each body's list. */
+static void joint_attach(OWorld* W, int j, int b1, int b2) {
+  OJoint* J = &W->joint[j];
+  if (b1 < 0) { b1 = b2; b2 = -1; J->reverse = 1; } else J->reverse = 0;
+  J->b[0] = b1; J->b[1] = b2;
+  if (b1 >= 0) body_attach(&W->body[b1], j);
+  if (b2 >= 0) body_attach(&W->body[b2], j);
+}
+
+/* setAnchors / setAxes, ode/src/joints/joint.cpp:260-322 */
+static void set_anchors(OWorld* W, OJoint* J, real x, real y, real z, real* a1, real* a2) {
+  if (J->b[0] >= 0) {
+    OBody* B1 = &W->body[J->b[0]];
+    real q[4] = {x - B1->pos[0], y - B1->pos[1], z - B1->pos[2], 0};
+    mul1_331(a1, B1->R, q);
+    if (J->b[1] >= 0) {
+      OBody* B2 = &W->body[J->b[1]];
+      real q2[4] = {x - B2->pos[0], y - B2->pos[1], z - B2->pos[2], 0};
+      mul1_331(a2, B2->R, q2);
+    } else {
+      a2[0] = x; a2[1] = y; a2[2] = z;
+    }
+  }
+  a1[3] = 0; a2[3] = 0;
+}
+static void set_axes(OWorld* W, OJoint* J, real x, real y, real z, real* ax1, real* ax2) {
+  if (J->b[0] >= 0) {
+    real q[4] = {x, y, z, 0};
+    safe_normalize3(q);
+    if (ax1) { mul1_331(ax1, W->body[J->b[0]].R, q); ax1[3] = 0; }
+    if (ax2) {
+      if (J->b[1] >= 0) mul1_331(ax2, W->body[J->b[1]].R, q);
+      else { ax2[0] = x; ax2[1] = y; ax2[2] = z; }
+      ax2[3] = 0;
+    }
+  }
+}
+/* dxJointHinge::computeInitialRelativeRotation, ode/src/joints/hinge.cpp:378-396 */
+static void hinge_qrel(OWorld* W, OJoint* J) {
+  if (J->b[0] >= 0) {
+    const real* q1 = W->body[J->b[0]].q;
+    if (J->b[1] >= 0) qmul1(J->qrel, q1, W->body[J->b[1]].q);
+    else { J->qrel[0] = q1[0]; J->qrel[1] = -q1[1]; J->qrel[2] = -q1[2]; J->qrel[3] = -q1[3]; }
+  }
+}
+/* dxJointHinge2::getAxisInfo / makeV1andV2, ode/src/joints/hinge2.cpp:97-106, :184-210 */
+static void hinge2_axis_info(OWorld* W, OJoint* J, real* ax1, real* ax2, real* axc, real* s, real* c) {
+  mul0_331(ax1, W->body[J->b[0]].R, J->axis1);
+  mul0_331(ax2, W->body[J->b[1]].R, J->axis2);
+  cross3(axc, ax1, ax2);
+  *s = sqrt(axc[0] * axc[0] + axc[1] * axc[1] + axc[2] * axc[2]);
+  *c = dot3(ax1, ax2);
+}
+static void hinge2_make_v(OWorld* W, OJoint* J) {
+  if (J->b[0] < 0) return;
+  real ax1[4], ax2[4], v[4];
+  mul0_331(ax1, W->body[J->b[0]].R, J->axis1);
+  mul0_331(ax2, W->body[J->b[1]].R, J->axis2);
+  if ((ax1[0] == 0 && ax1[1] == 0 && ax1[2] == 0) || (ax2[0] == 0 && ax2[1] == 0 && ax2[2] == 0) ||
+      (ax1[0] == ax2[0] && ax1[1] == ax2[1] && ax1[2] == ax2[2]))
+    return;
+  real k = dot3(ax1, ax2);
+  for (int i = 0; i < 3; ++i) ax2[i] -= k * ax1[i];
+  safe_normalize3(ax2);
+  cross3(v, ax1, ax2);
+  mul1_331(J->v1, W->body[J->b[0]].R, ax2);
+  mul1_331(J->v2, W->body[J->b[0]].R, v);
+}
+static void get_anchor(OWorld* W, OJoint* J, real* res, const real* a1) {
+  if (J->b[0] >= 0) {
+    OBody* B = &W->body[J->b[0]];
+    mul0_331(res, B->R, a1);
+    res[0] += B->pos[0]; res[1] += B->pos[1]; res[2] += B->pos[2];
+  }
+}
+static void get_anchor2(OWorld* W, OJoint* J, real* res, const real* a2) {
+  if (J->b[1] >= 0) {
+    OBody* B = &W->body[J->b[1]];
+    mul0_331(res, B->R, a2);
+    res[0] += B->pos[0]; res[1] += B->pos[1]; res[2] += B->pos[2];
+  } else {
+    res[0] = a2[0]; res[1] = a2[1]; res[2] = a2[2];
+  }
+}
+
+/* dxJointLimitMotor::init, ode/src/joints/joint.cpp:456-469 */
+static void limot_init(OLimot* L, const OWorld* W) {
+  L->vel = 0; L->fmax = 0; L->lostop = -R_INF; L->histop = R_INF; L->fudge = 1;
+  L->normal_cfm = W->cfm; L->stop_erp = W->erp; L->stop_cfm = W->cfm; L->bounce = 0;
+  L->limit = 0; L->limit_err = 0;
+}
+/* dxJointLimitMotor::set, ode/src/joints/joint.cpp:472-508, applied in the
+ * order the harness applies the parameters. */
+static void limot_set_all(OLimot* L, const double* p) {
+  L->lostop = p[0];
+  L->histop = p[1];
+  L->vel = p[2];
+  if (p[3] >= 0) L->fmax = p[3];
+  if (p[4] >= 0 && p[4] <= 1) L->fudge = p[4];
+  L->bounce = p[5];
+  L->normal_cfm = p[6];
+  L->stop_erp = p[7];
+  L->stop_cfm = p[8];
+}
+
+/* ------------------------------------------------------------------------ */
+/* colliders                                                                */
+
+typedef struct { real pos[3], normal[3], depth; } OContact;
+
+typedef struct {
+  int type;
+  const real* pos;   /* final_posr pos */
+  const real* R;     /* final_posr R (3x4) */
+  const real* p;     /* class parameters */
+  const OGeom* g;
+} GeomRef;
+
+/* dCollideSpheres, ode/src/collision_util.cpp:38-67 */
+static int collide_spheres(const real* p1, real r1, const real* p2, real r2, OContact* c) {
+  real t[3] = {p1[0] - p2[0], p1[1] - p2[1], p1[2] - p2[2]};
+  real d = sqrt(t[0] * t[0] + t[1] * t[1] + t[2] * t[2]);
+  if (d > (r1 + r2)) return 0;
+  if (d <= 0) {
+    c->pos[0] = p1[0]; c->pos[1] = p1[1]; c->pos[2] = p1[2];
+    c->normal[0] = 1; c->normal[1] = 0; c->normal[2] = 0;
+    c->depth = r1 + r2;
+  } else {
+    real d1 = 1.0 / d;
+    c->normal[0] = (p1[0] - p2[0]) * d1;
+    c->normal[1] = (p1[1] - p2[1]) * d1;
+    c->normal[2] = (p1[2] - p2[2]) * d1;
+    real k = 0.5 * (r2 - r1 - d);
+    c->pos[0] = p1[0] + c->normal[0] * k;
+    c->pos[1] = p1[1] + c->normal[1] * k;
+    c->pos[2] = p1[2] + c->normal[2] * k;
+    c->depth = r1 + r2 - d;
+  }
+  return 1;
+}
+
+/* dCollideSphereBox, ode/src/sphere.cpp:131-219 */
+static int collide_sphere_box(const GeomRef* s, const GeomRef* b, OContact* c) {
+  real l[3], t[4], p[3], q[3], r[3];
+  int onborder = 0;
+  const real* R = b->R;
+  p[0] = s->pos[0] - b->pos[0];
+  p[1] = s->pos[1] - b->pos[1];
+  p[2] = s->pos[2] - b->pos[2];
+  l[0] = b->p[0] * 0.5;
+  t[0] = dot3s(p, R, 1, 4);
+  if (t[0] < -l[0]) { t[0] = -l[0]; onborder = 1; }
+  if (t[0] > l[0]) { t[0] = l[0]; onborder = 1; }
+  l[1] = b->p[1] * 0.5;
+  t[1] = dot3s(p, R + 1, 1, 4);
+  if (t[1] < -l[1]) { t[1] = -l[1]; onborder = 1; }
+  if (t[1] > l[1]) { t[1] = l[1]; onborder = 1; }
+  t[2] = dot3s(p, R + 2, 1, 4);
+  l[2] = b->p[2] * 0.5;
+  if (t[2] < -l[2]) { t[2] = -l[2]; onborder = 1; }
+  if (t[2] > l[2]) { t[2] = l[2]; onborder = 1; }
+  if (!onborder) {
+    real min_distance = l[0] - fabs(t[0]);
+    int mini = 0;
+    for (int i = 1; i < 3; i++) {
+      real fd = l[i] - fabs(t[i]);
+      if (fd < min_distance) { min_distance = fd; mini = i; }
+    }
+    c->pos[0] = s->pos[0]; c->pos[1] = s->pos[1]; c->pos[2] = s->pos[2];
+    real tmp[3] = {0, 0, 0};
+    tmp[mini] = (t[mini] > 0) ? 1.0 : -1.0;
+    mul0_331(c->normal, R, tmp);
+    c->depth = min_distance + s->p[0];
+    return 1;
+  }
+  t[3] = 0;
+  mul0_331(q, R, t);
+  r[0] = p[0] - q[0]; r[1] = p[1] - q[1]; r[2] = p[2] - q[2];
+  real depth = s->p[0] - sqrt(dot3(r, r));
+  if (depth < 0) return 0;
+  c->pos[0] = q[0] + b->pos[0];
+  c->pos[1] = q[1] + b->pos[1];
+  c->pos[2] = q[2] + b->pos[2];
+  c->normal[0] = r[0]; c->normal[1] = r[1]; c->normal[2] = r[2];
+  safe_normalize3(c->normal);
+  c->depth = depth;
+  return 1;
+}
+
+/* dCollideSpherePlane, ode/src/sphere.cpp:222-251 */
+static int collide_sphere_plane(const GeomRef* s, const GeomRef* pl, OContact* c) {
+  const real* P = pl->p;
+  real k = dot3(s->pos, P);
+  real depth = P[3] - k + s->p[0];
+  if (depth >= 0) {
+    c->normal[0] = P[0]; c->normal[1] = P[1]; c->normal[2] = P[2];
+    c->pos[0] = s->pos[0] - P[0] * s->p[0];
+    c->pos[1] = s->pos[1] - P[1] * s->p[0];
+    c->pos[2] = s->pos[2] - P[2] * s->p[0];
+    c->depth = depth;
+    return 1;
+  }
+  return 0;
+}
+
+/* dLineClosestApproach, ode/src/collision_util.cpp:70-92 */
+static void line_closest_approach(const real* pa, const real* ua, const real* pb, const real* ub,
+                                  real* alpha, real* beta) {
+  real p[3] = {pb[0] - pa[0], pb[1] - pa[1], pb[2] - pa[2]};
+  real uaub = dot3(ua, ub);
+  real q1 = dot3(ua, p);
+  real q2 = -dot3(ub, p);
+  real d = 1 - uaub * uaub;
+  if (d <= 0.0001) { *alpha = 0; *beta = 0; }
+  else {
+    d = 1.0 / d;
+    *alpha = (q1 + uaub * q2) * d;
+    *beta = (uaub * q1 + q2) * d;
+  }
+}
+
+/* intersectRectQuad, ode/src/box.cpp:187-245: clip quad p against the
+ * rectangle |x|<h[0], |y|<h[1] with the same point-emission order. */
+static int intersect_rect_quad(const real h[2], real p[8], real ret[16]) {
+  int nq = 4, nr = 0;
+  real buffer[16];
+  real* q = p;
+  real* r = ret;
+  for (int dir = 0; dir <= 1; dir++) {
+    for (int sign = -1; sign <= 1; sign += 2) {
+      real* pq = q;
+      real* pr = r;
+      nr = 0;
+      for (int i = nq; i > 0; i--) {
+        if (sign * pq[dir] < h[dir]) {
+          pr[0] = pq[0]; pr[1] = pq[1];
+          pr += 2; nr++;
+          if (nr & 8) { q = r; goto done; }
+        }
+        real* nextq = (i > 1) ? pq + 2 : q;
+        if ((sign * pq[dir] < h[dir]) ^ (sign * nextq[dir] < h[dir])) {
+          pr[1 - dir] = pq[1 - dir] + (nextq[1 - dir] - pq[1 - dir]) / (nextq[dir] - pq[dir]) *
+                                          (sign * h[dir] - pq[dir]);
+          pr[dir] = sign * h[dir];
+          pr += 2; nr++;
+          if (nr & 8) { q = r; goto done; }
+        }
+        pq += 2;
+      }
+      q = r;
+      r = (q == ret) ? buffer : ret;
+      nq = nr;
+    }
+  }
+done:
+  if (q != ret) memcpy(ret, q, nr * 2 * sizeof(real));
+  return nr;
+}
+
+/* cullPoints, ode/src/box.cpp:249-322 */
+static void cull_points(int n, const real p[], int m, int i0, int iret[]) {
+  int i, j;
+  real a, cx, cy, q;
+  if (n == 1) { cx = p[0]; cy = p[1]; }
+  else if (n == 2) { cx = 0.5 * (p[0] + p[2]); cy = 0.5 * (p[1] + p[3]); }
+  else {
+    a = 0; cx = 0; cy = 0;
+    for (i = 0; i < (n - 1); i++) {
+      q = p[i * 2] * p[i * 2 + 3] - p[i * 2 + 2] * p[i * 2 + 1];
+      a += q;
+      cx += q * (p[i * 2] + p[i * 2 + 2]);
+      cy += q * (p[i * 2 + 1] + p[i * 2 + 3]);
+    }
+    q = p[n * 2 - 2] * p[1] - p[0] * p[n * 2 - 1];
+    a = 1.0 / (3.0 * (a + q));
+    cx = a * (cx + q * (p[n * 2 - 2] + p[0]));
+    cy = a * (cy + q * (p[n * 2 - 1] + p[1]));
+  }
+  real A[8];
+  for (i = 0; i < n; i++) A[i] = atan2(p[i * 2 + 1] - cy, p[i * 2] - cx);
+  int avail[8];
+  for (i = 0; i < n; i++) avail[i] = 1;
+  avail[i0] = 0;
+  iret[0] = i0;
+  iret++;
+  for (j = 1; j < m; j++) {
+    a = (real)((real)j * (2 * R_PI / m) + A[i0]);
+    if (a > R_PI) a -= (real)(2 * R_PI);
+    real maxdiff = 1e9, diff;
+    for (i = 0; i < n; i++) {
+      if (avail[i]) {
+        diff = fabs(A[i] - a);
+        if (diff > R_PI) diff = (real)(2 * R_PI - diff);
+        if (diff < maxdiff) { maxdiff = diff; *iret = i; }
+      }
+    }
+    avail[*iret] = 0;
+    iret++;
+  }
+}
+
+#define CONTACTS_UNIMPORTANT 0x80000000u
+
+/* dBoxBox, ode/src/box.cpp:331-713. Fills pos/depth; returns count. */
+static int box_box(const real* p1, const real* R1, const real* side1, const real* p2, const real* R2,
+                   const real* side2, real* normal, real* depth, int* return_code, unsigned flags,
+                   OContact* contact) {
+  const real fudge_factor = 1.05;
+  real p[3], pp[3], normalC[3] = {0, 0, 0};
+  const real* normalR = 0;
+  real A[3], B[3], R11, R12, R13, R21, R22, R23, R31, R32, R33, Q11, Q12, Q13, Q21, Q22, Q23, Q31, Q32,
+      Q33, s, s2, l, e1;
+  int i, j, invert_normal, code;
+
+  p[0] = p2[0] - p1[0]; p[1] = p2[1] - p1[1]; p[2] = p2[2] - p1[2];
+  mul1_331(pp, R1, p);
+  A[0] = side1[0] * 0.5; A[1] = side1[1] * 0.5; A[2] = side1[2] * 0.5;
+  B[0] = side2[0] * 0.5; B[1] = side2[1] * 0.5; B[2] = side2[2] * 0.5;
+
+  R11 = dot3s(R1 + 0, R2 + 0, 4, 4); R12 = dot3s(R1 + 0, R2 + 1, 4, 4); R13 = dot3s(R1 + 0, R2 + 2, 4, 4);
+  R21 = dot3s(R1 + 1, R2 + 0, 4, 4); R22 = dot3s(R1 + 1, R2 + 1, 4, 4); R23 = dot3s(R1 + 1, R2 + 2, 4, 4);
+  R31 = dot3s(R1 + 2, R2 + 0, 4, 4); R32 = dot3s(R1 + 2, R2 + 1, 4, 4); R33 = dot3s(R1 + 2, R2 + 2, 4, 4);
+  Q11 = fabs(R11); Q12 = fabs(R12); Q13 = fabs(R13);
+  Q21 = fabs(R21); Q22 = fabs(R22); Q23 = fabs(R23);
+  Q31 = fabs(R31); Q32 = fabs(R32); Q33 = fabs(R33);
+
+  s = -R_INF;
+  invert_normal = 0;
+  code = 0;
+  do {
+#define TST_FACE(expr1, expr2, norm, cc)          \
+  e1 = (expr1);                                   \
+  s2 = fabs(e1) - (expr2);                        \
+  if (s2 > 0) return 0;                           \
+  if (s2 > s) {                                   \
+    s = s2; normalR = norm; invert_normal = (e1 < 0); code = (cc); \
+    if (flags & CONTACTS_UNIMPORTANT) break;      \
+  }
+    TST_FACE(pp[0], (A[0] + B[0] * Q11 + B[1] * Q12 + B[2] * Q13), R1 + 0, 1);
+    TST_FACE(pp[1], (A[1] + B[0] * Q21 + B[1] * Q22 + B[2] * Q23), R1 + 1, 2);
+    TST_FACE(pp[2], (A[2] + B[0] * Q31 + B[1] * Q32 + B[2] * Q33), R1 + 2, 3);
+    TST_FACE(dot3s(R2 + 0, p, 4, 1), (A[0] * Q11 + A[1] * Q21 + A[2] * Q31 + B[0]), R2 + 0, 4);
+    TST_FACE(dot3s(R2 + 1, p, 4, 1), (A[0] * Q12 + A[1] * Q22 + A[2] * Q32 + B[1]), R2 + 1, 5);
+    TST_FACE(dot3s(R2 + 2, p, 4, 1), (A[0] * Q13 + A[1] * Q23 + A[2] * Q33 + B[2]), R2 + 2, 6);
+#undef TST_FACE
+#define TST_EDGE(expr1, expr2, n1, n2, n3, cc)              \
+  e1 = (expr1);                                             \
+  s2 = fabs(e1) - (expr2);                                  \
+  if (s2 > 0) return 0;                                     \
+  l = sqrt((n1) * (n1) + (n2) * (n2) + (n3) * (n3));        \
+  if (l > 0) {                                              \
+    s2 /= l;                                                \
+    if (s2 * fudge_factor > s) {                            \
+      s = s2; normalR = 0;                                  \
+      normalC[0] = (n1) / l; normalC[1] = (n2) / l; normalC[2] = (n3) / l; \
+      invert_normal = (e1 < 0); code = (cc);                \
+      if (flags & CONTACTS_UNIMPORTANT) break;              \
+    }                                                       \
+  }
+    TST_EDGE(pp[2] * R21 - pp[1] * R31, (A[1] * Q31 + A[2] * Q21 + B[1] * Q13 + B[2] * Q12), 0, -R31, R21, 7);
+    TST_EDGE(pp[2] * R22 - pp[1] * R32, (A[1] * Q32 + A[2] * Q22 + B[0] * Q13 + B[2] * Q11), 0, -R32, R22, 8);
+    TST_EDGE(pp[2] * R23 - pp[1] * R33, (A[1] * Q33 + A[2] * Q23 + B[0] * Q12 + B[1] * Q11), 0, -R33, R23, 9);
+    TST_EDGE(pp[0] * R31 - pp[2] * R11, (A[0] * Q31 + A[2] * Q11 + B[1] * Q23 + B[2] * Q22), R31, 0, -R11, 10);
+    TST_EDGE(pp[0] * R32 - pp[2] * R12, (A[0] * Q32 + A[2] * Q12 + B[0] * Q23 + B[2] * Q21), R32, 0, -R12, 11);
+    TST_EDGE(pp[0] * R33 - pp[2] * R13, (A[0] * Q33 + A[2] * Q13 + B[0] * Q22 + B[1] * Q21), R33, 0, -R13, 12);
+    TST_EDGE(pp[1] * R11 - pp[0] * R21, (A[0] * Q21 + A[1] * Q11 + B[1] * Q33 + B[2] * Q32), -R21, R11, 0, 13);
+    TST_EDGE(pp[1] * R12 - pp[0] * R22, (A[0] * Q22 + A[1] * Q12 + B[0] * Q33 + B[2] * Q31), -R22, R12, 0, 14);
+    TST_EDGE(pp[1] * R13 - pp[0] * R23, (A[0] * Q23 + A[1] * Q13 + B[0] * Q32 + B[1] * Q31), -R23, R13, 0, 15);
+#undef TST_EDGE
+  } while (0);
+
+  if (!code) return 0;
+
+  if (normalR) {
+    normal[0] = normalR[0]; normal[1] = normalR[4]; normal[2] = normalR[8];
+  } else {
+    mul0_331(normal, R1, normalC);
+  }
+  if (invert_normal) { normal[0] = -normal[0]; normal[1] = -normal[1]; normal[2] = -normal[2]; }
+  *depth = -s;
+
+  if (code > 6) {
+    real pa[3], pb[3], sign, alpha, beta, ua[3], ub[3];
+    for (i = 0; i < 3; i++) pa[i] = p1[i];
+    for (j = 0; j < 3; j++) {
+      sign = (dot3s(normal, R1 + j, 1, 4) > 0) ? 1.0 : -1.0;
+      for (i = 0; i < 3; i++) pa[i] += sign * A[j] * R1[i * 4 + j];
+    }
+    for (i = 0; i < 3; i++) pb[i] = p2[i];
+    for (j = 0; j < 3; j++) {
+      sign = (dot3s(normal, R2 + j, 1, 4) > 0) ? -1.0 : 1.0;
+      for (i = 0; i < 3; i++) pb[i] += sign * B[j] * R2[i * 4 + j];
+    }
+    for (i = 0; i < 3; i++) ua[i] = R1[((code)-7) / 3 + i * 4];
+    for (i = 0; i < 3; i++) ub[i] = R2[((code)-7) % 3 + i * 4];
+    line_closest_approach(pa, ua, pb, ub, &alpha, &beta);
+    for (i = 0; i < 3; i++) pa[i] += ua[i] * alpha;
+    for (i = 0; i < 3; i++) pb[i] += ub[i] * beta;
+    for (i = 0; i < 3; i++) contact[0].pos[i] = 0.5 * (pa[i] + pb[i]);
+    contact[0].depth = *depth;
+    *return_code = code;
+    return 1;
+  }
+
+  const real *Ra, *Rb, *pa, *pb, *Sa, *Sb;
+  if (code <= 3) { Ra = R1; Rb = R2; pa = p1; pb = p2; Sa = A; Sb = B; }
+  else { Ra = R2; Rb = R1; pa = p2; pb = p1; Sa = B; Sb = A; }
+
+  real normal2[3], nr[3], anr[3];
+  if (code <= 3) { normal2[0] = normal[0]; normal2[1] = normal[1]; normal2[2] = normal[2]; }
+  else { normal2[0] = -normal[0]; normal2[1] = -normal[1]; normal2[2] = -normal[2]; }
+  mul1_331(nr, Rb, normal2);
+  anr[0] = fabs(nr[0]); anr[1] = fabs(nr[1]); anr[2] = fabs(nr[2]);
+
+  int lanr, a1, a2;
+  if (anr[1] > anr[0]) {
+    if (anr[1] > anr[2]) { a1 = 0; lanr = 1; a2 = 2; }
+    else { a1 = 0; a2 = 1; lanr = 2; }
+  } else {
+    if (anr[0] > anr[2]) { lanr = 0; a1 = 1; a2 = 2; }
+    else { a1 = 0; a2 = 1; lanr = 2; }
+  }
+
+  real center[3];
+  if (nr[lanr] < 0) {
+    for (i = 0; i < 3; i++) center[i] = pb[i] - pa[i] + Sb[lanr] * Rb[i * 4 + lanr];
+  } else {
+    for (i = 0; i < 3; i++) center[i] = pb[i] - pa[i] - Sb[lanr] * Rb[i * 4 + lanr];
+  }
+
+  int codeN, code1, code2;
+  if (code <= 3) codeN = code - 1; else codeN = code - 4;
+  if (codeN == 0) { code1 = 1; code2 = 2; }
+  else if (codeN == 1) { code1 = 0; code2 = 2; }
+  else { code1 = 0; code2 = 1; }
+
+  real quad[8], c1, c2, m11, m12, m21, m22;
+  c1 = dot3s(center, Ra + code1, 1, 4);
+  c2 = dot3s(center, Ra + code2, 1, 4);
+  m11 = dot3s(Ra + code1, Rb + a1, 4, 4);
+  m12 = dot3s(Ra + code1, Rb + a2, 4, 4);
+  m21 = dot3s(Ra + code2, Rb + a1, 4, 4);
+  m22 = dot3s(Ra + code2, Rb + a2, 4, 4);
+  {
+    real k1 = m11 * Sb[a1], k2 = m21 * Sb[a1], k3 = m12 * Sb[a2], k4 = m22 * Sb[a2];
+    quad[0] = c1 - k1 - k3; quad[1] = c2 - k2 - k4;
+    quad[2] = c1 - k1 + k3; quad[3] = c2 - k2 + k4;
+    quad[4] = c1 + k1 + k3; quad[5] = c2 + k2 + k4;
+    quad[6] = c1 + k1 - k3; quad[7] = c2 + k2 - k4;
+  }
+  real rect[2] = {Sa[code1], Sa[code2]};
+  real ret[16];
+  int n = intersect_rect_quad(rect, quad, ret);
+  if (n < 1) return 0;
+
+  real point[3 * 8], dep[8];
+  real det1 = 1.0 / (m11 * m22 - m12 * m21);
+  m11 *= det1; m12 *= det1; m21 *= det1; m22 *= det1;
+  int cnum = 0;
+  for (j = 0; j < n; j++) {
+    real k1 = m22 * (ret[j * 2] - c1) - m12 * (ret[j * 2 + 1] - c2);
+    real k2 = -m21 * (ret[j * 2] - c1) + m11 * (ret[j * 2 + 1] - c2);
+    for (i = 0; i < 3; i++) point[cnum * 3 + i] = center[i] + k1 * Rb[i * 4 + a1] + k2 * Rb[i * 4 + a2];
+    dep[cnum] = Sa[codeN] - dot3(normal2, point + cnum * 3);
+    if (dep[cnum] >= 0) {
+      ret[cnum * 2] = ret[j * 2];
+      ret[cnum * 2 + 1] = ret[j * 2 + 1];
+      cnum++;
+      if ((cnum | CONTACTS_UNIMPORTANT) == (flags & (0xffffu | CONTACTS_UNIMPORTANT))) break;
+    }
+  }
+  if (cnum < 1) return 0;
+
+  int maxc = flags & 0xffff;
+  if (maxc > cnum) maxc = cnum;
+  if (maxc < 1) maxc = 1;
+  if (cnum <= maxc) {
+    for (j = 0; j < cnum; j++) {
+      for (i = 0; i < 3; i++) contact[j].pos[i] = point[j * 3 + i] + pa[i];
+      contact[j].depth = dep[j];
+    }
+  } else {
+    int i1 = 0;
+    real maxdepth = dep[0];
+    for (i = 1; i < cnum; i++) {
+      if (dep[i] > maxdepth) { maxdepth = dep[i]; i1 = i; }
+    }
+    int iret[8];
+    cull_points(cnum, ret, maxc, i1, iret);
+    for (j = 0; j < maxc; j++) {
+      for (i = 0; i < 3; i++) contact[j].pos[i] = point[iret[j] * 3 + i] + pa[i];
+      contact[j].depth = dep[iret[j]];
+    }
+    cnum = maxc;
+  }
+  *return_code = code;
+  return cnum;
+}
+
+/* dCollideBoxBox, ode/src/box.cpp:716-742 (normal negated) */
+static int collide_box_box(const GeomRef* a, const GeomRef* b, unsigned flags, OContact* c) {
+  real normal[3], depth;
+  int code;
+  int num = box_box(a->pos, a->R, a->p, b->pos, b->R, b->p, normal, &depth, &code, flags, c);
+  for (int i = 0; i < num; i++) {
+    c[i].normal[0] = -normal[0]; c[i].normal[1] = -normal[1]; c[i].normal[2] = -normal[2];
+  }
+  return num;
+}
+
+/* dCollideBoxPlane, ode/src/box.cpp:745-878 */
+static int collide_box_plane(const GeomRef* bx, const GeomRef* pl, unsigned flags, OContact* c) {
+  const real* R = bx->R;
+  const real* n = pl->p;
+  const real* side = bx->p;
+  real Q1 = dot3s(n, R + 0, 1, 4), Q2 = dot3s(n, R + 1, 1, 4), Q3 = dot3s(n, R + 2, 1, 4);
+  real A1 = side[0] * Q1, A2 = side[1] * Q2, A3 = side[2] * Q3;
+  real B1 = fabs(A1), B2 = fabs(A2), B3 = fabs(A3);
+  real depth = n[3] + 0.5 * (B1 + B2 + B3) - dot3(n, bx->pos);
+  if (depth < 0) return 0;
+  int maxc = flags & 0xffff;
+  if (maxc > 4) maxc = 4;
+  real p[3] = {bx->pos[0], bx->pos[1], bx->pos[2]};
+  real Aarr[3] = {A1, A2, A3};
+  for (int i = 0; i < 3; ++i) {
+    if (Aarr[i] > 0) {
+      p[0] -= 0.5 * side[i] * R[0 + i]; p[1] -= 0.5 * side[i] * R[4 + i]; p[2] -= 0.5 * side[i] * R[8 + i];
+    } else {
+      p[0] += 0.5 * side[i] * R[0 + i]; p[1] += 0.5 * side[i] * R[4 + i]; p[2] += 0.5 * side[i] * R[8 + i];
+    }
+  }
+  c[0].pos[0] = p[0]; c[0].pos[1] = p[1]; c[0].pos[2] = p[2];
+  c[0].depth = depth;
+  int ret = 1;
+  real Barr[3] = {B1, B2, B3};
+  /* add contact `ct` by walking from p along side `sd` (0-based) */
+#define ADD_SIDE(ct, sd)                                                    \
+  do {                                                                      \
+    if (depth - Barr[sd] < 0) goto done;                                    \
+    if (Aarr[sd] > 0) {                                                     \
+      c[ct].pos[0] = p[0] + side[sd] * R[0 + sd];                           \
+      c[ct].pos[1] = p[1] + side[sd] * R[4 + sd];                           \
+      c[ct].pos[2] = p[2] + side[sd] * R[8 + sd];                           \
+    } else {                                                                \
+      c[ct].pos[0] = p[0] - side[sd] * R[0 + sd];                           \
+      c[ct].pos[1] = p[1] - side[sd] * R[4 + sd];                           \
+      c[ct].pos[2] = p[2] - side[sd] * R[8 + sd];                           \
+    }                                                                       \
+    c[ct].depth = depth - Barr[sd];                                         \
+    ret++;                                                                  \
+  } while (0)
+  if (maxc == 1) goto done;
+  if (B1 < B2) {
+    if (B3 < B1) goto use_side_3;
+    ADD_SIDE(1, 0);
+    if (maxc == 2) goto done;
+    if (B2 < B3) goto contact2_2; else goto contact2_3;
+  } else {
+    if (B3 < B2) {
+    use_side_3:
+      ADD_SIDE(1, 2);
+      if (maxc == 2) goto done;
+      if (B1 < B2) goto contact2_1; else goto contact2_2;
+    } else {
+      ADD_SIDE(1, 1);
+      if (maxc == 2) goto done;
+      if (B1 < B3) goto contact2_1; else goto contact2_3;
+    }
+  }
+contact2_1: ADD_SIDE(2, 0); goto done;
+contact2_2: ADD_SIDE(2, 1); goto done;
+contact2_3: ADD_SIDE(2, 2); goto done;
+#undef ADD_SIDE
+done:
+  if (maxc == 4 && ret == 3) {
+    real d4 = c[1].depth + c[2].depth - depth;
+    if (d4 > 0) {
+      c[3].pos[0] = c[1].pos[0] + c[2].pos[0] - p[0];
+      c[3].pos[1] = c[1].pos[1] + c[2].pos[1] - p[1];
+      c[3].pos[2] = c[1].pos[2] + c[2].pos[2] - p[2];
+      c[3].depth = d4;
+      ret++;
+    }
+  }
+  for (int i = 0; i < ret; i++) {
+    c[i].normal[0] = n[0]; c[i].normal[1] = n[1]; c[i].normal[2] = n[2];
+  }
+  return ret;
+}
+
+/* dCollideCapsulePlane, ode/src/capsule.cpp:352-411 */
+static int collide_capsule_plane(const GeomRef* cp, const GeomRef* pl, unsigned flags, OContact* c) {
+  const real* R = cp->R;
+  const real* P = pl->p;
+  real radius = cp->p[0], lz = cp->p[1];
+  real sign = (dot3s(P, R + 2, 1, 4) > 0) ? -1.0 : 1.0;
+  real p[3];
+  p[0] = cp->pos[0] + R[2] * lz * 0.5 * sign;
+  p[1] = cp->pos[1] + R[6] * lz * 0.5 * sign;
+  p[2] = cp->pos[2] + R[10] * lz * 0.5 * sign;
+  real k = dot3(p, P);
+  real depth = P[3] - k + radius;
+  if (depth < 0) return 0;
+  c[0].normal[0] = P[0]; c[0].normal[1] = P[1]; c[0].normal[2] = P[2];
+  c[0].pos[0] = p[0] - P[0] * radius;
+  c[0].pos[1] = p[1] - P[1] * radius;
+  c[0].pos[2] = p[2] - P[2] * radius;
+  c[0].depth = depth;
+  int nc = 1;
+  if ((flags & 0xffff) >= 2) {
+    p[0] = cp->pos[0] - R[2] * lz * 0.5 * sign;
+    p[1] = cp->pos[1] - R[6] * lz * 0.5 * sign;
+    p[2] = cp->pos[2] - R[10] * lz * 0.5 * sign;
+    k = dot3(p, P);
+    depth = P[3] - k + radius;
+    if (depth >= 0) {
+      c[1].normal[0] = P[0]; c[1].normal[1] = P[1]; c[1].normal[2] = P[2];
+      c[1].pos[0] = p[0] - P[0] * radius;
+      c[1].pos[1] = p[1] - P[1] * radius;
+      c[1].pos[2] = p[2] - P[2] * radius;
+      c[1].depth = depth;
+      nc = 2;
+    }
+  }
+  return nc;
+}
+
+/* Collider table restricted to this path: returns the collider id for the
+ * ordered class pair and whether the call is reversed, as dInitColliders
+ * (ode/src/collision_kernel.cpp:167-268) arranges it. */
+enum { C_NONE, C_SS, C_SB, C_SP, C_BB, C_BP, C_CP, C_HF };
+static int collider_of(int t1, int t2, int* reverse) {
+  *reverse = 0;
+#define PAIR(a, b, id) \
+  if (t1 == (a) && t2 == (b)) return id; \
+  if (t1 == (b) && t2 == (a)) { *reverse = ((a) != (b)); return id; }
+  PAIR(ODEGPU_GEOM_SPHERE, ODEGPU_GEOM_SPHERE, C_SS);
+  PAIR(ODEGPU_GEOM_SPHERE, ODEGPU_GEOM_BOX, C_SB);
+  PAIR(ODEGPU_GEOM_SPHERE, ODEGPU_GEOM_PLANE, C_SP);
+  PAIR(ODEGPU_GEOM_BOX, ODEGPU_GEOM_BOX, C_BB);
+  PAIR(ODEGPU_GEOM_BOX, ODEGPU_GEOM_PLANE, C_BP);
+  PAIR(ODEGPU_GEOM_CAPSULE, ODEGPU_GEOM_PLANE, C_CP);
+  PAIR(ODEGPU_GEOM_HEIGHTFIELD, ODEGPU_GEOM_SPHERE, C_HF);
+  PAIR(ODEGPU_GEOM_HEIGHTFIELD, ODEGPU_GEOM_BOX, C_HF);
+  PAIR(ODEGPU_GEOM_HEIGHTFIELD, ODEGPU_GEOM_CAPSULE, C_HF);
+#undef PAIR
+  return C_NONE;
+}
+
+int oracle_heightfield_collide(const GeomRef* hf, const GeomRef* o2, unsigned flags, OContact* c);
+
+/* dCollide, ode/src/collision_kernel.cpp:292-340: dispatch, reversing the
+ * call and negating normals for reversed class pairs. */
+static int do_collide(const GeomRef* g1, const GeomRef* g2, unsigned flags, OContact* c) {
+  if ((flags & 0xffff) == 0) return 0;
+  int rev;
+  int id = collider_of(g1->type, g2->type, &rev);
+  const GeomRef* a = rev ? g2 : g1;
+  const GeomRef* b = rev ? g1 : g2;
+  int n = 0;
+  switch (id) {
+    case C_SS: n = collide_spheres(a->pos, a->p[0], b->pos, b->p[0], c); break;
+    case C_SB: n = collide_sphere_box(a, b, c); break;
+    case C_SP: n = collide_sphere_plane(a, b, c); break;
+    case C_BB: n = collide_box_box(a, b, flags, c); break;
+    case C_BP: n = collide_box_plane(a, b, flags, c); break;
+    case C_CP: n = collide_capsule_plane(a, b, flags, c); break;
+    case C_HF: n = oracle_heightfield_collide(a, b, flags, c); break;
+    default: n = 0;
+  }
+  if (rev) {
+    for (int i = 0; i < n; ++i) {
+      c[i].normal[0] = -c[i].normal[0]; c[i].normal[1] = -c[i].normal[1]; c[i].normal[2] = -c[i].normal[2];
+    }
+  }
+  return n;
+}
+
+/* Placeholder until the heightfield restatement lands: no contacts. */
+int oracle_heightfield_collide(const GeomRef* hf, const GeomRef* o2, unsigned flags, OContact* c) {
+  (void)hf; (void)o2; (void)flags; (void)c;
+  return 0;
+}
+
+static void fill_ref(const OWorld* W, int gi, GeomRef* r) {
+  const OGeom* g = &W->geom[gi];
+  r->type = g->type;
+  r->p = g->p;
+  r->g = g;
+  if (g->body >= 0) {
+    r->pos = W->body[g->body].pos;
+    r->R = W->body[g->body].R;
+  } else {
+    r->pos = g->hpos;
+    r->R = g->hR;
+  }
+}
+
+/* ------------------------------------------------------------------------ */
+/* joints: getInfo1 / getInfo2                                              */
+
+typedef struct {
+  real fps, erp;
+  real *J1l, *J1a, *J2l, *J2a;
+  int rowskip;
+  real *c, *cfm, *lo, *hi;
+  int* findex;
+} Info2;
+
+/* setBall, ode/src/joints/joint.cpp:85-128 */
+static void set_ball(OWorld* W, OJoint* J, Info2* info, const real* anchor1, const real* anchor2) {
+  real a1[3], a2[3];
+  int s = info->rowskip;
+  OBody* B1 = &W->body[J->b[0]];
+  info->J1l[0] = 1; info->J1l[s + 1] = 1; info->J1l[2 * s + 2] = 1;
+  mul0_331(a1, B1->R, anchor1);
+  /* dSetCrossMatrixMinus(J1a, a1, s) */
+  info->J1a[1] = +a1[2]; info->J1a[2] = -a1[1];
+  info->J1a[s + 0] = -a1[2]; info->J1a[s + 2] = +a1[0];
+  info->J1a[2 * s + 0] = +a1[1]; info->J1a[2 * s + 1] = -a1[0];
+  if (J->b[1] >= 0) {
+    OBody* B2 = &W->body[J->b[1]];
+    info->J2l[0] = -1; info->J2l[s + 1] = -1; info->J2l[2 * s + 2] = -1;
+    mul0_331(a2, B2->R, anchor2);
+    /* dSetCrossMatrixPlus(J2a, a2, s) */
+    info->J2a[1] = -a2[2]; info->J2a[2] = +a2[1];
+    info->J2a[s + 0] = +a2[2]; info->J2a[s + 2] = -a2[0];
+    info->J2a[2 * s + 0] = -a2[1]; info->J2a[2 * s + 1] = +a2[0];
+  }
+  real k = info->fps * info->erp;
+  if (J->b[1] >= 0) {
+    OBody* B2 = &W->body[J->b[1]];
+    for (int j = 0; j < 3; j++) info->c[j] = k * (a2[j] + B2->pos[j] - a1[j] - B1->pos[j]);
+  } else {
+    for (int j = 0; j < 3; j++) info->c[j] = k * (anchor2[j] - a1[j] - B1->pos[j]);
+  }
+}
+
+/* setBall2, ode/src/joints/joint.cpp:134-196 */
+static void set_ball2(OWorld* W, OJoint* J, Info2* info, const real* anchor1, const real* anchor2,
+                      const real* axis, real erp1) {
+  real a1[3], a2[3], q1[3], q2[3];
+  int i, s = info->rowskip;
+  OBody* B1 = &W->body[J->b[0]];
+  plane_space(axis, q1, q2);
+  for (i = 0; i < 3; i++) info->J1l[i] = axis[i];
+  for (i = 0; i < 3; i++) info->J1l[s + i] = q1[i];
+  for (i = 0; i < 3; i++) info->J1l[2 * s + i] = q2[i];
+  mul0_331(a1, B1->R, anchor1);
+  cross3(info->J1a, a1, axis);
+  cross3(info->J1a + s, a1, q1);
+  cross3(info->J1a + 2 * s, a1, q2);
+  if (J->b[1] >= 0) {
+    OBody* B2 = &W->body[J->b[1]];
+    for (i = 0; i < 3; i++) info->J2l[i] = -axis[i];
+    for (i = 0; i < 3; i++) info->J2l[s + i] = -q1[i];
+    for (i = 0; i < 3; i++) info->J2l[2 * s + i] = -q2[i];
+    mul0_331(a2, B2->R, anchor2);
+    real* J2a = info->J2a;
+    cross3(J2a, a2, axis); J2a[0] = -J2a[0]; J2a[1] = -J2a[1]; J2a[2] = -J2a[2];
+    cross3(J2a + s, a2, q1); J2a[s] = -J2a[s]; J2a[s + 1] = -J2a[s + 1]; J2a[s + 2] = -J2a[s + 2];
+    cross3(J2a + 2 * s, a2, q2);
+    J2a[2 * s] = -J2a[2 * s]; J2a[2 * s + 1] = -J2a[2 * s + 1]; J2a[2 * s + 2] = -J2a[2 * s + 2];
+  }
+  real k1 = info->fps * erp1;
+  real k = info->fps * info->erp;
+  for (i = 0; i < 3; i++) a1[i] += B1->pos[i];
+  real d[3];
+  if (J->b[1] >= 0) {
+    OBody* B2 = &W->body[J->b[1]];
+    for (i = 0; i < 3; i++) a2[i] += B2->pos[i];
+    d[0] = a2[0] - a1[0]; d[1] = a2[1] - a1[1]; d[2] = a2[2] - a1[2];
+  } else {
+    d[0] = anchor2[0] - a1[0]; d[1] = anchor2[1] - a1[1]; d[2] = anchor2[2] - a1[2];
+  }
+  info->c[0] = k1 * dot3(axis, d);
+  info->c[1] = k * dot3(q1, d);
+  info->c[2] = k * dot3(q2, d);
+}
+
+/* getHingeAngleFromRelativeQuat / getHingeAngle, ode/src/joints/joint.cpp:381-451 */
+static real hinge_angle(OWorld* W, OJoint* J) {
+  real qrel[4];
+  const real* q1 = W->body[J->b[0]].q;
+  if (J->b[1] >= 0) {
+    real qq[4];
+    qmul1(qq, q1, W->body[J->b[1]].q);
+    qmul2(qrel, qq, J->qrel);
+  } else {
+    qmul3(qrel, q1, J->qrel);
+  }
+  real cost2 = qrel[0];
+  real sint2 = sqrt(qrel[1] * qrel[1] + qrel[2] * qrel[2] + qrel[3] * qrel[3]);
+  real theta = (dot3(qrel + 1, J->axis1) >= 0) ? (2 * atan2(sint2, cost2)) : (2 * atan2(sint2, -cost2));
+  if (theta > R_PI) theta -= (real)(2 * R_PI);
+  theta = -theta;
+  return theta;
+}
+
+/* dxJointLimitMotor::testRotationalLimit, ode/src/joints/joint.cpp:534-553 */
+static int limot_test(OLimot* L, real angle) {
+  if (angle <= L->lostop) { L->limit = 1; L->limit_err = angle - L->lostop; return 1; }
+  if (angle >= L->histop) { L->limit = 2; L->limit_err = angle - L->histop; return 1; }
+  L->limit = 0;
+  return 0;
+}
+
+/* dxJointLimitMotor::addLimot (rotational rows only on this path),
+ * ode/src/joints/joint.cpp:556-733 */
+static int limot_add(OWorld* W, OJoint* J, OLimot* L, Info2* info, int row, const real* ax1) {
+  int srow = row * info->rowskip;
+  int powered = L->fmax > 0;
+  if (!(powered || L->limit)) return 0;
+  real* J1 = info->J1a;
+  real* J2 = info->J2a;
+  J1[srow + 0] = ax1[0]; J1[srow + 1] = ax1[1]; J1[srow + 2] = ax1[2];
+  if (J->b[1] >= 0) { J2[srow + 0] = -ax1[0]; J2[srow + 1] = -ax1[1]; J2[srow + 2] = -ax1[2]; }
+  if (L->limit && (L->lostop == L->histop)) powered = 0;
+  if (powered) {
+    info->cfm[row] = L->normal_cfm;
+    if (!L->limit) {
+      info->c[row] = L->vel;
+      info->lo[row] = -L->fmax;
+      info->hi[row] = L->fmax;
+    } else {
+      real fm = L->fmax;
+      if ((L->vel > 0) || (L->vel == 0 && L->limit == 2)) fm = -fm;
+      if ((L->limit == 1 && L->vel > 0) || (L->limit == 2 && L->vel < 0)) fm *= L->fudge;
+      OBody* B1 = &W->body[J->b[0]];
+      B1->tacc[0] += -fm * ax1[0]; B1->tacc[1] += -fm * ax1[1]; B1->tacc[2] += -fm * ax1[2];
+      if (J->b[1] >= 0) {
+        OBody* B2 = &W->body[J->b[1]];
+        B2->tacc[0] += fm * ax1[0]; B2->tacc[1] += fm * ax1[1]; B2->tacc[2] += fm * ax1[2];
+      }
+    }
+  }
+  if (L->limit) {
+    real k = info->fps * L->stop_erp;
+    info->c[row] = -k * L->limit_err;
+    info->cfm[row] = L->stop_cfm;
+    if (L->lostop == L->histop) {
+      info->lo[row] = -R_INF; info->hi[row] = R_INF;
+    } else {
+      if (L->limit == 1) { info->lo[row] = 0; info->hi[row] = R_INF; }
+      else { info->lo[row] = -R_INF; info->hi[row] = 0; }
+      if (L->bounce > 0) {
+        real vel = dot3(W->body[J->b[0]].avel, ax1);
+        if (J->b[1] >= 0) vel -= dot3(W->body[J->b[1]].avel, ax1);
+        if (L->limit == 1) {
+          if (vel < 0) { real newc = -L->bounce * vel; if (newc > info->c[row]) info->c[row] = newc; }
+        } else {
+          if (vel > 0) { real newc = -L->bounce * vel; if (newc < info->c[row]) info->c[row] = newc; }
+        }
+      }
+    }
+  }
+  return 1;
+}
+
+/* dxJointHinge2::measureAngle, ode/src/joints/hinge2.cpp:33-41 */
+static real hinge2_measure_angle(OWorld* W, OJoint* J) {
+  real a1[3], a2[3];
+  mul0_331(a1, W->body[J->b[1]].R, J->axis2);
+  mul1_331(a2, W->body[J->b[0]].R, a1);
+  real x = dot3(J->v1, a2);
+  real y = dot3(J->v2, a2);
+  return -atan2(y, x);
+}
+
+/* getInfo1 for each joint type: contact ode/src/joints/contact.cpp:47-71,
+ * ball ode/src/joints/ball.cpp:56-60, hinge ode/src/joints/hinge.cpp:54-74,
+ * hinge2 ode/src/joints/hinge2.cpp:81-101. Returns m. */
+static int joint_info1(OWorld* W, OJoint* J) {
+  switch (J->type) {
+    case ODEGPU_JOINT_CONTACT: {
+      int m = 1;
+      odegpuSurface* S = &J->surf;
+      if (S->mu < 0) S->mu = 0;
+      if (S->mode & ODEGPU_CONTACT_MU2) {
+        if ((S->mu > 0) || (S->mu2 > 0)) m++;
+        if (S->mu2 < 0) S->mu2 = 0;
+        if (S->mu2 > 0) m++;
+      } else {
+        if (S->mu > 0) m += 2;
+      }
+      J->the_m = m;
+      return m;
+    }
+    case ODEGPU_JOINT_BALL: return 3;
+    case ODEGPU_JOINT_HINGE: {
+      int m = (J->lm1.fmax > 0) ? 6 : 5;
+      if ((J->lm1.lostop >= -R_PI || J->lm1.histop <= R_PI) && J->lm1.lostop <= J->lm1.histop) {
+        real angle = hinge_angle(W, J);
+        if (limot_test(&J->lm1, angle)) m = 6;
+      }
+      return m;
+    }
+    case ODEGPU_JOINT_HINGE2: {
+      int m = 4;
+      J->lm1.limit = 0;
+      if ((J->lm1.lostop >= -R_PI || J->lm1.histop <= R_PI) && J->lm1.lostop <= J->lm1.histop) {
+        real angle = hinge2_measure_angle(W, J);
+        limot_test(&J->lm1, angle);
+      }
+      if (J->lm1.limit || J->lm1.fmax > 0) m++;
+      J->lm2.limit = 0;
+      if (J->lm2.fmax > 0) m++;
+      return m;
+    }
+  }
+  return 0;
+}
+
+/* getInfo2 for each joint type: contact ode/src/joints/contact.cpp:75-256,
+ * ball ode/src/joints/ball.cpp:63-70 (note: it overwrites info->erp, which
+ * then carries over to the joints that follow in the same island),
+ * hinge ode/src/joints/hinge.cpp:77-149, hinge2 ode/src/joints/hinge2.cpp:109-180. */
+static void joint_info2(OWorld* W, OJoint* J, Info2* info) {
+  int s = info->rowskip;
+  switch (J->type) {
+    case ODEGPU_JOINT_CONTACT: {
+      int s2 = 2 * s;
+      odegpuSurface* S = &J->surf;
+      OBody* B1 = &W->body[J->b[0]];
+      OBody* B2 = J->b[1] >= 0 ? &W->body[J->b[1]] : 0;
+      real normal[4];
+      if (J->reverse) { normal[0] = -J->cnormal[0]; normal[1] = -J->cnormal[1]; normal[2] = -J->cnormal[2]; }
+      else { normal[0] = J->cnormal[0]; normal[1] = J->cnormal[1]; normal[2] = J->cnormal[2]; }
+      normal[3] = 0;
+      real c1[3], c2[3] = {0, 0, 0};
+      c1[0] = J->cpos[0] - B1->pos[0]; c1[1] = J->cpos[1] - B1->pos[1]; c1[2] = J->cpos[2] - B1->pos[2];
+      info->J1l[0] = normal[0]; info->J1l[1] = normal[1]; info->J1l[2] = normal[2];
+      cross3(info->J1a, c1, normal);
+      if (B2) {
+        c2[0] = J->cpos[0] - B2->pos[0]; c2[1] = J->cpos[1] - B2->pos[1]; c2[2] = J->cpos[2] - B2->pos[2];
+        info->J2l[0] = -normal[0]; info->J2l[1] = -normal[1]; info->J2l[2] = -normal[2];
+        cross3(info->J2a, c2, normal);
+        info->J2a[0] = -info->J2a[0]; info->J2a[1] = -info->J2a[1]; info->J2a[2] = -info->J2a[2];
+      }
+      real erp = info->erp;
+      if (S->mode & ODEGPU_CONTACT_SOFT_ERP) erp = S->soft_erp;
+      real k = info->fps * erp;
+      real depth = J->cdepth - W->min_depth;
+      if (depth < 0) depth = 0;
+      if (S->mode & ODEGPU_CONTACT_SOFT_CFM) info->cfm[0] = S->soft_cfm;
+      real motionN = 0;
+      if (S->mode & ODEGPU_CONTACT_MOTIONN) motionN = S->motionN;
+      const real pushout = k * depth + motionN;
+      info->c[0] = pushout;
+      const real maxvel = W->max_vel;
+      if (info->c[0] > maxvel) info->c[0] = maxvel;
+      if (S->mode & ODEGPU_CONTACT_BOUNCE) {
+        real outgoing = dot3(info->J1l, B1->lvel) + dot3(info->J1a, B1->avel);
+        if (B2) outgoing += dot3(info->J2l, B2->lvel) + dot3(info->J2a, B2->avel);
+        outgoing -= motionN;
+        if (S->bounce_vel >= 0 && (-outgoing) > S->bounce_vel) {
+          real newc = -S->bounce * outgoing + motionN;
+          if (newc > info->c[0]) info->c[0] = newc;
+        }
+      }
+      info->lo[0] = 0;
+      info->hi[0] = R_INF;
+      real t1[3], t2[3];
+      if (J->the_m >= 2) {
+        plane_space(normal, t1, t2);
+        info->J1l[s + 0] = t1[0]; info->J1l[s + 1] = t1[1]; info->J1l[s + 2] = t1[2];
+        cross3(info->J1a + s, c1, t1);
+        if (B2) {
+          info->J2l[s + 0] = -t1[0]; info->J2l[s + 1] = -t1[1]; info->J2l[s + 2] = -t1[2];
+          real* p = info->J2a + s;
+          cross3(p, c2, t1); p[0] = -p[0]; p[1] = -p[1]; p[2] = -p[2];
+        }
+        if (S->mode & ODEGPU_CONTACT_MOTION1) info->c[1] = S->motion1;
+        info->lo[1] = -S->mu;
+        info->hi[1] = S->mu;
+        if (S->mode & ODEGPU_CONTACT_APPROX1_1) info->findex[1] = 0;
+        if (S->mode & ODEGPU_CONTACT_SLIP1) info->cfm[1] = S->slip1;
+      }
+      if (J->the_m >= 3) {
+        info->J1l[s2 + 0] = t2[0]; info->J1l[s2 + 1] = t2[1]; info->J1l[s2 + 2] = t2[2];
+        cross3(info->J1a + s2, c1, t2);
+        if (B2) {
+          info->J2l[s2 + 0] = -t2[0]; info->J2l[s2 + 1] = -t2[1]; info->J2l[s2 + 2] = -t2[2];
+          real* p = info->J2a + s2;
+          cross3(p, c2, t2); p[0] = -p[0]; p[1] = -p[1]; p[2] = -p[2];
+        }
+        if (S->mode & ODEGPU_CONTACT_MOTION2) info->c[2] = S->motion2;
+        if (S->mode & ODEGPU_CONTACT_MU2) { info->lo[2] = -S->mu2; info->hi[2] = S->mu2; }
+        else { info->lo[2] = -S->mu; info->hi[2] = S->mu; }
+        if (S->mode & ODEGPU_CONTACT_APPROX1_2) info->findex[2] = 0;
+        if (S->mode & ODEGPU_CONTACT_SLIP2) info->cfm[2] = S->slip2;
+      }
+      break;
+    }
+    case ODEGPU_JOINT_BALL:
+      info->erp = J->erp;
+      info->cfm[0] = J->cfm; info->cfm[1] = J->cfm; info->cfm[2] = J->cfm;
+      set_ball(W, J, info, J->anchor1, J->anchor2);
+      break;
+    case ODEGPU_JOINT_HINGE: {
+      set_ball(W, J, info, J->anchor1, J->anchor2);
+      real ax1[3], p[3], q[3];
+      mul0_331(ax1, W->body[J->b[0]].R, J->axis1);
+      plane_space(ax1, p, q);
+      int s3 = 3 * s, s4 = 4 * s;
+      info->J1a[s3 + 0] = p[0]; info->J1a[s3 + 1] = p[1]; info->J1a[s3 + 2] = p[2];
+      info->J1a[s4 + 0] = q[0]; info->J1a[s4 + 1] = q[1]; info->J1a[s4 + 2] = q[2];
+      if (J->b[1] >= 0) {
+        info->J2a[s3 + 0] = -p[0]; info->J2a[s3 + 1] = -p[1]; info->J2a[s3 + 2] = -p[2];
+        info->J2a[s4 + 0] = -q[0]; info->J2a[s4 + 1] = -q[1]; info->J2a[s4 + 2] = -q[2];
+      }
+      real ax2[3], b[3];
+      if (J->b[1] >= 0) mul0_331(ax2, W->body[J->b[1]].R, J->axis2);
+      else { ax2[0] = J->axis2[0]; ax2[1] = J->axis2[1]; ax2[2] = J->axis2[2]; }
+      cross3(b, ax1, ax2);
+      real k = info->fps * info->erp;
+      info->c[3] = k * dot3(b, p);
+      info->c[4] = k * dot3(b, q);
+      limot_add(W, J, &J->lm1, info, 5, ax1);
+      break;
+    }
+    case ODEGPU_JOINT_HINGE2: {
+      real sn, cs, q[4], ax1[4], ax2[4];
+      hinge2_axis_info(W, J, ax1, ax2, q, &sn, &cs);
+      safe_normalize3(q);
+      set_ball2(W, J, info, J->anchor1, J->anchor2, ax1, J->susp_erp);
+      int s3 = 3 * s;
+      info->J1a[s3 + 0] = q[0]; info->J1a[s3 + 1] = q[1]; info->J1a[s3 + 2] = q[2];
+      if (J->b[1] >= 0) { info->J2a[s3 + 0] = -q[0]; info->J2a[s3 + 1] = -q[1]; info->J2a[s3 + 2] = -q[2]; }
+      real k = info->fps * info->erp;
+      info->c[3] = k * (J->c0 * sn - J->s0 * cs);
+      int row = 4 + limot_add(W, J, &J->lm1, info, 4, ax1);
+      limot_add(W, J, &J->lm2, info, row, ax2);
+      info->cfm[0] = J->susp_cfm;
+      break;
+    }
+  }
+}
+
+/* ------------------------------------------------------------------------ */
+/* SOR_LCP, ode/src/quickstep.cpp:342-584 (WARM_STARTING and               */
+/* REORDER_CONSTRAINTS off, RANDOMLY_REORDER_CONSTRAINTS on, :47-64)        */
+
+static void sor_lcp_core(int m, int nb, real* J, const int* jb, const real* invMass, const real* invI,
+                         real* lambda, real* fc, real* b, const real* lo, const real* hi,
+                         const real* cfm, const int* findex, int num_iterations, real sor_w,
+                         real* iMJ_out) {
+  memset(lambda, 0, m * sizeof(real));
+  real* iMJ = iMJ_out ? iMJ_out : (real*)malloc((size_t)m * 12 * sizeof(real));
+  /* compute_invM_JT, :117-136 */
+  for (int i = 0; i < m; i++) {
+    const real* Jp = J + 12 * i;
+    real* ip = iMJ + 12 * i;
+    int b1 = jb[2 * i], b2 = jb[2 * i + 1];
+    real k1 = invMass[b1];
+    for (int j = 0; j < 3; j++) ip[j] = k1 * Jp[j];
+    mul0_331(ip + 3, invI + 12 * b1, Jp + 3);
+    if (b2 != -1) {
+      real k2 = invMass[b2];
+      for (int j = 0; j < 3; j++) ip[j + 6] = k2 * Jp[j + 6];
+      mul0_331(ip + 9, invI + 12 * b2, Jp + 9);
+    }
+  }
+  memset(fc, 0, (size_t)nb * 6 * sizeof(real));
+  real* Ad = (real*)malloc((size_t)m * sizeof(real));
+  for (int i = 0; i < m; i++) {
+    const real* Jp = J + 12 * i;
+    const real* ip = iMJ + 12 * i;
+    real sum = 0;
+    for (int j = 0; j < 6; j++) sum += ip[j] * Jp[j];
+    if (jb[2 * i + 1] != -1)
+      for (int k = 6; k < 12; k++) sum += ip[k] * Jp[k];
+    Ad[i] = sor_w / (sum + cfm[i]);
+  }
+  for (int i = 0; i < m; i++) {
+    real* Jp = J + 12 * i;
+    real Ad_i = Ad[i];
+    for (int j = 0; j < 12; j++) Jp[j] *= Ad_i;
+    b[i] *= Ad_i;
+    Ad[i] = Ad_i * cfm[i];
+  }
+  int* order = (int*)malloc((size_t)(m > 0 ? m : 1) * sizeof(int));
+  {
+    int head = 0, tail = m - 1;
+    for (int i = 0; i < m; i++) {
+      if (findex[i] == -1) order[head++] = i;
+      else order[tail--] = i;
+    }
+  }
+  for (int it = 0; it < num_iterations; it++) {
+    if ((it & 7) == 0) {
+      for (int i = 1; i < m; i++) {
+        int swapi = rand_int(i + 1);
+        int tmp = order[i];
+        order[i] = order[swapi];
+        order[swapi] = tmp;
+      }
+    }
+    for (int i = 0; i < m; i++) {
+      int index = order[i];
+      int b1 = jb[2 * index], b2 = jb[2 * index + 1];
+      real* fc1 = fc + 6 * b1;
+      real* fc2 = (b2 != -1) ? fc + 6 * b2 : 0;
+      real old_lambda = lambda[index];
+      real delta = b[index] - old_lambda * Ad[index];
+      const real* Jp = J + 12 * index;
+      delta -= fc1[0] * Jp[0] + fc1[1] * Jp[1] + fc1[2] * Jp[2] + fc1[3] * Jp[3] + fc1[4] * Jp[4] +
+               fc1[5] * Jp[5];
+      if (fc2)
+        delta -= fc2[0] * Jp[6] + fc2[1] * Jp[7] + fc2[2] * Jp[8] + fc2[3] * Jp[9] + fc2[4] * Jp[10] +
+                 fc2[5] * Jp[11];
+      real hi_act, lo_act;
+      if (findex[index] != -1) {
+        hi_act = fabs(hi[index] * lambda[findex[index]]);
+        lo_act = -hi_act;
+      } else {
+        hi_act = hi[index];
+        lo_act = lo[index];
+      }
+      real new_lambda = old_lambda + delta;
+      if (new_lambda < lo_act) { delta = lo_act - old_lambda; lambda[index] = lo_act; }
+      else if (new_lambda > hi_act) { delta = hi_act - old_lambda; lambda[index] = hi_act; }
+      else lambda[index] = new_lambda;
+      const real* ip = iMJ + 12 * index;
+      fc1[0] += delta * ip[0]; fc1[1] += delta * ip[1]; fc1[2] += delta * ip[2];
+      fc1[3] += delta * ip[3]; fc1[4] += delta * ip[4]; fc1[5] += delta * ip[5];
+      if (fc2) {
+        fc2[0] += delta * ip[6]; fc2[1] += delta * ip[7]; fc2[2] += delta * ip[8];
+        fc2[3] += delta * ip[9]; fc2[4] += delta * ip[10]; fc2[5] += delta * ip[11];
+      }
+    }
+  }
+  free(order);
+  free(Ad);
+  if (!iMJ_out) free(iMJ);
+}
+
+void oracle_sor_lcp(int m, int nb, double* J, const int* jb, const double* invMass, const double* invI,
+                    double* lambda, double* fc, double* b, const double* lo, const double* hi,
+                    const double* cfm, const int* findex, int iterations, double sor_w,
+                    unsigned int* seed) {
+  unsigned int saved = g_seed;
+  g_seed = *seed;
+  sor_lcp_core(m, nb, J, jb, invMass, invI, lambda, fc, b, lo, hi, cfm, findex, iterations, sor_w, 0);
+  *seed = g_seed;
+  g_seed = saved;
+}
+
+/* ------------------------------------------------------------------------ */
+/* dxStepBody, ode/src/util.cpp:255-360 (no finite rotation, no damping,   */
+/* no angular speed cap: the defaults on this path)                          */
+
+static void step_body(OBody* b, real h) {
+  for (int j = 0; j < 3; j++) b->pos[j] += h * b->lvel[j];
+  real dq[4];
+  const real* w = b->avel;
+  const real* q = b->q;
+  dq[0] = 0.5 * (-w[0] * q[1] - w[1] * q[2] - w[2] * q[3]);
+  dq[1] = 0.5 * (w[0] * q[0] + w[1] * q[3] - w[2] * q[2]);
+  dq[2] = 0.5 * (-w[0] * q[3] + w[1] * q[0] + w[2] * q[1]);
+  dq[3] = 0.5 * (w[0] * q[2] - w[1] * q[1] + w[2] * q[0]);
+  for (int j = 0; j < 4; j++) b->q[j] += h * dq[j];
+  normalize4(b->q);
+  r_from_q(b->R, b->q);
+}
+
+/* ------------------------------------------------------------------------ */
+/* dxQuickStepper, ode/src/quickstep.cpp:592-1025, for one island          */
+
+static void quick_stepper(OWorld* W, const int* bidx, int nb, const int* jidx, int nj_in, real h,
+                          int island_no) {
+  const real h1 = 1.0 / h;
+  real* invI = (real*)malloc((size_t)(nb > 0 ? nb : 1) * 12 * sizeof(real));
+  for (int i = 0; i < nb; i++) W->body[bidx[i]].tag = i;
+  for (int i = 0; i < nb; i++) {
+    OBody* b = &W->body[bidx[i]];
+    real tmp[12];
+    mul2_333(tmp, b->invI, b->R);
+    mul0_333(invI + 12 * i, b->R, tmp);
+    if (b->flags & ODEGPU_BODY_GYROSCOPIC) {
+      real I[12], t3[3];
+      mul2_333(tmp, b->I, b->R);
+      mul0_333(I, b->R, tmp);
+      mul0_331(t3, I, b->avel);
+      real cr[3];
+      cross3(cr, b->avel, t3);
+      b->tacc[0] = b->tacc[0] - cr[0];
+      b->tacc[1] = b->tacc[1] - cr[1];
+      b->tacc[2] = b->tacc[2] - cr[2];
+    }
+  }
+  for (int d = 0; d < 3; ++d) {
+    real g = W->gravity[d];
+    if (g) {
+      for (int i = 0; i < nb; i++) {
+        OBody* b = &W->body[bidx[i]];
+        if ((b->flags & ODEGPU_BODY_NO_GRAVITY) == 0) b->facc[d] += b->mass * g;
+      }
+    }
+  }
+  /* getInfo1; joints with m=0 dropped (:670-688) */
+  int* jl = (int*)malloc((size_t)(nj_in > 0 ? nj_in : 1) * sizeof(int));
+  int* jm = (int*)malloc((size_t)(nj_in > 0 ? nj_in : 1) * sizeof(int));
+  int nj = 0, m = 0;
+  for (int i = 0; i < nj_in; i++) {
+    int mm = joint_info1(W, &W->joint[jidx[i]]);
+    if (mm > 0) { jl[nj] = jidx[i]; jm[nj] = mm; nj++; m += mm; }
+  }
+  real* cforce = (real*)calloc((size_t)(nb > 0 ? nb : 1) * 6, sizeof(real));
+  real *J = 0, *lambda = 0;
+  int* jb = 0;
+  if (m > 0) {
+    J = (real*)calloc((size_t)m * 12, sizeof(real));
+    real* cfm = (real*)malloc(m * sizeof(real));
+    real* lo = (real*)malloc(m * sizeof(real));
+    real* hi = (real*)malloc(m * sizeof(real));
+    int* findex = (int*)malloc(m * sizeof(int));
+    jb = (int*)malloc((size_t)m * 2 * sizeof(int));
+    real* rhs = (real*)malloc(m * sizeof(real));
+    real* c = (real*)calloc(m, sizeof(real));
+    real* Jcopy = (real*)malloc((size_t)m * 12 * sizeof(real));
+    for (int i = 0; i < m; i++) { cfm[i] = W->cfm; lo[i] = -R_INF; hi[i] = R_INF; findex[i] = -1; }
+    Info2 info;
+    info.rowskip = 12;
+    info.fps = h1;
+    info.erp = W->erp;
+    int ofs = 0;
+    for (int k = 0; k < nj; k++) {
+      real* Jrow = J + (size_t)ofs * 12;
+      info.J1l = Jrow; info.J1a = Jrow + 3; info.J2l = Jrow + 6; info.J2a = Jrow + 9;
+      info.c = c + ofs; info.cfm = cfm + ofs; info.lo = lo + ofs; info.hi = hi + ofs;
+      info.findex = findex + ofs;
+      joint_info2(W, &W->joint[jl[k]], &info);
+      memcpy(Jcopy + (size_t)ofs * 12, Jrow, (size_t)jm[k] * 12 * sizeof(real));
+      for (int j = 0; j < jm[k]; j++)
+        if (findex[ofs + j] != -1) findex[ofs + j] += ofs;
+      ofs += jm[k];
+    }
+    {
+      int r = 0;
+      for (int k = 0; k < nj; k++) {
+        OJoint* Jt = &W->joint[jl[k]];
+        int b1 = Jt->b[0] >= 0 ? W->body[Jt->b[0]].tag : -1;
+        int b2 = Jt->b[1] >= 0 ? W->body[Jt->b[1]].tag : -1;
+        for (int j = 0; j < jm[k]; j++) { jb[2 * r] = b1; jb[2 * r + 1] = b2; r++; }
+      }
+    }
+    {
+      real* tmp1 = (real*)malloc((size_t)nb * 6 * sizeof(real));
+      for (int i = 0; i < nb; i++) {
+        OBody* b = &W->body[bidx[i]];
+        real* t = tmp1 + 6 * i;
+        for (int j = 0; j < 3; j++) t[j] = b->facc[j] * b->invMass + b->lvel[j] * h1;
+        mul0_331(t + 3, invI + 12 * i, b->tacc);
+        for (int k = 0; k < 3; k++) t[3 + k] += b->avel[k] * h1;
+      }
+      /* multiply_J, :163-181 */
+      for (int i = 0; i < m; i++) {
+        const real* Jp = J + 12 * i;
+        int b1 = jb[2 * i], b2 = jb[2 * i + 1];
+        real sum = 0;
+        const real* in = tmp1 + 6 * b1;
+        for (int j = 0; j < 6; j++) sum += Jp[j] * in[j];
+        if (b2 != -1) {
+          in = tmp1 + 6 * b2;
+          for (int j = 0; j < 6; j++) sum += Jp[6 + j] * in[j];
+        }
+        rhs[i] = sum;
+      }
+      free(tmp1);
+    }
+    for (int i = 0; i < m; i++) rhs[i] = c[i] * h1 - rhs[i];
+    for (int j = 0; j < m; j++) cfm[j] *= h1;
+
+    lambda = (real*)malloc(m * sizeof(real));
+    real* invMass = (real*)malloc((size_t)nb * sizeof(real));
+    for (int i = 0; i < nb; i++) invMass[i] = W->body[bidx[i]].invMass;
+
+    oracleTap* tap = W->tap;
+    int tap_base = 0;
+    if (tap) {
+      tap_base = 0;
+      for (int q = 0; q < tap->n_islands; ++q) tap_base += tap->island_rows[q];
+    }
+    if (tap && tap_base + m <= tap->cap_rows) {
+      memcpy(tap->J + (size_t)tap_base * 12, J, (size_t)m * 12 * sizeof(real));
+      memcpy(tap->rhs + tap_base, rhs, m * sizeof(real));
+      memcpy(tap->cfm + tap_base, cfm, m * sizeof(real));
+      memcpy(tap->lo + tap_base, lo, m * sizeof(real));
+      memcpy(tap->hi + tap_base, hi, m * sizeof(real));
+      memcpy(tap->findex + tap_base, findex, m * sizeof(int));
+      memcpy(tap->jb + (size_t)tap_base * 2, jb, (size_t)m * 2 * sizeof(int));
+      int r = 0;
+      for (int k = 0; k < nj; k++)
+        for (int j = 0; j < jm[k]; j++) tap->joint_of_row[tap_base + r++] = jl[k];
+    }
+
+    sor_lcp_core(m, nb, J, jb, invMass, invI, lambda, cforce, rhs, lo, hi, cfm, findex, W->iterations,
+                 W->sor_w, 0);
+
+    if (tap && tap_base + m <= tap->cap_rows) {
+      memcpy(tap->lambda + tap_base, lambda, m * sizeof(real));
+    }
+
+    for (int i = 0; i < nb; i++) {
+      OBody* b = &W->body[bidx[i]];
+      for (int j = 0; j < 3; j++) {
+        b->lvel[j] += h * cforce[6 * i + j];
+        b->avel[j] += h * cforce[6 * i + 3 + j];
+      }
+    }
+    /* joint feedback, :918-957 (Multiply1_12q1) */
+    {
+      int ofs2 = 0;
+      for (int k = 0; k < nj; k++) {
+        OJoint* Jt = &W->joint[jl[k]];
+        if (Jt->type != ODEGPU_JOINT_CONTACT) {
+          for (int half = 0; half < 2; ++half) {
+            if (half == 1 && Jt->b[1] < 0) break;
+            real a = 0, bb = 0, cc = 0, d = 0, e = 0, f = 0;
+            for (int i = 0; i < jm[k]; i++) {
+              const real* Bp = Jcopy + (size_t)(ofs2 + i) * 12 + 6 * half;
+              real s = lambda[ofs2 + i];
+              a += Bp[0] * s; bb += Bp[1] * s; cc += Bp[2] * s;
+              d += Bp[3] * s; e += Bp[4] * s; f += Bp[5] * s;
+            }
+            real* fb = Jt->fb + 6 * half;
+            fb[0] = a; fb[1] = bb; fb[2] = cc; fb[3] = d; fb[4] = e; fb[5] = f;
+          }
+        }
+        ofs2 += jm[k];
+      }
+    }
+    free(invMass); free(cfm); free(lo); free(hi); free(findex); free(rhs); free(c); free(Jcopy);
+  }
+  if (W->tap && W->tap->n_islands < W->tap->cap_islands) {
+    oracleTap* tap = W->tap;
+    tap->island_rows[tap->n_islands] = m;
+    tap->island_bodies[tap->n_islands] = nb;
+    int base = 0;
+    for (int q = 0; q < tap->n_islands; ++q) base += tap->island_bodies[q];
+    if (base + nb <= tap->cap_bodies) {
+      for (int i = 0; i < nb; ++i) {
+        tap->body_of[base + i] = bidx[i];
+        for (int k = 0; k < 6; ++k) tap->cforce[(size_t)(base + i) * 6 + k] = cforce[6 * i + k];
+      }
+    }
+    tap->n_islands++;
+  }
+  (void)island_no;
+  for (int i = 0; i < nb; i++) {
+    OBody* b = &W->body[bidx[i]];
+    real hm = h * b->invMass;
+    for (int j = 0; j < 3; j++) {
+      b->lvel[j] += hm * b->facc[j];
+      b->tacc[j] *= h;
+    }
+    real t3[3];
+    mul0_331(t3, invI + 12 * i, b->tacc);
+    b->avel[0] = b->avel[0] + t3[0];
+    b->avel[1] = b->avel[1] + t3[1];
+    b->avel[2] = b->avel[2] + t3[2];
+  }
+  for (int i = 0; i < nb; i++) step_body(&W->body[bidx[i]], h);
+  for (int i = 0; i < nb; i++) {
+    OBody* b = &W->body[bidx[i]];
+    b->facc[0] = b->facc[1] = b->facc[2] = 0;
+    b->tacc[0] = b->tacc[1] = b->tacc[2] = 0;
+  }
+  free(J); free(jb); free(lambda); free(cforce); free(jl); free(jm); free(invI);
+}
+
+/* ------------------------------------------------------------------------ */
+/* world construction from a scene, mirroring the harness's API sequence    */
+
+static void world_init(OWorld* W, const odegpuScene* sc, int w) {
+  memset(W, 0, sizeof(*W));
+  const odegpuWorldParams* P = &sc->world[w];
+  W->sc = sc; W->w = w;
+  const int b0 = sc->body_off[w], g0 = sc->geom_off[w], j0 = sc->joint_off[w];
+  W->nb = sc->body_off[w + 1] - b0;
+  W->ng = sc->geom_off[w + 1] - g0;
+  W->nj_persist = sc->joint_off[w + 1] - j0;
+  for (int d = 0; d < 3; ++d) W->gravity[d] = P->gravity[d];
+  W->erp = P->erp; W->cfm = P->cfm; W->iterations = P->iterations; W->sor_w = P->sor_w;
+  W->max_vel = P->max_vel; W->min_depth = P->min_depth; W->dt = P->dt;
+  W->max_contacts = P->max_contacts;
+  W->body = (OBody*)calloc(W->nb > 0 ? W->nb : 1, sizeof(OBody));
+  for (int i = 0; i < W->nb; ++i) {
+    OBody* b = &W->body[i];
+    const int g = b0 + i;
+    for (int k = 0; k < 3; ++k) b->pos[k] = sc->body_pos[3 * g + k];
+    for (int k = 0; k < 4; ++k) b->q[k] = sc->body_q[4 * g + k];
+    normalize4(b->q);                     /* dBodySetQuaternion, ode.cpp:383-391 */
+    r_from_q(b->R, b->q);
+    for (int k = 0; k < 3; ++k) b->lvel[k] = sc->body_lvel[3 * g + k];
+    for (int k = 0; k < 3; ++k) b->avel[k] = sc->body_avel[3 * g + k];
+    const double* I = sc->body_I + 9 * g;
+    b->mass = sc->body_mass[g];
+    /* dMassSetParameters layout (ode/src/mass.cpp:94-117) */
+    memset(b->I, 0, sizeof(b->I));
+    b->I[0] = I[0]; b->I[5] = I[4]; b->I[10] = I[8];
+    b->I[1] = I[1]; b->I[2] = I[2]; b->I[6] = I[5];
+    b->I[4] = I[1]; b->I[8] = I[2]; b->I[9] = I[5];
+    if (!invert_pd3(b->I, b->invI)) {
+      memset(b->invI, 0, sizeof(b->invI));
+      b->invI[0] = b->invI[5] = b->invI[10] = 1;
+    }
+    b->invMass = 1.0 / b->mass;
+    b->flags = sc->body_flags[g];
+  }
+  W->geom = (OGeom*)calloc(W->ng > 0 ? W->ng : 1, sizeof(OGeom));
+  for (int i = 0; i < W->ng; ++i) {
+    OGeom* G = &W->geom[i];
+    const int g = g0 + i;
+    G->type = sc->geom_type[g];
+    G->body = sc->geom_body[g];
+    G->surface = sc->geom_surface[g];
+    for (int k = 0; k < 4; ++k) G->p[k] = sc->geom_param[ODEGPU_GEOM_NPARAM * g + k];
+    if (G->type == ODEGPU_GEOM_PLANE) {
+      /* make_sure_plane_normal_has_unit_length, ode/src/plane.cpp:40-56 */
+      real l = G->p[0] * G->p[0] + G->p[1] * G->p[1] + G->p[2] * G->p[2];
+      if (l > 0) {
+        l = 1.0 / sqrt(l);
+        G->p[0] *= l; G->p[1] *= l; G->p[2] *= l; G->p[3] *= l;
+      } else {
+        G->p[0] = 1; G->p[1] = 0; G->p[2] = 0; G->p[3] = 0;
+      }
+    }
+    if (G->type == ODEGPU_GEOM_HEIGHTFIELD) {
+      G->hf = &sc->heightfields[(int)G->p[0]];
+      for (int k = 0; k < 3; ++k) G->hpos[k] = G->hf->pos[k];
+      for (int r = 0; r < 3; ++r) {
+        for (int c = 0; c < 3; ++c) G->hR[r * 4 + c] = G->hf->R[r * 3 + c];
+        G->hR[r * 4 + 3] = 0;
+      }
+    } else {
+      memset(G->hR, 0, sizeof(G->hR));
+      G->hR[0] = G->hR[5] = G->hR[10] = 1;
+    }
+  }
+  W->cap_j = W->nj_persist + 64;
+  W->joint = (OJoint*)calloc(W->cap_j, sizeof(OJoint));
+  W->nj = 0;
+  for (int i = 0; i < W->nj_persist; ++i) {
+    const int g = j0 + i;
+    OJoint* J = &W->joint[W->nj];
+    const int jj = W->nj++;
+    J->type = sc->joint_type[g];
+    J->b[0] = J->b[1] = -1;
+    const double* a = sc->joint_anchor + 3 * g;
+    const double* x1 = sc->joint_axis1 + 3 * g;
+    const double* x2 = sc->joint_axis2 + 3 * g;
+    const double* jp = sc->joint_param + ODEGPU_JOINT_NPARAM * g;
+    const int jb1 = sc->joint_body[2 * g], jb2 = sc->joint_body[2 * g + 1];
+    switch (J->type) {
+      case ODEGPU_JOINT_BALL:
+        J->erp = W->erp; J->cfm = W->cfm;
+        joint_attach(W, jj, jb1, jb2);
+        set_anchors(W, J, a[0], a[1], a[2], J->anchor1, J->anchor2);
+        J->erp = jp[0]; J->cfm = jp[1];
+        break;
+      case ODEGPU_JOINT_HINGE:
+        J->axis1[0] = 1; J->axis2[0] = 1;
+        limot_init(&J->lm1, W);
+        joint_attach(W, jj, jb1, jb2);
+        set_anchors(W, J, a[0], a[1], a[2], J->anchor1, J->anchor2);
+        hinge_qrel(W, J);
+        set_axes(W, J, x1[0], x1[1], x1[2], J->axis1, J->axis2);
+        hinge_qrel(W, J);
+        limot_set_all(&J->lm1, jp);
+        break;
+      case ODEGPU_JOINT_HINGE2: {
+        J->axis1[0] = 1; J->axis2[1] = 1;
+        J->v1[0] = 1; J->v2[1] = 1;
+        limot_init(&J->lm1, W);
+        limot_init(&J->lm2, W);
+        J->susp_erp = W->erp; J->susp_cfm = W->cfm;
+        joint_attach(W, jj, jb1, jb2);
+        /* setRelativeValues at attach (ode/src/joints/hinge2.cpp:425-448) */
+        {
+          real an[3], ax[3], ax1[4], ax2[4], axc[3];
+          get_anchor(W, J, an, J->anchor1);
+          set_anchors(W, J, an[0], an[1], an[2], J->anchor1, J->anchor2);
+          mul0_331(ax, W->body[J->b[0]].R, J->axis1);
+          set_axes(W, J, ax[0], ax[1], ax[2], J->axis1, 0);
+          if (J->b[1] >= 0) {
+            mul0_331(ax, W->body[J->b[1]].R, J->axis2);
+            set_axes(W, J, ax[0], ax[1], ax[2], 0, J->axis2);
+          }
+          hinge2_axis_info(W, J, ax1, ax2, axc, &J->s0, &J->c0);
+          hinge2_make_v(W, J);
+        }
+        set_anchors(W, J, a[0], a[1], a[2], J->anchor1, J->anchor2);
+        hinge2_make_v(W, J);
+        {
+          real ax1[4], ax2[4], axc[3];
+          set_axes(W, J, x1[0], x1[1], x1[2], J->axis1, 0);
+          hinge2_axis_info(W, J, ax1, ax2, axc, &J->s0, &J->c0);
+          hinge2_make_v(W, J);
+          set_axes(W, J, x2[0], x2[1], x2[2], 0, J->axis2);
+          hinge2_axis_info(W, J, ax1, ax2, axc, &J->s0, &J->c0);
+          hinge2_make_v(W, J);
+        }
+        limot_set_all(&J->lm1, jp);
+        limot_set_all(&J->lm2, jp + 9);
+        J->susp_erp = jp[18];
+        J->susp_cfm = jp[19];
+        break;
+      }
+      default: break;
+    }
+  }
+  for (int i = 0; i < W->nb; ++i) W->body[i].jl_persist = W->body[i].jl_n;
+}
+
+static void world_free(OWorld* W) {
+  for (int i = 0; i < W->nb; ++i) free(W->body[i].jl);
+  free(W->body); free(W->geom); free(W->joint);
+}
+
+static int new_contact_joint(OWorld* W) {
+  if (W->nj == W->cap_j) {
+    W->cap_j *= 2;
+    W->joint = (OJoint*)realloc(W->joint, W->cap_j * sizeof(OJoint));
+  }
+  OJoint* J = &W->joint[W->nj];
+  memset(J, 0, sizeof(*J));
+  J->type = ODEGPU_JOINT_CONTACT;
+  J->b[0] = J->b[1] = -1;
+  return W->nj++;
+}
+
+/* BuildIslandsAndEstimateStepperMemoryRequirements, ode/src/util.cpp:384-521,
+ * followed by dxProcessIslands, :534-568. Bodies are visited newest first
+ * (world list order) and each body's joints newest first (attach order
+ * reversed); the DFS stack is LIFO. */
+static void process_islands(OWorld* W) {
+  const int nb = W->nb, nj = W->nj;
+  int* ibody = (int*)malloc((size_t)(nb > 0 ? nb : 1) * sizeof(int));
+  int* ijoint = (int*)malloc((size_t)(nj > 0 ? nj : 1) * sizeof(int));
+  int* stack = (int*)malloc((size_t)(nb > 0 ? nb : 1) * sizeof(int));
+  for (int i = 0; i < nb; ++i) W->body[i].tag = 0;
+  for (int j = 0; j < nj; ++j) W->joint[j].tag = 0;
+  int island = 0;
+  for (int bb = nb - 1; bb >= 0; --bb) {
+    if (W->body[bb].tag) continue;
+    W->body[bb].tag = 1;
+    int nbi = 0, nji = 0, ss = 0;
+    ibody[nbi++] = bb;
+    int b = bb;
+    for (;;) {
+      OBody* B = &W->body[b];
+      for (int k = B->jl_n - 1; k >= 0; --k) {
+        const int j = B->jl[k];
+        OJoint* J = &W->joint[j];
+        if (J->tag) continue;
+        /* dxJoint::isEnabled, ode/src/joints/joint.cpp:66-71 */
+        int enabled = (W->body[J->b[0]].invMass > 0) || (J->b[1] >= 0 && W->body[J->b[1]].invMass > 0);
+        if (enabled) {
+          J->tag = 1;
+          ijoint[nji++] = j;
+          const int other = (J->b[0] == b) ? J->b[1] : J->b[0];
+          if (other >= 0 && W->body[other].tag <= 0) {
+            W->body[other].tag = 1;
+            stack[ss++] = other;
+          }
+        } else {
+          J->tag = -1;
+        }
+      }
+      if (ss == 0) break;
+      b = stack[--ss];
+      ibody[nbi++] = b;
+    }
+    quick_stepper(W, ibody, nbi, ijoint, nji, W->dt, island);
+    ++island;
+  }
+  free(ibody); free(ijoint); free(stack);
+}
+
+/* dAreConnectedExcluding(b1, b2, dJointTypeContact), ode/src/ode.cpp:1529-1537:
+ * contacts are never attached while this is asked, so only persistent joints
+ * (the first jl_persist entries of a body's list) can connect. */
+static int bodies_jointed(const OWorld* W, int b1, int b2) {
+  const OBody* B = &W->body[b1];
+  for (int k = 0; k < B->jl_persist; ++k) {
+    const OJoint* J = &W->joint[B->jl[k]];
+    const int other = (J->b[0] == b1) ? J->b[1] : J->b[0];
+    if (other == b2) return 1;
+  }
+  return 0;
+}
+
+/* One canonical world step (see include/odegpu_scene.h). */
+static int world_step(OWorld* W, int s, double* contacts, int max_rec) {
+  const odegpuScene* sc = W->sc;
+  int nc = 0;
+  OContact cg[16];
+  for (int i = 0; i < W->ng; ++i) {
+    for (int k = i + 1; k < W->ng; ++k) {
+      const int bi = W->geom[i].body, bk = W->geom[k].body;
+      if (bi < 0 && bk < 0) continue;
+      if (bi == bk) continue;
+      if (bi >= 0 && bk >= 0 && bodies_jointed(W, bi, bk)) continue;
+      GeomRef gi, gk;
+      fill_ref(W, i, &gi);
+      fill_ref(W, k, &gk);
+      const int n = do_collide(&gi, &gk, (unsigned)W->max_contacts, cg);
+      const int si = W->geom[i].surface, sk = W->geom[k].surface;
+      const odegpuSurface* S = &sc->surfaces[si > sk ? si : sk];
+      for (int c = 0; c < n; ++c) {
+        const int j = new_contact_joint(W);
+        OJoint* J = &W->joint[j];
+        J->surf = *S;
+        for (int q = 0; q < 3; ++q) { J->cpos[q] = cg[c].pos[q]; J->cnormal[q] = cg[c].normal[q]; }
+        J->cdepth = cg[c].depth;
+        joint_attach(W, j, bi, bk);
+        if (contacts && nc < max_rec) {
+          double* r = contacts + (size_t)nc * ORACLE_CONTACT_REC;
+          for (int q = 0; q < 3; ++q) r[q] = cg[c].pos[q];
+          for (int q = 0; q < 3; ++q) r[3 + q] = cg[c].normal[q];
+          r[6] = cg[c].depth;
+          r[7] = i;
+          r[8] = k;
+        }
+        ++nc;
+      }
+    }
+  }
+  if (sc->n_ctrl_steps > 0) {
+    const int cs = s % sc->n_ctrl_steps;
+    const int j0 = sc->joint_off[W->w], b0 = sc->body_off[W->w];
+    if (sc->joint_torque) {
+      for (int i = 0; i < W->nj_persist; ++i) {
+        const double* t = sc->joint_torque + ((size_t)cs * sc->joint_off[sc->n_worlds] + j0 + i) * 2;
+        OJoint* J = &W->joint[i];
+        if (J->type == ODEGPU_JOINT_HINGE) {
+          /* dJointAddHingeTorque, ode/src/joints/hinge.cpp:326-345 */
+          real torque = t[0];
+          if (J->reverse) torque = -torque;
+          real ax[3];
+          if (J->b[0] >= 0) {
+            mul0_331(ax, W->body[J->b[0]].R, J->axis1);
+            ax[0] *= torque; ax[1] *= torque; ax[2] *= torque;
+            OBody* B1 = &W->body[J->b[0]];
+            B1->tacc[0] += ax[0]; B1->tacc[1] += ax[1]; B1->tacc[2] += ax[2];
+            if (J->b[1] >= 0) {
+              OBody* B2 = &W->body[J->b[1]];
+              B2->tacc[0] += -ax[0]; B2->tacc[1] += -ax[1]; B2->tacc[2] += -ax[2];
+            }
+          }
+        } else if (J->type == ODEGPU_JOINT_HINGE2) {
+          /* dJointAddHinge2Torques, ode/src/joints/hinge2.cpp:393-410 */
+          if (J->b[0] >= 0 && J->b[1] >= 0) {
+            real a1[3], a2[3];
+            mul0_331(a1, W->body[J->b[0]].R, J->axis1);
+            mul0_331(a2, W->body[J->b[1]].R, J->axis2);
+            a1[0] = a1[0] * t[0] + a2[0] * t[1];
+            a1[1] = a1[1] * t[0] + a2[1] * t[1];
+            a1[2] = a1[2] * t[0] + a2[2] * t[1];
+            OBody* B1 = &W->body[J->b[0]];
+            OBody* B2 = &W->body[J->b[1]];
+            B1->tacc[0] += a1[0]; B1->tacc[1] += a1[1]; B1->tacc[2] += a1[2];
+            B2->tacc[0] += -a1[0]; B2->tacc[1] += -a1[1]; B2->tacc[2] += -a1[2];
+          }
+        }
+      }
+    }
+    if (sc->body_force) {
+      for (int i = 0; i < W->nb; ++i) {
+        const double* f = sc->body_force + ((size_t)cs * sc->body_off[sc->n_worlds] + b0 + i) * 6;
+        OBody* B = &W->body[i];
+        B->facc[0] += f[0]; B->facc[1] += f[1]; B->facc[2] += f[2];
+        B->tacc[0] += f[3]; B->tacc[1] += f[4]; B->tacc[2] += f[5];
+      }
+    }
+  }
+  process_islands(W);
+  /* dJointGroupEmpty, ode/src/ode.cpp:1305-1332: contacts leave every list */
+  W->nj = W->nj_persist;
+  for (int i = 0; i < W->nb; ++i) W->body[i].jl_n = W->body[i].jl_persist;
+  return nc;
+}
+
+static void read_state(const OWorld* W, double* out) {
+  for (int i = 0; i < W->nb; ++i) {
+    const OBody* b = &W->body[i];
+    double* r = out + ORACLE_BODY_REC * i;
+    for (int k = 0; k < 3; ++k) r[k] = b->pos[k];
+    for (int k = 0; k < 4; ++k) r[3 + k] = b->q[k];
+    for (int k = 0; k < 3; ++k) r[7 + k] = b->lvel[k];
+    for (int k = 0; k < 3; ++k) r[10 + k] = b->avel[k];
+  }
+}
+
+int oracle_run_world(const odegpuScene* sc, int w, int n_steps, double* state, int* ncontacts,
+                     double* contacts, int max_rec, double* feedback, unsigned int* seed_out) {
+  if (!sc || w < 0 || w >= sc->n_worlds || n_steps < 0) return -1;
+  OWorld W;
+  world_init(&W, sc, w);
+  g_seed = sc->world[w].seed;
+  if (state) read_state(&W, state);
+  for (int s = 0; s < n_steps; ++s) {
+    const int nc = world_step(&W, s, contacts ? contacts + (size_t)s * max_rec * ORACLE_CONTACT_REC : 0,
+                              max_rec);
+    if (ncontacts) ncontacts[s] = nc;
+    if (state) read_state(&W, state + (size_t)(s + 1) * W.nb * ORACLE_BODY_REC);
+    if (feedback)
+      for (int i = 0; i < W.nj_persist; ++i)
+        memcpy(feedback + ((size_t)s * W.nj_persist + i) * 12, W.joint[i].fb, 12 * sizeof(double));
+    if (seed_out) seed_out[s] = g_seed;
+  }
+  world_free(&W);
+  return 0;
+}
+
+typedef struct {
+  const odegpuScene* sc;
+  int w_begin, w_end, n_steps, stride, t;
+  double* out;
+  long long contacts;
+} ThreadArg;
+
+static void* run_worlds_thread(void* p) {
+  ThreadArg* a = (ThreadArg*)p;
+  const odegpuScene* sc = a->sc;
+  for (int w = a->w_begin + a->t; w < a->w_end; w += a->stride) {
+    OWorld W;
+    world_init(&W, sc, w);
+    g_seed = sc->world[w].seed;
+    for (int s = 0; s < a->n_steps; ++s) a->contacts += world_step(&W, s, 0, 0);
+    if (a->out) read_state(&W, a->out + (size_t)(sc->body_off[w] - sc->body_off[a->w_begin]) * ORACLE_BODY_REC);
+    world_free(&W);
+  }
+  return 0;
+}
+
+long long oracle_run_worlds(const odegpuScene* sc, int w_begin, int w_end, int n_steps, int n_threads,
+                            double* final_state) {
+  if (n_threads < 1) n_threads = 1;
+  pthread_t* th = (pthread_t*)malloc(n_threads * sizeof(pthread_t));
+  ThreadArg* args = (ThreadArg*)calloc(n_threads, sizeof(ThreadArg));
+  for (int t = 0; t < n_threads; ++t) {
+    args[t].sc = sc; args[t].w_begin = w_begin; args[t].w_end = w_end; args[t].n_steps = n_steps;
+    args[t].stride = n_threads; args[t].t = t; args[t].out = final_state;
+    pthread_create(&th[t], 0, run_worlds_thread, &args[t]);
+  }
+  long long total = 0;
+  for (int t = 0; t < n_threads; ++t) { pthread_join(th[t], 0); total += args[t].contacts; }
+  free(th); free(args);
+  return total;
+}
+
+int oracle_tap_step(const odegpuScene* sc, int w, int pre_steps, oracleTap* tap) {
+  if (!sc || !tap || w < 0 || w >= sc->n_worlds) return -1;
+  OWorld W;
+  world_init(&W, sc, w);
+  g_seed = sc->world[w].seed;
+  for (int s = 0; s < pre_steps; ++s) world_step(&W, s, 0, 0);
+  tap->n_islands = 0;
+  tap->seed_before = g_seed;
+  W.tap = tap;
+  world_step(&W, pre_steps, 0, 0);
+  int total = 0;
+  for (int i = 0; i < tap->n_islands; ++i) total += tap->island_rows[i];
+  world_free(&W);
+  return total;
+}
+
+int oracle_collide(int t1, const double* p1, const double* pos1, const double* R1, int t2, const double* p2,
+                   const double* pos2, const double* R2, int flags, double* out) {
+  OGeom G[2];
+  real pos[2][3], R[2][12];
+  const int tt[2] = {t1, t2};
+  const double* pp[2] = {p1, p2};
+  const double* ps[2] = {pos1, pos2};
+  const double* rs[2] = {R1, R2};
+  GeomRef ref[2];
+  for (int g = 0; g < 2; ++g) {
+    memset(&G[g], 0, sizeof(OGeom));
+    G[g].type = tt[g];
+    for (int k = 0; k < 4; ++k) G[g].p[k] = pp[g][k];
+    if (tt[g] == ODEGPU_GEOM_PLANE) {
+      real l = G[g].p[0] * G[g].p[0] + G[g].p[1] * G[g].p[1] + G[g].p[2] * G[g].p[2];
+      if (l > 0) {
+        l = 1.0 / sqrt(l);
+        G[g].p[0] *= l; G[g].p[1] *= l; G[g].p[2] *= l; G[g].p[3] *= l;
+      }
+      memset(pos[g], 0, sizeof(pos[g]));
+      memset(R[g], 0, sizeof(R[g]));
+    } else {
+      for (int k = 0; k < 3; ++k) pos[g][k] = ps[g][k];
+      for (int r = 0; r < 3; ++r) {
+        for (int c = 0; c < 3; ++c) R[g][r * 4 + c] = rs[g][r * 3 + c];
+        R[g][r * 4 + 3] = 0;
+      }
+    }
+    ref[g].type = tt[g]; ref[g].pos = pos[g]; ref[g].R = R[g]; ref[g].p = G[g].p; ref[g].g = &G[g];
+  }
+  OContact c[16];
+  int n = do_collide(&ref[0], &ref[1], (unsigned)flags, c);
+  for (int i = 0; i < n; ++i) {
+    double* r = out + 9 * i;
+    for (int q = 0; q < 3; ++q) r[q] = c[i].pos[q];
+    for (int q = 0; q < 3; ++q) r[3 + q] = c[i].normal[q];
+    r[6] = c[i].depth; r[7] = 0; r[8] = 0;
+  }
+  return n;
+}

@@ -1,0 +1,87 @@
+"""ctypes access to the test-only libraries: the CPU oracle (oracle/liboracle.so)
+and, where it was built in this checkout, the reference ODE 0.12 harness
+(oracle/_ref/libode_ref_d.so). Test infrastructure only."""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+ORACLE_DIR = os.path.join(ROOT, "oracle")
+_P = C.POINTER
+
+
+def build_oracle():
+    subprocess.run(["make", "-s", "-C", ORACLE_DIR, "liboracle.so"], check=True)
+
+
+def _bind(lib, prefix):
+    f = getattr(lib, prefix + "_run_world")
+    f.restype = C.c_int
+    f.argtypes = [C.c_void_p, C.c_int, C.c_int, _P(C.c_double), _P(C.c_int), _P(C.c_double),
+                  C.c_int, _P(C.c_double), _P(C.c_uint)]
+    return f
+
+
+_oracle = None
+_ref = {}
+
+
+def oracle():
+    global _oracle
+    if _oracle is None:
+        path = os.path.join(ORACLE_DIR, "liboracle.so")
+        if not os.path.exists(path):
+            build_oracle()
+        lib = C.CDLL(path)
+        _bind(lib, "oracle")
+        lib.oracle_run_worlds.restype = C.c_longlong
+        lib.oracle_run_worlds.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int,
+                                          _P(C.c_double)]
+        lib.oracle_collide.restype = C.c_int
+        lib.oracle_collide.argtypes = [C.c_int, _P(C.c_double), _P(C.c_double), _P(C.c_double),
+                                       C.c_int, _P(C.c_double), _P(C.c_double), _P(C.c_double),
+                                       C.c_int, _P(C.c_double)]
+        lib.oracle_rand_int.argtypes = [C.c_int]
+        lib.oracle_rand_set_seed.argtypes = [C.c_uint]
+        lib.oracle_rand_get_seed.restype = C.c_uint
+        _oracle = lib
+    return _oracle
+
+
+def ref_available(prec="d"):
+    return os.path.exists(os.path.join(ORACLE_DIR, "_ref", f"libode_ref_{prec}.so"))
+
+
+def ref(prec="d"):
+    if prec not in _ref:
+        lib = C.CDLL(os.path.join(ORACLE_DIR, "_ref", f"libode_ref_{prec}.so"))
+        _bind(lib, "ref")
+        lib.ref_collide.restype = C.c_int
+        lib.ref_collide.argtypes = oracle().oracle_collide.argtypes
+        lib.ref_rand_int.argtypes = [C.c_int]
+        lib.ref_rand_set_seed.argtypes = [C.c_uint]
+        lib.ref_rand_get_seed.restype = C.c_uint
+        _ref[prec] = lib
+    return _ref[prec]
+
+
+def run_world(fn, scene, w, n_steps, max_rec=512, feedback=False):
+    """Call a *_run_world entry; returns dict of numpy arrays."""
+    b0, b1 = scene.world_bodies(w)
+    j0, j1 = scene.world_joints(w)
+    nb, nj = b1 - b0, j1 - j0
+    state = np.zeros((n_steps + 1, nb, 13))
+    ncont = np.zeros(n_steps, np.int32)
+    cont = np.zeros((n_steps, max_rec, 9))
+    fb = np.zeros((n_steps, max(nj, 1), 12)) if feedback else None
+    seeds = np.zeros(n_steps, np.uint32)
+    rc = fn(C.byref(scene.c), w, n_steps, state.ctypes.data_as(_P(C.c_double)),
+            ncont.ctypes.data_as(_P(C.c_int)), cont.ctypes.data_as(_P(C.c_double)), max_rec,
+            fb.ctypes.data_as(_P(C.c_double)) if feedback else None,
+            seeds.ctypes.data_as(_P(C.c_uint)))
+    assert rc == 0
+    return dict(state=state, ncontacts=ncont, contacts=cont, feedback=fb, seeds=seeds)
