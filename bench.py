@@ -1,0 +1,285 @@
+"""Benchmark: batched ODE world stepping (collide + QuickStep) on GB300.
+
+Workload (one "step" = one collide+QuickStep step of every world of the batch):
+4096 independent worlds, N in [4,64] bodies log-uniform (spheres r U[0.1,0.5]
+or boxes edges U[0.2,1.0], density 1000), ~25% of bodies in ball-joint chains
+of 2-6 links, on plane z=0; mu=0.5, Approx1|SoftERP|SoftCFM, erp 0.2,
+cfm 1e-5, dt=0.01, 20 iterations, w=1.3, <=4 contacts per pair; seeded
+synthetic scene. Metric: world-steps/s (higher is better).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the CPU restatement of ODE's algorithm (the oracle
+port, oracle/liboracle.so) on a bounded sample of the same workload with all
+host threads.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "ode-0.12_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+
+METRIC = "world-steps/s, batched collide+QuickStep (4096 worlds)"
+N_WORLDS = 4096
+WORKLOAD = "batched_worlds: 4096 worlds, N~logU[4,64] spheres/boxes, 25% ball chains, plane"
+SCENE_SEED = 1
+
+
+def rank_env():
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+def build_scene(n_worlds, seed=SCENE_SEED):
+    from odegpu import scene as S
+    return S.batched_worlds(n_worlds=n_worlds, seed=seed)
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle sampling during the timed region."""
+
+    def __init__(self, gpu_index=0):
+        self.proc = None
+        self.lines = []
+        self.idx = gpu_index
+
+    def start(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.idx}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": float(max(mx)) if mx else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def algorithmic_bytes(sc, nc, nr, iters=20):
+    """Sweep-model bytes of one batched step: per world
+    208*nb + 56*nc + sum_joints Bj + m*(248 + 236*iters) (ball joint Bj=40)."""
+    nb = np.diff(sc.body_off)
+    nj = np.diff(sc.joint_off)
+    return float(np.sum(208.0 * nb + 56.0 * nc + 40.0 * nj + nr * (248.0 + 236.0 * iters)))
+
+
+def cpu_baseline(sc, n_worlds_sample=None, n_steps=20, threads=None):
+    """Oracle port (FP64 restatement of ODE's algorithm) on a bounded sample of
+    the workload, all host threads; returns world-steps/s."""
+    import oracle_lib as O
+    L = O.oracle()
+    threads = threads or (os.cpu_count() or 1)
+    n_worlds_sample = n_worlds_sample or min(sc.n_worlds, 64 * threads)
+    t0 = time.perf_counter()
+    L.oracle_run_worlds(C.byref(sc.c), 0, n_worlds_sample, n_steps, threads, None)
+    dt = time.perf_counter() - t0
+    return n_worlds_sample * n_steps / dt, threads, n_worlds_sample, n_steps, dt
+
+
+def run_reference(args):
+    rank, world_size, _ = rank_env()
+    if rank != 0:
+        return
+    sc = build_scene(N_WORLDS)
+    import oracle_lib as O
+    O.build_oracle()
+    vals = []
+    threads = os.cpu_count() or 1
+    sample_worlds = min(N_WORLDS, 32 * threads)
+    for _ in range(max(1, args.warmup)):
+        cpu_baseline(sc, sample_worlds, 5, threads)
+    t_total = 0.0
+    for _ in range(args.steps):
+        v, thr, nw, ns, dt = cpu_baseline(sc, sample_worlds, 5, threads)
+        vals.append(v)
+        t_total += dt
+    value = float(np.mean(vals))
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "world-steps/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * N_WORLDS / value, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "config": {"workload": WORKLOAD, "n_worlds": N_WORLDS, "iterations": 20,
+                       "dt": 0.01},
+            "cpu_baseline": {"value": value, "unit": "world-steps/s", "cores": threads,
+                             "kind": "port",
+                             "sample": f"first {sample_worlds} worlds x 5 steps from the initial "
+                                       f"state per bench step, {threads} threads"},
+            "e2e": {"value": value, "unit": "world-steps/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    from odegpu.batch import Batch
+
+    rank, world_size, local_rank = rank_env()
+    dist = world_size > 1
+    if dist:
+        import torch.distributed as tdist
+        tdist.init_process_group("nccl")
+    torch.cuda.set_device(local_rank)
+    # weak scaling: every rank steps its own 4096-world batch (distinct seeds)
+    sc = build_scene(N_WORLDS, seed=SCENE_SEED + rank)
+    B = Batch(sc, device=local_rank)
+    stream = torch.cuda.ExternalStream(B.stream_handle())
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    iters = sc.world_params[0].iterations
+
+    def barrier():
+        if dist:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    # warm-up (also settles the falling bodies into contact)
+    for _ in range(args.warmup):
+        B.step(1)
+    B.sync()
+    barrier()
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    bytes_total = 0.0
+    launches = 0
+    barrier()
+    for k in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.add_(1.0)           # evict L2 between timed steps (256 MB > 129 MB L2)
+            launches += 1
+            ev[k][0].record(stream)
+        B.step(1)
+        launches += 1
+        with torch.cuda.stream(stream):
+            ev[k][1].record(stream)
+    B.sync()
+    barrier()
+    clk = clocks.stop()
+    t_kernel = sum(a.elapsed_time(b) for a, b in ev) / 1e3
+    nc, nr, _ = B.counts()
+    bytes_total = algorithmic_bytes(sc, nc, nr, iters) * args.steps
+    # max over ranks
+    t_max = t_kernel
+    if dist:
+        t = torch.tensor([t_kernel], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_max = float(t.item())
+    value = N_WORLDS * world_size * args.steps / t_max
+
+    # e2e through the C ABI with host buffers: H2D state, step, D2H state, per step
+    nbt = B.nb_total
+    h_in = torch.empty(nbt * 13, dtype=torch.float32, pin_memory=True)
+    h_out = torch.empty(nbt * 13, dtype=torch.float32, pin_memory=True)
+    B.read_state_async(h_in.data_ptr())
+    B.sync()
+    e2e_steps = max(3, args.steps // 2)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        B.write_state_async(h_in.data_ptr())
+        B.step(1)
+        B.read_state_async(h_out.data_ptr())
+        B.sync()
+        h_in, h_out = h_out, h_in
+    barrier()
+    t_e2e = time.perf_counter() - t0
+    e2e = N_WORLDS * world_size * e2e_steps / t_e2e
+    stat = B.status()
+
+    if rank == 0:
+        hbm, src = peaks()
+        t_launch = t_kernel / args.steps
+        achieved = bytes_total / args.steps / t_launch / 1e9
+        line = {"metric": METRIC, "value": value, "unit": "world-steps/s", "n_gpus": world_size,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic (seeded)",
+                "config": {"workload": WORKLOAD, "n_worlds": N_WORLDS, "iterations": iters,
+                           "dt": 0.01, "l2": "flushed between timed steps (256 MB write)",
+                           "bodies": int(nbt), "contacts_last_step": int(nc.sum()),
+                           "rows_last_step": int(nr.sum()), "worlds_with_status": int((stat != 0).sum())},
+                "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                             "frac": achieved / hbm, "peak_source": src,
+                             "traffic": None,
+                             "kernel": "world_step_kernel (one warp per world)"},
+                "e2e": {"value": e2e, "unit": "world-steps/s", "h2d_bytes_per_step": nbt * 13 * 4,
+                        "d2h_bytes_per_step": nbt * 13 * 4},
+                "gpu_launches": launches, "clocks": clk}
+        if not args.no_cpu:
+            v, thr, nw, ns, dt = cpu_baseline(sc, min(N_WORLDS, 16 * (os.cpu_count() or 1)), 20)
+            line["cpu_baseline"] = {"value": v, "unit": "world-steps/s", "cores": thr, "kind": "port",
+                                    "sample": f"first {nw} worlds x {ns} steps from the initial state"}
+        print(json.dumps(line), flush=True)
+    B.close()
+    if dist:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=50)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,122 @@
+/*
+ * odegpu.h -- C ABI of libodegpu: the batched world-stepping extension.
+ *
+ * A batch holds many independent ODE worlds resident in GPU memory and steps
+ * them with the CUDA path: contact generation by the primitive colliders
+ * (dCollide, ode/src/collision_kernel.cpp:292) in the canonical pair order of
+ * odegpu_scene.h, then dWorldQuickStep (ode/src/ode.cpp:1807-1824) per world.
+ * Plain pointers and sizes only. All functions return 0 on success and a
+ * negative ODEGPU_E* code on failure; odegpuGetLastError() describes the last
+ * failure on the calling thread. The ODE-compatible single-world API lives in
+ * ode_gpu.h.
+ */
+#ifndef ODEGPU_H
+#define ODEGPU_H
+#include <stddef.h>
+#include "odegpu_scene.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  ODEGPU_OK = 0,
+  ODEGPU_E_ARG = -1,       /* invalid argument                                */
+  ODEGPU_E_CUDA = -2,      /* CUDA runtime error (no device, launch failure)  */
+  ODEGPU_E_NOMEM = -3,     /* device allocation failed                        */
+  ODEGPU_E_LIMIT = -4      /* a world exceeds a documented size limit         */
+};
+
+/* Per-world status bits reported by odegpuBatchGetStatus. */
+enum {
+  ODEGPU_ST_CONTACT_OVERFLOW = 1,
+  ODEGPU_ST_ROW_OVERFLOW = 2,
+  ODEGPU_ST_TOO_LARGE = 4,
+  ODEGPU_ST_NONFINITE = 8
+};
+
+/* Size limits of the on-chip step kernel: bodies and constraint rows per world. */
+#define ODEGPU_MAX_BODIES_PER_WORLD 64
+#define ODEGPU_MAX_ROWS_PER_WORLD 1024
+
+typedef struct odegpuBatch* odegpuBatchID;
+
+typedef struct odegpuBatchConfig {
+  int contacts_per_body;   /* contact capacity per world = this * nb + 16 (0 -> 8) */
+  int warps_per_block;     /* 0 -> chosen by the library                          */
+  int device;              /* CUDA device ordinal                                 */
+} odegpuBatchConfig;
+
+/* Body state record used by the read/write calls: pos[3] q[4] lvel[3] avel[3]. */
+#define ODEGPU_BODY_REC 13
+
+/* Create a batch from a scene (copied; the scene may be freed afterwards).
+ * Replaces building each world with dWorldCreate, dBodyCreate, the dCreate
+ * geom constructors and the dJointCreate calls (include/ode/objects.h,
+ * include/ode/collision.h). */
+int odegpuBatchCreate(const odegpuScene* scene, const odegpuBatchConfig* cfg,
+                      odegpuBatchID* out);
+void odegpuBatchDestroy(odegpuBatchID b);
+
+/* Enqueue n_steps full steps (collide + QuickStep) of every world on the
+ * batch's stream, all steps in one launch. Replaces, per world and step, the
+ * dSpaceCollide/dCollide + dJointCreateContact + dWorldQuickStep +
+ * dJointGroupEmpty sequence (ode/src/ode.cpp:1201, :1807, :1305). */
+int odegpuBatchStep(odegpuBatchID b, int n_steps);
+/* Same work as odegpuBatchStep but one world per launch (the plain, unbatched
+ * GPU path used as a comparator). */
+int odegpuBatchStepPlain(odegpuBatchID b, int n_steps);
+/* Capture n_steps single-step launches into a CUDA graph and replay it. */
+int odegpuBatchStepGraph(odegpuBatchID b, int n_steps);
+int odegpuBatchSynchronize(odegpuBatchID b);
+
+/* Body state exchange with host memory (FP64 records of ODEGPU_BODY_REC).
+ * Read = dBodyGetPosition/Quaternion/LinearVel/AngularVel over all bodies;
+ * write = dBodySetPosition/Quaternion/LinearVel/AngularVel. */
+int odegpuBatchReadState(odegpuBatchID b, double* state);
+int odegpuBatchWriteState(odegpuBatchID b, const double* state);
+/* FP32 variants for pinned-host or device buffers, enqueued on the stream
+ * without synchronising: float state[nb_total][ODEGPU_BODY_REC]. */
+int odegpuBatchReadStateF32Async(odegpuBatchID b, float* state);
+int odegpuBatchWriteStateF32Async(odegpuBatchID b, const float* state);
+
+/* Per-world bookkeeping of the last step. */
+int odegpuBatchGetStatus(odegpuBatchID b, int* status);
+int odegpuBatchGetCounts(odegpuBatchID b, int* ncontacts, int* nrows, int* nislands);
+int odegpuBatchGetSeeds(odegpuBatchID b, unsigned int* seeds);
+/* dRandSetSeed per world (the reference has one global seed; a batch has one
+ * per world). */
+int odegpuBatchSetSeeds(odegpuBatchID b, const unsigned int* seeds);
+int odegpuBatchInfo(odegpuBatchID b, int* n_worlds, int* nb_total, int* nj_total,
+                    long long* row_capacity, long long* contact_capacity);
+/* The CUDA stream the batch enqueues on (a cudaStream_t). */
+void* odegpuBatchStream(odegpuBatchID b);
+
+/* Replace the per-step controls (same layout as odegpuScene): joint_torque
+ * [n_ctrl_steps][nj_total][2], body_force [n_ctrl_steps][nb_total][6]; either
+ * may be NULL. Replaces dJointAddHingeTorque / dJointAddHinge2Torques /
+ * dBodyAddForce / dBodyAddTorque calls made before each step. */
+int odegpuBatchSetControls(odegpuBatchID b, int n_ctrl_steps, const double* joint_torque,
+                           const double* body_force);
+/* Index of the next step (selects the control row step % n_ctrl_steps); it
+ * advances by one per step taken. */
+int odegpuBatchSetStepIndex(odegpuBatchID b, int step);
+
+/* Parity taps: run ONE step and copy out, per world in ODE's island/row
+ * order, the rows before scaling (32 floats per row: J[12], rhs at [24],
+ * cfm/h at [25], lo [26], hi [27], findex [28], b1 [29], b2 [30], joint [31],
+ * as int bits for the last four), lambda after SOR, and cforce per body.
+ * rows: [row_capacity][32], lambda: [row_capacity], fc: [nb_total][6]; the
+ * world's rows start at row_off[w] (returned, [n_worlds]). */
+int odegpuBatchStepTap(odegpuBatchID b, float* rows, float* lambda, float* fc, int* row_off);
+
+/* Contacts generated by the last step of world w (up to cap records of
+ * pos[3] normal[3] depth b1 b2 as floats); returns the count or an error. */
+int odegpuBatchGetContacts(odegpuBatchID b, int w, float* out, int cap);
+
+const char* odegpuGetLastError(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,547 @@
+// collide.cuh -- FP32 primitive narrowphase on the device.
+//
+// Each collider keeps the case structure of its reference counterpart (cited
+// per function) so that the number of contacts, their order and which feature
+// produced them match the reference on the same inputs; only the arithmetic
+// precision differs (FP32 here, FP64 in the oracle).
+#pragma once
+#include "dmath.cuh"
+
+namespace og {
+
+struct Contact {
+  float pos[3], normal[3], depth;
+};
+
+// Placement + class parameters of one geom as the colliders see it.
+struct GeomView {
+  int type;
+  float pos[3];
+  float R[12];
+  float p[4];   // sphere r / box sides / capsule r,len / plane a,b,c,d
+};
+
+enum { G_SPHERE = 0, G_BOX = 1, G_CAPSULE = 2, G_PLANE = 4, G_HEIGHTFIELD = 9 };
+constexpr unsigned kContactsUnimportant = 0x80000000u;
+
+// dCollideSpheres (ode/src/collision_util.cpp:38-67)
+OG_HD int collide_spheres(const float* p1, float r1, const float* p2, float r2, Contact* c) {
+  float t[3] = {p1[0] - p2[0], p1[1] - p2[1], p1[2] - p2[2]};
+  float d = sqrtf(t[0] * t[0] + t[1] * t[1] + t[2] * t[2]);
+  if (d > (r1 + r2)) return 0;
+  if (d <= 0.f) {
+    c->pos[0] = p1[0]; c->pos[1] = p1[1]; c->pos[2] = p1[2];
+    c->normal[0] = 1.f; c->normal[1] = 0.f; c->normal[2] = 0.f;
+    c->depth = r1 + r2;
+  } else {
+    float d1 = 1.0f / d;
+    c->normal[0] = (p1[0] - p2[0]) * d1;
+    c->normal[1] = (p1[1] - p2[1]) * d1;
+    c->normal[2] = (p1[2] - p2[2]) * d1;
+    float k = 0.5f * (r2 - r1 - d);
+    c->pos[0] = p1[0] + c->normal[0] * k;
+    c->pos[1] = p1[1] + c->normal[1] * k;
+    c->pos[2] = p1[2] + c->normal[2] * k;
+    c->depth = r1 + r2 - d;
+  }
+  return 1;
+}
+
+// dCollideSphereBox (ode/src/sphere.cpp:131-219)
+OG_HD int collide_sphere_box(const GeomView& s, const GeomView& b, Contact* c) {
+  float l[3], t[4], p[3], q[3], r[3];
+  int onborder = 0;
+  const float* R = b.R;
+  p[0] = s.pos[0] - b.pos[0];
+  p[1] = s.pos[1] - b.pos[1];
+  p[2] = s.pos[2] - b.pos[2];
+  for (int i = 0; i < 3; ++i) {
+    l[i] = b.p[i] * 0.5f;
+    t[i] = dot3s(p, R + i, 1, 4);
+    if (t[i] < -l[i]) { t[i] = -l[i]; onborder = 1; }
+    if (t[i] > l[i]) { t[i] = l[i]; onborder = 1; }
+  }
+  if (!onborder) {
+    float min_distance = l[0] - fabsf(t[0]);
+    int mini = 0;
+    for (int i = 1; i < 3; i++) {
+      float fd = l[i] - fabsf(t[i]);
+      if (fd < min_distance) { min_distance = fd; mini = i; }
+    }
+    c->pos[0] = s.pos[0]; c->pos[1] = s.pos[1]; c->pos[2] = s.pos[2];
+    float tmp[3] = {0.f, 0.f, 0.f};
+    tmp[mini] = (t[mini] > 0.f) ? 1.0f : -1.0f;
+    mul0_331(c->normal, R, tmp);
+    c->depth = min_distance + s.p[0];
+    return 1;
+  }
+  t[3] = 0.f;
+  mul0_331(q, R, t);
+  r[0] = p[0] - q[0]; r[1] = p[1] - q[1]; r[2] = p[2] - q[2];
+  float depth = s.p[0] - sqrtf(dot3(r, r));
+  if (depth < 0.f) return 0;
+  c->pos[0] = q[0] + b.pos[0];
+  c->pos[1] = q[1] + b.pos[1];
+  c->pos[2] = q[2] + b.pos[2];
+  c->normal[0] = r[0]; c->normal[1] = r[1]; c->normal[2] = r[2];
+  safe_normalize3(c->normal);
+  c->depth = depth;
+  return 1;
+}
+
+// dCollideSpherePlane (ode/src/sphere.cpp:222-251)
+OG_HD int collide_sphere_plane(const GeomView& s, const GeomView& pl, Contact* c) {
+  const float* P = pl.p;
+  float k = dot3(s.pos, P);
+  float depth = P[3] - k + s.p[0];
+  if (depth >= 0.f) {
+    c->normal[0] = P[0]; c->normal[1] = P[1]; c->normal[2] = P[2];
+    c->pos[0] = s.pos[0] - P[0] * s.p[0];
+    c->pos[1] = s.pos[1] - P[1] * s.p[0];
+    c->pos[2] = s.pos[2] - P[2] * s.p[0];
+    c->depth = depth;
+    return 1;
+  }
+  return 0;
+}
+
+// dLineClosestApproach (ode/src/collision_util.cpp:70-92)
+OG_HD void line_closest_approach(const float* pa, const float* ua, const float* pb, const float* ub,
+                                 float* alpha, float* beta) {
+  float p[3] = {pb[0] - pa[0], pb[1] - pa[1], pb[2] - pa[2]};
+  float uaub = dot3(ua, ub);
+  float q1 = dot3(ua, p);
+  float q2 = -dot3(ub, p);
+  float d = 1.f - uaub * uaub;
+  if (d <= 0.0001f) { *alpha = 0.f; *beta = 0.f; }
+  else {
+    d = 1.0f / d;
+    *alpha = (q1 + uaub * q2) * d;
+    *beta = (uaub * q1 + q2) * d;
+  }
+}
+
+// intersectRectQuad (ode/src/box.cpp:187-245): clip the quad p against the
+// rectangle |x| < h[0], |y| < h[1]; emits points in the reference's order.
+OG_HD int intersect_rect_quad(const float h[2], float p[8], float ret[16]) {
+  int nq = 4, nr = 0;
+  float buffer[16];
+  float* q = p;
+  float* r = ret;
+  for (int dir = 0; dir <= 1; dir++) {
+    for (int sign = -1; sign <= 1; sign += 2) {
+      float* pq = q;
+      float* pr = r;
+      nr = 0;
+      for (int i = nq; i > 0; i--) {
+        if (sign * pq[dir] < h[dir]) {
+          pr[0] = pq[0]; pr[1] = pq[1];
+          pr += 2; nr++;
+          if (nr & 8) { q = r; goto done; }
+        }
+        float* nextq = (i > 1) ? pq + 2 : q;
+        if ((sign * pq[dir] < h[dir]) ^ (sign * nextq[dir] < h[dir])) {
+          pr[1 - dir] = pq[1 - dir] + (nextq[1 - dir] - pq[1 - dir]) / (nextq[dir] - pq[dir]) *
+                                          (sign * h[dir] - pq[dir]);
+          pr[dir] = sign * h[dir];
+          pr += 2; nr++;
+          if (nr & 8) { q = r; goto done; }
+        }
+        pq += 2;
+      }
+      q = r;
+      r = (q == ret) ? buffer : ret;
+      nq = nr;
+    }
+  }
+done:
+  if (q != ret)
+    for (int i = 0; i < nr * 2; ++i) ret[i] = q[i];
+  return nr;
+}
+
+// cullPoints (ode/src/box.cpp:249-322)
+OG_HD void cull_points(int n, const float p[], int m, int i0, int iret[]) {
+  int i, j;
+  float a, cx, cy, q;
+  if (n == 1) { cx = p[0]; cy = p[1]; }
+  else if (n == 2) { cx = 0.5f * (p[0] + p[2]); cy = 0.5f * (p[1] + p[3]); }
+  else {
+    a = 0.f; cx = 0.f; cy = 0.f;
+    for (i = 0; i < (n - 1); i++) {
+      q = p[i * 2] * p[i * 2 + 3] - p[i * 2 + 2] * p[i * 2 + 1];
+      a += q;
+      cx += q * (p[i * 2] + p[i * 2 + 2]);
+      cy += q * (p[i * 2 + 1] + p[i * 2 + 3]);
+    }
+    q = p[n * 2 - 2] * p[1] - p[0] * p[n * 2 - 1];
+    a = 1.0f / (3.0f * (a + q));
+    cx = a * (cx + q * (p[n * 2 - 2] + p[0]));
+    cy = a * (cy + q * (p[n * 2 - 1] + p[1]));
+  }
+  float A[8];
+  for (i = 0; i < n; i++) A[i] = atan2f(p[i * 2 + 1] - cy, p[i * 2] - cx);
+  int avail[8];
+  for (i = 0; i < n; i++) avail[i] = 1;
+  avail[i0] = 0;
+  iret[0] = i0;
+  int k = 1;
+  // The reference mixes a double-precision pi into these FP32 expressions
+  // (M_PI is double in <math.h>); the same promotions are kept here.
+  const double kPiD = 3.14159265358979323846;
+  for (j = 1; j < m; j++) {
+    a = (float)((double)j * (2.0 * kPiD / m) + (double)A[i0]);
+    if ((double)a > kPiD) a -= (float)(2.0 * kPiD);
+    float maxdiff = 1e9f, diff;
+    int best = i0;
+    for (i = 0; i < n; i++) {
+      if (avail[i]) {
+        diff = fabsf(A[i] - a);
+        if ((double)diff > kPiD) diff = (float)(2.0 * kPiD - (double)diff);
+        if (diff < maxdiff) { maxdiff = diff; best = i; }
+      }
+    }
+    iret[k] = best;
+    avail[best] = 0;
+    k++;
+  }
+}
+
+// dBoxBox (ode/src/box.cpp:331-713): separating-axis test over 15 axes (1.05
+// fudge on the edge axes), then edge-edge or face clipping + culling.
+OG_HD int box_box(const float* p1, const float* R1, const float* side1, const float* p2,
+                  const float* R2, const float* side2, float* normal, unsigned flags,
+                  Contact* contact) {
+  const float fudge_factor = 1.05f;
+  float p[3], pp[3], normalC[3] = {0.f, 0.f, 0.f};
+  const float* normalR = nullptr;
+  float A[3], B[3], s, s2, l, e1;
+  int invert_normal, code;
+  p[0] = p2[0] - p1[0]; p[1] = p2[1] - p1[1]; p[2] = p2[2] - p1[2];
+  mul1_331(pp, R1, p);
+  A[0] = side1[0] * 0.5f; A[1] = side1[1] * 0.5f; A[2] = side1[2] * 0.5f;
+  B[0] = side2[0] * 0.5f; B[1] = side2[1] * 0.5f; B[2] = side2[2] * 0.5f;
+  const float R11 = dot3s(R1 + 0, R2 + 0, 4, 4), R12 = dot3s(R1 + 0, R2 + 1, 4, 4), R13 = dot3s(R1 + 0, R2 + 2, 4, 4);
+  const float R21 = dot3s(R1 + 1, R2 + 0, 4, 4), R22 = dot3s(R1 + 1, R2 + 1, 4, 4), R23 = dot3s(R1 + 1, R2 + 2, 4, 4);
+  const float R31 = dot3s(R1 + 2, R2 + 0, 4, 4), R32 = dot3s(R1 + 2, R2 + 1, 4, 4), R33 = dot3s(R1 + 2, R2 + 2, 4, 4);
+  const float Q11 = fabsf(R11), Q12 = fabsf(R12), Q13 = fabsf(R13);
+  const float Q21 = fabsf(R21), Q22 = fabsf(R22), Q23 = fabsf(R23);
+  const float Q31 = fabsf(R31), Q32 = fabsf(R32), Q33 = fabsf(R33);
+  s = -INFINITY;
+  invert_normal = 0;
+  code = 0;
+  do {
+#define OG_TST_FACE(expr1, expr2, norm, cc)                          \
+  e1 = (expr1);                                                      \
+  s2 = fabsf(e1) - (expr2);                                          \
+  if (s2 > 0.f) return 0;                                            \
+  if (s2 > s) {                                                      \
+    s = s2; normalR = norm; invert_normal = (e1 < 0.f); code = (cc); \
+    if (flags & kContactsUnimportant) break;                         \
+  }
+    OG_TST_FACE(pp[0], (A[0] + B[0] * Q11 + B[1] * Q12 + B[2] * Q13), R1 + 0, 1);
+    OG_TST_FACE(pp[1], (A[1] + B[0] * Q21 + B[1] * Q22 + B[2] * Q23), R1 + 1, 2);
+    OG_TST_FACE(pp[2], (A[2] + B[0] * Q31 + B[1] * Q32 + B[2] * Q33), R1 + 2, 3);
+    OG_TST_FACE(dot3s(R2 + 0, p, 4, 1), (A[0] * Q11 + A[1] * Q21 + A[2] * Q31 + B[0]), R2 + 0, 4);
+    OG_TST_FACE(dot3s(R2 + 1, p, 4, 1), (A[0] * Q12 + A[1] * Q22 + A[2] * Q32 + B[1]), R2 + 1, 5);
+    OG_TST_FACE(dot3s(R2 + 2, p, 4, 1), (A[0] * Q13 + A[1] * Q23 + A[2] * Q33 + B[2]), R2 + 2, 6);
+#undef OG_TST_FACE
+#define OG_TST_EDGE(expr1, expr2, n1, n2, n3, cc)                        \
+  e1 = (expr1);                                                          \
+  s2 = fabsf(e1) - (expr2);                                              \
+  if (s2 > 0.f) return 0;                                                \
+  l = sqrtf((n1) * (n1) + (n2) * (n2) + (n3) * (n3));                    \
+  if (l > 0.f) {                                                         \
+    s2 /= l;                                                             \
+    if (s2 * fudge_factor > s) {                                         \
+      s = s2; normalR = nullptr;                                         \
+      normalC[0] = (n1) / l; normalC[1] = (n2) / l; normalC[2] = (n3) / l; \
+      invert_normal = (e1 < 0.f); code = (cc);                           \
+      if (flags & kContactsUnimportant) break;                           \
+    }                                                                    \
+  }
+    OG_TST_EDGE(pp[2] * R21 - pp[1] * R31, (A[1] * Q31 + A[2] * Q21 + B[1] * Q13 + B[2] * Q12), 0.f, -R31, R21, 7);
+    OG_TST_EDGE(pp[2] * R22 - pp[1] * R32, (A[1] * Q32 + A[2] * Q22 + B[0] * Q13 + B[2] * Q11), 0.f, -R32, R22, 8);
+    OG_TST_EDGE(pp[2] * R23 - pp[1] * R33, (A[1] * Q33 + A[2] * Q23 + B[0] * Q12 + B[1] * Q11), 0.f, -R33, R23, 9);
+    OG_TST_EDGE(pp[0] * R31 - pp[2] * R11, (A[0] * Q31 + A[2] * Q11 + B[1] * Q23 + B[2] * Q22), R31, 0.f, -R11, 10);
+    OG_TST_EDGE(pp[0] * R32 - pp[2] * R12, (A[0] * Q32 + A[2] * Q12 + B[0] * Q23 + B[2] * Q21), R32, 0.f, -R12, 11);
+    OG_TST_EDGE(pp[0] * R33 - pp[2] * R13, (A[0] * Q33 + A[2] * Q13 + B[0] * Q22 + B[1] * Q21), R33, 0.f, -R13, 12);
+    OG_TST_EDGE(pp[1] * R11 - pp[0] * R21, (A[0] * Q21 + A[1] * Q11 + B[1] * Q33 + B[2] * Q32), -R21, R11, 0.f, 13);
+    OG_TST_EDGE(pp[1] * R12 - pp[0] * R22, (A[0] * Q22 + A[1] * Q12 + B[0] * Q33 + B[2] * Q31), -R22, R12, 0.f, 14);
+    OG_TST_EDGE(pp[1] * R13 - pp[0] * R23, (A[0] * Q23 + A[1] * Q13 + B[0] * Q32 + B[1] * Q31), -R23, R13, 0.f, 15);
+#undef OG_TST_EDGE
+  } while (0);
+  if (!code) return 0;
+  if (normalR) {
+    normal[0] = normalR[0]; normal[1] = normalR[4]; normal[2] = normalR[8];
+  } else {
+    mul0_331(normal, R1, normalC);
+  }
+  if (invert_normal) { normal[0] = -normal[0]; normal[1] = -normal[1]; normal[2] = -normal[2]; }
+  const float depth = -s;
+  int i, j;
+  if (code > 6) {
+    float pa[3], pb[3], sign, alpha, beta, ua[3], ub[3];
+    for (i = 0; i < 3; i++) pa[i] = p1[i];
+    for (j = 0; j < 3; j++) {
+      sign = (dot3s(normal, R1 + j, 1, 4) > 0.f) ? 1.0f : -1.0f;
+      for (i = 0; i < 3; i++) pa[i] += sign * A[j] * R1[i * 4 + j];
+    }
+    for (i = 0; i < 3; i++) pb[i] = p2[i];
+    for (j = 0; j < 3; j++) {
+      sign = (dot3s(normal, R2 + j, 1, 4) > 0.f) ? -1.0f : 1.0f;
+      for (i = 0; i < 3; i++) pb[i] += sign * B[j] * R2[i * 4 + j];
+    }
+    for (i = 0; i < 3; i++) ua[i] = R1[((code)-7) / 3 + i * 4];
+    for (i = 0; i < 3; i++) ub[i] = R2[((code)-7) % 3 + i * 4];
+    line_closest_approach(pa, ua, pb, ub, &alpha, &beta);
+    for (i = 0; i < 3; i++) pa[i] += ua[i] * alpha;
+    for (i = 0; i < 3; i++) pb[i] += ub[i] * beta;
+    for (i = 0; i < 3; i++) contact[0].pos[i] = 0.5f * (pa[i] + pb[i]);
+    contact[0].depth = depth;
+    return 1;
+  }
+  const float *Ra, *Rb, *pa, *pb, *Sa, *Sb;
+  if (code <= 3) { Ra = R1; Rb = R2; pa = p1; pb = p2; Sa = A; Sb = B; }
+  else { Ra = R2; Rb = R1; pa = p2; pb = p1; Sa = B; Sb = A; }
+  float normal2[3], nr[3], anr[3];
+  if (code <= 3) { normal2[0] = normal[0]; normal2[1] = normal[1]; normal2[2] = normal[2]; }
+  else { normal2[0] = -normal[0]; normal2[1] = -normal[1]; normal2[2] = -normal[2]; }
+  mul1_331(nr, Rb, normal2);
+  anr[0] = fabsf(nr[0]); anr[1] = fabsf(nr[1]); anr[2] = fabsf(nr[2]);
+  int lanr, a1, a2;
+  if (anr[1] > anr[0]) {
+    if (anr[1] > anr[2]) { a1 = 0; lanr = 1; a2 = 2; }
+    else { a1 = 0; a2 = 1; lanr = 2; }
+  } else {
+    if (anr[0] > anr[2]) { lanr = 0; a1 = 1; a2 = 2; }
+    else { a1 = 0; a2 = 1; lanr = 2; }
+  }
+  float center[3];
+  if (nr[lanr] < 0.f) {
+    for (i = 0; i < 3; i++) center[i] = pb[i] - pa[i] + Sb[lanr] * Rb[i * 4 + lanr];
+  } else {
+    for (i = 0; i < 3; i++) center[i] = pb[i] - pa[i] - Sb[lanr] * Rb[i * 4 + lanr];
+  }
+  int codeN, code1, code2;
+  codeN = (code <= 3) ? code - 1 : code - 4;
+  if (codeN == 0) { code1 = 1; code2 = 2; }
+  else if (codeN == 1) { code1 = 0; code2 = 2; }
+  else { code1 = 0; code2 = 1; }
+  float quad[8];
+  const float c1 = dot3s(center, Ra + code1, 1, 4);
+  const float c2 = dot3s(center, Ra + code2, 1, 4);
+  float m11 = dot3s(Ra + code1, Rb + a1, 4, 4);
+  float m12 = dot3s(Ra + code1, Rb + a2, 4, 4);
+  float m21 = dot3s(Ra + code2, Rb + a1, 4, 4);
+  float m22 = dot3s(Ra + code2, Rb + a2, 4, 4);
+  {
+    float k1 = m11 * Sb[a1], k2 = m21 * Sb[a1], k3 = m12 * Sb[a2], k4 = m22 * Sb[a2];
+    quad[0] = c1 - k1 - k3; quad[1] = c2 - k2 - k4;
+    quad[2] = c1 - k1 + k3; quad[3] = c2 - k2 + k4;
+    quad[4] = c1 + k1 + k3; quad[5] = c2 + k2 + k4;
+    quad[6] = c1 + k1 - k3; quad[7] = c2 + k2 - k4;
+  }
+  const float rect[2] = {Sa[code1], Sa[code2]};
+  float ret[16];
+  const int n = intersect_rect_quad(rect, quad, ret);
+  if (n < 1) return 0;
+  float point[3 * 8], dep[8];
+  const float det1 = 1.0f / (m11 * m22 - m12 * m21);
+  m11 *= det1; m12 *= det1; m21 *= det1; m22 *= det1;
+  int cnum = 0;
+  for (j = 0; j < n; j++) {
+    float k1 = m22 * (ret[j * 2] - c1) - m12 * (ret[j * 2 + 1] - c2);
+    float k2 = -m21 * (ret[j * 2] - c1) + m11 * (ret[j * 2 + 1] - c2);
+    for (i = 0; i < 3; i++) point[cnum * 3 + i] = center[i] + k1 * Rb[i * 4 + a1] + k2 * Rb[i * 4 + a2];
+    dep[cnum] = Sa[codeN] - dot3(normal2, point + cnum * 3);
+    if (dep[cnum] >= 0.f) {
+      ret[cnum * 2] = ret[j * 2];
+      ret[cnum * 2 + 1] = ret[j * 2 + 1];
+      cnum++;
+      if ((cnum | kContactsUnimportant) == (flags & (0xffffu | kContactsUnimportant))) break;
+    }
+  }
+  if (cnum < 1) return 0;
+  int maxc = flags & 0xffff;
+  if (maxc > cnum) maxc = cnum;
+  if (maxc < 1) maxc = 1;
+  if (cnum <= maxc) {
+    for (j = 0; j < cnum; j++) {
+      for (i = 0; i < 3; i++) contact[j].pos[i] = point[j * 3 + i] + pa[i];
+      contact[j].depth = dep[j];
+    }
+  } else {
+    int i1 = 0;
+    float maxdepth = dep[0];
+    for (i = 1; i < cnum; i++) {
+      if (dep[i] > maxdepth) { maxdepth = dep[i]; i1 = i; }
+    }
+    int iret[8];
+    cull_points(cnum, ret, maxc, i1, iret);
+    for (j = 0; j < maxc; j++) {
+      for (i = 0; i < 3; i++) contact[j].pos[i] = point[iret[j] * 3 + i] + pa[i];
+      contact[j].depth = dep[iret[j]];
+    }
+    cnum = maxc;
+  }
+  return cnum;
+}
+
+// dCollideBoxBox (ode/src/box.cpp:716-742): normal returned negated.
+OG_HD int collide_box_box(const GeomView& a, const GeomView& b, unsigned flags, Contact* c) {
+  float normal[3];
+  const int num = box_box(a.pos, a.R, a.p, b.pos, b.R, b.p, normal, flags, c);
+  for (int i = 0; i < num; i++) {
+    c[i].normal[0] = -normal[0]; c[i].normal[1] = -normal[1]; c[i].normal[2] = -normal[2];
+  }
+  return num;
+}
+
+// dCollideBoxPlane (ode/src/box.cpp:745-878): deepest vertex, then vertices
+// along the two sides with the smallest projections, the fourth by vector sum.
+OG_HD int collide_box_plane(const GeomView& bx, const GeomView& pl, unsigned flags, Contact* c) {
+  const float* R = bx.R;
+  const float* n = pl.p;
+  const float* side = bx.p;
+  const float Aa[3] = {side[0] * dot3s(n, R + 0, 1, 4), side[1] * dot3s(n, R + 1, 1, 4),
+                       side[2] * dot3s(n, R + 2, 1, 4)};
+  const float Bb[3] = {fabsf(Aa[0]), fabsf(Aa[1]), fabsf(Aa[2])};
+  const float depth = n[3] + 0.5f * (Bb[0] + Bb[1] + Bb[2]) - dot3(n, bx.pos);
+  if (depth < 0.f) return 0;
+  int maxc = flags & 0xffff;
+  if (maxc > 4) maxc = 4;
+  float p[3] = {bx.pos[0], bx.pos[1], bx.pos[2]};
+  for (int i = 0; i < 3; ++i) {
+    const float sgn = (Aa[i] > 0.f) ? -0.5f : 0.5f;
+    p[0] += sgn * side[i] * R[0 + i];
+    p[1] += sgn * side[i] * R[4 + i];
+    p[2] += sgn * side[i] * R[8 + i];
+  }
+  c[0].pos[0] = p[0]; c[0].pos[1] = p[1]; c[0].pos[2] = p[2];
+  c[0].depth = depth;
+  int ret = 1;
+  if (maxc > 1) {
+    // sequence of sides to walk, as chosen by the reference's branch ladder
+    int s1, s2;
+    if (Bb[0] < Bb[1]) {
+      if (Bb[2] < Bb[0]) { s1 = 2; s2 = (Bb[0] < Bb[1]) ? 0 : 1; }
+      else { s1 = 0; s2 = (Bb[1] < Bb[2]) ? 1 : 2; }
+    } else {
+      if (Bb[2] < Bb[1]) { s1 = 2; s2 = (Bb[0] < Bb[1]) ? 0 : 1; }
+      else { s1 = 1; s2 = (Bb[0] < Bb[2]) ? 0 : 2; }
+    }
+    const int seq[2] = {s1, s2};
+    for (int k = 0; k < 2 && k + 1 < maxc; ++k) {
+      const int sd = seq[k];
+      if (depth - Bb[sd] < 0.f) break;
+      const float sg = (Aa[sd] > 0.f) ? 1.f : -1.f;
+      c[k + 1].pos[0] = p[0] + sg * side[sd] * R[0 + sd];
+      c[k + 1].pos[1] = p[1] + sg * side[sd] * R[4 + sd];
+      c[k + 1].pos[2] = p[2] + sg * side[sd] * R[8 + sd];
+      c[k + 1].depth = depth - Bb[sd];
+      ret++;
+    }
+  }
+  if (maxc == 4 && ret == 3) {
+    const float d4 = c[1].depth + c[2].depth - depth;
+    if (d4 > 0.f) {
+      c[3].pos[0] = c[1].pos[0] + c[2].pos[0] - p[0];
+      c[3].pos[1] = c[1].pos[1] + c[2].pos[1] - p[1];
+      c[3].pos[2] = c[1].pos[2] + c[2].pos[2] - p[2];
+      c[3].depth = d4;
+      ret++;
+    }
+  }
+  for (int i = 0; i < ret; i++) {
+    c[i].normal[0] = n[0]; c[i].normal[1] = n[1]; c[i].normal[2] = n[2];
+  }
+  return ret;
+}
+
+// dCollideCapsulePlane (ode/src/capsule.cpp:352-411)
+OG_HD int collide_capsule_plane(const GeomView& cp, const GeomView& pl, unsigned flags, Contact* c) {
+  const float* R = cp.R;
+  const float* P = pl.p;
+  const float radius = cp.p[0], lz = cp.p[1];
+  const float sign = (dot3s(P, R + 2, 1, 4) > 0.f) ? -1.0f : 1.0f;
+  float p[3];
+  p[0] = cp.pos[0] + R[2] * lz * 0.5f * sign;
+  p[1] = cp.pos[1] + R[6] * lz * 0.5f * sign;
+  p[2] = cp.pos[2] + R[10] * lz * 0.5f * sign;
+  float k = dot3(p, P);
+  float depth = P[3] - k + radius;
+  if (depth < 0.f) return 0;
+  c[0].normal[0] = P[0]; c[0].normal[1] = P[1]; c[0].normal[2] = P[2];
+  c[0].pos[0] = p[0] - P[0] * radius;
+  c[0].pos[1] = p[1] - P[1] * radius;
+  c[0].pos[2] = p[2] - P[2] * radius;
+  c[0].depth = depth;
+  int nc = 1;
+  if ((flags & 0xffff) >= 2) {
+    p[0] = cp.pos[0] - R[2] * lz * 0.5f * sign;
+    p[1] = cp.pos[1] - R[6] * lz * 0.5f * sign;
+    p[2] = cp.pos[2] - R[10] * lz * 0.5f * sign;
+    k = dot3(p, P);
+    depth = P[3] - k + radius;
+    if (depth >= 0.f) {
+      c[1].normal[0] = P[0]; c[1].normal[1] = P[1]; c[1].normal[2] = P[2];
+      c[1].pos[0] = p[0] - P[0] * radius;
+      c[1].pos[1] = p[1] - P[1] * radius;
+      c[1].pos[2] = p[2] - P[2] * radius;
+      c[1].depth = depth;
+      nc = 2;
+    }
+  }
+  return nc;
+}
+
+// Collider table for this path (ode/src/collision_kernel.cpp:167-268): returns
+// a collider id and whether the call runs with the geoms swapped (in which case
+// dCollide negates the normals, :319-335).
+enum { CL_NONE = 0, CL_SS, CL_SB, CL_SP, CL_BB, CL_BP, CL_CP, CL_HF };
+OG_HD int collider_of(int t1, int t2, int* reverse) {
+  *reverse = 0;
+  auto is = [&](int a, int b) { return t1 == a && t2 == b; };
+  if (is(G_SPHERE, G_SPHERE)) return CL_SS;
+  if (is(G_SPHERE, G_BOX)) return CL_SB;
+  if (is(G_BOX, G_SPHERE)) { *reverse = 1; return CL_SB; }
+  if (is(G_SPHERE, G_PLANE)) return CL_SP;
+  if (is(G_PLANE, G_SPHERE)) { *reverse = 1; return CL_SP; }
+  if (is(G_BOX, G_BOX)) return CL_BB;
+  if (is(G_BOX, G_PLANE)) return CL_BP;
+  if (is(G_PLANE, G_BOX)) { *reverse = 1; return CL_BP; }
+  if (is(G_CAPSULE, G_PLANE)) return CL_CP;
+  if (is(G_PLANE, G_CAPSULE)) { *reverse = 1; return CL_CP; }
+  if (t1 == G_HEIGHTFIELD && (t2 == G_SPHERE || t2 == G_BOX || t2 == G_CAPSULE)) return CL_HF;
+  if (t2 == G_HEIGHTFIELD && (t1 == G_SPHERE || t1 == G_BOX || t1 == G_CAPSULE)) { *reverse = 1; return CL_HF; }
+  return CL_NONE;
+}
+
+// dCollide for the classes above without a heightfield (the heightfield has
+// its own entry in heightfield.cuh). `c` must hold 4 (or flags & 0xffff, at
+// most 8) contacts.
+OG_HD int collide_primitive(const GeomView& g1, const GeomView& g2, unsigned flags, Contact* c) {
+  if ((flags & 0xffff) == 0) return 0;
+  int rev;
+  const int id = collider_of(g1.type, g2.type, &rev);
+  const GeomView& a = rev ? g2 : g1;
+  const GeomView& b = rev ? g1 : g2;
+  int n = 0;
+  switch (id) {
+    case CL_SS: n = collide_spheres(a.pos, a.p[0], b.pos, b.p[0], c); break;
+    case CL_SB: n = collide_sphere_box(a, b, c); break;
+    case CL_SP: n = collide_sphere_plane(a, b, c); break;
+    case CL_BB: n = collide_box_box(a, b, flags, c); break;
+    case CL_BP: n = collide_box_plane(a, b, flags, c); break;
+    case CL_CP: n = collide_capsule_plane(a, b, flags, c); break;
+    default: n = 0;
+  }
+  if (rev)
+    for (int i = 0; i < n; ++i) {
+      c[i].normal[0] = -c[i].normal[0]; c[i].normal[1] = -c[i].normal[1]; c[i].normal[2] = -c[i].normal[2];
+    }
+  return n;
+}
+
+}  // namespace og

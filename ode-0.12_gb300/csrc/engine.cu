@@ -1,0 +1,650 @@
+// engine.cu -- batch of ODE worlds on the GPU: upload, the persistent
+// warp-per-world step kernel, graph capture, state exchange and the C ABI of
+// include/odegpu.h.
+#include <cuda_runtime.h>
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "odegpu.h"
+#include "engine_types.cuh"
+#include "world_solve.cuh"
+#include "host_setup.hpp"
+
+using namespace og;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+#define OG_CUDA(call)                                                              \
+  do {                                                                             \
+    cudaError_t e_ = (call);                                                       \
+    if (e_ != cudaSuccess)                                                         \
+      return fail(ODEGPU_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+// Step kernel: warp w of the grid owns world (first_world + w) and runs
+// n_steps steps of it back to back. Warps never wait on each other.
+__global__ void __launch_bounds__(128) world_step_kernel(BatchDev d, int first_world, int n_worlds,
+                                                         int step0, int n_steps, StepOptions opt) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int w = first_world + blockIdx.x * (blockDim.x >> 5) + warp;
+  if (w >= first_world + n_worlds || w >= d.n_worlds) return;
+  const WarpSmem S = carve_smem(smem_raw + (size_t)warp * kSmemPerWarp);
+  if (d.world[w].nb > kMaxB) {
+    if (lane == 0) atomicOr(&d.status[w], ST_TOO_LARGE);
+    return;
+  }
+  for (int s = 0; s < n_steps; ++s) world_step(d, w, step0 + s, S, lane, opt);
+}
+
+// State exchange: FP32 records of 13 floats per body.
+__global__ void pack_state_kernel(BatchDev d, int nb, float* out) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nb) return;
+  const float4 p = d.pos[b], q = d.q[b], v = d.lvel[b], w = d.avel[b];
+  float* o = out + (size_t)b * ODEGPU_BODY_REC;
+  o[0] = p.x; o[1] = p.y; o[2] = p.z;
+  o[3] = q.x; o[4] = q.y; o[5] = q.z; o[6] = q.w;
+  o[7] = v.x; o[8] = v.y; o[9] = v.z;
+  o[10] = w.x; o[11] = w.y; o[12] = w.z;
+}
+__global__ void unpack_state_kernel(BatchDev d, int nb, const float* in) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nb) return;
+  const float* o = in + (size_t)b * ODEGPU_BODY_REC;
+  d.pos[b] = make_float4(o[0], o[1], o[2], 0.f);
+  d.q[b] = make_float4(o[3], o[4], o[5], o[6]);
+  d.lvel[b] = make_float4(o[7], o[8], o[9], 0.f);
+  d.avel[b] = make_float4(o[10], o[11], o[12], 0.f);
+}
+
+template <class T>
+struct DBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  ~DBuf() { if (p) cudaFree(p); }
+  int alloc(size_t count) {
+    n = count;
+    if (count == 0) count = 1;
+    if (cudaMalloc(&p, count * sizeof(T)) != cudaSuccess) {
+      cudaGetLastError();
+      p = nullptr;
+      return fail(ODEGPU_E_NOMEM, "cudaMalloc failed for " + std::to_string(count * sizeof(T)) + " bytes");
+    }
+    return 0;
+  }
+  int upload(const std::vector<T>& v) {
+    if (int rc = alloc(v.size())) return rc;
+    if (!v.empty() && cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice) != cudaSuccess)
+      return fail(ODEGPU_E_CUDA, "upload failed");
+    return 0;
+  }
+};
+
+}  // namespace
+
+struct odegpuBatch {
+  int device = 0;
+  int n_worlds = 0, nb_total = 0, ng_total = 0, nj_total = 0;
+  long long row_cap_total = 0, contact_cap_total = 0;
+  int warps_per_block = 4;
+  int step_counter = 0;
+  cudaStream_t stream = nullptr;
+  std::vector<WorldDesc> h_world;
+
+  DBuf<WorldDesc> world;
+  DBuf<unsigned> seed;
+  DBuf<int> status, ncontacts, nrows, nislands;
+  DBuf<float4> pos, q, lvel, avel, facc, tacc;
+  DBuf<float> mass, invMass, I, invI, invIw;
+  DBuf<int> bflags;
+  DBuf<int> gtype, gbody, gsurf;
+  DBuf<float4> gparam, gpos;
+  DBuf<float> gbound;
+  DBuf<DevSurface> surfaces;
+  DBuf<DevJoint> joints;
+  DBuf<int> padj_start, padj;
+  DBuf<float> joint_torque, body_force;
+  int n_ctrl_steps = 0;
+  DBuf<DevContact> contacts;
+  DBuf<float> rows;
+  DBuf<int> jlist, adj, adj_start, island_jstart, island_rstart, jrow, jm;
+  DBuf<float> state_scratch;
+
+  BatchDev dev() const {
+    BatchDev d;
+    d.n_worlds = n_worlds;
+    d.world = world.p;
+    d.seed = seed.p; d.status = status.p; d.ncontacts = ncontacts.p; d.nrows = nrows.p;
+    d.nislands = nislands.p;
+    d.pos = pos.p; d.q = q.p; d.lvel = lvel.p; d.avel = avel.p;
+    d.mass = mass.p; d.invMass = invMass.p; d.I = I.p; d.invI = invI.p; d.bflags = bflags.p;
+    d.invIw = invIw.p; d.facc = facc.p; d.tacc = tacc.p;
+    d.gtype = gtype.p; d.gbody = gbody.p; d.gparam = gparam.p; d.gbound = gbound.p; d.gpos = gpos.p;
+    d.gsurf = gsurf.p; d.surfaces = surfaces.p;
+    d.joints = joints.p; d.padj_start = padj_start.p; d.padj = padj.p;
+    d.n_ctrl_steps = n_ctrl_steps;
+    d.joint_torque = n_ctrl_steps > 0 ? joint_torque.p : nullptr;
+    d.body_force = n_ctrl_steps > 0 ? body_force.p : nullptr;
+    d.step_counter_base = 0;
+    d.contacts = contacts.p; d.rows = rows.p; d.jlist = jlist.p; d.adj = adj.p;
+    d.adj_start = adj_start.p; d.island_jstart = island_jstart.p; d.island_rstart = island_rstart.p;
+    d.jrow = jrow.p; d.jm = jm.p;
+    return d;
+  }
+
+  int launch(int first, int count, int n_steps, const StepOptions& opt) {
+    const int wpb = warps_per_block;
+    const int blocks = (count + wpb - 1) / wpb;
+    const size_t smem = (size_t)wpb * kSmemPerWarp;
+    world_step_kernel<<<blocks, wpb * 32, smem, stream>>>(dev(), first, count, step_counter, n_steps, opt);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(ODEGPU_E_CUDA, std::string("step launch: ") + cudaGetErrorString(e));
+    return 0;
+  }
+};
+
+extern "C" {
+
+const char* odegpuGetLastError(void) { return g_last_error.c_str(); }
+
+static float bound_radius(int type, const double* p) {
+  switch (type) {
+    case ODEGPU_GEOM_SPHERE: return (float)p[0];
+    case ODEGPU_GEOM_BOX: return (float)(0.5 * std::sqrt(p[0] * p[0] + p[1] * p[1] + p[2] * p[2]));
+    case ODEGPU_GEOM_CAPSULE: return (float)(p[0] + 0.5 * p[1]);
+    default: return INFINITY;
+  }
+}
+
+static int set_controls(odegpuBatch* B, int n_ctrl, const double* jt, const double* bf) {
+  B->n_ctrl_steps = n_ctrl;
+  if (n_ctrl <= 0) { B->n_ctrl_steps = 0; return 0; }
+  std::vector<float> t, f;
+  if (jt) {
+    t.resize((size_t)n_ctrl * B->nj_total * 2);
+    for (size_t i = 0; i < t.size(); ++i) t[i] = (float)jt[i];
+  }
+  if (bf) {
+    f.resize((size_t)n_ctrl * B->nb_total * 6);
+    for (size_t i = 0; i < f.size(); ++i) f[i] = (float)bf[i];
+  }
+  if (B->joint_torque.p) { cudaFree(B->joint_torque.p); B->joint_torque.p = nullptr; }
+  if (B->body_force.p) { cudaFree(B->body_force.p); B->body_force.p = nullptr; }
+  if (jt) { if (int rc = B->joint_torque.upload(t)) return rc; }
+  if (bf) { if (int rc = B->body_force.upload(f)) return rc; }
+  return 0;
+}
+
+int odegpuBatchCreate(const odegpuScene* sc, const odegpuBatchConfig* cfg, odegpuBatchID* out) {
+  if (!sc || !out || sc->n_worlds <= 0) return fail(ODEGPU_E_ARG, "bad scene");
+  *out = nullptr;
+  const int dev = cfg ? cfg->device : 0;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= dev) {
+    cudaGetLastError();
+    return fail(ODEGPU_E_CUDA, "no CUDA device available");
+  }
+  OG_CUDA(cudaSetDevice(dev));
+  auto* B = new odegpuBatch();
+  B->device = dev;
+  const int cpb = (cfg && cfg->contacts_per_body > 0) ? cfg->contacts_per_body : 8;
+  B->warps_per_block = (cfg && cfg->warps_per_block > 0) ? cfg->warps_per_block : 4;
+  const int W = sc->n_worlds;
+  B->n_worlds = W;
+  B->nb_total = sc->body_off[W];
+  B->ng_total = sc->geom_off[W];
+  B->nj_total = sc->joint_off[W];
+
+  // ---- bodies (dBodySetPosition/Quaternion/Velocity, dBodySetMass)
+  const int NB = B->nb_total;
+  std::vector<float4> pos(NB), q(NB), lv(NB), av(NB);
+  std::vector<float> mass(NB), invMass(NB), I(9 * (size_t)NB), invI(9 * (size_t)NB);
+  std::vector<int> flags(NB);
+  std::vector<og_host::HBody> hb(NB);
+  for (int b = 0; b < NB; ++b) {
+    og_host::HBody& H = hb[b];
+    for (int k = 0; k < 3; ++k) H.pos[k] = sc->body_pos[3 * b + k];
+    for (int k = 0; k < 4; ++k) H.q[k] = sc->body_q[4 * b + k];
+    og_host::normalize4(H.q);
+    og_host::r_from_q(H.R, H.q);
+    pos[b] = make_float4((float)H.pos[0], (float)H.pos[1], (float)H.pos[2], 0.f);
+    q[b] = make_float4((float)H.q[0], (float)H.q[1], (float)H.q[2], (float)H.q[3]);
+    lv[b] = make_float4((float)sc->body_lvel[3 * b], (float)sc->body_lvel[3 * b + 1],
+                        (float)sc->body_lvel[3 * b + 2], 0.f);
+    av[b] = make_float4((float)sc->body_avel[3 * b], (float)sc->body_avel[3 * b + 1],
+                        (float)sc->body_avel[3 * b + 2], 0.f);
+    mass[b] = (float)sc->body_mass[b];
+    invMass[b] = (float)(1.0 / sc->body_mass[b]);
+    double inv[9];
+    const double* Ib = sc->body_I + 9 * (size_t)b;
+    // dMassSetParameters keeps the matrix symmetric from its upper triangle
+    double Is[9] = {Ib[0], Ib[1], Ib[2], Ib[1], Ib[4], Ib[5], Ib[2], Ib[5], Ib[8]};
+    if (!og_host::invert_pd3(Is, inv)) {
+      for (int k = 0; k < 9; ++k) inv[k] = (k % 4 == 0) ? 1.0 : 0.0;
+    }
+    for (int k = 0; k < 9; ++k) { I[9 * (size_t)b + k] = (float)Is[k]; invI[9 * (size_t)b + k] = (float)inv[k]; }
+    flags[b] = sc->body_flags[b];
+  }
+
+  // ---- geoms
+  const int NG = B->ng_total;
+  std::vector<int> gtype(NG), gbody(NG), gsurf(NG);
+  std::vector<float4> gparam(NG), gpos(NG);
+  std::vector<float> gbound(NG);
+  for (int g = 0; g < NG; ++g) {
+    gtype[g] = sc->geom_type[g];
+    gbody[g] = sc->geom_body[g];
+    gsurf[g] = sc->geom_surface[g];
+    double p[4];
+    for (int k = 0; k < 4; ++k) p[k] = sc->geom_param[ODEGPU_GEOM_NPARAM * (size_t)g + k];
+    if (gtype[g] == ODEGPU_GEOM_PLANE) {
+      // make_sure_plane_normal_has_unit_length (ode/src/plane.cpp:40-56)
+      double l = p[0] * p[0] + p[1] * p[1] + p[2] * p[2];
+      if (l > 0) { l = 1.0 / std::sqrt(l); p[0] *= l; p[1] *= l; p[2] *= l; p[3] *= l; }
+      else { p[0] = 1; p[1] = p[2] = p[3] = 0; }
+    } else if (gtype[g] != ODEGPU_GEOM_SPHERE && gtype[g] != ODEGPU_GEOM_BOX &&
+               gtype[g] != ODEGPU_GEOM_CAPSULE) {
+      delete B;
+      return fail(ODEGPU_E_ARG, "unsupported geom class " + std::to_string(gtype[g]));
+    }
+    gparam[g] = make_float4((float)p[0], (float)p[1], (float)p[2], (float)p[3]);
+    gpos[g] = make_float4(0.f, 0.f, 0.f, 0.f);
+    gbound[g] = bound_radius(gtype[g], p);
+  }
+  std::vector<DevSurface> surf(std::max(1, sc->n_surfaces));
+  for (int s = 0; s < sc->n_surfaces; ++s) {
+    const odegpuSurface& S = sc->surfaces[s];
+    DevSurface& D = surf[s];
+    D.mode = S.mode;
+    D.mu = (float)S.mu; D.mu2 = (float)S.mu2; D.bounce = (float)S.bounce; D.bounce_vel = (float)S.bounce_vel;
+    D.soft_erp = (float)S.soft_erp; D.soft_cfm = (float)S.soft_cfm; D.motion1 = (float)S.motion1;
+    D.motion2 = (float)S.motion2; D.motionN = (float)S.motionN; D.slip1 = (float)S.slip1;
+    D.slip2 = (float)S.slip2;
+  }
+  if (sc->n_surfaces <= 0) std::memset(&surf[0], 0, sizeof(DevSurface));
+
+  // ---- worlds, joints, persistent adjacency
+  std::vector<WorldDesc>& wd = B->h_world;
+  wd.resize(W);
+  std::vector<unsigned> seeds(W);
+  std::vector<DevJoint> joints(std::max(1, B->nj_total));
+  std::vector<int> padj_start((size_t)NB + W);
+  std::vector<int> padj;
+  long long contact_off = 0, row_off = 0;
+  for (int w = 0; w < W; ++w) {
+    const odegpuWorldParams& P = sc->world[w];
+    WorldDesc& D = wd[w];
+    D.body_off = sc->body_off[w];
+    D.nb = sc->body_off[w + 1] - D.body_off;
+    D.geom_off = sc->geom_off[w];
+    D.ng = sc->geom_off[w + 1] - D.geom_off;
+    D.joint_off = sc->joint_off[w];
+    D.njp = sc->joint_off[w + 1] - D.joint_off;
+    if (D.nb > ODEGPU_MAX_BODIES_PER_WORLD) {
+      delete B;
+      return fail(ODEGPU_E_LIMIT, "world " + std::to_string(w) + " has " + std::to_string(D.nb) +
+                                      " bodies; this kernel handles at most " +
+                                      std::to_string(ODEGPU_MAX_BODIES_PER_WORLD));
+    }
+    if (P.max_contacts < 1 || P.max_contacts > 8) {
+      delete B;
+      return fail(ODEGPU_E_ARG, "max_contacts must be in [1, 8]");
+    }
+    D.contact_off = (int)contact_off;
+    D.contact_cap = cpb * D.nb + 16;
+    contact_off += D.contact_cap;
+    D.row_off = (int)row_off;
+    D.row_cap = std::min(ODEGPU_MAX_ROWS_PER_WORLD, 3 * D.contact_cap + 6 * D.njp);
+    row_off += D.row_cap;
+    D.max_contacts = P.max_contacts;
+    D.iterations = P.iterations;
+    for (int k = 0; k < 3; ++k) D.gravity[k] = (float)P.gravity[k];
+    D.erp = (float)P.erp; D.cfm = (float)P.cfm; D.sor_w = (float)P.sor_w;
+    D.max_vel = (float)P.max_vel; D.min_depth = (float)P.min_depth; D.dt = (float)P.dt;
+    seeds[w] = P.seed;
+    // joints: setters in FP64, stored FP32
+    std::vector<std::vector<int>> per_body(D.nb);
+    for (int j = 0; j < D.njp; ++j) {
+      const int gj = D.joint_off + j;
+      const int type = sc->joint_type[gj];
+      if (type != ODEGPU_JOINT_BALL && type != ODEGPU_JOINT_HINGE && type != ODEGPU_JOINT_HINGE2) {
+        delete B;
+        return fail(ODEGPU_E_ARG, "unsupported joint type " + std::to_string(type));
+      }
+      og_host::HJoint H;
+      og_host::setup_joint(type, H, hb.data() + D.body_off, sc->joint_body[2 * gj], sc->joint_body[2 * gj + 1],
+                           sc->joint_anchor + 3 * (size_t)gj, sc->joint_axis1 + 3 * (size_t)gj,
+                           sc->joint_axis2 + 3 * (size_t)gj);
+      DevJoint& J = joints[gj];
+      std::memset(&J, 0, sizeof(J));
+      J.type = type; J.b1 = H.b1; J.b2 = H.b2; J.reverse = H.reverse;
+      for (int k = 0; k < 4; ++k) {
+        J.anchor1[k] = (float)H.anchor1[k]; J.anchor2[k] = (float)H.anchor2[k];
+        J.axis1[k] = (float)H.axis1[k]; J.axis2[k] = (float)H.axis2[k];
+        J.qrel[k] = (float)H.qrel[k]; J.v1[k] = (float)H.v1[k]; J.v2[k] = (float)H.v2[k];
+      }
+      J.c0 = (float)H.c0; J.s0 = (float)H.s0;
+      const double* jp = sc->joint_param + ODEGPU_JOINT_NPARAM * (size_t)gj;
+      auto limot = [&](DevLimot& L, const double* p) {
+        // dxJointLimitMotor::init then ::set in parameter order (joint.cpp:456-508)
+        L.lostop = (float)p[0]; L.histop = (float)p[1]; L.vel = (float)p[2];
+        L.fmax = p[3] >= 0 ? (float)p[3] : 0.f;
+        L.fudge = (p[4] >= 0 && p[4] <= 1) ? (float)p[4] : 1.f;
+        L.bounce = (float)p[5]; L.normal_cfm = (float)p[6]; L.stop_erp = (float)p[7];
+        L.stop_cfm = (float)p[8];
+      };
+      if (type == ODEGPU_JOINT_BALL) { J.erp = (float)jp[0]; J.cfm = (float)jp[1]; }
+      if (type == ODEGPU_JOINT_HINGE) limot(J.lm1, jp);
+      if (type == ODEGPU_JOINT_HINGE2) {
+        limot(J.lm1, jp);
+        limot(J.lm2, jp + 9);
+        J.susp_erp = (float)jp[18];
+        J.susp_cfm = (float)jp[19];
+      }
+      if (J.b1 >= 0) per_body[J.b1].push_back(j);
+      if (J.b2 >= 0) per_body[J.b2].push_back(j);
+    }
+    // persistent adjacency, newest attach first (dJointAttach prepends)
+    int* ps = padj_start.data() + D.body_off + w;
+    for (int b = 0; b < D.nb; ++b) {
+      ps[b] = (int)padj.size();
+      for (auto it = per_body[b].rbegin(); it != per_body[b].rend(); ++it) padj.push_back(*it);
+    }
+    ps[D.nb] = (int)padj.size();
+  }
+  B->contact_cap_total = contact_off;
+  B->row_cap_total = row_off;
+  const long long jl_total = (long long)B->nj_total + contact_off;
+
+  int rc = 0;
+  rc = rc ? rc : B->world.upload(wd);
+  rc = rc ? rc : B->seed.upload(seeds);
+  rc = rc ? rc : B->status.upload(std::vector<int>(W, 0));
+  rc = rc ? rc : B->ncontacts.upload(std::vector<int>(W, 0));
+  rc = rc ? rc : B->nrows.upload(std::vector<int>(W, 0));
+  rc = rc ? rc : B->nislands.upload(std::vector<int>(W, 0));
+  rc = rc ? rc : B->pos.upload(pos);
+  rc = rc ? rc : B->q.upload(q);
+  rc = rc ? rc : B->lvel.upload(lv);
+  rc = rc ? rc : B->avel.upload(av);
+  rc = rc ? rc : B->facc.alloc(NB);
+  rc = rc ? rc : B->tacc.alloc(NB);
+  rc = rc ? rc : B->mass.upload(mass);
+  rc = rc ? rc : B->invMass.upload(invMass);
+  rc = rc ? rc : B->I.upload(I);
+  rc = rc ? rc : B->invI.upload(invI);
+  rc = rc ? rc : B->invIw.alloc(12 * (size_t)NB);
+  rc = rc ? rc : B->bflags.upload(flags);
+  rc = rc ? rc : B->gtype.upload(gtype);
+  rc = rc ? rc : B->gbody.upload(gbody);
+  rc = rc ? rc : B->gsurf.upload(gsurf);
+  rc = rc ? rc : B->gparam.upload(gparam);
+  rc = rc ? rc : B->gpos.upload(gpos);
+  rc = rc ? rc : B->gbound.upload(gbound);
+  rc = rc ? rc : B->surfaces.upload(surf);
+  rc = rc ? rc : B->joints.upload(joints);
+  rc = rc ? rc : B->padj_start.upload(padj_start);
+  if (padj.empty()) padj.push_back(0);
+  rc = rc ? rc : B->padj.upload(padj);
+  rc = rc ? rc : B->contacts.alloc(contact_off);
+  rc = rc ? rc : B->rows.alloc((size_t)row_off * kRowWords);
+  rc = rc ? rc : B->jlist.alloc(jl_total);
+  rc = rc ? rc : B->jrow.alloc(jl_total);
+  rc = rc ? rc : B->jm.alloc(jl_total);
+  rc = rc ? rc : B->adj.alloc(2 * jl_total);
+  rc = rc ? rc : B->adj_start.alloc((size_t)NB + W);
+  rc = rc ? rc : B->island_jstart.alloc((size_t)NB + W);
+  rc = rc ? rc : B->island_rstart.alloc((size_t)NB + W);
+  rc = rc ? rc : B->state_scratch.alloc((size_t)NB * ODEGPU_BODY_REC);
+  if (!rc) rc = set_controls(B, sc->n_ctrl_steps, sc->joint_torque, sc->body_force);
+  if (!rc && cudaStreamCreateWithFlags(&B->stream, cudaStreamNonBlocking) != cudaSuccess)
+    rc = fail(ODEGPU_E_CUDA, "stream creation failed");
+  if (!rc) {
+    const size_t smem = (size_t)B->warps_per_block * kSmemPerWarp;
+    if (cudaFuncSetAttribute(world_step_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+        cudaSuccess)
+      rc = fail(ODEGPU_E_CUDA, "cannot configure shared memory");
+  }
+  if (rc) { delete B; return rc; }
+  *out = B;
+  return 0;
+}
+
+void odegpuBatchDestroy(odegpuBatchID b) {
+  if (!b) return;
+  cudaSetDevice(b->device);
+  cudaStreamSynchronize(b->stream);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+}
+
+int odegpuBatchSetControls(odegpuBatchID b, int n_ctrl_steps, const double* jt, const double* bf) {
+  if (!b) return fail(ODEGPU_E_ARG, "null batch");
+  OG_CUDA(cudaSetDevice(b->device));
+  OG_CUDA(cudaStreamSynchronize(b->stream));
+  return set_controls(b, n_ctrl_steps, jt, bf);
+}
+
+int odegpuBatchSetStepIndex(odegpuBatchID b, int step) {
+  if (!b || step < 0) return fail(ODEGPU_E_ARG, "bad arguments");
+  b->step_counter = step;
+  return 0;
+}
+
+int odegpuBatchStep(odegpuBatchID b, int n_steps) {
+  if (!b || n_steps < 0) return fail(ODEGPU_E_ARG, "bad arguments");
+  if (n_steps == 0) return 0;
+  OG_CUDA(cudaSetDevice(b->device));
+  StepOptions opt{1, nullptr, nullptr, nullptr};
+  if (int rc = b->launch(0, b->n_worlds, n_steps, opt)) return rc;
+  b->step_counter += n_steps;
+  return 0;
+}
+
+int odegpuBatchStepPlain(odegpuBatchID b, int n_steps) {
+  if (!b || n_steps < 0) return fail(ODEGPU_E_ARG, "bad arguments");
+  OG_CUDA(cudaSetDevice(b->device));
+  StepOptions opt{1, nullptr, nullptr, nullptr};
+  const int saved = b->warps_per_block;
+  b->warps_per_block = 1;
+  for (int w = 0; w < b->n_worlds; ++w) {
+    for (int s = 0; s < n_steps; ++s) {
+      const int base = b->step_counter;
+      b->step_counter = base + s;
+      const int rc = b->launch(w, 1, 1, opt);
+      b->step_counter = base;
+      if (rc) { b->warps_per_block = saved; return rc; }
+    }
+  }
+  b->warps_per_block = saved;
+  b->step_counter += n_steps;
+  return 0;
+}
+
+int odegpuBatchStepGraph(odegpuBatchID b, int n_steps) {
+  if (!b || n_steps < 0) return fail(ODEGPU_E_ARG, "bad arguments");
+  OG_CUDA(cudaSetDevice(b->device));
+  StepOptions opt{1, nullptr, nullptr, nullptr};
+  cudaGraph_t graph;
+  OG_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+  for (int s = 0; s < n_steps; ++s) {
+    const int base = b->step_counter;
+    b->step_counter = base + s;
+    const int rc = b->launch(0, b->n_worlds, 1, opt);
+    b->step_counter = base;
+    if (rc) { cudaStreamEndCapture(b->stream, &graph); return rc; }
+  }
+  OG_CUDA(cudaStreamEndCapture(b->stream, &graph));
+  cudaGraphExec_t exec;
+  OG_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+  const cudaError_t e = cudaGraphLaunch(exec, b->stream);
+  cudaGraphExecDestroy(exec);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) return fail(ODEGPU_E_CUDA, cudaGetErrorString(e));
+  b->step_counter += n_steps;
+  return 0;
+}
+
+int odegpuBatchSynchronize(odegpuBatchID b) {
+  if (!b) return fail(ODEGPU_E_ARG, "null batch");
+  OG_CUDA(cudaSetDevice(b->device));
+  OG_CUDA(cudaStreamSynchronize(b->stream));
+  return 0;
+}
+
+int odegpuBatchReadStateF32Async(odegpuBatchID b, float* state) {
+  if (!b || !state) return fail(ODEGPU_E_ARG, "bad arguments");
+  OG_CUDA(cudaSetDevice(b->device));
+  const int nb = b->nb_total;
+  pack_state_kernel<<<(nb + 255) / 256, 256, 0, b->stream>>>(b->dev(), nb, b->state_scratch.p);
+  OG_CUDA(cudaGetLastError());
+  OG_CUDA(cudaMemcpyAsync(state, b->state_scratch.p, (size_t)nb * ODEGPU_BODY_REC * sizeof(float),
+                          cudaMemcpyDefault, b->stream));
+  return 0;
+}
+
+int odegpuBatchWriteStateF32Async(odegpuBatchID b, const float* state) {
+  if (!b || !state) return fail(ODEGPU_E_ARG, "bad arguments");
+  OG_CUDA(cudaSetDevice(b->device));
+  const int nb = b->nb_total;
+  OG_CUDA(cudaMemcpyAsync(b->state_scratch.p, state, (size_t)nb * ODEGPU_BODY_REC * sizeof(float),
+                          cudaMemcpyDefault, b->stream));
+  unpack_state_kernel<<<(nb + 255) / 256, 256, 0, b->stream>>>(b->dev(), nb, b->state_scratch.p);
+  OG_CUDA(cudaGetLastError());
+  return 0;
+}
+
+int odegpuBatchReadState(odegpuBatchID b, double* state) {
+  if (!b || !state) return fail(ODEGPU_E_ARG, "bad arguments");
+  std::vector<float> tmp((size_t)b->nb_total * ODEGPU_BODY_REC);
+  if (int rc = odegpuBatchReadStateF32Async(b, tmp.data())) return rc;
+  OG_CUDA(cudaStreamSynchronize(b->stream));
+  for (size_t i = 0; i < tmp.size(); ++i) state[i] = tmp[i];
+  return 0;
+}
+
+int odegpuBatchWriteState(odegpuBatchID b, const double* state) {
+  if (!b || !state) return fail(ODEGPU_E_ARG, "bad arguments");
+  std::vector<float> tmp((size_t)b->nb_total * ODEGPU_BODY_REC);
+  for (size_t i = 0; i < tmp.size(); ++i) tmp[i] = (float)state[i];
+  // quaternions are normalised on the way in, as dBodySetQuaternion does
+  for (int k = 0; k < b->nb_total; ++k) {
+    double qd[4];
+    for (int j = 0; j < 4; ++j) qd[j] = state[(size_t)k * ODEGPU_BODY_REC + 3 + j];
+    og_host::normalize4(qd);
+    for (int j = 0; j < 4; ++j) tmp[(size_t)k * ODEGPU_BODY_REC + 3 + j] = (float)qd[j];
+  }
+  if (int rc = odegpuBatchWriteStateF32Async(b, tmp.data())) return rc;
+  OG_CUDA(cudaStreamSynchronize(b->stream));
+  return 0;
+}
+
+static int copy_ints(odegpuBatchID b, const int* src, int* dst, size_t n) {
+  OG_CUDA(cudaSetDevice(b->device));
+  OG_CUDA(cudaMemcpyAsync(dst, src, n * sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+  OG_CUDA(cudaStreamSynchronize(b->stream));
+  return 0;
+}
+
+int odegpuBatchGetStatus(odegpuBatchID b, int* status) {
+  if (!b || !status) return fail(ODEGPU_E_ARG, "bad arguments");
+  return copy_ints(b, b->status.p, status, b->n_worlds);
+}
+
+int odegpuBatchGetCounts(odegpuBatchID b, int* nc, int* nr, int* ni) {
+  if (!b) return fail(ODEGPU_E_ARG, "bad arguments");
+  if (nc) if (int rc = copy_ints(b, b->ncontacts.p, nc, b->n_worlds)) return rc;
+  if (nr) if (int rc = copy_ints(b, b->nrows.p, nr, b->n_worlds)) return rc;
+  if (ni) if (int rc = copy_ints(b, b->nislands.p, ni, b->n_worlds)) return rc;
+  return 0;
+}
+
+int odegpuBatchGetSeeds(odegpuBatchID b, unsigned int* seeds) {
+  if (!b || !seeds) return fail(ODEGPU_E_ARG, "bad arguments");
+  return copy_ints(b, reinterpret_cast<const int*>(b->seed.p), reinterpret_cast<int*>(seeds), b->n_worlds);
+}
+
+int odegpuBatchSetSeeds(odegpuBatchID b, const unsigned int* seeds) {
+  if (!b || !seeds) return fail(ODEGPU_E_ARG, "bad arguments");
+  OG_CUDA(cudaSetDevice(b->device));
+  OG_CUDA(cudaMemcpyAsync(b->seed.p, seeds, b->n_worlds * sizeof(unsigned), cudaMemcpyHostToDevice, b->stream));
+  OG_CUDA(cudaStreamSynchronize(b->stream));
+  return 0;
+}
+
+int odegpuBatchInfo(odegpuBatchID b, int* n_worlds, int* nb_total, int* nj_total, long long* row_cap,
+                    long long* contact_cap) {
+  if (!b) return fail(ODEGPU_E_ARG, "null batch");
+  if (n_worlds) *n_worlds = b->n_worlds;
+  if (nb_total) *nb_total = b->nb_total;
+  if (nj_total) *nj_total = b->nj_total;
+  if (row_cap) *row_cap = b->row_cap_total;
+  if (contact_cap) *contact_cap = b->contact_cap_total;
+  return 0;
+}
+
+void* odegpuBatchStream(odegpuBatchID b) { return b ? (void*)b->stream : nullptr; }
+
+int odegpuBatchStepTap(odegpuBatchID b, float* rows, float* lambda, float* fc, int* row_off) {
+  if (!b) return fail(ODEGPU_E_ARG, "null batch");
+  OG_CUDA(cudaSetDevice(b->device));
+  DBuf<float> drows, dlam, dfc;
+  if (int rc = drows.alloc((size_t)b->row_cap_total * kRowWords)) return rc;
+  if (int rc = dlam.alloc(b->row_cap_total)) return rc;
+  if (int rc = dfc.alloc((size_t)b->nb_total * 6)) return rc;
+  OG_CUDA(cudaMemsetAsync(dfc.p, 0, (size_t)b->nb_total * 6 * sizeof(float), b->stream));
+  StepOptions opt{1, drows.p, dlam.p, dfc.p};
+  if (int rc = b->launch(0, b->n_worlds, 1, opt)) return rc;
+  b->step_counter += 1;
+  if (rows)
+    OG_CUDA(cudaMemcpyAsync(rows, drows.p, (size_t)b->row_cap_total * kRowWords * sizeof(float),
+                            cudaMemcpyDeviceToHost, b->stream));
+  if (lambda)
+    OG_CUDA(cudaMemcpyAsync(lambda, dlam.p, (size_t)b->row_cap_total * sizeof(float),
+                            cudaMemcpyDeviceToHost, b->stream));
+  if (fc)
+    OG_CUDA(cudaMemcpyAsync(fc, dfc.p, (size_t)b->nb_total * 6 * sizeof(float), cudaMemcpyDeviceToHost,
+                            b->stream));
+  OG_CUDA(cudaStreamSynchronize(b->stream));
+  if (row_off)
+    for (int w = 0; w < b->n_worlds; ++w) row_off[w] = b->h_world[w].row_off;
+  return 0;
+}
+
+int odegpuBatchGetContacts(odegpuBatchID b, int w, float* out, int cap) {
+  if (!b || w < 0 || w >= b->n_worlds || (!out && cap > 0)) return fail(ODEGPU_E_ARG, "bad arguments");
+  OG_CUDA(cudaSetDevice(b->device));
+  int nc = 0;
+  OG_CUDA(cudaMemcpyAsync(&nc, b->ncontacts.p + w, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+  OG_CUDA(cudaStreamSynchronize(b->stream));
+  const int n = std::min(nc, cap);
+  if (n > 0) {
+    std::vector<DevContact> tmp(n);
+    OG_CUDA(cudaMemcpy(tmp.data(), b->contacts.p + b->h_world[w].contact_off, n * sizeof(DevContact),
+                       cudaMemcpyDeviceToHost));
+    for (int i = 0; i < n; ++i) {
+      float* o = out + 9 * i;
+      const DevContact& c = tmp[i];
+      o[0] = c.pos[0]; o[1] = c.pos[1]; o[2] = c.pos[2];
+      // report the normal as dCollide returned it (before the attach swap)
+      o[3] = c.normal[0]; o[4] = c.normal[1]; o[5] = c.normal[2];
+      o[6] = c.depth;
+      o[7] = (float)(c.reverse ? -1 : c.b1);
+      o[8] = (float)(c.reverse ? c.b1 : c.b2);
+    }
+  }
+  return nc;
+}
+
+}  // extern "C"

@@ -1,0 +1,123 @@
+// engine_types.cuh -- device-resident data layout of a batch of worlds.
+//
+// Everything is structure-of-arrays indexed by a GLOBAL object index
+// (world offset + local index) so that the lanes of the warp owning a world
+// read consecutive bodies with coalesced 16-byte loads.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace og {
+
+// Joint types (ODE dJointType values) and surface mode bits (dContact).
+enum { J_BALL = 1, J_HINGE = 2, J_CONTACT = 4, J_HINGE2 = 6 };
+enum {
+  SURF_MU2 = 0x001, SURF_FDIR1 = 0x002, SURF_BOUNCE = 0x004, SURF_SOFT_ERP = 0x008,
+  SURF_SOFT_CFM = 0x010, SURF_MOTION1 = 0x020, SURF_MOTION2 = 0x040, SURF_MOTIONN = 0x080,
+  SURF_SLIP1 = 0x100, SURF_SLIP2 = 0x200, SURF_APPROX1_1 = 0x1000, SURF_APPROX1_2 = 0x2000
+};
+enum { BODY_GYROSCOPIC = 1, BODY_NO_GRAVITY = 2 };
+
+// Per-world status bits (odegpuBatchStatus).
+enum {
+  ST_CONTACT_OVERFLOW = 1,   // more contacts than the world's capacity
+  ST_ROW_OVERFLOW = 2,       // more constraint rows than the world's capacity
+  ST_TOO_LARGE = 4,          // world exceeds the on-chip limits of this kernel
+  ST_NONFINITE = 8           // a body state became NaN/Inf
+};
+
+// Row store: 32 words (128 bytes, one cache line) per constraint row.
+//   [0..11]  J (scaled by Ad after the setup phase)
+//   [12..23] iMJ = invM * J^T
+//   [24] c -> b (rhs * Ad)   [25] cfm -> Ad*cfm   [26] lo  [27] hi
+//   [28] findex (world row index or -1, int bits)  [29] b1  [30] b2  [31] joint
+constexpr int kRowWords = 32;
+constexpr int kRowC = 24, kRowCfm = 25, kRowLo = 26, kRowHi = 27, kRowFindex = 28;
+constexpr int kRowB1 = 29, kRowB2 = 30, kRowJoint = 31;
+
+struct DevSurface {
+  int mode;
+  float mu, mu2, bounce, bounce_vel, soft_erp, soft_cfm, motion1, motion2, motionN, slip1, slip2;
+};
+
+struct DevLimot {
+  float vel, fmax, lostop, histop, fudge, normal_cfm, stop_erp, stop_cfm, bounce;
+};
+
+// A persistent (non-contact) joint after dJointAttach and its setters.
+struct DevJoint {
+  int type, b1, b2, reverse;    // b1/b2 world-local, b2 = -1 for the environment
+  float anchor1[4], anchor2[4], axis1[4], axis2[4], qrel[4], v1[4], v2[4];
+  float erp, cfm, c0, s0, susp_erp, susp_cfm;
+  DevLimot lm1, lm2;
+};
+
+// A contact produced by the narrowphase and turned into a contact joint.
+struct DevContact {
+  float pos[3], depth;
+  float normal[3];
+  int surface;
+  int b1, b2, reverse, pad;     // attach result: b2 = -1 for the environment
+};
+
+// Static description of one world inside the batch.
+struct WorldDesc {
+  int body_off, nb, geom_off, ng, joint_off, njp;
+  int contact_off, contact_cap;
+  int row_off, row_cap;
+  int padj_off;                 // persistent adjacency (CSR) offset
+  int max_contacts;
+  int iterations;
+  float gravity[3], erp, cfm, sor_w, max_vel, min_depth, dt;
+};
+
+struct BatchDev {
+  int n_worlds;
+  const WorldDesc* world;
+  unsigned* seed;               // [n_worlds] dRand state
+  int* status;                  // [n_worlds] ST_* bits
+  int* ncontacts;               // [n_worlds] contacts of the last step
+  int* nrows;                   // [n_worlds] rows of the last step
+  int* nislands;                // [n_worlds] islands of the last step
+
+  // bodies
+  float4 *pos, *q, *lvel, *avel;       // [nb_total]
+  float *mass, *invMass;               // [nb_total]
+  float *I, *invI;                     // [nb_total][9] body frame
+  int* bflags;                         // [nb_total]
+  float* invIw;                        // [nb_total][12] scratch: world-frame invI
+  float4 *facc, *tacc;                 // [nb_total] scratch accumulators
+
+  // geoms
+  const int* gtype;                    // [ng_total]
+  const int* gbody;                    // world-local body or -1
+  const float4* gparam;                // class parameters
+  const float* gbound;                 // bounding radius (INFINITY for planes)
+  const float4* gpos;                  // static placement (geoms without body)
+  const int* gsurf;
+  const DevSurface* surfaces;
+
+  // persistent joints and their adjacency
+  const DevJoint* joints;              // [nj_total]
+  const int* padj_start;               // [nb_total + n_worlds]: per-world CSR starts
+  const int* padj;                     // persistent joint ordinals, newest first
+
+  // per-step controls
+  int n_ctrl_steps;
+  const float* joint_torque;           // [S][nj_total][2]
+  const float* body_force;             // [S][nb_total][6]
+  int step_counter_base;
+
+  // per-step scratch (capacity-sized per world)
+  DevContact* contacts;                // [contact_cap_total]
+  float* rows;                         // [row_cap_total][32]
+  int* jlist;                          // [njp + contact_cap per world] island order
+  int* adj;                            // [2 * (njp + contact_cap) per world]
+  int* adj_start;                      // [nb_total + n_worlds]
+  int* island_jstart;                  // [nb_total + n_worlds]
+  int* island_rstart;                  // [nb_total + n_worlds]
+  int* jrow;                           // [njp + contact_cap per world] first row per joint
+  int* jm;                             // [...] rows per joint
+};
+
+}  // namespace og

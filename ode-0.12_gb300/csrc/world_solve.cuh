@@ -1,0 +1,582 @@
+// world_solve.cuh -- phases 2 and 4-7 of a world step (see world_step.cuh).
+#pragma once
+#include "world_step.cuh"
+
+namespace og {
+
+// Phase 2 (quickstep.cpp:600-665): world-frame inverse inertia, gyroscopic
+// torque and gravity for every body of the world.
+OG_D void phase_body_prologue(const BatchDev& d, const WorldDesc& D, int lane) {
+  for (int b = lane; b < D.nb; b += 32) {
+    const int gb = D.body_off + b;
+    float R[12], tmp[12], invIb[12], invIw[12];
+    body_R(d, gb, R);
+    const float* ib = d.invI + 9 * gb;
+    for (int r = 0; r < 3; ++r) {
+      invIb[r * 4 + 0] = ib[r * 3 + 0]; invIb[r * 4 + 1] = ib[r * 3 + 1];
+      invIb[r * 4 + 2] = ib[r * 3 + 2]; invIb[r * 4 + 3] = 0.f;
+    }
+    mul2_333(tmp, invIb, R);
+    mul0_333(invIw, R, tmp);
+    float* out = d.invIw + 12 * gb;
+    for (int k = 0; k < 12; ++k) out[k] = invIw[k];
+    float4 t = d.tacc[gb];
+    const float4 av = d.avel[gb];
+    if (d.bflags[gb] & BODY_GYROSCOPIC) {
+      float Ib[12], Iw[12], t3[3], cr[3];
+      const float* ii = d.I + 9 * gb;
+      for (int r = 0; r < 3; ++r) {
+        Ib[r * 4 + 0] = ii[r * 3 + 0]; Ib[r * 4 + 1] = ii[r * 3 + 1];
+        Ib[r * 4 + 2] = ii[r * 3 + 2]; Ib[r * 4 + 3] = 0.f;
+      }
+      mul2_333(tmp, Ib, R);
+      mul0_333(Iw, R, tmp);
+      const float w3[3] = {av.x, av.y, av.z};
+      mul0_331(t3, Iw, w3);
+      cross3(cr, w3, t3);
+      t.x = t.x - cr[0]; t.y = t.y - cr[1]; t.z = t.z - cr[2];
+      d.tacc[gb] = t;
+    }
+    if (!(d.bflags[gb] & BODY_NO_GRAVITY)) {
+      float4 f = d.facc[gb];
+      const float m = d.mass[gb];
+      if (D.gravity[0] != 0.f) f.x += m * D.gravity[0];
+      if (D.gravity[1] != 0.f) f.y += m * D.gravity[1];
+      if (D.gravity[2] != 0.f) f.z += m * D.gravity[2];
+      d.facc[gb] = f;
+    }
+  }
+}
+
+// Phase 4: getInfo1 / getInfo2 over the joints in island order. Returns the
+// total row count M (or -1 when it exceeds the world's capacity).
+OG_D int phase_rows(const BatchDev& d, const WorldDesc& D, int w, int nj, int nisl, int lane) {
+  const int jl_off = D.joint_off + D.contact_off;
+  const float h1 = 1.0f / D.dt;
+  // pass 1: m per joint, prefix -> first row
+  int carry = 0;
+  for (int base = 0; base < nj; base += 32) {
+    const int k = base + lane;
+    int m = 0;
+    if (k < nj) {
+      const int ord = d.jlist[jl_off + k] & 0x3fffffff;
+      if (ord < D.njp) {
+        const DevJoint& J = d.joints[D.joint_off + ord];
+        BodyRef B1, B2;
+        load_body_ref(d, D.body_off + J.b1, B1);
+        if (J.b2 >= 0) load_body_ref(d, D.body_off + J.b2, B2);
+        m = persistent_info1(J, B1, J.b2 >= 0 ? &B2 : nullptr).m;
+      } else {
+        m = contact_info1(d.surfaces[d.contacts[D.contact_off + ord - D.njp].surface]);
+      }
+      d.jm[jl_off + k] = m;
+    }
+    const int incl = warp_incl_scan(m, lane);
+    if (k < nj) d.jrow[jl_off + k] = carry + incl - m;
+    carry += __shfl_sync(kFull, incl, 31);
+  }
+  const int M = carry;
+  if (M > D.row_cap || M > kMaxR) {
+    if (lane == 0) atomicOr(&d.status[w], ST_ROW_OVERFLOW);
+    return -1;
+  }
+  __syncwarp();
+  for (int i = lane; i <= nisl; i += 32) {
+    const int js = d.island_jstart[D.body_off + w + i];
+    d.island_rstart[D.body_off + w + i] = (js < nj) ? d.jrow[jl_off + js] : M;
+  }
+  // pass 2: getInfo2. The effective info->erp of a joint is the erp of the
+  // last ball joint at or before it in the same island (ball.cpp:59 writes it
+  // into the Info2 block the stepper reuses), else the world erp.
+  float erp_carry = D.erp;
+  for (int base = 0; base < nj; base += 32) {
+    const int k = base + lane;
+    int ord = -1;
+    bool start = false, is_ball = false;
+    float my_erp = 0.f;
+    if (k < nj) {
+      const int v = d.jlist[jl_off + k];
+      ord = v & 0x3fffffff;
+      start = (v >> 30) & 1;
+      if (ord < D.njp) {
+        const DevJoint& J = d.joints[D.joint_off + ord];
+        if (J.type == J_BALL) { is_ball = true; my_erp = J.erp; }
+      }
+    }
+    const unsigned balls = __ballot_sync(kFull, is_ball);
+    const unsigned starts = __ballot_sync(kFull, start);
+    const unsigned le = (lane == 31) ? kFull : ((1u << (lane + 1)) - 1u);
+    const unsigned lt = (1u << lane) - 1u;
+    // erp seen by this joint: balls strictly before it within its island
+    const unsigned b_lt = balls & lt;
+    const unsigned s_le = starts & le;
+    const int last_ball = b_lt ? 31 - __clz(b_lt) : -1;
+    const int last_start = s_le ? 31 - __clz(s_le) : -1;
+    const float ball_erp = __shfl_sync(kFull, my_erp, last_ball < 0 ? 0 : last_ball);
+    float erp;
+    if (last_ball >= 0 && last_ball >= last_start) erp = ball_erp;
+    else if (last_start >= 0) erp = D.erp;
+    else erp = erp_carry;
+    // carry for the next chunk: the erp after lane 31's joint
+    {
+      const unsigned b_all = balls, s_all = starts;
+      const int lb = b_all ? 31 - __clz(b_all) : -1;
+      const int ls = s_all ? 31 - __clz(s_all) : -1;
+      const float lb_erp = __shfl_sync(kFull, my_erp, lb < 0 ? 0 : lb);
+      if (lb >= 0 && lb >= ls) erp_carry = lb_erp;
+      else if (ls >= 0) erp_carry = D.erp;
+    }
+    if (k < nj) {
+      const int r0 = d.jrow[jl_off + k], m = d.jm[jl_off + k];
+      float* rows = d.rows + (size_t)(D.row_off + r0) * kRowWords;
+      int b1, b2;
+      joint_bodies(d, D, ord, b1, b2);
+      for (int r = 0; r < m; ++r) {
+        float* row = rows + r * kRowWords;
+        for (int q = 0; q < 12; ++q) row[q] = 0.f;
+        row[kRowC] = 0.f;
+        row[kRowCfm] = D.cfm;
+        row[kRowLo] = -INFINITY;
+        row[kRowHi] = INFINITY;
+        reinterpret_cast<int*>(row)[kRowFindex] = -1;
+        reinterpret_cast<int*>(row)[kRowB1] = b1;
+        reinterpret_cast<int*>(row)[kRowB2] = b2;
+        reinterpret_cast<int*>(row)[kRowJoint] = ord;
+      }
+      Info2 in;
+      in.fps = h1;
+      in.erp = erp;
+      in.rows = rows;
+      BodyRef B1, B2;
+      load_body_ref(d, D.body_off + b1, B1);
+      if (b2 >= 0) load_body_ref(d, D.body_off + b2, B2);
+      const BodyRef* pB2 = b2 >= 0 ? &B2 : nullptr;
+      if (ord < D.njp) {
+        const DevJoint& J = d.joints[D.joint_off + ord];
+        const JointInfo1 i1 = persistent_info1(J, B1, pB2);
+        LimotTorque t1{{0.f, 0.f, 0.f}, 0}, t2{{0.f, 0.f, 0.f}, 0};
+        persistent_info2(J, i1, B1, pB2, in, t1, t2);
+        // powered motor pushing against a limit adds torque inside getInfo2
+        // (joint.cpp:612-660); concurrent additions are rare and use atomics
+        for (int t = 0; t < 2; ++t) {
+          const LimotTorque& tq = t ? t2 : t1;
+          if (!tq.active) continue;
+          float* ta = reinterpret_cast<float*>(&d.tacc[D.body_off + b1]);
+          atomicAdd(ta + 0, tq.t[0]); atomicAdd(ta + 1, tq.t[1]); atomicAdd(ta + 2, tq.t[2]);
+          if (b2 >= 0) {
+            float* tb = reinterpret_cast<float*>(&d.tacc[D.body_off + b2]);
+            atomicAdd(tb + 0, -tq.t[0]); atomicAdd(tb + 1, -tq.t[1]); atomicAdd(tb + 2, -tq.t[2]);
+          }
+        }
+      } else {
+        const DevContact& ct = d.contacts[D.contact_off + ord - D.njp];
+        contact_info2(ct, d.surfaces[ct.surface], m, B1, pB2, D.min_depth, D.max_vel, in);
+      }
+      for (int r = 0; r < m; ++r) {
+        int* fi = reinterpret_cast<int*>(rows + r * kRowWords) + kRowFindex;
+        if (*fi != -1) *fi += r0;
+      }
+    }
+  }
+  __syncwarp();
+  return M;
+}
+
+// Phase 5: rhs, cfm/h, iMJ, Ad and the J/b scaling per row; tmp1 per body is
+// staged in S.fc first (quickstep.cpp:836-857 then :117-136, :370-402).
+OG_D void phase_row_setup(const BatchDev& d, const WorldDesc& D, int M, const WarpSmem& S, int lane,
+                          float* dbg_rows) {
+  const float h1 = 1.0f / D.dt;
+  for (int b = lane; b < D.nb; b += 32) {
+    const int gb = D.body_off + b;
+    const float4 f = d.facc[gb], t = d.tacc[gb], lv = d.lvel[gb], av = d.avel[gb];
+    const float im = d.invMass[gb];
+    float* t1 = S.fc + 6 * b;
+    t1[0] = f.x * im + lv.x * h1;
+    t1[1] = f.y * im + lv.y * h1;
+    t1[2] = f.z * im + lv.z * h1;
+    const float* iw = d.invIw + 12 * gb;
+    const float t3[3] = {t.x, t.y, t.z};
+    float r3[3];
+    mul0_331(r3, iw, t3);
+    t1[3] = r3[0] + av.x * h1;
+    t1[4] = r3[1] + av.y * h1;
+    t1[5] = r3[2] + av.z * h1;
+  }
+  __syncwarp();
+  const float sor_w = D.sor_w;
+  for (int r = lane; r < M; r += 32) {
+    float* row = d.rows + (size_t)(D.row_off + r) * kRowWords;
+    float4* row4 = reinterpret_cast<float4*>(row);
+    float J[12];
+    {
+      const float4 a = row4[0], b = row4[1], c = row4[2];
+      J[0] = a.x; J[1] = a.y; J[2] = a.z; J[3] = a.w;
+      J[4] = b.x; J[5] = b.y; J[6] = b.z; J[7] = b.w;
+      J[8] = c.x; J[9] = c.y; J[10] = c.z; J[11] = c.w;
+    }
+    const float4 w6 = row4[6];
+    const int4 w7 = reinterpret_cast<const int4*>(row4)[7];
+    const int b1 = w7.y, b2 = w7.z;
+    // multiply_J: rhs = J * tmp1
+    float sum = 0.f;
+    {
+      const float* in = S.fc + 6 * b1;
+      for (int j = 0; j < 6; ++j) sum += J[j] * in[j];
+      if (b2 != -1) {
+        in = S.fc + 6 * b2;
+        for (int j = 0; j < 6; ++j) sum += J[6 + j] * in[j];
+      }
+    }
+    const float rhs = w6.x * h1 - sum;
+    const float cfm = w6.y * h1;
+    if (dbg_rows) {
+      float* o = dbg_rows + (size_t)(D.row_off + r) * kRowWords;
+      for (int q = 0; q < 12; ++q) o[q] = J[q];
+      o[kRowC] = rhs; o[kRowCfm] = cfm; o[kRowLo] = w6.z; o[kRowHi] = w6.w;
+      reinterpret_cast<int*>(o)[kRowFindex] = w7.x;
+      reinterpret_cast<int*>(o)[kRowB1] = b1;
+      reinterpret_cast<int*>(o)[kRowB2] = b2;
+      reinterpret_cast<int*>(o)[kRowJoint] = w7.w;
+    }
+    // compute_invM_JT
+    float iMJ[12];
+    {
+      const int g1 = D.body_off + b1;
+      const float k1 = d.invMass[g1];
+      for (int j = 0; j < 3; ++j) iMJ[j] = k1 * J[j];
+      mul0_331(iMJ + 3, d.invIw + 12 * g1, J + 3);
+      if (b2 != -1) {
+        const int g2 = D.body_off + b2;
+        const float k2 = d.invMass[g2];
+        for (int j = 0; j < 3; ++j) iMJ[6 + j] = k2 * J[6 + j];
+        mul0_331(iMJ + 9, d.invIw + 12 * g2, J + 9);
+      } else {
+        for (int j = 6; j < 12; ++j) iMJ[j] = 0.f;
+      }
+    }
+    float s = 0.f;
+    for (int j = 0; j < 6; ++j) s += iMJ[j] * J[j];
+    if (b2 != -1)
+      for (int j = 6; j < 12; ++j) s += iMJ[j] * J[j];
+    const float Ad = sor_w / (s + cfm);
+    for (int j = 0; j < 12; ++j) J[j] *= Ad;
+    row4[0] = make_float4(J[0], J[1], J[2], J[3]);
+    row4[1] = make_float4(J[4], J[5], J[6], J[7]);
+    row4[2] = make_float4(J[8], J[9], J[10], J[11]);
+    row4[3] = make_float4(iMJ[0], iMJ[1], iMJ[2], iMJ[3]);
+    row4[4] = make_float4(iMJ[4], iMJ[5], iMJ[6], iMJ[7]);
+    row4[5] = make_float4(iMJ[8], iMJ[9], iMJ[10], iMJ[11]);
+    row4[6] = make_float4(rhs * Ad, Ad * cfm, w6.z, w6.w);
+    S.rowbod[r] = (uint16_t)((b1 + 1) | ((b2 + 1) << 8));
+  }
+  __syncwarp();
+}
+
+// Wavefront levels of the 32 positions of window `wi` (see file header).
+OG_D void compute_levels(const WarpSmem& S, int wi, int M, int lane) {
+  const int pos = wi * 32 + lane;
+  int b1 = -3, b2 = -4;
+  if (pos < M) {
+    const uint16_t rb = S.rowbod[S.seq[pos]];
+    b1 = (rb & 0xff) - 1;
+    b2 = (rb >> 8) - 1;
+  }
+  int level = 0;
+#pragma unroll 4
+  for (int k = 0; k < 31; ++k) {
+    const int kb1 = __shfl_sync(kFull, b1, k);
+    const int kb2 = __shfl_sync(kFull, b2, k);
+    const int kl = __shfl_sync(kFull, level, k);
+    if (lane > k) {
+      const bool share = (b1 == kb1) || (b1 == kb2) || (b2 >= 0 && (b2 == kb1 || b2 == kb2));
+      if (share && kl + 1 > level) level = kl + 1;
+    }
+  }
+  if (pos < M) S.lvl[pos] = (uint8_t)level;
+  const int mx = warp_max(pos < M ? level : 0);
+  if (lane == 0) S.wlev[wi] = (uint8_t)mx;
+}
+
+// Phase 6: SOR_LCP (quickstep.cpp:342-584) over all islands of the world.
+// Returns the RNG state after the step.
+OG_D unsigned phase_sor(const BatchDev& d, const WorldDesc& D, int w, int M, int nisl, unsigned seed,
+                        const WarpSmem& S, int lane) {
+  for (int i = lane; i < D.nb * 6; i += 32) S.fc[i] = 0.f;
+  for (int i = lane; i < M; i += 32) S.lambda[i] = 0.f;
+  const int* rstart = d.island_rstart + D.body_off + w;
+  const int iters = D.iterations;
+  const int n_shuffles = (iters + 7) / 8;
+  // initial order: findex == -1 rows first (ascending), the rest filled from the
+  // island's tail backwards (quickstep.cpp:405-425)
+  for (int isl = 0; isl < nisl; ++isl) {
+    const int rs = rstart[isl], re = rstart[isl + 1];
+    int negc = 0;
+    for (int base = rs; base < re; base += 32) {
+      const int r = base + lane;
+      bool neg = false;
+      if (r < re) neg = reinterpret_cast<const int*>(d.rows + (size_t)(D.row_off + r) * kRowWords)[kRowFindex] == -1;
+      const unsigned bal = __ballot_sync(kFull, neg && r < re);
+      const int negb = negc + __popc(bal & ((1u << lane) - 1u));
+      if (r < re) {
+        const int nonnegb = (r - rs) - negb;
+        const int p = neg ? rs + negb : re - 1 - nonnegb;
+        S.seq[p] = (uint16_t)r;
+      }
+      negc += __popc(bal);
+    }
+  }
+  __syncwarp();
+  // RNG stream offsets: islands consume ODE's global stream in island order,
+  // each island n_shuffles * (m - 1) draws.
+  unsigned total_draws = 0;
+  for (int isl = 0; isl < nisl; ++isl) {
+    const int m = rstart[isl + 1] - rstart[isl];
+    if (m > 0) total_draws += (unsigned)(n_shuffles * (m - 1));
+  }
+  const int nwin = (M + 31) / 32;
+  float4 rw[8];
+  for (int it = 0; it < iters; ++it) {
+    if ((it & 7) == 0) {
+      const int round = it >> 3;
+      // islands shuffled in parallel, one lane per island
+      unsigned prefix = 0;
+      for (int ib = 0; ib < nisl; ib += 32) {
+        const int isl = ib + lane;
+        int m = 0;
+        if (isl < nisl) m = rstart[isl + 1] - rstart[isl];
+        const int draws = m > 0 ? n_shuffles * (m - 1) : 0;
+        const int incl = warp_incl_scan(draws, lane);
+        if (isl < nisl && m > 1) {
+          unsigned s = lcg_jump(seed, prefix + (unsigned)(incl - draws) + (unsigned)(round * (m - 1)));
+          uint16_t* sq = S.seq + rstart[isl];
+          for (int q = 1; q < m; ++q) {
+            s = lcg_next(s);
+            const int sw = rand_int_from(s, q + 1);
+            const uint16_t t = sq[q];
+            sq[q] = sq[sw];
+            sq[sw] = t;
+          }
+        }
+        prefix += (unsigned)__shfl_sync(kFull, incl, 31);
+      }
+      __syncwarp();
+      for (int wi = 0; wi < nwin; ++wi) compute_levels(S, wi, M, lane);
+      __syncwarp();
+    }
+    for (int wi = 0; wi < nwin; ++wi) {
+      const int pos = wi * 32 + lane;
+      const bool valid = pos < M;
+      int r = 0, level = 255;
+      if (valid) {
+        r = S.seq[pos];
+        level = S.lvl[pos];
+        const float4* src = reinterpret_cast<const float4*>(d.rows + (size_t)(D.row_off + r) * kRowWords);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) rw[q] = src[q];
+      }
+      const int maxl = S.wlev[wi];
+      for (int l = 0; l <= maxl; ++l) {
+        if (level == l) {
+          const float* J = reinterpret_cast<const float*>(&rw[0]);
+          const float* iMJ = reinterpret_cast<const float*>(&rw[3]);
+          const float bb = rw[6].x, Ad = rw[6].y, lo = rw[6].z, hi = rw[6].w;
+          const int findex = __float_as_int(rw[7].x);
+          const int b1 = __float_as_int(rw[7].y), b2 = __float_as_int(rw[7].z);
+          float* fc1 = S.fc + 6 * b1;
+          const float old = S.lambda[r];
+          float delta = bb - old * Ad;
+          delta -= fc1[0] * J[0] + fc1[1] * J[1] + fc1[2] * J[2] + fc1[3] * J[3] + fc1[4] * J[4] +
+                   fc1[5] * J[5];
+          float* fc2 = nullptr;
+          if (b2 != -1) {
+            fc2 = S.fc + 6 * b2;
+            delta -= fc2[0] * J[6] + fc2[1] * J[7] + fc2[2] * J[8] + fc2[3] * J[9] + fc2[4] * J[10] +
+                     fc2[5] * J[11];
+          }
+          float hi_act, lo_act;
+          if (findex != -1) {
+            hi_act = fabsf(hi * S.lambda[findex]);
+            lo_act = -hi_act;
+          } else {
+            hi_act = hi;
+            lo_act = lo;
+          }
+          const float nl = old + delta;
+          float lam;
+          if (nl < lo_act) { delta = lo_act - old; lam = lo_act; }
+          else if (nl > hi_act) { delta = hi_act - old; lam = hi_act; }
+          else lam = nl;
+          S.lambda[r] = lam;
+          fc1[0] += delta * iMJ[0]; fc1[1] += delta * iMJ[1]; fc1[2] += delta * iMJ[2];
+          fc1[3] += delta * iMJ[3]; fc1[4] += delta * iMJ[4]; fc1[5] += delta * iMJ[5];
+          if (fc2) {
+            fc2[0] += delta * iMJ[6]; fc2[1] += delta * iMJ[7]; fc2[2] += delta * iMJ[8];
+            fc2[3] += delta * iMJ[9]; fc2[4] += delta * iMJ[10]; fc2[5] += delta * iMJ[11];
+          }
+        }
+        __syncwarp();
+      }
+    }
+  }
+  return lcg_jump(seed, total_draws);
+}
+
+// Phase 7: velocity update from the constraint forces and external forces,
+// then dxStepBody (quickstep.cpp:905-916, :960-975, :1001-1021; util.cpp:255-360).
+OG_D void phase_integrate(const BatchDev& d, const WorldDesc& D, int w, const WarpSmem& S, int lane,
+                          bool have_rows) {
+  const float h = D.dt;
+  bool bad = false;
+  for (int b = lane; b < D.nb; b += 32) {
+    const int gb = D.body_off + b;
+    float4 lv = d.lvel[gb], av = d.avel[gb];
+    if (have_rows) {
+      const float* fc = S.fc + 6 * b;
+      lv.x += h * fc[0]; lv.y += h * fc[1]; lv.z += h * fc[2];
+      av.x += h * fc[3]; av.y += h * fc[4]; av.z += h * fc[5];
+    }
+    const float4 f = d.facc[gb];
+    float4 t = d.tacc[gb];
+    const float hm = h * d.invMass[gb];
+    lv.x += hm * f.x; lv.y += hm * f.y; lv.z += hm * f.z;
+    t.x *= h; t.y *= h; t.z *= h;
+    {
+      const float t3[3] = {t.x, t.y, t.z};
+      float r3[3];
+      mul0_331(r3, d.invIw + 12 * gb, t3);
+      av.x = av.x + r3[0]; av.y = av.y + r3[1]; av.z = av.z + r3[2];
+    }
+    float4 p = d.pos[gb];
+    p.x += h * lv.x; p.y += h * lv.y; p.z += h * lv.z;
+    const float4 q4 = d.q[gb];
+    float q[4] = {q4.x, q4.y, q4.z, q4.w};
+    float dq[4];
+    dq[0] = 0.5f * (-av.x * q[1] - av.y * q[2] - av.z * q[3]);
+    dq[1] = 0.5f * (av.x * q[0] + av.y * q[3] - av.z * q[2]);
+    dq[2] = 0.5f * (-av.x * q[3] + av.y * q[0] + av.z * q[1]);
+    dq[3] = 0.5f * (av.x * q[2] - av.y * q[1] + av.z * q[0]);
+    for (int j = 0; j < 4; j++) q[j] += h * dq[j];
+    normalize4(q);
+    d.pos[gb] = p;
+    d.q[gb] = make_float4(q[0], q[1], q[2], q[3]);
+    d.lvel[gb] = lv;
+    d.avel[gb] = av;
+    if (!(isfinite(p.x) && isfinite(p.y) && isfinite(p.z) && isfinite(lv.x) && isfinite(lv.y) &&
+          isfinite(lv.z) && isfinite(av.x) && isfinite(av.y) && isfinite(av.z)))
+      bad = true;
+  }
+  if (__any_sync(kFull, bad) && lane == 0) atomicOr(&d.status[w], ST_NONFINITE);
+}
+
+// Phase 0: per-step controls into the accumulators, in the reference's order
+// (the caller's dBodyAdd* / dJointAdd*Torque calls precede dWorldQuickStep).
+OG_D void phase_controls(const BatchDev& d, const WorldDesc& D, int step, int lane) {
+  const int nbt = d.world[d.n_worlds - 1].body_off + d.world[d.n_worlds - 1].nb;
+  const int njt = d.world[d.n_worlds - 1].joint_off + d.world[d.n_worlds - 1].njp;
+  const int cs = d.n_ctrl_steps > 0 ? step % d.n_ctrl_steps : 0;
+  for (int b = lane; b < D.nb; b += 32) {
+    const int gb = D.body_off + b;
+    float4 f = make_float4(0.f, 0.f, 0.f, 0.f), t = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (d.body_force && d.n_ctrl_steps > 0) {
+      const float* bf = d.body_force + ((size_t)cs * nbt + gb) * 6;
+      f = make_float4(bf[0], bf[1], bf[2], 0.f);
+      t = make_float4(bf[3], bf[4], bf[5], 0.f);
+    }
+    d.facc[gb] = f;
+    d.tacc[gb] = t;
+  }
+  __syncwarp();
+  if (d.joint_torque && d.n_ctrl_steps > 0 && lane == 0) {
+    for (int j = 0; j < D.njp; ++j) {
+      const DevJoint& J = d.joints[D.joint_off + j];
+      const float* tq = d.joint_torque + ((size_t)cs * njt + D.joint_off + j) * 2;
+      if (J.type == J_HINGE) {
+        // dJointAddHingeTorque (ode/src/joints/hinge.cpp:326-345)
+        float torque = tq[0];
+        if (J.reverse) torque = -torque;
+        float R[12], ax[3];
+        body_R(d, D.body_off + J.b1, R);
+        mul0_331(ax, R, J.axis1);
+        ax[0] *= torque; ax[1] *= torque; ax[2] *= torque;
+        float4 t1 = d.tacc[D.body_off + J.b1];
+        t1.x += ax[0]; t1.y += ax[1]; t1.z += ax[2];
+        d.tacc[D.body_off + J.b1] = t1;
+        if (J.b2 >= 0) {
+          float4 t2 = d.tacc[D.body_off + J.b2];
+          t2.x += -ax[0]; t2.y += -ax[1]; t2.z += -ax[2];
+          d.tacc[D.body_off + J.b2] = t2;
+        }
+      } else if (J.type == J_HINGE2 && J.b2 >= 0) {
+        // dJointAddHinge2Torques (ode/src/joints/hinge2.cpp:393-410)
+        float R1[12], R2[12], a1[3], a2[3];
+        body_R(d, D.body_off + J.b1, R1);
+        body_R(d, D.body_off + J.b2, R2);
+        mul0_331(a1, R1, J.axis1);
+        mul0_331(a2, R2, J.axis2);
+        float t[3];
+        t[0] = a1[0] * tq[0] + a2[0] * tq[1];
+        t[1] = a1[1] * tq[0] + a2[1] * tq[1];
+        t[2] = a1[2] * tq[0] + a2[2] * tq[1];
+        float4 t1 = d.tacc[D.body_off + J.b1];
+        t1.x += t[0]; t1.y += t[1]; t1.z += t[2];
+        d.tacc[D.body_off + J.b1] = t1;
+        float4 t2 = d.tacc[D.body_off + J.b2];
+        t2.x += -t[0]; t2.y += -t[1]; t2.z += -t[2];
+        d.tacc[D.body_off + J.b2] = t2;
+      }
+    }
+  }
+  __syncwarp();
+}
+
+struct StepOptions {
+  int collide;          // 0: contacts were supplied by the host (ODE API path)
+  float* dbg_rows;      // optional: rows before scaling (parity taps)
+  float* dbg_lambda;    // optional: lambda after SOR, by world row
+  float* dbg_fc;        // optional: cforce per body
+};
+
+OG_D void world_step(const BatchDev& d, int w, int step, const WarpSmem& S, int lane,
+                     const StepOptions& opt) {
+  const WorldDesc D = d.world[w];
+  phase_controls(d, D, step, lane);
+  int nc;
+  if (opt.collide) {
+    nc = phase_collide(d, D, w, lane);
+    if (lane == 0) d.ncontacts[w] = nc;
+  } else {
+    nc = d.ncontacts[w];
+  }
+  __syncwarp();
+  phase_body_prologue(d, D, lane);
+  __syncwarp();
+  int M = 0, nisl = 0;
+  if (D.njp + nc > kMaxR) {
+    if (lane == 0) atomicOr(&d.status[w], ST_TOO_LARGE);
+    M = -1;
+  } else {
+    const int nj = phase_islands(d, D, w, nc, S, lane, &nisl);
+    M = phase_rows(d, D, w, nj, nisl, lane);
+  }
+  unsigned seed = d.seed[w];
+  const bool have_rows = M > 0;
+  if (have_rows) {
+    phase_row_setup(d, D, M, S, lane, opt.dbg_rows);
+    seed = phase_sor(d, D, w, M, nisl, seed, S, lane);
+    __syncwarp();
+    if (opt.dbg_lambda)
+      for (int r = lane; r < M; r += 32) opt.dbg_lambda[D.row_off + r] = S.lambda[r];
+    if (opt.dbg_fc)
+      for (int i = lane; i < D.nb * 6; i += 32) opt.dbg_fc[(size_t)D.body_off * 6 + i] = S.fc[i];
+  }
+  if (lane == 0) {
+    d.seed[w] = seed;
+    d.nrows[w] = M < 0 ? 0 : M;
+    d.nislands[w] = nisl;
+  }
+  phase_integrate(d, D, w, S, lane, have_rows);
+  __syncwarp();
+}
+
+}  // namespace og

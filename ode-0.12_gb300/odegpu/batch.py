@@ -1,0 +1,131 @@
+"""Batched world stepping through libodegpu's C ABI (include/odegpu.h)."""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from ._lib import lib, check
+
+_P = C.POINTER
+BODY_REC = 13
+
+
+class BatchConfig(C.Structure):
+    _fields_ = [("contacts_per_body", C.c_int), ("warps_per_block", C.c_int),
+                ("device", C.c_int)]
+
+
+class Batch:
+    """A set of independent worlds resident on one GPU.
+
+    ``step(n)`` runs n full steps (collide + QuickStep) of every world in one
+    launch; ``state()`` returns [nb_total, 13] FP64 records
+    (pos[3], q[4], lvel[3], avel[3])."""
+
+    def __init__(self, scene, contacts_per_body=8, warps_per_block=0, device=0):
+        self.scene = scene
+        cfg = BatchConfig(contacts_per_body, warps_per_block, device)
+        h = C.c_void_p()
+        check(lib().odegpuBatchCreate(C.byref(scene.c), C.byref(cfg), C.byref(h)))
+        self.h = h
+        nw, nb, nj = C.c_int(), C.c_int(), C.c_int()
+        rc, cc = C.c_longlong(), C.c_longlong()
+        check(lib().odegpuBatchInfo(h, C.byref(nw), C.byref(nb), C.byref(nj), C.byref(rc),
+                                    C.byref(cc)))
+        self.n_worlds, self.nb_total, self.nj_total = nw.value, nb.value, nj.value
+        self.row_capacity, self.contact_capacity = rc.value, cc.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().odegpuBatchDestroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def step(self, n=1):
+        check(lib().odegpuBatchStep(self.h, n))
+
+    def step_plain(self, n=1):
+        check(lib().odegpuBatchStepPlain(self.h, n))
+
+    def step_graph(self, n=1):
+        check(lib().odegpuBatchStepGraph(self.h, n))
+
+    def sync(self):
+        check(lib().odegpuBatchSynchronize(self.h))
+
+    def state(self):
+        out = np.zeros((self.nb_total, BODY_REC))
+        check(lib().odegpuBatchReadState(self.h, out.ctypes.data_as(_P(C.c_double))))
+        return out
+
+    def set_state(self, st):
+        st = np.ascontiguousarray(st, dtype=np.float64)
+        assert st.shape == (self.nb_total, BODY_REC)
+        check(lib().odegpuBatchWriteState(self.h, st.ctypes.data_as(_P(C.c_double))))
+
+    def read_state_async(self, ptr):
+        check(lib().odegpuBatchReadStateF32Async(self.h, C.c_void_p(ptr)))
+
+    def write_state_async(self, ptr):
+        check(lib().odegpuBatchWriteStateF32Async(self.h, C.c_void_p(ptr)))
+
+    def stream_handle(self):
+        return lib().odegpuBatchStream(self.h)
+
+    def status(self):
+        out = np.zeros(self.n_worlds, np.int32)
+        check(lib().odegpuBatchGetStatus(self.h, out.ctypes.data_as(_P(C.c_int))))
+        return out
+
+    def counts(self):
+        nc = np.zeros(self.n_worlds, np.int32)
+        nr = np.zeros(self.n_worlds, np.int32)
+        ni = np.zeros(self.n_worlds, np.int32)
+        check(lib().odegpuBatchGetCounts(self.h, nc.ctypes.data_as(_P(C.c_int)),
+                                         nr.ctypes.data_as(_P(C.c_int)),
+                                         ni.ctypes.data_as(_P(C.c_int))))
+        return nc, nr, ni
+
+    def seeds(self):
+        out = np.zeros(self.n_worlds, np.uint32)
+        check(lib().odegpuBatchGetSeeds(self.h, out.ctypes.data_as(_P(C.c_uint))))
+        return out
+
+    def set_step_index(self, step):
+        check(lib().odegpuBatchSetStepIndex(self.h, int(step)))
+
+    def set_seeds(self, seeds):
+        s = np.ascontiguousarray(seeds, dtype=np.uint32)
+        check(lib().odegpuBatchSetSeeds(self.h, s.ctypes.data_as(_P(C.c_uint))))
+
+    def set_controls(self, joint_torque=None, body_force=None):
+        S = 0
+        jt = bf = None
+        if joint_torque is not None:
+            jt = np.ascontiguousarray(joint_torque, dtype=np.float64)
+            S = jt.shape[0]
+        if body_force is not None:
+            bf = np.ascontiguousarray(body_force, dtype=np.float64)
+            S = bf.shape[0]
+        check(lib().odegpuBatchSetControls(
+            self.h, S, jt.ctypes.data_as(_P(C.c_double)) if jt is not None else None,
+            bf.ctypes.data_as(_P(C.c_double)) if bf is not None else None))
+
+    def step_tap(self):
+        """One step, returning (rows [R,32] f32, lambda [R], fc [nb,6], row_off [W])."""
+        rows = np.zeros((self.row_capacity, 32), np.float32)
+        lam = np.zeros(self.row_capacity, np.float32)
+        fc = np.zeros((self.nb_total, 6), np.float32)
+        ro = np.zeros(self.n_worlds, np.int32)
+        check(lib().odegpuBatchStepTap(self.h, rows.ctypes.data_as(_P(C.c_float)),
+                                       lam.ctypes.data_as(_P(C.c_float)),
+                                       fc.ctypes.data_as(_P(C.c_float)),
+                                       ro.ctypes.data_as(_P(C.c_int))))
+        return rows, lam, fc, ro
+
+    def contacts(self, w, cap=4096):
+        out = np.zeros((cap, 9), np.float32)
+        n = check(lib().odegpuBatchGetContacts(self.h, w, out.ctypes.data_as(_P(C.c_float)), cap))
+        return out[:min(n, cap)]

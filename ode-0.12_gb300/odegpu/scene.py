@@ -270,6 +270,66 @@ class Scene:
         c.body_force = _ptr(self.body_force, C.c_double)
         self.c = c
 
+    _ARRAYS = ("body_off", "geom_off", "joint_off", "body_pos", "body_q", "body_lvel",
+               "body_avel", "body_mass", "body_I", "body_flags", "geom_type", "geom_body",
+               "geom_param", "geom_surface", "joint_type", "joint_body", "joint_anchor",
+               "joint_axis1", "joint_axis2", "joint_param")
+
+    def to_arrays(self):
+        """Flat dict of numpy arrays that round-trips through from_arrays."""
+        out = {k: getattr(self, k) for k in self._ARRAYS}
+        out["world_params"] = np.array(
+            [[*wp.gravity, wp.erp, wp.cfm, wp.iterations, wp.sor_w, wp.max_vel, wp.min_depth,
+              wp.dt, wp.max_contacts, wp.seed] for wp in self.world_params[:self.n_worlds]])
+        out["surfaces"] = np.array([[s.mode, s.mu, s.mu2, s.bounce, s.bounce_vel, s.soft_erp,
+                                     s.soft_cfm, s.motion1, s.motion2, s.motionN, s.slip1, s.slip2]
+                                    for s in self.surfaces])
+        if self.joint_torque is not None:
+            out["joint_torque"] = self.joint_torque
+        if self.body_force is not None:
+            out["body_force"] = self.body_force
+        return out
+
+    @classmethod
+    def from_arrays(cls, a):
+        self = cls.__new__(cls)
+        for k in cls._ARRAYS:
+            setattr(self, k, np.ascontiguousarray(a[k]))
+        self.n_worlds = len(self.body_off) - 1
+        wpa = np.asarray(a["world_params"])
+        self.world_params = (WorldParams * max(1, self.n_worlds))()
+        for i, r in enumerate(wpa):
+            wp = self.world_params[i]
+            wp.gravity[:] = [float(x) for x in r[:3]]
+            wp.erp, wp.cfm = float(r[3]), float(r[4])
+            wp.iterations = int(r[5])
+            wp.sor_w, wp.max_vel, wp.min_depth, wp.dt = (float(x) for x in r[6:10])
+            wp.max_contacts = int(r[10])
+            wp.seed = int(r[11])
+        sa = np.asarray(a["surfaces"])
+        self.surfaces = (Surface * len(sa))()
+        for i, r in enumerate(sa):
+            self.surfaces[i].mode = int(r[0])
+            for k, v in zip(("mu", "mu2", "bounce", "bounce_vel", "soft_erp", "soft_cfm",
+                             "motion1", "motion2", "motionN", "slip1", "slip2"), r[1:]):
+                setattr(self.surfaces[i], k, float(v))
+        self.hf_heights = []
+        self.heightfields = (Heightfield * 1)()
+        self.n_heightfields = 0
+        self.n_ctrl_steps = 0
+        self.joint_torque = None
+        self.body_force = None
+        self.nb_total = int(self.body_off[-1])
+        self.nj_total = int(self.joint_off[-1])
+        self.ng_total = int(self.geom_off[-1])
+        jt = a["joint_torque"] if "joint_torque" in a else None
+        bf = a["body_force"] if "body_force" in a else None
+        if jt is not None or bf is not None:
+            self.set_controls(jt, bf)
+        else:
+            self._refresh()
+        return self
+
     def world_bodies(self, w):
         return int(self.body_off[w]), int(self.body_off[w + 1])
 

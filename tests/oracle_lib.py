@@ -85,3 +85,44 @@ def run_world(fn, scene, w, n_steps, max_rec=512, feedback=False):
             seeds.ctypes.data_as(_P(C.c_uint)))
     assert rc == 0
     return dict(state=state, ncontacts=ncont, contacts=cont, feedback=fb, seeds=seeds)
+
+
+class OracleTap(C.Structure):
+    _fields_ = [("n_islands", C.c_int), ("island_rows", _P(C.c_int)),
+                ("island_bodies", _P(C.c_int)), ("cap_islands", C.c_int),
+                ("J", _P(C.c_double)), ("rhs", _P(C.c_double)), ("cfm", _P(C.c_double)),
+                ("lo", _P(C.c_double)), ("hi", _P(C.c_double)), ("findex", _P(C.c_int)),
+                ("jb", _P(C.c_int)), ("cap_rows", C.c_int), ("body_of", _P(C.c_int)),
+                ("cap_bodies", C.c_int), ("lambda_", _P(C.c_double)), ("cforce", _P(C.c_double)),
+                ("joint_of_row", _P(C.c_int)), ("seed_before", C.c_uint)]
+
+
+def tap_step(scene, w, pre_steps, cap_rows=4096, cap_bodies=1024):
+    """Oracle stage taps of step `pre_steps` of world w (see ode_oracle.h)."""
+    L = oracle()
+    L.oracle_tap_step.restype = C.c_int
+    L.oracle_tap_step.argtypes = [C.c_void_p, C.c_int, C.c_int, _P(OracleTap)]
+    a = dict(island_rows=np.zeros(cap_bodies, np.int32), island_bodies=np.zeros(cap_bodies, np.int32),
+             J=np.zeros((cap_rows, 12)), rhs=np.zeros(cap_rows), cfm=np.zeros(cap_rows),
+             lo=np.zeros(cap_rows), hi=np.zeros(cap_rows), findex=np.zeros(cap_rows, np.int32),
+             jb=np.zeros((cap_rows, 2), np.int32), body_of=np.zeros(cap_bodies, np.int32),
+             lam=np.zeros(cap_rows), cforce=np.zeros((cap_bodies, 6)),
+             joint_of_row=np.zeros(cap_rows, np.int32))
+    t = OracleTap()
+    t.cap_islands = cap_bodies
+    t.cap_rows = cap_rows
+    t.cap_bodies = cap_bodies
+    for k in ("island_rows", "island_bodies", "findex", "jb", "body_of", "joint_of_row"):
+        setattr(t, k, a[k].ctypes.data_as(_P(C.c_int)))
+    for k in ("J", "rhs", "cfm", "lo", "hi", "cforce"):
+        setattr(t, k, a[k].ctypes.data_as(_P(C.c_double)))
+    t.lambda_ = a["lam"].ctypes.data_as(_P(C.c_double))
+    total = L.oracle_tap_step(C.byref(scene.c), w, pre_steps, C.byref(t))
+    assert total >= 0
+    n = t.n_islands
+    a["n_islands"] = n
+    a["total_rows"] = total
+    a["seed_before"] = t.seed_before
+    a["island_rows"] = a["island_rows"][:n]
+    a["island_bodies"] = a["island_bodies"][:n]
+    return a

@@ -1,0 +1,146 @@
+"""Parity of the CUDA path against the FP64 oracle (which is itself pinned
+bit-for-bit to the reference ODE 0.12 by test_oracle.py).
+
+Integer outputs (contact counts, island and row counts, row order, findex,
+lo/hi, RNG state) must be bit-exact. FP32 outputs are compared to the FP64
+oracle with the tolerances written in each test."""
+import numpy as np
+import pytest
+
+from odegpu import scene as S
+from gpu_helpers import oracle_states, stacked_state, seeds_before, state_err
+import oracle_lib as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def batch_cls():
+    from odegpu.batch import Batch
+    return Batch
+
+
+# one-step tolerances (state after one step from an identical FP64->FP32 start)
+POS_ATOL = 2e-5     # m
+Q_ATOL = 2e-5
+VEL_ATOL = 2e-3     # m/s, rad/s: SOR in FP32 vs FP64 after 20 iterations
+
+
+def _scenes():
+    return {
+        "box_drop": S.box_drop(seed=0),
+        "batched": S.batched_worlds(n_worlds=48, seed=11),
+        "hinge": S.hinge_chains(n_worlds=8, steps=40),
+        "stack": S.box_stack(n_worlds=4, height=5),
+    }
+
+
+@pytest.mark.parametrize("name", ["box_drop", "batched", "hinge", "stack"])
+def test_one_step_from_oracle_state(batch_cls, name):
+    sc = _scenes()[name]
+    n = 40
+    runs = oracle_states(sc, n)
+    B = batch_cls(sc)
+    worst = dict(pos=0, q=0, lvel=0, avel=0)
+    nc_mismatch = 0
+    for k in (0, 5, 15, 25, 39):
+        B.set_state(stacked_state(runs, k))
+        B.set_seeds(seeds_before(sc, runs, k))
+        B.set_step_index(k)
+        B.step(1)
+        g = B.state()
+        nc, nr, ni = B.counts()
+        ref_nc = np.array([r["ncontacts"][k] for r in runs])
+        nc_mismatch += int(np.sum(nc != ref_nc))
+        e = state_err(g, stacked_state(runs, k + 1))
+        for key in worst:
+            worst[key] = max(worst[key], e[key])
+        if np.array_equal(nc, ref_nc):
+            seeds = B.seeds()
+            ref_seeds = np.array([r["seeds"][k] for r in runs], np.uint32)
+            assert np.array_equal(seeds, ref_seeds), f"RNG state differs at step {k}"
+    assert (B.status() == 0).all()
+    assert nc_mismatch == 0, f"contact counts differ in {nc_mismatch} world-steps"
+    assert worst["pos"] < POS_ATOL and worst["q"] < Q_ATOL, worst
+    assert worst["lvel"] < VEL_ATOL and worst["avel"] < VEL_ATOL, worst
+
+
+@pytest.mark.parametrize("name", ["batched", "hinge", "box_drop"])
+def test_rows_and_lambda_tap(batch_cls, name):
+    """Row assembly (getInfo2 + rhs + cfm) and SOR lambda per world vs the oracle
+    taps, from the same starting state."""
+    sc = _scenes()[name]
+    k = 30
+    runs = oracle_states(sc, k)
+    B = batch_cls(sc)
+    B.set_state(stacked_state(runs, k))
+    B.set_seeds(seeds_before(sc, runs, k))
+    B.set_step_index(k)
+    rows, lam, fc, row_off = B.step_tap()
+    nc, nr, ni = B.counts()
+    checked = 0
+    for w in range(sc.n_worlds):
+        t = O.tap_step(sc, w, k)
+        M = t["total_rows"]
+        assert nr[w] == M, f"world {w}: rows {nr[w]} vs {M}"
+        assert ni[w] == int(np.sum(t["island_rows"] > 0)), f"world {w}: islands"
+        if M == 0:
+            continue
+        R = rows[row_off[w]:row_off[w] + M]
+        Ri = R.view(np.int32)
+        # island-local -> world rows: islands are contiguous in both
+        starts = np.concatenate([[0], np.cumsum(t["island_rows"])])
+        gfx = Ri[:, 28]
+        ofx = t["findex"][:M]
+        isl_of_row = np.searchsorted(starts, np.arange(M), side="right") - 1
+        ofx_world = np.where(ofx >= 0, ofx + starts[isl_of_row], -1)
+        assert np.array_equal(gfx, ofx_world), f"world {w}: findex"
+        assert np.array_equal(np.isinf(R[:, 26]), np.isinf(t["lo"][:M])), f"world {w}: lo inf"
+        fin = np.isfinite(t["lo"][:M])
+        np.testing.assert_allclose(R[fin, 26], t["lo"][:M][fin], rtol=1e-6, atol=0)
+        fin = np.isfinite(t["hi"][:M])
+        np.testing.assert_allclose(R[fin, 27], t["hi"][:M][fin], rtol=1e-6, atol=0)
+        # bodies: oracle island-local tags -> world-local through body_of
+        bstart = np.concatenate([[0], np.cumsum(t["island_bodies"])])
+        jb = t["jb"][:M]
+        wb1 = t["body_of"][bstart[isl_of_row] + jb[:, 0]]
+        wb2 = np.where(jb[:, 1] >= 0, t["body_of"][bstart[isl_of_row] + np.maximum(jb[:, 1], 0)], -1)
+        assert np.array_equal(Ri[:, 29], wb1), f"world {w}: b1"
+        assert np.array_equal(Ri[:, 30], wb2), f"world {w}: b2"
+        np.testing.assert_allclose(R[:, :12], t["J"][:M], rtol=1e-4, atol=2e-5)
+        np.testing.assert_allclose(R[:, 24], t["rhs"][:M], rtol=1e-3, atol=2e-3)
+        np.testing.assert_allclose(R[:, 25], t["cfm"][:M], rtol=1e-5)
+        # lambda after 20 FP32 PGS iterations vs FP64: impulse scale tolerance
+        scale = max(1.0, np.abs(t["lam"][:M]).max())
+        np.testing.assert_allclose(lam[row_off[w]:row_off[w] + M], t["lam"][:M], rtol=0,
+                                   atol=2e-3 * scale)
+        checked += 1
+    assert checked > 0
+
+
+def test_stack_trajectory_200_steps(batch_cls):
+    """Non-chaotic 5-box stacks, 200 steps: final positions within 1e-4 relative
+    (FP32 GPU vs FP64 oracle)."""
+    sc = S.box_stack(n_worlds=4, height=5)
+    runs = oracle_states(sc, 200)
+    B = batch_cls(sc)
+    B.step(200)
+    g = B.state()
+    ref = stacked_state(runs, 200)
+    rel = np.abs(g[:, 0:3] - ref[:, 0:3]) / np.maximum(np.abs(ref[:, 0:3]), 1e-3)
+    assert (B.status() == 0).all()
+    assert rel.max() <= 1e-4, rel.max()
+
+
+def test_launch_modes_agree(batch_cls):
+    """One launch of n steps, n graph-captured single-step launches and the
+    one-world-per-launch path run identical arithmetic: bit-identical states."""
+    sc = S.batched_worlds(n_worlds=24, seed=5)
+    outs = []
+    for mode in ("step", "graph", "plain"):
+        B = batch_cls(sc)
+        getattr(B, {"step": "step", "graph": "step_graph", "plain": "step_plain"}[mode])(12)
+        B.sync()
+        outs.append(B.state())
+    assert np.array_equal(outs[0], outs[1])
+    assert np.array_equal(outs[0], outs[2])
