@@ -482,3 +482,91 @@ def hinge_chains(n_worlds=1024, links=8, seed=4, steps=100):
     tq[:, :, 0] = rng.uniform(-2, 2, (steps, sc.nj_total))
     sc.set_controls(joint_torque=tq)
     return sc
+
+
+def capsule_mix(seed=6, n_bodies=12):
+    """Capsules (r U[0.1,0.3], length U[0.2,0.8]), spheres and boxes dropped on
+    plane z=0 on a 2 m grid (so capsules meet only the plane: capsule-box,
+    capsule-sphere and capsule-capsule are not on this path); same surface as
+    box_drop."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    b = SceneBuilder()
+    s = _std_surface(b, 0.5)
+    w = b.new_world(cfm=1e-5, seed=seed)
+    b.add_geom(w, GEOM_PLANE, -1, (0, 0, 1, 0), s)
+    for k in range(n_bodies):
+        x, y = 2.0 * (k % 4) + rng.uniform(-0.2, 0.2), 2.0 * (k // 4) + rng.uniform(-0.2, 0.2)
+        z = rng.uniform(0.3, 3)
+        ang = rng.uniform(-1, 1, 3)
+        qv = np.concatenate([[1.0], 0.5 * ang])
+        qv /= np.linalg.norm(qv)
+        kind = k % 3
+        if kind == 0:
+            r, L = rng.uniform(0.1, 0.3), rng.uniform(0.2, 0.8)
+            m, I = sphere_mass(1000.0, r)  # inertia of a comparable sphere
+            bi = b.add_body(w, (x, y, z), m, I, q=tuple(qv))
+            b.add_geom(w, GEOM_CAPSULE, bi, (r, L), s)
+        elif kind == 1:
+            r = rng.uniform(0.1, 0.4)
+            m, I = sphere_mass(1000.0, r)
+            bi = b.add_body(w, (x, y, z), m, I, q=tuple(qv))
+            b.add_geom(w, GEOM_SPHERE, bi, (r,), s)
+        else:
+            lx, ly, lz = rng.uniform(0.2, 0.8, 3)
+            m, I = box_mass(1000.0, lx, ly, lz)
+            bi = b.add_body(w, (x, y, z), m, I, q=tuple(qv))
+            b.add_geom(w, GEOM_BOX, bi, (lx, ly, lz), s)
+    return b.build()
+
+
+def sphere_pyramid(n_worlds=1, levels=3, r=0.25, seed=8, spacing=4.0):
+    """Non-chaotic stack: a triangular pyramid of equal spheres (levels 3 -> 6
+    base + 3 + 1) settled on plane z=0, mu=0.5; sphere-sphere contacts have no
+    feature ties, so FP32 and FP64 trajectories stay close. Worlds are placed
+    `spacing` apart with sub-mm seeded jitter."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    b = SceneBuilder()
+    s = _std_surface(b, 0.5)
+    for wi in range(n_worlds):
+        w = b.new_world(cfm=1e-5, seed=int(rng.integers(0, 2**32)))
+        b.add_geom(w, GEOM_PLANE, -1, (0, 0, 1, 0), s)
+        d = 2 * r
+        h = d * math.sqrt(2.0 / 3.0)
+        for lv in range(levels):
+            n = levels - lv
+            z = r + lv * h - 1e-4
+            # triangular layer of side n, centred over the layer below
+            cx = lv * d / 2.0
+            cy = lv * d / (2.0 * math.sqrt(3.0))
+            for i in range(n):
+                for j in range(n - i):
+                    x = cx + (j + 0.5 * i) * d + spacing * wi
+                    y = cy + i * d * math.sqrt(3.0) / 2.0
+                    jit = rng.uniform(-1e-4, 1e-4, 2)
+                    m, I = sphere_mass(1000.0, r)
+                    bi = b.add_body(w, (x + jit[0], y + jit[1], z), m, I)
+                    b.add_geom(w, GEOM_SPHERE, bi, (r,), s)
+    return b.build()
+
+
+def box_tower(n_worlds=1, height=5, seed=9, spacing=4.0, shrink=0.8, yaw=0.3):
+    """Stack of boxes of decreasing size (edge 0.6 m * shrink**k), each yawed by
+    `yaw`*k rad about z, resting on plane z=0 (1 mm initial overlap)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    b = SceneBuilder()
+    s = _std_surface(b, 0.5)
+    for wi in range(n_worlds):
+        w = b.new_world(cfm=1e-5, seed=int(rng.integers(0, 2**32)))
+        b.add_geom(w, GEOM_PLANE, -1, (0, 0, 1, 0), s)
+        z = 0.0
+        for k in range(height):
+            L = 0.6 * shrink ** k
+            H = 0.3 * shrink ** k
+            m, I = box_mass(1000.0, L, L, H)
+            a = yaw * k + rng.uniform(-0.01, 0.01)
+            q = (math.cos(a / 2), 0.0, 0.0, math.sin(a / 2))
+            jit = rng.uniform(-1e-3, 1e-3, 2)
+            bi = b.add_body(w, (spacing * wi + jit[0], jit[1], z + H / 2 - 1e-3), m, I, q=q)
+            b.add_geom(w, GEOM_BOX, bi, (L, L, H), s)
+            z += H - 1e-3
+    return b.build()

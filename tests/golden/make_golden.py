@@ -1,0 +1,140 @@
+"""Generates the golden fixtures in this directory from the REFERENCE ODE 0.12
+(built from its own sources by `make -C oracle ref` into oracle/_ref/,
+double precision, driven through its public C API by oracle/ref_harness.cpp).
+
+Run from the repository root where the reference sources are present:
+    make -C oracle ref && python tests/golden/make_golden.py
+Each .npz holds the scene arrays (so no generator has to be re-run), the
+reference's per-step contact counts, contact records, RNG seeds, body states
+at selected steps, and joint feedback. collider_kats.npz holds single dCollide
+calls on seeded near-contact poses for every collider on the path.
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(ROOT, "ode-0.12_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+
+from odegpu import scene as S  # noqa: E402
+import oracle_lib as O  # noqa: E402
+
+SCENES = {
+    "box_drop": (lambda: S.box_drop(seed=0), 80),
+    "batched": (lambda: S.batched_worlds(n_worlds=6, seed=7), 60),
+    "hinge": (lambda: S.hinge_chains(n_worlds=3, steps=60), 60),
+    "stack": (lambda: S.box_stack(n_worlds=2, height=5), 100),
+    "capsule": (lambda: S.capsule_mix(seed=6), 80),
+}
+KEEP = 10  # keep the state every KEEP steps
+
+
+def make_scene(name):
+    mk, steps = SCENES[name]
+    sc = mk()
+    ref = O.ref("d")
+    out = dict(sc.to_arrays())
+    out["n_steps"] = np.int64(steps)
+    for w in range(sc.n_worlds):
+        r = O.run_world(ref.ref_run_world, sc, w, steps, max_rec=96, feedback=True)
+        out[f"w{w}_ncontacts"] = r["ncontacts"]
+        out[f"w{w}_contacts"] = r["contacts"][:, :64].astype(np.float64)
+        out[f"w{w}_seeds"] = r["seeds"]
+        out[f"w{w}_state"] = r["state"][::KEEP]
+        out[f"w{w}_final"] = r["state"][-1]
+        out[f"w{w}_feedback"] = r["feedback"]
+    np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **out)
+
+
+def rot(rng):
+    q = rng.normal(size=4)
+    q /= np.linalg.norm(q)
+    w, x, y, z = q
+    return np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y)],
+                     [2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x)],
+                     [2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)]])
+
+
+def make_collider_kats(n=120, seed=123):
+    """Random near-contact poses for each class pair, both argument orders."""
+    import ctypes as C
+    rng = np.random.Generator(np.random.PCG64(seed))
+    ref = O.ref("d")
+    pairs = [(0, 0), (0, 1), (1, 0), (0, 4), (4, 0), (1, 1), (1, 4), (4, 1), (2, 4), (4, 2)]
+    recs = []
+    for (t1, t2) in pairs:
+        for _ in range(n):
+            def params(t):
+                if t == 0:
+                    return np.array([rng.uniform(0.1, 0.6), 0, 0, 0])
+                if t == 1:
+                    return np.concatenate([rng.uniform(0.2, 1.2, 3), [0]])
+                if t == 2:
+                    return np.array([rng.uniform(0.1, 0.4), rng.uniform(0.2, 1.0), 0, 0])
+                nrm = rng.normal(size=3)
+                nrm /= np.linalg.norm(nrm)
+                return np.concatenate([nrm, [rng.uniform(-0.3, 0.3)]])
+            p1, p2 = params(t1), params(t2)
+            pos1 = rng.uniform(-0.6, 0.6, 3)
+            pos2 = rng.uniform(-0.6, 0.6, 3)
+            R1, R2 = rot(rng), rot(rng)
+            flags = int(rng.choice([1, 2, 3, 4, 8]))
+            out = np.zeros((16, 9))
+            P = C.POINTER(C.c_double)
+            args = [np.ascontiguousarray(a, dtype=np.float64) for a in
+                    (p1, pos1, R1.ravel(), p2, pos2, R2.ravel())]
+            nc = ref.ref_collide(t1, args[0].ctypes.data_as(P), args[1].ctypes.data_as(P),
+                                 args[2].ctypes.data_as(P), t2, args[3].ctypes.data_as(P),
+                                 args[4].ctypes.data_as(P), args[5].ctypes.data_as(P), flags,
+                                 out.ctypes.data_as(P))
+            recs.append((t1, t2, flags, p1, pos1, R1.ravel(), p2, pos2, R2.ravel(), nc, out[:8]))
+    np.savez_compressed(
+        os.path.join(HERE, "collider_kats.npz"),
+        t1=np.array([r[0] for r in recs]), t2=np.array([r[1] for r in recs]),
+        flags=np.array([r[2] for r in recs]),
+        p1=np.array([r[3] for r in recs]), pos1=np.array([r[4] for r in recs]),
+        R1=np.array([r[5] for r in recs]), p2=np.array([r[6] for r in recs]),
+        pos2=np.array([r[7] for r in recs]), R2=np.array([r[8] for r in recs]),
+        nc=np.array([r[9] for r in recs]), out=np.array([r[10] for r in recs]))
+
+
+def make_tower():
+    """Non-chaotic stacks (boxes of decreasing size, aligned): FP64 reference
+    states after 200 steps plus the reference's own FP32 (dSINGLE) build on the
+    same scene, whose drift from FP64 sets the achievable FP32 bar."""
+    sc = S.box_tower(n_worlds=6, yaw=0.0, spacing=0.0)
+    out = dict(sc.to_arrays())
+    out["n_steps"] = np.int64(200)
+    for w in range(sc.n_worlds):
+        d = O.run_world(O.ref("d").ref_run_world, sc, w, 200)
+        s_ = O.run_world(O.ref("s").ref_run_world, sc, w, 200)
+        out[f"w{w}_final_d"] = d["state"][-1]
+        out[f"w{w}_final_s"] = s_["state"][-1]
+        out[f"w{w}_ncontacts"] = d["ncontacts"]
+    np.savez_compressed(os.path.join(HERE, "tower.npz"), **out)
+
+
+def make_rng_kat():
+    ref = O.ref("d")
+    seeds = [0, 1, 12345, 0xdeadbeef, 0xffffffff]
+    ns = [1, 2, 3, 4, 5, 16, 17, 100, 256, 257, 1000, 65536, 65537, 1000000]
+    vals = []
+    for s in seeds:
+        ref.ref_rand_set_seed(s)
+        vals.append([ref.ref_rand_int(n) for n in ns for _ in range(7)])
+    np.savez_compressed(os.path.join(HERE, "rng_kat.npz"), seeds=np.array(seeds, np.uint32),
+                        ns=np.array(ns), vals=np.array(vals))
+
+
+if __name__ == "__main__":
+    assert O.ref_available("d"), "build the reference first: make -C oracle ref"
+    for name in SCENES:
+        make_scene(name)
+        print("wrote", name)
+    make_collider_kats()
+    make_rng_kat()
+    make_tower()
+    print("wrote collider_kats, rng_kat")

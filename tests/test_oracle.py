@@ -1,0 +1,106 @@
+"""CPU tests of the oracle (the checker): known-answer tests from the reference,
+golden vectors produced by the reference ODE 0.12, and, where the reference was
+built in this checkout, live bit-for-bit comparison against it."""
+import ctypes as C
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from odegpu import scene as S
+import oracle_lib as O
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+_P = C.POINTER
+
+
+def test_rand_kat():
+    """dTestRand's first five LCG outputs from seed 0 (ode/src/misc.cpp:52-62)."""
+    L = O.oracle()
+    assert L.oracle_test_rand() == 1
+    L.oracle_rand_set_seed(0)
+    expect = [0x3c6ef35f, 0x47502932, 0xd1ccf6e9, 0xaaf95334, 0x6252e503]
+    got = []
+    for _ in expect:
+        L.oracle_rand_int(1 << 30)  # one dRand call each; seed readback below
+        got.append(L.oracle_rand_get_seed())
+    assert got == expect
+
+
+def test_rand_int_golden():
+    """dRandInt over the xor-fold branches, against reference output."""
+    g = np.load(os.path.join(GOLDEN, "rng_kat.npz"))
+    L = O.oracle()
+    for s, row in zip(g["seeds"], g["vals"]):
+        L.oracle_rand_set_seed(int(s))
+        got = [L.oracle_rand_int(int(n)) for n in g["ns"] for _ in range(7)]
+        assert got == list(row)
+
+
+def test_collider_kats_golden():
+    """Every collider on the path, single dCollide calls on seeded near-contact
+    poses, both argument orders: contact count and records bit-exact vs the
+    reference."""
+    g = np.load(os.path.join(GOLDEN, "collider_kats.npz"))
+    L = O.oracle()
+    n = len(g["t1"])
+    mism = 0
+    for i in range(n):
+        out = np.zeros((16, 9))
+        args = [np.ascontiguousarray(g[k][i], dtype=np.float64) for k in
+                ("p1", "pos1", "R1", "p2", "pos2", "R2")]
+        nc = L.oracle_collide(int(g["t1"][i]), *(a.ctypes.data_as(_P(C.c_double)) for a in args[:3]),
+                              int(g["t2"][i]), *(a.ctypes.data_as(_P(C.c_double)) for a in args[3:]),
+                              int(g["flags"][i]), out.ctypes.data_as(_P(C.c_double)))
+        if nc != g["nc"][i] or not np.array_equal(out[:nc, :7], g["out"][i][:nc, :7]):
+            mism += 1
+    assert mism == 0, f"{mism} of {n} collider calls differ"
+    assert (g["nc"] > 0).sum() > n // 4  # the poses do exercise contact
+
+
+@pytest.mark.parametrize("name", ["box_drop", "batched", "hinge", "stack", "capsule"])
+def test_oracle_matches_reference_golden(name):
+    """Whole-step parity: contact counts, contact records, RNG seeds, body
+    states and joint feedback are bit-identical to the reference (FP64)."""
+    g = dict(np.load(os.path.join(GOLDEN, f"{name}.npz")))
+    sc = S.Scene.from_arrays(g)
+    steps = int(g["n_steps"])
+    for w in range(sc.n_worlds):
+        r = O.run_world(O.oracle().oracle_run_world, sc, w, steps, max_rec=96, feedback=True)
+        assert np.array_equal(r["ncontacts"], g[f"w{w}_ncontacts"])
+        assert np.array_equal(r["seeds"], g[f"w{w}_seeds"])
+        assert np.array_equal(r["contacts"][:, :64], g[f"w{w}_contacts"])
+        assert np.array_equal(r["state"][::10], g[f"w{w}_state"])
+        assert np.array_equal(r["state"][-1], g[f"w{w}_final"])
+        assert np.array_equal(r["feedback"], g[f"w{w}_feedback"])
+
+
+@pytest.mark.skipif(not O.ref_available("d"), reason="reference not built in this checkout")
+@pytest.mark.parametrize("seed", [21, 22])
+def test_oracle_matches_reference_live(seed):
+    sc = S.batched_worlds(n_worlds=3, seed=seed)
+    for w in range(sc.n_worlds):
+        o = O.run_world(O.oracle().oracle_run_world, sc, w, 50)
+        r = O.run_world(O.ref("d").ref_run_world, sc, w, 50)
+        for k in ("ncontacts", "seeds", "state", "contacts"):
+            assert np.array_equal(o[k], r[k]), k
+
+
+def test_scene_roundtrip():
+    sc = S.hinge_chains(n_worlds=2, steps=5)
+    sc2 = S.Scene.from_arrays(sc.to_arrays())
+    for k in S.Scene._ARRAYS:
+        assert np.array_equal(getattr(sc, k), getattr(sc2, k))
+    assert np.array_equal(sc.joint_torque, sc2.joint_torque)
+
+
+def test_multithreaded_baseline_is_deterministic():
+    """The CPU-baseline entry (many worlds on host threads) gives the same
+    result as running the worlds one by one."""
+    sc = S.batched_worlds(n_worlds=6, seed=3)
+    out = np.zeros((sc.nb_total, 13))
+    O.oracle().oracle_run_worlds(C.byref(sc.c), 0, sc.n_worlds, 15, 4, out.ctypes.data_as(_P(C.c_double)))
+    ref = np.concatenate([O.run_world(O.oracle().oracle_run_world, sc, w, 15)["state"][-1]
+                          for w in range(sc.n_worlds)])
+    assert np.array_equal(out, ref)
