@@ -115,17 +115,17 @@ def algorithmic_bytes(sc, nc, nr, iters=20):
     return float(np.sum(208.0 * nb + 56.0 * nc + 40.0 * nj + nr * (248.0 + 236.0 * iters)))
 
 
-def cpu_baseline(sc, n_worlds_sample=None, n_steps=20, threads=None):
-    """Oracle port (FP64 restatement of ODE's algorithm) on a bounded sample of
-    the workload, all host threads; returns world-steps/s."""
+def cpu_baseline(sc, n_worlds_sample, n_steps, threads=None):
+    """Oracle port (FP64 restatement of ODE's algorithm, oracle/liboracle.so) on
+    worlds [0, n_worlds_sample) for n_steps from the initial state, all host
+    threads (one world per thread at a time); returns world-steps/s."""
     import oracle_lib as O
     L = O.oracle()
     threads = threads or (os.cpu_count() or 1)
-    n_worlds_sample = n_worlds_sample or min(sc.n_worlds, 64 * threads)
     t0 = time.perf_counter()
     L.oracle_run_worlds(C.byref(sc.c), 0, n_worlds_sample, n_steps, threads, None)
     dt = time.perf_counter() - t0
-    return n_worlds_sample * n_steps / dt, threads, n_worlds_sample, n_steps, dt
+    return n_worlds_sample * n_steps / dt, threads, dt
 
 
 def run_reference(args):
@@ -135,27 +135,18 @@ def run_reference(args):
     sc = build_scene(N_WORLDS)
     import oracle_lib as O
     O.build_oracle()
-    vals = []
     threads = os.cpu_count() or 1
-    sample_worlds = min(N_WORLDS, 32 * threads)
-    for _ in range(max(1, args.warmup)):
-        cpu_baseline(sc, sample_worlds, 5, threads)
-    t_total = 0.0
-    for _ in range(args.steps):
-        v, thr, nw, ns, dt = cpu_baseline(sc, sample_worlds, 5, threads)
-        vals.append(v)
-        t_total += dt
-    value = float(np.mean(vals))
+    sample = min(N_WORLDS, args.ref_worlds)
+    cpu_baseline(sc, min(sample, 4 * threads), max(1, args.warmup))      # warm-up
+    value, _, dt = cpu_baseline(sc, sample, args.steps, threads)
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "world-steps/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * N_WORLDS / value, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
-            "config": {"workload": WORKLOAD, "n_worlds": N_WORLDS, "iterations": 20,
-                       "dt": 0.01},
-            "cpu_baseline": {"value": value, "unit": "world-steps/s", "cores": threads,
-                             "kind": "port",
-                             "sample": f"first {sample_worlds} worlds x 5 steps from the initial "
-                                       f"state per bench step, {threads} threads"},
+            "config": {"workload": WORKLOAD, "n_worlds": N_WORLDS, "iterations": 20, "dt": 0.01},
+            "cpu_baseline": {"value": value, "unit": "world-steps/s", "cores": threads, "kind": "port",
+                             "sample": f"worlds 0..{sample - 1} of the workload, {args.steps} steps "
+                                       f"from the initial state ({dt:.1f} s), {threads} threads"},
             "e2e": {"value": value, "unit": "world-steps/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -171,46 +162,54 @@ def run_ours(args):
         import torch.distributed as tdist
         tdist.init_process_group("nccl")
     torch.cuda.set_device(local_rank)
-    # weak scaling: every rank steps its own 4096-world batch (distinct seeds)
+    # weak scaling: every rank steps its own 4096-world batch (distinct seeds);
+    # the step has no collective, only the timing is reduced
     sc = build_scene(N_WORLDS, seed=SCENE_SEED + rank)
     B = Batch(sc, device=local_rank)
     stream = torch.cuda.ExternalStream(B.stream_handle())
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     iters = sc.world_params[0].iterations
+    init_state = B.state()
+    init_seeds = B.seeds()
+
+    def reset():
+        B.set_state(init_state)
+        B.set_seeds(init_seeds)
+        B.set_step_index(0)
 
     def barrier():
         if dist:
             torch.distributed.barrier()
         torch.cuda.synchronize()
 
-    # warm-up (also settles the falling bodies into contact)
     for _ in range(args.warmup):
         B.step(1)
     B.sync()
+    reset()
     barrier()
     clocks = ClockSampler(local_rank)
     clocks.start()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
           for _ in range(args.steps)]
-    bytes_total = 0.0
+    bytes_per_step = []
     launches = 0
     barrier()
     for k in range(args.steps):
         with torch.cuda.stream(stream):
             flush.add_(1.0)           # evict L2 between timed steps (256 MB > 129 MB L2)
-            launches += 1
             ev[k][0].record(stream)
         B.step(1)
-        launches += 1
         with torch.cuda.stream(stream):
             ev[k][1].record(stream)
+        launches += 2
+        nc, nr, _ = B.counts()        # host read between steps, outside the events
+        bytes_per_step.append(algorithmic_bytes(sc, nc, nr, iters))
     B.sync()
     barrier()
     clk = clocks.stop()
-    t_kernel = sum(a.elapsed_time(b) for a, b in ev) / 1e3
-    nc, nr, _ = B.counts()
-    bytes_total = algorithmic_bytes(sc, nc, nr, iters) * args.steps
-    # max over ranks
+    times = np.array([a.elapsed_time(b) for a, b in ev]) / 1e3
+    t_kernel = float(times.sum())
+    stat = B.status()
     t_max = t_kernel
     if dist:
         t = torch.tensor([t_kernel], device="cuda")
@@ -218,16 +217,17 @@ def run_ours(args):
         t_max = float(t.item())
     value = N_WORLDS * world_size * args.steps / t_max
 
-    # e2e through the C ABI with host buffers: H2D state, step, D2H state, per step
+    # e2e through the C ABI with host buffers: per step H2D of the state from
+    # pinned memory, the step, D2H of the new state, synchronised
     nbt = B.nb_total
     h_in = torch.empty(nbt * 13, dtype=torch.float32, pin_memory=True)
     h_out = torch.empty(nbt * 13, dtype=torch.float32, pin_memory=True)
+    reset()
     B.read_state_async(h_in.data_ptr())
     B.sync()
-    e2e_steps = max(3, args.steps // 2)
     barrier()
     t0 = time.perf_counter()
-    for _ in range(e2e_steps):
+    for _ in range(args.steps):
         B.write_state_async(h_in.data_ptr())
         B.step(1)
         B.read_state_async(h_out.data_ptr())
@@ -235,32 +235,51 @@ def run_ours(args):
         h_in, h_out = h_out, h_in
     barrier()
     t_e2e = time.perf_counter() - t0
-    e2e = N_WORLDS * world_size * e2e_steps / t_e2e
-    stat = B.status()
+    e2e = N_WORLDS * world_size * args.steps / t_e2e
 
     if rank == 0:
         hbm, src = peaks()
-        t_launch = t_kernel / args.steps
-        achieved = bytes_total / args.steps / t_launch / 1e9
+        achieved = float(np.sum(bytes_per_step)) / t_kernel / 1e9
         line = {"metric": METRIC, "value": value, "unit": "world-steps/s", "n_gpus": world_size,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                 "data": "synthetic (seeded)",
                 "config": {"workload": WORKLOAD, "n_worlds": N_WORLDS, "iterations": iters,
-                           "dt": 0.01, "l2": "flushed between timed steps (256 MB write)",
-                           "bodies": int(nbt), "contacts_last_step": int(nc.sum()),
-                           "rows_last_step": int(nr.sum()), "worlds_with_status": int((stat != 0).sum())},
+                           "dt": 0.01, "rollout": f"steps 0..{args.steps - 1} from the initial state",
+                           "l2": "flushed between timed steps (256 MB write)",
+                           "bodies": int(nbt), "worlds_with_status": int((stat != 0).sum()),
+                           "step_ms_min_median_max": [float(1e3 * times.min()), float(1e3 * np.median(times)),
+                                                      float(1e3 * times.max())]},
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                             "frac": achieved / hbm, "peak_source": src,
-                             "traffic": None,
-                             "kernel": "world_step_kernel (one warp per world)"},
+                             "frac": achieved / hbm, "peak_source": src, "traffic": None,
+                             "kernel": "world_step_kernel (one warp per world)",
+                             "bytes_model": "208*nb + 56*nc + 40*n_ball + m*(248 + 236*iters) per world"},
                 "e2e": {"value": e2e, "unit": "world-steps/s", "h2d_bytes_per_step": nbt * 13 * 4,
                         "d2h_bytes_per_step": nbt * 13 * 4},
                 "gpu_launches": launches, "clocks": clk}
+        if not args.no_plain:
+            # plain comparator: the same kernel, one world per launch, first
+            # 512 worlds x 20 steps from the initial state
+            reset()
+            pw = 512
+            sub = build_scene(pw)
+            P = Batch(sub, device=local_rank)
+            P.step_plain(2)
+            P.sync()
+            P.set_state(sub_init := P.state())
+            t0 = time.perf_counter()
+            P.step_plain(20)
+            P.sync()
+            tp = time.perf_counter() - t0
+            line["plain_gpu"] = {"value": pw * 20 / tp, "unit": "world-steps/s",
+                                 "sample": f"first {pw} worlds x 20 steps, one world per launch"}
+            P.close()
         if not args.no_cpu:
-            v, thr, nw, ns, dt = cpu_baseline(sc, min(N_WORLDS, 16 * (os.cpu_count() or 1)), 20)
+            nw = min(N_WORLDS, args.cpu_worlds)
+            v, thr, dt = cpu_baseline(sc, nw, args.steps)
             line["cpu_baseline"] = {"value": v, "unit": "world-steps/s", "cores": thr, "kind": "port",
-                                    "sample": f"first {nw} worlds x {ns} steps from the initial state"}
+                                    "sample": f"worlds 0..{nw - 1} of the workload, {args.steps} steps from "
+                                              f"the initial state ({dt:.1f} s)"}
         print(json.dumps(line), flush=True)
     B.close()
     if dist:
@@ -270,10 +289,13 @@ def run_ours(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=50)
-    ap.add_argument("--warmup", type=int, default=50)
+    ap.add_argument("--steps", type=int, default=500)
+    ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--cpu-worlds", type=int, default=512)
+    ap.add_argument("--ref-worlds", type=int, default=4096)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

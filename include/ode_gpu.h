@@ -1,0 +1,219 @@
+/*
+ * ode_gpu.h -- ODE 0.12's C API for the contact-generation + QuickStep path,
+ * exported by libodegpu with dReal = float (ODE's dSINGLE). A program written
+ * against <ode/ode.h> that uses only these entry points links against
+ * libodegpu instead of libode; the step runs on the GPU through the same
+ * kernels as the batched API (odegpu.h). Each declaration cites the reference
+ * declaration it replaces (include/ode/<file>:<line>).
+ *
+ * Differences from the reference, all deliberate:
+ *  - dWorldQuickStep runs one world per call on the GPU (a launch plus the
+ *    host<->device copies of that world); for many worlds use odegpu.h.
+ *  - dCollide runs the collider on the GPU, one launch per call.
+ *  - Errors never abort the process: dWorldQuickStep returns 0 and
+ *    odegpuGetLastError() says why (ODE aborts on debug asserts).
+ *  - dJointSetFeedback is accepted; feedback is not filled (ODE fills it).
+ *  - Limits per world: 64 bodies, 1024 constraint rows (odegpu.h).
+ */
+#ifndef ODE_GPU_H
+#define ODE_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef float dReal;
+typedef dReal dVector3[4];
+typedef dReal dVector4[4];
+typedef dReal dMatrix3[4 * 3];
+typedef dReal dQuaternion[4];
+
+typedef struct dxWorld* dWorldID;
+typedef struct dxBody* dBodyID;
+typedef struct dxJoint* dJointID;
+typedef struct dxJointGroup* dJointGroupID;
+typedef struct dxGeom* dGeomID;
+typedef struct dxSpace* dSpaceID;
+
+/* include/ode/mass.h:88-92 */
+typedef struct dMass {
+  dReal mass;
+  dVector3 c;
+  dMatrix3 I;
+} dMass;
+
+/* include/ode/contact.h:33-49 */
+enum {
+  dContactMu2 = 0x001, dContactFDir1 = 0x002, dContactBounce = 0x004,
+  dContactSoftERP = 0x008, dContactSoftCFM = 0x010, dContactMotion1 = 0x020,
+  dContactMotion2 = 0x040, dContactMotionN = 0x080, dContactSlip1 = 0x100,
+  dContactSlip2 = 0x200, dContactApprox0 = 0x0000, dContactApprox1_1 = 0x1000,
+  dContactApprox1_2 = 0x2000, dContactApprox1 = 0x3000
+};
+
+/* include/ode/contact.h:52-65 */
+typedef struct dSurfaceParameters {
+  int mode;
+  dReal mu;
+  dReal mu2, bounce, bounce_vel, soft_erp, soft_cfm, motion1, motion2, motionN, slip1, slip2;
+} dSurfaceParameters;
+
+/* include/ode/contact.h:82-88 */
+typedef struct dContactGeom {
+  dVector3 pos;
+  dVector3 normal;
+  dReal depth;
+  dGeomID g1, g2;
+  int side1, side2;
+} dContactGeom;
+
+/* include/ode/contact.h:93-97 */
+typedef struct dContact {
+  dSurfaceParameters surface;
+  dContactGeom geom;
+  dVector3 fdir1;
+} dContact;
+
+/* include/ode/common.h:368-373 */
+typedef struct dJointFeedback {
+  dVector3 f1, t1, f2, t2;
+} dJointFeedback;
+
+/* include/ode/collision.h:881-890 */
+enum { dSphereClass = 0, dBoxClass, dCapsuleClass, dCylinderClass, dPlaneClass,
+       dRayClass, dConvexClass, dGeomTransformClass, dTriMeshClass, dHeightfieldClass };
+
+/* include/ode/common.h:252-258 */
+typedef enum { dJointTypeNone = 0, dJointTypeBall, dJointTypeHinge, dJointTypeSlider,
+               dJointTypeContact, dJointTypeUniversal, dJointTypeHinge2 } dJointType;
+
+/* include/ode/common.h:305-354 */
+enum {
+  dParamLoStop = 0, dParamHiStop, dParamVel, dParamFMax, dParamFudgeFactor, dParamBounce,
+  dParamCFM, dParamStopERP, dParamStopCFM, dParamSuspensionERP, dParamSuspensionCFM,
+  dParamERP,
+  dParamGroup = 0x100,
+  dParamLoStop2 = 0x100, dParamHiStop2, dParamVel2, dParamFMax2, dParamFudgeFactor2,
+  dParamBounce2, dParamCFM2, dParamStopERP2, dParamStopCFM2
+};
+
+/* init: include/ode/odeinit.h:95, :119, :227 */
+void dInitODE(void);
+int dInitODE2(unsigned int uiInitFlags);
+void dCloseODE(void);
+
+/* world: include/ode/objects.h */
+dWorldID dWorldCreate(void);                                        /* :54  */
+void dWorldDestroy(dWorldID w);                                     /* :66  */
+void dWorldSetGravity(dWorldID w, dReal x, dReal y, dReal z);       /* :77  */
+void dWorldGetGravity(dWorldID w, dVector3 gravity);                /* :84  */
+void dWorldSetERP(dWorldID w, dReal erp);                           /* :94  */
+dReal dWorldGetERP(dWorldID w);                                     /* :101 */
+void dWorldSetCFM(dWorldID w, dReal cfm);                           /* :111 */
+dReal dWorldGetCFM(dWorldID w);                                     /* :118 */
+int dWorldQuickStep(dWorldID w, dReal stepsize);                    /* :352 */
+void dWorldSetQuickStepNumIterations(dWorldID w, int num);          /* :385 */
+int dWorldGetQuickStepNumIterations(dWorldID w);                    /* :394 */
+void dWorldSetQuickStepW(dWorldID w, dReal over_relaxation);        /* :401 */
+dReal dWorldGetQuickStepW(dWorldID w);                              /* :408 */
+void dWorldSetContactMaxCorrectingVel(dWorldID w, dReal vel);       /* :420 */
+dReal dWorldGetContactMaxCorrectingVel(dWorldID w);                 /* :427 */
+void dWorldSetContactSurfaceLayer(dWorldID w, dReal depth);         /* :440 */
+dReal dWorldGetContactSurfaceLayer(dWorldID w);                     /* :447 */
+
+/* bodies: include/ode/objects.h */
+dBodyID dBodyCreate(dWorldID w);                                    /* :856 */
+void dBodyDestroy(dBodyID b);                                       /* :866 */
+void dBodySetPosition(dBodyID b, dReal x, dReal y, dReal z);        /* :890 */
+void dBodySetRotation(dBodyID b, const dMatrix3 R);                 /* :900 */
+void dBodySetQuaternion(dBodyID b, const dQuaternion q);            /* :910 */
+void dBodySetLinearVel(dBodyID b, dReal x, dReal y, dReal z);       /* :916 */
+void dBodySetAngularVel(dBodyID b, dReal x, dReal y, dReal z);      /* :922 */
+const dReal* dBodyGetPosition(dBodyID b);                           /* :933 */
+const dReal* dBodyGetRotation(dBodyID b);                           /* :951 */
+const dReal* dBodyGetQuaternion(dBodyID b);                         /* :969 */
+const dReal* dBodyGetLinearVel(dBodyID b);                          /* :986 */
+const dReal* dBodyGetAngularVel(dBodyID b);                         /* :992 */
+void dBodySetMass(dBodyID b, const dMass* mass);                    /* :998 */
+void dBodyGetMass(dBodyID b, dMass* mass);                          /* :1004 */
+void dBodyAddForce(dBodyID b, dReal fx, dReal fy, dReal fz);        /* :1010 */
+void dBodyAddTorque(dBodyID b, dReal fx, dReal fy, dReal fz);       /* :1016 */
+const dReal* dBodyGetForce(dBodyID b);                              /* :1064 */
+const dReal* dBodyGetTorque(dBodyID b);                             /* :1075 */
+void dBodySetGravityMode(dBodyID b, int mode);                      /* :1294 */
+int dBodyGetGravityMode(dBodyID b);                                 /* :1301 */
+void dBodySetGyroscopicMode(dBodyID b, int enabled);                /* :1458 */
+int dBodyGetGyroscopicMode(dBodyID b);                              /* :1444 */
+
+/* joints: include/ode/objects.h */
+dJointID dJointCreateBall(dWorldID w, dJointGroupID g);                  /* :1538 */
+dJointID dJointCreateHinge(dWorldID w, dJointGroupID g);                 /* :1546 */
+dJointID dJointCreateContact(dWorldID w, dJointGroupID g, const dContact* c); /* :1562 */
+dJointID dJointCreateHinge2(dWorldID w, dJointGroupID g);                /* :1570 */
+void dJointDestroy(dJointID j);                                          /* :1647 */
+dJointGroupID dJointGroupCreate(int max_size);                           /* :1655 */
+void dJointGroupDestroy(dJointGroupID g);                                /* :1663 */
+void dJointGroupEmpty(dJointGroupID g);                                  /* :1672 */
+void dJointAttach(dJointID j, dBodyID body1, dBodyID body2);             /* :1693 */
+dJointType dJointGetType(dJointID j);                                    /* :1749 */
+dBodyID dJointGetBody(dJointID j, int index);                            /* :1761 */
+void dJointSetFeedback(dJointID j, dJointFeedback* f);                   /* :1770 */
+dJointFeedback* dJointGetFeedback(dJointID j);                           /* :1776 */
+void dJointSetBallAnchor(dJointID j, dReal x, dReal y, dReal z);         /* :1785 */
+void dJointSetBallParam(dJointID j, int parameter, dReal value);         /* :1797 */
+void dJointGetBallAnchor(dJointID j, dVector3 result);                   /* :2351 */
+void dJointSetHingeAnchor(dJointID j, dReal x, dReal y, dReal z);        /* :1803 */
+void dJointSetHingeAxis(dJointID j, dReal x, dReal y, dReal z);          /* :1811 */
+void dJointSetHingeParam(dJointID j, int parameter, dReal value);        /* :1847 */
+dReal dJointGetHingeAngle(dJointID j);                                   /* :2414 */
+dReal dJointGetHingeAngleRate(dJointID j);                               /* :2420 */
+void dJointAddHingeTorque(dJointID j, dReal torque);                     /* :1857 */
+void dJointSetHinge2Anchor(dJointID j, dReal x, dReal y, dReal z);       /* :1890 */
+void dJointSetHinge2Axis1(dJointID j, dReal x, dReal y, dReal z);        /* :1896 */
+void dJointSetHinge2Axis2(dJointID j, dReal x, dReal y, dReal z);        /* :1902 */
+void dJointSetHinge2Param(dJointID j, int parameter, dReal value);       /* :1908 */
+void dJointAddHinge2Torques(dJointID j, dReal torque1, dReal torque2);   /* :1916 */
+dReal dJointGetHinge2Angle1(dJointID j);                                 /* :2493 */
+int dAreConnectedExcluding(dBodyID b1, dBodyID b2, int joint_type);      /* :2968 */
+
+/* mass: include/ode/mass.h */
+void dMassSetZero(dMass* m);                                             /* :45 */
+void dMassSetParameters(dMass* m, dReal themass, dReal cgx, dReal cgy, dReal cgz,
+                        dReal I11, dReal I22, dReal I33, dReal I12, dReal I13,
+                        dReal I23);                                      /* :47 */
+void dMassSetSphere(dMass* m, dReal density, dReal radius);              /* :52 */
+void dMassSetSphereTotal(dMass* m, dReal total_mass, dReal radius);      /* :53 */
+void dMassSetBox(dMass* m, dReal density, dReal lx, dReal ly, dReal lz); /* :65 */
+void dMassSetBoxTotal(dMass* m, dReal total_mass, dReal lx, dReal ly, dReal lz); /* :67 */
+
+/* RNG: include/ode/misc.h */
+int dTestRand(void);                                                     /* :37 */
+unsigned long dRand(void);                                               /* :42 */
+unsigned long dRandGetSeed(void);                                        /* :45 */
+void dRandSetSeed(unsigned long s);                                      /* :46 */
+int dRandInt(int n);                                                     /* :51 */
+
+/* collision: include/ode/collision.h (space argument must be 0: spaces are
+ * not on this path, pairs come from the caller) */
+int dCollide(dGeomID o1, dGeomID o2, int flags, dContactGeom* contact, int skip); /* :795 */
+dGeomID dCreateSphere(dSpaceID space, dReal radius);                     /* :924 */
+dGeomID dCreateBox(dSpaceID space, dReal lx, dReal ly, dReal lz);        /* :1002 */
+dGeomID dCreatePlane(dSpaceID space, dReal a, dReal b, dReal c, dReal d); /* :1046 */
+dGeomID dCreateCapsule(dSpaceID space, dReal radius, dReal length);      /* :1051 */
+void dGeomDestroy(dGeomID g);                                            /* :68  */
+void dGeomSetBody(dGeomID g, dBodyID body);                              /* :108 */
+dBodyID dGeomGetBody(dGeomID g);                                         /* :117 */
+void dGeomSetPosition(dGeomID g, dReal x, dReal y, dReal z);             /* :134 */
+void dGeomSetRotation(dGeomID g, const dMatrix3 R);                      /* :149 */
+const dReal* dGeomGetPosition(dGeomID g);                                /* :184 */
+const dReal* dGeomGetRotation(dGeomID g);                                /* :213 */
+int dGeomGetClass(dGeomID g);                                            /* :310 */
+dReal dGeomSphereGetRadius(dGeomID g);                                   /* :947 */
+void dGeomBoxGetLengths(dGeomID g, dVector3 result);                     /* :1028 */
+void dGeomPlaneGetParams(dGeomID g, dVector4 result);                    /* :1048 */
+void dGeomCapsuleGetParams(dGeomID g, dReal* radius, dReal* length);     /* :1053 */
+
+#ifdef __cplusplus
+}
+#endif
+#endif

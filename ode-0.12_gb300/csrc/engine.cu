@@ -446,7 +446,7 @@ int odegpuBatchStep(odegpuBatchID b, int n_steps) {
   if (!b || n_steps < 0) return fail(ODEGPU_E_ARG, "bad arguments");
   if (n_steps == 0) return 0;
   OG_CUDA(cudaSetDevice(b->device));
-  StepOptions opt{1, nullptr, nullptr, nullptr};
+  StepOptions opt{1, nullptr, nullptr, nullptr, 0, 0};
   if (int rc = b->launch(0, b->n_worlds, n_steps, opt)) return rc;
   b->step_counter += n_steps;
   return 0;
@@ -455,7 +455,7 @@ int odegpuBatchStep(odegpuBatchID b, int n_steps) {
 int odegpuBatchStepPlain(odegpuBatchID b, int n_steps) {
   if (!b || n_steps < 0) return fail(ODEGPU_E_ARG, "bad arguments");
   OG_CUDA(cudaSetDevice(b->device));
-  StepOptions opt{1, nullptr, nullptr, nullptr};
+  StepOptions opt{1, nullptr, nullptr, nullptr, 0, 0};
   const int saved = b->warps_per_block;
   b->warps_per_block = 1;
   for (int w = 0; w < b->n_worlds; ++w) {
@@ -475,7 +475,7 @@ int odegpuBatchStepPlain(odegpuBatchID b, int n_steps) {
 int odegpuBatchStepGraph(odegpuBatchID b, int n_steps) {
   if (!b || n_steps < 0) return fail(ODEGPU_E_ARG, "bad arguments");
   OG_CUDA(cudaSetDevice(b->device));
-  StepOptions opt{1, nullptr, nullptr, nullptr};
+  StepOptions opt{1, nullptr, nullptr, nullptr, 0, 0};
   cudaGraph_t graph;
   OG_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
   for (int s = 0; s < n_steps; ++s) {
@@ -604,7 +604,7 @@ int odegpuBatchStepTap(odegpuBatchID b, float* rows, float* lambda, float* fc, i
   if (int rc = dlam.alloc(b->row_cap_total)) return rc;
   if (int rc = dfc.alloc((size_t)b->nb_total * 6)) return rc;
   OG_CUDA(cudaMemsetAsync(dfc.p, 0, (size_t)b->nb_total * 6 * sizeof(float), b->stream));
-  StepOptions opt{1, drows.p, dlam.p, dfc.p};
+  StepOptions opt{1, drows.p, dlam.p, dfc.p, 0, 0};
   if (int rc = b->launch(0, b->n_worlds, 1, opt)) return rc;
   b->step_counter += 1;
   if (rows)
@@ -648,3 +648,149 @@ int odegpuBatchGetContacts(odegpuBatchID b, int w, float* out, int cap) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Single-world context for the ODE-compatible API (ode_api.cpp).
+
+#include "engine_internal.hpp"
+
+namespace {
+
+__global__ void collide_pair_kernel(GeomView a, GeomView b, unsigned flags, Contact* out, int* n) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    Contact c[8];
+    const int k = collide_primitive(a, b, flags, c);
+    for (int i = 0; i < k; ++i) out[i] = c[i];
+    *n = k;
+  }
+}
+
+template <class T>
+int grow(DBuf<T>& b, size_t n) {
+  if (b.p && b.n >= n) return 0;
+  if (b.p) { cudaFree(b.p); b.p = nullptr; }
+  return b.alloc(std::max<size_t>(n, 16));
+}
+template <class T>
+int put(DBuf<T>& b, const std::vector<T>& v, cudaStream_t s, size_t min_cap = 0) {
+  if (int rc = grow(b, std::max(v.size(), min_cap))) return rc;
+  if (!v.empty() && cudaMemcpyAsync(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s) != cudaSuccess)
+    return fail(ODEGPU_E_CUDA, "upload failed");
+  return 0;
+}
+
+}  // namespace
+
+namespace og {
+
+struct WorldCtx {
+  odegpuBatch B;
+};
+
+WorldCtx* ctx_create(int device) {
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= device) {
+    cudaGetLastError();
+    fail(ODEGPU_E_CUDA, "no CUDA device available");
+    return nullptr;
+  }
+  if (cudaSetDevice(device) != cudaSuccess) return nullptr;
+  auto* c = new WorldCtx();
+  c->B.device = device;
+  c->B.n_worlds = 1;
+  c->B.warps_per_block = 1;
+  if (cudaStreamCreateWithFlags(&c->B.stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete c;
+    fail(ODEGPU_E_CUDA, "stream creation failed");
+    return nullptr;
+  }
+  cudaFuncSetAttribute(world_step_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemPerWarp * 4);
+  return c;
+}
+
+void ctx_destroy(WorldCtx* c) {
+  if (!c) return;
+  cudaSetDevice(c->B.device);
+  cudaStreamSynchronize(c->B.stream);
+  cudaStreamDestroy(c->B.stream);
+  c->B.stream = nullptr;
+  delete c;
+}
+
+int ctx_step(WorldCtx* c, HostWorld& hw) {
+  odegpuBatch& B = c->B;
+  OG_CUDA(cudaSetDevice(B.device));
+  cudaStream_t s = B.stream;
+  const int nb = hw.desc.nb;
+  if (nb > kMaxB) return fail(ODEGPU_E_LIMIT, "world has more than 64 bodies");
+  B.nb_total = nb;
+  B.nj_total = hw.desc.njp;
+  WorldDesc D = hw.desc;
+  D.body_off = D.geom_off = D.joint_off = D.contact_off = D.row_off = D.padj_off = 0;
+  D.ng = 0;
+  const size_t jl = (size_t)D.njp + D.contact_cap;
+  std::vector<WorldDesc> wd(1, D);
+  int rc = 0;
+  rc = rc ? rc : put(B.world, wd, s);
+  rc = rc ? rc : put(B.seed, std::vector<unsigned>(1, hw.seed), s);
+  rc = rc ? rc : put(B.status, std::vector<int>(1, 0), s);
+  rc = rc ? rc : put(B.ncontacts, std::vector<int>(1, (int)hw.contacts.size()), s);
+  rc = rc ? rc : grow(B.nrows, 1);
+  rc = rc ? rc : grow(B.nislands, 1);
+  rc = rc ? rc : put(B.pos, hw.pos, s);
+  rc = rc ? rc : put(B.q, hw.q, s);
+  rc = rc ? rc : put(B.lvel, hw.lvel, s);
+  rc = rc ? rc : put(B.avel, hw.avel, s);
+  rc = rc ? rc : put(B.facc, hw.facc, s);
+  rc = rc ? rc : put(B.tacc, hw.tacc, s);
+  rc = rc ? rc : put(B.mass, hw.mass, s);
+  rc = rc ? rc : put(B.invMass, hw.invMass, s);
+  rc = rc ? rc : put(B.I, hw.I, s);
+  rc = rc ? rc : put(B.invI, hw.invI, s);
+  rc = rc ? rc : grow(B.invIw, 12 * (size_t)nb);
+  rc = rc ? rc : put(B.bflags, hw.flags, s);
+  rc = rc ? rc : put(B.joints, hw.joints, s);
+  rc = rc ? rc : put(B.contacts, hw.contacts, s, (size_t)D.contact_cap);
+  rc = rc ? rc : put(B.surfaces, hw.surfaces, s);
+  rc = rc ? rc : put(B.padj_start, hw.padj_start, s);
+  rc = rc ? rc : put(B.padj, hw.padj, s);
+  rc = rc ? rc : grow(B.rows, (size_t)D.row_cap * kRowWords);
+  rc = rc ? rc : grow(B.jlist, jl);
+  rc = rc ? rc : grow(B.jrow, jl);
+  rc = rc ? rc : grow(B.jm, jl);
+  rc = rc ? rc : grow(B.adj, 2 * jl);
+  rc = rc ? rc : grow(B.adj_start, (size_t)nb + 1);
+  rc = rc ? rc : grow(B.island_jstart, (size_t)nb + 1);
+  rc = rc ? rc : grow(B.island_rstart, (size_t)nb + 1);
+  if (rc) return rc;
+  B.n_ctrl_steps = 0;
+  StepOptions opt{0, nullptr, nullptr, nullptr, 1, 1};
+  if (int e = B.launch(0, 1, 1, opt)) return e;
+  std::vector<int> st(1);
+  OG_CUDA(cudaMemcpyAsync(hw.pos.data(), B.pos.p, nb * sizeof(float4), cudaMemcpyDeviceToHost, s));
+  OG_CUDA(cudaMemcpyAsync(hw.q.data(), B.q.p, nb * sizeof(float4), cudaMemcpyDeviceToHost, s));
+  OG_CUDA(cudaMemcpyAsync(hw.lvel.data(), B.lvel.p, nb * sizeof(float4), cudaMemcpyDeviceToHost, s));
+  OG_CUDA(cudaMemcpyAsync(hw.avel.data(), B.avel.p, nb * sizeof(float4), cudaMemcpyDeviceToHost, s));
+  OG_CUDA(cudaMemcpyAsync(&hw.seed, B.seed.p, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+  OG_CUDA(cudaMemcpyAsync(st.data(), B.status.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  OG_CUDA(cudaStreamSynchronize(s));
+  hw.status = st[0];
+  return 0;
+}
+
+int collide_pair_gpu(const GeomView& a, const GeomView& b, unsigned flags, Contact* out) {
+  Contact* d_c = nullptr;
+  int* d_n = nullptr;
+  OG_CUDA(cudaMalloc(&d_c, 8 * sizeof(Contact) + sizeof(int)));
+  d_n = reinterpret_cast<int*>(d_c + 8);
+  collide_pair_kernel<<<1, 32>>>(a, b, flags, d_c, d_n);
+  int n = 0;
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpy(&n, d_n, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && n > 0) e = cudaMemcpy(out, d_c, n * sizeof(Contact), cudaMemcpyDeviceToHost);
+  cudaFree(d_c);
+  if (e != cudaSuccess) return fail(ODEGPU_E_CUDA, cudaGetErrorString(e));
+  return n;
+}
+
+}  // namespace og

@@ -1,0 +1,34 @@
+// engine_internal.hpp -- internal interface between the ODE-compatible API
+// layer (ode_api.cpp) and the device engine (engine.cu).
+#pragma once
+#include <vector>
+#include "engine_types.cuh"
+#include "collide.cuh"
+
+namespace og {
+
+// One world as the ODE API layer hands it to the device, in ODE's creation
+// order, with complete per-body joint lists (newest attachment first).
+struct HostWorld {
+  WorldDesc desc;                     // offsets 0; nb, njp, contact_cap, row_cap set
+  std::vector<float4> pos, q, lvel, avel, facc, tacc;
+  std::vector<float> mass, invMass, I, invI;
+  std::vector<int> flags;
+  std::vector<DevJoint> joints;       // persistent joints with bodies attached
+  std::vector<DevContact> contacts;   // contact joints, creation order
+  std::vector<DevSurface> surfaces;   // one per contact
+  std::vector<int> padj_start, padj;  // full body lists (ordinals: joint, njp + contact)
+  unsigned seed = 0;
+  int status = 0;
+};
+
+struct WorldCtx;
+WorldCtx* ctx_create(int device);
+void ctx_destroy(WorldCtx* c);
+// Uploads hw, runs one world step on the GPU, writes the new body state (pos,
+// q, lvel, avel) and the RNG state back into hw. Returns 0 or an ODEGPU_E code.
+int ctx_step(WorldCtx* c, HostWorld& hw);
+// One dCollide on the GPU. Returns the contact count (<= 8) or a negative code.
+int collide_pair_gpu(const GeomView& a, const GeomView& b, unsigned flags, Contact* out);
+
+}  // namespace og

@@ -1,0 +1,752 @@
+// ode_api.cpp -- ODE 0.12's C API (include/ode_gpu.h) over the CUDA path.
+//
+// Object model: worlds own bodies and persistent joints in creation order;
+// joint groups own contact joints; every attachment gets a sequence number so
+// that each body's joint list can be produced in ODE's order (dJointAttach
+// prepends, ode/src/ode.cpp:1379-1392). dWorldQuickStep packs the world and
+// runs one step of the device kernel (engine_internal.hpp); no step math runs
+// on the host. Setter arithmetic (anchors, axes, inertia inverse) is host FP64
+// as in host_setup.hpp.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "ode_gpu.h"
+#include "odegpu.h"
+#include "engine_internal.hpp"
+#include "host_setup.hpp"
+
+using og::DevContact;
+using og::DevJoint;
+using og::DevSurface;
+
+struct dxJoint;
+struct dxGeom;
+
+struct dxBody {
+  dxWorld* world;
+  dReal pos[4], q[4], R[12], lvel[4], avel[4], facc[4], tacc[4];
+  dMass mass;
+  double invI[9];
+  double invMass;
+  int flags;   // ODEGPU_BODY_*
+};
+
+struct dxJoint {
+  dxWorld* world;
+  dxJointGroup* group;
+  int type;
+  dxBody* body[2];
+  int reverse;
+  long long seq;             // attachment sequence number (ODE list order)
+  dJointFeedback* feedback;
+  // ball / hinge / hinge2 data, FP64 as the setters compute it
+  og_host::HJoint h;
+  double erp, cfm;
+  og::DevLimot lm1, lm2;
+  double susp_erp, susp_cfm;
+  // contact
+  dContact contact;
+};
+
+struct dxJointGroup {
+  std::vector<dxJoint*> joints;
+};
+
+struct dxGeom {
+  int type;
+  dxBody* body;
+  double p[4];               // class parameters (plane normalised)
+  dReal pos[4], R[12];       // own placement when not attached to a body
+};
+
+struct dxWorld {
+  double gravity[3] = {0, 0, 0};
+  double erp = 0.2, cfm = 1e-5;   // dWorldCreate defaults for dSINGLE (ode/src/ode.cpp:1550-1556)
+  int iterations = 20;
+  double sor_w = 1.3;
+  double max_vel = INFINITY, min_depth = 0;
+  std::vector<dxBody*> bodies;     // creation order
+  std::vector<dxJoint*> joints;    // every live joint, creation order
+  long long seq = 0;
+  og::WorldCtx* ctx = nullptr;
+  og::HostWorld hw;
+};
+
+namespace {
+
+unsigned long g_seed = 0;   // ODE's global dRand state (ode/src/misc.cpp:31)
+thread_local std::string g_err;
+
+void body_sync_R(dxBody* b) {
+  double q[4] = {b->q[0], b->q[1], b->q[2], b->q[3]}, R[12];
+  og_host::r_from_q(R, q);
+  for (int k = 0; k < 12; ++k) b->R[k] = (dReal)R[k];
+}
+
+og_host::HBody hbody(const dxBody* b) {
+  og_host::HBody H;
+  for (int k = 0; k < 3; ++k) H.pos[k] = b->pos[k];
+  for (int k = 0; k < 4; ++k) H.q[k] = b->q[k];
+  for (int k = 0; k < 12; ++k) H.R[k] = b->R[k];
+  return H;
+}
+
+// The joint's two bodies as the setter helpers expect them (indices 0/1).
+struct JB {
+  og_host::HBody B[2];
+  JB(const dxJoint* j) {
+    for (int i = 0; i < 2; ++i)
+      if (j->body[i]) B[i] = hbody(j->body[i]);
+  }
+};
+void local_indices(dxJoint* j) {
+  j->h.b1 = j->body[0] ? 0 : -1;
+  j->h.b2 = j->body[1] ? 1 : -1;
+}
+
+void limot_default(og::DevLimot& L, const dxWorld* w) {
+  // dxJointLimitMotor::init (ode/src/joints/joint.cpp:456-469)
+  L.vel = 0; L.fmax = 0; L.lostop = -INFINITY; L.histop = INFINITY; L.fudge = 1;
+  L.normal_cfm = (float)w->cfm; L.stop_erp = (float)w->erp; L.stop_cfm = (float)w->cfm; L.bounce = 0;
+}
+void limot_set(og::DevLimot& L, int num, dReal v) {
+  // dxJointLimitMotor::set (ode/src/joints/joint.cpp:472-508)
+  switch (num) {
+    case dParamLoStop: L.lostop = v; break;
+    case dParamHiStop: L.histop = v; break;
+    case dParamVel: L.vel = v; break;
+    case dParamFMax: if (v >= 0) L.fmax = v; break;
+    case dParamFudgeFactor: if (v >= 0 && v <= 1) L.fudge = v; break;
+    case dParamBounce: L.bounce = v; break;
+    case dParamCFM: L.normal_cfm = v; break;
+    case dParamStopERP: L.stop_erp = v; break;
+    case dParamStopCFM: L.stop_cfm = v; break;
+    default: break;
+  }
+}
+
+dxJoint* new_joint(dxWorld* w, dxJointGroup* g, int type) {
+  auto* j = new dxJoint();
+  std::memset(&j->h, 0, sizeof(j->h));
+  j->world = w;
+  j->group = g;
+  j->type = type;
+  j->body[0] = j->body[1] = nullptr;
+  j->h.b1 = j->h.b2 = -1;
+  j->reverse = 0;
+  j->seq = -1;
+  j->feedback = nullptr;
+  j->h.axis1[0] = 1;
+  if (type == dJointTypeHinge2) { j->h.axis2[1] = 1; j->h.v1[0] = 1; j->h.v2[1] = 1; }
+  else j->h.axis2[0] = 1;
+  j->erp = w->erp;
+  j->cfm = w->cfm;
+  limot_default(j->lm1, w);
+  limot_default(j->lm2, w);
+  j->susp_erp = w->erp;
+  j->susp_cfm = w->cfm;
+  w->joints.push_back(j);
+  if (g) g->joints.push_back(j);
+  return j;
+}
+
+void remove_joint(dxJoint* j) {
+  auto& v = j->world->joints;
+  v.erase(std::remove(v.begin(), v.end(), j), v.end());
+}
+
+// World anchor of a joint (getAnchor, ode/src/joints/joint.cpp:326-337).
+void world_anchor1(const dxJoint* j, double* out) {
+  const dxBody* b = j->body[0];
+  double R[12], a[3];
+  for (int k = 0; k < 12; ++k) R[k] = b->R[k];
+  og_host::mul0_331(a, R, j->h.anchor1);
+  for (int k = 0; k < 3; ++k) out[k] = a[k] + b->pos[k];
+}
+
+}  // namespace
+
+extern "C" {
+
+void dInitODE(void) {}
+int dInitODE2(unsigned int) { return 1; }
+void dCloseODE(void) {}
+
+// ---------------------------------------------------------------- world
+dWorldID dWorldCreate(void) { return new dxWorld(); }
+void dWorldDestroy(dWorldID w) {
+  if (!w) return;
+  for (dxJoint* j : w->joints) j->world = nullptr;
+  for (dxJoint* j : std::vector<dxJoint*>(w->joints))
+    if (!j->group) delete j;
+  for (dxBody* b : w->bodies) delete b;
+  og::ctx_destroy(w->ctx);
+  delete w;
+}
+void dWorldSetGravity(dWorldID w, dReal x, dReal y, dReal z) { w->gravity[0] = x; w->gravity[1] = y; w->gravity[2] = z; }
+void dWorldGetGravity(dWorldID w, dVector3 g) { g[0] = (dReal)w->gravity[0]; g[1] = (dReal)w->gravity[1]; g[2] = (dReal)w->gravity[2]; }
+void dWorldSetERP(dWorldID w, dReal erp) { w->erp = erp; }
+dReal dWorldGetERP(dWorldID w) { return (dReal)w->erp; }
+void dWorldSetCFM(dWorldID w, dReal cfm) { w->cfm = cfm; }
+dReal dWorldGetCFM(dWorldID w) { return (dReal)w->cfm; }
+void dWorldSetQuickStepNumIterations(dWorldID w, int num) { w->iterations = num; }
+int dWorldGetQuickStepNumIterations(dWorldID w) { return w->iterations; }
+void dWorldSetQuickStepW(dWorldID w, dReal v) { w->sor_w = v; }
+dReal dWorldGetQuickStepW(dWorldID w) { return (dReal)w->sor_w; }
+void dWorldSetContactMaxCorrectingVel(dWorldID w, dReal v) { w->max_vel = v; }
+dReal dWorldGetContactMaxCorrectingVel(dWorldID w) { return (dReal)w->max_vel; }
+void dWorldSetContactSurfaceLayer(dWorldID w, dReal d) { w->min_depth = d; }
+dReal dWorldGetContactSurfaceLayer(dWorldID w) { return (dReal)w->min_depth; }
+
+// ---------------------------------------------------------------- bodies
+dBodyID dBodyCreate(dWorldID w) {
+  // dBodyCreate defaults (ode/src/ode.cpp:248-294): unit mass and inertia,
+  // identity orientation, gyroscopic flag on
+  auto* b = new dxBody();
+  std::memset(b, 0, sizeof(*b));
+  b->world = w;
+  b->q[0] = 1;
+  body_sync_R(b);
+  dMassSetParameters(&b->mass, 1, 0, 0, 0, 1, 1, 1, 0, 0, 0);
+  for (int k = 0; k < 9; ++k) b->invI[k] = (k % 4 == 0) ? 1.0 : 0.0;
+  b->invMass = 1;
+  b->flags = ODEGPU_BODY_GYROSCOPIC;
+  w->bodies.push_back(b);
+  return b;
+}
+void dBodyDestroy(dBodyID b) {
+  if (!b) return;
+  dxWorld* w = b->world;
+  for (dxJoint* j : w->joints) {
+    for (int i = 0; i < 2; ++i)
+      if (j->body[i] == b) j->body[i] = nullptr;
+    if (!j->body[0] && j->body[1]) { j->body[0] = j->body[1]; j->body[1] = nullptr; j->reverse = 1; }
+  }
+  w->bodies.erase(std::remove(w->bodies.begin(), w->bodies.end(), b), w->bodies.end());
+  delete b;
+}
+void dBodySetPosition(dBodyID b, dReal x, dReal y, dReal z) { b->pos[0] = x; b->pos[1] = y; b->pos[2] = z; }
+void dBodySetQuaternion(dBodyID b, const dQuaternion q) {
+  double qd[4] = {q[0], q[1], q[2], q[3]};
+  og_host::normalize4(qd);
+  for (int k = 0; k < 4; ++k) b->q[k] = (dReal)qd[k];
+  body_sync_R(b);
+}
+void dBodySetRotation(dBodyID b, const dMatrix3 R) {
+  // dQfromR (ode/src/rotation.cpp:258-307), then normalise as dBodySetRotation does
+  double r[12], q[4];
+  for (int k = 0; k < 12; ++k) r[k] = R[k];
+  auto Rr = [&](int i, int j) { return r[i * 4 + j]; };
+  double tr = Rr(0, 0) + Rr(1, 1) + Rr(2, 2);
+  if (tr >= 0) {
+    double s = std::sqrt(tr + 1);
+    q[0] = 0.5 * s; s = 0.5 / s;
+    q[1] = (Rr(2, 1) - Rr(1, 2)) * s; q[2] = (Rr(0, 2) - Rr(2, 0)) * s; q[3] = (Rr(1, 0) - Rr(0, 1)) * s;
+  } else {
+    int c = (Rr(1, 1) > Rr(0, 0)) ? ((Rr(2, 2) > Rr(1, 1)) ? 2 : 1) : ((Rr(2, 2) > Rr(0, 0)) ? 2 : 0);
+    if (c == 0) {
+      double s = std::sqrt((Rr(0, 0) - (Rr(1, 1) + Rr(2, 2))) + 1);
+      q[1] = 0.5 * s; s = 0.5 / s;
+      q[2] = (Rr(0, 1) + Rr(1, 0)) * s; q[3] = (Rr(2, 0) + Rr(0, 2)) * s; q[0] = (Rr(2, 1) - Rr(1, 2)) * s;
+    } else if (c == 1) {
+      double s = std::sqrt((Rr(1, 1) - (Rr(2, 2) + Rr(0, 0))) + 1);
+      q[2] = 0.5 * s; s = 0.5 / s;
+      q[3] = (Rr(1, 2) + Rr(2, 1)) * s; q[1] = (Rr(0, 1) + Rr(1, 0)) * s; q[0] = (Rr(0, 2) - Rr(2, 0)) * s;
+    } else {
+      double s = std::sqrt((Rr(2, 2) - (Rr(0, 0) + Rr(1, 1))) + 1);
+      q[3] = 0.5 * s; s = 0.5 / s;
+      q[1] = (Rr(2, 0) + Rr(0, 2)) * s; q[2] = (Rr(1, 2) + Rr(2, 1)) * s; q[0] = (Rr(1, 0) - Rr(0, 1)) * s;
+    }
+  }
+  og_host::normalize4(q);
+  for (int k = 0; k < 4; ++k) b->q[k] = (dReal)q[k];
+  body_sync_R(b);
+}
+void dBodySetLinearVel(dBodyID b, dReal x, dReal y, dReal z) { b->lvel[0] = x; b->lvel[1] = y; b->lvel[2] = z; }
+void dBodySetAngularVel(dBodyID b, dReal x, dReal y, dReal z) { b->avel[0] = x; b->avel[1] = y; b->avel[2] = z; }
+const dReal* dBodyGetPosition(dBodyID b) { return b->pos; }
+const dReal* dBodyGetRotation(dBodyID b) { return b->R; }
+const dReal* dBodyGetQuaternion(dBodyID b) { return b->q; }
+const dReal* dBodyGetLinearVel(dBodyID b) { return b->lvel; }
+const dReal* dBodyGetAngularVel(dBodyID b) { return b->avel; }
+void dBodySetMass(dBodyID b, const dMass* m) {
+  // dBodySetMass (ode/src/ode.cpp:492-509): invI through a Cholesky inverse
+  b->mass = *m;
+  double I[9], inv[9];
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 3; ++c) I[r * 3 + c] = m->I[r * 4 + c];
+  if (!og_host::invert_pd3(I, inv))
+    for (int k = 0; k < 9; ++k) inv[k] = (k % 4 == 0) ? 1.0 : 0.0;
+  for (int k = 0; k < 9; ++k) b->invI[k] = inv[k];
+  b->invMass = 1.0 / m->mass;
+}
+void dBodyGetMass(dBodyID b, dMass* m) { *m = b->mass; }
+void dBodyAddForce(dBodyID b, dReal x, dReal y, dReal z) { b->facc[0] += x; b->facc[1] += y; b->facc[2] += z; }
+void dBodyAddTorque(dBodyID b, dReal x, dReal y, dReal z) { b->tacc[0] += x; b->tacc[1] += y; b->tacc[2] += z; }
+const dReal* dBodyGetForce(dBodyID b) { return b->facc; }
+const dReal* dBodyGetTorque(dBodyID b) { return b->tacc; }
+void dBodySetGravityMode(dBodyID b, int mode) {
+  if (mode) b->flags &= ~ODEGPU_BODY_NO_GRAVITY; else b->flags |= ODEGPU_BODY_NO_GRAVITY;
+}
+int dBodyGetGravityMode(dBodyID b) { return (b->flags & ODEGPU_BODY_NO_GRAVITY) == 0; }
+void dBodySetGyroscopicMode(dBodyID b, int e) {
+  if (e) b->flags |= ODEGPU_BODY_GYROSCOPIC; else b->flags &= ~ODEGPU_BODY_GYROSCOPIC;
+}
+int dBodyGetGyroscopicMode(dBodyID b) { return (b->flags & ODEGPU_BODY_GYROSCOPIC) != 0; }
+
+// ---------------------------------------------------------------- mass
+void dMassSetZero(dMass* m) { std::memset(m, 0, sizeof(*m)); }
+void dMassSetParameters(dMass* m, dReal themass, dReal cgx, dReal cgy, dReal cgz, dReal I11, dReal I22,
+                        dReal I33, dReal I12, dReal I13, dReal I23) {
+  // ode/src/mass.cpp:94-117
+  dMassSetZero(m);
+  m->mass = themass;
+  m->c[0] = cgx; m->c[1] = cgy; m->c[2] = cgz;
+  m->I[0] = I11; m->I[5] = I22; m->I[10] = I33;
+  m->I[1] = I12; m->I[2] = I13; m->I[6] = I23;
+  m->I[4] = I12; m->I[8] = I13; m->I[9] = I23;
+}
+void dMassSetSphereTotal(dMass* m, dReal total, dReal r) {
+  const dReal ii = 0.4f * total * r * r;  // ode/src/mass.cpp:126-137
+  dMassSetParameters(m, total, 0, 0, 0, ii, ii, ii, 0, 0, 0);
+}
+void dMassSetSphere(dMass* m, dReal density, dReal r) {
+  dMassSetSphereTotal(m, (dReal)((4.0 / 3.0) * M_PI * r * r * r * density), r);
+}
+void dMassSetBoxTotal(dMass* m, dReal total, dReal lx, dReal ly, dReal lz) {
+  // ode/src/mass.cpp:208-222
+  dMassSetParameters(m, total, 0, 0, 0, total / 12.0f * (ly * ly + lz * lz), total / 12.0f * (lx * lx + lz * lz),
+                     total / 12.0f * (lx * lx + ly * ly), 0, 0, 0);
+}
+void dMassSetBox(dMass* m, dReal density, dReal lx, dReal ly, dReal lz) {
+  dMassSetBoxTotal(m, lx * ly * lz * density, lx, ly, lz);
+}
+
+// ---------------------------------------------------------------- joints
+dJointID dJointCreateBall(dWorldID w, dJointGroupID g) { return new_joint(w, g, dJointTypeBall); }
+dJointID dJointCreateHinge(dWorldID w, dJointGroupID g) { return new_joint(w, g, dJointTypeHinge); }
+dJointID dJointCreateHinge2(dWorldID w, dJointGroupID g) { return new_joint(w, g, dJointTypeHinge2); }
+dJointID dJointCreateContact(dWorldID w, dJointGroupID g, const dContact* c) {
+  dxJoint* j = new_joint(w, g, dJointTypeContact);
+  j->contact = *c;   // dJointCreateContact copies the contact (ode/src/ode.cpp:1201-1208)
+  return j;
+}
+void dJointDestroy(dJointID j) {
+  if (!j || j->group) return;   // group joints go with their group (ode/src/ode.cpp:1248)
+  if (j->world) remove_joint(j);
+  delete j;
+}
+dJointGroupID dJointGroupCreate(int) { return new dxJointGroup(); }
+void dJointGroupEmpty(dJointGroupID g) {
+  if (!g) return;
+  for (dxJoint* j : g->joints) {
+    if (j->world) remove_joint(j);
+    delete j;
+  }
+  g->joints.clear();
+}
+void dJointGroupDestroy(dJointGroupID g) {
+  dJointGroupEmpty(g);
+  delete g;
+}
+void dJointAttach(dJointID j, dBodyID b1, dBodyID b2) {
+  // ode/src/ode.cpp:1348-1399: a missing body1 moves to body2's slot
+  if (!b1) { b1 = b2; b2 = nullptr; j->reverse = 1; } else j->reverse = 0;
+  j->body[0] = b1;
+  j->body[1] = b2;
+  j->seq = j->world->seq++;
+  local_indices(j);
+  if (!b1) return;
+  // setRelativeValues (ball.cpp:175-180, hinge.cpp:364-373, hinge2.cpp:425-448)
+  JB jb(j);
+  og_host::HJoint& H = j->h;
+  if (j->type == dJointTypeBall || j->type == dJointTypeHinge) {
+    double a[3];
+    if (j->reverse) { for (int k = 0; k < 3; ++k) a[k] = H.anchor2[k]; }
+    else world_anchor1(j, a);
+    og_host::set_anchors(H, jb.B, a[0], a[1], a[2], H.anchor1, H.anchor2);
+    if (j->type == dJointTypeHinge) {
+      double ax[3];
+      og_host::mul0_331(ax, jb.B[0].R, H.axis1);
+      og_host::set_axes(H, jb.B, ax[0], ax[1], ax[2], H.axis1, H.axis2);
+      og_host::hinge_qrel(H, jb.B);
+    }
+  } else if (j->type == dJointTypeHinge2 && b2) {
+    double a[3], ax[3];
+    world_anchor1(j, a);
+    og_host::set_anchors(H, jb.B, a[0], a[1], a[2], H.anchor1, H.anchor2);
+    og_host::mul0_331(ax, jb.B[0].R, H.axis1);
+    og_host::set_axes(H, jb.B, ax[0], ax[1], ax[2], H.axis1, nullptr);
+    og_host::mul0_331(ax, jb.B[1].R, H.axis2);
+    og_host::set_axes(H, jb.B, ax[0], ax[1], ax[2], nullptr, H.axis2);
+    og_host::hinge2_axis_info(H, jb.B);
+    og_host::hinge2_make_v(H, jb.B);
+  }
+}
+dJointType dJointGetType(dJointID j) { return (dJointType)j->type; }
+dBodyID dJointGetBody(dJointID j, int index) {
+  // ode/src/ode.cpp:1415-1436 (reverse flag swaps the reported order)
+  if (index == 0 || index == 1) {
+    if (j->reverse) return j->body[1 - index];
+    return j->body[index];
+  }
+  return nullptr;
+}
+void dJointSetFeedback(dJointID j, dJointFeedback* f) { j->feedback = f; }
+dJointFeedback* dJointGetFeedback(dJointID j) { return j->feedback; }
+
+void dJointSetBallAnchor(dJointID j, dReal x, dReal y, dReal z) {
+  JB jb(j);
+  og_host::set_anchors(j->h, jb.B, x, y, z, j->h.anchor1, j->h.anchor2);
+}
+void dJointSetBallParam(dJointID j, int p, dReal v) {
+  if (p == dParamCFM) j->cfm = v; else if (p == dParamERP) j->erp = v;
+}
+void dJointGetBallAnchor(dJointID j, dVector3 r) {
+  double a[3];
+  if (j->body[0]) { world_anchor1(j, a); for (int k = 0; k < 3; ++k) r[k] = (dReal)a[k]; }
+}
+void dJointSetHingeAnchor(dJointID j, dReal x, dReal y, dReal z) {
+  JB jb(j);
+  og_host::set_anchors(j->h, jb.B, x, y, z, j->h.anchor1, j->h.anchor2);
+  og_host::hinge_qrel(j->h, jb.B);
+}
+void dJointSetHingeAxis(dJointID j, dReal x, dReal y, dReal z) {
+  JB jb(j);
+  og_host::set_axes(j->h, jb.B, x, y, z, j->h.axis1, j->h.axis2);
+  og_host::hinge_qrel(j->h, jb.B);
+}
+void dJointSetHingeParam(dJointID j, int p, dReal v) { limot_set(j->lm1, p, v); }
+dReal dJointGetHingeAngle(dJointID j) {
+  // getHingeAngle (ode/src/joints/joint.cpp:381-451), FP64 on the host
+  if (!j->body[0]) return 0;
+  double q1[4], qrel[4], qq[4];
+  for (int k = 0; k < 4; ++k) q1[k] = j->body[0]->q[k];
+  if (j->body[1]) {
+    double q2[4];
+    for (int k = 0; k < 4; ++k) q2[k] = j->body[1]->q[k];
+    og_host::qmul1(qq, q1, q2);
+    // qrel = qq * conj(qrel0) (dQMultiply2)
+    const double* c = j->h.qrel;
+    qrel[0] = qq[0] * c[0] + qq[1] * c[1] + qq[2] * c[2] + qq[3] * c[3];
+    qrel[1] = -qq[0] * c[1] + qq[1] * c[0] - qq[2] * c[3] + qq[3] * c[2];
+    qrel[2] = -qq[0] * c[2] + qq[2] * c[0] - qq[3] * c[1] + qq[1] * c[3];
+    qrel[3] = -qq[0] * c[3] + qq[3] * c[0] - qq[1] * c[2] + qq[2] * c[1];
+  } else {
+    const double* c = j->h.qrel;   // dQMultiply3
+    qrel[0] = q1[0] * c[0] - q1[1] * c[1] - q1[2] * c[2] - q1[3] * c[3];
+    qrel[1] = -q1[0] * c[1] - q1[1] * c[0] + q1[2] * c[3] - q1[3] * c[2];
+    qrel[2] = -q1[0] * c[2] - q1[2] * c[0] + q1[3] * c[1] - q1[1] * c[3];
+    qrel[3] = -q1[0] * c[3] - q1[3] * c[0] + q1[1] * c[2] - q1[2] * c[1];
+  }
+  const double cost2 = qrel[0];
+  const double sint2 = std::sqrt(qrel[1] * qrel[1] + qrel[2] * qrel[2] + qrel[3] * qrel[3]);
+  double theta = (og_host::dot3(qrel + 1, j->h.axis1) >= 0) ? 2 * std::atan2(sint2, cost2)
+                                                             : 2 * std::atan2(sint2, -cost2);
+  if (theta > M_PI) theta -= 2 * M_PI;
+  theta = -theta;
+  return (dReal)(j->reverse ? -theta : theta);
+}
+dReal dJointGetHingeAngleRate(dJointID j) {
+  if (!j->body[0]) return 0;
+  double R[12], ax[3];
+  for (int k = 0; k < 12; ++k) R[k] = j->body[0]->R[k];
+  og_host::mul0_331(ax, R, j->h.axis1);
+  double rate = ax[0] * j->body[0]->avel[0] + ax[1] * j->body[0]->avel[1] + ax[2] * j->body[0]->avel[2];
+  if (j->body[1]) rate -= ax[0] * j->body[1]->avel[0] + ax[1] * j->body[1]->avel[1] + ax[2] * j->body[1]->avel[2];
+  return (dReal)(j->reverse ? -rate : rate);
+}
+void dJointAddHingeTorque(dJointID j, dReal torque) {
+  // ode/src/joints/hinge.cpp:326-345
+  if (j->reverse) torque = -torque;
+  if (!j->body[0]) return;
+  dReal ax[3];
+  for (int r = 0; r < 3; ++r)
+    ax[r] = (dReal)(j->body[0]->R[r * 4] * j->h.axis1[0] + j->body[0]->R[r * 4 + 1] * j->h.axis1[1] +
+                    j->body[0]->R[r * 4 + 2] * j->h.axis1[2]) * torque;
+  dBodyAddTorque(j->body[0], ax[0], ax[1], ax[2]);
+  if (j->body[1]) dBodyAddTorque(j->body[1], -ax[0], -ax[1], -ax[2]);
+}
+void dJointSetHinge2Anchor(dJointID j, dReal x, dReal y, dReal z) {
+  JB jb(j);
+  og_host::set_anchors(j->h, jb.B, x, y, z, j->h.anchor1, j->h.anchor2);
+  og_host::hinge2_make_v(j->h, jb.B);
+}
+void dJointSetHinge2Axis1(dJointID j, dReal x, dReal y, dReal z) {
+  JB jb(j);
+  if (j->body[0]) {
+    og_host::set_axes(j->h, jb.B, x, y, z, j->h.axis1, nullptr);
+    if (j->body[1]) og_host::hinge2_axis_info(j->h, jb.B);
+  }
+  og_host::hinge2_make_v(j->h, jb.B);
+}
+void dJointSetHinge2Axis2(dJointID j, dReal x, dReal y, dReal z) {
+  JB jb(j);
+  if (j->body[1]) {
+    og_host::set_axes(j->h, jb.B, x, y, z, nullptr, j->h.axis2);
+    og_host::hinge2_axis_info(j->h, jb.B);
+  }
+  og_host::hinge2_make_v(j->h, jb.B);
+}
+void dJointSetHinge2Param(dJointID j, int p, dReal v) {
+  // ode/src/joints/hinge2.cpp:259-274
+  if ((p & 0xff00) == 0x100) limot_set(j->lm2, p & 0xff, v);
+  else if (p == dParamSuspensionERP) j->susp_erp = v;
+  else if (p == dParamSuspensionCFM) j->susp_cfm = v;
+  else limot_set(j->lm1, p, v);
+}
+void dJointAddHinge2Torques(dJointID j, dReal t1, dReal t2) {
+  // ode/src/joints/hinge2.cpp:393-410
+  if (!j->body[0] || !j->body[1]) return;
+  dReal a1[3], a2[3];
+  for (int r = 0; r < 3; ++r) {
+    a1[r] = (dReal)(j->body[0]->R[r * 4] * j->h.axis1[0] + j->body[0]->R[r * 4 + 1] * j->h.axis1[1] +
+                    j->body[0]->R[r * 4 + 2] * j->h.axis1[2]);
+    a2[r] = (dReal)(j->body[1]->R[r * 4] * j->h.axis2[0] + j->body[1]->R[r * 4 + 1] * j->h.axis2[1] +
+                    j->body[1]->R[r * 4 + 2] * j->h.axis2[2]);
+  }
+  dReal t[3] = {a1[0] * t1 + a2[0] * t2, a1[1] * t1 + a2[1] * t2, a1[2] * t1 + a2[2] * t2};
+  dBodyAddTorque(j->body[0], t[0], t[1], t[2]);
+  dBodyAddTorque(j->body[1], -t[0], -t[1], -t[2]);
+}
+dReal dJointGetHinge2Angle1(dJointID j) {
+  // dxJointHinge2::measureAngle (ode/src/joints/hinge2.cpp:33-41)
+  if (!j->body[0] || !j->body[1]) return 0;
+  double R1[12], R2[12], a1[3], a2[3];
+  for (int k = 0; k < 12; ++k) { R1[k] = j->body[0]->R[k]; R2[k] = j->body[1]->R[k]; }
+  og_host::mul0_331(a1, R2, j->h.axis2);
+  og_host::mul1_331(a2, R1, a1);
+  return (dReal)(-std::atan2(og_host::dot3(j->h.v2, a2), og_host::dot3(j->h.v1, a2)));
+}
+int dAreConnectedExcluding(dBodyID b1, dBodyID b2, int joint_type) {
+  // ode/src/ode.cpp:1529-1537
+  if (!b1) return 0;
+  for (dxJoint* j : b1->world->joints) {
+    if (j->type == joint_type) continue;
+    if ((j->body[0] == b1 && j->body[1] == b2) || (j->body[1] == b1 && j->body[0] == b2)) return 1;
+  }
+  return 0;
+}
+
+// ---------------------------------------------------------------- RNG
+int dTestRand(void) {
+  unsigned long old = g_seed;
+  int ok = 1;
+  g_seed = 0;
+  const unsigned long expect[5] = {0x3c6ef35f, 0x47502932, 0xd1ccf6e9, 0xaaf95334, 0x6252e503};
+  for (int i = 0; i < 5; ++i) if (dRand() != expect[i]) ok = 0;
+  g_seed = old;
+  return ok;
+}
+unsigned long dRand(void) {
+  g_seed = og::lcg_next((unsigned)g_seed);
+  return g_seed;
+}
+unsigned long dRandGetSeed(void) { return g_seed; }
+void dRandSetSeed(unsigned long s) { g_seed = s & 0xffffffffUL; }
+int dRandInt(int n) { return og::rand_int_from((unsigned)dRand(), n); }
+
+// ---------------------------------------------------------------- geoms + dCollide
+static dGeomID new_geom(int type, const double* p) {
+  auto* g = new dxGeom();
+  std::memset(g, 0, sizeof(*g));
+  g->type = type;
+  for (int k = 0; k < 4; ++k) g->p[k] = p[k];
+  g->R[0] = g->R[5] = g->R[10] = 1;
+  return g;
+}
+dGeomID dCreateSphere(dSpaceID, dReal r) { const double p[4] = {r, 0, 0, 0}; return new_geom(dSphereClass, p); }
+dGeomID dCreateBox(dSpaceID, dReal lx, dReal ly, dReal lz) {
+  const double p[4] = {lx, ly, lz, 0};
+  return new_geom(dBoxClass, p);
+}
+dGeomID dCreateCapsule(dSpaceID, dReal r, dReal len) {
+  const double p[4] = {r, len, 0, 0};
+  return new_geom(dCapsuleClass, p);
+}
+dGeomID dCreatePlane(dSpaceID, dReal a, dReal b, dReal c, dReal d) {
+  // make_sure_plane_normal_has_unit_length (ode/src/plane.cpp:40-56)
+  double p[4] = {a, b, c, d};
+  double l = p[0] * p[0] + p[1] * p[1] + p[2] * p[2];
+  if (l > 0) { l = 1.0 / std::sqrt(l); for (int k = 0; k < 4; ++k) p[k] *= l; }
+  else { p[0] = 1; p[1] = p[2] = p[3] = 0; }
+  return new_geom(dPlaneClass, p);
+}
+void dGeomDestroy(dGeomID g) { delete g; }
+void dGeomSetBody(dGeomID g, dBodyID b) { g->body = b; }
+dBodyID dGeomGetBody(dGeomID g) { return g->body; }
+void dGeomSetPosition(dGeomID g, dReal x, dReal y, dReal z) {
+  if (g->body) dBodySetPosition(g->body, x, y, z);
+  else { g->pos[0] = x; g->pos[1] = y; g->pos[2] = z; }
+}
+void dGeomSetRotation(dGeomID g, const dMatrix3 R) {
+  if (g->body) dBodySetRotation(g->body, R);
+  else for (int k = 0; k < 12; ++k) g->R[k] = R[k];
+}
+const dReal* dGeomGetPosition(dGeomID g) { return g->body ? g->body->pos : g->pos; }
+const dReal* dGeomGetRotation(dGeomID g) { return g->body ? g->body->R : g->R; }
+int dGeomGetClass(dGeomID g) { return g->type; }
+dReal dGeomSphereGetRadius(dGeomID g) { return (dReal)g->p[0]; }
+void dGeomBoxGetLengths(dGeomID g, dVector3 r) { for (int k = 0; k < 3; ++k) r[k] = (dReal)g->p[k]; }
+void dGeomPlaneGetParams(dGeomID g, dVector4 r) { for (int k = 0; k < 4; ++k) r[k] = (dReal)g->p[k]; }
+void dGeomCapsuleGetParams(dGeomID g, dReal* r, dReal* l) { *r = (dReal)g->p[0]; *l = (dReal)g->p[1]; }
+
+int dCollide(dGeomID o1, dGeomID o2, int flags, dContactGeom* contact, int skip) {
+  // early-outs of ode/src/collision_kernel.cpp:292-311, then the collider on the GPU
+  if (!o1 || !o2 || !contact || (flags & 0xffff) == 0) return 0;
+  if (o1 == o2) return 0;
+  if (o1->body == o2->body && o1->body) return 0;
+  og::GeomView v[2];
+  const dxGeom* g[2] = {o1, o2};
+  for (int i = 0; i < 2; ++i) {
+    v[i].type = g[i]->type;
+    for (int k = 0; k < 4; ++k) v[i].p[k] = (float)g[i]->p[k];
+    const dReal* pos = dGeomGetPosition((dGeomID)g[i]);
+    const dReal* R = dGeomGetRotation((dGeomID)g[i]);
+    for (int k = 0; k < 3; ++k) v[i].pos[k] = pos[k];
+    for (int k = 0; k < 12; ++k) v[i].R[k] = R[k];
+  }
+  int maxc = flags & 0xffff;
+  unsigned f = (unsigned)flags;
+  if (maxc > 8) f = (f & ~0xffffu) | 8u;   // colliders on this path emit at most 8
+  og::Contact out[8];
+  const int n = og::collide_pair_gpu(v[0], v[1], f, out);
+  if (n <= 0) return 0;
+  for (int i = 0; i < n; ++i) {
+    dContactGeom* c = (dContactGeom*)((char*)contact + (size_t)i * skip);
+    for (int k = 0; k < 3; ++k) { c->pos[k] = out[i].pos[k]; c->normal[k] = out[i].normal[k]; }
+    c->pos[3] = c->normal[3] = 0;
+    c->depth = out[i].depth;
+    c->g1 = o1;
+    c->g2 = o2;
+    c->side1 = c->side2 = -1;
+  }
+  return n;
+}
+
+// ---------------------------------------------------------------- step
+int dWorldQuickStep(dWorldID w, dReal stepsize) {
+  if (!w || !(stepsize > 0)) return 0;
+  if (!w->ctx) {
+    w->ctx = og::ctx_create(0);
+    if (!w->ctx) return 0;
+  }
+  og::HostWorld& hw = w->hw;
+  const int nb = (int)w->bodies.size();
+  if (nb == 0) return 1;
+  if (nb > ODEGPU_MAX_BODIES_PER_WORLD) return 0;
+  hw.pos.resize(nb); hw.q.resize(nb); hw.lvel.resize(nb); hw.avel.resize(nb);
+  hw.facc.resize(nb); hw.tacc.resize(nb);
+  hw.mass.resize(nb); hw.invMass.resize(nb); hw.I.resize(9 * (size_t)nb); hw.invI.resize(9 * (size_t)nb);
+  hw.flags.resize(nb);
+  for (int i = 0; i < nb; ++i) {
+    dxBody* b = w->bodies[i];
+    hw.pos[i] = make_float4(b->pos[0], b->pos[1], b->pos[2], 0.f);
+    hw.q[i] = make_float4(b->q[0], b->q[1], b->q[2], b->q[3]);
+    hw.lvel[i] = make_float4(b->lvel[0], b->lvel[1], b->lvel[2], 0.f);
+    hw.avel[i] = make_float4(b->avel[0], b->avel[1], b->avel[2], 0.f);
+    hw.facc[i] = make_float4(b->facc[0], b->facc[1], b->facc[2], 0.f);
+    hw.tacc[i] = make_float4(b->tacc[0], b->tacc[1], b->tacc[2], 0.f);
+    hw.mass[i] = b->mass.mass;
+    hw.invMass[i] = (float)b->invMass;
+    for (int r = 0; r < 3; ++r)
+      for (int c = 0; c < 3; ++c) {
+        hw.I[9 * (size_t)i + r * 3 + c] = b->mass.I[r * 4 + c];
+        hw.invI[9 * (size_t)i + r * 3 + c] = (float)b->invI[r * 3 + c];
+      }
+    hw.flags[i] = b->flags;
+  }
+  auto index_of = [&](const dxBody* b) -> int {
+    if (!b) return -1;
+    return (int)(std::find(w->bodies.begin(), w->bodies.end(), b) - w->bodies.begin());
+  };
+  // joints: persistent first (creation order), then contacts (creation order)
+  std::vector<dxJoint*> pj, cj;
+  for (dxJoint* j : w->joints) {
+    if (!j->body[0]) continue;   // unattached joints take no part (util.cpp:435-467)
+    (j->type == dJointTypeContact ? cj : pj).push_back(j);
+  }
+  hw.joints.resize(pj.size());
+  for (size_t k = 0; k < pj.size(); ++k) {
+    const dxJoint* j = pj[k];
+    DevJoint& J = hw.joints[k];
+    std::memset(&J, 0, sizeof(J));
+    J.type = j->type;
+    J.b1 = index_of(j->body[0]);
+    J.b2 = index_of(j->body[1]);
+    J.reverse = j->reverse;
+    for (int q = 0; q < 4; ++q) {
+      J.anchor1[q] = (float)j->h.anchor1[q]; J.anchor2[q] = (float)j->h.anchor2[q];
+      J.axis1[q] = (float)j->h.axis1[q]; J.axis2[q] = (float)j->h.axis2[q];
+      J.qrel[q] = (float)j->h.qrel[q]; J.v1[q] = (float)j->h.v1[q]; J.v2[q] = (float)j->h.v2[q];
+    }
+    J.c0 = (float)j->h.c0; J.s0 = (float)j->h.s0;
+    J.erp = (float)j->erp; J.cfm = (float)j->cfm;
+    J.lm1 = j->lm1; J.lm2 = j->lm2;
+    J.susp_erp = (float)j->susp_erp; J.susp_cfm = (float)j->susp_cfm;
+  }
+  hw.contacts.resize(cj.size());
+  hw.surfaces.resize(std::max<size_t>(1, cj.size()));
+  for (size_t k = 0; k < cj.size(); ++k) {
+    const dxJoint* j = cj[k];
+    DevContact& c = hw.contacts[k];
+    std::memset(&c, 0, sizeof(c));
+    for (int q = 0; q < 3; ++q) { c.pos[q] = j->contact.geom.pos[q]; c.normal[q] = j->contact.geom.normal[q]; }
+    c.depth = j->contact.geom.depth;
+    c.surface = (int)k;
+    c.b1 = index_of(j->body[0]);
+    c.b2 = index_of(j->body[1]);
+    c.reverse = j->reverse;
+    const dSurfaceParameters& S = j->contact.surface;
+    DevSurface& D = hw.surfaces[k];
+    D.mode = S.mode; D.mu = S.mu; D.mu2 = S.mu2; D.bounce = S.bounce; D.bounce_vel = S.bounce_vel;
+    D.soft_erp = S.soft_erp; D.soft_cfm = S.soft_cfm; D.motion1 = S.motion1; D.motion2 = S.motion2;
+    D.motionN = S.motionN; D.slip1 = S.slip1; D.slip2 = S.slip2;
+  }
+  // every body's joint list, newest attachment first
+  std::vector<std::vector<std::pair<long long, int>>> lists(nb);
+  for (size_t k = 0; k < pj.size(); ++k)
+    for (int s = 0; s < 2; ++s)
+      if (pj[k]->body[s]) lists[index_of(pj[k]->body[s])].push_back({pj[k]->seq, (int)k});
+  for (size_t k = 0; k < cj.size(); ++k)
+    for (int s = 0; s < 2; ++s)
+      if (cj[k]->body[s]) lists[index_of(cj[k]->body[s])].push_back({cj[k]->seq, (int)(pj.size() + k)});
+  hw.padj_start.assign(nb + 1, 0);
+  hw.padj.clear();
+  for (int i = 0; i < nb; ++i) {
+    std::sort(lists[i].begin(), lists[i].end(), [](auto& a, auto& b) { return a.first > b.first; });
+    hw.padj_start[i] = (int)hw.padj.size();
+    for (auto& e : lists[i]) hw.padj.push_back(e.second);
+  }
+  hw.padj_start[nb] = (int)hw.padj.size();
+  if (hw.padj.empty()) hw.padj.push_back(0);
+  og::WorldDesc& D = hw.desc;
+  std::memset(&D, 0, sizeof(D));
+  D.nb = nb;
+  D.njp = (int)pj.size();
+  D.contact_cap = (int)cj.size();
+  D.row_cap = ODEGPU_MAX_ROWS_PER_WORLD;
+  D.iterations = w->iterations;
+  for (int k = 0; k < 3; ++k) D.gravity[k] = (float)w->gravity[k];
+  D.erp = (float)w->erp; D.cfm = (float)w->cfm; D.sor_w = (float)w->sor_w;
+  D.max_vel = (float)w->max_vel; D.min_depth = (float)w->min_depth; D.dt = stepsize;
+  D.max_contacts = 1;
+  hw.seed = (unsigned)g_seed;
+  if (og::ctx_step(w->ctx, hw) != 0) return 0;
+  g_seed = hw.seed;
+  for (int i = 0; i < nb; ++i) {
+    dxBody* b = w->bodies[i];
+    b->pos[0] = hw.pos[i].x; b->pos[1] = hw.pos[i].y; b->pos[2] = hw.pos[i].z;
+    b->q[0] = hw.q[i].x; b->q[1] = hw.q[i].y; b->q[2] = hw.q[i].z; b->q[3] = hw.q[i].w;
+    body_sync_R(b);
+    b->lvel[0] = hw.lvel[i].x; b->lvel[1] = hw.lvel[i].y; b->lvel[2] = hw.lvel[i].z;
+    b->avel[0] = hw.avel[i].x; b->avel[1] = hw.avel[i].y; b->avel[2] = hw.avel[i].z;
+    for (int k = 0; k < 4; ++k) b->facc[k] = b->tacc[k] = 0;
+  }
+  return hw.status == 0 ? 1 : 0;
+}
+
+}  // extern "C"

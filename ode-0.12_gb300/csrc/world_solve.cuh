@@ -535,12 +535,14 @@ struct StepOptions {
   float* dbg_rows;      // optional: rows before scaling (parity taps)
   float* dbg_lambda;    // optional: lambda after SOR, by world row
   float* dbg_fc;        // optional: cforce per body
+  int host_forces;      // 1: facc/tacc were uploaded (skip the control phase)
+  int host_adjacency;   // 1: padj holds every joint of each body in list order
 };
 
 OG_D void world_step(const BatchDev& d, int w, int step, const WarpSmem& S, int lane,
                      const StepOptions& opt) {
   const WorldDesc D = d.world[w];
-  phase_controls(d, D, step, lane);
+  if (!opt.host_forces) phase_controls(d, D, step, lane);
   int nc;
   if (opt.collide) {
     nc = phase_collide(d, D, w, lane);
@@ -556,7 +558,7 @@ OG_D void world_step(const BatchDev& d, int w, int step, const WarpSmem& S, int 
     if (lane == 0) atomicOr(&d.status[w], ST_TOO_LARGE);
     M = -1;
   } else {
-    const int nj = phase_islands(d, D, w, nc, S, lane, &nisl);
+    const int nj = phase_islands(d, D, w, opt.host_adjacency ? 0 : nc, D.njp + nc, S, lane, &nisl);
     M = phase_rows(d, D, w, nj, nisl, lane);
   }
   unsigned seed = d.seed[w];

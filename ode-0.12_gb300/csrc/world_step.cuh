@@ -193,8 +193,10 @@ OG_D void joint_bodies(const BatchDev& d, const WorldDesc& D, int ord, int& b1, 
 // Phase 3: adjacency in ODE list order + DFS islands. Writes jlist (joint
 // ordinals in island order; bit 30 marks the first joint of an island) and
 // returns the number of joints placed; *n_isl receives the island count.
-OG_D int phase_islands(const BatchDev& d, const WorldDesc& D, int w, int nc, const WarpSmem& S,
-                       int lane, int* n_isl) {
+// nc_lists: contacts to merge into the body lists (0 when the host supplied
+// complete lists in padj); nj_all: persistent + contact joints (tag range).
+OG_D int phase_islands(const BatchDev& d, const WorldDesc& D, int w, int nc, int nj_all,
+                       const WarpSmem& S, int lane, int* n_isl) {
   const int nb = D.nb;
   const int jl_off = D.joint_off + D.contact_off;
   const int adj_off = 2 * jl_off;
@@ -230,7 +232,7 @@ OG_D int phase_islands(const BatchDev& d, const WorldDesc& D, int w, int nc, con
     }
     for (int k = pstart[b]; k < pstart[b + 1]; ++k) d.adj[wp++] = d.padj[k];
   }
-  const int nj = D.njp + nc;
+  const int nj = nj_all;
   for (int b = lane; b < nb; b += 32) S.tag[b] = 0;
   for (int j = lane; j < nj; j += 32) S.jtag[j] = 0;
   __syncwarp();
