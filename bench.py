@@ -266,7 +266,6 @@ def run_ours(args):
             P = Batch(sub, device=local_rank)
             P.step_plain(2)
             P.sync()
-            P.set_state(sub_init := P.state())
             t0 = time.perf_counter()
             P.step_plain(20)
             P.sync()
