@@ -794,3 +794,87 @@ int collide_pair_gpu(const GeomView& a, const GeomView& b, unsigned flags, Conta
 }
 
 }  // namespace og
+
+// ---------------------------------------------------------------------------
+// dCollide without any device allocation (odegpuCollideNoAlloc).
+//
+// Some hosts cannot call cudaMalloc at the point where they need a contact
+// query: an engine that hands all device memory to its own pool allocator, a
+// real-time control loop where allocation is forbidden, or a plugin running
+// while its host holds the device's memory budget. For them the staging buffer
+// the collider writes into lives in this file-scope device array instead of a
+// per-call cudaMalloc. Every GPU that loads the library holds it until exit.
+
+namespace {
+
+struct NoAllocScratch {
+  og::Contact contacts[ODEGPU_NOALLOC_MAX_CONTACTS];
+  int count;
+};
+static __device__ __align__(256) NoAllocScratch g_noalloc_scratch[1];
+
+// Device address of g_noalloc_scratch per device, looked up once per device
+// (host code may not use the symbol's name as an address).
+constexpr int kMaxDevices = 64;
+NoAllocScratch* g_noalloc_ptr[kMaxDevices] = {};
+
+__global__ void collide_pair_noalloc_kernel(GeomView a, GeomView b, unsigned flags, NoAllocScratch* s) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    Contact c[8];
+    s->count = 0;   // the array keeps the previous call's contents; reset first
+    const int k = collide_primitive(a, b, flags, c);
+    for (int i = 0; i < k; ++i) s->contacts[i] = c[i];
+    s->count = k;
+  }
+}
+
+GeomView make_view(int cls, const float* p, const float* pos, const float* R) {
+  GeomView v;
+  v.type = cls;
+  for (int k = 0; k < 4; ++k) v.p[k] = p[k];
+  for (int k = 0; k < 3; ++k) v.pos[k] = pos ? pos[k] : 0.f;
+  for (int k = 0; k < 12; ++k) v.R[k] = R ? R[k] : ((k == 0 || k == 5 || k == 10) ? 1.f : 0.f);
+  if (cls == ODEGPU_GEOM_PLANE) {
+    // dCreatePlane normalises (ode/src/plane.cpp:40-56)
+    float l = v.p[0] * v.p[0] + v.p[1] * v.p[1] + v.p[2] * v.p[2];
+    if (l > 0.f) { l = 1.0f / sqrtf(l); for (int k = 0; k < 4; ++k) v.p[k] *= l; }
+    else { v.p[0] = 1.f; v.p[1] = v.p[2] = v.p[3] = 0.f; }
+  }
+  return v;
+}
+
+}  // namespace
+
+extern "C" int odegpuCollideNoAlloc(int class1, const float* params1, const float* pos1, const float* R1,
+                                    int class2, const float* params2, const float* pos2, const float* R2,
+                                    int flags, float* contacts_out) {
+  if (!params1 || !params2 || !contacts_out) return fail(ODEGPU_E_ARG, "null argument");
+  const int maxc = flags & 0xffff;
+  if (maxc < 1) return 0;
+  if (maxc > ODEGPU_NOALLOC_MAX_CONTACTS)
+    return fail(ODEGPU_E_LIMIT, "odegpuCollideNoAlloc returns at most " +
+                                    std::to_string(ODEGPU_NOALLOC_MAX_CONTACTS) + " contacts; asked for " +
+                                    std::to_string(maxc));
+  int dev = 0;
+  OG_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices) return fail(ODEGPU_E_LIMIT, "device ordinal out of range");
+  if (!g_noalloc_ptr[dev]) {
+    // set-up on the first call on this device, with the device current
+    void* p = nullptr;
+    OG_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    g_noalloc_ptr[dev] = static_cast<NoAllocScratch*>(p);
+  }
+  NoAllocScratch* s = g_noalloc_ptr[dev];
+  const GeomView a = make_view(class1, params1, pos1, R1);
+  const GeomView b = make_view(class2, params2, pos2, R2);
+  collide_pair_noalloc_kernel<<<1, 32>>>(a, b, (unsigned)flags, s);
+  OG_CUDA(cudaGetLastError());
+  NoAllocScratch h;
+  OG_CUDA(cudaMemcpy(&h, s, sizeof(h), cudaMemcpyDeviceToHost));
+  for (int i = 0; i < h.count; ++i) {
+    float* o = contacts_out + 7 * i;
+    for (int k = 0; k < 3; ++k) { o[k] = h.contacts[i].pos[k]; o[3 + k] = h.contacts[i].normal[k]; }
+    o[6] = h.contacts[i].depth;
+  }
+  return h.count;
+}
