@@ -31,20 +31,39 @@ int fail(int code, const std::string& msg) {
       return fail(ODEGPU_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
   } while (0)
 
-// Step kernel: warp w of the grid owns world (first_world + w) and runs
-// n_steps steps of it back to back. Warps never wait on each other.
-__global__ void __launch_bounds__(128) world_step_kernel(BatchDev d, int first_world, int n_worlds,
-                                                         int step0, int n_steps, StepOptions opt) {
+// Step = two kernels, each one warp per world; warps never wait on each other.
+// `order` (optional) maps grid slots to worlds, largest worlds first, so the
+// long worlds start early and the short ones fill in behind them.
+__device__ __forceinline__ int slot_world(const int* order, int first, int count, int nw) {
+  const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (i >= count) return -1;
+  const int w = order ? order[first + i] : first + i;
+  return w < nw ? w : -1;
+}
+
+__global__ void __launch_bounds__(128) world_setup_kernel(BatchDev d, const int* order, int first, int count,
+                                                          int step, StepOptions opt) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int w = first_world + blockIdx.x * (blockDim.x >> 5) + warp;
-  if (w >= first_world + n_worlds || w >= d.n_worlds) return;
-  const WarpSmem S = carve_smem(smem_raw + (size_t)warp * kSmemPerWarp);
+  const int lane = threadIdx.x & 31;
+  const int w = slot_world(order, first, count, d.n_worlds);
+  if (w < 0) return;
   if (d.world[w].nb > kMaxB) {
-    if (lane == 0) atomicOr(&d.status[w], ST_TOO_LARGE);
+    if (lane == 0) { atomicOr(&d.status[w], ST_TOO_LARGE); d.nrows[w] = 0; d.nislands[w] = 0; }
     return;
   }
-  for (int s = 0; s < n_steps; ++s) world_step(d, w, step0 + s, S, lane, opt);
+  const WarpSmem S = carve_smem(smem_raw + (size_t)(threadIdx.x >> 5) * kSmemPerWarp);
+  world_setup(d, w, step, S, lane, opt);
+}
+
+__global__ void __launch_bounds__(128) world_solve_kernel(BatchDev d, const int* order, int first, int count,
+                                                          StepOptions opt) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lane = threadIdx.x & 31;
+  const int w = slot_world(order, first, count, d.n_worlds);
+  if (w < 0) return;
+  if (d.world[w].nb > kMaxB) return;
+  const SorSmem S = carve_sor(smem_raw + (size_t)(threadIdx.x >> 5) * kSorSmemPerWarp);
+  world_solve(d, w, S, lane, opt);
 }
 
 // State exchange: FP32 records of 13 floats per body.
@@ -143,16 +162,36 @@ struct odegpuBatch {
     return d;
   }
 
-  int launch(int first, int count, int n_steps, const StepOptions& opt) {
+  DBuf<int> order;   // worlds by decreasing size (launch slot -> world)
+
+  // n_steps steps of worlds [first, first+count) of the launch order (or of
+  // the identity order when use_order is false); 2 launches per step.
+  int launch(int first, int count, int n_steps, const StepOptions& opt, bool use_order = true) {
     const int wpb = warps_per_block;
     const int blocks = (count + wpb - 1) / wpb;
-    const size_t smem = (size_t)wpb * kSmemPerWarp;
-    world_step_kernel<<<blocks, wpb * 32, smem, stream>>>(dev(), first, count, step_counter, n_steps, opt);
+    const BatchDev d = dev();
+    const int* ord = (use_order && order.p) ? order.p : nullptr;
+    for (int s = 0; s < n_steps; ++s) {
+      world_setup_kernel<<<blocks, wpb * 32, (size_t)wpb * kSmemPerWarp, stream>>>(d, ord, first, count,
+                                                                                 step_counter + s, opt);
+      world_solve_kernel<<<blocks, wpb * 32, (size_t)wpb * kSorSmemPerWarp, stream>>>(d, ord, first, count,
+                                                                                    opt);
+    }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return fail(ODEGPU_E_CUDA, std::string("step launch: ") + cudaGetErrorString(e));
     return 0;
   }
 };
+
+static int configure_kernels(int wpb) {
+  if (cudaFuncSetAttribute(world_setup_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)(wpb * kSmemPerWarp)) != cudaSuccess)
+    return -1;
+  if (cudaFuncSetAttribute(world_solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)(wpb * kSorSmemPerWarp)) != cudaSuccess)
+    return -1;
+  return 0;
+}
 
 extern "C" {
 
@@ -411,11 +450,13 @@ int odegpuBatchCreate(const odegpuScene* sc, const odegpuBatchConfig* cfg, odegp
   if (!rc && cudaStreamCreateWithFlags(&B->stream, cudaStreamNonBlocking) != cudaSuccess)
     rc = fail(ODEGPU_E_CUDA, "stream creation failed");
   if (!rc) {
-    const size_t smem = (size_t)B->warps_per_block * kSmemPerWarp;
-    if (cudaFuncSetAttribute(world_step_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-        cudaSuccess)
-      rc = fail(ODEGPU_E_CUDA, "cannot configure shared memory");
+    // launch order: worlds by decreasing body count (ties by index)
+    std::vector<int> ord(W);
+    for (int w = 0; w < W; ++w) ord[w] = w;
+    std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return wd[a].nb > wd[b].nb; });
+    rc = B->order.upload(ord);
   }
+  if (!rc && configure_kernels(B->warps_per_block) != 0) rc = fail(ODEGPU_E_CUDA, "cannot configure shared memory");
   if (rc) { delete B; return rc; }
   *out = B;
   return 0;
@@ -462,7 +503,7 @@ int odegpuBatchStepPlain(odegpuBatchID b, int n_steps) {
     for (int s = 0; s < n_steps; ++s) {
       const int base = b->step_counter;
       b->step_counter = base + s;
-      const int rc = b->launch(w, 1, 1, opt);
+      const int rc = b->launch(w, 1, 1, opt, false);
       b->step_counter = base;
       if (rc) { b->warps_per_block = saved; return rc; }
     }
@@ -704,7 +745,7 @@ WorldCtx* ctx_create(int device) {
     fail(ODEGPU_E_CUDA, "stream creation failed");
     return nullptr;
   }
-  cudaFuncSetAttribute(world_step_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemPerWarp * 4);
+  configure_kernels(4);
   return c;
 }
 
@@ -765,7 +806,7 @@ int ctx_step(WorldCtx* c, HostWorld& hw) {
   if (rc) return rc;
   B.n_ctrl_steps = 0;
   StepOptions opt{0, nullptr, nullptr, nullptr, 1, 1};
-  if (int e = B.launch(0, 1, 1, opt)) return e;
+  if (int e = B.launch(0, 1, 1, opt, false)) return e;
   std::vector<int> st(1);
   OG_CUDA(cudaMemcpyAsync(hw.pos.data(), B.pos.p, nb * sizeof(float4), cudaMemcpyDeviceToHost, s));
   OG_CUDA(cudaMemcpyAsync(hw.q.data(), B.q.p, nb * sizeof(float4), cudaMemcpyDeviceToHost, s));

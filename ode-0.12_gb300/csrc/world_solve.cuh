@@ -1,6 +1,7 @@
 // world_solve.cuh -- phases 2 and 4-7 of a world step (see world_step.cuh).
 #pragma once
 #include "world_step.cuh"
+#include "sor.cuh"
 
 namespace og {
 
@@ -268,163 +269,13 @@ OG_D void phase_row_setup(const BatchDev& d, const WorldDesc& D, int M, const Wa
     row4[4] = make_float4(iMJ[4], iMJ[5], iMJ[6], iMJ[7]);
     row4[5] = make_float4(iMJ[8], iMJ[9], iMJ[10], iMJ[11]);
     row4[6] = make_float4(rhs * Ad, Ad * cfm, w6.z, w6.w);
-    S.rowbod[r] = (uint16_t)((b1 + 1) | ((b2 + 1) << 8));
   }
   __syncwarp();
-}
-
-// Wavefront levels of the 32 positions of window `wi` (see file header).
-OG_D void compute_levels(const WarpSmem& S, int wi, int M, int lane) {
-  const int pos = wi * 32 + lane;
-  int b1 = -3, b2 = -4;
-  if (pos < M) {
-    const uint16_t rb = S.rowbod[S.seq[pos]];
-    b1 = (rb & 0xff) - 1;
-    b2 = (rb >> 8) - 1;
-  }
-  int level = 0;
-#pragma unroll 4
-  for (int k = 0; k < 31; ++k) {
-    const int kb1 = __shfl_sync(kFull, b1, k);
-    const int kb2 = __shfl_sync(kFull, b2, k);
-    const int kl = __shfl_sync(kFull, level, k);
-    if (lane > k) {
-      const bool share = (b1 == kb1) || (b1 == kb2) || (b2 >= 0 && (b2 == kb1 || b2 == kb2));
-      if (share && kl + 1 > level) level = kl + 1;
-    }
-  }
-  if (pos < M) S.lvl[pos] = (uint8_t)level;
-  const int mx = warp_max(pos < M ? level : 0);
-  if (lane == 0) S.wlev[wi] = (uint8_t)mx;
-}
-
-// Phase 6: SOR_LCP (quickstep.cpp:342-584) over all islands of the world.
-// Returns the RNG state after the step.
-OG_D unsigned phase_sor(const BatchDev& d, const WorldDesc& D, int w, int M, int nisl, unsigned seed,
-                        const WarpSmem& S, int lane) {
-  for (int i = lane; i < D.nb * 6; i += 32) S.fc[i] = 0.f;
-  for (int i = lane; i < M; i += 32) S.lambda[i] = 0.f;
-  const int* rstart = d.island_rstart + D.body_off + w;
-  const int iters = D.iterations;
-  const int n_shuffles = (iters + 7) / 8;
-  // initial order: findex == -1 rows first (ascending), the rest filled from the
-  // island's tail backwards (quickstep.cpp:405-425)
-  for (int isl = 0; isl < nisl; ++isl) {
-    const int rs = rstart[isl], re = rstart[isl + 1];
-    int negc = 0;
-    for (int base = rs; base < re; base += 32) {
-      const int r = base + lane;
-      bool neg = false;
-      if (r < re) neg = reinterpret_cast<const int*>(d.rows + (size_t)(D.row_off + r) * kRowWords)[kRowFindex] == -1;
-      const unsigned bal = __ballot_sync(kFull, neg && r < re);
-      const int negb = negc + __popc(bal & ((1u << lane) - 1u));
-      if (r < re) {
-        const int nonnegb = (r - rs) - negb;
-        const int p = neg ? rs + negb : re - 1 - nonnegb;
-        S.seq[p] = (uint16_t)r;
-      }
-      negc += __popc(bal);
-    }
-  }
-  __syncwarp();
-  // RNG stream offsets: islands consume ODE's global stream in island order,
-  // each island n_shuffles * (m - 1) draws.
-  unsigned total_draws = 0;
-  for (int isl = 0; isl < nisl; ++isl) {
-    const int m = rstart[isl + 1] - rstart[isl];
-    if (m > 0) total_draws += (unsigned)(n_shuffles * (m - 1));
-  }
-  const int nwin = (M + 31) / 32;
-  float4 rw[8];
-  for (int it = 0; it < iters; ++it) {
-    if ((it & 7) == 0) {
-      const int round = it >> 3;
-      // islands shuffled in parallel, one lane per island
-      unsigned prefix = 0;
-      for (int ib = 0; ib < nisl; ib += 32) {
-        const int isl = ib + lane;
-        int m = 0;
-        if (isl < nisl) m = rstart[isl + 1] - rstart[isl];
-        const int draws = m > 0 ? n_shuffles * (m - 1) : 0;
-        const int incl = warp_incl_scan(draws, lane);
-        if (isl < nisl && m > 1) {
-          unsigned s = lcg_jump(seed, prefix + (unsigned)(incl - draws) + (unsigned)(round * (m - 1)));
-          uint16_t* sq = S.seq + rstart[isl];
-          for (int q = 1; q < m; ++q) {
-            s = lcg_next(s);
-            const int sw = rand_int_from(s, q + 1);
-            const uint16_t t = sq[q];
-            sq[q] = sq[sw];
-            sq[sw] = t;
-          }
-        }
-        prefix += (unsigned)__shfl_sync(kFull, incl, 31);
-      }
-      __syncwarp();
-      for (int wi = 0; wi < nwin; ++wi) compute_levels(S, wi, M, lane);
-      __syncwarp();
-    }
-    for (int wi = 0; wi < nwin; ++wi) {
-      const int pos = wi * 32 + lane;
-      const bool valid = pos < M;
-      int r = 0, level = 255;
-      if (valid) {
-        r = S.seq[pos];
-        level = S.lvl[pos];
-        const float4* src = reinterpret_cast<const float4*>(d.rows + (size_t)(D.row_off + r) * kRowWords);
-#pragma unroll
-        for (int q = 0; q < 8; ++q) rw[q] = src[q];
-      }
-      const int maxl = S.wlev[wi];
-      for (int l = 0; l <= maxl; ++l) {
-        if (level == l) {
-          const float* J = reinterpret_cast<const float*>(&rw[0]);
-          const float* iMJ = reinterpret_cast<const float*>(&rw[3]);
-          const float bb = rw[6].x, Ad = rw[6].y, lo = rw[6].z, hi = rw[6].w;
-          const int findex = __float_as_int(rw[7].x);
-          const int b1 = __float_as_int(rw[7].y), b2 = __float_as_int(rw[7].z);
-          float* fc1 = S.fc + 6 * b1;
-          const float old = S.lambda[r];
-          float delta = bb - old * Ad;
-          delta -= fc1[0] * J[0] + fc1[1] * J[1] + fc1[2] * J[2] + fc1[3] * J[3] + fc1[4] * J[4] +
-                   fc1[5] * J[5];
-          float* fc2 = nullptr;
-          if (b2 != -1) {
-            fc2 = S.fc + 6 * b2;
-            delta -= fc2[0] * J[6] + fc2[1] * J[7] + fc2[2] * J[8] + fc2[3] * J[9] + fc2[4] * J[10] +
-                     fc2[5] * J[11];
-          }
-          float hi_act, lo_act;
-          if (findex != -1) {
-            hi_act = fabsf(hi * S.lambda[findex]);
-            lo_act = -hi_act;
-          } else {
-            hi_act = hi;
-            lo_act = lo;
-          }
-          const float nl = old + delta;
-          float lam;
-          if (nl < lo_act) { delta = lo_act - old; lam = lo_act; }
-          else if (nl > hi_act) { delta = hi_act - old; lam = hi_act; }
-          else lam = nl;
-          S.lambda[r] = lam;
-          fc1[0] += delta * iMJ[0]; fc1[1] += delta * iMJ[1]; fc1[2] += delta * iMJ[2];
-          fc1[3] += delta * iMJ[3]; fc1[4] += delta * iMJ[4]; fc1[5] += delta * iMJ[5];
-          if (fc2) {
-            fc2[0] += delta * iMJ[6]; fc2[1] += delta * iMJ[7]; fc2[2] += delta * iMJ[8];
-            fc2[3] += delta * iMJ[9]; fc2[4] += delta * iMJ[10]; fc2[5] += delta * iMJ[11];
-          }
-        }
-        __syncwarp();
-      }
-    }
-  }
-  return lcg_jump(seed, total_draws);
 }
 
 // Phase 7: velocity update from the constraint forces and external forces,
 // then dxStepBody (quickstep.cpp:905-916, :960-975, :1001-1021; util.cpp:255-360).
-OG_D void phase_integrate(const BatchDev& d, const WorldDesc& D, int w, const WarpSmem& S, int lane,
+OG_D void phase_integrate(const BatchDev& d, const WorldDesc& D, int w, const float* cforce, int lane,
                           bool have_rows) {
   const float h = D.dt;
   bool bad = false;
@@ -432,7 +283,7 @@ OG_D void phase_integrate(const BatchDev& d, const WorldDesc& D, int w, const Wa
     const int gb = D.body_off + b;
     float4 lv = d.lvel[gb], av = d.avel[gb];
     if (have_rows) {
-      const float* fc = S.fc + 6 * b;
+      const float* fc = cforce + 6 * b;
       lv.x += h * fc[0]; lv.y += h * fc[1]; lv.z += h * fc[2];
       av.x += h * fc[3]; av.y += h * fc[4]; av.z += h * fc[5];
     }
@@ -539,8 +390,10 @@ struct StepOptions {
   int host_adjacency;   // 1: padj holds every joint of each body in list order
 };
 
-OG_D void world_step(const BatchDev& d, int w, int step, const WarpSmem& S, int lane,
-                     const StepOptions& opt) {
+// Setup kernel body: phases 0-5. Leaves the rows, island table, row count
+// and island count of the step in global memory for world_solve.
+OG_D void world_setup(const BatchDev& d, int w, int step, const WarpSmem& S, int lane,
+                      const StepOptions& opt) {
   const WorldDesc D = d.world[w];
   if (!opt.host_forces) phase_controls(d, D, step, lane);
   int nc;
@@ -561,23 +414,35 @@ OG_D void world_step(const BatchDev& d, int w, int step, const WarpSmem& S, int 
     const int nj = phase_islands(d, D, w, opt.host_adjacency ? 0 : nc, D.njp + nc, S, lane, &nisl);
     M = phase_rows(d, D, w, nj, nisl, lane);
   }
+  if (M > 0) phase_row_setup(d, D, M, S, lane, opt.dbg_rows);
+  if (lane == 0) {
+    d.nrows[w] = M < 0 ? 0 : M;
+    d.nislands[w] = M > 0 ? nisl : 0;
+  }
+  __syncwarp();
+}
+
+// Solve kernel body: phase 6 (SOR) and phase 7 (integration).
+OG_D void world_solve(const BatchDev& d, int w, const SorSmem& S, int lane, const StepOptions& opt) {
+  const WorldDesc D = d.world[w];
+  const int M = d.nrows[w];
+  const int nisl = d.nislands[w];
   unsigned seed = d.seed[w];
   const bool have_rows = M > 0;
   if (have_rows) {
-    phase_row_setup(d, D, M, S, lane, opt.dbg_rows);
-    seed = phase_sor(d, D, w, M, nisl, seed, S, lane);
+    const float* rows = d.rows + (size_t)D.row_off * kRowWords;
+    const int* rstart = d.island_rstart + D.body_off + w;
+    // rows of island i start at rstart[i] (world row index); shift so the
+    // row store pointer can be used with world-local row indices
+    seed = sor_world(rows, rstart, D.nb, M, nisl, D.iterations, seed, S, lane);
     __syncwarp();
     if (opt.dbg_lambda)
       for (int r = lane; r < M; r += 32) opt.dbg_lambda[D.row_off + r] = S.lambda[r];
     if (opt.dbg_fc)
       for (int i = lane; i < D.nb * 6; i += 32) opt.dbg_fc[(size_t)D.body_off * 6 + i] = S.fc[i];
   }
-  if (lane == 0) {
-    d.seed[w] = seed;
-    d.nrows[w] = M < 0 ? 0 : M;
-    d.nislands[w] = nisl;
-  }
-  phase_integrate(d, D, w, S, lane, have_rows);
+  if (lane == 0) d.seed[w] = seed;
+  phase_integrate(d, D, w, S.fc, lane, have_rows);
   __syncwarp();
 }
 

@@ -28,33 +28,22 @@ constexpr unsigned kFull = 0xffffffffu;
 constexpr int kMaxB = 64;      // bodies per world handled on chip
 constexpr int kMaxR = 1024;    // constraint rows per world handled on chip
 
-// Per-warp shared-memory working set.
+// Per-warp shared-memory working set of the setup phases.
 struct WarpSmem {
-  float* fc;          // [kMaxB*6]  constraint force accumulator (also tmp1)
-  float* lambda;      // [kMaxR]
-  uint16_t* seq;      // [kMaxR]    rows in current sweep order
-  uint16_t* rowbod;   // [kMaxR]    (b1+1) | (b2+1) << 8 for each row
-  uint8_t* lvl;       // [kMaxR]    wavefront level of each sweep position
-  uint8_t* wlev;      // [kMaxR/32] max level per window
+  float* fc;          // [kMaxB*6]  tmp1 = invM fe + v/h per body
+  int* cnt;           // [kMaxB+1]  contacts per body
+  int16_t* stack;     // [kMaxB]    island search stack
   uint8_t* tag;       // [kMaxB]    body tags for the island search
   uint8_t* jtag;      // [kMaxR]    joint tags for the island search
-  int16_t* stack;     // [kMaxB]
-  int* cnt;           // [kMaxB+1]
 };
-constexpr int kSmemPerWarp = kMaxB * 6 * 4 + kMaxR * 4 + kMaxR * 2 + kMaxR * 2 + kMaxR + kMaxR / 32 +
-                             kMaxB + kMaxR + kMaxB * 2 + (kMaxB + 1) * 4 + 16;
+constexpr int kSmemPerWarp = kMaxB * 6 * 4 + (kMaxB + 1) * 4 + kMaxB * 2 + kMaxB + kMaxR + 12;
 
 OG_D WarpSmem carve_smem(unsigned char* base) {
   WarpSmem s;
   unsigned char* p = base;
   s.fc = reinterpret_cast<float*>(p); p += kMaxB * 6 * 4;
-  s.lambda = reinterpret_cast<float*>(p); p += kMaxR * 4;
   s.cnt = reinterpret_cast<int*>(p); p += (kMaxB + 1) * 4;
-  s.seq = reinterpret_cast<uint16_t*>(p); p += kMaxR * 2;
-  s.rowbod = reinterpret_cast<uint16_t*>(p); p += kMaxR * 2;
   s.stack = reinterpret_cast<int16_t*>(p); p += kMaxB * 2;
-  s.lvl = p; p += kMaxR;
-  s.wlev = p; p += kMaxR / 32;
   s.tag = p; p += kMaxB;
   s.jtag = p; p += kMaxR;
   return s;
