@@ -41,18 +41,32 @@ __device__ __forceinline__ int slot_world(const int* order, int first, int count
   return w < nw ? w : -1;
 }
 
-__global__ void __launch_bounds__(128) world_setup_kernel(BatchDev d, const int* order, int first, int count,
-                                                          int step, StepOptions opt) {
+__global__ void __launch_bounds__(128) world_collide_kernel(BatchDev d, const int* order, int first, int count,
+                                                            int step, StepOptions opt) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & 31;
   const int w = slot_world(order, first, count, d.n_worlds);
   if (w < 0) return;
-  if (d.world[w].nb > kMaxB) {
-    if (lane == 0) { atomicOr(&d.status[w], ST_TOO_LARGE); d.nrows[w] = 0; d.nislands[w] = 0; }
+  if (d.world[w].nb > kMaxB || d.world[w].ng > kMaxB + 8) {
+    if (lane == 0) { atomicOr(&d.status[w], ST_TOO_LARGE); d.ncontacts[w] = 0; }
+    return;
+  }
+  const WarpSmem S = carve_collide_smem(smem_raw + (size_t)(threadIdx.x >> 5) * kCollideSmemPerWarp);
+  world_collide(d, w, step, S, lane, opt);
+}
+
+__global__ void __launch_bounds__(128) world_setup_kernel(BatchDev d, const int* order, int first, int count,
+                                                          StepOptions opt) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lane = threadIdx.x & 31;
+  const int w = slot_world(order, first, count, d.n_worlds);
+  if (w < 0) return;
+  if (d.world[w].nb > kMaxB || d.world[w].ng > kMaxB + 8) {
+    if (lane == 0) { d.nrows[w] = 0; d.nislands[w] = 0; }
     return;
   }
   const WarpSmem S = carve_smem(smem_raw + (size_t)(threadIdx.x >> 5) * kSmemPerWarp);
-  world_setup(d, w, step, S, lane, opt);
+  world_setup(d, w, S, lane, opt);
 }
 
 __global__ void __launch_bounds__(128) world_solve_kernel(BatchDev d, const int* order, int first, int count,
@@ -172,8 +186,9 @@ struct odegpuBatch {
     const BatchDev d = dev();
     const int* ord = (use_order && order.p) ? order.p : nullptr;
     for (int s = 0; s < n_steps; ++s) {
-      world_setup_kernel<<<blocks, wpb * 32, (size_t)wpb * kSmemPerWarp, stream>>>(d, ord, first, count,
-                                                                                 step_counter + s, opt);
+      world_collide_kernel<<<blocks, wpb * 32, (size_t)wpb * kCollideSmemPerWarp, stream>>>(
+          d, ord, first, count, step_counter + s, opt);
+      world_setup_kernel<<<blocks, wpb * 32, (size_t)wpb * kSmemPerWarp, stream>>>(d, ord, first, count, opt);
       world_solve_kernel<<<blocks, wpb * 32, (size_t)wpb * kSorSmemPerWarp, stream>>>(d, ord, first, count,
                                                                                     opt);
     }
@@ -184,6 +199,9 @@ struct odegpuBatch {
 };
 
 static int configure_kernels(int wpb) {
+  if (cudaFuncSetAttribute(world_collide_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)(wpb * kCollideSmemPerWarp)) != cudaSuccess)
+    return -1;
   if (cudaFuncSetAttribute(world_setup_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)(wpb * kSmemPerWarp)) != cudaSuccess)
     return -1;

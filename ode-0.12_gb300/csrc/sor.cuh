@@ -19,23 +19,29 @@ namespace og {
 struct SorSmem {
   float* fc;          // [kMaxB*6]   constraint force accumulator (cforce)
   float* lambda;      // [kMaxR]
-  uint32_t* seq;      // [kMaxR]     sweep order: row | level << 16
+  uint16_t* seq;      // [kMaxR]     sweep order (rows)
   uint16_t* lstart;   // [kMaxR+2]   per-level counts, then first exec slot
   uint16_t* exec;     // [kMaxR]     rows bucketed by level
+  uint16_t* chunk;    // [kMaxR+32]  level of each sweep position while
+                      //             scheduling, then the chunk list:
+                      //             first exec slot | (count - 1) << 11
   int* last;          // [kMaxB]     last level that touched each body
 };
+// 13.8 KB: 16 warps per SM, matching the register limit of the kernel
 constexpr int kSorSmemPerWarp =
-    kMaxB * 6 * 4 + kMaxR * 4 + kMaxR * 4 + (kMaxR + 2) * 2 + kMaxR * 2 + kMaxB * 4 + 16;
+    align16(kMaxB * 6 * 4 + kMaxR * 4 + kMaxR * 2 + (kMaxR + 2) * 2 + kMaxR * 2 + (kMaxR + 32) * 2 + kMaxB * 4 + 16);
+static_assert(kSorSmemPerWarp % 16 == 0, "per-warp slices must stay aligned");
 
 OG_D SorSmem carve_sor(unsigned char* base) {
   SorSmem s;
   unsigned char* p = base;
   s.fc = reinterpret_cast<float*>(p); p += kMaxB * 6 * 4;
   s.lambda = reinterpret_cast<float*>(p); p += kMaxR * 4;
-  s.seq = reinterpret_cast<uint32_t*>(p); p += kMaxR * 4;
   s.last = reinterpret_cast<int*>(p); p += kMaxB * 4;
+  s.seq = reinterpret_cast<uint16_t*>(p); p += kMaxR * 2;
   s.lstart = reinterpret_cast<uint16_t*>(p); p += (kMaxR + 2) * 2;
-  s.exec = reinterpret_cast<uint16_t*>(p);
+  s.exec = reinterpret_cast<uint16_t*>(p); p += kMaxR * 2;
+  s.chunk = reinterpret_cast<uint16_t*>(p);
   return s;
 }
 
@@ -63,7 +69,7 @@ OG_D int sor_schedule(const float* rows, int nb, const SorSmem& S, int M, int la
     const int pos = base + lane;
     int b1 = -3, b2 = -4, level = 0;
     if (pos < M) {
-      row_bodies(rows, S.seq[pos] & 0xffff, b1, b2);
+      row_bodies(rows, S.seq[pos], b1, b2);
       level = S.last[b1] + 1;
       if (b2 >= 0) level = max(level, S.last[b2] + 1);
     }
@@ -79,7 +85,7 @@ OG_D int sor_schedule(const float* rows, int nb, const SorSmem& S, int M, int la
     }
     __syncwarp();
     if (pos < M) {
-      S.seq[pos] = (S.seq[pos] & 0xffffu) | ((unsigned)level << 16);
+      S.chunk[pos] = (uint16_t)level;
       add_u16(S.lstart, level, 1u);
       // rows that share a body have strictly increasing levels along the
       // sequence, so the per-body maximum is the carry for later windows
@@ -106,12 +112,11 @@ OG_D int sor_schedule(const float* rows, int nb, const SorSmem& S, int M, int la
   // scatter (order inside a level does not matter: its rows are independent);
   // lstart[l] is advanced as slots are taken and restored afterwards
   for (int pos = lane; pos < M; pos += 32) {
-    const unsigned v = S.seq[pos];
-    const int l = (int)(v >> 16);
+    const int l = S.chunk[pos];
     unsigned* w = reinterpret_cast<unsigned*>(S.lstart + (l & ~1));
     const unsigned old = atomicAdd(w, 1u << (16 * (l & 1)));
     const int slot = (int)((old >> (16 * (l & 1))) & 0xffffu);
-    S.exec[slot] = (uint16_t)(v & 0xffffu);
+    S.exec[slot] = S.seq[pos];
   }
   __syncwarp();
   // lstart[l] now holds the end of level l = the start of level l+1: shift back
@@ -124,7 +129,28 @@ OG_D int sor_schedule(const float* rows, int nb, const SorSmem& S, int M, int la
   }
   if (lane == 0) S.lstart[0] = 0;
   __syncwarp();
-  return nlev;
+  // chunk list: each level split into runs of at most 32 rows
+  {
+    int carry = 0;
+    for (int base = 0; base < nlev; base += 32) {
+      const int l = base + lane;
+      int a = 0, n = 0, c = 0;
+      if (l < nlev) {
+        a = S.lstart[l];
+        n = S.lstart[l + 1] - a;
+        c = (n + 31) >> 5;
+      }
+      const int incl = warp_incl_scan(c, lane);
+      int k = carry + incl - c;
+      for (int q = 0; q < c; ++q, ++k) {
+        const int cnt = min(32, n - 32 * q);
+        S.chunk[k] = (uint16_t)((a + 32 * q) | ((cnt - 1) << 11));
+      }
+      carry += __shfl_sync(kFull, incl, 31);
+    }
+    __syncwarp();
+    return carry;   // number of chunks
+  }
 }
 
 // One projected Gauss-Seidel row update (quickstep.cpp:484-582) on row data
@@ -138,11 +164,13 @@ OG_D void sor_row(const float4 (&rw)[8], int r, const SorSmem& S) {
   float* fc1 = S.fc + 6 * b1;
   const float old = S.lambda[r];
   float delta = bb - old * Ad;
-  delta -= fc1[0] * J[0] + fc1[1] * J[1] + fc1[2] * J[2] + fc1[3] * J[3] + fc1[4] * J[4] + fc1[5] * J[5];
+  // the 6-term dot products are summed pairwise (shorter dependency chains
+  // than the reference's left-to-right sums; same terms)
+  delta -= (fc1[0] * J[0] + fc1[1] * J[1]) + (fc1[2] * J[2] + fc1[3] * J[3]) + (fc1[4] * J[4] + fc1[5] * J[5]);
   float* fc2 = nullptr;
   if (b2 != -1) {
     fc2 = S.fc + 6 * b2;
-    delta -= fc2[0] * J[6] + fc2[1] * J[7] + fc2[2] * J[8] + fc2[3] * J[9] + fc2[4] * J[10] + fc2[5] * J[11];
+    delta -= (fc2[0] * J[6] + fc2[1] * J[7]) + (fc2[2] * J[8] + fc2[3] * J[9]) + (fc2[4] * J[10] + fc2[5] * J[11]);
   }
   float hi_act, lo_act;
   if (findex != -1) {
@@ -194,7 +222,7 @@ OG_D unsigned sor_world(const float* rows, const int* rstart, int nb, int M, int
       if (r < re) {
         const int nonnegb = (r - rs) - negb;
         const int p = neg ? rs + negb : re - 1 - nonnegb;
-        S.seq[p] = (uint32_t)r;
+        S.seq[p] = (uint16_t)r;
       }
       negc += __popc(bal);
     }
@@ -205,7 +233,7 @@ OG_D unsigned sor_world(const float* rows, const int* rstart, int nb, int M, int
     const int m = rstart[isl + 1] - rstart[isl];
     if (m > 0) total_draws += (unsigned)(n_shuffles * (m - 1));
   }
-  int nlev = 0;
+  int nchunk = 0;
   for (int it = 0; it < iters; ++it) {
     if ((it & 7) == 0) {
       const int round = it >> 3;
@@ -218,11 +246,11 @@ OG_D unsigned sor_world(const float* rows, const int* rstart, int nb, int M, int
         const int incl = warp_incl_scan(draws, lane);
         if (isl < nisl && m > 1) {
           unsigned s = lcg_jump(seed, prefix + (unsigned)(incl - draws) + (unsigned)(round * (m - 1)));
-          uint32_t* sq = S.seq + rstart[isl];
+          uint16_t* sq = S.seq + rstart[isl];
           for (int q = 1; q < m; ++q) {
             s = lcg_next(s);
             const int sw = rand_int_from(s, q + 1);
-            const uint32_t t = sq[q];
+            const uint16_t t = sq[q];
             sq[q] = sq[sw];
             sq[sw] = t;
           }
@@ -230,39 +258,32 @@ OG_D unsigned sor_world(const float* rows, const int* rstart, int nb, int M, int
         prefix += (unsigned)__shfl_sync(kFull, incl, 31);
       }
       __syncwarp();
-      nlev = sor_schedule(rows, nb, S, M, lane);
+      nchunk = sor_schedule(rows, nb, S, M, lane);
     }
-    // sweep: levels in order, chunks of 32 rows, next chunk prefetched
-    int l = 0, off = 0;
-    while (l < nlev && S.lstart[l + 1] == S.lstart[l]) ++l;
-    if (l >= nlev) continue;
-    float4 cur[8], nxt[8];
-    int cur_r = -1;
+    // sweep: chunks in level order; the next chunk's rows are loaded while
+    // the current one computes (two register buffers used in turn)
+    float4 ra[8], rb[8];
+    int r_a = -1, r_b = -1;
     {
-      const int slot = S.lstart[l] + off + lane;
-      if (slot < S.lstart[l + 1]) { cur_r = S.exec[slot]; load_row(rows, cur_r, cur); }
+      const unsigned c0 = S.chunk[0];
+      if (lane <= (int)(c0 >> 11)) { r_a = S.exec[(c0 & 0x7ffu) + lane]; load_row(rows, r_a, ra); }
     }
-    for (;;) {
-      // next chunk position
-      int nl = l, noff = off + 32;
-      if (S.lstart[nl] + noff >= S.lstart[nl + 1]) {
-        nl = l + 1;
-        noff = 0;
-        while (nl < nlev && S.lstart[nl + 1] == S.lstart[nl]) ++nl;
+    for (int k = 0; k < nchunk; k += 2) {
+      r_b = -1;
+      if (k + 1 < nchunk) {
+        const unsigned c1 = S.chunk[k + 1];
+        if (lane <= (int)(c1 >> 11)) { r_b = S.exec[(c1 & 0x7ffu) + lane]; load_row(rows, r_b, rb); }
       }
-      int nxt_r = -1;
-      if (nl < nlev) {
-        const int slot = S.lstart[nl] + noff + lane;
-        if (slot < S.lstart[nl + 1]) { nxt_r = S.exec[slot]; load_row(rows, nxt_r, nxt); }
-      }
-      if (cur_r >= 0) sor_row(cur, cur_r, S);
+      if (r_a >= 0) sor_row(ra, r_a, S);
       __syncwarp();
-      if (nl >= nlev) break;
-      l = nl;
-      off = noff;
-      cur_r = nxt_r;
-#pragma unroll
-      for (int q = 0; q < 8; ++q) cur[q] = nxt[q];
+      if (k + 1 >= nchunk) break;
+      r_a = -1;
+      if (k + 2 < nchunk) {
+        const unsigned c2 = S.chunk[k + 2];
+        if (lane <= (int)(c2 >> 11)) { r_a = S.exec[(c2 & 0x7ffu) + lane]; load_row(rows, r_a, ra); }
+      }
+      if (r_b >= 0) sor_row(rb, r_b, S);
+      __syncwarp();
     }
   }
   return lcg_jump(seed, total_draws);

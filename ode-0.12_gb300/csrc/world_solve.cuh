@@ -392,20 +392,22 @@ struct StepOptions {
 
 // Setup kernel body: phases 0-5. Leaves the rows, island table, row count
 // and island count of the step in global memory for world_solve.
-OG_D void world_setup(const BatchDev& d, int w, int step, const WarpSmem& S, int lane,
-                      const StepOptions& opt) {
+OG_D void world_collide(const BatchDev& d, int w, int step, const WarpSmem& S, int lane,
+                        const StepOptions& opt) {
   const WorldDesc D = d.world[w];
   if (!opt.host_forces) phase_controls(d, D, step, lane);
-  int nc;
   if (opt.collide) {
-    nc = phase_collide(d, D, w, lane);
+    const int nc = phase_collide(d, D, w, S, lane);
     if (lane == 0) d.ncontacts[w] = nc;
-  } else {
-    nc = d.ncontacts[w];
   }
   __syncwarp();
   phase_body_prologue(d, D, lane);
   __syncwarp();
+}
+
+OG_D void world_setup(const BatchDev& d, int w, const WarpSmem& S, int lane, const StepOptions& opt) {
+  const WorldDesc D = d.world[w];
+  const int nc = d.ncontacts[w];
   int M = 0, nisl = 0;
   if (D.njp + nc > kMaxR) {
     if (lane == 0) atomicOr(&d.status[w], ST_TOO_LARGE);

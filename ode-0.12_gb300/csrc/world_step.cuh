@@ -28,24 +28,50 @@ constexpr unsigned kFull = 0xffffffffu;
 constexpr int kMaxB = 64;      // bodies per world handled on chip
 constexpr int kMaxR = 1024;    // constraint rows per world handled on chip
 
-// Per-warp shared-memory working set of the setup phases.
+// Per-warp shared-memory working sets of the collide and build kernels.
 struct WarpSmem {
-  float* fc;          // [kMaxB*6]  tmp1 = invM fe + v/h per body
-  int* cnt;           // [kMaxB+1]  contacts per body
-  int16_t* stack;     // [kMaxB]    island search stack
-  uint8_t* tag;       // [kMaxB]    body tags for the island search
-  uint8_t* jtag;      // [kMaxR]    joint tags for the island search
+  // build kernel
+  float* fc;          // [kMaxB*6]   tmp1 = invM fe + v/h per body
+  int* cnt;           // [kMaxB+1]   contacts per body, then list cursors
+  uint16_t* adj_start;// [kMaxB+1]   body joint lists (CSR)
+  uint16_t* adj;      // [2*kMaxR]   joint ordinals, ODE list order
+  int8_t* jb1;        // [kMaxR]     bodies of each joint ordinal
+  int8_t* jb2;        // [kMaxR]
+  uint16_t* jlist;    // [kMaxR]     joints in island order (bit 15: island start)
+  int16_t* stack;     // [kMaxB]     island search stack
+  uint8_t* tag;       // [kMaxB]     body tags for the island search
+  uint8_t* jtag;      // [kMaxR]     joint tags for the island search
+  // collide kernel
+  uint16_t* cand;     // [kMaxPairs] candidate pairs that pass the bound test
 };
-constexpr int kSmemPerWarp = kMaxB * 6 * 4 + (kMaxB + 1) * 4 + kMaxB * 2 + kMaxB + kMaxR + 12;
+constexpr int kMaxPairs = (kMaxB + 8) * (kMaxB + 7) / 2;   // geoms: bodies + a few static
+// Per-warp sizes are rounded up to 16 bytes so that every warp's slice (and
+// the float/int arrays at its start) stays aligned.
+constexpr int align16(int n) { return (n + 15) & ~15; }
+constexpr int kSmemPerWarp = align16(kMaxB * 6 * 4 + (kMaxB + 1) * 4 + (kMaxB + 1) * 2 + 2 * kMaxR * 2 +
+                                     kMaxR * 2 + kMaxR * 2 + kMaxB * 2 + kMaxB + kMaxR + 32);
+constexpr int kCollideSmemPerWarp = align16(kMaxPairs * 2 + 16);
+static_assert(kSmemPerWarp % 16 == 0 && kCollideSmemPerWarp % 16 == 0, "per-warp slices must stay aligned");
 
 OG_D WarpSmem carve_smem(unsigned char* base) {
   WarpSmem s;
   unsigned char* p = base;
   s.fc = reinterpret_cast<float*>(p); p += kMaxB * 6 * 4;
   s.cnt = reinterpret_cast<int*>(p); p += (kMaxB + 1) * 4;
+  s.adj = reinterpret_cast<uint16_t*>(p); p += 2 * kMaxR * 2;
+  s.jlist = reinterpret_cast<uint16_t*>(p); p += kMaxR * 2;
+  s.adj_start = reinterpret_cast<uint16_t*>(p); p += (kMaxB + 1) * 2 + 2;
   s.stack = reinterpret_cast<int16_t*>(p); p += kMaxB * 2;
+  s.jb1 = reinterpret_cast<int8_t*>(p); p += kMaxR;
+  s.jb2 = reinterpret_cast<int8_t*>(p); p += kMaxR;
   s.tag = p; p += kMaxB;
   s.jtag = p; p += kMaxR;
+  s.cand = nullptr;
+  return s;
+}
+OG_D WarpSmem carve_collide_smem(unsigned char* base) {
+  WarpSmem s{};
+  s.cand = reinterpret_cast<uint16_t*>(base);
   return s;
 }
 
@@ -101,46 +127,67 @@ OG_D bool jointed(const BatchDev& d, const WorldDesc& D, int w, int b1, int b2) 
   return false;
 }
 
-// Phase 1: canonical pair loop. Returns the number of contacts stored.
-OG_D int phase_collide(const BatchDev& d, const WorldDesc& D, int w, int lane) {
+OG_D void unrank_pair(int p, int ng, int& i, int& k) {
+  // p -> (i, k), i < k, row-major over i
+  const float tn = 2.f * ng - 1.f;
+  i = (int)floorf((tn - sqrtf(fmaxf(tn * tn - 8.f * p, 0.f))) * 0.5f);
+  i = max(0, min(i, ng - 2));
+  while (i > 0 && i * (2 * ng - i - 1) / 2 > p) --i;
+  while ((i + 1) * (2 * ng - (i + 1) - 1) / 2 <= p) ++i;
+  k = p - i * (2 * ng - i - 1) / 2 + i + 1;
+}
+
+// Phase 1: canonical pair loop. A first pass keeps, in pair order, the pairs
+// that the dCollide early-outs and a conservative bounding-sphere test cannot
+// reject; the colliders then run densely over those candidates and a warp
+// prefix scan writes the contacts in pair order. Returns the contact count.
+OG_D int phase_collide(const BatchDev& d, const WorldDesc& D, int w, const WarpSmem& S, int lane) {
   const int ng = D.ng;
   const int npairs = ng * (ng - 1) / 2;
-  int nc = 0;
+  int ncand = 0;
   for (int base = 0; base < npairs; base += 32) {
     const int p = base + lane;
-    int cnt = 0;
-    Contact cc[8];
-    int bi = -1, bk = -1, surf = 0;
+    bool keep = false;
     if (p < npairs) {
-      // unrank p -> (i, k), i < k, row-major over i
-      const float tn = 2.f * ng - 1.f;
-      int i = (int)floorf((tn - sqrtf(fmaxf(tn * tn - 8.f * p, 0.f))) * 0.5f);
-      i = max(0, min(i, ng - 2));
-      while (i > 0 && i * (2 * ng - i - 1) / 2 > p) --i;
-      while ((i + 1) * (2 * ng - (i + 1) - 1) / 2 <= p) ++i;
-      const int k = p - i * (2 * ng - i - 1) / 2 + i + 1;
+      int i, k;
+      unrank_pair(p, ng, i, k);
       const int gi = D.geom_off + i, gk = D.geom_off + k;
-      bi = d.gbody[gi];
-      bk = d.gbody[gk];
-      bool skip = (bi < 0 && bk < 0) || (bi == bk);
-      if (!skip && bi >= 0 && bk >= 0 && jointed(d, D, w, bi, bk)) skip = true;
-      if (!skip) {
+      const int bi = d.gbody[gi], bk = d.gbody[gk];
+      keep = !((bi < 0 && bk < 0) || (bi == bk));
+      if (keep) {
         const float ri = d.gbound[gi], rk = d.gbound[gk];
         if (isfinite(ri) && isfinite(rk)) {
           const float4 pi4 = d.pos[D.body_off + bi], pk4 = d.pos[D.body_off + bk];
           const float dx = pi4.x - pk4.x, dy = pi4.y - pk4.y, dz = pi4.z - pk4.z;
           const float lim = (ri + rk) * 1.001f + 1e-5f;
-          if (dx * dx + dy * dy + dz * dz > lim * lim) skip = true;
+          if (dx * dx + dy * dy + dz * dz > lim * lim) keep = false;
         }
       }
-      if (!skip) {
-        GeomView vi, vk;
-        geom_view(d, D, i, vi);
-        geom_view(d, D, k, vk);
-        cnt = collide_primitive(vi, vk, (unsigned)D.max_contacts, cc);
-        const int si = d.gsurf[gi], sk = d.gsurf[gk];
-        surf = si > sk ? si : sk;
-      }
+      if (keep && bi >= 0 && bk >= 0 && jointed(d, D, w, bi, bk)) keep = false;
+    }
+    const unsigned bal = __ballot_sync(kFull, keep);
+    if (keep) S.cand[ncand + __popc(bal & ((1u << lane) - 1u))] = (uint16_t)p;
+    ncand += __popc(bal);
+  }
+  __syncwarp();
+  int nc = 0;
+  for (int base = 0; base < ncand; base += 32) {
+    const int ci = base + lane;
+    int cnt = 0;
+    Contact cc[8];
+    int bi = -1, bk = -1, surf = 0;
+    if (ci < ncand) {
+      int i, k;
+      unrank_pair(S.cand[ci], ng, i, k);
+      const int gi = D.geom_off + i, gk = D.geom_off + k;
+      bi = d.gbody[gi];
+      bk = d.gbody[gk];
+      GeomView vi, vk;
+      geom_view(d, D, i, vi);
+      geom_view(d, D, k, vk);
+      cnt = collide_primitive(vi, vk, (unsigned)D.max_contacts, cc);
+      const int si = d.gsurf[gi], sk = d.gsurf[gk];
+      surf = si > sk ? si : sk;
     }
     const int incl = warp_incl_scan(cnt, lane);
     const int excl = incl - cnt;
@@ -179,69 +226,68 @@ OG_D void joint_bodies(const BatchDev& d, const WorldDesc& D, int ord, int& b1, 
   }
 }
 
-// Phase 3: adjacency in ODE list order + DFS islands. Writes jlist (joint
-// ordinals in island order; bit 30 marks the first joint of an island) and
-// returns the number of joints placed; *n_isl receives the island count.
-// nc_lists: contacts to merge into the body lists (0 when the host supplied
-// complete lists in padj); nj_all: persistent + contact joints (tag range).
+// Phase 3: adjacency in ODE list order + DFS islands (util.cpp:384-521), all
+// in shared memory. Body lists hold contacts newest first, then persistent
+// joints newest first (nc = 0 when the host supplied complete lists in padj).
+// Writes jlist (joint ordinals in island order; bit 15 marks an island's first
+// joint) and island_jstart; returns the number of joints placed.
 OG_D int phase_islands(const BatchDev& d, const WorldDesc& D, int w, int nc, int nj_all,
                        const WarpSmem& S, int lane, int* n_isl) {
   const int nb = D.nb;
-  const int jl_off = D.joint_off + D.contact_off;
-  const int adj_off = 2 * jl_off;
-  int* adj_start = d.adj_start + D.body_off + w;
-  // counts: contacts per body + persistent joints per body
-  for (int b = lane; b < nb; b += 32) S.cnt[b] = 0;
+  const int* pstart = d.padj_start + D.body_off + w;
+  // bodies of every joint ordinal
+  for (int j = lane; j < nj_all; j += 32) {
+    int b1, b2;
+    joint_bodies(d, D, j, b1, b2);
+    S.jb1[j] = (int8_t)b1;
+    S.jb2[j] = (int8_t)b2;
+    S.jtag[j] = 0;
+  }
+  for (int b = lane; b < nb; b += 32) { S.cnt[b] = 0; S.tag[b] = 0; }
   __syncwarp();
   for (int c = lane; c < nc; c += 32) {
-    const DevContact& ct = d.contacts[D.contact_off + c];
-    atomicAdd(&S.cnt[ct.b1], 1);
-    if (ct.b2 >= 0) atomicAdd(&S.cnt[ct.b2], 1);
+    atomicAdd(&S.cnt[S.jb1[D.njp + c]], 1);
+    if (S.jb2[D.njp + c] >= 0) atomicAdd(&S.cnt[S.jb2[D.njp + c]], 1);
   }
   __syncwarp();
-  const int* pstart = d.padj_start + D.body_off + w;
   {
     int carry = 0;
     for (int base = 0; base < nb; base += 32) {
       const int b = base + lane;
       const int v = (b < nb) ? S.cnt[b] + (pstart[b + 1] - pstart[b]) : 0;
       const int incl = warp_incl_scan(v, lane);
-      if (b < nb) adj_start[b] = carry + incl - v;
+      if (b < nb) S.adj_start[b] = (uint16_t)(carry + incl - v);
       carry += __shfl_sync(kFull, incl, 31);
     }
-    if (lane == 0) adj_start[nb] = carry;
+    if (lane == 0) S.adj_start[nb] = (uint16_t)carry;
   }
   __syncwarp();
-  // fill: contacts newest first, then persistent joints newest first
+  // fill: each lane owns bodies b = lane (mod 32) and walks the contacts
+  // newest first, then copies its persistent list
   for (int b = lane; b < nb; b += 32) {
-    int wp = adj_off + adj_start[b];
-    for (int c = nc - 1; c >= 0; --c) {
-      const DevContact& ct = d.contacts[D.contact_off + c];
-      if (ct.b1 == b || ct.b2 == b) d.adj[wp++] = D.njp + c;
-    }
-    for (int k = pstart[b]; k < pstart[b + 1]; ++k) d.adj[wp++] = d.padj[k];
+    int wp = S.adj_start[b];
+    for (int c = nc - 1; c >= 0; --c)
+      if (S.jb1[D.njp + c] == b || S.jb2[D.njp + c] == b) S.adj[wp++] = (uint16_t)(D.njp + c);
+    for (int k = pstart[b]; k < pstart[b + 1]; ++k) S.adj[wp++] = (uint16_t)d.padj[k];
   }
-  const int nj = nj_all;
-  for (int b = lane; b < nb; b += 32) S.tag[b] = 0;
-  for (int j = lane; j < nj; j += 32) S.jtag[j] = 0;
   __syncwarp();
   int jcount = 0, nisl = 0;
   if (lane == 0) {
+    int* istart = d.island_jstart + D.body_off + w;
     for (int bb = nb - 1; bb >= 0; --bb) {
       if (S.tag[bb]) continue;
       S.tag[bb] = 1;
       const int jstart = jcount;
       int sp = 0, b = bb;
       for (;;) {
-        const int e = adj_start[b + 1];
-        for (int k = adj_start[b]; k < e; ++k) {
-          const int j = d.adj[adj_off + k];
+        const int e = S.adj_start[b + 1];
+        for (int k = S.adj_start[b]; k < e; ++k) {
+          const int j = S.adj[k];
           if (S.jtag[j]) continue;
           S.jtag[j] = 1;
-          d.jlist[jl_off + jcount] = j | (jcount == jstart ? (1 << 30) : 0);
+          S.jlist[jcount] = (uint16_t)(j | (jcount == jstart ? 0x8000 : 0));
           ++jcount;
-          int b1, b2;
-          joint_bodies(d, D, j, b1, b2);
+          const int b1 = S.jb1[j], b2 = S.jb2[j];
           const int other = (b1 == b) ? b2 : b1;
           if (other >= 0 && !S.tag[other]) {
             S.tag[other] = 1;
@@ -251,15 +297,19 @@ OG_D int phase_islands(const BatchDev& d, const WorldDesc& D, int w, int nc, int
         if (sp == 0) break;
         b = S.stack[--sp];
       }
-      if (jcount > jstart) {
-        d.island_jstart[D.body_off + w + nisl] = jstart;
-        ++nisl;
-      }
+      if (jcount > jstart) istart[nisl++] = jstart;
     }
-    d.island_jstart[D.body_off + w + nisl] = jcount;
+    istart[nisl] = jcount;
   }
   jcount = __shfl_sync(kFull, jcount, 0);
   nisl = __shfl_sync(kFull, nisl, 0);
+  // publish the joint order for the row phase
+  const int jl_off = D.joint_off + D.contact_off;
+  __syncwarp();
+  for (int k = lane; k < jcount; k += 32) {
+    const int v = S.jlist[k];
+    d.jlist[jl_off + k] = (v & 0x7fff) | ((v & 0x8000) ? (1 << 30) : 0);
+  }
   __syncwarp();
   *n_isl = nisl;
   return jcount;
