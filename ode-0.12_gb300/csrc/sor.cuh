@@ -17,8 +17,10 @@
 namespace og {
 
 struct SorSmem {
-  float* fc;          // [kMaxB*6]   constraint force accumulator (cforce)
-  float* lambda;      // [kMaxR]
+  float* fc;          // [(kMaxB+1)*6] constraint force accumulator (cforce);
+                      //             slot kMaxB stays zero (second body of
+                      //             one-body rows and idle lanes)
+  float* lambda;      // [kMaxR+1]   entry kMaxR: idle lanes
   uint16_t* seq;      // [kMaxR]     sweep order (rows)
   uint16_t* lstart;   // [kMaxR+2]   per-level counts, then first exec slot
   uint16_t* exec;     // [kMaxR]     rows bucketed by level
@@ -28,15 +30,15 @@ struct SorSmem {
   int* last;          // [kMaxB]     last level that touched each body
 };
 // 13.8 KB: 16 warps per SM, matching the register limit of the kernel
-constexpr int kSorSmemPerWarp =
-    align16(kMaxB * 6 * 4 + kMaxR * 4 + kMaxR * 2 + (kMaxR + 2) * 2 + kMaxR * 2 + (kMaxR + 32) * 2 + kMaxB * 4 + 16);
+constexpr int kSorSmemPerWarp = align16((kMaxB + 1) * 6 * 4 + (kMaxR + 4) * 4 + kMaxR * 2 + (kMaxR + 2) * 2 +
+                                        kMaxR * 2 + (kMaxR + 32) * 2 + kMaxB * 4 + 16);
 static_assert(kSorSmemPerWarp % 16 == 0, "per-warp slices must stay aligned");
 
 OG_D SorSmem carve_sor(unsigned char* base) {
   SorSmem s;
   unsigned char* p = base;
-  s.fc = reinterpret_cast<float*>(p); p += kMaxB * 6 * 4;
-  s.lambda = reinterpret_cast<float*>(p); p += kMaxR * 4;
+  s.fc = reinterpret_cast<float*>(p); p += (kMaxB + 1) * 6 * 4;
+  s.lambda = reinterpret_cast<float*>(p); p += (kMaxR + 4) * 4;
   s.last = reinterpret_cast<int*>(p); p += kMaxB * 4;
   s.seq = reinterpret_cast<uint16_t*>(p); p += kMaxR * 2;
   s.lstart = reinterpret_cast<uint16_t*>(p); p += (kMaxR + 2) * 2;
@@ -154,44 +156,51 @@ OG_D int sor_schedule(const float* rows, int nb, const SorSmem& S, int M, int la
 }
 
 // One projected Gauss-Seidel row update (quickstep.cpp:484-582) on row data
-// held in registers; fc and lambda live in shared memory.
+// held in registers; fc and lambda live in shared memory. Written without
+// branches so the lanes of a chunk never diverge: a missing second body reads
+// the zero slot kMaxB (its J and iMJ halves are zero) and is not written back,
+// and the friction bound is selected rather than branched on.
 OG_D void sor_row(const float4 (&rw)[8], int r, const SorSmem& S) {
   const float* J = reinterpret_cast<const float*>(&rw[0]);
   const float* iMJ = reinterpret_cast<const float*>(&rw[3]);
   const float bb = rw[6].x, Ad = rw[6].y, lo = rw[6].z, hi = rw[6].w;
   const int findex = __float_as_int(rw[7].x);
   const int b1 = __float_as_int(rw[7].y), b2 = __float_as_int(rw[7].z);
+  const bool two = b2 >= 0;
   float* fc1 = S.fc + 6 * b1;
+  float* fc2 = S.fc + 6 * (two ? b2 : kMaxB);
   const float old = S.lambda[r];
+  const float lf = S.lambda[findex >= 0 ? findex : kMaxR];
+  const float f10 = fc1[0], f11 = fc1[1], f12 = fc1[2], f13 = fc1[3], f14 = fc1[4], f15 = fc1[5];
+  const float f20 = fc2[0], f21 = fc2[1], f22 = fc2[2], f23 = fc2[3], f24 = fc2[4], f25 = fc2[5];
   float delta = bb - old * Ad;
   // the 6-term dot products are summed pairwise (shorter dependency chains
   // than the reference's left-to-right sums; same terms)
-  delta -= (fc1[0] * J[0] + fc1[1] * J[1]) + (fc1[2] * J[2] + fc1[3] * J[3]) + (fc1[4] * J[4] + fc1[5] * J[5]);
-  float* fc2 = nullptr;
-  if (b2 != -1) {
-    fc2 = S.fc + 6 * b2;
-    delta -= (fc2[0] * J[6] + fc2[1] * J[7]) + (fc2[2] * J[8] + fc2[3] * J[9]) + (fc2[4] * J[10] + fc2[5] * J[11]);
-  }
-  float hi_act, lo_act;
-  if (findex != -1) {
-    hi_act = fabsf(hi * S.lambda[findex]);
-    lo_act = -hi_act;
-  } else {
-    hi_act = hi;
-    lo_act = lo;
-  }
+  delta -= (f10 * J[0] + f11 * J[1]) + (f12 * J[2] + f13 * J[3]) + (f14 * J[4] + f15 * J[5]);
+  delta -= (f20 * J[6] + f21 * J[7]) + (f22 * J[8] + f23 * J[9]) + (f24 * J[10] + f25 * J[11]);
+  const float hf = fabsf(hi * lf);
+  const float hi_act = findex >= 0 ? hf : hi;
+  const float lo_act = findex >= 0 ? -hf : lo;
   const float nl = old + delta;
-  float lam;
-  if (nl < lo_act) { delta = lo_act - old; lam = lo_act; }
-  else if (nl > hi_act) { delta = hi_act - old; lam = hi_act; }
-  else lam = nl;
-  S.lambda[r] = lam;
-  fc1[0] += delta * iMJ[0]; fc1[1] += delta * iMJ[1]; fc1[2] += delta * iMJ[2];
-  fc1[3] += delta * iMJ[3]; fc1[4] += delta * iMJ[4]; fc1[5] += delta * iMJ[5];
-  if (fc2) {
-    fc2[0] += delta * iMJ[6]; fc2[1] += delta * iMJ[7]; fc2[2] += delta * iMJ[8];
-    fc2[3] += delta * iMJ[9]; fc2[4] += delta * iMJ[10]; fc2[5] += delta * iMJ[11];
+  // the reference keeps delta when no bound is hit and uses bound - old otherwise
+  const bool clamped = (nl < lo_act) || (nl > hi_act);
+  const float lam = fminf(fmaxf(nl, lo_act), hi_act);
+  delta = clamped ? lam - old : delta;
+  S.lambda[r] = clamped ? lam : nl;
+  fc1[0] = f10 + delta * iMJ[0]; fc1[1] = f11 + delta * iMJ[1]; fc1[2] = f12 + delta * iMJ[2];
+  fc1[3] = f13 + delta * iMJ[3]; fc1[4] = f14 + delta * iMJ[4]; fc1[5] = f15 + delta * iMJ[5];
+  if (two) {
+    fc2[0] = f20 + delta * iMJ[6]; fc2[1] = f21 + delta * iMJ[7]; fc2[2] = f22 + delta * iMJ[8];
+    fc2[3] = f23 + delta * iMJ[9]; fc2[4] = f24 + delta * iMJ[10]; fc2[5] = f25 + delta * iMJ[11];
   }
+}
+
+// Row data of an idle lane: no effect (zero J and iMJ, bounds 0, first body is
+// the zero slot, lambda slot kMaxR).
+OG_D void idle_row(float4 (&rw)[8]) {
+#pragma unroll
+  for (int q = 0; q < 7; ++q) rw[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+  rw[7] = make_float4(__int_as_float(-1), __int_as_float(kMaxB), __int_as_float(-1), 0.f);
 }
 
 OG_D void load_row(const float* rows, int r, float4 (&rw)[8]) {
@@ -206,7 +215,9 @@ OG_D void load_row(const float* rows, int r, float4 (&rw)[8]) {
 OG_D unsigned sor_world(const float* rows, const int* rstart, int nb, int M, int nisl, int iters,
                         unsigned seed, const SorSmem& S, int lane) {
   for (int i = lane; i < nb * 6; i += 32) S.fc[i] = 0.f;
+  if (lane < 6) S.fc[kMaxB * 6 + lane] = 0.f;
   for (int i = lane; i < M; i += 32) S.lambda[i] = 0.f;
+  if (lane == 0) S.lambda[kMaxR] = 0.f;
   const int n_shuffles = (iters + 7) / 8;
   // initial order per island: findex == -1 rows first (ascending), the rest
   // from the island's tail backwards (quickstep.cpp:405-425)
@@ -261,28 +272,33 @@ OG_D unsigned sor_world(const float* rows, const int* rstart, int nb, int M, int
       nchunk = sor_schedule(rows, nb, S, M, lane);
     }
     // sweep: chunks in level order; the next chunk's rows are loaded while
-    // the current one computes (two register buffers used in turn)
+    // the current one computes (two register buffers used in turn). Idle lanes
+    // run a no-op row so the warp never diverges.
     float4 ra[8], rb[8];
-    int r_a = -1, r_b = -1;
+    int r_a, r_b;
     {
       const unsigned c0 = S.chunk[0];
+      r_a = kMaxR;
       if (lane <= (int)(c0 >> 11)) { r_a = S.exec[(c0 & 0x7ffu) + lane]; load_row(rows, r_a, ra); }
+      else idle_row(ra);
     }
     for (int k = 0; k < nchunk; k += 2) {
-      r_b = -1;
+      r_b = kMaxR;
       if (k + 1 < nchunk) {
         const unsigned c1 = S.chunk[k + 1];
         if (lane <= (int)(c1 >> 11)) { r_b = S.exec[(c1 & 0x7ffu) + lane]; load_row(rows, r_b, rb); }
+        else idle_row(rb);
       }
-      if (r_a >= 0) sor_row(ra, r_a, S);
+      sor_row(ra, r_a, S);
       __syncwarp();
       if (k + 1 >= nchunk) break;
-      r_a = -1;
+      r_a = kMaxR;
       if (k + 2 < nchunk) {
         const unsigned c2 = S.chunk[k + 2];
         if (lane <= (int)(c2 >> 11)) { r_a = S.exec[(c2 & 0x7ffu) + lane]; load_row(rows, r_a, ra); }
+        else idle_row(ra);
       }
-      if (r_b >= 0) sor_row(rb, r_b, S);
+      sor_row(rb, r_b, S);
       __syncwarp();
     }
   }
