@@ -115,6 +115,29 @@ def algorithmic_bytes(sc, nc, nr, iters=20):
     return float(np.sum(208.0 * nb + 56.0 * nc + 40.0 * nj + nr * (248.0 + 236.0 * iters)))
 
 
+def solve_bytes(nr, iters=20):
+    """Sweep-model bytes of one world_solve_kernel launch: 236 B per
+    row-iteration (J', iMJ, b', Ad', lo, hi, findex, jb, order = 32 words; lambda
+    r/w; lambda[findex]; fc r/w of two bodies)."""
+    return float(np.sum(nr) * 236.0 * iters)
+
+
+SOLVE_PROFILE = os.path.join(ROOT, "profiles", "world_solve_kernel_batched_4096.txt")
+
+
+def solve_traffic_per_row_iter():
+    """DRAM bytes (read + write) per row-iteration of one world_solve_kernel
+    launch, from the committed ncu capture summary (None without it)."""
+    try:
+        with open(SOLVE_PROFILE) as f:
+            for line in f:
+                if line.startswith("dram_bytes_per_row_iteration:"):
+                    return float(line.split(":", 1)[1])
+    except OSError:
+        pass
+    return None
+
+
 def cpu_baseline(sc, n_worlds_sample, n_steps, threads=None):
     """Oracle port (FP64 restatement of ODE's algorithm, oracle/liboracle.so) on
     worlds [0, n_worlds_sample) for n_steps from the initial state, all host
@@ -192,7 +215,10 @@ def run_ours(args):
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
           for _ in range(args.steps)]
     bytes_per_step = []
-    launches = 0
+    solve_bytes_total = 0.0
+    rows_total = 0
+    B.set_timing(True)                # events around each kernel, on the batch stream
+    launches0 = B.launch_count()
     barrier()
     for k in range(args.steps):
         with torch.cuda.stream(stream):
@@ -201,12 +227,16 @@ def run_ours(args):
         B.step(1)
         with torch.cuda.stream(stream):
             ev[k][1].record(stream)
-        launches += 2
         nc, nr, _ = B.counts()        # host read between steps, outside the events
         bytes_per_step.append(algorithmic_bytes(sc, nc, nr, iters))
+        solve_bytes_total += solve_bytes(nr, iters)
+        rows_total += int(np.sum(nr))
     B.sync()
     barrier()
     clk = clocks.stop()
+    launches = B.launch_count() - launches0
+    kern_ms, kern_steps = B.kernel_times()
+    B.set_timing(False)
     times = np.array([a.elapsed_time(b) for a, b in ev]) / 1e3
     t_kernel = float(times.sum())
     stat = B.status()
@@ -239,7 +269,12 @@ def run_ours(args):
 
     if rank == 0:
         hbm, src = peaks()
-        achieved = float(np.sum(bytes_per_step)) / t_kernel / 1e9
+        step_achieved = float(np.sum(bytes_per_step)) / t_kernel / 1e9
+        t_solve = kern_ms[2] / 1e3
+        achieved = solve_bytes_total / t_solve / 1e9
+        tpr = solve_traffic_per_row_iter()
+        traffic = tpr * rows_total * iters / args.steps if tpr is not None else None
+        share = kern_ms / kern_ms.sum()
         line = {"metric": METRIC, "value": value, "unit": "world-steps/s", "n_gpus": world_size,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
@@ -247,13 +282,20 @@ def run_ours(args):
                 "config": {"workload": WORKLOAD, "n_worlds": N_WORLDS, "iterations": iters,
                            "dt": 0.01, "rollout": f"steps 0..{args.steps - 1} from the initial state",
                            "l2": "flushed between timed steps (256 MB write)",
+                           "rows_per_world_avg": rows_total / (args.steps * N_WORLDS),
                            "bodies": int(nbt), "worlds_with_status": int((stat != 0).sum()),
                            "step_ms_min_median_max": [float(1e3 * times.min()), float(1e3 * np.median(times)),
                                                       float(1e3 * times.max())]},
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                             "frac": achieved / hbm, "peak_source": src, "traffic": None,
-                             "kernel": "world_step_kernel (one warp per world)",
-                             "bytes_model": "208*nb + 56*nc + 40*n_ball + m*(248 + 236*iters) per world"},
+                             "frac": achieved / hbm, "peak_source": src, "traffic": traffic,
+                             "kernel": "world_solve_kernel (SOR_LCP + integration, one warp per world)",
+                             "bytes_model": "236 B per row-iteration (rows x iterations of the launch)",
+                             "launch_ms_avg": kern_ms[2] / max(1, kern_steps),
+                             "traffic_source": "ncu dram bytes per row-iteration (profiles/) x rows x iters"},
+                "step_roofline": {"achieved": step_achieved, "frac": step_achieved / hbm,
+                                  "bytes_model": "208*nb + 56*nc + 40*n_ball + m*(248 + 236*iters) per world"},
+                "kernel_share": {"world_collide_kernel": share[0], "world_setup_kernel": share[1],
+                                 "world_solve_kernel": share[2]},
                 "e2e": {"value": e2e, "unit": "world-steps/s", "h2d_bytes_per_step": nbt * 13 * 4,
                         "d2h_bytes_per_step": nbt * 13 * 4},
                 "gpu_launches": launches, "clocks": clk}

@@ -70,6 +70,17 @@ int odegpuBatchStepPlain(odegpuBatchID b, int n_steps);
 int odegpuBatchStepGraph(odegpuBatchID b, int n_steps);
 int odegpuBatchSynchronize(odegpuBatchID b);
 
+/* Instrumentation (no counterpart in the reference).
+ * SetTiming(on) makes every following non-graph step record CUDA events on
+ * the batch stream around its three kernels (collide, setup, solve) and
+ * clears earlier records. GetKernelTimes synchronises the stream, returns
+ * the summed milliseconds of each kernel since the last call (ms[3]) and the
+ * number of steps they cover, and clears the records. GetLaunchCount
+ * returns how many kernels the batch has launched since creation. */
+int odegpuBatchSetTiming(odegpuBatchID b, int on);
+int odegpuBatchGetKernelTimes(odegpuBatchID b, double* ms, long long* n_steps);
+int odegpuBatchGetLaunchCount(odegpuBatchID b, long long* launches);
+
 /* Body state exchange with host memory (FP64 records of ODEGPU_BODY_REC).
  * Read = dBodyGetPosition/Quaternion/LinearVel/AngularVel over all bodies;
  * write = dBodySetPosition/Quaternion/LinearVel/AngularVel. */

@@ -178,19 +178,49 @@ struct odegpuBatch {
 
   DBuf<int> order;   // worlds by decreasing size (launch slot -> world)
 
+  long long launches = 0;             // kernels launched by this batch
+  // Optional per-kernel timing: 4 events per step on the batch stream
+  // (before collide, after collide, after setup, after solve).
+  bool timing = false;
+  std::vector<cudaEvent_t> ev_pool;
+  size_t ev_used = 0;
+  cudaEvent_t next_event() {
+    if (ev_used == ev_pool.size()) {
+      cudaEvent_t e;
+      if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+      ev_pool.push_back(e);
+    }
+    return ev_pool[ev_used++];
+  }
+  void mark(bool on) {
+    if (!on) return;
+    if (cudaEvent_t e = next_event()) cudaEventRecord(e, stream);
+  }
+  ~odegpuBatch() {
+    for (cudaEvent_t e : ev_pool) cudaEventDestroy(e);
+  }
+
   // n_steps steps of worlds [first, first+count) of the launch order (or of
-  // the identity order when use_order is false); 2 launches per step.
+  // the identity order when use_order is false); 3 launches per step.
   int launch(int first, int count, int n_steps, const StepOptions& opt, bool use_order = true) {
     const int wpb = warps_per_block;
     const int blocks = (count + wpb - 1) / wpb;
     const BatchDev d = dev();
     const int* ord = (use_order && order.p) ? order.p : nullptr;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    cudaStreamIsCapturing(stream, &cap);
+    const bool tm = timing && cap == cudaStreamCaptureStatusNone;
     for (int s = 0; s < n_steps; ++s) {
+      mark(tm);
       world_collide_kernel<<<blocks, wpb * 32, (size_t)wpb * kCollideSmemPerWarp, stream>>>(
           d, ord, first, count, step_counter + s, opt);
+      mark(tm);
       world_setup_kernel<<<blocks, wpb * 32, (size_t)wpb * kSmemPerWarp, stream>>>(d, ord, first, count, opt);
+      mark(tm);
       world_solve_kernel<<<blocks, wpb * 32, (size_t)wpb * kSorSmemPerWarp, stream>>>(d, ord, first, count,
                                                                                     opt);
+      mark(tm);
+      launches += 3;
     }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return fail(ODEGPU_E_CUDA, std::string("step launch: ") + cudaGetErrorString(e));
@@ -555,6 +585,37 @@ int odegpuBatchStepGraph(odegpuBatchID b, int n_steps) {
   return 0;
 }
 
+int odegpuBatchSetTiming(odegpuBatchID b, int on) {
+  if (!b) return fail(ODEGPU_E_ARG, "null batch");
+  b->timing = on != 0;
+  b->ev_used = 0;
+  return 0;
+}
+
+int odegpuBatchGetKernelTimes(odegpuBatchID b, double* ms, long long* n_steps) {
+  if (!b || !ms) return fail(ODEGPU_E_ARG, "bad arguments");
+  OG_CUDA(cudaSetDevice(b->device));
+  OG_CUDA(cudaStreamSynchronize(b->stream));
+  ms[0] = ms[1] = ms[2] = 0.0;
+  const size_t steps = b->ev_used / 4;
+  for (size_t k = 0; k < steps; ++k) {
+    for (int j = 0; j < 3; ++j) {
+      float t = 0.f;
+      OG_CUDA(cudaEventElapsedTime(&t, b->ev_pool[4 * k + j], b->ev_pool[4 * k + j + 1]));
+      ms[j] += t;
+    }
+  }
+  if (n_steps) *n_steps = (long long)steps;
+  b->ev_used = 0;
+  return 0;
+}
+
+int odegpuBatchGetLaunchCount(odegpuBatchID b, long long* launches) {
+  if (!b || !launches) return fail(ODEGPU_E_ARG, "bad arguments");
+  *launches = b->launches;
+  return 0;
+}
+
 int odegpuBatchSynchronize(odegpuBatchID b) {
   if (!b) return fail(ODEGPU_E_ARG, "null batch");
   OG_CUDA(cudaSetDevice(b->device));
@@ -567,6 +628,7 @@ int odegpuBatchReadStateF32Async(odegpuBatchID b, float* state) {
   OG_CUDA(cudaSetDevice(b->device));
   const int nb = b->nb_total;
   pack_state_kernel<<<(nb + 255) / 256, 256, 0, b->stream>>>(b->dev(), nb, b->state_scratch.p);
+  b->launches += 1;
   OG_CUDA(cudaGetLastError());
   OG_CUDA(cudaMemcpyAsync(state, b->state_scratch.p, (size_t)nb * ODEGPU_BODY_REC * sizeof(float),
                           cudaMemcpyDefault, b->stream));
@@ -580,6 +642,7 @@ int odegpuBatchWriteStateF32Async(odegpuBatchID b, const float* state) {
   OG_CUDA(cudaMemcpyAsync(b->state_scratch.p, state, (size_t)nb * ODEGPU_BODY_REC * sizeof(float),
                           cudaMemcpyDefault, b->stream));
   unpack_state_kernel<<<(nb + 255) / 256, 256, 0, b->stream>>>(b->dev(), nb, b->state_scratch.p);
+  b->launches += 1;
   OG_CUDA(cudaGetLastError());
   return 0;
 }

@@ -39,6 +39,9 @@ def _declare(L):
         "odegpuBatchStepPlain": (i, [v, i]),
         "odegpuBatchStepGraph": (i, [v, i]),
         "odegpuBatchSynchronize": (i, [v]),
+        "odegpuBatchSetTiming": (i, [v, i]),
+        "odegpuBatchGetKernelTimes": (i, [v, _P(d), _P(C.c_longlong)]),
+        "odegpuBatchGetLaunchCount": (i, [v, _P(C.c_longlong)]),
         "odegpuBatchReadState": (i, [v, _P(d)]),
         "odegpuBatchWriteState": (i, [v, _P(d)]),
         "odegpuBatchReadStateF32Async": (i, [v, v]),

@@ -55,6 +55,24 @@ class Batch:
     def sync(self):
         check(lib().odegpuBatchSynchronize(self.h))
 
+    def set_timing(self, on=True):
+        """Record CUDA events around the collide/setup/solve kernels of every
+        following (non-graph) step."""
+        check(lib().odegpuBatchSetTiming(self.h, 1 if on else 0))
+
+    def kernel_times(self):
+        """(ms[collide, setup, solve] summed since the last call, steps covered)."""
+        ms = (C.c_double * 3)()
+        n = C.c_longlong(0)
+        check(lib().odegpuBatchGetKernelTimes(self.h, ms, C.byref(n)))
+        return np.array(ms[:]), n.value
+
+    def launch_count(self):
+        """Kernels launched by this batch since creation."""
+        n = C.c_longlong(0)
+        check(lib().odegpuBatchGetLaunchCount(self.h, C.byref(n)))
+        return n.value
+
     def state(self):
         out = np.zeros((self.nb_total, BODY_REC))
         check(lib().odegpuBatchReadState(self.h, out.ctypes.data_as(_P(C.c_double))))
