@@ -151,6 +151,63 @@ def cpu_baseline(sc, n_worlds_sample, n_steps, threads=None):
     return n_worlds_sample * n_steps / dt, threads, dt
 
 
+ADJ_WORKLOAD = ("hinge_chains: 1024 worlds x 8-link hinge chains (0.5x0.1x0.1 m, 1 kg), per-step torques "
+                "U[-2,2], plane z=-2, 100 steps, dt 0.01, 20 iterations, checkpoints every 10; "
+                "loss |p_end - target|^2")
+
+
+def run_adjoint(local_rank, reps=3):
+    """Batched forward + hand-written adjoint on the differentiable-batch
+    workload: world-steps/s of (checkpointed forward rollout + backward), and
+    of the forward rollout alone, timed with CUDA events on the batch stream."""
+    import torch
+    from odegpu import scene as S
+    from odegpu.batch import Batch
+    n_w, n_steps, ckpt = 1024, 100, 10
+    sc = S.hinge_chains(n_worlds=n_w, steps=n_steps)
+    B = Batch(sc, device=local_rank)
+    stream = torch.cuda.ExternalStream(B.stream_handle())
+    x0 = torch.tensor(B.state(), dtype=torch.float32, device="cuda")
+    seeds = B.seeds()
+    nbt = B.nb_total
+    g_final = torch.zeros((nbt, 13), dtype=torch.float32, device="cuda")
+    ends = torch.tensor(sc.body_off[1:] - 1, dtype=torch.long, device="cuda")
+    g_final[ends, 0:3] = 1.0
+    g_init = torch.empty_like(g_final)
+    g_jt = torch.zeros((n_steps, B.nj_total, 2), dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    fwd_ms, tot_ms = [], []
+    launches0 = B.launch_count()
+    for r in range(reps + 1):
+        B.set_seeds(seeds)
+        B.set_step_index(0)
+        B.write_state_async(x0.data_ptr())
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+        B.rollout_forward(n_steps, ckpt)
+        with torch.cuda.stream(stream):
+            e1.record(stream)
+        B.rollout_backward(g_final.data_ptr(), g_init.data_ptr(), g_jt.data_ptr(), None)
+        with torch.cuda.stream(stream):
+            e2.record(stream)
+        B.sync()
+        if r > 0:                    # the first repetition is the warm-up
+            fwd_ms.append(e0.elapsed_time(e1))
+            tot_ms.append(e0.elapsed_time(e2))
+    launches = (B.launch_count() - launches0) // (reps + 1)
+    status = B.adjoint_status()
+    B.close()
+    t_tot = float(np.median(tot_ms)) / 1e3
+    t_fwd = float(np.median(fwd_ms)) / 1e3
+    return {"metric": "world-steps/s, batched forward + adjoint", "value": n_w * n_steps / t_tot,
+            "unit": "world-steps/s", "forward_only": n_w * n_steps / t_fwd,
+            "ms_forward_plus_backward": 1e3 * t_tot, "ms_forward": 1e3 * t_fwd,
+            "workload": ADJ_WORKLOAD, "gpu_launches_per_rollout": int(launches),
+            "worlds_with_unmodelled_terms": int((status != 0).sum()),
+            "gradient_check": "tests/test_gpu_adjoint.py (FP64 central differences of the oracle)"}
+
+
 def run_reference(args):
     rank, world_size, _ = rank_env()
     if rank != 0:
@@ -315,6 +372,8 @@ def run_ours(args):
             line["plain_gpu"] = {"value": pw * 20 / tp, "unit": "world-steps/s",
                                  "sample": f"first {pw} worlds x 20 steps, one world per launch"}
             P.close()
+        if not args.no_adjoint:
+            line["adjoint"] = run_adjoint(local_rank)
         if not args.no_cpu:
             nw = min(N_WORLDS, args.cpu_worlds)
             v, thr, dt = cpu_baseline(sc, nw, args.steps)
@@ -335,6 +394,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--cpu-worlds", type=int, default=512)
     ap.add_argument("--ref-worlds", type=int, default=4096)
     args = ap.parse_args()

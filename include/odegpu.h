@@ -70,6 +70,31 @@ int odegpuBatchStepPlain(odegpuBatchID b, int n_steps);
 int odegpuBatchStepGraph(odegpuBatchID b, int n_steps);
 int odegpuBatchSynchronize(odegpuBatchID b);
 
+/* Per-step controls from FP32 arrays in host or device memory (the layout
+ * of odegpuBatchSetControls); null leaves that kind of control off. */
+int odegpuBatchSetControlsF32(odegpuBatchID b, int n_ctrl_steps, const float* joint_torque,
+                              const float* body_force);
+
+/* Differentiation (no counterpart in the reference: ODE has no gradients).
+ * RolloutForward steps every world n_steps times from the current state like
+ * odegpuBatchStep, recording the state and RNG seeds every ckpt_every steps.
+ * RolloutBackward takes d(loss)/d(final state) ([nb_total][ODEGPU_BODY_REC]
+ * FP32, host or device memory) and writes d(loss)/d(initial state) (same
+ * layout), d(loss)/d(joint torques) ([n_ctrl_steps][nj_total][2]) and
+ * d(loss)/d(body forces) ([n_ctrl_steps][nb_total][6]); any output may be
+ * null. It recomputes each checkpoint segment and runs the hand-written
+ * adjoint of every step backwards (one thread per world), then leaves the
+ * batch in the state the forward rollout ended in. The derivative follows
+ * the recorded active set of the sweep (clamped rows pass nothing to their
+ * own lambda). AdjointStatus returns per-world bits: 1 a hinge2 joint or a
+ * hinge limit row was met, 2 a contact other than a sphere/box/capsule body
+ * against a plane (or a bouncing contact) was met (their derivative is left
+ * out), 4 the world exceeds the kernel's limits. */
+int odegpuBatchRolloutForward(odegpuBatchID b, int n_steps, int ckpt_every);
+int odegpuBatchRolloutBackward(odegpuBatchID b, const float* grad_state_final, float* grad_state_init,
+                               float* grad_joint_torque, float* grad_body_force);
+int odegpuBatchAdjointStatus(odegpuBatchID b, int* status);
+
 /* Instrumentation (no counterpart in the reference).
  * SetTiming(on) makes every following non-graph step record CUDA events on
  * the batch stream around its three kernels (collide, setup, solve) and

@@ -12,6 +12,7 @@
 #include "odegpu.h"
 #include "engine_types.cuh"
 #include "world_solve.cuh"
+#include "adjoint.cuh"
 #include "host_setup.hpp"
 
 using namespace og;
@@ -200,6 +201,43 @@ struct odegpuBatch {
     for (cudaEvent_t e : ev_pool) cudaEventDestroy(e);
   }
 
+  // Rollout record for the adjoint: state and RNG seeds every `ckpt` steps
+  // from step `start`, plus the state at the end.
+  struct Rollout {
+    int n_steps = 0, ckpt = 0, start = 0, valid = 0;
+    DBuf<float> ckpt_state, seg_state, final_state;
+    DBuf<unsigned> ckpt_seed, seg_seed, final_seed;
+    DBuf<float> state_bar, body_tmp, row_tmp, lam_tape, dbg;
+    DBuf<unsigned char> code_tape;
+    DBuf<uint16_t> seq_tape;
+    DBuf<int> status;
+    int iters_max = 0, rounds_max = 0;
+  } ro;
+
+  int pack_to(float* out) {
+    pack_state_kernel<<<(nb_total + 255) / 256, 256, 0, stream>>>(dev(), nb_total, out);
+    launches += 1;
+    return 0;
+  }
+  int unpack_from(const float* in) {
+    unpack_state_kernel<<<(nb_total + 255) / 256, 256, 0, stream>>>(dev(), nb_total, in);
+    launches += 1;
+    return 0;
+  }
+  // collide + setup of one step of every world (no solve), for the adjoint
+  int launch_setup(int step, const StepOptions& opt) {
+    const int wpb = warps_per_block;
+    const int blocks = (n_worlds + wpb - 1) / wpb;
+    const BatchDev d = dev();
+    world_collide_kernel<<<blocks, wpb * 32, (size_t)wpb * kCollideSmemPerWarp, stream>>>(d, order.p, 0,
+                                                                                         n_worlds, step, opt);
+    world_setup_kernel<<<blocks, wpb * 32, (size_t)wpb * kSmemPerWarp, stream>>>(d, order.p, 0, n_worlds, opt);
+    launches += 2;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(ODEGPU_E_CUDA, std::string("setup launch: ") + cudaGetErrorString(e));
+    return 0;
+  }
+
   // n_steps steps of worlds [first, first+count) of the launch order (or of
   // the identity order when use_order is false); 3 launches per step.
   int launch(int first, int count, int n_steps, const StepOptions& opt, bool use_order = true) {
@@ -237,6 +275,9 @@ static int configure_kernels(int wpb) {
     return -1;
   if (cudaFuncSetAttribute(world_solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)(wpb * kSorSmemPerWarp)) != cudaSuccess)
+    return -1;
+  if (cudaFuncSetAttribute(adjoint_step_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)(4 * kAdjSmemPerWarp)) != cudaSuccess)
     return -1;
   return 0;
 }
@@ -613,6 +654,153 @@ int odegpuBatchGetKernelTimes(odegpuBatchID b, double* ms, long long* n_steps) {
 int odegpuBatchGetLaunchCount(odegpuBatchID b, long long* launches) {
   if (!b || !launches) return fail(ODEGPU_E_ARG, "bad arguments");
   *launches = b->launches;
+  return 0;
+}
+
+int odegpuBatchSetControlsF32(odegpuBatchID b, int n_ctrl_steps, const float* jt, const float* bf) {
+  if (!b || n_ctrl_steps < 0) return fail(ODEGPU_E_ARG, "bad arguments");
+  OG_CUDA(cudaSetDevice(b->device));
+  OG_CUDA(cudaStreamSynchronize(b->stream));
+  if (b->joint_torque.p) { cudaFree(b->joint_torque.p); b->joint_torque.p = nullptr; }
+  if (b->body_force.p) { cudaFree(b->body_force.p); b->body_force.p = nullptr; }
+  b->n_ctrl_steps = n_ctrl_steps;
+  if (n_ctrl_steps == 0) return 0;
+  const size_t nt = (size_t)n_ctrl_steps * b->nj_total * 2, nf = (size_t)n_ctrl_steps * b->nb_total * 6;
+  if (jt) {
+    if (int rc = b->joint_torque.alloc(nt)) return rc;
+    OG_CUDA(cudaMemcpy(b->joint_torque.p, jt, nt * sizeof(float), cudaMemcpyDefault));
+  }
+  if (bf) {
+    if (int rc = b->body_force.alloc(nf)) return rc;
+    OG_CUDA(cudaMemcpy(b->body_force.p, bf, nf * sizeof(float), cudaMemcpyDefault));
+  }
+  return 0;
+}
+
+int odegpuBatchRolloutForward(odegpuBatchID b, int n_steps, int ckpt_every) {
+  if (!b || n_steps <= 0 || ckpt_every <= 0) return fail(ODEGPU_E_ARG, "bad arguments");
+  OG_CUDA(cudaSetDevice(b->device));
+  auto& R = b->ro;
+  const size_t rec = (size_t)b->nb_total * ODEGPU_BODY_REC;
+  const int n_ckpt = (n_steps + ckpt_every - 1) / ckpt_every;
+  R.valid = 0;
+  if (R.ckpt_state.n < (size_t)n_ckpt * rec) {
+    if (R.ckpt_state.p) { cudaFree(R.ckpt_state.p); R.ckpt_state.p = nullptr; }
+    if (int rc = R.ckpt_state.alloc((size_t)n_ckpt * rec)) return rc;
+  }
+  if (R.ckpt_seed.n < (size_t)n_ckpt * b->n_worlds) {
+    if (R.ckpt_seed.p) { cudaFree(R.ckpt_seed.p); R.ckpt_seed.p = nullptr; }
+    if (int rc = R.ckpt_seed.alloc((size_t)n_ckpt * b->n_worlds)) return rc;
+  }
+  if (!R.final_state.p && R.final_state.alloc(rec)) return ODEGPU_E_NOMEM;
+  if (!R.final_seed.p && R.final_seed.alloc(b->n_worlds)) return ODEGPU_E_NOMEM;
+  R.n_steps = n_steps;
+  R.ckpt = ckpt_every;
+  R.start = b->step_counter;
+  StepOptions opt{1, nullptr, nullptr, nullptr, 0, 0};
+  for (int s = 0; s < n_steps; ++s) {
+    if (s % ckpt_every == 0) {
+      const int c = s / ckpt_every;
+      b->pack_to(R.ckpt_state.p + (size_t)c * rec);
+      OG_CUDA(cudaMemcpyAsync(R.ckpt_seed.p + (size_t)c * b->n_worlds, b->seed.p, b->n_worlds * sizeof(unsigned),
+                              cudaMemcpyDeviceToDevice, b->stream));
+    }
+    if (int rc = b->launch(0, b->n_worlds, 1, opt)) return rc;
+    b->step_counter += 1;
+  }
+  b->pack_to(R.final_state.p);
+  OG_CUDA(cudaMemcpyAsync(R.final_seed.p, b->seed.p, b->n_worlds * sizeof(unsigned), cudaMemcpyDeviceToDevice,
+                          b->stream));
+  OG_CUDA(cudaGetLastError());
+  R.valid = 1;
+  return 0;
+}
+
+int odegpuBatchRolloutBackward(odegpuBatchID b, const float* grad_final, float* grad_init, float* grad_jt,
+                               float* grad_bf) {
+  if (!b || !grad_final) return fail(ODEGPU_E_ARG, "bad arguments");
+  auto& R = b->ro;
+  if (!R.valid) return fail(ODEGPU_E_ARG, "no rollout recorded (odegpuBatchRolloutForward)");
+  OG_CUDA(cudaSetDevice(b->device));
+  const size_t rec = (size_t)b->nb_total * ODEGPU_BODY_REC;
+  int iters_max = 1;
+  for (const WorldDesc& D : b->h_world) iters_max = std::max(iters_max, D.iterations);
+  const int rounds_max = (iters_max + 7) / 8;
+  const size_t rcap = (size_t)std::max<long long>(1, b->row_cap_total);
+  auto need = [](auto& buf, size_t n) -> int {
+    if (buf.n >= n && buf.p) return 0;
+    if (buf.p) { cudaFree(buf.p); buf.p = nullptr; }
+    return buf.alloc(n);
+  };
+  if (need(R.seg_state, (size_t)R.ckpt * rec) || need(R.seg_seed, (size_t)R.ckpt * b->n_worlds) ||
+      need(R.state_bar, rec) || need(R.body_tmp, (size_t)b->nb_total * kAdjBody) ||
+      need(R.row_tmp, rcap * kAdjRow) || need(R.lam_tape, rcap * iters_max) ||
+      need(R.code_tape, rcap * iters_max) || need(R.seq_tape, rcap * rounds_max) ||
+      need(R.dbg, rcap * kRowWords) || need(R.status, (size_t)b->n_worlds))
+    return ODEGPU_E_NOMEM;
+  OG_CUDA(cudaMemsetAsync(R.status.p, 0, b->n_worlds * sizeof(int), b->stream));
+  OG_CUDA(cudaMemcpyAsync(R.state_bar.p, grad_final, rec * sizeof(float), cudaMemcpyDefault, b->stream));
+  const int nctrl = b->n_ctrl_steps;
+  if (grad_jt && nctrl > 0)
+    OG_CUDA(cudaMemsetAsync(grad_jt, 0, (size_t)nctrl * b->nj_total * 2 * sizeof(float), b->stream));
+  if (grad_bf && nctrl > 0)
+    OG_CUDA(cudaMemsetAsync(grad_bf, 0, (size_t)nctrl * b->nb_total * 6 * sizeof(float), b->stream));
+  AdjDev a;
+  a.state_bar = R.state_bar.p; a.body_tmp = R.body_tmp.p; a.row_tmp = R.row_tmp.p;
+  a.lam_tape = R.lam_tape.p; a.code_tape = R.code_tape.p; a.seq_tape = R.seq_tape.p; a.dbg = R.dbg.p;
+  a.g_jt = nctrl > 0 ? grad_jt : nullptr;
+  a.g_bf = nctrl > 0 ? grad_bf : nullptr;
+  a.status = R.status.p;
+  a.iters_max = iters_max;
+  a.rounds_max = rounds_max;
+  StepOptions fwd{1, nullptr, nullptr, nullptr, 0, 0};
+  StepOptions tap{1, R.dbg.p, nullptr, nullptr, 0, 0};
+  const int saved_counter = b->step_counter;
+  const int n_ckpt = (R.n_steps + R.ckpt - 1) / R.ckpt;
+  for (int c = n_ckpt - 1; c >= 0; --c) {
+    const int s0 = c * R.ckpt, len = std::min(R.ckpt, R.n_steps - s0);
+    // recompute the segment from its checkpoint, keeping every pre-step state
+    b->unpack_from(R.ckpt_state.p + (size_t)c * rec);
+    OG_CUDA(cudaMemcpyAsync(b->seed.p, R.ckpt_seed.p + (size_t)c * b->n_worlds, b->n_worlds * sizeof(unsigned),
+                            cudaMemcpyDeviceToDevice, b->stream));
+    for (int j = 0; j < len; ++j) {
+      b->pack_to(R.seg_state.p + (size_t)j * rec);
+      OG_CUDA(cudaMemcpyAsync(R.seg_seed.p + (size_t)j * b->n_worlds, b->seed.p, b->n_worlds * sizeof(unsigned),
+                              cudaMemcpyDeviceToDevice, b->stream));
+      if (j + 1 < len) {
+        b->step_counter = R.start + s0 + j;
+        if (int rc = b->launch(0, b->n_worlds, 1, fwd)) { b->step_counter = saved_counter; return rc; }
+      }
+    }
+    // the segment's steps backwards
+    for (int j = len - 1; j >= 0; --j) {
+      const int step = R.start + s0 + j;
+      b->unpack_from(R.seg_state.p + (size_t)j * rec);
+      OG_CUDA(cudaMemcpyAsync(b->seed.p, R.seg_seed.p + (size_t)j * b->n_worlds, b->n_worlds * sizeof(unsigned),
+                              cudaMemcpyDeviceToDevice, b->stream));
+      if (int rc = b->launch_setup(step, tap)) { b->step_counter = saved_counter; return rc; }
+      adjoint_step_kernel<<<(b->n_worlds + 3) / 4, 128, 4 * (size_t)kAdjSmemPerWarp, b->stream>>>(b->dev(), a,
+                                                                                                step);
+      b->launches += 1;
+    }
+  }
+  if (grad_init)
+    OG_CUDA(cudaMemcpyAsync(grad_init, R.state_bar.p, rec * sizeof(float), cudaMemcpyDefault, b->stream));
+  // leave the batch where the forward rollout ended
+  b->unpack_from(R.final_state.p);
+  OG_CUDA(cudaMemcpyAsync(b->seed.p, R.final_seed.p, b->n_worlds * sizeof(unsigned), cudaMemcpyDeviceToDevice,
+                          b->stream));
+  b->step_counter = saved_counter;
+  OG_CUDA(cudaGetLastError());
+  return 0;
+}
+
+int odegpuBatchAdjointStatus(odegpuBatchID b, int* status) {
+  if (!b || !status) return fail(ODEGPU_E_ARG, "bad arguments");
+  OG_CUDA(cudaSetDevice(b->device));
+  OG_CUDA(cudaStreamSynchronize(b->stream));
+  if (!b->ro.status.p) { std::memset(status, 0, b->n_worlds * sizeof(int)); return 0; }
+  OG_CUDA(cudaMemcpy(status, b->ro.status.p, b->n_worlds * sizeof(int), cudaMemcpyDeviceToHost));
   return 0;
 }
 

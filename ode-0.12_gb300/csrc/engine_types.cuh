@@ -31,9 +31,12 @@ enum {
 //   [12..23] iMJ = invM * J^T
 //   [24] c -> b (rhs * Ad)   [25] cfm -> Ad*cfm   [26] lo  [27] hi
 //   [28] findex (world row index or -1, int bits)  [29] b1  [30] b2  [31] joint
+// The optional unscaled dump (StepOptions::dbg_rows) keeps J in [0..11], Ad in
+// [12], that erp in [13], rhs in [24], cfm/h in [25] and words 26..31 as above.
 constexpr int kRowWords = 32;
 constexpr int kRowC = 24, kRowCfm = 25, kRowLo = 26, kRowHi = 27, kRowFindex = 28;
 constexpr int kRowB1 = 29, kRowB2 = 30, kRowJoint = 31;
+constexpr int kDbgAd = 12, kDbgErp = 13;
 
 struct DevSurface {
   int mode;
@@ -57,7 +60,8 @@ struct DevContact {
   float pos[3], depth;
   float normal[3];
   int surface;
-  int b1, b2, reverse, pad;     // attach result: b2 = -1 for the environment
+  int b1, b2, reverse;          // attach result: b2 = -1 for the environment
+  int geoms;                    // world-local pair (g1 | g2 << 8) of the collider call, -1 unknown
 };
 
 // Static description of one world inside the batch.

@@ -700,6 +700,7 @@ int dWorldQuickStep(dWorldID w, dReal stepsize) {
     c.b1 = index_of(j->body[0]);
     c.b2 = index_of(j->body[1]);
     c.reverse = j->reverse;
+    c.geoms = -1;
     const dSurfaceParameters& S = j->contact.surface;
     DevSurface& D = hw.surfaces[k];
     D.mode = S.mode; D.mu = S.mu; D.mu2 = S.mu2; D.bounce = S.bounce; D.bounce_vel = S.bounce_vel;

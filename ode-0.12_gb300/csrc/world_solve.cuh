@@ -51,7 +51,8 @@ OG_D void phase_body_prologue(const BatchDev& d, const WorldDesc& D, int lane) {
 
 // Phase 4: getInfo1 / getInfo2 over the joints in island order. Returns the
 // total row count M (or -1 when it exceeds the world's capacity).
-OG_D int phase_rows(const BatchDev& d, const WorldDesc& D, int w, int nj, int nisl, int lane) {
+OG_D int phase_rows(const BatchDev& d, const WorldDesc& D, int w, int nj, int nisl, int lane,
+                      float* dbg_rows) {
   const int jl_off = D.joint_off + D.contact_off;
   const float h1 = 1.0f / D.dt;
   // pass 1: m per joint, prefix -> first row
@@ -177,6 +178,8 @@ OG_D int phase_rows(const BatchDev& d, const WorldDesc& D, int w, int nj, int ni
         int* fi = reinterpret_cast<int*>(rows + r * kRowWords) + kRowFindex;
         if (*fi != -1) *fi += r0;
       }
+      if (dbg_rows)
+        for (int r = 0; r < m; ++r) dbg_rows[(size_t)(D.row_off + r0 + r) * kRowWords + kDbgErp] = in.erp;
     }
   }
   __syncwarp();
@@ -261,6 +264,7 @@ OG_D void phase_row_setup(const BatchDev& d, const WorldDesc& D, int M, const Wa
     if (b2 != -1)
       for (int j = 6; j < 12; ++j) s += iMJ[j] * J[j];
     const float Ad = sor_w / (s + cfm);
+    if (dbg_rows) dbg_rows[(size_t)(D.row_off + r) * kRowWords + kDbgAd] = Ad;
     for (int j = 0; j < 12; ++j) J[j] *= Ad;
     row4[0] = make_float4(J[0], J[1], J[2], J[3]);
     row4[1] = make_float4(J[4], J[5], J[6], J[7]);
@@ -414,7 +418,7 @@ OG_D void world_setup(const BatchDev& d, int w, const WarpSmem& S, int lane, con
     M = -1;
   } else {
     const int nj = phase_islands(d, D, w, opt.host_adjacency ? 0 : nc, D.njp + nc, S, lane, &nisl);
-    M = phase_rows(d, D, w, nj, nisl, lane);
+    M = phase_rows(d, D, w, nj, nisl, lane, opt.dbg_rows);
   }
   if (M > 0) phase_row_setup(d, D, M, S, lane, opt.dbg_rows);
   if (lane == 0) {

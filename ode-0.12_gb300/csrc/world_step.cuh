@@ -175,10 +175,11 @@ OG_D int phase_collide(const BatchDev& d, const WorldDesc& D, int w, const WarpS
     const int ci = base + lane;
     int cnt = 0;
     Contact cc[8];
-    int bi = -1, bk = -1, surf = 0;
+    int bi = -1, bk = -1, surf = 0, pair = -1;
     if (ci < ncand) {
       int i, k;
       unrank_pair(S.cand[ci], ng, i, k);
+      pair = i | (k << 8);
       const int gi = D.geom_off + i, gk = D.geom_off + k;
       bi = d.gbody[gi];
       bk = d.gbody[gk];
@@ -203,7 +204,7 @@ OG_D int phase_collide(const BatchDev& d, const WorldDesc& D, int w, const WarpS
         // dJointAttach(body(gi), body(gk)): a missing first body swaps in the second
         if (bi < 0) { ct.b1 = bk; ct.b2 = -1; ct.reverse = 1; }
         else { ct.b1 = bi; ct.b2 = bk; ct.reverse = 0; }
-        ct.pad = 0;
+        ct.geoms = pair;
         d.contacts[D.contact_off + slot] = ct;
       }
     }

@@ -40,6 +40,10 @@ def _declare(L):
         "odegpuBatchStepGraph": (i, [v, i]),
         "odegpuBatchSynchronize": (i, [v]),
         "odegpuBatchSetTiming": (i, [v, i]),
+        "odegpuBatchSetControlsF32": (i, [v, i, v, v]),
+        "odegpuBatchRolloutForward": (i, [v, i, i]),
+        "odegpuBatchRolloutBackward": (i, [v, v, v, v, v]),
+        "odegpuBatchAdjointStatus": (i, [v, _P(i)]),
         "odegpuBatchGetKernelTimes": (i, [v, _P(d), _P(C.c_longlong)]),
         "odegpuBatchGetLaunchCount": (i, [v, _P(C.c_longlong)]),
         "odegpuBatchReadState": (i, [v, _P(d)]),

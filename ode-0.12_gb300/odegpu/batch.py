@@ -131,6 +131,23 @@ class Batch:
             self.h, S, jt.ctypes.data_as(_P(C.c_double)) if jt is not None else None,
             bf.ctypes.data_as(_P(C.c_double)) if bf is not None else None))
 
+    def set_controls_f32(self, n_ctrl_steps, joint_torque_ptr=None, body_force_ptr=None):
+        """Controls from FP32 arrays at host or device addresses (integers)."""
+        check(lib().odegpuBatchSetControlsF32(self.h, int(n_ctrl_steps), joint_torque_ptr,
+                                              body_force_ptr))
+
+    def rollout_forward(self, n_steps, ckpt_every=10):
+        check(lib().odegpuBatchRolloutForward(self.h, int(n_steps), int(ckpt_every)))
+
+    def rollout_backward(self, grad_final_ptr, grad_init_ptr=None, grad_jt_ptr=None, grad_bf_ptr=None):
+        check(lib().odegpuBatchRolloutBackward(self.h, grad_final_ptr, grad_init_ptr, grad_jt_ptr,
+                                               grad_bf_ptr))
+
+    def adjoint_status(self):
+        out = np.zeros(self.n_worlds, np.int32)
+        check(lib().odegpuBatchAdjointStatus(self.h, out.ctypes.data_as(_P(C.c_int))))
+        return out
+
     def step_tap(self):
         """One step, returning (rows [R,32] f32, lambda [R], fc [nb,6], row_off [W])."""
         rows = np.zeros((self.row_capacity, 32), np.float32)

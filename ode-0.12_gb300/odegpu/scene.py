@@ -438,19 +438,20 @@ def box_stack(n_worlds=1, height=5, seed=3, spacing=0.0):
     return b.build()
 
 
-def hinge_chains(n_worlds=1024, links=8, seed=4, steps=100):
+def hinge_chains(n_worlds=1024, links=8, seed=4, steps=100, plane_z=-2.0):
     """Differentiable batch: each world an 8-link hinge chain of 0.5x0.1x0.1 m,
     1 kg boxes along x, the first link hinged to the static environment, hinge
     axes along y, initial joint angles U[-0.5,0.5] rad (applied as a planar
     rotation about y accumulated down the chain) and joint rates U[-1,1] rad/s;
-    per-step hinge torques U[-2,2] N m; the end link can touch plane z=-2."""
+    per-step hinge torques U[-2,2] N m; the end link can touch plane z=plane_z
+    (-2 m)."""
     rng = np.random.Generator(np.random.PCG64(seed))
     b = SceneBuilder()
     s = _std_surface(b, 0.5)
     L = 0.5
     for wi in range(n_worlds):
         w = b.new_world(cfm=1e-5, seed=int(rng.integers(0, 2**32)))
-        b.add_geom(w, GEOM_PLANE, -1, (0, 0, 1, -2.0), s)
+        b.add_geom(w, GEOM_PLANE, -1, (0, 0, 1, plane_z), s)
         angles = rng.uniform(-0.5, 0.5, links)
         rates = rng.uniform(-1.0, 1.0, links)
         theta = 0.0

@@ -1965,6 +1965,35 @@ static void read_state(const OWorld* W, double* out) {
   }
 }
 
+/* Overwrite every body's state after the world was built from the scene (joint
+ * anchors, axes and reference angles stay as the scene set them up). The
+ * quaternion is taken as given and R follows from it (dRfromQ), which is how
+ * a step treats the state it starts from. */
+static void write_state(OWorld* W, const double* in) {
+  for (int i = 0; i < W->nb; ++i) {
+    OBody* b = &W->body[i];
+    const double* r = in + ORACLE_BODY_REC * i;
+    for (int k = 0; k < 3; ++k) b->pos[k] = r[k];
+    for (int k = 0; k < 4; ++k) b->q[k] = r[3 + k];
+    for (int k = 0; k < 3; ++k) b->lvel[k] = r[7 + k];
+    for (int k = 0; k < 3; ++k) b->avel[k] = r[10 + k];
+    r_from_q(b->R, b->q);
+  }
+}
+
+int oracle_run_world_from(const odegpuScene* sc, int w, int n_steps, const double* init_state,
+                          double* final_state) {
+  if (!sc || w < 0 || w >= sc->n_worlds || n_steps < 0 || !init_state) return -1;
+  OWorld W;
+  world_init(&W, sc, w);
+  g_seed = sc->world[w].seed;
+  write_state(&W, init_state);
+  for (int s = 0; s < n_steps; ++s) world_step(&W, s, 0, 0);
+  if (final_state) read_state(&W, final_state);
+  world_free(&W);
+  return 0;
+}
+
 int oracle_run_world(const odegpuScene* sc, int w, int n_steps, double* state, int* ncontacts,
                      double* contacts, int max_rec, double* feedback, unsigned int* seed_out) {
   if (!sc || w < 0 || w >= sc->n_worlds || n_steps < 0) return -1;

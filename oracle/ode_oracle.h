@@ -22,6 +22,13 @@ int oracle_run_world(const odegpuScene* sc, int w, int n_steps, double* state,
                      int* ncontacts, double* contacts, int max_rec, double* feedback,
                      unsigned int* seed_out);
 
+/* World w built from the scene, then every body's state replaced by
+ * init_state ([nb][13], quaternion used as given), stepped n_steps times;
+ * final_state receives [nb][13]. For finite differences of the step with
+ * respect to the state it starts from. */
+int oracle_run_world_from(const odegpuScene* sc, int w, int n_steps, const double* init_state,
+                          double* final_state);
+
 /* Run worlds [w_begin, w_end) for n_steps on n_threads host threads; writes the
  * final state [nb_total_in_range][13]. Returns total contacts created. */
 long long oracle_run_worlds(const odegpuScene* sc, int w_begin, int w_end, int n_steps,

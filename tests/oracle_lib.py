@@ -48,6 +48,9 @@ def oracle():
         lib.oracle_rand_int.argtypes = [C.c_int]
         lib.oracle_rand_set_seed.argtypes = [C.c_uint]
         lib.oracle_rand_get_seed.restype = C.c_uint
+        lib.oracle_run_world_from.restype = C.c_int
+        lib.oracle_run_world_from.argtypes = [C.c_void_p, C.c_int, C.c_int, _P(C.c_double),
+                                              _P(C.c_double)]
         _oracle = lib
     return _oracle
 
@@ -126,3 +129,14 @@ def tap_step(scene, w, pre_steps, cap_rows=4096, cap_bodies=1024):
     a["island_rows"] = a["island_rows"][:n]
     a["island_bodies"] = a["island_bodies"][:n]
     return a
+
+
+def run_world_from(scene, w, n_steps, init_state):
+    """Oracle world w built from the scene, body state replaced by init_state
+    ([nb, 13]), n_steps steps; returns the final state [nb, 13]."""
+    x0 = np.ascontiguousarray(init_state, dtype=np.float64)
+    out = np.zeros_like(x0)
+    rc = oracle().oracle_run_world_from(C.byref(scene.c), w, n_steps, x0.ctypes.data_as(_P(C.c_double)),
+                                        out.ctypes.data_as(_P(C.c_double)))
+    assert rc == 0
+    return out

@@ -1,0 +1,187 @@
+"""Hand-written adjoint of the batched step against FP64 central differences
+of the CPU oracle (no gradients exist in the reference; the oracle restates
+its dWorldQuickStep in FP64, so d(loss)/d(input) is taken by re-running it
+with the input moved by +-eps, the RNG seeds identical in both runs).
+
+Tolerance: the gradient vector of each case, against the finite-difference
+one, within 1e-3 relative (2-norm of the difference over 2-norm of the
+reference). The GPU runs in FP32, the reference in FP64. The difference step
+is 1e-4 for the hinge chains; the sliding-box contact case is stiff (contact
+rhs ~ erp/h^2 times depth), and there a 1e-4 step itself is off by ~5e-3, so
+it uses 1e-6 (FP64 rounding is ~1e-10 at that step)."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import oracle_lib as O
+from odegpu import scene as S
+
+torch = pytest.importorskip("torch")
+
+pytestmark = pytest.mark.gpu
+
+EPS = 1e-4
+TOL = 1e-3
+
+
+def _oracle_final(sc, w, n, x0=None):
+    if x0 is None:
+        return O.run_world(O.oracle().oracle_run_world, sc, w, n)["state"][n]
+    return O.run_world_from(sc, w, n, x0)
+
+
+def _fd(sc, w, n, loss, poke, x0, eps=EPS):
+    """Central difference of loss(final state of world w) for the input that
+    poke(sign * eps) moves (poke(0) puts it back); x0 is the world's initial
+    state array the pokes may edit."""
+    poke(eps)
+    lp = loss(_oracle_final(sc, w, n, x0))
+    poke(-eps)
+    lm = loss(_oracle_final(sc, w, n, x0))
+    poke(0.0)
+    return (lp - lm) / (2 * eps)
+
+
+def _gpu_grads(sc, n, coef, ckpt=10):
+    """GPU rollout of n steps with loss sum(coef * final) (coef [nb, 13]);
+    returns (grad init state [nb,13], grad joint torques [S,nj,2] or None, batch,
+    final state, initial state)."""
+    from odegpu.batch import Batch
+    from odegpu.adjoint import rollout
+    B = Batch(sc)
+    x0_np = B.state()
+    x0 = torch.tensor(x0_np, dtype=torch.float32, device="cuda", requires_grad=True)
+    jt = None
+    if sc.n_ctrl_steps > 0 and getattr(sc, "joint_torque", None) is not None:
+        jt = torch.tensor(sc.joint_torque, dtype=torch.float32, device="cuda", requires_grad=True)
+    final = rollout(B, n, x0, jt, None, ckpt_every=ckpt)
+    c = torch.tensor(coef, dtype=torch.float32, device="cuda")
+    (final * c).sum().backward()
+    gj = jt.grad.cpu().numpy() if jt is not None else None
+    return x0.grad.cpu().numpy(), gj, B, final.detach().cpu().numpy(), x0_np
+
+
+def _rel(a, b):
+    a, b = np.asarray(a, float), np.asarray(b, float)
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-12)
+
+
+def _check_case(sc, n, coef, n_vel=12, n_pos=6, n_tq=12, seed=0, q_dirs=2, eps=EPS):
+    rng = np.random.default_rng(seed)
+    g_state, g_jt, B, _, g0 = _gpu_grads(sc, n, coef)
+    status = B.adjoint_status()
+    assert (status == 0).all(), status
+    fd, gpu, names = [], [], []
+    for w in range(sc.n_worlds):
+        b0, b1 = sc.world_bodies(w)
+        cw = coef[b0:b1]
+        # the oracle starts from the FP32 state the GPU starts from
+        x0 = np.asarray(g0[b0:b1], dtype=np.float64).copy()
+
+        def loss(fin, cw=cw):
+            return float(np.sum(cw * fin))
+
+        def state_poke(b, k, x0=x0, b0=b0):
+            v0 = x0[b - b0, k]
+
+            def poke(e):
+                x0[b - b0, k] = v0 + e
+            return poke
+
+        for _ in range(n_vel):
+            b = int(rng.integers(b0, b1))
+            k = 7 + int(rng.integers(0, 6))
+            fd.append(_fd(sc, w, n, loss, state_poke(b, k), x0, eps)); gpu.append(g_state[b, k])
+            names.append(f"v{b},{k}")
+        for _ in range(n_pos):
+            b = int(rng.integers(b0, b1))
+            k = int(rng.integers(0, 3))
+            fd.append(_fd(sc, w, n, loss, state_poke(b, k), x0, eps)); gpu.append(g_state[b, k])
+            names.append(f"x{b},{k}")
+        for _ in range(q_dirs):
+            b = int(rng.integers(b0, b1))
+            k = 3 + int(rng.integers(0, 4))
+            fd.append(_fd(sc, w, n, loss, state_poke(b, k), x0, eps)); gpu.append(g_state[b, k])
+            names.append(f"q{b},{k}")
+        if g_jt is not None:
+            j0, j1 = sc.world_joints(w)
+            for _ in range(n_tq):
+                s = int(rng.integers(0, min(n, sc.n_ctrl_steps)))
+                j = int(rng.integers(j0, j1))
+                v0 = sc.joint_torque[s, j, 0]
+
+                def poke(e, s=s, j=j, v0=v0):
+                    sc.joint_torque[s, j, 0] = v0 + e
+                fd.append(_fd(sc, w, n, loss, poke, x0, eps)); gpu.append(g_jt[s, j, 0]); names.append(f"t{s},{j}")
+    B.close()
+    err = _rel(gpu, fd)
+    worst = np.argsort(-np.abs(np.array(gpu) - np.array(fd)))[:5]
+    detail = [(names[i], gpu[i], fd[i]) for i in worst]
+    return err, detail
+
+
+def _coef(sc, seed, cols=range(13)):
+    rng = np.random.default_rng(seed)
+    c = np.zeros((sc.body_off[-1], 13))
+    for k in cols:
+        c[:, k] = rng.standard_normal(sc.body_off[-1])
+    c[:, 3:7] = 0.0     # quaternion outputs: checked through the state they drive
+    return c
+
+
+def test_adjoint_one_step_hinge_chain():
+    sc = S.hinge_chains(n_worlds=2, steps=4, plane_z=-100.0)
+    err, detail = _check_case(sc, 1, _coef(sc, 1), seed=1)
+    assert err < TOL, (err, detail)
+
+
+def test_adjoint_chain_rollout_100_steps():
+    """Differentiable-batch workload (8-link hinge chains, per-step torques,
+    100 steps, checkpoints every 10) with the plane out of reach, so the
+    trajectory does not switch; loss = squared distance of the end link to a
+    seeded target; d/d(initial velocities) and d/d(torques)."""
+    n = 100
+    sc = S.hinge_chains(n_worlds=2, steps=n, plane_z=-100.0)
+    rng = np.random.default_rng(7)
+    fin = np.concatenate([_oracle_final(sc, w, n) for w in range(sc.n_worlds)])  # targets only
+    coef = np.zeros((sc.body_off[-1], 13))
+    # loss = sum over worlds |p_end - target|^2 is quadratic; its gradient at
+    # the final state is linear in the final state, so check d/d(input) of
+    # the linearisation sum(2 (p_end - target) . p_end) (same gradient).
+    for w in range(sc.n_worlds):
+        b_end = sc.body_off[w + 1] - 1
+        target = fin[b_end, 0:3] + rng.uniform(-0.5, 0.5, 3)
+        coef[b_end, 0:3] = 2 * (fin[b_end, 0:3] - target)
+    err, detail = _check_case(sc, n, coef, n_vel=16, n_pos=0, n_tq=16, seed=2, q_dirs=0)
+    assert err < TOL, (err, detail)
+
+
+def test_adjoint_sliding_box_contacts():
+    """A box sliding on a plane: four persistent contacts, friction rows held at
+    +-mu * lambda_normal (the clamp passes the derivative to the normal row)."""
+    b = S.SceneBuilder()
+    s = S._std_surface(b, 0.5)
+    w = b.new_world(cfm=1e-5, seed=5)
+    b.add_geom(w, S.GEOM_PLANE, -1, (0, 0, 1, 0), s)
+    m, I = S.box_mass(1000.0, 0.6, 0.4, 0.3)
+    bi = b.add_body(w, (0.0, 0.0, 0.149), m, I, lvel=(1.5, 0.4, 0.0), avel=(0.0, 0.0, 0.3))
+    b.add_geom(w, S.GEOM_BOX, bi, (0.6, 0.4, 0.3), s)
+    sc = b.build()
+    coef = _coef(sc, 3, cols=[0, 1, 7, 8, 12])
+    err, detail = _check_case(sc, 10, coef, n_vel=6, n_pos=3, n_tq=0, seed=3, q_dirs=1, eps=1e-6)
+    assert err < TOL, (err, detail)
+
+
+def test_adjoint_checkpoint_interval_invariant():
+    sc = S.hinge_chains(n_worlds=3, steps=30, plane_z=-100.0)
+    coef = _coef(sc, 4)
+    g1, j1, B1, f1, _ = _gpu_grads(sc, 30, coef, ckpt=1)
+    B1.close()
+    g2, j2, B2, f2, _ = _gpu_grads(sc, 30, coef, ckpt=7)
+    B2.close()
+    g3, j3, B3, f3, _ = _gpu_grads(sc, 30, coef, ckpt=30)
+    B3.close()
+    assert np.array_equal(f1, f2) and np.array_equal(f1, f3)
+    assert np.array_equal(g1, g2) and np.array_equal(g1, g3)
+    assert np.array_equal(j1, j2) and np.array_equal(j1, j3)
