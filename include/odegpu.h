@@ -32,7 +32,10 @@ enum {
   ODEGPU_ST_CONTACT_OVERFLOW = 1,
   ODEGPU_ST_ROW_OVERFLOW = 2,
   ODEGPU_ST_TOO_LARGE = 4,
-  ODEGPU_ST_NONFINITE = 8
+  ODEGPU_ST_NONFINITE = 8,
+  /* a geom covered more than 10 x 10 heightfield samples (the collider's
+     buffer); that pair produced no contacts in the step */
+  ODEGPU_ST_HF_ZONE = 32
 };
 
 /* Size limits of the on-chip step kernel: bodies and constraint rows per world. */
@@ -83,7 +86,7 @@ int odegpuBatchSetControlsF32(odegpuBatchID b, int n_ctrl_steps, const float* jo
  * layout), d(loss)/d(joint torques) ([n_ctrl_steps][nj_total][2]) and
  * d(loss)/d(body forces) ([n_ctrl_steps][nb_total][6]); any output may be
  * null. It recomputes each checkpoint segment and runs the hand-written
- * adjoint of every step backwards (one thread per world), then leaves the
+ * adjoint of every step backwards (one warp per world), then leaves the
  * batch in the state the forward rollout ended in. The derivative follows
  * the recorded active set of the sweep (clamped rows pass nothing to their
  * own lambda). AdjointStatus returns per-world bits: 1 a hinge2 joint or a
@@ -134,6 +137,11 @@ void* odegpuBatchStream(odegpuBatchID b);
  * dBodyAddForce / dBodyAddTorque calls made before each step. */
 int odegpuBatchSetControls(odegpuBatchID b, int n_ctrl_steps, const double* joint_torque,
                            const double* body_force);
+/* Replace the per-step joint stops (layout of odegpuScene::joint_stop:
+ * [n_ctrl_steps][nj_total], NaN keeps a joint's own stops); replaces the
+ * dJointSetHingeParam / dJointSetHinge2Param(dParamLoStop, dParamHiStop)
+ * calls made before each step. NULL removes them. */
+int odegpuBatchSetJointStops(odegpuBatchID b, int n_ctrl_steps, const double* stops);
 /* Index of the next step (selects the control row step % n_ctrl_steps); it
  * advances by one per step taken. */
 int odegpuBatchSetStepIndex(odegpuBatchID b, int step);

@@ -145,6 +145,11 @@ typedef struct odegpuScene {
   const double* joint_torque;  /* [n_ctrl_steps][nj][2]: hinge torque in [0],
                                   hinge2 torque1/torque2 in [0]/[1]           */
   const double* body_force;    /* [n_ctrl_steps][nb][6]: force, torque        */
+  const double* joint_stop;    /* [n_ctrl_steps][nj]: before the step, limot1
+                                  lostop = histop of a hinge / hinge2 joint to
+                                  this angle (dJointSetHinge{,2}Param with
+                                  dParamLoStop, dParamHiStop); NaN leaves the
+                                  joint's own stops from joint_param        */
 } odegpuScene;
 
 /*

@@ -42,7 +42,7 @@ __device__ __forceinline__ int slot_world(const int* order, int first, int count
   return w < nw ? w : -1;
 }
 
-__global__ void __launch_bounds__(128) world_collide_kernel(BatchDev d, const int* order, int first, int count,
+__global__ void __launch_bounds__(128, 4) world_collide_kernel(BatchDev d, const int* order, int first, int count,
                                                             int step, StepOptions opt) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & 31;
@@ -57,7 +57,7 @@ __global__ void __launch_bounds__(128) world_collide_kernel(BatchDev d, const in
 }
 
 __global__ void __launch_bounds__(128) world_setup_kernel(BatchDev d, const int* order, int first, int count,
-                                                          StepOptions opt) {
+                                                          int step, StepOptions opt) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & 31;
   const int w = slot_world(order, first, count, d.n_worlds);
@@ -67,7 +67,7 @@ __global__ void __launch_bounds__(128) world_setup_kernel(BatchDev d, const int*
     return;
   }
   const WarpSmem S = carve_smem(smem_raw + (size_t)(threadIdx.x >> 5) * kSmemPerWarp);
-  world_setup(d, w, S, lane, opt);
+  world_setup(d, w, step, S, lane, opt);
 }
 
 __global__ void __launch_bounds__(128) world_solve_kernel(BatchDev d, const int* order, int first, int count,
@@ -145,10 +145,12 @@ struct odegpuBatch {
   DBuf<int> gtype, gbody, gsurf;
   DBuf<float4> gparam, gpos;
   DBuf<float> gbound;
+  DBuf<DevHeightfield> hfs;
+  DBuf<float> hf_heights;
   DBuf<DevSurface> surfaces;
   DBuf<DevJoint> joints;
   DBuf<int> padj_start, padj;
-  DBuf<float> joint_torque, body_force;
+  DBuf<float> joint_torque, body_force, joint_stop;
   int n_ctrl_steps = 0;
   DBuf<DevContact> contacts;
   DBuf<float> rows;
@@ -166,10 +168,12 @@ struct odegpuBatch {
     d.invIw = invIw.p; d.facc = facc.p; d.tacc = tacc.p;
     d.gtype = gtype.p; d.gbody = gbody.p; d.gparam = gparam.p; d.gbound = gbound.p; d.gpos = gpos.p;
     d.gsurf = gsurf.p; d.surfaces = surfaces.p;
+    d.hfs = hfs.p; d.hf_heights = hf_heights.p;
     d.joints = joints.p; d.padj_start = padj_start.p; d.padj = padj.p;
     d.n_ctrl_steps = n_ctrl_steps;
     d.joint_torque = n_ctrl_steps > 0 ? joint_torque.p : nullptr;
     d.body_force = n_ctrl_steps > 0 ? body_force.p : nullptr;
+    d.joint_stop = n_ctrl_steps > 0 ? joint_stop.p : nullptr;
     d.step_counter_base = 0;
     d.contacts = contacts.p; d.rows = rows.p; d.jlist = jlist.p; d.adj = adj.p;
     d.adj_start = adj_start.p; d.island_jstart = island_jstart.p; d.island_rstart = island_rstart.p;
@@ -231,7 +235,8 @@ struct odegpuBatch {
     const BatchDev d = dev();
     world_collide_kernel<<<blocks, wpb * 32, (size_t)wpb * kCollideSmemPerWarp, stream>>>(d, order.p, 0,
                                                                                          n_worlds, step, opt);
-    world_setup_kernel<<<blocks, wpb * 32, (size_t)wpb * kSmemPerWarp, stream>>>(d, order.p, 0, n_worlds, opt);
+    world_setup_kernel<<<blocks, wpb * 32, (size_t)wpb * kSmemPerWarp, stream>>>(d, order.p, 0, n_worlds, step,
+                                                                                opt);
     launches += 2;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return fail(ODEGPU_E_CUDA, std::string("setup launch: ") + cudaGetErrorString(e));
@@ -253,7 +258,8 @@ struct odegpuBatch {
       world_collide_kernel<<<blocks, wpb * 32, (size_t)wpb * kCollideSmemPerWarp, stream>>>(
           d, ord, first, count, step_counter + s, opt);
       mark(tm);
-      world_setup_kernel<<<blocks, wpb * 32, (size_t)wpb * kSmemPerWarp, stream>>>(d, ord, first, count, opt);
+      world_setup_kernel<<<blocks, wpb * 32, (size_t)wpb * kSmemPerWarp, stream>>>(d, ord, first, count,
+                                                                                  step_counter + s, opt);
       mark(tm);
       world_solve_kernel<<<blocks, wpb * 32, (size_t)wpb * kSorSmemPerWarp, stream>>>(d, ord, first, count,
                                                                                     opt);
@@ -293,6 +299,14 @@ static float bound_radius(int type, const double* p) {
     case ODEGPU_GEOM_CAPSULE: return (float)(p[0] + 0.5 * p[1]);
     default: return INFINITY;
   }
+}
+
+static int set_joint_stops(odegpuBatch* B, int n_ctrl, const double* js) {
+  if (B->joint_stop.p) { cudaFree(B->joint_stop.p); B->joint_stop.p = nullptr; }
+  if (!js || n_ctrl <= 0) return 0;
+  std::vector<float> v((size_t)n_ctrl * B->nj_total);
+  for (size_t i = 0; i < v.size(); ++i) v[i] = (float)js[i];
+  return B->joint_stop.upload(v);
 }
 
 static int set_controls(odegpuBatch* B, int n_ctrl, const double* jt, const double* bf) {
@@ -381,6 +395,12 @@ int odegpuBatchCreate(const odegpuScene* sc, const odegpuBatchConfig* cfg, odegp
       double l = p[0] * p[0] + p[1] * p[1] + p[2] * p[2];
       if (l > 0) { l = 1.0 / std::sqrt(l); p[0] *= l; p[1] *= l; p[2] *= l; p[3] *= l; }
       else { p[0] = 1; p[1] = p[2] = p[3] = 0; }
+    } else if (gtype[g] == ODEGPU_GEOM_HEIGHTFIELD) {
+      const int hi = (int)p[0];
+      if (gbody[g] >= 0 || hi < 0 || hi >= sc->n_heightfields || !sc->heightfields) {
+        delete B;
+        return fail(ODEGPU_E_ARG, "heightfield geom: bad heightfield index or attached to a body");
+      }
     } else if (gtype[g] != ODEGPU_GEOM_SPHERE && gtype[g] != ODEGPU_GEOM_BOX &&
                gtype[g] != ODEGPU_GEOM_CAPSULE) {
       delete B;
@@ -390,6 +410,38 @@ int odegpuBatchCreate(const odegpuScene* sc, const odegpuBatchConfig* cfg, odegp
     gpos[g] = make_float4(0.f, 0.f, 0.f, 0.f);
     gbound[g] = bound_radius(gtype[g], p);
   }
+  // heightfields: dGeomHeightfieldDataBuildDouble + dxHeightfieldData::SetData
+  // caches (ode/src/heightfield.cpp:107-143), samples stored as FP32
+  std::vector<DevHeightfield> hfs(std::max(1, sc->n_heightfields));
+  std::vector<float> hf_heights;
+  for (int i = 0; i < sc->n_heightfields; ++i) {
+    const odegpuHeightfield& H = sc->heightfields[i];
+    if (H.nx < 2 || H.nz < 2 || !(H.width > 0) || !(H.depth > 0) || !H.heights) {
+      delete B;
+      return fail(ODEGPU_E_ARG, "heightfield " + std::to_string(i) + ": bad sample counts or extent");
+    }
+    DevHeightfield& D = hfs[i];
+    D.nx = H.nx; D.nz = H.nz; D.wrap = H.wrap; D.h_off = (int)hf_heights.size();
+    D.width = (float)H.width; D.depth = (float)H.depth;
+    D.scale = (float)H.scale; D.offset = (float)H.offset; D.thickness = (float)H.thickness;
+    const double sw = H.width / (H.nx - 1.0), sd = H.depth / (H.nz - 1.0);
+    D.sw = (float)sw; D.sd = (float)sd;
+    D.inv_sw = (float)(1.0 / sw); D.inv_sd = (float)(1.0 / sd);
+    D.zx = (float)(sd / sw);
+    D.half_w = (float)(H.width / 2.0); D.half_d = (float)(H.depth / 2.0);
+    for (int k = 0; k < 3; ++k) D.pos[k] = (float)H.pos[k];
+    D.pad = 0.f;
+    for (int r = 0; r < 3; ++r) {
+      for (int c = 0; c < 3; ++c) D.R[r * 4 + c] = (float)H.R[r * 3 + c];
+      D.R[r * 4 + 3] = 0.f;
+    }
+    for (long long k = 0; k < (long long)H.nx * H.nz; ++k) hf_heights.push_back((float)H.heights[k]);
+  }
+  for (int g = 0; g < NG; ++g)
+    if (gtype[g] == ODEGPU_GEOM_HEIGHTFIELD) {
+      const DevHeightfield& D = hfs[(int)sc->geom_param[ODEGPU_GEOM_NPARAM * (size_t)g]];
+      gpos[g] = make_float4(D.pos[0], D.pos[1], D.pos[2], 0.f);
+    }
   std::vector<DevSurface> surf(std::max(1, sc->n_surfaces));
   for (int s = 0; s < sc->n_surfaces; ++s) {
     const odegpuSurface& S = sc->surfaces[s];
@@ -519,6 +571,8 @@ int odegpuBatchCreate(const odegpuScene* sc, const odegpuBatchConfig* cfg, odegp
   rc = rc ? rc : B->gsurf.upload(gsurf);
   rc = rc ? rc : B->gparam.upload(gparam);
   rc = rc ? rc : B->gpos.upload(gpos);
+  rc = rc ? rc : B->hfs.upload(hfs);
+  rc = rc ? rc : B->hf_heights.upload(hf_heights);
   rc = rc ? rc : B->gbound.upload(gbound);
   rc = rc ? rc : B->surfaces.upload(surf);
   rc = rc ? rc : B->joints.upload(joints);
@@ -536,6 +590,7 @@ int odegpuBatchCreate(const odegpuScene* sc, const odegpuBatchConfig* cfg, odegp
   rc = rc ? rc : B->island_rstart.alloc((size_t)NB + W);
   rc = rc ? rc : B->state_scratch.alloc((size_t)NB * ODEGPU_BODY_REC);
   if (!rc) rc = set_controls(B, sc->n_ctrl_steps, sc->joint_torque, sc->body_force);
+  if (!rc) rc = set_joint_stops(B, sc->n_ctrl_steps, sc->joint_stop);
   if (!rc && cudaStreamCreateWithFlags(&B->stream, cudaStreamNonBlocking) != cudaSuccess)
     rc = fail(ODEGPU_E_CUDA, "stream creation failed");
   if (!rc) {
@@ -564,6 +619,16 @@ int odegpuBatchSetControls(odegpuBatchID b, int n_ctrl_steps, const double* jt, 
   OG_CUDA(cudaSetDevice(b->device));
   OG_CUDA(cudaStreamSynchronize(b->stream));
   return set_controls(b, n_ctrl_steps, jt, bf);
+}
+
+int odegpuBatchSetJointStops(odegpuBatchID b, int n_ctrl_steps, const double* stops) {
+  if (!b || n_ctrl_steps < 0) return fail(ODEGPU_E_ARG, "bad arguments");
+  if (b->n_ctrl_steps > 0 && n_ctrl_steps != b->n_ctrl_steps && (b->joint_torque.p || b->body_force.p))
+    return fail(ODEGPU_E_ARG, "joint stops must cover the same number of control steps as the torques/forces");
+  OG_CUDA(cudaSetDevice(b->device));
+  OG_CUDA(cudaStreamSynchronize(b->stream));
+  if (n_ctrl_steps > 0) b->n_ctrl_steps = n_ctrl_steps;
+  return set_joint_stops(b, n_ctrl_steps, stops);
 }
 
 int odegpuBatchSetStepIndex(odegpuBatchID b, int step) {

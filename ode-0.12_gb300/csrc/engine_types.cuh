@@ -23,7 +23,8 @@ enum {
   ST_CONTACT_OVERFLOW = 1,   // more contacts than the world's capacity
   ST_ROW_OVERFLOW = 2,       // more constraint rows than the world's capacity
   ST_TOO_LARGE = 4,          // world exceeds the on-chip limits of this kernel
-  ST_NONFINITE = 8           // a body state became NaN/Inf
+  ST_NONFINITE = 8,          // a body state became NaN/Inf
+  ST_HF_ZONE = 32            // a geom covered more heightfield samples than the collider's buffer
 };
 
 // Row store: 32 words (128 bytes, one cache line) per constraint row.
@@ -64,6 +65,16 @@ struct DevContact {
   int geoms;                    // world-local pair (g1 | g2 << 8) of the collider call, -1 unknown
 };
 
+// A heightfield (dGeomHeightfieldDataBuild* + placeable dCreateHeightfield)
+// with the caches of dxHeightfieldData::SetData (ode/src/heightfield.cpp:107-143).
+struct DevHeightfield {
+  int nx, nz, wrap, h_off;             // samples; wrap mode; first sample in the sample array
+  float width, depth, scale, offset, thickness;
+  float sw, sd, inv_sw, inv_sd, zx, half_w, half_d;
+  float pos[3], pad;
+  float R[12];                         // placement, 3x4 row-major
+};
+
 // Static description of one world inside the batch.
 struct WorldDesc {
   int body_off, nb, geom_off, ng, joint_off, njp;
@@ -100,6 +111,8 @@ struct BatchDev {
   const float4* gpos;                  // static placement (geoms without body)
   const int* gsurf;
   const DevSurface* surfaces;
+  const DevHeightfield* hfs;           // heightfields (geom param x = index)
+  const float* hf_heights;             // their samples, x fastest
 
   // persistent joints and their adjacency
   const DevJoint* joints;              // [nj_total]
@@ -110,6 +123,7 @@ struct BatchDev {
   int n_ctrl_steps;
   const float* joint_torque;           // [S][nj_total][2]
   const float* body_force;             // [S][nb_total][6]
+  const float* joint_stop;             // [S][nj_total] limot1 lostop = histop (NaN: the joint's own)
   int step_counter_base;
 
   // per-step scratch (capacity-sized per world)

@@ -1,0 +1,377 @@
+// heightfield.cuh -- dCollideHeightfield (ode/src/heightfield.cpp:1677-1853)
+// and dCollideHeightfieldZone (:952-1676) for sphere, box and capsule geoms,
+// FP32 on the device (the reference's dSINGLE build: dEpsilon = FLT_EPSILON).
+//
+// One lane runs one (heightfield, geom) pair: the geom is moved into the
+// heightfield's frame (Y up, origin at the field's centre), the sample zone
+// under its AABB is gathered into lane-local arrays, the zone's triangles
+// that reach above the geom's lowest point are grouped into planes (equal
+// plane definitions within dEpsilon), the planes are sorted by height, each
+// plane is collided with the geom's plane collider and every contact is kept
+// if it lies over one of the plane's triangles (IsOnHeightfield2). Geoms
+// larger than 1.5 cells then test the remaining triangle vertices with the
+// geom's point-depth function. The edge pass is compiled out in the
+// reference and here. The zone is limited to kHFZone x kHFZone samples; a
+// larger one reports overflow and yields no contacts.
+#pragma once
+#include "collide.cuh"
+#include "engine_types.cuh"
+
+namespace og {
+
+constexpr int kHFZone = 10;                                  // samples per axis
+constexpr int kHFMaxTri = 2 * (kHFZone - 1) * (kHFZone - 1);
+constexpr int kHFMaxcPerCell = 10;                           // HEIGHTFIELDMAXCONTACTPERCELL
+constexpr float kHFEps = 1.1920928955078125e-07f;            // FLT_EPSILON
+
+// GetHeight(int, int) (heightfield.cpp:302-364)
+OG_D float hf_sample(const DevHeightfield& H, const float* heights, int x, int z) {
+  if (H.wrap == 0) {
+    x = x < 0 ? 0 : (x > H.nx - 1 ? H.nx - 1 : x);
+    z = z < 0 ? 0 : (z > H.nz - 1 ? H.nz - 1 : z);
+  } else {
+    x %= H.nx - 1;
+    z %= H.nz - 1;
+    if (x < 0) x += H.nx - 1;
+    if (z < 0) z += H.nz - 1;
+  }
+  return heights[H.h_off + x + z * H.nx] * H.scale + H.offset;
+}
+
+// IsOnHeightfield2 (heightfield.cpp:241-299); corner = A (up) or D (down)
+OG_D bool hf_on_triangle(const DevHeightfield& H, const float* corner, int cx, int cz, const float* pos,
+                         bool up) {
+  if (up) {
+    const float minx = corner[0];
+    if (pos[0] < minx) return false;
+    const float maxx = (cx + 1) * H.sw;
+    if (pos[0] >= maxx) return false;
+    const float minz = corner[2];
+    if (pos[2] < minz) return false;
+    const float maxz = (cz + 1) * H.sd;
+    if (pos[2] >= maxz) return false;
+    return (maxz - pos[2]) > (pos[0] - minx) * H.zx;
+  }
+  const float maxx = corner[0];
+  if (pos[0] >= maxx) return false;
+  const float minx = (cx - 1) * H.sw;
+  if (pos[0] < minx) return false;
+  const float maxz = corner[2];
+  if (pos[2] >= maxz) return false;
+  const float minz = (cz - 1) * H.sd;
+  if (pos[2] < minz) return false;
+  return (maxz - pos[2]) <= (pos[0] - minx) * H.zx;
+}
+
+// computeAABB of sphere / box / capsule (sphere.cpp:59-67, box.cpp:60-78,
+// capsule.cpp:60-74)
+OG_D void geom_aabb(const GeomView& g, float* aabb) {
+  const float* R = g.R;
+  float xr, yr, zr;
+  if (g.type == G_SPHERE) {
+    xr = yr = zr = g.p[0];
+  } else if (g.type == G_BOX) {
+    xr = 0.5f * (fabsf(R[0] * g.p[0]) + fabsf(R[1] * g.p[1]) + fabsf(R[2] * g.p[2]));
+    yr = 0.5f * (fabsf(R[4] * g.p[0]) + fabsf(R[5] * g.p[1]) + fabsf(R[6] * g.p[2]));
+    zr = 0.5f * (fabsf(R[8] * g.p[0]) + fabsf(R[9] * g.p[1]) + fabsf(R[10] * g.p[2]));
+  } else {
+    xr = fabsf(R[2] * g.p[1]) * 0.5f + g.p[0];
+    yr = fabsf(R[6] * g.p[1]) * 0.5f + g.p[0];
+    zr = fabsf(R[10] * g.p[1]) * 0.5f + g.p[0];
+  }
+  aabb[0] = g.pos[0] - xr; aabb[1] = g.pos[0] + xr;
+  aabb[2] = g.pos[1] - yr; aabb[3] = g.pos[1] + yr;
+  aabb[4] = g.pos[2] - zr; aabb[5] = g.pos[2] + zr;
+}
+
+// dGeomSpherePointDepth (sphere.cpp:95-105), dGeomBoxPointDepth
+// (box.cpp:109-172), dGeomCapsulePointDepth (capsule.cpp:104-126)
+OG_D float geom_point_depth(const GeomView& g, const float* v) {
+  const float* pos = g.pos;
+  const float* R = g.R;
+  if (g.type == G_SPHERE) {
+    return g.p[0] - sqrtf((v[0] - pos[0]) * (v[0] - pos[0]) + (v[1] - pos[1]) * (v[1] - pos[1]) +
+                          (v[2] - pos[2]) * (v[2] - pos[2]));
+  }
+  if (g.type == G_BOX) {
+    const float p[3] = {v[0] - pos[0], v[1] - pos[1], v[2] - pos[2]};
+    float q[3], dist[6];
+    mul1_331(q, R, p);
+    bool inside = true;
+    for (int i = 0; i < 3; i++) {
+      const float side = g.p[i] * 0.5f;
+      dist[i] = side - q[i];
+      dist[i + 3] = side + q[i];
+      if ((dist[i] < 0.f) || (dist[i + 3] < 0.f)) inside = false;
+    }
+    if (inside) {
+      float smallest = (float)(unsigned)-1;
+      for (int i = 0; i < 6; i++)
+        if (dist[i] < smallest) smallest = dist[i];
+      return smallest;
+    }
+    float largest = 0.f;
+    for (int i = 0; i < 6; i++)
+      if (dist[i] > largest) largest = dist[i];
+    return -largest;
+  }
+  float a[3] = {v[0] - pos[0], v[1] - pos[1], v[2] - pos[2]};
+  float beta = a[0] * R[2] + a[1] * R[6] + a[2] * R[10];
+  const float lz2 = g.p[1] * 0.5f;
+  if (beta < -lz2) beta = -lz2;
+  else if (beta > lz2) beta = lz2;
+  a[0] = pos[0] + beta * R[2];
+  a[1] = pos[1] + beta * R[6];
+  a[2] = pos[2] + beta * R[10];
+  return g.p[0] - sqrtf((v[0] - a[0]) * (v[0] - a[0]) + (v[1] - a[1]) * (v[1] - a[1]) +
+                        (v[2] - a[2]) * (v[2] - a[2]));
+}
+
+OG_D int geom_plane_collide(const GeomView& g, const GeomView& pl, unsigned flags, Contact* c) {
+  if (g.type == G_SPHERE) return collide_sphere_plane(g, pl, c);
+  if (g.type == G_BOX) return collide_box_plane(g, pl, flags, c);
+  return collide_capsule_plane(g, pl, flags, c);
+}
+
+// dCollideHeightfieldZone (heightfield.cpp:952-1676); g in heightfield space.
+// Returns the contact count, or -1 when the zone exceeds the lane buffers.
+OG_D int hf_zone(const DevHeightfield& H, const float* heights, int minX, int maxX, int minZ, int maxZ,
+                 const GeomView& g, const float* aabb, int max_contacts, unsigned flags, Contact* out) {
+  const int numX = (maxX - minX) + 1, numZ = (maxZ - minZ) + 1;
+  if (numX > kHFZone || numZ > kHFZone || numX < 1 || numZ < 1) return -1;
+  const float minO2 = aabb[2], maxO2 = aabb[3];
+  float vh[kHFZone * kHFZone];           // sample heights of the zone
+  unsigned char vstate[kHFZone * kHFZone];
+  float maxY = -INFINITY, minY = INFINITY;
+  for (int xl = 0; xl < numX; ++xl)
+    for (int zl = 0; zl < numZ; ++zl) {
+      const float h = hf_sample(H, heights, minX + xl, minZ + zl);
+      vh[xl * numZ + zl] = h;
+      maxY = fmaxf(maxY, h);
+      minY = fminf(minY, h);
+    }
+  if (minO2 - maxY > -kHFEps) return 0;      // totally above
+  if (minY - maxO2 > -kHFEps) {              // totally under
+    out[0].pos[0] = g.pos[0]; out[0].pos[1] = minY; out[0].pos[2] = g.pos[2];
+    out[0].normal[0] = 0.f; out[0].normal[1] = -1.f; out[0].normal[2] = 0.f;
+    out[0].depth = minY - maxO2;
+    return 1;
+  }
+  bool further = false;
+  {
+    const float xratio = (aabb[1] - aabb[0]) * H.inv_sw;
+    if (xratio > 1.5f) further = true;
+    else if ((aabb[5] - aabb[4]) * H.inv_sd > 1.5f) further = true;
+  }
+  // triangles: vertex indices packed as i0 | i1 << 8 | i2 << 16 | up << 24
+  unsigned tv[kHFMaxTri];
+  float4 tp[kHFMaxTri];                  // plane (n, d)
+  float tmax[kHFMaxTri];                 // highest vertex
+  unsigned char tstate[kHFMaxTri];
+  int numTri = 0;
+  const int maxXl = maxX - minX, maxZl = maxZ - minZ;
+  for (int xl = 0; xl < maxXl; ++xl) {
+    for (int zl = 0; zl < maxZl; ++zl) {
+      const int ia = xl * numZ + zl, ib = (xl + 1) * numZ + zl;
+      const int ic = xl * numZ + zl + 1, id = (xl + 1) * numZ + zl + 1;
+      const float ah = vh[ia], bh = vh[ib], ch = vh[ic], dh = vh[id];
+      const bool ac = ah > minO2, bc = bh > minO2, cc = ch > minO2, dc = dh > minO2;
+      vstate[ia] = !ac; vstate[ib] = !bc; vstate[ic] = !cc; vstate[id] = !dc;
+      if (ac || bc || cc) {
+        tv[numTri] = (unsigned)ia | ((unsigned)ib << 8) | ((unsigned)ic << 16) | (1u << 24);
+        float m = ah > bh ? ah : bh;
+        tmax[numTri] = ch > m ? ch : m;
+        tstate[numTri] = 0;
+        ++numTri;
+      }
+      if (bc || cc || dc) {
+        tv[numTri] = (unsigned)id | ((unsigned)ib << 8) | ((unsigned)ic << 16);
+        float m = dh > bh ? dh : bh;
+        tmax[numTri] = ch > m ? ch : m;
+        tstate[numTri] = 0;
+        ++numTri;
+      }
+      if (further && (bc || cc) && (ah > ch && ah > bh && dh > ch && dh > bh)) {
+        vstate[ib] = 1;   // concave edge BC
+        vstate[ic] = 1;
+      }
+    }
+  }
+  auto vtx = [&](int i, float* v) {
+    const int xl = i / numZ, zl = i - xl * numZ;
+    v[0] = (minX + xl) * H.sw;
+    v[1] = vh[i];
+    v[2] = (minZ + zl) * H.sd;
+  };
+  // pass 1: planes of the triangles
+  for (int k = 0; k < numTri; ++k) {
+    float v0[3], v1[3], v2[3];
+    vtx(tv[k] & 0xff, v0);
+    vtx((tv[k] >> 8) & 0xff, v1);
+    vtx((tv[k] >> 16) & 0xff, v2);
+    const float e1[3] = {v2[0] - v0[0], v2[1] - v0[1], v2[2] - v0[2]};
+    const float e2[3] = {v1[0] - v0[0], v1[1] - v0[1], v1[2] - v0[2]};
+    float n[3];
+    if (tv[k] >> 24) cross3(n, e1, e2);
+    else cross3(n, e2, e1);
+    const float il = 1.0f / sqrtf(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+    n[0] *= il; n[1] *= il; n[2] *= il;
+    tp[k] = make_float4(n[0], n[1], n[2], dot3(n, v0));
+  }
+  // group by equal plane definition, in triangle order
+  unsigned char members[kHFMaxTri];      // triangles, grouped by plane
+  unsigned char pfirst[kHFMaxTri], pcount[kHFMaxTri];
+  float pmax[kHFMaxTri];
+  unsigned char porder[kHFMaxTri];       // planes in sorted order
+  int numPlanes = 0, nmem = 0;
+  for (int k = 0; k < numTri; ++k) {
+    if (tstate[k]) continue;
+    const float4 b = tp[k];
+    pfirst[numPlanes] = (unsigned char)nmem;
+    members[nmem++] = (unsigned char)k;
+    int cnt = 1;
+    float mx = tmax[k];
+    for (int m = k + 1; m < numTri; ++m) {
+      if (tstate[m]) continue;
+      const float4 t = tp[m];
+      if (fabsf(b.y - t.y) < kHFEps && fabsf(b.w - t.w) < kHFEps && fabsf(b.x - t.x) < kHFEps &&
+          fabsf(b.z - t.z) < kHFEps) {
+        members[nmem++] = (unsigned char)m;
+        ++cnt;
+        tstate[m] = 1;
+        if (tmax[m] > mx) mx = tmax[m];
+      }
+    }
+    tstate[k] = 1;
+    pcount[numPlanes] = (unsigned char)cnt;
+    pmax[numPlanes] = mx;
+    porder[numPlanes] = (unsigned char)numPlanes;
+    ++numPlanes;
+  }
+  // sortPlanes (heightfield.cpp:910-932): bubble sort, descending height
+  {
+    bool swapped = true;
+    while (swapped) {
+      swapped = false;
+      for (int i = 0; i < numPlanes - 1; ++i) {
+        if ((pmax[porder[i]] - pmax[porder[i + 1]]) > kHFEps) {
+          const unsigned char t = porder[i];
+          porder[i] = porder[i + 1];
+          porder[i + 1] = t;
+          swapped = true;
+        }
+      }
+    }
+  }
+  int nc = 0;
+  const unsigned plane_flags = (flags & ~0xffffu) | kHFMaxcPerCell;
+  GeomView pl;
+  pl.type = G_PLANE;
+  for (int k = 0; k < numPlanes; ++k) {
+    const int P = porder[k];
+    const float4 pd = tp[members[pfirst[P]]];
+    pl.p[0] = pd.x; pl.p[1] = pd.y; pl.p[2] = pd.z; pl.p[3] = pd.w;
+    Contact pc[4];   // the plane colliders return at most 4 contacts
+    const int npc = geom_plane_collide(g, pl, plane_flags, pc);
+    bool did = false;
+    for (int i = 0; i < npc; ++i) {
+      for (int bq = 0; bq < pcount[P]; ++bq) {
+        const int t = members[pfirst[P] + bq];
+        const int i0 = tv[t] & 0xff;
+        float corner[3];
+        vtx(i0, corner);
+        const int xl = i0 / numZ, zl = i0 - xl * numZ;
+        if (hf_on_triangle(H, corner, minX + xl, minZ + zl, pc[i].pos, (tv[t] >> 24) != 0)) {
+          Contact& o = out[nc];
+          for (int q = 0; q < 3; ++q) { o.pos[q] = pc[i].pos[q]; o.normal[q] = -pl.p[q]; }
+          o.depth = pc[i].depth;
+          if (++nc == max_contacts) return nc;
+          did = true;
+          break;
+        }
+      }
+    }
+    for (int bq = 0; bq < pcount[P]; ++bq) {
+      const int t = members[pfirst[P] + bq];
+      if (did) {
+        vstate[tv[t] & 0xff] = 1;
+        vstate[(tv[t] >> 8) & 0xff] = 1;
+        vstate[(tv[t] >> 16) & 0xff] = 1;
+      } else {
+        tstate[t] = 0;
+      }
+    }
+  }
+  // pass 2: triangle vertices against the geom's point depth
+  if (further) {
+    for (int k = 0; k < numTri; ++k) {
+      if (tstate[k]) continue;
+      for (int i = 0; i < 3; ++i) {
+        const int vi = (tv[k] >> (8 * i)) & 0xff;
+        if (vstate[vi]) continue;
+        float v[3];
+        vtx(vi, v);
+        const float depth = geom_point_depth(g, v);
+        if (depth > kHFEps) {
+          Contact& o = out[nc];
+          o.pos[0] = v[0]; o.pos[1] = v[1]; o.pos[2] = v[2];
+          o.normal[0] = -tp[k].x; o.normal[1] = -tp[k].y; o.normal[2] = -tp[k].z;
+          o.depth = depth;
+          if (++nc == max_contacts) return nc;
+          vstate[vi] = 1;
+        }
+      }
+    }
+  }
+  return nc;
+}
+
+// dCollideHeightfield(hf, g): placeable heightfield, centred origin. Returns
+// the contact count (normals as the reference: pointing into the field), or
+// -1 when the zone under the geom exceeds the lane buffers.
+__device__ __noinline__ int collide_heightfield(const DevHeightfield& H, const float* heights, const GeomView& g,
+                                               unsigned flags,
+                             Contact* out) {
+  const int maxc = (int)(flags & 0xffff);
+  if (maxc < 1) return 0;
+  const float p0[3] = {g.pos[0] - H.pos[0], g.pos[1] - H.pos[1], g.pos[2] - H.pos[2]};
+  GeomView g2 = g;
+  mul1_331(g2.pos, H.R, p0);
+  for (int i = 0; i < 3; ++i) {
+    for (int j = 0; j < 3; ++j)
+      g2.R[i * 4 + j] = H.R[0 * 4 + i] * g.R[0 * 4 + j] + H.R[1 * 4 + i] * g.R[1 * 4 + j] +
+                        H.R[2 * 4 + i] * g.R[2 * 4 + j];
+    g2.R[i * 4 + 3] = 0.f;
+  }
+  g2.pos[0] += H.half_w;
+  g2.pos[2] += H.half_d;
+  float aabb[6];
+  geom_aabb(g2, aabb);
+  const bool wrapped = H.wrap != 0;
+  if (!wrapped) {
+    if (aabb[0] > H.width || aabb[4] > H.depth) return 0;
+    if (aabb[1] < 0.f || aabb[5] < 0.f) return 0;
+  }
+  int nMinX = (int)floorf(nextafterf(aabb[0] * H.inv_sw, -INFINITY));
+  int nMaxX = (int)ceilf(nextafterf(aabb[1] * H.inv_sw, INFINITY));
+  int nMinZ = (int)floorf(nextafterf(aabb[4] * H.inv_sd, -INFINITY));
+  int nMaxZ = (int)ceilf(nextafterf(aabb[5] * H.inv_sd, INFINITY));
+  if (!wrapped) {
+    nMinX = nMinX > 0 ? nMinX : 0;
+    nMaxX = nMaxX < H.nx - 1 ? nMaxX : H.nx - 1;
+    nMinZ = nMinZ > 0 ? nMinZ : 0;
+    nMaxZ = nMaxZ < H.nz - 1 ? nMaxZ : H.nz - 1;
+  }
+  const int n = hf_zone(H, heights, nMinX, nMaxX, nMinZ, nMaxZ, g2, aabb, maxc, flags, out);
+  for (int i = 0; i < n; ++i) {
+    const float q[3] = {out[i].pos[0] - H.half_w, out[i].pos[1], out[i].pos[2] - H.half_d};
+    float w[3];
+    mul0_331(w, H.R, q);
+    for (int k = 0; k < 3; ++k) out[i].pos[k] = w[k] + H.pos[k];
+    const float nn[3] = {out[i].normal[0], out[i].normal[1], out[i].normal[2]};
+    mul0_331(out[i].normal, H.R, nn);
+  }
+  return n;
+}
+
+}  // namespace og

@@ -199,21 +199,22 @@ struct JointInfo1 {
 
 // getInfo1: contact (ode/src/joints/contact.cpp:47-71), ball (ball.cpp:56-60),
 // hinge (hinge.cpp:54-74), hinge2 (hinge2.cpp:81-101).
-OG_D JointInfo1 persistent_info1(const DevJoint& J, const BodyRef& B1, const BodyRef* B2) {
+// lm1: the joint's limot1 for this step (stops may differ from J.lm1).
+OG_D JointInfo1 persistent_info1(const DevJoint& J, const DevLimot& lm1, const BodyRef& B1, const BodyRef* B2) {
   JointInfo1 r{0, 0, 0, 0.f, 0.f};
   switch (J.type) {
     case J_BALL: r.m = 3; break;
     case J_HINGE: {
-      r.m = (J.lm1.fmax > 0.f) ? 6 : 5;
-      if (limot_tested(J.lm1)) {
-        if (limot_test(J.lm1, hinge_angle(B1, B2, J), r.limit1, r.err1)) r.m = 6;
+      r.m = (lm1.fmax > 0.f) ? 6 : 5;
+      if (limot_tested(lm1)) {
+        if (limot_test(lm1, hinge_angle(B1, B2, J), r.limit1, r.err1)) r.m = 6;
       }
       break;
     }
     case J_HINGE2: {
       r.m = 4;
-      if (limot_tested(J.lm1) && B2) limot_test(J.lm1, hinge2_angle(B1, *B2, J), r.limit1, r.err1);
-      if (r.limit1 || J.lm1.fmax > 0.f) r.m++;
+      if (limot_tested(lm1) && B2) limot_test(lm1, hinge2_angle(B1, *B2, J), r.limit1, r.err1);
+      if (r.limit1 || lm1.fmax > 0.f) r.m++;
       if (J.lm2.fmax > 0.f) r.m++;
       break;
     }
@@ -313,7 +314,7 @@ OG_D void contact_info2(const DevContact& ct, const DevSurface& S, int the_m, co
 // getInfo2 of the persistent joints: ball (ode/src/joints/ball.cpp:63-70),
 // hinge (hinge.cpp:77-149), hinge2 (hinge2.cpp:109-180). Up to two motor
 // torques (body-1 sense) are returned in tq1/tq2 for the caller to apply.
-OG_D void persistent_info2(const DevJoint& J, const JointInfo1& i1, const BodyRef& B1,
+OG_D void persistent_info2(const DevJoint& J, const DevLimot& lm1, const JointInfo1& i1, const BodyRef& B1,
                            const BodyRef* B2, Info2& in, LimotTorque& tq1, LimotTorque& tq2) {
   switch (J.type) {
     case J_BALL:
@@ -336,7 +337,7 @@ OG_D void persistent_info2(const DevJoint& J, const JointInfo1& i1, const BodyRe
       const float k = in.fps * in.erp;
       in.c(3) = k * dot3(b, p);
       in.c(4) = k * dot3(b, q);
-      limot_add(J.lm1, i1.limit1, i1.err1, B2 != nullptr, B1, B2, in, 5, ax1, tq1);
+      limot_add(lm1, i1.limit1, i1.err1, B2 != nullptr, B1, B2, in, 5, ax1, tq1);
       break;
     }
     case J_HINGE2: {
@@ -352,7 +353,7 @@ OG_D void persistent_info2(const DevJoint& J, const JointInfo1& i1, const BodyRe
       if (B2) for (int k = 0; k < 3; ++k) in.J2a(3, k) = -q[k];
       const float k = in.fps * in.erp;
       in.c(3) = k * (J.c0 * sn - J.s0 * cs);
-      const int row = 4 + limot_add(J.lm1, i1.limit1, i1.err1, true, B1, B2, in, 4, ax1, tq1);
+      const int row = 4 + limot_add(lm1, i1.limit1, i1.err1, true, B1, B2, in, 4, ax1, tq1);
       limot_add(J.lm2, 0, 0.f, true, B1, B2, in, row, ax2, tq2);
       in.cfm(0) = J.susp_cfm;
       break;

@@ -49,10 +49,26 @@ OG_D void phase_body_prologue(const BatchDev& d, const WorldDesc& D, int lane) {
   }
 }
 
+// limot1 as getInfo sees it this step: the stored one with the step's stops
+// (when given) in place of lostop / histop.
+OG_D DevLimot step_limot1(const DevJoint& J, const float* stops, int ord) {
+  DevLimot L = J.lm1;
+  if (stops && (J.type == J_HINGE || J.type == J_HINGE2)) {
+    const float v = stops[ord];
+    if (!isnan(v)) { L.lostop = v; L.histop = v; }
+  }
+  return L;
+}
+
 // Phase 4: getInfo1 / getInfo2 over the joints in island order. Returns the
 // total row count M (or -1 when it exceeds the world's capacity).
-OG_D int phase_rows(const BatchDev& d, const WorldDesc& D, int w, int nj, int nisl, int lane,
+OG_D int phase_rows(const BatchDev& d, const WorldDesc& D, int w, int nj, int nisl, int lane, int step,
                       float* dbg_rows) {
+  // per-step stops (dJointSetHinge{,2}Param lo/hi stop before the step)
+  const int njt = d.world[d.n_worlds - 1].joint_off + d.world[d.n_worlds - 1].njp;
+  const float* stops = (d.joint_stop && d.n_ctrl_steps > 0)
+                           ? d.joint_stop + (size_t)(step % d.n_ctrl_steps) * njt + D.joint_off
+                           : nullptr;
   const int jl_off = D.joint_off + D.contact_off;
   const float h1 = 1.0f / D.dt;
   // pass 1: m per joint, prefix -> first row
@@ -64,10 +80,11 @@ OG_D int phase_rows(const BatchDev& d, const WorldDesc& D, int w, int nj, int ni
       const int ord = d.jlist[jl_off + k] & 0x3fffffff;
       if (ord < D.njp) {
         const DevJoint& J = d.joints[D.joint_off + ord];
+        const DevLimot lm1 = step_limot1(J, stops, ord);
         BodyRef B1, B2;
         load_body_ref(d, D.body_off + J.b1, B1);
         if (J.b2 >= 0) load_body_ref(d, D.body_off + J.b2, B2);
-        m = persistent_info1(J, B1, J.b2 >= 0 ? &B2 : nullptr).m;
+        m = persistent_info1(J, lm1, B1, J.b2 >= 0 ? &B2 : nullptr).m;
       } else {
         m = contact_info1(d.surfaces[d.contacts[D.contact_off + ord - D.njp].surface]);
       }
@@ -155,9 +172,10 @@ OG_D int phase_rows(const BatchDev& d, const WorldDesc& D, int w, int nj, int ni
       const BodyRef* pB2 = b2 >= 0 ? &B2 : nullptr;
       if (ord < D.njp) {
         const DevJoint& J = d.joints[D.joint_off + ord];
-        const JointInfo1 i1 = persistent_info1(J, B1, pB2);
+        const DevLimot lm1 = step_limot1(J, stops, ord);
+        const JointInfo1 i1 = persistent_info1(J, lm1, B1, pB2);
         LimotTorque t1{{0.f, 0.f, 0.f}, 0}, t2{{0.f, 0.f, 0.f}, 0};
-        persistent_info2(J, i1, B1, pB2, in, t1, t2);
+        persistent_info2(J, lm1, i1, B1, pB2, in, t1, t2);
         // powered motor pushing against a limit adds torque inside getInfo2
         // (joint.cpp:612-660); concurrent additions are rare and use atomics
         for (int t = 0; t < 2; ++t) {
@@ -409,7 +427,7 @@ OG_D void world_collide(const BatchDev& d, int w, int step, const WarpSmem& S, i
   __syncwarp();
 }
 
-OG_D void world_setup(const BatchDev& d, int w, const WarpSmem& S, int lane, const StepOptions& opt) {
+OG_D void world_setup(const BatchDev& d, int w, int step, const WarpSmem& S, int lane, const StepOptions& opt) {
   const WorldDesc D = d.world[w];
   const int nc = d.ncontacts[w];
   int M = 0, nisl = 0;
@@ -418,7 +436,7 @@ OG_D void world_setup(const BatchDev& d, int w, const WarpSmem& S, int lane, con
     M = -1;
   } else {
     const int nj = phase_islands(d, D, w, opt.host_adjacency ? 0 : nc, D.njp + nc, S, lane, &nisl);
-    M = phase_rows(d, D, w, nj, nisl, lane, opt.dbg_rows);
+    M = phase_rows(d, D, w, nj, nisl, lane, step, opt.dbg_rows);
   }
   if (M > 0) phase_row_setup(d, D, M, S, lane, opt.dbg_rows);
   if (lane == 0) {

@@ -20,6 +20,7 @@
 // that sequence (a friction row and its normal row share their bodies).
 #pragma once
 #include "collide.cuh"
+#include "heightfield.cuh"
 #include "joints.cuh"
 
 namespace og {
@@ -186,7 +187,24 @@ OG_D int phase_collide(const BatchDev& d, const WorldDesc& D, int w, const WarpS
       GeomView vi, vk;
       geom_view(d, D, i, vi);
       geom_view(d, D, k, vk);
-      cnt = collide_primitive(vi, vk, (unsigned)D.max_contacts, cc);
+      if (vi.type == G_HEIGHTFIELD || vk.type == G_HEIGHTFIELD) {
+        // dCollide(gi, gk): the heightfield collider runs with the field first
+        // and the normals are negated when the call was reversed
+        const bool rev = vk.type == G_HEIGHTFIELD;
+        const GeomView& hv = rev ? vk : vi;
+        const GeomView& ov = rev ? vi : vk;
+        if (ov.type == G_SPHERE || ov.type == G_BOX || ov.type == G_CAPSULE) {
+          cnt = collide_heightfield(d.hfs[(int)hv.p[0]], d.hf_heights, ov, (unsigned)D.max_contacts, cc);
+          if (cnt < 0) { atomicOr(&d.status[w], ST_HF_ZONE); cnt = 0; }
+          if (rev)
+            for (int c = 0; c < cnt; ++c) {
+              cc[c].normal[0] = -cc[c].normal[0]; cc[c].normal[1] = -cc[c].normal[1];
+              cc[c].normal[2] = -cc[c].normal[2];
+            }
+        }
+      } else {
+        cnt = collide_primitive(vi, vk, (unsigned)D.max_contacts, cc);
+      }
       const int si = d.gsurf[gi], sk = d.gsurf[gk];
       surf = si > sk ? si : sk;
     }

@@ -41,6 +41,7 @@ def _declare(L):
         "odegpuBatchSynchronize": (i, [v]),
         "odegpuBatchSetTiming": (i, [v, i]),
         "odegpuBatchSetControlsF32": (i, [v, i, v, v]),
+        "odegpuBatchSetJointStops": (i, [v, i, _P(d)]),
         "odegpuBatchRolloutForward": (i, [v, i, i]),
         "odegpuBatchRolloutBackward": (i, [v, v, v, v, v]),
         "odegpuBatchAdjointStatus": (i, [v, _P(i)]),

@@ -70,6 +70,7 @@ class CScene(C.Structure):
         ("joint_axis1", _P(C.c_double)), ("joint_axis2", _P(C.c_double)),
         ("joint_param", _P(C.c_double)),
         ("n_ctrl_steps", C.c_int), ("joint_torque", _P(C.c_double)), ("body_force", _P(C.c_double)),
+        ("joint_stop", _P(C.c_double)),
     ]
 
 
@@ -231,13 +232,16 @@ class Scene:
         self.n_ctrl_steps = 0
         self.joint_torque = None
         self.body_force = None
+        self.joint_stop = None
         self.nb_total = int(self.body_off[-1])
         self.nj_total = int(self.joint_off[-1])
         self.ng_total = int(self.geom_off[-1])
         self._refresh()
 
-    def set_controls(self, joint_torque=None, body_force=None):
-        """Per-step controls: joint_torque [S][nj_total][2], body_force [S][nb_total][6]."""
+    def set_controls(self, joint_torque=None, body_force=None, joint_stop=None):
+        """Per-step controls: joint_torque [S][nj_total][2], body_force
+        [S][nb_total][6], joint_stop [S][nj_total] (hinge / hinge2 limot1
+        lostop = histop before the step; NaN keeps the joint's own stops)."""
         S = 0
         if joint_torque is not None:
             self.joint_torque = np.ascontiguousarray(joint_torque, dtype=np.float64)
@@ -245,6 +249,9 @@ class Scene:
         if body_force is not None:
             self.body_force = np.ascontiguousarray(body_force, dtype=np.float64)
             S = self.body_force.shape[0]
+        if joint_stop is not None:
+            self.joint_stop = np.ascontiguousarray(joint_stop, dtype=np.float64)
+            S = self.joint_stop.shape[0]
         self.n_ctrl_steps = S
         self._refresh()
 
@@ -268,6 +275,7 @@ class Scene:
         c.n_ctrl_steps = self.n_ctrl_steps
         c.joint_torque = _ptr(self.joint_torque, C.c_double)
         c.body_force = _ptr(self.body_force, C.c_double)
+        c.joint_stop = _ptr(self.joint_stop, C.c_double)
         self.c = c
 
     _ARRAYS = ("body_off", "geom_off", "joint_off", "body_pos", "body_q", "body_lvel",
@@ -288,6 +296,13 @@ class Scene:
             out["joint_torque"] = self.joint_torque
         if self.body_force is not None:
             out["body_force"] = self.body_force
+        if self.joint_stop is not None:
+            out["joint_stop"] = self.joint_stop
+        if self.n_heightfields > 0:
+            out["hf_meta"] = np.array([[H.nx, H.nz, H.width, H.depth, H.scale, H.offset, H.thickness, H.wrap,
+                                        *H.pos[:], *H.R[:]] for H in self.heightfields[:self.n_heightfields]])
+            for i, h in enumerate(self.hf_heights):
+                out[f"hf_heights_{i}"] = h
         return out
 
     @classmethod
@@ -316,16 +331,32 @@ class Scene:
         self.hf_heights = []
         self.heightfields = (Heightfield * 1)()
         self.n_heightfields = 0
+        if "hf_meta" in a:
+            meta = np.asarray(a["hf_meta"])
+            self.heightfields = (Heightfield * len(meta))()
+            for i, r in enumerate(meta):
+                h = np.ascontiguousarray(a[f"hf_heights_{i}"], dtype=np.float64)
+                self.hf_heights.append(h)
+                H = self.heightfields[i]
+                H.nx, H.nz = int(r[0]), int(r[1])
+                H.width, H.depth, H.scale, H.offset, H.thickness = (float(x) for x in r[2:7])
+                H.wrap = int(r[7])
+                H.heights = h.ctypes.data_as(_P(C.c_double))
+                H.pos[:] = [float(x) for x in r[8:11]]
+                H.R[:] = [float(x) for x in r[11:20]]
+            self.n_heightfields = len(meta)
         self.n_ctrl_steps = 0
         self.joint_torque = None
         self.body_force = None
+        self.joint_stop = None
         self.nb_total = int(self.body_off[-1])
         self.nj_total = int(self.joint_off[-1])
         self.ng_total = int(self.geom_off[-1])
         jt = a["joint_torque"] if "joint_torque" in a else None
         bf = a["body_force"] if "body_force" in a else None
-        if jt is not None or bf is not None:
-            self.set_controls(jt, bf)
+        js = a["joint_stop"] if "joint_stop" in a else None
+        if jt is not None or bf is not None or js is not None:
+            self.set_controls(jt, bf, js)
         else:
             self._refresh()
         return self
@@ -571,3 +602,97 @@ def box_tower(n_worlds=1, height=5, seed=9, spacing=4.0, shrink=0.8, yaw=0.3):
             b.add_geom(w, GEOM_BOX, bi, (L, L, H), s)
             z += H - 1e-3
     return b.build()
+
+
+def fractal_heights(n=256, sigma=0.3, beta=3.0, seed=11):
+    """Seeded fractal terrain: white noise shaped to a 1/f^beta power spectrum
+    (FFT), normalised to standard deviation sigma; [n, n] (z rows, x columns)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    noise = rng.standard_normal((n, n))
+    fx = np.fft.fftfreq(n)[None, :]
+    fz = np.fft.fftfreq(n)[:, None]
+    f = np.sqrt(fx * fx + fz * fz)
+    f[0, 0] = 1.0
+    spec = np.fft.fft2(noise) / f ** (beta / 2)
+    spec[0, 0] = 0.0
+    h = np.real(np.fft.ifft2(spec))
+    return h * (sigma / h.std())
+
+
+# rotation about x by +90 degrees: the heightfield's local y (up) becomes world z
+HF_Z_UP = ((1.0, 0.0, 0.0), (0.0, 0.0, -1.0), (0.0, 1.0, 0.0))
+
+
+def _hf_height_at(h, spacing, wx, wy):
+    """Bilinear terrain height under world (wx, wy) for a centred HF_Z_UP field."""
+    n = h.shape[0]
+    half = 0.5 * spacing * (n - 1)
+    lx, lz = wx + half, -wy + half
+    i, k = lx / spacing, lz / spacing
+    i0, k0 = int(np.clip(np.floor(i), 0, n - 2)), int(np.clip(np.floor(k), 0, n - 2))
+    fi, fk = i - i0, k - k0
+    return ((1 - fi) * (1 - fk) * h[k0, i0] + fi * (1 - fk) * h[k0, i0 + 1] +
+            (1 - fi) * fk * h[k0 + 1, i0] + fi * fk * h[k0 + 1, i0 + 1])
+
+
+def vehicles(n_worlds=2048, seed=10, steps=300, hf_samples=256, spacing=0.5, sigma=0.3):
+    """Vehicle batch: per world one car, a 2.0 x 1.0 x 0.5 m box chassis of
+    1000 kg on four sphere wheels (r 0.35 m, 20 kg) attached by hinge2 joints
+    (axis 1 vertical for steering and suspension, axis 2 the wheel axle;
+    suspension ERP 0.4, CFM 0.01), on one shared seeded fractal heightfield of
+    hf_samples^2 samples at `spacing` m (heights sigma), placeable with its up
+    axis along world z. Wheel surface mu 1.2, mu2 0.8 (Mu2 | Approx1 | SoftERP |
+    SoftCFM). Per step: steering angle U[-0.4, 0.4] rad on the front wheels as
+    limot1 lostop = histop (the rear wheels' steering held at 0 the same way),
+    and throttle U[0,1] * 400 N m as hinge2 torque2 on each rear wheel
+    (dJointAddHinge2Torques). Each car starts at a seeded spot and heading of
+    the field, just above the terrain."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    h = fractal_heights(hf_samples, sigma, seed=seed + 1)
+    width = spacing * (hf_samples - 1)
+    b = SceneBuilder()
+    hf = b.add_heightfield(h, width, width, thickness=1.0, pos=(0, 0, 0), R=np.array(HF_Z_UP))
+    s_ground = b.add_surface(CONTACT_MU2 | CONTACT_APPROX1 | CONTACT_SOFT_ERP | CONTACT_SOFT_CFM, 1.2,
+                             mu2=0.8, soft_erp=0.2, soft_cfm=1e-5)
+    r_w, m_w = 0.35, 20.0
+    lx, ly, lz = 2.0, 1.0, 0.5
+    wheel_off = [(0.7, 0.6), (0.7, -0.6), (-0.7, 0.6), (-0.7, -0.6)]   # front left/right, rear
+    drop = 0.3                                                         # wheel centre below chassis
+    for wi in range(n_worlds):
+        w = b.new_world(cfm=1e-5, seed=int(rng.integers(0, 2**32)))
+        b.add_geom(w, GEOM_HEIGHTFIELD, -1, (hf,), s_ground)
+        cx, cy = rng.uniform(-0.4 * width, 0.4 * width, 2)
+        yaw = rng.uniform(0, 2 * math.pi)
+        c, sn = math.cos(yaw), math.sin(yaw)
+        wheels = [(cx + c * ox - sn * oy, cy + sn * ox + c * oy) for ox, oy in wheel_off]
+        ground = max(_hf_height_at(h, spacing, x, y) for x, y in wheels)
+        zc = ground + r_w + 0.05 + drop
+        q = (math.cos(yaw / 2), 0.0, 0.0, math.sin(yaw / 2))
+        m, I = box_mass_total(1000.0, lx, ly, lz)
+        ch = b.add_body(w, (cx, cy, zc), m, I, q=q)
+        b.add_geom(w, GEOM_BOX, ch, (lx, ly, lz), s_ground)
+        axle = (-sn, c, 0.0)
+        for (x, y) in wheels:
+            mw, Iw = sphere_mass_total(m_w, r_w)
+            wb = b.add_body(w, (x, y, zc - drop), mw, Iw, q=q)
+            b.add_geom(w, GEOM_SPHERE, wb, (r_w,), s_ground)
+            p = np.zeros(JOINT_NPARAM)
+            p[0:9] = limot_params(lostop=0.0, histop=0.0)
+            p[9:18] = limot_params()
+            p[18], p[19] = 0.4, 0.01
+            b.add_joint(w, JOINT_HINGE2, ch, wb, anchor=(x, y, zc - drop), axis1=(0, 0, 1), axis2=axle,
+                        param=p)
+    sc = b.build()
+    nj = sc.nj_total
+    steer = rng.uniform(-0.4, 0.4, (steps, n_worlds))
+    throttle = rng.uniform(0.0, 1.0, (steps, n_worlds)) * 400.0
+    stops = np.zeros((steps, nj))
+    tq = np.zeros((steps, nj, 2))
+    for wi in range(n_worlds):
+        j0 = sc.joint_off[wi]
+        stops[:, j0 + 0] = steer[:, wi]
+        stops[:, j0 + 1] = steer[:, wi]
+        tq[:, j0 + 2, 1] = throttle[:, wi]
+        tq[:, j0 + 3, 1] = throttle[:, wi]
+    sc.set_controls(joint_torque=tq, joint_stop=stops)
+    return sc

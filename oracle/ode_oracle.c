@@ -14,6 +14,7 @@
  */
 #define _GNU_SOURCE
 #include <math.h>
+#include <float.h>
 #include <stdlib.h>
 #include <string.h>
 #include <pthread.h>
@@ -947,10 +948,403 @@ static int do_collide(const GeomRef* g1, const GeomRef* g2, unsigned flags, OCon
   return n;
 }
 
-/* Placeholder until the heightfield restatement lands: no contacts. */
+/* ---- heightfield (ode/src/heightfield.cpp, dDOUBLE build: dEpsilon = DBL_EPSILON) ---- */
+
+#define HF_EPS DBL_EPSILON
+#define HF_MAXC_PER_CELL 10   /* HEIGHTFIELDMAXCONTACTPERCELL, ode/src/heightfield.h:14 */
+
+typedef struct {
+  const odegpuHeightfield* H;
+  real sw, sd, inv_sw, inv_sd, zx_aspect, half_w, half_d;
+} HFData;
+
+/* dxHeightfieldData::SetData caches, heightfield.cpp:107-143 */
+static void hf_data(const odegpuHeightfield* H, HFData* D) {
+  D->H = H;
+  D->half_w = H->width / 2.0;
+  D->half_d = H->depth / 2.0;
+  D->sw = H->width / (H->nx - 1.0);
+  D->sd = H->depth / (H->nz - 1.0);
+  D->zx_aspect = D->sd / D->sw;
+  D->inv_sw = 1.0 / D->sw;
+  D->inv_sd = 1.0 / D->sd;
+}
+
+/* GetHeight(int, int), heightfield.cpp:302-364 (double samples) */
+static real hf_height(const HFData* D, int x, int z) {
+  const odegpuHeightfield* H = D->H;
+  if (H->wrap == 0) {
+    if (x < 0) x = 0;
+    if (z < 0) z = 0;
+    if (x > H->nx - 1) x = H->nx - 1;
+    if (z > H->nz - 1) z = H->nz - 1;
+  } else {
+    x %= H->nx - 1;
+    z %= H->nz - 1;
+    if (x < 0) x += H->nx - 1;
+    if (z < 0) z += H->nz - 1;
+  }
+  const real h = H->heights[x + z * H->nx];
+  return h * H->scale + H->offset;
+}
+
+/* IsOnHeightfield2, heightfield.cpp:241-299: is pos over the up (ABC, corner
+ * A) or down (DBC, corner D) triangle of a cell */
+static int hf_on_triangle(const HFData* D, const real* corner, const int* coords, const real* pos, int up) {
+  if (up) {
+    const real minx = corner[0];
+    if (pos[0] < minx) return 0;
+    const real maxx = (coords[0] + 1) * D->sw;
+    if (pos[0] >= maxx) return 0;
+    const real minz = corner[2];
+    if (pos[2] < minz) return 0;
+    const real maxz = (coords[1] + 1) * D->sd;
+    if (pos[2] >= maxz) return 0;
+    return (maxz - pos[2]) > (pos[0] - minx) * D->zx_aspect;
+  } else {
+    const real maxx = corner[0];
+    if (pos[0] >= maxx) return 0;
+    const real minx = (coords[0] - 1) * D->sw;
+    if (pos[0] < minx) return 0;
+    const real maxz = corner[2];
+    if (pos[2] >= maxz) return 0;
+    const real minz = (coords[1] - 1) * D->sd;
+    if (pos[2] < minz) return 0;
+    return (maxz - pos[2]) <= (pos[0] - minx) * D->zx_aspect;
+  }
+}
+
+/* computeAABB of sphere / box / capsule (sphere.cpp:59-67, box.cpp:60-78,
+ * capsule.cpp:60-74) */
+static void geom_aabb(const GeomRef* g, real* aabb) {
+  const real* R = g->R;
+  const real* pos = g->pos;
+  real xr, yr, zr;
+  if (g->type == ODEGPU_GEOM_SPHERE) {
+    xr = yr = zr = g->p[0];
+  } else if (g->type == ODEGPU_GEOM_BOX) {
+    const real* side = g->p;
+    xr = 0.5 * (fabs(R[0] * side[0]) + fabs(R[1] * side[1]) + fabs(R[2] * side[2]));
+    yr = 0.5 * (fabs(R[4] * side[0]) + fabs(R[5] * side[1]) + fabs(R[6] * side[2]));
+    zr = 0.5 * (fabs(R[8] * side[0]) + fabs(R[9] * side[1]) + fabs(R[10] * side[2]));
+  } else {
+    const real radius = g->p[0], lz = g->p[1];
+    xr = fabs(R[2] * lz) * 0.5 + radius;
+    yr = fabs(R[6] * lz) * 0.5 + radius;
+    zr = fabs(R[10] * lz) * 0.5 + radius;
+  }
+  aabb[0] = pos[0] - xr; aabb[1] = pos[0] + xr;
+  aabb[2] = pos[1] - yr; aabb[3] = pos[1] + yr;
+  aabb[4] = pos[2] - zr; aabb[5] = pos[2] + zr;
+}
+
+/* dGeomSpherePointDepth (sphere.cpp:95-105), dGeomBoxPointDepth
+ * (box.cpp:109-172), dGeomCapsulePointDepth (capsule.cpp:104-126) */
+static real geom_point_depth(const GeomRef* g, const real* v) {
+  const real* pos = g->pos;
+  const real* R = g->R;
+  if (g->type == ODEGPU_GEOM_SPHERE) {
+    return g->p[0] - sqrt((v[0] - pos[0]) * (v[0] - pos[0]) + (v[1] - pos[1]) * (v[1] - pos[1]) +
+                          (v[2] - pos[2]) * (v[2] - pos[2]));
+  }
+  if (g->type == ODEGPU_GEOM_BOX) {
+    real p[3] = {v[0] - pos[0], v[1] - pos[1], v[2] - pos[2]}, q[3], dist[6];
+    mul1_331(q, R, p);
+    int inside = 1;
+    for (int i = 0; i < 3; i++) {
+      const real side = g->p[i] * 0.5;
+      dist[i] = side - q[i];
+      dist[i + 3] = side + q[i];
+      if ((dist[i] < 0) || (dist[i + 3] < 0)) inside = 0;
+    }
+    if (inside) {
+      real smallest = (real)(unsigned)-1;
+      for (int i = 0; i < 6; i++)
+        if (dist[i] < smallest) smallest = dist[i];
+      return smallest;
+    }
+    real largest = 0;
+    for (int i = 0; i < 6; i++)
+      if (dist[i] > largest) largest = dist[i];
+    return -largest;
+  }
+  real a[3] = {v[0] - pos[0], v[1] - pos[1], v[2] - pos[2]};
+  real beta = a[0] * R[2] + a[1] * R[6] + a[2] * R[10];
+  const real lz2 = g->p[1] * 0.5;
+  if (beta < -lz2) beta = -lz2;
+  else if (beta > lz2) beta = lz2;
+  a[0] = pos[0] + beta * R[2];
+  a[1] = pos[1] + beta * R[6];
+  a[2] = pos[2] + beta * R[10];
+  return g->p[0] - sqrt((v[0] - a[0]) * (v[0] - a[0]) + (v[1] - a[1]) * (v[1] - a[1]) +
+                        (v[2] - a[2]) * (v[2] - a[2]));
+}
+
+static int geom_plane_collide(const GeomRef* g, const GeomRef* pl, unsigned flags, OContact* c) {
+  switch (g->type) {
+    case ODEGPU_GEOM_SPHERE: return collide_sphere_plane(g, pl, c);
+    case ODEGPU_GEOM_BOX: return collide_box_plane(g, pl, flags, c);
+    default: return collide_capsule_plane(g, pl, flags, c);
+  }
+}
+
+typedef struct {
+  real v[3];
+  int coords[2];
+  int state;
+} HFVertex;
+
+typedef struct {
+  int vi[3];          /* indices into the zone's vertex array */
+  real plane[4];
+  real maxy;
+  int up, state;
+} HFTri;
+
+typedef struct {
+  real plane[4];
+  real maxy;
+  int first, count;   /* triangles of the plane in the member list */
+} HFPlane;
+
+/* dxHeightfield::dCollideHeightfieldZone, heightfield.cpp:952-1676 (the edge
+ * pass is compiled out in the reference). o2 is in heightfield space. */
+static int hf_zone(const HFData* D, int minX, int maxX, int minZ, int maxZ, const GeomRef* o2,
+                   const real* aabb, int max_contacts, unsigned flags, OContact* out) {
+  const int numX = (maxX - minX) + 1, numZ = (maxZ - minZ) + 1;
+  const real minO2 = aabb[2], maxO2 = aabb[3];
+  HFVertex* V = (HFVertex*)calloc((size_t)numX * numZ, sizeof(HFVertex));
+  real maxY = -INFINITY, minY = INFINITY;
+  for (int xl = 0, x = minX; xl < numX; ++x, ++xl) {
+    const real xpos = x * D->sw;
+    for (int zl = 0, z = minZ; zl < numZ; ++z, ++zl) {
+      const real zpos = z * D->sd;
+      const real h = hf_height(D, x, z);
+      HFVertex* hv = &V[xl * numZ + zl];
+      hv->v[0] = xpos; hv->v[1] = h; hv->v[2] = zpos;
+      hv->coords[0] = x; hv->coords[1] = z;
+      maxY = fmax(maxY, h);
+      minY = fmin(minY, h);
+    }
+  }
+  if (minO2 - maxY > -HF_EPS) { free(V); return 0; }      /* totally above */
+  if (minY - maxO2 > -HF_EPS) {                            /* totally under */
+    out[0].pos[0] = o2->pos[0]; out[0].pos[1] = minY; out[0].pos[2] = o2->pos[2];
+    out[0].normal[0] = 0; out[0].normal[1] = -1; out[0].normal[2] = 0;
+    out[0].depth = minY - maxO2;
+    free(V);
+    return 1;
+  }
+  int nc = 0;
+  int further = 0;
+  {
+    const real xratio = (aabb[1] - aabb[0]) * D->inv_sw;
+    if (xratio > 1.5) further = 1;
+    else {
+      const real zratio = (aabb[5] - aabb[4]) * D->inv_sd;
+      if (zratio > 1.5) further = 1;
+    }
+  }
+  const int maxXl = maxX - minX, maxZl = maxZ - minZ;
+  HFTri* T = (HFTri*)calloc((size_t)2 * (maxXl > 0 ? maxXl : 1) * (maxZl > 0 ? maxZl : 1), sizeof(HFTri));
+  int numTri = 0;
+  for (int xl = 0; xl < maxXl; ++xl) {
+    int ic = xl * numZ, id = (xl + 1) * numZ;       /* C, D of z_local 0 */
+    for (int zl = 0; zl < maxZl; ++zl) {
+      const int ia = ic, ib = id;
+      ic = xl * numZ + zl + 1;
+      id = (xl + 1) * numZ + zl + 1;
+      const real ah = V[ia].v[1], bh = V[ib].v[1], ch = V[ic].v[1], dh = V[id].v[1];
+      const int ac = ah > minO2, bc = bh > minO2, cc = ch > minO2, dc = dh > minO2;
+      V[ia].state = !ac; V[ib].state = !bc; V[ic].state = !cc; V[id].state = !dc;
+      if (ac || bc || cc) {
+        HFTri* t = &T[numTri++];
+        t->state = 0;
+        t->vi[0] = ia; t->vi[1] = ib; t->vi[2] = ic;
+        t->maxy = ah > bh ? ah : bh;
+        t->maxy = ch > t->maxy ? ch : t->maxy;
+        t->up = 1;
+      }
+      if (bc || cc || dc) {
+        HFTri* t = &T[numTri++];
+        t->state = 0;
+        t->vi[0] = id; t->vi[1] = ib; t->vi[2] = ic;
+        t->maxy = dh > bh ? dh : bh;
+        t->maxy = ch > t->maxy ? ch : t->maxy;
+        t->up = 0;
+      }
+      if (further && (bc || cc) && (ah > ch && ah > bh && dh > ch && dh > bh)) {
+        V[ib].state = 1;    /* concave edge BC */
+        V[ic].state = 1;
+      }
+    }
+  }
+  /* pass 1: triangle planes, grouped by plane, sorted by height */
+  for (int k = 0; k < numTri; ++k) {
+    HFTri* t = &T[k];
+    const real* v0 = V[t->vi[0]].v;
+    const real* v1 = V[t->vi[1]].v;
+    const real* v2 = V[t->vi[2]].v;
+    real e1[3] = {v2[0] - v0[0], v2[1] - v0[1], v2[2] - v0[2]};
+    real e2[3] = {v1[0] - v0[0], v1[1] - v0[1], v1[2] - v0[2]};
+    real n[3];
+    if (t->up) cross3(n, e1, e2);
+    else cross3(n, e2, e1);
+    const real il = 1.0 / sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+    n[0] *= il; n[1] *= il; n[2] *= il;
+    t->plane[0] = n[0]; t->plane[1] = n[1]; t->plane[2] = n[2];
+    t->plane[3] = dot3(n, v0);
+  }
+  HFPlane* P = (HFPlane*)calloc(numTri > 0 ? numTri : 1, sizeof(HFPlane));
+  int* members = (int*)calloc(numTri > 0 ? numTri : 1, sizeof(int));
+  int numPlanes = 0, nmem = 0;
+  for (int k = 0; k < numTri; ++k) {
+    HFTri* tb = &T[k];
+    if (tb->state) continue;
+    HFPlane* pl = &P[numPlanes];
+    pl->first = nmem;
+    pl->count = 0;
+    members[nmem++] = k; pl->count++;
+    for (int q = 0; q < 4; ++q) pl->plane[q] = tb->plane[q];
+    for (int m = k + 1; m < numTri; ++m) {
+      HFTri* tt = &T[m];
+      if (tt->state) continue;
+      if (fabs(tb->plane[1] - tt->plane[1]) < HF_EPS && fabs(tb->plane[3] - tt->plane[3]) < HF_EPS &&
+          fabs(tb->plane[0] - tt->plane[0]) < HF_EPS && fabs(tb->plane[2] - tt->plane[2]) < HF_EPS) {
+        members[nmem++] = m; pl->count++;
+        tt->state = 1;
+      }
+    }
+    tb->state = 1;
+    pl->maxy = T[members[pl->first]].maxy;
+    for (int q = 1; q < pl->count; ++q)
+      if (T[members[pl->first + q]].maxy > pl->maxy) pl->maxy = T[members[pl->first + q]].maxy;
+    numPlanes++;
+  }
+  /* sortPlanes (heightfield.cpp:910-932): bubble sort, descending height */
+  {
+    int swapped = 1;
+    while (swapped) {
+      swapped = 0;
+      for (int i = 0; i < numPlanes - 1; ++i) {
+        if ((P[i].maxy - P[i + 1].maxy) > HF_EPS) {
+          HFPlane tmp = P[i]; P[i] = P[i + 1]; P[i + 1] = tmp;
+          swapped = 1;
+        }
+      }
+    }
+  }
+  const unsigned plane_flags = (flags & ~0xffffu) | HF_MAXC_PER_CELL;
+  for (int k = 0; k < numPlanes; ++k) {
+    HFPlane* pl = &P[k];
+    GeomRef gp;
+    memset(&gp, 0, sizeof(gp));
+    gp.type = ODEGPU_GEOM_PLANE;
+    gp.p = pl->plane;
+    OContact pc[HF_MAXC_PER_CELL];
+    int did = 0;
+    const int npc = geom_plane_collide(o2, &gp, plane_flags, pc);
+    for (int i = 0; i < npc; ++i) {
+      for (int b = 0; b < pl->count; ++b) {
+        const HFTri* t = &T[members[pl->first + b]];
+        const HFVertex* cv = &V[t->vi[0]];
+        if (hf_on_triangle(D, cv->v, cv->coords, pc[i].pos, t->up)) {
+          OContact* o = &out[nc];
+          for (int q = 0; q < 3; ++q) { o->pos[q] = pc[i].pos[q]; o->normal[q] = -pl->plane[q]; }
+          o->depth = pc[i].depth;
+          nc++;
+          if (nc == max_contacts) goto done;
+          did = 1;
+          break;
+        }
+      }
+    }
+    if (did) {
+      for (int b = 0; b < pl->count; ++b) {
+        const HFTri* t = &T[members[pl->first + b]];
+        for (int i = 0; i < 3; ++i) V[t->vi[i]].state = 1;
+      }
+    } else {
+      for (int b = 0; b < pl->count; ++b) T[members[pl->first + b]].state = 0;
+    }
+  }
+  /* pass 2: triangle vertices against the geom's point depth */
+  if (further) {
+    for (int k = 0; k < numTri; ++k) {
+      const HFTri* t = &T[k];
+      if (t->state) continue;
+      for (int i = 0; i < 3; ++i) {
+        HFVertex* hv = &V[t->vi[i]];
+        if (hv->state) continue;
+        const real depth = geom_point_depth(o2, hv->v);
+        if (depth > HF_EPS) {
+          OContact* o = &out[nc];
+          for (int q = 0; q < 3; ++q) { o->pos[q] = hv->v[q]; o->normal[q] = -t->plane[q]; }
+          o->depth = depth;
+          nc++;
+          if (nc == max_contacts) goto done;
+          hv->state = 1;
+        }
+      }
+    }
+  }
+done:
+  free(V); free(T); free(P); free(members);
+  return nc;
+}
+
+/* dCollideHeightfield, heightfield.cpp:1677-1853 (placeable heightfield,
+ * centred origin: DHEIGHTFIELD_CORNER_ORIGIN undefined). */
 int oracle_heightfield_collide(const GeomRef* hf, const GeomRef* o2, unsigned flags, OContact* c) {
-  (void)hf; (void)o2; (void)flags; (void)c;
-  return 0;
+  const int maxc = (int)(flags & 0xffff);
+  if (maxc < 1 || !hf->g || !hf->g->hf) return 0;
+  HFData D;
+  hf_data(hf->g->hf, &D);
+  const odegpuHeightfield* H = hf->g->hf;
+  /* o2 into heightfield space */
+  real p0[3] = {o2->pos[0] - hf->pos[0], o2->pos[1] - hf->pos[1], o2->pos[2] - hf->pos[2]};
+  real pos1[3], R1[12];
+  mul1_331(pos1, hf->R, p0);
+  /* dMultiply1_333(R1, Rhf, Ro2) = Rhf^T Ro2 */
+  for (int i = 0; i < 3; ++i) {
+    for (int j = 0; j < 3; ++j)
+      R1[i * 4 + j] = hf->R[0 * 4 + i] * o2->R[0 * 4 + j] + hf->R[1 * 4 + i] * o2->R[1 * 4 + j] +
+                      hf->R[2 * 4 + i] * o2->R[2 * 4 + j];
+    R1[i * 4 + 3] = 0;
+  }
+  pos1[0] += D.half_w;
+  pos1[2] += D.half_d;
+  GeomRef g2 = *o2;
+  g2.pos = pos1;
+  g2.R = R1;
+  real aabb[6];
+  geom_aabb(&g2, aabb);
+  const int wrapped = H->wrap != 0;
+  if (!wrapped) {
+    if (aabb[0] > H->width || aabb[4] > H->depth) return 0;
+    if (aabb[1] < 0 || aabb[5] < 0) return 0;
+  }
+  int nMinX = (int)floor(nextafter(aabb[0] * D.inv_sw, -INFINITY));
+  int nMaxX = (int)ceil(nextafter(aabb[1] * D.inv_sw, INFINITY));
+  int nMinZ = (int)floor(nextafter(aabb[4] * D.inv_sd, -INFINITY));
+  int nMaxZ = (int)ceil(nextafter(aabb[5] * D.inv_sd, INFINITY));
+  if (!wrapped) {
+    nMinX = nMinX > 0 ? nMinX : 0;
+    nMaxX = nMaxX < H->nx - 1 ? nMaxX : H->nx - 1;
+    nMinZ = nMinZ > 0 ? nMinZ : 0;
+    nMaxZ = nMaxZ < H->nz - 1 ? nMaxZ : H->nz - 1;
+  }
+  const int n = hf_zone(&D, nMinX, nMaxX, nMinZ, nMaxZ, &g2, aabb, maxc, flags, c);
+  /* contacts back to world space */
+  for (int i = 0; i < n; ++i) {
+    real q[3] = {c[i].pos[0] - D.half_w, c[i].pos[1], c[i].pos[2] - D.half_d};
+    real w[3];
+    mul0_331(w, hf->R, q);
+    for (int k = 0; k < 3; ++k) c[i].pos[k] = w[k] + hf->pos[k];
+    real nn[3] = {c[i].normal[0], c[i].normal[1], c[i].normal[2]};
+    mul0_331(c[i].normal, hf->R, nn);
+  }
+  return n;
 }
 
 static void fill_ref(const OWorld* W, int gi, GeomRef* r) {
@@ -1902,6 +2296,18 @@ static int world_step(OWorld* W, int s, double* contacts, int max_rec) {
   if (sc->n_ctrl_steps > 0) {
     const int cs = s % sc->n_ctrl_steps;
     const int j0 = sc->joint_off[W->w], b0 = sc->body_off[W->w];
+    if (sc->joint_stop) {
+      /* dJointSetHinge{,2}Param(dParamLoStop / dParamHiStop): plain
+       * assignment (dxJointLimitMotor::set, ode/src/joints/joint.cpp:471-503) */
+      for (int i = 0; i < W->nj_persist; ++i) {
+        OJoint* J = &W->joint[i];
+        if (J->type != ODEGPU_JOINT_HINGE && J->type != ODEGPU_JOINT_HINGE2) continue;
+        const double v = sc->joint_stop[(size_t)cs * sc->joint_off[sc->n_worlds] + j0 + i];
+        const double* jp = sc->joint_param + (size_t)(j0 + i) * ODEGPU_JOINT_NPARAM;
+        J->lm1.lostop = isnan(v) ? jp[0] : v;
+        J->lm1.histop = isnan(v) ? jp[1] : v;
+      }
+    }
     if (sc->joint_torque) {
       for (int i = 0; i < W->nj_persist; ++i) {
         const double* t = sc->joint_torque + ((size_t)cs * sc->joint_off[sc->n_worlds] + j0 + i) * 2;
@@ -2100,6 +2506,34 @@ int oracle_collide(int t1, const double* p1, const double* pos1, const double* R
   }
   OContact c[16];
   int n = do_collide(&ref[0], &ref[1], (unsigned)flags, c);
+  for (int i = 0; i < n; ++i) {
+    double* r = out + 9 * i;
+    for (int q = 0; q < 3; ++q) r[q] = c[i].pos[q];
+    for (int q = 0; q < 3; ++q) r[3 + q] = c[i].normal[q];
+    r[6] = c[i].depth; r[7] = 0; r[8] = 0;
+  }
+  return n;
+}
+
+int oracle_collide_hf(const odegpuHeightfield* H, int t2, const double* p2, const double* pos2, const double* R2,
+                      int flags, double* out) {
+  OGeom G[2];
+  real R[2][12], pos[2][3];
+  memset(G, 0, sizeof(G));
+  G[0].type = ODEGPU_GEOM_HEIGHTFIELD;
+  G[0].hf = H;
+  G[1].type = t2;
+  for (int k = 0; k < 4; ++k) G[1].p[k] = p2[k];
+  for (int k = 0; k < 3; ++k) { pos[0][k] = H->pos[k]; pos[1][k] = pos2[k]; }
+  for (int r = 0; r < 3; ++r) {
+    for (int c = 0; c < 3; ++c) { R[0][r * 4 + c] = H->R[r * 3 + c]; R[1][r * 4 + c] = R2[r * 3 + c]; }
+    R[0][r * 4 + 3] = R[1][r * 4 + 3] = 0;
+  }
+  GeomRef a = {ODEGPU_GEOM_HEIGHTFIELD, pos[0], R[0], G[0].p, &G[0]};
+  GeomRef b = {t2, pos[1], R[1], G[1].p, &G[1]};
+  OContact c[64];
+  if ((flags & 0xffff) > 64) flags = (flags & ~0xffff) | 64;
+  const int n = do_collide(&a, &b, (unsigned)flags, c);
   for (int i = 0; i < n; ++i) {
     double* r = out + 9 * i;
     for (int q = 0; q < 3; ++q) r[q] = c[i].pos[q];

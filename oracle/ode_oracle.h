@@ -22,6 +22,12 @@ int oracle_run_world(const odegpuScene* sc, int w, int n_steps, double* state,
                      int* ncontacts, double* contacts, int max_rec, double* feedback,
                      unsigned int* seed_out);
 
+/* dCollide(heightfield H placed at H->pos / H->R, geom of class t2 with
+ * parameters p2 at pos2 / R2 (row-major 3x3)); out: [n][9] pos, normal,
+ * depth, 0, 0. Returns the contact count. */
+int oracle_collide_hf(const odegpuHeightfield* H, int t2, const double* p2, const double* pos2,
+                      const double* R2, int flags, double* out);
+
 /* World w built from the scene, then every body's state replaced by
  * init_state ([nb][13], quaternion used as given), stepped n_steps times;
  * final_state receives [nb][13]. For finite differences of the step with

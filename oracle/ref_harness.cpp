@@ -17,6 +17,7 @@
  *   5. dJointGroupEmpty (ode.cpp:1305)
  */
 #include <ode/ode.h>
+#include <cmath>
 #include <string.h>
 #include <stdlib.h>
 #include "odegpu_scene.h"
@@ -232,6 +233,22 @@ int ref_run_world(const odegpuScene* sc, int w, int n_steps, double* state,
 
     if (sc->n_ctrl_steps > 0) {
       const int cs = s % sc->n_ctrl_steps;
+      if (sc->joint_stop) {
+        for (int i = 0; i < nj; ++i) {
+          const int t = sc->joint_type[j0 + i];
+          if (t != ODEGPU_JOINT_HINGE && t != ODEGPU_JOINT_HINGE2) continue;
+          const double v = sc->joint_stop[(size_t)cs * sc->joint_off[sc->n_worlds] + j0 + i];
+          const double* jp = sc->joint_param + (size_t)(j0 + i) * ODEGPU_JOINT_NPARAM;
+          const double lo = std::isnan(v) ? jp[0] : v, hi = std::isnan(v) ? jp[1] : v;
+          if (t == ODEGPU_JOINT_HINGE) {
+            dJointSetHingeParam(joints[i], dParamLoStop, lo);
+            dJointSetHingeParam(joints[i], dParamHiStop, hi);
+          } else {
+            dJointSetHinge2Param(joints[i], dParamLoStop, lo);
+            dJointSetHinge2Param(joints[i], dParamHiStop, hi);
+          }
+        }
+      }
       if (sc->joint_torque) {
         for (int i = 0; i < nj; ++i) {
           const double* t = sc->joint_torque + ((size_t)cs * sc->joint_off[sc->n_worlds] + j0 + i) * 2;
@@ -329,6 +346,41 @@ int ref_collide(int t1, const double* p1, const double* pos1, const double* R1, 
   }
   dGeomDestroy(a);
   dGeomDestroy(b);
+  dCloseODE();
+  return n;
+}
+
+/* dCollide(heightfield, geom) with the heightfield placed at H->pos / H->R
+ * (placeable), the geom of class t2 at pos2 / R2; same output as ref_collide. */
+int ref_collide_hf(const odegpuHeightfield* H, int t2, const double* p2, const double* pos2,
+                   const double* R2, int flags, double* out) {
+  dInitODE2(0);
+  dHeightfieldDataID hd = dGeomHeightfieldDataCreate();
+  dGeomHeightfieldDataBuildDouble(hd, H->heights, 1, H->width, H->depth, H->nx, H->nz, H->scale,
+                                  H->offset, H->thickness, H->wrap);
+  dGeomID a = dCreateHeightfield(0, hd, 1);
+  dGeomSetPosition(a, H->pos[0], H->pos[1], H->pos[2]);
+  dMatrix3 RH = {H->R[0], H->R[1], H->R[2], 0, H->R[3], H->R[4], H->R[5], 0,
+                 H->R[6], H->R[7], H->R[8], 0};
+  dGeomSetRotation(a, RH);
+  dGeomID b = make_geom(t2, p2);
+  if (!b) return -1;
+  dGeomSetPosition(b, pos2[0], pos2[1], pos2[2]);
+  dMatrix3 R = {R2[0], R2[1], R2[2], 0, R2[3], R2[4], R2[5], 0, R2[6], R2[7], R2[8], 0};
+  dGeomSetRotation(b, R);
+  dContactGeom cg[64];
+  const int n = dCollide(a, b, flags, cg, sizeof(dContactGeom));
+  for (int c = 0; c < n; ++c) {
+    double* r = out + 9 * c;
+    for (int q = 0; q < 3; ++q) r[q] = cg[c].pos[q];
+    for (int q = 0; q < 3; ++q) r[3 + q] = cg[c].normal[q];
+    r[6] = cg[c].depth;
+    r[7] = 0;
+    r[8] = 0;
+  }
+  dGeomDestroy(a);
+  dGeomDestroy(b);
+  dGeomHeightfieldDataDestroy(hd);
   dCloseODE();
   return n;
 }

@@ -28,6 +28,7 @@ SCENES = {
     "hinge": (lambda: S.hinge_chains(n_worlds=3, steps=60), 60),
     "stack": (lambda: S.box_stack(n_worlds=2, height=5), 100),
     "capsule": (lambda: S.capsule_mix(seed=6), 80),
+    "vehicles": (lambda: S.vehicles(n_worlds=3, steps=60, hf_samples=64), 60),
 }
 KEEP = 10  # keep the state every KEEP steps
 
@@ -101,6 +102,57 @@ def make_collider_kats(n=120, seed=123):
         nc=np.array([r[9] for r in recs]), out=np.array([r[10] for r in recs]))
 
 
+def make_hf_kats(n=150, seed=321):
+    """dCollide(heightfield, geom) on a seeded 33 x 29 fractal field placed with
+    its up axis along world z, for spheres, boxes and capsules in random poses
+    near the surface and random contact limits."""
+    import ctypes as C
+    rng = np.random.Generator(np.random.PCG64(seed))
+    ref = O.ref("d")
+    f = ref.ref_collide_hf
+    P = C.POINTER(C.c_double)
+    f.restype = C.c_int
+    f.argtypes = [C.c_void_p, C.c_int, P, P, P, C.c_int, P]
+    nx, nz, sp = 33, 29, 0.5
+    h = np.ascontiguousarray(S.fractal_heights(64, 0.3, seed=seed)[:nz, :nx])
+    Rh = np.array(S.HF_Z_UP)
+    pos_h = np.array([0.4, -0.3, 0.2])
+    H = S.Heightfield()
+    H.nx, H.nz = nx, nz
+    H.width, H.depth = sp * (nx - 1), sp * (nz - 1)
+    H.scale, H.offset, H.thickness, H.wrap = 1.0, 0.0, 1.0, 0
+    H.heights = h.ctypes.data_as(P)
+    H.pos[:] = list(pos_h)
+    H.R[:] = list(Rh.ravel())
+    recs = []
+    for t2 in (0, 1, 2):
+        for _ in range(n):
+            if t2 == 0:
+                p2 = np.array([rng.uniform(0.2, 0.5), 0, 0, 0])
+            elif t2 == 1:
+                p2 = np.concatenate([rng.uniform(0.3, 2.0, 3), [0]])
+            else:
+                p2 = np.array([rng.uniform(0.1, 0.3), rng.uniform(0.2, 1.0), 0, 0])
+            local = np.array([rng.uniform(-0.45, 0.45) * H.width, 0.0, rng.uniform(-0.45, 0.45) * H.depth])
+            ix = int(np.clip(round((local[0] + H.width / 2) / sp), 0, nx - 1))
+            iz = int(np.clip(round((local[2] + H.depth / 2) / sp), 0, nz - 1))
+            local[1] = h[iz, ix] + rng.uniform(-0.3, 0.6)
+            pos2 = Rh @ local + pos_h
+            R2 = rot(rng) if rng.uniform() < 0.8 else np.eye(3)
+            flags = int(rng.choice([1, 2, 3, 4, 8]))
+            out = np.zeros((64, 9))
+            args = [np.ascontiguousarray(a, dtype=np.float64) for a in (p2, pos2, R2.ravel())]
+            nc = f(C.byref(H), t2, args[0].ctypes.data_as(P), args[1].ctypes.data_as(P),
+                   args[2].ctypes.data_as(P), flags, out.ctypes.data_as(P))
+            recs.append((t2, flags, p2, pos2, R2.ravel(), nc, out[:8]))
+    np.savez_compressed(
+        os.path.join(HERE, "hf_kats.npz"), heights=h, spacing=sp, hf_pos=pos_h, hf_R=Rh.ravel(),
+        t2=np.array([r[0] for r in recs]), flags=np.array([r[1] for r in recs]),
+        p2=np.array([r[2] for r in recs]), pos2=np.array([r[3] for r in recs]),
+        R2=np.array([r[4] for r in recs]), nc=np.array([r[5] for r in recs]),
+        out=np.array([r[6] for r in recs]))
+
+
 def make_tower():
     """Non-chaotic stacks (boxes of decreasing size, aligned): FP64 reference
     states after 200 steps plus the reference's own FP32 (dSINGLE) build on the
@@ -135,6 +187,7 @@ if __name__ == "__main__":
         make_scene(name)
         print("wrote", name)
     make_collider_kats()
+    make_hf_kats()
     make_rng_kat()
     make_tower()
     print("wrote collider_kats, rng_kat")

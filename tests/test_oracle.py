@@ -59,7 +59,46 @@ def test_collider_kats_golden():
     assert (g["nc"] > 0).sum() > n // 4  # the poses do exercise contact
 
 
-@pytest.mark.parametrize("name", ["box_drop", "batched", "hinge", "stack", "capsule"])
+def hf_from_golden(g):
+    """The heightfield of hf_kats.npz as a ctypes odegpuHeightfield (the
+    returned tuple keeps the height array alive)."""
+    h = np.ascontiguousarray(g["heights"], dtype=np.float64)
+    sp = float(g["spacing"])
+    H = S.Heightfield()
+    H.nz, H.nx = h.shape
+    H.width, H.depth = sp * (H.nx - 1), sp * (H.nz - 1)
+    H.scale, H.offset, H.thickness, H.wrap = 1.0, 0.0, 1.0, 0
+    H.heights = h.ctypes.data_as(_P(C.c_double))
+    H.pos[:] = [float(x) for x in g["hf_pos"]]
+    H.R[:] = [float(x) for x in g["hf_R"]]
+    return H, h
+
+
+def test_heightfield_kats_golden():
+    """dCollide(heightfield, sphere / box / capsule) on a placeable fractal
+    field (dCollideHeightfield, ode/src/heightfield.cpp:1677-1853): contact
+    count and records bit-exact vs the reference."""
+    g = np.load(os.path.join(GOLDEN, "hf_kats.npz"))
+    H, _h = hf_from_golden(g)
+    L = O.oracle()
+    f = L.oracle_collide_hf
+    f.restype = C.c_int
+    f.argtypes = [C.c_void_p, C.c_int, _P(C.c_double), _P(C.c_double), _P(C.c_double), C.c_int,
+                  _P(C.c_double)]
+    n = len(g["t2"])
+    mism = 0
+    for i in range(n):
+        out = np.zeros((64, 9))
+        args = [np.ascontiguousarray(g[k][i], dtype=np.float64) for k in ("p2", "pos2", "R2")]
+        nc = f(C.byref(H), int(g["t2"][i]), *(a.ctypes.data_as(_P(C.c_double)) for a in args),
+               int(g["flags"][i]), out.ctypes.data_as(_P(C.c_double)))
+        if nc != g["nc"][i] or not np.array_equal(out[:nc, :7], g["out"][i][:nc, :7]):
+            mism += 1
+    assert mism == 0, f"{mism} of {n} heightfield calls differ"
+    assert (g["nc"] > 0).sum() > n // 2
+
+
+@pytest.mark.parametrize("name", ["box_drop", "batched", "hinge", "stack", "capsule", "vehicles"])
 def test_oracle_matches_reference_golden(name):
     """Whole-step parity: contact counts, contact records, RNG seeds, body
     states and joint feedback are bit-identical to the reference (FP64)."""
