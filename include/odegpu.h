@@ -119,6 +119,14 @@ int odegpuBatchWriteState(odegpuBatchID b, const double* state);
 int odegpuBatchReadStateF32Async(odegpuBatchID b, float* state);
 int odegpuBatchWriteStateF32Async(odegpuBatchID b, const float* state);
 
+/* Joint feedback (dJointSetFeedback, include/ode/objects.h; filled by
+ * dxQuickStepper at ode/src/quickstep.cpp:918-957): SetFeedback(1) makes
+ * every following step compute, for every persistent joint, f1 t1 f2 t2 =
+ * J^T lambda of its rows (f2 = t2 = 0 without a second body); GetFeedback
+ * copies the last step's values to out[nj_total][12] (f1[3] t1[3] f2[3] t2[3]). */
+int odegpuBatchSetFeedback(odegpuBatchID b, int on);
+int odegpuBatchGetFeedback(odegpuBatchID b, double* out);
+
 /* Per-world bookkeeping of the last step. */
 int odegpuBatchGetStatus(odegpuBatchID b, int* status);
 int odegpuBatchGetCounts(odegpuBatchID b, int* ncontacts, int* nrows, int* nislands);

@@ -245,7 +245,12 @@ struct odegpuBatch {
 
   // n_steps steps of worlds [first, first+count) of the launch order (or of
   // the identity order when use_order is false); 3 launches per step.
-  int launch(int first, int count, int n_steps, const StepOptions& opt, bool use_order = true) {
+  DBuf<float> jcopy, feedback;       // joint feedback (odegpuBatchSetFeedback)
+  bool feedback_on = false;
+
+  int launch(int first, int count, int n_steps, const StepOptions& opt_in, bool use_order = true) {
+    StepOptions opt = opt_in;
+    if (feedback_on) { opt.jcopy = jcopy.p; opt.feedback = feedback.p; }
     const int wpb = warps_per_block;
     const int blocks = (count + wpb - 1) / wpb;
     const BatchDev d = dev();
@@ -713,6 +718,31 @@ int odegpuBatchGetKernelTimes(odegpuBatchID b, double* ms, long long* n_steps) {
   }
   if (n_steps) *n_steps = (long long)steps;
   b->ev_used = 0;
+  return 0;
+}
+
+int odegpuBatchSetFeedback(odegpuBatchID b, int on) {
+  if (!b) return fail(ODEGPU_E_ARG, "null batch");
+  OG_CUDA(cudaSetDevice(b->device));
+  OG_CUDA(cudaStreamSynchronize(b->stream));
+  if (on && !b->feedback.p) {
+    if (int rc = b->jcopy.alloc((size_t)std::max<long long>(1, b->row_cap_total) * 12)) return rc;
+    if (int rc = b->feedback.alloc((size_t)std::max(1, b->nj_total) * 12)) return rc;
+    OG_CUDA(cudaMemset(b->feedback.p, 0, (size_t)std::max(1, b->nj_total) * 12 * sizeof(float)));
+  }
+  b->feedback_on = on != 0;
+  return 0;
+}
+
+int odegpuBatchGetFeedback(odegpuBatchID b, double* out) {
+  if (!b || !out) return fail(ODEGPU_E_ARG, "bad arguments");
+  if (!b->feedback.p) return fail(ODEGPU_E_ARG, "feedback is not enabled (odegpuBatchSetFeedback)");
+  OG_CUDA(cudaSetDevice(b->device));
+  OG_CUDA(cudaStreamSynchronize(b->stream));
+  std::vector<float> tmp((size_t)b->nj_total * 12);
+  if (!tmp.empty())
+    OG_CUDA(cudaMemcpy(tmp.data(), b->feedback.p, tmp.size() * sizeof(float), cudaMemcpyDeviceToHost));
+  for (size_t i = 0; i < tmp.size(); ++i) out[i] = tmp[i];
   return 0;
 }
 

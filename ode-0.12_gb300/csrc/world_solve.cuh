@@ -207,7 +207,7 @@ OG_D int phase_rows(const BatchDev& d, const WorldDesc& D, int w, int nj, int ni
 // Phase 5: rhs, cfm/h, iMJ, Ad and the J/b scaling per row; tmp1 per body is
 // staged in S.fc first (quickstep.cpp:836-857 then :117-136, :370-402).
 OG_D void phase_row_setup(const BatchDev& d, const WorldDesc& D, int M, const WarpSmem& S, int lane,
-                          float* dbg_rows) {
+                          float* dbg_rows, float* jcopy) {
   const float h1 = 1.0f / D.dt;
   for (int b = lane; b < D.nb; b += 32) {
     const int gb = D.body_off + b;
@@ -252,6 +252,12 @@ OG_D void phase_row_setup(const BatchDev& d, const WorldDesc& D, int M, const Wa
     }
     const float rhs = w6.x * h1 - sum;
     const float cfm = w6.y * h1;
+    if (jcopy) {
+      float4* o = reinterpret_cast<float4*>(jcopy + (size_t)(D.row_off + r) * 12);
+      o[0] = make_float4(J[0], J[1], J[2], J[3]);
+      o[1] = make_float4(J[4], J[5], J[6], J[7]);
+      o[2] = make_float4(J[8], J[9], J[10], J[11]);
+    }
     if (dbg_rows) {
       float* o = dbg_rows + (size_t)(D.row_off + r) * kRowWords;
       for (int q = 0; q < 12; ++q) o[q] = J[q];
@@ -293,6 +299,33 @@ OG_D void phase_row_setup(const BatchDev& d, const WorldDesc& D, int M, const Wa
     row4[6] = make_float4(rhs * Ad, Ad * cfm, w6.z, w6.w);
   }
   __syncwarp();
+}
+
+// Joint feedback (quickstep.cpp:918-957, Multiply1_12q1 :70-101): for every
+// persistent joint, f1 t1 = J1^T lambda and f2 t2 = J2^T lambda over its rows,
+// with J as getInfo2 produced it; one lane per joint sums its rows in order.
+// A joint without a second body gets f2 = t2 = 0.
+OG_D void phase_feedback(const BatchDev& d, const WorldDesc& D, int w, const float* lambda, const float* jcopy,
+                         float* feedback, int lane) {
+  const int jl_off = D.joint_off + D.contact_off;
+  const int nisl = d.nislands[w];
+  const int nj = d.island_jstart[D.body_off + w + nisl];
+  for (int k = lane; k < nj; k += 32) {
+    const int ord = d.jlist[jl_off + k] & 0x3fffffff;
+    if (ord >= D.njp) continue;
+    const int r0 = d.jrow[jl_off + k], m = d.jm[jl_off + k];
+    float f[12];
+    for (int q = 0; q < 12; ++q) f[q] = 0.f;
+    for (int r = r0; r < r0 + m; ++r) {
+      const float s = lambda[r];
+      const float* J = jcopy + (size_t)(D.row_off + r) * 12;
+      for (int q = 0; q < 12; ++q) f[q] += J[q] * s;
+    }
+    if (d.joints[D.joint_off + ord].b2 < 0)
+      for (int q = 6; q < 12; ++q) f[q] = 0.f;
+    float* o = feedback + (size_t)(D.joint_off + ord) * 12;
+    for (int q = 0; q < 12; ++q) o[q] = f[q];
+  }
 }
 
 // Phase 7: velocity update from the constraint forces and external forces,
@@ -410,6 +443,8 @@ struct StepOptions {
   float* dbg_fc;        // optional: cforce per body
   int host_forces;      // 1: facc/tacc were uploaded (skip the control phase)
   int host_adjacency;   // 1: padj holds every joint of each body in list order
+  float* jcopy;         // optional: J of every row before scaling, 12 per row (feedback)
+  float* feedback;      // optional: [nj_total][12] f1 t1 f2 t2 of the persistent joints
 };
 
 // Setup kernel body: phases 0-5. Leaves the rows, island table, row count
@@ -438,7 +473,7 @@ OG_D void world_setup(const BatchDev& d, int w, int step, const WarpSmem& S, int
     const int nj = phase_islands(d, D, w, opt.host_adjacency ? 0 : nc, D.njp + nc, S, lane, &nisl);
     M = phase_rows(d, D, w, nj, nisl, lane, step, opt.dbg_rows);
   }
-  if (M > 0) phase_row_setup(d, D, M, S, lane, opt.dbg_rows);
+  if (M > 0) phase_row_setup(d, D, M, S, lane, opt.dbg_rows, opt.jcopy);
   if (lane == 0) {
     d.nrows[w] = M < 0 ? 0 : M;
     d.nislands[w] = M > 0 ? nisl : 0;
@@ -464,6 +499,7 @@ OG_D void world_solve(const BatchDev& d, int w, const SorSmem& S, int lane, cons
       for (int r = lane; r < M; r += 32) opt.dbg_lambda[D.row_off + r] = S.lambda[r];
     if (opt.dbg_fc)
       for (int i = lane; i < D.nb * 6; i += 32) opt.dbg_fc[(size_t)D.body_off * 6 + i] = S.fc[i];
+    if (opt.feedback && opt.jcopy) phase_feedback(d, D, w, S.lambda, opt.jcopy, opt.feedback, lane);
   }
   if (lane == 0) d.seed[w] = seed;
   phase_integrate(d, D, w, S.fc, lane, have_rows);

@@ -42,6 +42,8 @@ def _declare(L):
         "odegpuBatchSetTiming": (i, [v, i]),
         "odegpuBatchSetControlsF32": (i, [v, i, v, v]),
         "odegpuBatchSetJointStops": (i, [v, i, _P(d)]),
+        "odegpuBatchSetFeedback": (i, [v, i]),
+        "odegpuBatchGetFeedback": (i, [v, _P(d)]),
         "odegpuBatchRolloutForward": (i, [v, i, i]),
         "odegpuBatchRolloutBackward": (i, [v, v, v, v, v]),
         "odegpuBatchAdjointStatus": (i, [v, _P(i)]),

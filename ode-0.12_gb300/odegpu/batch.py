@@ -143,6 +143,16 @@ class Batch:
         check(lib().odegpuBatchRolloutBackward(self.h, grad_final_ptr, grad_init_ptr, grad_jt_ptr,
                                                grad_bf_ptr))
 
+    def set_feedback(self, on=True):
+        """Compute joint feedback (f1 t1 f2 t2 per persistent joint) in every step."""
+        check(lib().odegpuBatchSetFeedback(self.h, 1 if on else 0))
+
+    def feedback(self):
+        """[nj_total, 12] f1 t1 f2 t2 of the last step."""
+        out = np.zeros((max(self.nj_total, 1), 12))
+        check(lib().odegpuBatchGetFeedback(self.h, out.ctypes.data_as(_P(C.c_double))))
+        return out[:self.nj_total]
+
     def adjoint_status(self):
         out = np.zeros(self.n_worlds, np.int32)
         check(lib().odegpuBatchAdjointStatus(self.h, out.ctypes.data_as(_P(C.c_int))))

@@ -182,3 +182,42 @@ def test_launch_modes_agree(batch_cls):
         outs.append(B.state())
     assert np.array_equal(outs[0], outs[1])
     assert np.array_equal(outs[0], outs[2])
+
+
+@pytest.mark.parametrize("name", ["hinge", "batched"])
+def test_joint_feedback_one_step(batch_cls, name):
+    """dJointFeedback of every persistent joint (quickstep.cpp:918-957): one
+    GPU step from the oracle's state against the oracle's feedback of that
+    step. FP32 against FP64 after 20 SOR iterations: |gpu - oracle| <=
+    1e-2 * max|oracle| + 5e-3 * |oracle| + 1e-3 * (weight of the world's
+    heaviest body) per component; the last term covers constraint forces that
+    the FP32 rounding of the starting state alone produces (anchor errors of
+    ~1e-6 m times erp / h^2 times the body mass)."""
+    sc = _scenes()[name]
+    n = 30
+    runs = [O.run_world(O.oracle().oracle_run_world, sc, w, n, feedback=True) for w in range(sc.n_worlds)]
+    B = batch_cls(sc)
+    B.set_feedback(True)
+    checked = 0
+    for k in (0, 10, 29):
+        B.set_state(stacked_state(runs, k))
+        B.set_seeds(seeds_before(sc, runs, k))
+        B.set_step_index(k)
+        B.step(1)
+        g = B.feedback()
+        nc, _, _ = B.counts()
+        for w in range(sc.n_worlds):
+            if nc[w] != runs[w]["ncontacts"][k]:
+                continue
+            j0, j1 = sc.world_joints(w)
+            if j1 == j0:
+                continue
+            ref = runs[w]["feedback"][k][: j1 - j0]
+            got = g[j0:j1]
+            b0, b1 = sc.world_bodies(w)
+            floor = 1e-3 * 9.81 * float(sc.body_mass[b0:b1].max())
+            bar = 1e-2 * np.abs(ref).max() + 5e-3 * np.abs(ref) + floor
+            assert (np.abs(got - ref) <= bar).all(), (name, k, w, np.abs(got - ref).max(), np.abs(ref).max())
+            checked += 1
+    B.close()
+    assert checked > 0
