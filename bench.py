@@ -208,6 +208,44 @@ def run_adjoint(local_rank, reps=3):
             "gradient_check": "tests/test_gpu_adjoint.py (FP64 central differences of the oracle)"}
 
 
+def run_vehicles(local_rank, steps=300):
+    """Vehicle batch: 2048 cars (box chassis, four sphere wheels on hinge2
+    joints) on a 256 x 256 heightfield at 0.5 m, per-step steering stops and
+    wheel torques; world-steps/s of the 300-step rollout from the initial
+    state, timed with CUDA events on the batch stream."""
+    import torch
+    from odegpu import scene as S
+    from odegpu.batch import Batch
+    sc = S.vehicles(n_worlds=2048, steps=steps)
+    B = Batch(sc, device=local_rank)
+    stream = torch.cuda.ExternalStream(B.stream_handle())
+    x0, seeds = B.state(), B.seeds()
+    B.step(3)
+    B.sync()
+    B.set_state(x0)
+    B.set_seeds(seeds)
+    B.set_step_index(0)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        e0.record(stream)
+    B.step(steps)
+    with torch.cuda.stream(stream):
+        e1.record(stream)
+    B.sync()
+    t = e0.elapsed_time(e1) / 1e3
+    nc, nr, _ = B.counts()
+    status = B.status()
+    B.close()
+    return {"metric": "world-steps/s, vehicle batch (heightfield + hinge2)", "value": 2048 * steps / t,
+            "unit": "world-steps/s", "ms_per_step": 1e3 * t / steps,
+            "workload": "vehicles: 2048 cars (2x1x0.5 m 1000 kg chassis, 4 sphere wheels r 0.35 m 20 kg, "
+                        "hinge2 suspension ERP 0.4 CFM 0.01), 256x256 fractal heightfield (0.5 m, sigma 0.3), "
+                        "steer U[-0.4,0.4] rad, throttle U[0,1]*400 N m, 300 steps from the initial state",
+            "contacts_last_step": int(nc.sum()), "rows_last_step": int(nr.sum()),
+            "worlds_with_status": int((status != 0).sum())}
+
+
 def run_reference(args):
     rank, world_size, _ = rank_env()
     if rank != 0:
@@ -374,6 +412,8 @@ def run_ours(args):
             P.close()
         if not args.no_adjoint:
             line["adjoint"] = run_adjoint(local_rank)
+        if not args.no_vehicles:
+            line["vehicles"] = run_vehicles(local_rank)
         if not args.no_cpu:
             nw = min(N_WORLDS, args.cpu_worlds)
             v, thr, dt = cpu_baseline(sc, nw, args.steps)
@@ -395,6 +435,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-vehicles", action="store_true")
     ap.add_argument("--cpu-worlds", type=int, default=512)
     ap.add_argument("--ref-worlds", type=int, default=4096)
     args = ap.parse_args()

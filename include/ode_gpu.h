@@ -12,7 +12,8 @@
  *  - dCollide runs the collider on the GPU, one launch per call.
  *  - Errors never abort the process: dWorldQuickStep returns 0 and
  *    odegpuGetLastError() says why (ODE aborts on debug asserts).
- *  - dJointSetFeedback is accepted; feedback is not filled (ODE fills it).
+ *  - joints with dJointSetFeedback get f1 t1 (and f2 t2 with a second body)
+ *    after each dWorldQuickStep, as ODE's quickstep fills them.
  *  - Limits per world: 64 bodies, 1024 constraint rows (odegpu.h).
  */
 #ifndef ODE_GPU_H

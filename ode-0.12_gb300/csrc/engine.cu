@@ -1090,6 +1090,7 @@ namespace og {
 
 struct WorldCtx {
   odegpuBatch B;
+  DBuf<float> contact_fb;   // contact-joint feedback of the last step
 };
 
 WorldCtx* ctx_create(int device) {
@@ -1170,7 +1171,27 @@ int ctx_step(WorldCtx* c, HostWorld& hw) {
   if (rc) return rc;
   B.n_ctrl_steps = 0;
   StepOptions opt{0, nullptr, nullptr, nullptr, 1, 1};
+  B.feedback_on = false;
+  if (hw.want_feedback) {
+    rc = rc ? rc : grow(B.jcopy, (size_t)D.row_cap * 12);
+    rc = rc ? rc : grow(B.feedback, (size_t)std::max(1, D.njp) * 12);
+    rc = rc ? rc : grow(c->contact_fb, (size_t)std::max(1, D.contact_cap) * 12);
+    if (rc) return rc;
+    opt.jcopy = B.jcopy.p;
+    opt.feedback = B.feedback.p;
+    opt.contact_feedback = c->contact_fb.p;
+  }
   if (int e = B.launch(0, 1, 1, opt, false)) return e;
+  if (hw.want_feedback) {
+    hw.feedback.resize((size_t)D.njp * 12);
+    hw.contact_feedback.resize((size_t)D.contact_cap * 12);
+    if (!hw.feedback.empty())
+      OG_CUDA(cudaMemcpyAsync(hw.feedback.data(), B.feedback.p, hw.feedback.size() * sizeof(float),
+                              cudaMemcpyDeviceToHost, s));
+    if (!hw.contact_feedback.empty())
+      OG_CUDA(cudaMemcpyAsync(hw.contact_feedback.data(), c->contact_fb.p,
+                              hw.contact_feedback.size() * sizeof(float), cudaMemcpyDeviceToHost, s));
+  }
   std::vector<int> st(1);
   OG_CUDA(cudaMemcpyAsync(hw.pos.data(), B.pos.p, nb * sizeof(float4), cudaMemcpyDeviceToHost, s));
   OG_CUDA(cudaMemcpyAsync(hw.q.data(), B.q.p, nb * sizeof(float4), cudaMemcpyDeviceToHost, s));

@@ -20,6 +20,9 @@ struct HostWorld {
   std::vector<int> padj_start, padj;  // full body lists (ordinals: joint, njp + contact)
   unsigned seed = 0;
   int status = 0;
+  bool want_feedback = false;         // compute joint feedback in ctx_step
+  std::vector<float> feedback;        // out: [njp][12] persistent joints (f1 t1 f2 t2)
+  std::vector<float> contact_feedback;// out: [contacts][12]
 };
 
 struct WorldCtx;

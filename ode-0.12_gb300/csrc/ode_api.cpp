@@ -736,8 +736,24 @@ int dWorldQuickStep(dWorldID w, dReal stepsize) {
   D.max_vel = (float)w->max_vel; D.min_depth = (float)w->min_depth; D.dt = stepsize;
   D.max_contacts = 1;
   hw.seed = (unsigned)g_seed;
+  hw.want_feedback = false;
+  for (const dxJoint* j : pj) hw.want_feedback |= j->feedback != nullptr;
+  for (const dxJoint* j : cj) hw.want_feedback |= j->feedback != nullptr;
   if (og::ctx_step(w->ctx, hw) != 0) return 0;
   g_seed = hw.seed;
+  if (hw.want_feedback) {
+    // dxQuickStepper fills f1 t1, and f2 t2 when the joint has a second body
+    // (ode/src/quickstep.cpp:918-957)
+    auto fill = [](dxJoint* j, const float* f) {
+      dJointFeedback* fb = j->feedback;
+      if (!fb) return;
+      for (int q = 0; q < 3; ++q) { fb->f1[q] = f[q]; fb->t1[q] = f[3 + q]; }
+      if (j->body[1])
+        for (int q = 0; q < 3; ++q) { fb->f2[q] = f[6 + q]; fb->t2[q] = f[9 + q]; }
+    };
+    for (size_t k = 0; k < pj.size(); ++k) fill(pj[k], hw.feedback.data() + 12 * k);
+    for (size_t k = 0; k < cj.size(); ++k) fill(cj[k], hw.contact_feedback.data() + 12 * k);
+  }
   for (int i = 0; i < nb; ++i) {
     dxBody* b = w->bodies[i];
     b->pos[0] = hw.pos[i].x; b->pos[1] = hw.pos[i].y; b->pos[2] = hw.pos[i].z;

@@ -306,13 +306,23 @@ OG_D void phase_row_setup(const BatchDev& d, const WorldDesc& D, int M, const Wa
 // with J as getInfo2 produced it; one lane per joint sums its rows in order.
 // A joint without a second body gets f2 = t2 = 0.
 OG_D void phase_feedback(const BatchDev& d, const WorldDesc& D, int w, const float* lambda, const float* jcopy,
-                         float* feedback, int lane) {
+                         float* feedback, float* contact_feedback, int lane) {
   const int jl_off = D.joint_off + D.contact_off;
   const int nisl = d.nislands[w];
   const int nj = d.island_jstart[D.body_off + w + nisl];
   for (int k = lane; k < nj; k += 32) {
     const int ord = d.jlist[jl_off + k] & 0x3fffffff;
-    if (ord >= D.njp) continue;
+    float* o;
+    int b2;
+    if (ord < D.njp) {
+      if (!feedback) continue;
+      o = feedback + (size_t)(D.joint_off + ord) * 12;
+      b2 = d.joints[D.joint_off + ord].b2;
+    } else {
+      if (!contact_feedback) continue;
+      o = contact_feedback + (size_t)(D.contact_off + ord - D.njp) * 12;
+      b2 = d.contacts[D.contact_off + ord - D.njp].b2;
+    }
     const int r0 = d.jrow[jl_off + k], m = d.jm[jl_off + k];
     float f[12];
     for (int q = 0; q < 12; ++q) f[q] = 0.f;
@@ -321,9 +331,8 @@ OG_D void phase_feedback(const BatchDev& d, const WorldDesc& D, int w, const flo
       const float* J = jcopy + (size_t)(D.row_off + r) * 12;
       for (int q = 0; q < 12; ++q) f[q] += J[q] * s;
     }
-    if (d.joints[D.joint_off + ord].b2 < 0)
+    if (b2 < 0)
       for (int q = 6; q < 12; ++q) f[q] = 0.f;
-    float* o = feedback + (size_t)(D.joint_off + ord) * 12;
     for (int q = 0; q < 12; ++q) o[q] = f[q];
   }
 }
@@ -445,6 +454,7 @@ struct StepOptions {
   int host_adjacency;   // 1: padj holds every joint of each body in list order
   float* jcopy;         // optional: J of every row before scaling, 12 per row (feedback)
   float* feedback;      // optional: [nj_total][12] f1 t1 f2 t2 of the persistent joints
+  float* contact_feedback;  // optional: [contact_cap_total][12] the same for contact joints
 };
 
 // Setup kernel body: phases 0-5. Leaves the rows, island table, row count
@@ -499,7 +509,8 @@ OG_D void world_solve(const BatchDev& d, int w, const SorSmem& S, int lane, cons
       for (int r = lane; r < M; r += 32) opt.dbg_lambda[D.row_off + r] = S.lambda[r];
     if (opt.dbg_fc)
       for (int i = lane; i < D.nb * 6; i += 32) opt.dbg_fc[(size_t)D.body_off * 6 + i] = S.fc[i];
-    if (opt.feedback && opt.jcopy) phase_feedback(d, D, w, S.lambda, opt.jcopy, opt.feedback, lane);
+    if ((opt.feedback || opt.contact_feedback) && opt.jcopy)
+      phase_feedback(d, D, w, S.lambda, opt.jcopy, opt.feedback, opt.contact_feedback, lane);
   }
   if (lane == 0) d.seed[w] = seed;
   phase_integrate(d, D, w, S.fc, lane, have_rows);

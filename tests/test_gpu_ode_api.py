@@ -99,3 +99,68 @@ def test_dcollide_on_reference_kats():
             L.dGeomDestroy(h)
     assert count_mism <= n // 200, (count_mism, near)
     assert worst < 1e-3, worst
+
+
+class JointFeedback(C.Structure):
+    _fields_ = [("f1", C.c_float * 4), ("t1", C.c_float * 4), ("f2", C.c_float * 4), ("t2", C.c_float * 4)]
+
+
+class Mass(C.Structure):
+    _fields_ = [("mass", C.c_float), ("c", C.c_float * 4), ("I", C.c_float * 12)]
+
+
+def test_joint_feedback_through_ode_api():
+    """dJointSetFeedback on a three-link ball chain hanging at rest from the
+    environment: after a step the top joint's f1 carries the chain's weight,
+    the middle joint two links' weight (force on body 1 = J1^T lambda), and f2
+    of the lower joints is the reaction on the link below."""
+    from odegpu._lib import lib
+    L = lib()
+    f, v, i = C.c_float, C.c_void_p, C.c_int
+    L.dWorldCreate.restype = v
+    L.dWorldSetGravity.argtypes = [v, f, f, f]
+    L.dWorldSetCFM.argtypes = [v, f]
+    L.dBodyCreate.restype = v; L.dBodyCreate.argtypes = [v]
+    L.dBodySetPosition.argtypes = [v, f, f, f]
+    L.dMassSetSphereTotal.argtypes = [C.POINTER(Mass), f, f]
+    L.dBodySetMass.argtypes = [v, C.POINTER(Mass)]
+    L.dJointCreateBall.restype = v; L.dJointCreateBall.argtypes = [v, v]
+    L.dJointAttach.argtypes = [v, v, v]
+    L.dJointSetBallAnchor.argtypes = [v, f, f, f]
+    L.dJointSetFeedback.argtypes = [v, C.POINTER(JointFeedback)]
+    L.dWorldQuickStep.restype = i; L.dWorldQuickStep.argtypes = [v, f]
+    L.dWorldDestroy.argtypes = [v]
+    w = L.dWorldCreate()
+    L.dWorldSetGravity(w, 0.0, 0.0, -9.81)
+    L.dWorldSetCFM(w, 1e-5)
+    m = 2.0
+    bodies, joints, fbs = [], [], []
+    for k in range(3):
+        b = L.dBodyCreate(w)
+        L.dBodySetPosition(b, 0.0, 0.0, -0.5 - k)
+        M = Mass()
+        L.dMassSetSphereTotal(C.byref(M), m, 0.1)
+        L.dBodySetMass(b, C.byref(M))
+        bodies.append(b)
+    for k in range(3):
+        j = L.dJointCreateBall(w, None)
+        L.dJointAttach(j, bodies[k], bodies[k - 1] if k > 0 else None)
+        L.dJointSetBallAnchor(j, 0.0, 0.0, -float(k))
+        fb = JointFeedback()
+        L.dJointSetFeedback(j, C.byref(fb))
+        joints.append(j)
+        fbs.append(fb)
+    for _ in range(5):
+        assert L.dWorldQuickStep(w, 0.01) == 1
+    weight = m * 9.81
+    # joint k holds link k (body 1) to link k-1 / the environment (body 2)
+    for k in range(3):
+        f1 = np.array(fbs[k].f1[:3])
+        assert abs(f1[2] - (3 - k) * weight) < 0.05 * weight, (k, f1)
+        assert np.abs(f1[:2]).max() < 0.05 * weight
+        if k > 0:
+            f2 = np.array(fbs[k].f2[:3])
+            assert np.abs(f2 + f1).max() < 1e-3 * weight, (k, f1, f2)
+        else:
+            assert np.array(fbs[k].f2[:3]).tolist() == [0.0, 0.0, 0.0]
+    L.dWorldDestroy(w)
