@@ -167,8 +167,15 @@ def run_adjoint(local_rank, reps=3):
     sc = S.hinge_chains(n_worlds=n_w, steps=n_steps)
     B = Batch(sc, device=local_rank)
     stream = torch.cuda.ExternalStream(B.stream_handle())
-    x0 = torch.tensor(B.state(), dtype=torch.float32, device="cuda")
     seeds = B.seeds()
+    x0n = B.state()
+    B.step(20)
+    B.sync()
+    B.autotune(4)
+    B.set_state(x0n)
+    B.set_seeds(seeds)
+    B.set_step_index(0)
+    x0 = torch.tensor(x0n, dtype=torch.float32, device="cuda")
     nbt = B.nb_total
     g_final = torch.zeros((nbt, 13), dtype=torch.float32, device="cuda")
     ends = torch.tensor(sc.body_off[1:] - 1, dtype=torch.long, device="cuda")
@@ -220,13 +227,15 @@ def run_vehicles(local_rank, steps=300):
     B = Batch(sc, device=local_rank)
     stream = torch.cuda.ExternalStream(B.stream_handle())
     x0, seeds = B.state(), B.seeds()
-    B.step(3)
+    B.step(30)
     B.sync()
+    B.autotune(4)
     B.set_state(x0)
     B.set_seeds(seeds)
     B.set_step_index(0)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
+    B.set_timing(True)
     with torch.cuda.stream(stream):
         e0.record(stream)
     B.step(steps)
@@ -234,6 +243,8 @@ def run_vehicles(local_rank, steps=300):
         e1.record(stream)
     B.sync()
     t = e0.elapsed_time(e1) / 1e3
+    kern_ms, kern_steps = B.kernel_times()
+    B.set_timing(False)
     nc, nr, _ = B.counts()
     status = B.status()
     B.close()
@@ -243,6 +254,9 @@ def run_vehicles(local_rank, steps=300):
                         "hinge2 suspension ERP 0.4 CFM 0.01), 256x256 fractal heightfield (0.5 m, sigma 0.3), "
                         "steer U[-0.4,0.4] rad, throttle U[0,1]*400 N m, 300 steps from the initial state",
             "contacts_last_step": int(nc.sum()), "rows_last_step": int(nr.sum()),
+            "kernel_ms_per_step": {"collide": kern_ms[0] / max(1, kern_steps),
+                                   "setup": kern_ms[1] / max(1, kern_steps),
+                                   "solve": kern_ms[2] / max(1, kern_steps)},
             "worlds_with_status": int((status != 0).sum())}
 
 
@@ -303,6 +317,9 @@ def run_ours(args):
     for _ in range(args.warmup):
         B.step(1)
     B.sync()
+    # launch shapes picked by the library's autotuner on the warmed-up state
+    # (outside the timed region; the state is restored below)
+    launch_cfg = B.autotune(4)
     reset()
     barrier()
     clocks = ClockSampler(local_rank)
@@ -379,6 +396,8 @@ def run_ours(args):
                            "l2": "flushed between timed steps (256 MB write)",
                            "rows_per_world_avg": rows_total / (args.steps * N_WORLDS),
                            "bodies": int(nbt), "worlds_with_status": int((stat != 0).sum()),
+                           "launch_shape": {"collide": launch_cfg[0], "setup": launch_cfg[1],
+                                            "solve": launch_cfg[2]},
                            "step_ms_min_median_max": [float(1e3 * times.min()), float(1e3 * np.median(times)),
                                                       float(1e3 * times.max())]},
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
@@ -436,11 +455,21 @@ def main():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-vehicles", action="store_true")
+    ap.add_argument("--only-adjoint", action="store_true",
+                    help="print only the forward + adjoint measurement (for profiling)")
+    ap.add_argument("--only-vehicles", action="store_true",
+                    help="print only the vehicle-batch measurement (for profiling)")
     ap.add_argument("--cpu-worlds", type=int, default=512)
     ap.add_argument("--ref-worlds", type=int, default=4096)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.only_adjoint or args.only_vehicles:
+        import torch
+        _, _, local_rank = rank_env()
+        torch.cuda.set_device(local_rank)
+        out = run_adjoint(local_rank) if args.only_adjoint else run_vehicles(local_rank)
+        print(json.dumps(out), flush=True)
     else:
         run_ours(args)
 

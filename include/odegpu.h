@@ -98,6 +98,18 @@ int odegpuBatchRolloutBackward(odegpuBatchID b, const float* grad_state_final, f
                                float* grad_joint_torque, float* grad_body_force);
 int odegpuBatchAdjointStatus(odegpuBatchID b, int* status);
 
+/* Launch shape of each kernel (no counterpart in the reference): kernel 0
+ * collide, 1 setup, 2 solve, 3 adjoint; warps per block (one world per warp;
+ * at most 4, 8, 8, 4) and the preferred shared-memory carveout in percent of
+ * the unified L1/shared array (-1 = driver default). GetLaunchConfig writes
+ * cfg[8] = {wpb, carveout} per kernel. Autotune times n_steps steps of every
+ * candidate shape on the batch's current state (restored after each trial)
+ * and keeps the fastest per kernel; the batch state, seeds and step index are
+ * unchanged afterwards. */
+int odegpuBatchSetLaunchConfig(odegpuBatchID b, int kernel, int warps_per_block, int smem_carveout);
+int odegpuBatchGetLaunchConfig(odegpuBatchID b, int* cfg);
+int odegpuBatchAutotune(odegpuBatchID b, int n_steps);
+
 /* Instrumentation (no counterpart in the reference).
  * SetTiming(on) makes every following non-graph step record CUDA events on
  * the batch stream around its three kernels (collide, setup, solve) and

@@ -108,13 +108,22 @@ OG_D void vjp_rar(const float* R, const float* A, const float* Mb, float* Rb) {
     }
 }
 
+// One 128-byte row with eight 16-byte loads (the row store is 128-byte aligned).
 OG_D void load_row_words(const float* row, float* J, float* iMJ, float& b, float& cfmA, float& lo, float& hi,
                          int& f, int& b1, int& b2) {
-  for (int k = 0; k < 12; ++k) { J[k] = row[k]; iMJ[k] = row[12 + k]; }
-  b = row[kRowC]; cfmA = row[kRowCfm]; lo = row[kRowLo]; hi = row[kRowHi];
-  f = __float_as_int(row[kRowFindex]);
-  b1 = __float_as_int(row[kRowB1]);
-  b2 = __float_as_int(row[kRowB2]);
+  const float4* r4 = reinterpret_cast<const float4*>(row);
+  float4 v[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) v[k] = r4[k];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    J[4 * k] = v[k].x; J[4 * k + 1] = v[k].y; J[4 * k + 2] = v[k].z; J[4 * k + 3] = v[k].w;
+    iMJ[4 * k] = v[3 + k].x; iMJ[4 * k + 1] = v[3 + k].y; iMJ[4 * k + 2] = v[3 + k].z; iMJ[4 * k + 3] = v[3 + k].w;
+  }
+  b = v[6].x; cfmA = v[6].y; lo = v[6].z; hi = v[6].w;
+  f = __float_as_int(v[7].x);
+  b1 = __float_as_int(v[7].y);
+  b2 = __float_as_int(v[7].z);
 }
 
 // Derivative of the rows of persistent joint `ord` (rows r0..r0+m-1) with
@@ -484,7 +493,13 @@ __global__ void __launch_bounds__(128) adjoint_step_kernel(BatchDev d, AdjDev a,
           float Jp[12], iMJ[12], bb, cfmA, lo, hi;
           int f, b1, b2;
           load_row_words(rows + (size_t)r * kRowWords, Jp, iMJ, bb, cfmA, lo, hi, f, b1, b2);
-          float* rt = rt0 + r * kAdjRow;
+          float4* rt4 = reinterpret_cast<float4*>(rt0 + r * kAdjRow);   // 112-byte records, 16-byte aligned
+          float acc[kAdjRow];
+#pragma unroll
+          for (int q = 0; q < 7; ++q) {
+            const float4 t = rt4[q];
+            acc[4 * q] = t.x; acc[4 * q + 1] = t.y; acc[4 * q + 2] = t.z; acc[4 * q + 3] = t.w;
+          }
           const float old = lamT[(size_t)it * rc + r];
           const unsigned char code = codeT[(size_t)it * rc + r];
           const float dl = S.lambda[r] - old;
@@ -496,9 +511,9 @@ __global__ void __launch_bounds__(128) adjoint_step_kernel(BatchDev d, AdjDev a,
           for (int q = 0; q < 6; ++q) fc1[q] -= dl * iMJ[q];
           if (fc2) for (int q = 0; q < 6; ++q) fc2[q] -= dl * iMJ[6 + q];
           float dlb = 0.f;
-          for (int q = 0; q < 6; ++q) { dlb += iMJ[q] * fb1[q]; rt[kRiMJ + q] += dl * fb1[q]; }
+          for (int q = 0; q < 6; ++q) { dlb += iMJ[q] * fb1[q]; acc[kRiMJ + q] += dl * fb1[q]; }
           if (fc2)
-            for (int q = 0; q < 6; ++q) { dlb += iMJ[6 + q] * fb2[q]; rt[kRiMJ + 6 + q] += dl * fb2[q]; }
+            for (int q = 0; q < 6; ++q) { dlb += iMJ[6 + q] * fb2[q]; acc[kRiMJ + 6 + q] += dl * fb2[q]; }
           const float lnb = lamb[r] + dlb;
           float oldb = -dlb;
           float ub = 0.f;
@@ -511,11 +526,14 @@ __global__ void __launch_bounds__(128) adjoint_step_kernel(BatchDev d, AdjDev a,
           }
           // u = old + b' - old cfmA - J'.fc
           oldb += ub * (1.f - cfmA);
-          rt[kRb] += ub;
-          rt[kRcfm] -= ub * old;
-          for (int q = 0; q < 6; ++q) { rt[kRJ + q] -= ub * fc1[q]; fb1[q] -= ub * Jp[q]; }
+          acc[kRb] += ub;
+          acc[kRcfm] -= ub * old;
+          for (int q = 0; q < 6; ++q) { acc[kRJ + q] -= ub * fc1[q]; fb1[q] -= ub * Jp[q]; }
           if (fc2)
-            for (int q = 0; q < 6; ++q) { rt[kRJ + 6 + q] -= ub * fc2[q]; fb2[q] -= ub * Jp[6 + q]; }
+            for (int q = 0; q < 6; ++q) { acc[kRJ + 6 + q] -= ub * fc2[q]; fb2[q] -= ub * Jp[6 + q]; }
+#pragma unroll
+          for (int q = 0; q < 7; ++q)
+            rt4[q] = make_float4(acc[4 * q], acc[4 * q + 1], acc[4 * q + 2], acc[4 * q + 3]);
           lamb[r] = oldb;
           S.lambda[r] = old;
         }

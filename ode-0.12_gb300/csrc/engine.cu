@@ -56,7 +56,7 @@ __global__ void __launch_bounds__(128, 4) world_collide_kernel(BatchDev d, const
   world_collide(d, w, step, S, lane, opt);
 }
 
-__global__ void __launch_bounds__(128) world_setup_kernel(BatchDev d, const int* order, int first, int count,
+__global__ void __launch_bounds__(256) world_setup_kernel(BatchDev d, const int* order, int first, int count,
                                                           int step, StepOptions opt) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & 31;
@@ -70,7 +70,7 @@ __global__ void __launch_bounds__(128) world_setup_kernel(BatchDev d, const int*
   world_setup(d, w, step, S, lane, opt);
 }
 
-__global__ void __launch_bounds__(128) world_solve_kernel(BatchDev d, const int* order, int first, int count,
+__global__ void __launch_bounds__(256) world_solve_kernel(BatchDev d, const int* order, int first, int count,
                                                           StepOptions opt) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & 31;
@@ -132,6 +132,12 @@ struct odegpuBatch {
   int n_worlds = 0, nb_total = 0, ng_total = 0, nj_total = 0;
   long long row_cap_total = 0, contact_cap_total = 0;
   int warps_per_block = 4;
+  // per-kernel launch shape: warps per block and preferred shared-memory
+  // carveout (percent of the unified L1/shared array, -1 = driver default)
+  // for the collide, setup, solve and adjoint kernels (odegpuBatchSetLaunchConfig
+  // / odegpuBatchAutotune)
+  int kwpb[4] = {4, 4, 4, 4};
+  int kcarve[4] = {-1, -1, -1, -1};
   int step_counter = 0;
   cudaStream_t stream = nullptr;
   std::vector<WorldDesc> h_world;
@@ -230,13 +236,13 @@ struct odegpuBatch {
   }
   // collide + setup of one step of every world (no solve), for the adjoint
   int launch_setup(int step, const StepOptions& opt) {
-    const int wpb = warps_per_block;
-    const int blocks = (n_worlds + wpb - 1) / wpb;
     const BatchDev d = dev();
-    world_collide_kernel<<<blocks, wpb * 32, (size_t)wpb * kCollideSmemPerWarp, stream>>>(d, order.p, 0,
-                                                                                         n_worlds, step, opt);
-    world_setup_kernel<<<blocks, wpb * 32, (size_t)wpb * kSmemPerWarp, stream>>>(d, order.p, 0, n_worlds, step,
-                                                                                opt);
+    apply_carveout(0);
+    world_collide_kernel<<<nblocks(n_worlds, 0), kwpb[0] * 32, (size_t)kwpb[0] * kCollideSmemPerWarp, stream>>>(
+        d, order.p, 0, n_worlds, step, opt);
+    apply_carveout(1);
+    world_setup_kernel<<<nblocks(n_worlds, 1), kwpb[1] * 32, (size_t)kwpb[1] * kSmemPerWarp, stream>>>(
+        d, order.p, 0, n_worlds, step, opt);
     launches += 2;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return fail(ODEGPU_E_CUDA, std::string("setup launch: ") + cudaGetErrorString(e));
@@ -247,27 +253,46 @@ struct odegpuBatch {
   // the identity order when use_order is false); 3 launches per step.
   DBuf<float> jcopy, feedback;       // joint feedback (odegpuBatchSetFeedback)
   bool feedback_on = false;
+  bool single_world = false;         // one world per launch (the plain comparator)
+
+  int nblocks(int count, int k) const { return (count + kwpb[k] - 1) / kwpb[k]; }
+  // the carveout is a property of the kernel function: set it when it differs
+  // from what the last launch of that kernel used (any batch)
+  void apply_carveout(int k) {
+    static int current[4] = {-1, -1, -1, -1};
+    if (current[k] == kcarve[k]) return;
+    const void* fn = k == 0 ? (const void*)world_collide_kernel
+                   : k == 1 ? (const void*)world_setup_kernel
+                   : k == 2 ? (const void*)world_solve_kernel : (const void*)adjoint_step_kernel;
+    if (cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, kcarve[k]) == cudaSuccess)
+      current[k] = kcarve[k];
+    else
+      cudaGetLastError();
+  }
 
   int launch(int first, int count, int n_steps, const StepOptions& opt_in, bool use_order = true) {
     StepOptions opt = opt_in;
     if (feedback_on) { opt.jcopy = jcopy.p; opt.feedback = feedback.p; }
-    const int wpb = warps_per_block;
-    const int blocks = (count + wpb - 1) / wpb;
     const BatchDev d = dev();
     const int* ord = (use_order && order.p) ? order.p : nullptr;
     cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
     cudaStreamIsCapturing(stream, &cap);
     const bool tm = timing && cap == cudaStreamCaptureStatusNone;
+    int w[3];
+    for (int k = 0; k < 3; ++k) w[k] = single_world ? 1 : kwpb[k];
     for (int s = 0; s < n_steps; ++s) {
       mark(tm);
-      world_collide_kernel<<<blocks, wpb * 32, (size_t)wpb * kCollideSmemPerWarp, stream>>>(
+      apply_carveout(0);
+      world_collide_kernel<<<(count + w[0] - 1) / w[0], w[0] * 32, (size_t)w[0] * kCollideSmemPerWarp, stream>>>(
           d, ord, first, count, step_counter + s, opt);
       mark(tm);
-      world_setup_kernel<<<blocks, wpb * 32, (size_t)wpb * kSmemPerWarp, stream>>>(d, ord, first, count,
-                                                                                  step_counter + s, opt);
+      apply_carveout(1);
+      world_setup_kernel<<<(count + w[1] - 1) / w[1], w[1] * 32, (size_t)w[1] * kSmemPerWarp, stream>>>(
+          d, ord, first, count, step_counter + s, opt);
       mark(tm);
-      world_solve_kernel<<<blocks, wpb * 32, (size_t)wpb * kSorSmemPerWarp, stream>>>(d, ord, first, count,
-                                                                                    opt);
+      apply_carveout(2);
+      world_solve_kernel<<<(count + w[2] - 1) / w[2], w[2] * 32, (size_t)w[2] * kSorSmemPerWarp, stream>>>(
+          d, ord, first, count, opt);
       mark(tm);
       launches += 3;
     }
@@ -277,18 +302,21 @@ struct odegpuBatch {
   }
 };
 
-static int configure_kernels(int wpb) {
+// Largest block shapes (warps per block) the launch configuration accepts.
+constexpr int kMaxWpb[4] = {4, 8, 8, 4};
+
+static int configure_kernels() {
   if (cudaFuncSetAttribute(world_collide_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)(wpb * kCollideSmemPerWarp)) != cudaSuccess)
+                           (int)(kMaxWpb[0] * kCollideSmemPerWarp)) != cudaSuccess)
     return -1;
   if (cudaFuncSetAttribute(world_setup_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)(wpb * kSmemPerWarp)) != cudaSuccess)
+                           (int)(kMaxWpb[1] * kSmemPerWarp)) != cudaSuccess)
     return -1;
   if (cudaFuncSetAttribute(world_solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)(wpb * kSorSmemPerWarp)) != cudaSuccess)
+                           (int)(kMaxWpb[2] * kSorSmemPerWarp)) != cudaSuccess)
     return -1;
   if (cudaFuncSetAttribute(adjoint_step_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)(4 * kAdjSmemPerWarp)) != cudaSuccess)
+                           (int)(kMaxWpb[3] * kAdjSmemPerWarp)) != cudaSuccess)
     return -1;
   return 0;
 }
@@ -605,7 +633,8 @@ int odegpuBatchCreate(const odegpuScene* sc, const odegpuBatchConfig* cfg, odegp
     std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return wd[a].nb > wd[b].nb; });
     rc = B->order.upload(ord);
   }
-  if (!rc && configure_kernels(B->warps_per_block) != 0) rc = fail(ODEGPU_E_CUDA, "cannot configure shared memory");
+  if (!rc && configure_kernels() != 0) rc = fail(ODEGPU_E_CUDA, "cannot configure shared memory");
+  for (int k = 0; k < 3; ++k) B->kwpb[k] = std::min(B->warps_per_block, kMaxWpb[k]);
   if (rc) { delete B; return rc; }
   *out = B;
   return 0;
@@ -656,18 +685,17 @@ int odegpuBatchStepPlain(odegpuBatchID b, int n_steps) {
   if (!b || n_steps < 0) return fail(ODEGPU_E_ARG, "bad arguments");
   OG_CUDA(cudaSetDevice(b->device));
   StepOptions opt{1, nullptr, nullptr, nullptr, 0, 0};
-  const int saved = b->warps_per_block;
-  b->warps_per_block = 1;
+  b->single_world = true;
   for (int w = 0; w < b->n_worlds; ++w) {
     for (int s = 0; s < n_steps; ++s) {
       const int base = b->step_counter;
       b->step_counter = base + s;
       const int rc = b->launch(w, 1, 1, opt, false);
       b->step_counter = base;
-      if (rc) { b->warps_per_block = saved; return rc; }
+      if (rc) { b->single_world = false; return rc; }
     }
   }
-  b->warps_per_block = saved;
+  b->single_world = false;
   b->step_counter += n_steps;
   return 0;
 }
@@ -743,6 +771,81 @@ int odegpuBatchGetFeedback(odegpuBatchID b, double* out) {
   if (!tmp.empty())
     OG_CUDA(cudaMemcpy(tmp.data(), b->feedback.p, tmp.size() * sizeof(float), cudaMemcpyDeviceToHost));
   for (size_t i = 0; i < tmp.size(); ++i) out[i] = tmp[i];
+  return 0;
+}
+
+int odegpuBatchSetLaunchConfig(odegpuBatchID b, int kernel, int warps_per_block, int smem_carveout) {
+  if (!b || kernel < 0 || kernel > 3) return fail(ODEGPU_E_ARG, "bad kernel index");
+  if (warps_per_block < 1 || warps_per_block > kMaxWpb[kernel])
+    return fail(ODEGPU_E_ARG, "warps per block out of range for this kernel");
+  if (smem_carveout < -1 || smem_carveout > 100) return fail(ODEGPU_E_ARG, "carveout must be -1 or 0..100");
+  b->kwpb[kernel] = warps_per_block;
+  b->kcarve[kernel] = smem_carveout;
+  return 0;
+}
+
+int odegpuBatchAutotune(odegpuBatchID b, int n_steps) {
+  if (!b || n_steps < 1) return fail(ODEGPU_E_ARG, "bad arguments");
+  OG_CUDA(cudaSetDevice(b->device));
+  OG_CUDA(cudaStreamSynchronize(b->stream));
+  const size_t rec = (size_t)b->nb_total * ODEGPU_BODY_REC;
+  DBuf<float> st;
+  DBuf<unsigned> sd;
+  if (int rc = st.alloc(rec)) return rc;
+  if (int rc = sd.alloc((size_t)b->n_worlds)) return rc;
+  b->pack_to(st.p);
+  OG_CUDA(cudaMemcpyAsync(sd.p, b->seed.p, b->n_worlds * sizeof(unsigned), cudaMemcpyDeviceToDevice, b->stream));
+  const int saved_counter = b->step_counter;
+  const bool saved_timing = b->timing;
+  auto restore = [&]() -> int {
+    b->unpack_from(st.p);
+    OG_CUDA(cudaMemcpyAsync(b->seed.p, sd.p, b->n_worlds * sizeof(unsigned), cudaMemcpyDeviceToDevice,
+                            b->stream));
+    b->step_counter = saved_counter;
+    return 0;
+  };
+  static const int kWpb[] = {1, 2, 4, 8};
+  static const int kCarve[] = {-1, 25, 50, 75, 100};
+  double best[3] = {INFINITY, INFINITY, INFINITY};
+  int best_w[3] = {b->kwpb[0], b->kwpb[1], b->kwpb[2]}, best_c[3] = {b->kcarve[0], b->kcarve[1], b->kcarve[2]};
+  StepOptions opt{1, nullptr, nullptr, nullptr, 0, 0};
+  b->timing = true;
+  int rc = 0;
+  for (int wi = 0; wi < 4 && !rc; ++wi) {
+    for (int ci = 0; ci < 5 && !rc; ++ci) {
+      bool tried[3];
+      for (int k = 0; k < 3; ++k) {
+        tried[k] = kWpb[wi] <= kMaxWpb[k];
+        b->kwpb[k] = tried[k] ? kWpb[wi] : best_w[k];
+        b->kcarve[k] = tried[k] ? kCarve[ci] : best_c[k];
+      }
+      if ((rc = restore())) break;
+      if ((rc = b->launch(0, b->n_worlds, 1, opt))) break;       // warm-up step (not counted)
+      b->ev_used = 0;
+      if ((rc = b->launch(0, b->n_worlds, n_steps, opt))) break;
+      if (cudaStreamSynchronize(b->stream) != cudaSuccess) { rc = fail(ODEGPU_E_CUDA, "autotune step"); break; }
+      double ms[3] = {0, 0, 0};
+      for (size_t q = 0; q + 3 < b->ev_used; q += 4)
+        for (int k = 0; k < 3; ++k) {
+          float t = 0.f;
+          cudaEventElapsedTime(&t, b->ev_pool[q + k], b->ev_pool[q + k + 1]);
+          ms[k] += t;
+        }
+      for (int k = 0; k < 3; ++k)
+        if (tried[k] && ms[k] < best[k]) { best[k] = ms[k]; best_w[k] = kWpb[wi]; best_c[k] = kCarve[ci]; }
+    }
+  }
+  for (int k = 0; k < 3; ++k) { b->kwpb[k] = best_w[k]; b->kcarve[k] = best_c[k]; }
+  b->ev_used = 0;
+  b->timing = saved_timing;
+  if (!rc) rc = restore();
+  if (!rc && cudaStreamSynchronize(b->stream) != cudaSuccess) rc = fail(ODEGPU_E_CUDA, "autotune restore");
+  return rc;
+}
+
+int odegpuBatchGetLaunchConfig(odegpuBatchID b, int* cfg) {
+  if (!b || !cfg) return fail(ODEGPU_E_ARG, "bad arguments");
+  for (int k = 0; k < 4; ++k) { cfg[2 * k] = b->kwpb[k]; cfg[2 * k + 1] = b->kcarve[k]; }
   return 0;
 }
 
@@ -874,8 +977,9 @@ int odegpuBatchRolloutBackward(odegpuBatchID b, const float* grad_final, float* 
       OG_CUDA(cudaMemcpyAsync(b->seed.p, R.seg_seed.p + (size_t)j * b->n_worlds, b->n_worlds * sizeof(unsigned),
                               cudaMemcpyDeviceToDevice, b->stream));
       if (int rc = b->launch_setup(step, tap)) { b->step_counter = saved_counter; return rc; }
-      adjoint_step_kernel<<<(b->n_worlds + 3) / 4, 128, 4 * (size_t)kAdjSmemPerWarp, b->stream>>>(b->dev(), a,
-                                                                                                step);
+      b->apply_carveout(3);
+      adjoint_step_kernel<<<b->nblocks(b->n_worlds, 3), b->kwpb[3] * 32, b->kwpb[3] * (size_t)kAdjSmemPerWarp,
+                            b->stream>>>(b->dev(), a, step);
       b->launches += 1;
     }
   }
@@ -1105,12 +1209,13 @@ WorldCtx* ctx_create(int device) {
   c->B.device = device;
   c->B.n_worlds = 1;
   c->B.warps_per_block = 1;
+  for (int k = 0; k < 4; ++k) c->B.kwpb[k] = 1;
   if (cudaStreamCreateWithFlags(&c->B.stream, cudaStreamNonBlocking) != cudaSuccess) {
     delete c;
     fail(ODEGPU_E_CUDA, "stream creation failed");
     return nullptr;
   }
-  configure_kernels(4);
+  configure_kernels();
   return c;
 }
 

@@ -248,20 +248,20 @@ OG_D int hf_zone(const DevHeightfield& H, const float* heights, int minX, int ma
     porder[numPlanes] = (unsigned char)numPlanes;
     ++numPlanes;
   }
-  // sortPlanes (heightfield.cpp:910-932): bubble sort, descending height
-  {
-    bool swapped = true;
-    while (swapped) {
-      swapped = false;
-      for (int i = 0; i < numPlanes - 1; ++i) {
-        if ((pmax[porder[i]] - pmax[porder[i + 1]]) > kHFEps) {
-          const unsigned char t = porder[i];
-          porder[i] = porder[i + 1];
-          porder[i + 1] = t;
-          swapped = true;
-        }
-      }
+  // sortPlanes (heightfield.cpp:910-932) bubble-sorts the planes, swapping
+  // neighbours whose first height exceeds the second by more than dEpsilon.
+  // An insertion sort with the same neighbour test performs only such swaps
+  // and yields the same order whenever heights are equal or further apart
+  // than dEpsilon; it needs far fewer passes.
+  for (int i = 1; i < numPlanes; ++i) {
+    const unsigned char cur = porder[i];
+    const float key = pmax[cur];
+    int j = i;
+    while (j > 0 && (pmax[porder[j - 1]] - key) > kHFEps) {
+      porder[j] = porder[j - 1];
+      --j;
     }
+    porder[j] = cur;
   }
   int nc = 0;
   const unsigned plane_flags = (flags & ~0xffffu) | kHFMaxcPerCell;

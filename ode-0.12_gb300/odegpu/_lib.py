@@ -43,6 +43,9 @@ def _declare(L):
         "odegpuBatchSetControlsF32": (i, [v, i, v, v]),
         "odegpuBatchSetJointStops": (i, [v, i, _P(d)]),
         "odegpuBatchSetFeedback": (i, [v, i]),
+        "odegpuBatchSetLaunchConfig": (i, [v, i, i, i]),
+        "odegpuBatchGetLaunchConfig": (i, [v, _P(i)]),
+        "odegpuBatchAutotune": (i, [v, i]),
         "odegpuBatchGetFeedback": (i, [v, _P(d)]),
         "odegpuBatchRolloutForward": (i, [v, i, i]),
         "odegpuBatchRolloutBackward": (i, [v, v, v, v, v]),

@@ -153,6 +153,20 @@ class Batch:
         check(lib().odegpuBatchGetFeedback(self.h, out.ctypes.data_as(_P(C.c_double))))
         return out[:self.nj_total]
 
+    def set_launch_config(self, kernel, warps_per_block, smem_carveout=-1):
+        """kernel: 0 collide, 1 setup, 2 solve, 3 adjoint."""
+        check(lib().odegpuBatchSetLaunchConfig(self.h, int(kernel), int(warps_per_block), int(smem_carveout)))
+
+    def launch_config(self):
+        cfg = (C.c_int * 8)()
+        check(lib().odegpuBatchGetLaunchConfig(self.h, cfg))
+        return [(cfg[2 * k], cfg[2 * k + 1]) for k in range(4)]
+
+    def autotune(self, n_steps=4):
+        """Pick each kernel's launch shape by timing candidates on the current state."""
+        check(lib().odegpuBatchAutotune(self.h, int(n_steps)))
+        return self.launch_config()
+
     def adjoint_status(self):
         out = np.zeros(self.n_worlds, np.int32)
         check(lib().odegpuBatchAdjointStatus(self.h, out.ctypes.data_as(_P(C.c_int))))
