@@ -41,6 +41,23 @@ def rank_env():
             int(os.environ.get("LOCAL_RANK", "0")))
 
 
+def rank_scene_seed(rank):
+    """Weak scaling: every rank steps its own batch of the workload, seeded by rank."""
+    return SCENE_SEED + rank
+
+
+def max_over_ranks(value, device="cpu"):
+    """Max of a per-rank number over the process group (the value itself
+    without one): the timed region ends when the slowest rank ends."""
+    import torch
+    import torch.distributed as tdist
+    if not (tdist.is_available() and tdist.is_initialized()) or tdist.get_world_size() == 1:
+        return float(value)
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def build_scene(n_worlds, seed=SCENE_SEED):
     from odegpu import scene as S
     return S.batched_worlds(n_worlds=n_worlds, seed=seed)
@@ -296,7 +313,7 @@ def run_ours(args):
     torch.cuda.set_device(local_rank)
     # weak scaling: every rank steps its own 4096-world batch (distinct seeds);
     # the step has no collective, only the timing is reduced
-    sc = build_scene(N_WORLDS, seed=SCENE_SEED + rank)
+    sc = build_scene(N_WORLDS, seed=rank_scene_seed(rank))
     B = Batch(sc, device=local_rank)
     stream = torch.cuda.ExternalStream(B.stream_handle())
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
@@ -352,11 +369,7 @@ def run_ours(args):
     times = np.array([a.elapsed_time(b) for a, b in ev]) / 1e3
     t_kernel = float(times.sum())
     stat = B.status()
-    t_max = t_kernel
-    if dist:
-        t = torch.tensor([t_kernel], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_max = float(t.item())
+    t_max = max_over_ranks(t_kernel, device="cuda")
     value = N_WORLDS * world_size * args.steps / t_max
 
     # e2e through the C ABI with host buffers: per step H2D of the state from
@@ -376,7 +389,7 @@ def run_ours(args):
         B.sync()
         h_in, h_out = h_out, h_in
     barrier()
-    t_e2e = time.perf_counter() - t0
+    t_e2e = max_over_ranks(time.perf_counter() - t0, device="cuda")
     e2e = N_WORLDS * world_size * args.steps / t_e2e
 
     if rank == 0:
