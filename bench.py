@@ -264,8 +264,31 @@ def run_vehicles(local_rank, steps=300):
     B.set_timing(False)
     nc, nr, _ = B.counts()
     status = B.status()
+    # forward + adjoint of the final chassis positions with respect to the
+    # control sequence (drive torques), checkpoints every 10 steps
+    B.set_state(x0)
+    B.set_seeds(seeds)
+    B.set_step_index(0)
+    nbt = B.nb_total
+    g_final = torch.zeros((nbt, 13), dtype=torch.float32, device="cuda")
+    chassis = torch.tensor(sc.body_off[:-1], dtype=torch.long, device="cuda")
+    g_final[chassis, 0:3] = 1.0
+    g_jt = torch.zeros((steps, B.nj_total, 2), dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        a0.record(stream)
+    B.rollout_forward(steps, 10)
+    B.rollout_backward(g_final.data_ptr(), None, g_jt.data_ptr(), None)
+    with torch.cuda.stream(stream):
+        a1.record(stream)
+    B.sync()
+    t_adj = a0.elapsed_time(a1) / 1e3
+    adj_status = B.adjoint_status()
     B.close()
     return {"metric": "world-steps/s, vehicle batch (heightfield + hinge2)", "value": 2048 * steps / t,
+            "forward_plus_adjoint": 2048 * steps / t_adj,
+            "adjoint_worlds_with_unmodelled_terms": int((adj_status != 0).sum()),
             "unit": "world-steps/s", "ms_per_step": 1e3 * t / steps,
             "workload": "vehicles: 2048 cars (2x1x0.5 m 1000 kg chassis, 4 sphere wheels r 0.35 m 20 kg, "
                         "hinge2 suspension ERP 0.4 CFM 0.01), 256x256 fractal heightfield (0.5 m, sigma 0.3), "

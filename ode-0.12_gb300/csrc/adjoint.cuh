@@ -26,8 +26,8 @@ namespace og {
 // Status bits of the adjoint (per world): a part of the step whose
 // derivative is not modelled was met (the gradient leaves it out).
 enum {
-  ADJ_UNSUPPORTED_JOINT = 1,     // hinge2 rows, or a hinge limit row
-  ADJ_UNSUPPORTED_CONTACT = 2,   // contact not between a body geom and a plane, or bounce
+  ADJ_UNSUPPORTED_JOINT = 1,     // a hinge limit row, a bouncing hinge2 limit, hinge2 without body 2
+  ADJ_UNSUPPORTED_CONTACT = 2,   // body-body contact, capsule vertex contact, geom under a field, bounce
   ADJ_TOO_LARGE = 4
 };
 
@@ -129,9 +129,135 @@ OG_D void load_row_words(const float* row, float* J, float* iMJ, float& b, float
 // Derivative of the rows of persistent joint `ord` (rows r0..r0+m-1) with
 // respect to its bodies' positions (into state_bar) and rotations (into the
 // d/dR scratch).
+// hinge2 (ode/src/joints/hinge2.cpp:109-180, setBall2 joint.cpp:134-196,
+// measureAngle hinge2.cpp:33-41): d/d of its rows with respect to the bodies'
+// positions and rotations. lm1: limot1 with this step's stops.
+OG_D int vjp_hinge2(const BatchDev& d, const WorldDesc& D, const AdjDev& a, const DevJoint& J, const DevLimot& lm1,
+                    int r0, int m, float k) {
+  if (J.b2 < 0) return ADJ_UNSUPPORTED_JOINT;
+  const int g1 = D.body_off + J.b1, g2 = D.body_off + J.b2;
+  float R1[12], R2[12];
+  body_R(d, g1, R1);
+  body_R(d, g2, R2);
+  const float4 x1 = d.pos[g1], x2 = d.pos[g2];
+  float ax1[3], ax2[3], q1[3], q2[3], a1[3], a2[3];
+  mul0_331(ax1, R1, J.axis1);
+  mul0_331(ax2, R2, J.axis2);
+  plane_space(ax1, q1, q2);
+  mul0_331(a1, R1, J.anchor1);
+  mul0_331(a2, R2, J.anchor2);
+  const float dd[3] = {a2[0] + x2.x - a1[0] - x1.x, a2[1] + x2.y - a1[1] - x1.y, a2[2] + x2.z - a1[2] - x1.z};
+  const float h1 = 1.0f / D.dt;
+  const float kr[3] = {h1 * J.susp_erp, k, k};
+  const float* dirs[3] = {ax1, q1, q2};
+  const float* RT0 = a.row_tmp + (size_t)(D.row_off + r0) * kAdjRow;
+  float ax1b[3] = {0.f, 0.f, 0.f}, ax2b[3] = {0.f, 0.f, 0.f}, q1b[3] = {0.f, 0.f, 0.f}, q2b[3] = {0.f, 0.f, 0.f};
+  float a1b[3] = {0.f, 0.f, 0.f}, a2b[3] = {0.f, 0.f, 0.f}, db[3] = {0.f, 0.f, 0.f};
+  float* dirb[3] = {ax1b, q1b, q2b};
+  // rows 0..2: J1l = dir, J1a = a1 x dir, J2l = -dir, J2a = -(a2 x dir), c = k_r dir.d
+  for (int r = 0; r < 3; ++r) {
+    const float* t = RT0 + r * kAdjRow;
+    const float* dir = dirs[r];
+    float* dbar = dirb[r];
+    float u[3];
+    for (int i = 0; i < 3; ++i) dbar[i] += t[i] - t[6 + i];
+    cross3(u, dir, t + 3);                 // d/da1 of a1 x dir
+    for (int i = 0; i < 3; ++i) a1b[i] += u[i];
+    cross3(u, t + 3, a1);                  // d/ddir of a1 x dir
+    for (int i = 0; i < 3; ++i) dbar[i] += u[i];
+    cross3(u, dir, t + 9);                 // J2a = -(a2 x dir)
+    for (int i = 0; i < 3; ++i) a2b[i] -= u[i];
+    cross3(u, t + 9, a2);
+    for (int i = 0; i < 3; ++i) dbar[i] -= u[i];
+    const float cb = kr[r] * t[kRC];
+    for (int i = 0; i < 3; ++i) { dbar[i] += cb * dd[i]; db[i] += cb * dir[i]; }
+  }
+  vjp_plane_space(ax1, q1b, q2b, ax1b);
+  // row 3: J1a = qn, J2a = -qn, c = k (c0 sn - s0 cs), q = ax1 x ax2, sn = |q|, cs = ax1.ax2
+  {
+    float q[3];
+    cross3(q, ax1, ax2);
+    const float sn = sqrtf(dot3(q, q));
+    const float* t = RT0 + 3 * kAdjRow;
+    if (sn > 0.f) {
+      const float qn[3] = {q[0] / sn, q[1] / sn, q[2] / sn};
+      float qnb[3];
+      for (int i = 0; i < 3; ++i) qnb[i] = t[3 + i] - t[9 + i];
+      const float snb = k * t[kRC] * J.c0;
+      const float csb = -k * t[kRC] * J.s0;
+      const float pr = dot3(qn, qnb);
+      float qb[3];
+      for (int i = 0; i < 3; ++i) qb[i] = snb * qn[i] + (qnb[i] - qn[i] * pr) / sn;
+      float u[3];
+      cross3(u, ax2, qb);
+      for (int i = 0; i < 3; ++i) ax1b[i] += u[i] + csb * ax2[i];
+      cross3(u, qb, ax1);
+      for (int i = 0; i < 3; ++i) ax2b[i] += u[i] + csb * ax1[i];
+    }
+  }
+  int flags = 0;
+  // limot rows: limot1 about ax1 (row 4), limot2 about ax2 (next row)
+  int row = 4;
+  if (row < m) {
+    // is row 4 limot1's? (it is when limot1 is limited or powered)
+    BodyRef B1, B2;
+    load_body_ref(d, g1, B1);
+    load_body_ref(d, g2, B2);
+    int limit = 0;
+    float err = 0.f;
+    if (limot_tested(lm1)) limot_test(lm1, hinge2_angle(B1, B2, J), limit, err);
+    if (limit || lm1.fmax > 0.f) {
+      const float* t = RT0 + row * kAdjRow;
+      for (int i = 0; i < 3; ++i) ax1b[i] += t[3 + i] - t[9 + i];
+      if (limit) {
+        if (lm1.bounce > 0.f && lm1.lostop != lm1.histop) flags |= ADJ_UNSUPPORTED_JOINT;
+        // c = -fps stop_erp (angle - stop); angle = -atan2(v2.b, v1.b), b = R1^T R2 axis2
+        const float angb = -(h1 * lm1.stop_erp) * t[kRC];
+        float e[3], bb[3];
+        mul0_331(e, R2, J.axis2);
+        mul1_331(bb, R1, e);
+        const float y = dot3(J.v2, bb), x = dot3(J.v1, bb);
+        const float r2 = x * x + y * y;
+        if (r2 > 0.f) {
+          const float yb = -angb * x / r2, xb = angb * y / r2;
+          float bbar[3], ebar[3];
+          for (int i = 0; i < 3; ++i) bbar[i] = yb * J.v2[i] + xb * J.v1[i];
+          mul0_331(ebar, R1, bbar);
+          float* Rb1 = a.body_tmp + (size_t)g1 * kAdjBody + kBR;
+          float* Rb2 = a.body_tmp + (size_t)g2 * kAdjBody + kBR;
+          for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) {
+              atomicAdd(Rb1 + i * 3 + j, e[i] * bbar[j]);
+              atomicAdd(Rb2 + i * 3 + j, ebar[i] * J.axis2[j]);
+            }
+        }
+      }
+      ++row;
+    }
+  }
+  if (row < m) {
+    const float* t = RT0 + row * kAdjRow;
+    for (int i = 0; i < 3; ++i) ax2b[i] += t[3 + i] - t[9 + i];
+  }
+  // chain to the bodies
+  for (int i = 0; i < 3; ++i) { a1b[i] -= db[i]; a2b[i] += db[i]; }
+  float* xb1 = a.state_bar + (size_t)g1 * 13;
+  float* xb2 = a.state_bar + (size_t)g2 * 13;
+  for (int i = 0; i < 3; ++i) { atomicAdd(xb1 + i, -db[i]); atomicAdd(xb2 + i, db[i]); }
+  float* Rb1 = a.body_tmp + (size_t)g1 * kAdjBody + kBR;
+  float* Rb2 = a.body_tmp + (size_t)g2 * kAdjBody + kBR;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      atomicAdd(Rb1 + i * 3 + j, ax1b[i] * J.axis1[j] + a1b[i] * J.anchor1[j]);
+      atomicAdd(Rb2 + i * 3 + j, ax2b[i] * J.axis2[j] + a2b[i] * J.anchor2[j]);
+    }
+  return flags;
+}
+
 OG_D int vjp_joint(const BatchDev& d, const WorldDesc& D, const AdjDev& a, int w, int ord, int r0, int m,
-                   float k) {
+                   float k, const float* stops) {
   const DevJoint& J = d.joints[D.joint_off + ord];
+  if (J.type == J_HINGE2) return vjp_hinge2(d, D, a, J, step_limot1(J, stops, ord), r0, m, k);
   if (J.type != J_BALL && J.type != J_HINGE) return ADJ_UNSUPPORTED_JOINT;
   int flags = 0;
   const int g1 = D.body_off + J.b1, g2 = J.b2 >= 0 ? D.body_off + J.b2 : -1;
@@ -221,10 +347,15 @@ OG_D int vjp_contact(const BatchDev& d, const WorldDesc& D, const AdjDev& a, int
   const DevSurface& S = d.surfaces[ct.surface];
   if (ct.geoms < 0 || ct.b2 >= 0) return ADJ_UNSUPPORTED_CONTACT;
   const int gA = D.geom_off + (ct.geoms & 0xff), gB = D.geom_off + ((ct.geoms >> 8) & 0xff);
+  const unsigned kind = ((unsigned)ct.geoms >> 16) & 3u;
   int gp, gs;
-  if (d.gtype[gA] == 4) { gp = gA; gs = gB; }
-  else if (d.gtype[gB] == 4) { gp = gB; gs = gA; }
+  bool hf = false;
+  if (d.gtype[gA] == G_PLANE || d.gtype[gA] == G_HEIGHTFIELD) { gp = gA; gs = gB; hf = d.gtype[gA] == G_HEIGHTFIELD; }
+  else if (d.gtype[gB] == G_PLANE || d.gtype[gB] == G_HEIGHTFIELD) {
+    gp = gB; gs = gA; hf = d.gtype[gB] == G_HEIGHTFIELD;
+  }
   else return ADJ_UNSUPPORTED_CONTACT;
+  if (hf && kind == kHFUnder) return ADJ_UNSUPPORTED_CONTACT;
   const int ts = d.gtype[gs];
   if (d.gbody[gs] != ct.b1 || (ts != 0 && ts != 1 && ts != 2)) return ADJ_UNSUPPORTED_CONTACT;
   if (S.mode & SURF_BOUNCE) return ADJ_UNSUPPORTED_CONTACT;
@@ -255,10 +386,55 @@ OG_D int vjp_contact(const BatchDev& d, const WorldDesc& D, const AdjDev& a, int
   const float motionN = (S.mode & SURF_MOTIONN) ? S.motionN : 0.f;
   float depth_b = 0.f;
   if (dep > 0.f && kk * dep + motionN < D.max_vel) depth_b = RT0[kRC] * kk;
-  // contact point and depth of the body-side geom against the plane
-  const float4 pp = d.gparam[gp];
-  const float np[3] = {pp.x, pp.y, pp.z};
+  // contact point and depth of the body-side geom against the plane; for a
+  // heightfield's plane pass, the plane of the triangle (its upward normal
+  // is the collider's normal, negated when the field came first)
+  float np[3];
+  if (hf) {
+    const float sgn = (gp == gA) ? -1.f : 1.f;
+    for (int i = 0; i < 3; ++i) np[i] = sgn * ct.normal[i];
+  } else {
+    const float4 pp = d.gparam[gp];
+    np[0] = pp.x; np[1] = pp.y; np[2] = pp.z;
+  }
   const float4 gprm = d.gparam[gs];
+  if (hf && kind == kHFVertex) {
+    // vertex pass: the contact point is a field sample (fixed); the depth is
+    // the geom's point depth at it (dGeomSpherePointDepth / dGeomBoxPointDepth)
+    float* xb = a.state_bar + (size_t)g1 * 13;
+    float* Rb = a.body_tmp + (size_t)g1 * kAdjBody + kBR;
+    for (int i = 0; i < 3; ++i) atomicAdd(xb + i, -c1b[i]);       // c1 = pos - x1
+    if (depth_b == 0.f) return 0;
+    const float v[3] = {ct.pos[0] - x[0], ct.pos[1] - x[1], ct.pos[2] - x[2]};
+    if (ts == 0) {
+      const float l = sqrtf(dot3(v, v));
+      if (l > 0.f)
+        for (int i = 0; i < 3; ++i) atomicAdd(xb + i, depth_b * v[i] / l);
+      return 0;
+    }
+    if (ts != 1) return ADJ_UNSUPPORTED_CONTACT;
+    float qv[3];
+    mul1_331(qv, R, v);
+    const float hs[3] = {0.5f * gprm.x, 0.5f * gprm.y, 0.5f * gprm.z};
+    float dist[6];
+    bool inside = true;
+    for (int i = 0; i < 3; ++i) {
+      dist[i] = hs[i] - qv[i];
+      dist[i + 3] = hs[i] + qv[i];
+      if (dist[i] < 0.f || dist[i + 3] < 0.f) inside = false;
+    }
+    int best = 0;
+    for (int i = 1; i < 6; ++i)
+      if (inside ? (dist[i] < dist[best]) : (dist[i] > dist[best])) best = i;
+    // depth = +-dist[best]; dist = h -+ q_j, q = R^T (v - x)
+    const int j = best % 3;
+    const float dq = (inside ? 1.f : -1.f) * (best < 3 ? -1.f : 1.f) * depth_b;   // d/dq_j
+    for (int i = 0; i < 3; ++i) {
+      atomicAdd(xb + i, -dq * R[i * 4 + j]);
+      atomicAdd(Rb + i * 3 + j, dq * v[i]);
+    }
+    return 0;
+  }
   float s[3] = {0.f, 0.f, 0.f};
   float rad = 0.f;
   const float rel[3] = {ct.pos[0] - x[0], ct.pos[1] - x[1], ct.pos[2] - x[2]};
@@ -591,13 +767,17 @@ __global__ void __launch_bounds__(128) adjoint_step_kernel(BatchDev d, AdjDev a,
 
     // 5. joint and contact rows backwards; the lane owning a joint's first row
     //    handles the joint (its rows are contiguous)
+    const int njt_all = d.world[d.n_worlds - 1].joint_off + d.world[d.n_worlds - 1].njp;
+    const float* stops = (d.joint_stop && d.n_ctrl_steps > 0)
+                             ? d.joint_stop + (size_t)(step % d.n_ctrl_steps) * njt_all + D.joint_off
+                             : nullptr;
     for (int r0 = lane; r0 < M; r0 += 32) {
       const int ord = __float_as_int(dbg[(size_t)r0 * kRowWords + kRowJoint]);
       if (r0 > 0 && __float_as_int(dbg[(size_t)(r0 - 1) * kRowWords + kRowJoint]) == ord) continue;
       int r1 = r0 + 1;
       while (r1 < M && __float_as_int(dbg[(size_t)r1 * kRowWords + kRowJoint]) == ord) ++r1;
       const float erp = dbg[(size_t)r0 * kRowWords + kDbgErp];
-      if (ord < D.njp) flags |= vjp_joint(d, D, a, w, ord, r0, r1 - r0, h1 * erp);
+      if (ord < D.njp) flags |= vjp_joint(d, D, a, w, ord, r0, r1 - r0, h1 * erp, stops);
       else flags |= vjp_contact(d, D, a, ord - D.njp, r0, r1 - r0, erp);
     }
     __syncwarp();

@@ -62,7 +62,8 @@ struct DevContact {
   float normal[3];
   int surface;
   int b1, b2, reverse;          // attach result: b2 = -1 for the environment
-  int geoms;                    // world-local pair (g1 | g2 << 8) of the collider call, -1 unknown
+  int geoms;                    // world-local pair (g1 | g2 << 8) of the collider call and, for a
+                                // heightfield contact, how it arose << 16; -1 unknown
 };
 
 // A heightfield (dGeomHeightfieldDataBuild* + placeable dCreateHeightfield)

@@ -23,6 +23,10 @@ constexpr int kHFZone = 10;                                  // samples per axis
 constexpr int kHFMaxTri = 2 * (kHFZone - 1) * (kHFZone - 1);
 constexpr int kHFMaxcPerCell = 10;                           // HEIGHTFIELDMAXCONTACTPERCELL
 constexpr float kHFEps = 1.1920928955078125e-07f;            // FLT_EPSILON
+// How a heightfield contact arose (two bits per contact in `kinds`): the
+// plane pass (a plane collider against a triangle's plane), the vertex pass
+// (a field sample inside the geom), or the geom entirely under the field.
+constexpr unsigned kHFPlane = 0u, kHFVertex = 1u, kHFUnder = 2u;
 
 // GetHeight(int, int) (heightfield.cpp:302-364)
 OG_D float hf_sample(const DevHeightfield& H, const float* heights, int x, int z) {
@@ -136,7 +140,9 @@ OG_D int geom_plane_collide(const GeomView& g, const GeomView& pl, unsigned flag
 // dCollideHeightfieldZone (heightfield.cpp:952-1676); g in heightfield space.
 // Returns the contact count, or -1 when the zone exceeds the lane buffers.
 OG_D int hf_zone(const DevHeightfield& H, const float* heights, int minX, int maxX, int minZ, int maxZ,
-                 const GeomView& g, const float* aabb, int max_contacts, unsigned flags, Contact* out) {
+                 const GeomView& g, const float* aabb, int max_contacts, unsigned flags, Contact* out,
+                 unsigned& kinds) {
+  kinds = 0u;
   const int numX = (maxX - minX) + 1, numZ = (maxZ - minZ) + 1;
   if (numX > kHFZone || numZ > kHFZone || numX < 1 || numZ < 1) return -1;
   const float minO2 = aabb[2], maxO2 = aabb[3];
@@ -155,6 +161,7 @@ OG_D int hf_zone(const DevHeightfield& H, const float* heights, int minX, int ma
     out[0].pos[0] = g.pos[0]; out[0].pos[1] = minY; out[0].pos[2] = g.pos[2];
     out[0].normal[0] = 0.f; out[0].normal[1] = -1.f; out[0].normal[2] = 0.f;
     out[0].depth = minY - maxO2;
+    kinds = kHFUnder;
     return 1;
   }
   bool further = false;
@@ -317,6 +324,7 @@ OG_D int hf_zone(const DevHeightfield& H, const float* heights, int minX, int ma
           o.pos[0] = v[0]; o.pos[1] = v[1]; o.pos[2] = v[2];
           o.normal[0] = -tp[k].x; o.normal[1] = -tp[k].y; o.normal[2] = -tp[k].z;
           o.depth = depth;
+          kinds |= kHFVertex << (2 * nc);
           if (++nc == max_contacts) return nc;
           vstate[vi] = 1;
         }
@@ -330,9 +338,9 @@ OG_D int hf_zone(const DevHeightfield& H, const float* heights, int minX, int ma
 // the contact count (normals as the reference: pointing into the field), or
 // -1 when the zone under the geom exceeds the lane buffers.
 __device__ __noinline__ int collide_heightfield(const DevHeightfield& H, const float* heights, const GeomView& g,
-                                               unsigned flags,
-                             Contact* out) {
+                                               unsigned flags, Contact* out, unsigned* kinds) {
   const int maxc = (int)(flags & 0xffff);
+  if (kinds) *kinds = 0u;
   if (maxc < 1) return 0;
   const float p0[3] = {g.pos[0] - H.pos[0], g.pos[1] - H.pos[1], g.pos[2] - H.pos[2]};
   GeomView g2 = g;
@@ -362,7 +370,9 @@ __device__ __noinline__ int collide_heightfield(const DevHeightfield& H, const f
     nMinZ = nMinZ > 0 ? nMinZ : 0;
     nMaxZ = nMaxZ < H.nz - 1 ? nMaxZ : H.nz - 1;
   }
-  const int n = hf_zone(H, heights, nMinX, nMaxX, nMinZ, nMaxZ, g2, aabb, maxc, flags, out);
+  unsigned kd = 0u;
+  const int n = hf_zone(H, heights, nMinX, nMaxX, nMinZ, nMaxZ, g2, aabb, maxc, flags, out, kd);
+  if (kinds) *kinds = kd;
   for (int i = 0; i < n; ++i) {
     const float q[3] = {out[i].pos[0] - H.half_w, out[i].pos[1], out[i].pos[2] - H.half_d};
     float w[3];

@@ -177,6 +177,7 @@ OG_D int phase_collide(const BatchDev& d, const WorldDesc& D, int w, const WarpS
     int cnt = 0;
     Contact cc[8];
     int bi = -1, bk = -1, surf = 0, pair = -1;
+    unsigned kinds = 0u;
     if (ci < ncand) {
       int i, k;
       unrank_pair(S.cand[ci], ng, i, k);
@@ -194,7 +195,7 @@ OG_D int phase_collide(const BatchDev& d, const WorldDesc& D, int w, const WarpS
         const GeomView& hv = rev ? vk : vi;
         const GeomView& ov = rev ? vi : vk;
         if (ov.type == G_SPHERE || ov.type == G_BOX || ov.type == G_CAPSULE) {
-          cnt = collide_heightfield(d.hfs[(int)hv.p[0]], d.hf_heights, ov, (unsigned)D.max_contacts, cc);
+          cnt = collide_heightfield(d.hfs[(int)hv.p[0]], d.hf_heights, ov, (unsigned)D.max_contacts, cc, &kinds);
           if (cnt < 0) { atomicOr(&d.status[w], ST_HF_ZONE); cnt = 0; }
           if (rev)
             for (int c = 0; c < cnt; ++c) {
@@ -222,7 +223,7 @@ OG_D int phase_collide(const BatchDev& d, const WorldDesc& D, int w, const WarpS
         // dJointAttach(body(gi), body(gk)): a missing first body swaps in the second
         if (bi < 0) { ct.b1 = bk; ct.b2 = -1; ct.reverse = 1; }
         else { ct.b1 = bi; ct.b2 = bk; ct.reverse = 0; }
-        ct.geoms = pair;
+        ct.geoms = pair | (int)(((kinds >> (2 * c)) & 3u) << 16);
         d.contacts[D.contact_off + slot] = ct;
       }
     }

@@ -43,13 +43,15 @@ def _fd(sc, w, n, loss, poke, x0, eps=EPS):
     return (lp - lm) / (2 * eps)
 
 
-def _gpu_grads(sc, n, coef, ckpt=10):
+def _gpu_grads(sc, n, coef, ckpt=10, x_init=None):
     """GPU rollout of n steps with loss sum(coef * final) (coef [nb, 13]);
     returns (grad init state [nb,13], grad joint torques [S,nj,2] or None, batch,
     final state, initial state)."""
     from odegpu.batch import Batch
     from odegpu.adjoint import rollout
     B = Batch(sc)
+    if x_init is not None:
+        B.set_state(x_init)
     x0_np = B.state()
     x0 = torch.tensor(x0_np, dtype=torch.float32, device="cuda", requires_grad=True)
     jt = None
@@ -67,9 +69,10 @@ def _rel(a, b):
     return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-12)
 
 
-def _check_case(sc, n, coef, n_vel=12, n_pos=6, n_tq=12, seed=0, q_dirs=2, eps=EPS):
+def _check_case(sc, n, coef, n_vel=12, n_pos=6, n_tq=12, seed=0, q_dirs=2, eps=EPS, x_init=None, tq_col=0,
+                tq_joints=None):
     rng = np.random.default_rng(seed)
-    g_state, g_jt, B, _, g0 = _gpu_grads(sc, n, coef)
+    g_state, g_jt, B, _, g0 = _gpu_grads(sc, n, coef, x_init=x_init)
     status = B.adjoint_status()
     assert (status == 0).all(), status
     fd, gpu, names = [], [], []
@@ -108,12 +111,13 @@ def _check_case(sc, n, coef, n_vel=12, n_pos=6, n_tq=12, seed=0, q_dirs=2, eps=E
             j0, j1 = sc.world_joints(w)
             for _ in range(n_tq):
                 s = int(rng.integers(0, min(n, sc.n_ctrl_steps)))
-                j = int(rng.integers(j0, j1))
-                v0 = sc.joint_torque[s, j, 0]
+                j = j0 + int(rng.choice(tq_joints)) if tq_joints is not None else int(rng.integers(j0, j1))
+                v0 = sc.joint_torque[s, j, tq_col]
 
                 def poke(e, s=s, j=j, v0=v0):
-                    sc.joint_torque[s, j, 0] = v0 + e
-                fd.append(_fd(sc, w, n, loss, poke, x0, eps)); gpu.append(g_jt[s, j, 0]); names.append(f"t{s},{j}")
+                    sc.joint_torque[s, j, tq_col] = v0 + e
+                fd.append(_fd(sc, w, n, loss, poke, x0, eps)); gpu.append(g_jt[s, j, tq_col])
+                names.append(f"t{s},{j}")
     B.close()
     err = _rel(gpu, fd)
     worst = np.argsort(-np.abs(np.array(gpu) - np.array(fd)))[:5]
@@ -185,3 +189,26 @@ def test_adjoint_checkpoint_interval_invariant():
     assert np.array_equal(f1, f2) and np.array_equal(f1, f3)
     assert np.array_equal(g1, g2) and np.array_equal(g1, g3)
     assert np.array_equal(j1, j2) and np.array_equal(j1, j3)
+
+
+def test_adjoint_vehicles_on_heightfield():
+    """Vehicle batch from a settled state (oracle step 40): four steps with
+    hinge2 suspension, steering held by per-step stops (limit rows whose rhs
+    follows the hinge2 angle) and heightfield contacts of wheels and chassis
+    (plane-pass and vertex-pass). d/d(initial velocities) and d/d(rear-wheel
+    drive torques) of a linear loss on the chassis state; the contact sets do
+    not change over the four steps, so central differences (step 1e-6) are
+    smooth."""
+    from gpu_helpers import oracle_states, stacked_state
+    sc = S.vehicles(n_worlds=4, steps=60, hf_samples=64)
+    runs = oracle_states(sc, 41)
+    x_init = stacked_state(runs, 40)
+    coef = np.zeros((sc.body_off[-1], 13))
+    rng = np.random.default_rng(8)
+    for w in range(sc.n_worlds):
+        b0 = sc.body_off[w]
+        coef[b0, 0:3] = rng.standard_normal(3)
+        coef[b0, 7:10] = rng.standard_normal(3)
+    err, detail = _check_case(sc, 4, coef, n_vel=10, n_pos=0, n_tq=6, seed=9, q_dirs=0, eps=1e-6,
+                              x_init=x_init, tq_col=1, tq_joints=[2, 3])
+    assert err < TOL, (err, detail)
