@@ -201,6 +201,18 @@ dGeomID dCreateSphere(dSpaceID space, dReal radius);                     /* :924
 dGeomID dCreateBox(dSpaceID space, dReal lx, dReal ly, dReal lz);        /* :1002 */
 dGeomID dCreatePlane(dSpaceID space, dReal a, dReal b, dReal c, dReal d); /* :1046 */
 dGeomID dCreateCapsule(dSpaceID space, dReal radius, dReal length);      /* :1051 */
+/* Heightfields: the samples are copied when the data is built (ODE can keep
+ * a reference to the caller's array when bCopyHeightData is 0). */
+typedef struct dxHeightfieldData* dHeightfieldDataID;                   /* collision.h:1101 */
+dGeomID dCreateHeightfield(dSpaceID space, dHeightfieldDataID data, int bPlaceable);  /* :1144 */
+dHeightfieldDataID dGeomHeightfieldDataCreate(void);                    /* :1160 */
+void dGeomHeightfieldDataDestroy(dHeightfieldDataID d);                 /* :1171 */
+void dGeomHeightfieldDataBuildSingle(dHeightfieldDataID d, const float* pHeightData, int bCopyHeightData,
+                                     dReal width, dReal depth, int widthSamples, int depthSamples,
+                                     dReal scale, dReal offset, dReal thickness, int bWrap);  /* :1361 */
+void dGeomHeightfieldDataBuildDouble(dHeightfieldDataID d, const double* pHeightData, int bCopyHeightData,
+                                     dReal width, dReal depth, int widthSamples, int depthSamples,
+                                     dReal scale, dReal offset, dReal thickness, int bWrap);  /* :1411 */
 void dGeomDestroy(dGeomID g);                                            /* :68  */
 void dGeomSetBody(dGeomID g, dBodyID body);                              /* :108 */
 dBodyID dGeomGetBody(dGeomID g);                                         /* :117 */

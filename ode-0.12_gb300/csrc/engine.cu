@@ -13,6 +13,7 @@
 #include "engine_types.cuh"
 #include "world_solve.cuh"
 #include "adjoint.cuh"
+#include "engine_internal.hpp"
 #include "host_setup.hpp"
 
 using namespace og;
@@ -453,21 +454,8 @@ int odegpuBatchCreate(const odegpuScene* sc, const odegpuBatchConfig* cfg, odegp
       delete B;
       return fail(ODEGPU_E_ARG, "heightfield " + std::to_string(i) + ": bad sample counts or extent");
     }
-    DevHeightfield& D = hfs[i];
-    D.nx = H.nx; D.nz = H.nz; D.wrap = H.wrap; D.h_off = (int)hf_heights.size();
-    D.width = (float)H.width; D.depth = (float)H.depth;
-    D.scale = (float)H.scale; D.offset = (float)H.offset; D.thickness = (float)H.thickness;
-    const double sw = H.width / (H.nx - 1.0), sd = H.depth / (H.nz - 1.0);
-    D.sw = (float)sw; D.sd = (float)sd;
-    D.inv_sw = (float)(1.0 / sw); D.inv_sd = (float)(1.0 / sd);
-    D.zx = (float)(sd / sw);
-    D.half_w = (float)(H.width / 2.0); D.half_d = (float)(H.depth / 2.0);
-    for (int k = 0; k < 3; ++k) D.pos[k] = (float)H.pos[k];
-    D.pad = 0.f;
-    for (int r = 0; r < 3; ++r) {
-      for (int c = 0; c < 3; ++c) D.R[r * 4 + c] = (float)H.R[r * 3 + c];
-      D.R[r * 4 + 3] = 0.f;
-    }
+    hfs[i] = og::make_dev_heightfield(H.nx, H.nz, H.width, H.depth, H.scale, H.offset, H.thickness, H.wrap,
+                                      H.pos, H.R, (int)hf_heights.size());
     for (long long k = 0; k < (long long)H.nx * H.nz; ++k) hf_heights.push_back((float)H.heights[k]);
   }
   for (int g = 0; g < NG; ++g)
@@ -1307,6 +1295,69 @@ int ctx_step(WorldCtx* c, HostWorld& hw) {
   OG_CUDA(cudaStreamSynchronize(s));
   hw.status = st[0];
   return 0;
+}
+
+DevHeightfield make_dev_heightfield(int nx, int nz, double width, double depth, double scale, double offset,
+                                   double thickness, int wrap, const double* pos, const double* R9, int h_off) {
+  DevHeightfield D;
+  D.nx = nx; D.nz = nz; D.wrap = wrap; D.h_off = h_off;
+  D.width = (float)width; D.depth = (float)depth;
+  D.scale = (float)scale; D.offset = (float)offset; D.thickness = (float)thickness;
+  const double sw = width / (nx - 1.0), sd = depth / (nz - 1.0);
+  D.sw = (float)sw; D.sd = (float)sd;
+  D.inv_sw = (float)(1.0 / sw); D.inv_sd = (float)(1.0 / sd);
+  D.zx = (float)(sd / sw);
+  D.half_w = (float)(width / 2.0); D.half_d = (float)(depth / 2.0);
+  for (int k = 0; k < 3; ++k) D.pos[k] = (float)pos[k];
+  D.pad = 0.f;
+  for (int r = 0; r < 3; ++r) {
+    for (int c = 0; c < 3; ++c) D.R[r * 4 + c] = (float)R9[r * 3 + c];
+    D.R[r * 4 + 3] = 0.f;
+  }
+  return D;
+}
+
+__global__ void collide_hf_kernel(DevHeightfield H, const float* heights, GeomView g, unsigned flags, Contact* out,
+                                  int* n) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    Contact c[8];
+    int k = collide_heightfield(H, heights, g, flags, c, nullptr);
+    if (k < 0) k = -1;
+    for (int i = 0; i < k; ++i) out[i] = c[i];
+    *n = k;
+  }
+}
+
+int upload_heights(const std::vector<float>& h, float** dev) {
+  if (*dev) { cudaFree(*dev); *dev = nullptr; }
+  if (h.empty()) return 0;
+  if (cudaMalloc(dev, h.size() * sizeof(float)) != cudaSuccess) {
+    cudaGetLastError();
+    *dev = nullptr;
+    return fail(ODEGPU_E_NOMEM, "heightfield upload");
+  }
+  if (cudaMemcpy(*dev, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess)
+    return fail(ODEGPU_E_CUDA, "heightfield upload");
+  return 0;
+}
+
+void free_heights(float* dev) {
+  if (dev) cudaFree(dev);
+}
+
+int collide_hf_gpu(const DevHeightfield& H, const float* d_heights, const GeomView& g, unsigned flags, Contact* out) {
+  Contact* d_c = nullptr;
+  OG_CUDA(cudaMalloc(&d_c, 8 * sizeof(Contact) + sizeof(int)));
+  int* d_n = reinterpret_cast<int*>(d_c + 8);
+  collide_hf_kernel<<<1, 32>>>(H, d_heights, g, flags, d_c, d_n);
+  int n = 0;
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpy(&n, d_n, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && n > 0) e = cudaMemcpy(out, d_c, n * sizeof(Contact), cudaMemcpyDeviceToHost);
+  cudaFree(d_c);
+  if (e != cudaSuccess) return fail(ODEGPU_E_CUDA, cudaGetErrorString(e));
+  if (n < 0) return fail(ODEGPU_E_LIMIT, "the geom covers more than 10 x 10 heightfield samples");
+  return n;
 }
 
 int collide_pair_gpu(const GeomView& a, const GeomView& b, unsigned flags, Contact* out) {

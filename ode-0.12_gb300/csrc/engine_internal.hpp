@@ -33,5 +33,12 @@ void ctx_destroy(WorldCtx* c);
 int ctx_step(WorldCtx* c, HostWorld& hw);
 // One dCollide on the GPU. Returns the contact count (<= 8) or a negative code.
 int collide_pair_gpu(const GeomView& a, const GeomView& b, unsigned flags, Contact* out);
+// Heightfields for the ODE API: the dxHeightfieldData caches, the device copy
+// of the samples, and dCollide(heightfield, g) with the field first.
+DevHeightfield make_dev_heightfield(int nx, int nz, double width, double depth, double scale, double offset,
+                                   double thickness, int wrap, const double* pos, const double* R9, int h_off);
+int upload_heights(const std::vector<float>& h, float** dev);
+void free_heights(float* dev);
+int collide_hf_gpu(const DevHeightfield& H, const float* d_heights, const GeomView& g, unsigned flags, Contact* out);
 
 }  // namespace og

@@ -55,11 +55,21 @@ struct dxJointGroup {
   std::vector<dxJoint*> joints;
 };
 
+struct dxHeightfieldData {
+  int nx = 0, nz = 0, wrap = 0;
+  double width = 0, depth = 0, scale = 1, offset = 0, thickness = 0;
+  std::vector<float> heights;      // copied at build time (x fastest, then z)
+  float* d_heights = nullptr;      // device copy
+  bool built = false;
+};
+
 struct dxGeom {
   int type;
   dxBody* body;
   double p[4];               // class parameters (plane normalised)
   dReal pos[4], R[12];       // own placement when not attached to a body
+  dxHeightfieldData* hf;     // heightfield geoms: their data
+  int placeable;             // heightfield geoms: created placeable
 };
 
 struct dxWorld {
@@ -576,6 +586,46 @@ dGeomID dCreatePlane(dSpaceID, dReal a, dReal b, dReal c, dReal d) {
   return new_geom(dPlaneClass, p);
 }
 void dGeomDestroy(dGeomID g) { delete g; }
+
+// Heightfields (ode/src/heightfield.cpp:107-143, :1860-2000): the samples are
+// copied at build time whatever bCopyHeightData says, and uploaded to the GPU.
+dHeightfieldDataID dGeomHeightfieldDataCreate(void) { return new dxHeightfieldData(); }
+void dGeomHeightfieldDataDestroy(dHeightfieldDataID d) {
+  if (!d) return;
+  og::free_heights(d->d_heights);
+  delete d;
+}
+static bool hf_shape(dHeightfieldDataID d, dReal width, dReal depth, int widthSamples, int depthSamples,
+                     dReal scale, dReal offset, dReal thickness, int bWrap) {
+  if (!d || widthSamples < 2 || depthSamples < 2 || !(width > 0) || !(depth > 0)) return false;
+  d->nx = widthSamples; d->nz = depthSamples; d->wrap = bWrap;
+  d->width = width; d->depth = depth; d->scale = scale; d->offset = offset; d->thickness = thickness;
+  d->heights.assign((size_t)widthSamples * depthSamples, 0.f);
+  return true;
+}
+void dGeomHeightfieldDataBuildSingle(dHeightfieldDataID d, const float* pHeightData, int, dReal width,
+                                     dReal depth, int widthSamples, int depthSamples, dReal scale, dReal offset,
+                                     dReal thickness, int bWrap) {
+  if (!pHeightData || !hf_shape(d, width, depth, widthSamples, depthSamples, scale, offset, thickness, bWrap))
+    return;
+  for (size_t k = 0; k < d->heights.size(); ++k) d->heights[k] = pHeightData[k];
+  d->built = og::upload_heights(d->heights, &d->d_heights) == 0;
+}
+void dGeomHeightfieldDataBuildDouble(dHeightfieldDataID d, const double* pHeightData, int, dReal width,
+                                     dReal depth, int widthSamples, int depthSamples, dReal scale, dReal offset,
+                                     dReal thickness, int bWrap) {
+  if (!pHeightData || !hf_shape(d, width, depth, widthSamples, depthSamples, scale, offset, thickness, bWrap))
+    return;
+  for (size_t k = 0; k < d->heights.size(); ++k) d->heights[k] = (float)pHeightData[k];
+  d->built = og::upload_heights(d->heights, &d->d_heights) == 0;
+}
+dGeomID dCreateHeightfield(dSpaceID, dHeightfieldDataID data, int bPlaceable) {
+  const double p[4] = {0, 0, 0, 0};
+  dGeomID g = new_geom(dHeightfieldClass, p);
+  g->hf = data;
+  g->placeable = bPlaceable;
+  return g;
+}
 void dGeomSetBody(dGeomID g, dBodyID b) { g->body = b; }
 dBodyID dGeomGetBody(dGeomID g) { return g->body; }
 void dGeomSetPosition(dGeomID g, dReal x, dReal y, dReal z) {
@@ -599,6 +649,50 @@ int dCollide(dGeomID o1, dGeomID o2, int flags, dContactGeom* contact, int skip)
   if (!o1 || !o2 || !contact || (flags & 0xffff) == 0) return 0;
   if (o1 == o2) return 0;
   if (o1->body == o2->body && o1->body) return 0;
+  if (o1->type == dHeightfieldClass || o2->type == dHeightfieldClass) {
+    // dCollideHeightfield runs with the field first; the reversed call
+    // negates the normals (ode/src/collision_kernel.cpp:319-335)
+    const bool rev = o2->type == dHeightfieldClass;
+    const dxGeom* hg = rev ? o2 : o1;
+    const dxGeom* og2 = rev ? o1 : o2;
+    if (og2->type != dSphereClass && og2->type != dBoxClass && og2->type != dCapsuleClass) return 0;
+    if (!hg->hf || !hg->hf->built) return 0;
+    double hpos[3] = {0, 0, 0}, hR[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+    if (hg->placeable) {
+      const dReal* P = dGeomGetPosition((dGeomID)hg);
+      const dReal* R = dGeomGetRotation((dGeomID)hg);
+      for (int k = 0; k < 3; ++k) hpos[k] = P[k];
+      for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) hR[r * 3 + c] = R[r * 4 + c];
+    }
+    const dxHeightfieldData* D = hg->hf;
+    const og::DevHeightfield H = og::make_dev_heightfield(D->nx, D->nz, D->width, D->depth, D->scale, D->offset,
+                                                          D->thickness, D->wrap, hpos, hR, 0);
+    og::GeomView gv;
+    gv.type = og2->type;
+    for (int k = 0; k < 4; ++k) gv.p[k] = (float)og2->p[k];
+    const dReal* pos = dGeomGetPosition((dGeomID)og2);
+    const dReal* R = dGeomGetRotation((dGeomID)og2);
+    for (int k = 0; k < 3; ++k) gv.pos[k] = pos[k];
+    for (int k = 0; k < 12; ++k) gv.R[k] = R[k];
+    int maxc = flags & 0xffff;
+    unsigned f = (unsigned)flags;
+    if (maxc > 8) f = (f & ~0xffffu) | 8u;
+    og::Contact out[8];
+    const int n = og::collide_hf_gpu(H, D->d_heights, gv, f, out);
+    if (n <= 0) return 0;
+    const float sgn = rev ? -1.f : 1.f;
+    for (int i = 0; i < n; ++i) {
+      dContactGeom* c = (dContactGeom*)((char*)contact + (size_t)i * skip);
+      for (int k = 0; k < 3; ++k) { c->pos[k] = out[i].pos[k]; c->normal[k] = sgn * out[i].normal[k]; }
+      c->pos[3] = c->normal[3] = 0;
+      c->depth = out[i].depth;
+      c->g1 = o1;
+      c->g2 = o2;
+      c->side1 = c->side2 = -1;
+    }
+    return n;
+  }
   og::GeomView v[2];
   const dxGeom* g[2] = {o1, o2};
   for (int i = 0; i < 2; ++i) {

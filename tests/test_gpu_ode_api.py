@@ -164,3 +164,53 @@ def test_joint_feedback_through_ode_api():
         else:
             assert np.array(fbs[k].f2[:3]).tolist() == [0.0, 0.0, 0.0]
     L.dWorldDestroy(w)
+
+
+def test_dcollide_heightfield_through_ode_api():
+    """dGeomHeightfieldDataBuildDouble + dCreateHeightfield (placeable) +
+    dCollide on the reference's golden heightfield calls, in both argument
+    orders (the reversed call negates the normals): counts exact, records
+    within 1e-4."""
+    g = np.load(os.path.join(GOLDEN, "hf_kats.npz"))
+    L = _api()
+    f, v, i = C.c_float, C.c_void_p, C.c_int
+    L.dGeomHeightfieldDataCreate.restype = v
+    L.dGeomHeightfieldDataBuildDouble.argtypes = [v, C.POINTER(C.c_double), i, f, f, i, i, f, f, f, i]
+    L.dCreateHeightfield.restype = v
+    L.dCreateHeightfield.argtypes = [v, v, i]
+    L.dGeomHeightfieldDataDestroy.argtypes = [v]
+    h = np.ascontiguousarray(g["heights"], dtype=np.float64)
+    sp = float(g["spacing"])
+    nz, nx = h.shape
+    hd = L.dGeomHeightfieldDataCreate()
+    L.dGeomHeightfieldDataBuildDouble(hd, h.ctypes.data_as(C.POINTER(C.c_double)), 1, sp * (nx - 1),
+                                      sp * (nz - 1), nx, nz, 1.0, 0.0, 1.0, 0)
+    hg = L.dCreateHeightfield(None, hd, 1)
+    L.dGeomSetPosition(hg, *[float(x) for x in g["hf_pos"]])
+    Rh = g["hf_R"]
+    L.dGeomSetRotation(hg, (C.c_float * 12)(*[Rh[0], Rh[1], Rh[2], 0, Rh[3], Rh[4], Rh[5], 0, Rh[6], Rh[7],
+                                               Rh[8], 0]))
+    mk = {0: lambda p: L.dCreateSphere(None, p[0]), 1: lambda p: L.dCreateBox(None, p[0], p[1], p[2]),
+          2: lambda p: L.dCreateCapsule(None, p[0], p[1])}
+    n = len(g["t2"])
+    count_mism, worst = [], 0.0
+    for k in range(n):
+        t, p, pos, R = int(g["t2"][k]), g["p2"][k], g["pos2"][k], g["R2"][k]
+        gh = mk[t](p)
+        L.dGeomSetPosition(gh, *pos)
+        L.dGeomSetRotation(gh, (C.c_float * 12)(*[R[0], R[1], R[2], 0, R[3], R[4], R[5], 0, R[6], R[7], R[8], 0]))
+        ref_n, ref = int(g["nc"][k]), g["out"][k]
+        for order, sgn in (((hg, gh), 1.0), ((gh, hg), -1.0)):
+            out = (ContactGeom * 16)()
+            nc = L.dCollide(order[0], order[1], int(g["flags"][k]), out, C.sizeof(ContactGeom))
+            if nc != ref_n:
+                count_mism.append((k, nc, ref_n))
+                continue
+            for c in range(nc):
+                got = np.array(list(out[c].pos[:3]) + [sgn * x for x in out[c].normal[:3]] + [out[c].depth])
+                worst = max(worst, np.abs(got - ref[c, :7]).max())
+        L.dGeomDestroy(gh)
+    L.dGeomDestroy(hg)
+    L.dGeomHeightfieldDataDestroy(hd)
+    assert not count_mism, count_mism[:10]
+    assert worst < 1e-4, worst
