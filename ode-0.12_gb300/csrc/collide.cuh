@@ -496,10 +496,226 @@ OG_HD int collide_capsule_plane(const GeomView& cp, const GeomView& pl, unsigned
   return nc;
 }
 
+// dCollideCapsuleSphere (ode/src/capsule.cpp:130-160)
+OG_HD int collide_capsule_sphere(const GeomView& cp, const GeomView& sp, Contact* c) {
+  const float* R = cp.R;
+  float alpha = R[2] * (sp.pos[0] - cp.pos[0]) + R[6] * (sp.pos[1] - cp.pos[1]) + R[10] * (sp.pos[2] - cp.pos[2]);
+  const float lz2 = cp.p[1] * 0.5f;
+  if (alpha > lz2) alpha = lz2;
+  if (alpha < -lz2) alpha = -lz2;
+  const float p[3] = {cp.pos[0] + alpha * R[2], cp.pos[1] + alpha * R[6], cp.pos[2] + alpha * R[10]};
+  return collide_spheres(p, cp.p[0], sp.pos, sp.p[0], c);
+}
+
+// dCollideSpheresZeroDist (ode/src/capsule.cpp:164-176)
+OG_HD int collide_spheres_zero_dist(const float* p1, float r1, float r2, const float* normal, Contact* c) {
+  c->normal[0] = normal[0]; c->normal[1] = normal[1]; c->normal[2] = normal[2];
+  c->depth = r1 + r2;
+  const float k = 0.5f * (r2 - r1);
+  c->pos[0] = p1[0] + c->normal[0] * k;
+  c->pos[1] = p1[1] + c->normal[1] * k;
+  c->pos[2] = p1[2] + c->normal[2] * k;
+  return 1;
+}
+
+// dClosestLineBoxPoints (ode/src/collision_util.cpp:247-372), dSINGLE epsilon:
+// t walks along the segment p1 -> p2 through the box's clip planes until
+// d|D(t)|^2/dt turns non-negative.
+OG_HD void closest_line_box_points(const float* p1, const float* p2, const float* c, const float* R,
+                                   const float* side, float* lret, float* bret) {
+  float tmp[3], s[3], v[3], sign[3], v2[3], h[3], tanchor[3];
+  int region[3];
+  tmp[0] = p1[0] - c[0]; tmp[1] = p1[1] - c[1]; tmp[2] = p1[2] - c[2];
+  mul1_331(s, R, tmp);
+  tmp[0] = p2[0] - p1[0]; tmp[1] = p2[1] - p1[1]; tmp[2] = p2[2] - p1[2];
+  mul1_331(v, R, tmp);
+  for (int i = 0; i < 3; i++) {
+    if (v[i] < 0.f) { s[i] = -s[i]; v[i] = -v[i]; sign[i] = -1.f; }
+    else sign[i] = 1.f;
+  }
+  for (int i = 0; i < 3; i++) v2[i] = v[i] * v[i];
+  for (int i = 0; i < 3; i++) h[i] = 0.5f * side[i];
+  const float tanchor_eps = 1e-19f;
+  for (int i = 0; i < 3; i++) {
+    if (v[i] > tanchor_eps) {
+      if (s[i] < -h[i]) { region[i] = -1; tanchor[i] = (-h[i] - s[i]) / v[i]; }
+      else { region[i] = (s[i] > h[i]); tanchor[i] = (h[i] - s[i]) / v[i]; }
+    } else {
+      region[i] = 0;
+      tanchor[i] = 2.f;
+    }
+  }
+  float t = 0.f, dd2dt = 0.f;
+  for (int i = 0; i < 3; i++) dd2dt -= (region[i] ? v2[i] : 0.f) * tanchor[i];
+  if (dd2dt < 0.f) {
+    bool done = false;
+    do {
+      float next_t = 1.f;
+      for (int i = 0; i < 3; i++)
+        if (tanchor[i] > t && tanchor[i] < 1.f && tanchor[i] < next_t) next_t = tanchor[i];
+      float next_dd2dt = 0.f;
+      for (int i = 0; i < 3; i++) next_dd2dt += (region[i] ? v2[i] : 0.f) * (next_t - tanchor[i]);
+      if (next_dd2dt >= 0.f) {
+        const float m = (next_dd2dt - dd2dt) / (next_t - t);
+        t -= dd2dt / m;
+        done = true;
+        break;
+      }
+      for (int i = 0; i < 3; i++) {
+        if (tanchor[i] == next_t) {
+          tanchor[i] = (h[i] - s[i]) / v[i];
+          region[i]++;
+        }
+      }
+      t = next_t;
+      dd2dt = next_dd2dt;
+    } while (t < 1.f);
+    if (!done) t = 1.f;
+  }
+  for (int i = 0; i < 3; i++) lret[i] = p1[i] + t * tmp[i];
+  for (int i = 0; i < 3; i++) {
+    tmp[i] = sign[i] * (s[i] + t * v[i]);
+    if (tmp[i] < -h[i]) tmp[i] = -h[i];
+    else if (tmp[i] > h[i]) tmp[i] = h[i];
+  }
+  mul0_331(s, R, tmp);
+  for (int i = 0; i < 3; i++) bret[i] = s[i] + c[i];
+}
+
+// dClosestLineSegmentPoints (ode/src/collision_util.cpp:109-209): vertex-vertex,
+// then edge-vertex, then edge-edge features.
+OG_HD void closest_segment_points(const float* a1, const float* a2, const float* b1, const float* b2, float* cp1,
+                                  float* cp2) {
+  float a1a2[3], b1b2[3], a1b1[3], a1b2[3], a2b1[3], a2b2[3], n[3];
+  for (int i = 0; i < 3; ++i) { a1a2[i] = a2[i] - a1[i]; b1b2[i] = b2[i] - b1[i]; a1b1[i] = b1[i] - a1[i]; }
+  const float da1 = dot3(a1a2, a1b1), db1 = dot3(b1b2, a1b1);
+  if (da1 <= 0.f && db1 >= 0.f) { for (int i = 0; i < 3; ++i) { cp1[i] = a1[i]; cp2[i] = b1[i]; } return; }
+  for (int i = 0; i < 3; ++i) a1b2[i] = b2[i] - a1[i];
+  const float da2 = dot3(a1a2, a1b2), db2 = dot3(b1b2, a1b2);
+  if (da2 <= 0.f && db2 <= 0.f) { for (int i = 0; i < 3; ++i) { cp1[i] = a1[i]; cp2[i] = b2[i]; } return; }
+  for (int i = 0; i < 3; ++i) a2b1[i] = b1[i] - a2[i];
+  const float da3 = dot3(a1a2, a2b1), db3 = dot3(b1b2, a2b1);
+  if (da3 >= 0.f && db3 >= 0.f) { for (int i = 0; i < 3; ++i) { cp1[i] = a2[i]; cp2[i] = b1[i]; } return; }
+  for (int i = 0; i < 3; ++i) a2b2[i] = b2[i] - a2[i];
+  const float da4 = dot3(a1a2, a2b2), db4 = dot3(b1b2, a2b2);
+  if (da4 >= 0.f && db4 <= 0.f) { for (int i = 0; i < 3; ++i) { cp1[i] = a2[i]; cp2[i] = b2[i]; } return; }
+  const float la = dot3(a1a2, a1a2);
+  if (da1 >= 0.f && da3 <= 0.f) {
+    const float k = da1 / la;
+    for (int i = 0; i < 3; ++i) n[i] = a1b1[i] - k * a1a2[i];
+    if (dot3(b1b2, n) >= 0.f) {
+      for (int i = 0; i < 3; ++i) { cp1[i] = a1[i] + k * a1a2[i]; cp2[i] = b1[i]; }
+      return;
+    }
+  }
+  if (da2 >= 0.f && da4 <= 0.f) {
+    const float k = da2 / la;
+    for (int i = 0; i < 3; ++i) n[i] = a1b2[i] - k * a1a2[i];
+    if (dot3(b1b2, n) <= 0.f) {
+      for (int i = 0; i < 3; ++i) { cp1[i] = a1[i] + k * a1a2[i]; cp2[i] = b2[i]; }
+      return;
+    }
+  }
+  const float lb = dot3(b1b2, b1b2);
+  if (db1 <= 0.f && db2 >= 0.f) {
+    const float k = -db1 / lb;
+    for (int i = 0; i < 3; ++i) n[i] = -a1b1[i] - k * b1b2[i];
+    if (dot3(a1a2, n) >= 0.f) {
+      for (int i = 0; i < 3; ++i) { cp1[i] = a1[i]; cp2[i] = b1[i] + k * b1b2[i]; }
+      return;
+    }
+  }
+  if (db3 <= 0.f && db4 >= 0.f) {
+    const float k = -db3 / lb;
+    for (int i = 0; i < 3; ++i) n[i] = -a2b1[i] - k * b1b2[i];
+    if (dot3(a1a2, n) <= 0.f) {
+      for (int i = 0; i < 3; ++i) { cp1[i] = a2[i]; cp2[i] = b1[i] + k * b1b2[i]; }
+      return;
+    }
+  }
+  const float k = dot3(a1a2, b1b2);
+  float det = la * lb - k * k;
+  if (det <= 0.f) { for (int i = 0; i < 3; ++i) { cp1[i] = a1[i]; cp2[i] = b1[i]; } return; }
+  det = 1.0f / det;
+  const float alpha = (lb * da1 - k * db1) * det;
+  const float beta = (k * da1 - la * db1) * det;
+  for (int i = 0; i < 3; ++i) { cp1[i] = a1[i] + alpha * a1a2[i]; cp2[i] = b1[i] + beta * b1b2[i]; }
+}
+
+// dCollideCapsuleBox (ode/src/capsule.cpp:178-229), dSINGLE minimum distance
+OG_HD int collide_capsule_box(const GeomView& cp, const GeomView& bx, Contact* c) {
+  const float clen = cp.p[1] * 0.5f;
+  float p1[3], p2[3], pl[3], pb[3];
+  for (int i = 0; i < 3; ++i) {
+    p1[i] = cp.pos[i] + clen * cp.R[4 * i + 2];
+    p2[i] = cp.pos[i] - clen * cp.R[4 * i + 2];
+  }
+  closest_line_box_points(p1, p2, bx.pos, bx.R, bx.p, pl, pb);
+  const float dx = pl[0] - pb[0], dy = pl[1] - pb[1], dz = pl[2] - pb[2];
+  if (sqrtf(dx * dx + dy * dy + dz * dz) < 1e-9f) {
+    float normal[3] = {pb[0] - bx.pos[0], pb[1] - bx.pos[1], pb[2] - bx.pos[2]};
+    safe_normalize3(normal);
+    return collide_spheres_zero_dist(pl, cp.p[0], 0.f, normal, c);
+  }
+  return collide_spheres(pl, cp.p[0], pb, 0.f, c);
+}
+
+// dCollideCapsuleCapsule (ode/src/capsule.cpp:232-350): near-parallel axes
+// give up to two contacts along the overlap, otherwise the closest points of
+// the two segments.
+OG_HD int collide_capsule_capsule(const GeomView& g1, const GeomView& g2, unsigned flags, Contact* c) {
+  const float tolerance = 1e-5f;
+  const float lz1 = g1.p[1] * 0.5f, lz2 = g2.p[1] * 0.5f;
+  const float* pos1 = g1.pos;
+  const float* pos2 = g2.pos;
+  const float axis1[3] = {g1.R[2], g1.R[6], g1.R[10]};
+  float axis2[3] = {g2.R[2], g2.R[6], g2.R[10]};
+  float sphere1[3], sphere2[3];
+  const float a1a2 = dot3(axis1, axis2);
+  const float det = 1.0f - a1a2 * a1a2;
+  if (det < tolerance) {
+    if (a1a2 < 0.f) { axis2[0] = -axis2[0]; axis2[1] = -axis2[1]; axis2[2] = -axis2[2]; }
+    float q[3];
+    for (int i = 0; i < 3; i++) q[i] = pos1[i] - pos2[i];
+    const float k = dot3(axis1, q);
+    const float a1lo = -lz1, a1hi = lz1, a2lo = -lz2 - k, a2hi = lz2 - k;
+    const float lo = (a1lo > a2lo) ? a1lo : a2lo;
+    const float hi = (a1hi < a2hi) ? a1hi : a2hi;
+    if (lo <= hi) {
+      const int num_contacts = (int)(flags & 0xffff);
+      if (num_contacts >= 2 && lo < hi) {
+        for (int i = 0; i < 3; i++) sphere1[i] = pos1[i] + lo * axis1[i];
+        for (int i = 0; i < 3; i++) sphere2[i] = pos2[i] + (lo + k) * axis2[i];
+        const int n1 = collide_spheres(sphere1, g1.p[0], sphere2, g2.p[0], c);
+        if (n1) {
+          for (int i = 0; i < 3; i++) sphere1[i] = pos1[i] + hi * axis1[i];
+          for (int i = 0; i < 3; i++) sphere2[i] = pos2[i] + (hi + k) * axis2[i];
+          const int n2 = collide_spheres(sphere1, g1.p[0], sphere2, g2.p[0], c + 1);
+          if (n2) return 2;
+        }
+      }
+      const float alpha1 = (lo + hi) * 0.5f;
+      const float alpha2 = alpha1 + k;
+      for (int i = 0; i < 3; i++) sphere1[i] = pos1[i] + alpha1 * axis1[i];
+      for (int i = 0; i < 3; i++) sphere2[i] = pos2[i] + alpha2 * axis2[i];
+      return collide_spheres(sphere1, g1.p[0], sphere2, g2.p[0], c);
+    }
+  }
+  float a1[3], a2[3], b1[3], b2[3];
+  for (int i = 0; i < 3; ++i) {
+    a1[i] = pos1[i] + axis1[i] * lz1;
+    a2[i] = pos1[i] - axis1[i] * lz1;
+    b1[i] = pos2[i] + axis2[i] * lz2;
+    b2[i] = pos2[i] - axis2[i] * lz2;
+  }
+  closest_segment_points(a1, a2, b1, b2, sphere1, sphere2);
+  return collide_spheres(sphere1, g1.p[0], sphere2, g2.p[0], c);
+}
+
 // Collider table for this path (ode/src/collision_kernel.cpp:167-268): returns
 // a collider id and whether the call runs with the geoms swapped (in which case
 // dCollide negates the normals, :319-335).
-enum { CL_NONE = 0, CL_SS, CL_SB, CL_SP, CL_BB, CL_BP, CL_CP, CL_HF };
+enum { CL_NONE = 0, CL_SS, CL_SB, CL_SP, CL_BB, CL_BP, CL_CP, CL_HF, CL_CS, CL_CB, CL_CC };
 OG_HD int collider_of(int t1, int t2, int* reverse) {
   *reverse = 0;
   auto is = [&](int a, int b) { return t1 == a && t2 == b; };
@@ -511,6 +727,11 @@ OG_HD int collider_of(int t1, int t2, int* reverse) {
   if (is(G_BOX, G_BOX)) return CL_BB;
   if (is(G_BOX, G_PLANE)) return CL_BP;
   if (is(G_PLANE, G_BOX)) { *reverse = 1; return CL_BP; }
+  if (is(G_CAPSULE, G_SPHERE)) return CL_CS;
+  if (is(G_SPHERE, G_CAPSULE)) { *reverse = 1; return CL_CS; }
+  if (is(G_CAPSULE, G_BOX)) return CL_CB;
+  if (is(G_BOX, G_CAPSULE)) { *reverse = 1; return CL_CB; }
+  if (is(G_CAPSULE, G_CAPSULE)) return CL_CC;
   if (is(G_CAPSULE, G_PLANE)) return CL_CP;
   if (is(G_PLANE, G_CAPSULE)) { *reverse = 1; return CL_CP; }
   if (t1 == G_HEIGHTFIELD && (t2 == G_SPHERE || t2 == G_BOX || t2 == G_CAPSULE)) return CL_HF;
@@ -535,6 +756,9 @@ OG_HD int collide_primitive(const GeomView& g1, const GeomView& g2, unsigned fla
     case CL_BB: n = collide_box_box(a, b, flags, c); break;
     case CL_BP: n = collide_box_plane(a, b, flags, c); break;
     case CL_CP: n = collide_capsule_plane(a, b, flags, c); break;
+    case CL_CS: n = collide_capsule_sphere(a, b, c); break;
+    case CL_CB: n = collide_capsule_box(a, b, c); break;
+    case CL_CC: n = collide_capsule_capsule(a, b, flags, c); break;
     default: n = 0;
   }
   if (rev)

@@ -98,6 +98,19 @@ def sphere_mass(density, r):
     return sphere_mass_total(m, r)
 
 
+def capsule_mass(density, r, length):
+    """dMassSetCapsule (ode/src/mass.cpp:125-155) with the axis along z:
+    mass and body-frame inertia of a cylinder of `length` with two
+    hemispherical caps."""
+    M1 = math.pi * r * r * length * density
+    M2 = 4.0 / 3.0 * math.pi * r ** 3 * density
+    m = M1 + M2
+    Ia = M1 * (0.25 * r * r + length * length / 12.0) + \
+        M2 * (0.4 * r * r + 0.375 * r * length + 0.25 * length * length)
+    Iz = (0.5 * M1 + 0.4 * M2) * r * r
+    return m, np.diag([Ia, Ia, Iz])
+
+
 def sphere_mass_total(m, r):
     ii = 0.4 * m * r * r
     return m, np.diag([ii, ii, ii])
@@ -545,6 +558,40 @@ def capsule_mix(seed=6, n_bodies=12):
             b.add_geom(w, GEOM_SPHERE, bi, (r,), s)
         else:
             lx, ly, lz = rng.uniform(0.2, 0.8, 3)
+            m, I = box_mass(1000.0, lx, ly, lz)
+            bi = b.add_body(w, (x, y, z), m, I, q=tuple(qv))
+            b.add_geom(w, GEOM_BOX, bi, (lx, ly, lz), s)
+    return b.build()
+
+
+def capsule_pile(seed=12, n_bodies=14):
+    """Capsules (r U[0.1,0.25], length U[0.2,0.8]), spheres and boxes dropped
+    into a 1.6 x 1.6 m column onto plane z=0, so capsules land on each other
+    and on spheres and boxes (capsule-sphere, capsule-box, capsule-capsule);
+    density 1000, same surface as box_drop."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    b = SceneBuilder()
+    s = _std_surface(b, 0.5)
+    w = b.new_world(cfm=1e-5, seed=seed)
+    b.add_geom(w, GEOM_PLANE, -1, (0, 0, 1, 0), s)
+    for k in range(n_bodies):
+        x, y = rng.uniform(-0.8, 0.8, 2)
+        z = 0.4 + 0.45 * k
+        qv = np.concatenate([[1.0], rng.uniform(-1, 1, 3)])
+        qv /= np.linalg.norm(qv)
+        kind = k % 3
+        if kind == 0:
+            r, L = rng.uniform(0.1, 0.25), rng.uniform(0.2, 0.8)
+            m, I = capsule_mass(1000.0, r, L)
+            bi = b.add_body(w, (x, y, z), m, I, q=tuple(qv))
+            b.add_geom(w, GEOM_CAPSULE, bi, (r, L), s)
+        elif kind == 1:
+            r = rng.uniform(0.1, 0.3)
+            m, I = sphere_mass(1000.0, r)
+            bi = b.add_body(w, (x, y, z), m, I, q=tuple(qv))
+            b.add_geom(w, GEOM_SPHERE, bi, (r,), s)
+        else:
+            lx, ly, lz = rng.uniform(0.2, 0.6, 3)
             m, I = box_mass(1000.0, lx, ly, lz)
             bi = b.add_body(w, (x, y, z), m, I, q=tuple(qv))
             b.add_geom(w, GEOM_BOX, bi, (lx, ly, lz), s)

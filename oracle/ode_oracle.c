@@ -897,10 +897,222 @@ static int collide_capsule_plane(const GeomRef* cp, const GeomRef* pl, unsigned 
   return nc;
 }
 
+/* dCollideCapsuleSphere, ode/src/capsule.cpp:130-160 */
+static int collide_capsule_sphere(const GeomRef* cp, const GeomRef* sp, OContact* c) {
+  const real* R = cp->R;
+  real alpha = R[2] * (sp->pos[0] - cp->pos[0]) + R[6] * (sp->pos[1] - cp->pos[1]) +
+               R[10] * (sp->pos[2] - cp->pos[2]);
+  const real lz2 = cp->p[1] * 0.5;
+  if (alpha > lz2) alpha = lz2;
+  if (alpha < -lz2) alpha = -lz2;
+  real p[3] = {cp->pos[0] + alpha * R[2], cp->pos[1] + alpha * R[6], cp->pos[2] + alpha * R[10]};
+  return collide_spheres(p, cp->p[0], sp->pos, sp->p[0], c);
+}
+
+/* dCollideSpheresZeroDist, ode/src/capsule.cpp:164-176 */
+static int collide_spheres_zero_dist(const real* p1, real r1, real r2, const real* normal, OContact* c) {
+  c->normal[0] = normal[0]; c->normal[1] = normal[1]; c->normal[2] = normal[2];
+  c->depth = r1 + r2;
+  const real k = 0.5 * (r2 - r1);
+  c->pos[0] = p1[0] + c->normal[0] * k;
+  c->pos[1] = p1[1] + c->normal[1] * k;
+  c->pos[2] = p1[2] + c->normal[2] * k;
+  return 1;
+}
+
+/* dClosestLineBoxPoints, ode/src/collision_util.cpp:247-372 (dDOUBLE) */
+static void closest_line_box_points(const real* p1, const real* p2, const real* c, const real* R,
+                                    const real* side, real* lret, real* bret) {
+  real tmp[3], s[3], v[3], sign[3], v2[3], h[3], tanchor[3];
+  int region[3];
+  tmp[0] = p1[0] - c[0]; tmp[1] = p1[1] - c[1]; tmp[2] = p1[2] - c[2];
+  mul1_331(s, R, tmp);
+  tmp[0] = p2[0] - p1[0]; tmp[1] = p2[1] - p1[1]; tmp[2] = p2[2] - p1[2];
+  mul1_331(v, R, tmp);
+  for (int i = 0; i < 3; i++) {
+    if (v[i] < 0) { s[i] = -s[i]; v[i] = -v[i]; sign[i] = -1; }
+    else sign[i] = 1;
+  }
+  for (int i = 0; i < 3; i++) v2[i] = v[i] * v[i];
+  for (int i = 0; i < 3; i++) h[i] = 0.5 * side[i];
+  const real tanchor_eps = 1e-307;
+  for (int i = 0; i < 3; i++) {
+    if (v[i] > tanchor_eps) {
+      if (s[i] < -h[i]) { region[i] = -1; tanchor[i] = (-h[i] - s[i]) / v[i]; }
+      else { region[i] = (s[i] > h[i]); tanchor[i] = (h[i] - s[i]) / v[i]; }
+    } else {
+      region[i] = 0;
+      tanchor[i] = 2;
+    }
+  }
+  real t = 0, dd2dt = 0;
+  for (int i = 0; i < 3; i++) dd2dt -= (region[i] ? v2[i] : 0) * tanchor[i];
+  if (dd2dt >= 0) goto got_answer;
+  do {
+    real next_t = 1;
+    for (int i = 0; i < 3; i++)
+      if (tanchor[i] > t && tanchor[i] < 1 && tanchor[i] < next_t) next_t = tanchor[i];
+    real next_dd2dt = 0;
+    for (int i = 0; i < 3; i++) next_dd2dt += (region[i] ? v2[i] : 0) * (next_t - tanchor[i]);
+    if (next_dd2dt >= 0) {
+      const real m = (next_dd2dt - dd2dt) / (next_t - t);
+      t -= dd2dt / m;
+      goto got_answer;
+    }
+    for (int i = 0; i < 3; i++) {
+      if (tanchor[i] == next_t) {
+        tanchor[i] = (h[i] - s[i]) / v[i];
+        region[i]++;
+      }
+    }
+    t = next_t;
+    dd2dt = next_dd2dt;
+  } while (t < 1);
+  t = 1;
+got_answer:
+  for (int i = 0; i < 3; i++) lret[i] = p1[i] + t * tmp[i];
+  for (int i = 0; i < 3; i++) {
+    tmp[i] = sign[i] * (s[i] + t * v[i]);
+    if (tmp[i] < -h[i]) tmp[i] = -h[i];
+    else if (tmp[i] > h[i]) tmp[i] = h[i];
+  }
+  mul0_331(s, R, tmp);
+  for (int i = 0; i < 3; i++) bret[i] = s[i] + c[i];
+}
+
+/* dClosestLineSegmentPoints, ode/src/collision_util.cpp:109-209 */
+static void closest_segment_points(const real* a1, const real* a2, const real* b1, const real* b2, real* cp1,
+                                   real* cp2) {
+  real a1a2[3], b1b2[3], a1b1[3], a1b2[3], a2b1[3], a2b2[3], n[3];
+  for (int i = 0; i < 3; ++i) { a1a2[i] = a2[i] - a1[i]; b1b2[i] = b2[i] - b1[i]; a1b1[i] = b1[i] - a1[i]; }
+  const real da1 = dot3(a1a2, a1b1), db1 = dot3(b1b2, a1b1);
+  if (da1 <= 0 && db1 >= 0) { for (int i = 0; i < 3; ++i) { cp1[i] = a1[i]; cp2[i] = b1[i]; } return; }
+  for (int i = 0; i < 3; ++i) a1b2[i] = b2[i] - a1[i];
+  const real da2 = dot3(a1a2, a1b2), db2 = dot3(b1b2, a1b2);
+  if (da2 <= 0 && db2 <= 0) { for (int i = 0; i < 3; ++i) { cp1[i] = a1[i]; cp2[i] = b2[i]; } return; }
+  for (int i = 0; i < 3; ++i) a2b1[i] = b1[i] - a2[i];
+  const real da3 = dot3(a1a2, a2b1), db3 = dot3(b1b2, a2b1);
+  if (da3 >= 0 && db3 >= 0) { for (int i = 0; i < 3; ++i) { cp1[i] = a2[i]; cp2[i] = b1[i]; } return; }
+  for (int i = 0; i < 3; ++i) a2b2[i] = b2[i] - a2[i];
+  const real da4 = dot3(a1a2, a2b2), db4 = dot3(b1b2, a2b2);
+  if (da4 >= 0 && db4 <= 0) { for (int i = 0; i < 3; ++i) { cp1[i] = a2[i]; cp2[i] = b2[i]; } return; }
+  const real la = dot3(a1a2, a1a2);
+  if (da1 >= 0 && da3 <= 0) {
+    const real k = da1 / la;
+    for (int i = 0; i < 3; ++i) n[i] = a1b1[i] - k * a1a2[i];
+    if (dot3(b1b2, n) >= 0) {
+      for (int i = 0; i < 3; ++i) { cp1[i] = a1[i] + k * a1a2[i]; cp2[i] = b1[i]; }
+      return;
+    }
+  }
+  if (da2 >= 0 && da4 <= 0) {
+    const real k = da2 / la;
+    for (int i = 0; i < 3; ++i) n[i] = a1b2[i] - k * a1a2[i];
+    if (dot3(b1b2, n) <= 0) {
+      for (int i = 0; i < 3; ++i) { cp1[i] = a1[i] + k * a1a2[i]; cp2[i] = b2[i]; }
+      return;
+    }
+  }
+  const real lb = dot3(b1b2, b1b2);
+  if (db1 <= 0 && db2 >= 0) {
+    const real k = -db1 / lb;
+    for (int i = 0; i < 3; ++i) n[i] = -a1b1[i] - k * b1b2[i];
+    if (dot3(a1a2, n) >= 0) {
+      for (int i = 0; i < 3; ++i) { cp1[i] = a1[i]; cp2[i] = b1[i] + k * b1b2[i]; }
+      return;
+    }
+  }
+  if (db3 <= 0 && db4 >= 0) {
+    const real k = -db3 / lb;
+    for (int i = 0; i < 3; ++i) n[i] = -a2b1[i] - k * b1b2[i];
+    if (dot3(a1a2, n) <= 0) {
+      for (int i = 0; i < 3; ++i) { cp1[i] = a2[i]; cp2[i] = b1[i] + k * b1b2[i]; }
+      return;
+    }
+  }
+  const real k = dot3(a1a2, b1b2);
+  real det = la * lb - k * k;
+  if (det <= 0) { for (int i = 0; i < 3; ++i) { cp1[i] = a1[i]; cp2[i] = b1[i]; } return; }
+  det = 1.0 / det;
+  const real alpha = (lb * da1 - k * db1) * det;
+  const real beta = (k * da1 - la * db1) * det;
+  for (int i = 0; i < 3; ++i) { cp1[i] = a1[i] + alpha * a1a2[i]; cp2[i] = b1[i] + beta * b1b2[i]; }
+}
+
+/* dCollideCapsuleBox, ode/src/capsule.cpp:178-229 */
+static int collide_capsule_box(const GeomRef* cp, const GeomRef* bx, OContact* c) {
+  const real* R1 = cp->R;
+  const real clen = cp->p[1] * 0.5;
+  real p1[3], p2[3], pl[3], pb[3];
+  for (int i = 0; i < 3; ++i) {
+    p1[i] = cp->pos[i] + clen * R1[4 * i + 2];
+    p2[i] = cp->pos[i] - clen * R1[4 * i + 2];
+  }
+  closest_line_box_points(p1, p2, bx->pos, bx->R, bx->p, pl, pb);
+  const real mindist = 1e-18;
+  const real dx = pl[0] - pb[0], dy = pl[1] - pb[1], dz = pl[2] - pb[2];
+  if (sqrt(dx * dx + dy * dy + dz * dz) < mindist) {
+    real normal[3] = {pb[0] - bx->pos[0], pb[1] - bx->pos[1], pb[2] - bx->pos[2]};
+    safe_normalize3(normal);
+    return collide_spheres_zero_dist(pl, cp->p[0], 0, normal, c);
+  }
+  return collide_spheres(pl, cp->p[0], pb, 0, c);
+}
+
+/* dCollideCapsuleCapsule, ode/src/capsule.cpp:232-350 */
+static int collide_capsule_capsule(const GeomRef* g1, const GeomRef* g2, unsigned flags, OContact* c) {
+  const real tolerance = 1e-5;
+  const real lz1 = g1->p[1] * 0.5, lz2 = g2->p[1] * 0.5;
+  const real* pos1 = g1->pos;
+  const real* pos2 = g2->pos;
+  real axis1[3] = {g1->R[2], g1->R[6], g1->R[10]};
+  real axis2[3] = {g2->R[2], g2->R[6], g2->R[10]};
+  real sphere1[3], sphere2[3];
+  const real a1a2 = dot3(axis1, axis2);
+  const real det = 1.0 - a1a2 * a1a2;
+  if (det < tolerance) {
+    if (a1a2 < 0) { axis2[0] = -axis2[0]; axis2[1] = -axis2[1]; axis2[2] = -axis2[2]; }
+    real q[3];
+    for (int i = 0; i < 3; i++) q[i] = pos1[i] - pos2[i];
+    const real k = dot3(axis1, q);
+    const real a1lo = -lz1, a1hi = lz1, a2lo = -lz2 - k, a2hi = lz2 - k;
+    const real lo = (a1lo > a2lo) ? a1lo : a2lo;
+    const real hi = (a1hi < a2hi) ? a1hi : a2hi;
+    if (lo <= hi) {
+      const int num_contacts = (int)(flags & 0xffff);
+      if (num_contacts >= 2 && lo < hi) {
+        for (int i = 0; i < 3; i++) sphere1[i] = pos1[i] + lo * axis1[i];
+        for (int i = 0; i < 3; i++) sphere2[i] = pos2[i] + (lo + k) * axis2[i];
+        const int n1 = collide_spheres(sphere1, g1->p[0], sphere2, g2->p[0], c);
+        if (n1) {
+          for (int i = 0; i < 3; i++) sphere1[i] = pos1[i] + hi * axis1[i];
+          for (int i = 0; i < 3; i++) sphere2[i] = pos2[i] + (hi + k) * axis2[i];
+          const int n2 = collide_spheres(sphere1, g1->p[0], sphere2, g2->p[0], c + 1);
+          if (n2) return 2;
+        }
+      }
+      const real alpha1 = (lo + hi) * 0.5;
+      const real alpha2 = alpha1 + k;
+      for (int i = 0; i < 3; i++) sphere1[i] = pos1[i] + alpha1 * axis1[i];
+      for (int i = 0; i < 3; i++) sphere2[i] = pos2[i] + alpha2 * axis2[i];
+      return collide_spheres(sphere1, g1->p[0], sphere2, g2->p[0], c);
+    }
+  }
+  real a1[3], a2[3], b1[3], b2[3];
+  for (int i = 0; i < 3; ++i) {
+    a1[i] = pos1[i] + axis1[i] * lz1;
+    a2[i] = pos1[i] - axis1[i] * lz1;
+    b1[i] = pos2[i] + axis2[i] * lz2;
+    b2[i] = pos2[i] - axis2[i] * lz2;
+  }
+  closest_segment_points(a1, a2, b1, b2, sphere1, sphere2);
+  return collide_spheres(sphere1, g1->p[0], sphere2, g2->p[0], c);
+}
+
 /* Collider table restricted to this path: returns the collider id for the
  * ordered class pair and whether the call is reversed, as dInitColliders
  * (ode/src/collision_kernel.cpp:167-268) arranges it. */
-enum { C_NONE, C_SS, C_SB, C_SP, C_BB, C_BP, C_CP, C_HF };
+enum { C_NONE, C_SS, C_SB, C_SP, C_BB, C_BP, C_CP, C_HF, C_CS, C_CB, C_CC };
 static int collider_of(int t1, int t2, int* reverse) {
   *reverse = 0;
 #define PAIR(a, b, id) \
@@ -911,6 +1123,9 @@ static int collider_of(int t1, int t2, int* reverse) {
   PAIR(ODEGPU_GEOM_SPHERE, ODEGPU_GEOM_PLANE, C_SP);
   PAIR(ODEGPU_GEOM_BOX, ODEGPU_GEOM_BOX, C_BB);
   PAIR(ODEGPU_GEOM_BOX, ODEGPU_GEOM_PLANE, C_BP);
+  PAIR(ODEGPU_GEOM_CAPSULE, ODEGPU_GEOM_SPHERE, C_CS);
+  PAIR(ODEGPU_GEOM_CAPSULE, ODEGPU_GEOM_BOX, C_CB);
+  PAIR(ODEGPU_GEOM_CAPSULE, ODEGPU_GEOM_CAPSULE, C_CC);
   PAIR(ODEGPU_GEOM_CAPSULE, ODEGPU_GEOM_PLANE, C_CP);
   PAIR(ODEGPU_GEOM_HEIGHTFIELD, ODEGPU_GEOM_SPHERE, C_HF);
   PAIR(ODEGPU_GEOM_HEIGHTFIELD, ODEGPU_GEOM_BOX, C_HF);
@@ -937,6 +1152,9 @@ static int do_collide(const GeomRef* g1, const GeomRef* g2, unsigned flags, OCon
     case C_BB: n = collide_box_box(a, b, flags, c); break;
     case C_BP: n = collide_box_plane(a, b, flags, c); break;
     case C_CP: n = collide_capsule_plane(a, b, flags, c); break;
+    case C_CS: n = collide_capsule_sphere(a, b, c); break;
+    case C_CB: n = collide_capsule_box(a, b, c); break;
+    case C_CC: n = collide_capsule_capsule(a, b, flags, c); break;
     case C_HF: n = oracle_heightfield_collide(a, b, flags, c); break;
     default: n = 0;
   }

@@ -29,6 +29,7 @@ SCENES = {
     "stack": (lambda: S.box_stack(n_worlds=2, height=5), 100),
     "capsule": (lambda: S.capsule_mix(seed=6), 80),
     "vehicles": (lambda: S.vehicles(n_worlds=3, steps=60, hf_samples=64), 60),
+    "capsule_pile": (lambda: S.capsule_pile(), 120),
 }
 KEEP = 10  # keep the state every KEEP steps
 
@@ -64,7 +65,8 @@ def make_collider_kats(n=120, seed=123):
     import ctypes as C
     rng = np.random.Generator(np.random.PCG64(seed))
     ref = O.ref("d")
-    pairs = [(0, 0), (0, 1), (1, 0), (0, 4), (4, 0), (1, 1), (1, 4), (4, 1), (2, 4), (4, 2)]
+    pairs = [(0, 0), (0, 1), (1, 0), (0, 4), (4, 0), (1, 1), (1, 4), (4, 1), (2, 4), (4, 2),
+             (2, 0), (0, 2), (2, 1), (1, 2), (2, 2)]
     recs = []
     for (t1, t2) in pairs:
         for _ in range(n):

@@ -62,7 +62,7 @@ def test_dcollide_on_reference_kats():
     """dCollide through the ODE API on the GPU for every collider on the path,
     against the reference's FP64 outputs: contact counts equal except where the
     deepest point is within 1e-5 of touching; positions/normals/depths within
-    FP32 tolerance."""
+    FP32 tolerance (depth only where the reference's normal is undefined)."""
     g = np.load(os.path.join(GOLDEN, "collider_kats.npz"))
     L = _api()
     n = len(g["t1"])
@@ -92,9 +92,18 @@ def test_dcollide_on_reference_kats():
             else:
                 near += 1
         else:
+            t1, t2 = int(g["t1"][k]), int(g["t2"][k])
+            # capsule-box with the capsule's axis inside the box: the closest
+            # line and box points coincide, and the reference takes the normal
+            # (and the position built on it) from rounding noise of pl - pb
+            # (dCollideCapsuleBox, ode/src/capsule.cpp:216-228); only the depth
+            # (the radius) is defined there
+            rc = g["p1"][k][0] if t1 == 2 else g["p2"][k][0]
+            degenerate = {t1, t2} == {1, 2} and nc and abs(ref[0, 6] - rc) < 1e-4
             for c in range(nc):
                 got = np.array(list(out[c].pos[:3]) + list(out[c].normal[:3]) + [out[c].depth])
-                worst = max(worst, np.abs(got - ref[c, :7]).max())
+                cols = [6] if degenerate else list(range(7))
+                worst = max(worst, np.abs(got[cols] - ref[c, cols]).max())
         for h in geoms:
             L.dGeomDestroy(h)
     assert count_mism <= n // 200, (count_mism, near)

@@ -33,13 +33,14 @@ def _scenes():
         "hinge": S.hinge_chains(n_worlds=8, steps=40),
         "tower": S.box_tower(n_worlds=6, yaw=0.0, spacing=0.0),
         "capsule": S.capsule_mix(seed=6),
+        "capsule_pile": S.capsule_pile(),
         # aligned equal boxes: exact SAT ties between parallel faces, which FP32
         # and FP64 break differently (ODE's own FP32 build drifts mm here)
         "stack": S.box_stack(n_worlds=4, height=5),
     }
 
 
-@pytest.mark.parametrize("name", ["box_drop", "batched", "hinge", "tower", "capsule"])
+@pytest.mark.parametrize("name", ["box_drop", "batched", "hinge", "tower", "capsule", "capsule_pile"])
 def test_one_step_from_oracle_state(batch_cls, name):
     sc = _scenes()[name]
     n = 40
