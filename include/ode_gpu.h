@@ -86,7 +86,7 @@ enum { dSphereClass = 0, dBoxClass, dCapsuleClass, dCylinderClass, dPlaneClass,
 
 /* include/ode/common.h:252-258 */
 typedef enum { dJointTypeNone = 0, dJointTypeBall, dJointTypeHinge, dJointTypeSlider,
-               dJointTypeContact, dJointTypeUniversal, dJointTypeHinge2 } dJointType;
+               dJointTypeContact, dJointTypeUniversal, dJointTypeHinge2, dJointTypeFixed } dJointType;
 
 /* include/ode/common.h:305-354 */
 enum {
@@ -151,6 +151,9 @@ dJointID dJointCreateBall(dWorldID w, dJointGroupID g);                  /* :153
 dJointID dJointCreateHinge(dWorldID w, dJointGroupID g);                 /* :1546 */
 dJointID dJointCreateContact(dWorldID w, dJointGroupID g, const dContact* c); /* :1562 */
 dJointID dJointCreateHinge2(dWorldID w, dJointGroupID g);                /* :1570 */
+dJointID dJointCreateSlider(dWorldID w, dJointGroupID g);                /* :1554 */
+dJointID dJointCreateUniversal(dWorldID w, dJointGroupID g);             /* :1578 */
+dJointID dJointCreateFixed(dWorldID w, dJointGroupID g);                 /* :1611 */
 void dJointDestroy(dJointID j);                                          /* :1647 */
 dJointGroupID dJointGroupCreate(int max_size);                           /* :1655 */
 void dJointGroupDestroy(dJointGroupID g);                                /* :1663 */
@@ -175,6 +178,28 @@ void dJointSetHinge2Axis2(dJointID j, dReal x, dReal y, dReal z);        /* :190
 void dJointSetHinge2Param(dJointID j, int parameter, dReal value);       /* :1908 */
 void dJointAddHinge2Torques(dJointID j, dReal torque1, dReal torque2);   /* :1916 */
 dReal dJointGetHinge2Angle1(dJointID j);                                 /* :2493 */
+void dJointSetSliderAxis(dJointID j, dReal x, dReal y, dReal z);         /* :1863 */
+void dJointSetSliderParam(dJointID j, int parameter, dReal value);       /* :1874 */
+void dJointAddSliderForce(dJointID j, dReal force);                      /* :1884 */
+dReal dJointGetSliderPosition(dJointID j);                               /* :2433 */
+dReal dJointGetSliderPositionRate(dJointID j);                           /* :2439 */
+void dJointGetSliderAxis(dJointID j, dVector3 result);                   /* :2445 */
+dReal dJointGetSliderParam(dJointID j, int parameter);                   /* :2451 */
+void dJointSetUniversalAnchor(dJointID j, dReal x, dReal y, dReal z);    /* :1922 */
+void dJointSetUniversalAxis1(dJointID j, dReal x, dReal y, dReal z);     /* :1928 */
+void dJointSetUniversalAxis2(dJointID j, dReal x, dReal y, dReal z);     /* :1973 */
+void dJointSetUniversalParam(dJointID j, int parameter, dReal value);    /* :2020 */
+void dJointAddUniversalTorques(dJointID j, dReal torque1, dReal torque2);/* :2028 */
+void dJointGetUniversalAnchor(dJointID j, dVector3 result);              /* :2513 */
+void dJointGetUniversalAxis1(dJointID j, dVector3 result);               /* :2534 */
+void dJointGetUniversalAxis2(dJointID j, dVector3 result);               /* :2540 */
+dReal dJointGetUniversalParam(dJointID j, int parameter);                /* :2547 */
+void dJointGetUniversalAngles(dJointID j, dReal* angle1, dReal* angle2); /* :2560 */
+dReal dJointGetUniversalAngle1(dJointID j);                              /* :2566 */
+dReal dJointGetUniversalAngle2(dJointID j);                              /* :2572 */
+void dJointSetFixed(dJointID j);                                         /* :2247 */
+void dJointSetFixedParam(dJointID j, int parameter, dReal value);        /* :2254 */
+dReal dJointGetFixedParam(dJointID j, int parameter);                    /* :2934 */
 int dAreConnectedExcluding(dBodyID b1, dBodyID b2, int joint_type);      /* :2968 */
 
 /* mass: include/ode/mass.h */

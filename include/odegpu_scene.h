@@ -38,8 +38,11 @@ enum {
 enum {
   ODEGPU_JOINT_BALL = 1,
   ODEGPU_JOINT_HINGE = 2,
+  ODEGPU_JOINT_SLIDER = 3,
   ODEGPU_JOINT_CONTACT = 4,
-  ODEGPU_JOINT_HINGE2 = 6
+  ODEGPU_JOINT_UNIVERSAL = 5,
+  ODEGPU_JOINT_HINGE2 = 6,
+  ODEGPU_JOINT_FIXED = 7
 };
 
 /* dContact surface mode bits (include/ode/contact.h:33-49). */
@@ -84,11 +87,16 @@ typedef struct odegpuWorldParams {
 } odegpuWorldParams;
 
 /* Number of doubles per joint in odegpuScene.joint_param. Layout:
- *   ball:   [0]=erp [1]=cfm
- *   hinge:  [0..8] = limot {lostop, histop, vel, fmax, fudge, bounce, cfm,
- *                           stop_erp, stop_cfm}
+ *   ball, fixed: [0]=erp [1]=cfm
+ *   hinge, slider: [0..8] = limot {lostop, histop, vel, fmax, fudge, bounce,
+ *                           cfm, stop_erp, stop_cfm}
+ *   universal: [0..8] limot1, [9..17] limot2
  *   hinge2: [0..8] limot1, [9..17] limot2, [18] susp_erp, [19] susp_cfm
- * (dxJointLimitMotor fields, ode/src/joints/joint.h:160-170). */
+ * (dxJointLimitMotor fields, ode/src/joints/joint.h:160-170). The geometry
+ * setters used per type: ball and universal take joint_anchor; hinge,
+ * hinge2, slider and universal take joint_axis1; hinge2 and universal take
+ * joint_axis2; the fixed joint takes the bodies' placement at creation
+ * (dJointSetFixed). */
 #define ODEGPU_JOINT_NPARAM 20
 /* Number of doubles per geom in odegpuScene.geom_param:
  *   sphere [0]=r; box [0..2]=side; capsule [0]=r [1]=length;
@@ -142,14 +150,19 @@ typedef struct odegpuScene {
   /* optional per-step controls (NULL = none); n_ctrl_steps steps are stored and
    * step s uses row (s % n_ctrl_steps). */
   int n_ctrl_steps;
-  const double* joint_torque;  /* [n_ctrl_steps][nj][2]: hinge torque in [0],
-                                  hinge2 torque1/torque2 in [0]/[1]           */
+  const double* joint_torque;  /* [n_ctrl_steps][nj][2]: hinge torque in [0]
+                                  (dJointAddHingeTorque), hinge2 and universal
+                                  torque1/torque2 in [0]/[1]
+                                  (dJointAddHinge2Torques,
+                                  dJointAddUniversalTorques), slider force in
+                                  [0] (dJointAddSliderForce)                  */
   const double* body_force;    /* [n_ctrl_steps][nb][6]: force, torque        */
   const double* joint_stop;    /* [n_ctrl_steps][nj]: before the step, limot1
-                                  lostop = histop of a hinge / hinge2 joint to
-                                  this angle (dJointSetHinge{,2}Param with
-                                  dParamLoStop, dParamHiStop); NaN leaves the
-                                  joint's own stops from joint_param        */
+                                  lostop = histop of a hinge, hinge2 or
+                                  universal joint (an angle) or of a slider (a
+                                  position) to this value (dJointSet*Param
+                                  with dParamLoStop, dParamHiStop); NaN leaves
+                                  the joint's own stops from joint_param    */
 } odegpuScene;
 
 /*

@@ -26,7 +26,8 @@ namespace og {
 // Status bits of the adjoint (per world): a part of the step whose
 // derivative is not modelled was met (the gradient leaves it out).
 enum {
-  ADJ_UNSUPPORTED_JOINT = 1,     // a hinge limit row, a bouncing hinge2 limit, hinge2 without body 2
+  ADJ_UNSUPPORTED_JOINT = 1,     // a hinge limit row, a bouncing hinge2 limit, hinge2 without body 2,
+                                 // slider, universal and fixed joints
   ADJ_UNSUPPORTED_CONTACT = 2,   // body-body contact, capsule vertex contact, geom under a field, bounce
   ADJ_TOO_LARGE = 4
 };

@@ -99,7 +99,13 @@ OG_HD void r_from_q(float* R, const float* q) {
   R[4] = 2.f * (q[1] * q[2] + q[0] * q[3]); R[5] = 1.f - qq1 - qq3; R[6] = 2.f * (q[2] * q[3] - q[0] * q[1]); R[7] = 0.f;
   R[8] = 2.f * (q[1] * q[3] - q[0] * q[2]); R[9] = 2.f * (q[2] * q[3] + q[0] * q[1]); R[10] = 1.f - qq1 - qq2; R[11] = 0.f;
 }
-// dQMultiply1/2/3 (ode/src/rotation.cpp:201-226)
+// dQMultiply0/1/2/3 (ode/src/rotation.cpp:191-226)
+OG_HD void qmul0(float* qa, const float* qb, const float* qc) {
+  qa[0] = qb[0] * qc[0] - qb[1] * qc[1] - qb[2] * qc[2] - qb[3] * qc[3];
+  qa[1] = qb[0] * qc[1] + qb[1] * qc[0] + qb[2] * qc[3] - qb[3] * qc[2];
+  qa[2] = qb[0] * qc[2] + qb[2] * qc[0] + qb[3] * qc[1] - qb[1] * qc[3];
+  qa[3] = qb[0] * qc[3] + qb[3] * qc[0] + qb[1] * qc[2] - qb[2] * qc[1];
+}
 OG_HD void qmul1(float* qa, const float* qb, const float* qc) {
   qa[0] = qb[0] * qc[0] + qb[1] * qc[1] + qb[2] * qc[2] + qb[3] * qc[3];
   qa[1] = qb[0] * qc[1] - qb[1] * qc[0] - qb[2] * qc[3] + qb[3] * qc[2];

@@ -519,7 +519,8 @@ int odegpuBatchCreate(const odegpuScene* sc, const odegpuBatchConfig* cfg, odegp
     for (int j = 0; j < D.njp; ++j) {
       const int gj = D.joint_off + j;
       const int type = sc->joint_type[gj];
-      if (type != ODEGPU_JOINT_BALL && type != ODEGPU_JOINT_HINGE && type != ODEGPU_JOINT_HINGE2) {
+      if (type != ODEGPU_JOINT_BALL && type != ODEGPU_JOINT_HINGE && type != ODEGPU_JOINT_HINGE2 &&
+          type != ODEGPU_JOINT_SLIDER && type != ODEGPU_JOINT_UNIVERSAL && type != ODEGPU_JOINT_FIXED) {
         delete B;
         return fail(ODEGPU_E_ARG, "unsupported joint type " + std::to_string(type));
       }
@@ -530,12 +531,7 @@ int odegpuBatchCreate(const odegpuScene* sc, const odegpuBatchConfig* cfg, odegp
       DevJoint& J = joints[gj];
       std::memset(&J, 0, sizeof(J));
       J.type = type; J.b1 = H.b1; J.b2 = H.b2; J.reverse = H.reverse;
-      for (int k = 0; k < 4; ++k) {
-        J.anchor1[k] = (float)H.anchor1[k]; J.anchor2[k] = (float)H.anchor2[k];
-        J.axis1[k] = (float)H.axis1[k]; J.axis2[k] = (float)H.axis2[k];
-        J.qrel[k] = (float)H.qrel[k]; J.v1[k] = (float)H.v1[k]; J.v2[k] = (float)H.v2[k];
-      }
-      J.c0 = (float)H.c0; J.s0 = (float)H.s0;
+      pack_joint_geometry(type, H, J);
       const double* jp = sc->joint_param + ODEGPU_JOINT_NPARAM * (size_t)gj;
       auto limot = [&](DevLimot& L, const double* p) {
         // dxJointLimitMotor::init then ::set in parameter order (joint.cpp:456-508)
@@ -545,8 +541,12 @@ int odegpuBatchCreate(const odegpuScene* sc, const odegpuBatchConfig* cfg, odegp
         L.bounce = (float)p[5]; L.normal_cfm = (float)p[6]; L.stop_erp = (float)p[7];
         L.stop_cfm = (float)p[8];
       };
-      if (type == ODEGPU_JOINT_BALL) { J.erp = (float)jp[0]; J.cfm = (float)jp[1]; }
-      if (type == ODEGPU_JOINT_HINGE) limot(J.lm1, jp);
+      if (type == ODEGPU_JOINT_BALL || type == ODEGPU_JOINT_FIXED) { J.erp = (float)jp[0]; J.cfm = (float)jp[1]; }
+      if (type == ODEGPU_JOINT_HINGE || type == ODEGPU_JOINT_SLIDER) limot(J.lm1, jp);
+      if (type == ODEGPU_JOINT_UNIVERSAL) {
+        limot(J.lm1, jp);
+        limot(J.lm2, jp + 9);
+      }
       if (type == ODEGPU_JOINT_HINGE2) {
         limot(J.lm1, jp);
         limot(J.lm2, jp + 9);

@@ -4,8 +4,24 @@
 #include <vector>
 #include "engine_types.cuh"
 #include "collide.cuh"
+#include "host_setup.hpp"
 
 namespace og {
+
+// FP32 copy of the setter results: the fields every joint has, plus the
+// per-type ones that share storage in DevJoint (hinge2 v1/v2, slider / fixed
+// offset, universal qrel2).
+inline void pack_joint_geometry(int type, const og_host::HJoint& H, DevJoint& J) {
+  for (int k = 0; k < 4; ++k) {
+    J.anchor1[k] = (float)H.anchor1[k]; J.anchor2[k] = (float)H.anchor2[k];
+    J.axis1[k] = (float)H.axis1[k]; J.axis2[k] = (float)H.axis2[k];
+    J.qrel[k] = (float)H.qrel[k];
+    if (type == J_HINGE2) { J.v1[k] = (float)H.v1[k]; J.v2[k] = (float)H.v2[k]; }
+    else if (type == J_SLIDER || type == J_FIXED) J.offset[k] = (float)H.offset[k];
+    else if (type == J_UNIVERSAL) J.qrel2[k] = (float)H.qrel2[k];
+  }
+  J.c0 = (float)H.c0; J.s0 = (float)H.s0;
+}
 
 // One world as the ODE API layer hands it to the device, in ODE's creation
 // order, with complete per-body joint lists (newest attachment first).

@@ -10,7 +10,7 @@
 namespace og {
 
 // Joint types (ODE dJointType values) and surface mode bits (dContact).
-enum { J_BALL = 1, J_HINGE = 2, J_CONTACT = 4, J_HINGE2 = 6 };
+enum { J_BALL = 1, J_HINGE = 2, J_SLIDER = 3, J_CONTACT = 4, J_UNIVERSAL = 5, J_HINGE2 = 6, J_FIXED = 7 };
 enum {
   SURF_MU2 = 0x001, SURF_FDIR1 = 0x002, SURF_BOUNCE = 0x004, SURF_SOFT_ERP = 0x008,
   SURF_SOFT_CFM = 0x010, SURF_MOTION1 = 0x020, SURF_MOTION2 = 0x040, SURF_MOTIONN = 0x080,
@@ -51,8 +51,17 @@ struct DevLimot {
 // A persistent (non-contact) joint after dJointAttach and its setters.
 struct DevJoint {
   int type, b1, b2, reverse;    // b1/b2 world-local, b2 = -1 for the environment
-  float anchor1[4], anchor2[4], axis1[4], axis2[4], qrel[4], v1[4], v2[4];
-  float erp, cfm, c0, s0, susp_erp, susp_cfm;
+  float anchor1[4], anchor2[4], axis1[4], axis2[4];
+  float qrel[4];                // hinge, slider, fixed: qrel; universal: qrel1
+  union {
+    float v1[4];                // hinge2
+    float offset[4];            // slider, fixed: body-1 centre relative to body 2
+  };
+  union {
+    float v2[4];                // hinge2
+    float qrel2[4];             // universal
+  };
+  float erp, cfm, c0, s0, susp_erp, susp_cfm;   // erp / cfm: ball and fixed
   DevLimot lm1, lm2;
 };
 

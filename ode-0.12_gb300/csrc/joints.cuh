@@ -101,7 +101,17 @@ OG_D void set_ball2(const BodyRef& B1, const BodyRef* B2, Info2& in, const float
   in.c(2) = k * dot3(q2, d);
 }
 
-// getHingeAngle (ode/src/joints/joint.cpp:381-451)
+// getHingeAngleFromRelativeQuat (ode/src/joints/joint.cpp:381-420)
+OG_D float hinge_angle_from_qrel(const float* qrel, const float* axis) {
+  const float cost2 = qrel[0];
+  const float sint2 = sqrtf(qrel[1] * qrel[1] + qrel[2] * qrel[2] + qrel[3] * qrel[3]);
+  float theta = (dot3(qrel + 1, axis) >= 0.f) ? (2.f * atan2f(sint2, cost2))
+                                               : (2.f * atan2f(sint2, -cost2));
+  if ((double)theta > 3.14159265358979323846) theta -= (float)(2.0 * 3.14159265358979323846);
+  return -theta;
+}
+
+// getHingeAngle (ode/src/joints/joint.cpp:432-450)
 OG_D float hinge_angle(const BodyRef& B1, const BodyRef* B2, const DevJoint& J) {
   float qrel[4];
   if (B2) {
@@ -111,12 +121,132 @@ OG_D float hinge_angle(const BodyRef& B1, const BodyRef* B2, const DevJoint& J) 
   } else {
     qmul3(qrel, B1.q, J.qrel);
   }
-  const float cost2 = qrel[0];
-  const float sint2 = sqrtf(qrel[1] * qrel[1] + qrel[2] * qrel[2] + qrel[3] * qrel[3]);
-  float theta = (dot3(qrel + 1, J.axis1) >= 0.f) ? (2.f * atan2f(sint2, cost2))
-                                                  : (2.f * atan2f(sint2, -cost2));
-  if ((double)theta > 3.14159265358979323846) theta -= (float)(2.0 * 3.14159265358979323846);
-  return -theta;
+  return hinge_angle_from_qrel(qrel, J.axis1);
+}
+
+// dRFrom2Axes (ode/src/rotation.cpp:94-133): columns a, b orthogonalised
+// against a, and a x b. A zero-length input leaves R as given.
+OG_D void r_from_2axes(float* R, float ax, float ay, float az, float bx, float by, float bz) {
+  float l = sqrtf(ax * ax + ay * ay + az * az);
+  if (l <= 0.f) return;
+  l = 1.0f / l;
+  ax *= l; ay *= l; az *= l;
+  const float k = ax * bx + ay * by + az * bz;
+  bx -= k * ax; by -= k * ay; bz -= k * az;
+  l = sqrtf(bx * bx + by * by + bz * bz);
+  if (l <= 0.f) return;
+  l = 1.0f / l;
+  bx *= l; by *= l; bz *= l;
+  R[0] = ax; R[4] = ay; R[8] = az;
+  R[1] = bx; R[5] = by; R[9] = bz;
+  R[2] = -by * az + ay * bz; R[6] = -bz * ax + az * bx; R[10] = -bx * ay + ax * by;
+  R[3] = 0.f; R[7] = 0.f; R[11] = 0.f;
+}
+
+// dQfromR (ode/src/rotation.cpp:258-306)
+OG_D void q_from_r(float* q, const float* R) {
+  const float tr = R[0] + R[5] + R[10];
+  float s;
+  if (tr >= 0.f) {
+    s = sqrtf(tr + 1.f);
+    q[0] = 0.5f * s;
+    s = 0.5f * (1.0f / s);
+    q[1] = (R[9] - R[6]) * s; q[2] = (R[2] - R[8]) * s; q[3] = (R[4] - R[1]) * s;
+    return;
+  }
+  int c;
+  if (R[5] > R[0]) c = (R[10] > R[5]) ? 2 : 1;
+  else c = (R[10] > R[0]) ? 2 : 0;
+  if (c == 0) {
+    s = sqrtf((R[0] - (R[5] + R[10])) + 1.f);
+    q[1] = 0.5f * s;
+    s = 0.5f * (1.0f / s);
+    q[2] = (R[1] + R[4]) * s; q[3] = (R[8] + R[2]) * s; q[0] = (R[9] - R[6]) * s;
+  } else if (c == 1) {
+    s = sqrtf((R[5] - (R[10] + R[0])) + 1.f);
+    q[2] = 0.5f * s;
+    s = 0.5f * (1.0f / s);
+    q[3] = (R[6] + R[9]) * s; q[1] = (R[1] + R[4]) * s; q[0] = (R[2] - R[8]) * s;
+  } else {
+    s = sqrtf((R[10] - (R[0] + R[5])) + 1.f);
+    q[3] = 0.5f * s;
+    s = 0.5f * (1.0f / s);
+    q[1] = (R[8] + R[2]) * s; q[2] = (R[6] + R[9]) * s; q[0] = (R[4] - R[1]) * s;
+  }
+}
+
+// dxJointUniversal::getAxes (ode/src/joints/universal.cpp:55-70)
+OG_D void universal_axes(const BodyRef& B1, const BodyRef* B2, const DevJoint& J, float* ax1, float* ax2) {
+  mul0_331(ax1, B1.R, J.axis1);
+  if (B2) mul0_331(ax2, B2->R, J.axis2);
+  else { ax2[0] = J.axis2[0]; ax2[1] = J.axis2[1]; ax2[2] = J.axis2[2]; }
+}
+
+// dxJointUniversal::getAngles (ode/src/joints/universal.cpp:73-167): angle 1
+// from the cross frame dRFrom2Axes(ax1, ax2) against qrel1, angle 2 from that
+// frame turned half a revolution about the bisector of ax1 and ax2 against qrel2.
+OG_D void universal_angles(const BodyRef& B1, const BodyRef* B2, const DevJoint& J, float& angle1,
+                           float& angle2) {
+  float ax1[3], ax2[3], R[12], qcross[4], qq[4], qrel[4];
+  universal_axes(B1, B2, J, ax1, ax2);
+  for (int k = 0; k < 12; ++k) R[k] = (k % 5 == 0) ? 1.f : 0.f;
+  r_from_2axes(R, ax1[0], ax1[1], ax1[2], ax2[0], ax2[1], ax2[2]);
+  q_from_r(qcross, R);
+  qmul1(qq, B1.q, qcross);
+  qmul2(qrel, qq, J.qrel);
+  angle1 = hinge_angle_from_qrel(qrel, J.axis1);
+  qrel[0] = 0.f;
+  qrel[1] = ax1[0] + ax2[0];
+  qrel[2] = ax1[1] + ax2[1];
+  qrel[3] = ax1[2] + ax2[2];
+  const float l = 1.0f / sqrtf(qrel[1] * qrel[1] + qrel[2] * qrel[2] + qrel[3] * qrel[3]);
+  qrel[1] *= l; qrel[2] *= l; qrel[3] *= l;
+  float qcross2[4];
+  qmul0(qcross2, qrel, qcross);
+  if (B2) {
+    qmul1(qq, B2->q, qcross2);
+    qmul2(qrel, qq, J.qrel2);
+  } else {
+    qmul2(qrel, qcross2, J.qrel2);
+  }
+  angle2 = -hinge_angle_from_qrel(qrel, J.axis2);
+}
+
+// dJointGetSliderPosition (ode/src/joints/slider.cpp:42-79)
+OG_D float slider_position(const BodyRef& B1, const BodyRef* B2, const DevJoint& J) {
+  float ax1[3], q[3];
+  mul0_331(ax1, B1.R, J.axis1);
+  if (B2) {
+    mul0_331(q, B2->R, J.offset);
+    for (int i = 0; i < 3; ++i) q[i] = B1.pos[i] - q[i] - B2->pos[i];
+  } else {
+    for (int i = 0; i < 3; ++i) q[i] = B1.pos[i] - J.offset[i];
+    if (J.reverse) { ax1[0] = -ax1[0]; ax1[1] = -ax1[1]; ax1[2] = -ax1[2]; }
+  }
+  return dot3(ax1, q);
+}
+
+// setFixedOrientation (ode/src/joints/joint.cpp:202-255): three rows from r0
+// that hold the relative orientation at qrel, with info->erp as the joint
+// finds it.
+OG_D void set_fixed_orientation(const BodyRef& B1, const BodyRef* B2, Info2& in, const float* qrel, int r0) {
+  in.J1a(r0, 0) = 1.f; in.J1a(r0 + 1, 1) = 1.f; in.J1a(r0 + 2, 2) = 1.f;
+  if (B2) { in.J2a(r0, 0) = -1.f; in.J2a(r0 + 1, 1) = -1.f; in.J2a(r0 + 2, 2) = -1.f; }
+  float qerr[4];
+  if (B2) {
+    float qq[4];
+    qmul1(qq, B1.q, B2->q);
+    qmul2(qerr, qq, qrel);
+  } else {
+    qmul3(qerr, B1.q, qrel);
+  }
+  if (qerr[0] < 0.f) { qerr[1] = -qerr[1]; qerr[2] = -qerr[2]; qerr[3] = -qerr[3]; }
+  float e[3];
+  mul0_331(e, B1.R, qerr + 1);
+  const float k = in.fps * in.erp;
+  in.c(r0) = 2.f * k * e[0];
+  in.c(r0 + 1) = 2.f * k * e[1];
+  in.c(r0 + 2) = 2.f * k * e[2];
 }
 
 // dxJointHinge2::measureAngle (ode/src/joints/hinge2.cpp:33-41)
@@ -137,21 +267,41 @@ OG_D int limot_test(const DevLimot& L, float angle, int& limit, float& err) {
 OG_D bool limot_tested(const DevLimot& L) {
   return (L.lostop >= -kPi || L.histop <= kPi) && L.lostop <= L.histop;
 }
+// the slider's test (ode/src/joints/slider.cpp:150-151): any finite stop
+OG_D bool limot_tested_linear(const DevLimot& L) {
+  return (L.lostop > -INFINITY || L.histop < INFINITY) && L.lostop <= L.histop;
+}
 
-// Torque a powered-at-limit motor adds to body 1 (body 2 gets the negation),
-// which the reference applies from inside getInfo2 via dBodyAddTorque.
-struct LimotTorque {
-  float t[3];
+// Force and torques a powered-at-limit motor adds to the bodies, which the
+// reference applies from inside getInfo2 via dBodyAddForce / dBodyAddTorque:
+// body 1 gets f1 and t1, body 2 gets -f1 and t2.
+struct LimotForce {
+  float f1[3], t1[3], t2[3];
   int active;
 };
+OG_D LimotForce limot_force_none() { return LimotForce{{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, 0}; }
 
-// addLimot, rotational case (ode/src/joints/joint.cpp:556-733)
+// dxJointLimitMotor::addLimot (ode/src/joints/joint.cpp:556-733). A linear
+// limot (rotational = false) acts on J1l/J2l and, between two bodies, sets
+// the angular parts to the torque-decoupling vector ltd = (x2 - x1)/2 x ax1.
 OG_D int limot_add(const DevLimot& L, int limit, float limit_err, bool has_b2, const BodyRef& B1,
-                   const BodyRef* B2, Info2& in, int row, const float* ax1, LimotTorque& tq) {
+                   const BodyRef* B2, Info2& in, int row, const float* ax1, LimotForce& tq,
+                   bool rotational = true) {
   int powered = L.fmax > 0.f;
   if (!(powered || limit)) return 0;
-  in.J1a(row, 0) = ax1[0]; in.J1a(row, 1) = ax1[1]; in.J1a(row, 2) = ax1[2];
-  if (has_b2) { in.J2a(row, 0) = -ax1[0]; in.J2a(row, 1) = -ax1[1]; in.J2a(row, 2) = -ax1[2]; }
+  float* J1 = rotational ? in.J1a_ptr(row) : &in.J1l(row, 0);
+  float* J2 = rotational ? in.J2a_ptr(row) : &in.J2l(row, 0);
+  J1[0] = ax1[0]; J1[1] = ax1[1]; J1[2] = ax1[2];
+  if (has_b2) { J2[0] = -ax1[0]; J2[1] = -ax1[1]; J2[2] = -ax1[2]; }
+  float ltd[3] = {0.f, 0.f, 0.f};
+  if (!rotational && has_b2) {
+    float c[3];
+    c[0] = 0.5f * (B2->pos[0] - B1.pos[0]);
+    c[1] = 0.5f * (B2->pos[1] - B1.pos[1]);
+    c[2] = 0.5f * (B2->pos[2] - B1.pos[2]);
+    cross3(ltd, c, ax1);
+    for (int k = 0; k < 3; ++k) { in.J1a(row, k) = ltd[k]; in.J2a(row, k) = ltd[k]; }
+  }
   if (limit && (L.lostop == L.histop)) powered = 0;
   if (powered) {
     in.cfm(row) = L.normal_cfm;
@@ -163,7 +313,15 @@ OG_D int limot_add(const DevLimot& L, int limit, float limit_err, bool has_b2, c
       float fm = L.fmax;
       if ((L.vel > 0.f) || (L.vel == 0.f && limit == 2)) fm = -fm;
       if ((limit == 1 && L.vel > 0.f) || (limit == 2 && L.vel < 0.f)) fm *= L.fudge;
-      tq.t[0] = -fm * ax1[0]; tq.t[1] = -fm * ax1[1]; tq.t[2] = -fm * ax1[2];
+      if (rotational) {
+        for (int k = 0; k < 3; ++k) { tq.t1[k] = -fm * ax1[k]; tq.t2[k] = fm * ax1[k]; }
+      } else {
+        for (int k = 0; k < 3; ++k) {
+          tq.f1[k] = -fm * ax1[k];
+          tq.t1[k] = has_b2 ? -fm * ltd[k] : 0.f;
+          tq.t2[k] = -fm * ltd[k];
+        }
+      }
       tq.active = 1;
     }
   }
@@ -177,8 +335,14 @@ OG_D int limot_add(const DevLimot& L, int limit, float limit_err, bool has_b2, c
       if (limit == 1) { in.lo(row) = 0.f; in.hi(row) = INFINITY; }
       else { in.lo(row) = -INFINITY; in.hi(row) = 0.f; }
       if (L.bounce > 0.f) {
-        float vel = dot3(B1.avel, ax1);
-        if (B2) vel -= dot3(B2->avel, ax1);
+        float vel;
+        if (rotational) {
+          vel = dot3(B1.avel, ax1);
+          if (B2) vel -= dot3(B2->avel, ax1);
+        } else {
+          vel = dot3(B1.lvel, ax1);
+          if (B2) vel -= dot3(B2->lvel, ax1);
+        }
         if (limit == 1) {
           if (vel < 0.f) { float nc = -L.bounce * vel; if (nc > in.c(row)) in.c(row) = nc; }
         } else {
@@ -198,7 +362,8 @@ struct JointInfo1 {
 };
 
 // getInfo1: contact (ode/src/joints/contact.cpp:47-71), ball (ball.cpp:56-60),
-// hinge (hinge.cpp:54-74), hinge2 (hinge2.cpp:81-101).
+// hinge (hinge.cpp:54-74), slider (slider.cpp:134-167), universal
+// (universal.cpp:265-293), hinge2 (hinge2.cpp:81-101), fixed (fixed.cpp:53-58).
 // lm1: the joint's limot1 for this step (stops may differ from J.lm1).
 OG_D JointInfo1 persistent_info1(const DevJoint& J, const DevLimot& lm1, const BodyRef& B1, const BodyRef* B2) {
   JointInfo1 r{0, 0, 0, 0.f, 0.f};
@@ -218,6 +383,28 @@ OG_D JointInfo1 persistent_info1(const DevJoint& J, const DevLimot& lm1, const B
       if (J.lm2.fmax > 0.f) r.m++;
       break;
     }
+    case J_SLIDER: {
+      r.m = (lm1.fmax > 0.f) ? 6 : 5;
+      if (limot_tested_linear(lm1)) {
+        // the same comparisons as testRotationalLimit, on the slider position
+        if (limot_test(lm1, slider_position(B1, B2, J), r.limit1, r.err1)) r.m = 6;
+      }
+      break;
+    }
+    case J_UNIVERSAL: {
+      r.m = 4;
+      const bool lim1 = limot_tested(lm1), lim2 = limot_tested(J.lm2);
+      if (lim1 || lim2) {
+        float a1, a2;
+        universal_angles(B1, B2, J, a1, a2);
+        if (lim1) limot_test(lm1, a1, r.limit1, r.err1);
+        if (lim2) limot_test(J.lm2, a2, r.limit2, r.err2);
+      }
+      if (r.limit1 || lm1.fmax > 0.f) r.m++;
+      if (r.limit2 || J.lm2.fmax > 0.f) r.m++;
+      break;
+    }
+    case J_FIXED: r.m = 6; break;
     default: break;
   }
   return r;
@@ -311,11 +498,98 @@ OG_D void contact_info2(const DevContact& ct, const DevSurface& S, int the_m, co
   }
 }
 
+// getInfo2 of the slider (slider.cpp:171-246), universal (universal.cpp:296-362)
+// and fixed (fixed.cpp:62-105) joints; kept out of line so that the common
+// joints' code does not carry their registers.
+__device__ __noinline__ void persistent_info2_more(const DevJoint& J, const DevLimot& lm1, const JointInfo1& i1,
+                                                   const BodyRef& B1, const BodyRef* B2, Info2& in,
+                                                   LimotForce& tq1, LimotForce& tq2) {
+  switch (J.type) {
+    case J_SLIDER: {
+      float c[3];
+      if (B2) for (int i = 0; i < 3; ++i) c[i] = B2->pos[i] - B1.pos[i];
+      set_fixed_orientation(B1, B2, in, J.qrel, 0);
+      float ax1[3], p[3], q[3];
+      mul0_331(ax1, B1.R, J.axis1);
+      plane_space(ax1, p, q);
+      if (B2) {
+        float t[3];
+        cross3(t, c, p);
+        for (int i = 0; i < 3; ++i) { t[i] *= 0.5f; in.J1a(3, i) = t[i]; in.J2a(3, i) = t[i]; }
+        cross3(t, c, q);
+        for (int i = 0; i < 3; ++i) { t[i] *= 0.5f; in.J1a(4, i) = t[i]; in.J2a(4, i) = t[i]; }
+        for (int i = 0; i < 3; ++i) { in.J2l(3, i) = -p[i]; in.J2l(4, i) = -q[i]; }
+      }
+      for (int i = 0; i < 3; ++i) { in.J1l(3, i) = p[i]; in.J1l(4, i) = q[i]; }
+      const float k = in.fps * in.erp;
+      if (B2) {
+        float ofs[3];
+        mul0_331(ofs, B2->R, J.offset);
+        for (int i = 0; i < 3; ++i) c[i] += ofs[i];
+        in.c(3) = k * dot3(p, c);
+        in.c(4) = k * dot3(q, c);
+      } else {
+        float ofs[3];
+        for (int i = 0; i < 3; ++i) ofs[i] = J.offset[i] - B1.pos[i];
+        in.c(3) = k * dot3(p, ofs);
+        in.c(4) = k * dot3(q, ofs);
+        if (J.reverse) { ax1[0] = -ax1[0]; ax1[1] = -ax1[1]; ax1[2] = -ax1[2]; }
+      }
+      limot_add(lm1, i1.limit1, i1.err1, B2 != nullptr, B1, B2, in, 5, ax1, tq1, false);
+      break;
+    }
+    case J_UNIVERSAL: {
+      set_ball(B1, B2, in, J.anchor1, J.anchor2);
+      float ax1[3], ax2[3], t[3], p[3];
+      universal_axes(B1, B2, J, ax1, ax2);
+      const float k = dot3(ax1, ax2);
+      t[0] = ax2[0] - k * ax1[0];
+      t[1] = ax2[1] - k * ax1[1];
+      t[2] = ax2[2] - k * ax1[2];
+      cross3(p, ax1, t);
+      safe_normalize3(p);
+      for (int i = 0; i < 3; ++i) in.J1a(3, i) = p[i];
+      if (B2) for (int i = 0; i < 3; ++i) in.J2a(3, i) = -p[i];
+      in.c(3) = in.fps * in.erp * -k;
+      const int row = 4 + limot_add(lm1, i1.limit1, i1.err1, B2 != nullptr, B1, B2, in, 4, ax1, tq1);
+      limot_add(J.lm2, i1.limit2, i1.err2, B2 != nullptr, B1, B2, in, row, ax2, tq2);
+      break;
+    }
+    case J_FIXED: {
+      // orientation rows with the erp the joint finds, then (like the ball
+      // joint) info->erp = the joint's erp for the position rows and onwards
+      set_fixed_orientation(B1, B2, in, J.qrel, 3);
+      in.J1l(0, 0) = 1.f; in.J1l(1, 1) = 1.f; in.J1l(2, 2) = 1.f;
+      in.erp = J.erp;
+      in.cfm(0) = J.cfm; in.cfm(1) = J.cfm; in.cfm(2) = J.cfm;
+      float ofs[3];
+      mul0_331(ofs, B1.R, J.offset);
+      if (B2) {
+        // dSetCrossMatrixPlus
+        in.J1a(0, 1) = -ofs[2]; in.J1a(0, 2) = +ofs[1];
+        in.J1a(1, 0) = +ofs[2]; in.J1a(1, 2) = -ofs[0];
+        in.J1a(2, 0) = -ofs[1]; in.J1a(2, 1) = +ofs[0];
+        in.J2l(0, 0) = -1.f; in.J2l(1, 1) = -1.f; in.J2l(2, 2) = -1.f;
+      }
+      const float k = in.fps * in.erp;
+      if (B2) {
+        for (int j = 0; j < 3; ++j) in.c(j) = k * (B2->pos[j] - B1.pos[j] + ofs[j]);
+      } else {
+        for (int j = 0; j < 3; ++j) in.c(j) = k * (J.offset[j] - B1.pos[j]);
+      }
+      break;
+    }
+    default: break;
+  }
+}
+
 // getInfo2 of the persistent joints: ball (ode/src/joints/ball.cpp:63-70),
-// hinge (hinge.cpp:77-149), hinge2 (hinge2.cpp:109-180). Up to two motor
-// torques (body-1 sense) are returned in tq1/tq2 for the caller to apply.
+// hinge (hinge.cpp:77-149), slider (slider.cpp:171-246), universal
+// (universal.cpp:296-362), hinge2 (hinge2.cpp:109-180), fixed (fixed.cpp:62-105).
+// The forces of up to two motors at a limit are returned in tq1/tq2 for the
+// caller to apply.
 OG_D void persistent_info2(const DevJoint& J, const DevLimot& lm1, const JointInfo1& i1, const BodyRef& B1,
-                           const BodyRef* B2, Info2& in, LimotTorque& tq1, LimotTorque& tq2) {
+                           const BodyRef* B2, Info2& in, LimotForce& tq1, LimotForce& tq2) {
   switch (J.type) {
     case J_BALL:
       // the reference writes info->erp here; the caller carries it forward
@@ -358,6 +632,9 @@ OG_D void persistent_info2(const DevJoint& J, const DevLimot& lm1, const JointIn
       in.cfm(0) = J.susp_cfm;
       break;
     }
+    case J_SLIDER:
+    case J_UNIVERSAL:
+    case J_FIXED: persistent_info2_more(J, lm1, i1, B1, B2, in, tq1, tq2); break;
     default: break;
   }
 }

@@ -151,6 +151,7 @@ dxJoint* new_joint(dxWorld* w, dxJointGroup* g, int type) {
   j->feedback = nullptr;
   j->h.axis1[0] = 1;
   if (type == dJointTypeHinge2) { j->h.axis2[1] = 1; j->h.v1[0] = 1; j->h.v2[1] = 1; }
+  else if (type == dJointTypeUniversal) j->h.axis2[1] = 1;
   else j->h.axis2[0] = 1;
   j->erp = w->erp;
   j->cfm = w->cfm;
@@ -339,6 +340,9 @@ void dMassSetBox(dMass* m, dReal density, dReal lx, dReal ly, dReal lz) {
 dJointID dJointCreateBall(dWorldID w, dJointGroupID g) { return new_joint(w, g, dJointTypeBall); }
 dJointID dJointCreateHinge(dWorldID w, dJointGroupID g) { return new_joint(w, g, dJointTypeHinge); }
 dJointID dJointCreateHinge2(dWorldID w, dJointGroupID g) { return new_joint(w, g, dJointTypeHinge2); }
+dJointID dJointCreateSlider(dWorldID w, dJointGroupID g) { return new_joint(w, g, dJointTypeSlider); }
+dJointID dJointCreateUniversal(dWorldID w, dJointGroupID g) { return new_joint(w, g, dJointTypeUniversal); }
+dJointID dJointCreateFixed(dWorldID w, dJointGroupID g) { return new_joint(w, g, dJointTypeFixed); }
 dJointID dJointCreateContact(dWorldID w, dJointGroupID g, const dContact* c) {
   dxJoint* j = new_joint(w, g, dJointTypeContact);
   j->contact = *c;   // dJointCreateContact copies the contact (ode/src/ode.cpp:1201-1208)
@@ -384,6 +388,27 @@ void dJointAttach(dJointID j, dBodyID b1, dBodyID b2) {
       og_host::set_axes(H, jb.B, ax[0], ax[1], ax[2], H.axis1, H.axis2);
       og_host::hinge_qrel(H, jb.B);
     }
+  } else if (j->type == dJointTypeSlider) {
+    // slider.cpp:349-353
+    og_host::slider_offset(H, jb.B);
+    og_host::initial_qrel(H, jb.B);
+  } else if (j->type == dJointTypeUniversal) {
+    // universal.cpp:772-796: anchor and axes re-expressed in the new bodies'
+    // frames (a reversed joint's anchor getter has no body 2 and leaves the
+    // anchor alone here)
+    double a[3], ax1[3], ax2[3];
+    if (j->reverse) { for (int k = 0; k < 3; ++k) a[k] = H.anchor2[k]; }
+    else world_anchor1(j, a);
+    og_host::set_anchors(H, jb.B, a[0], a[1], a[2], H.anchor1, H.anchor2);
+    og_host::universal_axes(H, jb.B, ax1, ax2);
+    if (j->reverse) {
+      og_host::set_axes(H, jb.B, ax2[0], ax2[1], ax2[2], nullptr, H.axis2);
+      og_host::set_axes(H, jb.B, ax1[0], ax1[1], ax1[2], H.axis1, nullptr);
+    } else {
+      og_host::set_axes(H, jb.B, ax1[0], ax1[1], ax1[2], H.axis1, nullptr);
+      og_host::set_axes(H, jb.B, ax2[0], ax2[1], ax2[2], nullptr, H.axis2);
+    }
+    og_host::universal_qrels(H, jb.B);
   } else if (j->type == dJointTypeHinge2 && b2) {
     double a[3], ax[3];
     world_anchor1(j, a);
@@ -531,6 +556,177 @@ dReal dJointGetHinge2Angle1(dJointID j) {
   og_host::mul1_331(a2, R1, a1);
   return (dReal)(-std::atan2(og_host::dot3(j->h.v2, a2), og_host::dot3(j->h.v1, a2)));
 }
+dReal limot_get(const og::DevLimot& L, int num) {
+  // dxJointLimitMotor::get (ode/src/joints/joint.cpp:506-532)
+  switch (num) {
+    case dParamLoStop: return L.lostop;
+    case dParamHiStop: return L.histop;
+    case dParamVel: return L.vel;
+    case dParamFMax: return L.fmax;
+    case dParamFudgeFactor: return L.fudge;
+    case dParamBounce: return L.bounce;
+    case dParamCFM: return L.normal_cfm;
+    case dParamStopERP: return L.stop_erp;
+    case dParamStopCFM: return L.stop_cfm;
+    default: return 0;
+  }
+}
+// World-frame axis of body 1 / body 2 (getAxis / getAxis2, ode/src/joints/joint.cpp:357-378).
+void world_axis1(const dxJoint* j, const double* axis, dVector3 r) {
+  if (!j->body[0]) return;
+  double R[12], a[3];
+  for (int k = 0; k < 12; ++k) R[k] = j->body[0]->R[k];
+  og_host::mul0_331(a, R, axis);
+  for (int k = 0; k < 3; ++k) r[k] = (dReal)a[k];
+}
+void world_axis2(const dxJoint* j, const double* axis, dVector3 r) {
+  if (j->body[1]) {
+    double R[12], a[3];
+    for (int k = 0; k < 12; ++k) R[k] = j->body[1]->R[k];
+    og_host::mul0_331(a, R, axis);
+    for (int k = 0; k < 3; ++k) r[k] = (dReal)a[k];
+  } else {
+    for (int k = 0; k < 3; ++k) r[k] = (dReal)axis[k];
+  }
+}
+
+// slider (ode/src/joints/slider.cpp)
+void dJointSetSliderAxis(dJointID j, dReal x, dReal y, dReal z) {
+  // :250-258
+  JB jb(j);
+  og_host::set_axes(j->h, jb.B, x, y, z, j->h.axis1, nullptr);
+  og_host::slider_offset(j->h, jb.B);
+  og_host::initial_qrel(j->h, jb.B);
+}
+void dJointGetSliderAxis(dJointID j, dVector3 r) { world_axis1(j, j->h.axis1, r); }
+void dJointSetSliderParam(dJointID j, int p, dReal v) { limot_set(j->lm1, p, v); }
+dReal dJointGetSliderParam(dJointID j, int p) { return limot_get(j->lm1, p); }
+dReal dJointGetSliderPosition(dJointID j) {
+  if (!j->body[0]) return 0;
+  JB jb(j);
+  return (dReal)og_host::slider_position(j->h, jb.B);
+}
+dReal dJointGetSliderPositionRate(dJointID j) {
+  // :82-104
+  if (!j->body[0]) return 0;
+  dVector3 ax;
+  world_axis1(j, j->h.axis1, ax);
+  const dReal* v1 = j->body[0]->lvel;
+  if (j->body[1]) {
+    const dReal* v2 = j->body[1]->lvel;
+    return ax[0] * v1[0] + ax[1] * v1[1] + ax[2] * v1[2] - (ax[0] * v2[0] + ax[1] * v2[1] + ax[2] * v2[2]);
+  }
+  dReal rate = ax[0] * v1[0] + ax[1] * v1[1] + ax[2] * v1[2];
+  return j->reverse ? -rate : rate;
+}
+void dJointAddSliderForce(dJointID j, dReal force) {
+  // :305-342; on a reversed joint the reference computes force -= force (zero)
+  if (j->reverse) force -= force;
+  dVector3 ax = {0, 0, 0, 0};
+  world_axis1(j, j->h.axis1, ax);
+  for (int k = 0; k < 3; ++k) ax[k] *= force;
+  if (j->body[0]) dBodyAddForce(j->body[0], ax[0], ax[1], ax[2]);
+  if (j->body[1]) dBodyAddForce(j->body[1], -ax[0], -ax[1], -ax[2]);
+  if (j->body[0] && j->body[1]) {
+    dReal c[3], ltd[3];
+    for (int k = 0; k < 3; ++k) c[k] = (dReal)0.5 * (j->body[1]->pos[k] - j->body[0]->pos[k]);
+    ltd[0] = c[1] * ax[2] - c[2] * ax[1];
+    ltd[1] = c[2] * ax[0] - c[0] * ax[2];
+    ltd[2] = c[0] * ax[1] - c[1] * ax[0];
+    dBodyAddTorque(j->body[0], ltd[0], ltd[1], ltd[2]);
+    dBodyAddTorque(j->body[1], ltd[0], ltd[1], ltd[2]);
+  }
+}
+
+// universal (ode/src/joints/universal.cpp)
+void dJointSetUniversalAnchor(dJointID j, dReal x, dReal y, dReal z) {
+  // :396-403
+  JB jb(j);
+  og_host::set_anchors(j->h, jb.B, x, y, z, j->h.anchor1, j->h.anchor2);
+  og_host::universal_qrels(j->h, jb.B);
+}
+void dJointSetUniversalAxis1(dJointID j, dReal x, dReal y, dReal z) {
+  // :406-415: on a reversed joint axis 1 is body 2's axis
+  JB jb(j);
+  if (j->reverse) og_host::set_axes(j->h, jb.B, x, y, z, nullptr, j->h.axis2);
+  else og_host::set_axes(j->h, jb.B, x, y, z, j->h.axis1, nullptr);
+  og_host::universal_qrels(j->h, jb.B);
+}
+void dJointSetUniversalAxis2(dJointID j, dReal x, dReal y, dReal z) {
+  // :481-490
+  JB jb(j);
+  if (j->reverse) og_host::set_axes(j->h, jb.B, x, y, z, j->h.axis1, nullptr);
+  else og_host::set_axes(j->h, jb.B, x, y, z, nullptr, j->h.axis2);
+  og_host::universal_qrels(j->h, jb.B);
+}
+void dJointGetUniversalAnchor(dJointID j, dVector3 r) {
+  // :559-569 (a reversed joint reports the body-2 anchor, which it lacks)
+  if (j->reverse) return;
+  double a[3];
+  if (j->body[0]) { world_anchor1(j, a); for (int k = 0; k < 3; ++k) r[k] = (dReal)a[k]; }
+}
+void dJointGetUniversalAxis1(dJointID j, dVector3 r) {
+  if (j->reverse) world_axis2(j, j->h.axis2, r); else world_axis1(j, j->h.axis1, r);
+}
+void dJointGetUniversalAxis2(dJointID j, dVector3 r) {
+  if (j->reverse) world_axis1(j, j->h.axis1, r); else world_axis2(j, j->h.axis2, r);
+}
+void dJointSetUniversalParam(dJointID j, int p, dReal v) {
+  // :611-624
+  if ((p & 0xff00) == 0x100) limot_set(j->lm2, p & 0xff, v);
+  else limot_set(j->lm1, p, v);
+}
+dReal dJointGetUniversalParam(dJointID j, int p) {
+  if ((p & 0xff00) == 0x100) return limot_get(j->lm2, p & 0xff);
+  return limot_get(j->lm1, p);
+}
+void dJointGetUniversalAngles(dJointID j, dReal* angle1, dReal* angle2) {
+  // :642-655
+  JB jb(j);
+  double a1 = 0, a2 = 0;
+  if (j->body[0]) og_host::universal_angles(j->h, jb.B, &a1, &a2);
+  if (j->reverse) { *angle1 = (dReal)a2; *angle2 = (dReal)-a1; }
+  else { *angle1 = (dReal)a1; *angle2 = (dReal)a2; }
+}
+dReal dJointGetUniversalAngle1(dJointID j) {
+  // :658-667
+  if (!j->body[0]) return 0;
+  JB jb(j);
+  return (dReal)(j->reverse ? og_host::universal_angle2(j->h, jb.B) : og_host::universal_angle1(j->h, jb.B));
+}
+dReal dJointGetUniversalAngle2(dJointID j) {
+  // :670-679
+  if (!j->body[0]) return 0;
+  JB jb(j);
+  return (dReal)(j->reverse ? -og_host::universal_angle1(j->h, jb.B) : og_host::universal_angle2(j->h, jb.B));
+}
+void dJointAddUniversalTorques(dJointID j, dReal t1, dReal t2) {
+  // :729-754
+  if (j->reverse) { const dReal tmp = t1; t1 = -t2; t2 = -tmp; }
+  dVector3 a1 = {0, 0, 0, 0}, a2 = {0, 0, 0, 0};
+  world_axis1(j, j->h.axis1, a1);
+  world_axis2(j, j->h.axis2, a2);
+  for (int k = 0; k < 3; ++k) a1[k] = a1[k] * t1 + a2[k] * t2;
+  if (j->body[0]) dBodyAddTorque(j->body[0], a1[0], a1[1], a1[2]);
+  if (j->body[1]) dBodyAddTorque(j->body[1], -a1[0], -a1[1], -a1[2]);
+}
+
+// fixed (ode/src/joints/fixed.cpp)
+void dJointSetFixed(dJointID j) {
+  // :110-132
+  JB jb(j);
+  og_host::fixed_offset(j->h, jb.B);
+  og_host::initial_qrel(j->h, jb.B);
+}
+void dJointSetFixedParam(dJointID j, int p, dReal v) {
+  if (p == dParamCFM) j->cfm = v; else if (p == dParamERP) j->erp = v;
+}
+dReal dJointGetFixedParam(dJointID j, int p) {
+  if (p == dParamCFM) return (dReal)j->cfm;
+  if (p == dParamERP) return (dReal)j->erp;
+  return 0;
+}
+
 int dAreConnectedExcluding(dBodyID b1, dBodyID b2, int joint_type) {
   // ode/src/ode.cpp:1529-1537
   if (!b1) return 0;
@@ -772,12 +968,7 @@ int dWorldQuickStep(dWorldID w, dReal stepsize) {
     J.b1 = index_of(j->body[0]);
     J.b2 = index_of(j->body[1]);
     J.reverse = j->reverse;
-    for (int q = 0; q < 4; ++q) {
-      J.anchor1[q] = (float)j->h.anchor1[q]; J.anchor2[q] = (float)j->h.anchor2[q];
-      J.axis1[q] = (float)j->h.axis1[q]; J.axis2[q] = (float)j->h.axis2[q];
-      J.qrel[q] = (float)j->h.qrel[q]; J.v1[q] = (float)j->h.v1[q]; J.v2[q] = (float)j->h.v2[q];
-    }
-    J.c0 = (float)j->h.c0; J.s0 = (float)j->h.s0;
+    og::pack_joint_geometry(j->type, j->h, J);
     J.erp = (float)j->erp; J.cfm = (float)j->cfm;
     J.lm1 = j->lm1; J.lm2 = j->lm2;
     J.susp_erp = (float)j->susp_erp; J.susp_cfm = (float)j->susp_cfm;

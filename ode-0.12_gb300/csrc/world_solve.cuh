@@ -53,7 +53,7 @@ OG_D void phase_body_prologue(const BatchDev& d, const WorldDesc& D, int lane) {
 // (when given) in place of lostop / histop.
 OG_D DevLimot step_limot1(const DevJoint& J, const float* stops, int ord) {
   DevLimot L = J.lm1;
-  if (stops && (J.type == J_HINGE || J.type == J_HINGE2)) {
+  if (stops && (J.type == J_HINGE || J.type == J_HINGE2 || J.type == J_SLIDER || J.type == J_UNIVERSAL)) {
     const float v = stops[ord];
     if (!isnan(v)) { L.lostop = v; L.histop = v; }
   }
@@ -105,8 +105,9 @@ OG_D int phase_rows(const BatchDev& d, const WorldDesc& D, int w, int nj, int ni
     d.island_rstart[D.body_off + w + i] = (js < nj) ? d.jrow[jl_off + js] : M;
   }
   // pass 2: getInfo2. The effective info->erp of a joint is the erp of the
-  // last ball joint at or before it in the same island (ball.cpp:59 writes it
-  // into the Info2 block the stepper reuses), else the world erp.
+  // last ball or fixed joint before it in the same island (ball.cpp:59 and
+  // fixed.cpp:80 write it into the Info2 block the stepper reuses), else the
+  // world erp.
   float erp_carry = D.erp;
   for (int base = 0; base < nj; base += 32) {
     const int k = base + lane;
@@ -119,14 +120,14 @@ OG_D int phase_rows(const BatchDev& d, const WorldDesc& D, int w, int nj, int ni
       start = (v >> 30) & 1;
       if (ord < D.njp) {
         const DevJoint& J = d.joints[D.joint_off + ord];
-        if (J.type == J_BALL) { is_ball = true; my_erp = J.erp; }
+        if (J.type == J_BALL || J.type == J_FIXED) { is_ball = true; my_erp = J.erp; }
       }
     }
     const unsigned balls = __ballot_sync(kFull, is_ball);
     const unsigned starts = __ballot_sync(kFull, start);
     const unsigned le = (lane == 31) ? kFull : ((1u << (lane + 1)) - 1u);
     const unsigned lt = (1u << lane) - 1u;
-    // erp seen by this joint: balls strictly before it within its island
+    // erp seen by this joint: ball / fixed joints strictly before it within its island
     const unsigned b_lt = balls & lt;
     const unsigned s_le = starts & le;
     const int last_ball = b_lt ? 31 - __clz(b_lt) : -1;
@@ -174,18 +175,26 @@ OG_D int phase_rows(const BatchDev& d, const WorldDesc& D, int w, int nj, int ni
         const DevJoint& J = d.joints[D.joint_off + ord];
         const DevLimot lm1 = step_limot1(J, stops, ord);
         const JointInfo1 i1 = persistent_info1(J, lm1, B1, pB2);
-        LimotTorque t1{{0.f, 0.f, 0.f}, 0}, t2{{0.f, 0.f, 0.f}, 0};
+        LimotForce t1 = limot_force_none(), t2 = limot_force_none();
         persistent_info2(J, lm1, i1, B1, pB2, in, t1, t2);
-        // powered motor pushing against a limit adds torque inside getInfo2
-        // (joint.cpp:612-660); concurrent additions are rare and use atomics
+        // a powered motor pushing against a limit adds force / torque inside
+        // getInfo2 (joint.cpp:612-660); concurrent additions are rare and use atomics
         for (int t = 0; t < 2; ++t) {
-          const LimotTorque& tq = t ? t2 : t1;
+          const LimotForce& tq = t ? t2 : t1;
           if (!tq.active) continue;
+          float* fa = reinterpret_cast<float*>(&d.facc[D.body_off + b1]);
           float* ta = reinterpret_cast<float*>(&d.tacc[D.body_off + b1]);
-          atomicAdd(ta + 0, tq.t[0]); atomicAdd(ta + 1, tq.t[1]); atomicAdd(ta + 2, tq.t[2]);
+          for (int k = 0; k < 3; ++k) {
+            if (tq.f1[k] != 0.f) atomicAdd(fa + k, tq.f1[k]);
+            atomicAdd(ta + k, tq.t1[k]);
+          }
           if (b2 >= 0) {
+            float* fb = reinterpret_cast<float*>(&d.facc[D.body_off + b2]);
             float* tb = reinterpret_cast<float*>(&d.tacc[D.body_off + b2]);
-            atomicAdd(tb + 0, -tq.t[0]); atomicAdd(tb + 1, -tq.t[1]); atomicAdd(tb + 2, -tq.t[2]);
+            for (int k = 0; k < 3; ++k) {
+              if (tq.f1[k] != 0.f) atomicAdd(fb + k, -tq.f1[k]);
+              atomicAdd(tb + k, tq.t2[k]);
+            }
           }
         }
       } else {
@@ -439,6 +448,60 @@ OG_D void phase_controls(const BatchDev& d, const WorldDesc& D, int step, int la
         float4 t2 = d.tacc[D.body_off + J.b2];
         t2.x += -t[0]; t2.y += -t[1]; t2.z += -t[2];
         d.tacc[D.body_off + J.b2] = t2;
+      } else if (J.type == J_SLIDER) {
+        // dJointAddSliderForce (ode/src/joints/slider.cpp:305-342); on a
+        // reversed joint the reference computes force -= force, i.e. zero
+        float force = tq[0];
+        if (J.reverse) force -= force;
+        float R[12], ax[3];
+        body_R(d, D.body_off + J.b1, R);
+        mul0_331(ax, R, J.axis1);
+        ax[0] *= force; ax[1] *= force; ax[2] *= force;
+        float4 f1 = d.facc[D.body_off + J.b1];
+        f1.x += ax[0]; f1.y += ax[1]; f1.z += ax[2];
+        d.facc[D.body_off + J.b1] = f1;
+        if (J.b2 >= 0) {
+          float4 f2 = d.facc[D.body_off + J.b2];
+          f2.x += -ax[0]; f2.y += -ax[1]; f2.z += -ax[2];
+          d.facc[D.body_off + J.b2] = f2;
+          // linear torque decoupling: both bodies get (x2 - x1)/2 x force
+          const float4 p1 = d.pos[D.body_off + J.b1], p2 = d.pos[D.body_off + J.b2];
+          const float c[3] = {0.5f * (p2.x - p1.x), 0.5f * (p2.y - p1.y), 0.5f * (p2.z - p1.z)};
+          float ltd[3];
+          cross3(ltd, c, ax);
+          float4 t1 = d.tacc[D.body_off + J.b1];
+          t1.x += ltd[0]; t1.y += ltd[1]; t1.z += ltd[2];
+          d.tacc[D.body_off + J.b1] = t1;
+          float4 t2 = d.tacc[D.body_off + J.b2];
+          t2.x += ltd[0]; t2.y += ltd[1]; t2.z += ltd[2];
+          d.tacc[D.body_off + J.b2] = t2;
+        }
+      } else if (J.type == J_UNIVERSAL) {
+        // dJointAddUniversalTorques (ode/src/joints/universal.cpp:729-754)
+        float tq1 = tq[0], tq2 = tq[1];
+        if (J.reverse) { const float tmp = tq1; tq1 = -tq2; tq2 = -tmp; }
+        float R1[12], a1[3], a2[3];
+        body_R(d, D.body_off + J.b1, R1);
+        mul0_331(a1, R1, J.axis1);
+        if (J.b2 >= 0) {
+          float R2[12];
+          body_R(d, D.body_off + J.b2, R2);
+          mul0_331(a2, R2, J.axis2);
+        } else {
+          a2[0] = J.axis2[0]; a2[1] = J.axis2[1]; a2[2] = J.axis2[2];
+        }
+        float t[3];
+        t[0] = a1[0] * tq1 + a2[0] * tq2;
+        t[1] = a1[1] * tq1 + a2[1] * tq2;
+        t[2] = a1[2] * tq1 + a2[2] * tq2;
+        float4 t1 = d.tacc[D.body_off + J.b1];
+        t1.x += t[0]; t1.y += t[1]; t1.z += t[2];
+        d.tacc[D.body_off + J.b1] = t1;
+        if (J.b2 >= 0) {
+          float4 t2 = d.tacc[D.body_off + J.b2];
+          t2.x += -t[0]; t2.y += -t[1]; t2.z += -t[2];
+          d.tacc[D.body_off + J.b2] = t2;
+        }
       }
     }
   }

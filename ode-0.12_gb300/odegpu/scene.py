@@ -17,7 +17,8 @@ import math
 import numpy as np
 
 GEOM_SPHERE, GEOM_BOX, GEOM_CAPSULE, GEOM_PLANE, GEOM_HEIGHTFIELD = 0, 1, 2, 4, 9
-JOINT_BALL, JOINT_HINGE, JOINT_CONTACT, JOINT_HINGE2 = 1, 2, 4, 6
+JOINT_BALL, JOINT_HINGE, JOINT_SLIDER, JOINT_CONTACT, JOINT_UNIVERSAL, JOINT_HINGE2, JOINT_FIXED = \
+    1, 2, 3, 4, 5, 6, 7
 BODY_GYROSCOPIC, BODY_NO_GRAVITY = 1, 2
 
 CONTACT_MU2 = 0x001
@@ -252,9 +253,11 @@ class Scene:
         self._refresh()
 
     def set_controls(self, joint_torque=None, body_force=None, joint_stop=None):
-        """Per-step controls: joint_torque [S][nj_total][2], body_force
-        [S][nb_total][6], joint_stop [S][nj_total] (hinge / hinge2 limot1
-        lostop = histop before the step; NaN keeps the joint's own stops)."""
+        """Per-step controls: joint_torque [S][nj_total][2] (hinge torque,
+        hinge2 / universal torque pair, slider force), body_force
+        [S][nb_total][6], joint_stop [S][nj_total] (hinge / hinge2 / universal
+        / slider limot1 lostop = histop before the step; NaN keeps the joint's
+        own stops)."""
         S = 0
         if joint_torque is not None:
             self.joint_torque = np.ascontiguousarray(joint_torque, dtype=np.float64)
@@ -743,3 +746,144 @@ def vehicles(n_worlds=2048, seed=10, steps=300, hf_samples=256, spacing=0.5, sig
         tq[:, j0 + 3, 1] = throttle[:, wi]
     sc.set_controls(joint_torque=tq, joint_stop=stops)
     return sc
+
+
+def _unit(v):
+    v = np.asarray(v, float)
+    return v / np.linalg.norm(v)
+
+
+def mechanisms(n_worlds=256, seed=13, steps=200):
+    """Joint-type batch: per world, on a ground plane z=0, five mechanisms
+    side by side 2.5 m apart along x (seeded per world):
+      0. rail: a 0.4x0.2x0.2 m, 2 kg box on a slider to the environment along a
+         near-horizontal axis; stops -/+U[0.2,0.5] m, a motor (vel U[-1,1] m/s,
+         fmax 20 N) in half the worlds, stop bounce 0.3 in a third; per-step
+         slider force U[-10,10] N, and in every third block of 10 steps a servo
+         stop lostop = histop = U[-0.2,0.2] m.
+      1. drop rail: a 0.3 m, 1 kg cube on a slider attached the other way round
+         (body 1 = environment, so the joint is reversed) along a near-vertical
+         axis, falling onto the plane; per-step slider force U[-10,10] N (a
+         reversed slider's dJointAddSliderForce adds nothing).
+      2. piston: a 0.2x0.2x0.6 m, 3 kg cylinder box hinged to the environment
+         about y at its top, tilted U[-0.5,0.5] rad, with a 0.1x0.1x0.4 m, 1 kg
+         piston on a body-body slider along its long axis: motor vel
+         U[-0.5,0.5] m/s, fmax 30 N, stops -/+0.15 m; per-step slider force
+         U[-5,5] N.
+      3. chain: a capsule (r 0.06 m, length 0.5 m, 1.5 kg) hanging from the
+         environment by a universal joint (axes x, y; axis-1 stops -/+0.6 rad,
+         an axis-2 motor in half the worlds), a 0.2 m box below it on a ball
+         joint (erp 0.5), a box welded under that by a fixed joint (erp
+         U[0.1,0.6], cfm 1e-4) and a box hinged under it about x (stops
+         -/+0.8 rad); per-step universal torques U[-1,1] N m and hinge torque
+         U[-0.5,0.5] N m; small initial spin.
+      4. a pair of 0.3 m, 1 kg cubes glued by a body-body fixed joint, dropped
+         from 0.6 m with a random orientation and spin, and a 0.25 m cube
+         welded to the environment (reversed fixed joint) given an initial
+         velocity.
+    Surface mu 0.6 (pyramid friction). Max 4 contacts per pair."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    b = SceneBuilder()
+    s = _std_surface(b, 0.6)
+    NAN = float("nan")
+    rail, drop, piston, uni, hinge3 = [], [], [], [], []
+    for wi in range(n_worlds):
+        w = b.new_world(cfm=1e-5, seed=int(rng.integers(0, 2**32)))
+        b.add_geom(w, GEOM_PLANE, -1, (0, 0, 1, 0), s)
+        # 0. rail
+        a = rng.uniform(0, 2 * math.pi)
+        ax = _unit((math.cos(a), math.sin(a), rng.uniform(-0.3, 0.3)))
+        m, I = box_mass_total(2.0, 0.4, 0.2, 0.2)
+        bi = b.add_body(w, (0.0, 0.0, 0.6), m, I, lvel=tuple(ax * rng.uniform(-1, 1)))
+        b.add_geom(w, GEOM_BOX, bi, (0.4, 0.2, 0.2), s)
+        lim = rng.uniform(0.2, 0.5)
+        motor = wi % 2 == 0
+        rail.append(b.add_joint(w, JOINT_SLIDER, bi, -1, axis1=tuple(ax), param=limot_params(
+            lostop=-lim, histop=lim, vel=rng.uniform(-1, 1) if motor else 0.0, fmax=20.0 if motor else 0.0,
+            bounce=0.3 if wi % 3 == 0 else 0.0)))
+        # 1. drop rail (reversed)
+        ax = _unit((rng.uniform(-0.2, 0.2), rng.uniform(-0.2, 0.2), 1.0))
+        m, I = box_mass_total(1.0, 0.3, 0.3, 0.3)
+        bi = b.add_body(w, (2.5, 0.0, rng.uniform(0.25, 0.6)), m, I)
+        b.add_geom(w, GEOM_BOX, bi, (0.3, 0.3, 0.3), s)
+        drop.append(b.add_joint(w, JOINT_SLIDER, -1, bi, axis1=tuple(ax), param=limot_params()))
+        # 2. piston
+        t = rng.uniform(-0.5, 0.5)
+        u = np.array([math.sin(t), 0.0, math.cos(t)])
+        q = (math.cos(t / 2), 0.0, math.sin(t / 2), 0.0)
+        top = np.array([5.0, 0.0, 1.8])
+        cc = top - 0.3 * u
+        m, I = box_mass_total(3.0, 0.2, 0.2, 0.6)
+        cyl = b.add_body(w, tuple(cc), m, I, q=q)
+        b.add_geom(w, GEOM_BOX, cyl, (0.2, 0.2, 0.6), s)
+        m, I = box_mass_total(1.0, 0.1, 0.1, 0.4)
+        pis = b.add_body(w, tuple(cc - 0.5 * u), m, I, q=q)
+        b.add_geom(w, GEOM_BOX, pis, (0.1, 0.1, 0.4), s)
+        b.add_joint(w, JOINT_HINGE, cyl, -1, anchor=tuple(top), axis1=(0, 1, 0), param=limot_params())
+        piston.append(b.add_joint(w, JOINT_SLIDER, cyl, pis, axis1=tuple(u), param=limot_params(
+            lostop=-0.15, histop=0.15, vel=rng.uniform(-0.5, 0.5), fmax=30.0)))
+        # 3. universal / ball / fixed / hinge chain
+        x3 = 7.5
+        m, I = capsule_mass(1.0, 0.06, 0.5)
+        scale = 1.5 / m
+        ca = b.add_body(w, (x3, 0.0, 2.0 - 0.31), 1.5, np.asarray(I) * scale,
+                        avel=tuple(rng.uniform(-0.5, 0.5, 3)))
+        b.add_geom(w, GEOM_CAPSULE, ca, (0.06, 0.5), s)
+        p = np.zeros(JOINT_NPARAM)
+        p[0:9] = limot_params(lostop=-0.6, histop=0.6)
+        umotor = wi % 2 == 1
+        p[9:18] = limot_params(vel=rng.uniform(-1, 1) if umotor else 0.0, fmax=2.0 if umotor else 0.0)
+        uni.append(b.add_joint(w, JOINT_UNIVERSAL, ca, -1, anchor=(x3, 0.0, 2.0), axis1=(1, 0, 0),
+                               axis2=(0, 1, 0), param=p))
+        m, I = box_mass_total(1.0, 0.2, 0.2, 0.2)
+        bb = b.add_body(w, (x3, 0.0, 2.0 - 0.62 - 0.1), m, I)
+        b.add_geom(w, GEOM_BOX, bb, (0.2, 0.2, 0.2), s)
+        b.add_joint(w, JOINT_BALL, ca, bb, anchor=(x3, 0.0, 2.0 - 0.62), param=[0.5, 1e-5])
+        bc = b.add_body(w, (x3, 0.0, 2.0 - 0.62 - 0.3), m, I)
+        b.add_geom(w, GEOM_BOX, bc, (0.2, 0.2, 0.2), s)
+        b.add_joint(w, JOINT_FIXED, bb, bc, param=[rng.uniform(0.1, 0.6), 1e-4])
+        bd = b.add_body(w, (x3, 0.0, 2.0 - 0.62 - 0.5), m, I)
+        b.add_geom(w, GEOM_BOX, bd, (0.2, 0.2, 0.2), s)
+        hinge3.append(b.add_joint(w, JOINT_HINGE, bc, bd, anchor=(x3, 0.0, 2.0 - 0.62 - 0.4), axis1=(1, 0, 0),
+                                  param=limot_params(lostop=-0.8, histop=0.8)))
+        # 4. glued pair and a welded cube
+        qa = _unit(rng.normal(size=4))
+        R = _R_from_q(qa)
+        c0 = np.array([10.0, 0.0, 0.6])
+        m, I = box_mass_total(1.0, 0.3, 0.3, 0.3)
+        av = tuple(rng.uniform(-2, 2, 3))
+        g1 = b.add_body(w, tuple(c0 - 0.16 * R[:, 0]), m, I, q=tuple(qa), avel=av)
+        b.add_geom(w, GEOM_BOX, g1, (0.3, 0.3, 0.3), s)
+        g2 = b.add_body(w, tuple(c0 + 0.16 * R[:, 0]), m, I, q=tuple(qa), avel=av)
+        b.add_geom(w, GEOM_BOX, g2, (0.3, 0.3, 0.3), s)
+        b.add_joint(w, JOINT_FIXED, g1, g2, param=[rng.uniform(0.1, 0.4), 1e-5])
+        m, I = box_mass_total(1.0, 0.25, 0.25, 0.25)
+        wq = _unit((1.0, *rng.uniform(-0.1, 0.1, 3)))
+        wb = b.add_body(w, (11.0, 0.0, 0.5), m, I, q=tuple(wq), lvel=tuple(rng.uniform(-0.5, 0.5, 3)),
+                        avel=tuple(rng.uniform(-1, 1, 3)))
+        b.add_geom(w, GEOM_BOX, wb, (0.25, 0.25, 0.25), s)
+        b.add_joint(w, JOINT_FIXED, -1, wb, param=[0.2, 1e-5])
+    sc = b.build()
+    nj = sc.nj_total
+    tq = np.zeros((steps, nj, 2))
+    stops = np.full((steps, nj), NAN)
+    servo = (np.arange(steps) // 10) % 3 == 2
+    for wi in range(n_worlds):
+        j0 = int(sc.joint_off[wi])
+        tq[:, j0 + rail[wi], 0] = rng.uniform(-10, 10, steps)
+        tq[:, j0 + drop[wi], 0] = rng.uniform(-10, 10, steps)
+        tq[:, j0 + piston[wi], 0] = rng.uniform(-5, 5, steps)
+        tq[:, j0 + uni[wi], :] = rng.uniform(-1, 1, (steps, 2))
+        tq[:, j0 + hinge3[wi], 0] = rng.uniform(-0.5, 0.5, steps)
+        target = rng.uniform(-0.2, 0.2, steps)
+        stops[servo, j0 + rail[wi]] = target[servo]
+    sc.set_controls(joint_torque=tq, joint_stop=stops)
+    return sc
+
+
+def _R_from_q(q):
+    """3x3 rotation of a unit quaternion (w, x, y, z), as dRfromQ."""
+    w, x, y, z = q
+    return np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y)],
+                     [2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x)],
+                     [2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)]])

@@ -113,6 +113,12 @@ static void r_from_q(real* R, const real* q) {
   R[8] = 2 * (q[1] * q[3] - q[0] * q[2]); R[9] = 2 * (q[2] * q[3] + q[0] * q[1]); R[10] = 1 - qq1 - qq2; R[11] = 0;
 }
 /* dQMultiply0..3, ode/src/rotation.cpp:191-226 */
+static void qmul0(real* qa, const real* qb, const real* qc) {
+  qa[0] = qb[0] * qc[0] - qb[1] * qc[1] - qb[2] * qc[2] - qb[3] * qc[3];
+  qa[1] = qb[0] * qc[1] + qb[1] * qc[0] + qb[2] * qc[3] - qb[3] * qc[2];
+  qa[2] = qb[0] * qc[2] + qb[2] * qc[0] + qb[3] * qc[1] - qb[1] * qc[3];
+  qa[3] = qb[0] * qc[3] + qb[3] * qc[0] + qb[1] * qc[2] - qb[2] * qc[1];
+}
 static void qmul1(real* qa, const real* qb, const real* qc) {
   qa[0] = qb[0] * qc[0] + qb[1] * qc[1] + qb[2] * qc[2] + qb[3] * qc[3];
   qa[1] = qb[0] * qc[1] - qb[1] * qc[0] - qb[2] * qc[3] + qb[3] * qc[2];
@@ -130,6 +136,53 @@ static void qmul3(real* qa, const real* qb, const real* qc) {
   qa[1] = -qb[0] * qc[1] - qb[1] * qc[0] + qb[2] * qc[3] - qb[3] * qc[2];
   qa[2] = -qb[0] * qc[2] - qb[2] * qc[0] + qb[3] * qc[1] - qb[1] * qc[3];
   qa[3] = -qb[0] * qc[3] - qb[3] * qc[0] + qb[1] * qc[2] - qb[2] * qc[1];
+}
+/* dRFrom2Axes, ode/src/rotation.cpp:94-133 (a zero-length input leaves R) */
+static void r_from_2axes(real* R, real ax, real ay, real az, real bx, real by, real bz) {
+  real l = sqrt(ax * ax + ay * ay + az * az);
+  if (l <= 0) return;
+  l = 1 / l;
+  ax *= l; ay *= l; az *= l;
+  real k = ax * bx + ay * by + az * bz;
+  bx -= k * ax; by -= k * ay; bz -= k * az;
+  l = sqrt(bx * bx + by * by + bz * bz);
+  if (l <= 0) return;
+  l = 1 / l;
+  bx *= l; by *= l; bz *= l;
+  R[0] = ax; R[4] = ay; R[8] = az;
+  R[1] = bx; R[5] = by; R[9] = bz;
+  R[2] = -by * az + ay * bz; R[6] = -bz * ax + az * bx; R[10] = -bx * ay + ax * by;
+  R[3] = 0; R[7] = 0; R[11] = 0;
+}
+/* dQfromR, ode/src/rotation.cpp:258-306 */
+static void q_from_r(real* q, const real* R) {
+  real tr = R[0] + R[5] + R[10], s;
+  if (tr >= 0) {
+    s = sqrt(tr + 1);
+    q[0] = 0.5 * s;
+    s = 0.5 * (1 / s);
+    q[1] = (R[9] - R[6]) * s; q[2] = (R[2] - R[8]) * s; q[3] = (R[4] - R[1]) * s;
+    return;
+  }
+  int c;
+  if (R[5] > R[0]) c = (R[10] > R[5]) ? 2 : 1;
+  else c = (R[10] > R[0]) ? 2 : 0;
+  if (c == 0) {
+    s = sqrt((R[0] - (R[5] + R[10])) + 1);
+    q[1] = 0.5 * s;
+    s = 0.5 * (1 / s);
+    q[2] = (R[1] + R[4]) * s; q[3] = (R[8] + R[2]) * s; q[0] = (R[9] - R[6]) * s;
+  } else if (c == 1) {
+    s = sqrt((R[5] - (R[10] + R[0])) + 1);
+    q[2] = 0.5 * s;
+    s = 0.5 * (1 / s);
+    q[3] = (R[6] + R[9]) * s; q[1] = (R[1] + R[4]) * s; q[0] = (R[2] - R[8]) * s;
+  } else {
+    s = sqrt((R[10] - (R[0] + R[5])) + 1);
+    q[3] = 0.5 * s;
+    s = 0.5 * (1 / s);
+    q[1] = (R[8] + R[2]) * s; q[2] = (R[6] + R[9]) * s; q[0] = (R[4] - R[1]) * s;
+  }
 }
 
 /* ------------------------------------------------------------------------ */
@@ -235,6 +288,8 @@ typedef struct {
   real erp, cfm;
   OLimot lm1, lm2;
   real c0, s0, v1[4], v2[4], susp_erp, susp_cfm;
+  real offset[4];    /* slider, fixed */
+  real qrel2[4];     /* universal (qrel holds qrel1) */
   /* contact */
   odegpuSurface surf;
   real cpos[3], cnormal[3], cdepth;
@@ -314,6 +369,49 @@ static void hinge_qrel(OWorld* W, OJoint* J) {
     if (J->b[1] >= 0) qmul1(J->qrel, q1, W->body[J->b[1]].q);
     else { J->qrel[0] = q1[0]; J->qrel[1] = -q1[1]; J->qrel[2] = -q1[2]; J->qrel[3] = -q1[3]; }
   }
+}
+/* dxJointSlider::computeOffset, ode/src/joints/slider.cpp:380-398 */
+static void slider_offset(OWorld* W, OJoint* J) {
+  if (J->b[1] >= 0) {
+    real c[3];
+    for (int i = 0; i < 3; ++i) c[i] = W->body[J->b[0]].pos[i] - W->body[J->b[1]].pos[i];
+    mul1_331(J->offset, W->body[J->b[1]].R, c);
+  } else if (J->b[0] >= 0) {
+    for (int i = 0; i < 3; ++i) J->offset[i] = W->body[J->b[0]].pos[i];
+  }
+}
+/* dJointSetFixed, ode/src/joints/fixed.cpp:110-132 */
+static void fixed_set(OWorld* W, OJoint* J) {
+  if (J->b[0] >= 0) {
+    if (J->b[1] >= 0) {
+      real ofs[3];
+      for (int i = 0; i < 3; ++i) ofs[i] = W->body[J->b[0]].pos[i] - W->body[J->b[1]].pos[i];
+      mul1_331(J->offset, W->body[J->b[0]].R, ofs);
+    } else {
+      for (int i = 0; i < 3; ++i) J->offset[i] = W->body[J->b[0]].pos[i];
+    }
+  }
+  hinge_qrel(W, J);   /* the fixed joint's computeInitialRelativeRotation is the same */
+}
+/* dxJointUniversal::getAxes, ode/src/joints/universal.cpp:55-70 */
+static void universal_axes(OWorld* W, OJoint* J, real* ax1, real* ax2) {
+  mul0_331(ax1, W->body[J->b[0]].R, J->axis1);
+  if (J->b[1] >= 0) mul0_331(ax2, W->body[J->b[1]].R, J->axis2);
+  else { ax2[0] = J->axis2[0]; ax2[1] = J->axis2[1]; ax2[2] = J->axis2[2]; }
+}
+/* dxJointUniversal::computeInitialRelativeRotations, ode/src/joints/universal.cpp:365-393 */
+static void universal_qrels(OWorld* W, OJoint* J) {
+  if (J->b[0] < 0) return;
+  real ax1[3], ax2[3], qcross[4];
+  real R[12] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0};
+  universal_axes(W, J, ax1, ax2);
+  r_from_2axes(R, ax1[0], ax1[1], ax1[2], ax2[0], ax2[1], ax2[2]);
+  q_from_r(qcross, R);
+  qmul1(J->qrel, W->body[J->b[0]].q, qcross);
+  r_from_2axes(R, ax2[0], ax2[1], ax2[2], ax1[0], ax1[1], ax1[2]);
+  q_from_r(qcross, R);
+  if (J->b[1] >= 0) qmul1(J->qrel2, W->body[J->b[1]].q, qcross);
+  else for (int i = 0; i < 4; ++i) J->qrel2[i] = qcross[i];
 }
 /* dxJointHinge2::getAxisInfo / makeV1andV2, ode/src/joints/hinge2.cpp:97-106, :184-210 */
 static void hinge2_axis_info(OWorld* W, OJoint* J, real* ax1, real* ax2, real* axc, real* s, real* c) {
@@ -1661,7 +1759,16 @@ static void set_ball2(OWorld* W, OJoint* J, Info2* info, const real* anchor1, co
   info->c[2] = k * dot3(q2, d);
 }
 
-/* getHingeAngleFromRelativeQuat / getHingeAngle, ode/src/joints/joint.cpp:381-451 */
+/* getHingeAngleFromRelativeQuat, ode/src/joints/joint.cpp:381-420 */
+static real hinge_angle_from_qrel(const real* qrel, const real* axis) {
+  real cost2 = qrel[0];
+  real sint2 = sqrt(qrel[1] * qrel[1] + qrel[2] * qrel[2] + qrel[3] * qrel[3]);
+  real theta = (dot3(qrel + 1, axis) >= 0) ? (2 * atan2(sint2, cost2)) : (2 * atan2(sint2, -cost2));
+  if (theta > R_PI) theta -= (real)(2 * R_PI);
+  theta = -theta;
+  return theta;
+}
+/* getHingeAngle, ode/src/joints/joint.cpp:432-450 */
 static real hinge_angle(OWorld* W, OJoint* J) {
   real qrel[4];
   const real* q1 = W->body[J->b[0]].q;
@@ -1672,12 +1779,7 @@ static real hinge_angle(OWorld* W, OJoint* J) {
   } else {
     qmul3(qrel, q1, J->qrel);
   }
-  real cost2 = qrel[0];
-  real sint2 = sqrt(qrel[1] * qrel[1] + qrel[2] * qrel[2] + qrel[3] * qrel[3]);
-  real theta = (dot3(qrel + 1, J->axis1) >= 0) ? (2 * atan2(sint2, cost2)) : (2 * atan2(sint2, -cost2));
-  if (theta > R_PI) theta -= (real)(2 * R_PI);
-  theta = -theta;
-  return theta;
+  return hinge_angle_from_qrel(qrel, J->axis1);
 }
 
 /* dxJointLimitMotor::testRotationalLimit, ode/src/joints/joint.cpp:534-553 */
@@ -1688,16 +1790,26 @@ static int limot_test(OLimot* L, real angle) {
   return 0;
 }
 
-/* dxJointLimitMotor::addLimot (rotational rows only on this path),
- * ode/src/joints/joint.cpp:556-733 */
-static int limot_add(OWorld* W, OJoint* J, OLimot* L, Info2* info, int row, const real* ax1) {
+/* dxJointLimitMotor::addLimot, ode/src/joints/joint.cpp:556-733. A linear
+ * limot (rotational = 0, the slider's) works on J1l/J2l and, between two
+ * bodies, puts the torque-decoupling vector ltd = (x2 - x1)/2 x ax1 in both
+ * angular parts. */
+static int limot_add(OWorld* W, OJoint* J, OLimot* L, Info2* info, int row, const real* ax1, int rotational) {
   int srow = row * info->rowskip;
   int powered = L->fmax > 0;
   if (!(powered || L->limit)) return 0;
-  real* J1 = info->J1a;
-  real* J2 = info->J2a;
+  real* J1 = rotational ? info->J1a : info->J1l;
+  real* J2 = rotational ? info->J2a : info->J2l;
   J1[srow + 0] = ax1[0]; J1[srow + 1] = ax1[1]; J1[srow + 2] = ax1[2];
   if (J->b[1] >= 0) { J2[srow + 0] = -ax1[0]; J2[srow + 1] = -ax1[1]; J2[srow + 2] = -ax1[2]; }
+  real ltd[3] = {0, 0, 0};
+  if (!rotational && J->b[1] >= 0) {
+    const real* p1 = W->body[J->b[0]].pos;
+    const real* p2 = W->body[J->b[1]].pos;
+    real c[3] = {0.5 * (p2[0] - p1[0]), 0.5 * (p2[1] - p1[1]), 0.5 * (p2[2] - p1[2])};
+    cross3(ltd, c, ax1);
+    for (int k = 0; k < 3; ++k) { info->J1a[srow + k] = ltd[k]; info->J2a[srow + k] = ltd[k]; }
+  }
   if (L->limit && (L->lostop == L->histop)) powered = 0;
   if (powered) {
     info->cfm[row] = L->normal_cfm;
@@ -1710,10 +1822,17 @@ static int limot_add(OWorld* W, OJoint* J, OLimot* L, Info2* info, int row, cons
       if ((L->vel > 0) || (L->vel == 0 && L->limit == 2)) fm = -fm;
       if ((L->limit == 1 && L->vel > 0) || (L->limit == 2 && L->vel < 0)) fm *= L->fudge;
       OBody* B1 = &W->body[J->b[0]];
-      B1->tacc[0] += -fm * ax1[0]; B1->tacc[1] += -fm * ax1[1]; B1->tacc[2] += -fm * ax1[2];
-      if (J->b[1] >= 0) {
-        OBody* B2 = &W->body[J->b[1]];
-        B2->tacc[0] += fm * ax1[0]; B2->tacc[1] += fm * ax1[1]; B2->tacc[2] += fm * ax1[2];
+      OBody* B2 = J->b[1] >= 0 ? &W->body[J->b[1]] : 0;
+      if (rotational) {
+        for (int k = 0; k < 3; ++k) B1->tacc[k] += -fm * ax1[k];
+        if (B2) for (int k = 0; k < 3; ++k) B2->tacc[k] += fm * ax1[k];
+      } else {
+        for (int k = 0; k < 3; ++k) B1->facc[k] += -fm * ax1[k];
+        if (B2) {
+          for (int k = 0; k < 3; ++k) B2->facc[k] += fm * ax1[k];
+          for (int k = 0; k < 3; ++k) B1->tacc[k] += -fm * ltd[k];
+          for (int k = 0; k < 3; ++k) B2->tacc[k] += -fm * ltd[k];
+        }
       }
     }
   }
@@ -1727,8 +1846,14 @@ static int limot_add(OWorld* W, OJoint* J, OLimot* L, Info2* info, int row, cons
       if (L->limit == 1) { info->lo[row] = 0; info->hi[row] = R_INF; }
       else { info->lo[row] = -R_INF; info->hi[row] = 0; }
       if (L->bounce > 0) {
-        real vel = dot3(W->body[J->b[0]].avel, ax1);
-        if (J->b[1] >= 0) vel -= dot3(W->body[J->b[1]].avel, ax1);
+        real vel;
+        if (rotational) {
+          vel = dot3(W->body[J->b[0]].avel, ax1);
+          if (J->b[1] >= 0) vel -= dot3(W->body[J->b[1]].avel, ax1);
+        } else {
+          vel = dot3(W->body[J->b[0]].lvel, ax1);
+          if (J->b[1] >= 0) vel -= dot3(W->body[J->b[1]].lvel, ax1);
+        }
         if (L->limit == 1) {
           if (vel < 0) { real newc = -L->bounce * vel; if (newc > info->c[row]) info->c[row] = newc; }
         } else {
@@ -1738,6 +1863,69 @@ static int limot_add(OWorld* W, OJoint* J, OLimot* L, Info2* info, int row, cons
     }
   }
   return 1;
+}
+
+/* dJointGetSliderPosition, ode/src/joints/slider.cpp:42-79 */
+static real slider_position(OWorld* W, OJoint* J) {
+  real ax1[3], q[3];
+  const OBody* B1 = &W->body[J->b[0]];
+  mul0_331(ax1, B1->R, J->axis1);
+  if (J->b[1] >= 0) {
+    const OBody* B2 = &W->body[J->b[1]];
+    mul0_331(q, B2->R, J->offset);
+    for (int i = 0; i < 3; ++i) q[i] = B1->pos[i] - q[i] - B2->pos[i];
+  } else {
+    for (int i = 0; i < 3; ++i) q[i] = B1->pos[i] - J->offset[i];
+    if (J->reverse) { ax1[0] = -ax1[0]; ax1[1] = -ax1[1]; ax1[2] = -ax1[2]; }
+  }
+  return dot3(ax1, q);
+}
+
+/* dxJointUniversal::getAngles, ode/src/joints/universal.cpp:73-167 */
+static void universal_angles(OWorld* W, OJoint* J, real* angle1, real* angle2) {
+  real ax1[3], ax2[3], qcross[4], qq[4], qrel[4], qcross2[4];
+  real R[12] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0};
+  universal_axes(W, J, ax1, ax2);
+  r_from_2axes(R, ax1[0], ax1[1], ax1[2], ax2[0], ax2[1], ax2[2]);
+  q_from_r(qcross, R);
+  qmul1(qq, W->body[J->b[0]].q, qcross);
+  qmul2(qrel, qq, J->qrel);
+  *angle1 = hinge_angle_from_qrel(qrel, J->axis1);
+  qrel[0] = 0;
+  qrel[1] = ax1[0] + ax2[0];
+  qrel[2] = ax1[1] + ax2[1];
+  qrel[3] = ax1[2] + ax2[2];
+  real l = 1 / sqrt(qrel[1] * qrel[1] + qrel[2] * qrel[2] + qrel[3] * qrel[3]);
+  qrel[1] *= l; qrel[2] *= l; qrel[3] *= l;
+  qmul0(qcross2, qrel, qcross);
+  if (J->b[1] >= 0) {
+    qmul1(qq, W->body[J->b[1]].q, qcross2);
+    qmul2(qrel, qq, J->qrel2);
+  } else {
+    qmul2(qrel, qcross2, J->qrel2);
+  }
+  *angle2 = -hinge_angle_from_qrel(qrel, J->axis2);
+}
+
+/* setFixedOrientation, ode/src/joints/joint.cpp:202-255 */
+static void set_fixed_orientation(OWorld* W, OJoint* J, Info2* info, const real* qrel, int start_row) {
+  int s = info->rowskip, si = start_row * s;
+  info->J1a[si] = 1; info->J1a[si + s + 1] = 1; info->J1a[si + 2 * s + 2] = 1;
+  if (J->b[1] >= 0) { info->J2a[si] = -1; info->J2a[si + s + 1] = -1; info->J2a[si + 2 * s + 2] = -1; }
+  real qerr[4], e[3];
+  if (J->b[1] >= 0) {
+    real qq[4];
+    qmul1(qq, W->body[J->b[0]].q, W->body[J->b[1]].q);
+    qmul2(qerr, qq, qrel);
+  } else {
+    qmul3(qerr, W->body[J->b[0]].q, qrel);
+  }
+  if (qerr[0] < 0) { qerr[1] = -qerr[1]; qerr[2] = -qerr[2]; qerr[3] = -qerr[3]; }
+  mul0_331(e, W->body[J->b[0]].R, qerr + 1);
+  real k = info->fps * info->erp;
+  info->c[start_row] = 2 * k * e[0];
+  info->c[start_row + 1] = 2 * k * e[1];
+  info->c[start_row + 2] = 2 * k * e[2];
 }
 
 /* dxJointHinge2::measureAngle, ode/src/joints/hinge2.cpp:33-41 */
@@ -1790,6 +1978,34 @@ static int joint_info1(OWorld* W, OJoint* J) {
       if (J->lm2.fmax > 0) m++;
       return m;
     }
+    case ODEGPU_JOINT_SLIDER: {
+      /* ode/src/joints/slider.cpp:134-167 */
+      int m = (J->lm1.fmax > 0) ? 6 : 5;
+      J->lm1.limit = 0;
+      if ((J->lm1.lostop > -R_INF || J->lm1.histop < R_INF) && J->lm1.lostop <= J->lm1.histop) {
+        real pos = slider_position(W, J);
+        if (limot_test(&J->lm1, pos)) m = 6;
+      }
+      return m;
+    }
+    case ODEGPU_JOINT_UNIVERSAL: {
+      /* ode/src/joints/universal.cpp:265-293 */
+      int m = 4;
+      int lim1 = (J->lm1.lostop >= -R_PI || J->lm1.histop <= R_PI) && J->lm1.lostop <= J->lm1.histop;
+      int lim2 = (J->lm2.lostop >= -R_PI || J->lm2.histop <= R_PI) && J->lm2.lostop <= J->lm2.histop;
+      J->lm1.limit = 0;
+      J->lm2.limit = 0;
+      if (lim1 || lim2) {
+        real a1, a2;
+        universal_angles(W, J, &a1, &a2);
+        if (lim1) limot_test(&J->lm1, a1);
+        if (lim2) limot_test(&J->lm2, a2);
+      }
+      if (J->lm1.limit || J->lm1.fmax > 0) m++;
+      if (J->lm2.limit || J->lm2.fmax > 0) m++;
+      return m;
+    }
+    case ODEGPU_JOINT_FIXED: return 6;   /* ode/src/joints/fixed.cpp:53-58 */
   }
   return 0;
 }
@@ -1899,7 +2115,7 @@ static void joint_info2(OWorld* W, OJoint* J, Info2* info) {
       real k = info->fps * info->erp;
       info->c[3] = k * dot3(b, p);
       info->c[4] = k * dot3(b, q);
-      limot_add(W, J, &J->lm1, info, 5, ax1);
+      limot_add(W, J, &J->lm1, info, 5, ax1, 1);
       break;
     }
     case ODEGPU_JOINT_HINGE2: {
@@ -1912,9 +2128,90 @@ static void joint_info2(OWorld* W, OJoint* J, Info2* info) {
       if (J->b[1] >= 0) { info->J2a[s3 + 0] = -q[0]; info->J2a[s3 + 1] = -q[1]; info->J2a[s3 + 2] = -q[2]; }
       real k = info->fps * info->erp;
       info->c[3] = k * (J->c0 * sn - J->s0 * cs);
-      int row = 4 + limot_add(W, J, &J->lm1, info, 4, ax1);
-      limot_add(W, J, &J->lm2, info, row, ax2);
+      int row = 4 + limot_add(W, J, &J->lm1, info, 4, ax1, 1);
+      limot_add(W, J, &J->lm2, info, row, ax2, 1);
       info->cfm[0] = J->susp_cfm;
+      break;
+    }
+    case ODEGPU_JOINT_SLIDER: {
+      /* ode/src/joints/slider.cpp:171-246 */
+      int s3 = 3 * s, s4 = 4 * s;
+      OBody* B1 = &W->body[J->b[0]];
+      OBody* B2 = J->b[1] >= 0 ? &W->body[J->b[1]] : 0;
+      real c[3] = {0, 0, 0};
+      if (B2) for (int i = 0; i < 3; ++i) c[i] = B2->pos[i] - B1->pos[i];
+      set_fixed_orientation(W, J, info, J->qrel, 0);
+      real ax1[3], p[3], q[3];
+      mul0_331(ax1, B1->R, J->axis1);
+      plane_space(ax1, p, q);
+      if (B2) {
+        real t[3];
+        cross3(t, c, p);
+        for (int i = 0; i < 3; ++i) t[i] *= 0.5;
+        for (int i = 0; i < 3; ++i) { info->J1a[s3 + i] = t[i]; info->J2a[s3 + i] = t[i]; }
+        cross3(t, c, q);
+        for (int i = 0; i < 3; ++i) t[i] *= 0.5;
+        for (int i = 0; i < 3; ++i) { info->J1a[s4 + i] = t[i]; info->J2a[s4 + i] = t[i]; }
+        for (int i = 0; i < 3; ++i) { info->J2l[s3 + i] = -p[i]; info->J2l[s4 + i] = -q[i]; }
+      }
+      for (int i = 0; i < 3; ++i) { info->J1l[s3 + i] = p[i]; info->J1l[s4 + i] = q[i]; }
+      real k = info->fps * info->erp;
+      if (B2) {
+        real ofs[3];
+        mul0_331(ofs, B2->R, J->offset);
+        for (int i = 0; i < 3; ++i) c[i] += ofs[i];
+        info->c[3] = k * dot3(p, c);
+        info->c[4] = k * dot3(q, c);
+      } else {
+        real ofs[3];
+        for (int i = 0; i < 3; ++i) ofs[i] = J->offset[i] - B1->pos[i];
+        info->c[3] = k * dot3(p, ofs);
+        info->c[4] = k * dot3(q, ofs);
+        if (J->reverse) { ax1[0] = -ax1[0]; ax1[1] = -ax1[1]; ax1[2] = -ax1[2]; }
+      }
+      limot_add(W, J, &J->lm1, info, 5, ax1, 0);
+      break;
+    }
+    case ODEGPU_JOINT_UNIVERSAL: {
+      /* ode/src/joints/universal.cpp:296-362 */
+      set_ball(W, J, info, J->anchor1, J->anchor2);
+      real ax1[3], ax2[3], t[3], p[3];
+      universal_axes(W, J, ax1, ax2);
+      real k = dot3(ax1, ax2);
+      t[0] = ax2[0] - k * ax1[0];
+      t[1] = ax2[1] - k * ax1[1];
+      t[2] = ax2[2] - k * ax1[2];
+      cross3(p, ax1, t);
+      safe_normalize3(p);
+      int s3 = 3 * s;
+      for (int i = 0; i < 3; ++i) info->J1a[s3 + i] = p[i];
+      if (J->b[1] >= 0) for (int i = 0; i < 3; ++i) info->J2a[s3 + i] = -p[i];
+      info->c[3] = info->fps * info->erp * -k;
+      int row = 4 + limot_add(W, J, &J->lm1, info, 4, ax1, 1);
+      limot_add(W, J, &J->lm2, info, row, ax2, 1);
+      break;
+    }
+    case ODEGPU_JOINT_FIXED: {
+      /* ode/src/joints/fixed.cpp:62-105: the orientation rows use the erp
+       * the joint finds in info, then info->erp becomes the joint's own */
+      OBody* B1 = &W->body[J->b[0]];
+      OBody* B2 = J->b[1] >= 0 ? &W->body[J->b[1]] : 0;
+      set_fixed_orientation(W, J, info, J->qrel, 3);
+      info->J1l[0] = 1; info->J1l[s + 1] = 1; info->J1l[2 * s + 2] = 1;
+      info->erp = J->erp;
+      info->cfm[0] = J->cfm; info->cfm[1] = J->cfm; info->cfm[2] = J->cfm;
+      real ofs[3];
+      mul0_331(ofs, B1->R, J->offset);
+      if (B2) {
+        /* dSetCrossMatrixPlus(J1a, ofs, s) */
+        info->J1a[1] = -ofs[2]; info->J1a[2] = +ofs[1];
+        info->J1a[s + 0] = +ofs[2]; info->J1a[s + 2] = -ofs[0];
+        info->J1a[2 * s + 0] = -ofs[1]; info->J1a[2 * s + 1] = +ofs[0];
+        info->J2l[0] = -1; info->J2l[s + 1] = -1; info->J2l[2 * s + 2] = -1;
+      }
+      real k = info->fps * info->erp;
+      if (B2) for (int j = 0; j < 3; ++j) info->c[j] = k * (B2->pos[j] - B1->pos[j] + ofs[j]);
+      else for (int j = 0; j < 3; ++j) info->c[j] = k * (J->offset[j] - B1->pos[j]);
       break;
     }
   }
@@ -2391,6 +2688,44 @@ static void world_init(OWorld* W, const odegpuScene* sc, int w) {
         J->susp_cfm = jp[19];
         break;
       }
+      case ODEGPU_JOINT_SLIDER:
+        /* dJointCreateSlider, dJointAttach (setRelativeValues, overwritten
+         * next), dJointSetSliderAxis (ode/src/joints/slider.cpp:250-258) */
+        J->axis1[0] = 1;
+        limot_init(&J->lm1, W);
+        joint_attach(W, jj, jb1, jb2);
+        set_axes(W, J, x1[0], x1[1], x1[2], J->axis1, 0);
+        slider_offset(W, J);
+        hinge_qrel(W, J);
+        limot_set_all(&J->lm1, jp);
+        break;
+      case ODEGPU_JOINT_UNIVERSAL:
+        /* dJointCreateUniversal, dJointAttach (setRelativeValues, overwritten
+         * next), dJointSetUniversalAnchor / Axis1 / Axis2
+         * (ode/src/joints/universal.cpp:396-490); on a reversed joint the
+         * API's axis 1 is the second body axis and the other way round */
+        J->axis1[0] = 1; J->axis2[1] = 1;
+        limot_init(&J->lm1, W);
+        limot_init(&J->lm2, W);
+        joint_attach(W, jj, jb1, jb2);
+        set_anchors(W, J, a[0], a[1], a[2], J->anchor1, J->anchor2);
+        universal_qrels(W, J);
+        if (J->reverse) set_axes(W, J, x1[0], x1[1], x1[2], 0, J->axis2);
+        else set_axes(W, J, x1[0], x1[1], x1[2], J->axis1, 0);
+        universal_qrels(W, J);
+        if (J->reverse) set_axes(W, J, x2[0], x2[1], x2[2], J->axis1, 0);
+        else set_axes(W, J, x2[0], x2[1], x2[2], 0, J->axis2);
+        universal_qrels(W, J);
+        limot_set_all(&J->lm1, jp);
+        limot_set_all(&J->lm2, jp + 9);
+        break;
+      case ODEGPU_JOINT_FIXED:
+        /* dJointCreateFixed, dJointAttach, dJointSetFixed, dJointSetFixedParam */
+        J->erp = W->erp; J->cfm = W->cfm;
+        joint_attach(W, jj, jb1, jb2);
+        fixed_set(W, J);
+        J->erp = jp[0]; J->cfm = jp[1];
+        break;
       default: break;
     }
   }
@@ -2515,11 +2850,12 @@ static int world_step(OWorld* W, int s, double* contacts, int max_rec) {
     const int cs = s % sc->n_ctrl_steps;
     const int j0 = sc->joint_off[W->w], b0 = sc->body_off[W->w];
     if (sc->joint_stop) {
-      /* dJointSetHinge{,2}Param(dParamLoStop / dParamHiStop): plain
+      /* dJointSet{Hinge,Hinge2,Slider,Universal}Param(dParamLoStop / dParamHiStop): plain
        * assignment (dxJointLimitMotor::set, ode/src/joints/joint.cpp:471-503) */
       for (int i = 0; i < W->nj_persist; ++i) {
         OJoint* J = &W->joint[i];
-        if (J->type != ODEGPU_JOINT_HINGE && J->type != ODEGPU_JOINT_HINGE2) continue;
+        if (J->type != ODEGPU_JOINT_HINGE && J->type != ODEGPU_JOINT_HINGE2 &&
+            J->type != ODEGPU_JOINT_SLIDER && J->type != ODEGPU_JOINT_UNIVERSAL) continue;
         const double v = sc->joint_stop[(size_t)cs * sc->joint_off[sc->n_worlds] + j0 + i];
         const double* jp = sc->joint_param + (size_t)(j0 + i) * ODEGPU_JOINT_NPARAM;
         J->lm1.lostop = isnan(v) ? jp[0] : v;
@@ -2558,6 +2894,41 @@ static int world_step(OWorld* W, int s, double* contacts, int max_rec) {
             OBody* B2 = &W->body[J->b[1]];
             B1->tacc[0] += a1[0]; B1->tacc[1] += a1[1]; B1->tacc[2] += a1[2];
             B2->tacc[0] += -a1[0]; B2->tacc[1] += -a1[1]; B2->tacc[2] += -a1[2];
+          }
+        } else if (J->type == ODEGPU_JOINT_SLIDER) {
+          /* dJointAddSliderForce, ode/src/joints/slider.cpp:305-342 (a
+           * reversed joint computes force -= force, i.e. zero) */
+          real force = t[0];
+          if (J->reverse) force -= force;
+          if (J->b[0] >= 0) {
+            OBody* B1 = &W->body[J->b[0]];
+            real ax[3];
+            mul0_331(ax, B1->R, J->axis1);
+            ax[0] *= force; ax[1] *= force; ax[2] *= force;
+            B1->facc[0] += ax[0]; B1->facc[1] += ax[1]; B1->facc[2] += ax[2];
+            if (J->b[1] >= 0) {
+              OBody* B2 = &W->body[J->b[1]];
+              B2->facc[0] += -ax[0]; B2->facc[1] += -ax[1]; B2->facc[2] += -ax[2];
+              real c[3], ltd[3];
+              for (int k = 0; k < 3; ++k) c[k] = 0.5 * (B2->pos[k] - B1->pos[k]);
+              cross3(ltd, c, ax);
+              for (int k = 0; k < 3; ++k) { B1->tacc[k] += ltd[k]; B2->tacc[k] += ltd[k]; }
+            }
+          }
+        } else if (J->type == ODEGPU_JOINT_UNIVERSAL) {
+          /* dJointAddUniversalTorques, ode/src/joints/universal.cpp:729-754 */
+          real t1 = t[0], t2 = t[1];
+          if (J->reverse) { real tmp = t1; t1 = -t2; t2 = -tmp; }
+          if (J->b[0] >= 0) {
+            real a1[3], a2[3];
+            universal_axes(W, J, a1, a2);
+            for (int k = 0; k < 3; ++k) a1[k] = a1[k] * t1 + a2[k] * t2;
+            OBody* B1 = &W->body[J->b[0]];
+            B1->tacc[0] += a1[0]; B1->tacc[1] += a1[1]; B1->tacc[2] += a1[2];
+            if (J->b[1] >= 0) {
+              OBody* B2 = &W->body[J->b[1]];
+              B2->tacc[0] += -a1[0]; B2->tacc[1] += -a1[1]; B2->tacc[2] += -a1[2];
+            }
           }
         }
       }

@@ -11,7 +11,8 @@
  *      ode.cpp:1529, as ODE's demos do in their near-callbacks)
  *   2. dJointCreateContact + dJointAttach(body(gi), body(gj)) per contact
  *      (ode.cpp:1201, :1348)
- *   3. per-step controls via dJointAddHingeTorque / dJointAddHinge2Torques /
+ *   3. per-step controls via dJointAdd{Hinge,Hinge2,Universal}Torque(s) /
+ *      dJointAddSliderForce /
  *      dBodyAddForce / dBodyAddTorque
  *   4. dWorldQuickStep (ode.cpp:1807)
  *   5. dJointGroupEmpty (ode.cpp:1305)
@@ -173,6 +174,28 @@ int ref_run_world(const odegpuScene* sc, int w, int n_steps, double* state,
         dJointSetHinge2Param(j, dParamSuspensionERP, jp[18]);
         dJointSetHinge2Param(j, dParamSuspensionCFM, jp[19]);
         break;
+      case ODEGPU_JOINT_SLIDER:
+        j = dJointCreateSlider(world, 0);
+        dJointAttach(j, B1, B2);
+        dJointSetSliderAxis(j, x1[0], x1[1], x1[2]);
+        set_limot(j, 0, jp, dJointSetSliderParam);
+        break;
+      case ODEGPU_JOINT_UNIVERSAL:
+        j = dJointCreateUniversal(world, 0);
+        dJointAttach(j, B1, B2);
+        dJointSetUniversalAnchor(j, a[0], a[1], a[2]);
+        dJointSetUniversalAxis1(j, x1[0], x1[1], x1[2]);
+        dJointSetUniversalAxis2(j, x2[0], x2[1], x2[2]);
+        set_limot(j, 0, jp, dJointSetUniversalParam);
+        set_limot(j, 1, jp + 9, dJointSetUniversalParam);
+        break;
+      case ODEGPU_JOINT_FIXED:
+        j = dJointCreateFixed(world, 0);
+        dJointAttach(j, B1, B2);
+        dJointSetFixed(j);
+        dJointSetFixedParam(j, dParamERP, jp[0]);
+        dJointSetFixedParam(j, dParamCFM, jp[1]);
+        break;
       default: break;
     }
     joints[i] = j;
@@ -236,25 +259,27 @@ int ref_run_world(const odegpuScene* sc, int w, int n_steps, double* state,
       if (sc->joint_stop) {
         for (int i = 0; i < nj; ++i) {
           const int t = sc->joint_type[j0 + i];
-          if (t != ODEGPU_JOINT_HINGE && t != ODEGPU_JOINT_HINGE2) continue;
+          void (*setp)(dJointID, int, dReal) = 0;
+          if (t == ODEGPU_JOINT_HINGE) setp = dJointSetHingeParam;
+          else if (t == ODEGPU_JOINT_HINGE2) setp = dJointSetHinge2Param;
+          else if (t == ODEGPU_JOINT_SLIDER) setp = dJointSetSliderParam;
+          else if (t == ODEGPU_JOINT_UNIVERSAL) setp = dJointSetUniversalParam;
+          if (!setp) continue;
           const double v = sc->joint_stop[(size_t)cs * sc->joint_off[sc->n_worlds] + j0 + i];
           const double* jp = sc->joint_param + (size_t)(j0 + i) * ODEGPU_JOINT_NPARAM;
           const double lo = std::isnan(v) ? jp[0] : v, hi = std::isnan(v) ? jp[1] : v;
-          if (t == ODEGPU_JOINT_HINGE) {
-            dJointSetHingeParam(joints[i], dParamLoStop, lo);
-            dJointSetHingeParam(joints[i], dParamHiStop, hi);
-          } else {
-            dJointSetHinge2Param(joints[i], dParamLoStop, lo);
-            dJointSetHinge2Param(joints[i], dParamHiStop, hi);
-          }
+          setp(joints[i], dParamLoStop, lo);
+          setp(joints[i], dParamHiStop, hi);
         }
       }
       if (sc->joint_torque) {
         for (int i = 0; i < nj; ++i) {
           const double* t = sc->joint_torque + ((size_t)cs * sc->joint_off[sc->n_worlds] + j0 + i) * 2;
-          if (sc->joint_type[j0 + i] == ODEGPU_JOINT_HINGE) dJointAddHingeTorque(joints[i], t[0]);
-          else if (sc->joint_type[j0 + i] == ODEGPU_JOINT_HINGE2)
-            dJointAddHinge2Torques(joints[i], t[0], t[1]);
+          const int jt = sc->joint_type[j0 + i];
+          if (jt == ODEGPU_JOINT_HINGE) dJointAddHingeTorque(joints[i], t[0]);
+          else if (jt == ODEGPU_JOINT_HINGE2) dJointAddHinge2Torques(joints[i], t[0], t[1]);
+          else if (jt == ODEGPU_JOINT_SLIDER) dJointAddSliderForce(joints[i], t[0]);
+          else if (jt == ODEGPU_JOINT_UNIVERSAL) dJointAddUniversalTorques(joints[i], t[0], t[1]);
         }
       }
       if (sc->body_force) {

@@ -30,6 +30,7 @@ SCENES = {
     "capsule": (lambda: S.capsule_mix(seed=6), 80),
     "vehicles": (lambda: S.vehicles(n_worlds=3, steps=60, hf_samples=64), 60),
     "capsule_pile": (lambda: S.capsule_pile(), 120),
+    "mechanisms": (lambda: S.mechanisms(n_worlds=3, steps=80), 80),
 }
 KEEP = 10  # keep the state every KEEP steps
 
@@ -185,6 +186,12 @@ def make_rng_kat():
 
 if __name__ == "__main__":
     assert O.ref_available("d"), "build the reference first: make -C oracle ref"
+    only = sys.argv[1:]
+    if only:
+        for name in only:
+            make_scene(name)
+            print("wrote", name)
+        sys.exit(0)
     for name in SCENES:
         make_scene(name)
         print("wrote", name)

@@ -34,13 +34,18 @@ def _scenes():
         "tower": S.box_tower(n_worlds=6, yaw=0.0, spacing=0.0),
         "capsule": S.capsule_mix(seed=6),
         "capsule_pile": S.capsule_pile(),
+        # slider (to the environment, reversed, body-body with motor / limits /
+        # servo stops), universal, fixed (body-body and reversed) joints with
+        # ball / fixed erp carried along an island
+        "mechanisms": S.mechanisms(n_worlds=16, steps=40),
         # aligned equal boxes: exact SAT ties between parallel faces, which FP32
         # and FP64 break differently (ODE's own FP32 build drifts mm here)
         "stack": S.box_stack(n_worlds=4, height=5),
     }
 
 
-@pytest.mark.parametrize("name", ["box_drop", "batched", "hinge", "tower", "capsule", "capsule_pile"])
+@pytest.mark.parametrize("name", ["box_drop", "batched", "hinge", "tower", "capsule", "capsule_pile",
+                                  "mechanisms"])
 def test_one_step_from_oracle_state(batch_cls, name):
     sc = _scenes()[name]
     n = 40
@@ -88,7 +93,7 @@ def test_degenerate_stack_integer_parity(batch_cls):
         assert e["lvel"] < 1e-2 and e["avel"] < 1e-2, e
 
 
-@pytest.mark.parametrize("name", ["batched", "hinge", "box_drop", "tower"])
+@pytest.mark.parametrize("name", ["batched", "hinge", "box_drop", "tower", "mechanisms"])
 def test_rows_and_lambda_tap(batch_cls, name):
     """Row assembly (getInfo2 + rhs + cfm) and SOR lambda per world vs the oracle
     taps, from the same starting state."""
@@ -185,7 +190,7 @@ def test_launch_modes_agree(batch_cls):
     assert np.array_equal(outs[0], outs[2])
 
 
-@pytest.mark.parametrize("name", ["hinge", "batched"])
+@pytest.mark.parametrize("name", ["hinge", "batched", "mechanisms"])
 def test_joint_feedback_one_step(batch_cls, name):
     """dJointFeedback of every persistent joint (quickstep.cpp:918-957): one
     GPU step from the oracle's state against the oracle's feedback of that

@@ -98,7 +98,8 @@ def test_heightfield_kats_golden():
     assert (g["nc"] > 0).sum() > n // 2
 
 
-@pytest.mark.parametrize("name", ["box_drop", "batched", "hinge", "stack", "capsule", "vehicles", "capsule_pile"])
+@pytest.mark.parametrize("name", ["box_drop", "batched", "hinge", "stack", "capsule", "vehicles", "capsule_pile",
+                                  "mechanisms"])
 def test_oracle_matches_reference_golden(name):
     """Whole-step parity: contact counts, contact records, RNG seeds, body
     states and joint feedback are bit-identical to the reference (FP64)."""
