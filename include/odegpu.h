@@ -35,12 +35,22 @@ enum {
   ODEGPU_ST_NONFINITE = 8,
   /* a geom covered more than 10 x 10 heightfield samples (the collider's
      buffer); that pair produced no contacts in the step */
-  ODEGPU_ST_HF_ZONE = 32
+  ODEGPU_ST_HF_ZONE = 32,
+  /* large world: a geom had more than 64 candidate partners, or the
+     candidate pairs exceeded the batch's pair capacity; pairs were dropped */
+  ODEGPU_ST_PAIR_OVERFLOW = 64,
+  /* large world: a wait of the constraint sweep gave up (bounded); the step's
+     constraint forces are incomplete */
+  ODEGPU_ST_SOLVE_STALL = 128
 };
 
-/* Size limits of the on-chip step kernel: bodies and constraint rows per world. */
+/* Size limits of the on-chip step kernel: bodies and constraint rows per
+ * world. A batch with a single world may exceed them: that world is stepped
+ * by the large-world pipeline (every kernel spread over the GPU), up to
+ * ODEGPU_MAX_BODIES_LARGE bodies. */
 #define ODEGPU_MAX_BODIES_PER_WORLD 64
 #define ODEGPU_MAX_ROWS_PER_WORLD 1024
+#define ODEGPU_MAX_BODIES_LARGE 65536
 
 typedef struct odegpuBatch* odegpuBatchID;
 
@@ -48,6 +58,8 @@ typedef struct odegpuBatchConfig {
   int contacts_per_body;   /* contact capacity per world = this * nb + 16 (0 -> 8) */
   int warps_per_block;     /* 0 -> chosen by the library                          */
   int device;              /* CUDA device ordinal                                 */
+  int large_world;         /* 1: step the batch's single world with the large-world
+                              pipeline even when it fits the on-chip kernel     */
 } odegpuBatchConfig;
 
 /* Body state record used by the read/write calls: pos[3] q[4] lvel[3] avel[3]. */

@@ -13,6 +13,7 @@
 #include "engine_types.cuh"
 #include "world_solve.cuh"
 #include "adjoint.cuh"
+#include "large_world.cuh"
 #include "engine_internal.hpp"
 #include "host_setup.hpp"
 
@@ -126,6 +127,24 @@ struct DBuf {
   }
 };
 
+// Buffers of the large-world pipeline (large_world.cuh), sized at creation.
+struct LargeWorld {
+  LWDev L{};
+  DBuf<int> statics, ghash, hcount, hfill, hgeoms, plist, pcnt, own, sflag, pair_i, pair_k, npairs, pnc;
+  DBuf<Contact> staged;
+  DBuf<int> ccount, acount, afill, adj_joint, adj_other, jentry, jlist, istart, nj, stack;
+  DBuf<unsigned char> bflag;
+  DBuf<int> jm, bfk, rstart;
+  DBuf<float> tmp1;
+  DBuf<int> rowisl, neg, draws, order, order2, rnd, tcount, tfill, tlist, bcount, bfill, blist;
+  DBuf<int4> prec;
+  DBuf<float> lambda, fc;
+  DBuf<int> err;
+  int sweep_smem = 0, islands_smem = 0;
+};
+
+constexpr int kLwIslandsSmem = 227 * 1024;
+
 }  // namespace
 
 struct odegpuBatch {
@@ -189,6 +208,7 @@ struct odegpuBatch {
   }
 
   DBuf<int> order;   // worlds by decreasing size (launch slot -> world)
+  LargeWorld* lw = nullptr;           // set when the batch is one world above the on-chip limits
 
   long long launches = 0;             // kernels launched by this batch
   // Optional per-kernel timing: 4 events per step on the batch stream
@@ -210,6 +230,7 @@ struct odegpuBatch {
   }
   ~odegpuBatch() {
     for (cudaEvent_t e : ev_pool) cudaEventDestroy(e);
+    delete lw;
   }
 
   // Rollout record for the adjoint: state and RNG seeds every `ckpt` steps
@@ -271,7 +292,130 @@ struct odegpuBatch {
       cudaGetLastError();
   }
 
+  // Steps of the large world (large_world.cuh): ~30 launches plus ~11 per
+  // reshuffle round, all on the batch stream (capturable into a graph).
+  int lw_launch(int n_steps, const StepOptions& opt) {
+    LargeWorld& W = *lw;
+    const BatchDev d = dev();
+    const WorldDesc& D = h_world[0];
+    const LWDev L0 = W.L;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    cudaStreamIsCapturing(stream, &cap);
+    const bool tm = timing && cap == cudaStreamCaptureStatusNone;
+    auto g = [](long long n, int t) { return (unsigned)std::max(1LL, (n + t - 1) / t); };
+    const int T = 256;
+    const int nb = L0.nb, ng = L0.ng, njall = L0.njp + L0.contact_cap, R = L0.row_cap;
+    auto scan = [&](int* a, const int* n_dev, int n_host, int rows = 1, size_t stride = 0) {
+      lw_scan_kernel<<<rows, kLwScanThreads, 0, stream>>>(a, n_dev, n_host, stride);
+      ++launches;
+    };
+    const bool joint_ctl = !opt.host_forces && n_ctrl_steps > 0 && joint_torque.p && D.njp > 0;
+    for (int s = 0; s < n_steps; ++s) {
+      const int step = step_counter + s;
+      mark(tm);
+      cudaMemsetAsync(L0.err, 0, sizeof(int), stream);
+      if (joint_ctl) {
+        lw_bodies_pre_kernel<<<g(nb, T), T, 0, stream>>>(d, step, 1, 0);
+        lw_controls_joints_kernel<<<1, 32, 0, stream>>>(d, step);
+        lw_bodies_pre_kernel<<<g(nb, T), T, 0, stream>>>(d, step, 0, 1);
+        launches += 3;
+      } else {
+        lw_bodies_pre_kernel<<<g(nb, T), T, 0, stream>>>(d, step, opt.host_forces ? 0 : 1, 1);
+        launches += 1;
+      }
+      // broadphase + narrowphase in canonical pair order
+      cudaMemsetAsync(L0.hcount, 0, sizeof(int) * (L0.hsize + 1), stream);
+      cudaMemsetAsync(L0.hfill, 0, sizeof(int) * L0.hsize, stream);
+      if (L0.nstat) cudaMemsetAsync(L0.sflag, 0, sizeof(int) * (size_t)L0.nstat * (ng + 1), stream);
+      cudaMemsetAsync(L0.ccount, 0, sizeof(int) * nb, stream);
+      cudaMemsetAsync(L0.afill, 0, sizeof(int) * nb, stream);
+      lw_hash_kernel<<<g(ng, T), T, 0, stream>>>(d, L0);
+      scan(L0.hcount, nullptr, L0.hsize);
+      lw_hfill_kernel<<<g(ng, T), T, 0, stream>>>(L0);
+      lw_candidates_kernel<<<g(ng, 128), 128, 0, stream>>>(d, L0);
+      launches += 3;
+      if (L0.nstat) {
+        scan(L0.sflag, nullptr, ng, L0.nstat, (size_t)ng + 1);
+        lw_static_own_kernel<<<1, 32, 0, stream>>>(L0);
+        ++launches;
+      }
+      scan(L0.own, nullptr, ng);
+      lw_pairs_fill_kernel<<<g(ng, T), T, 0, stream>>>(d, L0);
+      lw_narrow_kernel<<<g(L0.pair_cap, 128), 128, 0, stream>>>(d, L0);
+      scan(L0.pnc, L0.npairs, 0);
+      lw_contacts_kernel<<<g(L0.pair_cap, T), T, 0, stream>>>(d, L0);
+      launches += 3;
+      mark(tm);
+      // body joint lists, islands, rows
+      lw_adj_count_kernel<<<g(nb, T), T, 0, stream>>>(d, L0);
+      scan(L0.acount, nullptr, nb);
+      lw_adj_fill_kernel<<<g(L0.contact_cap, T), T, 0, stream>>>(d, L0);
+      lw_adj_finish_kernel<<<g(nb, T), T, 0, stream>>>(d, L0);
+      lw_islands_kernel<<<1, 32, W.islands_smem, stream>>>(d, L0, W.islands_smem);
+      lw_info1_kernel<<<g(njall, 128), 128, 0, stream>>>(d, L0, step);
+      launches += 5;
+      scan(L0.jm, L0.nj, 0);
+      lw_max_scan_kernel<<<1, kLwScanThreads, 0, stream>>>(L0.bfk, L0.nj);
+      lw_info2_kernel<<<g(njall, 128), 128, 0, stream>>>(d, L0, step);
+      lw_tmp1_kernel<<<g(nb, T), T, 0, stream>>>(d, L0);
+      lw_row_setup_kernel<<<g(R, T), T, 0, stream>>>(d, L0);
+      launches += 4;
+      mark(tm);
+      // SOR: initial order, then per reshuffle round the exact permutation,
+      // the per-body ranks and the cluster sweep of up to 8 iterations
+      lw_order_flags_kernel<<<g(std::max(R, nb), T), T, 0, stream>>>(d, L0);
+      ++launches;
+      scan(L0.neg, d.nrows, 0);
+      scan(L0.draws, d.nislands, 0);
+      lw_order_init_kernel<<<g(R, T), T, 0, stream>>>(d, L0);
+      ++launches;
+      int* cur = L0.order;
+      int* nxt = L0.order2;
+      const int iters = D.iterations;
+      for (int round = 0; round * 8 < iters; ++round) {
+        cudaMemsetAsync(L0.tcount, 0, sizeof(int) * (R + 1), stream);
+        cudaMemsetAsync(L0.tfill, 0, sizeof(int) * R, stream);
+        cudaMemsetAsync(L0.bcount, 0, sizeof(int) * (nb + 1), stream);
+        cudaMemsetAsync(L0.bfill, 0, sizeof(int) * nb, stream);
+        lw_rand_kernel<<<g(R, T), T, 0, stream>>>(d, L0, round);
+        scan(L0.tcount, d.nrows, 0);
+        lw_tfill_kernel<<<g(R, T), T, 0, stream>>>(d, L0);
+        lw_tsort_kernel<<<g(R, T), T, 0, stream>>>(d, L0);
+        lw_permute_kernel<<<g(R, T), T, 0, stream>>>(d, L0, cur, nxt);
+        std::swap(cur, nxt);
+        lw_bodypos_kernel<<<g(R, T), T, 0, stream>>>(d, L0, cur);
+        scan(L0.bcount, nullptr, nb);
+        lw_bfill_kernel<<<g(R, T), T, 0, stream>>>(d, L0, cur);
+        lw_branks_kernel<<<g(nb, T), T, 0, stream>>>(d, L0, cur);
+        launches += 7;
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3((unsigned)L0.cluster);
+        cfg.blockDim = dim3(kLwSweepThreads);
+        cfg.dynamicSmemBytes = (size_t)W.sweep_smem;
+        cfg.stream = stream;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = (unsigned)L0.cluster;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        const int it1 = std::min(iters, 8 * round + 8);
+        cudaError_t e = cudaLaunchKernelEx(&cfg, lw_sweep_kernel, d, L0, 8 * round, it1, round == 0 ? 1 : 0);
+        if (e != cudaSuccess) return fail(ODEGPU_E_CUDA, std::string("sweep launch: ") + cudaGetErrorString(e));
+        ++launches;
+      }
+      lw_integrate_kernel<<<g(nb, T), T, 0, stream>>>(d, L0);
+      ++launches;
+      mark(tm);
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(ODEGPU_E_CUDA, std::string("large-world step: ") + cudaGetErrorString(e));
+    return 0;
+  }
+
   int launch(int first, int count, int n_steps, const StepOptions& opt_in, bool use_order = true) {
+    if (lw) return lw_launch(n_steps, opt_in);
     StepOptions opt = opt_in;
     if (feedback_on) { opt.jcopy = jcopy.p; opt.feedback = feedback.p; }
     const BatchDev d = dev();
@@ -359,6 +503,127 @@ static int set_controls(odegpuBatch* B, int n_ctrl, const double* jt, const doub
   if (B->body_force.p) { cudaFree(B->body_force.p); B->body_force.p = nullptr; }
   if (jt) { if (int rc = B->joint_torque.upload(t)) return rc; }
   if (bf) { if (int rc = B->body_force.upload(f)) return rc; }
+  return 0;
+}
+
+// Buffers and launch shapes of the large-world pipeline for the batch's only world.
+static int lw_setup(odegpuBatch* B, const odegpuScene* sc) {
+  LargeWorld& W = *B->lw;
+  const WorldDesc& D = B->h_world[0];
+  LWDev& L = W.L;
+  L.nb = D.nb; L.ng = D.ng; L.njp = D.njp;
+  L.contact_cap = D.contact_cap;
+  L.row_cap = D.row_cap;
+  L.pair_cap = 16 * D.ng + 1024;
+  L.adj_cap = 2 * (D.njp + D.contact_cap);
+  int hs = 1024;
+  while (hs < 2 * D.ng) hs <<= 1;
+  L.hsize = hs;
+  // grid cell: at least the widest pair pre-test between two geoms on bodies
+  double rmax = 0;
+  std::vector<int> st;
+  for (int g = 0; g < D.ng; ++g) {
+    const int gg = D.geom_off + g;
+    if (sc->geom_body[gg] < 0) { st.push_back(g); continue; }
+    rmax = std::max(rmax, (double)bound_radius(sc->geom_type[gg], sc->geom_param + ODEGPU_GEOM_NPARAM * (size_t)gg));
+  }
+  const double cell = rmax > 0 ? 1.01 * (2.0 * rmax * 1.001 + 1e-5) : 1.0;
+  L.cell = (float)cell;
+  L.inv_cell = (float)(1.0 / cell);
+  L.nstat = (int)st.size();
+  const int nb = D.nb, ng = D.ng, R = D.row_cap, njall = D.njp + D.contact_cap;
+  int rc = 0;
+  rc = rc ? rc : W.statics.upload(st.empty() ? std::vector<int>{0} : st);
+  rc = rc ? rc : W.ghash.alloc(ng);
+  rc = rc ? rc : W.hcount.alloc((size_t)hs + 1);
+  rc = rc ? rc : W.hfill.alloc(hs);
+  rc = rc ? rc : W.hgeoms.alloc(ng);
+  rc = rc ? rc : W.plist.alloc((size_t)ng * kLwPartners);
+  rc = rc ? rc : W.pcnt.alloc(ng);
+  rc = rc ? rc : W.own.alloc((size_t)ng + 1);
+  rc = rc ? rc : W.sflag.alloc((size_t)std::max(1, L.nstat) * (ng + 1));
+  rc = rc ? rc : W.pair_i.alloc(L.pair_cap);
+  rc = rc ? rc : W.pair_k.alloc(L.pair_cap);
+  rc = rc ? rc : W.npairs.alloc(1);
+  rc = rc ? rc : W.pnc.alloc((size_t)L.pair_cap + 1);
+  rc = rc ? rc : W.staged.alloc((size_t)L.pair_cap * D.max_contacts);
+  rc = rc ? rc : W.ccount.alloc(nb);
+  rc = rc ? rc : W.acount.alloc((size_t)nb + 1);
+  rc = rc ? rc : W.afill.alloc(nb);
+  rc = rc ? rc : W.adj_joint.alloc(L.adj_cap);
+  rc = rc ? rc : W.adj_other.alloc(L.adj_cap);
+  rc = rc ? rc : W.jentry.alloc(njall);
+  rc = rc ? rc : W.jlist.alloc(njall);
+  rc = rc ? rc : W.istart.alloc((size_t)nb + 1);
+  rc = rc ? rc : W.nj.alloc(1);
+  rc = rc ? rc : W.stack.alloc(nb);
+  rc = rc ? rc : W.bflag.alloc(nb);
+  rc = rc ? rc : W.jm.alloc((size_t)njall + 1);
+  rc = rc ? rc : W.bfk.alloc(njall);
+  rc = rc ? rc : W.rstart.alloc((size_t)nb + 1);
+  rc = rc ? rc : W.tmp1.alloc((size_t)nb * 6);
+  rc = rc ? rc : W.rowisl.alloc(R);
+  rc = rc ? rc : W.neg.alloc((size_t)R + 1);
+  rc = rc ? rc : W.draws.alloc((size_t)nb + 1);
+  rc = rc ? rc : W.order.alloc(R);
+  rc = rc ? rc : W.order2.alloc(R);
+  rc = rc ? rc : W.rnd.alloc(R);
+  rc = rc ? rc : W.tcount.alloc((size_t)R + 1);
+  rc = rc ? rc : W.tfill.alloc(R);
+  rc = rc ? rc : W.tlist.alloc(R);
+  rc = rc ? rc : W.bcount.alloc((size_t)nb + 1);
+  rc = rc ? rc : W.bfill.alloc(nb);
+  rc = rc ? rc : W.blist.alloc(2 * (size_t)R);
+  rc = rc ? rc : W.prec.alloc(R);
+  rc = rc ? rc : W.lambda.alloc(R);
+  rc = rc ? rc : W.fc.alloc((size_t)nb * 6);
+  rc = rc ? rc : W.err.alloc(1);
+  if (rc) return rc;
+  L.statics = W.statics.p; L.ghash = W.ghash.p; L.hcount = W.hcount.p; L.hfill = W.hfill.p;
+  L.hgeoms = W.hgeoms.p; L.plist = W.plist.p; L.pcnt = W.pcnt.p; L.own = W.own.p; L.sflag = W.sflag.p;
+  L.pair_i = W.pair_i.p; L.pair_k = W.pair_k.p; L.npairs = W.npairs.p; L.pnc = W.pnc.p;
+  L.staged = W.staged.p; L.ccount = W.ccount.p; L.acount = W.acount.p; L.afill = W.afill.p;
+  L.adj_joint = W.adj_joint.p; L.adj_other = W.adj_other.p; L.jentry = W.jentry.p; L.jlist = W.jlist.p;
+  L.istart = W.istart.p; L.nj = W.nj.p; L.stack = W.stack.p; L.bflag = W.bflag.p; L.jm = W.jm.p;
+  L.bfk = W.bfk.p; L.rstart = W.rstart.p; L.tmp1 = W.tmp1.p; L.rowisl = W.rowisl.p; L.neg = W.neg.p;
+  L.draws = W.draws.p; L.order = W.order.p; L.order2 = W.order2.p; L.rnd = W.rnd.p;
+  L.tcount = W.tcount.p; L.tfill = W.tfill.p; L.tlist = W.tlist.p; L.bcount = W.bcount.p;
+  L.bfill = W.bfill.p; L.blist = W.blist.p; L.prec = W.prec.p; L.lambda = W.lambda.p; L.fc = W.fc.p;
+  L.err = W.err.p;
+  int optin = 0;
+  OG_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, B->device));
+  const int smem_max = std::min(optin, kLwIslandsSmem);
+  OG_CUDA(cudaFuncSetAttribute(lw_islands_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max));
+  W.islands_smem = smem_max;
+  // the sweep cluster: the largest cluster (16, non-portable, down to 1) the
+  // device can place with the body slots and lambdas split over its CTAs
+  OG_CUDA(cudaFuncSetAttribute(lw_sweep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max));
+  cudaFuncSetAttribute(lw_sweep_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  cudaGetLastError();
+  for (int C : {16, 8, 4, 2, 1}) {
+    const size_t smem = (size_t)((nb + C - 1) / C) * sizeof(LwBody) + (size_t)((R + C - 1) / C) * sizeof(float);
+    if (smem > (size_t)smem_max) continue;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)C);
+    cfg.blockDim = dim3(kLwSweepThreads);
+    cfg.dynamicSmemBytes = smem;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)C;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int ncl = 0;
+    if (cudaOccupancyMaxActiveClusters(&ncl, (void*)lw_sweep_kernel, &cfg) == cudaSuccess && ncl >= 1) {
+      L.cluster = C;
+      W.sweep_smem = (int)smem;
+      break;
+    }
+    cudaGetLastError();
+  }
+  if (L.cluster == 0)
+    return fail(ODEGPU_E_LIMIT, "the world's bodies and rows do not fit the sweep cluster's shared memory");
   return 0;
 }
 
@@ -492,12 +757,20 @@ int odegpuBatchCreate(const odegpuScene* sc, const odegpuBatchConfig* cfg, odegp
     D.ng = sc->geom_off[w + 1] - D.geom_off;
     D.joint_off = sc->joint_off[w];
     D.njp = sc->joint_off[w + 1] - D.joint_off;
-    if (D.nb > ODEGPU_MAX_BODIES_PER_WORLD) {
+    if (D.nb > ODEGPU_MAX_BODIES_PER_WORLD && W > 1) {
       delete B;
       return fail(ODEGPU_E_LIMIT, "world " + std::to_string(w) + " has " + std::to_string(D.nb) +
-                                      " bodies; this kernel handles at most " +
-                                      std::to_string(ODEGPU_MAX_BODIES_PER_WORLD));
+                                      " bodies; the on-chip kernel handles at most " +
+                                      std::to_string(ODEGPU_MAX_BODIES_PER_WORLD) +
+                                      " (a larger world must be the only world of its batch)");
     }
+    if (D.nb > ODEGPU_MAX_BODIES_LARGE) {
+      delete B;
+      return fail(ODEGPU_E_LIMIT, "world has " + std::to_string(D.nb) + " bodies; at most " +
+                                      std::to_string(ODEGPU_MAX_BODIES_LARGE));
+    }
+    const bool large = W == 1 && ((cfg && cfg->large_world) || D.nb > kMaxB || D.ng > kMaxB + 8 ||
+                                  D.njp + cpb * D.nb + 16 > kMaxR);
     if (P.max_contacts < 1 || P.max_contacts > 8) {
       delete B;
       return fail(ODEGPU_E_ARG, "max_contacts must be in [1, 8]");
@@ -506,7 +779,9 @@ int odegpuBatchCreate(const odegpuScene* sc, const odegpuBatchConfig* cfg, odegp
     D.contact_cap = cpb * D.nb + 16;
     contact_off += D.contact_cap;
     D.row_off = (int)row_off;
-    D.row_cap = std::min(ODEGPU_MAX_ROWS_PER_WORLD, 3 * D.contact_cap + 6 * D.njp);
+    D.row_cap = large ? 3 * D.contact_cap + 6 * D.njp
+                      : std::min(ODEGPU_MAX_ROWS_PER_WORLD, 3 * D.contact_cap + 6 * D.njp);
+    if (large) B->lw = new LargeWorld();
     row_off += D.row_cap;
     D.max_contacts = P.max_contacts;
     D.iterations = P.iterations;
@@ -623,6 +898,7 @@ int odegpuBatchCreate(const odegpuScene* sc, const odegpuBatchConfig* cfg, odegp
   }
   if (!rc && configure_kernels() != 0) rc = fail(ODEGPU_E_CUDA, "cannot configure shared memory");
   for (int k = 0; k < 3; ++k) B->kwpb[k] = std::min(B->warps_per_block, kMaxWpb[k]);
+  if (!rc && B->lw) rc = lw_setup(B, sc);
   if (rc) { delete B; return rc; }
   *out = B;
   return 0;
@@ -738,6 +1014,7 @@ int odegpuBatchGetKernelTimes(odegpuBatchID b, double* ms, long long* n_steps) {
 }
 
 int odegpuBatchSetFeedback(odegpuBatchID b, int on) {
+  if (b && b->lw) return fail(ODEGPU_E_ARG, "not available for a large world (one world above the on-chip limits)");
   if (!b) return fail(ODEGPU_E_ARG, "null batch");
   OG_CUDA(cudaSetDevice(b->device));
   OG_CUDA(cudaStreamSynchronize(b->stream));
@@ -773,6 +1050,7 @@ int odegpuBatchSetLaunchConfig(odegpuBatchID b, int kernel, int warps_per_block,
 }
 
 int odegpuBatchAutotune(odegpuBatchID b, int n_steps) {
+  if (b && b->lw) return fail(ODEGPU_E_ARG, "not available for a large world (one world above the on-chip limits)");
   if (!b || n_steps < 1) return fail(ODEGPU_E_ARG, "bad arguments");
   OG_CUDA(cudaSetDevice(b->device));
   OG_CUDA(cudaStreamSynchronize(b->stream));
@@ -864,6 +1142,7 @@ int odegpuBatchSetControlsF32(odegpuBatchID b, int n_ctrl_steps, const float* jt
 }
 
 int odegpuBatchRolloutForward(odegpuBatchID b, int n_steps, int ckpt_every) {
+  if (b && b->lw) return fail(ODEGPU_E_ARG, "not available for a large world (one world above the on-chip limits)");
   if (!b || n_steps <= 0 || ckpt_every <= 0) return fail(ODEGPU_E_ARG, "bad arguments");
   OG_CUDA(cudaSetDevice(b->device));
   auto& R = b->ro;
@@ -904,6 +1183,7 @@ int odegpuBatchRolloutForward(odegpuBatchID b, int n_steps, int ckpt_every) {
 
 int odegpuBatchRolloutBackward(odegpuBatchID b, const float* grad_final, float* grad_init, float* grad_jt,
                                float* grad_bf) {
+  if (b && b->lw) return fail(ODEGPU_E_ARG, "not available for a large world (one world above the on-chip limits)");
   if (!b || !grad_final) return fail(ODEGPU_E_ARG, "bad arguments");
   auto& R = b->ro;
   if (!R.valid) return fail(ODEGPU_E_ARG, "no rollout recorded (odegpuBatchRolloutForward)");
@@ -1094,6 +1374,7 @@ int odegpuBatchInfo(odegpuBatchID b, int* n_worlds, int* nb_total, int* nj_total
 void* odegpuBatchStream(odegpuBatchID b) { return b ? (void*)b->stream : nullptr; }
 
 int odegpuBatchStepTap(odegpuBatchID b, float* rows, float* lambda, float* fc, int* row_off) {
+  if (b && b->lw) return fail(ODEGPU_E_ARG, "not available for a large world (one world above the on-chip limits)");
   if (!b) return fail(ODEGPU_E_ARG, "null batch");
   OG_CUDA(cudaSetDevice(b->device));
   DBuf<float> drows, dlam, dfc;

@@ -24,7 +24,9 @@ enum {
   ST_ROW_OVERFLOW = 2,       // more constraint rows than the world's capacity
   ST_TOO_LARGE = 4,          // world exceeds the on-chip limits of this kernel
   ST_NONFINITE = 8,          // a body state became NaN/Inf
-  ST_HF_ZONE = 32            // a geom covered more heightfield samples than the collider's buffer
+  ST_HF_ZONE = 32,           // a geom covered more heightfield samples than the collider's buffer
+  ST_PAIR_OVERFLOW = 64,     // large world: candidate partners or pairs above capacity
+  ST_SOLVE_STALL = 128       // large world: a bounded wait of the sweep gave up
 };
 
 // Row store: 32 words (128 bytes, one cache line) per constraint row.

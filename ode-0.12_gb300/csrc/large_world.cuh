@@ -1,0 +1,865 @@
+// large_world.cuh -- one world of thousands of bodies stepped by the whole
+// GPU (the warp-per-world kernels hold a world on chip and stop at 64 bodies).
+//
+// The step keeps the reference's results and order:
+//   * controls, world-frame inertia, gyroscopic torque, gravity: a thread per body;
+//   * dCollide over the canonical pair list (geoms i < k in index order, the
+//     same early-outs and jointed-body test as the small path): geoms on bodies
+//     hash into a uniform grid whose cells are at least one bounding-sphere
+//     test wide, each geom lists its partners k > i in index order, static
+//     geoms get theirs by an ordered compaction, and one thread per pair runs
+//     the collider; prefix sums place every contact at its canonical index;
+//   * each body's joint list in ODE's order (contacts newest first, then
+//     persistent joints newest first), then the island walk of
+//     ode/src/util.cpp:384-521 by one warp;
+//   * getInfo1/getInfo2 per joint in island order with the ball / fixed erp
+//     carried along each island, rows set up per row;
+//   * SOR_LCP (quickstep.cpp:405-583): the findex tail reversal and ODE's
+//     Fisher-Yates reshuffle every 8 iterations, computed exactly in parallel
+//     (see lw_permute_kernel), then the sweep in that sequential order run as
+//     dataflow in one thread-block cluster: every body's velocity accumulator
+//     and a counter of the row updates it has received live in distributed
+//     shared memory, and a row waits (bounded) until both of its bodies have
+//     received exactly the updates that precede it in the order;
+//   * integration per body.
+#pragma once
+#include <cooperative_groups.h>
+#include "world_solve.cuh"
+
+namespace og {
+
+constexpr int kLwPartners = 64;        // candidate partners (k > i) one geom may own
+constexpr int kLwSweepThreads = 512;   // threads per CTA of the sweep cluster
+constexpr int kLwScanThreads = 1024;
+constexpr unsigned kLwSpinLimit = 1u << 22;
+
+// One body's slot in the sweep cluster's shared memory.
+struct __align__(16) LwBody {
+  float f[6];        // constraint force accumulator (cforce)
+  unsigned cnt;      // row updates applied to the body in this sweep launch
+  unsigned pad;
+};
+
+struct LWDev {
+  int nb, ng, njp, nstat, contact_cap, row_cap, pair_cap, adj_cap, hsize, cluster;
+  float cell, inv_cell;
+  const int* statics;    // [nstat] static geoms (world-local), ascending
+  // broadphase
+  int* ghash;            // [ng] bucket of each geom on a body, -1 for static geoms
+  int* hcount;           // [hsize+1] geoms per bucket -> first slot
+  int* hfill;            // [hsize]
+  int* hgeoms;           // [ng]
+  int* plist;            // [ng][kLwPartners] partners k > i of geoms on bodies, ascending
+  int* pcnt;             // [ng] number of those partners
+  int* own;              // [ng+1] pairs owned by each geom -> first pair
+  int* sflag;            // [nstat][ng+1] geom k (> s) pairs with static s -> rank
+  int* pair_i;           // [pair_cap]
+  int* pair_k;           // [pair_cap]
+  int* npairs;           // [1]
+  int* pnc;              // [pair_cap+1] contacts per pair -> first contact
+  Contact* staged;       // [pair_cap][max_contacts]
+  // body joint lists
+  int* ccount;           // [nb] contacts per body
+  int* acount;           // [nb+1] list length -> first entry
+  int* afill;            // [nb]
+  int* adj_joint;        // [adj_cap] joint ordinal of each entry (persistent j, contact njp + c)
+  int* adj_other;        // [adj_cap] the other body of each entry, -1 for none
+  // islands
+  int* jentry;           // [njp+contact_cap] island order as list entries
+  int* jlist;            // [njp+contact_cap] island order as joint ordinals
+  int* istart;           // [nb+1] first island-order position of each island with joints
+  int* nj;               // [1] joints taken into islands
+  int* stack;            // [nb] walk stack when the walk's arrays do not fit on chip
+  unsigned char* bflag;  // [nb] walk flags when they do not fit on chip
+  // rows
+  int* jm;               // [njp+contact_cap+1] rows per island-ordered joint -> first row
+  int* bfk;              // [njp+contact_cap] position of a ball / fixed joint, else -1 -> running max
+  int* rstart;           // [nb+1] first row of each island
+  float* tmp1;           // [nb][6]
+  // SOR
+  int* rowisl;           // [row_cap] island of each row
+  int* neg;              // [row_cap+1] findex == -1 flags -> exclusive scan
+  int* draws;            // [nb+1] reshuffle draws of each island -> first draw
+  int* order;            // [row_cap] position -> row (two buffers)
+  int* order2;
+  int* rnd;              // [row_cap] swap partner of each position's reshuffle step
+  int* tcount;           // [row_cap+1] steps that swap with each position -> first
+  int* tfill;            // [row_cap]
+  int* tlist;            // [row_cap]
+  int* bcount;           // [nb+1] positions touching each body -> first
+  int* bfill;            // [nb]
+  int* blist;            // [2*row_cap]
+  int4* prec;            // [row_cap] per position: row, rank1 << 16 | deg1, rank2 << 16 | deg2
+  float* lambda;         // [row_cap]
+  float* fc;             // [nb][6]
+  int* err;              // [1] a sweep wait gave up
+};
+
+// ---------------------------------------------------------------- scans
+// In-place exclusive prefix sum of a[0..n) (row blockIdx.x of stride `stride`),
+// total in a[n]; n from n_dev when given. One block per row.
+__global__ void __launch_bounds__(kLwScanThreads) lw_scan_kernel(int* a, const int* n_dev, int n_host,
+                                                                 size_t stride) {
+  __shared__ int wsum[32];
+  a += (size_t)blockIdx.x * stride;
+  const int n = n_dev ? *n_dev : n_host;
+  const int T = blockDim.x, tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const int per = (n + T - 1) / T;
+  const int s = min(n, tid * per), e = min(n, s + per);
+  int sum = 0;
+  for (int i = s; i < e; ++i) sum += a[i];
+  const int incl = warp_incl_scan(sum, lane);
+  if (lane == 31) wsum[wid] = incl;
+  __syncthreads();
+  if (wid == 0) {
+    const int v = (lane < (T >> 5)) ? wsum[lane] : 0;
+    const int wi = warp_incl_scan(v, lane);
+    wsum[lane] = wi;
+  }
+  __syncthreads();
+  int run = (wid > 0 ? wsum[wid - 1] : 0) + incl - sum;
+  for (int i = s; i < e; ++i) {
+    const int v = a[i];
+    a[i] = run;
+    run += v;
+  }
+  if (tid == 0) a[n] = wsum[(T >> 5) - 1];
+}
+
+// In-place inclusive running maximum of a[0..n), n from n_dev.
+__global__ void __launch_bounds__(kLwScanThreads) lw_max_scan_kernel(int* a, const int* n_dev) {
+  __shared__ int wmax[32];
+  const int n = *n_dev;
+  const int T = blockDim.x, tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const int per = (n + T - 1) / T;
+  const int s = min(n, tid * per), e = min(n, s + per);
+  int m = -1;
+  for (int i = s; i < e; ++i) m = max(m, a[i]);
+  // inclusive max-scan across threads
+  int incl = m;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int v = __shfl_up_sync(kFull, incl, o);
+    if (lane >= o) incl = max(incl, v);
+  }
+  if (lane == 31) wmax[wid] = incl;
+  __syncthreads();
+  if (wid == 0) {
+    int v = (lane < (T >> 5)) ? wmax[lane] : -1;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int u = __shfl_up_sync(kFull, v, o);
+      if (lane >= o) v = max(v, u);
+    }
+    wmax[lane] = v;
+  }
+  __syncthreads();
+  int excl = __shfl_up_sync(kFull, incl, 1);
+  if (lane == 0) excl = -1;
+  int run = max(wid > 0 ? wmax[wid - 1] : -1, excl);
+  for (int i = s; i < e; ++i) {
+    run = max(run, a[i]);
+    a[i] = run;
+  }
+}
+
+// ---------------------------------------------------------------- bodies
+__global__ void lw_bodies_pre_kernel(BatchDev d, int step, int controls, int prologue) {
+  const WorldDesc D = d.world[0];
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= D.nb) return;
+  if (controls) controls_body(d, step, D.body_off + b);
+  if (prologue) body_prologue(d, D, D.body_off + b);
+}
+__global__ void lw_controls_joints_kernel(BatchDev d, int step) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) controls_joints(d, d.world[0], step);
+}
+
+// ---------------------------------------------------------------- broadphase
+OG_D int lw_cell_hash(int ix, int iy, int iz, int mask) {
+  unsigned h = (unsigned)ix * 73856093u ^ (unsigned)iy * 19349663u ^ (unsigned)iz * 83492791u;
+  return (int)(h & (unsigned)mask);
+}
+OG_D void lw_cell_of(const LWDev& L, const float4& p, int& ix, int& iy, int& iz) {
+  ix = (int)floorf(p.x * L.inv_cell);
+  iy = (int)floorf(p.y * L.inv_cell);
+  iz = (int)floorf(p.z * L.inv_cell);
+}
+
+__global__ void lw_hash_kernel(BatchDev d, LWDev L) {
+  const WorldDesc D = d.world[0];
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= L.ng) return;
+  const int b = d.gbody[D.geom_off + g];
+  if (b < 0) { L.ghash[g] = -1; return; }
+  int ix, iy, iz;
+  lw_cell_of(L, d.pos[D.body_off + b], ix, iy, iz);
+  const int h = lw_cell_hash(ix, iy, iz, L.hsize - 1);
+  L.ghash[g] = h;
+  atomicAdd(&L.hcount[h], 1);
+}
+
+__global__ void lw_hfill_kernel(LWDev L) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= L.ng) return;
+  const int h = L.ghash[g];
+  if (h < 0) return;
+  const int slot = atomicAdd(&L.hfill[h], 1);
+  L.hgeoms[L.hcount[h] + slot] = g;
+}
+
+// Could geom g (on a body, bounding radius r at p) touch static geom s? Planes
+// are culled by the signed distance of the bounding sphere with the margin of
+// the pair pre-test; other static geoms are always candidates.
+OG_D bool lw_static_candidate(const BatchDev& d, const WorldDesc& D, int s, const float4& p, float r) {
+  const int gs = D.geom_off + s;
+  if (d.gtype[gs] != G_PLANE || !isfinite(r)) return true;
+  const float4 pl = d.gparam[gs];
+  const float dist = pl.x * p.x + pl.y * p.y + pl.z * p.z - pl.w;
+  return dist <= r * 1.001f + 1e-5f;
+}
+
+// Per geom i on a body: its partners k > i (statics after it, and geoms on
+// other bodies within the pair pre-test, not jointed to it), ascending, and
+// the flags of the statics before it that pair with it.
+__global__ void lw_candidates_kernel(BatchDev d, LWDev L) {
+  const WorldDesc D = d.world[0];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= L.ng) return;
+  const int gi = D.geom_off + i;
+  const int bi = d.gbody[gi];
+  if (bi < 0) { L.pcnt[i] = 0; L.own[i] = 0; return; }
+  const float4 pi4 = d.pos[D.body_off + bi];
+  const float ri = d.gbound[gi];
+  int* out = L.plist + (size_t)i * kLwPartners;
+  int n = 0;
+  bool over = false;
+  for (int si = 0; si < L.nstat; ++si) {
+    const int s = L.statics[si];
+    if (!lw_static_candidate(d, D, s, pi4, ri)) continue;
+    if (s > i) {
+      if (n < kLwPartners) out[n++] = s; else over = true;
+    } else {
+      L.sflag[(size_t)si * (L.ng + 1) + i] = 1;
+    }
+  }
+  int ix, iy, iz;
+  lw_cell_of(L, pi4, ix, iy, iz);
+  int buckets[27];
+  int nbk = 0;
+  for (int dx = -1; dx <= 1; ++dx)
+    for (int dy = -1; dy <= 1; ++dy)
+      for (int dz = -1; dz <= 1; ++dz) {
+        const int h = lw_cell_hash(ix + dx, iy + dy, iz + dz, L.hsize - 1);
+        bool seen = false;
+        for (int q = 0; q < nbk; ++q) seen |= (buckets[q] == h);
+        if (!seen) buckets[nbk++] = h;
+      }
+  for (int q = 0; q < nbk; ++q) {
+    const int h = buckets[q];
+    for (int e = L.hcount[h]; e < L.hcount[h + 1]; ++e) {
+      const int k = L.hgeoms[e];
+      if (k <= i) continue;
+      const int gk = D.geom_off + k;
+      const int bk = d.gbody[gk];
+      if (bk == bi) continue;
+      const float rk = d.gbound[gk];
+      if (isfinite(ri) && isfinite(rk)) {
+        const float4 pk4 = d.pos[D.body_off + bk];
+        const float dx = pi4.x - pk4.x, dy = pi4.y - pk4.y, dz = pi4.z - pk4.z;
+        const float lim = (ri + rk) * 1.001f + 1e-5f;
+        if (dx * dx + dy * dy + dz * dz > lim * lim) continue;
+      }
+      if (jointed(d, D, 0, bi, bk)) continue;
+      if (n < kLwPartners) out[n++] = k; else over = true;
+    }
+  }
+  // ascending partner order (the canonical pair order within this owner)
+  for (int a = 1; a < n; ++a) {
+    const int v = out[a];
+    int b = a - 1;
+    while (b >= 0 && out[b] > v) { out[b + 1] = out[b]; --b; }
+    out[b + 1] = v;
+  }
+  if (over) atomicOr(&d.status[0], ST_PAIR_OVERFLOW);
+  L.pcnt[i] = n;
+  L.own[i] = n;
+}
+
+__global__ void lw_static_own_kernel(LWDev L) {
+  const int si = blockIdx.x * blockDim.x + threadIdx.x;
+  if (si >= L.nstat) return;
+  L.own[L.statics[si]] = L.sflag[(size_t)si * (L.ng + 1) + L.ng];
+}
+
+__global__ void lw_pairs_fill_kernel(BatchDev d, LWDev L) {
+  const WorldDesc D = d.world[0];
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k == 0) {
+    const int total = L.own[L.ng];
+    if (total > L.pair_cap) atomicOr(&d.status[0], ST_PAIR_OVERFLOW);
+    *L.npairs = min(total, L.pair_cap);
+  }
+  if (k >= L.ng || d.gbody[D.geom_off + k] < 0) return;
+  const int* in = L.plist + (size_t)k * kLwPartners;
+  const int base = L.own[k];
+  for (int j = 0; j < L.pcnt[k]; ++j) {
+    const int pos = base + j;
+    if (pos < L.pair_cap) { L.pair_i[pos] = k; L.pair_k[pos] = in[j]; }
+  }
+  for (int si = 0; si < L.nstat; ++si) {
+    const int s = L.statics[si];
+    if (s >= k) break;
+    const int* f = L.sflag + (size_t)si * (L.ng + 1);
+    if (f[k + 1] == f[k]) continue;
+    const int pos = L.own[s] + f[k];
+    if (pos < L.pair_cap) { L.pair_i[pos] = s; L.pair_k[pos] = k; }
+  }
+}
+
+// dCollide(g_i, g_k) of every candidate pair into its staging slots.
+__global__ void __launch_bounds__(128) lw_narrow_kernel(BatchDev d, LWDev L) {
+  const WorldDesc D = d.world[0];
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  const int np = *L.npairs;
+  if (p >= np) return;
+  const int i = L.pair_i[p], k = L.pair_k[p];
+  GeomView vi, vk;
+  geom_view(d, D, i, vi);
+  geom_view(d, D, k, vk);
+  Contact cc[8];
+  int cnt = 0;
+  if (vi.type == G_HEIGHTFIELD || vk.type == G_HEIGHTFIELD) {
+    const bool rev = vk.type == G_HEIGHTFIELD;
+    const GeomView& hv = rev ? vk : vi;
+    const GeomView& ov = rev ? vi : vk;
+    if (ov.type == G_SPHERE || ov.type == G_BOX || ov.type == G_CAPSULE) {
+      cnt = collide_heightfield(d.hfs[(int)hv.p[0]], d.hf_heights, ov, (unsigned)D.max_contacts, cc, nullptr);
+      if (cnt < 0) { atomicOr(&d.status[0], ST_HF_ZONE); cnt = 0; }
+      if (rev)
+        for (int c = 0; c < cnt; ++c) {
+          cc[c].normal[0] = -cc[c].normal[0]; cc[c].normal[1] = -cc[c].normal[1];
+          cc[c].normal[2] = -cc[c].normal[2];
+        }
+    }
+  } else {
+    cnt = collide_primitive(vi, vk, (unsigned)D.max_contacts, cc);
+  }
+  Contact* o = L.staged + (size_t)p * D.max_contacts;
+  for (int c = 0; c < cnt; ++c) o[c] = cc[c];
+  L.pnc[p] = cnt;
+}
+
+// Contact joints in canonical order (dJointCreateContact + dJointAttach(body(g_i), body(g_k))).
+__global__ void lw_contacts_kernel(BatchDev d, LWDev L) {
+  const WorldDesc D = d.world[0];
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  const int np = *L.npairs;
+  if (p == 0) {
+    const int total = L.pnc[np];
+    if (total > L.contact_cap) atomicOr(&d.status[0], ST_CONTACT_OVERFLOW);
+    d.ncontacts[0] = min(total, L.contact_cap);
+  }
+  if (p >= np) return;
+  const int n = L.pnc[p + 1] - L.pnc[p];
+  if (n == 0) return;
+  const int i = L.pair_i[p], k = L.pair_k[p];
+  const int bi = d.gbody[D.geom_off + i], bk = d.gbody[D.geom_off + k];
+  const int si = d.gsurf[D.geom_off + i], sk = d.gsurf[D.geom_off + k];
+  const Contact* in = L.staged + (size_t)p * D.max_contacts;
+  for (int c = 0; c < n; ++c) {
+    const int slot = L.pnc[p] + c;
+    if (slot >= L.contact_cap) break;
+    DevContact ct;
+    ct.pos[0] = in[c].pos[0]; ct.pos[1] = in[c].pos[1]; ct.pos[2] = in[c].pos[2];
+    ct.depth = in[c].depth;
+    ct.normal[0] = in[c].normal[0]; ct.normal[1] = in[c].normal[1]; ct.normal[2] = in[c].normal[2];
+    ct.surface = si > sk ? si : sk;
+    if (bi < 0) { ct.b1 = bk; ct.b2 = -1; ct.reverse = 1; }
+    else { ct.b1 = bi; ct.b2 = bk; ct.reverse = 0; }
+    ct.geoms = -1;
+    d.contacts[D.contact_off + slot] = ct;
+    atomicAdd(&L.ccount[ct.b1], 1);
+    if (ct.b2 >= 0) atomicAdd(&L.ccount[ct.b2], 1);
+  }
+}
+
+// ---------------------------------------------------------------- body joint lists
+__global__ void lw_adj_count_kernel(BatchDev d, LWDev L) {
+  const WorldDesc D = d.world[0];
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= L.nb) return;
+  const int* ps = d.padj_start + D.body_off;
+  L.acount[b] = L.ccount[b] + (ps[b + 1] - ps[b]);
+}
+
+__global__ void lw_adj_fill_kernel(BatchDev d, LWDev L) {
+  const WorldDesc D = d.world[0];
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= d.ncontacts[0]) return;
+  const DevContact& ct = d.contacts[D.contact_off + c];
+  {
+    const int e = L.acount[ct.b1] + atomicAdd(&L.afill[ct.b1], 1);
+    L.adj_joint[e] = L.njp + c;
+    L.adj_other[e] = ct.b2;
+  }
+  if (ct.b2 >= 0) {
+    const int e = L.acount[ct.b2] + atomicAdd(&L.afill[ct.b2], 1);
+    L.adj_joint[e] = L.njp + c;
+    L.adj_other[e] = ct.b1;
+  }
+}
+
+// Each body's list: contacts newest first (dJointAttach prepends), then its
+// persistent joints in their stored newest-first order.
+__global__ void lw_adj_finish_kernel(BatchDev d, LWDev L) {
+  const WorldDesc D = d.world[0];
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= L.nb) return;
+  const int s = L.acount[b], nc = L.ccount[b];
+  int* J = L.adj_joint + s;
+  int* O = L.adj_other + s;
+  for (int a = 1; a < nc; ++a) {
+    const int vj = J[a], vo = O[a];
+    int q = a - 1;
+    while (q >= 0 && J[q] < vj) { J[q + 1] = J[q]; O[q + 1] = O[q]; --q; }
+    J[q + 1] = vj;
+    O[q + 1] = vo;
+  }
+  const int* ps = d.padj_start + D.body_off;
+  int e = s + nc;
+  for (int k = ps[b]; k < ps[b + 1]; ++k, ++e) {
+    const int j = d.padj[k];
+    const DevJoint& Jt = d.joints[D.joint_off + j];
+    L.adj_joint[e] = j;
+    L.adj_other[e] = (Jt.b1 == b) ? Jt.b2 : Jt.b1;
+  }
+}
+
+// The island walk of ode/src/util.cpp:384-521 by one warp: bodies from the
+// newest (ODE's body list is newest first), each untagged one starting a
+// depth-first walk; a body's list entries are taken in order. An entry's joint
+// is still untagged exactly when its other body has not been walked yet (a
+// joint is tagged when the first of its two bodies is walked), so the walk
+// needs only the other body of each entry. Output: the island order as list
+// entries, and the first position of every island that has joints.
+__global__ void __launch_bounds__(32) lw_islands_kernel(BatchDev d, LWDev L, int smem_bytes) {
+  extern __shared__ __align__(16) unsigned char lw_sm[];
+  const int lane = threadIdx.x;
+  const int nb = L.nb;
+  const int E = L.acount[nb];
+  // on-chip copies when they fit: list starts, flags, stack, other bodies
+  const size_t need_fixed = (size_t)(nb + 1) * 4 + (size_t)nb * 4 + ((nb + 16) & ~15);
+  const bool fit_all = need_fixed + (size_t)E * 4 <= (size_t)smem_bytes;
+  const bool fit_fixed = need_fixed <= (size_t)smem_bytes;
+  int* astart = fit_fixed ? reinterpret_cast<int*>(lw_sm) : L.acount;
+  int* stack = fit_fixed ? astart + (nb + 1) : L.stack;
+  unsigned char* flags = fit_fixed ? reinterpret_cast<unsigned char*>(stack + nb) : L.bflag;
+  int* other = fit_all ? reinterpret_cast<int*>(flags + ((nb + 16) & ~15)) : L.adj_other;
+  if (fit_fixed)
+    for (int b = lane; b <= nb; b += 32) astart[b] = L.acount[b];
+  if (fit_all)
+    for (int e = lane; e < E; e += 32) other[e] = L.adj_other[e];
+  for (int b = lane; b < nb; b += 32) flags[b] = 0;
+  __syncwarp();
+  const unsigned lt = (1u << lane) - 1u;
+  int jcount = 0, nisl = 0;
+  for (int bb = nb - 1; bb >= 0; --bb) {
+    if (flags[bb] & 1) continue;
+    __syncwarp();
+    if (lane == 0) flags[bb] = 1;
+    __syncwarp();
+    const int jstart = jcount;
+    int sp = 0, b = bb;
+    for (;;) {
+      const int s = astart[b], e = astart[b + 1];
+      for (int base = s; base < e; base += 32) {
+        const int k = base + lane;
+        int o = -1;
+        bool take = false;
+        if (k < e) {
+          o = other[k];
+          take = (o < 0) || !(flags[o] & 2);
+        }
+        const unsigned bal = __ballot_sync(kFull, take);
+        if (take) L.jentry[jcount + __popc(bal & lt)] = k;
+        jcount += __popc(bal);
+        const bool cand = take && o >= 0 && !(flags[o] & 1);
+        const unsigned same = __match_any_sync(kFull, cand ? o : -1 - lane);
+        const bool first = cand && (same & lt) == 0;
+        const unsigned bp = __ballot_sync(kFull, first);
+        __syncwarp();
+        if (first) {
+          flags[o] |= 1;
+          stack[sp + __popc(bp & lt)] = o;
+        }
+        sp += __popc(bp);
+        __syncwarp();
+      }
+      if (lane == 0) flags[b] |= 2;
+      __syncwarp();
+      if (sp == 0) break;
+      b = stack[--sp];
+    }
+    if (jcount > jstart) {
+      if (lane == 0) L.istart[nisl] = jstart;
+      ++nisl;
+    }
+  }
+  if (lane == 0) {
+    L.istart[nisl] = jcount;
+    *L.nj = jcount;
+    d.nislands[0] = nisl;
+  }
+}
+
+OG_D int lw_island_of(const int* start, int n, int k) {
+  // last island whose first position is <= k
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (start[mid] <= k) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// ---------------------------------------------------------------- rows
+__global__ void lw_info1_kernel(BatchDev d, LWDev L, int step) {
+  const WorldDesc D = d.world[0];
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nj = *L.nj;
+  if (k >= nj) return;
+  const int ord = L.adj_joint[L.jentry[k]];
+  L.jlist[k] = ord;
+  int m;
+  bool bf = false;
+  if (ord < D.njp) {
+    const DevJoint& J = d.joints[D.joint_off + ord];
+    const DevLimot lm1 = step_limot1(J, step_stops(d, D, step), ord);
+    BodyRef B1, B2;
+    load_body_ref(d, D.body_off + J.b1, B1);
+    if (J.b2 >= 0) load_body_ref(d, D.body_off + J.b2, B2);
+    m = persistent_info1(J, lm1, B1, J.b2 >= 0 ? &B2 : nullptr).m;
+    bf = J.type == J_BALL || J.type == J_FIXED;
+  } else {
+    m = contact_info1(d.surfaces[d.contacts[D.contact_off + ord - D.njp].surface]);
+  }
+  L.jm[k] = m;
+  L.bfk[k] = bf ? k : -1;
+}
+
+__global__ void lw_info2_kernel(BatchDev d, LWDev L, int step) {
+  const WorldDesc D = d.world[0];
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nj = *L.nj;
+  const int M = L.jm[nj];
+  if (k == 0) {
+    if (M > L.row_cap) atomicOr(&d.status[0], ST_ROW_OVERFLOW);
+    d.nrows[0] = M > L.row_cap ? 0 : M;
+  }
+  if (M > L.row_cap || k >= nj) return;
+  const int nisl = d.nislands[0];
+  const int isl = lw_island_of(L.istart, nisl, k);
+  if (k == L.istart[isl]) L.rstart[isl] = L.jm[k];
+  if (k == 0) L.rstart[nisl] = M;
+  // the erp this joint meets: that of the last ball / fixed joint before it
+  // in its island (ball.cpp:59, fixed.cpp:80), else the world's
+  float erp = D.erp;
+  if (k > 0) {
+    const int j = L.bfk[k - 1];
+    if (j >= L.istart[isl]) erp = d.joints[D.joint_off + L.jlist[j]].erp;
+  }
+  assemble_joint_rows(d, D, L.jlist[k], L.jm[k], L.jm[k + 1] - L.jm[k], erp, step_stops(d, D, step), nullptr);
+}
+
+__global__ void lw_tmp1_kernel(BatchDev d, LWDev L) {
+  const WorldDesc D = d.world[0];
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= L.nb || d.nrows[0] == 0) return;
+  body_tmp1(d, D.body_off + b, 1.0f / D.dt, L.tmp1 + 6 * (size_t)b);
+}
+
+__global__ void lw_row_setup_kernel(BatchDev d, LWDev L) {
+  const WorldDesc D = d.world[0];
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= d.nrows[0]) return;
+  row_setup(d, D, r, L.tmp1, 1.0f / D.dt, D.sor_w, nullptr, nullptr);
+}
+
+// ---------------------------------------------------------------- SOR order
+// Per row: its island and whether findex == -1; per island: its reshuffle draws.
+__global__ void lw_order_flags_kernel(BatchDev d, LWDev L) {
+  const WorldDesc D = d.world[0];
+  const int M = d.nrows[0];
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nisl = d.nislands[0];
+  if (r < nisl) {
+    const int m = L.rstart[r + 1] - L.rstart[r];
+    L.draws[r] = m > 0 ? ((D.iterations + 7) / 8) * (m - 1) : 0;
+  }
+  if (r >= M) return;
+  L.rowisl[r] = lw_island_of(L.rstart, nisl, r);
+  L.neg[r] = reinterpret_cast<const int*>(d.rows + (size_t)(D.row_off + r) * kRowWords)[kRowFindex] == -1 ? 1 : 0;
+}
+
+// quickstep.cpp:405-425: rows with findex == -1 first in row order, the rest
+// from the island's tail backwards.
+__global__ void lw_order_init_kernel(BatchDev d, LWDev L) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= d.nrows[0]) return;
+  const int isl = L.rowisl[r];
+  const int rs = L.rstart[isl], re = L.rstart[isl + 1];
+  const int negb = L.neg[r] - L.neg[rs];
+  const bool is_neg = (L.neg[r + 1] - L.neg[r]) != 0;
+  const int p = is_neg ? rs + negb : re - 1 - ((r - rs) - negb);
+  L.order[p] = r;
+}
+
+// Reshuffle `round` (iteration 8 * round): for island position q >= 1 the
+// reference swaps order[q] with order[dRandInt(q + 1)], the q-th draw of the
+// island's round (quickstep.cpp:471-478). Record the partner and count, per
+// position, the steps that swap with it.
+__global__ void lw_rand_kernel(BatchDev d, LWDev L, int round) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= d.nrows[0]) return;
+  const int isl = L.rowisl[p];
+  const int rs = L.rstart[isl], m = L.rstart[isl + 1] - rs;
+  const int q = p - rs;
+  if (q == 0) { L.rnd[p] = -1; return; }
+  const unsigned k = (unsigned)L.draws[isl] + (unsigned)(round * (m - 1)) + (unsigned)q;
+  const int sw = rand_int_from(lcg_jump(d.seed[0], k), q + 1);
+  L.rnd[p] = rs + sw;
+  atomicAdd(&L.tcount[rs + sw], 1);
+}
+
+__global__ void lw_tfill_kernel(BatchDev d, LWDev L) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= d.nrows[0]) return;
+  const int t = L.rnd[p];
+  if (t < 0) return;
+  L.tlist[L.tcount[t] + atomicAdd(&L.tfill[t], 1)] = p;
+}
+
+__global__ void lw_tsort_kernel(BatchDev d, LWDev L) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= d.nrows[0]) return;
+  int* a = L.tlist + L.tcount[q];
+  const int n = L.tcount[q + 1] - L.tcount[q];
+  for (int i = 1; i < n; ++i) {
+    const int v = a[i];
+    int j = i - 1;
+    while (j >= 0 && a[j] > v) { a[j + 1] = a[j]; --j; }
+    a[j + 1] = v;
+  }
+}
+
+// The permutation the reshuffle's swap sequence applies, without running it
+// in sequence. Step j (1 <= j < m) swaps positions j and r_j <= j, and
+// position j is untouched before step j, so step j writes the round's old
+// entry j to position r_j. Hence the entry at position q just before step t
+// (t > q) is old[j] for the last step j < t with r_j = q (j = q when r_q = q),
+// and when there is none, what step q moved there: the entry at position r_q
+// just before step q (position 0 keeps old[0]). The final entry at q follows
+// this chain down r_q < q (O(log m) links for a uniform draw).
+__global__ void lw_permute_kernel(BatchDev d, LWDev L, const int* src_order, int* dst_order) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= d.nrows[0]) return;
+  const int isl = L.rowisl[p];
+  const int rs = L.rstart[isl], re = L.rstart[isl + 1];
+  int t = re, q = p, src = -1;
+  for (int guard = 0; guard <= re - rs; ++guard) {
+    const int a = L.tcount[q], b = L.tcount[q + 1];
+    int j = -1;
+    for (int e = b - 1; e >= a; --e) {
+      const int v = L.tlist[e];
+      if (v < t) { j = v; break; }
+    }
+    if (j >= 0) { src = j; break; }
+    if (q == rs) { src = rs; break; }
+    t = q;
+    q = L.rnd[q];
+  }
+  dst_order[p] = src_order[src >= 0 ? src : p];
+}
+
+// Positions touching each body, in order: a body's k-th position waits for k
+// of the body's updates in every iteration.
+__global__ void lw_bodypos_kernel(BatchDev d, LWDev L, const int* ord) {
+  const WorldDesc D = d.world[0];
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= d.nrows[0]) return;
+  const int r = ord[p];
+  const int* w = reinterpret_cast<const int*>(d.rows + (size_t)(D.row_off + r) * kRowWords);
+  L.prec[p].x = r;
+  atomicAdd(&L.bcount[w[kRowB1]], 1);
+  if (w[kRowB2] >= 0) atomicAdd(&L.bcount[w[kRowB2]], 1);
+}
+
+__global__ void lw_bfill_kernel(BatchDev d, LWDev L, const int* ord) {
+  const WorldDesc D = d.world[0];
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= d.nrows[0]) return;
+  const int* w = reinterpret_cast<const int*>(d.rows + (size_t)(D.row_off + ord[p]) * kRowWords);
+  const int b1 = w[kRowB1], b2 = w[kRowB2];
+  L.blist[L.bcount[b1] + atomicAdd(&L.bfill[b1], 1)] = p;
+  if (b2 >= 0) L.blist[L.bcount[b2] + atomicAdd(&L.bfill[b2], 1)] = p;
+}
+
+__global__ void lw_branks_kernel(BatchDev d, LWDev L, const int* ord) {
+  const WorldDesc D = d.world[0];
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= L.nb) return;
+  int* a = L.blist + L.bcount[b];
+  const int n = L.bcount[b + 1] - L.bcount[b];
+  if (n >= 65536) { atomicOr(&d.status[0], ST_ROW_OVERFLOW); return; }
+  for (int i = 1; i < n; ++i) {
+    const int v = a[i];
+    int j = i - 1;
+    while (j >= 0 && a[j] > v) { a[j + 1] = a[j]; --j; }
+    a[j + 1] = v;
+  }
+  for (int i = 0; i < n; ++i) {
+    const int p = a[i];
+    const int* w = reinterpret_cast<const int*>(d.rows + (size_t)(D.row_off + ord[p]) * kRowWords);
+    const int v = (i << 16) | n;
+    if (w[kRowB1] == b) L.prec[p].y = v;
+    else L.prec[p].z = v;
+  }
+}
+
+// ---------------------------------------------------------------- sweep
+OG_D unsigned lw_ld_acquire(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.cluster.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+OG_D void lw_st_release(unsigned* p, unsigned v) {
+  asm volatile("st.release.cluster.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Wait until *c == target; false when the wait gave up (bounded, or another
+// thread gave up first).
+OG_D bool lw_wait(const unsigned* c, unsigned target, const volatile int* err) {
+  for (unsigned spins = 0;; ++spins) {
+    if (lw_ld_acquire(c) == target) return true;
+    if (spins >= kLwSpinLimit) return false;
+    if ((spins & 255u) == 255u && *err) return false;
+  }
+}
+
+// Iterations [it0, it1) of SOR_LCP over every island in the current order, as
+// one cluster. Body b's slot lives in CTA b % C, row r's lambda in CTA r % C.
+// Thread t takes positions t' , t' + T, ... (t' spreads a warp's lanes over the
+// order) in every iteration, so each thread meets its rows in the sequential
+// order and the earliest unfinished row can always run. A row waits until its
+// bodies have received exactly the updates that precede it: the k-th of deg
+// positions touching a body waits for it * deg + k.
+__global__ void __launch_bounds__(kLwSweepThreads) lw_sweep_kernel(BatchDev d, LWDev L, int it0, int it1,
+                                                                   int first) {
+  namespace cg = cooperative_groups;
+  extern __shared__ __align__(16) unsigned char lw_sw[];
+  cg::cluster_group cluster = cg::this_cluster();
+  const int C = (int)cluster.num_blocks();
+  const int rank = (int)cluster.block_rank();
+  const WorldDesc D = d.world[0];
+  const int M = d.nrows[0];
+  const int nb = L.nb;
+  const int nbs = (nb + C - 1) / C;
+  LwBody* bodies = reinterpret_cast<LwBody*>(lw_sw);
+  float* lam = reinterpret_cast<float*>(bodies + nbs);
+  const int nrs = (L.row_cap + C - 1) / C;
+  for (int s = threadIdx.x; s < nbs; s += blockDim.x) {
+    const int b = s * C + rank;
+    LwBody v;
+    for (int k = 0; k < 6; ++k) v.f[k] = (b < nb && !first) ? L.fc[6 * (size_t)b + k] : 0.f;
+    v.cnt = 0u;
+    v.pad = 0u;
+    bodies[s] = v;
+  }
+  for (int s = threadIdx.x; s < nrs; s += blockDim.x) {
+    const int r = s * C + rank;
+    lam[s] = (r < M && !first) ? L.lambda[r] : 0.f;
+  }
+  cluster.sync();
+  const int T = C * (int)blockDim.x;
+  const int tid = rank * (int)blockDim.x + (int)threadIdx.x;
+  const int lane = tid & 31, wid = tid >> 5, nw = T >> 5;
+  const int t0 = lane * nw + wid;
+  const float* rows = d.rows + (size_t)D.row_off * kRowWords;
+  bool ok = M > 0 && !*L.err;
+  for (int it = it0; ok && it < it1; ++it) {
+    const unsigned li = (unsigned)(it - it0);
+    for (int p = t0; ok && p < M; p += T) {
+      const int4 rec = L.prec[p];
+      const int r = rec.x;
+      float4 rw[8];
+      load_row(rows, r, rw);
+      const float* J = reinterpret_cast<const float*>(&rw[0]);
+      const float* iMJ = reinterpret_cast<const float*>(&rw[3]);
+      const float bb = rw[6].x, Ad = rw[6].y, lo = rw[6].z, hi = rw[6].w;
+      const int findex = __float_as_int(rw[7].x);
+      const int b1 = __float_as_int(rw[7].y), b2 = __float_as_int(rw[7].z);
+      LwBody* B1 = cluster.map_shared_rank(bodies + b1 / C, b1 % C);
+      LwBody* B2 = b2 >= 0 ? cluster.map_shared_rank(bodies + b2 / C, b2 % C) : nullptr;
+      const unsigned tg1 = li * (unsigned)(rec.y & 0xffff) + ((unsigned)rec.y >> 16);
+      const unsigned tg2 = li * (unsigned)(rec.z & 0xffff) + ((unsigned)rec.z >> 16);
+      if (!lw_wait(&B1->cnt, tg1, L.err) || (B2 && !lw_wait(&B2->cnt, tg2, L.err))) {
+        atomicExch(L.err, 1);
+        ok = false;
+        break;
+      }
+      float* lr = cluster.map_shared_rank(lam + r / C, r % C);
+      const float old = *lr;
+      const float lf = findex >= 0 ? *cluster.map_shared_rank(lam + findex / C, findex % C) : 0.f;
+      const float f10 = B1->f[0], f11 = B1->f[1], f12 = B1->f[2], f13 = B1->f[3], f14 = B1->f[4], f15 = B1->f[5];
+      float f20 = 0.f, f21 = 0.f, f22 = 0.f, f23 = 0.f, f24 = 0.f, f25 = 0.f;
+      if (B2) { f20 = B2->f[0]; f21 = B2->f[1]; f22 = B2->f[2]; f23 = B2->f[3]; f24 = B2->f[4]; f25 = B2->f[5]; }
+      // the row update of sor_row, term for term
+      float delta = bb - old * Ad;
+      delta -= (f10 * J[0] + f11 * J[1]) + (f12 * J[2] + f13 * J[3]) + (f14 * J[4] + f15 * J[5]);
+      delta -= (f20 * J[6] + f21 * J[7]) + (f22 * J[8] + f23 * J[9]) + (f24 * J[10] + f25 * J[11]);
+      const float hf = fabsf(hi * lf);
+      const float hi_act = findex >= 0 ? hf : hi;
+      const float lo_act = findex >= 0 ? -hf : lo;
+      const float nl = old + delta;
+      const bool clamped = (nl < lo_act) || (nl > hi_act);
+      const float lamv = fminf(fmaxf(nl, lo_act), hi_act);
+      delta = clamped ? lamv - old : delta;
+      *lr = clamped ? lamv : nl;
+      B1->f[0] = f10 + delta * iMJ[0]; B1->f[1] = f11 + delta * iMJ[1]; B1->f[2] = f12 + delta * iMJ[2];
+      B1->f[3] = f13 + delta * iMJ[3]; B1->f[4] = f14 + delta * iMJ[4]; B1->f[5] = f15 + delta * iMJ[5];
+      if (B2) {
+        B2->f[0] = f20 + delta * iMJ[6]; B2->f[1] = f21 + delta * iMJ[7]; B2->f[2] = f22 + delta * iMJ[8];
+        B2->f[3] = f23 + delta * iMJ[9]; B2->f[4] = f24 + delta * iMJ[10]; B2->f[5] = f25 + delta * iMJ[11];
+        lw_st_release(&B2->cnt, tg2 + 1u);
+      }
+      lw_st_release(&B1->cnt, tg1 + 1u);
+    }
+  }
+  cluster.sync();
+  for (int s = threadIdx.x; s < nbs; s += blockDim.x) {
+    const int b = s * C + rank;
+    if (b < nb)
+      for (int k = 0; k < 6; ++k) L.fc[6 * (size_t)b + k] = bodies[s].f[k];
+  }
+  for (int s = threadIdx.x; s < nrs; s += blockDim.x) {
+    const int r = s * C + rank;
+    if (r < M) L.lambda[r] = lam[s];
+  }
+}
+
+// ---------------------------------------------------------------- integration
+__global__ void lw_integrate_kernel(BatchDev d, LWDev L) {
+  const WorldDesc D = d.world[0];
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  const int M = d.nrows[0];
+  if (b == 0) {
+    const unsigned total = (unsigned)L.draws[d.nislands[0]];
+    const unsigned seed = d.seed[0];
+    if (M > 0) d.seed[0] = lcg_jump(seed, total);
+    if (*L.err) atomicOr(&d.status[0], ST_SOLVE_STALL);
+  }
+  if (b >= L.nb) return;
+  const bool bad = integrate_body(d, D, D.body_off + b, M > 0 ? L.fc + 6 * (size_t)b : nullptr);
+  if (bad) atomicOr(&d.status[0], ST_NONFINITE);
+}
+
+}  // namespace og

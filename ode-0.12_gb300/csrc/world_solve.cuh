@@ -6,47 +6,54 @@
 namespace og {
 
 // Phase 2 (quickstep.cpp:600-665): world-frame inverse inertia, gyroscopic
-// torque and gravity for every body of the world.
-OG_D void phase_body_prologue(const BatchDev& d, const WorldDesc& D, int lane) {
-  for (int b = lane; b < D.nb; b += 32) {
-    const int gb = D.body_off + b;
-    float R[12], tmp[12], invIb[12], invIw[12];
-    body_R(d, gb, R);
-    const float* ib = d.invI + 9 * gb;
-    for (int r = 0; r < 3; ++r) {
-      invIb[r * 4 + 0] = ib[r * 3 + 0]; invIb[r * 4 + 1] = ib[r * 3 + 1];
-      invIb[r * 4 + 2] = ib[r * 3 + 2]; invIb[r * 4 + 3] = 0.f;
-    }
-    mul2_333(tmp, invIb, R);
-    mul0_333(invIw, R, tmp);
-    float* out = d.invIw + 12 * gb;
-    for (int k = 0; k < 12; ++k) out[k] = invIw[k];
-    float4 t = d.tacc[gb];
-    const float4 av = d.avel[gb];
-    if (d.bflags[gb] & BODY_GYROSCOPIC) {
-      float Ib[12], Iw[12], t3[3], cr[3];
-      const float* ii = d.I + 9 * gb;
-      for (int r = 0; r < 3; ++r) {
-        Ib[r * 4 + 0] = ii[r * 3 + 0]; Ib[r * 4 + 1] = ii[r * 3 + 1];
-        Ib[r * 4 + 2] = ii[r * 3 + 2]; Ib[r * 4 + 3] = 0.f;
-      }
-      mul2_333(tmp, Ib, R);
-      mul0_333(Iw, R, tmp);
-      const float w3[3] = {av.x, av.y, av.z};
-      mul0_331(t3, Iw, w3);
-      cross3(cr, w3, t3);
-      t.x = t.x - cr[0]; t.y = t.y - cr[1]; t.z = t.z - cr[2];
-      d.tacc[gb] = t;
-    }
-    if (!(d.bflags[gb] & BODY_NO_GRAVITY)) {
-      float4 f = d.facc[gb];
-      const float m = d.mass[gb];
-      if (D.gravity[0] != 0.f) f.x += m * D.gravity[0];
-      if (D.gravity[1] != 0.f) f.y += m * D.gravity[1];
-      if (D.gravity[2] != 0.f) f.z += m * D.gravity[2];
-      d.facc[gb] = f;
-    }
+// torque and gravity of one body (global index gb).
+OG_D void body_prologue(const BatchDev& d, const WorldDesc& D, int gb) {
+  float R[12], tmp[12], invIb[12], invIw[12];
+  body_R(d, gb, R);
+  const float* ib = d.invI + 9 * gb;
+  for (int r = 0; r < 3; ++r) {
+    invIb[r * 4 + 0] = ib[r * 3 + 0]; invIb[r * 4 + 1] = ib[r * 3 + 1];
+    invIb[r * 4 + 2] = ib[r * 3 + 2]; invIb[r * 4 + 3] = 0.f;
   }
+  mul2_333(tmp, invIb, R);
+  mul0_333(invIw, R, tmp);
+  float* out = d.invIw + 12 * gb;
+  for (int k = 0; k < 12; ++k) out[k] = invIw[k];
+  float4 t = d.tacc[gb];
+  const float4 av = d.avel[gb];
+  if (d.bflags[gb] & BODY_GYROSCOPIC) {
+    float Ib[12], Iw[12], t3[3], cr[3];
+    const float* ii = d.I + 9 * gb;
+    for (int r = 0; r < 3; ++r) {
+      Ib[r * 4 + 0] = ii[r * 3 + 0]; Ib[r * 4 + 1] = ii[r * 3 + 1];
+      Ib[r * 4 + 2] = ii[r * 3 + 2]; Ib[r * 4 + 3] = 0.f;
+    }
+    mul2_333(tmp, Ib, R);
+    mul0_333(Iw, R, tmp);
+    const float w3[3] = {av.x, av.y, av.z};
+    mul0_331(t3, Iw, w3);
+    cross3(cr, w3, t3);
+    t.x = t.x - cr[0]; t.y = t.y - cr[1]; t.z = t.z - cr[2];
+    d.tacc[gb] = t;
+  }
+  if (!(d.bflags[gb] & BODY_NO_GRAVITY)) {
+    float4 f = d.facc[gb];
+    const float m = d.mass[gb];
+    if (D.gravity[0] != 0.f) f.x += m * D.gravity[0];
+    if (D.gravity[1] != 0.f) f.y += m * D.gravity[1];
+    if (D.gravity[2] != 0.f) f.z += m * D.gravity[2];
+    d.facc[gb] = f;
+  }
+}
+OG_D void phase_body_prologue(const BatchDev& d, const WorldDesc& D, int lane) {
+  for (int b = lane; b < D.nb; b += 32) body_prologue(d, D, D.body_off + b);
+}
+
+// the step's row of per-joint stops (dJointSet*Param lo/hi stop before the step), or null
+OG_D const float* step_stops(const BatchDev& d, const WorldDesc& D, int step) {
+  const int njt = d.world[d.n_worlds - 1].joint_off + d.world[d.n_worlds - 1].njp;
+  return (d.joint_stop && d.n_ctrl_steps > 0) ? d.joint_stop + (size_t)(step % d.n_ctrl_steps) * njt + D.joint_off
+                                               : nullptr;
 }
 
 // limot1 as getInfo sees it this step: the stored one with the step's stops
@@ -60,17 +67,81 @@ OG_D DevLimot step_limot1(const DevJoint& J, const float* stops, int ord) {
   return L;
 }
 
+// getInfo2 of one joint (ordinal ord: persistent joints first, then
+// contacts) into its m rows starting at world row r0, with the erp it meets
+// (quickstep.cpp:763-830): rows cleared to the stepper's defaults, the
+// joint's rows, powered-at-limit motor forces added to the bodies, and findex
+// rebased to world rows.
+OG_D void assemble_joint_rows(const BatchDev& d, const WorldDesc& D, int ord, int r0, int m, float erp,
+                              const float* stops, float* dbg_rows) {
+  const float h1 = 1.0f / D.dt;
+  float* rows = d.rows + (size_t)(D.row_off + r0) * kRowWords;
+  int b1, b2;
+  joint_bodies(d, D, ord, b1, b2);
+  for (int r = 0; r < m; ++r) {
+    float* row = rows + r * kRowWords;
+    for (int q = 0; q < 12; ++q) row[q] = 0.f;
+    row[kRowC] = 0.f;
+    row[kRowCfm] = D.cfm;
+    row[kRowLo] = -INFINITY;
+    row[kRowHi] = INFINITY;
+    reinterpret_cast<int*>(row)[kRowFindex] = -1;
+    reinterpret_cast<int*>(row)[kRowB1] = b1;
+    reinterpret_cast<int*>(row)[kRowB2] = b2;
+    reinterpret_cast<int*>(row)[kRowJoint] = ord;
+  }
+  Info2 in;
+  in.fps = h1;
+  in.erp = erp;
+  in.rows = rows;
+  BodyRef B1, B2;
+  load_body_ref(d, D.body_off + b1, B1);
+  if (b2 >= 0) load_body_ref(d, D.body_off + b2, B2);
+  const BodyRef* pB2 = b2 >= 0 ? &B2 : nullptr;
+  if (ord < D.njp) {
+    const DevJoint& J = d.joints[D.joint_off + ord];
+    const DevLimot lm1 = step_limot1(J, stops, ord);
+    const JointInfo1 i1 = persistent_info1(J, lm1, B1, pB2);
+    LimotForce t1 = limot_force_none(), t2 = limot_force_none();
+    persistent_info2(J, lm1, i1, B1, pB2, in, t1, t2);
+    // a powered motor pushing against a limit adds force / torque inside
+    // getInfo2 (joint.cpp:612-660); concurrent additions are rare and use atomics
+    for (int t = 0; t < 2; ++t) {
+      const LimotForce& tq = t ? t2 : t1;
+      if (!tq.active) continue;
+      float* fa = reinterpret_cast<float*>(&d.facc[D.body_off + b1]);
+      float* ta = reinterpret_cast<float*>(&d.tacc[D.body_off + b1]);
+      for (int k = 0; k < 3; ++k) {
+        if (tq.f1[k] != 0.f) atomicAdd(fa + k, tq.f1[k]);
+        atomicAdd(ta + k, tq.t1[k]);
+      }
+      if (b2 >= 0) {
+        float* fb = reinterpret_cast<float*>(&d.facc[D.body_off + b2]);
+        float* tb = reinterpret_cast<float*>(&d.tacc[D.body_off + b2]);
+        for (int k = 0; k < 3; ++k) {
+          if (tq.f1[k] != 0.f) atomicAdd(fb + k, -tq.f1[k]);
+          atomicAdd(tb + k, tq.t2[k]);
+        }
+      }
+    }
+  } else {
+    const DevContact& ct = d.contacts[D.contact_off + ord - D.njp];
+    contact_info2(ct, d.surfaces[ct.surface], m, B1, pB2, D.min_depth, D.max_vel, in);
+  }
+  for (int r = 0; r < m; ++r) {
+    int* fi = reinterpret_cast<int*>(rows + r * kRowWords) + kRowFindex;
+    if (*fi != -1) *fi += r0;
+  }
+  if (dbg_rows)
+    for (int r = 0; r < m; ++r) dbg_rows[(size_t)(D.row_off + r0 + r) * kRowWords + kDbgErp] = in.erp;
+}
+
 // Phase 4: getInfo1 / getInfo2 over the joints in island order. Returns the
 // total row count M (or -1 when it exceeds the world's capacity).
 OG_D int phase_rows(const BatchDev& d, const WorldDesc& D, int w, int nj, int nisl, int lane, int step,
                       float* dbg_rows) {
-  // per-step stops (dJointSetHinge{,2}Param lo/hi stop before the step)
-  const int njt = d.world[d.n_worlds - 1].joint_off + d.world[d.n_worlds - 1].njp;
-  const float* stops = (d.joint_stop && d.n_ctrl_steps > 0)
-                           ? d.joint_stop + (size_t)(step % d.n_ctrl_steps) * njt + D.joint_off
-                           : nullptr;
+  const float* stops = step_stops(d, D, step);
   const int jl_off = D.joint_off + D.contact_off;
-  const float h1 = 1.0f / D.dt;
   // pass 1: m per joint, prefix -> first row
   int carry = 0;
   for (int base = 0; base < nj; base += 32) {
@@ -146,167 +217,115 @@ OG_D int phase_rows(const BatchDev& d, const WorldDesc& D, int w, int nj, int ni
       if (lb >= 0 && lb >= ls) erp_carry = lb_erp;
       else if (ls >= 0) erp_carry = D.erp;
     }
-    if (k < nj) {
-      const int r0 = d.jrow[jl_off + k], m = d.jm[jl_off + k];
-      float* rows = d.rows + (size_t)(D.row_off + r0) * kRowWords;
-      int b1, b2;
-      joint_bodies(d, D, ord, b1, b2);
-      for (int r = 0; r < m; ++r) {
-        float* row = rows + r * kRowWords;
-        for (int q = 0; q < 12; ++q) row[q] = 0.f;
-        row[kRowC] = 0.f;
-        row[kRowCfm] = D.cfm;
-        row[kRowLo] = -INFINITY;
-        row[kRowHi] = INFINITY;
-        reinterpret_cast<int*>(row)[kRowFindex] = -1;
-        reinterpret_cast<int*>(row)[kRowB1] = b1;
-        reinterpret_cast<int*>(row)[kRowB2] = b2;
-        reinterpret_cast<int*>(row)[kRowJoint] = ord;
-      }
-      Info2 in;
-      in.fps = h1;
-      in.erp = erp;
-      in.rows = rows;
-      BodyRef B1, B2;
-      load_body_ref(d, D.body_off + b1, B1);
-      if (b2 >= 0) load_body_ref(d, D.body_off + b2, B2);
-      const BodyRef* pB2 = b2 >= 0 ? &B2 : nullptr;
-      if (ord < D.njp) {
-        const DevJoint& J = d.joints[D.joint_off + ord];
-        const DevLimot lm1 = step_limot1(J, stops, ord);
-        const JointInfo1 i1 = persistent_info1(J, lm1, B1, pB2);
-        LimotForce t1 = limot_force_none(), t2 = limot_force_none();
-        persistent_info2(J, lm1, i1, B1, pB2, in, t1, t2);
-        // a powered motor pushing against a limit adds force / torque inside
-        // getInfo2 (joint.cpp:612-660); concurrent additions are rare and use atomics
-        for (int t = 0; t < 2; ++t) {
-          const LimotForce& tq = t ? t2 : t1;
-          if (!tq.active) continue;
-          float* fa = reinterpret_cast<float*>(&d.facc[D.body_off + b1]);
-          float* ta = reinterpret_cast<float*>(&d.tacc[D.body_off + b1]);
-          for (int k = 0; k < 3; ++k) {
-            if (tq.f1[k] != 0.f) atomicAdd(fa + k, tq.f1[k]);
-            atomicAdd(ta + k, tq.t1[k]);
-          }
-          if (b2 >= 0) {
-            float* fb = reinterpret_cast<float*>(&d.facc[D.body_off + b2]);
-            float* tb = reinterpret_cast<float*>(&d.tacc[D.body_off + b2]);
-            for (int k = 0; k < 3; ++k) {
-              if (tq.f1[k] != 0.f) atomicAdd(fb + k, -tq.f1[k]);
-              atomicAdd(tb + k, tq.t2[k]);
-            }
-          }
-        }
-      } else {
-        const DevContact& ct = d.contacts[D.contact_off + ord - D.njp];
-        contact_info2(ct, d.surfaces[ct.surface], m, B1, pB2, D.min_depth, D.max_vel, in);
-      }
-      for (int r = 0; r < m; ++r) {
-        int* fi = reinterpret_cast<int*>(rows + r * kRowWords) + kRowFindex;
-        if (*fi != -1) *fi += r0;
-      }
-      if (dbg_rows)
-        for (int r = 0; r < m; ++r) dbg_rows[(size_t)(D.row_off + r0 + r) * kRowWords + kDbgErp] = in.erp;
-    }
+    if (k < nj)
+      assemble_joint_rows(d, D, ord, d.jrow[jl_off + k], d.jm[jl_off + k], erp, stops, dbg_rows);
   }
   __syncwarp();
   return M;
 }
 
-// Phase 5: rhs, cfm/h, iMJ, Ad and the J/b scaling per row; tmp1 per body is
-// staged in S.fc first (quickstep.cpp:836-857 then :117-136, :370-402).
+// Phase 5 (quickstep.cpp:836-857): tmp1 = invM * fe + v / h of one body
+// (global index gb), written to out[6].
+OG_D void body_tmp1(const BatchDev& d, int gb, float h1, float* out) {
+  const float4 f = d.facc[gb], t = d.tacc[gb], lv = d.lvel[gb], av = d.avel[gb];
+  const float im = d.invMass[gb];
+  float* t1 = out;
+  t1[0] = f.x * im + lv.x * h1;
+  t1[1] = f.y * im + lv.y * h1;
+  t1[2] = f.z * im + lv.z * h1;
+  const float* iw = d.invIw + 12 * gb;
+  const float t3[3] = {t.x, t.y, t.z};
+  float r3[3];
+  mul0_331(r3, iw, t3);
+  t1[3] = r3[0] + av.x * h1;
+  t1[4] = r3[1] + av.y * h1;
+  t1[5] = r3[2] + av.z * h1;
+}
+
+// Phase 5 for one row (world-local index r): rhs = c / h - J tmp1, cfm / h,
+// iMJ = invM J^T, Ad = w / (J iMJ + cfm), then J, rhs and cfm scaled by Ad
+// (quickstep.cpp:117-136, :370-402). tmp1 holds 6 floats per world-local body.
+OG_D void row_setup(const BatchDev& d, const WorldDesc& D, int r, const float* tmp1, float h1, float sor_w,
+                    float* dbg_rows, float* jcopy) {
+  float* row = d.rows + (size_t)(D.row_off + r) * kRowWords;
+  float4* row4 = reinterpret_cast<float4*>(row);
+  float J[12];
+  {
+    const float4 a = row4[0], b = row4[1], c = row4[2];
+    J[0] = a.x; J[1] = a.y; J[2] = a.z; J[3] = a.w;
+    J[4] = b.x; J[5] = b.y; J[6] = b.z; J[7] = b.w;
+    J[8] = c.x; J[9] = c.y; J[10] = c.z; J[11] = c.w;
+  }
+  const float4 w6 = row4[6];
+  const int4 w7 = reinterpret_cast<const int4*>(row4)[7];
+  const int b1 = w7.y, b2 = w7.z;
+  // multiply_J: rhs = J * tmp1
+  float sum = 0.f;
+  {
+    const float* in = tmp1 + 6 * b1;
+    for (int j = 0; j < 6; ++j) sum += J[j] * in[j];
+    if (b2 != -1) {
+      in = tmp1 + 6 * b2;
+      for (int j = 0; j < 6; ++j) sum += J[6 + j] * in[j];
+    }
+  }
+  const float rhs = w6.x * h1 - sum;
+  const float cfm = w6.y * h1;
+  if (jcopy) {
+    float4* o = reinterpret_cast<float4*>(jcopy + (size_t)(D.row_off + r) * 12);
+    o[0] = make_float4(J[0], J[1], J[2], J[3]);
+    o[1] = make_float4(J[4], J[5], J[6], J[7]);
+    o[2] = make_float4(J[8], J[9], J[10], J[11]);
+  }
+  if (dbg_rows) {
+    float* o = dbg_rows + (size_t)(D.row_off + r) * kRowWords;
+    for (int q = 0; q < 12; ++q) o[q] = J[q];
+    o[kRowC] = rhs; o[kRowCfm] = cfm; o[kRowLo] = w6.z; o[kRowHi] = w6.w;
+    reinterpret_cast<int*>(o)[kRowFindex] = w7.x;
+    reinterpret_cast<int*>(o)[kRowB1] = b1;
+    reinterpret_cast<int*>(o)[kRowB2] = b2;
+    reinterpret_cast<int*>(o)[kRowJoint] = w7.w;
+  }
+  // compute_invM_JT
+  float iMJ[12];
+  {
+    const int g1 = D.body_off + b1;
+    const float k1 = d.invMass[g1];
+    for (int j = 0; j < 3; ++j) iMJ[j] = k1 * J[j];
+    mul0_331(iMJ + 3, d.invIw + 12 * g1, J + 3);
+    if (b2 != -1) {
+      const int g2 = D.body_off + b2;
+      const float k2 = d.invMass[g2];
+      for (int j = 0; j < 3; ++j) iMJ[6 + j] = k2 * J[6 + j];
+      mul0_331(iMJ + 9, d.invIw + 12 * g2, J + 9);
+    } else {
+      for (int j = 6; j < 12; ++j) iMJ[j] = 0.f;
+    }
+  }
+  float s = 0.f;
+  for (int j = 0; j < 6; ++j) s += iMJ[j] * J[j];
+  if (b2 != -1)
+    for (int j = 6; j < 12; ++j) s += iMJ[j] * J[j];
+  const float Ad = sor_w / (s + cfm);
+  if (dbg_rows) dbg_rows[(size_t)(D.row_off + r) * kRowWords + kDbgAd] = Ad;
+  for (int j = 0; j < 12; ++j) J[j] *= Ad;
+  row4[0] = make_float4(J[0], J[1], J[2], J[3]);
+  row4[1] = make_float4(J[4], J[5], J[6], J[7]);
+  row4[2] = make_float4(J[8], J[9], J[10], J[11]);
+  row4[3] = make_float4(iMJ[0], iMJ[1], iMJ[2], iMJ[3]);
+  row4[4] = make_float4(iMJ[4], iMJ[5], iMJ[6], iMJ[7]);
+  row4[5] = make_float4(iMJ[8], iMJ[9], iMJ[10], iMJ[11]);
+  row4[6] = make_float4(rhs * Ad, Ad * cfm, w6.z, w6.w);
+}
+
+// Phase 5 over a world's rows; tmp1 per body is staged in S.fc first.
 OG_D void phase_row_setup(const BatchDev& d, const WorldDesc& D, int M, const WarpSmem& S, int lane,
                           float* dbg_rows, float* jcopy) {
   const float h1 = 1.0f / D.dt;
-  for (int b = lane; b < D.nb; b += 32) {
-    const int gb = D.body_off + b;
-    const float4 f = d.facc[gb], t = d.tacc[gb], lv = d.lvel[gb], av = d.avel[gb];
-    const float im = d.invMass[gb];
-    float* t1 = S.fc + 6 * b;
-    t1[0] = f.x * im + lv.x * h1;
-    t1[1] = f.y * im + lv.y * h1;
-    t1[2] = f.z * im + lv.z * h1;
-    const float* iw = d.invIw + 12 * gb;
-    const float t3[3] = {t.x, t.y, t.z};
-    float r3[3];
-    mul0_331(r3, iw, t3);
-    t1[3] = r3[0] + av.x * h1;
-    t1[4] = r3[1] + av.y * h1;
-    t1[5] = r3[2] + av.z * h1;
-  }
+  for (int b = lane; b < D.nb; b += 32) body_tmp1(d, D.body_off + b, h1, S.fc + 6 * b);
   __syncwarp();
   const float sor_w = D.sor_w;
-  for (int r = lane; r < M; r += 32) {
-    float* row = d.rows + (size_t)(D.row_off + r) * kRowWords;
-    float4* row4 = reinterpret_cast<float4*>(row);
-    float J[12];
-    {
-      const float4 a = row4[0], b = row4[1], c = row4[2];
-      J[0] = a.x; J[1] = a.y; J[2] = a.z; J[3] = a.w;
-      J[4] = b.x; J[5] = b.y; J[6] = b.z; J[7] = b.w;
-      J[8] = c.x; J[9] = c.y; J[10] = c.z; J[11] = c.w;
-    }
-    const float4 w6 = row4[6];
-    const int4 w7 = reinterpret_cast<const int4*>(row4)[7];
-    const int b1 = w7.y, b2 = w7.z;
-    // multiply_J: rhs = J * tmp1
-    float sum = 0.f;
-    {
-      const float* in = S.fc + 6 * b1;
-      for (int j = 0; j < 6; ++j) sum += J[j] * in[j];
-      if (b2 != -1) {
-        in = S.fc + 6 * b2;
-        for (int j = 0; j < 6; ++j) sum += J[6 + j] * in[j];
-      }
-    }
-    const float rhs = w6.x * h1 - sum;
-    const float cfm = w6.y * h1;
-    if (jcopy) {
-      float4* o = reinterpret_cast<float4*>(jcopy + (size_t)(D.row_off + r) * 12);
-      o[0] = make_float4(J[0], J[1], J[2], J[3]);
-      o[1] = make_float4(J[4], J[5], J[6], J[7]);
-      o[2] = make_float4(J[8], J[9], J[10], J[11]);
-    }
-    if (dbg_rows) {
-      float* o = dbg_rows + (size_t)(D.row_off + r) * kRowWords;
-      for (int q = 0; q < 12; ++q) o[q] = J[q];
-      o[kRowC] = rhs; o[kRowCfm] = cfm; o[kRowLo] = w6.z; o[kRowHi] = w6.w;
-      reinterpret_cast<int*>(o)[kRowFindex] = w7.x;
-      reinterpret_cast<int*>(o)[kRowB1] = b1;
-      reinterpret_cast<int*>(o)[kRowB2] = b2;
-      reinterpret_cast<int*>(o)[kRowJoint] = w7.w;
-    }
-    // compute_invM_JT
-    float iMJ[12];
-    {
-      const int g1 = D.body_off + b1;
-      const float k1 = d.invMass[g1];
-      for (int j = 0; j < 3; ++j) iMJ[j] = k1 * J[j];
-      mul0_331(iMJ + 3, d.invIw + 12 * g1, J + 3);
-      if (b2 != -1) {
-        const int g2 = D.body_off + b2;
-        const float k2 = d.invMass[g2];
-        for (int j = 0; j < 3; ++j) iMJ[6 + j] = k2 * J[6 + j];
-        mul0_331(iMJ + 9, d.invIw + 12 * g2, J + 9);
-      } else {
-        for (int j = 6; j < 12; ++j) iMJ[j] = 0.f;
-      }
-    }
-    float s = 0.f;
-    for (int j = 0; j < 6; ++j) s += iMJ[j] * J[j];
-    if (b2 != -1)
-      for (int j = 6; j < 12; ++j) s += iMJ[j] * J[j];
-    const float Ad = sor_w / (s + cfm);
-    if (dbg_rows) dbg_rows[(size_t)(D.row_off + r) * kRowWords + kDbgAd] = Ad;
-    for (int j = 0; j < 12; ++j) J[j] *= Ad;
-    row4[0] = make_float4(J[0], J[1], J[2], J[3]);
-    row4[1] = make_float4(J[4], J[5], J[6], J[7]);
-    row4[2] = make_float4(J[8], J[9], J[10], J[11]);
-    row4[3] = make_float4(iMJ[0], iMJ[1], iMJ[2], iMJ[3]);
-    row4[4] = make_float4(iMJ[4], iMJ[5], iMJ[6], iMJ[7]);
-    row4[5] = make_float4(iMJ[8], iMJ[9], iMJ[10], iMJ[11]);
-    row4[6] = make_float4(rhs * Ad, Ad * cfm, w6.z, w6.w);
-  }
+  for (int r = lane; r < M; r += 32) row_setup(d, D, r, S.fc, h1, sor_w, dbg_rows, jcopy);
   __syncwarp();
 }
 
@@ -346,72 +365,79 @@ OG_D void phase_feedback(const BatchDev& d, const WorldDesc& D, int w, const flo
   }
 }
 
-// Phase 7: velocity update from the constraint forces and external forces,
-// then dxStepBody (quickstep.cpp:905-916, :960-975, :1001-1021; util.cpp:255-360).
+// Phase 7 for one body (global index gb): velocity update from the
+// constraint forces cforce[6] (null: none) and the external forces, then
+// dxStepBody (quickstep.cpp:905-916, :960-975, :1001-1021; util.cpp:255-360).
+// Returns true when the new state is not finite.
+OG_D bool integrate_body(const BatchDev& d, const WorldDesc& D, int gb, const float* cforce) {
+  const float h = D.dt;
+  float4 lv = d.lvel[gb], av = d.avel[gb];
+  if (cforce) {
+    const float* fc = cforce;
+    lv.x += h * fc[0]; lv.y += h * fc[1]; lv.z += h * fc[2];
+    av.x += h * fc[3]; av.y += h * fc[4]; av.z += h * fc[5];
+  }
+  const float4 f = d.facc[gb];
+  float4 t = d.tacc[gb];
+  const float hm = h * d.invMass[gb];
+  lv.x += hm * f.x; lv.y += hm * f.y; lv.z += hm * f.z;
+  t.x *= h; t.y *= h; t.z *= h;
+  {
+    const float t3[3] = {t.x, t.y, t.z};
+    float r3[3];
+    mul0_331(r3, d.invIw + 12 * gb, t3);
+    av.x = av.x + r3[0]; av.y = av.y + r3[1]; av.z = av.z + r3[2];
+  }
+  float4 p = d.pos[gb];
+  p.x += h * lv.x; p.y += h * lv.y; p.z += h * lv.z;
+  const float4 q4 = d.q[gb];
+  float q[4] = {q4.x, q4.y, q4.z, q4.w};
+  float dq[4];
+  dq[0] = 0.5f * (-av.x * q[1] - av.y * q[2] - av.z * q[3]);
+  dq[1] = 0.5f * (av.x * q[0] + av.y * q[3] - av.z * q[2]);
+  dq[2] = 0.5f * (-av.x * q[3] + av.y * q[0] + av.z * q[1]);
+  dq[3] = 0.5f * (av.x * q[2] - av.y * q[1] + av.z * q[0]);
+  for (int j = 0; j < 4; j++) q[j] += h * dq[j];
+  normalize4(q);
+  d.pos[gb] = p;
+  d.q[gb] = make_float4(q[0], q[1], q[2], q[3]);
+  d.lvel[gb] = lv;
+  d.avel[gb] = av;
+  if (!(isfinite(p.x) && isfinite(p.y) && isfinite(p.z) && isfinite(lv.x) && isfinite(lv.y) &&
+        isfinite(lv.z) && isfinite(av.x) && isfinite(av.y) && isfinite(av.z)))
+    return true;
+  return false;
+}
 OG_D void phase_integrate(const BatchDev& d, const WorldDesc& D, int w, const float* cforce, int lane,
                           bool have_rows) {
-  const float h = D.dt;
   bool bad = false;
-  for (int b = lane; b < D.nb; b += 32) {
-    const int gb = D.body_off + b;
-    float4 lv = d.lvel[gb], av = d.avel[gb];
-    if (have_rows) {
-      const float* fc = cforce + 6 * b;
-      lv.x += h * fc[0]; lv.y += h * fc[1]; lv.z += h * fc[2];
-      av.x += h * fc[3]; av.y += h * fc[4]; av.z += h * fc[5];
-    }
-    const float4 f = d.facc[gb];
-    float4 t = d.tacc[gb];
-    const float hm = h * d.invMass[gb];
-    lv.x += hm * f.x; lv.y += hm * f.y; lv.z += hm * f.z;
-    t.x *= h; t.y *= h; t.z *= h;
-    {
-      const float t3[3] = {t.x, t.y, t.z};
-      float r3[3];
-      mul0_331(r3, d.invIw + 12 * gb, t3);
-      av.x = av.x + r3[0]; av.y = av.y + r3[1]; av.z = av.z + r3[2];
-    }
-    float4 p = d.pos[gb];
-    p.x += h * lv.x; p.y += h * lv.y; p.z += h * lv.z;
-    const float4 q4 = d.q[gb];
-    float q[4] = {q4.x, q4.y, q4.z, q4.w};
-    float dq[4];
-    dq[0] = 0.5f * (-av.x * q[1] - av.y * q[2] - av.z * q[3]);
-    dq[1] = 0.5f * (av.x * q[0] + av.y * q[3] - av.z * q[2]);
-    dq[2] = 0.5f * (-av.x * q[3] + av.y * q[0] + av.z * q[1]);
-    dq[3] = 0.5f * (av.x * q[2] - av.y * q[1] + av.z * q[0]);
-    for (int j = 0; j < 4; j++) q[j] += h * dq[j];
-    normalize4(q);
-    d.pos[gb] = p;
-    d.q[gb] = make_float4(q[0], q[1], q[2], q[3]);
-    d.lvel[gb] = lv;
-    d.avel[gb] = av;
-    if (!(isfinite(p.x) && isfinite(p.y) && isfinite(p.z) && isfinite(lv.x) && isfinite(lv.y) &&
-          isfinite(lv.z) && isfinite(av.x) && isfinite(av.y) && isfinite(av.z)))
-      bad = true;
-  }
+  for (int b = lane; b < D.nb; b += 32)
+    bad |= integrate_body(d, D, D.body_off + b, have_rows ? cforce + 6 * b : nullptr);
   if (__any_sync(kFull, bad) && lane == 0) atomicOr(&d.status[w], ST_NONFINITE);
 }
 
 // Phase 0: per-step controls into the accumulators, in the reference's order
 // (the caller's dBodyAdd* / dJointAdd*Torque calls precede dWorldQuickStep).
-OG_D void phase_controls(const BatchDev& d, const WorldDesc& D, int step, int lane) {
+// the body forces of the step (global body index gb), replacing last step's accumulators
+OG_D void controls_body(const BatchDev& d, int step, int gb) {
   const int nbt = d.world[d.n_worlds - 1].body_off + d.world[d.n_worlds - 1].nb;
+  const int cs = d.n_ctrl_steps > 0 ? step % d.n_ctrl_steps : 0;
+  float4 f = make_float4(0.f, 0.f, 0.f, 0.f), t = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (d.body_force && d.n_ctrl_steps > 0) {
+    const float* bf = d.body_force + ((size_t)cs * nbt + gb) * 6;
+    f = make_float4(bf[0], bf[1], bf[2], 0.f);
+    t = make_float4(bf[3], bf[4], bf[5], 0.f);
+  }
+  d.facc[gb] = f;
+  d.tacc[gb] = t;
+}
+
+// the joint torques / forces of the step, added joint by joint in creation
+// order (one thread)
+OG_D void controls_joints(const BatchDev& d, const WorldDesc& D, int step) {
   const int njt = d.world[d.n_worlds - 1].joint_off + d.world[d.n_worlds - 1].njp;
   const int cs = d.n_ctrl_steps > 0 ? step % d.n_ctrl_steps : 0;
-  for (int b = lane; b < D.nb; b += 32) {
-    const int gb = D.body_off + b;
-    float4 f = make_float4(0.f, 0.f, 0.f, 0.f), t = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (d.body_force && d.n_ctrl_steps > 0) {
-      const float* bf = d.body_force + ((size_t)cs * nbt + gb) * 6;
-      f = make_float4(bf[0], bf[1], bf[2], 0.f);
-      t = make_float4(bf[3], bf[4], bf[5], 0.f);
-    }
-    d.facc[gb] = f;
-    d.tacc[gb] = t;
-  }
-  __syncwarp();
-  if (d.joint_torque && d.n_ctrl_steps > 0 && lane == 0) {
+  if (d.joint_torque && d.n_ctrl_steps > 0) {
     for (int j = 0; j < D.njp; ++j) {
       const DevJoint& J = d.joints[D.joint_off + j];
       const float* tq = d.joint_torque + ((size_t)cs * njt + D.joint_off + j) * 2;
@@ -505,6 +531,12 @@ OG_D void phase_controls(const BatchDev& d, const WorldDesc& D, int step, int la
       }
     }
   }
+}
+
+OG_D void phase_controls(const BatchDev& d, const WorldDesc& D, int step, int lane) {
+  for (int b = lane; b < D.nb; b += 32) controls_body(d, step, D.body_off + b);
+  __syncwarp();
+  if (lane == 0) controls_joints(d, D, step);
   __syncwarp();
 }
 

@@ -13,7 +13,7 @@ BODY_REC = 13
 
 class BatchConfig(C.Structure):
     _fields_ = [("contacts_per_body", C.c_int), ("warps_per_block", C.c_int),
-                ("device", C.c_int)]
+                ("device", C.c_int), ("large_world", C.c_int)]
 
 
 class Batch:
@@ -23,9 +23,9 @@ class Batch:
     launch; ``state()`` returns [nb_total, 13] FP64 records
     (pos[3], q[4], lvel[3], avel[3])."""
 
-    def __init__(self, scene, contacts_per_body=8, warps_per_block=0, device=0):
+    def __init__(self, scene, contacts_per_body=8, warps_per_block=0, device=0, large_world=False):
         self.scene = scene
-        cfg = BatchConfig(contacts_per_body, warps_per_block, device)
+        cfg = BatchConfig(contacts_per_body, warps_per_block, device, 1 if large_world else 0)
         h = C.c_void_p()
         check(lib().odegpuBatchCreate(C.byref(scene.c), C.byref(cfg), C.byref(h)))
         self.h = h

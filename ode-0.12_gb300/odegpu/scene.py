@@ -887,3 +887,36 @@ def _R_from_q(q):
     return np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y)],
                      [2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x)],
                      [2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)]])
+
+
+def sphere_pile(n=10000, seed=14, box=(6.0, 6.0, 20.0), rmin=0.1, rmax=0.3, mu=0.8, iterations=50,
+                dt=0.005, jitter=0.05):
+    """Large single world: n spheres, r U[rmin, rmax], density 1000, on a
+    jittered grid (cells of equal size filling the box, lowest layers first,
+    offsets U[-jitter, jitter] of a cell) inside a box[0] x box[1] x box[2] m
+    box centred on x = y = 0 whose five static planes are the floor z = 0 and
+    the four walls (created first, then one geom per sphere). Surface mu 0.8
+    (Approx1 | SoftERP | SoftCFM, soft_erp 0.2, soft_cfm 1e-5), 50 iterations,
+    w = 1.3, dt = 0.005, <= 4 contacts per pair. With the defaults neighbouring
+    spheres overlap at the start and the pile settles under gravity."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    b = SceneBuilder()
+    s = _std_surface(b, mu)
+    bx, by, bz = box
+    w = b.new_world(cfm=1e-5, iterations=iterations, dt=dt, seed=int(rng.integers(0, 2**32)))
+    for pl in ((0, 0, 1, 0), (1, 0, 0, -bx / 2), (-1, 0, 0, -bx / 2), (0, 1, 0, -by / 2), (0, -1, 0, -by / 2)):
+        b.add_geom(w, GEOM_PLANE, -1, pl, s)
+    cell = (bx * by * bz / n) ** (1.0 / 3.0)
+    nx, ny = max(1, int(bx / cell)), max(1, int(by / cell))
+    nz = -(-n // (nx * ny))
+    dx, dy, dz = bx / nx, by / ny, bz / nz
+    for k in range(n):
+        iz, rem = divmod(k, nx * ny)
+        iy, ix = divmod(rem, nx)
+        j = rng.uniform(-jitter, jitter, 3)
+        pos = (-bx / 2 + (ix + 0.5 + j[0]) * dx, -by / 2 + (iy + 0.5 + j[1]) * dy, (iz + 0.5 + j[2]) * dz)
+        r = rng.uniform(rmin, rmax)
+        m, I = sphere_mass(1000.0, r)
+        bi = b.add_body(w, pos, m, I)
+        b.add_geom(w, GEOM_SPHERE, bi, (r,), s)
+    return b.build()
