@@ -62,6 +62,15 @@ typedef struct odegpuBatchConfig {
                               pipeline even when it fits the on-chip kernel     */
 } odegpuBatchConfig;
 
+/* Diagnostics of a large-world batch, accumulated since creation or the last
+ * reset (reset != 0 clears them after reading): out[0] ns in the island walk,
+ * out[1] ns in the sweeps' first iterations, out[2] ns sorting rows by
+ * dependency level, out[3] ns in the remaining iterations, out[4] the largest
+ * level count met, out[5] sweep launches, out[6] island walks, out[7] ns of
+ * the walks spent staging their arrays on chip, out[8] the sweep cluster's
+ * CTA count. No counterpart in the reference. */
+int odegpuBatchLargeWorldStats(odegpuBatchID b, long long* out, int n, int reset);
+
 /* Body state record used by the read/write calls: pos[3] q[4] lvel[3] avel[3]. */
 #define ODEGPU_BODY_REC 13
 

@@ -138,8 +138,12 @@ struct LargeWorld {
   DBuf<float> tmp1;
   DBuf<int> rowisl, neg, draws, order, order2, rnd, tcount, tfill, tlist, bcount, bfill, blist;
   DBuf<int4> prec;
+  DBuf<int> plev, lorder;
+  DBuf<int2> ppred;
+  DBuf<float> rsort;
   DBuf<float> lambda, fc;
   DBuf<int> err;
+  DBuf<unsigned long long> stats;
   int sweep_smem = 0, islands_smem = 0;
 };
 
@@ -575,10 +579,16 @@ static int lw_setup(odegpuBatch* B, const odegpuScene* sc) {
   rc = rc ? rc : W.bfill.alloc(nb);
   rc = rc ? rc : W.blist.alloc(2 * (size_t)R);
   rc = rc ? rc : W.prec.alloc(R);
+  rc = rc ? rc : W.plev.alloc(R);
+  rc = rc ? rc : W.lorder.alloc(R);
+  rc = rc ? rc : W.ppred.alloc(R);
+  rc = rc ? rc : W.rsort.alloc((size_t)R * kRowWords);
   rc = rc ? rc : W.lambda.alloc(R);
   rc = rc ? rc : W.fc.alloc((size_t)nb * 6);
   rc = rc ? rc : W.err.alloc(1);
+  rc = rc ? rc : W.stats.alloc(9);
   if (rc) return rc;
+  OG_CUDA(cudaMemset(W.stats.p, 0, 9 * sizeof(unsigned long long)));
   L.statics = W.statics.p; L.ghash = W.ghash.p; L.hcount = W.hcount.p; L.hfill = W.hfill.p;
   L.hgeoms = W.hgeoms.p; L.plist = W.plist.p; L.pcnt = W.pcnt.p; L.own = W.own.p; L.sflag = W.sflag.p;
   L.pair_i = W.pair_i.p; L.pair_k = W.pair_k.p; L.npairs = W.npairs.p; L.pnc = W.pnc.p;
@@ -588,8 +598,9 @@ static int lw_setup(odegpuBatch* B, const odegpuScene* sc) {
   L.bfk = W.bfk.p; L.rstart = W.rstart.p; L.tmp1 = W.tmp1.p; L.rowisl = W.rowisl.p; L.neg = W.neg.p;
   L.draws = W.draws.p; L.order = W.order.p; L.order2 = W.order2.p; L.rnd = W.rnd.p;
   L.tcount = W.tcount.p; L.tfill = W.tfill.p; L.tlist = W.tlist.p; L.bcount = W.bcount.p;
-  L.bfill = W.bfill.p; L.blist = W.blist.p; L.prec = W.prec.p; L.lambda = W.lambda.p; L.fc = W.fc.p;
+  L.bfill = W.bfill.p; L.blist = W.blist.p; L.prec = W.prec.p; L.plev = W.plev.p; L.lorder = W.lorder.p; L.ppred = W.ppred.p; L.rsort = W.rsort.p; L.lambda = W.lambda.p; L.fc = W.fc.p;
   L.err = W.err.p;
+  L.stats = W.stats.p;
   int optin = 0;
   OG_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, B->device));
   const int smem_max = std::min(optin, kLwIslandsSmem);
@@ -597,12 +608,16 @@ static int lw_setup(odegpuBatch* B, const odegpuScene* sc) {
   W.islands_smem = smem_max;
   // the sweep cluster: the largest cluster (16, non-portable, down to 1) the
   // device can place with the body slots and lambdas split over its CTAs
-  OG_CUDA(cudaFuncSetAttribute(lw_sweep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max));
+  cudaFuncAttributes fa{};
+  OG_CUDA(cudaFuncGetAttributes(&fa, lw_sweep_kernel));
+  const int sweep_dyn_max = optin - (int)fa.sharedSizeBytes;
+  OG_CUDA(cudaFuncSetAttribute(lw_sweep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, sweep_dyn_max));
   cudaFuncSetAttribute(lw_sweep_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
   cudaGetLastError();
   for (int C : {16, 8, 4, 2, 1}) {
-    const size_t smem = (size_t)((nb + C - 1) / C) * sizeof(LwBody) + (size_t)((R + C - 1) / C) * sizeof(float);
-    if (smem > (size_t)smem_max) continue;
+    // body slots, then per row slot a lambda and a level
+    const size_t smem = (size_t)((nb + C - 1) / C) * sizeof(LwBody) + (size_t)((R + C - 1) / C) * 2 * sizeof(float);
+    if (smem > (size_t)sweep_dyn_max) continue;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)C);
     cfg.blockDim = dim3(kLwSweepThreads);
@@ -1372,6 +1387,18 @@ int odegpuBatchInfo(odegpuBatchID b, int* n_worlds, int* nb_total, int* nj_total
 }
 
 void* odegpuBatchStream(odegpuBatchID b) { return b ? (void*)b->stream : nullptr; }
+
+int odegpuBatchLargeWorldStats(odegpuBatchID b, long long* out, int n, int reset) {
+  if (!b || !out || n < 0) return fail(ODEGPU_E_ARG, "bad arguments");
+  if (!b->lw) return fail(ODEGPU_E_ARG, "the batch has no large world");
+  OG_CUDA(cudaSetDevice(b->device));
+  OG_CUDA(cudaStreamSynchronize(b->stream));
+  unsigned long long v[9];
+  OG_CUDA(cudaMemcpy(v, b->lw->stats.p, sizeof(v), cudaMemcpyDeviceToHost));
+  for (int k = 0; k < n && k < 9; ++k) out[k] = (long long)v[k];
+  if (reset) OG_CUDA(cudaMemset(b->lw->stats.p, 0, sizeof(v)));
+  return 0;
+}
 
 int odegpuBatchStepTap(odegpuBatchID b, float* rows, float* lambda, float* fc, int* row_off) {
   if (b && b->lw) return fail(ODEGPU_E_ARG, "not available for a large world (one world above the on-chip limits)");

@@ -37,8 +37,10 @@ constexpr unsigned kLwSpinLimit = 1u << 22;
 struct __align__(16) LwBody {
   float f[6];        // constraint force accumulator (cforce)
   unsigned cnt;      // row updates applied to the body in this sweep launch
-  unsigned pad;
+  int lvl;           // dependency level of the last row that updated it (first iteration)
 };
+constexpr int kLwLevels = 2048;        // levels the sweep sorts by (more: position order)
+constexpr int kLwLevelWindow = 8;      // positions per thread polled together for their levels
 
 struct LWDev {
   int nb, ng, njp, nstat, contact_cap, row_cap, pair_cap, adj_cap, hsize, cluster;
@@ -90,10 +92,24 @@ struct LWDev {
   int* bfill;            // [nb]
   int* blist;            // [2*row_cap]
   int4* prec;            // [row_cap] per position: row, rank1 << 16 | deg1, rank2 << 16 | deg2
+  int* plev;             // [row_cap] dependency level of each position in the round's order
+  int2* ppred;           // [row_cap] previous position on the row's body 1 / body 2 (-1: none)
+  float* rsort;          // [row_cap][32] the round's rows in level order (word 31: row index)
+  int* lorder;           // [row_cap] positions sorted by level
   float* lambda;         // [row_cap]
   float* fc;             // [nb][6]
   int* err;              // [1] a sweep wait gave up
+  unsigned long long* stats;  // [9] diagnostics, see odegpuBatchLargeWorldStats
 };
+
+// Diagnostics accumulated on the device (nanoseconds from the global timer).
+enum { LWS_WALK_NS = 0, LWS_SWEEP_FIRST_NS = 1, LWS_SWEEP_SORT_NS = 2, LWS_SWEEP_REST_NS = 3,
+       LWS_LEVELS_MAX = 4, LWS_SWEEPS = 5, LWS_WALKS = 6, LWS_WALK_COPY_NS = 7, LWS_CLUSTER = 8 };
+OG_D unsigned long long lw_now() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+  return t;
+}
 
 // ---------------------------------------------------------------- scans
 // In-place exclusive prefix sum of a[0..n) (row blockIdx.x of stride `stride`),
@@ -434,80 +450,80 @@ __global__ void lw_adj_finish_kernel(BatchDev d, LWDev L) {
   }
 }
 
-// The island walk of ode/src/util.cpp:384-521 by one warp: bodies from the
-// newest (ODE's body list is newest first), each untagged one starting a
-// depth-first walk; a body's list entries are taken in order. An entry's joint
-// is still untagged exactly when its other body has not been walked yet (a
-// joint is tagged when the first of its two bodies is walked), so the walk
-// needs only the other body of each entry. Output: the island order as list
-// entries, and the first position of every island that has joints.
-__global__ void __launch_bounds__(32) lw_islands_kernel(BatchDev d, LWDev L, int smem_bytes) {
-  extern __shared__ __align__(16) unsigned char lw_sm[];
-  const int lane = threadIdx.x;
-  const int nb = L.nb;
-  const int E = L.acount[nb];
-  // on-chip copies when they fit: list starts, flags, stack, other bodies
-  const size_t need_fixed = (size_t)(nb + 1) * 4 + (size_t)nb * 4 + ((nb + 16) & ~15);
-  const bool fit_all = need_fixed + (size_t)E * 4 <= (size_t)smem_bytes;
-  const bool fit_fixed = need_fixed <= (size_t)smem_bytes;
-  int* astart = fit_fixed ? reinterpret_cast<int*>(lw_sm) : L.acount;
-  int* stack = fit_fixed ? astart + (nb + 1) : L.stack;
-  unsigned char* flags = fit_fixed ? reinterpret_cast<unsigned char*>(stack + nb) : L.bflag;
-  int* other = fit_all ? reinterpret_cast<int*>(flags + ((nb + 16) & ~15)) : L.adj_other;
-  if (fit_fixed)
-    for (int b = lane; b <= nb; b += 32) astart[b] = L.acount[b];
-  if (fit_all)
-    for (int e = lane; e < E; e += 32) other[e] = L.adj_other[e];
-  for (int b = lane; b < nb; b += 32) flags[b] = 0;
-  __syncwarp();
-  const unsigned lt = (1u << lane) - 1u;
-  int jcount = 0, nisl = 0;
+// The island walk of ode/src/util.cpp:384-521: bodies from the newest (ODE's
+// body list is newest first), each untagged one starting a depth-first walk;
+// a body's list entries are taken in order. An entry's joint is still
+// untagged exactly when its other body has not been walked yet (a joint is
+// tagged when the first of its two bodies is walked), so the walk needs only
+// the other body of each entry. Every step depends on the one before, so one
+// thread runs it; the pointer types tell the compiler which instance keeps its
+// arrays on chip (plain shared-memory accesses) and which in global memory.
+// Output: the island order as list entries, and the first position of every
+// island that has joints.
+template <typename OtherT>
+OG_D void lw_walk(const LWDev& L, const int* astart, int* stack, unsigned char* flags, const OtherT* other,
+                  int nb, int& jc_out, int& ni_out) {
+  int jc = 0, ni = 0;
   for (int bb = nb - 1; bb >= 0; --bb) {
     if (flags[bb] & 1) continue;
-    __syncwarp();
-    if (lane == 0) flags[bb] = 1;
-    __syncwarp();
-    const int jstart = jcount;
+    flags[bb] = 1;
+    const int jstart = jc;
     int sp = 0, b = bb;
     for (;;) {
-      const int s = astart[b], e = astart[b + 1];
-      for (int base = s; base < e; base += 32) {
-        const int k = base + lane;
-        int o = -1;
-        bool take = false;
-        if (k < e) {
-          o = other[k];
-          take = (o < 0) || !(flags[o] & 2);
-        }
-        const unsigned bal = __ballot_sync(kFull, take);
-        if (take) L.jentry[jcount + __popc(bal & lt)] = k;
-        jcount += __popc(bal);
-        const bool cand = take && o >= 0 && !(flags[o] & 1);
-        const unsigned same = __match_any_sync(kFull, cand ? o : -1 - lane);
-        const bool first = cand && (same & lt) == 0;
-        const unsigned bp = __ballot_sync(kFull, first);
-        __syncwarp();
-        if (first) {
-          flags[o] |= 1;
-          stack[sp + __popc(bp & lt)] = o;
-        }
-        sp += __popc(bp);
-        __syncwarp();
+      const int s0 = astart[b], e0 = astart[b + 1];
+      for (int k = s0; k < e0; ++k) {
+        const int o = (int)other[k];
+        if (o < 0) { L.jentry[jc++] = k; continue; }
+        const unsigned char fo = flags[o];
+        if (fo & 2) continue;
+        L.jentry[jc++] = k;
+        if (!(fo & 1)) { flags[o] = (unsigned char)(fo | 1); stack[sp++] = o; }
       }
-      if (lane == 0) flags[b] |= 2;
-      __syncwarp();
+      flags[b] |= 2;
       if (sp == 0) break;
       b = stack[--sp];
     }
-    if (jcount > jstart) {
-      if (lane == 0) L.istart[nisl] = jstart;
-      ++nisl;
+    if (jc > jstart) L.istart[ni++] = jstart;
+  }
+  jc_out = jc;
+  ni_out = ni;
+}
+
+__global__ void __launch_bounds__(32) lw_islands_kernel(BatchDev d, LWDev L, int smem_bytes) {
+  extern __shared__ __align__(16) unsigned char lw_sm[];
+  const int lane = threadIdx.x;
+  const unsigned long long t_start = lw_now();
+  const int nb = L.nb;
+  const int E = L.acount[nb];
+  // on chip when they fit: list starts, stack, flags, and the other body of
+  // every entry as 16 bits (below 32767 bodies)
+  const size_t fixed = (size_t)(nb + 1) * 4 + (size_t)nb * 4 + ((nb + 16) & ~15);
+  const bool on_chip = nb < 32767 && fixed + (size_t)E * 2 <= (size_t)smem_bytes;
+  int jc = 0, ni = 0;
+  if (on_chip) {
+    int* astart = reinterpret_cast<int*>(lw_sm);
+    int* stack = astart + (nb + 1);
+    unsigned char* flags = reinterpret_cast<unsigned char*>(stack + nb);
+    short* other = reinterpret_cast<short*>(flags + ((nb + 16) & ~15));
+    for (int b = lane; b <= nb; b += 32) astart[b] = L.acount[b];
+    for (int e = lane; e < E; e += 32) other[e] = (short)L.adj_other[e];
+    for (int b = lane; b < nb; b += 32) flags[b] = 0;
+    __syncwarp();
+    if (lane == 0) {
+      atomicAdd(&L.stats[LWS_WALK_COPY_NS], lw_now() - t_start);
+      lw_walk<short>(L, astart, stack, flags, other, nb, jc, ni);
     }
+  } else {
+    for (int b = lane; b < nb; b += 32) L.bflag[b] = 0;
+    __syncwarp();
+    if (lane == 0) lw_walk<int>(L, L.acount, L.stack, L.bflag, L.adj_other, nb, jc, ni);
   }
   if (lane == 0) {
-    L.istart[nisl] = jcount;
-    *L.nj = jcount;
-    d.nislands[0] = nisl;
+    L.istart[ni] = jc;
+    *L.nj = jc;
+    d.nislands[0] = ni;
+    atomicAdd(&L.stats[LWS_WALK_NS], lw_now() - t_start);
+    atomicAdd(&L.stats[LWS_WALKS], 1ull);
   }
 }
 
@@ -689,6 +705,7 @@ __global__ void lw_bodypos_kernel(BatchDev d, LWDev L, const int* ord) {
   const int r = ord[p];
   const int* w = reinterpret_cast<const int*>(d.rows + (size_t)(D.row_off + r) * kRowWords);
   L.prec[p].x = r;
+  L.ppred[p] = make_int2(-1, -1);
   atomicAdd(&L.bcount[w[kRowB1]], 1);
   if (w[kRowB2] >= 0) atomicAdd(&L.bcount[w[kRowB2]], 1);
 }
@@ -720,8 +737,9 @@ __global__ void lw_branks_kernel(BatchDev d, LWDev L, const int* ord) {
     const int p = a[i];
     const int* w = reinterpret_cast<const int*>(d.rows + (size_t)(D.row_off + ord[p]) * kRowWords);
     const int v = (i << 16) | n;
-    if (w[kRowB1] == b) L.prec[p].y = v;
-    else L.prec[p].z = v;
+    const int pred = i > 0 ? a[i - 1] : -1;
+    if (w[kRowB1] == b) { L.prec[p].y = v; L.ppred[p].x = pred; }
+    else { L.prec[p].z = v; L.ppred[p].y = pred; }
   }
 }
 
@@ -735,113 +753,363 @@ OG_D void lw_st_release(unsigned* p, unsigned v) {
   asm volatile("st.release.cluster.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
+// Cluster barrier in two halves: work issued between them (a prefetch) is
+// not held up by the release, which waits only for what precedes the arrive.
+OG_D void lw_arrive() { asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory"); }
+OG_D void lw_wait_all() { asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory"); }
+
+OG_D int lw_ld_acquire_int(const int* p) {
+  int v;
+  asm volatile("ld.acquire.cluster.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+OG_D void lw_st_release_int(int* p, int v) {
+  asm volatile("st.release.cluster.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+// Wait (bounded, backing off) until a level is set; false when it gave up.
+OG_D bool lw_wait_level(const int* p, int& out, const volatile int* err) {
+  unsigned ns = 0;
+  for (unsigned spins = 0;; ++spins) {
+    const int v = lw_ld_acquire_int(p);
+    if (v != 0) { out = v; return true; }
+    if (spins >= kLwSpinLimit) return false;
+    if ((spins & 255u) == 255u && *err) return false;
+    if (spins >= 2) {
+      ns = ns ? min(ns * 2u, 256u) : 32u;
+      __nanosleep(ns);
+    }
+  }
+}
+
 // Wait until *c == target; false when the wait gave up (bounded, or another
 // thread gave up first).
+// Polls back off (up to 256 ns apart) so that waiting threads leave the
+// cluster's shared-memory network to the rows that are running.
 OG_D bool lw_wait(const unsigned* c, unsigned target, const volatile int* err) {
+  unsigned ns = 0;
   for (unsigned spins = 0;; ++spins) {
     if (lw_ld_acquire(c) == target) return true;
     if (spins >= kLwSpinLimit) return false;
     if ((spins & 255u) == 255u && *err) return false;
+    if (spins >= 2) {
+      ns = ns ? min(ns * 2u, 256u) : 32u;
+      __nanosleep(ns);
+    }
   }
 }
 
+// One row update of the sweep (quickstep.cpp:484-582, the arithmetic of
+// sor_row term for term) once both bodies have received exactly the updates
+// that precede the row: the k-th of deg positions touching a body waits for
+// li * deg + k. When lvl_out is given, the row's dependency level (one more
+// than the last level recorded on either body) is recorded and passed on.
+struct LwRow {
+  float4 rw[8];
+  int4 rec;
+};
+OG_D void lw_load(const float* rows, const LWDev& L, int p, LwRow& R) {
+  R.rec = L.prec[p];
+  load_row(rows, R.rec.x, R.rw);
+}
+// the j-th row of the round's level order (its row index in word 31)
+OG_D void lw_load_sorted(const LWDev& L, int j, LwRow& R) {
+  load_row(L.rsort, j, R.rw);
+  R.rec = make_int4(__float_as_int(R.rw[7].w), 0, 0, 0);
+}
+OG_D bool lw_update(cooperative_groups::cluster_group& cluster, int C, LwBody* bodies, float* lam, const LwRow& R,
+                    unsigned li, const LWDev& L, int* lvl_out, bool wait = true) {
+  const float* J = reinterpret_cast<const float*>(&R.rw[0]);
+  const float* iMJ = reinterpret_cast<const float*>(&R.rw[3]);
+  const float bb = R.rw[6].x, Ad = R.rw[6].y, lo = R.rw[6].z, hi = R.rw[6].w;
+  const int findex = __float_as_int(R.rw[7].x);
+  const int b1 = __float_as_int(R.rw[7].y), b2 = __float_as_int(R.rw[7].z);
+  const int r = R.rec.x;
+  const int lc = __ffs(C) - 1, cm = C - 1;   // C is a power of two
+  LwBody* B1 = cluster.map_shared_rank(bodies + (b1 >> lc), b1 & cm);
+  LwBody* B2 = b2 >= 0 ? cluster.map_shared_rank(bodies + (b2 >> lc), b2 & cm) : nullptr;
+  const unsigned tg1 = li * (unsigned)(R.rec.y & 0xffff) + ((unsigned)R.rec.y >> 16);
+  const unsigned tg2 = li * (unsigned)(R.rec.z & 0xffff) + ((unsigned)R.rec.z >> 16);
+  if (wait && (!lw_wait(&B1->cnt, tg1, L.err) || (B2 && !lw_wait(&B2->cnt, tg2, L.err)))) {
+    atomicExch(L.err, 1);
+    return false;
+  }
+  float* lr = cluster.map_shared_rank(lam + (r >> lc), r & cm);
+  const float old = *lr;
+  const float lf = findex >= 0 ? *cluster.map_shared_rank(lam + (findex >> lc), findex & cm) : 0.f;
+  const float4 a1 = *reinterpret_cast<const float4*>(B1->f);
+  const float2 c1 = *reinterpret_cast<const float2*>(B1->f + 4);
+  const float f10 = a1.x, f11 = a1.y, f12 = a1.z, f13 = a1.w, f14 = c1.x, f15 = c1.y;
+  float f20 = 0.f, f21 = 0.f, f22 = 0.f, f23 = 0.f, f24 = 0.f, f25 = 0.f;
+  if (B2) {
+    const float4 a2 = *reinterpret_cast<const float4*>(B2->f);
+    const float2 c2 = *reinterpret_cast<const float2*>(B2->f + 4);
+    f20 = a2.x; f21 = a2.y; f22 = a2.z; f23 = a2.w; f24 = c2.x; f25 = c2.y;
+  }
+  float delta = bb - old * Ad;
+  delta -= (f10 * J[0] + f11 * J[1]) + (f12 * J[2] + f13 * J[3]) + (f14 * J[4] + f15 * J[5]);
+  delta -= (f20 * J[6] + f21 * J[7]) + (f22 * J[8] + f23 * J[9]) + (f24 * J[10] + f25 * J[11]);
+  const float hf = fabsf(hi * lf);
+  const float hi_act = findex >= 0 ? hf : hi;
+  const float lo_act = findex >= 0 ? -hf : lo;
+  const float nl = old + delta;
+  const bool clamped = (nl < lo_act) || (nl > hi_act);
+  const float lamv = fminf(fmaxf(nl, lo_act), hi_act);
+  delta = clamped ? lamv - old : delta;
+  *lr = clamped ? lamv : nl;
+  *reinterpret_cast<float4*>(B1->f) =
+      make_float4(f10 + delta * iMJ[0], f11 + delta * iMJ[1], f12 + delta * iMJ[2], f13 + delta * iMJ[3]);
+  *reinterpret_cast<float2*>(B1->f + 4) = make_float2(f14 + delta * iMJ[4], f15 + delta * iMJ[5]);
+  if (lvl_out) {
+    const int lv = 1 + max(B1->lvl, B2 ? B2->lvl : 0);
+    *lvl_out = lv;
+    B1->lvl = lv;
+    if (B2) B2->lvl = lv;
+  }
+  if (B2) {
+    *reinterpret_cast<float4*>(B2->f) =
+        make_float4(f20 + delta * iMJ[6], f21 + delta * iMJ[7], f22 + delta * iMJ[8], f23 + delta * iMJ[9]);
+    *reinterpret_cast<float2*>(B2->f + 4) = make_float2(f24 + delta * iMJ[10], f25 + delta * iMJ[11]);
+    if (wait) lw_st_release(&B2->cnt, tg2 + 1u);
+  }
+  if (wait) lw_st_release(&B1->cnt, tg1 + 1u);
+  return true;
+}
+
 // Iterations [it0, it1) of SOR_LCP over every island in the current order, as
-// one cluster. Body b's slot lives in CTA b % C, row r's lambda in CTA r % C.
-// Thread t takes positions t' , t' + T, ... (t' spreads a warp's lanes over the
-// order) in every iteration, so each thread meets its rows in the sequential
-// order and the earliest unfinished row can always run. A row waits until its
-// bodies have received exactly the updates that precede it: the k-th of deg
-// positions touching a body waits for it * deg + k.
+// one cluster of C = 2^lc CTAs. Body b's slot lives in CTA b & (C-1), row r's
+// lambda in CTA r & (C-1).
+//   1. Levels: a row's dependency level is one more than the larger level of
+//      the previous position on either of its bodies (the per-body position
+//      lists give those links); relaxed in parallel passes until no level
+//      changes (as many passes as the longest chain).
+//   2. Positions counting-sorted by level (per-CTA histograms merged over
+//      distributed shared memory).
+//   3. Every iteration level by level: the rows of a level touch disjoint
+//      bodies and run in parallel, spread over all CTAs; a cluster barrier
+//      orders the levels. Each body meets its rows in the sequential order,
+//      so the result is the sequential sweep.
+// When the levels exceed the histogram the sweep runs in order position as
+// dataflow instead: a row waits (bounded) until both bodies have received
+// the updates that precede it (the k-th of deg positions touching a body
+// waits for it * deg + k).
 __global__ void __launch_bounds__(kLwSweepThreads) lw_sweep_kernel(BatchDev d, LWDev L, int it0, int it1,
                                                                    int first) {
   namespace cg = cooperative_groups;
   extern __shared__ __align__(16) unsigned char lw_sw[];
+  __shared__ int hist[kLwLevels];       // this CTA's positions per level (read by every CTA)
+  __shared__ int ltot[kLwLevels + 1];   // the cluster's positions per level, then each level's first slot
+  __shared__ int base[kLwLevels];       // this CTA's next slot of each level
+  __shared__ int wsum[32];
+  __shared__ int cmax;
+  __shared__ int gmax[32];
   cg::cluster_group cluster = cg::this_cluster();
   const int C = (int)cluster.num_blocks();
+  const int lc = __ffs(C) - 1;
   const int rank = (int)cluster.block_rank();
   const WorldDesc D = d.world[0];
   const int M = d.nrows[0];
   const int nb = L.nb;
-  const int nbs = (nb + C - 1) / C;
+  const int nbs = (nb + C - 1) >> lc;
   LwBody* bodies = reinterpret_cast<LwBody*>(lw_sw);
   float* lam = reinterpret_cast<float*>(bodies + nbs);
-  const int nrs = (L.row_cap + C - 1) / C;
+  const int nrs = (L.row_cap + C - 1) >> lc;
   for (int s = threadIdx.x; s < nbs; s += blockDim.x) {
-    const int b = s * C + rank;
+    const int b = (s << lc) + rank;
     LwBody v;
     for (int k = 0; k < 6; ++k) v.f[k] = (b < nb && !first) ? L.fc[6 * (size_t)b + k] : 0.f;
     v.cnt = 0u;
-    v.pad = 0u;
+    v.lvl = 0;
     bodies[s] = v;
   }
   for (int s = threadIdx.x; s < nrs; s += blockDim.x) {
-    const int r = s * C + rank;
+    const int r = (s << lc) + rank;
     lam[s] = (r < M && !first) ? L.lambda[r] : 0.f;
   }
-  cluster.sync();
+  for (int l = threadIdx.x; l < kLwLevels; l += blockDim.x) hist[l] = 0;
   const int T = C * (int)blockDim.x;
   const int tid = rank * (int)blockDim.x + (int)threadIdx.x;
+  const float* rows = d.rows + (size_t)D.row_off * kRowWords;
+  const bool timer = rank == 0 && threadIdx.x == 0;
+  unsigned long long t_mark = timer ? lw_now() : 0ull;
+  // levels live in distributed shared memory next to the lambdas: position p
+  // in CTA p & (C-1), 0 until set
+  int* lvl = reinterpret_cast<int*>(lam + nrs);
+  for (int s = threadIdx.x; s < nrs; s += blockDim.x) lvl[s] = 0;
+  if (threadIdx.x == 0) cmax = 0;
+  cluster.sync();
+  // 1. levels as dataflow: a position takes its level once both predecessors
+  //    have theirs. A thread holds up to kLwLevelWindow positions and polls
+  //    them in turn, taking whichever is ready, so it never waits behind one
+  //    that is not; more positions per thread are taken in order.
   const int lane = tid & 31, wid = tid >> 5, nw = T >> 5;
   const int t0 = lane * nw + wid;
-  const float* rows = d.rows + (size_t)D.row_off * kRowWords;
   bool ok = M > 0 && !*L.err;
-  for (int it = it0; ok && it < it1; ++it) {
-    const unsigned li = (unsigned)(it - it0);
-    for (int p = t0; ok && p < M; p += T) {
-      const int4 rec = L.prec[p];
-      const int r = rec.x;
-      float4 rw[8];
-      load_row(rows, r, rw);
-      const float* J = reinterpret_cast<const float*>(&rw[0]);
-      const float* iMJ = reinterpret_cast<const float*>(&rw[3]);
-      const float bb = rw[6].x, Ad = rw[6].y, lo = rw[6].z, hi = rw[6].w;
-      const int findex = __float_as_int(rw[7].x);
-      const int b1 = __float_as_int(rw[7].y), b2 = __float_as_int(rw[7].z);
-      LwBody* B1 = cluster.map_shared_rank(bodies + b1 / C, b1 % C);
-      LwBody* B2 = b2 >= 0 ? cluster.map_shared_rank(bodies + b2 / C, b2 % C) : nullptr;
-      const unsigned tg1 = li * (unsigned)(rec.y & 0xffff) + ((unsigned)rec.y >> 16);
-      const unsigned tg2 = li * (unsigned)(rec.z & 0xffff) + ((unsigned)rec.z >> 16);
-      if (!lw_wait(&B1->cnt, tg1, L.err) || (B2 && !lw_wait(&B2->cnt, tg2, L.err))) {
+  {
+    int lmax = 0;
+    int2 pr[kLwLevelWindow];
+    unsigned pending = 0u;
+#pragma unroll
+    for (int q = 0; q < kLwLevelWindow; ++q) {
+      const int p = t0 + q * T;
+      pr[q] = p < M ? L.ppred[p] : make_int2(-1, -1);
+      if (p < M) pending |= 1u << q;
+    }
+    unsigned ns = 0;
+    for (unsigned spins = 0; ok && pending; ++spins) {
+      bool progress = false;
+#pragma unroll
+      for (int q = 0; q < kLwLevelWindow; ++q) {
+        if (!(pending & (1u << q))) continue;
+        const int a = pr[q].x, c = pr[q].y;
+        const int l1 = a >= 0 ? lw_ld_acquire_int(cluster.map_shared_rank(lvl + (a >> lc), a & (C - 1))) : 1 << 30;
+        const int l2 = c >= 0 ? lw_ld_acquire_int(cluster.map_shared_rank(lvl + (c >> lc), c & (C - 1))) : 1 << 30;
+        if (l1 == 0 || l2 == 0) continue;
+        const int lv = 1 + max(a >= 0 ? l1 : 0, c >= 0 ? l2 : 0);
+        const int p = t0 + q * T;
+        lw_st_release_int(cluster.map_shared_rank(lvl + (p >> lc), p & (C - 1)), lv);
+        lmax = max(lmax, lv);
+        pending &= ~(1u << q);
+        progress = true;
+      }
+      if (progress) { ns = 0; continue; }
+      if (spins >= kLwSpinLimit || ((spins & 255u) == 255u && *L.err)) { atomicExch(L.err, 1); ok = false; break; }
+      ns = ns ? min(ns * 2u, 256u) : 32u;
+      __nanosleep(ns);
+    }
+    for (int p = t0 + kLwLevelWindow * T; ok && p < M; p += T) {
+      const int2 pp = L.ppred[p];
+      int l1 = 0, l2 = 0;
+      if ((pp.x >= 0 && !lw_wait_level(cluster.map_shared_rank(lvl + (pp.x >> lc), pp.x & (C - 1)), l1, L.err)) ||
+          (pp.y >= 0 && !lw_wait_level(cluster.map_shared_rank(lvl + (pp.y >> lc), pp.y & (C - 1)), l2, L.err))) {
         atomicExch(L.err, 1);
         ok = false;
         break;
       }
-      float* lr = cluster.map_shared_rank(lam + r / C, r % C);
-      const float old = *lr;
-      const float lf = findex >= 0 ? *cluster.map_shared_rank(lam + findex / C, findex % C) : 0.f;
-      const float f10 = B1->f[0], f11 = B1->f[1], f12 = B1->f[2], f13 = B1->f[3], f14 = B1->f[4], f15 = B1->f[5];
-      float f20 = 0.f, f21 = 0.f, f22 = 0.f, f23 = 0.f, f24 = 0.f, f25 = 0.f;
-      if (B2) { f20 = B2->f[0]; f21 = B2->f[1]; f22 = B2->f[2]; f23 = B2->f[3]; f24 = B2->f[4]; f25 = B2->f[5]; }
-      // the row update of sor_row, term for term
-      float delta = bb - old * Ad;
-      delta -= (f10 * J[0] + f11 * J[1]) + (f12 * J[2] + f13 * J[3]) + (f14 * J[4] + f15 * J[5]);
-      delta -= (f20 * J[6] + f21 * J[7]) + (f22 * J[8] + f23 * J[9]) + (f24 * J[10] + f25 * J[11]);
-      const float hf = fabsf(hi * lf);
-      const float hi_act = findex >= 0 ? hf : hi;
-      const float lo_act = findex >= 0 ? -hf : lo;
-      const float nl = old + delta;
-      const bool clamped = (nl < lo_act) || (nl > hi_act);
-      const float lamv = fminf(fmaxf(nl, lo_act), hi_act);
-      delta = clamped ? lamv - old : delta;
-      *lr = clamped ? lamv : nl;
-      B1->f[0] = f10 + delta * iMJ[0]; B1->f[1] = f11 + delta * iMJ[1]; B1->f[2] = f12 + delta * iMJ[2];
-      B1->f[3] = f13 + delta * iMJ[3]; B1->f[4] = f14 + delta * iMJ[4]; B1->f[5] = f15 + delta * iMJ[5];
-      if (B2) {
-        B2->f[0] = f20 + delta * iMJ[6]; B2->f[1] = f21 + delta * iMJ[7]; B2->f[2] = f22 + delta * iMJ[8];
-        B2->f[3] = f23 + delta * iMJ[9]; B2->f[4] = f24 + delta * iMJ[10]; B2->f[5] = f25 + delta * iMJ[11];
-        lw_st_release(&B2->cnt, tg2 + 1u);
+      const int lv = 1 + max(l1, l2);
+      lw_st_release_int(cluster.map_shared_rank(lvl + (p >> lc), p & (C - 1)), lv);
+      lmax = max(lmax, lv);
+    }
+    atomicMax(&cmax, lmax);
+  }
+  cluster.sync();
+  if ((int)threadIdx.x < C) gmax[threadIdx.x] = *cluster.map_shared_rank(&cmax, (int)threadIdx.x);
+  cluster.sync();
+  int nlev = 0;
+  for (int c = 0; c < C; ++c) nlev = max(nlev, gmax[c]);
+  // every thread reads the flag here, two barriers before any can set it again
+  ok = M > 0 && atomicOr(L.err, 0) == 0;
+  if (timer) { const unsigned long long t = lw_now(); atomicAdd(&L.stats[LWS_SWEEP_FIRST_NS], t - t_mark); t_mark = t; }
+  const bool sorted = ok && nlev <= kLwLevels;
+  if (sorted) {
+    // 2. counting sort by level (levels are 1 .. nlev); each position's row
+    //    is copied to its sorted slot
+    for (int p = t0; p < M; p += T) atomicAdd(&hist[*cluster.map_shared_rank(lvl + (p >> lc), p & (C - 1)) - 1], 1);
+    cluster.sync();
+    const int per = (nlev + (int)blockDim.x - 1) / (int)blockDim.x;
+    const int l0 = min(nlev, (int)threadIdx.x * per), l1 = min(nlev, l0 + per);
+    int sum = 0;
+    for (int l = l0; l < l1; ++l) {
+      int tot = 0, mine = 0;
+      for (int c = 0; c < C; ++c) {
+        const int v = *cluster.map_shared_rank(&hist[l], c);
+        tot += v;
+        if (c < rank) mine += v;
       }
-      lw_st_release(&B1->cnt, tg1 + 1u);
+      base[l] = mine;
+      ltot[l] = tot;
+      sum += tot;
+    }
+    const int wl = (int)threadIdx.x & 31, ww = (int)threadIdx.x >> 5;
+    const int incl = warp_incl_scan(sum, wl);
+    if (wl == 31) wsum[ww] = incl;
+    __syncthreads();
+    if (ww == 0) {
+      const int v = (wl < ((int)blockDim.x >> 5)) ? wsum[wl] : 0;
+      wsum[wl] = warp_incl_scan(v, wl);
+    }
+    __syncthreads();
+    int run = (ww > 0 ? wsum[ww - 1] : 0) + incl - sum;
+    for (int l = l0; l < l1; ++l) {
+      const int t = ltot[l];
+      ltot[l] = run;
+      base[l] += run;
+      run += t;
+    }
+    if (threadIdx.x == 0) ltot[nlev] = M;
+    cluster.sync();
+    for (int p = t0; p < M; p += T) {
+      const int slot = atomicAdd(&base[*cluster.map_shared_rank(lvl + (p >> lc), p & (C - 1)) - 1], 1);
+      const int r = L.prec[p].x;
+      float4 rw[8];
+      load_row(rows, r, rw);
+      rw[7].w = __int_as_float(r);
+      float4* dst = reinterpret_cast<float4*>(L.rsort + (size_t)slot * kRowWords);
+#pragma unroll
+      for (int q = 0; q < 8; ++q) dst[q] = rw[q];
+    }
+    cluster.sync();
+    if (timer) {
+      const unsigned long long t = lw_now();
+      atomicAdd(&L.stats[LWS_SWEEP_SORT_NS], t - t_mark);
+      t_mark = t;
+    }
+    // 3. level by level; slot a + k of a level goes to CTA k & (C-1), so every
+    //    level is spread over the whole cluster
+    const int tl = ((int)threadIdx.x << lc) + rank;
+    for (int it = it0; it < it1; ++it) {
+      LwRow R;
+      bool have = false;
+      {
+        const int j = ltot[0] + tl;
+        if (j < ltot[1]) { lw_load_sorted(L, j, R); have = true; }
+      }
+      for (int l = 0; l < nlev; ++l) {
+        if (have) {
+          lw_update(cluster, C, bodies, lam, R, 0u, L, nullptr, false);
+          for (int j = ltot[l] + tl + T; j < ltot[l + 1]; j += T) {
+            LwRow Rx;
+            lw_load_sorted(L, j, Rx);
+            lw_update(cluster, C, bodies, lam, Rx, 0u, L, nullptr, false);
+          }
+        }
+        lw_arrive();
+        // the next level's first row of this thread loads during the barrier
+        have = false;
+        if (l + 1 < nlev) {
+          const int j = ltot[l + 1] + tl;
+          if (j < ltot[l + 2]) { lw_load_sorted(L, j, R); have = true; }
+        }
+        lw_wait_all();
+      }
+    }
+  } else if (ok) {
+    // order position as bounded dataflow (levels deeper than the histogram)
+    bool run_ok = true;
+    for (int it = it0; run_ok && it < it1; ++it) {
+      const unsigned li = (unsigned)(it - it0);
+      LwRow cur, nxt;
+      if (t0 < M) lw_load(rows, L, t0, cur);
+      for (int j = t0; run_ok && j < M; j += T) {
+        if (j + T < M) lw_load(rows, L, j + T, nxt);
+        if (!lw_update(cluster, C, bodies, lam, cur, li, L, nullptr)) { run_ok = false; break; }
+        cur = nxt;
+      }
     }
   }
   cluster.sync();
+  if (timer) {
+    atomicAdd(&L.stats[LWS_SWEEP_REST_NS], lw_now() - t_mark);
+    atomicMax(&L.stats[LWS_LEVELS_MAX], (unsigned long long)nlev);
+    atomicAdd(&L.stats[LWS_SWEEPS], 1ull);
+    L.stats[LWS_CLUSTER] = (unsigned long long)C;
+  }
   for (int s = threadIdx.x; s < nbs; s += blockDim.x) {
-    const int b = s * C + rank;
+    const int b = (s << lc) + rank;
     if (b < nb)
       for (int k = 0; k < 6; ++k) L.fc[6 * (size_t)b + k] = bodies[s].f[k];
   }
   for (int s = threadIdx.x; s < nrs; s += blockDim.x) {
-    const int r = s * C + rank;
+    const int r = (s << lc) + rank;
     if (r < M) L.lambda[r] = lam[s];
   }
 }

@@ -66,6 +66,7 @@ def _declare(L):
         "odegpuBatchSetStepIndex": (i, [v, i]),
         "odegpuBatchStepTap": (i, [v, _P(f), _P(f), _P(f), _P(i)]),
         "odegpuBatchGetContacts": (i, [v, i, _P(f), i]),
+        "odegpuBatchLargeWorldStats": (i, [v, _P(C.c_longlong), i, i]),
         "odegpuGetLastError": (C.c_char_p, []),
     }
     for name, (res, args) in sig.items():

@@ -52,6 +52,17 @@ class Batch:
     def step_graph(self, n=1):
         check(lib().odegpuBatchStepGraph(self.h, n))
 
+    def large_world_stats(self, reset=True):
+        """Device-side diagnostics of a large-world batch: island walk, sweep
+        first iterations, level sort and remaining iterations (ms), the
+        largest level count, sweep launches and walks."""
+        out = (C.c_longlong * 9)()
+        check(lib().odegpuBatchLargeWorldStats(self.h, out, 9, 1 if reset else 0))
+        v = list(out)
+        return dict(walk_ms=v[0] / 1e6, sweep_first_ms=v[1] / 1e6, sort_ms=v[2] / 1e6,
+                    sweep_rest_ms=v[3] / 1e6, levels_max=v[4], sweeps=v[5], walks=v[6],
+                    walk_copy_ms=v[7] / 1e6, cluster=v[8])
+
     def sync(self):
         check(lib().odegpuBatchSynchronize(self.h))
 
