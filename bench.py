@@ -300,6 +300,65 @@ def run_vehicles(local_rank, steps=300):
             "worlds_with_status": int((status != 0).sum())}
 
 
+def run_large_world(local_rank, steps=100, cpu_steps=20):
+    """Large single world: 10,000 spheres (r U[0.1,0.3] m, density 1000) on a
+    jittered grid in a 6 x 6 x 20 m box of five static planes, mu 0.8, 50
+    iterations, dt 0.005, stepped by the large-world pipeline; ms per step over
+    the first `steps` steps from the initial state (the pile settling), timed
+    with CUDA events on the batch stream, and the FP64 oracle port (grid
+    broadphase, same canonical pairs) on one host core over the first
+    `cpu_steps` steps, against the GPU over the same steps."""
+    import torch
+    import oracle_lib as O
+    from odegpu import scene as S
+    from odegpu.batch import Batch
+    sc = S.sphere_pile(n=10000)
+    B = Batch(sc, device=local_rank)
+    stream = torch.cuda.ExternalStream(B.stream_handle())
+    x0, seeds = B.state(), B.seeds()
+    B.step(3)
+    B.sync()
+
+    def timed(n):
+        B.set_state(x0)
+        B.set_seeds(seeds)
+        B.set_step_index(0)
+        B.large_world_stats(reset=True)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+        B.step(n)
+        with torch.cuda.stream(stream):
+            e1.record(stream)
+        B.sync()
+        return e0.elapsed_time(e1) / 1e3, B.large_world_stats(reset=True)
+
+    t_cpu_span, _ = timed(cpu_steps)
+    t, st = timed(steps)
+    nc, nr, ni = B.counts()
+    status = int(B.status()[0])
+    B.close()
+    t0 = time.perf_counter()
+    O.run_world(O.oracle().oracle_run_world, sc, 0, cpu_steps, max_rec=1)
+    t_cpu = time.perf_counter() - t0
+    return {"metric": "steps/s, one 10k-sphere world", "value": steps / t, "unit": "steps/s",
+            "ms_per_step": 1e3 * t / steps,
+            "workload": "large world: 10,000 spheres r U[0.1,0.3] m, density 1000, jittered grid in a 6x6x20 m box "
+                        "of 5 static planes, mu 0.8, 50 iterations, w 1.3, dt 0.005; first %d steps from the "
+                        "initial state" % steps,
+            "contacts_last_step": int(nc[0]), "rows_last_step": int(nr[0]), "islands_last_step": int(ni[0]),
+            "status": status,
+            "phase_ms_per_step": {"island_walk": st["walk_ms"] / steps, "levels": st["sweep_first_ms"] / steps,
+                                  "level_sort": st["sort_ms"] / steps,
+                                  "level_sweeps": st["sweep_rest_ms"] / steps},
+            "levels_max": st["levels_max"], "sweep_cluster_ctas": st["cluster"],
+            "cpu_port": {"ms_per_step": 1e3 * t_cpu / cpu_steps, "cores": 1,
+                         "sample": f"FP64 oracle port, first {cpu_steps} steps from the initial state",
+                         "gpu_ms_per_step_same_steps": 1e3 * t_cpu_span / cpu_steps,
+                         "gpu_speedup_same_steps": (t_cpu / cpu_steps) / (t_cpu_span / cpu_steps)}}
+
+
 def run_reference(args):
     rank, world_size, _ = rank_env()
     if rank != 0:
@@ -469,6 +528,8 @@ def run_ours(args):
             line["adjoint"] = run_adjoint(local_rank)
         if not args.no_vehicles:
             line["vehicles"] = run_vehicles(local_rank)
+        if not args.no_large:
+            line["large_world"] = run_large_world(local_rank)
         if not args.no_cpu:
             nw = min(N_WORLDS, args.cpu_worlds)
             v, thr, dt = cpu_baseline(sc, nw, args.steps)
@@ -495,16 +556,20 @@ def main():
                     help="print only the forward + adjoint measurement (for profiling)")
     ap.add_argument("--only-vehicles", action="store_true",
                     help="print only the vehicle-batch measurement (for profiling)")
+    ap.add_argument("--no-large", action="store_true")
+    ap.add_argument("--only-large", action="store_true",
+                    help="print only the large-world measurement (for profiling)")
     ap.add_argument("--cpu-worlds", type=int, default=512)
     ap.add_argument("--ref-worlds", type=int, default=4096)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
-    elif args.only_adjoint or args.only_vehicles:
+    elif args.only_adjoint or args.only_vehicles or args.only_large:
         import torch
         _, _, local_rank = rank_env()
         torch.cuda.set_device(local_rank)
-        out = run_adjoint(local_rank) if args.only_adjoint else run_vehicles(local_rank)
+        out = (run_adjoint(local_rank) if args.only_adjoint else
+               run_vehicles(local_rank) if args.only_vehicles else run_large_world(local_rank))
         print(json.dumps(out), flush=True)
     else:
         run_ours(args)

@@ -2810,13 +2810,116 @@ static int bodies_jointed(const OWorld* W, int b1, int b2) {
   return 0;
 }
 
+/* Bounding radius of a geom on a body (sphere r, box half diagonal, capsule
+ * r + length / 2); static geoms have none. */
+static real geom_bound(const OGeom* G) {
+  switch (G->type) {
+    case ODEGPU_GEOM_SPHERE: return G->p[0];
+    case ODEGPU_GEOM_BOX: return 0.5 * sqrt(G->p[0] * G->p[0] + G->p[1] * G->p[1] + G->p[2] * G->p[2]);
+    case ODEGPU_GEOM_CAPSULE: return G->p[0] + 0.5 * G->p[1];
+    default: return R_INF;
+  }
+}
+
+typedef struct { long long key; int g; } CellGeom;
+static int cmp_cell(const void* a, const void* b) {
+  const long long x = ((const CellGeom*)a)->key, y = ((const CellGeom*)b)->key;
+  return (x > y) - (x < y);
+}
+static int cmp_pair(const void* a, const void* b) {
+  const long long x = *(const long long*)a, y = *(const long long*)b;
+  return (x > y) - (x < y);
+}
+static long long cell_key(long long ix, long long iy, long long iz) {
+  return ((ix + (1 << 20)) << 42) | ((iy + (1 << 20)) << 21) | (iz + (1 << 20));
+}
+
+/* Candidate pairs of a large world in the canonical order, for the CPU
+ * baseline: pairs of geoms on bodies within the conservative bounding-sphere
+ * test (a uniform grid, cells one test wide), plus every pair of a static and
+ * a body geom; sorted by (i, k). Pairs left out cannot produce contacts, so
+ * the step is the same as with the full pair loop. Returns the count; *out
+ * holds i << 32 | k. */
+static int large_world_pairs(OWorld* W, long long** out) {
+  const int ng = W->ng;
+  real rmax = 0;
+  for (int g = 0; g < ng; ++g)
+    if (W->geom[g].body >= 0) { const real r = geom_bound(&W->geom[g]); if (r > rmax) rmax = r; }
+  const real cell = rmax > 0 ? 1.01 * (2 * rmax * 1.001 + 1e-5) : 1.0;
+  CellGeom* cg = (CellGeom*)malloc(sizeof(CellGeom) * (size_t)(ng > 0 ? ng : 1));
+  int* cix = (int*)malloc(sizeof(int) * 3 * (size_t)(ng > 0 ? ng : 1));
+  int nd = 0;
+  for (int g = 0; g < ng; ++g) {
+    const int b = W->geom[g].body;
+    if (b < 0) continue;
+    const real* p = W->body[b].pos;
+    const long long ix = (long long)floor(p[0] / cell), iy = (long long)floor(p[1] / cell),
+                    iz = (long long)floor(p[2] / cell);
+    cix[3 * g] = (int)ix; cix[3 * g + 1] = (int)iy; cix[3 * g + 2] = (int)iz;
+    cg[nd].key = cell_key(ix, iy, iz);
+    cg[nd].g = g;
+    ++nd;
+  }
+  qsort(cg, nd, sizeof(CellGeom), cmp_cell);
+  size_t cap = 1024, n = 0;
+  long long* pairs = (long long*)malloc(sizeof(long long) * cap);
+#define PUSH_PAIR(a, b)                                                           \
+  do {                                                                            \
+    if (n == cap) { cap *= 2; pairs = (long long*)realloc(pairs, sizeof(long long) * cap); } \
+    pairs[n++] = ((long long)(a) << 32) | (long long)(b);                         \
+  } while (0)
+  for (int g = 0; g < ng; ++g) {
+    const int b = W->geom[g].body;
+    if (b < 0) continue;
+    for (int s = 0; s < ng; ++s)
+      if (W->geom[s].body < 0) { if (s < g) PUSH_PAIR(s, g); else PUSH_PAIR(g, s); }
+    const real* p = W->body[b].pos;
+    const real rg = geom_bound(&W->geom[g]);
+    for (int dx = -1; dx <= 1; ++dx)
+      for (int dy = -1; dy <= 1; ++dy)
+        for (int dz = -1; dz <= 1; ++dz) {
+          const long long key = cell_key(cix[3 * g] + dx, cix[3 * g + 1] + dy, cix[3 * g + 2] + dz);
+          int lo = 0, hi = nd;
+          while (lo < hi) { const int mid = (lo + hi) / 2; if (cg[mid].key < key) lo = mid + 1; else hi = mid; }
+          for (int e = lo; e < nd && cg[e].key == key; ++e) {
+            const int k = cg[e].g;
+            if (k <= g) continue;
+            const int bk = W->geom[k].body;
+            if (bk == b) continue;
+            const real* q = W->body[bk].pos;
+            const real lim = (rg + geom_bound(&W->geom[k])) * 1.001 + 1e-5;
+            const real d0 = p[0] - q[0], d1 = p[1] - q[1], d2 = p[2] - q[2];
+            if (d0 * d0 + d1 * d1 + d2 * d2 > lim * lim) continue;
+            PUSH_PAIR(g, k);
+          }
+        }
+  }
+#undef PUSH_PAIR
+  qsort(pairs, n, sizeof(long long), cmp_pair);
+  free(cg);
+  free(cix);
+  *out = pairs;
+  return (int)n;
+}
+
 /* One canonical world step (see include/odegpu_scene.h). */
 static int world_step(OWorld* W, int s, double* contacts, int max_rec) {
   const odegpuScene* sc = W->sc;
   int nc = 0;
   OContact cg[16];
-  for (int i = 0; i < W->ng; ++i) {
-    for (int k = i + 1; k < W->ng; ++k) {
+  long long* cand = 0;
+  const int ncand = W->ng > 512 ? large_world_pairs(W, &cand) : -1;
+  const int npair = ncand >= 0 ? ncand : W->ng * (W->ng - 1) / 2;
+  for (int pi = 0, i = 0, k = 0; pi < npair; ++pi) {
+    if (ncand >= 0) {
+      i = (int)(cand[pi] >> 32);
+      k = (int)(cand[pi] & 0xffffffff);
+    } else {
+      /* i < k in order: advance k, then i */
+      if (pi == 0) { i = 0; k = 1; }
+      else if (++k >= W->ng) { ++i; k = i + 1; }
+    }
+    {
       const int bi = W->geom[i].body, bk = W->geom[k].body;
       if (bi < 0 && bk < 0) continue;
       if (bi == bk) continue;
@@ -2846,6 +2949,7 @@ static int world_step(OWorld* W, int s, double* contacts, int max_rec) {
       }
     }
   }
+  free(cand);
   if (sc->n_ctrl_steps > 0) {
     const int cs = s % sc->n_ctrl_steps;
     const int j0 = sc->joint_off[W->w], b0 = sc->body_off[W->w];
