@@ -86,7 +86,10 @@ enum { dSphereClass = 0, dBoxClass, dCapsuleClass, dCylinderClass, dPlaneClass,
 
 /* include/ode/common.h:252-258 */
 typedef enum { dJointTypeNone = 0, dJointTypeBall, dJointTypeHinge, dJointTypeSlider,
-               dJointTypeContact, dJointTypeUniversal, dJointTypeHinge2, dJointTypeFixed } dJointType;
+               dJointTypeContact, dJointTypeUniversal, dJointTypeHinge2, dJointTypeFixed,
+               dJointTypeNull, dJointTypeAMotor } dJointType;
+/* angular motor modes (include/ode/common.h:360-363) */
+enum { dAMotorUser = 0, dAMotorEuler = 1 };
 
 /* include/ode/common.h:305-354 */
 enum {
@@ -200,6 +203,19 @@ dReal dJointGetUniversalAngle2(dJointID j);                              /* :257
 void dJointSetFixed(dJointID j);                                         /* :2247 */
 void dJointSetFixedParam(dJointID j, int parameter, dReal value);        /* :2254 */
 dReal dJointGetFixedParam(dJointID j, int parameter);                    /* :2934 */
+dJointID dJointCreateAMotor(dWorldID w, dJointGroupID g);                /* :1621 */
+void dJointSetAMotorNumAxes(dJointID j, int num);                        /* :2261 */
+void dJointSetAMotorAxis(dJointID j, int anum, int rel, dReal x, dReal y, dReal z); /* :2267 */
+void dJointSetAMotorAngle(dJointID j, int anum, dReal angle);            /* :2279 */
+void dJointSetAMotorParam(dJointID j, int parameter, dReal value);       /* :2285 */
+void dJointSetAMotorMode(dJointID j, int mode);                          /* :2291 */
+void dJointAddAMotorTorques(dJointID j, dReal torque1, dReal torque2, dReal torque3); /* :2301 */
+int dJointGetAMotorNumAxes(dJointID j);                                  /* :2840 */
+void dJointGetAMotorAxis(dJointID j, int anum, dVector3 result);         /* :2851 */
+int dJointGetAMotorAxisRel(dJointID j, int anum);                        /* :2869 */
+dReal dJointGetAMotorAngle(dJointID j, int anum);                        /* :2879 */
+dReal dJointGetAMotorParam(dJointID j, int parameter);                   /* :2895 */
+int dJointGetAMotorMode(dJointID j);                                     /* :2910 */
 int dAreConnectedExcluding(dBodyID b1, dBodyID b2, int joint_type);      /* :2968 */
 
 /* mass: include/ode/mass.h */

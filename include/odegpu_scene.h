@@ -42,7 +42,8 @@ enum {
   ODEGPU_JOINT_CONTACT = 4,
   ODEGPU_JOINT_UNIVERSAL = 5,
   ODEGPU_JOINT_HINGE2 = 6,
-  ODEGPU_JOINT_FIXED = 7
+  ODEGPU_JOINT_FIXED = 7,
+  ODEGPU_JOINT_AMOTOR = 9
 };
 
 /* dContact surface mode bits (include/ode/contact.h:33-49). */
@@ -92,12 +93,18 @@ typedef struct odegpuWorldParams {
  *                           cfm, stop_erp, stop_cfm}
  *   universal: [0..8] limot1, [9..17] limot2
  *   hinge2: [0..8] limot1, [9..17] limot2, [18] susp_erp, [19] susp_cfm
+ *   amotor: [0] number of axes, [1] mode (0 user, 1 Euler), [2..4] rel of
+ *           axes 0..2 (0 global, 1 body 1, 2 body 2), [5..13] limot of axis 0,
+ *           [14..22] axis 1, [23..31] axis 2, [32..34] user-mode angles
  * (dxJointLimitMotor fields, ode/src/joints/joint.h:160-170). The geometry
  * setters used per type: ball and universal take joint_anchor; hinge,
  * hinge2, slider and universal take joint_axis1; hinge2 and universal take
  * joint_axis2; the fixed joint takes the bodies' placement at creation
- * (dJointSetFixed). */
-#define ODEGPU_JOINT_NPARAM 20
+ * (dJointSetFixed); the amotor's axes 0, 1, 2 (world frame, as
+ * dJointSetAMotorAxis takes them) are joint_anchor, joint_axis1,
+ * joint_axis2, set in the order mode, number of axes, axes, parameters,
+ * angles. */
+#define ODEGPU_JOINT_NPARAM 36
 /* Number of doubles per geom in odegpuScene.geom_param:
  *   sphere [0]=r; box [0..2]=side; capsule [0]=r [1]=length;
  *   plane [0..3]=a,b,c,d (normalised as dCreatePlane does). */
@@ -155,7 +162,9 @@ typedef struct odegpuScene {
                                   torque1/torque2 in [0]/[1]
                                   (dJointAddHinge2Torques,
                                   dJointAddUniversalTorques), slider force in
-                                  [0] (dJointAddSliderForce)                  */
+                                  [0] (dJointAddSliderForce), amotor torques
+                                  about axes 0 and 1 in [0]/[1]
+                                  (dJointAddAMotorTorques with 0 about axis 2) */
   const double* body_force;    /* [n_ctrl_steps][nb][6]: force, torque        */
   const double* joint_stop;    /* [n_ctrl_steps][nj]: before the step, limot1
                                   lostop = histop of a hinge, hinge2 or

@@ -810,14 +810,15 @@ int odegpuBatchCreate(const odegpuScene* sc, const odegpuBatchConfig* cfg, odegp
       const int gj = D.joint_off + j;
       const int type = sc->joint_type[gj];
       if (type != ODEGPU_JOINT_BALL && type != ODEGPU_JOINT_HINGE && type != ODEGPU_JOINT_HINGE2 &&
-          type != ODEGPU_JOINT_SLIDER && type != ODEGPU_JOINT_UNIVERSAL && type != ODEGPU_JOINT_FIXED) {
+          type != ODEGPU_JOINT_SLIDER && type != ODEGPU_JOINT_UNIVERSAL && type != ODEGPU_JOINT_FIXED &&
+          type != ODEGPU_JOINT_AMOTOR) {
         delete B;
         return fail(ODEGPU_E_ARG, "unsupported joint type " + std::to_string(type));
       }
       og_host::HJoint H;
       og_host::setup_joint(type, H, hb.data() + D.body_off, sc->joint_body[2 * gj], sc->joint_body[2 * gj + 1],
                            sc->joint_anchor + 3 * (size_t)gj, sc->joint_axis1 + 3 * (size_t)gj,
-                           sc->joint_axis2 + 3 * (size_t)gj);
+                           sc->joint_axis2 + 3 * (size_t)gj, sc->joint_param + ODEGPU_JOINT_NPARAM * (size_t)gj);
       DevJoint& J = joints[gj];
       std::memset(&J, 0, sizeof(J));
       J.type = type; J.b1 = H.b1; J.b2 = H.b2; J.reverse = H.reverse;
@@ -836,6 +837,11 @@ int odegpuBatchCreate(const odegpuScene* sc, const odegpuBatchConfig* cfg, odegp
       if (type == ODEGPU_JOINT_UNIVERSAL) {
         limot(J.lm1, jp);
         limot(J.lm2, jp + 9);
+      }
+      if (type == ODEGPU_JOINT_AMOTOR) {
+        limot(J.lm1, jp + 5);
+        limot(J.lm2, jp + 14);
+        limot(J.lm3, jp + 23);
       }
       if (type == ODEGPU_JOINT_HINGE2) {
         limot(J.lm1, jp);

@@ -21,6 +21,16 @@ inline void pack_joint_geometry(int type, const og_host::HJoint& H, DevJoint& J)
     else if (type == J_UNIVERSAL) J.qrel2[k] = (float)H.qrel2[k];
   }
   J.c0 = (float)H.c0; J.s0 = (float)H.s0;
+  if (type == J_AMOTOR) {
+    J.am_num = H.am_num;
+    J.am_mode = H.am_mode;
+    for (int i = 0; i < 3; ++i) {
+      J.am_rel[i] = H.am_rel[i];
+      J.am_angle[i] = (float)H.am_angle[i];
+      for (int k = 0; k < 4; ++k) J.am_axis[i][k] = (float)H.am_axis[i][k];
+    }
+    for (int k = 0; k < 4; ++k) { J.am_ref1[k] = (float)H.am_ref1[k]; J.am_ref2[k] = (float)H.am_ref2[k]; }
+  }
 }
 
 // One world as the ODE API layer hands it to the device, in ODE's creation

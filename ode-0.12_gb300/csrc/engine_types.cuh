@@ -10,7 +10,9 @@
 namespace og {
 
 // Joint types (ODE dJointType values) and surface mode bits (dContact).
-enum { J_BALL = 1, J_HINGE = 2, J_SLIDER = 3, J_CONTACT = 4, J_UNIVERSAL = 5, J_HINGE2 = 6, J_FIXED = 7 };
+enum { J_BALL = 1, J_HINGE = 2, J_SLIDER = 3, J_CONTACT = 4, J_UNIVERSAL = 5, J_HINGE2 = 6, J_FIXED = 7,
+       J_AMOTOR = 9 };
+enum { AMOTOR_USER = 0, AMOTOR_EULER = 1 };
 enum {
   SURF_MU2 = 0x001, SURF_FDIR1 = 0x002, SURF_BOUNCE = 0x004, SURF_SOFT_ERP = 0x008,
   SURF_SOFT_CFM = 0x010, SURF_MOTION1 = 0x020, SURF_MOTION2 = 0x040, SURF_MOTIONN = 0x080,
@@ -65,6 +67,12 @@ struct DevJoint {
   };
   float erp, cfm, c0, s0, susp_erp, susp_cfm;   // erp / cfm: ball and fixed
   DevLimot lm1, lm2;
+  // angular motor (ode/src/joints/amotor.h): lm1 / lm2 / lm3 drive axes 0 / 1 / 2
+  DevLimot lm3;
+  int am_num, am_mode, am_rel[3];
+  float am_axis[3][4];          // axes in the frame rel selects (0 world, 1 body 1, 2 body 2)
+  float am_ref1[4], am_ref2[4]; // Euler mode reference vectors
+  float am_angle[3];            // user mode angles (dJointSetAMotorAngle)
 };
 
 // A contact produced by the narrowphase and turned into a contact joint.

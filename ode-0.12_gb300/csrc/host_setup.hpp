@@ -181,6 +181,9 @@ struct HJoint {
   double offset[4];   // slider, fixed
   double qrel2[4];    // universal (qrel holds qrel1)
   double c0, s0;
+  // angular motor (ode/src/joints/amotor.h)
+  int am_num, am_mode, am_rel[3];
+  double am_axis[3][4], am_ref1[4], am_ref2[4], am_angle[3];
 };
 
 inline void attach(HJoint& J, int b1, int b2) {
@@ -351,6 +354,50 @@ inline double slider_position(const HJoint& J, const HBody* B) {
   return dot3(ax1, q);
 }
 
+// dxJointAMotor::setEulerReferenceVectors (ode/src/joints/amotor.cpp:148-181);
+// without a second body the reference adds to reference2 on every call.
+inline void amotor_euler_refs(HJoint& J, const HBody* B) {
+  if (J.b1 < 0) return;
+  if (J.b2 >= 0) {
+    double r[3];
+    mul0_331(r, B[J.b2].R, J.am_axis[2]);
+    mul1_331(J.am_ref1, B[J.b1].R, r);
+    mul0_331(r, B[J.b1].R, J.am_axis[0]);
+    mul1_331(J.am_ref2, B[J.b2].R, r);
+  } else {
+    double r[4] = {J.am_axis[2][0], J.am_axis[2][1], J.am_axis[2][2], J.am_axis[2][3]};
+    mul1_331(J.am_ref1, B[J.b1].R, r);
+    mul0_331(r, B[J.b1].R, J.am_axis[0]);
+    for (int k = 0; k < 4; ++k) J.am_ref2[k] += r[k];
+  }
+}
+// dJointSetAMotorMode / NumAxes / Axis (ode/src/joints/amotor.cpp:260-323, :350-363)
+inline void amotor_set_mode(HJoint& J, const HBody* B, int mode) {
+  J.am_mode = mode;
+  if (mode == 1) { J.am_num = 3; amotor_euler_refs(J, B); }
+}
+inline void amotor_set_num(HJoint& J, int num) {
+  if (J.am_mode == 1) J.am_num = 3;
+  else J.am_num = num < 0 ? 0 : (num > 3 ? 3 : num);
+}
+inline void amotor_set_axis(HJoint& J, const HBody* B, int anum, int rel, double x, double y, double z) {
+  if (anum < 0) anum = 0;
+  if (anum > 2) anum = 2;
+  if (J.b2 < 0 && rel == 2) rel = 1;
+  J.am_rel[anum] = rel;
+  double r[4] = {x, y, z, 0};
+  double* a = J.am_axis[anum];
+  if (rel > 0) {
+    if (rel == 1) mul1_331(a, B[J.b1].R, r);
+    else if (J.b2 >= 0) mul1_331(a, B[J.b2].R, r);
+    else for (int k = 0; k < 4; ++k) a[k] = r[k];
+  } else {
+    a[0] = r[0]; a[1] = r[1]; a[2] = r[2];
+  }
+  safe_normalize3(a);
+  if (J.am_mode == 1) amotor_euler_refs(J, B);
+}
+
 // The setter sequence a scene's joint goes through: dJointAttach, then
 //   ball:   dJointSetBallAnchor
 //   hinge:  dJointSetHingeAnchor, dJointSetHingeAxis
@@ -358,10 +405,13 @@ inline double slider_position(const HJoint& J, const HBody* B) {
 //   slider: dJointSetSliderAxis
 //   universal: dJointSetUniversalAnchor, dJointSetUniversalAxis1, dJointSetUniversalAxis2
 //   fixed:  dJointSetFixed
+//   amotor: dJointSetAMotorMode, dJointSetAMotorNumAxes, dJointSetAMotorAxis
+//           (axes 0..num-1 in user mode, 0 and 2 in Euler mode), the angles of
+//           user mode (dJointSetAMotorAngle); jp is its parameter block
 // (with the attach-time setRelativeValues of hinge2, hinge2.cpp:425-448; the
 // slider's and universal's are overwritten in full by their setters).
 inline void setup_joint(int type, HJoint& J, const HBody* B, int b1, int b2, const double* a,
-                        const double* x1, const double* x2) {
+                        const double* x1, const double* x2, const double* jp = nullptr) {
   std::memset(&J, 0, sizeof(J));
   J.axis1[0] = 1;
   if (type == 6) { J.axis2[1] = 1; J.v1[0] = 1; J.v2[1] = 1; }
@@ -413,6 +463,15 @@ inline void setup_joint(int type, HJoint& J, const HBody* B, int b1, int b2, con
   } else if (type == 7) {
     fixed_offset(J, B);
     initial_qrel(J, B);
+  } else if (type == 9 && jp && J.b1 >= 0) {
+    const int mode = (int)jp[1];
+    amotor_set_mode(J, B, mode);
+    amotor_set_num(J, (int)jp[0]);
+    const double* ax[3] = {a, x1, x2};
+    for (int i = 0; i < 3; ++i)
+      if (mode == 1 ? i != 1 : i < J.am_num) amotor_set_axis(J, B, i, (int)jp[2 + i], ax[i][0], ax[i][1], ax[i][2]);
+    if (mode == 0)
+      for (int i = 0; i < J.am_num; ++i) J.am_angle[i] = jp[32 + i];
   }
 }
 

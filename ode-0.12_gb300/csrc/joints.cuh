@@ -226,6 +226,41 @@ OG_D float slider_position(const BodyRef& B1, const BodyRef* B2, const DevJoint&
   return dot3(ax1, q);
 }
 
+// dxJointAMotor::computeGlobalAxes (ode/src/joints/amotor.cpp:52-94)
+OG_D void amotor_axes(const BodyRef& B1, const BodyRef* B2, const DevJoint& J, float (&ax)[3][3]) {
+  if (J.am_mode == AMOTOR_EULER) {
+    mul0_331(ax[0], B1.R, J.am_axis[0]);
+    if (B2) mul0_331(ax[2], B2->R, J.am_axis[2]);
+    else { ax[2][0] = J.am_axis[2][0]; ax[2][1] = J.am_axis[2][1]; ax[2][2] = J.am_axis[2][2]; }
+    cross3(ax[1], ax[2], ax[0]);
+    safe_normalize3(ax[1]);
+    return;
+  }
+  for (int i = 0; i < J.am_num; ++i) {
+    if (J.am_rel[i] == 1) mul0_331(ax[i], B1.R, J.am_axis[i]);
+    else if (J.am_rel[i] == 2) {
+      if (B2) mul0_331(ax[i], B2->R, J.am_axis[i]);
+    } else {
+      ax[i][0] = J.am_axis[i][0]; ax[i][1] = J.am_axis[i][1]; ax[i][2] = J.am_axis[i][2];
+    }
+  }
+}
+
+// dxJointAMotor::computeEulerAngles (ode/src/joints/amotor.cpp:98-139)
+OG_D void amotor_euler_angles(const BodyRef& B1, const BodyRef* B2, const DevJoint& J, const float (&ax)[3][3],
+                              float* angle) {
+  float ref1[3], ref2[3], q[3];
+  mul0_331(ref1, B1.R, J.am_ref1);
+  if (B2) mul0_331(ref2, B2->R, J.am_ref2);
+  else { ref2[0] = J.am_ref2[0]; ref2[1] = J.am_ref2[1]; ref2[2] = J.am_ref2[2]; }
+  cross3(q, ax[0], ref1);
+  angle[0] = -atan2f(dot3(ax[2], q), dot3(ax[2], ref1));
+  cross3(q, ax[0], ax[1]);
+  angle[1] = -atan2f(dot3(ax[2], ax[0]), dot3(ax[2], q));
+  cross3(q, ax[1], ax[2]);
+  angle[2] = -atan2f(dot3(ref2, ax[1]), dot3(ref2, q));
+}
+
 // setFixedOrientation (ode/src/joints/joint.cpp:202-255): three rows from r0
 // that hold the relative orientation at qrel, with info->erp as the joint
 // finds it.
@@ -313,13 +348,14 @@ OG_D int limot_add(const DevLimot& L, int limit, float limit_err, bool has_b2, c
       float fm = L.fmax;
       if ((L.vel > 0.f) || (L.vel == 0.f && limit == 2)) fm = -fm;
       if ((limit == 1 && L.vel > 0.f) || (limit == 2 && L.vel < 0.f)) fm *= L.fudge;
+      // accumulated: an angular motor can meet limits on several axes
       if (rotational) {
-        for (int k = 0; k < 3; ++k) { tq.t1[k] = -fm * ax1[k]; tq.t2[k] = fm * ax1[k]; }
+        for (int k = 0; k < 3; ++k) { tq.t1[k] += -fm * ax1[k]; tq.t2[k] += fm * ax1[k]; }
       } else {
         for (int k = 0; k < 3; ++k) {
-          tq.f1[k] = -fm * ax1[k];
-          tq.t1[k] = has_b2 ? -fm * ltd[k] : 0.f;
-          tq.t2[k] = -fm * ltd[k];
+          tq.f1[k] += -fm * ax1[k];
+          tq.t1[k] += has_b2 ? -fm * ltd[k] : 0.f;
+          tq.t2[k] += -fm * ltd[k];
         }
       }
       tq.active = 1;
@@ -357,8 +393,8 @@ OG_D int limot_add(const DevLimot& L, int limit, float limit_err, bool has_b2, c
 // Per-joint state carried from getInfo1 to getInfo2 within a step.
 struct JointInfo1 {
   int m;
-  int limit1, limit2;
-  float err1, err2;
+  int limit1, limit2, limit3;
+  float err1, err2, err3;
 };
 
 // getInfo1: contact (ode/src/joints/contact.cpp:47-71), ball (ball.cpp:56-60),
@@ -366,7 +402,7 @@ struct JointInfo1 {
 // (universal.cpp:265-293), hinge2 (hinge2.cpp:81-101), fixed (fixed.cpp:53-58).
 // lm1: the joint's limot1 for this step (stops may differ from J.lm1).
 OG_D JointInfo1 persistent_info1(const DevJoint& J, const DevLimot& lm1, const BodyRef& B1, const BodyRef* B2) {
-  JointInfo1 r{0, 0, 0, 0.f, 0.f};
+  JointInfo1 r{0, 0, 0, 0, 0.f, 0.f, 0.f};
   switch (J.type) {
     case J_BALL: r.m = 3; break;
     case J_HINGE: {
@@ -405,6 +441,21 @@ OG_D JointInfo1 persistent_info1(const DevJoint& J, const DevLimot& lm1, const B
       break;
     }
     case J_FIXED: r.m = 6; break;
+    case J_AMOTOR: {
+      // ode/src/joints/amotor.cpp:187-210: each axis's limit is tested every step
+      float ang[3] = {J.am_angle[0], J.am_angle[1], J.am_angle[2]};
+      if (J.am_mode == AMOTOR_EULER) {
+        float ax[3][3];
+        amotor_axes(B1, B2, J, ax);
+        amotor_euler_angles(B1, B2, J, ax, ang);
+      }
+      const DevLimot* lm[3] = {&lm1, &J.lm2, &J.lm3};
+      int* lim[3] = {&r.limit1, &r.limit2, &r.limit3};
+      float* err[3] = {&r.err1, &r.err2, &r.err3};
+      for (int i = 0; i < J.am_num; ++i)
+        if (limot_test(*lm[i], ang[i], *lim[i], *err[i]) || lm[i]->fmax > 0.f) r.m++;
+      break;
+    }
     default: break;
   }
   return r;
@@ -555,6 +606,27 @@ __device__ __noinline__ void persistent_info2_more(const DevJoint& J, const DevL
       limot_add(J.lm2, i1.limit2, i1.err2, B2 != nullptr, B1, B2, in, row, ax2, tq2);
       break;
     }
+    case J_AMOTOR: {
+      // ode/src/joints/amotor.cpp:213-256: in Euler mode the rows constrain
+      // w2 - w1 along ax1 x ax2, ax1 and ax0 x ax1
+      float ax[3][3];
+      amotor_axes(B1, B2, J, ax);
+      float e0[3], e2[3];
+      const float* axp[3] = {ax[0], ax[1], ax[2]};
+      if (J.am_mode == AMOTOR_EULER) {
+        cross3(e2, ax[0], ax[1]);
+        axp[2] = e2;
+        cross3(e0, ax[1], ax[2]);
+        axp[0] = e0;
+      }
+      const DevLimot* lm[3] = {&lm1, &J.lm2, &J.lm3};
+      const int lim[3] = {i1.limit1, i1.limit2, i1.limit3};
+      const float err[3] = {i1.err1, i1.err2, i1.err3};
+      int row = 0;
+      for (int i = 0; i < J.am_num; ++i)
+        row += limot_add(*lm[i], lim[i], err[i], B2 != nullptr, B1, B2, in, row, axp[i], i == 0 ? tq1 : tq2);
+      break;
+    }
     case J_FIXED: {
       // orientation rows with the erp the joint finds, then (like the ball
       // joint) info->erp = the joint's erp for the position rows and onwards
@@ -634,7 +706,8 @@ OG_D void persistent_info2(const DevJoint& J, const DevLimot& lm1, const JointIn
     }
     case J_SLIDER:
     case J_UNIVERSAL:
-    case J_FIXED: persistent_info2_more(J, lm1, i1, B1, B2, in, tq1, tq2); break;
+    case J_FIXED:
+    case J_AMOTOR: persistent_info2_more(J, lm1, i1, B1, B2, in, tq1, tq2); break;
     default: break;
   }
 }

@@ -45,7 +45,7 @@ struct dxJoint {
   // ball / hinge / hinge2 data, FP64 as the setters compute it
   og_host::HJoint h;
   double erp, cfm;
-  og::DevLimot lm1, lm2;
+  og::DevLimot lm1, lm2, lm3;
   double susp_erp, susp_cfm;
   // contact
   dContact contact;
@@ -157,6 +157,7 @@ dxJoint* new_joint(dxWorld* w, dxJointGroup* g, int type) {
   j->cfm = w->cfm;
   limot_default(j->lm1, w);
   limot_default(j->lm2, w);
+  limot_default(j->lm3, w);
   j->susp_erp = w->erp;
   j->susp_cfm = w->cfm;
   w->joints.push_back(j);
@@ -343,6 +344,7 @@ dJointID dJointCreateHinge2(dWorldID w, dJointGroupID g) { return new_joint(w, g
 dJointID dJointCreateSlider(dWorldID w, dJointGroupID g) { return new_joint(w, g, dJointTypeSlider); }
 dJointID dJointCreateUniversal(dWorldID w, dJointGroupID g) { return new_joint(w, g, dJointTypeUniversal); }
 dJointID dJointCreateFixed(dWorldID w, dJointGroupID g) { return new_joint(w, g, dJointTypeFixed); }
+dJointID dJointCreateAMotor(dWorldID w, dJointGroupID g) { return new_joint(w, g, dJointTypeAMotor); }
 dJointID dJointCreateContact(dWorldID w, dJointGroupID g, const dContact* c) {
   dxJoint* j = new_joint(w, g, dJointTypeContact);
   j->contact = *c;   // dJointCreateContact copies the contact (ode/src/ode.cpp:1201-1208)
@@ -727,6 +729,94 @@ dReal dJointGetFixedParam(dJointID j, int p) {
   return 0;
 }
 
+// angular motor (ode/src/joints/amotor.cpp)
+void dJointSetAMotorNumAxes(dJointID j, int num) { og_host::amotor_set_num(j->h, num); }
+void dJointSetAMotorAxis(dJointID j, int anum, int rel, dReal x, dReal y, dReal z) {
+  JB jb(j);
+  og_host::amotor_set_axis(j->h, jb.B, anum, rel, x, y, z);
+}
+void dJointSetAMotorAngle(dJointID j, int anum, dReal angle) {
+  // :326-336 (user mode only)
+  if (j->h.am_mode == dAMotorUser && anum >= 0 && anum < 3) j->h.am_angle[anum] = angle;
+}
+static og::DevLimot& amotor_limot(dJointID j, int parameter) {
+  const int anum = std::min(2, std::max(0, parameter >> 8));
+  return anum == 0 ? j->lm1 : anum == 1 ? j->lm2 : j->lm3;
+}
+void dJointSetAMotorParam(dJointID j, int p, dReal v) { limot_set(amotor_limot(j, p), p & 0xff, v); }
+dReal dJointGetAMotorParam(dJointID j, int p) { return limot_get(amotor_limot(j, p), p & 0xff); }
+void dJointSetAMotorMode(dJointID j, int mode) {
+  JB jb(j);
+  og_host::amotor_set_mode(j->h, jb.B, mode);
+}
+int dJointGetAMotorMode(dJointID j) { return j->h.am_mode; }
+int dJointGetAMotorNumAxes(dJointID j) { return j->h.am_num; }
+int dJointGetAMotorAxisRel(dJointID j, int anum) { return j->h.am_rel[std::min(2, std::max(0, anum))]; }
+// the global axes (computeGlobalAxes, :52-94)
+static void amotor_global_axes(const dxJoint* j, double ax[3][3]) {
+  JB jb(j);
+  const og_host::HJoint& H = j->h;
+  const og_host::HBody* B2 = j->body[1] ? &jb.B[1] : nullptr;
+  if (H.am_mode == dAMotorEuler) {
+    og_host::mul0_331(ax[0], jb.B[0].R, H.am_axis[0]);
+    if (B2) og_host::mul0_331(ax[2], B2->R, H.am_axis[2]);
+    else for (int k = 0; k < 3; ++k) ax[2][k] = H.am_axis[2][k];
+    og_host::cross3(ax[1], ax[2], ax[0]);
+    og_host::safe_normalize3(ax[1]);
+    return;
+  }
+  for (int i = 0; i < H.am_num; ++i) {
+    if (H.am_rel[i] == 1) og_host::mul0_331(ax[i], jb.B[0].R, H.am_axis[i]);
+    else if (H.am_rel[i] == 2 && B2) og_host::mul0_331(ax[i], B2->R, H.am_axis[i]);
+    else for (int k = 0; k < 3; ++k) ax[i][k] = H.am_axis[i][k];
+  }
+}
+void dJointGetAMotorAxis(dJointID j, int anum, dVector3 r) {
+  // :393-420
+  anum = std::min(2, std::max(0, anum));
+  const og_host::HJoint& H = j->h;
+  if (H.am_rel[anum] == 1) world_axis1(j, H.am_axis[anum], r);
+  else if (H.am_rel[anum] == 2) world_axis2(j, H.am_axis[anum], r);
+  else for (int k = 0; k < 3; ++k) r[k] = (dReal)H.am_axis[anum][k];
+}
+dReal dJointGetAMotorAngle(dJointID j, int anum) {
+  // user mode: the angle set; Euler mode: the angles of the bodies' current
+  // placement (the reference returns those its last getInfo1 computed)
+  anum = std::min(2, std::max(0, anum));
+  const og_host::HJoint& H = j->h;
+  if (H.am_mode != dAMotorEuler || !j->body[0]) return (dReal)H.am_angle[anum];
+  double ax[3][3], ref1[3], ref2[3], q[3];
+  amotor_global_axes(j, ax);
+  JB jb(j);
+  og_host::mul0_331(ref1, jb.B[0].R, H.am_ref1);
+  if (j->body[1]) og_host::mul0_331(ref2, jb.B[1].R, H.am_ref2);
+  else for (int k = 0; k < 3; ++k) ref2[k] = H.am_ref2[k];
+  if (anum == 0) {
+    og_host::cross3(q, ax[0], ref1);
+    return (dReal)-std::atan2(og_host::dot3(ax[2], q), og_host::dot3(ax[2], ref1));
+  }
+  if (anum == 1) {
+    og_host::cross3(q, ax[0], ax[1]);
+    return (dReal)-std::atan2(og_host::dot3(ax[2], ax[0]), og_host::dot3(ax[2], q));
+  }
+  og_host::cross3(q, ax[1], ax[2]);
+  return (dReal)-std::atan2(og_host::dot3(ref2, ax[1]), og_host::dot3(ref2, q));
+}
+void dJointAddAMotorTorques(dJointID j, dReal t1, dReal t2, dReal t3) {
+  // :474-504
+  if (j->h.am_num == 0 || !j->body[0]) return;
+  double ax[3][3];
+  amotor_global_axes(j, ax);
+  dReal t[3];
+  for (int k = 0; k < 3; ++k) t[k] = (dReal)ax[0][k] * t1;
+  if (j->h.am_num >= 2) {
+    for (int k = 0; k < 3; ++k) t[k] += (dReal)ax[1][k] * t2;
+    if (j->h.am_num >= 3) for (int k = 0; k < 3; ++k) t[k] += (dReal)ax[2][k] * t3;
+  }
+  dBodyAddTorque(j->body[0], t[0], t[1], t[2]);
+  if (j->body[1]) dBodyAddTorque(j->body[1], -t[0], -t[1], -t[2]);
+}
+
 int dAreConnectedExcluding(dBodyID b1, dBodyID b2, int joint_type) {
   // ode/src/ode.cpp:1529-1537
   if (!b1) return 0;
@@ -970,7 +1060,7 @@ int dWorldQuickStep(dWorldID w, dReal stepsize) {
     J.reverse = j->reverse;
     og::pack_joint_geometry(j->type, j->h, J);
     J.erp = (float)j->erp; J.cfm = (float)j->cfm;
-    J.lm1 = j->lm1; J.lm2 = j->lm2;
+    J.lm1 = j->lm1; J.lm2 = j->lm2; J.lm3 = j->lm3;
     J.susp_erp = (float)j->susp_erp; J.susp_cfm = (float)j->susp_cfm;
   }
   hw.contacts.resize(cj.size());

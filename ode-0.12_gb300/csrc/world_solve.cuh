@@ -60,7 +60,8 @@ OG_D const float* step_stops(const BatchDev& d, const WorldDesc& D, int step) {
 // (when given) in place of lostop / histop.
 OG_D DevLimot step_limot1(const DevJoint& J, const float* stops, int ord) {
   DevLimot L = J.lm1;
-  if (stops && (J.type == J_HINGE || J.type == J_HINGE2 || J.type == J_SLIDER || J.type == J_UNIVERSAL)) {
+  if (stops && (J.type == J_HINGE || J.type == J_HINGE2 || J.type == J_SLIDER || J.type == J_UNIVERSAL ||
+                J.type == J_AMOTOR)) {
     const float v = stops[ord];
     if (!isnan(v)) { L.lostop = v; L.histop = v; }
   }
@@ -500,6 +501,26 @@ OG_D void controls_joints(const BatchDev& d, const WorldDesc& D, int step) {
           d.tacc[D.body_off + J.b1] = t1;
           float4 t2 = d.tacc[D.body_off + J.b2];
           t2.x += ltd[0]; t2.y += ltd[1]; t2.z += ltd[2];
+          d.tacc[D.body_off + J.b2] = t2;
+        }
+      } else if (J.type == J_AMOTOR && J.am_num > 0) {
+        // dJointAddAMotorTorques(j, tq[0], tq[1], 0) (ode/src/joints/amotor.cpp:474-504)
+        BodyRef A1, A2;
+        load_body_ref(d, D.body_off + J.b1, A1);
+        if (J.b2 >= 0) load_body_ref(d, D.body_off + J.b2, A2);
+        float ax[3][3];
+        amotor_axes(A1, J.b2 >= 0 ? &A2 : nullptr, J, ax);
+        float t[3] = {ax[0][0] * tq[0], ax[0][1] * tq[0], ax[0][2] * tq[0]};
+        if (J.am_num >= 2) {
+          t[0] += ax[1][0] * tq[1]; t[1] += ax[1][1] * tq[1]; t[2] += ax[1][2] * tq[1];
+          if (J.am_num >= 3) { t[0] += ax[2][0] * 0.f; t[1] += ax[2][1] * 0.f; t[2] += ax[2][2] * 0.f; }
+        }
+        float4 t1 = d.tacc[D.body_off + J.b1];
+        t1.x += t[0]; t1.y += t[1]; t1.z += t[2];
+        d.tacc[D.body_off + J.b1] = t1;
+        if (J.b2 >= 0) {
+          float4 t2 = d.tacc[D.body_off + J.b2];
+          t2.x += -t[0]; t2.y += -t[1]; t2.z += -t[2];
           d.tacc[D.body_off + J.b2] = t2;
         }
       } else if (J.type == J_UNIVERSAL) {

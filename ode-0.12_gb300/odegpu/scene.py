@@ -19,6 +19,8 @@ import numpy as np
 GEOM_SPHERE, GEOM_BOX, GEOM_CAPSULE, GEOM_PLANE, GEOM_HEIGHTFIELD = 0, 1, 2, 4, 9
 JOINT_BALL, JOINT_HINGE, JOINT_SLIDER, JOINT_CONTACT, JOINT_UNIVERSAL, JOINT_HINGE2, JOINT_FIXED = \
     1, 2, 3, 4, 5, 6, 7
+JOINT_AMOTOR = 9
+AMOTOR_USER, AMOTOR_EULER = 0, 1
 BODY_GYROSCOPIC, BODY_NO_GRAVITY = 1, 2
 
 CONTACT_MU2 = 0x001
@@ -28,7 +30,7 @@ CONTACT_SOFT_CFM = 0x010
 CONTACT_APPROX1 = 0x3000
 
 GEOM_NPARAM = 4
-JOINT_NPARAM = 20
+JOINT_NPARAM = 36
 INF = float("inf")
 
 
@@ -326,6 +328,10 @@ class Scene:
         self = cls.__new__(cls)
         for k in cls._ARRAYS:
             setattr(self, k, np.ascontiguousarray(a[k]))
+        jp = self.joint_param.reshape(len(self.joint_type), -1)
+        if jp.shape[1] < JOINT_NPARAM:   # fixtures written with fewer parameters per joint
+            jp = np.concatenate([jp, np.zeros((jp.shape[0], JOINT_NPARAM - jp.shape[1]))], axis=1)
+        self.joint_param = np.ascontiguousarray(jp)
         self.n_worlds = len(self.body_off) - 1
         wpa = np.asarray(a["world_params"])
         self.world_params = (WorldParams * max(1, self.n_worlds))()
@@ -781,12 +787,20 @@ def mechanisms(n_worlds=256, seed=13, steps=200):
          from 0.6 m with a random orientation and spin, and a 0.25 m cube
          welded to the environment (reversed fixed joint) given an initial
          velocity.
+      5. arm: an upper link (0.15x0.15x0.6 m, 1.5 kg) on a ball joint to the
+         environment and a lower link (0.12x0.12x0.6 m, 1 kg) on a ball joint
+         below it, spun U[-2,2] rad/s; an Euler-mode angular motor between
+         them (axis 0 = x on the upper link, axis 2 = z on the lower; stops
+         -/+0.5, -/+0.4, -/+0.6 rad) and a user-mode angular motor on the
+         upper link (2 axes: world y powered at vel U[-1,1] rad/s, fmax 3 N m;
+         upper-link x with stops [-0.1, 0.2] and user angle 0.3, so its limit
+         row is active); per-step torques U[-1,1] N m on that motor's axes.
     Surface mu 0.6 (pyramid friction). Max 4 contacts per pair."""
     rng = np.random.Generator(np.random.PCG64(seed))
     b = SceneBuilder()
     s = _std_surface(b, 0.6)
     NAN = float("nan")
-    rail, drop, piston, uni, hinge3 = [], [], [], [], []
+    rail, drop, piston, uni, hinge3, umot = [], [], [], [], [], []
     for wi in range(n_worlds):
         w = b.new_world(cfm=1e-5, seed=int(rng.integers(0, 2**32)))
         b.add_geom(w, GEOM_PLANE, -1, (0, 0, 1, 0), s)
@@ -863,6 +877,30 @@ def mechanisms(n_worlds=256, seed=13, steps=200):
                         avel=tuple(rng.uniform(-1, 1, 3)))
         b.add_geom(w, GEOM_BOX, wb, (0.25, 0.25, 0.25), s)
         b.add_joint(w, JOINT_FIXED, -1, wb, param=[0.2, 1e-5])
+        # 5. arm with an Euler angular motor and a user-mode angular motor
+        x5 = 12.5
+        m, I = box_mass_total(1.5, 0.15, 0.15, 0.6)
+        ua = b.add_body(w, (x5, 0.0, 1.7), m, I, avel=tuple(rng.uniform(-0.5, 0.5, 3)))
+        b.add_geom(w, GEOM_BOX, ua, (0.15, 0.15, 0.6), s)
+        m, I = box_mass_total(1.0, 0.12, 0.12, 0.6)
+        la = b.add_body(w, (x5, 0.0, 1.1), m, I, avel=tuple(rng.uniform(-2, 2, 3)))
+        b.add_geom(w, GEOM_BOX, la, (0.12, 0.12, 0.6), s)
+        b.add_joint(w, JOINT_BALL, ua, -1, anchor=(x5, 0.0, 2.0), param=[0.2, 1e-5])
+        b.add_joint(w, JOINT_BALL, ua, la, anchor=(x5, 0.0, 1.4), param=[0.2, 1e-5])
+        p = np.zeros(JOINT_NPARAM)
+        p[0], p[1] = 3, AMOTOR_EULER
+        p[2], p[3], p[4] = 1, 0, 2
+        p[5:14] = limot_params(lostop=-0.5, histop=0.5)
+        p[14:23] = limot_params(lostop=-0.4, histop=0.4)
+        p[23:32] = limot_params(lostop=-0.6, histop=0.6)
+        b.add_joint(w, JOINT_AMOTOR, ua, la, anchor=(1, 0, 0), axis1=(0, 1, 0), axis2=(0, 0, 1), param=p)
+        p = np.zeros(JOINT_NPARAM)
+        p[0], p[1] = 2, AMOTOR_USER
+        p[2], p[3] = 0, 1
+        p[5:14] = limot_params(vel=rng.uniform(-1, 1), fmax=3.0)
+        p[14:23] = limot_params(lostop=-0.1, histop=0.2)
+        p[32], p[33] = 0.0, 0.3
+        umot.append(b.add_joint(w, JOINT_AMOTOR, ua, -1, anchor=(0, 1, 0), axis1=(1, 0, 0), param=p))
     sc = b.build()
     nj = sc.nj_total
     tq = np.zeros((steps, nj, 2))
@@ -875,6 +913,7 @@ def mechanisms(n_worlds=256, seed=13, steps=200):
         tq[:, j0 + piston[wi], 0] = rng.uniform(-5, 5, steps)
         tq[:, j0 + uni[wi], :] = rng.uniform(-1, 1, (steps, 2))
         tq[:, j0 + hinge3[wi], 0] = rng.uniform(-0.5, 0.5, steps)
+        tq[:, j0 + umot[wi], :] = rng.uniform(-1, 1, (steps, 2))
         target = rng.uniform(-0.2, 0.2, steps)
         stops[servo, j0 + rail[wi]] = target[servo]
     sc.set_controls(joint_torque=tq, joint_stop=stops)

@@ -290,6 +290,10 @@ typedef struct {
   real c0, s0, v1[4], v2[4], susp_erp, susp_cfm;
   real offset[4];    /* slider, fixed */
   real qrel2[4];     /* universal (qrel holds qrel1) */
+  /* angular motor: lm1 / lm2 / lm3 drive axes 0 / 1 / 2 */
+  OLimot lm3;
+  int am_num, am_mode, am_rel[3];
+  real am_axis[3][4], am_ref1[4], am_ref2[4], am_angle[3];
   /* contact */
   odegpuSurface surf;
   real cpos[3], cnormal[3], cdepth;
@@ -412,6 +416,84 @@ static void universal_qrels(OWorld* W, OJoint* J) {
   q_from_r(qcross, R);
   if (J->b[1] >= 0) qmul1(J->qrel2, W->body[J->b[1]].q, qcross);
   else for (int i = 0; i < 4; ++i) J->qrel2[i] = qcross[i];
+}
+/* dxJointAMotor::setEulerReferenceVectors, ode/src/joints/amotor.cpp:148-181
+ * (without a second body reference2 is added to on every call) */
+static void amotor_euler_refs(OWorld* W, OJoint* J) {
+  if (J->b[0] < 0) return;
+  const real* R1 = W->body[J->b[0]].R;
+  if (J->b[1] >= 0) {
+    const real* R2 = W->body[J->b[1]].R;
+    real r[4];
+    mul0_331(r, R2, J->am_axis[2]);
+    mul1_331(J->am_ref1, R1, r);
+    mul0_331(r, R1, J->am_axis[0]);
+    mul1_331(J->am_ref2, R2, r);
+  } else {
+    real r[4] = {J->am_axis[2][0], J->am_axis[2][1], J->am_axis[2][2], J->am_axis[2][3]};
+    mul1_331(J->am_ref1, R1, r);
+    mul0_331(r, R1, J->am_axis[0]);
+    for (int k = 0; k < 4; ++k) J->am_ref2[k] += r[k];
+  }
+}
+/* dJointSetAMotorMode / NumAxes / Axis, ode/src/joints/amotor.cpp:260-323, :350-363 */
+static void amotor_set_mode(OWorld* W, OJoint* J, int mode) {
+  J->am_mode = mode;
+  if (mode == 1) { J->am_num = 3; amotor_euler_refs(W, J); }
+}
+static void amotor_set_num(OJoint* J, int num) {
+  if (J->am_mode == 1) J->am_num = 3;
+  else J->am_num = num < 0 ? 0 : (num > 3 ? 3 : num);
+}
+static void amotor_set_axis(OWorld* W, OJoint* J, int anum, int rel, real x, real y, real z) {
+  if (anum < 0) anum = 0;
+  if (anum > 2) anum = 2;
+  if (J->b[1] < 0 && rel == 2) rel = 1;
+  J->am_rel[anum] = rel;
+  real r[4] = {x, y, z, 0};
+  real* a = J->am_axis[anum];
+  if (rel > 0) {
+    if (rel == 1) mul1_331(a, W->body[J->b[0]].R, r);
+    else if (J->b[1] >= 0) mul1_331(a, W->body[J->b[1]].R, r);
+    else for (int k = 0; k < 4; ++k) a[k] = r[k];
+  } else {
+    a[0] = r[0]; a[1] = r[1]; a[2] = r[2];
+  }
+  safe_normalize3(a);
+  if (J->am_mode == 1) amotor_euler_refs(W, J);
+}
+/* dxJointAMotor::computeGlobalAxes, ode/src/joints/amotor.cpp:52-94 */
+static void amotor_axes(OWorld* W, OJoint* J, real ax[3][4]) {
+  const real* R1 = W->body[J->b[0]].R;
+  if (J->am_mode == 1) {
+    mul0_331(ax[0], R1, J->am_axis[0]);
+    if (J->b[1] >= 0) mul0_331(ax[2], W->body[J->b[1]].R, J->am_axis[2]);
+    else { ax[2][0] = J->am_axis[2][0]; ax[2][1] = J->am_axis[2][1]; ax[2][2] = J->am_axis[2][2]; }
+    cross3(ax[1], ax[2], ax[0]);
+    safe_normalize3(ax[1]);
+    return;
+  }
+  for (int i = 0; i < J->am_num; ++i) {
+    if (J->am_rel[i] == 1) mul0_331(ax[i], R1, J->am_axis[i]);
+    else if (J->am_rel[i] == 2) {
+      if (J->b[1] >= 0) mul0_331(ax[i], W->body[J->b[1]].R, J->am_axis[i]);
+    } else {
+      ax[i][0] = J->am_axis[i][0]; ax[i][1] = J->am_axis[i][1]; ax[i][2] = J->am_axis[i][2];
+    }
+  }
+}
+/* dxJointAMotor::computeEulerAngles, ode/src/joints/amotor.cpp:98-139 */
+static void amotor_euler_angles(OWorld* W, OJoint* J, real ax[3][4]) {
+  real ref1[3], ref2[3], q[3];
+  mul0_331(ref1, W->body[J->b[0]].R, J->am_ref1);
+  if (J->b[1] >= 0) mul0_331(ref2, W->body[J->b[1]].R, J->am_ref2);
+  else { ref2[0] = J->am_ref2[0]; ref2[1] = J->am_ref2[1]; ref2[2] = J->am_ref2[2]; }
+  cross3(q, ax[0], ref1);
+  J->am_angle[0] = -atan2(dot3(ax[2], q), dot3(ax[2], ref1));
+  cross3(q, ax[0], ax[1]);
+  J->am_angle[1] = -atan2(dot3(ax[2], ax[0]), dot3(ax[2], q));
+  cross3(q, ax[1], ax[2]);
+  J->am_angle[2] = -atan2(dot3(ref2, ax[1]), dot3(ref2, q));
 }
 /* dxJointHinge2::getAxisInfo / makeV1andV2, ode/src/joints/hinge2.cpp:97-106, :184-210 */
 static void hinge2_axis_info(OWorld* W, OJoint* J, real* ax1, real* ax2, real* axc, real* s, real* c) {
@@ -2006,6 +2088,19 @@ static int joint_info1(OWorld* W, OJoint* J) {
       return m;
     }
     case ODEGPU_JOINT_FIXED: return 6;   /* ode/src/joints/fixed.cpp:53-58 */
+    case ODEGPU_JOINT_AMOTOR: {
+      /* ode/src/joints/amotor.cpp:187-210 */
+      int m = 0;
+      if (J->am_mode == 1) {
+        real ax[3][4];
+        amotor_axes(W, J, ax);
+        amotor_euler_angles(W, J, ax);
+      }
+      OLimot* lm[3] = {&J->lm1, &J->lm2, &J->lm3};
+      for (int i = 0; i < J->am_num; ++i)
+        if (limot_test(lm[i], J->am_angle[i]) || lm[i]->fmax > 0) m++;
+      return m;
+    }
   }
   return 0;
 }
@@ -2189,6 +2284,23 @@ static void joint_info2(OWorld* W, OJoint* J, Info2* info) {
       info->c[3] = info->fps * info->erp * -k;
       int row = 4 + limot_add(W, J, &J->lm1, info, 4, ax1, 1);
       limot_add(W, J, &J->lm2, info, row, ax2, 1);
+      break;
+    }
+    case ODEGPU_JOINT_AMOTOR: {
+      /* ode/src/joints/amotor.cpp:213-256 */
+      real ax[3][4], e0[4], e2[4];
+      const real* axp[3];
+      amotor_axes(W, J, ax);
+      axp[0] = ax[0]; axp[1] = ax[1]; axp[2] = ax[2];
+      if (J->am_mode == 1) {
+        cross3(e2, ax[0], ax[1]);
+        axp[2] = e2;
+        cross3(e0, ax[1], ax[2]);
+        axp[0] = e0;
+      }
+      OLimot* lm[3] = {&J->lm1, &J->lm2, &J->lm3};
+      int row = 0;
+      for (int i = 0; i < J->am_num; ++i) row += limot_add(W, J, lm[i], info, row, axp[i], 1);
       break;
     }
     case ODEGPU_JOINT_FIXED: {
@@ -2719,6 +2831,28 @@ static void world_init(OWorld* W, const odegpuScene* sc, int w) {
         limot_set_all(&J->lm1, jp);
         limot_set_all(&J->lm2, jp + 9);
         break;
+      case ODEGPU_JOINT_AMOTOR: {
+        /* dJointCreateAMotor, dJointAttach, dJointSetAMotorMode / NumAxes /
+         * Axis (user mode: axes 0..num-1; Euler mode: 0 and 2) / Param / Angle */
+        limot_init(&J->lm1, W);
+        limot_init(&J->lm2, W);
+        limot_init(&J->lm3, W);
+        joint_attach(W, jj, jb1, jb2);
+        if (J->b[0] >= 0) {
+          const int mode = (int)jp[1];
+          amotor_set_mode(W, J, mode);
+          amotor_set_num(J, (int)jp[0]);
+          const double* ax[3] = {a, x1, x2};
+          for (int i = 0; i < 3; ++i)
+            if (mode == 1 ? i != 1 : i < J->am_num) amotor_set_axis(W, J, i, (int)jp[2 + i], ax[i][0], ax[i][1], ax[i][2]);
+          limot_set_all(&J->lm1, jp + 5);
+          limot_set_all(&J->lm2, jp + 14);
+          limot_set_all(&J->lm3, jp + 23);
+          if (mode == 0)
+            for (int i = 0; i < J->am_num; ++i) J->am_angle[i] = jp[32 + i];
+        }
+        break;
+      }
       case ODEGPU_JOINT_FIXED:
         /* dJointCreateFixed, dJointAttach, dJointSetFixed, dJointSetFixedParam */
         J->erp = W->erp; J->cfm = W->cfm;
@@ -2959,11 +3093,13 @@ static int world_step(OWorld* W, int s, double* contacts, int max_rec) {
       for (int i = 0; i < W->nj_persist; ++i) {
         OJoint* J = &W->joint[i];
         if (J->type != ODEGPU_JOINT_HINGE && J->type != ODEGPU_JOINT_HINGE2 &&
-            J->type != ODEGPU_JOINT_SLIDER && J->type != ODEGPU_JOINT_UNIVERSAL) continue;
+            J->type != ODEGPU_JOINT_SLIDER && J->type != ODEGPU_JOINT_UNIVERSAL &&
+            J->type != ODEGPU_JOINT_AMOTOR) continue;
         const double v = sc->joint_stop[(size_t)cs * sc->joint_off[sc->n_worlds] + j0 + i];
         const double* jp = sc->joint_param + (size_t)(j0 + i) * ODEGPU_JOINT_NPARAM;
-        J->lm1.lostop = isnan(v) ? jp[0] : v;
-        J->lm1.histop = isnan(v) ? jp[1] : v;
+        const double* lp = J->type == ODEGPU_JOINT_AMOTOR ? jp + 5 : jp;
+        J->lm1.lostop = isnan(v) ? lp[0] : v;
+        J->lm1.histop = isnan(v) ? lp[1] : v;
       }
     }
     if (sc->joint_torque) {
@@ -3017,6 +3153,23 @@ static int world_step(OWorld* W, int s, double* contacts, int max_rec) {
               for (int k = 0; k < 3; ++k) c[k] = 0.5 * (B2->pos[k] - B1->pos[k]);
               cross3(ltd, c, ax);
               for (int k = 0; k < 3; ++k) { B1->tacc[k] += ltd[k]; B2->tacc[k] += ltd[k]; }
+            }
+          }
+        } else if (J->type == ODEGPU_JOINT_AMOTOR) {
+          /* dJointAddAMotorTorques(j, t[0], t[1], 0), ode/src/joints/amotor.cpp:474-504 */
+          if (J->am_num > 0 && J->b[0] >= 0) {
+            real ax[3][4];
+            amotor_axes(W, J, ax);
+            ax[0][0] *= t[0]; ax[0][1] *= t[0]; ax[0][2] *= t[0];
+            if (J->am_num >= 2) {
+              for (int k = 0; k < 3; ++k) ax[0][k] += ax[1][k] * t[1];
+              if (J->am_num >= 3) for (int k = 0; k < 3; ++k) ax[0][k] += ax[2][k] * 0.0;
+            }
+            OBody* B1 = &W->body[J->b[0]];
+            for (int k = 0; k < 3; ++k) B1->tacc[k] += ax[0][k];
+            if (J->b[1] >= 0) {
+              OBody* B2 = &W->body[J->b[1]];
+              for (int k = 0; k < 3; ++k) B2->tacc[k] += -ax[0][k];
             }
           }
         } else if (J->type == ODEGPU_JOINT_UNIVERSAL) {

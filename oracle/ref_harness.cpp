@@ -189,6 +189,24 @@ int ref_run_world(const odegpuScene* sc, int w, int n_steps, double* state,
         set_limot(j, 0, jp, dJointSetUniversalParam);
         set_limot(j, 1, jp + 9, dJointSetUniversalParam);
         break;
+      case ODEGPU_JOINT_AMOTOR: {
+        j = dJointCreateAMotor(world, 0);
+        dJointAttach(j, B1, B2);
+        const int mode = (int)jp[1];
+        dJointSetAMotorMode(j, mode);
+        dJointSetAMotorNumAxes(j, (int)jp[0]);
+        const double* ax[3] = {a, x1, x2};
+        const int num = dJointGetAMotorNumAxes(j);
+        for (int k = 0; k < 3; ++k)
+          if (mode == dAMotorEuler ? k != 1 : k < num)
+            dJointSetAMotorAxis(j, k, (int)jp[2 + k], ax[k][0], ax[k][1], ax[k][2]);
+        set_limot(j, 0, jp + 5, dJointSetAMotorParam);
+        set_limot(j, 1, jp + 14, dJointSetAMotorParam);
+        set_limot(j, 2, jp + 23, dJointSetAMotorParam);
+        if (mode == dAMotorUser)
+          for (int k = 0; k < num; ++k) dJointSetAMotorAngle(j, k, jp[32 + k]);
+        break;
+      }
       case ODEGPU_JOINT_FIXED:
         j = dJointCreateFixed(world, 0);
         dJointAttach(j, B1, B2);
@@ -264,10 +282,12 @@ int ref_run_world(const odegpuScene* sc, int w, int n_steps, double* state,
           else if (t == ODEGPU_JOINT_HINGE2) setp = dJointSetHinge2Param;
           else if (t == ODEGPU_JOINT_SLIDER) setp = dJointSetSliderParam;
           else if (t == ODEGPU_JOINT_UNIVERSAL) setp = dJointSetUniversalParam;
+          else if (t == ODEGPU_JOINT_AMOTOR) setp = dJointSetAMotorParam;
           if (!setp) continue;
           const double v = sc->joint_stop[(size_t)cs * sc->joint_off[sc->n_worlds] + j0 + i];
           const double* jp = sc->joint_param + (size_t)(j0 + i) * ODEGPU_JOINT_NPARAM;
-          const double lo = std::isnan(v) ? jp[0] : v, hi = std::isnan(v) ? jp[1] : v;
+          const double* lp = t == ODEGPU_JOINT_AMOTOR ? jp + 5 : jp;
+          const double lo = std::isnan(v) ? lp[0] : v, hi = std::isnan(v) ? lp[1] : v;
           setp(joints[i], dParamLoStop, lo);
           setp(joints[i], dParamHiStop, hi);
         }
@@ -280,6 +300,7 @@ int ref_run_world(const odegpuScene* sc, int w, int n_steps, double* state,
           else if (jt == ODEGPU_JOINT_HINGE2) dJointAddHinge2Torques(joints[i], t[0], t[1]);
           else if (jt == ODEGPU_JOINT_SLIDER) dJointAddSliderForce(joints[i], t[0]);
           else if (jt == ODEGPU_JOINT_UNIVERSAL) dJointAddUniversalTorques(joints[i], t[0], t[1]);
+          else if (jt == ODEGPU_JOINT_AMOTOR) dJointAddAMotorTorques(joints[i], t[0], t[1], 0);
         }
       }
       if (sc->body_force) {

@@ -1,7 +1,8 @@
 /*
  * scene_player.c -- a plain ODE program that replays one world of an
  * odegpuScene (bodies, sphere / box / capsule / plane geoms, ball, hinge,
- * slider, universal, hinge2 and fixed joints, per-step controls) through ODE
+ * slider, universal, hinge2, fixed and angular motor joints, per-step
+ * controls) through ODE
  * 0.12's public C API only. Built against the reference (<ode/ode.h>,
  * -DdSINGLE, linked with the reference library) it runs ODE on the CPU; built
  * against include/ode_gpu.h and linked with libodegpu it runs the same calls
@@ -18,7 +19,7 @@
  *   nsurf lines:  mode mu mu2 bounce bounce_vel soft_erp soft_cfm motion1 motion2 motionN slip1 slip2
  *   nb lines:     px py pz qw qx qy qz vx vy vz wx wy wz mass I[9] flags
  *   ng lines:     type body surface p0 p1 p2 p3
- *   nj lines:     type b1 b2 anchor[3] axis1[3] axis2[3] param[20]
+ *   nj lines:     type b1 b2 anchor[3] axis1[3] axis2[3] param[36]
  *   nctrl blocks: nj lines "torque0 torque1 stop", then nb lines "force[3] torque[3]"
  * Output: one line per body after the last step: pos[3] q[4] lvel[3] avel[3].
  */
@@ -33,8 +34,8 @@
 #endif
 
 enum { SPHERE = 0, BOX = 1, CAPSULE = 2, PLANE = 4 };
-enum { BALL = 1, HINGE = 2, SLIDER = 3, UNIVERSAL = 5, HINGE2 = 6, FIXED = 7 };
-#define NPARAM 20
+enum { BALL = 1, HINGE = 2, SLIDER = 3, UNIVERSAL = 5, HINGE2 = 6, FIXED = 7, AMOTOR = 9 };
+#define NPARAM 36
 
 static int rd(FILE* f, double* v, int n) {
   for (int i = 0; i < n; ++i)
@@ -63,6 +64,7 @@ static setp_fn stop_setter(int type) {
     case HINGE2: return dJointSetHinge2Param;
     case SLIDER: return dJointSetSliderParam;
     case UNIVERSAL: return dJointSetUniversalParam;
+    case AMOTOR: return dJointSetAMotorParam;
     default: return 0;
   }
 }
@@ -184,6 +186,24 @@ int main(int argc, char** argv) {
         dJointSetHinge2Param(j, dParamSuspensionERP, jp[18]);
         dJointSetHinge2Param(j, dParamSuspensionCFM, jp[19]);
         break;
+      case AMOTOR: {
+        j = dJointCreateAMotor(world, 0);
+        dJointAttach(j, B1, B2);
+        const int mode = (int)jp[1];
+        dJointSetAMotorMode(j, mode);
+        dJointSetAMotorNumAxes(j, (int)jp[0]);
+        const double* ax[3] = {a, x1, x2};
+        const int num = dJointGetAMotorNumAxes(j);
+        for (int k = 0; k < 3; ++k)
+          if (mode == dAMotorEuler ? k != 1 : k < num)
+            dJointSetAMotorAxis(j, k, (int)jp[2 + k], ax[k][0], ax[k][1], ax[k][2]);
+        set_limot(j, 0, jp + 5, dJointSetAMotorParam);
+        set_limot(j, 1, jp + 14, dJointSetAMotorParam);
+        set_limot(j, 2, jp + 23, dJointSetAMotorParam);
+        if (mode == dAMotorUser)
+          for (int k = 0; k < num; ++k) dJointSetAMotorAngle(j, k, jp[32 + k]);
+        break;
+      }
       case FIXED:
         j = dJointCreateFixed(world, 0);
         dJointAttach(j, B1, B2);
@@ -242,8 +262,9 @@ int main(int argc, char** argv) {
         setp_fn setp = stop_setter(jtype[i]);
         if (!setp) continue;
         const double v = jc[3 * i + 2], *jp = jparam + NPARAM * i;
-        setp(joints[i], dParamLoStop, isnan(v) ? jp[0] : v);
-        setp(joints[i], dParamHiStop, isnan(v) ? jp[1] : v);
+        const double* lp = jtype[i] == AMOTOR ? jp + 5 : jp;
+        setp(joints[i], dParamLoStop, isnan(v) ? lp[0] : v);
+        setp(joints[i], dParamHiStop, isnan(v) ? lp[1] : v);
       }
       for (int i = 0; i < nj; ++i) {
         const double* t = jc + 3 * i;
@@ -252,6 +273,7 @@ int main(int argc, char** argv) {
           case HINGE2: dJointAddHinge2Torques(joints[i], t[0], t[1]); break;
           case SLIDER: dJointAddSliderForce(joints[i], t[0]); break;
           case UNIVERSAL: dJointAddUniversalTorques(joints[i], t[0], t[1]); break;
+          case AMOTOR: dJointAddAMotorTorques(joints[i], t[0], t[1], 0); break;
           default: break;
         }
       }

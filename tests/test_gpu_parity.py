@@ -136,7 +136,9 @@ def test_rows_and_lambda_tap(batch_cls, name):
         assert np.array_equal(Ri[:, 29], wb1), f"world {w}: b1"
         assert np.array_equal(Ri[:, 30], wb2), f"world {w}: b2"
         np.testing.assert_allclose(R[:, :12], t["J"][:M], rtol=1e-4, atol=2e-5)
-        np.testing.assert_allclose(R[:, 24], t["rhs"][:M], rtol=1e-3, atol=2e-3)
+        # rhs of a limit row is fps^2 * stop_erp * (angle - stop): 2000 x the
+        # FP32 error of an angle read through rotated axes (Euler angular motor)
+        np.testing.assert_allclose(R[:, 24], t["rhs"][:M], rtol=1e-3, atol=5e-3)
         np.testing.assert_allclose(R[:, 25], t["cfm"][:M], rtol=1e-5)
         # SOR output per body: cforce = invM J^T lambda (acceleration units; times
         # h it is the velocity change). 20 FP32 PGS iterations vs FP64.
