@@ -242,6 +242,17 @@ dGeomID dCreateSphere(dSpaceID space, dReal radius);                     /* :924
 dGeomID dCreateBox(dSpaceID space, dReal lx, dReal ly, dReal lz);        /* :1002 */
 dGeomID dCreatePlane(dSpaceID space, dReal a, dReal b, dReal c, dReal d); /* :1046 */
 dGeomID dCreateCapsule(dSpaceID space, dReal radius, dReal length);      /* :1051 */
+/* Rays: dCollide of a ray with a sphere, box, capsule, plane or heightfield
+ * returns at most one contact whose depth is the distance along the ray. */
+dGeomID dCreateRay(dSpaceID space, dReal length);                        /* :1067 */
+void dGeomRaySetLength(dGeomID ray, dReal length);                       /* :1068 */
+dReal dGeomRayGetLength(dGeomID ray);                                    /* :1069 */
+void dGeomRaySet(dGeomID ray, dReal px, dReal py, dReal pz, dReal dx, dReal dy, dReal dz);  /* :1070 */
+void dGeomRayGet(dGeomID ray, dVector3 start, dVector3 dir);             /* :1072 */
+void dGeomRaySetParams(dGeomID g, int FirstContact, int BackfaceCull);   /* :1079 */
+void dGeomRayGetParams(dGeomID g, int* FirstContact, int* BackfaceCull); /* :1080 */
+void dGeomRaySetClosestHit(dGeomID g, int closestHit);                   /* :1081 */
+int dGeomRayGetClosestHit(dGeomID g);                                    /* :1082 */
 /* Heightfields: the samples are copied when the data is built (ODE can keep
  * a reference to the caller's array when bCopyHeightData is 0). */
 typedef struct dxHeightfieldData* dHeightfieldDataID;                   /* collision.h:1101 */

@@ -195,6 +195,44 @@ int odegpuBatchSetStepIndex(odegpuBatchID b, int step);
  * world's rows start at row_off[w] (returned, [n_worlds]). */
 int odegpuBatchStepTap(odegpuBatchID b, float* rows, float* lambda, float* fc, int* row_off);
 
+/* Ray queries (ODE's ray geom, dRayClass). For each ray, dCollide(ray, g,
+ * flags) runs on the GPU against every geom g of the ray's world
+ * (ode/src/ray.cpp:196-498; a heightfield through its plane pass,
+ * ode/src/heightfield.cpp:1035-1040) and the contact of least depth (the
+ * distance along the ray) is kept, the lower geom index on ties: the nearest
+ * hit that dSpaceCollide2(ray, space, ...) with a nearest-contact callback
+ * finds (ode/src/collision_space.cpp; its bounding-box test only culls). A
+ * ray attached to a body (body >= 0, world-local) skips that body's geoms as
+ * dCollide does for two geoms on one body (ode/src/collision_kernel.cpp:296-303),
+ * and its start and direction are in the body frame, placed with the body's
+ * pose at the time of the query (a geom offset, dGeomSetOffsetPosition,
+ * include/ode/collision.h:545). The direction is normalised as dGeomRaySet
+ * does (ode/src/ray.cpp:115-136). flags: dCollide's, 1 to 8 contacts per
+ * geom. */
+typedef struct {
+  int world;           /* world index */
+  int body;            /* world-local body the ray is attached to, or -1 */
+  float start[3];      /* world frame, or body frame when attached */
+  float dir[3];        /* same frame as start */
+  float length;        /* dGeomRaySetLength */
+} odegpuRay;           /* 36 bytes */
+typedef struct {
+  int geom;            /* world-local geom index of the nearest hit; -1: no hit;
+                          -2: invalid ray (world / body out of range, length
+                          negative or not finite); -3: a heightfield zone under
+                          the ray exceeds the collider's buffers */
+  float pos[3];        /* dContactGeom pos, normal, depth of dCollide(ray, geom) */
+  float normal[3];
+  float depth;
+} odegpuRayHit;        /* 32 bytes */
+/* Host arrays; returns the number of rays that hit something, or an error
+ * (ODEGPU_E_ARG for an invalid ray). Runs after the batch's queued work. */
+int odegpuBatchRayCast(odegpuBatchID b, const odegpuRay* rays, int n, int flags, odegpuRayHit* hits);
+/* Device arrays, enqueued on the batch stream without synchronising (so it can
+ * sit between steps and inside a captured graph); invalid rays come back with
+ * geom = -2. */
+int odegpuBatchRayCastAsync(odegpuBatchID b, const odegpuRay* d_rays, int n, int flags, odegpuRayHit* d_hits);
+
 /* Contacts generated by the last step of world w (up to cap records of
  * pos[3] normal[3] depth b1 b2 as floats); returns the count or an error. */
 int odegpuBatchGetContacts(odegpuBatchID b, int w, float* out, int cap);

@@ -31,6 +31,8 @@ enum {
   ODEGPU_GEOM_BOX = 1,
   ODEGPU_GEOM_CAPSULE = 2,
   ODEGPU_GEOM_PLANE = 4,
+  ODEGPU_GEOM_RAY = 5,          /* queries only (dCollide, odegpuBatchRayCast);
+                                   a scene may not hold one */
   ODEGPU_GEOM_HEIGHTFIELD = 9
 };
 

@@ -18,10 +18,10 @@ struct GeomView {
   int type;
   float pos[3];
   float R[12];
-  float p[4];   // sphere r / box sides / capsule r,len / plane a,b,c,d
+  float p[4];   // sphere r / box sides / capsule r,len / plane a,b,c,d / ray length
 };
 
-enum { G_SPHERE = 0, G_BOX = 1, G_CAPSULE = 2, G_PLANE = 4, G_HEIGHTFIELD = 9 };
+enum { G_SPHERE = 0, G_BOX = 1, G_CAPSULE = 2, G_PLANE = 4, G_RAY = 5, G_HEIGHTFIELD = 9 };
 constexpr unsigned kContactsUnimportant = 0x80000000u;
 
 // dCollideSpheres (ode/src/collision_util.cpp:38-67)
@@ -712,10 +712,166 @@ OG_HD int collide_capsule_capsule(const GeomView& g1, const GeomView& g2, unsign
   return collide_spheres(sphere1, g1.p[0], sphere2, g2.p[0], c);
 }
 
+// ---- rays (ode/src/ray.cpp). A ray geom holds its length in p[0], starts at
+// pos and points along column 2 of R. Each collider returns at most one
+// contact; its depth is the distance from the start along the ray.
+
+// ray_sphere_helper (ray.cpp:196-233); mode 1 takes the exit point.
+OG_HD int ray_sphere_helper(const GeomView& ray, const float* spos, float radius, Contact* c, int mode) {
+  const float* rp = ray.pos;
+  const float* R = ray.R;
+  const float q[3] = {rp[0] - spos[0], rp[1] - spos[1], rp[2] - spos[2]};
+  const float B = q[0] * R[2] + q[1] * R[6] + q[2] * R[10];
+  const float C = dot3(q, q) - radius * radius;
+  float k = B * B - C;
+  if (k < 0.f) return 0;
+  k = sqrtf(k);
+  float alpha;
+  if (mode && C >= 0.f) {
+    alpha = -B + k;
+    if (alpha < 0.f) return 0;
+  } else {
+    alpha = -B - k;
+    if (alpha < 0.f) {
+      alpha = -B + k;
+      if (alpha < 0.f) return 0;
+    }
+  }
+  if (alpha > ray.p[0]) return 0;
+  for (int i = 0; i < 3; ++i) c->pos[i] = rp[i] + alpha * R[i * 4 + 2];
+  const float nsign = (C < 0.f || mode) ? -1.f : 1.f;
+  for (int i = 0; i < 3; ++i) c->normal[i] = nsign * (c->pos[i] - spos[i]);
+  safe_normalize3(c->normal);
+  c->depth = alpha;
+  return 1;
+}
+
+// dCollideRayBox (ray.cpp:253-350): slab test in the box frame, the ray
+// mirrored so that its direction has no negative component.
+OG_HD int collide_ray_box(const GeomView& ray, const GeomView& bx, Contact* c) {
+  const float* rp = ray.pos;
+  const float* RR = ray.R;
+  const float* BR = bx.R;
+  float tmp[3] = {rp[0] - bx.pos[0], rp[1] - bx.pos[1], rp[2] - bx.pos[2]};
+  float s[3], v[3], sign[3];
+  mul1_331(s, BR, tmp);
+  tmp[0] = RR[2]; tmp[1] = RR[6]; tmp[2] = RR[10];
+  mul1_331(v, BR, tmp);
+  for (int i = 0; i < 3; ++i) {
+    if (v[i] < 0.f) { s[i] = -s[i]; v[i] = -v[i]; sign[i] = 1.f; }
+    else sign[i] = -1.f;
+  }
+  const float h[3] = {0.5f * bx.p[0], 0.5f * bx.p[1], 0.5f * bx.p[2]};
+  if ((s[0] < -h[0] && v[0] <= 0.f) || s[0] > h[0] || (s[1] < -h[1] && v[1] <= 0.f) || s[1] > h[1] ||
+      (s[2] < -h[2] && v[2] <= 0.f) || s[2] > h[2] || (v[0] == 0.f && v[1] == 0.f && v[2] == 0.f))
+    return 0;
+  float lo = -INFINITY, hi = INFINITY;
+  int nlo = 0, nhi = 0;
+  for (int i = 0; i < 3; ++i) {
+    if (v[i] != 0.f) {
+      float k = (-h[i] - s[i]) / v[i];
+      if (k > lo) { lo = k; nlo = i; }
+      k = (h[i] - s[i]) / v[i];
+      if (k < hi) { hi = k; nhi = i; }
+    }
+  }
+  if (lo > hi) return 0;
+  const bool front = lo >= 0.f;
+  const float alpha = front ? lo : hi;
+  const int n = front ? nlo : nhi;
+  if (alpha < 0.f || alpha > ray.p[0]) return 0;
+  for (int i = 0; i < 3; ++i) {
+    c->pos[i] = rp[i] + alpha * RR[i * 4 + 2];
+    c->normal[i] = BR[i * 4 + n] * sign[n];
+  }
+  c->depth = alpha;
+  return 1;
+}
+
+// dCollideRayCapsule (ray.cpp:352-465): the infinite cylinder first, then the
+// cap sphere on the side where the hit (or the start) lies.
+OG_HD int collide_ray_capsule(const GeomView& ray, const GeomView& cp, Contact* c) {
+  const float* rp = ray.pos;
+  const float* RR = ray.R;
+  const float* CR = cp.R;
+  const float* cpos = cp.pos;
+  const float radius = cp.p[0];
+  const float lz2 = cp.p[1] * 0.5f;
+  const float cs[3] = {rp[0] - cpos[0], rp[1] - cpos[1], rp[2] - cpos[2]};
+  float k = CR[2] * cs[0] + CR[6] * cs[1] + CR[10] * cs[2];
+  float q[3], r[3];
+  for (int i = 0; i < 3; ++i) q[i] = k * CR[i * 4 + 2] - cs[i];
+  const float C = dot3(q, q) - radius * radius;
+  int inside = 0;
+  if (C < 0.f) {
+    if (k < -lz2) k = -lz2;
+    else if (k > lz2) k = lz2;
+    for (int i = 0; i < 3; ++i) r[i] = cpos[i] + k * CR[i * 4 + 2];
+    if ((rp[0] - r[0]) * (rp[0] - r[0]) + (rp[1] - r[1]) * (rp[1] - r[1]) + (rp[2] - r[2]) * (rp[2] - r[2]) <
+        radius * radius)
+      inside = 1;
+  }
+  if (!inside && C < 0.f) {
+    k = (k < 0.f) ? -lz2 : lz2;
+  } else {
+    const float uv = CR[2] * RR[2] + CR[6] * RR[6] + CR[10] * RR[10];
+    for (int i = 0; i < 3; ++i) r[i] = uv * CR[i * 4 + 2] - RR[i * 4 + 2];
+    float A = dot3(r, r);
+    const float B = 2.f * dot3(q, r);
+    k = B * B - 4.f * A * C;
+    if (k < 0.f) {
+      if (!inside) return 0;
+      k = (uv < 0.f) ? -lz2 : lz2;
+    } else {
+      k = sqrtf(k);
+      A = 1.0f / (2.f * A);
+      float alpha = (-B - k) * A;
+      if (alpha < 0.f) {
+        alpha = (-B + k) * A;
+        if (alpha < 0.f) return 0;
+      }
+      if (alpha > ray.p[0]) return 0;
+      for (int i = 0; i < 3; ++i) c->pos[i] = rp[i] + alpha * RR[i * 4 + 2];
+      for (int i = 0; i < 3; ++i) q[i] = c->pos[i] - cpos[i];
+      k = q[0] * CR[2] + q[1] * CR[6] + q[2] * CR[10];
+      const float nsign = inside ? -1.f : 1.f;
+      if (k >= -lz2 && k <= lz2) {
+        for (int i = 0; i < 3; ++i) c->normal[i] = nsign * (c->pos[i] - (cpos[i] + k * CR[i * 4 + 2]));
+        safe_normalize3(c->normal);
+        c->depth = alpha;
+        return 1;
+      }
+      k = (k < 0.f) ? -lz2 : lz2;
+    }
+  }
+  for (int i = 0; i < 3; ++i) q[i] = cpos[i] + k * CR[i * 4 + 2];
+  return ray_sphere_helper(ray, q, radius, c, inside);
+}
+
+// dCollideRayPlane (ray.cpp:467-498)
+OG_HD int collide_ray_plane(const GeomView& ray, const GeomView& pl, Contact* c) {
+  const float* rp = ray.pos;
+  const float* RR = ray.R;
+  const float* P = pl.p;
+  float alpha = P[3] - (P[0] * rp[0] + P[1] * rp[1] + P[2] * rp[2]);
+  const float nsign = (alpha > 0.f) ? -1.f : 1.f;
+  const float k = P[0] * RR[2] + P[1] * RR[6] + P[2] * RR[10];
+  if (k == 0.f) return 0;
+  alpha /= k;
+  if (alpha < 0.f || alpha > ray.p[0]) return 0;
+  for (int i = 0; i < 3; ++i) {
+    c->pos[i] = rp[i] + alpha * RR[i * 4 + 2];
+    c->normal[i] = nsign * P[i];
+  }
+  c->depth = alpha;
+  return 1;
+}
+
 // Collider table for this path (ode/src/collision_kernel.cpp:167-268): returns
 // a collider id and whether the call runs with the geoms swapped (in which case
 // dCollide negates the normals, :319-335).
-enum { CL_NONE = 0, CL_SS, CL_SB, CL_SP, CL_BB, CL_BP, CL_CP, CL_HF, CL_CS, CL_CB, CL_CC };
+enum { CL_NONE = 0, CL_SS, CL_SB, CL_SP, CL_BB, CL_BP, CL_CP, CL_HF, CL_CS, CL_CB, CL_CC,
+       CL_RS, CL_RB, CL_RC, CL_RP };
 OG_HD int collider_of(int t1, int t2, int* reverse) {
   *reverse = 0;
   auto is = [&](int a, int b) { return t1 == a && t2 == b; };
@@ -734,8 +890,17 @@ OG_HD int collider_of(int t1, int t2, int* reverse) {
   if (is(G_CAPSULE, G_CAPSULE)) return CL_CC;
   if (is(G_CAPSULE, G_PLANE)) return CL_CP;
   if (is(G_PLANE, G_CAPSULE)) { *reverse = 1; return CL_CP; }
-  if (t1 == G_HEIGHTFIELD && (t2 == G_SPHERE || t2 == G_BOX || t2 == G_CAPSULE)) return CL_HF;
-  if (t2 == G_HEIGHTFIELD && (t1 == G_SPHERE || t1 == G_BOX || t1 == G_CAPSULE)) { *reverse = 1; return CL_HF; }
+  if (is(G_RAY, G_SPHERE)) return CL_RS;
+  if (is(G_SPHERE, G_RAY)) { *reverse = 1; return CL_RS; }
+  if (is(G_RAY, G_BOX)) return CL_RB;
+  if (is(G_BOX, G_RAY)) { *reverse = 1; return CL_RB; }
+  if (is(G_RAY, G_CAPSULE)) return CL_RC;
+  if (is(G_CAPSULE, G_RAY)) { *reverse = 1; return CL_RC; }
+  if (is(G_RAY, G_PLANE)) return CL_RP;
+  if (is(G_PLANE, G_RAY)) { *reverse = 1; return CL_RP; }
+  auto hf_other = [](int t) { return t == G_SPHERE || t == G_BOX || t == G_CAPSULE || t == G_RAY; };
+  if (t1 == G_HEIGHTFIELD && hf_other(t2)) return CL_HF;
+  if (t2 == G_HEIGHTFIELD && hf_other(t1)) { *reverse = 1; return CL_HF; }
   return CL_NONE;
 }
 
@@ -759,6 +924,10 @@ OG_HD int collide_primitive(const GeomView& g1, const GeomView& g2, unsigned fla
     case CL_CS: n = collide_capsule_sphere(a, b, c); break;
     case CL_CB: n = collide_capsule_box(a, b, c); break;
     case CL_CC: n = collide_capsule_capsule(a, b, flags, c); break;
+    case CL_RS: n = ray_sphere_helper(a, b.pos, b.p[0], c, 0); break;
+    case CL_RB: n = collide_ray_box(a, b, c); break;
+    case CL_RC: n = collide_ray_capsule(a, b, c); break;
+    case CL_RP: n = collide_ray_plane(a, b, c); break;
     default: n = 0;
   }
   if (rev)

@@ -12,6 +12,7 @@
 #include "odegpu.h"
 #include "engine_types.cuh"
 #include "world_solve.cuh"
+#include "raycast.cuh"
 #include "adjoint.cuh"
 #include "large_world.cuh"
 #include "engine_internal.hpp"
@@ -186,6 +187,8 @@ struct odegpuBatch {
   DBuf<float> rows;
   DBuf<int> jlist, adj, adj_start, island_jstart, island_rstart, jrow, jm;
   DBuf<float> state_scratch;
+  DBuf<odegpuRay> ray_in;          // odegpuBatchRayCast staging, grown on demand
+  DBuf<odegpuRayHit> ray_out;
 
   BatchDev dev() const {
     BatchDev d;
@@ -715,6 +718,9 @@ int odegpuBatchCreate(const odegpuScene* sc, const odegpuBatchConfig* cfg, odegp
         delete B;
         return fail(ODEGPU_E_ARG, "heightfield geom: bad heightfield index or attached to a body");
       }
+    } else if (gtype[g] == ODEGPU_GEOM_RAY) {
+      delete B;
+      return fail(ODEGPU_E_ARG, "a scene may not hold a ray geom: rays are queries (odegpuBatchRayCast)");
     } else if (gtype[g] != ODEGPU_GEOM_SPHERE && gtype[g] != ODEGPU_GEOM_BOX &&
                gtype[g] != ODEGPU_GEOM_CAPSULE) {
       delete B;
@@ -1393,6 +1399,47 @@ int odegpuBatchInfo(odegpuBatchID b, int* n_worlds, int* nb_total, int* nj_total
 }
 
 void* odegpuBatchStream(odegpuBatchID b) { return b ? (void*)b->stream : nullptr; }
+
+int odegpuBatchRayCastAsync(odegpuBatchID b, const odegpuRay* d_rays, int n, int flags, odegpuRayHit* d_hits) {
+  if (!b || n < 0 || (n > 0 && (!d_rays || !d_hits))) return fail(ODEGPU_E_ARG, "bad arguments");
+  const int maxc = flags & 0xffff;
+  if (maxc < 1 || maxc > 8) return fail(ODEGPU_E_ARG, "ray casts take 1 to 8 contacts per geom");
+  if (n == 0) return 0;
+  OG_CUDA(cudaSetDevice(b->device));
+  constexpr int kThreads = 128;   // 4 rays per block, one warp each
+  const long long blocks = ((long long)n * 32 + kThreads - 1) / kThreads;
+  raycast_kernel<<<(unsigned)blocks, kThreads, 0, b->stream>>>(b->dev(), d_rays, n, (unsigned)flags, d_hits);
+  b->launches += 1;
+  OG_CUDA(cudaGetLastError());
+  return 0;
+}
+
+int odegpuBatchRayCast(odegpuBatchID b, const odegpuRay* rays, int n, int flags, odegpuRayHit* hits) {
+  if (!b || n < 0 || (n > 0 && (!rays || !hits))) return fail(ODEGPU_E_ARG, "bad arguments");
+  for (int i = 0; i < n; ++i) {
+    const odegpuRay& r = rays[i];
+    if (r.world < 0 || r.world >= b->n_worlds) return fail(ODEGPU_E_ARG, "ray " + std::to_string(i) + ": bad world");
+    if (r.body >= b->h_world[r.world].nb) return fail(ODEGPU_E_ARG, "ray " + std::to_string(i) + ": bad body");
+    if (!std::isfinite(r.length) || r.length < 0)
+      return fail(ODEGPU_E_ARG, "ray " + std::to_string(i) + ": length must be finite and >= 0");
+  }
+  if (n == 0) return 0;
+  OG_CUDA(cudaSetDevice(b->device));
+  if (b->ray_in.n < (size_t)n) {
+    cudaFree(b->ray_in.p); b->ray_in.p = nullptr;
+    cudaFree(b->ray_out.p); b->ray_out.p = nullptr;
+    if (int rc = b->ray_in.alloc(n)) return rc;
+    if (int rc = b->ray_out.alloc(n)) return rc;
+  }
+  OG_CUDA(cudaMemcpyAsync(b->ray_in.p, rays, (size_t)n * sizeof(odegpuRay), cudaMemcpyHostToDevice, b->stream));
+  if (int rc = odegpuBatchRayCastAsync(b, b->ray_in.p, n, flags, b->ray_out.p)) return rc;
+  OG_CUDA(cudaMemcpyAsync(hits, b->ray_out.p, (size_t)n * sizeof(odegpuRayHit), cudaMemcpyDeviceToHost,
+                          b->stream));
+  OG_CUDA(cudaStreamSynchronize(b->stream));
+  int nhit = 0;
+  for (int i = 0; i < n; ++i) nhit += hits[i].geom >= 0;
+  return nhit;
+}
 
 int odegpuBatchLargeWorldStats(odegpuBatchID b, long long* out, int n, int reset) {
   if (!b || !out || n < 0) return fail(ODEGPU_E_ARG, "bad arguments");

@@ -67,11 +67,19 @@ OG_D bool hf_on_triangle(const DevHeightfield& H, const float* corner, int cx, i
   return (maxz - pos[2]) <= (pos[0] - minx) * H.zx;
 }
 
-// computeAABB of sphere / box / capsule (sphere.cpp:59-67, box.cpp:60-78,
-// capsule.cpp:60-74)
+// computeAABB of sphere / box / capsule / ray (sphere.cpp:59-67,
+// box.cpp:60-78, capsule.cpp:60-74, ray.cpp:56-89)
 OG_D void geom_aabb(const GeomView& g, float* aabb) {
   const float* R = g.R;
   float xr, yr, zr;
+  if (g.type == G_RAY) {
+    for (int i = 0; i < 3; ++i) {
+      const float e = g.pos[i] + R[i * 4 + 2] * g.p[0];
+      aabb[2 * i] = g.pos[i] < e ? g.pos[i] : e;
+      aabb[2 * i + 1] = g.pos[i] < e ? e : g.pos[i];
+    }
+    return;
+  }
   if (g.type == G_SPHERE) {
     xr = yr = zr = g.p[0];
   } else if (g.type == G_BOX) {
@@ -134,6 +142,7 @@ OG_D float geom_point_depth(const GeomView& g, const float* v) {
 OG_D int geom_plane_collide(const GeomView& g, const GeomView& pl, unsigned flags, Contact* c) {
   if (g.type == G_SPHERE) return collide_sphere_plane(g, pl, c);
   if (g.type == G_BOX) return collide_box_plane(g, pl, flags, c);
+  if (g.type == G_RAY) return collide_ray_plane(g, pl, c);
   return collide_capsule_plane(g, pl, flags, c);
 }
 
@@ -165,7 +174,7 @@ OG_D int hf_zone(const DevHeightfield& H, const float* heights, int minX, int ma
     return 1;
   }
   bool further = false;
-  {
+  if (g.type != G_RAY) {   // rays take the plane pass only
     const float xratio = (aabb[1] - aabb[0]) * H.inv_sw;
     if (xratio > 1.5f) further = true;
     else if ((aabb[5] - aabb[4]) * H.inv_sd > 1.5f) further = true;

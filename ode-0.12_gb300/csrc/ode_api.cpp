@@ -70,7 +70,13 @@ struct dxGeom {
   dReal pos[4], R[12];       // own placement when not attached to a body
   dxHeightfieldData* hf;     // heightfield geoms: their data
   int placeable;             // heightfield geoms: created placeable
+  int ray_flags;             // ray geoms: kRay* below
 };
+
+// dxGeom::gflags bits of a ray (ode/src/collision_kernel.h: RAY_FIRSTCONTACT,
+// RAY_BACKFACECULL, RAY_CLOSEST_HIT). They steer the trimesh collider only, so
+// the colliders on this path ignore them; the setters keep them for the getters.
+constexpr int kRayFirstContact = 1, kRayBackfaceCull = 2, kRayClosestHit = 4;
 
 struct dxWorld {
   double gravity[3] = {0, 0, 0};
@@ -873,6 +879,50 @@ dGeomID dCreatePlane(dSpaceID, dReal a, dReal b, dReal c, dReal d) {
 }
 void dGeomDestroy(dGeomID g) { delete g; }
 
+// Rays (ode/src/ray.cpp:49-194): the length is the class parameter; the start
+// is the geom's position and the direction column 2 of its rotation, so a ray
+// attached to a body follows that body.
+dGeomID dCreateRay(dSpaceID, dReal length) {
+  const double p[4] = {length, 0, 0, 0};
+  return new_geom(dRayClass, p);
+}
+void dGeomRaySetLength(dGeomID g, dReal length) {
+  if (g && g->type == dRayClass) g->p[0] = length;
+}
+dReal dGeomRayGetLength(dGeomID g) { return (g && g->type == dRayClass) ? (dReal)g->p[0] : 0; }
+void dGeomRaySet(dGeomID g, dReal px, dReal py, dReal pz, dReal dx, dReal dy, dReal dz) {
+  // writes the placement the ray reads: a body's own when attached
+  // (final_posr is the body's, ray.cpp:115-136), with the direction normalised
+  if (!g || g->type != dRayClass) return;
+  double n[3] = {dx, dy, dz};
+  og_host::safe_normalize3(n);
+  dReal* pos = g->body ? g->body->pos : g->pos;
+  dReal* R = g->body ? g->body->R : g->R;
+  pos[0] = px; pos[1] = py; pos[2] = pz;
+  R[2] = (dReal)n[0]; R[6] = (dReal)n[1]; R[10] = (dReal)n[2];
+}
+void dGeomRayGet(dGeomID g, dVector3 start, dVector3 dir) {
+  if (!g || g->type != dRayClass) return;
+  const dReal* pos = dGeomGetPosition(g);
+  const dReal* R = dGeomGetRotation(g);
+  for (int k = 0; k < 3; ++k) { start[k] = pos[k]; dir[k] = R[k * 4 + 2]; }
+}
+void dGeomRaySetParams(dGeomID g, int FirstContact, int BackfaceCull) {
+  if (!g || g->type != dRayClass) return;
+  g->ray_flags = (g->ray_flags & kRayClosestHit) | (FirstContact ? kRayFirstContact : 0) |
+                 (BackfaceCull ? kRayBackfaceCull : 0);
+}
+void dGeomRayGetParams(dGeomID g, int* FirstContact, int* BackfaceCull) {
+  if (!g || g->type != dRayClass) return;
+  *FirstContact = (g->ray_flags & kRayFirstContact) != 0;
+  *BackfaceCull = (g->ray_flags & kRayBackfaceCull) != 0;
+}
+void dGeomRaySetClosestHit(dGeomID g, int closestHit) {
+  if (!g || g->type != dRayClass) return;
+  g->ray_flags = closestHit ? (g->ray_flags | kRayClosestHit) : (g->ray_flags & ~kRayClosestHit);
+}
+int dGeomRayGetClosestHit(dGeomID g) { return (g && g->type == dRayClass && (g->ray_flags & kRayClosestHit)) ? 1 : 0; }
+
 // Heightfields (ode/src/heightfield.cpp:107-143, :1860-2000): the samples are
 // copied at build time whatever bCopyHeightData says, and uploaded to the GPU.
 dHeightfieldDataID dGeomHeightfieldDataCreate(void) { return new dxHeightfieldData(); }
@@ -941,7 +991,9 @@ int dCollide(dGeomID o1, dGeomID o2, int flags, dContactGeom* contact, int skip)
     const bool rev = o2->type == dHeightfieldClass;
     const dxGeom* hg = rev ? o2 : o1;
     const dxGeom* og2 = rev ? o1 : o2;
-    if (og2->type != dSphereClass && og2->type != dBoxClass && og2->type != dCapsuleClass) return 0;
+    if (og2->type != dSphereClass && og2->type != dBoxClass && og2->type != dCapsuleClass &&
+        og2->type != dRayClass)
+      return 0;
     if (!hg->hf || !hg->hf->built) return 0;
     double hpos[3] = {0, 0, 0}, hR[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
     if (hg->placeable) {

@@ -67,6 +67,8 @@ def _declare(L):
         "odegpuBatchStepTap": (i, [v, _P(f), _P(f), _P(f), _P(i)]),
         "odegpuBatchGetContacts": (i, [v, i, _P(f), i]),
         "odegpuBatchLargeWorldStats": (i, [v, _P(C.c_longlong), i, i]),
+        "odegpuBatchRayCast": (i, [v, v, i, i, v]),
+        "odegpuBatchRayCastAsync": (i, [v, v, i, i, v]),
         "odegpuGetLastError": (C.c_char_p, []),
     }
     for name, (res, args) in sig.items():

@@ -10,6 +10,13 @@ from ._lib import lib, check
 _P = C.POINTER
 BODY_REC = 13
 
+# odegpuRay / odegpuRayHit (include/odegpu.h)
+RAY_DTYPE = np.dtype([("world", np.int32), ("body", np.int32), ("start", np.float32, 3),
+                      ("dir", np.float32, 3), ("length", np.float32)])
+HIT_DTYPE = np.dtype([("geom", np.int32), ("pos", np.float32, 3), ("normal", np.float32, 3),
+                      ("depth", np.float32)])
+assert RAY_DTYPE.itemsize == 36 and HIT_DTYPE.itemsize == 32
+
 
 class BatchConfig(C.Structure):
     _fields_ = [("contacts_per_body", C.c_int), ("warps_per_block", C.c_int),
@@ -62,6 +69,23 @@ class Batch:
         return dict(walk_ms=v[0] / 1e6, sweep_first_ms=v[1] / 1e6, sort_ms=v[2] / 1e6,
                     sweep_rest_ms=v[3] / 1e6, levels_max=v[4], sweeps=v[5], walks=v[6],
                     walk_copy_ms=v[7] / 1e6, cluster=v[8])
+
+    def ray_cast(self, rays, flags=1):
+        """Nearest hit of each ray among its world's geoms (odegpuBatchRayCast).
+        rays: a RAY_DTYPE array (world, body, start[3], dir[3], length; body -1
+        for a world-frame ray, else the world-local body it is attached to, with
+        start / dir in that body's frame). Returns a HIT_DTYPE array (geom,
+        pos[3], normal[3], depth; geom -1 where nothing is hit)."""
+        r = np.ascontiguousarray(rays, dtype=RAY_DTYPE)
+        hits = np.zeros(len(r), dtype=HIT_DTYPE)
+        rc = lib().odegpuBatchRayCast(self.h, r.ctypes.data, len(r), int(flags), hits.ctypes.data)
+        check(rc)
+        return hits
+
+    def ray_cast_async(self, d_rays, n, d_hits, flags=1):
+        """odegpuBatchRayCastAsync on device pointers (e.g. torch tensors'
+        data_ptr()), enqueued on the batch stream."""
+        check(lib().odegpuBatchRayCastAsync(self.h, int(d_rays), int(n), int(flags), int(d_hits)))
 
     def sync(self):
         check(lib().odegpuBatchSynchronize(self.h))

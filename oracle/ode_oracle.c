@@ -1289,10 +1289,172 @@ static int collide_capsule_capsule(const GeomRef* g1, const GeomRef* g2, unsigne
   return collide_spheres(sphere1, g1->p[0], sphere2, g2->p[0], c);
 }
 
+/* ---- rays (ode/src/ray.cpp). A ray geom holds its length in p[0]; it starts
+ * at pos and points along column 2 of R (dGeomRaySet, ray.cpp:115-136). Each
+ * ray collider returns at most one contact whose depth is the distance from
+ * the ray's start along the ray. */
+
+/* ray_sphere_helper, ray.cpp:196-233: mode 1 takes the exit point. */
+static int ray_sphere_helper(const GeomRef* ray, const real* spos, real radius, OContact* c, int mode) {
+  const real* rp = ray->pos;
+  const real* R = ray->R;
+  const real q[3] = {rp[0] - spos[0], rp[1] - spos[1], rp[2] - spos[2]};
+  const real B = q[0] * R[2] + q[1] * R[6] + q[2] * R[10];
+  const real C = dot3(q, q) - radius * radius;
+  real k = B * B - C;
+  if (k < 0) return 0;
+  k = sqrt(k);
+  real alpha;
+  if (mode && C >= 0) {
+    alpha = -B + k;
+    if (alpha < 0) return 0;
+  } else {
+    alpha = -B - k;
+    if (alpha < 0) {
+      alpha = -B + k;
+      if (alpha < 0) return 0;
+    }
+  }
+  if (alpha > ray->p[0]) return 0;
+  for (int i = 0; i < 3; ++i) c->pos[i] = rp[i] + alpha * R[i * 4 + 2];
+  const real nsign = (C < 0 || mode) ? -1.0 : 1.0;
+  for (int i = 0; i < 3; ++i) c->normal[i] = nsign * (c->pos[i] - spos[i]);
+  safe_normalize3(c->normal);
+  c->depth = alpha;
+  return 1;
+}
+
+/* dCollideRaySphere, ray.cpp:235-251 */
+static int collide_ray_sphere(const GeomRef* ray, const GeomRef* s, OContact* c) {
+  return ray_sphere_helper(ray, s->pos, s->p[0], c, 0);
+}
+
+/* dCollideRayBox, ray.cpp:253-350: slab test in the box frame with the ray
+ * mirrored so that its direction has no negative component. */
+static int collide_ray_box(const GeomRef* ray, const GeomRef* bx, OContact* c) {
+  const real* rp = ray->pos;
+  const real* RR = ray->R;
+  const real* BR = bx->R;
+  real tmp[3] = {rp[0] - bx->pos[0], rp[1] - bx->pos[1], rp[2] - bx->pos[2]};
+  real s[3], v[3], sign[3];
+  mul1_331(s, BR, tmp);
+  tmp[0] = RR[2]; tmp[1] = RR[6]; tmp[2] = RR[10];
+  mul1_331(v, BR, tmp);
+  for (int i = 0; i < 3; ++i) {
+    if (v[i] < 0) { s[i] = -s[i]; v[i] = -v[i]; sign[i] = 1; }
+    else sign[i] = -1;
+  }
+  const real h[3] = {0.5 * bx->p[0], 0.5 * bx->p[1], 0.5 * bx->p[2]};
+  if ((s[0] < -h[0] && v[0] <= 0) || s[0] > h[0] || (s[1] < -h[1] && v[1] <= 0) || s[1] > h[1] ||
+      (s[2] < -h[2] && v[2] <= 0) || s[2] > h[2] || (v[0] == 0 && v[1] == 0 && v[2] == 0))
+    return 0;
+  real lo = -INFINITY, hi = INFINITY;
+  int nlo = 0, nhi = 0;
+  for (int i = 0; i < 3; ++i) {
+    if (v[i] != 0) {
+      real k = (-h[i] - s[i]) / v[i];
+      if (k > lo) { lo = k; nlo = i; }
+      k = (h[i] - s[i]) / v[i];
+      if (k < hi) { hi = k; nhi = i; }
+    }
+  }
+  if (lo > hi) return 0;
+  real alpha;
+  int n;
+  if (lo >= 0) { alpha = lo; n = nlo; }
+  else { alpha = hi; n = nhi; }
+  if (alpha < 0 || alpha > ray->p[0]) return 0;
+  for (int i = 0; i < 3; ++i) {
+    c->pos[i] = rp[i] + alpha * RR[i * 4 + 2];
+    c->normal[i] = BR[i * 4 + n] * sign[n];
+  }
+  c->depth = alpha;
+  return 1;
+}
+
+/* dCollideRayCapsule, ray.cpp:352-465: the infinite cylinder first, then the
+ * cap sphere on the side the hit (or the start) lies. */
+static int collide_ray_capsule(const GeomRef* ray, const GeomRef* cp, OContact* c) {
+  const real* rp = ray->pos;
+  const real* RR = ray->R;
+  const real* CR = cp->R;
+  const real* cpos = cp->pos;
+  const real radius = cp->p[0];
+  const real lz2 = cp->p[1] * 0.5;
+  const real cs[3] = {rp[0] - cpos[0], rp[1] - cpos[1], rp[2] - cpos[2]};
+  real k = CR[2] * cs[0] + CR[6] * cs[1] + CR[10] * cs[2];
+  real q[3], r[3];
+  for (int i = 0; i < 3; ++i) q[i] = k * CR[i * 4 + 2] - cs[i];
+  real C = dot3(q, q) - radius * radius;
+  int inside = 0;
+  if (C < 0) {
+    if (k < -lz2) k = -lz2;
+    else if (k > lz2) k = lz2;
+    for (int i = 0; i < 3; ++i) r[i] = cpos[i] + k * CR[i * 4 + 2];
+    if ((rp[0] - r[0]) * (rp[0] - r[0]) + (rp[1] - r[1]) * (rp[1] - r[1]) + (rp[2] - r[2]) * (rp[2] - r[2]) <
+        radius * radius)
+      inside = 1;
+  }
+  if (!inside && C < 0) {
+    k = (k < 0) ? -lz2 : lz2;
+  } else {
+    const real uv = CR[2] * RR[2] + CR[6] * RR[6] + CR[10] * RR[10];
+    for (int i = 0; i < 3; ++i) r[i] = uv * CR[i * 4 + 2] - RR[i * 4 + 2];
+    real A = dot3(r, r);
+    const real B = 2 * dot3(q, r);
+    k = B * B - 4 * A * C;
+    if (k < 0) {
+      if (!inside) return 0;
+      k = (uv < 0) ? -lz2 : lz2;
+    } else {
+      k = sqrt(k);
+      A = 1.0 / (2 * A);
+      real alpha = (-B - k) * A;
+      if (alpha < 0) {
+        alpha = (-B + k) * A;
+        if (alpha < 0) return 0;
+      }
+      if (alpha > ray->p[0]) return 0;
+      for (int i = 0; i < 3; ++i) c->pos[i] = rp[i] + alpha * RR[i * 4 + 2];
+      for (int i = 0; i < 3; ++i) q[i] = c->pos[i] - cpos[i];
+      k = q[0] * CR[2] + q[1] * CR[6] + q[2] * CR[10];
+      const real nsign = inside ? -1.0 : 1.0;
+      if (k >= -lz2 && k <= lz2) {
+        for (int i = 0; i < 3; ++i) c->normal[i] = nsign * (c->pos[i] - (cpos[i] + k * CR[i * 4 + 2]));
+        safe_normalize3(c->normal);
+        c->depth = alpha;
+        return 1;
+      }
+      k = (k < 0) ? -lz2 : lz2;
+    }
+  }
+  for (int i = 0; i < 3; ++i) q[i] = cpos[i] + k * CR[i * 4 + 2];
+  return ray_sphere_helper(ray, q, radius, c, inside);
+}
+
+/* dCollideRayPlane, ray.cpp:467-498 */
+static int collide_ray_plane(const GeomRef* ray, const GeomRef* pl, OContact* c) {
+  const real* rp = ray->pos;
+  const real* RR = ray->R;
+  const real* P = pl->p;
+  real alpha = P[3] - dot3(P, rp);
+  const real nsign = (alpha > 0) ? -1.0 : 1.0;
+  const real k = P[0] * RR[2] + P[1] * RR[6] + P[2] * RR[10];
+  if (k == 0) return 0;
+  alpha /= k;
+  if (alpha < 0 || alpha > ray->p[0]) return 0;
+  for (int i = 0; i < 3; ++i) {
+    c->pos[i] = rp[i] + alpha * RR[i * 4 + 2];
+    c->normal[i] = nsign * P[i];
+  }
+  c->depth = alpha;
+  return 1;
+}
+
 /* Collider table restricted to this path: returns the collider id for the
  * ordered class pair and whether the call is reversed, as dInitColliders
  * (ode/src/collision_kernel.cpp:167-268) arranges it. */
-enum { C_NONE, C_SS, C_SB, C_SP, C_BB, C_BP, C_CP, C_HF, C_CS, C_CB, C_CC };
+enum { C_NONE, C_SS, C_SB, C_SP, C_BB, C_BP, C_CP, C_HF, C_CS, C_CB, C_CC, C_RS, C_RB, C_RC, C_RP };
 static int collider_of(int t1, int t2, int* reverse) {
   *reverse = 0;
 #define PAIR(a, b, id) \
@@ -1310,6 +1472,11 @@ static int collider_of(int t1, int t2, int* reverse) {
   PAIR(ODEGPU_GEOM_HEIGHTFIELD, ODEGPU_GEOM_SPHERE, C_HF);
   PAIR(ODEGPU_GEOM_HEIGHTFIELD, ODEGPU_GEOM_BOX, C_HF);
   PAIR(ODEGPU_GEOM_HEIGHTFIELD, ODEGPU_GEOM_CAPSULE, C_HF);
+  PAIR(ODEGPU_GEOM_RAY, ODEGPU_GEOM_SPHERE, C_RS);
+  PAIR(ODEGPU_GEOM_RAY, ODEGPU_GEOM_BOX, C_RB);
+  PAIR(ODEGPU_GEOM_RAY, ODEGPU_GEOM_CAPSULE, C_RC);
+  PAIR(ODEGPU_GEOM_RAY, ODEGPU_GEOM_PLANE, C_RP);
+  PAIR(ODEGPU_GEOM_HEIGHTFIELD, ODEGPU_GEOM_RAY, C_HF);
 #undef PAIR
   return C_NONE;
 }
@@ -1336,6 +1503,10 @@ static int do_collide(const GeomRef* g1, const GeomRef* g2, unsigned flags, OCon
     case C_CB: n = collide_capsule_box(a, b, c); break;
     case C_CC: n = collide_capsule_capsule(a, b, flags, c); break;
     case C_HF: n = oracle_heightfield_collide(a, b, flags, c); break;
+    case C_RS: n = collide_ray_sphere(a, b, c); break;
+    case C_RB: n = collide_ray_box(a, b, c); break;
+    case C_RC: n = collide_ray_capsule(a, b, c); break;
+    case C_RP: n = collide_ray_plane(a, b, c); break;
     default: n = 0;
   }
   if (rev) {
@@ -1412,12 +1583,20 @@ static int hf_on_triangle(const HFData* D, const real* corner, const int* coords
   }
 }
 
-/* computeAABB of sphere / box / capsule (sphere.cpp:59-67, box.cpp:60-78,
- * capsule.cpp:60-74) */
+/* computeAABB of sphere / box / capsule / ray (sphere.cpp:59-67,
+ * box.cpp:60-78, capsule.cpp:60-74, ray.cpp:56-89) */
 static void geom_aabb(const GeomRef* g, real* aabb) {
   const real* R = g->R;
   const real* pos = g->pos;
   real xr, yr, zr;
+  if (g->type == ODEGPU_GEOM_RAY) {
+    for (int i = 0; i < 3; ++i) {
+      const real e = pos[i] + R[i * 4 + 2] * g->p[0];
+      aabb[2 * i] = pos[i] < e ? pos[i] : e;
+      aabb[2 * i + 1] = pos[i] < e ? e : pos[i];
+    }
+    return;
+  }
   if (g->type == ODEGPU_GEOM_SPHERE) {
     xr = yr = zr = g->p[0];
   } else if (g->type == ODEGPU_GEOM_BOX) {
@@ -1482,6 +1661,7 @@ static int geom_plane_collide(const GeomRef* g, const GeomRef* pl, unsigned flag
   switch (g->type) {
     case ODEGPU_GEOM_SPHERE: return collide_sphere_plane(g, pl, c);
     case ODEGPU_GEOM_BOX: return collide_box_plane(g, pl, flags, c);
+    case ODEGPU_GEOM_RAY: return collide_ray_plane(g, pl, c);
     default: return collide_capsule_plane(g, pl, flags, c);
   }
 }
@@ -1535,7 +1715,7 @@ static int hf_zone(const HFData* D, int minX, int maxX, int minZ, int maxZ, cons
   }
   int nc = 0;
   int further = 0;
-  {
+  if (o2->type != ODEGPU_GEOM_RAY) {   /* rays take the plane pass only */
     const real xratio = (aabb[1] - aabb[0]) * D->inv_sw;
     if (xratio > 1.5) further = 1;
     else {

@@ -360,6 +360,7 @@ static dGeomID make_geom(int type, const double* p) {
     case ODEGPU_GEOM_BOX: return dCreateBox(0, p[0], p[1], p[2]);
     case ODEGPU_GEOM_CAPSULE: return dCreateCapsule(0, p[0], p[1]);
     case ODEGPU_GEOM_PLANE: return dCreatePlane(0, p[0], p[1], p[2], p[3]);
+    case ODEGPU_GEOM_RAY: return dCreateRay(0, p[0]);
     default: return 0;
   }
 }

@@ -156,6 +156,111 @@ def make_hf_kats(n=150, seed=321):
         out=np.array([r[6] for r in recs]))
 
 
+def frame_with_z(d):
+    """A rotation whose third column is the unit vector d (a ray geom points
+    along column 2 of its rotation, ode/src/ray.cpp:115-136)."""
+    d = d / np.linalg.norm(d)
+    a = np.array([1.0, 0, 0]) if abs(d[0]) < 0.9 else np.array([0, 1.0, 0])
+    x = np.cross(a, d)
+    x /= np.linalg.norm(x)
+    y = np.cross(d, x)
+    return np.stack([x, y, d], axis=1)
+
+
+def make_ray_kats(n=150, seed=555):
+    """Rays (ODE's dRayClass) through dCollide: against sphere / box / capsule /
+    plane in both argument orders, and against the placeable fractal field of
+    hf_kats.npz. Starts are spread around the target, inside it for some, and
+    directions aim near it so that most calls hit."""
+    import ctypes as C
+    rng = np.random.Generator(np.random.PCG64(seed))
+    ref = O.ref("d")
+    P = C.POINTER(C.c_double)
+    recs = []
+    for (t1, t2) in [(5, 0), (0, 5), (5, 1), (1, 5), (5, 2), (2, 5), (5, 4), (4, 5), (5, 5)]:
+        other = t2 if t1 == 5 else t1
+        for _ in range(n):
+            if other == 0:
+                po = np.array([rng.uniform(0.1, 0.6), 0, 0, 0])
+            elif other == 1:
+                po = np.concatenate([rng.uniform(0.2, 1.2, 3), [0]])
+            elif other == 2:
+                po = np.array([rng.uniform(0.1, 0.4), rng.uniform(0.2, 1.0), 0, 0])
+            elif other == 4:
+                nrm = rng.normal(size=3)
+                nrm /= np.linalg.norm(nrm)
+                po = np.concatenate([nrm, [rng.uniform(-0.3, 0.3)]])
+            else:
+                po = np.array([rng.uniform(0.2, 2.0), 0, 0, 0])
+            pos_o = rng.uniform(-0.3, 0.3, 3)
+            Ro = rot(rng)
+            start = pos_o + rng.normal(size=3) * rng.uniform(0.0, 1.5)
+            aim = pos_o + rng.normal(size=3) * 0.3 - start
+            if rng.uniform() < 0.2 or np.linalg.norm(aim) < 1e-6:
+                aim = rng.normal(size=3)
+            pr = np.array([rng.uniform(0.2, 3.0), 0, 0, 0])
+            Rr = frame_with_z(aim)
+            if t1 == 5:
+                p1, pos1, R1, p2, pos2, R2 = pr, start, Rr, po, pos_o, Ro
+            else:
+                p1, pos1, R1, p2, pos2, R2 = po, pos_o, Ro, pr, start, Rr
+            flags = int(rng.choice([1, 2, 4]))
+            out = np.zeros((16, 9))
+            args = [np.ascontiguousarray(a, dtype=np.float64) for a in
+                    (p1, pos1, R1.ravel(), p2, pos2, R2.ravel())]
+            nc = ref.ref_collide(t1, args[0].ctypes.data_as(P), args[1].ctypes.data_as(P),
+                                 args[2].ctypes.data_as(P), t2, args[3].ctypes.data_as(P),
+                                 args[4].ctypes.data_as(P), args[5].ctypes.data_as(P), flags,
+                                 out.ctypes.data_as(P))
+            recs.append((t1, t2, flags, p1, pos1, R1.ravel(), p2, pos2, R2.ravel(), nc, out[:8]))
+    # rays against the heightfield of hf_kats.npz, mostly downwards (wheel probes)
+    g = np.load(os.path.join(HERE, "hf_kats.npz"))
+    h = np.ascontiguousarray(g["heights"])
+    sp = float(g["spacing"])
+    nz, nx = h.shape
+    Rh = g["hf_R"].reshape(3, 3)
+    pos_h = g["hf_pos"]
+    H = S.Heightfield()
+    H.nx, H.nz = nx, nz
+    H.width, H.depth = sp * (nx - 1), sp * (nz - 1)
+    H.scale, H.offset, H.thickness, H.wrap = 1.0, 0.0, 1.0, 0
+    H.heights = h.ctypes.data_as(P)
+    H.pos[:] = list(pos_h)
+    H.R[:] = list(Rh.ravel())
+    f = ref.ref_collide_hf
+    f.restype = C.c_int
+    f.argtypes = [C.c_void_p, C.c_int, P, P, P, C.c_int, P]
+    hrecs = []
+    for _ in range(2 * n):
+        local = np.array([rng.uniform(-0.45, 0.45) * H.width, 0.0, rng.uniform(-0.45, 0.45) * H.depth])
+        ix = int(np.clip(round((local[0] + H.width / 2) / sp), 0, nx - 1))
+        iz = int(np.clip(round((local[2] + H.depth / 2) / sp), 0, nz - 1))
+        local[1] = h[iz, ix] + rng.uniform(-0.3, 1.5)
+        d_local = np.array([rng.normal() * 0.3, -1.0, rng.normal() * 0.3])
+        if rng.uniform() < 0.15:
+            d_local[1] = 1.0
+        pos2 = Rh @ local + pos_h
+        R2 = frame_with_z(Rh @ d_local)
+        p2 = np.array([rng.uniform(0.3, 2.0), 0, 0, 0])
+        flags = int(rng.choice([1, 2, 4]))
+        out = np.zeros((64, 9))
+        args = [np.ascontiguousarray(a, dtype=np.float64) for a in (p2, pos2, R2.ravel())]
+        nc = f(C.byref(H), 5, args[0].ctypes.data_as(P), args[1].ctypes.data_as(P),
+               args[2].ctypes.data_as(P), flags, out.ctypes.data_as(P))
+        hrecs.append((flags, p2, pos2, R2.ravel(), nc, out[:8]))
+    np.savez_compressed(
+        os.path.join(HERE, "ray_kats.npz"),
+        t1=np.array([r[0] for r in recs]), t2=np.array([r[1] for r in recs]),
+        flags=np.array([r[2] for r in recs]),
+        p1=np.array([r[3] for r in recs]), pos1=np.array([r[4] for r in recs]),
+        R1=np.array([r[5] for r in recs]), p2=np.array([r[6] for r in recs]),
+        pos2=np.array([r[7] for r in recs]), R2=np.array([r[8] for r in recs]),
+        nc=np.array([r[9] for r in recs]), out=np.array([r[10] for r in recs]),
+        hf_flags=np.array([r[0] for r in hrecs]), hf_p2=np.array([r[1] for r in hrecs]),
+        hf_pos2=np.array([r[2] for r in hrecs]), hf_R2=np.array([r[3] for r in hrecs]),
+        hf_nc=np.array([r[4] for r in hrecs]), hf_out=np.array([r[5] for r in hrecs]))
+
+
 def make_tower():
     """Non-chaotic stacks (boxes of decreasing size, aligned): FP64 reference
     states after 200 steps plus the reference's own FP32 (dSINGLE) build on the
@@ -189,7 +294,10 @@ if __name__ == "__main__":
     only = sys.argv[1:]
     if only:
         for name in only:
-            make_scene(name)
+            if name == "ray_kats":
+                make_ray_kats()
+            else:
+                make_scene(name)
             print("wrote", name)
         sys.exit(0)
     for name in SCENES:
@@ -197,6 +305,7 @@ if __name__ == "__main__":
         print("wrote", name)
     make_collider_kats()
     make_hf_kats()
+    make_ray_kats()
     make_rng_kat()
     make_tower()
     print("wrote collider_kats, rng_kat")

@@ -98,6 +98,45 @@ def test_heightfield_kats_golden():
     assert (g["nc"] > 0).sum() > n // 2
 
 
+def test_ray_kats_golden():
+    """Rays through dCollide (ode/src/ray.cpp:196-498; the heightfield's plane
+    pass with dCollideRayPlane, ode/src/heightfield.cpp:1035-1040): against
+    sphere / box / capsule / plane in both argument orders, ray against ray,
+    and against the placeable field of hf_kats.npz: counts and records
+    bit-exact vs the reference."""
+    g = np.load(os.path.join(GOLDEN, "ray_kats.npz"))
+    L = O.oracle()
+    n = len(g["t1"])
+    mism = 0
+    for i in range(n):
+        out = np.zeros((16, 9))
+        args = [np.ascontiguousarray(g[k][i], dtype=np.float64) for k in
+                ("p1", "pos1", "R1", "p2", "pos2", "R2")]
+        nc = L.oracle_collide(int(g["t1"][i]), *(a.ctypes.data_as(_P(C.c_double)) for a in args[:3]),
+                              int(g["t2"][i]), *(a.ctypes.data_as(_P(C.c_double)) for a in args[3:]),
+                              int(g["flags"][i]), out.ctypes.data_as(_P(C.c_double)))
+        if nc != g["nc"][i] or not np.array_equal(out[:nc, :7], g["out"][i][:nc, :7]):
+            mism += 1
+    assert mism == 0, f"{mism} of {n} ray collider calls differ"
+    assert (g["nc"] > 0).sum() > n // 4
+    H, _h = hf_from_golden(np.load(os.path.join(GOLDEN, "hf_kats.npz")))
+    f = L.oracle_collide_hf
+    f.restype = C.c_int
+    f.argtypes = [C.c_void_p, C.c_int, _P(C.c_double), _P(C.c_double), _P(C.c_double), C.c_int,
+                  _P(C.c_double)]
+    m = len(g["hf_nc"])
+    mism = 0
+    for i in range(m):
+        out = np.zeros((64, 9))
+        args = [np.ascontiguousarray(g[k][i], dtype=np.float64) for k in ("hf_p2", "hf_pos2", "hf_R2")]
+        nc = f(C.byref(H), 5, *(a.ctypes.data_as(_P(C.c_double)) for a in args), int(g["hf_flags"][i]),
+               out.ctypes.data_as(_P(C.c_double)))
+        if nc != g["hf_nc"][i] or not np.array_equal(out[:nc, :7], g["hf_out"][i][:nc, :7]):
+            mism += 1
+    assert mism == 0, f"{mism} of {m} heightfield ray calls differ"
+    assert (g["hf_nc"] > 0).sum() > m // 2
+
+
 @pytest.mark.parametrize("name", ["box_drop", "batched", "hinge", "stack", "capsule", "vehicles", "capsule_pile",
                                   "mechanisms"])
 def test_oracle_matches_reference_golden(name):
