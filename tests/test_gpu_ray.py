@@ -257,10 +257,12 @@ def _vehicle_rays(sc, rng, per_world=12):
             rays.append((w, 0, (ox, oy, 0.0), (0.0, 0.0, -1.0), 2.0))
         b0, _ = sc.world_bodies(w)
         c = sc.body_pos[b0]
+        # world-frame rays at the car; short enough that the heightfield zone
+        # under each stays within the collider's 10 x 10 samples
         for _ in range(per_world - 4):
-            start = c + rng.normal(size=3) * 2.0 + np.array([0, 0, 2.0])
-            aim = c + rng.normal(size=3) * 0.8 - start
-            rays.append((w, -1, tuple(start), tuple(aim), float(rng.uniform(1.0, 6.0))))
+            start = c + rng.normal(size=3) * 0.8 + np.array([0, 0, 1.2])
+            aim = c + rng.normal(size=3) * 0.6 - start
+            rays.append((w, -1, tuple(start), tuple(aim), float(rng.uniform(1.0, 2.5))))
     return np.array(rays, dtype=_ray_dtype())
 
 
@@ -273,7 +275,7 @@ def test_batch_ray_cast_vehicles_vs_oracle():
     """Vehicle worlds after 30 steps: body-attached suspension probes (the
     chassis' own geoms skipped) and world-frame rays at the cars, against the
     oracle's FP64 dCollide over every geom of the world: the same geom hit,
-    records within 2e-4 (rays of up to 6 m in FP32)."""
+    records within 2e-4 (rays of up to 2.5 m in FP32)."""
     from odegpu.batch import Batch
     sc = S.vehicles(n_worlds=6, steps=40, hf_samples=64)
     B = Batch(sc)
@@ -288,6 +290,12 @@ def test_batch_ray_cast_vehicles_vs_oracle():
         # every suspension probe hits the terrain or a wheel
         probes = hits[np.asarray(rays["body"]) == 0]
         assert (probes["geom"] >= 0).all(), probes
+    # a ray whose heightfield zone exceeds the collider's buffers is refused
+    # (geom -3) rather than answered from part of the zone
+    b0, _ = sc.world_bodies(0)
+    far = np.array([(0, -1, tuple(sc.body_pos[b0] + np.array([0, 0, 3.0])), (1.0, 0.3, -0.05), 30.0)],
+                   dtype=_ray_dtype())
+    assert B.ray_cast(far)["geom"][0] == -3
     B.close()
 
 
