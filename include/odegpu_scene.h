@@ -30,6 +30,7 @@ enum {
   ODEGPU_GEOM_SPHERE = 0,
   ODEGPU_GEOM_BOX = 1,
   ODEGPU_GEOM_CAPSULE = 2,
+  ODEGPU_GEOM_CYLINDER = 3,     /* flat-ended; param radius, length along local z */
   ODEGPU_GEOM_PLANE = 4,
   ODEGPU_GEOM_RAY = 5,          /* queries only (dCollide, odegpuBatchRayCast);
                                    a scene may not hold one */
@@ -109,7 +110,9 @@ typedef struct odegpuWorldParams {
 #define ODEGPU_JOINT_NPARAM 36
 /* Number of doubles per geom in odegpuScene.geom_param:
  *   sphere [0]=r; box [0..2]=side; capsule [0]=r [1]=length;
- *   plane [0..3]=a,b,c,d (normalised as dCreatePlane does). */
+ *   cylinder [0]=r [1]=length; plane [0..3]=a,b,c,d (normalised as
+ *   dCreatePlane does); heightfield [0]=index into heightfields; ray
+ *   [0]=length (queries only). */
 #define ODEGPU_GEOM_NPARAM 4
 
 typedef struct odegpuHeightfield {

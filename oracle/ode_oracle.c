@@ -1451,10 +1451,465 @@ static int collide_ray_plane(const GeomRef* ray, const GeomRef* pl, OContact* c)
   return 1;
 }
 
+/* ---- cylinders (flat-ended; ode/src/cylinder.cpp): p[0] radius, p[1] length
+ * along column 2 of R. The dDOUBLE build's tolerance ("toleranz") is 1e-7. */
+#define CYL_TOL 1e-7
+
+/* dCollideCylinderSphere, ode/src/collision_cylinder_sphere.cpp:56-276: side,
+ * disc or disc-rim contact from the sphere centre's axial (s) and radial (t)
+ * distances. */
+static int collide_cylinder_sphere(const GeomRef* cy, const GeomRef* sp, OContact* c) {
+  const real radius = cy->p[0], length = cy->p[1];
+  const real* cp = cy->pos;
+  const real r2 = sp->p[0];
+  const real* S = sp->pos;
+  const real v[3] = {cy->R[2], cy->R[6], cy->R[10]};
+  real s = length * 0.5;
+  real P1[3], P2[3], C[3];
+  for (int i = 0; i < 3; ++i) { P2[i] = v[i] * s + cp[i]; P1[i] = v[i] * -s + cp[i]; }
+  s = (S[0] - P1[0]) * v[0] - (P1[1] - S[1]) * v[1] - (P1[2] - S[2]) * v[2];
+  if (s < (-r2) || s > (length + r2)) return 0;
+  for (int i = 0; i < 3; ++i) C[i] = s * v[i] + P1[i] - S[i];
+  const real t = sqrt(dot3(C, C));
+  if (t > (radius + r2)) return 0;
+  if (t > radius && (s < 0 || s > length)) {
+    const real* P = (s <= 0) ? P1 : P2;
+    const real ds = (s <= 0) ? s : (s - length);
+    c->depth = r2 - sqrt(ds * ds + (t - radius) * (t - radius));
+    if (c->depth < 0) return 0;
+    for (int i = 0; i < 3; ++i) c->pos[i] = C[i] / t * -radius + P[i];
+    for (int i = 0; i < 3; ++i) c->normal[i] = (c->pos[i] - S[i]) / (r2 - c->depth);
+    return 1;
+  } else if ((radius - t) <= s && (radius - t) <= (length - s)) {
+    c->depth = (r2 + radius) - t;
+    if (c->depth < 0) return 0;
+    if (t > (r2 + CYL_TOL)) {
+      for (int i = 0; i < 3; ++i) C[i] /= t;
+      for (int i = 0; i < 3; ++i) { c->pos[i] = C[i] * r2 + S[i]; c->normal[i] = C[i]; }
+    } else {
+      for (int i = 0; i < 3; ++i) { c->pos[i] = C[i] + S[i]; c->normal[i] = C[i] / t; }
+    }
+    return 1;
+  }
+  if (s <= (length * 0.5)) {
+    c->depth = s + r2;
+    if (c->depth < 0) return 0;
+    for (int i = 0; i < 3; ++i) { c->pos[i] = r2 * v[i] + S[i]; c->normal[i] = v[i]; }
+  } else {
+    c->depth = (r2 + length - s);
+    if (c->depth < 0) return 0;
+    for (int i = 0; i < 3; ++i) { c->pos[i] = r2 * -v[i] + S[i]; c->normal[i] = -v[i]; }
+  }
+  return 1;
+}
+
+/* dCollideCylinderPlane, ode/src/collision_cylinder_plane.cpp:43-265: four rim
+ * points of the lower disc when the axis is parallel to the plane normal, else
+ * the deepest rim point of each disc. */
+static int collide_cylinder_plane(const GeomRef* cy, const GeomRef* pl, unsigned flags, OContact* c) {
+  const int maxc = (int)(flags & 0xffff);
+  const real radius = cy->p[0], length = cy->p[1];
+  const real* cp = cy->pos;
+  const real* P = pl->p;
+  const real v[3] = {cy->R[2], cy->R[6], cy->R[10]};
+  real s = length * 0.5;
+  real P1[3], P2[3];
+  for (int i = 0; i < 3; ++i) { P2[i] = v[i] * s + cp[i]; P1[i] = v[i] * -s + cp[i]; }
+  int n = 0;
+  s = v[0] * P[0] + v[1] * P[1] + v[2] * P[2];
+  if (s < 0) s += 1.0;
+  else s -= 1.0;
+  if (s < CYL_TOL && s > (-CYL_TOL)) {
+    real Q[3];
+    s = P[3] - dot3(P, P1);
+    real t = P[3] - dot3(P, P2);
+    if (s >= t) {
+      if (s >= 0) { Q[0] = P1[0]; Q[1] = P1[1]; Q[2] = P1[2]; }
+      else return 0;
+    } else {
+      if (t >= 0) { Q[0] = P2[0]; Q[1] = P2[1]; Q[2] = P2[2]; }
+      else return 0;
+    }
+    real V1[3], V2[3];
+    if (v[0] < CYL_TOL && v[0] > (-CYL_TOL)) { V1[0] = v[0] + 1.0; V1[1] = v[1]; V1[2] = v[2]; }
+    else { V1[0] = v[0]; V1[1] = v[1] + 1.0; V1[2] = v[2]; }
+    cross3(V2, V1, v);
+    t = sqrt(dot3(V2, V2));
+    t = radius / t;
+    for (int i = 0; i < 3; ++i) V2[i] *= t;
+    cross3(V1, V2, v);
+    for (int k = 0; k < 4; ++k) {
+      const real* A = (k < 2) ? V1 : V2;
+      const real sg = (k & 1) ? -1.0 : 1.0;
+      OContact* o = &c[n];
+      for (int i = 0; i < 3; ++i) o->pos[i] = Q[i] + sg * A[i];
+      o->depth = P[3] - dot3(P, o->pos);
+      if (o->depth > 0) {
+        o->normal[0] = P[0]; o->normal[1] = P[1]; o->normal[2] = P[2];
+        if (++n >= maxc) return n;
+      }
+    }
+  } else {
+    const real t = dot3(P, v);
+    real C[3];
+    for (int i = 0; i < 3; ++i) C[i] = v[i] * t - P[i];
+    s = sqrt(dot3(C, C));
+    s = radius / s;
+    for (int i = 0; i < 3; ++i) C[i] *= s;
+    OContact* o = &c[n];
+    for (int i = 0; i < 3; ++i) o->pos[i] = C[i] + P1[i];
+    o->depth = P[3] - dot3(P, o->pos);
+    if (o->depth >= 0) {
+      o->normal[0] = P[0]; o->normal[1] = P[1]; o->normal[2] = P[2];
+      if (++n >= maxc) return n;
+    }
+    o = &c[n];
+    for (int i = 0; i < 3; ++i) o->pos[i] = C[i] + P2[i];
+    o->depth = P[3] - P[0] * o->pos[0] - P[1] * o->pos[1] - P[2] * o->pos[2];
+    if (o->depth >= 0) {
+      o->normal[0] = P[0]; o->normal[1] = P[1]; o->normal[2] = P[2];
+      if (++n >= maxc) return n;
+    }
+  }
+  return n;
+}
+
+/* dCollideRayCylinder, ode/src/ray.cpp:500-698: the flat caps when the ray
+ * starts inside the infinite cylinder and runs along the axis, else the curved
+ * side between the caps. eps is dEpsilon of the build. */
+static int collide_ray_cylinder(const GeomRef* ray, const GeomRef* cy, OContact* c) {
+  const real* RR = ray->R;
+  const real* CR = cy->R;
+  const real half = cy->p[1] * 0.5;
+  real r[3] = {ray->pos[0] - cy->pos[0], ray->pos[1] - cy->pos[1], ray->pos[2] - cy->pos[2]};
+  real d = CR[2] * r[0] + CR[6] * r[1] + CR[10] * r[2];
+  real q[3];
+  for (int i = 0; i < 3; ++i) q[i] = (d * CR[i * 4 + 2]) - r[i];
+  const real C = dot3(q, q) - (cy->p[0] * cy->p[0]);
+  const real uv = CR[2] * RR[2] + CR[6] * RR[6] + CR[10] * RR[10];
+  for (int i = 0; i < 3; ++i) r[i] = (uv * CR[i * 4 + 2]) - RR[i * 4 + 2];
+  real A = dot3(r, r);
+  const real B = 2 * dot3(q, r);
+  real k = B * B - 4 * A * C;
+  if (k < DBL_EPSILON && C <= 0) {
+    const real uvsign = (uv < 0) ? -1.0 : 1.0;
+    const real internal = (d >= -half && d <= +half) ? -1.0 : 1.0;
+    if (((uv > 0) && (d + (uvsign * ray->p[0]) < half * internal)) ||
+        ((uv < 0) && (d + (uvsign * ray->p[0]) > half * internal)))
+      return 0;
+    c->depth = ((-uvsign * d) - (internal * half));
+    for (int i = 0; i < 3; ++i) {
+      c->pos[i] = ray->pos[i] + (c->depth * RR[i * 4 + 2]);
+      c->normal[i] = uvsign * (CR[i * 4 + 2]);
+    }
+    return 1;
+  }
+  if (k > 0) {
+    k = sqrt(k);
+    A = 1.0 / (2 * A);
+    real alpha = (-B - k) * A;
+    if (alpha < 0) alpha = (-B + k) * A;
+    if (alpha >= 0 && alpha <= ray->p[0]) {
+      for (int i = 0; i < 3; ++i) c->pos[i] = ray->pos[i] + (alpha * RR[i * 4 + 2]);
+      for (int i = 0; i < 3; ++i) q[i] = c->pos[i] - cy->pos[i];
+      d = q[0] * CR[2] + q[1] * CR[6] + q[2] * CR[10];
+      if (d >= -half && d <= +half) {
+        const real nsign = (C < 0) ? -1.0 : 1.0;
+        for (int i = 0; i < 3; ++i) c->normal[i] = nsign * (c->pos[i] - (cy->pos[i] + d * CR[i * 4 + 2]));
+        safe_normalize3(c->normal);
+        c->depth = alpha;
+        return 1;
+      }
+    }
+  }
+  return 0;
+}
+
+/* dCollideCylinderBox (ode/src/collision_cylinder_box.cpp:44-1036): separating
+ * axes over the box faces, the cylinder axis, their cross products, the box
+ * vertices and the box edges against both rims; then the cylinder's side edge
+ * clipped by the box, or the box face clipped by the rim's octagon. */
+typedef struct {
+  real cR[12], cpos[3], caxis[3], crad, clen, cnorm[8][3];
+  real bR[12], bpos[3], bhalf[3], bv[8][3];
+  real diff[3], normal[3], best_depth, best_rb, best_rc;
+  int best_axis;
+} CylBox;
+
+/* dMatrix3Inv, ode/src/collision_util.h:192-212, its operator precedence kept */
+static void cb_mat3_inv(const real* ma, real* dst) {
+  const real det = ma[0] * (ma[5] * ma[10] - ma[9] * ma[6]) - ma[1] * (ma[4] * ma[10] - ma[8] * ma[6]) +
+                   ma[2] * (ma[4] * ma[9] - ma[8] * ma[5]);
+  if (fabs(det) < 0.0005) {
+    memset(dst, 0, 12 * sizeof(real));
+    dst[0] = dst[5] = dst[10] = 1;
+    return;
+  }
+  dst[0] = ma[5] * ma[10] - ma[6] * ma[9] / det;
+  dst[1] = -(ma[1] * ma[10] - ma[9] * ma[2]) / det;
+  dst[2] = ma[1] * ma[6] - ma[5] * ma[2] / det;
+  dst[4] = -(ma[4] * ma[10] - ma[6] * ma[8]) / det;
+  dst[5] = ma[0] * ma[10] - ma[8] * ma[2] / det;
+  dst[6] = -(ma[0] * ma[6] - ma[4] * ma[2]) / det;
+  dst[8] = ma[4] * ma[9] - ma[8] * ma[5] / det;
+  dst[9] = -(ma[0] * ma[9] - ma[8] * ma[1]) / det;
+  dst[10] = ma[0] * ma[5] - ma[1] * ma[4] / det;
+  dst[3] = dst[7] = dst[11] = 0;
+}
+
+/* _cldTestAxis (collision_cylinder_box.cpp:206-285) */
+static int cb_test_axis(CylBox* D, real* n, int iAxis) {
+  const real fL = sqrt(dot3(n, n));
+  if (fL < 1e-5) return 1;
+  safe_normalize3(n);
+  const real fdot1 = dot3(D->caxis, n);
+  real frc;
+  if (fdot1 > 1.0 || fdot1 < -1.0) frc = D->clen * 0.5;
+  else frc = fabs(fdot1 * (D->clen * 0.5)) + D->crad * sqrt(1.0 - (fdot1 * fdot1));
+  real frb = 0;
+  for (int j = 0; j < 3; ++j) {
+    const real col[3] = {D->bR[j], D->bR[4 + j], D->bR[8 + j]};
+    frb += fabs(dot3(col, n)) * D->bhalf[j];
+  }
+  const real fd = dot3(D->diff, n);
+  real fDepth = frc + frb;
+  if (fabs(fd) > fDepth) return 0;
+  fDepth -= fabs(fd);
+  if (fDepth < D->best_depth) {
+    D->best_depth = fDepth;
+    D->normal[0] = n[0]; D->normal[1] = n[1]; D->normal[2] = n[2];
+    D->best_axis = iAxis;
+    D->best_rb = frb;
+    D->best_rc = frc;
+    if (fd > 0) { D->normal[0] = -D->normal[0]; D->normal[1] = -D->normal[1]; D->normal[2] = -D->normal[2]; }
+  }
+  return 1;
+}
+
+/* _cldTestEdgeCircleAxis (collision_cylinder_box.cpp:289-333) */
+static int cb_test_edge_circle(CylBox* D, const real* cc, const real* v0, const real* v1, int iAxis) {
+  real e[3] = {v1[0] - v0[0], v1[1] - v0[1], v1[2] - v0[2]};
+  safe_normalize3(e);
+  const real fdot2 = dot3(e, D->caxis);
+  if (fabs(fdot2) < 1e-5) return 1;
+  real t1[3] = {cc[0] - v0[0], cc[1] - v0[1], cc[2] - v0[2]};
+  const real fdot1 = dot3(t1, D->caxis);
+  real p[3];
+  for (int i = 0; i < 3; ++i) p[i] = v0[i] + e[i] * (fdot1 / fdot2);
+  real tan_[3], ax[3];
+  for (int i = 0; i < 3; ++i) t1[i] = cc[i] - p[i];
+  cross3(tan_, t1, D->caxis);
+  cross3(ax, tan_, e);
+  return cb_test_axis(D, ax, iAxis);
+}
+
+/* dClipEdgeToPlane, ode/src/collision_util.cpp:471-510 */
+static int cb_clip_edge(real* e0, real* e1, const real* pl) {
+  const real d0 = pl[0] * e0[0] + pl[1] * e0[1] + pl[2] * e0[2] + pl[3];
+  const real d1 = pl[0] * e1[0] + pl[1] * e1[1] + pl[2] * e1[2] + pl[3];
+  if (d0 < 0 && d1 < 0) return 0;
+  if (d0 > 0 && d1 > 0) return 1;
+  if ((d0 > 0 && d1 < 0) || (d0 < 0 && d1 > 0)) {
+    real ip[3];
+    for (int i = 0; i < 3; ++i) ip[i] = e0[i] - (e0[i] - e1[i]) * d0 / (d0 - d1);
+    real* dst = (d0 < 0) ? e0 : e1;
+    dst[0] = ip[0]; dst[1] = ip[1]; dst[2] = ip[2];
+  }
+  return 1;
+}
+
+/* dClipPolyToPlane, ode/src/collision_util.cpp:512-553 */
+#define CB_MAX_CLIP 16   /* MAX_CYLBOX_CLIP_POINTS; points beyond it are dropped */
+static void cb_clip_poly(const real (*in)[3], int nin, real (*out)[3], int* nout, const real* pl) {
+  int n = 0;
+  for (int i1 = 0, i0 = nin - 1; i1 < nin; i0 = i1, i1++) {
+    const real d0 = pl[0] * in[i0][0] + pl[1] * in[i0][1] + pl[2] * in[i0][2] + pl[3];
+    const real d1 = pl[0] * in[i1][0] + pl[1] * in[i1][1] + pl[2] * in[i1][2] + pl[3];
+    if (d0 >= 0 && n < CB_MAX_CLIP) { out[n][0] = in[i0][0]; out[n][1] = in[i0][1]; out[n][2] = in[i0][2]; n++; }
+    if (((d0 > 0 && d1 < 0) || (d0 < 0 && d1 > 0)) && n < CB_MAX_CLIP) {
+      for (int i = 0; i < 3; ++i) out[n][i] = in[i0][i] - (in[i0][i] - in[i1][i]) * d0 / (d0 - d1);
+      n++;
+    }
+  }
+  *nout = n;
+}
+
+static int collide_cylinder_box(const GeomRef* cy, const GeomRef* bx, unsigned flags, OContact* c) {
+  const int maxc = (int)(flags & 0xffff);
+  CylBox D;
+  /* _cldInitCylinderBox, :100-203 */
+  memcpy(D.cR, cy->R, sizeof(D.cR));
+  for (int i = 0; i < 3; ++i) { D.cpos[i] = cy->pos[i]; D.caxis[i] = cy->R[i * 4 + 2]; }
+  D.crad = cy->p[0];
+  D.clen = cy->p[1];
+  memcpy(D.bR, bx->R, sizeof(D.bR));
+  for (int i = 0; i < 3; ++i) { D.bpos[i] = bx->pos[i]; D.bhalf[i] = bx->p[i] * 0.5; }
+  static const signed char sgn[8][3] = {{-1, 1, -1}, {1, 1, -1}, {-1, -1, -1}, {1, -1, -1},
+                                        {1, 1, 1},   {1, -1, 1}, {-1, -1, 1}, {-1, 1, 1}};
+  for (int k = 0; k < 8; ++k) {
+    const real v[3] = {sgn[k][0] * D.bhalf[0], sgn[k][1] * D.bhalf[1], sgn[k][2] * D.bhalf[2]};
+    real w[3];
+    mul0_331(w, D.bR, v);
+    for (int i = 0; i < 3; ++i) D.bv[k][i] = w[i] + D.bpos[i];
+  }
+  for (int i = 0; i < 3; ++i) D.diff[i] = D.cpos[i] - D.bpos[i];
+  {
+    real ang = M_PI / 8;
+    const real inc = ang * 2.0;
+    for (int k = 0; k < 8; ++k) {
+      D.cnorm[k][0] = -cos(ang);
+      D.cnorm[k][1] = -sin(ang);
+      D.cnorm[k][2] = 0;
+      ang += inc;
+    }
+  }
+  /* _cldTestSeparatingAxes, :336-574 */
+  D.best_depth = INFINITY;
+  D.best_axis = 0;
+  D.best_rb = D.best_rc = 0;
+  D.normal[0] = D.normal[1] = D.normal[2] = 0;
+  real ax[3];
+  for (int j = 0; j < 3; ++j) {
+    ax[0] = D.bR[j]; ax[1] = D.bR[4 + j]; ax[2] = D.bR[8 + j];
+    if (!cb_test_axis(&D, ax, 1 + j)) return 0;
+  }
+  ax[0] = D.caxis[0]; ax[1] = D.caxis[1]; ax[2] = D.caxis[2];
+  if (!cb_test_axis(&D, ax, 4)) return 0;
+  for (int j = 0; j < 3; ++j) {
+    const real col[3] = {D.bR[j], D.bR[4 + j], D.bR[8 + j]};
+    cross3(ax, D.caxis, col);
+    if (dot3(ax, ax) > 1e-6 && !cb_test_axis(&D, ax, 5 + j)) return 0;
+  }
+  for (int k = 0; k < 8; ++k) {
+    real t1[3] = {D.bv[k][0] - D.cpos[0], D.bv[k][1] - D.cpos[1], D.bv[k][2] - D.cpos[2]}, t2[3];
+    cross3(t2, D.caxis, t1);
+    cross3(ax, D.caxis, t2);
+    if (dot3(ax, ax) > 1e-6 && !cb_test_axis(&D, ax, 8 + k)) return 0;
+  }
+  static const unsigned char edges[12][2] = {{1, 0}, {1, 3}, {2, 3}, {2, 0}, {4, 1}, {4, 7},
+                                             {0, 7}, {5, 3}, {5, 6}, {2, 6}, {4, 5}, {6, 7}};
+  for (int side = 0; side < 2; ++side) {   /* top rim, then bottom rim */
+    real cc[3];
+    for (int i = 0; i < 3; ++i) cc[i] = (side == 0) ? D.cpos[i] + D.caxis[i] * (D.clen * 0.5)
+                                                     : D.cpos[i] - D.caxis[i] * (D.clen * 0.5);
+    for (int e = 0; e < 12; ++e)
+      if (!cb_test_edge_circle(&D, cc, D.bv[edges[e][0]], D.bv[edges[e][1]], 16 + 12 * side + e)) return 0;
+  }
+  if (D.best_axis == 0) return 0;
+  int n = 0;
+  const real fdot = dot3(D.normal, D.caxis);
+  if (fabs(fdot) < 0.9) {
+    /* _cldClipCylinderToBox, :576-717 */
+    const real t = dot3(D.caxis, D.normal);
+    real vN[3];
+    for (int i = 0; i < 3; ++i) vN[i] = D.normal[i] - D.caxis[i] * t;
+    safe_normalize3(vN);
+    real e0[3], e1[3];
+    for (int i = 0; i < 3; ++i) {
+      const real ct = D.cpos[i] + vN[i] * D.crad;
+      e0[i] = ct + D.caxis[i] * (D.clen * 0.5);
+      e1[i] = ct - D.caxis[i] * (D.clen * 0.5);
+    }
+    for (int i = 0; i < 3; ++i) { e0[i] -= D.bpos[i]; e1[i] -= D.bpos[i]; }
+    for (int sgn2 = 0; sgn2 < 2; ++sgn2)
+      for (int j = 0; j < 3; ++j) {
+        real pl[4] = {D.bR[j], D.bR[4 + j], D.bR[8 + j], D.bhalf[j]};
+        if (sgn2) { pl[0] = -pl[0]; pl[1] = -pl[1]; pl[2] = -pl[2]; }
+        if (!cb_clip_edge(e0, e1, pl)) return 0;
+      }
+    real d0 = D.best_rb + dot3(e0, D.normal);
+    real d1 = D.best_rb + dot3(e1, D.normal);
+    if (d0 < 0) d0 = 0;
+    if (d1 < 0) d1 = 0;
+    for (int i = 0; i < 3; ++i) { e0[i] += D.bpos[i]; e1[i] += D.bpos[i]; }
+    c[n].depth = d0;
+    for (int i = 0; i < 3; ++i) { c[n].normal[i] = -D.normal[i]; c[n].pos[i] = e0[i]; }
+    n++;
+    if (n != maxc) {
+      c[n].depth = d1;
+      for (int i = 0; i < 3; ++i) { c[n].normal[i] = -D.normal[i]; c[n].pos[i] = e1[i]; }
+      n++;
+    }
+    return n;
+  }
+  /* _cldClipBoxToCylinder, :720-983 */
+  real ccp[3], cn_rel[3] = {0, 0, 0};
+  if (dot3(D.caxis, D.normal) > 0) {
+    for (int i = 0; i < 3; ++i) ccp[i] = D.cpos[i] + D.caxis[i] * (D.clen * 0.5);
+    cn_rel[2] = -1.0;
+  } else {
+    for (int i = 0; i < 3; ++i) ccp[i] = D.cpos[i] - D.caxis[i] * (D.clen * 0.5);
+    cn_rel[2] = 1.0;
+  }
+  real binv[12], vNr[3];
+  cb_mat3_inv(D.bR, binv);
+  mul0_331(vNr, binv, D.normal);
+  const real an[3] = {fabs(vNr[0]), fabs(vNr[1]), fabs(vNr[2])};
+  int iB0, iB1, iB2;
+  if (an[1] > an[0]) {
+    if (an[0] > an[2]) { iB0 = 1; iB1 = 0; iB2 = 2; }
+    else if (an[1] > an[2]) { iB0 = 1; iB1 = 2; iB2 = 0; }
+    else { iB0 = 2; iB1 = 1; iB2 = 0; }
+  } else {
+    if (an[1] > an[2]) { iB0 = 0; iB1 = 1; iB2 = 2; }
+    else if (an[0] > an[2]) { iB0 = 0; iB1 = 2; iB2 = 1; }
+    else { iB0 = 2; iB1 = 0; iB2 = 1; }
+  }
+  real ctr[3];
+  {
+    const real col[3] = {D.bR[iB0], D.bR[4 + iB0], D.bR[8 + iB0]};
+    for (int i = 0; i < 3; ++i)
+      ctr[i] = (vNr[iB0] > 0) ? D.bpos[i] - D.bhalf[iB0] * col[i] : D.bpos[i] + D.bhalf[iB0] * col[i];
+  }
+  real pts[4][3], A1[16][3], A2[16][3];
+  memset(A1, 0, sizeof(A1));
+  memset(A2, 0, sizeof(A2));
+  const real a1[3] = {D.bR[iB1], D.bR[4 + iB1], D.bR[8 + iB1]};
+  const real a2[3] = {D.bR[iB2], D.bR[4 + iB2], D.bR[8 + iB2]};
+  const real h1 = D.bhalf[iB1], h2 = D.bhalf[iB2];
+  for (int i = 0; i < 3; ++i) {
+    pts[0][i] = ctr[i] + h1 * a1[i] - h2 * a2[i];
+    pts[1][i] = ctr[i] - h1 * a1[i] - h2 * a2[i];
+    pts[2][i] = ctr[i] - h1 * a1[i] + h2 * a2[i];
+    pts[3][i] = ctr[i] + h1 * a1[i] + h2 * a2[i];
+  }
+  real cinv[12];
+  cb_mat3_inv(D.cR, cinv);
+  for (int k = 0; k < 4; ++k) {
+    const real t[3] = {pts[k][0] - ccp[0], pts[k][1] - ccp[1], pts[k][2] - ccp[2]};
+    mul0_331(pts[k], cinv, t);
+  }
+  int n1 = 0, n2 = 0;
+  real pl[4] = {cn_rel[0], cn_rel[1], cn_rel[2], 0.0};
+  cb_clip_poly((const real(*)[3])pts, 4, A1, &n1, pl);
+  int seg;
+  for (seg = 0; seg < 8; ++seg) {
+    pl[0] = D.cnorm[seg][0]; pl[1] = D.cnorm[seg][1]; pl[2] = D.cnorm[seg][2]; pl[3] = D.crad;
+    if (seg % 2 == 0) cb_clip_poly((const real(*)[3])A1, n1, A2, &n2, pl);
+    else cb_clip_poly((const real(*)[3])A2, n2, A1, &n1, pl);
+  }
+  const int np = (seg % 2) ? n2 : n1;
+  real (*A)[3] = (seg % 2) ? A2 : A1;
+  for (int k = 0; k < np; ++k) {
+    real p[3];
+    mul0_331(p, D.cR, A[k]);
+    for (int i = 0; i < 3; ++i) p[i] += ccp[i];
+    const real t[3] = {p[0] - D.cpos[0], p[1] - D.cpos[1], p[2] - D.cpos[2]};
+    const real dep = D.best_rc - dot3(t, D.normal);
+    if (dep > 0) {
+      c[n].depth = dep;
+      for (int i = 0; i < 3; ++i) { c[n].normal[i] = -D.normal[i]; c[n].pos[i] = p[i]; }
+      if (++n == maxc) break;
+    }
+  }
+  return n;
+}
+
 /* Collider table restricted to this path: returns the collider id for the
  * ordered class pair and whether the call is reversed, as dInitColliders
  * (ode/src/collision_kernel.cpp:167-268) arranges it. */
-enum { C_NONE, C_SS, C_SB, C_SP, C_BB, C_BP, C_CP, C_HF, C_CS, C_CB, C_CC, C_RS, C_RB, C_RC, C_RP };
+enum { C_NONE, C_SS, C_SB, C_SP, C_BB, C_BP, C_CP, C_HF, C_CS, C_CB, C_CC, C_RS, C_RB, C_RC, C_RP,
+       C_YS, C_YB, C_YP, C_RY };
 static int collider_of(int t1, int t2, int* reverse) {
   *reverse = 0;
 #define PAIR(a, b, id) \
@@ -1477,6 +1932,12 @@ static int collider_of(int t1, int t2, int* reverse) {
   PAIR(ODEGPU_GEOM_RAY, ODEGPU_GEOM_CAPSULE, C_RC);
   PAIR(ODEGPU_GEOM_RAY, ODEGPU_GEOM_PLANE, C_RP);
   PAIR(ODEGPU_GEOM_HEIGHTFIELD, ODEGPU_GEOM_RAY, C_HF);
+  /* cylinder-cylinder and capsule-cylinder need libccd (collision_kernel.cpp:215-220) */
+  PAIR(ODEGPU_GEOM_CYLINDER, ODEGPU_GEOM_SPHERE, C_YS);
+  PAIR(ODEGPU_GEOM_CYLINDER, ODEGPU_GEOM_BOX, C_YB);
+  PAIR(ODEGPU_GEOM_CYLINDER, ODEGPU_GEOM_PLANE, C_YP);
+  PAIR(ODEGPU_GEOM_RAY, ODEGPU_GEOM_CYLINDER, C_RY);
+  PAIR(ODEGPU_GEOM_HEIGHTFIELD, ODEGPU_GEOM_CYLINDER, C_HF);
 #undef PAIR
   return C_NONE;
 }
@@ -1507,6 +1968,10 @@ static int do_collide(const GeomRef* g1, const GeomRef* g2, unsigned flags, OCon
     case C_RB: n = collide_ray_box(a, b, c); break;
     case C_RC: n = collide_ray_capsule(a, b, c); break;
     case C_RP: n = collide_ray_plane(a, b, c); break;
+    case C_YS: n = collide_cylinder_sphere(a, b, c); break;
+    case C_YB: n = collide_cylinder_box(a, b, flags, c); break;
+    case C_YP: n = collide_cylinder_plane(a, b, flags, c); break;
+    case C_RY: n = collide_ray_cylinder(a, b, c); break;
     default: n = 0;
   }
   if (rev) {
@@ -1599,6 +2064,11 @@ static void geom_aabb(const GeomRef* g, real* aabb) {
   }
   if (g->type == ODEGPU_GEOM_SPHERE) {
     xr = yr = zr = g->p[0];
+  } else if (g->type == ODEGPU_GEOM_CYLINDER) {   /* cylinder.cpp:58-73 */
+    const real radius = g->p[0], lz = g->p[1];
+    xr = fabs(R[0] * radius) + fabs(R[1] * radius) + 0.5 * fabs(R[2] * lz);
+    yr = fabs(R[4] * radius) + fabs(R[5] * radius) + 0.5 * fabs(R[6] * lz);
+    zr = fabs(R[8] * radius) + fabs(R[9] * radius) + 0.5 * fabs(R[10] * lz);
   } else if (g->type == ODEGPU_GEOM_BOX) {
     const real* side = g->p;
     xr = 0.5 * (fabs(R[0] * side[0]) + fabs(R[1] * side[1]) + fabs(R[2] * side[2]));
@@ -1662,6 +2132,7 @@ static int geom_plane_collide(const GeomRef* g, const GeomRef* pl, unsigned flag
     case ODEGPU_GEOM_SPHERE: return collide_sphere_plane(g, pl, c);
     case ODEGPU_GEOM_BOX: return collide_box_plane(g, pl, flags, c);
     case ODEGPU_GEOM_RAY: return collide_ray_plane(g, pl, c);
+    case ODEGPU_GEOM_CYLINDER: return collide_cylinder_plane(g, pl, flags, c);
     default: return collide_capsule_plane(g, pl, flags, c);
   }
 }
@@ -1854,8 +2325,23 @@ static int hf_zone(const HFData* D, int minX, int maxX, int minZ, int maxZ, cons
       for (int i = 0; i < 3; ++i) {
         HFVertex* hv = &V[t->vi[i]];
         if (hv->state) continue;
-        const real depth = geom_point_depth(o2, hv->v);
-        if (depth > HF_EPS) {
+        real depth;
+        int hit;
+        if (o2->type == ODEGPU_GEOM_CYLINDER) {
+          /* no point-depth function for cylinders: a ray from the vertex along
+           * the triangle's normal, of length (minO2 - y) * 1000, and the ray's
+           * depth (heightfield.cpp:1562-1584) */
+          real rR[12] = {1, 0, t->plane[0], 0, 0, 1, t->plane[1], 0, 0, 0, t->plane[2], 0};
+          real rp[4] = {(minO2 - hv->v[1]) * 1000.0, 0, 0, 0};
+          GeomRef ray = {ODEGPU_GEOM_RAY, hv->v, rR, rp, NULL};
+          OContact rc;
+          hit = collide_ray_cylinder(&ray, o2, &rc);
+          depth = rc.depth;
+        } else {
+          depth = geom_point_depth(o2, hv->v);
+          hit = depth > HF_EPS;
+        }
+        if (hit) {
           OContact* o = &out[nc];
           for (int q = 0; q < 3; ++q) { o->pos[q] = hv->v[q]; o->normal[q] = -t->plane[q]; }
           o->depth = depth;
@@ -3131,6 +3617,7 @@ static real geom_bound(const OGeom* G) {
     case ODEGPU_GEOM_SPHERE: return G->p[0];
     case ODEGPU_GEOM_BOX: return 0.5 * sqrt(G->p[0] * G->p[0] + G->p[1] * G->p[1] + G->p[2] * G->p[2]);
     case ODEGPU_GEOM_CAPSULE: return G->p[0] + 0.5 * G->p[1];
+    case ODEGPU_GEOM_CYLINDER: return sqrt(G->p[0] * G->p[0] + 0.25 * G->p[1] * G->p[1]);
     default: return R_INF;
   }
 }

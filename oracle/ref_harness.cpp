@@ -117,6 +117,7 @@ int ref_run_world(const odegpuScene* sc, int w, int n_steps, double* state,
       case ODEGPU_GEOM_SPHERE: geom = dCreateSphere(0, gp[0]); break;
       case ODEGPU_GEOM_BOX: geom = dCreateBox(0, gp[0], gp[1], gp[2]); break;
       case ODEGPU_GEOM_CAPSULE: geom = dCreateCapsule(0, gp[0], gp[1]); break;
+      case ODEGPU_GEOM_CYLINDER: geom = dCreateCylinder(0, gp[0], gp[1]); break;
       case ODEGPU_GEOM_PLANE: geom = dCreatePlane(0, gp[0], gp[1], gp[2], gp[3]); break;
       case ODEGPU_GEOM_HEIGHTFIELD: {
         const odegpuHeightfield* H = &sc->heightfields[(int)gp[0]];
@@ -361,6 +362,7 @@ static dGeomID make_geom(int type, const double* p) {
     case ODEGPU_GEOM_CAPSULE: return dCreateCapsule(0, p[0], p[1]);
     case ODEGPU_GEOM_PLANE: return dCreatePlane(0, p[0], p[1], p[2], p[3]);
     case ODEGPU_GEOM_RAY: return dCreateRay(0, p[0]);
+    case ODEGPU_GEOM_CYLINDER: return dCreateCylinder(0, p[0], p[1]);
     default: return 0;
   }
 }

@@ -261,6 +261,120 @@ def make_ray_kats(n=150, seed=555):
         hf_nc=np.array([r[4] for r in hrecs]), hf_out=np.array([r[5] for r in hrecs]))
 
 
+def _axis_rot(rng):
+    """A rotation about a random coordinate axis by a multiple of 90 degrees
+    (exactly representable), for the aligned cases of the cylinder colliders."""
+    R = np.eye(3)
+    k = int(rng.integers(0, 3))
+    for _ in range(int(rng.integers(0, 4))):
+        Q = np.zeros((3, 3))
+        a, b = [(1, 2), (0, 2), (0, 1)][k]
+        Q[k, k] = 1
+        Q[a, b], Q[b, a] = -1, 1
+        R = Q @ R
+    return R
+
+
+def make_cylinder_kats(n=150, seed=777):
+    """Cylinders (dCylinderClass) through dCollide: with sphere, box and plane
+    in both argument orders, rays into cylinders, cylinder against cylinder
+    and capsule (no collider without libccd), and dCollide(heightfield,
+    cylinder) on the field of hf_kats.npz. A fifth of the poses are axis
+    aligned (the parallel-disc and box-face clipping branches)."""
+    import ctypes as C
+    rng = np.random.Generator(np.random.PCG64(seed))
+    ref = O.ref("d")
+    P = C.POINTER(C.c_double)
+
+    def params(t):
+        if t == 0:
+            return np.array([rng.uniform(0.1, 0.6), 0, 0, 0])
+        if t == 1:
+            return np.concatenate([rng.uniform(0.2, 1.2, 3), [0]])
+        if t == 2:
+            return np.array([rng.uniform(0.1, 0.4), rng.uniform(0.2, 1.0), 0, 0])
+        if t == 3:
+            return np.array([rng.uniform(0.1, 0.5), rng.uniform(0.2, 1.2), 0, 0])
+        if t == 5:
+            return np.array([rng.uniform(0.2, 3.0), 0, 0, 0])
+        nrm = rng.normal(size=3) if rng.uniform() < 0.7 else np.eye(3)[int(rng.integers(0, 3))]
+        nrm = nrm / np.linalg.norm(nrm)
+        return np.concatenate([nrm, [rng.uniform(-0.3, 0.3)]])
+
+    recs = []
+    for (t1, t2) in [(3, 0), (0, 3), (3, 1), (1, 3), (3, 4), (4, 3), (5, 3), (3, 5), (3, 3), (2, 3), (3, 2)]:
+        for _ in range(n):
+            p1, p2 = params(t1), params(t2)
+            aligned = rng.uniform() < 0.2
+            pos1 = rng.uniform(-0.5, 0.5, 3)
+            pos2 = rng.uniform(-0.5, 0.5, 3)
+            R1 = _axis_rot(rng) if aligned else rot(rng)
+            R2 = _axis_rot(rng) if aligned else rot(rng)
+            if 5 in (t1, t2):
+                start = (pos2 if t1 == 5 else pos1) + rng.normal(size=3) * rng.uniform(0.0, 1.5)
+                aim = (pos1 if t1 == 5 else pos2) + rng.normal(size=3) * 0.2 - start
+                if aligned:   # along the cylinder's axis
+                    Rc = R2 if t1 == 5 else R1
+                    aim = Rc[:, 2] * rng.choice([-1.0, 1.0])
+                    start = (pos2 if t1 == 5 else pos1) + Rc[:, 0] * rng.uniform(-0.3, 0.3) - aim * 1.0
+                Rr = frame_with_z(aim)
+                if t1 == 5:
+                    pos1, R1 = start, Rr
+                else:
+                    pos2, R2 = start, Rr
+            flags = int(rng.choice([1, 2, 3, 4, 8]))
+            out = np.zeros((16, 9))
+            args = [np.ascontiguousarray(a, dtype=np.float64) for a in
+                    (p1, pos1, R1.ravel(), p2, pos2, R2.ravel())]
+            nc = ref.ref_collide(t1, args[0].ctypes.data_as(P), args[1].ctypes.data_as(P),
+                                 args[2].ctypes.data_as(P), t2, args[3].ctypes.data_as(P),
+                                 args[4].ctypes.data_as(P), args[5].ctypes.data_as(P), flags,
+                                 out.ctypes.data_as(P))
+            recs.append((t1, t2, flags, p1, pos1, R1.ravel(), p2, pos2, R2.ravel(), nc, out[:8]))
+    g = np.load(os.path.join(HERE, "hf_kats.npz"))
+    h = np.ascontiguousarray(g["heights"])
+    sp = float(g["spacing"])
+    nz, nx = h.shape
+    Rh = g["hf_R"].reshape(3, 3)
+    pos_h = g["hf_pos"]
+    H = S.Heightfield()
+    H.nx, H.nz = nx, nz
+    H.width, H.depth = sp * (nx - 1), sp * (nz - 1)
+    H.scale, H.offset, H.thickness, H.wrap = 1.0, 0.0, 1.0, 0
+    H.heights = h.ctypes.data_as(P)
+    H.pos[:] = list(pos_h)
+    H.R[:] = list(Rh.ravel())
+    f = ref.ref_collide_hf
+    f.restype = C.c_int
+    f.argtypes = [C.c_void_p, C.c_int, P, P, P, C.c_int, P]
+    hrecs = []
+    for _ in range(2 * n):
+        p2 = np.array([rng.uniform(0.1, 0.6), rng.uniform(0.2, 1.5), 0, 0])
+        local = np.array([rng.uniform(-0.45, 0.45) * H.width, 0.0, rng.uniform(-0.45, 0.45) * H.depth])
+        ix = int(np.clip(round((local[0] + H.width / 2) / sp), 0, nx - 1))
+        iz = int(np.clip(round((local[2] + H.depth / 2) / sp), 0, nz - 1))
+        local[1] = h[iz, ix] + rng.uniform(-0.3, 0.6)
+        pos2 = Rh @ local + pos_h
+        R2 = rot(rng) if rng.uniform() < 0.8 else np.eye(3)
+        flags = int(rng.choice([1, 2, 3, 4, 8]))
+        out = np.zeros((64, 9))
+        args = [np.ascontiguousarray(a, dtype=np.float64) for a in (p2, pos2, R2.ravel())]
+        nc = f(C.byref(H), 3, args[0].ctypes.data_as(P), args[1].ctypes.data_as(P),
+               args[2].ctypes.data_as(P), flags, out.ctypes.data_as(P))
+        hrecs.append((flags, p2, pos2, R2.ravel(), nc, out[:8]))
+    np.savez_compressed(
+        os.path.join(HERE, "cylinder_kats.npz"),
+        t1=np.array([r[0] for r in recs]), t2=np.array([r[1] for r in recs]),
+        flags=np.array([r[2] for r in recs]),
+        p1=np.array([r[3] for r in recs]), pos1=np.array([r[4] for r in recs]),
+        R1=np.array([r[5] for r in recs]), p2=np.array([r[6] for r in recs]),
+        pos2=np.array([r[7] for r in recs]), R2=np.array([r[8] for r in recs]),
+        nc=np.array([r[9] for r in recs]), out=np.array([r[10] for r in recs]),
+        hf_flags=np.array([r[0] for r in hrecs]), hf_p2=np.array([r[1] for r in hrecs]),
+        hf_pos2=np.array([r[2] for r in hrecs]), hf_R2=np.array([r[3] for r in hrecs]),
+        hf_nc=np.array([r[4] for r in hrecs]), hf_out=np.array([r[5] for r in hrecs]))
+
+
 def make_tower():
     """Non-chaotic stacks (boxes of decreasing size, aligned): FP64 reference
     states after 200 steps plus the reference's own FP32 (dSINGLE) build on the
@@ -296,6 +410,8 @@ if __name__ == "__main__":
         for name in only:
             if name == "ray_kats":
                 make_ray_kats()
+            elif name == "cylinder_kats":
+                make_cylinder_kats()
             else:
                 make_scene(name)
             print("wrote", name)
@@ -306,6 +422,7 @@ if __name__ == "__main__":
     make_collider_kats()
     make_hf_kats()
     make_ray_kats()
+    make_cylinder_kats()
     make_rng_kat()
     make_tower()
     print("wrote collider_kats, rng_kat")

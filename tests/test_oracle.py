@@ -98,13 +98,17 @@ def test_heightfield_kats_golden():
     assert (g["nc"] > 0).sum() > n // 2
 
 
-def test_ray_kats_golden():
-    """Rays through dCollide (ode/src/ray.cpp:196-498; the heightfield's plane
-    pass with dCollideRayPlane, ode/src/heightfield.cpp:1035-1040): against
-    sphere / box / capsule / plane in both argument orders, ray against ray,
-    and against the placeable field of hf_kats.npz: counts and records
-    bit-exact vs the reference."""
-    g = np.load(os.path.join(GOLDEN, "ray_kats.npz"))
+@pytest.mark.parametrize("fixture,hf_class", [("ray_kats", 5), ("cylinder_kats", 3)])
+def test_ray_and_cylinder_kats_golden(fixture, hf_class):
+    """Rays (ode/src/ray.cpp:196-698) and cylinders (ode/src/cylinder.cpp,
+    collision_cylinder_sphere.cpp, collision_cylinder_box.cpp,
+    collision_cylinder_plane.cpp) through dCollide, every collider in both
+    argument orders plus the pairs without a collider (ray-ray,
+    cylinder-cylinder, capsule-cylinder), and against the placeable field of
+    hf_kats.npz (rays take the plane pass only; cylinders have no point-depth
+    function, so the vertex pass casts rays, ode/src/heightfield.cpp:1035-1068,
+    1562-1584): counts and records bit-exact vs the reference."""
+    g = np.load(os.path.join(GOLDEN, f"{fixture}.npz"))
     L = O.oracle()
     n = len(g["t1"])
     mism = 0
@@ -117,7 +121,7 @@ def test_ray_kats_golden():
                               int(g["flags"][i]), out.ctypes.data_as(_P(C.c_double)))
         if nc != g["nc"][i] or not np.array_equal(out[:nc, :7], g["out"][i][:nc, :7]):
             mism += 1
-    assert mism == 0, f"{mism} of {n} ray collider calls differ"
+    assert mism == 0, f"{mism} of {n} {fixture} collider calls differ"
     assert (g["nc"] > 0).sum() > n // 4
     H, _h = hf_from_golden(np.load(os.path.join(GOLDEN, "hf_kats.npz")))
     f = L.oracle_collide_hf
@@ -129,11 +133,11 @@ def test_ray_kats_golden():
     for i in range(m):
         out = np.zeros((64, 9))
         args = [np.ascontiguousarray(g[k][i], dtype=np.float64) for k in ("hf_p2", "hf_pos2", "hf_R2")]
-        nc = f(C.byref(H), 5, *(a.ctypes.data_as(_P(C.c_double)) for a in args), int(g["hf_flags"][i]),
+        nc = f(C.byref(H), hf_class, *(a.ctypes.data_as(_P(C.c_double)) for a in args), int(g["hf_flags"][i]),
                out.ctypes.data_as(_P(C.c_double)))
         if nc != g["hf_nc"][i] or not np.array_equal(out[:nc, :7], g["hf_out"][i][:nc, :7]):
             mism += 1
-    assert mism == 0, f"{mism} of {m} heightfield ray calls differ"
+    assert mism == 0, f"{mism} of {m} heightfield calls differ"
     assert (g["hf_nc"] > 0).sum() > m // 2
 
 
