@@ -227,6 +227,11 @@ void dMassSetSphere(dMass* m, dReal density, dReal radius);              /* :52 
 void dMassSetSphereTotal(dMass* m, dReal total_mass, dReal radius);      /* :53 */
 void dMassSetBox(dMass* m, dReal density, dReal lx, dReal ly, dReal lz); /* :65 */
 void dMassSetBoxTotal(dMass* m, dReal total_mass, dReal lx, dReal ly, dReal lz); /* :67 */
+void dMassSetCapsule(dMass* m, dReal density, int direction, dReal radius, dReal length);       /* :55 */
+void dMassSetCapsuleTotal(dMass* m, dReal total_mass, int direction, dReal radius, dReal length); /* :57 */
+void dMassSetCylinder(dMass* m, dReal density, int direction, dReal radius, dReal length);      /* :60 */
+void dMassSetCylinderTotal(dMass* m, dReal total_mass, int direction, dReal radius, dReal length); /* :62 */
+void dMassAdjust(dMass* m, dReal newmass);                               /* :74 */
 
 /* RNG: include/ode/misc.h */
 int dTestRand(void);                                                     /* :37 */
@@ -242,6 +247,12 @@ dGeomID dCreateSphere(dSpaceID space, dReal radius);                     /* :924
 dGeomID dCreateBox(dSpaceID space, dReal lx, dReal ly, dReal lz);        /* :1002 */
 dGeomID dCreatePlane(dSpaceID space, dReal a, dReal b, dReal c, dReal d); /* :1046 */
 dGeomID dCreateCapsule(dSpaceID space, dReal radius, dReal length);      /* :1051 */
+/* Flat-ended cylinders: dCollide with sphere, box, plane, ray and heightfield;
+ * cylinder-cylinder and capsule-cylinder return no contacts, as in a reference
+ * build without libccd. */
+dGeomID dCreateCylinder(dSpaceID space, dReal radius, dReal length);     /* :1063 */
+void dGeomCylinderSetParams(dGeomID cylinder, dReal radius, dReal length);   /* :1064 */
+void dGeomCylinderGetParams(dGeomID cylinder, dReal* radius, dReal* length); /* :1065 */
 /* Rays: dCollide of a ray with a sphere, box, capsule, plane or heightfield
  * returns at most one contact whose depth is the distance along the ray. */
 dGeomID dCreateRay(dSpaceID space, dReal length);                        /* :1067 */

@@ -18,10 +18,10 @@ struct GeomView {
   int type;
   float pos[3];
   float R[12];
-  float p[4];   // sphere r / box sides / capsule r,len / plane a,b,c,d / ray length
+  float p[4];   // sphere r / box sides / capsule, cylinder r,len / plane a,b,c,d / ray length
 };
 
-enum { G_SPHERE = 0, G_BOX = 1, G_CAPSULE = 2, G_PLANE = 4, G_RAY = 5, G_HEIGHTFIELD = 9 };
+enum { G_SPHERE = 0, G_BOX = 1, G_CAPSULE = 2, G_CYLINDER = 3, G_PLANE = 4, G_RAY = 5, G_HEIGHTFIELD = 9 };
 constexpr unsigned kContactsUnimportant = 0x80000000u;
 
 // dCollideSpheres (ode/src/collision_util.cpp:38-67)
@@ -867,11 +867,458 @@ OG_HD int collide_ray_plane(const GeomView& ray, const GeomView& pl, Contact* c)
   return 1;
 }
 
+// ---- cylinders (flat-ended, ode/src/cylinder.cpp): p[0] radius, p[1] length
+// along column 2 of R. kCylTol is the dSINGLE build's "toleranz".
+constexpr float kCylTol = 1e-4f;
+
+// dCollideCylinderSphere (ode/src/collision_cylinder_sphere.cpp:56-276): side,
+// disc or rim contact from the sphere centre's axial (s) and radial (t)
+// distances.
+OG_HD int collide_cylinder_sphere(const GeomView& cy, const GeomView& sp, Contact* c) {
+  const float radius = cy.p[0], length = cy.p[1];
+  const float* cp = cy.pos;
+  const float r2 = sp.p[0];
+  const float* S = sp.pos;
+  const float v[3] = {cy.R[2], cy.R[6], cy.R[10]};
+  float s = length * 0.5f;
+  float P1[3], P2[3], C[3];
+  for (int i = 0; i < 3; ++i) { P2[i] = v[i] * s + cp[i]; P1[i] = v[i] * -s + cp[i]; }
+  s = (S[0] - P1[0]) * v[0] - (P1[1] - S[1]) * v[1] - (P1[2] - S[2]) * v[2];
+  if (s < (-r2) || s > (length + r2)) return 0;
+  for (int i = 0; i < 3; ++i) C[i] = s * v[i] + P1[i] - S[i];
+  const float t = sqrtf(dot3(C, C));
+  if (t > (radius + r2)) return 0;
+  if (t > radius && (s < 0.f || s > length)) {
+    const float* P = (s <= 0.f) ? P1 : P2;
+    const float ds = (s <= 0.f) ? s : (s - length);
+    c->depth = r2 - sqrtf(ds * ds + (t - radius) * (t - radius));
+    if (c->depth < 0.f) return 0;
+    for (int i = 0; i < 3; ++i) c->pos[i] = C[i] / t * -radius + P[i];
+    for (int i = 0; i < 3; ++i) c->normal[i] = (c->pos[i] - S[i]) / (r2 - c->depth);
+    return 1;
+  } else if ((radius - t) <= s && (radius - t) <= (length - s)) {
+    c->depth = (r2 + radius) - t;
+    if (c->depth < 0.f) return 0;
+    if (t > (r2 + kCylTol)) {
+      for (int i = 0; i < 3; ++i) C[i] /= t;
+      for (int i = 0; i < 3; ++i) { c->pos[i] = C[i] * r2 + S[i]; c->normal[i] = C[i]; }
+    } else {
+      for (int i = 0; i < 3; ++i) { c->pos[i] = C[i] + S[i]; c->normal[i] = C[i] / t; }
+    }
+    return 1;
+  }
+  if (s <= (length * 0.5f)) {
+    c->depth = s + r2;
+    if (c->depth < 0.f) return 0;
+    for (int i = 0; i < 3; ++i) { c->pos[i] = r2 * v[i] + S[i]; c->normal[i] = v[i]; }
+  } else {
+    c->depth = (r2 + length - s);
+    if (c->depth < 0.f) return 0;
+    for (int i = 0; i < 3; ++i) { c->pos[i] = r2 * -v[i] + S[i]; c->normal[i] = -v[i]; }
+  }
+  return 1;
+}
+
+// dCollideCylinderPlane (ode/src/collision_cylinder_plane.cpp:43-265): four rim
+// points of the lower disc when the axis is parallel to the plane normal (within
+// kCylTol), else the deepest rim point of each disc.
+OG_HD int collide_cylinder_plane(const GeomView& cy, const GeomView& pl, unsigned flags, Contact* c) {
+  const int maxc = (int)(flags & 0xffff);
+  const float radius = cy.p[0], length = cy.p[1];
+  const float* cp = cy.pos;
+  const float* P = pl.p;
+  const float v[3] = {cy.R[2], cy.R[6], cy.R[10]};
+  float s = length * 0.5f;
+  float P1[3], P2[3];
+  for (int i = 0; i < 3; ++i) { P2[i] = v[i] * s + cp[i]; P1[i] = v[i] * -s + cp[i]; }
+  int n = 0;
+  s = v[0] * P[0] + v[1] * P[1] + v[2] * P[2];
+  if (s < 0.f) s += 1.0f;
+  else s -= 1.0f;
+  if (s < kCylTol && s > (-kCylTol)) {
+    float Q[3];
+    s = P[3] - dot3(P, P1);
+    float t = P[3] - dot3(P, P2);
+    if (s >= t) {
+      if (s >= 0.f) { Q[0] = P1[0]; Q[1] = P1[1]; Q[2] = P1[2]; }
+      else return 0;
+    } else {
+      if (t >= 0.f) { Q[0] = P2[0]; Q[1] = P2[1]; Q[2] = P2[2]; }
+      else return 0;
+    }
+    float V1[3], V2[3];
+    if (v[0] < kCylTol && v[0] > (-kCylTol)) { V1[0] = v[0] + 1.0f; V1[1] = v[1]; V1[2] = v[2]; }
+    else { V1[0] = v[0]; V1[1] = v[1] + 1.0f; V1[2] = v[2]; }
+    cross3(V2, V1, v);
+    t = sqrtf(dot3(V2, V2));
+    t = radius / t;
+    for (int i = 0; i < 3; ++i) V2[i] *= t;
+    cross3(V1, V2, v);
+    for (int k = 0; k < 4; ++k) {
+      const float* A = (k < 2) ? V1 : V2;
+      Contact* o = &c[n];
+      for (int i = 0; i < 3; ++i) o->pos[i] = (k & 1) ? Q[i] - A[i] : Q[i] + A[i];
+      o->depth = P[3] - dot3(P, o->pos);
+      if (o->depth > 0.f) {
+        o->normal[0] = P[0]; o->normal[1] = P[1]; o->normal[2] = P[2];
+        if (++n >= maxc) return n;
+      }
+    }
+  } else {
+    const float t = dot3(P, v);
+    float C[3];
+    for (int i = 0; i < 3; ++i) C[i] = v[i] * t - P[i];
+    s = sqrtf(dot3(C, C));
+    s = radius / s;
+    for (int i = 0; i < 3; ++i) C[i] *= s;
+    Contact* o = &c[n];
+    for (int i = 0; i < 3; ++i) o->pos[i] = C[i] + P1[i];
+    o->depth = P[3] - dot3(P, o->pos);
+    if (o->depth >= 0.f) {
+      o->normal[0] = P[0]; o->normal[1] = P[1]; o->normal[2] = P[2];
+      if (++n >= maxc) return n;
+    }
+    o = &c[n];
+    for (int i = 0; i < 3; ++i) o->pos[i] = C[i] + P2[i];
+    o->depth = P[3] - P[0] * o->pos[0] - P[1] * o->pos[1] - P[2] * o->pos[2];
+    if (o->depth >= 0.f) {
+      o->normal[0] = P[0]; o->normal[1] = P[1]; o->normal[2] = P[2];
+      if (++n >= maxc) return n;
+    }
+  }
+  return n;
+}
+
+// dCollideRayCylinder (ode/src/ray.cpp:500-698): the flat caps when the ray
+// starts inside the infinite cylinder running along the axis (the test uses
+// FLT_EPSILON, dEpsilon of dSINGLE), else the curved side between the caps.
+OG_HD int collide_ray_cylinder(const GeomView& ray, const GeomView& cy, Contact* c) {
+  const float* RR = ray.R;
+  const float* CR = cy.R;
+  const float half = cy.p[1] * 0.5f;
+  float r[3] = {ray.pos[0] - cy.pos[0], ray.pos[1] - cy.pos[1], ray.pos[2] - cy.pos[2]};
+  float d = CR[2] * r[0] + CR[6] * r[1] + CR[10] * r[2];
+  float q[3];
+  for (int i = 0; i < 3; ++i) q[i] = (d * CR[i * 4 + 2]) - r[i];
+  const float C = dot3(q, q) - (cy.p[0] * cy.p[0]);
+  const float uv = CR[2] * RR[2] + CR[6] * RR[6] + CR[10] * RR[10];
+  for (int i = 0; i < 3; ++i) r[i] = (uv * CR[i * 4 + 2]) - RR[i * 4 + 2];
+  float A = dot3(r, r);
+  const float B = 2.f * dot3(q, r);
+  float k = B * B - 4.f * A * C;
+  if (k < 1.1920929e-7f && C <= 0.f) {
+    const float uvsign = (uv < 0.f) ? -1.0f : 1.0f;
+    const float internal = (d >= -half && d <= +half) ? -1.0f : 1.0f;
+    if (((uv > 0.f) && (d + (uvsign * ray.p[0]) < half * internal)) ||
+        ((uv < 0.f) && (d + (uvsign * ray.p[0]) > half * internal)))
+      return 0;
+    c->depth = ((-uvsign * d) - (internal * half));
+    for (int i = 0; i < 3; ++i) {
+      c->pos[i] = ray.pos[i] + (c->depth * RR[i * 4 + 2]);
+      c->normal[i] = uvsign * (CR[i * 4 + 2]);
+    }
+    return 1;
+  }
+  if (k > 0.f) {
+    k = sqrtf(k);
+    A = 1.0f / (2.f * A);
+    float alpha = (-B - k) * A;
+    if (alpha < 0.f) alpha = (-B + k) * A;
+    if (alpha >= 0.f && alpha <= ray.p[0]) {
+      for (int i = 0; i < 3; ++i) c->pos[i] = ray.pos[i] + (alpha * RR[i * 4 + 2]);
+      for (int i = 0; i < 3; ++i) q[i] = c->pos[i] - cy.pos[i];
+      d = q[0] * CR[2] + q[1] * CR[6] + q[2] * CR[10];
+      if (d >= -half && d <= +half) {
+        const float nsign = (C < 0.f) ? -1.0f : 1.0f;
+        for (int i = 0; i < 3; ++i) c->normal[i] = nsign * (c->pos[i] - (cy.pos[i] + d * CR[i * 4 + 2]));
+        safe_normalize3(c->normal);
+        c->depth = alpha;
+        return 1;
+      }
+    }
+  }
+  return 0;
+}
+
+// dCollideCylinderBox (ode/src/collision_cylinder_box.cpp:44-1036): separating
+// axes over the box faces, the cylinder axis, their cross products, the box
+// vertices and the box edges against both rims; then the cylinder's side edge
+// clipped by the box, or the box face clipped by the rim's octagon. Out of line
+// (its scratch stays out of the callers' registers).
+struct CylBox {
+  float cpos[3], caxis[3], crad, clen;
+  float bhalf[3], bv[8][3];
+  float diff[3], normal[3], best_depth, best_rb, best_rc;
+  int best_axis;
+};
+
+// dMatrix3Inv (ode/src/collision_util.h:192-212), its operator precedence kept
+OG_HD void cb_mat3_inv(const float* ma, float* dst) {
+  const float det = ma[0] * (ma[5] * ma[10] - ma[9] * ma[6]) - ma[1] * (ma[4] * ma[10] - ma[8] * ma[6]) +
+                    ma[2] * (ma[4] * ma[9] - ma[8] * ma[5]);
+  if (fabsf(det) < 0.0005f) {
+    for (int k = 0; k < 12; ++k) dst[k] = 0.f;
+    dst[0] = dst[5] = dst[10] = 1.f;
+    return;
+  }
+  dst[0] = ma[5] * ma[10] - ma[6] * ma[9] / det;
+  dst[1] = -(ma[1] * ma[10] - ma[9] * ma[2]) / det;
+  dst[2] = ma[1] * ma[6] - ma[5] * ma[2] / det;
+  dst[4] = -(ma[4] * ma[10] - ma[6] * ma[8]) / det;
+  dst[5] = ma[0] * ma[10] - ma[8] * ma[2] / det;
+  dst[6] = -(ma[0] * ma[6] - ma[4] * ma[2]) / det;
+  dst[8] = ma[4] * ma[9] - ma[8] * ma[5] / det;
+  dst[9] = -(ma[0] * ma[9] - ma[8] * ma[1]) / det;
+  dst[10] = ma[0] * ma[5] - ma[1] * ma[4] / det;
+  dst[3] = dst[7] = dst[11] = 0.f;
+}
+
+// _cldTestAxis (collision_cylinder_box.cpp:206-285)
+OG_HD int cb_test_axis(CylBox& D, const float* bR, float* n, int iAxis) {
+  const float fL = sqrtf(dot3(n, n));
+  if (fL < 1e-5f) return 1;
+  safe_normalize3(n);
+  const float fdot1 = dot3(D.caxis, n);
+  float frc;
+  if (fdot1 > 1.0f || fdot1 < -1.0f) frc = D.clen * 0.5f;
+  else frc = fabsf(fdot1 * (D.clen * 0.5f)) + D.crad * sqrtf(1.0f - (fdot1 * fdot1));
+  float frb = 0.f;
+  for (int j = 0; j < 3; ++j) {
+    const float col[3] = {bR[j], bR[4 + j], bR[8 + j]};
+    frb += fabsf(dot3(col, n)) * D.bhalf[j];
+  }
+  const float fd = dot3(D.diff, n);
+  float fDepth = frc + frb;
+  if (fabsf(fd) > fDepth) return 0;
+  fDepth -= fabsf(fd);
+  if (fDepth < D.best_depth) {
+    D.best_depth = fDepth;
+    D.normal[0] = n[0]; D.normal[1] = n[1]; D.normal[2] = n[2];
+    D.best_axis = iAxis;
+    D.best_rb = frb;
+    D.best_rc = frc;
+    if (fd > 0.f) { D.normal[0] = -D.normal[0]; D.normal[1] = -D.normal[1]; D.normal[2] = -D.normal[2]; }
+  }
+  return 1;
+}
+
+// _cldTestEdgeCircleAxis (collision_cylinder_box.cpp:289-333)
+OG_HD int cb_test_edge_circle(CylBox& D, const float* bR, const float* cc, const float* v0, const float* v1,
+                              int iAxis) {
+  float e[3] = {v1[0] - v0[0], v1[1] - v0[1], v1[2] - v0[2]};
+  safe_normalize3(e);
+  const float fdot2 = dot3(e, D.caxis);
+  if (fabsf(fdot2) < 1e-5f) return 1;
+  float t1[3] = {cc[0] - v0[0], cc[1] - v0[1], cc[2] - v0[2]};
+  const float fdot1 = dot3(t1, D.caxis);
+  float p[3];
+  for (int i = 0; i < 3; ++i) p[i] = v0[i] + e[i] * (fdot1 / fdot2);
+  float tn[3], ax[3];
+  for (int i = 0; i < 3; ++i) t1[i] = cc[i] - p[i];
+  cross3(tn, t1, D.caxis);
+  cross3(ax, tn, e);
+  return cb_test_axis(D, bR, ax, iAxis);
+}
+
+// dClipEdgeToPlane (ode/src/collision_util.cpp:471-510)
+OG_HD int cb_clip_edge(float* e0, float* e1, const float* pl) {
+  const float d0 = pl[0] * e0[0] + pl[1] * e0[1] + pl[2] * e0[2] + pl[3];
+  const float d1 = pl[0] * e1[0] + pl[1] * e1[1] + pl[2] * e1[2] + pl[3];
+  if (d0 < 0.f && d1 < 0.f) return 0;
+  if (d0 > 0.f && d1 > 0.f) return 1;
+  if ((d0 > 0.f && d1 < 0.f) || (d0 < 0.f && d1 > 0.f)) {
+    float ip[3];
+    for (int i = 0; i < 3; ++i) ip[i] = e0[i] - (e0[i] - e1[i]) * d0 / (d0 - d1);
+    float* dst = (d0 < 0.f) ? e0 : e1;
+    dst[0] = ip[0]; dst[1] = ip[1]; dst[2] = ip[2];
+  }
+  return 1;
+}
+
+// dClipPolyToPlane (ode/src/collision_util.cpp:512-553); points beyond the
+// reference's 16-entry buffers (MAX_CYLBOX_CLIP_POINTS) are dropped.
+constexpr int kCylBoxClip = 16;
+OG_HD int cb_clip_poly(const float (*in)[3], int nin, float (*out)[3], const float* pl) {
+  int n = 0;
+  for (int i1 = 0, i0 = nin - 1; i1 < nin; i0 = i1, i1++) {
+    const float d0 = pl[0] * in[i0][0] + pl[1] * in[i0][1] + pl[2] * in[i0][2] + pl[3];
+    const float d1 = pl[0] * in[i1][0] + pl[1] * in[i1][1] + pl[2] * in[i1][2] + pl[3];
+    if (d0 >= 0.f && n < kCylBoxClip) { out[n][0] = in[i0][0]; out[n][1] = in[i0][1]; out[n][2] = in[i0][2]; n++; }
+    if (((d0 > 0.f && d1 < 0.f) || (d0 < 0.f && d1 > 0.f)) && n < kCylBoxClip) {
+      for (int i = 0; i < 3; ++i) out[n][i] = in[i0][i] - (in[i0][i] - in[i1][i]) * d0 / (d0 - d1);
+      n++;
+    }
+  }
+  return n;
+}
+
+#if defined(__CUDACC__)
+#define OG_HD_OUTLINE static __host__ __device__ __noinline__
+#else
+#define OG_HD_OUTLINE static
+#endif
+OG_HD_OUTLINE int collide_cylinder_box(const GeomView& cy, const GeomView& bx, unsigned flags, Contact* c) {
+  const int maxc = (int)(flags & 0xffff);
+  const float* cR = cy.R;
+  const float* bR = bx.R;
+  CylBox D;
+  // _cldInitCylinderBox (:100-203)
+  for (int i = 0; i < 3; ++i) { D.cpos[i] = cy.pos[i]; D.caxis[i] = cR[i * 4 + 2]; D.bhalf[i] = bx.p[i] * 0.5f; }
+  D.crad = cy.p[0];
+  D.clen = cy.p[1];
+  for (int k = 0; k < 8; ++k) {
+    // vertex signs: (-,+,-) (+,+,-) (-,-,-) (+,-,-) (+,+,+) (+,-,+) (-,-,+) (-,+,+)
+    const float sx = (0x3Au >> k) & 1u ? 1.f : -1.f;
+    const float sy = (0x93u >> k) & 1u ? 1.f : -1.f;
+    const float sz = (k >= 4) ? 1.f : -1.f;
+    const float v[3] = {sx * D.bhalf[0], sy * D.bhalf[1], sz * D.bhalf[2]};
+    float w[3];
+    mul0_331(w, bR, v);
+    for (int i = 0; i < 3; ++i) D.bv[k][i] = w[i] + bx.pos[i];
+  }
+  for (int i = 0; i < 3; ++i) D.diff[i] = D.cpos[i] - bx.pos[i];
+  // _cldTestSeparatingAxes (:336-574)
+  D.best_depth = INFINITY;
+  D.best_axis = 0;
+  D.best_rb = D.best_rc = 0.f;
+  D.normal[0] = D.normal[1] = D.normal[2] = 0.f;
+  float ax[3];
+  for (int j = 0; j < 3; ++j) {
+    ax[0] = bR[j]; ax[1] = bR[4 + j]; ax[2] = bR[8 + j];
+    if (!cb_test_axis(D, bR, ax, 1 + j)) return 0;
+  }
+  ax[0] = D.caxis[0]; ax[1] = D.caxis[1]; ax[2] = D.caxis[2];
+  if (!cb_test_axis(D, bR, ax, 4)) return 0;
+  for (int j = 0; j < 3; ++j) {
+    const float col[3] = {bR[j], bR[4 + j], bR[8 + j]};
+    cross3(ax, D.caxis, col);
+    if (dot3(ax, ax) > 1e-6f && !cb_test_axis(D, bR, ax, 5 + j)) return 0;
+  }
+  for (int k = 0; k < 8; ++k) {
+    float t1[3] = {D.bv[k][0] - D.cpos[0], D.bv[k][1] - D.cpos[1], D.bv[k][2] - D.cpos[2]}, t2[3];
+    cross3(t2, D.caxis, t1);
+    cross3(ax, D.caxis, t2);
+    if (dot3(ax, ax) > 1e-6f && !cb_test_axis(D, bR, ax, 8 + k)) return 0;
+  }
+  // box edges (vertex pairs) against the top rim, then the bottom rim
+  const unsigned char edges[12][2] = {{1, 0}, {1, 3}, {2, 3}, {2, 0}, {4, 1}, {4, 7},
+                                      {0, 7}, {5, 3}, {5, 6}, {2, 6}, {4, 5}, {6, 7}};
+  for (int side = 0; side < 2; ++side) {
+    float cc[3];
+    for (int i = 0; i < 3; ++i)
+      cc[i] = (side == 0) ? D.cpos[i] + D.caxis[i] * (D.clen * 0.5f) : D.cpos[i] - D.caxis[i] * (D.clen * 0.5f);
+    for (int e = 0; e < 12; ++e)
+      if (!cb_test_edge_circle(D, bR, cc, D.bv[edges[e][0]], D.bv[edges[e][1]], 16 + 12 * side + e)) return 0;
+  }
+  if (D.best_axis == 0) return 0;
+  int n = 0;
+  if (fabsf(dot3(D.normal, D.caxis)) < 0.9f) {
+    // _cldClipCylinderToBox (:576-717)
+    const float t = dot3(D.caxis, D.normal);
+    float vN[3];
+    for (int i = 0; i < 3; ++i) vN[i] = D.normal[i] - D.caxis[i] * t;
+    safe_normalize3(vN);
+    float e0[3], e1[3];
+    for (int i = 0; i < 3; ++i) {
+      const float ct = D.cpos[i] + vN[i] * D.crad;
+      e0[i] = ct + D.caxis[i] * (D.clen * 0.5f);
+      e1[i] = ct - D.caxis[i] * (D.clen * 0.5f);
+    }
+    for (int i = 0; i < 3; ++i) { e0[i] -= bx.pos[i]; e1[i] -= bx.pos[i]; }
+    for (int neg = 0; neg < 2; ++neg)
+      for (int j = 0; j < 3; ++j) {
+        float pl[4] = {bR[j], bR[4 + j], bR[8 + j], D.bhalf[j]};
+        if (neg) { pl[0] = -pl[0]; pl[1] = -pl[1]; pl[2] = -pl[2]; }
+        if (!cb_clip_edge(e0, e1, pl)) return 0;
+      }
+    float d0 = D.best_rb + dot3(e0, D.normal);
+    float d1 = D.best_rb + dot3(e1, D.normal);
+    if (d0 < 0.f) d0 = 0.f;
+    if (d1 < 0.f) d1 = 0.f;
+    for (int i = 0; i < 3; ++i) { e0[i] += bx.pos[i]; e1[i] += bx.pos[i]; }
+    c[n].depth = d0;
+    for (int i = 0; i < 3; ++i) { c[n].normal[i] = -D.normal[i]; c[n].pos[i] = e0[i]; }
+    n++;
+    if (n != maxc) {
+      c[n].depth = d1;
+      for (int i = 0; i < 3; ++i) { c[n].normal[i] = -D.normal[i]; c[n].pos[i] = e1[i]; }
+      n++;
+    }
+    return n;
+  }
+  // _cldClipBoxToCylinder (:720-983)
+  float ccp[3], cn_z;
+  if (dot3(D.caxis, D.normal) > 0.f) {
+    for (int i = 0; i < 3; ++i) ccp[i] = D.cpos[i] + D.caxis[i] * (D.clen * 0.5f);
+    cn_z = -1.0f;
+  } else {
+    for (int i = 0; i < 3; ++i) ccp[i] = D.cpos[i] - D.caxis[i] * (D.clen * 0.5f);
+    cn_z = 1.0f;
+  }
+  float inv[12], vNr[3];
+  cb_mat3_inv(bR, inv);
+  mul0_331(vNr, inv, D.normal);
+  const float an[3] = {fabsf(vNr[0]), fabsf(vNr[1]), fabsf(vNr[2])};
+  int iB0, iB1, iB2;
+  if (an[1] > an[0]) {
+    if (an[0] > an[2]) { iB0 = 1; iB1 = 0; iB2 = 2; }
+    else if (an[1] > an[2]) { iB0 = 1; iB1 = 2; iB2 = 0; }
+    else { iB0 = 2; iB1 = 1; iB2 = 0; }
+  } else {
+    if (an[1] > an[2]) { iB0 = 0; iB1 = 1; iB2 = 2; }
+    else if (an[0] > an[2]) { iB0 = 0; iB1 = 2; iB2 = 1; }
+    else { iB0 = 2; iB1 = 0; iB2 = 1; }
+  }
+  float ctr[3];
+  for (int i = 0; i < 3; ++i) {
+    const float col = bR[i * 4 + iB0];
+    ctr[i] = (vNr[iB0] > 0.f) ? bx.pos[i] - D.bhalf[iB0] * col : bx.pos[i] + D.bhalf[iB0] * col;
+  }
+  float A1[kCylBoxClip][3], A2[kCylBoxClip][3], pts[4][3];
+  const float h1 = D.bhalf[iB1], h2 = D.bhalf[iB2];
+  for (int i = 0; i < 3; ++i) {
+    const float a1 = bR[i * 4 + iB1], a2 = bR[i * 4 + iB2];
+    pts[0][i] = ctr[i] + h1 * a1 - h2 * a2;
+    pts[1][i] = ctr[i] - h1 * a1 - h2 * a2;
+    pts[2][i] = ctr[i] - h1 * a1 + h2 * a2;
+    pts[3][i] = ctr[i] + h1 * a1 + h2 * a2;
+  }
+  cb_mat3_inv(cR, inv);
+  for (int k = 0; k < 4; ++k) {
+    const float t[3] = {pts[k][0] - ccp[0], pts[k][1] - ccp[1], pts[k][2] - ccp[2]};
+    mul0_331(pts[k], inv, t);
+  }
+  float pl[4] = {0.f, 0.f, cn_z, 0.f};
+  int n1 = cb_clip_poly(pts, 4, A1, pl), n2 = 0;
+  // the rim as an octagon: plane normals -(cos, sin) of pi/8 + k pi/4
+  float ang = (float)(3.14159265358979323846 / 8);
+  const float inc = ang * 2.0f;
+  for (int seg = 0; seg < 8; ++seg) {
+    pl[0] = -cosf(ang); pl[1] = -sinf(ang); pl[2] = 0.f; pl[3] = D.crad;
+    ang += inc;
+    if (seg % 2 == 0) n2 = cb_clip_poly(A1, n1, A2, pl);
+    else n1 = cb_clip_poly(A2, n2, A1, pl);
+  }
+  for (int k = 0; k < n1; ++k) {   // after 8 segments the result is in A1
+    float p[3];
+    mul0_331(p, cR, A1[k]);
+    for (int i = 0; i < 3; ++i) p[i] += ccp[i];
+    const float t[3] = {p[0] - D.cpos[0], p[1] - D.cpos[1], p[2] - D.cpos[2]};
+    const float dep = D.best_rc - dot3(t, D.normal);
+    if (dep > 0.f) {
+      c[n].depth = dep;
+      for (int i = 0; i < 3; ++i) { c[n].normal[i] = -D.normal[i]; c[n].pos[i] = p[i]; }
+      if (++n == maxc) break;
+    }
+  }
+  return n;
+}
+
 // Collider table for this path (ode/src/collision_kernel.cpp:167-268): returns
 // a collider id and whether the call runs with the geoms swapped (in which case
 // dCollide negates the normals, :319-335).
 enum { CL_NONE = 0, CL_SS, CL_SB, CL_SP, CL_BB, CL_BP, CL_CP, CL_HF, CL_CS, CL_CB, CL_CC,
-       CL_RS, CL_RB, CL_RC, CL_RP };
+       CL_RS, CL_RB, CL_RC, CL_RP, CL_YS, CL_YB, CL_YP, CL_RY };
 OG_HD int collider_of(int t1, int t2, int* reverse) {
   *reverse = 0;
   auto is = [&](int a, int b) { return t1 == a && t2 == b; };
@@ -898,7 +1345,18 @@ OG_HD int collider_of(int t1, int t2, int* reverse) {
   if (is(G_CAPSULE, G_RAY)) { *reverse = 1; return CL_RC; }
   if (is(G_RAY, G_PLANE)) return CL_RP;
   if (is(G_PLANE, G_RAY)) { *reverse = 1; return CL_RP; }
-  auto hf_other = [](int t) { return t == G_SPHERE || t == G_BOX || t == G_CAPSULE || t == G_RAY; };
+  // cylinder-cylinder and capsule-cylinder need libccd (collision_kernel.cpp:215-220): no collider
+  if (is(G_CYLINDER, G_SPHERE)) return CL_YS;
+  if (is(G_SPHERE, G_CYLINDER)) { *reverse = 1; return CL_YS; }
+  if (is(G_CYLINDER, G_BOX)) return CL_YB;
+  if (is(G_BOX, G_CYLINDER)) { *reverse = 1; return CL_YB; }
+  if (is(G_CYLINDER, G_PLANE)) return CL_YP;
+  if (is(G_PLANE, G_CYLINDER)) { *reverse = 1; return CL_YP; }
+  if (is(G_RAY, G_CYLINDER)) return CL_RY;
+  if (is(G_CYLINDER, G_RAY)) { *reverse = 1; return CL_RY; }
+  auto hf_other = [](int t) {
+    return t == G_SPHERE || t == G_BOX || t == G_CAPSULE || t == G_CYLINDER || t == G_RAY;
+  };
   if (t1 == G_HEIGHTFIELD && hf_other(t2)) return CL_HF;
   if (t2 == G_HEIGHTFIELD && hf_other(t1)) { *reverse = 1; return CL_HF; }
   return CL_NONE;
@@ -928,6 +1386,10 @@ OG_HD int collide_primitive(const GeomView& g1, const GeomView& g2, unsigned fla
     case CL_RB: n = collide_ray_box(a, b, c); break;
     case CL_RC: n = collide_ray_capsule(a, b, c); break;
     case CL_RP: n = collide_ray_plane(a, b, c); break;
+    case CL_YS: n = collide_cylinder_sphere(a, b, c); break;
+    case CL_YB: n = collide_cylinder_box(a, b, flags, c); break;
+    case CL_YP: n = collide_cylinder_plane(a, b, flags, c); break;
+    case CL_RY: n = collide_ray_cylinder(a, b, c); break;
     default: n = 0;
   }
   if (rev)

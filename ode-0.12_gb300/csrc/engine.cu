@@ -482,6 +482,7 @@ static float bound_radius(int type, const double* p) {
     case ODEGPU_GEOM_SPHERE: return (float)p[0];
     case ODEGPU_GEOM_BOX: return (float)(0.5 * std::sqrt(p[0] * p[0] + p[1] * p[1] + p[2] * p[2]));
     case ODEGPU_GEOM_CAPSULE: return (float)(p[0] + 0.5 * p[1]);
+    case ODEGPU_GEOM_CYLINDER: return (float)std::sqrt(p[0] * p[0] + 0.25 * p[1] * p[1]);
     default: return INFINITY;
   }
 }
@@ -722,7 +723,7 @@ int odegpuBatchCreate(const odegpuScene* sc, const odegpuBatchConfig* cfg, odegp
       delete B;
       return fail(ODEGPU_E_ARG, "a scene may not hold a ray geom: rays are queries (odegpuBatchRayCast)");
     } else if (gtype[g] != ODEGPU_GEOM_SPHERE && gtype[g] != ODEGPU_GEOM_BOX &&
-               gtype[g] != ODEGPU_GEOM_CAPSULE) {
+               gtype[g] != ODEGPU_GEOM_CAPSULE && gtype[g] != ODEGPU_GEOM_CYLINDER) {
       delete B;
       return fail(ODEGPU_E_ARG, "unsupported geom class " + std::to_string(gtype[g]));
     }

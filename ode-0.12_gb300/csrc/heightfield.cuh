@@ -67,8 +67,8 @@ OG_D bool hf_on_triangle(const DevHeightfield& H, const float* corner, int cx, i
   return (maxz - pos[2]) <= (pos[0] - minx) * H.zx;
 }
 
-// computeAABB of sphere / box / capsule / ray (sphere.cpp:59-67,
-// box.cpp:60-78, capsule.cpp:60-74, ray.cpp:56-89)
+// computeAABB of sphere / box / capsule / cylinder / ray (sphere.cpp:59-67,
+// box.cpp:60-78, capsule.cpp:60-74, cylinder.cpp:58-73, ray.cpp:56-89)
 OG_D void geom_aabb(const GeomView& g, float* aabb) {
   const float* R = g.R;
   float xr, yr, zr;
@@ -82,6 +82,10 @@ OG_D void geom_aabb(const GeomView& g, float* aabb) {
   }
   if (g.type == G_SPHERE) {
     xr = yr = zr = g.p[0];
+  } else if (g.type == G_CYLINDER) {   // cylinder.cpp:58-73
+    xr = fabsf(R[0] * g.p[0]) + fabsf(R[1] * g.p[0]) + 0.5f * fabsf(R[2] * g.p[1]);
+    yr = fabsf(R[4] * g.p[0]) + fabsf(R[5] * g.p[0]) + 0.5f * fabsf(R[6] * g.p[1]);
+    zr = fabsf(R[8] * g.p[0]) + fabsf(R[9] * g.p[0]) + 0.5f * fabsf(R[10] * g.p[1]);
   } else if (g.type == G_BOX) {
     xr = 0.5f * (fabsf(R[0] * g.p[0]) + fabsf(R[1] * g.p[1]) + fabsf(R[2] * g.p[2]));
     yr = 0.5f * (fabsf(R[4] * g.p[0]) + fabsf(R[5] * g.p[1]) + fabsf(R[6] * g.p[2]));
@@ -143,6 +147,7 @@ OG_D int geom_plane_collide(const GeomView& g, const GeomView& pl, unsigned flag
   if (g.type == G_SPHERE) return collide_sphere_plane(g, pl, c);
   if (g.type == G_BOX) return collide_box_plane(g, pl, flags, c);
   if (g.type == G_RAY) return collide_ray_plane(g, pl, c);
+  if (g.type == G_CYLINDER) return collide_cylinder_plane(g, pl, flags, c);
   return collide_capsule_plane(g, pl, flags, c);
 }
 
@@ -327,8 +332,27 @@ OG_D int hf_zone(const DevHeightfield& H, const float* heights, int minX, int ma
         if (vstate[vi]) continue;
         float v[3];
         vtx(vi, v);
-        const float depth = geom_point_depth(g, v);
-        if (depth > kHFEps) {
+        float depth;
+        bool hit;
+        if (g.type == G_CYLINDER) {
+          // no point-depth function for cylinders: a ray from the vertex along
+          // the triangle's normal, of length (minO2 - y) * 1000, gives the
+          // depth (heightfield.cpp:1562-1584)
+          GeomView ray;
+          ray.type = G_RAY;
+          ray.pos[0] = v[0]; ray.pos[1] = v[1]; ray.pos[2] = v[2];
+          for (int q = 0; q < 12; ++q) ray.R[q] = 0.f;
+          ray.R[2] = tp[k].x; ray.R[6] = tp[k].y; ray.R[10] = tp[k].z;
+          ray.p[0] = (minO2 - v[1]) * 1000.0f;
+          ray.p[1] = ray.p[2] = ray.p[3] = 0.f;
+          Contact rc;
+          hit = collide_ray_cylinder(ray, g, &rc) != 0;
+          depth = rc.depth;
+        } else {
+          depth = geom_point_depth(g, v);
+          hit = depth > kHFEps;
+        }
+        if (hit) {
           Contact& o = out[nc];
           o.pos[0] = v[0]; o.pos[1] = v[1]; o.pos[2] = v[2];
           o.normal[0] = -tp[k].x; o.normal[1] = -tp[k].y; o.normal[2] = -tp[k].z;

@@ -347,7 +347,7 @@ __global__ void __launch_bounds__(128) lw_narrow_kernel(BatchDev d, LWDev L) {
     const bool rev = vk.type == G_HEIGHTFIELD;
     const GeomView& hv = rev ? vk : vi;
     const GeomView& ov = rev ? vi : vk;
-    if (ov.type == G_SPHERE || ov.type == G_BOX || ov.type == G_CAPSULE) {
+    if (ov.type == G_SPHERE || ov.type == G_BOX || ov.type == G_CAPSULE || ov.type == G_CYLINDER) {
       cnt = collide_heightfield(d.hfs[(int)hv.p[0]], d.hf_heights, ov, (unsigned)D.max_contacts, cc, nullptr);
       if (cnt < 0) { atomicOr(&d.status[0], ST_HF_ZONE); cnt = 0; }
       if (rev)

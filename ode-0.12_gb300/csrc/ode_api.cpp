@@ -342,6 +342,43 @@ void dMassSetBoxTotal(dMass* m, dReal total, dReal lx, dReal ly, dReal lz) {
 void dMassSetBox(dMass* m, dReal density, dReal lx, dReal ly, dReal lz) {
   dMassSetBoxTotal(m, lx * ly * lz * density, lx, ly, lz);
 }
+void dMassAdjust(dMass* m, dReal newmass) {
+  // ode/src/mass.cpp:441-451
+  const dReal scale = newmass / m->mass;
+  m->mass = newmass;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) m->I[i * 4 + j] *= scale;
+}
+void dMassSetCapsule(dMass* m, dReal density, int direction, dReal radius, dReal length) {
+  // ode/src/mass.cpp:140-165: cylinder part plus the two hemispherical caps
+  if (direction < 1 || direction > 3) return;
+  dMassSetZero(m);
+  const dReal M1 = (dReal)(M_PI * radius * radius * length * density);
+  const dReal M2 = (dReal)((4.0f / 3.0f) * M_PI * radius * radius * radius * density);
+  m->mass = M1 + M2;
+  const dReal Ia = M1 * (0.25f * radius * radius + (1.0f / 12.0f) * length * length) +
+                   M2 * (0.4f * radius * radius + 0.375f * radius * length + 0.25f * length * length);
+  const dReal Ib = (M1 * 0.5f + M2 * 0.4f) * radius * radius;
+  m->I[0] = m->I[5] = m->I[10] = Ia;
+  m->I[(direction - 1) * 5] = Ib;
+}
+void dMassSetCapsuleTotal(dMass* m, dReal total_mass, int direction, dReal radius, dReal length) {
+  dMassSetCapsule(m, 1.0f, direction, radius, length);
+  dMassAdjust(m, total_mass);
+}
+void dMassSetCylinderTotal(dMass* m, dReal total_mass, int direction, dReal radius, dReal length) {
+  // ode/src/mass.cpp:180-200
+  if (direction < 1 || direction > 3) return;
+  dMassSetZero(m);
+  const dReal r2 = radius * radius;
+  m->mass = total_mass;
+  const dReal I = total_mass * (0.25f * r2 + (1.0f / 12.0f) * length * length);
+  m->I[0] = m->I[5] = m->I[10] = I;
+  m->I[(direction - 1) * 5] = total_mass * 0.5f * r2;
+}
+void dMassSetCylinder(dMass* m, dReal density, int direction, dReal radius, dReal length) {
+  dMassSetCylinderTotal(m, (dReal)(M_PI * radius * radius * length * density), direction, radius, length);
+}
 
 // ---------------------------------------------------------------- joints
 dJointID dJointCreateBall(dWorldID w, dJointGroupID g) { return new_joint(w, g, dJointTypeBall); }
@@ -869,6 +906,16 @@ dGeomID dCreateCapsule(dSpaceID, dReal r, dReal len) {
   const double p[4] = {r, len, 0, 0};
   return new_geom(dCapsuleClass, p);
 }
+dGeomID dCreateCylinder(dSpaceID, dReal r, dReal len) {
+  const double p[4] = {r, len, 0, 0};
+  return new_geom(dCylinderClass, p);
+}
+void dGeomCylinderSetParams(dGeomID g, dReal r, dReal len) {
+  if (g && g->type == dCylinderClass) { g->p[0] = r; g->p[1] = len; }
+}
+void dGeomCylinderGetParams(dGeomID g, dReal* r, dReal* l) {
+  if (g && g->type == dCylinderClass) { *r = (dReal)g->p[0]; *l = (dReal)g->p[1]; }
+}
 dGeomID dCreatePlane(dSpaceID, dReal a, dReal b, dReal c, dReal d) {
   // make_sure_plane_normal_has_unit_length (ode/src/plane.cpp:40-56)
   double p[4] = {a, b, c, d};
@@ -992,7 +1039,7 @@ int dCollide(dGeomID o1, dGeomID o2, int flags, dContactGeom* contact, int skip)
     const dxGeom* hg = rev ? o2 : o1;
     const dxGeom* og2 = rev ? o1 : o2;
     if (og2->type != dSphereClass && og2->type != dBoxClass && og2->type != dCapsuleClass &&
-        og2->type != dRayClass)
+        og2->type != dCylinderClass && og2->type != dRayClass)
       return 0;
     if (!hg->hf || !hg->hf->built) return 0;
     double hpos[3] = {0, 0, 0}, hR[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};

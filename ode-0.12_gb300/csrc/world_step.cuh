@@ -194,7 +194,7 @@ OG_D int phase_collide(const BatchDev& d, const WorldDesc& D, int w, const WarpS
         const bool rev = vk.type == G_HEIGHTFIELD;
         const GeomView& hv = rev ? vk : vi;
         const GeomView& ov = rev ? vi : vk;
-        if (ov.type == G_SPHERE || ov.type == G_BOX || ov.type == G_CAPSULE) {
+        if (ov.type == G_SPHERE || ov.type == G_BOX || ov.type == G_CAPSULE || ov.type == G_CYLINDER) {
           cnt = collide_heightfield(d.hfs[(int)hv.p[0]], d.hf_heights, ov, (unsigned)D.max_contacts, cc, &kinds);
           if (cnt < 0) { atomicOr(&d.status[w], ST_HF_ZONE); cnt = 0; }
           if (rev)

@@ -16,7 +16,7 @@ import math
 
 import numpy as np
 
-GEOM_SPHERE, GEOM_BOX, GEOM_CAPSULE, GEOM_PLANE, GEOM_HEIGHTFIELD = 0, 1, 2, 4, 9
+GEOM_SPHERE, GEOM_BOX, GEOM_CAPSULE, GEOM_CYLINDER, GEOM_PLANE, GEOM_RAY, GEOM_HEIGHTFIELD = 0, 1, 2, 3, 4, 5, 9
 JOINT_BALL, JOINT_HINGE, JOINT_SLIDER, JOINT_CONTACT, JOINT_UNIVERSAL, JOINT_HINGE2, JOINT_FIXED = \
     1, 2, 3, 4, 5, 6, 7
 JOINT_AMOTOR = 9
@@ -112,6 +112,13 @@ def capsule_mass(density, r, length):
         M2 * (0.4 * r * r + 0.375 * r * length + 0.25 * length * length)
     Iz = (0.5 * M1 + 0.4 * M2) * r * r
     return m, np.diag([Ia, Ia, Iz])
+
+
+def cylinder_mass(density, r, length):
+    """dMassSetCylinder (ode/src/mass.cpp:173-200) with the axis along z."""
+    m = math.pi * r * r * length * density
+    i = m * (0.25 * r * r + length * length / 12.0)
+    return m, np.diag([i, i, 0.5 * m * r * r])
 
 
 def sphere_mass_total(m, r):
@@ -570,6 +577,52 @@ def capsule_mix(seed=6, n_bodies=12):
             m, I = box_mass(1000.0, lx, ly, lz)
             bi = b.add_body(w, (x, y, z), m, I, q=tuple(qv))
             b.add_geom(w, GEOM_BOX, bi, (lx, ly, lz), s)
+    return b.build()
+
+
+def cylinder_pile(seed=21, n_bodies=14, n_worlds=2):
+    """Cylinders (r U[0.1,0.3], length U[0.2,0.8]), spheres and boxes dropped
+    into a 1.6 x 1.6 m column, density 1000, same surface as box_drop. World 0
+    lands on plane z=0; world 1 on a seeded 32 x 32 fractal heightfield (0.25
+    m spacing, heights sigma 0.15) placed with its up axis along world z.
+    Covers cylinder-sphere, cylinder-box, cylinder-plane and
+    heightfield-cylinder (the field's vertex pass casts rays into the
+    cylinder); cylinder-cylinder has no collider without libccd, so cylinders
+    pass through each other as in the reference."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    b = SceneBuilder()
+    s = _std_surface(b, 0.5)
+    hf = None
+    for wi in range(n_worlds):
+        w = b.new_world(cfm=1e-5, seed=seed + wi)
+        if wi % 2 == 0:
+            b.add_geom(w, GEOM_PLANE, -1, (0, 0, 1, 0), s)
+        else:
+            if hf is None:
+                h = fractal_heights(32, 0.15, seed=seed)
+                hf = b.add_heightfield(h, 0.25 * 31, 0.25 * 31, thickness=1.0, pos=(0, 0, 0), R=np.array(HF_Z_UP))
+            b.add_geom(w, GEOM_HEIGHTFIELD, -1, (hf,), s)
+        for k in range(n_bodies):
+            x, y = rng.uniform(-0.8, 0.8, 2)
+            z = 0.6 + 0.45 * k + rng.uniform(0, 0.2)
+            qv = rng.normal(size=4)
+            qv /= np.linalg.norm(qv)
+            kind = k % 3
+            if kind == 0 or kind == 2 and k % 2:
+                r, L = rng.uniform(0.1, 0.3), rng.uniform(0.2, 0.8)
+                m, I = cylinder_mass(1000.0, r, L)
+                bi = b.add_body(w, (x, y, z), m, I, q=tuple(qv))
+                b.add_geom(w, GEOM_CYLINDER, bi, (r, L), s)
+            elif kind == 1:
+                r = rng.uniform(0.1, 0.3)
+                m, I = sphere_mass(1000.0, r)
+                bi = b.add_body(w, (x, y, z), m, I, q=tuple(qv))
+                b.add_geom(w, GEOM_SPHERE, bi, (r,), s)
+            else:
+                lx, ly, lz = rng.uniform(0.2, 0.6, 3)
+                m, I = box_mass(1000.0, lx, ly, lz)
+                bi = b.add_body(w, (x, y, z), m, I, q=tuple(qv))
+                b.add_geom(w, GEOM_BOX, bi, (lx, ly, lz), s)
     return b.build()
 
 

@@ -31,6 +31,7 @@ SCENES = {
     "vehicles": (lambda: S.vehicles(n_worlds=3, steps=60, hf_samples=64), 60),
     "capsule_pile": (lambda: S.capsule_pile(), 120),
     "mechanisms": (lambda: S.mechanisms(n_worlds=3, steps=80), 80),
+    "cylinder_pile": (lambda: S.cylinder_pile(), 120),
 }
 KEEP = 10  # keep the state every KEEP steps
 
@@ -375,6 +376,65 @@ def make_cylinder_kats(n=150, seed=777):
         hf_nc=np.array([r[4] for r in hrecs]), hf_out=np.array([r[5] for r in hrecs]))
 
 
+def add_single_outputs(name, hf_class=None):
+    """Adds the reference's dSINGLE (FP32) outputs of the same dCollide calls to
+    a known-answer fixture (nc_s / out_s, and hf_nc_s / hf_out_s for its
+    heightfield calls): the bar for the FP32 path, whose colliders keep the
+    FP32 build's tolerances (collision_cylinder_*.cpp "toleranz", dEpsilon)."""
+    import ctypes as C
+    path = os.path.join(HERE, f"{name}.npz")
+    g = dict(np.load(path))
+    ref = O.ref("s")
+    P = C.POINTER(C.c_double)
+    n = len(g["t1"]) if "t1" in g else 0
+    nc_s, out_s = np.zeros(n, np.int64), np.zeros((n, 8, 9))
+    # and every contact the collider can give (16 asked for): where a tie
+    # picks which of several equally deep points come first, the FP32 path
+    # may return other points of the same set
+    nc_all, out_all = np.zeros(n, np.int64), np.zeros((n, 16, 9))
+    for k in range(n):
+        out = np.zeros((16, 9))
+        args = [np.ascontiguousarray(g[x][k], dtype=np.float64) for x in ("p1", "pos1", "R1", "p2", "pos2", "R2")]
+        nc_s[k] = ref.ref_collide(int(g["t1"][k]), *(a.ctypes.data_as(P) for a in args[:3]), int(g["t2"][k]),
+                                  *(a.ctypes.data_as(P) for a in args[3:]), int(g["flags"][k]), out.ctypes.data_as(P))
+        out_s[k] = out[:8]
+        out = np.zeros((16, 9))
+        nc_all[k] = ref.ref_collide(int(g["t1"][k]), *(a.ctypes.data_as(P) for a in args[:3]), int(g["t2"][k]),
+                                    *(a.ctypes.data_as(P) for a in args[3:]), (int(g["flags"][k]) & ~0xffff) | 16,
+                                    out.ctypes.data_as(P))
+        out_all[k] = out
+    if n:
+        g["nc_s"], g["out_s"] = nc_s, out_s
+        g["nc_s_all"], g["out_s_all"] = nc_all, out_all
+    hkey = "hf_nc" if "hf_nc" in g else ("nc" if name == "hf_kats" else None)
+    if hkey:
+        pre = "hf_" if hkey == "hf_nc" else ""
+        hg = np.load(os.path.join(HERE, "hf_kats.npz"))
+        h = np.ascontiguousarray(hg["heights"])
+        sp = float(hg["spacing"])
+        H = S.Heightfield()
+        H.nz, H.nx = h.shape
+        H.width, H.depth = sp * (H.nx - 1), sp * (H.nz - 1)
+        H.scale, H.offset, H.thickness, H.wrap = 1.0, 0.0, 1.0, 0
+        H.heights = h.ctypes.data_as(P)
+        H.pos[:] = [float(x) for x in hg["hf_pos"]]
+        H.R[:] = [float(x) for x in hg["hf_R"]]
+        f = ref.ref_collide_hf
+        f.restype = C.c_int
+        f.argtypes = [C.c_void_p, C.c_int, P, P, P, C.c_int, P]
+        m = len(g[hkey])
+        hn, ho = np.zeros(m, np.int64), np.zeros((m, 8, 9))
+        for k in range(m):
+            out = np.zeros((64, 9))
+            t2 = hf_class if hf_class is not None else int(g["t2"][k])
+            args = [np.ascontiguousarray(g[pre + x][k], dtype=np.float64) for x in ("p2", "pos2", "R2")]
+            hn[k] = f(C.byref(H), t2, *(a.ctypes.data_as(P) for a in args), int(g[pre + "flags"][k]),
+                      out.ctypes.data_as(P))
+            ho[k] = out[:8]
+        g[pre + "nc_s"], g[pre + "out_s"] = hn, ho
+    np.savez_compressed(path, **g)
+
+
 def make_tower():
     """Non-chaotic stacks (boxes of decreasing size, aligned): FP64 reference
     states after 200 steps plus the reference's own FP32 (dSINGLE) build on the
@@ -412,6 +472,12 @@ if __name__ == "__main__":
                 make_ray_kats()
             elif name == "cylinder_kats":
                 make_cylinder_kats()
+                add_single_outputs("cylinder_kats", hf_class=3)
+            elif name == "single_outputs":
+                add_single_outputs("collider_kats")
+                add_single_outputs("hf_kats")
+                add_single_outputs("ray_kats", hf_class=5)
+                add_single_outputs("cylinder_kats", hf_class=3)
             else:
                 make_scene(name)
             print("wrote", name)
@@ -423,6 +489,10 @@ if __name__ == "__main__":
     make_hf_kats()
     make_ray_kats()
     make_cylinder_kats()
+    add_single_outputs("collider_kats")
+    add_single_outputs("hf_kats")
+    add_single_outputs("ray_kats", hf_class=5)
+    add_single_outputs("cylinder_kats", hf_class=3)
     make_rng_kat()
     make_tower()
     print("wrote collider_kats, rng_kat")

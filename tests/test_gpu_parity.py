@@ -38,6 +38,9 @@ def _scenes():
         # servo stops), universal, fixed (body-body and reversed) joints with
         # ball / fixed erp carried along an island
         "mechanisms": S.mechanisms(n_worlds=16, steps=40),
+        # cylinders on a plane and on a heightfield (cylinder-sphere / -box /
+        # -plane, heightfield-cylinder)
+        "cylinder_pile": S.cylinder_pile(n_worlds=4),
         # aligned equal boxes: exact SAT ties between parallel faces, which FP32
         # and FP64 break differently (ODE's own FP32 build drifts mm here)
         "stack": S.box_stack(n_worlds=4, height=5),
@@ -45,7 +48,7 @@ def _scenes():
 
 
 @pytest.mark.parametrize("name", ["box_drop", "batched", "hinge", "tower", "capsule", "capsule_pile",
-                                  "mechanisms"])
+                                  "mechanisms", "cylinder_pile"])
 def test_one_step_from_oracle_state(batch_cls, name):
     sc = _scenes()[name]
     n = 40

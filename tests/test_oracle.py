@@ -142,7 +142,7 @@ def test_ray_and_cylinder_kats_golden(fixture, hf_class):
 
 
 @pytest.mark.parametrize("name", ["box_drop", "batched", "hinge", "stack", "capsule", "vehicles", "capsule_pile",
-                                  "mechanisms"])
+                                  "mechanisms", "cylinder_pile"])
 def test_oracle_matches_reference_golden(name):
     """Whole-step parity: contact counts, contact records, RNG seeds, body
     states and joint feedback are bit-identical to the reference (FP64)."""
