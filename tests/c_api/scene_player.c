@@ -33,7 +33,7 @@
 #include "ode_gpu.h"
 #endif
 
-enum { SPHERE = 0, BOX = 1, CAPSULE = 2, PLANE = 4 };
+enum { SPHERE = 0, BOX = 1, CAPSULE = 2, CYLINDER = 3, PLANE = 4 };
 enum { BALL = 1, HINGE = 2, SLIDER = 3, UNIVERSAL = 5, HINGE2 = 6, FIXED = 7, AMOTOR = 9 };
 #define NPARAM 36
 
@@ -125,6 +125,7 @@ int main(int argc, char** argv) {
       case SPHERE: geom = dCreateSphere(0, p[0]); break;
       case BOX: geom = dCreateBox(0, p[0], p[1], p[2]); break;
       case CAPSULE: geom = dCreateCapsule(0, p[0], p[1]); break;
+      case CYLINDER: geom = dCreateCylinder(0, p[0], p[1]); break;
       case PLANE: geom = dCreatePlane(0, p[0], p[1], p[2], p[3]); break;
       default: return 2;
     }

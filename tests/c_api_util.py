@@ -48,7 +48,7 @@ def player_input(sc, w, steps, path):
         lines.append(f((*sc.body_pos[i], *sc.body_q[i], *sc.body_lvel[i], *sc.body_avel[i], sc.body_mass[i],
                         *sc.body_I[i], sc.body_flags[i])))
     for g in range(g0, g1):
-        assert sc.geom_type[g] in (0, 1, 2, 4), "scene_player takes sphere / box / capsule / plane geoms"
+        assert sc.geom_type[g] in (0, 1, 2, 3, 4), "scene_player takes sphere / box / capsule / cylinder / plane geoms"
         lines.append(f((sc.geom_type[g], sc.geom_body[g], sc.geom_surface[g], *sc.geom_param[g])))
     for j in range(j0, j1):
         lines.append(f((sc.joint_type[j], *sc.joint_body[j], *sc.joint_anchor[j], *sc.joint_axis1[j],

@@ -45,7 +45,7 @@ def test_demo_links_against_libodegpu():
 def test_scene_player_is_the_reference_harness_sequence():
     """tests/c_api/scene_player.c, built against the reference ODE 0.12
     (dSINGLE) where it was built in this checkout, reproduces the reference
-    harness bit for bit on the joint-type scene: the program the GPU test
+    harness bit for bit on the joint-type scene and the cylinder pile: the program the GPU test
     links against libodegpu is a faithful ODE program."""
     import c_api_util as U
     import numpy as np
@@ -53,15 +53,15 @@ def test_scene_player_is_the_reference_harness_sequence():
     from odegpu import scene as S
     if not (U.ref_demo_available() and O.ref_available("s")):
         pytest.skip("reference not built in this checkout")
-    sc = S.mechanisms(n_worlds=2, steps=60)
     with tempfile.TemporaryDirectory() as d:
         exe = U.build_ref_demo(os.path.join(d, "player"), src=U.PLAYER)
-        for w in range(sc.n_worlds):
-            inp = os.path.join(d, f"in{w}.txt")
-            U.player_input(sc, w, 60, inp)
-            st = U.run_demo(exe, inp).astype(np.float32).astype(np.float64)
-            ref = O.run_world(O.ref("s").ref_run_world, sc, w, 60)["state"][-1]
-            assert np.array_equal(st, ref), float(np.abs(st - ref).max())
+        for sc in (S.mechanisms(n_worlds=2, steps=60), S.cylinder_pile(n_worlds=1)):
+            for w in range(sc.n_worlds):
+                inp = os.path.join(d, f"in{w}.txt")
+                U.player_input(sc, w, 60, inp)
+                st = U.run_demo(exe, inp).astype(np.float32).astype(np.float64)
+                ref = O.run_world(O.ref("s").ref_run_world, sc, w, 60)["state"][-1]
+                assert np.array_equal(st, ref), float(np.abs(st - ref).max())
 
 
 def test_no_device_fails_loudly():

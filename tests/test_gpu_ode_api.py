@@ -69,6 +69,26 @@ def test_scene_player_joint_types_on_gpu():
             assert np.abs(st[:, :3] - ref[:, :3]).max() < 2e-3, w
 
 
+def test_scene_player_cylinders_on_gpu():
+    """scene_player.c with dCreateCylinder geoms (the plane world of the
+    cylinder pile) linked against libodegpu: agrees with the batched path
+    after 60 steps (same kernels; FP32 inputs to the host setters)."""
+    from odegpu.batch import Batch
+    sc = S.cylinder_pile(n_worlds=1)
+    steps = 60
+    B = Batch(sc)
+    B.step(steps)
+    bt = B.state()
+    B.close()
+    with tempfile.TemporaryDirectory() as d:
+        exe = U.build_gpu_demo(os.path.join(d, "player"), src=U.PLAYER)
+        inp = os.path.join(d, "in.txt")
+        U.player_input(sc, 0, steps, inp)
+        st = U.run_demo(exe, inp)
+        assert np.abs(st[:, :3] - bt[:, :3]).max() < 1e-4
+        assert np.abs(st[:, 7:] - bt[:, 7:]).max() < 1e-2
+
+
 def _api():
     from odegpu._lib import lib
     L = lib()
