@@ -3329,6 +3329,804 @@ static void quick_stepper(OWorld* W, const int* bidx, int nb, const int* jidx, i
 }
 
 /* ------------------------------------------------------------------------ */
+/* dWorldStep: the exact stepper (ode/src/step.cpp:187-846) with the Dantzig */
+/* LCP solver (ode/src/lcp.cpp:360-1073) and the LDL^T kernels it calls      */
+/* (ode/src/fastldlt.c, fastlsolve.c, fastltsolve.c, fastdot.c,              */
+/* ode/src/matrix.cpp:242-436). The blocked kernels are restated with the    */
+/* reference's accumulation order (sums over earlier columns first, then the */
+/* terms inside the 2- or 4-row block), which is what makes this FP64        */
+/* restatement agree with the reference bit for bit.                         */
+
+/* info->nub of each joint's getInfo1 (ball.cpp:52, hinge.cpp:56,
+ * hinge2.cpp:84, slider.cpp:118, universal.cpp:267, fixed.cpp:54,
+ * amotor.cpp:194, contact.cpp:51-70); J->the_m / limits set by joint_info1. */
+static int joint_nub(const OJoint* J) {
+  switch (J->type) {
+    case ODEGPU_JOINT_CONTACT: {
+      const odegpuSurface* S = &J->surf;
+      int nub = 0;
+      if (S->mode & ODEGPU_CONTACT_MU2) {
+        if (S->mu == R_INF) nub++;
+        if (S->mu2 == R_INF) nub++;
+      } else if (S->mu == R_INF) {
+        nub += 2;
+      }
+      return nub;
+    }
+    case ODEGPU_JOINT_BALL: return 3;
+    case ODEGPU_JOINT_HINGE: return 5;
+    case ODEGPU_JOINT_HINGE2: return 4;
+    case ODEGPU_JOINT_SLIDER: return 5;
+    case ODEGPU_JOINT_UNIVERSAL: return 4;
+    case ODEGPU_JOINT_FIXED: return 6;
+    default: return 0;
+  }
+}
+
+static real lcp_dot(const real* a, const real* b, int n) {   /* _dDot, fastdot.c */
+  real sum = 0;
+  for (int k = 0; k < n; ++k) sum += a[k] * b[k];
+  return sum;
+}
+
+/* Unit lower-triangular solve in blocks of 4 rows (_dSolveL1, fastlsolve.c;
+ * _dSolveL1T, fastltsolve.c, is the same on the reversed transposed system).
+ * M(r, c) is the matrix entry of row r, column c < r in processing order;
+ * x is indexed in processing order too. */
+#define LSOLVE_BLOCKED(n, M, X)                                                              \
+  do {                                                                                        \
+    int i_ = 0;                                                                               \
+    for (; i_ <= (n) - 4; i_ += 4) {                                                          \
+      real z_[4] = {0, 0, 0, 0};                                                              \
+      for (int c_ = 0; c_ < i_; ++c_)                                                         \
+        for (int q_ = 0; q_ < 4; ++q_) z_[q_] += M(i_ + q_, c_) * X(c_);                      \
+      real v0 = X(i_) - z_[0];                                                                \
+      X(i_) = v0;                                                                             \
+      real v1 = X(i_ + 1) - z_[1] - M(i_ + 1, i_) * v0;                                       \
+      X(i_ + 1) = v1;                                                                         \
+      real v2 = X(i_ + 2) - z_[2] - M(i_ + 2, i_) * v0 - M(i_ + 2, i_ + 1) * v1;             \
+      X(i_ + 2) = v2;                                                                         \
+      X(i_ + 3) = X(i_ + 3) - z_[3] - M(i_ + 3, i_) * v0 - M(i_ + 3, i_ + 1) * v1 -           \
+                  M(i_ + 3, i_ + 2) * v2;                                                     \
+    }                                                                                         \
+    for (; i_ < (n); ++i_) {                                                                  \
+      real z0 = 0;                                                                            \
+      for (int c_ = 0; c_ < i_; ++c_) z0 += M(i_, c_) * X(c_);                                \
+      X(i_) = X(i_) - z0;                                                                     \
+    }                                                                                         \
+  } while (0)
+
+static void lcp_solve_l1(const real* L, real* B, int n, int ns) {
+#define ML(r, c) L[(size_t)(r) * ns + (c)]
+#define XB(i) B[i]
+  LSOLVE_BLOCKED(n, ML, XB);
+#undef ML
+#undef XB
+}
+static void lcp_solve_l1t(const real* L, real* B, int n, int ns) {
+#define MLT(r, c) L[(size_t)(n - 1 - (c)) * ns + (n - 1 - (r))]
+#define XBT(i) B[n - 1 - (i)]
+  LSOLVE_BLOCKED(n, MLT, XBT);
+#undef MLT
+#undef XBT
+}
+
+/* dSolveL1_1 / dSolveL1_2 of fastldlt.c: blocks of 2 rows, one or two right
+ * hand sides (rows of A, B1 / B2 stored at stride 1). */
+static void lcp_solve_l1_pair(const real* L, real* B1, real* B2, int n, int ns) {
+  for (int i = 0; i < n; i += 2) {
+    real z11 = 0, z12 = 0, z21 = 0, z22 = 0;
+    for (int c = 0; c < i; ++c) {
+      const real p1 = L[(size_t)i * ns + c], p2 = L[(size_t)(i + 1) * ns + c];
+      z11 += p1 * B1[c];
+      if (B2) z12 += p1 * B2[c];
+      z21 += p2 * B1[c];
+      if (B2) z22 += p2 * B2[c];
+    }
+    const real l = L[(size_t)(i + 1) * ns + i];
+    z11 = B1[i] - z11;
+    B1[i] = z11;
+    if (B2) { z12 = B2[i] - z12; B2[i] = z12; }
+    B1[i + 1] = B1[i + 1] - z21 - l * z11;
+    if (B2) B2[i + 1] = B2[i + 1] - z22 - l * z12;
+  }
+}
+
+/* _dFactorLDLT (fastldlt.c): A = L D L^T in place (L below the diagonal),
+ * d = 1 / D, two rows at a time. */
+static void lcp_factor_ldlt(real* A, real* d, int n, int ns) {
+  if (n < 1) return;
+  int i = 0;
+  for (; i <= n - 2; i += 2) {
+    real* r1 = A + (size_t)i * ns;
+    real* r2 = A + (size_t)(i + 1) * ns;
+    lcp_solve_l1_pair(A, r1, r2, i, ns);
+    real z11 = 0, z21 = 0, z22 = 0;
+    for (int j = 0; j < i; ++j) {
+      const real p1 = r1[j], p2 = r2[j], dd = d[j];
+      const real q1 = p1 * dd, q2 = p2 * dd;
+      r1[j] = q1;
+      r2[j] = q2;
+      z11 += p1 * q1;
+      z21 += p2 * q1;
+      z22 += p2 * q2;
+    }
+    z11 = r1[i] - z11;
+    z21 = r2[i] - z21;
+    z22 = r2[i + 1] - z22;
+    d[i] = 1.0 / z11;
+    const real q1 = z21, q2 = q1 * d[i];
+    d[i + 1] = 1.0 / (z22 - q1 * q2);
+    r2[i] = q2;
+  }
+  if (n - i == 1) {
+    real* r1 = A + (size_t)i * ns;
+    lcp_solve_l1_pair(A, r1, NULL, i, ns);
+    real z11 = 0;
+    for (int j = 0; j < i; ++j) {
+      const real p1 = r1[j], q1 = p1 * d[j];
+      r1[j] = q1;
+      z11 += p1 * q1;
+    }
+    d[i] = 1.0 / (r1[i] - z11);
+  }
+}
+
+static void lcp_solve_ldlt(const real* L, const real* d, real* b, int n, int ns) {   /* matrix.cpp:251-257 */
+  lcp_solve_l1(L, b, n, ns);
+  for (int i = 0; i < n; ++i) b[i] *= d[i];
+  lcp_solve_l1t(L, b, n, ns);
+}
+
+/* _dLDLTAddTL, matrix.cpp:260-336: rank-2 update of the factorization for
+ * the top-left row / column replaced by a. */
+static void lcp_ldlt_add_tl(real* L, real* d, const real* a, int n, int ns, real* W1, real* W2) {
+  if (n < 2) return;
+  W1[0] = W2[0] = 0;
+  for (int j = 1; j < n; ++j) W1[j] = W2[j] = a[j] * M_SQRT1_2;
+  const real W11 = (0.5 * a[0] + 1) * M_SQRT1_2;
+  const real W21 = (0.5 * a[0] - 1) * M_SQRT1_2;
+  real alpha1 = 1.0, alpha2 = 1.0;
+  {
+    real dee = d[0];
+    real alphanew = alpha1 + (W11 * W11) * dee;
+    dee /= alphanew;
+    const real gamma1 = W11 * dee;
+    dee *= alpha1;
+    alpha1 = alphanew;
+    alphanew = alpha2 - (W21 * W21) * dee;
+    dee /= alphanew;
+    alpha2 = alphanew;
+    const real k1 = 1.0 - W21 * gamma1;
+    const real k2 = W21 * gamma1 * W11 - W21;
+    for (int p = 1; p < n; ++p) {
+      const real Wp = W1[p], ell = L[(size_t)p * ns];
+      W1[p] = Wp - W11 * ell;
+      W2[p] = k1 * Wp + k2 * ell;
+    }
+  }
+  for (int j = 1; j < n; ++j) {
+    const real k1 = W1[j], k2 = W2[j];
+    real dee = d[j];
+    real alphanew = alpha1 + (k1 * k1) * dee;
+    dee /= alphanew;
+    const real gamma1 = k1 * dee;
+    dee *= alpha1;
+    alpha1 = alphanew;
+    alphanew = alpha2 - (k2 * k2) * dee;
+    dee /= alphanew;
+    const real gamma2 = k2 * dee;
+    dee *= alpha2;
+    d[j] = dee;
+    alpha2 = alphanew;
+    for (int p = j + 1; p < n; ++p) {
+      real* l = &L[(size_t)p * ns + j];
+      real ell = *l;
+      real Wp = W1[p] - k1 * ell;
+      ell += gamma1 * Wp;
+      W1[p] = Wp;
+      Wp = W2[p] - k2 * ell;
+      ell -= gamma2 * Wp;
+      W2[p] = Wp;
+      *l = ell;
+    }
+  }
+}
+
+/* Dantzig LCP state (the dLCP object, lcp.cpp:362-785), rows of A reached
+ * through row pointers so that row swaps exchange pointers. */
+typedef struct {
+  int n, ns, nub, nC, nN;
+  real** A;
+  real *x, *b, *w, *lo, *hi, *L, *d, *Dell, *ell, *tmp, *W1, *W2, *t;
+  int *state, *findex, *p, *C;
+} LcpState;
+
+#define LCP_GETA(S, i, j) (((i) > (j)) ? (S)->A[i][j] : (S)->A[j][i])
+
+/* swapRowsAndCols (lcp.cpp:148-213, row-pointer variant) */
+static void lcp_swap_rows_cols(LcpState* S, int i1, int i2, int fast) {
+  real** A = S->A;
+  real* A_i1 = A[i1];
+  real* A_i2 = A[i2];
+  for (int i = i1 + 1; i < i2; ++i) {
+    real* A_i_i1 = A[i] + i1;
+    A_i1[i] = *A_i_i1;
+    *A_i_i1 = A_i2[i];
+  }
+  A_i1[i2] = A_i1[i1];
+  A_i1[i1] = A_i2[i1];
+  A_i2[i1] = A_i2[i2];
+  if (fast) {
+    A[i1] = A_i2;
+    A[i2] = A_i1;
+  } else {
+    for (int k = 0; k <= i2; ++k) { const real t = A_i1[k]; A_i1[k] = A_i2[k]; A_i2[k] = t; }
+  }
+  for (int j = i2 + 1; j < S->n; ++j) {
+    real* A_j = A[j];
+    const real t = A_j[i1]; A_j[i1] = A_j[i2]; A_j[i2] = t;
+  }
+}
+
+/* swapProblem (lcp.cpp:216-267) */
+static void lcp_swap_problem(LcpState* S, int i1, int i2, int fast) {
+  if (i1 == i2) return;
+  lcp_swap_rows_cols(S, i1, i2, fast);
+#define SWPR(v) { const real t_ = S->v[i1]; S->v[i1] = S->v[i2]; S->v[i2] = t_; }
+#define SWPI(v) { const int t_ = S->v[i1]; S->v[i1] = S->v[i2]; S->v[i2] = t_; }
+  SWPR(x) SWPR(b) SWPR(w) SWPR(lo) SWPR(hi) SWPI(p) SWPI(state)
+  if (S->findex) SWPI(findex)
+#undef SWPR
+#undef SWPI
+}
+
+static void lcp_transfer_i_to_C(LcpState* S, int i) {   /* lcp.cpp:524-551 */
+  if (S->nC > 0) {
+    real* Lt = S->L + (size_t)S->nC * S->ns;
+    for (int j = 0; j < S->nC; ++j) Lt[j] = S->ell[j];
+    S->d[S->nC] = 1.0 / (S->A[i][i] - lcp_dot(S->ell, S->Dell, S->nC));
+  } else {
+    S->d[0] = 1.0 / S->A[i][i];
+  }
+  lcp_swap_problem(S, S->nC, i, 1);
+  S->C[S->nC] = S->nC;
+  S->nC++;
+}
+
+static void lcp_gather_dell(LcpState* S, int i) {   /* Dell = A(i, C), NUB_OPTIMIZATIONS */
+  const real* aptr = S->A[i];
+  int j = 0;
+  for (; j < S->nub; ++j) S->Dell[j] = aptr[j];
+  for (; j < S->nC; ++j) S->Dell[j] = aptr[S->C[j]];
+}
+
+static void lcp_transfer_i_from_N_to_C(LcpState* S, int i) {   /* lcp.cpp:555-605 */
+  if (S->nC > 0) {
+    lcp_gather_dell(S, i);
+    lcp_solve_l1(S->L, S->Dell, S->nC, S->ns);
+    real* Lt = S->L + (size_t)S->nC * S->ns;
+    for (int j = 0; j < S->nC; ++j) Lt[j] = S->ell[j] = S->Dell[j] * S->d[j];
+    S->d[S->nC] = 1.0 / (S->A[i][i] - lcp_dot(S->ell, S->Dell, S->nC));
+  } else {
+    S->d[0] = 1.0 / S->A[i][i];
+  }
+  lcp_swap_problem(S, S->nC, i, 1);
+  S->C[S->nC] = S->nC;
+  S->nN--;
+  S->nC++;
+}
+
+/* _dRemoveRowCol, matrix.cpp:402-434 */
+static void lcp_remove_row_col(real* A, int n, int ns, int r) {
+  if (r >= n - 1) return;
+  if (r > 0) {
+    for (int i = 0; i < r; ++i) memmove(A + (size_t)i * ns + r, A + (size_t)i * ns + r + 1, (n - r - 1) * sizeof(real));
+    for (int i = r; i < n - 1; ++i) memcpy(A + (size_t)i * ns, A + (size_t)(i + 1) * ns, r * sizeof(real));
+  }
+  for (int i = r; i < n - 1; ++i)
+    memcpy(A + (size_t)i * ns + r, A + (size_t)(i + 1) * ns + r + 1, (n - r - 1) * sizeof(real));
+}
+
+/* _dLDLTRemove, matrix.cpp:348-399: drop row / column r of the factorized
+ * set C (indices p into A) */
+static void lcp_ldlt_remove(LcpState* S, const int* p, int n2, int r) {
+  real* L = S->L;
+  real* d = S->d;
+  const int ns = S->ns;
+  if (r == n2 - 1) return;
+  if (r == 0) {
+    real* a = S->t;
+    const int p0 = p[0];
+    for (int i = 0; i < n2; ++i) a[i] = -LCP_GETA(S, p[i], p0);
+    a[0] += 1.0;
+    lcp_ldlt_add_tl(L, d, a, n2, ns, S->W1, S->W2);
+  } else {
+    real* t = S->t;
+    const real* Lr = L + (size_t)r * ns;
+    for (int i = 0; i < r; ++i) t[i] = Lr[i] / d[i];
+    real* a = t + r;
+    const int p_r = p[r];
+    for (int i = 0; i < n2 - r; ++i) a[i] = lcp_dot(L + (size_t)(r + i) * ns, t, r) - LCP_GETA(S, p[r + i], p_r);
+    a[0] += 1.0;
+    lcp_ldlt_add_tl(L + (size_t)r * ns + r, d + r, a, n2 - r, ns, S->W1, S->W2);
+  }
+  lcp_remove_row_col(L, n2, ns, r);
+  if (r < n2 - 1) memmove(d + r, d + r + 1, (n2 - r - 1) * sizeof(real));
+}
+
+static void lcp_transfer_i_from_C_to_N(LcpState* S, int i) {   /* lcp.cpp:609-651 */
+  int* C = S->C;
+  const int nC = S->nC;
+  int last_idx = -1, j = 0;
+  for (; j < nC; ++j) {
+    if (C[j] == nC - 1) last_idx = j;
+    if (C[j] == i) {
+      lcp_ldlt_remove(S, C, nC, j);
+      int k;
+      if (last_idx == -1) {
+        for (k = j + 1; k < nC; ++k)
+          if (C[k] == nC - 1) break;
+      } else {
+        k = last_idx;
+      }
+      C[k] = C[j];
+      if (j < nC - 1) memmove(C + j, C + j + 1, (nC - j - 1) * sizeof(int));
+      break;
+    }
+  }
+  lcp_swap_problem(S, i, nC - 1, 1);
+  S->nN++;
+  S->nC = nC - 1;
+}
+
+/* solve1 (lcp.cpp:704-757): a(C) = -dir A(C,C) \ A(C,i) */
+static void lcp_solve1(LcpState* S, real* a, int i, int dir, int only_transfer) {
+  if (S->nC <= 0) return;
+  lcp_gather_dell(S, i);
+  lcp_solve_l1(S->L, S->Dell, S->nC, S->ns);
+  for (int j = 0; j < S->nC; ++j) S->ell[j] = S->Dell[j] * S->d[j];
+  if (!only_transfer) {
+    for (int j = 0; j < S->nC; ++j) S->tmp[j] = S->ell[j];
+    lcp_solve_l1t(S->L, S->tmp, S->nC, S->ns);
+    if (dir > 0)
+      for (int j = 0; j < S->nC; ++j) a[S->C[j]] = -S->tmp[j];
+    else
+      for (int j = 0; j < S->nC; ++j) a[S->C[j]] = S->tmp[j];
+  }
+}
+
+/* dSolveLCP (lcp.cpp:784-1073). A is n x ns, row-major, lower triangle used;
+ * it is destroyed. Returns 0, or 1 when the solver stopped on s <= 0. */
+static int solve_lcp(int n, real* A, real* x, real* b, int nub, real* lo, real* hi, int* findex) {
+  const int ns = n;
+  if (nub >= n) {
+    real* d = (real*)calloc(n, sizeof(real));
+    lcp_factor_ldlt(A, d, n, ns);
+    lcp_solve_ldlt(A, d, b, n, ns);
+    memcpy(x, b, n * sizeof(real));
+    free(d);
+    return 0;
+  }
+  LcpState S_, *S = &S_;
+  memset(S, 0, sizeof(*S));
+  S->n = n; S->ns = ns; S->nub = nub;
+  S->A = (real**)malloc(n * sizeof(real*));
+  for (int k = 0; k < n; ++k) S->A[k] = A + (size_t)k * ns;
+  S->x = x; S->b = b; S->lo = lo; S->hi = hi; S->findex = findex;
+  real* buf = (real*)calloc((size_t)n * ns + 12 * (size_t)n + 8, sizeof(real));
+  S->L = buf;
+  S->d = S->L + (size_t)n * ns;
+  S->w = S->d + n; S->Dell = S->w + n; S->ell = S->Dell + n; S->tmp = S->ell + n;
+  real* delta_x = S->tmp + n;
+  S->W1 = delta_x + n; S->W2 = S->W1 + n; S->t = S->W2 + n;
+  real* delta_w = S->tmp;   /* tmp doubles as delta_w (lcp.cpp:835-836) */
+  S->state = (int*)calloc(n, sizeof(int));
+  S->p = (int*)malloc(n * sizeof(int));
+  S->C = (int*)malloc(n * sizeof(int));
+  /* dLCP::dLCP, lcp.cpp:400-520 */
+  for (int k = 0; k < n; ++k) { x[k] = 0; S->p[k] = k; }
+  for (int k = S->nub; k < n; ++k) {
+    if (findex && findex[k] >= 0) continue;
+    if (lo[k] == -R_INF && hi[k] == R_INF) {
+      lcp_swap_problem(S, S->nub, k, 0);
+      S->nub++;
+    }
+  }
+  if (S->nub > 0) {
+    for (int j = 0; j < S->nub; ++j) memcpy(S->L + (size_t)j * ns, S->A[j], (j + 1) * sizeof(real));
+    lcp_factor_ldlt(S->L, S->d, S->nub, ns);
+    memcpy(x, b, S->nub * sizeof(real));
+    lcp_solve_ldlt(S->L, S->d, x, S->nub, ns);
+    for (int k = 0; k < S->nub; ++k) { S->w[k] = 0; S->C[k] = k; }
+    S->nC = S->nub;
+  }
+  if (findex) {
+    int at_end = 0;
+    for (int k = n - 1; k >= S->nub; k--)
+      if (findex[k] >= 0) {
+        lcp_swap_problem(S, k, n - 1 - at_end, 1);
+        at_end++;
+      }
+  }
+  const int adj_nub = S->nub;
+  real* w = S->w;
+  int hit_first_friction = 0, err = 0;
+  for (int i = adj_nub; i < n; ++i) {
+    int s_error = 0;
+    if (!hit_first_friction && findex && findex[i] >= 0) {
+      for (int j = 0; j < n; ++j) delta_w[S->p[j]] = x[j];
+      for (int k = i; k < n; ++k) {
+        const real wfk = delta_w[findex[k]];
+        if (wfk == 0) { hi[k] = 0; lo[k] = 0; }
+        else { hi[k] = fabs(hi[k] * wfk); lo[k] = -hi[k]; }
+      }
+      hit_first_friction = 1;
+    }
+    w[i] = lcp_dot(S->A[i], x, S->nC) + lcp_dot(S->A[i] + S->nC, x + S->nC, S->nN) - b[i];
+    if (lo[i] == 0 && w[i] >= 0) {
+      S->nN++;
+      S->state[i] = 0;
+    } else if (hi[i] == 0 && w[i] <= 0) {
+      S->nN++;
+      S->state[i] = 1;
+    } else if (w[i] == 0) {
+      lcp_solve1(S, delta_x, i, 0, 1);
+      lcp_transfer_i_to_C(S, i);
+    } else {
+      for (;;) {
+        int dir;
+        real dirf;
+        if (w[i] <= 0) { dir = 1; dirf = 1.0; }
+        else { dir = -1; dirf = -1.0; }
+        lcp_solve1(S, delta_x, i, dir, 0);
+        {   /* delta_w(N) = A(N,C) delta_x(C), then += dir A(N,i) */
+          const int nC = S->nC, nN = S->nN;
+          for (int k = 0; k < nN; ++k) delta_w[nC + k] = lcp_dot(S->A[k + nC], delta_x, nC);
+          const real* aptr = S->A[i] + nC;
+          if (dir > 0) for (int k = 0; k < nN; ++k) delta_w[nC + k] += aptr[k];
+          else for (int k = 0; k < nN; ++k) delta_w[nC + k] -= aptr[k];
+        }
+        delta_w[i] = lcp_dot(S->A[i], delta_x, S->nC) + S->A[i][i] * dirf;
+        int cmd = 1, si = 0;
+        real s = -w[i] / delta_w[i];
+        if (dir > 0) {
+          if (hi[i] < R_INF) {
+            const real s2 = (hi[i] - x[i]) * dirf;
+            if (s2 < s) { s = s2; cmd = 3; }
+          }
+        } else {
+          if (lo[i] > -R_INF) {
+            const real s2 = (lo[i] - x[i]) * dirf;
+            if (s2 < s) { s = s2; cmd = 2; }
+          }
+        }
+        for (int k = 0; k < S->nN; ++k) {
+          const int ik = S->nC + k;
+          if (!S->state[ik] ? delta_w[ik] < 0 : delta_w[ik] > 0) {
+            if (lo[ik] == 0 && hi[ik] == 0) continue;
+            const real s2 = -w[ik] / delta_w[ik];
+            if (s2 < s) { s = s2; cmd = 4; si = ik; }
+          }
+        }
+        for (int k = adj_nub; k < S->nC; ++k) {
+          if (delta_x[k] < 0 && lo[k] > -R_INF) {
+            const real s2 = (lo[k] - x[k]) / delta_x[k];
+            if (s2 < s) { s = s2; cmd = 5; si = k; }
+          }
+          if (delta_x[k] > 0 && hi[k] < R_INF) {
+            const real s2 = (hi[k] - x[k]) / delta_x[k];
+            if (s2 < s) { s = s2; cmd = 6; si = k; }
+          }
+        }
+        if (s <= 0.0) {
+          for (int k = i; k < n; ++k) { x[k] = 0; w[k] = 0; }
+          s_error = 1;
+          break;
+        }
+        for (int k = 0; k < S->nC; ++k) x[k] += s * delta_x[k];
+        x[i] += s * dirf;
+        for (int k = 0; k < S->nN; ++k) w[S->nC + k] += s * delta_w[S->nC + k];
+        w[i] += s * delta_w[i];
+        switch (cmd) {
+          case 1: w[i] = 0; lcp_transfer_i_to_C(S, i); break;
+          case 2: x[i] = lo[i]; S->state[i] = 0; S->nN++; break;
+          case 3: x[i] = hi[i]; S->state[i] = 1; S->nN++; break;
+          case 4: w[si] = 0; lcp_transfer_i_from_N_to_C(S, si); break;
+          case 5: x[si] = lo[si]; S->state[si] = 0; lcp_transfer_i_from_C_to_N(S, si); break;
+          case 6: x[si] = hi[si]; S->state[si] = 1; lcp_transfer_i_from_C_to_N(S, si); break;
+        }
+        if (cmd <= 3) break;
+      }
+    }
+    if (s_error) { err = 1; break; }
+  }
+  /* unpermute (lcp.cpp:759-781) */
+  memcpy(S->tmp, x, n * sizeof(real));
+  for (int j = 0; j < n; ++j) x[S->p[j]] = S->tmp[j];
+  memcpy(S->tmp, w, n * sizeof(real));
+  for (int j = 0; j < n; ++j) w[S->p[j]] = S->tmp[j];
+  free(S->A); free(buf); free(S->state); free(S->p); free(S->C);
+  return err;
+}
+
+typedef struct { int j, m, nub; } JInfo1;
+
+/* The joint order of step.cpp:265-403: purely unbounded joints first, then
+ * mixed, then purely LCP ones, built by the reference's two-ended scheme
+ * (joints are placed alternately growing forward and backward from the middle
+ * of a 2 nj buffer, swapping a mixed joint into place when a group boundary
+ * moves). Joints with m = 0 are dropped. Returns the joint count; *nub_out is
+ * the number of purely unbounded joints, which the reference passes to the
+ * LCP as its nub. */
+static int exact_joint_order(OWorld* W, const int* jidx, int nj_in, JInfo1* out, int* nub_out) {
+  JInfo1* a = (JInfo1*)malloc((size_t)(2 * nj_in + 2) * sizeof(JInfo1));
+  int unb_start, mix_start, mix_end, lcp_end;
+  unb_start = mix_start = mix_end = lcp_end = nj_in;
+  int cur = lcp_end, src = 0;
+  for (;;) {
+    int fwd_end = 0;
+    {
+      int mixend = mix_end;
+      for (;;) {
+        if (src == nj_in) { lcp_end = cur; fwd_end = 1; break; }
+        OJoint* J = &W->joint[jidx[src++]];
+        JInfo1 in = {(int)(J - W->joint), joint_info1(W, J), 0};
+        in.nub = joint_nub(J);
+        if (in.m > 0) {
+          if (in.nub == 0) {
+            a[cur++] = in;
+          } else if (in.nub < in.m) {
+            if (unb_start == mix_start) {
+              unb_start = mix_start = mix_start - 1;
+              a[mix_start] = in;
+            } else if (mixend != cur) {
+              a[cur] = a[mixend];
+              a[mixend] = in;
+              ++mixend; ++cur;
+            } else {
+              a[cur] = in;
+              mixend = cur = cur + 1;
+            }
+          } else {
+            unb_start = unb_start - 1;
+            a[unb_start] = in;
+            lcp_end = cur;
+            mix_end = mixend;
+            cur = unb_start - 1;
+            break;
+          }
+        }
+      }
+    }
+    if (fwd_end) break;
+    int bkw_end = 0;
+    {
+      int mixstart = mix_start - 1;
+      for (;;) {
+        if (src == nj_in) { unb_start = cur + 1; mix_start = mixstart + 1; bkw_end = 1; break; }
+        OJoint* J = &W->joint[jidx[src++]];
+        JInfo1 in = {(int)(J - W->joint), joint_info1(W, J), 0};
+        in.nub = joint_nub(J);
+        if (in.m > 0) {
+          if (in.nub == in.m) {
+            a[cur--] = in;
+          } else if (in.nub > 0) {
+            if (mix_end == lcp_end) {
+              const int e = mix_end;
+              lcp_end = mix_end = mix_end + 1;
+              a[e] = in;
+            } else if (mixstart != cur) {
+              a[cur] = a[mixstart];
+              a[mixstart] = in;
+              --mixstart; --cur;
+            } else {
+              a[cur] = in;
+              mixstart = cur = cur - 1;
+            }
+          } else {
+            const int e = lcp_end;
+            lcp_end = lcp_end + 1;
+            a[e] = in;
+            unb_start = cur + 1;
+            mix_start = mixstart + 1;
+            cur = e + 1;
+            break;
+          }
+        }
+      }
+    }
+    if (bkw_end) break;
+  }
+  *nub_out = mix_start - unb_start;
+  const int nj = lcp_end - unb_start;
+  memcpy(out, a + unb_start, (size_t)nj * sizeof(JInfo1));
+  free(a);
+  return nj;
+}
+
+static int g_lcp_errors = 0;   /* LCP runs that stopped on s <= 0 */
+static int g_exact_stepper = 0;   /* 1: worlds step with dWorldStep instead of dWorldQuickStep */
+void oracle_set_stepper(int exact) { g_exact_stepper = exact; }
+int oracle_lcp_errors(void) { return g_lcp_errors; }
+
+static void exact_stepper(OWorld* W, const int* bidx, int nb, const int* jidx, int nj_in, real h) {
+  const real h1 = 1.0 / h;
+  real* invI = (real*)malloc((size_t)(nb > 0 ? nb : 1) * 12 * sizeof(real));
+  for (int i = 0; i < nb; i++) W->body[bidx[i]].tag = i;
+  for (int i = 0; i < nb; i++) {   /* step.cpp:205-229 */
+    OBody* b = &W->body[bidx[i]];
+    real tmp[12];
+    mul2_333(tmp, b->invI, b->R);
+    mul0_333(invI + 12 * i, b->R, tmp);
+    if (b->flags & ODEGPU_BODY_GYROSCOPIC) {
+      real I[12], t3[3], cr[3];
+      mul2_333(tmp, b->I, b->R);
+      mul0_333(I, b->R, tmp);
+      mul0_331(t3, I, b->avel);
+      cross3(cr, b->avel, t3);
+      b->tacc[0] = b->tacc[0] - cr[0];
+      b->tacc[1] = b->tacc[1] - cr[1];
+      b->tacc[2] = b->tacc[2] - cr[2];
+    }
+  }
+  for (int d = 0; d < 3; ++d) {   /* :231-262 */
+    const real g = W->gravity[d];
+    if (g)
+      for (int i = 0; i < nb; i++) {
+        OBody* b = &W->body[bidx[i]];
+        if ((b->flags & ODEGPU_BODY_NO_GRAVITY) == 0) b->facc[d] += b->mass * g;
+      }
+  }
+  JInfo1* ji = (JInfo1*)malloc((size_t)(nj_in > 0 ? nj_in : 1) * sizeof(JInfo1));
+  int nub = 0;
+  const int nj = exact_joint_order(W, jidx, nj_in, ji, &nub);
+  int m = 0;
+  int* ofs = (int*)malloc((size_t)(nj > 0 ? nj : 1) * sizeof(int));
+  for (int k = 0; k < nj; ++k) { ofs[k] = m; m += ji[k].m; }
+  real* cforce = (real*)calloc((size_t)(nb > 0 ? nb : 1) * 6, sizeof(real));
+  if (m > 0) {
+    real* lo = (real*)malloc(m * sizeof(real));
+    real* hi = (real*)malloc(m * sizeof(real));
+    real* J = (real*)calloc((size_t)m * 12, sizeof(real));
+    real* JinvM = (real*)calloc((size_t)m * 12, sizeof(real));
+    int* findex = (int*)malloc(m * sizeof(int));
+    real* A = (real*)calloc((size_t)m * m, sizeof(real));
+    real* rhs = (real*)calloc(m, sizeof(real));   /* c, then rhs */
+    real* cfm = (real*)malloc(m * sizeof(real));
+    int* jb = (int*)malloc((size_t)nj * 2 * sizeof(int));
+    for (int i = 0; i < m; ++i) { lo[i] = -R_INF; hi[i] = R_INF; findex[i] = -1; cfm[i] = W->cfm; }
+    /* create J (:457-497) */
+    Info2 info;
+    info.rowskip = 12;
+    info.fps = h1;
+    info.erp = W->erp;
+    for (int k = 0; k < nj; ++k) {
+      real* Jrow = J + (size_t)ofs[k] * 12;
+      info.J1l = Jrow; info.J1a = Jrow + 3; info.J2l = Jrow + 6; info.J2a = Jrow + 9;
+      info.c = rhs + ofs[k]; info.cfm = cfm + ofs[k]; info.lo = lo + ofs[k]; info.hi = hi + ofs[k];
+      info.findex = findex + ofs[k];
+      OJoint* Jt = &W->joint[ji[k].j];
+      joint_info2(W, Jt, &info);
+      for (int r = 0; r < ji[k].m; ++r)
+        if (findex[ofs[k] + r] != -1) findex[ofs[k] + r] += ofs[k];
+      jb[2 * k] = Jt->b[0] >= 0 ? W->body[Jt->b[0]].tag : -1;
+      jb[2 * k + 1] = Jt->b[1] >= 0 ? W->body[Jt->b[1]].tag : -1;
+    }
+    /* JinvM = J invM (:505-541) */
+    for (int k = 0; k < nj; ++k)
+      for (int half = 0; half < 2; ++half) {
+        const int bt = jb[2 * k + half];
+        if (bt < 0) continue;
+        const real im = W->body[bidx[bt]].invMass;
+        const real* iI = invI + 12 * bt;
+        for (int r = 0; r < ji[k].m; ++r) {
+          const real* s = J + (size_t)(ofs[k] + r) * 12 + 6 * half;
+          real* t = JinvM + (size_t)(ofs[k] + r) * 12 + 6 * half;
+          for (int q = 0; q < 3; ++q) t[q] = s[q] * im;
+          for (int q = 0; q < 3; ++q) t[3 + q] = s[3] * iI[q] + s[4] * iI[4 + q] + s[5] * iI[8 + q];
+        }
+      }
+#define DOT6(u, v) ((u)[0] * (v)[0] + (u)[1] * (v)[1] + (u)[2] * (v)[2] + (u)[3] * (v)[3] + (u)[4] * (v)[4] + \
+                    (u)[5] * (v)[5])
+    /* off-diagonal blocks through shared bodies (:547-607), body 1 then 2 */
+    for (int k = 0; k < nj; ++k)
+      for (int half = 0; half < 2; ++half) {
+        const int bt = jb[2 * k + half];
+        if (bt < 0) continue;
+        for (int k0 = 0; k0 < k; ++k0) {
+          int oh = -1;
+          if (jb[2 * k0] == bt) oh = 0;
+          else if (jb[2 * k0 + 1] == bt) oh = 1;
+          if (oh < 0) continue;
+          for (int r = 0; r < ji[k].m; ++r) {
+            const real* u = JinvM + (size_t)(ofs[k] + r) * 12 + 6 * half;
+            real* Arow = A + (size_t)(ofs[k] + r) * m + ofs[k0];
+            for (int c = 0; c < ji[k0].m; ++c) {
+              const real* v = J + (size_t)(ofs[k0] + c) * 12 + 6 * oh;
+              Arow[c] += DOT6(u, v);
+            }
+          }
+        }
+      }
+    /* diagonal blocks (:610-627) and cfm / h on the diagonal (:630-637) */
+    for (int k = 0; k < nj; ++k)
+      for (int r = 0; r < ji[k].m; ++r) {
+        real* Arow = A + (size_t)(ofs[k] + r) * m + ofs[k];
+        const real* u1 = JinvM + (size_t)(ofs[k] + r) * 12;
+        for (int c = 0; c < ji[k].m; ++c) {
+          const real* v1 = J + (size_t)(ofs[k] + c) * 12;
+          Arow[c] = DOT6(u1, v1);
+          if (jb[2 * k + 1] >= 0) Arow[c] += DOT6(u1 + 6, v1 + 6);
+        }
+      }
+    for (int i = 0; i < m; ++i) A[(size_t)i * m + i] += cfm[i] * h1;
+    /* rhs = c / h - J (v / h + invM fe) (:643-687) */
+    {
+      real* tmp1 = (real*)malloc((size_t)nb * 6 * sizeof(real));
+      for (int i = 0; i < nb; i++) {
+        OBody* b = &W->body[bidx[i]];
+        real* t = tmp1 + 6 * i;
+        for (int j = 0; j < 3; j++) t[j] = b->facc[j] * b->invMass + b->lvel[j] * h1;
+        mul0_331(t + 3, invI + 12 * i, b->tacc);
+        for (int q = 0; q < 3; q++) t[3 + q] += b->avel[q] * h1;
+      }
+      for (int i = 0; i < m; ++i) rhs[i] = rhs[i] * h1;
+      for (int k = 0; k < nj; ++k)
+        for (int half = 0; half < 2; ++half) {
+          const int bt = jb[2 * k + half];
+          if (bt < 0) continue;
+          for (int r = 0; r < ji[k].m; ++r) {
+            const real* u = J + (size_t)(ofs[k] + r) * 12 + 6 * half;
+            rhs[ofs[k] + r] -= DOT6(u, tmp1 + 6 * bt);
+          }
+        }
+      free(tmp1);
+    }
+    real* lambda = (real*)malloc(m * sizeof(real));
+    g_lcp_errors += solve_lcp(m, A, lambda, rhs, nub, lo, hi, findex);
+    /* cforce = J^T lambda (:720-786), with joint feedback */
+    for (int k = 0; k < nj; ++k) {
+      OJoint* Jt = &W->joint[ji[k].j];
+      for (int half = 0; half < 2; ++half) {
+        const int bt = jb[2 * k + half];
+        if (bt < 0) continue;
+        real s[6] = {0, 0, 0, 0, 0, 0};
+        for (int r = 0; r < ji[k].m; ++r) {
+          const real* u = J + (size_t)(ofs[k] + r) * 12 + 6 * half;
+          const real l = lambda[ofs[k] + r];
+          for (int q = 0; q < 6; ++q) s[q] += u[q] * l;
+        }
+        real* cf = cforce + 6 * bt;
+        for (int q = 0; q < 6; ++q) cf[q] += s[q];
+        if (Jt->type != ODEGPU_JOINT_CONTACT)
+          for (int q = 0; q < 6; ++q) Jt->fb[6 * half + q] = s[q];
+      }
+    }
+#undef DOT6
+    free(lo); free(hi); free(J); free(JinvM); free(findex); free(A); free(rhs); free(cfm); free(jb); free(lambda);
+  }
+  /* velocity update (:790-806), position update, accumulators cleared */
+  for (int i = 0; i < nb; i++) {
+    OBody* b = &W->body[bidx[i]];
+    const real* cf = cforce + 6 * i;
+    const real hm = h * b->invMass;
+    for (int j = 0; j < 3; j++) b->lvel[j] += (cf[j] + b->facc[j]) * hm;
+    real data[3], t3[3];
+    for (int k = 0; k < 3; k++) data[k] = (cf[3 + k] + b->tacc[k]) * h;
+    mul0_331(t3, invI + 12 * i, data);
+    for (int k = 0; k < 3; k++) b->avel[k] += t3[k];
+  }
+  for (int i = 0; i < nb; i++) step_body(&W->body[bidx[i]], h);
+  for (int i = 0; i < nb; i++) {
+    OBody* b = &W->body[bidx[i]];
+    b->facc[0] = b->facc[1] = b->facc[2] = 0;
+    b->tacc[0] = b->tacc[1] = b->tacc[2] = 0;
+  }
+  free(ji); free(ofs); free(cforce); free(invI);
+}
+
+/* ------------------------------------------------------------------------ */
 /* world construction from a scene, mirroring the harness's API sequence    */
 
 static void world_init(OWorld* W, const odegpuScene* sc, int w) {
@@ -3591,7 +4389,8 @@ static void process_islands(OWorld* W) {
       b = stack[--ss];
       ibody[nbi++] = b;
     }
-    quick_stepper(W, ibody, nbi, ijoint, nji, W->dt, island);
+    if (g_exact_stepper) exact_stepper(W, ibody, nbi, ijoint, nji, W->dt);
+    else quick_stepper(W, ibody, nbi, ijoint, nji, W->dt, island);
     ++island;
   }
   free(ibody); free(ijoint); free(stack);

@@ -79,6 +79,11 @@ int oracle_collide(int t1, const double* p1, const double* pos1, const double* R
                    double* out);
 
 /* RNG (ode/src/misc.cpp:33-117). */
+/* 1: worlds step with dWorldStep (ode/src/step.cpp + lcp.cpp) instead of
+ * dWorldQuickStep; process-wide. */
+void oracle_set_stepper(int exact);
+/* LCP solves that stopped early on a non-positive step (s <= 0) so far. */
+int oracle_lcp_errors(void);
 void oracle_rand_set_seed(unsigned int s);
 unsigned int oracle_rand_get_seed(void);
 int oracle_rand_int(int n);

@@ -68,6 +68,9 @@ static void set_limot(dJointID j, int group, const double* p,
  *   seed_out   [n_steps]                 dRandGetSeed after each step
  * Returns 0 on success, -1 on bad arguments.
  */
+static int g_exact = 0;   /* 1: dWorldStep (ode.cpp:1787) instead of dWorldQuickStep */
+void ref_set_stepper(int exact) { g_exact = exact; }
+
 int ref_run_world(const odegpuScene* sc, int w, int n_steps, double* state,
                   int* ncontacts, double* contacts, int max_rec,
                   double* feedback, unsigned int* seed_out) {
@@ -313,7 +316,8 @@ int ref_run_world(const odegpuScene* sc, int w, int n_steps, double* state,
       }
     }
 
-    dWorldQuickStep(world, P->dt);
+    if (g_exact) dWorldStep(world, P->dt);
+    else dWorldQuickStep(world, P->dt);
     dJointGroupEmpty(group);
 
     if (state)

@@ -36,10 +36,15 @@ SCENES = {
 KEEP = 10  # keep the state every KEEP steps
 
 
-def make_scene(name):
+# dWorldStep (the exact stepper, ode/src/step.cpp + lcp.cpp) on the same scenes
+EXACT_SCENES = ["box_drop", "batched", "mechanisms", "vehicles", "cylinder_pile"]
+
+
+def make_scene(name, exact=False):
     mk, steps = SCENES[name]
     sc = mk()
     ref = O.ref("d")
+    ref.ref_set_stepper(1 if exact else 0)
     out = dict(sc.to_arrays())
     out["n_steps"] = np.int64(steps)
     for w in range(sc.n_worlds):
@@ -50,7 +55,8 @@ def make_scene(name):
         out[f"w{w}_state"] = r["state"][::KEEP]
         out[f"w{w}_final"] = r["state"][-1]
         out[f"w{w}_feedback"] = r["feedback"]
-    np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **out)
+    ref.ref_set_stepper(0)
+    np.savez_compressed(os.path.join(HERE, f"{'exact_' if exact else ''}{name}.npz"), **out)
 
 
 def rot(rng):
@@ -473,6 +479,8 @@ if __name__ == "__main__":
             elif name == "cylinder_kats":
                 make_cylinder_kats()
                 add_single_outputs("cylinder_kats", hf_class=3)
+            elif name.startswith("exact_"):
+                make_scene(name[len("exact_"):], exact=True)
             elif name == "single_outputs":
                 add_single_outputs("collider_kats")
                 add_single_outputs("hf_kats")
@@ -485,6 +493,9 @@ if __name__ == "__main__":
     for name in SCENES:
         make_scene(name)
         print("wrote", name)
+    for name in EXACT_SCENES:
+        make_scene(name, exact=True)
+        print("wrote exact_" + name)
     make_collider_kats()
     make_hf_kats()
     make_ray_kats()

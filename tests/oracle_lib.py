@@ -51,6 +51,8 @@ def oracle():
         lib.oracle_run_world_from.restype = C.c_int
         lib.oracle_run_world_from.argtypes = [C.c_void_p, C.c_int, C.c_int, _P(C.c_double),
                                               _P(C.c_double)]
+        lib.oracle_set_stepper.argtypes = [C.c_int]
+        lib.oracle_lcp_errors.restype = C.c_int
         _oracle = lib
     return _oracle
 
@@ -68,6 +70,7 @@ def ref(prec="d"):
         lib.ref_rand_int.argtypes = [C.c_int]
         lib.ref_rand_set_seed.argtypes = [C.c_uint]
         lib.ref_rand_get_seed.restype = C.c_uint
+        lib.ref_set_stepper.argtypes = [C.c_int]
         _ref[prec] = lib
     return _ref[prec]
 
@@ -140,3 +143,21 @@ def run_world_from(scene, w, n_steps, init_state):
                                         out.ctypes.data_as(_P(C.c_double)))
     assert rc == 0
     return out
+
+
+class exact_stepper:
+    """Within the block the oracle (and, when given, the reference library)
+    steps worlds with dWorldStep instead of dWorldQuickStep."""
+
+    def __init__(self, *libs):
+        self.libs = libs or (oracle(),)
+
+    def __enter__(self):
+        for lib in self.libs:
+            (lib.oracle_set_stepper if hasattr(lib, "oracle_set_stepper") else lib.ref_set_stepper)(1)
+        return self
+
+    def __exit__(self, *exc):
+        for lib in self.libs:
+            (lib.oracle_set_stepper if hasattr(lib, "oracle_set_stepper") else lib.ref_set_stepper)(0)
+        return False

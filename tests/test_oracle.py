@@ -159,6 +159,40 @@ def test_oracle_matches_reference_golden(name):
         assert np.array_equal(r["feedback"], g[f"w{w}_feedback"])
 
 
+@pytest.mark.parametrize("name", ["box_drop", "batched", "mechanisms", "vehicles", "cylinder_pile"])
+def test_oracle_exact_stepper_matches_reference_golden(name):
+    """dWorldStep (ode/src/step.cpp:187-846: joints ordered unbounded / mixed /
+    LCP, A = J invM J' + cfm / h, the Dantzig LCP of ode/src/lcp.cpp with
+    ODE's LDL' kernels) on the same scenes: contact counts, RNG seeds, body
+    states and joint feedback bit-identical to the reference (FP64)."""
+    g = dict(np.load(os.path.join(GOLDEN, f"exact_{name}.npz")))
+    sc = S.Scene.from_arrays(g)
+    steps = int(g["n_steps"])
+    with O.exact_stepper():
+        for w in range(sc.n_worlds):
+            r = O.run_world(O.oracle().oracle_run_world, sc, w, steps, max_rec=96, feedback=True)
+            assert np.array_equal(r["ncontacts"], g[f"w{w}_ncontacts"])
+            assert np.array_equal(r["seeds"], g[f"w{w}_seeds"])
+            assert np.array_equal(r["contacts"][:, :64], g[f"w{w}_contacts"])
+            assert np.array_equal(r["state"][::10], g[f"w{w}_state"])
+            assert np.array_equal(r["state"][-1], g[f"w{w}_final"])
+            assert np.array_equal(r["feedback"], g[f"w{w}_feedback"])
+    assert O.oracle().oracle_lcp_errors() == 0
+
+
+@pytest.mark.skipif(not O.ref_available("d"), reason="reference not built in this checkout")
+def test_oracle_exact_stepper_matches_reference_live():
+    """dWorldStep on freshly seeded batched worlds against the reference built
+    here: bit-identical states."""
+    sc = S.batched_worlds(n_worlds=4, seed=31)
+    with O.exact_stepper(O.oracle(), O.ref("d")):
+        for w in range(sc.n_worlds):
+            o = O.run_world(O.oracle().oracle_run_world, sc, w, 60)
+            r = O.run_world(O.ref("d").ref_run_world, sc, w, 60)
+            for k in ("ncontacts", "seeds", "state", "contacts"):
+                assert np.array_equal(o[k], r[k]), k
+
+
 @pytest.mark.skipif(not O.ref_available("d"), reason="reference not built in this checkout")
 @pytest.mark.parametrize("seed", [21, 22])
 def test_oracle_matches_reference_live(seed):
