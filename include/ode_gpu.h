@@ -116,6 +116,8 @@ dReal dWorldGetERP(dWorldID w);                                     /* :101 */
 void dWorldSetCFM(dWorldID w, dReal cfm);                           /* :111 */
 dReal dWorldGetCFM(dWorldID w);                                     /* :118 */
 int dWorldQuickStep(dWorldID w, dReal stepsize);                    /* :352 */
+/* The exact stepper (dense LCP per island, Dantzig pivoting) on the GPU. */
+int dWorldStep(dWorldID w, dReal stepsize);                         /* :309 */
 void dWorldSetQuickStepNumIterations(dWorldID w, int num);          /* :385 */
 int dWorldGetQuickStepNumIterations(dWorldID w);                    /* :394 */
 void dWorldSetQuickStepW(dWorldID w, dReal over_relaxation);        /* :401 */

@@ -41,7 +41,11 @@ enum {
   ODEGPU_ST_PAIR_OVERFLOW = 64,
   /* large world: a wait of the constraint sweep gave up (bounded); the step's
      constraint forces are incomplete */
-  ODEGPU_ST_SOLVE_STALL = 128
+  ODEGPU_ST_SOLVE_STALL = 128,
+  /* dWorldStep: the LCP solver stopped on a non-positive step, as the
+   * reference does (ode/src/lcp.cpp:985-993), or after a bounded number of
+   * index-set changes for one driving index */
+  ODEGPU_ST_LCP_STOP = 256
 };
 
 /* Size limits of the on-chip step kernel: bodies and constraint rows per
@@ -92,6 +96,13 @@ int odegpuBatchStep(odegpuBatchID b, int n_steps);
 int odegpuBatchStepPlain(odegpuBatchID b, int n_steps);
 /* Capture n_steps single-step launches into a CUDA graph and replay it. */
 int odegpuBatchStepGraph(odegpuBatchID b, int n_steps);
+/* The stepper every step entry point uses from now on: 0 dWorldQuickStep
+ * (ode/src/ode.cpp:1807), 1 dWorldStep (ode/src/ode.cpp:1787; ode/src/step.cpp
+ * with the Dantzig LCP of ode/src/lcp.cpp). dWorldStep works on a dense
+ * m x m matrix per island (scratch of about 8 m^2 bytes per world, m the
+ * world's row capacity, allocated on first use); it is not available for a
+ * large world, the parity taps, the adjoint or the autotuner. */
+int odegpuBatchSetStepper(odegpuBatchID b, int exact);
 int odegpuBatchSynchronize(odegpuBatchID b);
 
 /* Per-step controls from FP32 arrays in host or device memory (the layout

@@ -13,6 +13,7 @@
 #include "engine_types.cuh"
 #include "world_solve.cuh"
 #include "raycast.cuh"
+#include "world_exact.cuh"
 #include "adjoint.cuh"
 #include "large_world.cuh"
 #include "engine_internal.hpp"
@@ -83,6 +84,21 @@ __global__ void __launch_bounds__(256) world_solve_kernel(BatchDev d, const int*
   const SorSmem S = carve_sor(smem_raw + (size_t)(threadIdx.x >> 5) * kSorSmemPerWarp);
   world_solve(d, w, S, lane, opt);
 }
+
+__global__ void __launch_bounds__(128) world_exact_kernel(BatchDev d, ExactDev X, const int* order, int first,
+                                                          int count, int step, StepOptions opt) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lane = threadIdx.x & 31;
+  const int w = slot_world(order, first, count, d.n_worlds);
+  if (w < 0) return;
+  if (d.world[w].nb > kMaxB || d.world[w].ng > kMaxB + 8) {
+    if (lane == 0) { d.nrows[w] = 0; d.nislands[w] = 0; }
+    return;
+  }
+  const WarpSmem S = carve_smem(smem_raw + (size_t)(threadIdx.x >> 5) * kSmemPerWarp);
+  world_exact(d, X, w, step, S, lane, opt);
+}
+constexpr int kExactWarps = 4;
 
 // State exchange: FP32 records of 13 floats per body.
 __global__ void pack_state_kernel(BatchDev d, int nb, float* out) {
@@ -189,6 +205,32 @@ struct odegpuBatch {
   DBuf<float> state_scratch;
   DBuf<odegpuRay> ray_in;          // odegpuBatchRayCast staging, grown on demand
   DBuf<odegpuRayHit> ray_out;
+  bool exact = false;              // dWorldStep instead of dWorldQuickStep
+  DBuf<float> xscratch;            // dWorldStep scratch (world_exact.cuh), first use
+  DBuf<long long> xoff;
+  DBuf<int> xcap;
+  std::vector<int> xcap_h;
+  int ensure_exact_scratch() {
+    std::vector<long long> off(n_worlds);
+    std::vector<int> cap(n_worlds);
+    long long total = 0;
+    for (int w = 0; w < n_worlds; ++w) {
+      cap[w] = std::max(1, std::min(h_world[w].row_cap, kMaxR));
+      off[w] = total;
+      total += (exact_scratch_floats(cap[w]) + 3) & ~3LL;
+    }
+    if (xscratch.p && cap == xcap_h) return 0;
+    for (auto* p : {(void*)xscratch.p, (void*)xoff.p, (void*)xcap.p})
+      if (p) cudaFree(p);
+    xscratch.p = nullptr; xoff.p = nullptr; xcap.p = nullptr;
+    xcap_h = cap;
+    if (int rc = xscratch.alloc((size_t)total)) return rc;
+    if (int rc = xoff.alloc(n_worlds)) return rc;
+    if (int rc = xcap.alloc(n_worlds)) return rc;
+    OG_CUDA(cudaMemcpy(xoff.p, off.data(), n_worlds * sizeof(long long), cudaMemcpyHostToDevice));
+    OG_CUDA(cudaMemcpy(xcap.p, cap.data(), n_worlds * sizeof(int), cudaMemcpyHostToDevice));
+    return 0;
+  }
 
   BatchDev dev() const {
     BatchDev d;
@@ -432,6 +474,26 @@ struct odegpuBatch {
     const bool tm = timing && cap == cudaStreamCaptureStatusNone;
     int w[3];
     for (int k = 0; k < 3; ++k) w[k] = single_world ? 1 : kwpb[k];
+    if (exact) {
+      if (int rc = ensure_exact_scratch()) return rc;
+      const ExactDev X{xscratch.p, xoff.p, xcap.p};
+      const int wx = single_world ? 1 : kExactWarps;
+      for (int s = 0; s < n_steps; ++s) {
+        mark(tm);
+        apply_carveout(0);
+        world_collide_kernel<<<(count + w[0] - 1) / w[0], w[0] * 32, (size_t)w[0] * kCollideSmemPerWarp,
+                               stream>>>(d, ord, first, count, step_counter + s, opt);
+        mark(tm);
+        world_exact_kernel<<<(count + wx - 1) / wx, wx * 32, (size_t)wx * kSmemPerWarp, stream>>>(
+            d, X, ord, first, count, step_counter + s, opt);
+        mark(tm);
+        mark(tm);
+        launches += 2;
+      }
+      cudaError_t e = cudaGetLastError();
+      if (e != cudaSuccess) return fail(ODEGPU_E_CUDA, std::string("step launch: ") + cudaGetErrorString(e));
+      return 0;
+    }
     for (int s = 0; s < n_steps; ++s) {
       mark(tm);
       apply_carveout(0);
@@ -469,6 +531,9 @@ static int configure_kernels() {
     return -1;
   if (cudaFuncSetAttribute(adjoint_step_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)(kMaxWpb[3] * kAdjSmemPerWarp)) != cudaSuccess)
+    return -1;
+  if (cudaFuncSetAttribute(world_exact_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)(kExactWarps * kSmemPerWarp)) != cudaSuccess)
     return -1;
   return 0;
 }
@@ -1016,6 +1081,13 @@ int odegpuBatchStepGraph(odegpuBatchID b, int n_steps) {
   return 0;
 }
 
+int odegpuBatchSetStepper(odegpuBatchID b, int exact) {
+  if (!b || (exact != 0 && exact != 1)) return fail(ODEGPU_E_ARG, "bad arguments");
+  if (exact && b->lw) return fail(ODEGPU_E_ARG, "dWorldStep is not available for a large world");
+  b->exact = exact != 0;
+  return 0;
+}
+
 int odegpuBatchSetTiming(odegpuBatchID b, int on) {
   if (!b) return fail(ODEGPU_E_ARG, "null batch");
   b->timing = on != 0;
@@ -1079,6 +1151,7 @@ int odegpuBatchSetLaunchConfig(odegpuBatchID b, int kernel, int warps_per_block,
 
 int odegpuBatchAutotune(odegpuBatchID b, int n_steps) {
   if (b && b->lw) return fail(ODEGPU_E_ARG, "not available for a large world (one world above the on-chip limits)");
+  if (b && b->exact) return fail(ODEGPU_E_ARG, "not available with the dWorldStep stepper (odegpuBatchSetStepper)");
   if (!b || n_steps < 1) return fail(ODEGPU_E_ARG, "bad arguments");
   OG_CUDA(cudaSetDevice(b->device));
   OG_CUDA(cudaStreamSynchronize(b->stream));
@@ -1171,6 +1244,7 @@ int odegpuBatchSetControlsF32(odegpuBatchID b, int n_ctrl_steps, const float* jt
 
 int odegpuBatchRolloutForward(odegpuBatchID b, int n_steps, int ckpt_every) {
   if (b && b->lw) return fail(ODEGPU_E_ARG, "not available for a large world (one world above the on-chip limits)");
+  if (b && b->exact) return fail(ODEGPU_E_ARG, "not available with the dWorldStep stepper (odegpuBatchSetStepper)");
   if (!b || n_steps <= 0 || ckpt_every <= 0) return fail(ODEGPU_E_ARG, "bad arguments");
   OG_CUDA(cudaSetDevice(b->device));
   auto& R = b->ro;
@@ -1212,6 +1286,7 @@ int odegpuBatchRolloutForward(odegpuBatchID b, int n_steps, int ckpt_every) {
 int odegpuBatchRolloutBackward(odegpuBatchID b, const float* grad_final, float* grad_init, float* grad_jt,
                                float* grad_bf) {
   if (b && b->lw) return fail(ODEGPU_E_ARG, "not available for a large world (one world above the on-chip limits)");
+  if (b && b->exact) return fail(ODEGPU_E_ARG, "not available with the dWorldStep stepper (odegpuBatchSetStepper)");
   if (!b || !grad_final) return fail(ODEGPU_E_ARG, "bad arguments");
   auto& R = b->ro;
   if (!R.valid) return fail(ODEGPU_E_ARG, "no rollout recorded (odegpuBatchRolloutForward)");
@@ -1456,6 +1531,7 @@ int odegpuBatchLargeWorldStats(odegpuBatchID b, long long* out, int n, int reset
 
 int odegpuBatchStepTap(odegpuBatchID b, float* rows, float* lambda, float* fc, int* row_off) {
   if (b && b->lw) return fail(ODEGPU_E_ARG, "not available for a large world (one world above the on-chip limits)");
+  if (b && b->exact) return fail(ODEGPU_E_ARG, "not available with the dWorldStep stepper (odegpuBatchSetStepper)");
   if (!b) return fail(ODEGPU_E_ARG, "null batch");
   OG_CUDA(cudaSetDevice(b->device));
   DBuf<float> drows, dlam, dfc;
@@ -1636,6 +1712,9 @@ int ctx_step(WorldCtx* c, HostWorld& hw) {
     opt.feedback = B.feedback.p;
     opt.contact_feedback = c->contact_fb.p;
   }
+  B.exact = hw.exact;
+  B.n_worlds = 1;
+  B.h_world.assign(1, D);
   if (int e = B.launch(0, 1, 1, opt, false)) return e;
   if (hw.want_feedback) {
     hw.feedback.resize((size_t)D.njp * 12);

@@ -47,6 +47,7 @@ struct HostWorld {
   unsigned seed = 0;
   int status = 0;
   bool want_feedback = false;         // compute joint feedback in ctx_step
+  bool exact = false;                 // dWorldStep instead of dWorldQuickStep
   std::vector<float> feedback;        // out: [njp][12] persistent joints (f1 t1 f2 t2)
   std::vector<float> contact_feedback;// out: [contacts][12]
 };

@@ -28,7 +28,8 @@ enum {
   ST_NONFINITE = 8,          // a body state became NaN/Inf
   ST_HF_ZONE = 32,           // a geom covered more heightfield samples than the collider's buffer
   ST_PAIR_OVERFLOW = 64,     // large world: candidate partners or pairs above capacity
-  ST_SOLVE_STALL = 128       // large world: a bounded wait of the sweep gave up
+  ST_SOLVE_STALL = 128,      // large world: a bounded wait of the sweep gave up
+  ST_LCP_STOP = 256          // dWorldStep: the LCP stopped on a non-positive step (s <= 0)
 };
 
 // Row store: 32 words (128 bytes, one cache line) per constraint row.

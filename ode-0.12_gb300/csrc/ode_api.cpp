@@ -1107,7 +1107,13 @@ int dCollide(dGeomID o1, dGeomID o2, int flags, dContactGeom* contact, int skip)
 }
 
 // ---------------------------------------------------------------- step
-int dWorldQuickStep(dWorldID w, dReal stepsize) {
+static int world_step(dWorldID w, dReal stepsize, bool exact);
+int dWorldQuickStep(dWorldID w, dReal stepsize) { return world_step(w, stepsize, false); }
+// dWorldStep (ode/src/ode.cpp:1787): the same pipeline with the exact stepper
+// of ode/src/step.cpp and its Dantzig LCP on the GPU (world_exact.cuh)
+int dWorldStep(dWorldID w, dReal stepsize) { return world_step(w, stepsize, true); }
+
+static int world_step(dWorldID w, dReal stepsize, bool exact) {
   if (!w || !(stepsize > 0)) return 0;
   if (!w->ctx) {
     w->ctx = og::ctx_create(0);
@@ -1213,6 +1219,7 @@ int dWorldQuickStep(dWorldID w, dReal stepsize) {
   hw.want_feedback = false;
   for (const dxJoint* j : pj) hw.want_feedback |= j->feedback != nullptr;
   for (const dxJoint* j : cj) hw.want_feedback |= j->feedback != nullptr;
+  hw.exact = exact;
   if (og::ctx_step(w->ctx, hw) != 0) return 0;
   g_seed = hw.seed;
   if (hw.want_feedback) {

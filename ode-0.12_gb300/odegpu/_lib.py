@@ -68,6 +68,7 @@ def _declare(L):
         "odegpuBatchGetContacts": (i, [v, i, _P(f), i]),
         "odegpuBatchLargeWorldStats": (i, [v, _P(C.c_longlong), i, i]),
         "odegpuBatchRayCast": (i, [v, v, i, i, v]),
+        "odegpuBatchSetStepper": (i, [v, i]),
         "odegpuBatchRayCastAsync": (i, [v, v, i, i, v]),
         "odegpuGetLastError": (C.c_char_p, []),
     }

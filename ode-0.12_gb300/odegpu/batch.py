@@ -70,6 +70,11 @@ class Batch:
                     sweep_rest_ms=v[3] / 1e6, levels_max=v[4], sweeps=v[5], walks=v[6],
                     walk_copy_ms=v[7] / 1e6, cluster=v[8])
 
+    def set_stepper(self, exact=True):
+        """Step with dWorldStep (the exact stepper: dense LCP per island,
+        Dantzig pivoting) instead of dWorldQuickStep from now on."""
+        check(lib().odegpuBatchSetStepper(self.h, 1 if exact else 0))
+
     def ray_cast(self, rays, flags=1):
         """Nearest hit of each ray among its world's geoms (odegpuBatchRayCast).
         rays: a RAY_DTYPE array (world, body, start[3], dir[3], length; body -1
