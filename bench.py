@@ -359,6 +359,50 @@ def run_large_world(local_rank, steps=100, cpu_steps=20):
                          "gpu_speedup_same_steps": (t_cpu / cpu_steps) / (t_cpu_span / cpu_steps)}}
 
 
+def run_exact(local_rank, steps=100, cpu_worlds=N_WORLDS):
+    """dWorldStep (the exact stepper: dense LCP per island, the reference's
+    Dantzig pivoting) on the batched-worlds workload: world-steps/s of the
+    first `steps` steps from the initial state, timed with CUDA events on the
+    batch stream, beside the FP64 oracle port of dWorldStep on all host
+    threads over worlds [0, cpu_worlds) for the same steps."""
+    import torch
+    import oracle_lib as O
+    from odegpu.batch import Batch
+    sc = build_scene(N_WORLDS)
+    B = Batch(sc, device=local_rank)
+    B.set_stepper(True)
+    stream = torch.cuda.ExternalStream(B.stream_handle())
+    x0, seeds = B.state(), B.seeds()
+    B.step(3)
+    B.sync()
+    B.set_state(x0)
+    B.set_seeds(seeds)
+    B.set_step_index(0)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        e0.record(stream)
+    B.step(steps)
+    with torch.cuda.stream(stream):
+        e1.record(stream)
+    B.sync()
+    t = e0.elapsed_time(e1) / 1e3
+    nc, nr, ni = B.counts()
+    status = B.status()
+    B.close()
+    with O.exact_stepper():
+        v_cpu, thr, dt = cpu_baseline(sc, cpu_worlds, steps)
+    return {"metric": "world-steps/s, batched collide + dWorldStep (4096 worlds)", "value": N_WORLDS * steps / t,
+            "unit": "world-steps/s", "ms_per_step": 1e3 * t / steps,
+            "workload": WORKLOAD + f"; dWorldStep, first {steps} steps from the initial state",
+            "rows_last_step": int(nr.sum()), "contacts_last_step": int(nc.sum()),
+            "worlds_with_status": int((status != 0).sum()),
+            "worlds_with_lcp_stop": int(((status & 256) != 0).sum()),
+            "cpu_port": {"value": v_cpu, "unit": "world-steps/s", "cores": thr,
+                         "sample": f"FP64 oracle port of dWorldStep, worlds 0..{cpu_worlds - 1}, {steps} steps "
+                                   f"from the initial state ({dt:.1f} s)"}}
+
+
 def run_reference(args):
     rank, world_size, _ = rank_env()
     if rank != 0:
@@ -530,6 +574,8 @@ def run_ours(args):
             line["vehicles"] = run_vehicles(local_rank)
         if not args.no_large:
             line["large_world"] = run_large_world(local_rank)
+        if not args.no_exact:
+            line["exact_step"] = run_exact(local_rank)
         if not args.no_cpu:
             nw = min(N_WORLDS, args.cpu_worlds)
             v, thr, dt = cpu_baseline(sc, nw, args.steps)
@@ -557,6 +603,9 @@ def main():
     ap.add_argument("--only-vehicles", action="store_true",
                     help="print only the vehicle-batch measurement (for profiling)")
     ap.add_argument("--no-large", action="store_true")
+    ap.add_argument("--no-exact", action="store_true")
+    ap.add_argument("--only-exact", action="store_true",
+                    help="print only the dWorldStep measurement (for profiling)")
     ap.add_argument("--only-large", action="store_true",
                     help="print only the large-world measurement (for profiling)")
     ap.add_argument("--cpu-worlds", type=int, default=512)
@@ -564,12 +613,13 @@ def main():
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
-    elif args.only_adjoint or args.only_vehicles or args.only_large:
+    elif args.only_adjoint or args.only_vehicles or args.only_large or args.only_exact:
         import torch
         _, _, local_rank = rank_env()
         torch.cuda.set_device(local_rank)
         out = (run_adjoint(local_rank) if args.only_adjoint else
-               run_vehicles(local_rank) if args.only_vehicles else run_large_world(local_rank))
+               run_vehicles(local_rank) if args.only_vehicles else
+               run_exact(local_rank) if args.only_exact else run_large_world(local_rank))
         print(json.dumps(out), flush=True)
     else:
         run_ours(args)

@@ -10,7 +10,7 @@
  * include/odegpu_scene.h: dCollide over geom pairs i < k (skipping static
  * pairs, same-body pairs and jointed bodies), one contact joint per contact
  * with the surface of the higher surface index, the step's joint stops,
- * joint torques / slider forces and body forces, dWorldQuickStep,
+ * joint torques / slider forces and body forces, dWorldQuickStep (or dWorldStep),
  * dJointGroupEmpty.
  *
  * Input (text; numbers may be inf / nan):
@@ -71,6 +71,8 @@ static setp_fn stop_setter(int type) {
 
 int main(int argc, char** argv) {
   FILE* in = argc > 1 ? fopen(argv[1], "r") : stdin;
+  /* a second argument "exact" steps with dWorldStep instead of dWorldQuickStep */
+  const int exact = argc > 2 && strcmp(argv[2], "exact") == 0;
   double h[8], wp[10];
   if (!in || !rd(in, h, 8) || !rd(in, wp, 10)) return 2;
   const int nb = (int)h[0], ng = (int)h[1], nj = (int)h[2], ns = (int)h[3];
@@ -285,7 +287,8 @@ int main(int argc, char** argv) {
         dBodyAddTorque(bodies[i], f[3], f[4], f[5]);
       }
     }
-    if (!dWorldQuickStep(world, dt)) { fprintf(stderr, "step %d failed\n", s); return 1; }
+    const int ok = exact ? dWorldStep(world, dt) : dWorldQuickStep(world, dt);
+    if (!ok) { fprintf(stderr, "step %d failed\n", s); return 1; }
     dJointGroupEmpty(group);
   }
   for (int i = 0; i < nb; ++i) {

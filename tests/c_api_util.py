@@ -78,6 +78,6 @@ def scene_input(sc, steps, path):
         f.write("\n".join(lines) + "\n")
 
 
-def run_demo(exe, inp):
-    out = subprocess.run([exe, inp], check=True, capture_output=True, text=True).stdout
+def run_demo(exe, inp, *args):
+    out = subprocess.run([exe, inp, *args], check=True, capture_output=True, text=True).stdout
     return np.array([[float(x) for x in ln.split()] for ln in out.strip().splitlines()])

@@ -62,6 +62,15 @@ def test_scene_player_is_the_reference_harness_sequence():
                 st = U.run_demo(exe, inp).astype(np.float32).astype(np.float64)
                 ref = O.run_world(O.ref("s").ref_run_world, sc, w, 60)["state"][-1]
                 assert np.array_equal(st, ref), float(np.abs(st - ref).max())
+        # and with dWorldStep
+        sc = S.mechanisms(n_worlds=2, steps=60)
+        with O.exact_stepper(O.ref("s")):
+            for w in range(sc.n_worlds):
+                inp = os.path.join(d, f"in{w}.txt")
+                U.player_input(sc, w, 40, inp)
+                st = U.run_demo(exe, inp, "exact").astype(np.float32).astype(np.float64)
+                ref = O.run_world(O.ref("s").ref_run_world, sc, w, 40)["state"][-1]
+                assert np.array_equal(st, ref), float(np.abs(st - ref).max())
 
 
 def test_no_device_fails_loudly():

@@ -69,6 +69,33 @@ def test_scene_player_joint_types_on_gpu():
             assert np.abs(st[:, :3] - ref[:, :3]).max() < 2e-3, w
 
 
+def test_scene_player_dworldstep_on_gpu():
+    """scene_player.c stepping with dWorldStep (ode.cpp:1787), linked against
+    libodegpu, on the joint-type scene: agrees with the batched dWorldStep
+    path after 40 steps and with the FP64 oracle's dWorldStep after 20."""
+    from odegpu.batch import Batch
+    sc = S.mechanisms(n_worlds=2, steps=40)
+    steps = 40
+    B = Batch(sc)
+    B.set_stepper(True)
+    B.step(steps)
+    bt = B.state()
+    B.close()
+    with tempfile.TemporaryDirectory() as d:
+        exe = U.build_gpu_demo(os.path.join(d, "player"), src=U.PLAYER)
+        for w in range(sc.n_worlds):
+            b0, b1 = sc.world_bodies(w)
+            inp = os.path.join(d, "in.txt")
+            U.player_input(sc, w, steps, inp)
+            st = U.run_demo(exe, inp, "exact")
+            assert np.abs(st[:, :3] - bt[b0:b1, :3]).max() < 1e-4, w
+            U.player_input(sc, w, 20, inp)
+            st = U.run_demo(exe, inp, "exact")
+            with O.exact_stepper():
+                ref = O.run_world(O.oracle().oracle_run_world, sc, w, 20)["state"][-1]
+            assert np.abs(st[:, :3] - ref[:, :3]).max() < 2e-3, w
+
+
 def test_scene_player_cylinders_on_gpu():
     """scene_player.c with dCreateCylinder geoms (the plane world of the
     cylinder pile) linked against libodegpu: agrees with the batched path
