@@ -359,7 +359,7 @@ def run_large_world(local_rank, steps=100, cpu_steps=20):
                          "gpu_speedup_same_steps": (t_cpu / cpu_steps) / (t_cpu_span / cpu_steps)}}
 
 
-def run_exact(local_rank, steps=100, cpu_worlds=N_WORLDS):
+def run_exact(local_rank, steps=100, cpu_worlds=N_WORLDS, n_worlds=N_WORLDS):
     """dWorldStep (the exact stepper: dense LCP per island, the reference's
     Dantzig pivoting) on the batched-worlds workload: world-steps/s of the
     first `steps` steps from the initial state, timed with CUDA events on the
@@ -368,7 +368,7 @@ def run_exact(local_rank, steps=100, cpu_worlds=N_WORLDS):
     import torch
     import oracle_lib as O
     from odegpu.batch import Batch
-    sc = build_scene(N_WORLDS)
+    sc = build_scene(n_worlds)
     B = Batch(sc, device=local_rank)
     B.set_stepper(True)
     stream = torch.cuda.ExternalStream(B.stream_handle())
@@ -391,15 +391,16 @@ def run_exact(local_rank, steps=100, cpu_worlds=N_WORLDS):
     status = B.status()
     B.close()
     with O.exact_stepper():
-        v_cpu, thr, dt = cpu_baseline(sc, cpu_worlds, steps)
-    return {"metric": "world-steps/s, batched collide + dWorldStep (4096 worlds)", "value": N_WORLDS * steps / t,
+        v_cpu, thr, dt = cpu_baseline(sc, min(cpu_worlds, n_worlds), steps)
+    return {"metric": f"world-steps/s, batched collide + dWorldStep ({n_worlds} worlds)", "value": n_worlds * steps / t,
             "unit": "world-steps/s", "ms_per_step": 1e3 * t / steps,
-            "workload": WORKLOAD + f"; dWorldStep, first {steps} steps from the initial state",
+            "workload": WORKLOAD.replace("4096 worlds", f"{n_worlds} worlds") +
+                        f"; dWorldStep, first {steps} steps from the initial state",
             "rows_last_step": int(nr.sum()), "contacts_last_step": int(nc.sum()),
             "worlds_with_status": int((status != 0).sum()),
             "worlds_with_lcp_stop": int(((status & 256) != 0).sum()),
             "cpu_port": {"value": v_cpu, "unit": "world-steps/s", "cores": thr,
-                         "sample": f"FP64 oracle port of dWorldStep, worlds 0..{cpu_worlds - 1}, {steps} steps "
+                         "sample": f"FP64 oracle port of dWorldStep, worlds 0..{min(cpu_worlds, n_worlds) - 1}, {steps} steps "
                                    f"from the initial state ({dt:.1f} s)"}}
 
 
@@ -606,6 +607,8 @@ def main():
     ap.add_argument("--no-exact", action="store_true")
     ap.add_argument("--only-exact", action="store_true",
                     help="print only the dWorldStep measurement (for profiling)")
+    ap.add_argument("--exact-worlds", type=int, default=N_WORLDS)
+    ap.add_argument("--exact-steps", type=int, default=100)
     ap.add_argument("--only-large", action="store_true",
                     help="print only the large-world measurement (for profiling)")
     ap.add_argument("--cpu-worlds", type=int, default=512)
@@ -619,7 +622,8 @@ def main():
         torch.cuda.set_device(local_rank)
         out = (run_adjoint(local_rank) if args.only_adjoint else
                run_vehicles(local_rank) if args.only_vehicles else
-               run_exact(local_rank) if args.only_exact else run_large_world(local_rank))
+               run_exact(local_rank, steps=args.exact_steps, n_worlds=args.exact_worlds) if args.only_exact
+               else run_large_world(local_rank))
         print(json.dumps(out), flush=True)
     else:
         run_ours(args)

@@ -30,23 +30,48 @@ OG_D float xw_dot(const float* a, const float* b, int n, int lane) {
   return xw_sum(s);
 }
 
-// L x = b in place (unit lower triangular, rows of L at stride ns)
+// L x = b in place (unit lower triangular, rows of L at stride ns), in
+// blocks of 32 rows with lane j owning row r0 + j: each lane first takes the
+// dot product of its row with the solved part x[0, r0) (its own row, no
+// reduction), then the block's triangle is solved through shuffles.
 OG_D void xw_solve_l1(const float* L, float* B, int n, int ns, int lane) {
-  for (int r = 0; r < n; ++r) {
-    const float s = xw_dot(L + (size_t)r * ns, B, r, lane);
-    if (lane == 0) B[r] -= s;
+  for (int r0 = 0; r0 < n; r0 += 32) {
+    const int r = r0 + lane;
+    const int nbk = min(32, n - r0);
+    float v = 0.f;
+    if (r < n) {
+      const float* Lr = L + (size_t)r * ns;
+      float s = 0.f;
+      for (int c = 0; c < r0; ++c) s += Lr[c] * B[c];
+      v = B[r] - s;
+    }
+    for (int j = 0; j < nbk; ++j) {
+      const float xj = __shfl_sync(kFull, v, j);
+      if (lane > j && r < n) v -= L[(size_t)r * ns + r0 + j] * xj;
+    }
+    if (r < n) B[r] = v;
     __syncwarp();
   }
 }
-// L' x = b in place
+// L' x = b in place, blocks of 32 from the bottom; lane j owns row lo + j and
+// reads column-wise across the lanes (rows of L are contiguous).
 OG_D void xw_solve_l1t(const float* L, float* B, int n, int ns, int lane) {
-  for (int c = n - 1; c >= 0; --c) {
+  for (int hi = n; hi > 0; hi -= 32) {
+    const int lo = max(0, hi - 32);
+    const int a = lo + lane;
+    float v = 0.f;
+    if (a < hi) {
+      float s = 0.f;
+      for (int c = hi; c < n; ++c) s += L[(size_t)c * ns + a] * B[c];
+      v = B[a] - s;
+    }
+    for (int j = hi - 1 - lo; j >= 0; --j) {
+      const float xc = __shfl_sync(kFull, v, j);
+      if (lane < j && a < hi) v -= L[(size_t)(lo + j) * ns + a] * xc;
+    }
+    if (a < hi) B[a] = v;
     __syncwarp();
-    const float xc = B[c];
-    const float* Lc = L + (size_t)c * ns;
-    for (int a = lane; a < c; a += 32) B[a] -= Lc[a] * xc;
   }
-  __syncwarp();
 }
 // A = L D L' in place (L below the diagonal), d = 1 / D
 OG_D void xw_factor_ldlt(float* A, float* d, int n, int ns, int lane) {
@@ -808,24 +833,31 @@ OG_D void world_exact(const BatchDev& d, const ExactDev& XD, int w, int step, co
         const int ba[2] = {ria[kRowB1], ria[kRowB2]};
         const float* u = X.JinvM + (size_t)a * 12;
         float* Arow = X.A + (size_t)a * cap;
-        for (int c = 0; c < end; ++c) {
-          const float* rc = rows + (size_t)c * kRowWords;
-          const int* ric = reinterpret_cast<const int*>(rc);
-          float v = 0.f;
-          if (X.C[c] == qa) {
-            v = dot6(u, rc);
-            if (ba[1] >= 0) v += dot6(u + 6, rc + 6);
-          } else {
-            for (int half = 0; half < 2; ++half) {
-              const int bt = ba[half];
-              if (bt < 0) continue;
-              const int oh = (ric[kRowB1] == bt) ? 0 : (ric[kRowB2] == bt ? 1 : -1);
-              if (oh >= 0) v += dot6(u + 6 * half, rc + 6 * oh);
+        // only joints sharing a body with row a's joint give non-zero blocks
+        for (int c = 0; c < end; ++c) Arow[c] = 0.f;
+        for (int q = 0; q <= qa; ++q) {
+          const int ofs = X.jofs[q], mk = X.jm[X.rq[q]];
+          const int* riq = reinterpret_cast<const int*>(rows + (size_t)ofs * kRowWords);
+          const int qb1 = riq[kRowB1], qb2 = riq[kRowB2];
+          if (q == qa) {
+            for (int r = 0; r < mk; ++r) {
+              const float* rc = rows + (size_t)(ofs + r) * kRowWords;
+              float v = dot6(u, rc);
+              if (ba[1] >= 0) v += dot6(u + 6, rc + 6);
+              Arow[ofs + r] = v;
             }
+            continue;
           }
-          if (c == a) v += ra[kRowCfm] * h1;
-          Arow[c] = v;
+          for (int half = 0; half < 2; ++half) {
+            const int bt = ba[half];
+            if (bt < 0) continue;
+            const int oh = (qb1 == bt) ? 0 : (qb2 == bt ? 1 : -1);
+            if (oh < 0) continue;
+            for (int r = 0; r < mk; ++r)
+              Arow[ofs + r] += dot6(u + 6 * half, rows + (size_t)(ofs + r) * kRowWords + 6 * oh);
+          }
         }
+        Arow[a] += ra[kRowCfm] * h1;
         float t1[6];
         float bb = ra[kRowC] * h1;
         body_tmp1(d, D.body_off + ba[0], h1, t1);
