@@ -1084,6 +1084,11 @@ int odegpuBatchStepGraph(odegpuBatchID b, int n_steps) {
 int odegpuBatchSetStepper(odegpuBatchID b, int exact) {
   if (!b || (exact != 0 && exact != 1)) return fail(ODEGPU_E_ARG, "bad arguments");
   if (exact && b->lw) return fail(ODEGPU_E_ARG, "dWorldStep is not available for a large world");
+  if (exact) {
+    // the scratch is allocated here, outside any stream capture
+    OG_CUDA(cudaSetDevice(b->device));
+    if (int rc = b->ensure_exact_scratch()) return rc;
+  }
   b->exact = exact != 0;
   return 0;
 }

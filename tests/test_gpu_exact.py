@@ -108,6 +108,21 @@ def test_exact_joint_feedback_one_step():
         assert (np.abs(g[j0:j1] - ref) <= bar).all(), (w, np.abs(g[j0:j1] - ref).max(), np.abs(ref).max())
 
 
+def test_exact_launch_modes_agree():
+    """dWorldStep through one launch per step, a captured CUDA graph and one
+    world per launch gives bit-identical states."""
+    from odegpu.batch import Batch
+    sc = S.batched_worlds(n_worlds=16, seed=5)
+    out = []
+    for mode in ("step", "graph", "plain"):
+        B = Batch(sc)
+        B.set_stepper(True)
+        getattr(B, {"step": "step", "graph": "step_graph", "plain": "step_plain"}[mode])(12)
+        out.append(B.state())
+        B.close()
+    assert np.array_equal(out[0], out[1]) and np.array_equal(out[0], out[2])
+
+
 def test_exact_stepper_guards():
     """The adjoint, the parity taps and the autotuner refuse the exact
     stepper; switching back restores dWorldQuickStep."""
