@@ -196,11 +196,13 @@ class Mass(C.Structure):
     _fields_ = [("mass", C.c_float), ("c", C.c_float * 4), ("I", C.c_float * 12)]
 
 
-def test_joint_feedback_through_ode_api():
+@pytest.mark.parametrize("stepper", ["dWorldQuickStep", "dWorldStep"])
+def test_joint_feedback_through_ode_api(stepper):
     """dJointSetFeedback on a three-link ball chain hanging at rest from the
     environment: after a step the top joint's f1 carries the chain's weight,
     the middle joint two links' weight (force on body 1 = J1^T lambda), and f2
-    of the lower joints is the reaction on the link below."""
+    of the lower joints is the reaction on the link below; with either
+    stepper."""
     from odegpu._lib import lib
     L = lib()
     f, v, i = C.c_float, C.c_void_p, C.c_int
@@ -215,7 +217,8 @@ def test_joint_feedback_through_ode_api():
     L.dJointAttach.argtypes = [v, v, v]
     L.dJointSetBallAnchor.argtypes = [v, f, f, f]
     L.dJointSetFeedback.argtypes = [v, C.POINTER(JointFeedback)]
-    L.dWorldQuickStep.restype = i; L.dWorldQuickStep.argtypes = [v, f]
+    step = getattr(L, stepper)
+    step.restype = i; step.argtypes = [v, f]
     L.dWorldDestroy.argtypes = [v]
     w = L.dWorldCreate()
     L.dWorldSetGravity(w, 0.0, 0.0, -9.81)
@@ -238,7 +241,7 @@ def test_joint_feedback_through_ode_api():
         joints.append(j)
         fbs.append(fb)
     for _ in range(5):
-        assert L.dWorldQuickStep(w, 0.01) == 1
+        assert step(w, 0.01) == 1
     weight = m * 9.81
     # joint k holds link k (body 1) to link k-1 / the environment (body 2)
     for k in range(3):
