@@ -275,6 +275,13 @@ void dGeomHeightfieldDataDestroy(dHeightfieldDataID d);                 /* :1171
 void dGeomHeightfieldDataBuildSingle(dHeightfieldDataID d, const float* pHeightData, int bCopyHeightData,
                                      dReal width, dReal depth, int widthSamples, int depthSamples,
                                      dReal scale, dReal offset, dReal thickness, int bWrap);  /* :1361 */
+void dGeomHeightfieldDataBuildByte(dHeightfieldDataID d, const unsigned char* pHeightData, int bCopyHeightData,
+                                   dReal width, dReal depth, int widthSamples, int depthSamples,
+                                   dReal scale, dReal offset, dReal thickness, int bWrap);  /* :1263 */
+void dGeomHeightfieldDataBuildShort(dHeightfieldDataID d, const short* pHeightData, int bCopyHeightData,
+                                    dReal width, dReal depth, int widthSamples, int depthSamples,
+                                    dReal scale, dReal offset, dReal thickness, int bWrap);  /* :1311 */
+void dGeomHeightfieldDataSetBounds(dHeightfieldDataID d, dReal minHeight, dReal maxHeight);  /* :1433 */
 void dGeomHeightfieldDataBuildDouble(dHeightfieldDataID d, const double* pHeightData, int bCopyHeightData,
                                      dReal width, dReal depth, int widthSamples, int depthSamples,
                                      dReal scale, dReal offset, dReal thickness, int bWrap);  /* :1411 */

@@ -61,6 +61,7 @@ struct dxHeightfieldData {
   std::vector<float> heights;      // copied at build time (x fastest, then z)
   float* d_heights = nullptr;      // device copy
   bool built = false;
+  double min_height = -INFINITY, max_height = INFINITY;   // dGeomHeightfieldDataSetBounds
 };
 
 struct dxGeom {
@@ -1001,6 +1002,30 @@ void dGeomHeightfieldDataBuildDouble(dHeightfieldDataID d, const double* pHeight
     return;
   for (size_t k = 0; k < d->heights.size(); ++k) d->heights[k] = (float)pHeightData[k];
   d->built = og::upload_heights(d->heights, &d->d_heights) == 0;
+}
+void dGeomHeightfieldDataBuildByte(dHeightfieldDataID d, const unsigned char* pHeightData, int, dReal width,
+                                   dReal depth, int widthSamples, int depthSamples, dReal scale, dReal offset,
+                                   dReal thickness, int bWrap) {
+  if (!pHeightData || !hf_shape(d, width, depth, widthSamples, depthSamples, scale, offset, thickness, bWrap))
+    return;
+  for (size_t k = 0; k < d->heights.size(); ++k) d->heights[k] = (float)pHeightData[k];
+  d->built = og::upload_heights(d->heights, &d->d_heights) == 0;
+}
+void dGeomHeightfieldDataBuildShort(dHeightfieldDataID d, const short* pHeightData, int, dReal width, dReal depth,
+                                    int widthSamples, int depthSamples, dReal scale, dReal offset, dReal thickness,
+                                    int bWrap) {
+  if (!pHeightData || !hf_shape(d, width, depth, widthSamples, depthSamples, scale, offset, thickness, bWrap))
+    return;
+  for (size_t k = 0; k < d->heights.size(); ++k) d->heights[k] = (float)pHeightData[k];
+  d->built = og::upload_heights(d->heights, &d->d_heights) == 0;
+}
+// The bounds tighten the field's bounding box, which only a space's early
+// rejection reads (heightfield.cpp:147-156); dCollide does not, so they are kept
+// for completeness only.
+void dGeomHeightfieldDataSetBounds(dHeightfieldDataID d, dReal minHeight, dReal maxHeight) {
+  if (!d) return;
+  d->min_height = minHeight;
+  d->max_height = maxHeight;
 }
 dGeomID dCreateHeightfield(dSpaceID, dHeightfieldDataID data, int bPlaceable) {
   const double p[4] = {0, 0, 0, 0};

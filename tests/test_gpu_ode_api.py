@@ -304,3 +304,69 @@ def test_dcollide_heightfield_through_ode_api():
     L.dGeomHeightfieldDataDestroy(hd)
     assert not count_mism, count_mism[:10]
     assert worst < 1e-4, worst
+
+
+def test_hinge_motor_velocity_after_one_dworldstep():
+    """The reference's test_Hinge_dParamVel (tests/joints/hinge.cpp:898-922):
+    two unit bodies at the origin on a hinge along x, motor FMax = inf,
+    Vel = 100; after one dWorldStep(0.001) the relative angular velocity is
+    (100, 0, 0) within the reference's dSINGLE tolerance (1e-2 x 100)."""
+    from odegpu._lib import lib
+    L = lib()
+    f, v, i = C.c_float, C.c_void_p, C.c_int
+    L.dWorldCreate.restype = v
+    L.dBodyCreate.restype = v; L.dBodyCreate.argtypes = [v]
+    L.dBodySetPosition.argtypes = [v, f, f, f]
+    L.dJointCreateHinge.restype = v; L.dJointCreateHinge.argtypes = [v, v]
+    L.dJointAttach.argtypes = [v, v, v]
+    L.dJointSetHingeAnchor.argtypes = [v, f, f, f]
+    L.dJointSetHingeParam.argtypes = [v, i, f]
+    L.dWorldStep.restype = i; L.dWorldStep.argtypes = [v, f]
+    L.dBodyGetAngularVel.restype = C.POINTER(f); L.dBodyGetAngularVel.argtypes = [v]
+    L.dWorldDestroy.argtypes = [v]
+    dParamVel, dParamFMax = 2, 3     # include/ode/common.h: dParamLoStop = 0, dParamHiStop, dParamVel, dParamFMax
+    w = L.dWorldCreate()
+    b1, b2 = L.dBodyCreate(w), L.dBodyCreate(w)
+    L.dBodySetPosition(b1, 0, 0, 0)
+    L.dBodySetPosition(b2, 0, 0, 0)
+    j = L.dJointCreateHinge(w, None)
+    L.dJointAttach(j, b1, b2)
+    L.dJointSetHingeAnchor(j, 0, 0, 0)
+    L.dJointSetHingeParam(j, dParamFMax, float("inf"))
+    L.dJointSetHingeParam(j, dParamVel, 100.0)
+    assert L.dWorldStep(w, 0.001) == 1
+    v1, v2 = L.dBodyGetAngularVel(b1), L.dBodyGetAngularVel(b2)
+    rvel = np.array([v1[k] - v2[k] for k in range(3)])
+    assert np.abs(rvel - np.array([100.0, 0.0, 0.0])).max() < 1.0, rvel
+    L.dWorldDestroy(w)
+
+
+def test_heightfield_ray_outside_bounds():
+    """The reference's test_collision_heightfield_ray_fail
+    (tests/collision.cpp:103-131): a 4 x 4 byte heightfield with bounds, a
+    ray of length 20 outside the field pointing along -y; dCollide must not
+    fail and, as the reference built here returns, finds no contact."""
+    from odegpu._lib import lib
+    L = lib()
+    f, v, i = C.c_float, C.c_void_p, C.c_int
+    L.dGeomHeightfieldDataCreate.restype = v
+    L.dGeomHeightfieldDataBuildByte.argtypes = [v, C.c_char_p, i, f, f, i, i, f, f, f, i]
+    L.dGeomHeightfieldDataSetBounds.argtypes = [v, f, f]
+    L.dCreateHeightfield.restype = v; L.dCreateHeightfield.argtypes = [v, v, i]
+    L.dCreateRay.restype = v; L.dCreateRay.argtypes = [v, f]
+    L.dGeomRaySet.argtypes = [v, f, f, f, f, f, f]
+    L.dCollide.restype = i; L.dCollide.argtypes = [v, v, i, v, i]
+    L.dGeomDestroy.argtypes = [v]
+    L.dGeomHeightfieldDataDestroy.argtypes = [v]
+    hd = L.dGeomHeightfieldDataCreate()
+    L.dGeomHeightfieldDataBuildByte(hd, b"1234567890123456", 0, 4, 4, 4, 4, 1, 0, 0, 0)
+    L.dGeomHeightfieldDataSetBounds(hd, float(ord("0")), float(ord("9")))
+    h = L.dCreateHeightfield(None, hd, 1)
+    r = L.dCreateRay(None, 20)
+    L.dGeomRaySet(r, 5, 10, 1, 0, -1, 0)
+    out = (ContactGeom * 10)()
+    assert L.dCollide(r, h, 10, out, C.sizeof(ContactGeom)) == 0
+    assert L.dCollide(h, r, 10, out, C.sizeof(ContactGeom)) == 0
+    L.dGeomDestroy(r)
+    L.dGeomDestroy(h)
+    L.dGeomHeightfieldDataDestroy(hd)
