@@ -173,6 +173,9 @@ void dJointSetBallParam(dJointID j, int parameter, dReal value);         /* :179
 void dJointGetBallAnchor(dJointID j, dVector3 result);                   /* :2351 */
 void dJointSetHingeAnchor(dJointID j, dReal x, dReal y, dReal z);        /* :1803 */
 void dJointSetHingeAxis(dJointID j, dReal x, dReal y, dReal z);          /* :1811 */
+void dJointGetHingeAnchor(dJointID j, dVector3 result);                  /* :2378 */
+void dJointGetHingeAnchor2(dJointID j, dVector3 result);                 /* :2388 */
+void dJointGetHingeAxis(dJointID j, dVector3 result);                    /* :2394 */
 void dJointSetHingeParam(dJointID j, int parameter, dReal value);        /* :1847 */
 dReal dJointGetHingeAngle(dJointID j);                                   /* :2414 */
 dReal dJointGetHingeAngleRate(dJointID j);                               /* :2420 */
@@ -180,6 +183,10 @@ void dJointAddHingeTorque(dJointID j, dReal torque);                     /* :185
 void dJointSetHinge2Anchor(dJointID j, dReal x, dReal y, dReal z);       /* :1890 */
 void dJointSetHinge2Axis1(dJointID j, dReal x, dReal y, dReal z);        /* :1896 */
 void dJointSetHinge2Axis2(dJointID j, dReal x, dReal y, dReal z);        /* :1902 */
+void dJointGetHinge2Anchor(dJointID j, dVector3 result);                 /* :2459 */
+void dJointGetHinge2Anchor2(dJointID j, dVector3 result);                /* :2469 */
+void dJointGetHinge2Axis1(dJointID j, dVector3 result);                  /* :2475 */
+void dJointGetHinge2Axis2(dJointID j, dVector3 result);                  /* :2481 */
 void dJointSetHinge2Param(dJointID j, int parameter, dReal value);       /* :1908 */
 void dJointAddHinge2Torques(dJointID j, dReal torque1, dReal torque2);   /* :1916 */
 dReal dJointGetHinge2Angle1(dJointID j);                                 /* :2493 */
@@ -241,6 +248,28 @@ unsigned long dRand(void);                                               /* :42 
 unsigned long dRandGetSeed(void);                                        /* :45 */
 void dRandSetSeed(unsigned long s);                                      /* :46 */
 int dRandInt(int n);                                                     /* :51 */
+
+/* rotation and vector utilities: include/ode/rotation.h, include/ode/odemath.h
+ * (FP32, the reference's operation order) */
+void dRSetIdentity(dMatrix3 R);                                          /* rotation.h:34 */
+void dRFromAxisAndAngle(dMatrix3 R, dReal ax, dReal ay, dReal az, dReal angle);   /* :36 */
+void dRFromEulerAngles(dMatrix3 R, dReal phi, dReal theta, dReal psi);  /* :39 */
+void dRFrom2Axes(dMatrix3 R, dReal ax, dReal ay, dReal az, dReal bx, dReal by, dReal bz);  /* :41 */
+void dRFromZAxis(dMatrix3 R, dReal ax, dReal ay, dReal az);             /* :44 */
+void dQSetIdentity(dQuaternion q);                                       /* :46 */
+void dQFromAxisAndAngle(dQuaternion q, dReal ax, dReal ay, dReal az, dReal angle);  /* :48 */
+void dQMultiply0(dQuaternion qa, const dQuaternion qb, const dQuaternion qc);  /* :53 */
+void dQMultiply1(dQuaternion qa, const dQuaternion qb, const dQuaternion qc);  /* :55 */
+void dQMultiply2(dQuaternion qa, const dQuaternion qb, const dQuaternion qc);  /* :57 */
+void dQMultiply3(dQuaternion qa, const dQuaternion qb, const dQuaternion qc);  /* :59 */
+void dRfromQ(dMatrix3 R, const dQuaternion q);                           /* :61 */
+void dQfromR(dQuaternion q, const dMatrix3 R);                           /* :62 */
+void dDQfromW(dReal dq[4], const dVector3 w, const dQuaternion q);      /* :63 */
+int dSafeNormalize3(dVector3 a);                                         /* odemath.h:424 */
+int dSafeNormalize4(dVector4 a);                                         /* :425 */
+void dNormalize3(dVector3 a);                                            /* :426 */
+void dNormalize4(dVector4 a);                                            /* :427 */
+void dPlaneSpace(const dVector3 n, dVector3 p, dVector3 q);              /* :462 */
 
 /* collision: include/ode/collision.h (space argument must be 0: spaces are
  * not on this path, pairs come from the caller) */

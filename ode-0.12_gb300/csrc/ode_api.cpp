@@ -186,6 +186,26 @@ void world_anchor1(const dxJoint* j, double* out) {
   for (int k = 0; k < 3; ++k) out[k] = a[k] + b->pos[k];
 }
 
+// getAnchor2 (ode/src/joints/joint.cpp:329-345): body 2's anchor in world
+// coordinates, or the stored world point when there is no body 2
+void world_anchor2(const dxJoint* j, double* out) {
+  const dxBody* b = j->body[1];
+  if (!b) { for (int k = 0; k < 3; ++k) out[k] = j->h.anchor2[k]; return; }
+  double R[12], a[3];
+  for (int k = 0; k < 12; ++k) R[k] = b->R[k];
+  og_host::mul0_331(a, R, j->h.anchor2);
+  for (int k = 0; k < 3; ++k) out[k] = a[k] + b->pos[k];
+}
+// dJointGet{Hinge,Hinge2}Anchor[2] (hinge.cpp, hinge2.cpp): the first anchor
+// is body 1's unless the joint is attached reversed
+void joint_anchor(const dxJoint* j, bool second, dVector3 r) {
+  if (!j->body[0]) return;
+  double a[3];
+  if (second != (j->reverse != 0)) world_anchor2(j, a);
+  else world_anchor1(j, a);
+  for (int k = 0; k < 3; ++k) r[k] = (dReal)a[k];
+}
+
 }  // namespace
 
 extern "C" {
@@ -495,6 +515,10 @@ void dJointSetHingeAnchor(dJointID j, dReal x, dReal y, dReal z) {
   og_host::set_anchors(j->h, jb.B, x, y, z, j->h.anchor1, j->h.anchor2);
   og_host::hinge_qrel(j->h, jb.B);
 }
+void dJointGetHingeAnchor(dJointID j, dVector3 r) { joint_anchor(j, false, r); }
+void dJointGetHingeAnchor2(dJointID j, dVector3 r) { joint_anchor(j, true, r); }
+void dJointGetHinge2Anchor(dJointID j, dVector3 r) { joint_anchor(j, false, r); }
+void dJointGetHinge2Anchor2(dJointID j, dVector3 r) { joint_anchor(j, true, r); }
 void dJointSetHingeAxis(dJointID j, dReal x, dReal y, dReal z) {
   JB jb(j);
   og_host::set_axes(j->h, jb.B, x, y, z, j->h.axis1, j->h.axis2);
@@ -634,6 +658,13 @@ void world_axis2(const dxJoint* j, const double* axis, dVector3 r) {
   } else {
     for (int k = 0; k < 3; ++k) r[k] = (dReal)axis[k];
   }
+}
+
+// hinge / hinge2 axes in world coordinates (hinge.cpp, hinge2.cpp)
+void dJointGetHingeAxis(dJointID j, dVector3 r) { world_axis1(j, j->h.axis1, r); }
+void dJointGetHinge2Axis1(dJointID j, dVector3 r) { world_axis1(j, j->h.axis1, r); }
+void dJointGetHinge2Axis2(dJointID j, dVector3 r) {
+  if (j->body[1]) world_axis2(j, j->h.axis2, r);
 }
 
 // slider (ode/src/joints/slider.cpp)
@@ -1270,6 +1301,179 @@ static int world_step(dWorldID w, dReal stepsize, bool exact) {
     for (int k = 0; k < 4; ++k) b->facc[k] = b->tacc[k] = 0;
   }
   return hw.status == 0 ? 1 : 0;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------- rotation / vector utilities
+// ode/src/rotation.cpp and ode/src/odemath.cpp, in dReal (FP32) arithmetic with
+// the reference's operation order, so that a program's set-up code gives the
+// values the reference's dSINGLE build gives.
+extern "C" {
+
+int dSafeNormalize3(dVector3 a) {   // odemath.cpp:74-117
+  const float aa[3] = {std::fabs(a[0]), std::fabs(a[1]), std::fabs(a[2])};
+  int idx;
+  if (aa[1] > aa[0]) {
+    idx = (aa[2] > aa[1]) ? 2 : 1;
+  } else if (aa[2] > aa[0]) {
+    idx = 2;
+  } else {
+    if (aa[0] <= 0.f) { a[0] = 1; a[1] = 0; a[2] = 0; return 0; }
+    idx = 0;
+  }
+  a[0] /= aa[idx]; a[1] /= aa[idx]; a[2] /= aa[idx];
+  const float l = 1.0f / std::sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
+  a[0] *= l; a[1] *= l; a[2] *= l;
+  return 1;
+}
+void dNormalize3(dVector3 a) { dSafeNormalize3(a); }
+int dSafeNormalize4(dVector4 a) {   // odemath.cpp:119-138
+  float l = a[0] * a[0] + a[1] * a[1] + a[2] * a[2] + a[3] * a[3];
+  if (l > 0.f) {
+    l = 1.0f / std::sqrt(l);
+    a[0] *= l; a[1] *= l; a[2] *= l; a[3] *= l;
+    return 1;
+  }
+  a[0] = 1; a[1] = 0; a[2] = 0; a[3] = 0;
+  return 0;
+}
+void dNormalize4(dVector4 a) { dSafeNormalize4(a); }
+void dPlaneSpace(const dVector3 n, dVector3 p, dVector3 q) {   // odemath.cpp:151-178
+  if (std::fabs(n[2]) > 0.70710678118654752440f) {
+    const float a = n[1] * n[1] + n[2] * n[2];
+    const float k = 1.0f / std::sqrt(a);
+    p[0] = 0; p[1] = -n[2] * k; p[2] = n[1] * k;
+    q[0] = a * k; q[1] = -n[0] * p[2]; q[2] = n[0] * p[1];
+  } else {
+    const float a = n[0] * n[0] + n[1] * n[1];
+    const float k = 1.0f / std::sqrt(a);
+    p[0] = -n[1] * k; p[1] = n[0] * k; p[2] = 0;
+    q[0] = -n[2] * p[1]; q[1] = n[2] * p[0]; q[2] = a * k;
+  }
+}
+void dRSetIdentity(dMatrix3 R) {
+  for (int k = 0; k < 12; ++k) R[k] = 0;
+  R[0] = R[5] = R[10] = 1;
+}
+void dQSetIdentity(dQuaternion q) { q[0] = 1; q[1] = q[2] = q[3] = 0; }
+void dQFromAxisAndAngle(dQuaternion q, dReal ax, dReal ay, dReal az, dReal angle) {   // rotation.cpp:169-189
+  float l = ax * ax + ay * ay + az * az;
+  if (l > 0.f) {
+    angle *= 0.5f;
+    q[0] = std::cos(angle);
+    l = std::sin(angle) * (1.0f / std::sqrt(l));
+    q[1] = ax * l; q[2] = ay * l; q[3] = az * l;
+  } else {
+    dQSetIdentity(q);
+  }
+}
+void dRfromQ(dMatrix3 R, const dQuaternion q) {   // rotation.cpp:236-255
+  const float qq1 = 2 * q[1] * q[1], qq2 = 2 * q[2] * q[2], qq3 = 2 * q[3] * q[3];
+  R[0] = 1 - qq2 - qq3; R[1] = 2 * (q[1] * q[2] - q[0] * q[3]); R[2] = 2 * (q[1] * q[3] + q[0] * q[2]); R[3] = 0;
+  R[4] = 2 * (q[1] * q[2] + q[0] * q[3]); R[5] = 1 - qq1 - qq3; R[6] = 2 * (q[2] * q[3] - q[0] * q[1]); R[7] = 0;
+  R[8] = 2 * (q[1] * q[3] - q[0] * q[2]); R[9] = 2 * (q[2] * q[3] + q[0] * q[1]); R[10] = 1 - qq1 - qq2; R[11] = 0;
+}
+void dRFromAxisAndAngle(dMatrix3 R, dReal ax, dReal ay, dReal az, dReal angle) {
+  dQuaternion q;
+  dQFromAxisAndAngle(q, ax, ay, az, angle);
+  dRfromQ(R, q);
+}
+void dRFromEulerAngles(dMatrix3 R, dReal phi, dReal theta, dReal psi) {   // rotation.cpp:69-91
+  const float sphi = std::sin(phi), cphi = std::cos(phi), stheta = std::sin(theta), ctheta = std::cos(theta);
+  const float spsi = std::sin(psi), cpsi = std::cos(psi);
+  R[0] = cpsi * ctheta; R[1] = spsi * ctheta; R[2] = -stheta; R[3] = 0;
+  R[4] = cpsi * stheta * sphi - spsi * cphi; R[5] = spsi * stheta * sphi + cpsi * cphi; R[6] = ctheta * sphi;
+  R[7] = 0;
+  R[8] = cpsi * stheta * cphi + spsi * sphi; R[9] = spsi * stheta * cphi - cpsi * sphi; R[10] = ctheta * cphi;
+  R[11] = 0;
+}
+void dRFrom2Axes(dMatrix3 R, dReal ax, dReal ay, dReal az, dReal bx, dReal by, dReal bz) {   // rotation.cpp:94-133
+  float l = std::sqrt(ax * ax + ay * ay + az * az);
+  if (l <= 0.f) return;
+  l = 1.0f / l;
+  ax *= l; ay *= l; az *= l;
+  const float k = ax * bx + ay * by + az * bz;
+  bx -= k * ax; by -= k * ay; bz -= k * az;
+  l = std::sqrt(bx * bx + by * by + bz * bz);
+  if (l <= 0.f) return;
+  l = 1.0f / l;
+  bx *= l; by *= l; bz *= l;
+  R[0] = ax; R[4] = ay; R[8] = az;
+  R[1] = bx; R[5] = by; R[9] = bz;
+  R[2] = -by * az + ay * bz; R[6] = -bz * ax + az * bx; R[10] = -bx * ay + ax * by;
+  R[3] = R[7] = R[11] = 0;
+}
+void dRFromZAxis(dMatrix3 R, dReal ax, dReal ay, dReal az) {   // rotation.cpp:136-156
+  dVector3 n = {ax, ay, az, 0}, p, q;
+  dNormalize3(n);
+  dPlaneSpace(n, p, q);
+  R[0] = p[0]; R[4] = p[1]; R[8] = p[2];
+  R[1] = q[0]; R[5] = q[1]; R[9] = q[2];
+  R[2] = n[0]; R[6] = n[1]; R[10] = n[2];
+  R[3] = R[7] = R[11] = 0;
+}
+void dQMultiply0(dQuaternion qa, const dQuaternion qb, const dQuaternion qc) {   // rotation.cpp:191-226
+  const float a0 = qb[0] * qc[0] - qb[1] * qc[1] - qb[2] * qc[2] - qb[3] * qc[3];
+  const float a1 = qb[0] * qc[1] + qb[1] * qc[0] + qb[2] * qc[3] - qb[3] * qc[2];
+  const float a2 = qb[0] * qc[2] + qb[2] * qc[0] + qb[3] * qc[1] - qb[1] * qc[3];
+  const float a3 = qb[0] * qc[3] + qb[3] * qc[0] + qb[1] * qc[2] - qb[2] * qc[1];
+  qa[0] = a0; qa[1] = a1; qa[2] = a2; qa[3] = a3;
+}
+void dQMultiply1(dQuaternion qa, const dQuaternion qb, const dQuaternion qc) {
+  const float a0 = qb[0] * qc[0] + qb[1] * qc[1] + qb[2] * qc[2] + qb[3] * qc[3];
+  const float a1 = qb[0] * qc[1] - qb[1] * qc[0] - qb[2] * qc[3] + qb[3] * qc[2];
+  const float a2 = qb[0] * qc[2] - qb[2] * qc[0] - qb[3] * qc[1] + qb[1] * qc[3];
+  const float a3 = qb[0] * qc[3] - qb[3] * qc[0] - qb[1] * qc[2] + qb[2] * qc[1];
+  qa[0] = a0; qa[1] = a1; qa[2] = a2; qa[3] = a3;
+}
+void dQMultiply2(dQuaternion qa, const dQuaternion qb, const dQuaternion qc) {
+  const float a0 = qb[0] * qc[0] + qb[1] * qc[1] + qb[2] * qc[2] + qb[3] * qc[3];
+  const float a1 = -qb[0] * qc[1] + qb[1] * qc[0] - qb[2] * qc[3] + qb[3] * qc[2];
+  const float a2 = -qb[0] * qc[2] + qb[2] * qc[0] - qb[3] * qc[1] + qb[1] * qc[3];
+  const float a3 = -qb[0] * qc[3] + qb[3] * qc[0] - qb[1] * qc[2] + qb[2] * qc[1];
+  qa[0] = a0; qa[1] = a1; qa[2] = a2; qa[3] = a3;
+}
+void dQMultiply3(dQuaternion qa, const dQuaternion qb, const dQuaternion qc) {
+  const float a0 = qb[0] * qc[0] - qb[1] * qc[1] - qb[2] * qc[2] - qb[3] * qc[3];
+  const float a1 = -qb[0] * qc[1] - qb[1] * qc[0] + qb[2] * qc[3] - qb[3] * qc[2];
+  const float a2 = -qb[0] * qc[2] - qb[2] * qc[0] + qb[3] * qc[1] - qb[1] * qc[3];
+  const float a3 = -qb[0] * qc[3] - qb[3] * qc[0] + qb[1] * qc[2] - qb[2] * qc[1];
+  qa[0] = a0; qa[1] = a1; qa[2] = a2; qa[3] = a3;
+}
+void dQfromR(dQuaternion q, const dMatrix3 R) {   // rotation.cpp:258-306
+  const float tr = R[0] + R[5] + R[10];
+  float s;
+  if (tr >= 0) {
+    s = std::sqrt(tr + 1);
+    q[0] = 0.5f * s;
+    s = 0.5f * (1.0f / s);
+    q[1] = (R[9] - R[6]) * s; q[2] = (R[2] - R[8]) * s; q[3] = (R[4] - R[1]) * s;
+    return;
+  }
+  const int c = (R[5] > R[0]) ? ((R[10] > R[5]) ? 2 : 1) : ((R[10] > R[0]) ? 2 : 0);
+  if (c == 0) {
+    s = std::sqrt((R[0] - (R[5] + R[10])) + 1);
+    q[1] = 0.5f * s;
+    s = 0.5f * (1.0f / s);
+    q[2] = (R[1] + R[4]) * s; q[3] = (R[8] + R[2]) * s; q[0] = (R[9] - R[6]) * s;
+  } else if (c == 1) {
+    s = std::sqrt((R[5] - (R[10] + R[0])) + 1);
+    q[2] = 0.5f * s;
+    s = 0.5f * (1.0f / s);
+    q[3] = (R[6] + R[9]) * s; q[1] = (R[1] + R[4]) * s; q[0] = (R[2] - R[8]) * s;
+  } else {
+    s = std::sqrt((R[10] - (R[0] + R[5])) + 1);
+    q[3] = 0.5f * s;
+    s = 0.5f * (1.0f / s);
+    q[1] = (R[8] + R[2]) * s; q[2] = (R[6] + R[9]) * s; q[0] = (R[4] - R[1]) * s;
+  }
+}
+void dDQfromW(dReal dq[4], const dVector3 w, const dQuaternion q) {   // rotation.cpp:310-317
+  dq[0] = 0.5f * (-w[0] * q[1] - w[1] * q[2] - w[2] * q[3]);
+  dq[1] = 0.5f * (w[0] * q[0] + w[1] * q[3] - w[2] * q[2]);
+  dq[2] = 0.5f * (-w[0] * q[3] + w[1] * q[0] + w[2] * q[1]);
+  dq[3] = 0.5f * (w[0] * q[2] - w[1] * q[1] + w[2] * q[0]);
 }
 
 }  // extern "C"

@@ -87,3 +87,59 @@ def test_no_device_fails_loudly():
     from odegpu.batch import Batch
     with pytest.raises(OdeGpuError, match="CUDA"):
         Batch(S.box_drop(seed=0))
+
+
+def test_rotation_utilities_match_reference_fp32():
+    """dRFromAxisAndAngle, dRFromEulerAngles, dRFrom2Axes, dRFromZAxis,
+    dQFromAxisAndAngle, dQMultiply0-3, dRfromQ, dQfromR, dDQfromW,
+    dSafeNormalize3/4 and dPlaneSpace of the library (host code, no GPU)
+    against the reference's dSINGLE build on seeded inputs: bit-identical
+    (the reference's transcendentals are the same libm calls)."""
+    import ctypes as C
+    import numpy as np
+    import c_api_util as U
+    import oracle_lib as O
+    if not O.ref_available("s"):
+        pytest.skip("reference not built in this checkout")
+    ours = C.CDLL(os.path.join(ROOT, "ode-0.12_gb300", "libodegpu.so"))
+    ref = C.CDLL(os.path.join(ROOT, "oracle", "_ref", "libode_ref_s.so"))
+    F = C.c_float
+    V4 = F * 4
+    M12 = F * 12
+    rng = np.random.default_rng(4)
+    for lib in (ours, ref):
+        for name in ("dRFromAxisAndAngle", "dQFromAxisAndAngle"):
+            getattr(lib, name).argtypes = [C.c_void_p, F, F, F, F]
+        lib.dRFromEulerAngles.argtypes = [C.c_void_p, F, F, F]
+        lib.dRFrom2Axes.argtypes = [C.c_void_p, F, F, F, F, F, F]
+        lib.dRFromZAxis.argtypes = [C.c_void_p, F, F, F]
+    for _ in range(200):
+        a = [float(x) for x in rng.normal(size=7)]
+        outs = []
+        for lib in (ours, ref):
+            R1, R2, R3, R4 = M12(), M12(), M12(), M12()
+            q1, q2 = V4(), V4()
+            lib.dRFromAxisAndAngle(R1, *a[:4])
+            lib.dRFromEulerAngles(R2, *a[:3])
+            lib.dRFrom2Axes(R3, *a[:6])
+            lib.dRFromZAxis(R4, *a[:3])
+            lib.dQFromAxisAndAngle(q1, *a[3:7])
+            lib.dQfromR(q2, R1)
+            qm = []
+            for k in range(4):
+                r = V4()
+                getattr(lib, f"dQMultiply{k}")(r, q1, q2)
+                qm += list(r)
+            R5, dq = M12(), V4()
+            lib.dRfromQ(R5, q1)
+            w = V4(*a[:3], 0.0)
+            lib.dDQfromW(dq, w, q1)
+            n3, n4 = V4(*a[:3], 0.0), V4(*a[:4])
+            r3 = lib.dSafeNormalize3(n3)
+            r4 = lib.dSafeNormalize4(n4)
+            p, q = V4(), V4()
+            lib.dPlaneSpace(n3, p, q)
+            outs.append(np.array(list(R1) + list(R2) + list(R3) + list(R4) + list(q1) + list(q2) + qm + list(R5) +
+                                 list(dq) + list(n3)[:3] + list(n4) + [r3, r4] + list(p)[:3] + list(q)[:3],
+                                 dtype=np.float32))
+        assert np.array_equal(outs[0], outs[1]), np.abs(outs[0] - outs[1]).max()

@@ -370,3 +370,71 @@ def test_heightfield_ray_outside_bounds():
     L.dGeomDestroy(r)
     L.dGeomDestroy(h)
     L.dGeomHeightfieldDataDestroy(hd)
+
+
+@pytest.mark.parametrize("kind,tol", [("Ball", 1e-4), ("Hinge", 1e-6), ("Hinge2", 1e-4)])
+def test_reference_joint_fixtures_with_dworldstep(kind, tol):
+    """The reference's set/get consistency fixtures that step the world
+    (tests/joints/ball.cpp:41-151, hinge.cpp:786-895, hinge2.cpp:46-160): two
+    identical body pairs at (-1,-2,-3) and (11,22,33), rotated 27 degrees
+    about fixed axes, joined by a joint; the second joint's anchor (and axes)
+    are read back and set again; after four dWorldStep(0.5) both pairs agree
+    within the reference's tolerance."""
+    from odegpu._lib import lib
+    L = lib()
+    f, v, i = C.c_float, C.c_void_p, C.c_int
+    V4 = f * 4
+    L.dWorldCreate.restype = v
+    L.dWorldSetGravity.argtypes = [v, f, f, f]
+    L.dBodyCreate.restype = v; L.dBodyCreate.argtypes = [v]
+    L.dBodySetPosition.argtypes = [v, f, f, f]
+    L.dBodySetRotation.argtypes = [v, C.POINTER(f)]
+    L.dRFromAxisAndAngle.argtypes = [C.POINTER(f), f, f, f, f]
+    L.dNormalize3.argtypes = [C.POINTER(f)]
+    create = getattr(L, f"dJointCreate{kind}")
+    create.restype = v; create.argtypes = [v, v]
+    L.dJointAttach.argtypes = [v, v, v]
+    L.dWorldStep.restype = i; L.dWorldStep.argtypes = [v, f]
+    L.dBodyGetQuaternion.restype = C.POINTER(f); L.dBodyGetQuaternion.argtypes = [v]
+    L.dBodyGetPosition.restype = C.POINTER(f); L.dBodyGetPosition.argtypes = [v]
+    L.dWorldDestroy.argtypes = [v]
+    w = L.dWorldCreate()
+    L.dWorldSetGravity(w, 0, 0, 0)
+    bodies, joints = [], []
+    for _ in range(2):
+        pair = []
+        for pos, ax in (((-1, -2, -3), (0.53, -0.71, 0.43)), ((11, 22, 33), (1.2, 0.87, -0.33))):
+            b = L.dBodyCreate(w)
+            L.dBodySetPosition(b, *pos)
+            a = V4(*ax, 0.0)
+            L.dNormalize3(a)
+            R = (f * 12)()
+            L.dRFromAxisAndAngle(R, a[0], a[1], a[2], 0.47123)
+            L.dBodySetRotation(b, R)
+            pair.append(b)
+        j = create(w, None)
+        L.dJointAttach(j, pair[0], pair[1])
+        bodies.append(pair)
+        joints.append(j)
+
+    def roundtrip(get, set_):
+        g = getattr(L, get); g.argtypes = [v, C.POINTER(f)]
+        s = getattr(L, set_); s.argtypes = [v, f, f, f]
+        out = V4()
+        g(joints[1], out)
+        s(joints[1], out[0], out[1], out[2])
+
+    if kind == "Hinge":
+        roundtrip("dJointGetHingeAxis", "dJointSetHingeAxis")
+    roundtrip(f"dJointGet{kind}Anchor", f"dJointSet{kind}Anchor")
+    if kind == "Hinge2":
+        roundtrip("dJointGetHinge2Axis1", "dJointSetHinge2Axis1")
+        roundtrip("dJointGetHinge2Axis2", "dJointSetHinge2Axis2")
+    for _ in range(4):
+        assert L.dWorldStep(w, 0.5) == 1
+    for b in range(2):
+        qa, qb = L.dBodyGetQuaternion(bodies[0][b]), L.dBodyGetQuaternion(bodies[1][b])
+        pa, pb = L.dBodyGetPosition(bodies[0][b]), L.dBodyGetPosition(bodies[1][b])
+        assert max(abs(qa[k] - qb[k]) for k in range(4)) < tol, (kind, b)
+        assert max(abs(pa[k] - pb[k]) for k in range(3)) < tol, (kind, b)
+    L.dWorldDestroy(w)
