@@ -146,6 +146,28 @@ void dBodyAddForce(dBodyID b, dReal fx, dReal fy, dReal fz);        /* :1010 */
 void dBodyAddTorque(dBodyID b, dReal fx, dReal fy, dReal fz);       /* :1016 */
 const dReal* dBodyGetForce(dBodyID b);                              /* :1064 */
 const dReal* dBodyGetTorque(dBodyID b);                             /* :1075 */
+void dBodySetForce(dBodyID b, dReal x, dReal y, dReal z);           /* :1085 */
+void dBodySetTorque(dBodyID b, dReal x, dReal y, dReal z);          /* :1095 */
+void dBodyAddRelForce(dBodyID b, dReal fx, dReal fy, dReal fz);     /* :1022 */
+void dBodyAddRelTorque(dBodyID b, dReal fx, dReal fy, dReal fz);    /* :1028 */
+void dBodyAddForceAtPos(dBodyID b, dReal fx, dReal fy, dReal fz,
+                        dReal px, dReal py, dReal pz);              /* :1034 */
+void dBodyAddForceAtRelPos(dBodyID b, dReal fx, dReal fy, dReal fz,
+                           dReal px, dReal py, dReal pz);           /* :1040 */
+void dBodyAddRelForceAtPos(dBodyID b, dReal fx, dReal fy, dReal fz,
+                           dReal px, dReal py, dReal pz);           /* :1046 */
+void dBodyAddRelForceAtRelPos(dBodyID b, dReal fx, dReal fy, dReal fz,
+                              dReal px, dReal py, dReal pz);        /* :1052 */
+void dBodyGetRelPointPos(dBodyID b, dReal px, dReal py, dReal pz, dVector3 result);  /* :1102 */
+void dBodyGetRelPointVel(dBodyID b, dReal px, dReal py, dReal pz, dVector3 result);  /* :1113 */
+void dBodyGetPointVel(dBodyID b, dReal px, dReal py, dReal pz, dVector3 result);     /* :1125 */
+void dBodyGetPosRelPoint(dBodyID b, dReal px, dReal py, dReal pz, dVector3 result);  /* :1139 */
+void dBodyVectorToWorld(dBodyID b, dReal px, dReal py, dReal pz, dVector3 result);   /* :1150 */
+void dBodyVectorFromWorld(dBodyID b, dReal px, dReal py, dReal pz, dVector3 result); /* :1161 */
+void dBodySetData(dBodyID b, void* data);                           /* :873 */
+void* dBodyGetData(dBodyID b);                                      /* :880 */
+int dBodyGetNumJoints(dBodyID b);                                   /* :1223 */
+dJointID dBodyGetJoint(dBodyID b, int index);                       /* :1231 */
 void dBodySetGravityMode(dBodyID b, int mode);                      /* :1294 */
 int dBodyGetGravityMode(dBodyID b);                                 /* :1301 */
 void dBodySetGyroscopicMode(dBodyID b, int enabled);                /* :1458 */
@@ -160,6 +182,8 @@ dJointID dJointCreateSlider(dWorldID w, dJointGroupID g);                /* :155
 dJointID dJointCreateUniversal(dWorldID w, dJointGroupID g);             /* :1578 */
 dJointID dJointCreateFixed(dWorldID w, dJointGroupID g);                 /* :1611 */
 void dJointDestroy(dJointID j);                                          /* :1647 */
+void dJointSetData(dJointID j, void* data);                              /* :1722 */
+void* dJointGetData(dJointID j);                                         /* :1728 */
 dJointGroupID dJointGroupCreate(int max_size);                           /* :1655 */
 void dJointGroupDestroy(dJointGroupID g);                                /* :1663 */
 void dJointGroupEmpty(dJointGroupID g);                                  /* :1672 */
@@ -226,6 +250,7 @@ dReal dJointGetAMotorAngle(dJointID j, int anum);                        /* :287
 dReal dJointGetAMotorParam(dJointID j, int parameter);                   /* :2895 */
 int dJointGetAMotorMode(dJointID j);                                     /* :2910 */
 int dAreConnectedExcluding(dBodyID b1, dBodyID b2, int joint_type);      /* :2968 */
+int dAreConnected(dBodyID b1, dBodyID b2);                               /* :2953 */
 
 /* mass: include/ode/mass.h */
 void dMassSetZero(dMass* m);                                             /* :45 */
@@ -241,6 +266,9 @@ void dMassSetCapsuleTotal(dMass* m, dReal total_mass, int direction, dReal radiu
 void dMassSetCylinder(dMass* m, dReal density, int direction, dReal radius, dReal length);      /* :60 */
 void dMassSetCylinderTotal(dMass* m, dReal total_mass, int direction, dReal radius, dReal length); /* :62 */
 void dMassAdjust(dMass* m, dReal newmass);                               /* :74 */
+void dMassTranslate(dMass* m, dReal x, dReal y, dReal z);                /* :76 */
+void dMassRotate(dMass* m, const dMatrix3 R);                            /* :78 */
+void dMassAdd(dMass* a, const dMass* b);                                 /* :80 */
 
 /* RNG: include/ode/misc.h */
 int dTestRand(void);                                                     /* :37 */
@@ -315,6 +343,8 @@ void dGeomHeightfieldDataBuildDouble(dHeightfieldDataID d, const double* pHeight
                                      dReal width, dReal depth, int widthSamples, int depthSamples,
                                      dReal scale, dReal offset, dReal thickness, int bWrap);  /* :1411 */
 void dGeomDestroy(dGeomID g);                                            /* :68  */
+void dGeomSetData(dGeomID g, void* data);                                /* :78  */
+void* dGeomGetData(dGeomID g);                                           /* :87  */
 void dGeomSetBody(dGeomID g, dBodyID body);                              /* :108 */
 dBodyID dGeomGetBody(dGeomID g);                                         /* :117 */
 void dGeomSetPosition(dGeomID g, dReal x, dReal y, dReal z);             /* :134 */

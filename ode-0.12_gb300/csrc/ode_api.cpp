@@ -32,6 +32,7 @@ struct dxBody {
   double invI[9];
   double invMass;
   int flags;   // ODEGPU_BODY_*
+  void* data;  // dBodySetData
 };
 
 struct dxJoint {
@@ -42,6 +43,7 @@ struct dxJoint {
   int reverse;
   long long seq;             // attachment sequence number (ODE list order)
   dJointFeedback* feedback;
+  void* data;                // dJointSetData
   // ball / hinge / hinge2 data, FP64 as the setters compute it
   og_host::HJoint h;
   double erp, cfm;
@@ -72,6 +74,7 @@ struct dxGeom {
   dxHeightfieldData* hf;     // heightfield geoms: their data
   int placeable;             // heightfield geoms: created placeable
   int ray_flags;             // ray geoms: kRay* below
+  void* data;                // dGeomSetData
 };
 
 // dxGeom::gflags bits of a ray (ode/src/collision_kernel.h: RAY_FIRSTCONTACT,
@@ -156,6 +159,7 @@ dxJoint* new_joint(dxWorld* w, dxJointGroup* g, int type) {
   j->reverse = 0;
   j->seq = -1;
   j->feedback = nullptr;
+  j->data = nullptr;
   j->h.axis1[0] = 1;
   if (type == dJointTypeHinge2) { j->h.axis2[1] = 1; j->h.v1[0] = 1; j->h.v2[1] = 1; }
   else if (type == dJointTypeUniversal) j->h.axis2[1] = 1;
@@ -1474,6 +1478,171 @@ void dDQfromW(dReal dq[4], const dVector3 w, const dQuaternion q) {   // rotatio
   dq[1] = 0.5f * (w[0] * q[0] + w[1] * q[3] - w[2] * q[2]);
   dq[2] = 0.5f * (-w[0] * q[3] + w[1] * q[0] + w[2] * q[1]);
   dq[3] = 0.5f * (w[0] * q[2] - w[1] * q[1] + w[2] * q[0]);
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------- user data, body helpers, mass algebra
+extern "C" {
+
+void dBodySetData(dBodyID b, void* data) { b->data = data; }               // ode.cpp:305-316
+void* dBodyGetData(dBodyID b) { return b->data; }
+void dGeomSetData(dGeomID g, void* data) { g->data = data; }               // collision_kernel.cpp:386-399
+void* dGeomGetData(dGeomID g) { return g->data; }
+void dJointSetData(dJointID j, void* data) { j->data = data; }             // ode.cpp:1262-1273
+void* dJointGetData(dJointID j) { return j->data; }
+
+// dAreConnected (ode.cpp:1518-1526): a joint of any type attaches the two;
+// b2 = 0 asks for a joint to the static environment
+int dAreConnected(dBodyID b1, dBodyID b2) {
+  if (!b1) return 0;
+  for (const dxJoint* j : b1->world->joints)
+    if ((j->body[0] == b1 && j->body[1] == b2) || (j->body[1] == b1 && j->body[0] == b2)) return 1;
+  return 0;
+}
+// dBodyGetNumJoints / dBodyGetJoint (ode.cpp:735-758): the body's joints in its
+// list order, newest attachment first
+static std::vector<dxJoint*> body_joints(dBodyID b) {
+  std::vector<dxJoint*> js;
+  for (dxJoint* j : b->world->joints)
+    if (j->body[0] == b || j->body[1] == b) js.push_back(j);
+  std::stable_sort(js.begin(), js.end(), [](const dxJoint* x, const dxJoint* y) { return x->seq > y->seq; });
+  return js;
+}
+int dBodyGetNumJoints(dBodyID b) { return b ? (int)body_joints(b).size() : 0; }
+dJointID dBodyGetJoint(dBodyID b, int index) {
+  if (!b || index < 0) return nullptr;
+  const auto js = body_joints(b);
+  return index < (int)js.size() ? js[index] : nullptr;
+}
+
+// body-frame vectors and points in world coordinates (ode.cpp:645-733)
+static void body_rot(const dxBody* b, const float* v, float* out) {
+  for (int i = 0; i < 3; ++i) out[i] = b->R[i * 4 + 0] * v[0] + b->R[i * 4 + 1] * v[1] + b->R[i * 4 + 2] * v[2];
+}
+void dBodyVectorToWorld(dBodyID b, dReal px, dReal py, dReal pz, dVector3 result) {
+  const float p[3] = {px, py, pz};
+  body_rot(b, p, result);
+}
+void dBodyGetRelPointPos(dBodyID b, dReal px, dReal py, dReal pz, dVector3 result) {
+  const float p[3] = {px, py, pz};
+  body_rot(b, p, result);
+  for (int i = 0; i < 3; ++i) result[i] += b->pos[i];
+}
+void dBodyVectorFromWorld(dBodyID b, dReal px, dReal py, dReal pz, dVector3 result) {   // ode.cpp:757-770
+  for (int i = 0; i < 3; ++i) result[i] = b->R[0 * 4 + i] * px + b->R[1 * 4 + i] * py + b->R[2 * 4 + i] * pz;
+}
+void dBodyGetPosRelPoint(dBodyID b, dReal px, dReal py, dReal pz, dVector3 result) {    // ode.cpp:728-741
+  dBodyVectorFromWorld(b, px - b->pos[0], py - b->pos[1], pz - b->pos[2], result);
+}
+// velocity of a body point: v + w x (p - pos) (ode.cpp:696-726)
+void dBodyGetRelPointVel(dBodyID b, dReal px, dReal py, dReal pz, dVector3 result) {
+  float q[3];
+  const float p[3] = {px, py, pz};
+  body_rot(b, p, q);
+  const float* w = b->avel;
+  result[0] = b->lvel[0] + w[1] * q[2] - w[2] * q[1];
+  result[1] = b->lvel[1] + w[2] * q[0] - w[0] * q[2];
+  result[2] = b->lvel[2] + w[0] * q[1] - w[1] * q[0];
+}
+void dBodyGetPointVel(dBodyID b, dReal px, dReal py, dReal pz, dVector3 result) {
+  const float q[3] = {px - b->pos[0], py - b->pos[1], pz - b->pos[2]};
+  const float* w = b->avel;
+  result[0] = b->lvel[0] + w[1] * q[2] - w[2] * q[1];
+  result[1] = b->lvel[1] + w[2] * q[0] - w[0] * q[2];
+  result[2] = b->lvel[2] + w[0] * q[1] - w[1] * q[0];
+}
+void dBodySetForce(dBodyID b, dReal x, dReal y, dReal z) { b->facc[0] = x; b->facc[1] = y; b->facc[2] = z; }   // ode.cpp:656-663
+void dBodySetTorque(dBodyID b, dReal x, dReal y, dReal z) { b->tacc[0] = x; b->tacc[1] = y; b->tacc[2] = z; }
+
+// force helpers (ode.cpp:537-641): forces and torques in world coordinates
+// into the accumulators
+void dBodyAddRelForce(dBodyID b, dReal fx, dReal fy, dReal fz) {
+  const float f[3] = {fx, fy, fz};
+  float w[3];
+  body_rot(b, f, w);
+  for (int i = 0; i < 3; ++i) b->facc[i] += w[i];
+}
+void dBodyAddRelTorque(dBodyID b, dReal fx, dReal fy, dReal fz) {
+  const float f[3] = {fx, fy, fz};
+  float w[3];
+  body_rot(b, f, w);
+  for (int i = 0; i < 3; ++i) b->tacc[i] += w[i];
+}
+static void add_force_at(dxBody* b, const float* f, const float* p) {
+  const float q[3] = {p[0] - b->pos[0], p[1] - b->pos[1], p[2] - b->pos[2]};
+  for (int i = 0; i < 3; ++i) b->facc[i] += f[i];
+  b->tacc[0] += q[1] * f[2] - q[2] * f[1];
+  b->tacc[1] += q[2] * f[0] - q[0] * f[2];
+  b->tacc[2] += q[0] * f[1] - q[1] * f[0];
+}
+void dBodyAddForceAtPos(dBodyID b, dReal fx, dReal fy, dReal fz, dReal px, dReal py, dReal pz) {
+  const float f[3] = {fx, fy, fz}, p[3] = {px, py, pz};
+  add_force_at(b, f, p);
+}
+void dBodyAddForceAtRelPos(dBodyID b, dReal fx, dReal fy, dReal fz, dReal px, dReal py, dReal pz) {
+  const float f[3] = {fx, fy, fz};
+  float p[3];
+  dBodyGetRelPointPos(b, px, py, pz, p);
+  add_force_at(b, f, p);
+}
+void dBodyAddRelForceAtPos(dBodyID b, dReal fx, dReal fy, dReal fz, dReal px, dReal py, dReal pz) {
+  const float fl[3] = {fx, fy, fz}, p[3] = {px, py, pz};
+  float f[3];
+  body_rot(b, fl, f);
+  add_force_at(b, f, p);
+}
+void dBodyAddRelForceAtRelPos(dBodyID b, dReal fx, dReal fy, dReal fz, dReal px, dReal py, dReal pz) {
+  const float fl[3] = {fx, fy, fz};
+  float f[3], p[3];
+  body_rot(b, fl, f);
+  dBodyGetRelPointPos(b, px, py, pz, p);
+  add_force_at(b, f, p);
+}
+
+// mass algebra (ode/src/mass.cpp:454-537)
+static void mul0_333f(float* A, const float* B, const float* C) {   // A = B C (3x4 rows)
+  for (int i = 0; i < 3; ++i) {
+    for (int j = 0; j < 3; ++j)
+      A[i * 4 + j] = B[i * 4 + 0] * C[0 * 4 + j] + B[i * 4 + 1] * C[1 * 4 + j] + B[i * 4 + 2] * C[2 * 4 + j];
+    A[i * 4 + 3] = 0;
+  }
+}
+static void cross_mat(float* A, const float* a) {   // A v = a x v
+  for (int k = 0; k < 12; ++k) A[k] = 0;
+  A[1] = -a[2]; A[2] = a[1];
+  A[4] = a[2]; A[6] = -a[0];
+  A[8] = -a[1]; A[9] = a[0];
+}
+void dMassTranslate(dMass* m, dReal x, dReal y, dReal z) {
+  // I + mass (crossmat(c)^2 - crossmat(c + a)^2), then c += a
+  float chat[12], ahat[12], t1[12], t2[12];
+  cross_mat(chat, m->c);
+  const float a[3] = {x + m->c[0], y + m->c[1], z + m->c[2]};
+  cross_mat(ahat, a);
+  mul0_333f(t1, ahat, ahat);
+  mul0_333f(t2, chat, chat);
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) m->I[i * 4 + j] += m->mass * (t2[i * 4 + j] - t1[i * 4 + j]);
+  m->I[4] = m->I[1]; m->I[8] = m->I[2]; m->I[9] = m->I[6];
+  m->c[0] += x; m->c[1] += y; m->c[2] += z;
+}
+void dMassRotate(dMass* m, const dMatrix3 R) {
+  // R I R', c = R c
+  float t1[12], RT[12];
+  for (int i = 0; i < 3; ++i) { for (int j = 0; j < 3; ++j) RT[i * 4 + j] = R[j * 4 + i]; RT[i * 4 + 3] = 0; }
+  mul0_333f(t1, m->I, RT);
+  mul0_333f(m->I, R, t1);
+  m->I[4] = m->I[1]; m->I[8] = m->I[2]; m->I[9] = m->I[6];
+  float t2[3];
+  for (int i = 0; i < 3; ++i) t2[i] = R[i * 4 + 0] * m->c[0] + R[i * 4 + 1] * m->c[1] + R[i * 4 + 2] * m->c[2];
+  m->c[0] = t2[0]; m->c[1] = t2[1]; m->c[2] = t2[2];
+}
+void dMassAdd(dMass* a, const dMass* b) {
+  const float denom = 1.0f / (a->mass + b->mass);
+  for (int i = 0; i < 3; ++i) a->c[i] = (a->c[i] * a->mass + b->c[i] * b->mass) * denom;
+  a->mass += b->mass;
+  for (int i = 0; i < 12; ++i) a->I[i] += b->I[i];
 }
 
 }  // extern "C"

@@ -143,3 +143,116 @@ def test_rotation_utilities_match_reference_fp32():
                                  list(dq) + list(n3)[:3] + list(n4) + [r3, r4] + list(p)[:3] + list(q)[:3],
                                  dtype=np.float32))
         assert np.array_equal(outs[0], outs[1]), np.abs(outs[0] - outs[1]).max()
+
+
+def test_mass_algebra_and_body_helpers_match_reference_fp32():
+    """dMassTranslate / dMassRotate / dMassAdd (ode/src/mass.cpp:454-541) and
+    the body helpers dBodyAddRel*/At*Pos, dBodyGetRelPointPos / PosRelPoint /
+    RelPointVel / PointVel, dBodyVectorTo/FromWorld, dBodyGetNumJoints /
+    GetJoint and dAreConnected (ode/src/ode.cpp:537-830, 1518-1526) of the
+    library (host code, no GPU) against the reference's dSINGLE build on
+    seeded inputs."""
+    import ctypes as C
+    import numpy as np
+    import oracle_lib as O
+    if not O.ref_available("s"):
+        pytest.skip("reference not built in this checkout")
+    ours = C.CDLL(os.path.join(ROOT, "ode-0.12_gb300", "libodegpu.so"))
+    ref = C.CDLL(os.path.join(ROOT, "oracle", "_ref", "libode_ref_s.so"))
+    F, P = C.c_float, C.c_void_p
+    V4 = F * 4
+    M12 = F * 12
+
+    class Mass(C.Structure):
+        _fields_ = [("mass", F), ("c", F * 4), ("I", F * 12)]
+
+    for lib in (ours, ref):
+        lib.dRFromAxisAndAngle.argtypes = [P, F, F, F, F]
+        lib.dMassSetBox.argtypes = [P, F, F, F, F]
+        lib.dMassSetSphereTotal.argtypes = [P, F, F]
+        lib.dMassTranslate.argtypes = [P, F, F, F]
+        lib.dMassRotate.argtypes = [P, P]
+        lib.dMassAdd.argtypes = [P, P]
+        lib.dWorldCreate.restype = P
+        lib.dBodyCreate.restype = P
+        lib.dBodyCreate.argtypes = [P]
+        lib.dBodySetPosition.argtypes = [P, F, F, F]
+        lib.dBodySetRotation.argtypes = [P, P]
+        lib.dBodySetLinearVel.argtypes = [P, F, F, F]
+        lib.dBodySetAngularVel.argtypes = [P, F, F, F]
+        for name in ("dBodyAddRelForce", "dBodyAddRelTorque", "dBodySetForce", "dBodySetTorque"):
+            getattr(lib, name).argtypes = [P, F, F, F]
+        for name in ("dBodyAddForceAtPos", "dBodyAddForceAtRelPos", "dBodyAddRelForceAtPos",
+                     "dBodyAddRelForceAtRelPos"):
+            getattr(lib, name).argtypes = [P] + [F] * 6
+        for name in ("dBodyGetRelPointPos", "dBodyGetPosRelPoint", "dBodyGetRelPointVel", "dBodyGetPointVel",
+                     "dBodyVectorToWorld", "dBodyVectorFromWorld"):
+            getattr(lib, name).argtypes = [P, F, F, F, P]
+        lib.dBodyGetForce.restype = C.POINTER(F)
+        lib.dBodyGetTorque.restype = C.POINTER(F)
+        lib.dBodyGetForce.argtypes = lib.dBodyGetTorque.argtypes = [P]
+        lib.dJointCreateBall.restype = lib.dJointCreateHinge.restype = P
+        lib.dJointCreateBall.argtypes = lib.dJointCreateHinge.argtypes = [P, P]
+        lib.dJointAttach.argtypes = [P, P, P]
+        lib.dBodyGetJoint.restype = P
+        lib.dBodyGetJoint.argtypes = [P, C.c_int]
+        lib.dBodyGetNumJoints.argtypes = [P]
+        lib.dAreConnected.argtypes = [P, P]
+        lib.dWorldDestroy.argtypes = [P]
+    rng = np.random.default_rng(9)
+    for _ in range(100):
+        a = [float(x) for x in rng.normal(size=24)]
+        outs = []
+        for lib in (ours, ref):
+            R = M12()
+            lib.dRFromAxisAndAngle(R, *a[:4])
+            m1, m2 = Mass(), Mass()
+            lib.dMassSetBox(C.byref(m1), 500.0, abs(a[4]) + 0.1, abs(a[5]) + 0.1, abs(a[6]) + 0.1)
+            lib.dMassTranslate(C.byref(m1), *a[7:10])
+            lib.dMassRotate(C.byref(m1), R)
+            lib.dMassSetSphereTotal(C.byref(m2), abs(a[10]) + 0.5, abs(a[11]) + 0.05)
+            lib.dMassTranslate(C.byref(m2), *a[12:15])
+            lib.dMassAdd(C.byref(m1), C.byref(m2))
+            out = [m1.mass] + list(m1.c)[:3] + list(m1.I)
+            w = lib.dWorldCreate()
+            b = lib.dBodyCreate(w)
+            lib.dBodySetPosition(b, *a[15:18])
+            lib.dBodySetRotation(b, R)
+            lib.dBodySetLinearVel(b, *a[18:21])
+            lib.dBodySetAngularVel(b, *a[21:24])
+            lib.dBodySetForce(b, 1.0, -2.0, 0.5)
+            lib.dBodySetTorque(b, 0.0, 0.25, -1.0)
+            lib.dBodyAddRelForce(b, *a[:3])
+            lib.dBodyAddRelTorque(b, *a[3:6])
+            lib.dBodyAddForceAtPos(b, *a[6:12])
+            lib.dBodyAddForceAtRelPos(b, *a[9:15])
+            lib.dBodyAddRelForceAtPos(b, *a[12:18])
+            lib.dBodyAddRelForceAtRelPos(b, *a[15:21])
+            fp, tp = lib.dBodyGetForce(b), lib.dBodyGetTorque(b)
+            out += [fp[k] for k in range(3)] + [tp[k] for k in range(3)]
+            for name in ("dBodyGetRelPointPos", "dBodyGetPosRelPoint", "dBodyGetRelPointVel", "dBodyGetPointVel",
+                         "dBodyVectorToWorld", "dBodyVectorFromWorld"):
+                r = V4()
+                getattr(lib, name)(b, *a[18:21], r)
+                out += list(r)[:3]
+            b2, b3 = lib.dBodyCreate(w), lib.dBodyCreate(w)
+            j1, j2, j3 = lib.dJointCreateBall(w, None), lib.dJointCreateHinge(w, None), lib.dJointCreateBall(w, None)
+            lib.dJointAttach(j1, b, b2)
+            lib.dJointAttach(j2, b2, b)
+            lib.dJointAttach(j3, b3, None)
+            js = [j1, j2, j3]
+            order = [js.index(lib.dBodyGetJoint(b, k)) for k in range(lib.dBodyGetNumJoints(b))]
+            out += [float(x) for x in order] + [float(lib.dBodyGetNumJoints(b3)),
+                                                float(lib.dAreConnected(b, b2)), float(lib.dAreConnected(b2, b3)),
+                                                float(lib.dAreConnected(b3, None)), float(lib.dAreConnected(b, None))]
+            lib.dWorldDestroy(w)
+            outs.append(np.array(out, dtype=np.float32))
+        # the mass algebra and the integer answers bit-identical; the body
+        # helpers within FP32 rounding, since dBodySetRotation keeps its
+        # orientation through a quaternion formed in FP64 here and in FP32
+        # in the reference (a few ulps of R)
+        assert np.array_equal(outs[0][:16], outs[1][:16]), np.abs(outs[0][:16] - outs[1][:16]).max()
+        assert np.array_equal(outs[0][40:], outs[1][40:]), (outs[0][40:], outs[1][40:])
+        scale = 1.0 + np.abs(outs[1][16:40])
+        assert (np.abs(outs[0][16:40] - outs[1][16:40]) <= 4e-6 * scale).all(), \
+            np.abs(outs[0][16:40] - outs[1][16:40]).max()
