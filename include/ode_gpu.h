@@ -116,6 +116,8 @@ dReal dWorldGetERP(dWorldID w);                                     /* :101 */
 void dWorldSetCFM(dWorldID w, dReal cfm);                           /* :111 */
 dReal dWorldGetCFM(dWorldID w);                                     /* :118 */
 int dWorldQuickStep(dWorldID w, dReal stepsize);                    /* :352 */
+void dWorldImpulseToForce(dWorldID w, dReal stepsize, dReal ix, dReal iy, dReal iz,
+                          dVector3 force);                            /* :369 */
 /* The exact stepper (dense LCP per island, Dantzig pivoting) on the GPU. */
 int dWorldStep(dWorldID w, dReal stepsize);                         /* :309 */
 void dWorldSetQuickStepNumIterations(dWorldID w, int num);          /* :385 */
@@ -167,6 +169,10 @@ void dBodyVectorFromWorld(dBodyID b, dReal px, dReal py, dReal pz, dVector3 resu
 void dBodySetData(dBodyID b, void* data);                           /* :873 */
 void* dBodyGetData(dBodyID b);                                      /* :880 */
 int dBodyGetNumJoints(dBodyID b);                                   /* :1223 */
+void dBodyCopyPosition(dBodyID b, dVector3 pos);                    /* :943 */
+void dBodyCopyRotation(dBodyID b, dMatrix3 R);                      /* :961 */
+void dBodyCopyQuaternion(dBodyID b, dQuaternion quat);              /* :979 */
+dWorldID dBodyGetWorld(dBodyID b);                                  /* :848 */
 dJointID dBodyGetJoint(dBodyID b, int index);                       /* :1231 */
 void dBodySetGravityMode(dBodyID b, int mode);                      /* :1294 */
 int dBodyGetGravityMode(dBodyID b);                                 /* :1301 */
@@ -190,17 +196,23 @@ void dJointGroupEmpty(dJointGroupID g);                                  /* :167
 void dJointAttach(dJointID j, dBodyID body1, dBodyID body2);             /* :1693 */
 dJointType dJointGetType(dJointID j);                                    /* :1749 */
 dBodyID dJointGetBody(dJointID j, int index);                            /* :1761 */
+int dJointGetNumBodies(dJointID j);                                      /* :1678 */
+dJointID dConnectingJoint(dBodyID b1, dBodyID b2);                       /* :2940 */
+int dConnectingJointList(dBodyID b1, dBodyID b2, dJointID* out);         /* :2945 */
 void dJointSetFeedback(dJointID j, dJointFeedback* f);                   /* :1770 */
 dJointFeedback* dJointGetFeedback(dJointID j);                           /* :1776 */
 void dJointSetBallAnchor(dJointID j, dReal x, dReal y, dReal z);         /* :1785 */
 void dJointSetBallParam(dJointID j, int parameter, dReal value);         /* :1797 */
 void dJointGetBallAnchor(dJointID j, dVector3 result);                   /* :2351 */
+void dJointGetBallAnchor2(dJointID j, dVector3 result);                  /* :2363 */
+dReal dJointGetBallParam(dJointID j, int parameter);                     /* :2369 */
 void dJointSetHingeAnchor(dJointID j, dReal x, dReal y, dReal z);        /* :1803 */
 void dJointSetHingeAxis(dJointID j, dReal x, dReal y, dReal z);          /* :1811 */
 void dJointGetHingeAnchor(dJointID j, dVector3 result);                  /* :2378 */
 void dJointGetHingeAnchor2(dJointID j, dVector3 result);                 /* :2388 */
 void dJointGetHingeAxis(dJointID j, dVector3 result);                    /* :2394 */
 void dJointSetHingeParam(dJointID j, int parameter, dReal value);        /* :1847 */
+dReal dJointGetHingeParam(dJointID j, int parameter);                    /* :2400 */
 dReal dJointGetHingeAngle(dJointID j);                                   /* :2414 */
 dReal dJointGetHingeAngleRate(dJointID j);                               /* :2420 */
 void dJointAddHingeTorque(dJointID j, dReal torque);                     /* :1857 */
@@ -212,6 +224,7 @@ void dJointGetHinge2Anchor2(dJointID j, dVector3 result);                /* :246
 void dJointGetHinge2Axis1(dJointID j, dVector3 result);                  /* :2475 */
 void dJointGetHinge2Axis2(dJointID j, dVector3 result);                  /* :2481 */
 void dJointSetHinge2Param(dJointID j, int parameter, dReal value);       /* :1908 */
+dReal dJointGetHinge2Param(dJointID j, int parameter);                   /* :2487 */
 void dJointAddHinge2Torques(dJointID j, dReal torque1, dReal torque2);   /* :1916 */
 dReal dJointGetHinge2Angle1(dJointID j);                                 /* :2493 */
 void dJointSetSliderAxis(dJointID j, dReal x, dReal y, dReal z);         /* :1863 */
@@ -227,6 +240,7 @@ void dJointSetUniversalAxis2(dJointID j, dReal x, dReal y, dReal z);     /* :197
 void dJointSetUniversalParam(dJointID j, int parameter, dReal value);    /* :2020 */
 void dJointAddUniversalTorques(dJointID j, dReal torque1, dReal torque2);/* :2028 */
 void dJointGetUniversalAnchor(dJointID j, dVector3 result);              /* :2513 */
+void dJointGetUniversalAnchor2(dJointID j, dVector3 result);             /* :2528 */
 void dJointGetUniversalAxis1(dJointID j, dVector3 result);               /* :2534 */
 void dJointGetUniversalAxis2(dJointID j, dVector3 result);               /* :2540 */
 dReal dJointGetUniversalParam(dJointID j, int parameter);                /* :2547 */
@@ -269,6 +283,9 @@ void dMassAdjust(dMass* m, dReal newmass);                               /* :74 
 void dMassTranslate(dMass* m, dReal x, dReal y, dReal z);                /* :76 */
 void dMassRotate(dMass* m, const dMatrix3 R);                            /* :78 */
 void dMassAdd(dMass* a, const dMass* b);                                 /* :80 */
+void dMassSetCappedCylinder(dMass* m, dReal density, int direction, dReal radius, dReal length);  /* :84 */
+void dMassSetCappedCylinderTotal(dMass* m, dReal total_mass, int direction, dReal radius,
+                                 dReal length);                                               /* :85 */
 
 /* RNG: include/ode/misc.h */
 int dTestRand(void);                                                     /* :37 */
@@ -276,6 +293,7 @@ unsigned long dRand(void);                                               /* :42 
 unsigned long dRandGetSeed(void);                                        /* :45 */
 void dRandSetSeed(unsigned long s);                                      /* :46 */
 int dRandInt(int n);                                                     /* :51 */
+dReal dRandReal(void);                                                   /* :54 */
 
 /* rotation and vector utilities: include/ode/rotation.h, include/ode/odemath.h
  * (FP32, the reference's operation order) */

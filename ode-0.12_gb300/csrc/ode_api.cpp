@@ -1646,3 +1646,59 @@ void dMassAdd(dMass* a, const dMass* b) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------- small accessors
+extern "C" {
+
+void dBodyCopyPosition(dBodyID b, dVector3 pos) { for (int k = 0; k < 3; ++k) pos[k] = b->pos[k]; }   // ode.cpp:410-440
+void dBodyCopyRotation(dBodyID b, dMatrix3 R) { for (int k = 0; k < 12; ++k) R[k] = b->R[k]; }
+void dBodyCopyQuaternion(dBodyID b, dQuaternion q) { for (int k = 0; k < 4; ++k) q[k] = b->q[k]; }
+dWorldID dBodyGetWorld(dBodyID b) { return b->world; }                                         // ode.cpp:333-337
+// ode.cpp:1399-1410: 0 for a detached joint, 1 for a joint to the environment
+int dJointGetNumBodies(dJointID j) { return !j->body[0] ? 0 : (!j->body[1] ? 1 : 2); }
+// dConnectingJoint / dConnectingJointList (ode.cpp:1466-1515): the joints
+// joining b1 to b2 (0 = the environment) in b1's list order, newest first
+dJointID dConnectingJoint(dBodyID in_b1, dBodyID in_b2) {
+  dBodyID b1 = in_b1 ? in_b1 : in_b2, b2 = in_b1 ? in_b2 : in_b1;
+  if (!b1) return nullptr;
+  for (dxJoint* j : body_joints(b1))
+    if ((j->body[0] == b1 && j->body[1] == b2) || (j->body[1] == b1 && j->body[0] == b2)) return j;
+  return nullptr;
+}
+int dConnectingJointList(dBodyID in_b1, dBodyID in_b2, dJointID* out) {
+  dBodyID b1 = in_b1 ? in_b1 : in_b2, b2 = in_b1 ? in_b2 : in_b1;
+  if (!b1) return 0;
+  int n = 0;
+  for (dxJoint* j : body_joints(b1))
+    if ((j->body[0] == b1 && j->body[1] == b2) || (j->body[1] == b1 && j->body[0] == b2)) out[n++] = j;
+  return n;
+}
+// ode.cpp:1783-1791
+void dWorldImpulseToForce(dWorldID, dReal stepsize, dReal ix, dReal iy, dReal iz, dVector3 force) {
+  const float s = 1.0f / stepsize;
+  force[0] = s * ix; force[1] = s * iy; force[2] = s * iz;
+}
+// misc.cpp:57-60
+dReal dRandReal(void) { return (dReal)dRand() / (dReal)0xffffffffUL; }
+// the pre-0.9 names of the capsule mass functions (mass.cpp:544-553)
+void dMassSetCappedCylinder(dMass* m, dReal density, int direction, dReal radius, dReal length) {
+  dMassSetCapsule(m, density, direction, radius, length);
+}
+void dMassSetCappedCylinderTotal(dMass* m, dReal total_mass, int direction, dReal radius, dReal length) {
+  dMassSetCapsuleTotal(m, total_mass, direction, radius, length);
+}
+void dJointGetBallAnchor2(dJointID j, dVector3 r) { joint_anchor(j, true, r); }          // ball.cpp:103-113
+void dJointGetUniversalAnchor2(dJointID j, dVector3 r) { joint_anchor(j, true, r); }     // universal.cpp:572-582
+// ball.cpp:128-143: ERP and CFM only
+dReal dJointGetBallParam(dJointID j, int p) {
+  return p == dParamCFM ? (dReal)j->cfm : (p == dParamERP ? (dReal)j->erp : 0);
+}
+dReal dJointGetHingeParam(dJointID j, int p) { return limot_get(j->lm1, p); }             // hinge.cpp:260-266
+dReal dJointGetHinge2Param(dJointID j, int p) {                                           // hinge2.cpp:278-299
+  if ((p & 0xff00) == 0x100) return limot_get(j->lm2, p & 0xff);
+  if (p == dParamSuspensionERP) return (dReal)j->susp_erp;
+  if (p == dParamSuspensionCFM) return (dReal)j->susp_cfm;
+  return limot_get(j->lm1, p);
+}
+
+}  // extern "C"

@@ -256,3 +256,82 @@ def test_mass_algebra_and_body_helpers_match_reference_fp32():
         scale = 1.0 + np.abs(outs[1][16:40])
         assert (np.abs(outs[0][16:40] - outs[1][16:40]) <= 4e-6 * scale).all(), \
             np.abs(outs[0][16:40] - outs[1][16:40]).max()
+
+
+def test_connecting_joints_and_small_accessors_match_reference_fp32():
+    """dConnectingJoint[List], dJointGetNumBodies, dWorldImpulseToForce,
+    dRandReal, dJointGetBallAnchor2 and dJointGetBall/Hinge/Hinge2Param
+    (ode/src/ode.cpp:1399-1515, 1783-1791; misc.cpp:57-60; joints/ball.cpp,
+    hinge.cpp, hinge2.cpp) against the reference's dSINGLE build."""
+    import ctypes as C
+    import numpy as np
+    import oracle_lib as O
+    if not O.ref_available("s"):
+        pytest.skip("reference not built in this checkout")
+    ours = C.CDLL(os.path.join(ROOT, "ode-0.12_gb300", "libodegpu.so"))
+    ref = C.CDLL(os.path.join(ROOT, "oracle", "_ref", "libode_ref_s.so"))
+    F, P = C.c_float, C.c_void_p
+    outs = []
+    for lib in (ours, ref):
+        lib.dWorldCreate.restype = lib.dBodyCreate.restype = P
+        lib.dBodyCreate.argtypes = [P]
+        lib.dBodySetPosition.argtypes = [P, F, F, F]
+        for n in ("dJointCreateBall", "dJointCreateHinge", "dJointCreateHinge2"):
+            getattr(lib, n).restype = P
+            getattr(lib, n).argtypes = [P, P]
+        lib.dJointAttach.argtypes = [P, P, P]
+        lib.dJointSetBallAnchor.argtypes = [P, F, F, F]
+        lib.dJointGetBallAnchor2.argtypes = [P, P]
+        lib.dConnectingJoint.restype = P
+        lib.dConnectingJoint.argtypes = [P, P]
+        lib.dConnectingJointList.argtypes = [P, P, P]
+        lib.dJointGetNumBodies.argtypes = [P]
+        lib.dWorldImpulseToForce.argtypes = [P, F, F, F, F, P]
+        lib.dRandReal.restype = F
+        lib.dRandSetSeed.argtypes = [C.c_ulong]
+        for n in ("dJointSetBallParam", "dJointSetHingeParam", "dJointSetHinge2Param"):
+            getattr(lib, n).argtypes = [P, C.c_int, F]
+        for n in ("dJointGetBallParam", "dJointGetHingeParam", "dJointGetHinge2Param"):
+            getattr(lib, n).restype = F
+            getattr(lib, n).argtypes = [P, C.c_int]
+        w = lib.dWorldCreate()
+        b1, b2, b3 = lib.dBodyCreate(w), lib.dBodyCreate(w), lib.dBodyCreate(w)
+        lib.dBodySetPosition(b1, 0.1, 0.2, 0.3)
+        lib.dBodySetPosition(b2, 1.1, -0.4, 0.7)
+        lib.dBodySetPosition(b3, 0.0, 2.0, 0.0)
+        jb, jh, jh2, jd = (lib.dJointCreateBall(w, None), lib.dJointCreateHinge(w, None),
+                           lib.dJointCreateHinge2(w, None), lib.dJointCreateBall(w, None))
+        js = [jb, jh, jh2, jd, None]
+        lib.dJointAttach(jb, b2, b1)
+        lib.dJointSetBallAnchor(jb, 0.5, 0.0, 0.5)
+        lib.dBodySetPosition(b2, 1.3, -0.4, 0.9)
+        lib.dJointAttach(jh, b1, b2)
+        lib.dJointAttach(jh2, b3, b2)
+        lib.dJointAttach(jd, b3, None)
+        out = []
+        a2 = (F * 4)()
+        lib.dJointGetBallAnchor2(jb, a2)
+        out += list(a2)[:3]
+        lst = (P * 8)()
+        n = lib.dConnectingJointList(b1, b2, lst)
+        out += [n] + [js.index(lst[k]) for k in range(n)]
+        out += [js.index(lib.dConnectingJoint(b1, b2)), js.index(lib.dConnectingJoint(None, b3)),
+                js.index(lib.dConnectingJoint(b2, b3)), js.index(lib.dConnectingJoint(b1, b3))]
+        out += [lib.dJointGetNumBodies(j) for j in (jb, jh2, jd)]
+        f = (F * 4)()
+        lib.dWorldImpulseToForce(w, 0.01, 1.5, -2.0, 0.3, f)
+        out += list(f)[:3]
+        lib.dRandSetSeed(12345)
+        out += [lib.dRandReal() for _ in range(4)]
+        lib.dJointSetBallParam(jb, 3, 0.5)      # dParamVel: not a ball parameter
+        lib.dJointSetBallParam(jb, 6, 1e-4)     # dParamCFM
+        lib.dJointSetHingeParam(jh, 0, -0.7)    # dParamLoStop
+        lib.dJointSetHingeParam(jh, 2, 1.25)    # dParamVel
+        lib.dJointSetHinge2Param(jh2, 0x102, 3.0)   # dParamVel2
+        lib.dJointSetHinge2Param(jh2, 9, 0.4)       # dParamSuspensionERP
+        out += [lib.dJointGetBallParam(jb, p) for p in (3, 6, 11)]
+        out += [lib.dJointGetHingeParam(jh, p) for p in (0, 1, 2, 3, 4, 5, 6, 7, 8)]
+        out += [lib.dJointGetHinge2Param(jh2, p) for p in (0, 2, 9, 10, 0x100, 0x102, 0x103)]
+        lib.dWorldDestroy(w)
+        outs.append(np.array(out, dtype=np.float32))
+    assert np.array_equal(outs[0], outs[1]), (outs[0], outs[1])
