@@ -196,6 +196,9 @@ void dJointGroupEmpty(dJointGroupID g);                                  /* :167
 void dJointAttach(dJointID j, dBodyID body1, dBodyID body2);             /* :1693 */
 dJointType dJointGetType(dJointID j);                                    /* :1749 */
 dBodyID dJointGetBody(dJointID j, int index);                            /* :1761 */
+void dJointEnable(dJointID j);                                            /* :1700 */
+void dJointDisable(dJointID j);                                           /* :1709 */
+int dJointIsEnabled(dJointID j);                                          /* :1716 */
 int dJointGetNumBodies(dJointID j);                                      /* :1678 */
 dJointID dConnectingJoint(dBodyID b1, dBodyID b2);                       /* :2940 */
 int dConnectingJointList(dBodyID b1, dBodyID b2, dJointID* out);         /* :2945 */

@@ -44,6 +44,7 @@ struct dxJoint {
   long long seq;             // attachment sequence number (ODE list order)
   dJointFeedback* feedback;
   void* data;                // dJointSetData
+  int disabled;              // dJointDisable
   // ball / hinge / hinge2 data, FP64 as the setters compute it
   og_host::HJoint h;
   double erp, cfm;
@@ -160,6 +161,7 @@ dxJoint* new_joint(dxWorld* w, dxJointGroup* g, int type) {
   j->seq = -1;
   j->feedback = nullptr;
   j->data = nullptr;
+  j->disabled = 0;
   j->h.axis1[0] = 1;
   if (type == dJointTypeHinge2) { j->h.axis2[1] = 1; j->h.v1[0] = 1; j->h.v2[1] = 1; }
   else if (type == dJointTypeUniversal) j->h.axis2[1] = 1;
@@ -1211,7 +1213,9 @@ static int world_step(dWorldID w, dReal stepsize, bool exact) {
   // joints: persistent first (creation order), then contacts (creation order)
   std::vector<dxJoint*> pj, cj;
   for (dxJoint* j : w->joints) {
-    if (!j->body[0]) continue;   // unattached joints take no part (util.cpp:435-467)
+    // unattached and disabled joints take no part (util.cpp:435-467, 500-510):
+    // they neither join islands nor add rows
+    if (!j->body[0] || j->disabled) continue;
     (j->type == dJointTypeContact ? cj : pj).push_back(j);
   }
   hw.joints.resize(pj.size());
@@ -1693,6 +1697,10 @@ void dJointGetUniversalAnchor2(dJointID j, dVector3 r) { joint_anchor(j, true, r
 dReal dJointGetBallParam(dJointID j, int p) {
   return p == dParamCFM ? (dReal)j->cfm : (p == dParamERP ? (dReal)j->erp : 0);
 }
+// ode.cpp:1401-1417
+void dJointEnable(dJointID j) { j->disabled = 0; }
+void dJointDisable(dJointID j) { j->disabled = 1; }
+int dJointIsEnabled(dJointID j) { return !j->disabled; }
 dReal dJointGetHingeParam(dJointID j, int p) { return limot_get(j->lm1, p); }             // hinge.cpp:260-266
 dReal dJointGetHinge2Param(dJointID j, int p) {                                           // hinge2.cpp:278-299
   if ((p & 0xff00) == 0x100) return limot_get(j->lm2, p & 0xff);

@@ -438,3 +438,67 @@ def test_reference_joint_fixtures_with_dworldstep(kind, tol):
         assert max(abs(qa[k] - qb[k]) for k in range(4)) < tol, (kind, b)
         assert max(abs(pa[k] - pb[k]) for k in range(3)) < tol, (kind, b)
     L.dWorldDestroy(w)
+
+
+@pytest.mark.parametrize("stepper", ["dWorldQuickStep", "dWorldStep"])
+def test_disabled_joint_takes_no_part(stepper):
+    """dJointDisable / dJointEnable / dJointIsEnabled (ode/src/ode.cpp:1401-1417):
+    a disabled joint neither joins islands nor adds rows (util.cpp:435-510),
+    so a pendulum chain carrying a disabled extra ball joint steps
+    bit-identically to the same chain without it; once re-enabled it acts."""
+    from odegpu._lib import lib
+    L = lib()
+    f, v, i = C.c_float, C.c_void_p, C.c_int
+    L.dWorldCreate.restype = v
+    L.dWorldSetGravity.argtypes = [v, f, f, f]
+    L.dBodyCreate.restype = v; L.dBodyCreate.argtypes = [v]
+    L.dBodySetPosition.argtypes = [v, f, f, f]
+    L.dBodyGetPosition.restype = C.POINTER(f); L.dBodyGetPosition.argtypes = [v]
+    L.dJointCreateHinge.restype = v; L.dJointCreateHinge.argtypes = [v, v]
+    L.dJointCreateBall.restype = v; L.dJointCreateBall.argtypes = [v, v]
+    L.dJointAttach.argtypes = [v, v, v]
+    L.dJointSetHingeAnchor.argtypes = [v, f, f, f]
+    L.dJointSetHingeAxis.argtypes = [v, f, f, f]
+    L.dJointSetBallAnchor.argtypes = [v, f, f, f]
+    L.dJointDisable.argtypes = L.dJointEnable.argtypes = L.dJointIsEnabled.argtypes = [v]
+    step = getattr(L, stepper)
+    step.restype = i; step.argtypes = [v, f]
+    L.dWorldDestroy.argtypes = [v]
+
+    def chain(extra):
+        w = L.dWorldCreate()
+        L.dWorldSetGravity(w, 0, 0, -9.81)
+        bs = [L.dBodyCreate(w) for _ in range(3)]
+        for k, b in enumerate(bs):
+            L.dBodySetPosition(b, 0.5 * (k + 1), 0.1 * k, 2.0)
+        prev = None
+        for k, b in enumerate(bs):
+            j = L.dJointCreateHinge(w, None)
+            L.dJointAttach(j, b, prev)
+            L.dJointSetHingeAnchor(j, 0.5 * k + 0.25, 0.05 * k, 2.0)
+            L.dJointSetHingeAxis(j, 0, 1, 0.2 * k)
+            prev = b
+        jx = None
+        if extra:
+            jx = L.dJointCreateBall(w, None)
+            L.dJointAttach(jx, bs[0], bs[2])
+            L.dJointSetBallAnchor(jx, 1.0, 0.0, 2.0)
+            L.dJointDisable(jx)
+            assert L.dJointIsEnabled(jx) == 0
+        return w, bs, jx
+
+    def pos(bs):
+        return np.array([[L.dBodyGetPosition(b)[k] for k in range(3)] for b in bs])
+
+    wa, ba, jx = chain(True)
+    wb, bb, _ = chain(False)
+    for _ in range(20):
+        assert step(wa, 0.01) == 1 and step(wb, 0.01) == 1
+    assert np.array_equal(pos(ba), pos(bb))
+    L.dJointEnable(jx)
+    assert L.dJointIsEnabled(jx) == 1
+    for _ in range(5):
+        step(wa, 0.01), step(wb, 0.01)
+    assert not np.array_equal(pos(ba), pos(bb))
+    L.dWorldDestroy(wa)
+    L.dWorldDestroy(wb)
