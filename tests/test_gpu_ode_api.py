@@ -490,15 +490,25 @@ def test_disabled_joint_takes_no_part(stepper):
     def pos(bs):
         return np.array([[L.dBodyGetPosition(b)[k] for k in range(3)] for b in bs])
 
+    L.dRandSetSeed.argtypes = [C.c_ulong]
+
+    def step_both(k):
+        # QuickStep's row shuffle draws from ODE's one global RNG: both
+        # worlds start each step from the same seed
+        L.dRandSetSeed(1000 + k)
+        assert step(wa, 0.01) == 1
+        L.dRandSetSeed(1000 + k)
+        assert step(wb, 0.01) == 1
+
     wa, ba, jx = chain(True)
     wb, bb, _ = chain(False)
-    for _ in range(20):
-        assert step(wa, 0.01) == 1 and step(wb, 0.01) == 1
+    for k in range(20):
+        step_both(k)
     assert np.array_equal(pos(ba), pos(bb))
     L.dJointEnable(jx)
     assert L.dJointIsEnabled(jx) == 1
-    for _ in range(5):
-        step(wa, 0.01), step(wb, 0.01)
+    for k in range(5):
+        step_both(20 + k)
     assert not np.array_equal(pos(ba), pos(bb))
     L.dWorldDestroy(wa)
     L.dWorldDestroy(wb)
