@@ -283,6 +283,7 @@ void dMassSetCapsuleTotal(dMass* m, dReal total_mass, int direction, dReal radiu
 void dMassSetCylinder(dMass* m, dReal density, int direction, dReal radius, dReal length);      /* :60 */
 void dMassSetCylinderTotal(dMass* m, dReal total_mass, int direction, dReal radius, dReal length); /* :62 */
 void dMassAdjust(dMass* m, dReal newmass);                               /* :74 */
+int dMassCheck(const dMass* m);                                          /* :43 */
 void dMassTranslate(dMass* m, dReal x, dReal y, dReal z);                /* :76 */
 void dMassRotate(dMass* m, const dMatrix3 R);                            /* :78 */
 void dMassAdd(dMass* a, const dMass* b);                                 /* :80 */

@@ -1642,6 +1642,38 @@ void dMassRotate(dMass* m, const dMatrix3 R) {
   for (int i = 0; i < 3; ++i) t2[i] = R[i * 4 + 0] * m->c[0] + R[i * 4 + 1] * m->c[1] + R[i * 4 + 2] * m->c[2];
   m->c[0] = t2[0]; m->c[1] = t2[1]; m->c[2] = t2[2];
 }
+// Cholesky test of a 3x3 (row stride 4) over its lower triangle, as
+// dIsPositiveDefinite does (matrix.cpp:124-160, 226-238): positive definite
+// when every pivot's reduced diagonal stays above 0
+static int positive_definite3(const float* A) {
+  float L[12], recip[3];
+  for (int k = 0; k < 12; ++k) L[k] = A[k];
+  for (int i = 0; i < 3; ++i) {
+    for (int j = 0; j < i; ++j) {
+      float sum = L[i * 4 + j];
+      for (int k = 0; k < j; ++k) sum -= L[i * 4 + k] * L[j * 4 + k];
+      L[i * 4 + j] = sum * recip[j];
+    }
+    float sum = L[i * 4 + i];
+    for (int k = 0; k < i; ++k) sum -= L[i * 4 + k] * L[i * 4 + k];
+    if (sum <= 0.0f) return 0;
+    L[i * 4 + i] = std::sqrt(sum);
+    recip[i] = 1.0f / L[i * 4 + i];
+  }
+  return 1;
+}
+// dMassCheck (mass.cpp:44-83): mass > 0, I positive definite, and the
+// inertia about the centre of mass, I + mass crossmat(c)^2, as well
+int dMassCheck(const dMass* m) {
+  if (!(m->mass > 0)) return 0;
+  if (!positive_definite3(m->I)) return 0;
+  float chat[12], I2[12];
+  cross_mat(chat, m->c);
+  mul0_333f(I2, chat, chat);
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) I2[i * 4 + j] = m->I[i * 4 + j] + m->mass * I2[i * 4 + j];
+  return positive_definite3(I2);
+}
 void dMassAdd(dMass* a, const dMass* b) {
   const float denom = 1.0f / (a->mass + b->mass);
   for (int i = 0; i < 3; ++i) a->c[i] = (a->c[i] * a->mass + b->c[i] * b->mass) * denom;

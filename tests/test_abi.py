@@ -335,3 +335,44 @@ def test_connecting_joints_and_small_accessors_match_reference_fp32():
         lib.dWorldDestroy(w)
         outs.append(np.array(out, dtype=np.float32))
     assert np.array_equal(outs[0], outs[1]), (outs[0], outs[1])
+
+
+def test_mass_check_matches_reference():
+    """dMassCheck (ode/src/mass.cpp:44-83, dIsPositiveDefinite of
+    matrix.cpp:124-160) against the reference's dSINGLE build on valid masses,
+    masses moved far off their centre, and random (mostly indefinite) ones."""
+    import ctypes as C
+    import numpy as np
+    import oracle_lib as O
+    if not O.ref_available("s"):
+        pytest.skip("reference not built in this checkout")
+    ours = C.CDLL(os.path.join(ROOT, "ode-0.12_gb300", "libodegpu.so"))
+    ref = C.CDLL(os.path.join(ROOT, "oracle", "_ref", "libode_ref_s.so"))
+    F = C.c_float
+
+    class Mass(C.Structure):
+        _fields_ = [("mass", F), ("c", F * 4), ("I", F * 12)]
+
+    for lib in (ours, ref):
+        lib.dMassCheck.argtypes = [C.c_void_p]
+    rng = np.random.default_rng(17)
+    got, want = [], []
+    for k in range(600):
+        m = Mass()
+        m.mass = float(rng.uniform(-0.5, 3.0))
+        if k % 3 == 0:    # a box's inertia, possibly with its centre moved away
+            d = rng.uniform(0.1, 2.0, 3)
+            I = m.mass / 12 * np.diag([d[1] ** 2 + d[2] ** 2, d[0] ** 2 + d[2] ** 2, d[0] ** 2 + d[1] ** 2])
+            c = rng.normal(size=3) * (0.05 if k % 2 else 2.0)
+        else:
+            a = rng.normal(size=(3, 3))
+            I = a @ a.T if k % 3 == 1 else (a + a.T) / 2
+            c = rng.normal(size=3) * 0.3
+        for i in range(3):
+            m.c[i] = float(c[i])
+            for j in range(3):
+                m.I[i * 4 + j] = float(I[i, j])
+        got.append(ours.dMassCheck(C.byref(m)))
+        want.append(ref.dMassCheck(C.byref(m)))
+    assert got == want
+    assert 100 < sum(want) < 500
