@@ -34,6 +34,21 @@ METRIC = "world-steps/s, batched collide+QuickStep (4096 worlds)"
 N_WORLDS = 4096
 WORKLOAD = "batched_worlds: 4096 worlds, N~logU[4,64] spheres/boxes, 25% ball chains, plane"
 SCENE_SEED = 1
+# The timed window starts from the rollout's state at this step: the piles have
+# settled (about 130 constraint rows per world), where the steady-state cost
+# of a step lies. Steps 0-20 are mostly free fall (about 15 rows per world).
+SETTLE_STEP = 150
+# CPU timings repeat their window from the same state until at least this long
+CPU_MIN_SECONDS = 2.0
+
+
+def bench_config(steps, iters=20):
+    """The workload description both arms print (identical for the same
+    --steps)."""
+    return {"workload": WORKLOAD, "n_worlds": N_WORLDS, "iterations": iters, "dt": 0.01,
+            "rollout": f"steps {SETTLE_STEP}..{SETTLE_STEP + steps - 1} of the rollout (state at step "
+                       f"{SETTLE_STEP} reached untimed)",
+            "l2": "flushed between timed GPU steps (256 MB write)"}
 
 
 def rank_env():
@@ -166,6 +181,25 @@ def cpu_baseline(sc, n_worlds_sample, n_steps, threads=None):
     L.oracle_run_worlds(C.byref(sc.c), 0, n_worlds_sample, n_steps, threads, None)
     dt = time.perf_counter() - t0
     return n_worlds_sample * n_steps / dt, threads, dt
+
+
+def cpu_window(sc, start_step, n_steps, threads=None, min_seconds=CPU_MIN_SECONDS):
+    """The oracle port on every world of the workload: its own FP64 rollout
+    to `start_step` (untimed), then the window of n_steps steps from that state
+    timed on all host threads, repeated from the same state until at least
+    min_seconds have been timed. Returns (world-steps/s, threads, seconds
+    timed, repeats)."""
+    import oracle_lib as O
+    threads = threads or (os.cpu_count() or 1)
+    x, seeds, _ = O.step_worlds_from(sc, 0, start_step, threads=threads, counts=False)
+    done, t_sum, reps = 0, 0.0, 0
+    while t_sum < min_seconds or reps == 0:
+        t0 = time.perf_counter()
+        O.step_worlds_from(sc, start_step, n_steps, state=x, seeds=seeds, threads=threads, counts=False)
+        t_sum += time.perf_counter() - t0
+        done += sc.n_worlds * n_steps
+        reps += 1
+    return done / t_sum, threads, t_sum, reps
 
 
 ADJ_WORKLOAD = ("hinge_chains: 1024 worlds x 8-link hinge chains (0.5x0.1x0.1 m, 1 kg), per-step torques "
@@ -412,20 +446,48 @@ def run_reference(args):
     import oracle_lib as O
     O.build_oracle()
     threads = os.cpu_count() or 1
-    sample = min(N_WORLDS, args.ref_worlds)
-    cpu_baseline(sc, min(sample, 4 * threads), max(1, args.warmup))      # warm-up
-    value, _, dt = cpu_baseline(sc, sample, args.steps, threads)
+    # warm-up: W steps of every world from the initial state
+    O.step_worlds_from(sc, 0, max(1, args.warmup), threads=threads, counts=False)
+    value, _, dt, reps = cpu_window(sc, SETTLE_STEP, args.steps, threads)
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "world-steps/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * N_WORLDS / value, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
-            "config": {"workload": WORKLOAD, "n_worlds": N_WORLDS, "iterations": 20, "dt": 0.01},
+            "config": bench_config(args.steps),
             "cpu_baseline": {"value": value, "unit": "world-steps/s", "cores": threads, "kind": "port",
-                             "sample": f"worlds 0..{sample - 1} of the workload, {args.steps} steps "
-                                       f"from the initial state ({dt:.1f} s), {threads} threads"},
+                             "sample": f"all {N_WORLDS} worlds, steps {SETTLE_STEP}..{SETTLE_STEP + args.steps - 1} "
+                                       f"of the oracle's own rollout, repeated {reps}x ({dt:.1f} s timed), "
+                                       f"{threads} threads, one world per thread at a time"},
             "e2e": {"value": value, "unit": "world-steps/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def state_error_sample(sc, B, x_start, seeds_start, step, n_sample=64):
+    """One GPU step from the batch's FP32 state at `step` against one oracle
+    step from the same state, on n_sample worlds spread over the batch: max
+    abs position error (m), max position error relative to the world's
+    extent, max linear / angular velocity error."""
+    import oracle_lib as O
+    B.set_state(x_start)
+    B.set_seeds(seeds_start)
+    B.set_step_index(step)
+    B.step(1)
+    g = B.state()
+    ws = np.linspace(0, sc.n_worlds - 1, n_sample).astype(int)
+    pos_abs = pos_rel = lv = av = 0.0
+    for w in ws:
+        b0, b1 = sc.world_bodies(int(w))
+        o, _, _ = O.step_worlds_from(sc, step, 1, state=x_start[b0:b1], seeds=seeds_start[w:w + 1],
+                                     w_begin=int(w), w_end=int(w) + 1, threads=1, counts=False)
+        e = np.abs(g[b0:b1] - o)
+        pos_abs = max(pos_abs, float(e[:, 0:3].max()))
+        pos_rel = max(pos_rel, float(e[:, 0:3].max() / max(1.0, np.abs(o[:, 0:3]).max())))
+        lv = max(lv, float(e[:, 7:10].max()))
+        av = max(av, float(e[:, 10:13].max()))
+    return {"pos_abs_m": pos_abs, "pos_rel": pos_rel, "lvel_abs": lv, "avel_abs": av,
+            "sample": f"{n_sample} worlds, one step from the GPU's FP32 state at step {step} against "
+                      f"one FP64 oracle step from the same state"}
 
 
 def run_ours(args):
@@ -445,59 +507,70 @@ def run_ours(args):
     stream = torch.cuda.ExternalStream(B.stream_handle())
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     iters = sc.world_params[0].iterations
-    init_state = B.state()
-    init_seeds = B.seeds()
-
-    def reset():
-        B.set_state(init_state)
-        B.set_seeds(init_seeds)
-        B.set_step_index(0)
+    init_state, init_seeds = B.state(), B.seeds()
 
     def barrier():
         if dist:
             torch.distributed.barrier()
         torch.cuda.synchronize()
 
-    for _ in range(args.warmup):
-        B.step(1)
+    # the rollout to the settled state (untimed)
+    B.step(SETTLE_STEP)
     B.sync()
-    # launch shapes picked by the library's autotuner on the warmed-up state
+    settled_state, settled_seeds = B.state(), B.seeds()
+
+    def reset(to_initial=False):
+        B.set_state(init_state if to_initial else settled_state)
+        B.set_seeds(init_seeds if to_initial else settled_seeds)
+        B.set_step_index(0 if to_initial else SETTLE_STEP)
+
+    # launch shapes picked by the library's autotuner on the settled state
     # (outside the timed region; the state is restored below)
     launch_cfg = B.autotune(4)
     reset()
-    barrier()
+    for _ in range(args.warmup):
+        B.step(1)
+    B.sync()
+
+    def timed_window(from_initial=False):
+        reset(from_initial)
+        barrier()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(args.steps)]
+        rec = dict(bytes=[], solve_bytes=0.0, rows=0)
+        B.set_timing(True)                # events around each kernel, on the batch stream
+        B.kernel_times()                  # reset the per-kernel sums
+        launches0 = B.launch_count()
+        barrier()
+        for k in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.add_(1.0)           # evict L2 between timed steps (256 MB > 129 MB L2)
+                ev[k][0].record(stream)
+            B.step(1)
+            with torch.cuda.stream(stream):
+                ev[k][1].record(stream)
+            nc, nr, _ = B.counts()        # host read between steps, outside the events
+            rec["bytes"].append(algorithmic_bytes(sc, nc, nr, iters))
+            rec["solve_bytes"] += solve_bytes(nr, iters)
+            rec["rows"] += int(np.sum(nr))
+        B.sync()
+        barrier()
+        rec["launches"] = B.launch_count() - launches0
+        rec["kern_ms"], rec["kern_steps"] = B.kernel_times()
+        B.set_timing(False)
+        rec["times"] = np.array([a.elapsed_time(b) for a, b in ev]) / 1e3
+        rec["status"] = B.status()
+        return rec
+
     clocks = ClockSampler(local_rank)
     clocks.start()
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-          for _ in range(args.steps)]
-    bytes_per_step = []
-    solve_bytes_total = 0.0
-    rows_total = 0
-    B.set_timing(True)                # events around each kernel, on the batch stream
-    launches0 = B.launch_count()
-    barrier()
-    for k in range(args.steps):
-        with torch.cuda.stream(stream):
-            flush.add_(1.0)           # evict L2 between timed steps (256 MB > 129 MB L2)
-            ev[k][0].record(stream)
-        B.step(1)
-        with torch.cuda.stream(stream):
-            ev[k][1].record(stream)
-        nc, nr, _ = B.counts()        # host read between steps, outside the events
-        bytes_per_step.append(algorithmic_bytes(sc, nc, nr, iters))
-        solve_bytes_total += solve_bytes(nr, iters)
-        rows_total += int(np.sum(nr))
-    B.sync()
-    barrier()
+    main = timed_window()
     clk = clocks.stop()
-    launches = B.launch_count() - launches0
-    kern_ms, kern_steps = B.kernel_times()
-    B.set_timing(False)
-    times = np.array([a.elapsed_time(b) for a, b in ev]) / 1e3
-    t_kernel = float(times.sum())
-    stat = B.status()
+    t_kernel = float(main["times"].sum())
     t_max = max_over_ranks(t_kernel, device="cuda")
     value = N_WORLDS * world_size * args.steps / t_max
+    first = timed_window(from_initial=True)
+    t_first = max_over_ranks(float(first["times"].sum()), device="cuda")
 
     # e2e through the C ABI with host buffers: per step H2D of the state from
     # pinned memory, the step, D2H of the new state, synchronised
@@ -521,28 +594,32 @@ def run_ours(args):
 
     if rank == 0:
         hbm, src = peaks()
-        step_achieved = float(np.sum(bytes_per_step)) / t_kernel / 1e9
+        kern_ms, kern_steps = main["kern_ms"], main["kern_steps"]
+        step_achieved = float(np.sum(main["bytes"])) / t_kernel / 1e9
         t_solve = kern_ms[2] / 1e3
-        achieved = solve_bytes_total / t_solve / 1e9
+        achieved = main["solve_bytes"] / t_solve / 1e9
         tpr = solve_traffic_per_row_iter()
-        traffic = tpr * rows_total * iters / args.steps if tpr is not None else None
+        traffic = tpr * main["rows"] * iters / args.steps if tpr is not None else None
         share = kern_ms / kern_ms.sum()
+        times = main["times"]
         line = {"metric": METRIC, "value": value, "unit": "world-steps/s", "n_gpus": world_size,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                 "data": "synthetic (seeded)",
-                "config": {"workload": WORKLOAD, "n_worlds": N_WORLDS, "iterations": iters,
-                           "dt": 0.01, "rollout": f"steps 0..{args.steps - 1} from the initial state",
-                           "l2": "flushed between timed steps (256 MB write)",
-                           "rows_per_world_avg": rows_total / (args.steps * N_WORLDS),
-                           "bodies": int(nbt), "worlds_with_status": int((stat != 0).sum()),
+                "config": bench_config(args.steps, iters),
+                "window": {"rows_per_world_avg": main["rows"] / (args.steps * N_WORLDS),
+                           "bodies": int(nbt), "worlds_with_status": int((main["status"] != 0).sum()),
                            "launch_shape": {"collide": launch_cfg[0], "setup": launch_cfg[1],
                                             "solve": launch_cfg[2]},
                            "step_ms_min_median_max": [float(1e3 * times.min()), float(1e3 * np.median(times)),
                                                       float(1e3 * times.max())]},
+                "from_initial_state": {"value": N_WORLDS * world_size * args.steps / t_first,
+                                       "unit": "world-steps/s",
+                                       "rollout": f"steps 0..{args.steps - 1} from the initial state",
+                                       "rows_per_world_avg": first["rows"] / (args.steps * N_WORLDS)},
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                              "frac": achieved / hbm, "peak_source": src, "traffic": traffic,
-                             "kernel": "world_solve_kernel (SOR_LCP + integration, one warp per world)",
+                             "kernel": "world_solve_kernel (SOR_LCP + integration)",
                              "bytes_model": "236 B per row-iteration (rows x iterations of the launch)",
                              "launch_ms_avg": kern_ms[2] / max(1, kern_steps),
                              "traffic_source": "ncu dram bytes per row-iteration (profiles/) x rows x iters"},
@@ -552,11 +629,13 @@ def run_ours(args):
                                  "world_solve_kernel": share[2]},
                 "e2e": {"value": e2e, "unit": "world-steps/s", "h2d_bytes_per_step": nbt * 13 * 4,
                         "d2h_bytes_per_step": nbt * 13 * 4},
-                "gpu_launches": launches, "clocks": clk}
+                "gpu_launches": main["launches"], "clocks": clk}
+        if not args.no_cpu:
+            line["state_err"] = state_error_sample(sc, B, settled_state, settled_seeds, SETTLE_STEP)
         if not args.no_plain:
-            # plain comparator: the same kernel, one world per launch, first
-            # 512 worlds x 20 steps from the initial state
-            reset()
+            # plain comparator: the same kernels, one world per launch, first
+            # 512 worlds x 20 steps from the initial state, against the batched
+            # path over the same worlds and steps
             pw = 512
             sub = build_scene(pw)
             P = Batch(sub, device=local_rank)
@@ -567,7 +646,8 @@ def run_ours(args):
             P.sync()
             tp = time.perf_counter() - t0
             line["plain_gpu"] = {"value": pw * 20 / tp, "unit": "world-steps/s",
-                                 "sample": f"first {pw} worlds x 20 steps, one world per launch"}
+                                 "sample": f"first {pw} worlds x 20 steps, one world per launch",
+                                 "batched_from_initial_over_plain": N_WORLDS * args.steps / t_first / (pw * 20 / tp)}
             P.close()
         if not args.no_adjoint:
             line["adjoint"] = run_adjoint(local_rank)
@@ -578,11 +658,10 @@ def run_ours(args):
         if not args.no_exact:
             line["exact_step"] = run_exact(local_rank)
         if not args.no_cpu:
-            nw = min(N_WORLDS, args.cpu_worlds)
-            v, thr, dt = cpu_baseline(sc, nw, args.steps)
+            v, thr, dt, reps = cpu_window(sc, SETTLE_STEP, args.steps)
             line["cpu_baseline"] = {"value": v, "unit": "world-steps/s", "cores": thr, "kind": "port",
-                                    "sample": f"worlds 0..{nw - 1} of the workload, {args.steps} steps from "
-                                              f"the initial state ({dt:.1f} s)"}
+                                    "sample": f"all {N_WORLDS} worlds, steps {SETTLE_STEP}..{SETTLE_STEP + args.steps - 1} "
+                                              f"of the oracle's own rollout, repeated {reps}x ({dt:.1f} s timed)"}
         print(json.dumps(line), flush=True)
     B.close()
     if dist:
@@ -611,8 +690,6 @@ def main():
     ap.add_argument("--exact-steps", type=int, default=100)
     ap.add_argument("--only-large", action="store_true",
                     help="print only the large-world measurement (for profiling)")
-    ap.add_argument("--cpu-worlds", type=int, default=512)
-    ap.add_argument("--ref-worlds", type=int, default=4096)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -256,18 +256,23 @@ int odegpuBatchGetContacts(odegpuBatchID b, int w, float* out, int cap);
  * in a fixed device array compiled into the library instead (a few hundred
  * bytes, held by every GPU that loads the library until the process exits)
  * and allocates nothing.
- *   - Geoms are given by class (ODEGPU_GEOM_SPHERE/BOX/CAPSULE/PLANE),
- *     class parameters as in odegpuScene (4 floats), position (3) and a 3x4
- *     row-major rotation (12); pos/R may be NULL for a plane.
+ *   - Geoms are given by class (ODEGPU_GEOM_SPHERE, _BOX, _CAPSULE,
+ *     _CYLINDER, _PLANE or _RAY; any other class, heightfields included,
+ *     fails with ODEGPU_E_ARG), class parameters as in odegpuScene
+ *     (4 floats), position (3) and a 3x4 row-major rotation (12); pos/R may
+ *     be NULL for a plane.
  *   - flags & 0xffff contacts are requested, at most
  *     ODEGPU_NOALLOC_MAX_CONTACTS; a larger request fails with ODEGPU_E_LIMIT.
  *   - contacts_out (host memory) receives count x 7 floats: pos[3],
- *     normal[3], depth, with dCollide's conventions. Returns the count.
- *   - The first call on a device looks up the array's device address (done
- *     once per device, with that device current); make that first call before
- *     any stream capture.
- *   - All calls share the one array; it is reset at the start of each call.
- *     Calls from several host threads that overlap on the GPU race on it. */
+ *     normal[3], depth, with dCollide's conventions; nothing past the count
+ *     is written. Returns the count.
+ *   - Each call, with the caller's device current, looks up the array's
+ *     device address in the current context (cudaGetSymbolAddress, which
+ *     allocates nothing), launches the collider on the legacy default stream
+ *     and copies the contacts back synchronously before returning.
+ *   - All calls share the one array; its count is reset at the start of each
+ *     call, and it keeps the last call's contents afterwards. Calls from
+ *     several host threads that overlap on the GPU race on it. */
 #define ODEGPU_NOALLOC_MAX_CONTACTS 8
 int odegpuCollideNoAlloc(int class1, const float* params1, const float* pos1, const float* R1,
                          int class2, const float* params2, const float* pos2, const float* R2,

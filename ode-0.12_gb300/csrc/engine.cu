@@ -1841,11 +1841,6 @@ struct NoAllocScratch {
 };
 static __device__ __align__(256) NoAllocScratch g_noalloc_scratch[1];
 
-// Device address of g_noalloc_scratch per device, looked up once per device
-// (host code may not use the symbol's name as an address).
-constexpr int kMaxDevices = 64;
-NoAllocScratch* g_noalloc_ptr[kMaxDevices] = {};
-
 __global__ void collide_pair_noalloc_kernel(GeomView a, GeomView b, unsigned flags, NoAllocScratch* s) {
   if (threadIdx.x == 0 && blockIdx.x == 0) {
     Contact c[8];
@@ -1883,16 +1878,18 @@ extern "C" int odegpuCollideNoAlloc(int class1, const float* params1, const floa
     return fail(ODEGPU_E_LIMIT, "odegpuCollideNoAlloc returns at most " +
                                     std::to_string(ODEGPU_NOALLOC_MAX_CONTACTS) + " contacts; asked for " +
                                     std::to_string(maxc));
-  int dev = 0;
-  OG_CUDA(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= kMaxDevices) return fail(ODEGPU_E_LIMIT, "device ordinal out of range");
-  if (!g_noalloc_ptr[dev]) {
-    // set-up on the first call on this device, with the device current
-    void* p = nullptr;
-    OG_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
-    g_noalloc_ptr[dev] = static_cast<NoAllocScratch*>(p);
-  }
-  NoAllocScratch* s = g_noalloc_ptr[dev];
+  for (const int cls : {class1, class2})
+    if (cls < ODEGPU_GEOM_SPHERE || cls > ODEGPU_GEOM_RAY)
+      return fail(ODEGPU_E_ARG, "odegpuCollideNoAlloc takes sphere, box, capsule, cylinder, plane and ray geoms; "
+                                "got class " + std::to_string(cls));
+  // Set-up, with the caller's device current: the array's device address in
+  // the current context. Host code may not use the symbol's name as an
+  // address. The lookup allocates nothing and is repeated on every call
+  // rather than cached per device, so a cudaDeviceReset or a host that runs
+  // the device under its own context never leaves a stale address behind.
+  void* sp = nullptr;
+  OG_CUDA(cudaGetSymbolAddress(&sp, g_noalloc_scratch));
+  NoAllocScratch* s = static_cast<NoAllocScratch*>(sp);
   const GeomView a = make_view(class1, params1, pos1, R1);
   const GeomView b = make_view(class2, params2, pos2, R2);
   collide_pair_noalloc_kernel<<<1, 32>>>(a, b, (unsigned)flags, s);

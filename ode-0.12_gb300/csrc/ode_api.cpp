@@ -1663,9 +1663,11 @@ static int positive_definite3(const float* A) {
   return 1;
 }
 // dMassCheck (mass.cpp:44-83): mass > 0, I positive definite, and the
-// inertia about the centre of mass, I + mass crossmat(c)^2, as well
+// inertia about the centre of mass, I + mass crossmat(c)^2, as well. The
+// mass test is the reference's `mass <= 0`, so a NaN mass goes on to the
+// inertia tests as it does there.
 int dMassCheck(const dMass* m) {
-  if (!(m->mass > 0)) return 0;
+  if (m->mass <= 0) return 0;
   if (!positive_definite3(m->I)) return 0;
   float chat[12], I2[12];
   cross_mat(chat, m->c);

@@ -318,6 +318,7 @@ typedef struct {
   real gravity[3], erp, cfm, sor_w, max_vel, min_depth, dt;
   int iterations, max_contacts;
   oracleTap* tap;
+  int last_rows, last_islands;   /* rows and islands with rows of the last step */
 } OWorld;
 
 static void body_attach(OBody* b, int j) {
@@ -3164,6 +3165,8 @@ static void quick_stepper(OWorld* W, const int* bidx, int nb, const int* jidx, i
     int mm = joint_info1(W, &W->joint[jidx[i]]);
     if (mm > 0) { jl[nj] = jidx[i]; jm[nj] = mm; nj++; m += mm; }
   }
+  W->last_rows += m;
+  W->last_islands += m > 0;
   real* cforce = (real*)calloc((size_t)(nb > 0 ? nb : 1) * 6, sizeof(real));
   real *J = 0, *lambda = 0;
   int* jb = 0;
@@ -3984,6 +3987,8 @@ static void exact_stepper(OWorld* W, const int* bidx, int nb, const int* jidx, i
   int m = 0;
   int* ofs = (int*)malloc((size_t)(nj > 0 ? nj : 1) * sizeof(int));
   for (int k = 0; k < nj; ++k) { ofs[k] = m; m += ji[k].m; }
+  W->last_rows += m;
+  W->last_islands += m > 0;
   real* cforce = (real*)calloc((size_t)(nb > 0 ? nb : 1) * 6, sizeof(real));
   if (m > 0) {
     real* lo = (real*)malloc(m * sizeof(real));
@@ -4358,6 +4363,7 @@ static void process_islands(OWorld* W) {
   int* stack = (int*)malloc((size_t)(nb > 0 ? nb : 1) * sizeof(int));
   for (int i = 0; i < nb; ++i) W->body[i].tag = 0;
   for (int j = 0; j < nj; ++j) W->joint[j].tag = 0;
+  W->last_rows = W->last_islands = 0;
   int island = 0;
   for (int bb = nb - 1; bb >= 0; --bb) {
     if (W->body[bb].tag) continue;
@@ -4768,6 +4774,80 @@ long long oracle_run_worlds(const odegpuScene* sc, int w_begin, int w_end, int n
   for (int t = 0; t < n_threads; ++t) { pthread_join(th[t], 0); total += args[t].contacts; }
   free(th); free(args);
   return total;
+}
+
+typedef struct {
+  const odegpuScene* sc;
+  int w_begin, w_end, step0, n_steps, t;
+  const double* state_in;
+  const unsigned* seed_in;
+  double* state_out;
+  unsigned* seed_out;
+  int* counts;
+  int* next;          /* shared work counter (worlds are handed out in order) */
+  pthread_mutex_t* mu;
+} FromArg;
+
+static void* step_from_thread(void* p) {
+  FromArg* a = (FromArg*)p;
+  const odegpuScene* sc = a->sc;
+  const size_t b_first = (size_t)sc->body_off[a->w_begin];
+  for (;;) {
+    pthread_mutex_lock(a->mu);
+    const int w = (*a->next)++;
+    pthread_mutex_unlock(a->mu);
+    if (w >= a->w_end) break;
+    OWorld W;
+    world_init(&W, sc, w);
+    const size_t b0 = (size_t)sc->body_off[w] - b_first;
+    if (a->state_in) write_state(&W, a->state_in + b0 * ORACLE_BODY_REC);
+    g_seed = a->seed_in ? a->seed_in[w - a->w_begin] : sc->world[w].seed;
+    for (int s = 0; s < a->n_steps; ++s) {
+      const int nc = world_step(&W, a->step0 + s, 0, 0);
+      if (a->counts) {
+        int* c = a->counts + ((size_t)(w - a->w_begin) * a->n_steps + s) * 3;
+        c[0] = nc; c[1] = W.last_rows; c[2] = W.last_islands;
+      }
+    }
+    if (a->state_out) read_state(&W, a->state_out + b0 * ORACLE_BODY_REC);
+    if (a->seed_out) a->seed_out[w - a->w_begin] = g_seed;
+    world_free(&W);
+  }
+  return 0;
+}
+
+int oracle_step_worlds_from(const odegpuScene* sc, int w_begin, int w_end, int step0, int n_steps,
+                            int n_threads, const double* state_in, const unsigned int* seed_in,
+                            double* state_out, unsigned int* seed_out, int* counts) {
+  if (!sc || w_begin < 0 || w_end > sc->n_worlds || w_begin > w_end || n_steps < 0 || step0 < 0) return -1;
+  if (n_threads < 1) n_threads = 1;
+  pthread_t* th = (pthread_t*)malloc(n_threads * sizeof(pthread_t));
+  FromArg* args = (FromArg*)calloc(n_threads, sizeof(FromArg));
+  pthread_mutex_t mu = PTHREAD_MUTEX_INITIALIZER;
+  int next = w_begin;
+  for (int t = 0; t < n_threads; ++t) {
+    FromArg* a = &args[t];
+    a->sc = sc; a->w_begin = w_begin; a->w_end = w_end; a->step0 = step0; a->n_steps = n_steps; a->t = t;
+    a->state_in = state_in; a->seed_in = seed_in; a->state_out = state_out; a->seed_out = seed_out;
+    a->counts = counts; a->next = &next; a->mu = &mu;
+    pthread_create(&th[t], 0, step_from_thread, a);
+  }
+  for (int t = 0; t < n_threads; ++t) pthread_join(th[t], 0);
+  free(th); free(args);
+  return 0;
+}
+
+int oracle_step_world_contacts(const odegpuScene* sc, int w, int step, const double* state_in,
+                               unsigned int seed, double* contacts, int max_rec, double* state_out) {
+  if (!sc || w < 0 || w >= sc->n_worlds || step < 0) return -1;
+  OWorld W;
+  world_init(&W, sc, w);
+  if (state_in) write_state(&W, state_in);
+  g_seed = seed;
+  const int nc = world_step(&W, step, contacts, max_rec);
+  if (state_out) read_state(&W, state_out);
+  world_free(&W);
+  return nc;
 }
 
 int oracle_tap_step(const odegpuScene* sc, int w, int pre_steps, oracleTap* tap) {

@@ -40,6 +40,26 @@ int oracle_run_world_from(const odegpuScene* sc, int w, int n_steps, const doubl
 long long oracle_run_worlds(const odegpuScene* sc, int w_begin, int w_end, int n_steps,
                             int n_threads, double* final_state);
 
+/* Worlds [w_begin, w_end), each built from the scene with its body state
+ * replaced by state_in (the range's bodies, [nb][13]; NULL: the scene's
+ * initial state) and its dRand seed by seed_in[w - w_begin] (NULL: the
+ * scene's), stepped n_steps times as steps step0, step0 + 1, ... (the step
+ * index selects the per-step controls), on n_threads host threads.
+ * state_out receives the final states, seed_out the seeds after the last
+ * step, counts [w][n_steps][3] each step's contacts, constraint rows and
+ * islands with rows (any output may be NULL). Returns 0 or -1. */
+int oracle_step_worlds_from(const odegpuScene* sc, int w_begin, int w_end, int step0, int n_steps,
+                            int n_threads, const double* state_in, const unsigned int* seed_in,
+                            double* state_out, unsigned int* seed_out, int* counts);
+
+/* One step (step index `step`) of world w from state_in ([nb][13]; NULL: the
+ * scene's initial state) with dRand seed `seed`; contacts receives up to
+ * max_rec records [9] (pos, normal, depth, geom i, geom k) in creation order,
+ * state_out (may be NULL) the state after the step. Returns the contact
+ * count or -1. */
+int oracle_step_world_contacts(const odegpuScene* sc, int w, int step, const double* state_in,
+                               unsigned int seed, double* contacts, int max_rec, double* state_out);
+
 /* Stage taps for per-kernel parity. For world w, run `pre_steps` full steps,
  * then for the next step record, in ODE's island/row order:
  *   n_islands, island_rows[i] (rows per island), island_bodies[i],

@@ -9,7 +9,9 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 SRC = os.path.join(ROOT, "tests", "c_api", "box_drop_demo.c")
 PLAYER = os.path.join(ROOT, "tests", "c_api", "scene_player.c")
 PKG = os.path.join(ROOT, "ode-0.12_gb300")
-REF_ROOT = "/root/reference/ode-0.12"
+# the reference checkout (headers of the reference build): ODE_REF_SRC, else
+# the checkout beside this repository
+REF_ROOT = os.environ.get("ODE_REF_SRC") or os.path.normpath(os.path.join(ROOT, "..", "reference", "ode-0.12"))
 
 
 def build_gpu_demo(out, src=SRC):

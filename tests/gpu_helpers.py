@@ -32,3 +32,89 @@ def state_err(gpu, ref):
                 q=np.abs(q_g * sgn - q_r).max(initial=0),
                 lvel=np.abs(gpu[:, 7:10] - ref[:, 7:10]).max(initial=0),
                 avel=np.abs(gpu[:, 10:13] - ref[:, 10:13]).max(initial=0))
+
+
+def round32(x):
+    """A state as the GPU stores it (FP32), back in FP64."""
+    return np.asarray(x, np.float64).astype(np.float32).astype(np.float64)
+
+
+def world_errors(gpu, ref, body_off):
+    """Per world max abs error of pos / sign-aligned quaternion / lvel / avel:
+    array [n_worlds, 4]."""
+    q_g, q_r = gpu[:, 3:7], ref[:, 3:7]
+    sgn = np.sign(np.sum(q_g * q_r, axis=1, keepdims=True))
+    sgn[sgn == 0] = 1
+    e = np.stack([np.abs(gpu[:, 0:3] - ref[:, 0:3]).max(axis=1),
+                  np.abs(q_g * sgn - q_r).max(axis=1),
+                  np.abs(gpu[:, 7:10] - ref[:, 7:10]).max(axis=1),
+                  np.abs(gpu[:, 10:13] - ref[:, 10:13]).max(axis=1)], axis=1)
+    return np.maximum.reduceat(e, np.asarray(body_off[:-1]), axis=0)
+
+
+def ill_conditioned(scene, w, step, x_world, seed, want, trials=16, ulps=16, seed_rng=0):
+    """Does the oracle's own (contacts, rows, islands) of world w at `step`
+    change when its starting positions and orientations move by up to `ulps`
+    FP32 units in the last place? A decision that flips under perturbations of
+    that size is a tie at FP32 resolution, which FP32 and FP64 arithmetic may
+    break either way."""
+    rng = np.random.default_rng(seed_rng)
+    x32 = np.asarray(x_world, np.float64).astype(np.float32)
+    for _ in range(trials):
+        xp = x32.copy()
+        sp = np.spacing(np.abs(xp[:, 0:7])).astype(np.float32)
+        xp[:, 0:7] += (rng.integers(-ulps, ulps + 1, size=xp[:, 0:7].shape) * sp).astype(np.float32)
+        _, _, c = O.step_worlds_from(scene, step, 1, state=xp.astype(np.float64), seeds=[seed],
+                                     w_begin=w, w_end=w + 1, threads=1)
+        if not np.array_equal(c[0, 0], want):
+            return True
+    return False
+
+
+def rollout_parity(scene, n_steps, make_batch, state_steps=(), tol=None, max_ill_frac=1e-3):
+    """Every step of the oracle's own FP64 rollout of `scene` is rounded to
+    FP32 (what the GPU stores) and stepped once by the GPU and once by the
+    oracle from that identical input. Per world and step, contacts, rows,
+    islands with rows and the dRand seed after the step must be equal; a
+    difference is accepted only where the oracle's own counts flip under
+    FP32-sized perturbations of the input (ill_conditioned), and such cases
+    stay below max_ill_frac of the world-steps. At the steps in state_steps
+    the GPU's state after the step must agree with the oracle's within tol
+    (pos, q, lvel, avel) in every world whose integer outputs agree.
+    Returns a summary dict."""
+    B = make_batch(scene)
+    off = np.asarray(scene.body_off)
+    x, seeds, _ = O.step_worlds_from(scene, 0, 0, counts=False)
+    nw = scene.n_worlds
+    ill, bad, worst, checked = [], [], np.zeros(4), 0
+    for k in range(n_steps):
+        x32 = round32(x)
+        xo, so, co = O.step_worlds_from(scene, k, 1, state=x32, seeds=seeds)
+        B.set_state(x32)
+        B.set_seeds(seeds)
+        B.set_step_index(k)
+        B.step(1)
+        nc, nr, ni = B.counts()
+        g_counts = np.stack([nc, nr, ni], axis=1)
+        ok = (g_counts == co[:, 0]).all(axis=1) & (B.seeds() == so)
+        assert (B.status() == 0).all(), (k, np.nonzero(B.status())[0][:8])
+        for w in np.nonzero(~ok)[0]:
+            if ill_conditioned(scene, int(w), k, x32[off[w]:off[w + 1]], int(seeds[w]), co[w, 0],
+                               seed_rng=k * nw + int(w)):
+                ill.append((k, int(w)))
+            else:
+                bad.append((k, int(w), g_counts[w].tolist(), co[w, 0].tolist()))
+        if k in state_steps:
+            e = world_errors(B.state(), xo, off)[ok]
+            worst = np.maximum(worst, e.max(axis=0, initial=0))
+            checked += int(ok.sum())
+            if tol is not None:
+                lim = np.asarray(tol)
+                over = np.nonzero((e > lim).any(axis=1))[0]
+                assert len(over) == 0, (k, e[over][:4], lim)
+        x, seeds, _ = O.step_worlds_from(scene, k, 1, state=x, seeds=seeds, counts=False)
+    B.close()
+    assert not bad, bad[:8]
+    assert len(ill) <= max_ill_frac * n_steps * nw, (len(ill), ill[:8])
+    return dict(world_steps=n_steps * nw, ill_conditioned=len(ill), worst=worst.tolist(),
+                state_worlds_checked=checked)

@@ -51,6 +51,13 @@ def oracle():
         lib.oracle_run_world_from.restype = C.c_int
         lib.oracle_run_world_from.argtypes = [C.c_void_p, C.c_int, C.c_int, _P(C.c_double),
                                               _P(C.c_double)]
+        lib.oracle_step_worlds_from.restype = C.c_int
+        lib.oracle_step_worlds_from.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                                _P(C.c_double), _P(C.c_uint), _P(C.c_double), _P(C.c_uint),
+                                                _P(C.c_int)]
+        lib.oracle_step_world_contacts.restype = C.c_int
+        lib.oracle_step_world_contacts.argtypes = [C.c_void_p, C.c_int, C.c_int, _P(C.c_double), C.c_uint,
+                                                   _P(C.c_double), C.c_int, _P(C.c_double)]
         lib.oracle_set_stepper.argtypes = [C.c_int]
         lib.oracle_lcp_errors.restype = C.c_int
         _oracle = lib
@@ -143,6 +150,43 @@ def run_world_from(scene, w, n_steps, init_state):
                                         out.ctypes.data_as(_P(C.c_double)))
     assert rc == 0
     return out
+
+
+def step_worlds_from(scene, step0, n_steps, state=None, seeds=None, w_begin=0, w_end=None, threads=None,
+                     counts=True):
+    """Worlds [w_begin, w_end) stepped n_steps times (as steps step0, ...)
+    from `state` ([bodies of the range, 13], FP64; None: the scene's initial
+    state) and `seeds` (None: the scene's), on all host threads. Returns
+    (final state [nb, 13], seeds after [n], counts [n, n_steps, 3] of
+    contacts / rows / islands with rows, or None)."""
+    w_end = scene.n_worlds if w_end is None else w_end
+    nbr = int(scene.body_off[w_end] - scene.body_off[w_begin])
+    out = np.zeros((nbr, 13))
+    so = np.zeros(w_end - w_begin, np.uint32)
+    cnt = np.zeros((w_end - w_begin, n_steps, 3), np.int32) if counts else None
+    xin = None if state is None else np.ascontiguousarray(state, dtype=np.float64)
+    sin = None if seeds is None else np.ascontiguousarray(seeds, dtype=np.uint32)
+    rc = oracle().oracle_step_worlds_from(
+        C.byref(scene.c), w_begin, w_end, step0, n_steps, threads or (os.cpu_count() or 1),
+        None if xin is None else xin.ctypes.data_as(_P(C.c_double)),
+        None if sin is None else sin.ctypes.data_as(_P(C.c_uint)),
+        out.ctypes.data_as(_P(C.c_double)), so.ctypes.data_as(_P(C.c_uint)),
+        None if cnt is None else cnt.ctypes.data_as(_P(C.c_int)))
+    assert rc == 0
+    return out, so, cnt
+
+
+def step_world_contacts(scene, w, step, state, seed, max_rec=65536):
+    """One oracle step of world w from `state` ([nb, 13]) with `seed`:
+    (contacts [n, 9] pos normal depth gi gk, state after [nb, 13])."""
+    x = np.ascontiguousarray(state, dtype=np.float64)
+    out = np.zeros((max_rec, 9))
+    after = np.zeros_like(x)
+    n = oracle().oracle_step_world_contacts(C.byref(scene.c), w, step, x.ctypes.data_as(_P(C.c_double)),
+                                            int(seed), out.ctypes.data_as(_P(C.c_double)), max_rec,
+                                            after.ctypes.data_as(_P(C.c_double)))
+    assert n >= 0
+    return out[:min(n, max_rec)], after
 
 
 class exact_stepper:

@@ -376,3 +376,16 @@ def test_mass_check_matches_reference():
         want.append(ref.dMassCheck(C.byref(m)))
     assert got == want
     assert 100 < sum(want) < 500
+    # NaN in the mass, the centre or the inertia
+    for field in ("mass", "c", "I"):
+        m = Mass()
+        m.mass = 1.0
+        for i in range(3):
+            m.I[i * 4 + i] = 0.1
+        if field == "mass":
+            m.mass = float("nan")
+        elif field == "c":
+            m.c[1] = float("nan")
+        else:
+            m.I[0] = float("nan")
+        assert ours.dMassCheck(C.byref(m)) == ref.dMassCheck(C.byref(m)), field
