@@ -500,9 +500,20 @@ def run_ours(args):
         import torch.distributed as tdist
         tdist.init_process_group("nccl")
     torch.cuda.set_device(local_rank)
-    # weak scaling: every rank steps its own 4096-world batch (distinct seeds);
-    # the step has no collective, only the timing is reduced
-    sc = build_scene(N_WORLDS, seed=rank_scene_seed(rank))
+    # weak scaling (default): every rank steps its own 4096-world batch
+    # (distinct seeds). --split (strong scaling): the ranks share one
+    # 4096-world scene, each stepping its contiguous block of worlds
+    # (odegpu.shard). Either way the step has no collective; only the timing
+    # is reduced.
+    if args.split and world_size > 1:
+        from odegpu.shard import bodies_per_world, slice_scene, world_blocks
+        full = build_scene(N_WORLDS)
+        b0, b1 = world_blocks(N_WORLDS, world_size, weights=bodies_per_world(full))[rank]
+        sc = slice_scene(full, b0, b1)
+        total_worlds, scaling = N_WORLDS, "strong"
+    else:
+        sc = build_scene(N_WORLDS, seed=rank_scene_seed(rank))
+        total_worlds, scaling = N_WORLDS * world_size, "weak"
     B = Batch(sc, device=local_rank)
     stream = torch.cuda.ExternalStream(B.stream_handle())
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
@@ -568,7 +579,7 @@ def run_ours(args):
     clk = clocks.stop()
     t_kernel = float(main["times"].sum())
     t_max = max_over_ranks(t_kernel, device="cuda")
-    value = N_WORLDS * world_size * args.steps / t_max
+    value = total_worlds * args.steps / t_max
     first = timed_window(from_initial=True)
     t_first = max_over_ranks(float(first["times"].sum()), device="cuda")
 
@@ -590,7 +601,7 @@ def run_ours(args):
         h_in, h_out = h_out, h_in
     barrier()
     t_e2e = max_over_ranks(time.perf_counter() - t0, device="cuda")
-    e2e = N_WORLDS * world_size * args.steps / t_e2e
+    e2e = total_worlds * args.steps / t_e2e
 
     if rank == 0:
         hbm, src = peaks()
@@ -604,19 +615,19 @@ def run_ours(args):
         times = main["times"]
         line = {"metric": METRIC, "value": value, "unit": "world-steps/s", "n_gpus": world_size,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps,
-                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "higher_is_better": True, "scaling": scaling, "vs_baseline": None, "dtype": "f32",
                 "data": "synthetic (seeded)",
                 "config": bench_config(args.steps, iters),
-                "window": {"rows_per_world_avg": main["rows"] / (args.steps * N_WORLDS),
+                "window": {"rows_per_world_avg": main["rows"] / (args.steps * sc.n_worlds),
                            "bodies": int(nbt), "worlds_with_status": int((main["status"] != 0).sum()),
                            "launch_shape": {"collide": launch_cfg[0], "setup": launch_cfg[1],
                                             "solve": launch_cfg[2]},
                            "step_ms_min_median_max": [float(1e3 * times.min()), float(1e3 * np.median(times)),
                                                       float(1e3 * times.max())]},
-                "from_initial_state": {"value": N_WORLDS * world_size * args.steps / t_first,
+                "from_initial_state": {"value": total_worlds * args.steps / t_first,
                                        "unit": "world-steps/s",
                                        "rollout": f"steps 0..{args.steps - 1} from the initial state",
-                                       "rows_per_world_avg": first["rows"] / (args.steps * N_WORLDS)},
+                                       "rows_per_world_avg": first["rows"] / (args.steps * sc.n_worlds)},
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                              "frac": achieved / hbm, "peak_source": src, "traffic": traffic,
                              "kernel": "world_solve_kernel (SOR_LCP + integration)",
@@ -647,7 +658,7 @@ def run_ours(args):
             tp = time.perf_counter() - t0
             line["plain_gpu"] = {"value": pw * 20 / tp, "unit": "world-steps/s",
                                  "sample": f"first {pw} worlds x 20 steps, one world per launch",
-                                 "batched_from_initial_over_plain": N_WORLDS * args.steps / t_first / (pw * 20 / tp)}
+                                 "batched_from_initial_over_plain": sc.n_worlds * args.steps / t_first / (pw * 20 / tp)}
             P.close()
         if not args.no_adjoint:
             line["adjoint"] = run_adjoint(local_rank)
@@ -687,6 +698,8 @@ def main():
     ap.add_argument("--only-exact", action="store_true",
                     help="print only the dWorldStep measurement (for profiling)")
     ap.add_argument("--exact-worlds", type=int, default=N_WORLDS)
+    ap.add_argument("--split", action="store_true",
+                    help="under torchrun: the ranks share one 4096-world scene (strong scaling)")
     ap.add_argument("--exact-steps", type=int, default=100)
     ap.add_argument("--only-large", action="store_true",
                     help="print only the large-world measurement (for profiling)")
