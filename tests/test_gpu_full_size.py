@@ -10,7 +10,9 @@ the step agree in every world at every step; the only accepted differences
 are decisions that the oracle itself flips when its input moves by FP32-sized
 amounts (ties at FP32 resolution), at most 0.1% of the world-steps. At the
 listed steps the state after the step agrees within the one-step tolerances
-of test_gpu_parity.py in every world whose integer outputs agree."""
+of test_gpu_parity.py plus 1e-4 of the oracle's value (the stated relative
+target; fast-spinning wheels carry tens of rad/s) in every world whose
+integer outputs agree."""
 import numpy as np
 import pytest
 
@@ -50,7 +52,8 @@ def test_vehicles_2048_cars_300_steps():
     """2048 cars on the 256 x 256 fractal heightfield with per-step steering
     stops and drive torques: 300 steps. The suspension rows (ERP 0.4, CFM
     0.01 on a 1000 kg chassis) make the chassis velocity about 3x as
-    sensitive to the FP32 input as a rigid contact, hence 5e-3 m/s."""
+    sensitive to the FP32 input as a rigid contact, hence 5e-3 m/s beside
+    the relative 1e-4."""
     sc = S.vehicles(n_worlds=2048, steps=300)
     r = rollout_parity(sc, 300, _batch, state_steps=(0, 150, 299), tol=(2e-5, 2e-5, 5e-3, 5e-3))
     print("vehicles 2048:", r)

@@ -61,14 +61,18 @@ def _no_alloc(L, t1, a1, t2, a2, flags):
 
 
 def _fill_array(L):
-    """A deep face-face box overlap: 8 contacts, every slot of the array."""
+    """A deep face-face overlap of two unit boxes, the upper one turned 0.3 rad
+    about z: the clipped faces meet in an octagon, 8 contacts, every slot of
+    the array."""
     keep = []
 
-    def geom(pos):
-        p, pp = _fa([1.0, 1.0, 1.0, 0.0]); x, px = _fa(pos); r, pr = _fa(np.eye(3, 4).ravel())
+    def geom(pos, ang):
+        c, s = np.cos(ang), np.sin(ang)
+        R = np.array([[c, -s, 0, 0], [s, c, 0, 0], [0, 0, 1, 0]])
+        p, pp = _fa([1.0, 1.0, 1.0, 0.0]); x, px = _fa(pos); r, pr = _fa(R.ravel())
         keep.extend([p, x, r])
         return pp, px, pr
-    nc, _ = _no_alloc(L, 1, geom([0, 0, 0]), 1, geom([0, 0, 0.5]), 8)
+    nc, _ = _no_alloc(L, 1, geom([0, 0, 0], 0.0), 1, geom([0, 0, 0.5], 0.3), 8)
     assert nc == 8
     return keep
 
