@@ -53,9 +53,13 @@ def test_vehicles_2048_cars_300_steps():
     stops and drive torques: 300 steps. The suspension rows (ERP 0.4, CFM
     0.01 on a 1000 kg chassis) make the chassis velocity about 3x as
     sensitive to the FP32 input as a rigid contact, hence 5e-3 m/s beside
-    the relative 1e-4."""
+    the relative 1e-4. A wheel's spin takes the friction impulse of a quarter
+    of the car (~25 N s per step) through its 0.35 m radius and 0.98 kg m^2
+    inertia: the 1e-3 relative difference that 20 unconverged FP32 Gauss-
+    Seidel iterations leave in that impulse is ~9e-3 rad/s, hence 1e-2
+    rad/s for angular velocity."""
     sc = S.vehicles(n_worlds=2048, steps=300)
-    r = rollout_parity(sc, 300, _batch, state_steps=(0, 150, 299), tol=(2e-5, 2e-5, 5e-3, 5e-3))
+    r = rollout_parity(sc, 300, _batch, state_steps=(0, 150, 299), tol=(2e-5, 2e-5, 5e-3, 1e-2))
     print("vehicles 2048:", r)
 
 
