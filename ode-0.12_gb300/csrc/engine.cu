@@ -81,8 +81,7 @@ __global__ void __launch_bounds__(256) world_solve_kernel(BatchDev d, const int*
   const int w = slot_world(order, first, count, d.n_worlds);
   if (w < 0) return;
   if (d.world[w].nb > kMaxB) return;
-  const SorSmem S = carve_sor(smem_raw + (size_t)(threadIdx.x >> 5) * kSorSmemPerWarp);
-  world_solve(d, w, S, lane, opt);
+  world_solve(d, w, smem_raw + (size_t)(threadIdx.x >> 5) * kFwdSmemPerWarp, lane, opt);
 }
 
 __global__ void __launch_bounds__(128) world_exact_kernel(BatchDev d, ExactDev X, const int* order, int first,
@@ -201,6 +200,8 @@ struct odegpuBatch {
   int n_ctrl_steps = 0;
   DBuf<DevContact> contacts;
   DBuf<float> rows;
+  DBuf<float4> sweep;                // forward sweep buffers (sor_fwd.cuh)
+  DBuf<unsigned char> fwd_scratch;
   DBuf<int> jlist, adj, adj_start, island_jstart, island_rstart, jrow, jm;
   DBuf<float> state_scratch;
   DBuf<odegpuRay> ray_in;          // odegpuBatchRayCast staging, grown on demand
@@ -250,7 +251,8 @@ struct odegpuBatch {
     d.body_force = n_ctrl_steps > 0 ? body_force.p : nullptr;
     d.joint_stop = n_ctrl_steps > 0 ? joint_stop.p : nullptr;
     d.step_counter_base = 0;
-    d.contacts = contacts.p; d.rows = rows.p; d.jlist = jlist.p; d.adj = adj.p;
+    d.contacts = contacts.p; d.rows = rows.p; d.sweep = sweep.p; d.fwd_scratch = fwd_scratch.p;
+    d.jlist = jlist.p; d.adj = adj.p;
     d.adj_start = adj_start.p; d.island_jstart = island_jstart.p; d.island_rstart = island_rstart.p;
     d.jrow = jrow.p; d.jm = jm.p;
     return d;
@@ -505,7 +507,7 @@ struct odegpuBatch {
           d, ord, first, count, step_counter + s, opt);
       mark(tm);
       apply_carveout(2);
-      world_solve_kernel<<<(count + w[2] - 1) / w[2], w[2] * 32, (size_t)w[2] * kSorSmemPerWarp, stream>>>(
+      world_solve_kernel<<<(count + w[2] - 1) / w[2], w[2] * 32, (size_t)w[2] * kFwdSmemPerWarp, stream>>>(
           d, ord, first, count, opt);
       mark(tm);
       launches += 3;
@@ -527,7 +529,7 @@ static int configure_kernels() {
                            (int)(kMaxWpb[1] * kSmemPerWarp)) != cudaSuccess)
     return -1;
   if (cudaFuncSetAttribute(world_solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)(kMaxWpb[2] * kSorSmemPerWarp)) != cudaSuccess)
+                           (int)(kMaxWpb[2] * kFwdSmemPerWarp)) != cudaSuccess)
     return -1;
   if (cudaFuncSetAttribute(adjoint_step_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)(kMaxWpb[3] * kAdjSmemPerWarp)) != cudaSuccess)
@@ -835,6 +837,7 @@ int odegpuBatchCreate(const odegpuScene* sc, const odegpuBatchConfig* cfg, odegp
   std::vector<int> padj_start((size_t)NB + W);
   std::vector<int> padj;
   long long contact_off = 0, row_off = 0;
+  int n_fwd_scratch = 0;
   for (int w = 0; w < W; ++w) {
     const odegpuWorldParams& P = sc->world[w];
     WorldDesc& D = wd[w];
@@ -870,6 +873,7 @@ int odegpuBatchCreate(const odegpuScene* sc, const odegpuBatchConfig* cfg, odegp
                       : std::min(ODEGPU_MAX_ROWS_PER_WORLD, 3 * D.contact_cap + 6 * D.njp);
     if (large) B->lw = new LargeWorld();
     row_off += D.row_cap;
+    D.fwd_scratch = (!large && D.row_cap > kFwdRows) ? n_fwd_scratch++ : -1;
     D.max_contacts = P.max_contacts;
     D.iterations = P.iterations;
     for (int k = 0; k < 3; ++k) D.gravity[k] = (float)P.gravity[k];
@@ -970,6 +974,8 @@ int odegpuBatchCreate(const odegpuScene* sc, const odegpuBatchConfig* cfg, odegp
   rc = rc ? rc : B->padj.upload(padj);
   rc = rc ? rc : B->contacts.alloc(contact_off);
   rc = rc ? rc : B->rows.alloc((size_t)row_off * kRowWords);
+  rc = rc ? rc : B->sweep.alloc(((size_t)row_off + 32 * (size_t)W) * 8);
+  rc = rc ? rc : B->fwd_scratch.alloc((size_t)std::max(1, n_fwd_scratch) * kFwdScratchPerWorld);
   rc = rc ? rc : B->jlist.alloc(jl_total);
   rc = rc ? rc : B->jrow.alloc(jl_total);
   rc = rc ? rc : B->jm.alloc(jl_total);
@@ -1670,6 +1676,7 @@ int ctx_step(WorldCtx* c, HostWorld& hw) {
   WorldDesc D = hw.desc;
   D.body_off = D.geom_off = D.joint_off = D.contact_off = D.row_off = D.padj_off = 0;
   D.ng = 0;
+  D.fwd_scratch = D.row_cap > kFwdRows ? 0 : -1;
   const size_t jl = (size_t)D.njp + D.contact_cap;
   std::vector<WorldDesc> wd(1, D);
   int rc = 0;
@@ -1697,6 +1704,8 @@ int ctx_step(WorldCtx* c, HostWorld& hw) {
   rc = rc ? rc : put(B.padj_start, hw.padj_start, s);
   rc = rc ? rc : put(B.padj, hw.padj, s);
   rc = rc ? rc : grow(B.rows, (size_t)D.row_cap * kRowWords);
+  rc = rc ? rc : grow(B.sweep, ((size_t)D.row_cap + 32) * 8);
+  if (D.fwd_scratch >= 0) rc = rc ? rc : grow(B.fwd_scratch, (size_t)kFwdScratchPerWorld);
   rc = rc ? rc : grow(B.jlist, jl);
   rc = rc ? rc : grow(B.jrow, jl);
   rc = rc ? rc : grow(B.jm, jl);

@@ -102,6 +102,8 @@ struct WorldDesc {
   int contact_off, contact_cap;
   int row_off, row_cap;
   int padj_off;                 // persistent adjacency (CSR) offset
+  int fwd_scratch;              // slot of the forward sweep's global scratch (a row capacity
+                                // above what the warp's shared memory holds), or -1
   int max_contacts;
   int iterations;
   float gravity[3], erp, cfm, sor_w, max_vel, min_depth, dt;
@@ -150,6 +152,9 @@ struct BatchDev {
   // per-step scratch (capacity-sized per world)
   DevContact* contacts;                // [contact_cap_total]
   float* rows;                         // [row_cap_total][32]
+  float4* sweep;                       // per world (row_cap + 32) x 8 float4: the rows of the
+                                       // current reshuffle round in execution order, quad-major
+  unsigned char* fwd_scratch;          // row-indexed SOR arrays of worlds with a large row capacity
   int* jlist;                          // [njp + contact_cap per world] island order
   int* adj;                            // [2 * (njp + contact_cap) per world]
   int* adj_start;                      // [nb_total + n_worlds]

@@ -2,6 +2,7 @@
 #pragma once
 #include "world_step.cuh"
 #include "sor.cuh"
+#include "sor_fwd.cuh"
 
 namespace og {
 
@@ -607,19 +608,27 @@ OG_D void world_setup(const BatchDev& d, int w, int step, const WarpSmem& S, int
   __syncwarp();
 }
 
-// Solve kernel body: phase 6 (SOR) and phase 7 (integration).
-OG_D void world_solve(const BatchDev& d, int w, const SorSmem& S, int lane, const StepOptions& opt) {
+// Solve kernel body: phase 6 (SOR) and phase 7 (integration). smem: the
+// warp's kFwdSmemPerWarp bytes of shared memory.
+OG_D void world_solve(const BatchDev& d, int w, unsigned char* smem, int lane, const StepOptions& opt) {
   const WorldDesc D = d.world[w];
   const int M = d.nrows[w];
   const int nisl = d.nislands[w];
   unsigned seed = d.seed[w];
-  const bool have_rows = M > 0;
+  unsigned char* scratch =
+      D.fwd_scratch >= 0 ? d.fwd_scratch + (size_t)D.fwd_scratch * kFwdScratchPerWorld : nullptr;
+  const FwdSmem S = carve_fwd(smem, M, scratch);
+  const bool have_rows = M > 0 && M <= S.cap;
+  if (M > S.cap) {
+    if (lane == 0) atomicOr(&d.status[w], ST_ROW_OVERFLOW);
+    for (int i = lane; i < (kMaxB + 1) * 6; i += 32) S.fc[i] = 0.f;
+    __syncwarp();
+  }
   if (have_rows) {
     const float* rows = d.rows + (size_t)D.row_off * kRowWords;
     const int* rstart = d.island_rstart + D.body_off + w;
-    // rows of island i start at rstart[i] (world row index); shift so the
-    // row store pointer can be used with world-local row indices
-    seed = sor_world(rows, rstart, D.nb, M, nisl, D.iterations, seed, S, lane);
+    float4* sweep = d.sweep + (size_t)(D.row_off + 32 * w) * 8;
+    seed = fwd_sor_world(rows, rstart, D.nb, M, nisl, D.iterations, seed, S, lane, sweep, D.row_cap + 32);
     __syncwarp();
     if (opt.dbg_lambda)
       for (int r = lane; r < M; r += 32) opt.dbg_lambda[D.row_off + r] = S.lambda[r];
