@@ -53,6 +53,7 @@ constexpr int kSmemPerWarp = align16(kMaxB * 6 * 4 + (kMaxB + 1) * 4 + (kMaxB + 
                                      kMaxR * 2 + kMaxR * 2 + kMaxB * 2 + kMaxB + kMaxR + 32);
 constexpr int kCollideSmemPerWarp = align16(kMaxPairs * 2 + 16);
 static_assert(kSmemPerWarp % 16 == 0 && kCollideSmemPerWarp % 16 == 0, "per-warp slices must stay aligned");
+static_assert(kMaxB * 6 * sizeof(float) >= 6 * kMaxB * sizeof(int), "the island phase borrows the tmp1 area");
 
 OG_D WarpSmem carve_smem(unsigned char* base) {
   WarpSmem s;
@@ -246,15 +247,36 @@ OG_D void joint_bodies(const BatchDev& d, const WorldDesc& D, int ord, int& b1, 
   }
 }
 
-// Phase 3: adjacency in ODE list order + DFS islands (util.cpp:384-521), all
-// in shared memory. Body lists hold contacts newest first, then persistent
-// joints newest first (nc = 0 when the host supplied complete lists in padj).
-// Writes jlist (joint ordinals in island order; bit 15 marks an island's first
-// joint) and island_jstart; returns the number of joints placed.
+// Phase 3: adjacency in ODE list order + islands in ODE's DFS order
+// (util.cpp:384-521), all in shared memory. Body lists hold contacts newest
+// first, then persistent joints newest first (nc = 0 when the host supplied
+// complete lists in padj). Writes jlist (joint ordinals in island order; bit
+// 15 marks an island's first joint) and island_jstart; returns the number of
+// joints placed.
+//
+// The reference walks the bodies from the last one down and runs a
+// depth-first search from every body not yet reached; the body that starts an
+// island is therefore the largest of its connected component, islands come in
+// decreasing order of that body, and an island's joints come in the order its
+// search first meets them. Here the components are labelled first, lanes in
+// parallel (every body takes the largest label among its neighbours, with
+// pointer jumping, until nothing changes), which gives every island's start
+// body, joint count and place in jlist; then each island's search runs on a
+// lane of its own, in the reference's order, with a slice of the stack sized
+// by its body count. Islands are disjoint, so the lanes never touch the same
+// body or joint.
 OG_D int phase_islands(const BatchDev& d, const WorldDesc& D, int w, int nc, int nj_all,
                        const WarpSmem& S, int lane, int* n_isl) {
   const int nb = D.nb;
   const int* pstart = d.padj_start + D.body_off + w;
+  const unsigned below = (1u << lane) - 1u;
+  // per-body scratch in the (not yet used) tmp1 area: 6 x kMaxB ints
+  int* lab = reinterpret_cast<int*>(S.fc);   // component label: its largest body
+  int* jcnt = lab + kMaxB;                   // joints of the component (by label)
+  int* bcnt = jcnt + kMaxB;                  // bodies of the component (by label)
+  int* jst = bcnt + kMaxB;                   // first jlist slot of the island (by start body)
+  int* sst = jst + kMaxB;                    // first stack slot of the island (by start body)
+  int* iroot = sst + kMaxB;                  // start body of island i, in island order
   // bodies of every joint ordinal
   for (int j = lane; j < nj_all; j += 32) {
     int b1, b2;
@@ -263,7 +285,10 @@ OG_D int phase_islands(const BatchDev& d, const WorldDesc& D, int w, int nc, int
     S.jb2[j] = (int8_t)b2;
     S.jtag[j] = 0;
   }
-  for (int b = lane; b < nb; b += 32) { S.cnt[b] = 0; S.tag[b] = 0; }
+  for (int b = lane; b < nb; b += 32) {
+    S.cnt[b] = 0; S.tag[b] = 0; S.stack[b] = 0;
+    lab[b] = b; jcnt[b] = 0; bcnt[b] = 0;
+  }
   __syncwarp();
   for (int c = lane; c < nc; c += 32) {
     atomicAdd(&S.cnt[S.jb1[D.njp + c]], 1);
@@ -282,47 +307,101 @@ OG_D int phase_islands(const BatchDev& d, const WorldDesc& D, int w, int nc, int
     if (lane == 0) S.adj_start[nb] = (uint16_t)carry;
   }
   __syncwarp();
-  // fill: each lane owns bodies b = lane (mod 32) and walks the contacts
-  // newest first, then copies its persistent list
+  // fill, contacts newest first: sixteen contacts per window, a contact's two
+  // bodies on two lanes; an entry's place in its body's list is the body's
+  // cursor (S.stack) plus the number of earlier entries in the window on the
+  // same body (__match_any_sync)
+  for (int base = 0; base < nc; base += 16) {
+    const int ci = base + (lane >> 1);
+    const int c = nc - 1 - ci;
+    int body = -1;
+    if (ci < nc) body = (lane & 1) ? S.jb2[D.njp + c] : S.jb1[D.njp + c];
+    const bool valid = body >= 0;
+    const unsigned mask = __match_any_sync(kFull, valid ? body : -1 - lane);
+    const int rank = __popc(mask & below);
+    if (valid) S.adj[S.adj_start[body] + S.stack[body] + rank] = (uint16_t)(D.njp + c);
+    __syncwarp();
+    if (valid && (mask >> lane) == 1u) S.stack[body] = (int16_t)(S.stack[body] + rank + 1);
+    __syncwarp();
+  }
+  // then each body's persistent joints
   for (int b = lane; b < nb; b += 32) {
-    int wp = S.adj_start[b];
-    for (int c = nc - 1; c >= 0; --c)
-      if (S.jb1[D.njp + c] == b || S.jb2[D.njp + c] == b) S.adj[wp++] = (uint16_t)(D.njp + c);
+    int wp = S.adj_start[b] + S.cnt[b];
     for (int k = pstart[b]; k < pstart[b + 1]; ++k) S.adj[wp++] = (uint16_t)d.padj[k];
   }
-  __syncwarp();
-  int jcount = 0, nisl = 0;
-  if (lane == 0) {
-    int* istart = d.island_jstart + D.body_off + w;
-    for (int bb = nb - 1; bb >= 0; --bb) {
-      if (S.tag[bb]) continue;
-      S.tag[bb] = 1;
-      const int jstart = jcount;
-      int sp = 0, b = bb;
-      for (;;) {
-        const int e = S.adj_start[b + 1];
-        for (int k = S.adj_start[b]; k < e; ++k) {
-          const int j = S.adj[k];
-          if (S.jtag[j]) continue;
-          S.jtag[j] = 1;
-          S.jlist[jcount] = (uint16_t)(j | (jcount == jstart ? 0x8000 : 0));
-          ++jcount;
-          const int b1 = S.jb1[j], b2 = S.jb2[j];
-          const int other = (b1 == b) ? b2 : b1;
-          if (other >= 0 && !S.tag[other]) {
-            S.tag[other] = 1;
-            S.stack[sp++] = (int16_t)other;
-          }
-        }
-        if (sp == 0) break;
-        b = S.stack[--sp];
+  // components: largest label along every joint, pointer jumping, until stable
+  for (;;) {
+    bool changed = false;
+    for (int j = lane; j < nj_all; j += 32) {
+      const int b1 = S.jb1[j], b2 = S.jb2[j];
+      if (b1 < 0 || b2 < 0) continue;
+      const int l1 = lab[b1], l2 = lab[b2];
+      if (l1 != l2) {
+        const int m = max(l1, l2);
+        atomicMax(&lab[b1], m);
+        atomicMax(&lab[b2], m);
+        changed = true;
       }
-      if (jcount > jstart) istart[nisl++] = jstart;
     }
-    istart[nisl] = jcount;
+    __syncwarp();
+    for (int b = lane; b < nb; b += 32) {
+      const int l = lab[b];
+      const int ll = lab[l];
+      if (ll > l) atomicMax(&lab[b], ll);
+    }
+    __syncwarp();
+    if (!__any_sync(kFull, changed)) break;
   }
-  jcount = __shfl_sync(kFull, jcount, 0);
-  nisl = __shfl_sync(kFull, nisl, 0);
+  for (int b = lane; b < nb; b += 32) atomicAdd(&bcnt[lab[b]], 1);
+  for (int j = lane; j < nj_all; j += 32)
+    if (S.jb1[j] >= 0) atomicAdd(&jcnt[lab[S.jb1[j]]], 1);
+  __syncwarp();
+  // islands: components with joints, by decreasing start body
+  int jcount = 0, nisl = 0, scarry = 0;
+  for (int base = 0; base < nb; base += 32) {
+    const int b = nb - 1 - (base + lane);
+    const bool isl = b >= 0 && lab[b] == b && jcnt[b] > 0;
+    const int jn = isl ? jcnt[b] : 0, bn = isl ? bcnt[b] : 0;
+    const int ji = warp_incl_scan(jn, lane), bi = warp_incl_scan(bn, lane);
+    const unsigned bal = __ballot_sync(kFull, isl);
+    if (isl) {
+      jst[b] = jcount + ji - jn;
+      sst[b] = scarry + bi - bn;
+      iroot[nisl + __popc(bal & below)] = b;
+    }
+    jcount += __shfl_sync(kFull, ji, 31);
+    scarry += __shfl_sync(kFull, bi, 31);
+    nisl += __popc(bal);
+  }
+  __syncwarp();
+  // every island's depth-first search on a lane of its own
+  int* istart = d.island_jstart + D.body_off + w;
+  for (int i = lane; i < nisl; i += 32) {
+    const int root = iroot[i];
+    const int jstart = jst[root], sbase = sst[root];
+    int jc = jstart, sp = 0, b = root;
+    S.tag[root] = 1;
+    for (;;) {
+      const int e = S.adj_start[b + 1];
+      for (int k = S.adj_start[b]; k < e; ++k) {
+        const int j = S.adj[k];
+        if (S.jtag[j]) continue;
+        S.jtag[j] = 1;
+        S.jlist[jc] = (uint16_t)(j | (jc == jstart ? 0x8000 : 0));
+        ++jc;
+        const int b1 = S.jb1[j], b2 = S.jb2[j];
+        const int other = (b1 == b) ? b2 : b1;
+        if (other >= 0 && !S.tag[other]) {
+          S.tag[other] = 1;
+          S.stack[sbase + sp++] = (int16_t)other;
+        }
+      }
+      if (sp == 0) break;
+      b = S.stack[sbase + --sp];
+    }
+    istart[i] = jstart;
+  }
+  if (lane == 0) istart[nisl] = jcount;
   // publish the joint order for the row phase
   const int jl_off = D.joint_off + D.contact_off;
   __syncwarp();

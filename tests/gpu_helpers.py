@@ -93,13 +93,16 @@ def pair_diff(scene, B, w, step, x_world, seed):
     return {k: (gc.get(k, 0), oc.get(k, 0)) for k in set(oc) | set(gc) if gc.get(k, 0) != oc.get(k, 0)}
 
 
-def rollout_parity(scene, n_steps, make_batch, state_steps=(), tol=None, rtol=1e-4, max_ill_frac=1e-3):
+def rollout_parity(scene, n_steps, make_batch, state_steps=(), tol=None, rtol=1e-4, max_ill_frac=1e-3,
+                   accept=None):
     """Every step of the oracle's own FP64 rollout of `scene` is rounded to
     FP32 (what the GPU stores) and stepped once by the GPU and once by the
     oracle from that identical input. Per world and step, contacts, rows,
     islands with rows and the dRand seed after the step must be equal; a
     difference is accepted only where the oracle's own counts flip under
-    FP32-sized perturbations of the input (ill_conditioned), and such cases
+    FP32-sized perturbations of the input (ill_conditioned) or where
+    accept(step, world, gpu_counts) vouches for the GPU's counts (a recorded
+    answer of the reference's own FP32 build at that input), and such cases
     stay below max_ill_frac of the world-steps. At the steps in state_steps
     the GPU's state after the step must agree with the oracle's within
     tol + rtol * |oracle| (pos, q, lvel, avel) in every world whose integer
@@ -125,6 +128,8 @@ def rollout_parity(scene, n_steps, make_batch, state_steps=(), tol=None, rtol=1e
             lvl = ill_conditioned(scene, int(w), k, xw, int(seeds[w]), co[w, 0], seed_rng=k * nw + int(w))
             if lvl:
                 ill.append((k, int(w), lvl))
+            elif accept is not None and accept(k, int(w), g_counts[w]):
+                ill.append((k, int(w), "reference FP32 build"))
             else:
                 bad.append((k, int(w), g_counts[w].tolist(), co[w, 0].tolist(),
                             pair_diff(scene, B, int(w), k, xw, int(seeds[w]))))
@@ -140,6 +145,6 @@ def rollout_parity(scene, n_steps, make_batch, state_steps=(), tol=None, rtol=1e
     B.close()
     assert not bad, bad[:8]
     assert len(ill) <= max_ill_frac * n_steps * nw, (len(ill), ill[:8])
-    levels = {u: sum(1 for c in ill if c[2] == u) for u in ILL_ULPS}
+    levels = {u: sum(1 for c in ill if c[2] == u) for u in ILL_ULPS + ("reference FP32 build",)}
     return dict(world_steps=n_steps * nw, ill_conditioned=len(ill), ill_by_ulps=levels,
                 worst_beyond_rtol=worst.tolist(), state_worlds_checked=checked)

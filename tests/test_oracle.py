@@ -221,3 +221,26 @@ def test_multithreaded_baseline_is_deterministic():
     ref = np.concatenate([O.run_world(O.oracle().oracle_run_world, sc, w, 15)["state"][-1]
                           for w in range(sc.n_worlds)])
     assert np.array_equal(out, ref)
+
+
+def test_vehicle_heightfield_cases_are_reference_precision_splits():
+    """tests/golden/vehicle_hf_cases.npz: at each recorded world-step of the
+    full-size vehicle rollout (FP32-rounded oracle state), the oracle's FP64
+    contact count is the stored dDOUBLE one, and, where the reference is
+    built here, its dSINGLE and dDOUBLE builds give the stored per-geom
+    heightfield contact counts, which differ."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("mk_hf_cases", os.path.join(GOLDEN, "make_vehicle_hf_cases.py"))
+    mk = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mk)
+    from odegpu import scene as S
+    g = np.load(os.path.join(GOLDEN, "vehicle_hf_cases.npz"))
+    sc = S.vehicles(n_worlds=2048, steps=300)
+    for i, (k, w) in enumerate(zip(g["step"], g["world"])):
+        x32, n = mk.case_inputs(sc, int(k), int(w))
+        assert n == g["contacts_double"][i], (k, w, n)
+        if O.ref_available("d") and O.ref_available("s"):
+            d = mk.hf_counts(sc, int(w), x32, "d")
+            s_ = mk.hf_counts(sc, int(w), x32, "s")
+            assert np.array_equal(d, g["hf_double"][i]) and np.array_equal(s_, g["hf_single"][i]), (k, w)
+            assert not np.array_equal(d, s_)
