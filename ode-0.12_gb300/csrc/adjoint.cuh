@@ -26,9 +26,11 @@ namespace og {
 // Status bits of the adjoint (per world): a part of the step whose
 // derivative is not modelled was met (the gradient leaves it out).
 enum {
-  ADJ_UNSUPPORTED_JOINT = 1,     // a hinge limit row, a bouncing hinge2 limit, hinge2 without body 2,
+  ADJ_UNSUPPORTED_JOINT = 1,     // a bouncing or motor-driven limit row, hinge2 without body 2,
                                  // slider, universal and fixed joints
-  ADJ_UNSUPPORTED_CONTACT = 2,   // body-body contact, capsule vertex contact, geom under a field, bounce
+  ADJ_UNSUPPORTED_CONTACT = 2,   // capsule vertex contact, geom under a field, bounce, fixed friction
+                                 // direction, a body-body contact whose collider case switches
+                                 // within the difference step
   ADJ_TOO_LARGE = 4
 };
 
@@ -255,6 +257,52 @@ OG_D int vjp_hinge2(const BatchDev& d, const WorldDesc& D, const AdjDev& a, cons
   return flags;
 }
 
+// d/d(b, c) of a = f(b, c) for the bilinear quaternion products (qmul1:
+// b* c, qmul2: b c*, qmul3: b* c*), given d/da: each partial is the product
+// with a unit quaternion in that slot.
+template <void (*F)(float*, const float*, const float*)>
+OG_D void vjp_qmul(const float* qb_, const float* qc_, const float* ab, float* bb, float* cb) {
+  for (int i = 0; i < 4; ++i) {
+    float e[4] = {0.f, 0.f, 0.f, 0.f}, t[4];
+    e[i] = 1.f;
+    if (bb) { F(t, e, qc_); bb[i] += ab[0] * t[0] + ab[1] * t[1] + ab[2] * t[2] + ab[3] * t[3]; }
+    if (cb) { F(t, qb_, e); cb[i] += ab[0] * t[0] + ab[1] * t[1] + ab[2] * t[2] + ab[3] * t[3]; }
+  }
+}
+
+// d/dq1, d/dq2 of the hinge angle (getHingeAngle, ode/src/joints/joint.cpp:
+// 381-450, as hinge_angle computes it from the bodies' quaternions) given its
+// derivative angb. The angle is -2 atan2(|v|, +-w) of the relative rotation
+// qrel = (q1* q2) qrel0* (w, v), the sign of w that of v . axis.
+OG_D void vjp_hinge_angle(const BodyRef& B1, const BodyRef* B2, const DevJoint& J, float angb, float* q1b,
+                          float* q2b) {
+  float qq[4], qrel[4];
+  if (B2) {
+    qmul1(qq, B1.q, B2->q);
+    qmul2(qrel, qq, J.qrel);
+  } else {
+    qmul3(qrel, B1.q, J.qrel);
+  }
+  const float* v = qrel + 1;
+  const float sn = sqrtf(dot3(v, v));
+  const float sgn = dot3(v, J.axis1) >= 0.f ? 1.f : -1.f;
+  const float c = sgn * qrel[0];
+  const float den = sn * sn + c * c;
+  if (!(sn > 0.f) || !(den > 0.f)) return;
+  const float thb = -angb;                          // angle = -theta
+  float qrelb[4];
+  qrelb[0] = thb * (-2.f * sn / den) * sgn;
+  const float vs = thb * (2.f * c / den) / sn;
+  qrelb[1] = vs * v[0]; qrelb[2] = vs * v[1]; qrelb[3] = vs * v[2];
+  if (B2) {
+    float qqb[4] = {0.f, 0.f, 0.f, 0.f};
+    vjp_qmul<qmul2>(qq, J.qrel, qrelb, qqb, nullptr);
+    vjp_qmul<qmul1>(B1.q, B2->q, qqb, q1b, q2b);
+  } else {
+    vjp_qmul<qmul3>(B1.q, J.qrel, qrelb, q1b, nullptr);
+  }
+}
+
 OG_D int vjp_joint(const BatchDev& d, const WorldDesc& D, const AdjDev& a, int w, int ord, int r0, int m,
                    float k, const float* stops) {
   const DevJoint& J = d.joints[D.joint_off + ord];
@@ -326,9 +374,27 @@ OG_D int vjp_joint(const BatchDev& d, const WorldDesc& D, const AdjDev& a, int w
     if (m > 5) {
       const float* t5 = RT0 + 5 * kAdjRow;
       for (int i = 0; i < 3; ++i) ax1b[i] += t5[3 + i] - (g2 >= 0 ? t5[9 + i] : 0.f);
-      // a limit row's rhs depends on the hinge angle (not modelled); a motor
-      // row's rhs is the constant target velocity
-      if (limot_tested(J.lm1)) flags |= ADJ_UNSUPPORTED_JOINT;
+      // a motor row's rhs is the constant target velocity; a limit row's is
+      // -fps stop_erp (angle - stop) (joint.cpp:556-733), through the hinge
+      // angle into both quaternions
+      const DevLimot lm1 = step_limot1(J, stops, ord);
+      BodyRef B1, B2;
+      load_body_ref(d, g1, B1);
+      if (g2 >= 0) load_body_ref(d, g2, B2);
+      int limit = 0;
+      float err = 0.f;
+      if (limot_tested(lm1)) limot_test(lm1, hinge_angle(B1, g2 >= 0 ? &B2 : nullptr, J), limit, err);
+      if (limit) {
+        // a bounce adds the relative velocity; a powered motor at the limit
+        // adds torques to the bodies from inside getInfo2
+        if (lm1.lostop != lm1.histop && (lm1.bounce > 0.f || lm1.fmax > 0.f)) flags |= ADJ_UNSUPPORTED_JOINT;
+        float q1b[4] = {0.f, 0.f, 0.f, 0.f}, q2b[4] = {0.f, 0.f, 0.f, 0.f};
+        vjp_hinge_angle(B1, g2 >= 0 ? &B2 : nullptr, J, -(lm1.stop_erp / D.dt) * t5[kRC], q1b, q2b);
+        for (int i = 0; i < 4; ++i) {
+          atomicAdd(xb1 + 3 + i, q1b[i]);
+          if (g2 >= 0) atomicAdd(xb2 + 3 + i, q2b[i]);
+        }
+      }
     }
     for (int i = 0; i < 3; ++i)
       for (int j = 0; j < 3; ++j) {
@@ -339,6 +405,152 @@ OG_D int vjp_joint(const BatchDev& d, const WorldDesc& D, const AdjDev& a, int w
   return flags;
 }
 
+// Contact between two bodies (dCollide(g_i, g_k), body 1 = body(g_i)): the
+// rows (contact.cpp:75-256: J1l = n, J1a = (pos - x1) x n, J2l = -n,
+// J2a = -(pos - x2) x n, the friction rows along dPlaneSpace(n), the normal
+// row's rhs k depth) are differentiated analytically with respect to the
+// contact point, normal and depth and the two body positions; the contact
+// point, normal and depth with respect to both bodies' positions and
+// rotation matrices are the collider's Jacobian, taken by central
+// differences of the same FP32 collider along the seven directions per body
+// that a change of position and quaternion can take (three translations,
+// three rotations, the scale of R). The pair's contacts come back in the same order as long as no
+// difference step crosses one of the collider's case boundaries (axis choice,
+// clipping, culling, a shallow point's depth test); a step that changes the
+// contact count or moves the contact by far more than the step is retried at
+// a quarter of its size, three times (down to 7.8e-6), and marks the contact
+// unsupported when all four fail.
+constexpr float kPairStep = 5e-4f;
+__device__ __noinline__ int vjp_contact_pair(const BatchDev& d, const WorldDesc& D, const AdjDev& a, int ci, int r0, int m,
+                          float erp_world) {
+  const DevContact& ct = d.contacts[D.contact_off + ci];
+  const DevSurface& S = d.surfaces[ct.surface];
+  if (ct.geoms < 0 || ct.reverse || (S.mode & (SURF_BOUNCE | SURF_FDIR1)) || m == 2) return ADJ_UNSUPPORTED_CONTACT;
+  const int pair = ct.geoms & 0xffff;
+  const int gi = pair & 0xff, gk = (pair >> 8) & 0xff;
+  if (d.gtype[D.geom_off + gi] == G_HEIGHTFIELD || d.gtype[D.geom_off + gk] == G_HEIGHTFIELD)
+    return ADJ_UNSUPPORTED_CONTACT;
+  if (d.gbody[D.geom_off + gi] != ct.b1 || d.gbody[D.geom_off + gk] != ct.b2) return ADJ_UNSUPPORTED_CONTACT;
+  // this contact's place among its pair's (they are consecutive)
+  int idx = 0;
+  while (ci - idx - 1 >= 0 && (d.contacts[D.contact_off + ci - idx - 1].geoms & 0xffff) == pair) ++idx;
+  const int g1 = D.body_off + ct.b1, g2 = D.body_off + ct.b2;
+  const float4 x14 = d.pos[g1], x24 = d.pos[g2];
+  const float x1[3] = {x14.x, x14.y, x14.z}, x2[3] = {x24.x, x24.y, x24.z};
+  const float* n = ct.normal;
+  float t1[3], t2[3];
+  plane_space(n, t1, t2);
+  const float* dirs[3] = {n, t1, t2};
+  const float c1[3] = {ct.pos[0] - x1[0], ct.pos[1] - x1[1], ct.pos[2] - x1[2]};
+  const float c2[3] = {ct.pos[0] - x2[0], ct.pos[1] - x2[1], ct.pos[2] - x2[2]};
+  const float* RT0 = a.row_tmp + (size_t)(D.row_off + r0) * kAdjRow;
+  float dirb[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+  float c1b[3] = {0.f, 0.f, 0.f}, c2b[3] = {0.f, 0.f, 0.f};
+  for (int r = 0; r < m; ++r) {
+    const float* t = RT0 + r * kAdjRow;
+    float u[3];
+    for (int i = 0; i < 3; ++i) dirb[r][i] += t[i] - t[6 + i];
+    cross3(u, t + 3, c1);                    // J1a = c1 x dir
+    for (int i = 0; i < 3; ++i) dirb[r][i] += u[i];
+    cross3(u, dirs[r], t + 3);
+    for (int i = 0; i < 3; ++i) c1b[i] += u[i];
+    cross3(u, t + 9, c2);                    // J2a = -(c2 x dir)
+    for (int i = 0; i < 3; ++i) dirb[r][i] -= u[i];
+    cross3(u, dirs[r], t + 9);
+    for (int i = 0; i < 3; ++i) c2b[i] -= u[i];
+  }
+  float nb[3] = {dirb[0][0], dirb[0][1], dirb[0][2]};
+  if (m == 3) vjp_plane_space(n, dirb[1], dirb[2], nb);
+  float erp = erp_world;
+  if (S.mode & SURF_SOFT_ERP) erp = S.soft_erp;
+  const float kk = (1.0f / D.dt) * erp;
+  const float dep = ct.depth - D.min_depth;
+  const float motionN = (S.mode & SURF_MOTIONN) ? S.motionN : 0.f;
+  const float depth_b = (dep > 0.f && kk * dep + motionN < D.max_vel) ? RT0[kRC] * kk : 0.f;
+  const float posb[3] = {c1b[0] + c2b[0], c1b[1] + c2b[1], c1b[2] + c2b[2]};
+  float* xb1 = a.state_bar + (size_t)g1 * 13;
+  float* xb2 = a.state_bar + (size_t)g2 * 13;
+  for (int i = 0; i < 3; ++i) { atomicAdd(xb1 + i, -c1b[i]); atomicAdd(xb2 + i, -c2b[i]); }
+  // the collider's Jacobian by central differences, evaluated with body 1
+  // at the origin (the colliders move with a common translation, and the
+  // smaller coordinates carry less FP32 rounding); a step that changes the
+  // contact count or jumps the contact is retried at a quarter of its size
+  GeomView v0[2];
+  geom_view(d, D, gi, v0[0]);
+  geom_view(d, D, gk, v0[1]);
+  for (int i = 0; i < 3; ++i) { v0[1].pos[i] -= v0[0].pos[i]; v0[0].pos[i] = 0.f; }
+  const float pos_l[3] = {ct.pos[0] - x1[0], ct.pos[1] - x1[1], ct.pos[2] - x1[2]};
+  Contact cc[8];
+  const int n0 = collide_primitive(v0[0], v0[1], (unsigned)D.max_contacts, cc);
+  if (n0 <= idx) return ADJ_UNSUPPORTED_CONTACT;
+  float* Rb[2] = {a.body_tmp + (size_t)g1 * kAdjBody + kBR, a.body_tmp + (size_t)g2 * kAdjBody + kBR};
+  float* xb[2] = {xb1, xb2};
+  // per body: three translations, three small rotations about the world axes
+  // (R -> (I + d [e_k]x) R) and a scale (R -> (1 + d) R): the directions a
+  // change of the quaternion moves R in (dRfromQ of a non-unit q scales R)
+  float gdir[2][7];
+  for (int k = 0; k < 14; ++k) {
+    const int side = k / 7, e = k % 7;
+    float f[2][7];
+    float step = kPairStep;
+    bool ok = false;
+    for (int attempt = 0; attempt < 4 && !ok; ++attempt, step *= 0.25f) {
+      ok = true;
+      for (int sg = 0; sg < 2 && ok; ++sg) {
+        GeomView v[2] = {v0[0], v0[1]};
+        const float delta = sg ? -step : step;
+        float* R = v[side].R;
+        if (e < 3) {
+          v[side].pos[e] += delta;
+        } else if (e < 6) {
+          float w[3] = {0.f, 0.f, 0.f};
+          w[e - 3] = delta;
+          for (int j = 0; j < 3; ++j) {
+            const float col[3] = {R[j], R[4 + j], R[8 + j]};
+            float u[3];
+            cross3(u, w, col);
+            R[j] = col[0] + u[0]; R[4 + j] = col[1] + u[1]; R[8 + j] = col[2] + u[2];
+          }
+        } else {
+          for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) R[i * 4 + j] *= 1.f + delta;
+        }
+        const int nn = collide_primitive(v[0], v[1], (unsigned)D.max_contacts, cc);
+        if (nn != n0) { ok = false; break; }
+        for (int i = 0; i < 3; ++i) { f[sg][i] = cc[idx].pos[i]; f[sg][3 + i] = cc[idx].normal[i]; }
+        f[sg][6] = cc[idx].depth;
+        for (int i = 0; i < 3; ++i)
+          if (fabsf(f[sg][i] - pos_l[i]) > 50.f * step) ok = false;
+      }
+      if (ok) break;
+    }
+    if (!ok) return ADJ_UNSUPPORTED_CONTACT;
+    const float s2 = 0.5f / step;
+    float g = depth_b * (f[0][6] - f[1][6]) * s2;
+    for (int i = 0; i < 3; ++i) g += posb[i] * (f[0][i] - f[1][i]) * s2 + nb[i] * (f[0][3 + i] - f[1][3 + i]) * s2;
+    gdir[side][e] = g;
+  }
+  // back to d/dx and d/dR: d/dR = sum_k g_k / (2 s^2) [e_k]x R + g_scale / (3 s^2) R,
+  // s^2 = |R|^2 / 3 (the directions are orthogonal with these norms)
+  for (int side = 0; side < 2; ++side) {
+    const float* R = v0[side].R;
+    float n2 = 0.f;
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) n2 += R[i * 4 + j] * R[i * 4 + j];
+    if (!(n2 > 0.f)) return ADJ_UNSUPPORTED_CONTACT;
+    const float cr = 1.5f / n2, cs = gdir[side][6] / n2;
+    const float w[3] = {cr * gdir[side][3], cr * gdir[side][4], cr * gdir[side][5]};
+    for (int i = 0; i < 3; ++i) atomicAdd(xb[side] + i, gdir[side][i]);
+    for (int j = 0; j < 3; ++j) {
+      const float col[3] = {R[j], R[4 + j], R[8 + j]};
+      float u[3];
+      cross3(u, w, col);
+      for (int i = 0; i < 3; ++i) atomicAdd(Rb[side] + i * 3 + j, u[i] + cs * col[i]);
+    }
+  }
+  return 0;
+}
+
 // Derivative of a contact's rows with respect to the contact point and depth,
 // and of those (sphere / box / capsule against a plane) with respect to the
 // body's position and rotation.
@@ -346,7 +558,8 @@ OG_D int vjp_contact(const BatchDev& d, const WorldDesc& D, const AdjDev& a, int
                      float erp_world) {
   const DevContact& ct = d.contacts[D.contact_off + ci];
   const DevSurface& S = d.surfaces[ct.surface];
-  if (ct.geoms < 0 || ct.b2 >= 0) return ADJ_UNSUPPORTED_CONTACT;
+  if (ct.b2 >= 0) return vjp_contact_pair(d, D, a, ci, r0, m, erp_world);
+  if (ct.geoms < 0) return ADJ_UNSUPPORTED_CONTACT;
   const int gA = D.geom_off + (ct.geoms & 0xff), gB = D.geom_off + ((ct.geoms >> 8) & 0xff);
   const unsigned kind = ((unsigned)ct.geoms >> 16) & 3u;
   int gp, gs;

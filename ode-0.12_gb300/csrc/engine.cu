@@ -1363,6 +1363,11 @@ int odegpuBatchRolloutBackward(odegpuBatchID b, const float* grad_final, float* 
       adjoint_step_kernel<<<b->nblocks(b->n_worlds, 3), b->kwpb[3] * 32, b->kwpb[3] * (size_t)kAdjSmemPerWarp,
                             b->stream>>>(b->dev(), a, step);
       b->launches += 1;
+      const cudaError_t e = cudaGetLastError();
+      if (e != cudaSuccess) {
+        b->step_counter = saved_counter;
+        return fail(ODEGPU_E_CUDA, std::string("adjoint launch: ") + cudaGetErrorString(e));
+      }
     }
   }
   if (grad_init)

@@ -212,3 +212,132 @@ def test_adjoint_vehicles_on_heightfield():
     err, detail = _check_case(sc, 4, coef, n_vel=10, n_pos=0, n_tq=6, seed=9, q_dirs=0, eps=1e-6,
                               x_init=x_init, tq_col=1, tq_joints=[2, 3])
     assert err < TOL, (err, detail)
+
+
+def test_adjoint_hinge_limit_rows():
+    """Hinge chains with stops at [0.1, 0.6] rad; a hinge's angle is 0 at the
+    pose it is created in, so every joint starts 0.1 rad below its low stop,
+    at a limit: the limit row's rhs -fps stop_erp (angle - stop) follows the hinge
+    angle (getHingeAngle, ode/src/joints/joint.cpp:381-450), differentiated
+    through both bodies' quaternions. Three steps with the plane out of
+    reach; every world must be fully modelled."""
+    sc = S.hinge_chains(n_worlds=3, steps=6, plane_z=-100.0)
+    sc.joint_param[:, 0] = 0.1       # lostop
+    sc.joint_param[:, 1] = 0.6       # histop
+    # joints starting beyond a stop: their sixth row is a limit row
+    for w in range(sc.n_worlds):
+        j0, j1 = sc.world_joints(w)
+        assert O.tap_step(sc, w, 0)["total_rows"] > 5 * (j1 - j0)
+    err, detail = _check_case(sc, 3, _coef(sc, 11), n_vel=12, n_pos=4, n_tq=8, seed=11, q_dirs=2)
+    assert err < TOL, (err, detail)
+
+
+def _quat_mul(a, b):
+    w1, x1, y1, z1 = a
+    w2, x2, y2, z2 = b
+    return (w1 * w2 - x1 * x2 - y1 * y2 - z1 * z2, w1 * x2 + x1 * w2 + y1 * z2 - z1 * y2,
+            w1 * y2 - x1 * z2 + y1 * w2 + z1 * x2, w1 * z2 + x1 * y2 - y1 * x2 + z1 * w2)
+
+
+def _body_body_scene(top_tilt, top_yaw, spheres=True, top_box=True, lower_q=(1.0, 0.0, 0.0, 0.0)):
+    """A 0.4 x 0.3 x 0.2 m box turned top_yaw rad about z and tipped
+    top_tilt rad about its x axis, resting on one edge 1 mm deep in a
+    0.9 x 0.9 x 0.3 m box that sits on the plane z = 0 (the lower box's top
+    face against the tipped box's bottom face: two points; the yaw keeps the
+    resting edge off the lower box's edge directions, so no edge axis ties
+    with the face axis), and, with spheres, a 0.15 m sphere on the lower box
+    and a 0.1 m sphere on that sphere (sphere-box and sphere-sphere)."""
+    b = S.SceneBuilder()
+    s = S._std_surface(b, 0.5)
+    w = b.new_world(cfm=1e-5, seed=9)
+    b.add_geom(w, S.GEOM_PLANE, -1, (0, 0, 1, 0), s)
+    m0, I0 = S.box_mass(500.0, 0.9, 0.9, 0.3)
+    b0 = b.add_body(w, (0.0, 0.0, 0.1495), m0, I0, q=lower_q, lvel=(0.05, 0.0, 0.0))
+    b.add_geom(w, S.GEOM_BOX, b0, (0.9, 0.9, 0.3), s)
+    if top_box:
+        m1, I1 = S.box_mass(300.0, 0.4, 0.3, 0.2)
+        qz = (np.cos(top_yaw / 2), 0.0, 0.0, np.sin(top_yaw / 2))
+        qx = (np.cos(top_tilt / 2), np.sin(top_tilt / 2), 0.0, 0.0)
+        h = 0.5 * (0.3 * np.sin(top_tilt) + 0.2 * np.cos(top_tilt))
+        b1 = b.add_body(w, (0.1, 0.05, 0.299 + h), m1, I1, q=_quat_mul(qz, qx), lvel=(0.1, -0.05, 0.0),
+                        avel=(0.2, 0.0, 0.1))
+        b.add_geom(w, S.GEOM_BOX, b1, (0.4, 0.3, 0.2), s)
+    if spheres:
+        m2, I2 = S.sphere_mass(400.0, 0.15)
+        b2 = b.add_body(w, (-0.25, -0.25, 0.449), m2, I2, lvel=(0.0, 0.2, 0.0))
+        b.add_geom(w, S.GEOM_SPHERE, b2, (0.15,), s)
+        m3, I3 = S.sphere_mass(400.0, 0.1)
+        b3 = b.add_body(w, (-0.25, -0.24, 0.6985), m3, I3, avel=(0.5, 0.0, 0.0))
+        b.add_geom(w, S.GEOM_SPHERE, b3, (0.1,), s)
+    return b.build()
+
+
+def test_adjoint_sphere_body_contacts():
+    """Sphere-box and sphere-sphere contacts between dynamic bodies (a sphere
+    on a box on the plane, a sphere on that sphere): three steps against
+    FP64 central differences (step 1e-6)."""
+    sc = _body_body_scene(0.0, 0.0, top_box=False)
+    coef = _coef(sc, 14, cols=[0, 1, 2, 7, 8, 9, 10, 11, 12])
+    err, detail = _check_case(sc, 3, coef, n_vel=12, n_pos=6, n_tq=0, seed=14, q_dirs=2, eps=1e-6)
+    assert err < TOL, (err, detail)
+
+
+def test_adjoint_body_body_contacts():
+    """Contacts between two dynamic bodies (box-box, sphere-box and
+    sphere-sphere): the rows
+    are differentiated with respect to the contact point, normal and depth
+    and both bodies, the collider's geometry by central differences of the
+    FP32 collider. Two steps, FP64 central differences of the oracle (step
+    1e-6: stiff contacts), every world fully modelled."""
+    # the lower box starts tipped by a few milliradians (no orientation is
+    # exactly axis aligned, so no collider decision - which vertex of a box on
+    # the plane comes first, which of two parallel faces is the reference -
+    # hangs on the sign of an exact zero that a difference step would flip);
+    # the check runs steps 1-2, over which the contact sets do not change
+    sc = _body_body_scene(0.3, 0.4, lower_q=_quat_mul((np.cos(0.002), np.sin(0.002), 0.0, 0.0),
+                                                      (np.cos(0.003), 0.0, np.sin(0.003), 0.0)))
+    from gpu_helpers import oracle_states, stacked_state
+    runs = oracle_states(sc, 3)
+    x_init = stacked_state(runs, 1)
+    gb = sc.geom_body
+    for k in (1, 2):
+        c = runs[0]["contacts"][k][: runs[0]["ncontacts"][k]]
+        pairs = [(int(gb[int(x[7])]), int(gb[int(x[8])])) for x in c]
+        assert pairs.count((0, 1)) == 2 and (0, 2) in pairs and (2, 3) in pairs, (k, pairs)
+    coef = _coef(sc, 12, cols=[0, 1, 2, 7, 8, 9, 10, 11, 12])
+    err, detail = _check_case(sc, 2, coef, n_vel=12, n_pos=6, n_tq=0, seed=12, q_dirs=2, eps=1e-6, x_init=x_init)
+    assert err < TOL, (err, detail)
+
+
+def _link_contact_windows(sc, n_steps, max_windows):
+    """(world, step) of the hinge-chain workload where two links touch."""
+    out = []
+    gb = sc.geom_body
+    for w in range(sc.n_worlds):
+        r = O.run_world(O.oracle().oracle_run_world, sc, w, n_steps, max_rec=64)
+        g0 = sc.geom_off[w]
+        for k in range(n_steps):
+            c = r["contacts"][k][: r["ncontacts"][k]]
+            if any(gb[g0 + int(x[7])] >= 0 and gb[g0 + int(x[8])] >= 0 for x in c):
+                out.append((w, k, r["state"][k]))
+                break
+        if len(out) >= max_windows:
+            break
+    return out
+
+
+def test_adjoint_hinge_chains_configured_plane_link_contacts():
+    """The differentiable-batch workload as configured (plane at z = -2):
+    links of a chain touch each other (box-box contacts between two dynamic
+    bodies). Windows of two steps starting where such a contact is present,
+    from the oracle's state there: d/d(initial velocities) and d/d(torques)
+    against FP64 central differences, every world fully modelled."""
+    sc = S.hinge_chains(n_worlds=64, steps=100)
+    wins = _link_contact_windows(sc, 100, 4)
+    assert len(wins) >= 2
+    from odegpu.shard import slice_scene
+    for w, k, state in wins:
+        sub = slice_scene(sc, w, w + 1)
+        err, detail = _check_case(sub, 2, _coef(sub, 13 + w), n_vel=10, n_pos=0, n_tq=6, seed=13 + w, q_dirs=0,
+                                  eps=1e-6, x_init=state)
+        assert err < TOL, (w, k, err, detail)
