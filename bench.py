@@ -263,6 +263,9 @@ def run_adjoint(local_rank, reps=3):
             "ms_forward_plus_backward": 1e3 * t_tot, "ms_forward": 1e3 * t_fwd,
             "workload": ADJ_WORKLOAD, "gpu_launches_per_rollout": int(launches),
             "worlds_with_unmodelled_terms": int((status != 0).sum()),
+            "unmodelled_by_bit": {"joint": int(((status & 1) != 0).sum()), "contact": int(((status & 2) != 0).sum()),
+                                  "too_large": int(((status & 4) != 0).sum()),
+                                  "body_body_case_switch": int(((status & 8) != 0).sum())},
             "gradient_check": "tests/test_gpu_adjoint.py (FP64 central differences of the oracle)"}
 
 

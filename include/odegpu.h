@@ -121,10 +121,15 @@ int odegpuBatchSetControlsF32(odegpuBatchID b, int n_ctrl_steps, const float* jo
  * adjoint of every step backwards (one warp per world), then leaves the
  * batch in the state the forward rollout ended in. The derivative follows
  * the recorded active set of the sweep (clamped rows pass nothing to their
- * own lambda). AdjointStatus returns per-world bits: 1 a hinge2 joint or a
- * hinge limit row was met, 2 a contact other than a sphere/box/capsule body
- * against a plane (or a bouncing contact) was met (their derivative is left
- * out), 4 the world exceeds the kernel's limits. */
+ * own lambda). AdjointStatus returns per-world bits, each for a part whose
+ * derivative is left out: 1 a joint the adjoint does not model (slider,
+ * universal, fixed, angular motor, hinge2 without a second body) or a limit
+ * row that bounces or has a powered motor pushing against it; 2 a contact it
+ * does not model (a bouncing contact, a fixed friction direction, a capsule
+ * or cylinder vertex on a heightfield, a geom under a heightfield); 4 the
+ * world exceeds the kernel's limits; 8 a contact between two bodies whose
+ * collider answer changes case within every difference step (the geometry
+ * Jacobian of such contacts is a central difference of the FP32 collider). */
 int odegpuBatchRolloutForward(odegpuBatchID b, int n_steps, int ckpt_every);
 int odegpuBatchRolloutBackward(odegpuBatchID b, const float* grad_state_final, float* grad_state_init,
                                float* grad_joint_torque, float* grad_body_force);

@@ -29,9 +29,10 @@ enum {
   ADJ_UNSUPPORTED_JOINT = 1,     // a bouncing or motor-driven limit row, hinge2 without body 2,
                                  // slider, universal and fixed joints
   ADJ_UNSUPPORTED_CONTACT = 2,   // capsule vertex contact, geom under a field, bounce, fixed friction
-                                 // direction, a body-body contact whose collider case switches
-                                 // within the difference step
-  ADJ_TOO_LARGE = 4
+                                 // direction
+  ADJ_TOO_LARGE = 4,
+  ADJ_PAIR_SWITCH = 8            // a body-body contact whose collider answer changes case within
+                                 // every difference step
 };
 
 constexpr int kAdjBody = 48;   // per-body scratch words
@@ -418,8 +419,9 @@ OG_D int vjp_joint(const BatchDev& d, const WorldDesc& D, const AdjDev& a, int w
 // the nearest one with nearly the same normal; a step that crosses one of the
 // collider's case boundaries (axis choice, clipping, culling, a shallow
 // point's depth test) so that no such contact lies within 50 steps is
-// retried at a quarter of its size, three times (down to 7.8e-6), and marks
-// the contact unsupported when all four fail.
+// retried at a quarter of its size, three times (down to 7.8e-6); a contact
+// that vanishes on one side at every size takes the one-sided difference on
+// the other, and is unsupported only when it vanishes on both.
 constexpr float kPairStep = 5e-4f;
 __device__ __noinline__ int vjp_contact_pair(const BatchDev& d, const WorldDesc& D, const AdjDev& a, int ci,
                                              int r0, int m, float erp_world) {
@@ -484,14 +486,38 @@ __device__ __noinline__ int vjp_contact_pair(const BatchDev& d, const WorldDesc&
   // (R -> (I + d [e_k]x) R) and a scale (R -> (1 + d) R): the directions a
   // change of the quaternion moves R in (dRfromQ of a non-unit q scales R)
   float gdir[2][7];
+  // the contact in an answer of the collider: the nearest one with a normal
+  // within a few degrees of this one's (another shallow contact of the pair
+  // may come and go without changing this one); false when none lies within
+  // `reach`
+  auto match = [&](const GeomView* v, float reach, float* out) {
+    const int nn = collide_primitive(v[0], v[1], (unsigned)D.max_contacts, cc);
+    int best = -1;
+    float bd = reach * reach;
+    for (int j = 0; j < nn; ++j) {
+      const float dx = cc[j].pos[0] - pos_l[0], dy = cc[j].pos[1] - pos_l[1], dz = cc[j].pos[2] - pos_l[2];
+      const float d2 = dx * dx + dy * dy + dz * dz;
+      if (d2 <= bd && dot3(cc[j].normal, n) > 0.99f) { bd = d2; best = j; }
+    }
+    if (best < 0) return false;
+    for (int i = 0; i < 3; ++i) { out[i] = cc[best].pos[i]; out[3 + i] = cc[best].normal[i]; }
+    out[6] = cc[best].depth;
+    return true;
+  };
+  float fbase[7];
+  if (!match(v0, 1e-4f, fbase)) return ADJ_PAIR_SWITCH;
   for (int k = 0; k < 14; ++k) {
     const int side = k / 7, e = k % 7;
+    // one direction's derivative: central differences at the first step of
+    // 5e-4, 1.25e-4, 3.1e-5, 7.8e-6 where the contact is found on both sides;
+    // failing that (a contact within a step of vanishing), the one-sided
+    // difference on the side where it is found at 1.25e-4
     float f[2][7];
-    float step = kPairStep;
-    bool ok = false;
-    for (int attempt = 0; attempt < 4 && !ok; ++attempt, step *= 0.25f) {
-      ok = true;
-      for (int sg = 0; sg < 2 && ok; ++sg) {
+    bool have[2] = {false, false};
+    float step = kPairStep, used = 0.f;
+    int mode = 0;   // 1 central, 2 plus side only, 3 minus side only
+    for (int attempt = 0; attempt < 4 && !mode; ++attempt, step *= 0.25f) {
+      for (int sg = 0; sg < 2; ++sg) {
         GeomView v[2] = {v0[0], v0[1]};
         const float delta = sg ? -step : step;
         float* R = v[side].R;
@@ -510,27 +536,18 @@ __device__ __noinline__ int vjp_contact_pair(const BatchDev& d, const WorldDesc&
           for (int i = 0; i < 3; ++i)
             for (int j = 0; j < 3; ++j) R[i * 4 + j] *= 1.f + delta;
         }
-        const int nn = collide_primitive(v[0], v[1], (unsigned)D.max_contacts, cc);
-        // this contact in the perturbed answer: the nearest one with a normal
-        // within a few degrees (another shallow contact of the pair may come
-        // and go without changing this one)
-        int best = -1;
-        float bd = 2500.f * step * step;
-        for (int j = 0; j < nn; ++j) {
-          const float dx = cc[j].pos[0] - pos_l[0], dy = cc[j].pos[1] - pos_l[1], dz = cc[j].pos[2] - pos_l[2];
-          const float d2 = dx * dx + dy * dy + dz * dz;
-          if (d2 < bd && dot3(cc[j].normal, n) > 0.99f) { bd = d2; best = j; }
-        }
-        if (best < 0) { ok = false; break; }
-        for (int i = 0; i < 3; ++i) { f[sg][i] = cc[best].pos[i]; f[sg][3 + i] = cc[best].normal[i]; }
-        f[sg][6] = cc[best].depth;
+        have[sg] = match(v, 50.f * step, f[sg]);
       }
-      if (ok) break;
+      if (have[0] && have[1]) { mode = 1; used = step; }
+      else if (attempt == 1 && (have[0] || have[1])) { mode = have[0] ? 2 : 3; used = step; }
     }
-    if (!ok) return ADJ_UNSUPPORTED_CONTACT;
-    const float s2 = 0.5f / step;
-    float g = depth_b * (f[0][6] - f[1][6]) * s2;
-    for (int i = 0; i < 3; ++i) g += posb[i] * (f[0][i] - f[1][i]) * s2 + nb[i] * (f[0][3 + i] - f[1][3 + i]) * s2;
+    if (!mode) return ADJ_PAIR_SWITCH;
+    float dfd[7];
+    for (int i = 0; i < 7; ++i)
+      dfd[i] = mode == 1 ? (f[0][i] - f[1][i]) * (0.5f / used)
+                         : mode == 2 ? (f[0][i] - fbase[i]) / used : (fbase[i] - f[1][i]) / used;
+    float g = depth_b * dfd[6];
+    for (int i = 0; i < 3; ++i) g += posb[i] * dfd[i] + nb[i] * dfd[3 + i];
     gdir[side][e] = g;
   }
   // back to d/dx and d/dR: d/dR = sum_k g_k / (2 s^2) [e_k]x R + g_scale / (3 s^2) R,
