@@ -14,7 +14,12 @@
  *    odegpuGetLastError() says why (ODE aborts on debug asserts).
  *  - joints with dJointSetFeedback get f1 t1 (and f2 t2 with a second body)
  *    after each dWorldQuickStep, as ODE's quickstep fills them.
- *  - Limits per world: 64 bodies, 1024 constraint rows (odegpu.h).
+ *  - A world of up to 64 bodies whose joints and contacts cannot need more
+ *    than 1024 constraint rows steps in one on-chip kernel per phase; a
+ *    larger world (up to 65536 bodies) steps through the large-world
+ *    pipeline of odegpu.h with the caller's contacts. dWorldStep and joint
+ *    feedback are available on the first path only: for a larger world
+ *    those calls return 0.
  */
 #ifndef ODE_GPU_H
 #define ODE_GPU_H

@@ -98,10 +98,15 @@ int odegpuBatchStepPlain(odegpuBatchID b, int n_steps);
 int odegpuBatchStepGraph(odegpuBatchID b, int n_steps);
 /* The stepper every step entry point uses from now on: 0 dWorldQuickStep
  * (ode/src/ode.cpp:1807), 1 dWorldStep (ode/src/ode.cpp:1787; ode/src/step.cpp
- * with the Dantzig LCP of ode/src/lcp.cpp). dWorldStep works on a dense
- * m x m matrix per island (scratch of about 8 m^2 bytes per world, m the
- * world's row capacity, allocated on first use); it is not available for a
- * large world, the parity taps, the adjoint or the autotuner. */
+ * with the Dantzig LCP of ode/src/lcp.cpp). dWorldStep works on dense
+ * m x m matrices per island: each step sizes a world's scratch (about
+ * 8 m^2 bytes) by the rows its joints and that step's contacts can need
+ * (3 per contact, 6 per persistent joint), reads the total back once and
+ * grows a shared arena when it is short. A captured graph cannot read back,
+ * so odegpuBatchStepGraph under dWorldStep first lays the arena out by
+ * every world's row capacity (up to 1024 rows: ~8 MB per world). dWorldStep
+ * is not available for a large world, the parity taps, the adjoint or the
+ * autotuner. */
 int odegpuBatchSetStepper(odegpuBatchID b, int exact);
 int odegpuBatchSynchronize(odegpuBatchID b);
 

@@ -207,11 +207,23 @@ struct odegpuBatch {
   DBuf<odegpuRay> ray_in;          // odegpuBatchRayCast staging, grown on demand
   DBuf<odegpuRayHit> ray_out;
   bool exact = false;              // dWorldStep instead of dWorldQuickStep
-  DBuf<float> xscratch;            // dWorldStep scratch (world_exact.cuh), first use
-  DBuf<long long> xoff;
-  DBuf<int> xcap;
-  std::vector<int> xcap_h;
-  int ensure_exact_scratch() {
+  // dWorldStep scratch (world_exact.cuh). A step outside a graph sizes each
+  // world's region by the rows its joints and this step's contacts can need
+  // (exact_size_kernel), reads the total back and grows the arena to fit.
+  // A graph cannot read anything back, so capturing dWorldStep first lays
+  // the arena out by every world's row capacity (xoff_cap / xcap_cap).
+  DBuf<float> xscratch;
+  DBuf<long long> xoff, xoff_cap, xtotal;
+  DBuf<int> xcap, xcap_cap;
+  long long* xtotal_h = nullptr;     // pinned
+  bool xcap_ready = false;
+  int grow_exact_arena(long long floats) {
+    if (xscratch.p && (long long)xscratch.n >= floats) return 0;
+    if (xscratch.p) { cudaFree(xscratch.p); xscratch.p = nullptr; }
+    return xscratch.alloc((size_t)(floats + floats / 4));
+  }
+  int ensure_exact_by_capacity() {
+    if (xcap_ready) return grow_exact_arena(xtotal_cap);
     std::vector<long long> off(n_worlds);
     std::vector<int> cap(n_worlds);
     long long total = 0;
@@ -220,17 +232,29 @@ struct odegpuBatch {
       off[w] = total;
       total += (exact_scratch_floats(cap[w]) + 3) & ~3LL;
     }
-    if (xscratch.p && cap == xcap_h) return 0;
-    for (auto* p : {(void*)xscratch.p, (void*)xoff.p, (void*)xcap.p})
-      if (p) cudaFree(p);
-    xscratch.p = nullptr; xoff.p = nullptr; xcap.p = nullptr;
-    xcap_h = cap;
-    if (int rc = xscratch.alloc((size_t)total)) return rc;
-    if (int rc = xoff.alloc(n_worlds)) return rc;
-    if (int rc = xcap.alloc(n_worlds)) return rc;
-    OG_CUDA(cudaMemcpy(xoff.p, off.data(), n_worlds * sizeof(long long), cudaMemcpyHostToDevice));
-    OG_CUDA(cudaMemcpy(xcap.p, cap.data(), n_worlds * sizeof(int), cudaMemcpyHostToDevice));
-    return 0;
+    if (int rc = xoff_cap.upload(off)) return rc;
+    if (int rc = xcap_cap.upload(cap)) return rc;
+    xtotal_cap = total;
+    xcap_ready = true;
+    return grow_exact_arena(total);
+  }
+  long long xtotal_cap = 0;
+  int size_exact_step() {
+    if (!xoff.p) {
+      if (int rc = xoff.alloc(n_worlds)) return rc;
+      if (int rc = xcap.alloc(n_worlds)) return rc;
+      if (int rc = xtotal.alloc(1)) return rc;
+    }
+    if (!xtotal_h && cudaHostAlloc(&xtotal_h, sizeof(long long), cudaHostAllocDefault) != cudaSuccess) {
+      cudaGetLastError();
+      xtotal_h = nullptr;
+      return fail(ODEGPU_E_NOMEM, "pinned host allocation failed");
+    }
+    exact_size_kernel<<<1, kExactSizeThreads, 0, stream>>>(dev(), xcap.p, xoff.p, xtotal.p);
+    ++launches;
+    OG_CUDA(cudaMemcpyAsync(xtotal_h, xtotal.p, sizeof(long long), cudaMemcpyDeviceToHost, stream));
+    OG_CUDA(cudaStreamSynchronize(stream));
+    return grow_exact_arena(*xtotal_h);
   }
 
   BatchDev dev() const {
@@ -281,6 +305,7 @@ struct odegpuBatch {
   }
   ~odegpuBatch() {
     for (cudaEvent_t e : ev_pool) cudaEventDestroy(e);
+    if (xtotal_h) cudaFreeHost(xtotal_h);
     delete lw;
   }
 
@@ -374,37 +399,43 @@ struct odegpuBatch {
         lw_bodies_pre_kernel<<<g(nb, T), T, 0, stream>>>(d, step, opt.host_forces ? 0 : 1, 1);
         launches += 1;
       }
-      // broadphase + narrowphase in canonical pair order
-      cudaMemsetAsync(L0.hcount, 0, sizeof(int) * (L0.hsize + 1), stream);
-      cudaMemsetAsync(L0.hfill, 0, sizeof(int) * L0.hsize, stream);
-      if (L0.nstat) cudaMemsetAsync(L0.sflag, 0, sizeof(int) * (size_t)L0.nstat * (ng + 1), stream);
       cudaMemsetAsync(L0.ccount, 0, sizeof(int) * nb, stream);
       cudaMemsetAsync(L0.afill, 0, sizeof(int) * nb, stream);
-      lw_hash_kernel<<<g(ng, T), T, 0, stream>>>(d, L0);
-      scan(L0.hcount, nullptr, L0.hsize);
-      lw_hfill_kernel<<<g(ng, T), T, 0, stream>>>(L0);
-      lw_candidates_kernel<<<g(ng, 128), 128, 0, stream>>>(d, L0);
-      launches += 3;
-      if (L0.nstat) {
-        scan(L0.sflag, nullptr, ng, L0.nstat, (size_t)ng + 1);
-        lw_static_own_kernel<<<1, 32, 0, stream>>>(L0);
-        ++launches;
+      if (opt.collide) {
+        // broadphase + narrowphase in canonical pair order
+        cudaMemsetAsync(L0.hcount, 0, sizeof(int) * (L0.hsize + 1), stream);
+        cudaMemsetAsync(L0.hfill, 0, sizeof(int) * L0.hsize, stream);
+        if (L0.nstat) cudaMemsetAsync(L0.sflag, 0, sizeof(int) * (size_t)L0.nstat * (ng + 1), stream);
+        lw_hash_kernel<<<g(ng, T), T, 0, stream>>>(d, L0);
+        scan(L0.hcount, nullptr, L0.hsize);
+        lw_hfill_kernel<<<g(ng, T), T, 0, stream>>>(L0);
+        lw_candidates_kernel<<<g(ng, 128), 128, 0, stream>>>(d, L0);
+        launches += 3;
+        if (L0.nstat) {
+          scan(L0.sflag, nullptr, ng, L0.nstat, (size_t)ng + 1);
+          lw_static_own_kernel<<<1, 32, 0, stream>>>(L0);
+          ++launches;
+        }
+        scan(L0.own, nullptr, ng);
+        lw_pairs_fill_kernel<<<g(ng, T), T, 0, stream>>>(d, L0);
+        lw_narrow_kernel<<<g(L0.pair_cap, 128), 128, 0, stream>>>(d, L0);
+        scan(L0.pnc, L0.npairs, 0);
+        lw_contacts_kernel<<<g(L0.pair_cap, T), T, 0, stream>>>(d, L0);
+        launches += 3;
       }
-      scan(L0.own, nullptr, ng);
-      lw_pairs_fill_kernel<<<g(ng, T), T, 0, stream>>>(d, L0);
-      lw_narrow_kernel<<<g(L0.pair_cap, 128), 128, 0, stream>>>(d, L0);
-      scan(L0.pnc, L0.npairs, 0);
-      lw_contacts_kernel<<<g(L0.pair_cap, T), T, 0, stream>>>(d, L0);
-      launches += 3;
       mark(tm);
-      // body joint lists, islands, rows
+      // body joint lists (contacts newest first, then persistent joints; or
+      // the host's complete lists), islands, rows
       lw_adj_count_kernel<<<g(nb, T), T, 0, stream>>>(d, L0);
       scan(L0.acount, nullptr, nb);
-      lw_adj_fill_kernel<<<g(L0.contact_cap, T), T, 0, stream>>>(d, L0);
+      if (!opt.host_adjacency) {
+        lw_adj_fill_kernel<<<g(L0.contact_cap, T), T, 0, stream>>>(d, L0);
+        ++launches;
+      }
       lw_adj_finish_kernel<<<g(nb, T), T, 0, stream>>>(d, L0);
       lw_islands_kernel<<<1, 32, W.islands_smem, stream>>>(d, L0, W.islands_smem);
       lw_info1_kernel<<<g(njall, 128), 128, 0, stream>>>(d, L0, step);
-      launches += 5;
+      launches += 4;
       scan(L0.jm, L0.nj, 0);
       lw_max_scan_kernel<<<1, kLwScanThreads, 0, stream>>>(L0.bfk, L0.nj);
       lw_info2_kernel<<<g(njall, 128), 128, 0, stream>>>(d, L0, step);
@@ -477,14 +508,19 @@ struct odegpuBatch {
     int w[3];
     for (int k = 0; k < 3; ++k) w[k] = single_world ? 1 : kwpb[k];
     if (exact) {
-      if (int rc = ensure_exact_scratch()) return rc;
-      const ExactDev X{xscratch.p, xoff.p, xcap.p};
+      const bool capturing = cap != cudaStreamCaptureStatusNone;
+      if (capturing && !(xcap_ready && xscratch.p && (long long)xscratch.n >= xtotal_cap))
+        return fail(ODEGPU_E_ARG, "dWorldStep scratch was not laid out before the capture");
       const int wx = single_world ? 1 : kExactWarps;
       for (int s = 0; s < n_steps; ++s) {
         mark(tm);
         apply_carveout(0);
         world_collide_kernel<<<(count + w[0] - 1) / w[0], w[0] * 32, (size_t)w[0] * kCollideSmemPerWarp,
                                stream>>>(d, ord, first, count, step_counter + s, opt);
+        if (!capturing)
+          if (int rc = size_exact_step()) return rc;
+        const ExactDev X = capturing ? ExactDev{xscratch.p, xoff_cap.p, xcap_cap.p}
+                                     : ExactDev{xscratch.p, xoff.p, xcap.p};
         mark(tm);
         world_exact_kernel<<<(count + wx - 1) / wx, wx * 32, (size_t)wx * kSmemPerWarp, stream>>>(
             d, X, ord, first, count, step_counter + s, opt);
@@ -1067,6 +1103,8 @@ int odegpuBatchStepGraph(odegpuBatchID b, int n_steps) {
   if (!b || n_steps < 0) return fail(ODEGPU_E_ARG, "bad arguments");
   OG_CUDA(cudaSetDevice(b->device));
   StepOptions opt{1, nullptr, nullptr, nullptr, 0, 0};
+  if (b->exact)
+    if (int rc = b->ensure_exact_by_capacity()) return rc;
   cudaGraph_t graph;
   OG_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
   for (int s = 0; s < n_steps; ++s) {
@@ -1090,11 +1128,6 @@ int odegpuBatchStepGraph(odegpuBatchID b, int n_steps) {
 int odegpuBatchSetStepper(odegpuBatchID b, int exact) {
   if (!b || (exact != 0 && exact != 1)) return fail(ODEGPU_E_ARG, "bad arguments");
   if (exact && b->lw) return fail(ODEGPU_E_ARG, "dWorldStep is not available for a large world");
-  if (exact) {
-    // the scratch is allocated here, outside any stream capture
-    OG_CUDA(cudaSetDevice(b->device));
-    if (int rc = b->ensure_exact_scratch()) return rc;
-  }
   b->exact = exact != 0;
   return 0;
 }
@@ -1637,6 +1670,9 @@ namespace og {
 struct WorldCtx {
   odegpuBatch B;
   DBuf<float> contact_fb;   // contact-joint feedback of the last step
+  // capacities the large-world buffers were made for (nb, persistent joints,
+  // contacts), kept while a world's next step fits them
+  int lw_nb = 0, lw_njp = 0, lw_ccap = 0;
 };
 
 WorldCtx* ctx_create(int device) {
@@ -1670,19 +1706,10 @@ void ctx_destroy(WorldCtx* c) {
   delete c;
 }
 
-int ctx_step(WorldCtx* c, HostWorld& hw) {
-  odegpuBatch& B = c->B;
-  OG_CUDA(cudaSetDevice(B.device));
+// Uploads of the body, joint and contact arrays shared by both step paths.
+static int ctx_upload(odegpuBatch& B, const HostWorld& hw, const WorldDesc& D) {
   cudaStream_t s = B.stream;
-  const int nb = hw.desc.nb;
-  if (nb > kMaxB) return fail(ODEGPU_E_LIMIT, "world has more than 64 bodies");
-  B.nb_total = nb;
-  B.nj_total = hw.desc.njp;
-  WorldDesc D = hw.desc;
-  D.body_off = D.geom_off = D.joint_off = D.contact_off = D.row_off = D.padj_off = 0;
-  D.ng = 0;
-  D.fwd_scratch = D.row_cap > kFwdRows ? 0 : -1;
-  const size_t jl = (size_t)D.njp + D.contact_cap;
+  const int nb = D.nb;
   std::vector<WorldDesc> wd(1, D);
   int rc = 0;
   rc = rc ? rc : put(B.world, wd, s);
@@ -1709,6 +1736,88 @@ int ctx_step(WorldCtx* c, HostWorld& hw) {
   rc = rc ? rc : put(B.padj_start, hw.padj_start, s);
   rc = rc ? rc : put(B.padj, hw.padj, s);
   rc = rc ? rc : grow(B.rows, (size_t)D.row_cap * kRowWords);
+  return rc;
+}
+
+static int ctx_download(odegpuBatch& B, HostWorld& hw) {
+  cudaStream_t s = B.stream;
+  const int nb = hw.desc.nb;
+  std::vector<int> st(1);
+  OG_CUDA(cudaMemcpyAsync(hw.pos.data(), B.pos.p, nb * sizeof(float4), cudaMemcpyDeviceToHost, s));
+  OG_CUDA(cudaMemcpyAsync(hw.q.data(), B.q.p, nb * sizeof(float4), cudaMemcpyDeviceToHost, s));
+  OG_CUDA(cudaMemcpyAsync(hw.lvel.data(), B.lvel.p, nb * sizeof(float4), cudaMemcpyDeviceToHost, s));
+  OG_CUDA(cudaMemcpyAsync(hw.avel.data(), B.avel.p, nb * sizeof(float4), cudaMemcpyDeviceToHost, s));
+  OG_CUDA(cudaMemcpyAsync(&hw.seed, B.seed.p, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+  OG_CUDA(cudaMemcpyAsync(st.data(), B.status.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  OG_CUDA(cudaStreamSynchronize(s));
+  hw.status = st[0];
+  return 0;
+}
+
+// A world above the on-chip limits (more than 64 bodies, or joints and
+// contacts that may need more than 1024 rows) steps through the large-world
+// pipeline with the host's contacts and joint lists: no collision, one world.
+static int ctx_step_large(WorldCtx* c, HostWorld& hw) {
+  odegpuBatch& B = c->B;
+  const int nb = hw.desc.nb;
+  if (nb > ODEGPU_MAX_BODIES_LARGE)
+    return fail(ODEGPU_E_LIMIT, "world has " + std::to_string(nb) + " bodies; at most " +
+                                    std::to_string(ODEGPU_MAX_BODIES_LARGE));
+  if (hw.exact) return fail(ODEGPU_E_ARG, "dWorldStep is not available for a world above 64 bodies or 1024 rows");
+  if (hw.want_feedback)
+    return fail(ODEGPU_E_ARG, "joint feedback is not available for a world above 64 bodies or 1024 rows");
+  WorldDesc D = hw.desc;
+  D.body_off = D.geom_off = D.joint_off = D.contact_off = D.row_off = D.padj_off = 0;
+  D.ng = 0;
+  D.fwd_scratch = -1;
+  const int nc = (int)hw.contacts.size();
+  const bool fits = B.lw && c->lw_nb == nb && c->lw_njp == D.njp && c->lw_ccap >= nc;
+  D.contact_cap = fits ? c->lw_ccap : std::max(64, nc + nc / 2);
+  D.row_cap = 3 * D.contact_cap + 6 * D.njp;
+  B.nb_total = nb;
+  B.nj_total = D.njp;
+  if (int rc = ctx_upload(B, hw, D)) return rc;
+  B.n_ctrl_steps = 0;
+  B.feedback_on = false;
+  B.exact = false;
+  B.n_worlds = 1;
+  B.h_world.assign(1, D);
+  if (!fits) {
+    delete B.lw;
+    B.lw = new LargeWorld();
+    c->lw_nb = c->lw_njp = c->lw_ccap = 0;
+    if (int rc = ::lw_setup(&B, nullptr)) {
+      delete B.lw;
+      B.lw = nullptr;
+      return rc;
+    }
+    c->lw_nb = nb; c->lw_njp = D.njp; c->lw_ccap = D.contact_cap;
+  }
+  const StepOptions opt{0, nullptr, nullptr, nullptr, 1, 1};
+  if (int e = B.launch(0, 1, 1, opt, false)) return e;
+  return ctx_download(B, hw);
+}
+
+int ctx_step(WorldCtx* c, HostWorld& hw) {
+  odegpuBatch& B = c->B;
+  OG_CUDA(cudaSetDevice(B.device));
+  cudaStream_t s = B.stream;
+  const int nb = hw.desc.nb;
+  if (nb > kMaxB || 6LL * hw.desc.njp + 3LL * (long long)hw.contacts.size() > ODEGPU_MAX_ROWS_PER_WORLD)
+    return ctx_step_large(c, hw);
+  if (B.lw) {
+    delete B.lw;
+    B.lw = nullptr;
+    c->lw_nb = c->lw_njp = c->lw_ccap = 0;
+  }
+  B.nb_total = nb;
+  B.nj_total = hw.desc.njp;
+  WorldDesc D = hw.desc;
+  D.body_off = D.geom_off = D.joint_off = D.contact_off = D.row_off = D.padj_off = 0;
+  D.ng = 0;
+  D.fwd_scratch = D.row_cap > kFwdRows ? 0 : -1;
+  const size_t jl = (size_t)D.njp + D.contact_cap;
+  int rc = ctx_upload(B, hw, D);
   rc = rc ? rc : grow(B.sweep, ((size_t)D.row_cap + 32) * 8);
   if (D.fwd_scratch >= 0) rc = rc ? rc : grow(B.fwd_scratch, (size_t)kFwdScratchPerWorld);
   rc = rc ? rc : grow(B.jlist, jl);
@@ -1745,16 +1854,7 @@ int ctx_step(WorldCtx* c, HostWorld& hw) {
       OG_CUDA(cudaMemcpyAsync(hw.contact_feedback.data(), c->contact_fb.p,
                               hw.contact_feedback.size() * sizeof(float), cudaMemcpyDeviceToHost, s));
   }
-  std::vector<int> st(1);
-  OG_CUDA(cudaMemcpyAsync(hw.pos.data(), B.pos.p, nb * sizeof(float4), cudaMemcpyDeviceToHost, s));
-  OG_CUDA(cudaMemcpyAsync(hw.q.data(), B.q.p, nb * sizeof(float4), cudaMemcpyDeviceToHost, s));
-  OG_CUDA(cudaMemcpyAsync(hw.lvel.data(), B.lvel.p, nb * sizeof(float4), cudaMemcpyDeviceToHost, s));
-  OG_CUDA(cudaMemcpyAsync(hw.avel.data(), B.avel.p, nb * sizeof(float4), cudaMemcpyDeviceToHost, s));
-  OG_CUDA(cudaMemcpyAsync(&hw.seed, B.seed.p, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
-  OG_CUDA(cudaMemcpyAsync(st.data(), B.status.p, sizeof(int), cudaMemcpyDeviceToHost, s));
-  OG_CUDA(cudaStreamSynchronize(s));
-  hw.status = st[0];
-  return 0;
+  return ctx_download(B, hw);
 }
 
 DevHeightfield make_dev_heightfield(int nx, int nz, double width, double depth, double scale, double offset,

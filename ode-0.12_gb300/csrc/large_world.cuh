@@ -440,13 +440,21 @@ __global__ void lw_adj_finish_kernel(BatchDev d, LWDev L) {
     J[q + 1] = vj;
     O[q + 1] = vo;
   }
+  // (a host-supplied list may hold contacts too: ordinals njp and up)
   const int* ps = d.padj_start + D.body_off;
   int e = s + nc;
   for (int k = ps[b]; k < ps[b + 1]; ++k, ++e) {
     const int j = d.padj[k];
-    const DevJoint& Jt = d.joints[D.joint_off + j];
+    int b1, b2;
+    if (j < L.njp) {
+      const DevJoint& Jt = d.joints[D.joint_off + j];
+      b1 = Jt.b1; b2 = Jt.b2;
+    } else {
+      const DevContact& ct = d.contacts[D.contact_off + j - L.njp];
+      b1 = ct.b1; b2 = ct.b2;
+    }
     L.adj_joint[e] = j;
-    L.adj_other[e] = (Jt.b1 == b) ? Jt.b2 : Jt.b1;
+    L.adj_other[e] = (b1 == b) ? b2 : b1;
   }
 }
 

@@ -1184,7 +1184,7 @@ static int world_step(dWorldID w, dReal stepsize, bool exact) {
   og::HostWorld& hw = w->hw;
   const int nb = (int)w->bodies.size();
   if (nb == 0) return 1;
-  if (nb > ODEGPU_MAX_BODIES_PER_WORLD) return 0;
+  if (nb > ODEGPU_MAX_BODIES_LARGE) return 0;
   hw.pos.resize(nb); hw.q.resize(nb); hw.lvel.resize(nb); hw.avel.resize(nb);
   hw.facc.resize(nb); hw.tacc.resize(nb);
   hw.mass.resize(nb); hw.invMass.resize(nb); hw.I.resize(9 * (size_t)nb); hw.invI.resize(9 * (size_t)nb);

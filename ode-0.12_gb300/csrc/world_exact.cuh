@@ -599,8 +599,44 @@ OG_D XWorld carve_exact(float* base, int cap) {
   return X;
 }
 // floats of scratch a world with `cap` rows needs
-constexpr long long exact_scratch_floats(int cap) {
+OG_HD constexpr long long exact_scratch_floats(int cap) {
   return 2LL * cap * cap + 40LL * cap + 12LL * kMaxB + 16;
+}
+
+// The regions of a dWorldStep: every world's row bound for this step (at
+// most 3 rows per contact and 6 per persistent joint, within its row
+// capacity; it also bounds the joint count, nj <= rows) and the float
+// offsets of the worlds' regions, with their total. One block; each thread
+// sums a run of worlds, then a block scan over the runs.
+constexpr int kExactSizeThreads = 1024;
+__global__ void __launch_bounds__(kExactSizeThreads)
+exact_size_kernel(BatchDev d, int* cap, long long* off, long long* total) {
+  __shared__ long long part[kExactSizeThreads];
+  const int n = d.n_worlds, t = threadIdx.x;
+  const int per = (n + kExactSizeThreads - 1) / kExactSizeThreads;
+  const int w0 = min(n, t * per), w1 = min(n, w0 + per);
+  long long sum = 0;
+  for (int w = w0; w < w1; ++w) {
+    const WorldDesc D = d.world[w];
+    const long long bound = 6LL * D.njp + 3LL * d.ncontacts[w];
+    const int c = (int)max(1LL, min(bound, (long long)min(D.row_cap, kMaxR)));
+    cap[w] = c;
+    sum += (exact_scratch_floats(c) + 3) & ~3LL;
+  }
+  part[t] = sum;
+  __syncthreads();
+  for (int o = 1; o < kExactSizeThreads; o <<= 1) {
+    const long long v = t >= o ? part[t - o] : 0;
+    __syncthreads();
+    part[t] += v;
+    __syncthreads();
+  }
+  long long base = part[t] - sum;
+  for (int w = w0; w < w1; ++w) {
+    off[w] = base;
+    base += (exact_scratch_floats(cap[w]) + 3) & ~3LL;
+  }
+  if (t == kExactSizeThreads - 1) *total = part[t];
 }
 
 // The two-ended joint order of step.cpp:265-403 over island-local joints

@@ -123,6 +123,33 @@ def test_exact_launch_modes_agree():
     assert np.array_equal(out[0], out[1]) and np.array_equal(out[0], out[2])
 
 
+def test_exact_scratch_sized_by_each_step():
+    """The 4096-world batched workload under dWorldStep for 200 steps: each
+    step sizes a world's dense scratch by the rows its joints and that step's
+    contacts can need, so the device memory the batch holds stays a fraction
+    of the layout by row capacity (8 bytes x cap^2 per world, cap = min(1024,
+    3 x contact capacity + 6 x joints)), which a captured graph still uses."""
+    import torch
+    from odegpu.batch import Batch
+    sc = S.batched_worlds(n_worlds=4096, seed=1)
+    nb = np.diff(sc.body_off)
+    nj = np.diff(sc.joint_off)
+    cap = np.minimum(1024, 3 * (8 * nb + 16) + 6 * nj).astype(np.float64)
+    by_capacity = float((8.0 * cap * cap).sum())
+    torch.cuda.init()
+    free0, _ = torch.cuda.mem_get_info()
+    B = Batch(sc)
+    B.set_stepper(True)
+    B.step(200)
+    free1, _ = torch.cuda.mem_get_info()
+    nc = B.counts()[0]
+    B.close()
+    used = free0 - free1
+    assert nc.sum() > 4096 * 10
+    assert by_capacity > 8e9
+    assert used < 0.2 * by_capacity, (used / 1e9, by_capacity / 1e9)
+
+
 def test_exact_stepper_guards():
     """The adjoint, the parity taps and the autotuner refuse the exact
     stepper; switching back restores dWorldQuickStep."""

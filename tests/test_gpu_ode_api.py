@@ -512,3 +512,40 @@ def test_disabled_joint_takes_no_part(stepper):
     assert not np.array_equal(pos(ba), pos(bb))
     L.dWorldDestroy(wa)
     L.dWorldDestroy(wb)
+
+
+def test_worlds_above_64_bodies_step_through_large_pipeline():
+    """dWorldQuickStep on a world above the on-chip kernel's 64 bodies steps
+    it through the large-world pipeline with the program's own contacts and
+    body joint lists (ode.cpp:1807-1824 puts no cap on the world's size).
+    An 80-box drop (box_drop_demo.c) and an 80-link hinge chain with per-step
+    hinge torques touching the plane (scene_player.c), each against the
+    batched path stepping the same single world through the same pipeline:
+    contacts come from the same collider in the same pair order, so the
+    states agree to FP32 rounding (1e-4 m, 1e-2 m/s). dWorldStep is not
+    available for such a world: the call returns 0 and the program stops."""
+    import subprocess
+    from odegpu.batch import Batch
+    drop = S.box_drop(seed=1, n_boxes=80)
+    chain = S.hinge_chains(n_worlds=1, links=80, seed=11, steps=40, plane_z=-2.0)
+    with tempfile.TemporaryDirectory() as d:
+        inp = os.path.join(d, "in.txt")
+        for sc, steps, exe, write in (
+                (drop, 70, U.build_gpu_demo(os.path.join(d, "demo")), U.scene_input),
+                (chain, 40, U.build_gpu_demo(os.path.join(d, "player"), src=U.PLAYER),
+                 lambda s, n, p: U.player_input(s, 0, n, p))):
+            assert sc.nb_total > 64
+            B = Batch(sc)
+            B.step(steps)
+            bt = B.state()
+            nc = int(B.counts()[0][0])
+            assert (B.status() == 0).all(), B.status()
+            B.close()
+            write(sc, steps, inp)
+            st = U.run_demo(exe, inp)
+            assert nc > 0
+            assert np.abs(st[:, :3] - bt[:, :3]).max() < 1e-4
+            assert np.abs(st[:, 7:] - bt[:, 7:]).max() < 1e-2
+        U.player_input(chain, 0, 2, inp)
+        with pytest.raises(subprocess.CalledProcessError):
+            U.run_demo(exe, inp, "exact")
