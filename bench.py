@@ -42,6 +42,16 @@ SETTLE_STEP = 150
 CPU_MIN_SECONDS = 2.0
 
 
+def _set_worlds(n):
+    """Resize the batched workload (profiling of a smaller case)."""
+    global N_WORLDS, WORKLOAD, METRIC
+    if n < 1:
+        raise SystemExit("--worlds must be >= 1")
+    WORKLOAD = WORKLOAD.replace(f"{N_WORLDS} worlds", f"{n} worlds")
+    METRIC = METRIC.replace(f"({N_WORLDS} worlds)", f"({n} worlds)")
+    N_WORLDS = n
+
+
 def bench_config(steps, iters=20):
     """The workload description both arms print (identical for the same
     --steps)."""
@@ -541,6 +551,8 @@ def run_ours(args):
     # launch shapes picked by the library's autotuner on the settled state
     # (outside the timed region; the state is restored below)
     launch_cfg = B.autotune(4)
+    if args.step_kernels != "auto":
+        B.set_step_kernels(args.step_kernels == "fused")
     reset()
     for _ in range(args.warmup):
         B.step(1)
@@ -610,11 +622,29 @@ def run_ours(args):
         hbm, src = peaks()
         kern_ms, kern_steps = main["kern_ms"], main["kern_steps"]
         step_achieved = float(np.sum(main["bytes"])) / t_kernel / 1e9
-        t_solve = kern_ms[2] / 1e3
-        achieved = main["solve_bytes"] / t_solve / 1e9
-        tpr = solve_traffic_per_row_iter()
-        traffic = tpr * main["rows"] * iters / args.steps if tpr is not None else None
-        share = kern_ms / kern_ms.sum()
+        fused, fused_wpb, fused_carve = B.step_kernels()
+        if fused:
+            # one kernel per step (the autotuner picked the fused step kernel):
+            # its roofline is the whole step's byte model
+            t_dom = kern_ms[0] / 1e3
+            achieved = float(np.sum(main["bytes"])) / t_dom / 1e9
+            traffic = None
+            dom = {"kernel": "world_step_kernel (collide + setup + SOR_LCP + integration)",
+                   "bytes_model": "208*nb + 56*nc + 40*n_ball + m*(248 + 236*iters) per world",
+                   "launch_ms_avg": kern_ms[0] / max(1, kern_steps), "traffic_source": None}
+            share_d = {"world_step_kernel": 1.0}
+        else:
+            t_solve = kern_ms[2] / 1e3
+            achieved = main["solve_bytes"] / t_solve / 1e9
+            tpr = solve_traffic_per_row_iter()
+            traffic = tpr * main["rows"] * iters / args.steps if tpr is not None else None
+            dom = {"kernel": "world_solve_kernel (SOR_LCP + integration)",
+                   "bytes_model": "236 B per row-iteration (rows x iterations of the launch)",
+                   "launch_ms_avg": kern_ms[2] / max(1, kern_steps),
+                   "traffic_source": "ncu dram bytes per row-iteration (profiles/) x rows x iters"}
+            share = kern_ms / kern_ms.sum()
+            share_d = {"world_collide_kernel": share[0], "world_setup_kernel": share[1],
+                       "world_solve_kernel": share[2]}
         times = main["times"]
         line = {"metric": METRIC, "value": value, "unit": "world-steps/s", "n_gpus": world_size,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps,
@@ -624,23 +654,19 @@ def run_ours(args):
                 "window": {"rows_per_world_avg": main["rows"] / (args.steps * sc.n_worlds),
                            "bodies": int(nbt), "worlds_with_status": int((main["status"] != 0).sum()),
                            "launch_shape": {"collide": launch_cfg[0], "setup": launch_cfg[1],
-                                            "solve": launch_cfg[2]},
+                                            "solve": launch_cfg[2], "fused_step": [fused_wpb, fused_carve],
+                                            "step_kernels": "fused" if fused else "collide, setup, solve"},
                            "step_ms_min_median_max": [float(1e3 * times.min()), float(1e3 * np.median(times)),
                                                       float(1e3 * times.max())]},
                 "from_initial_state": {"value": total_worlds * args.steps / t_first,
                                        "unit": "world-steps/s",
                                        "rollout": f"steps 0..{args.steps - 1} from the initial state",
                                        "rows_per_world_avg": first["rows"] / (args.steps * sc.n_worlds)},
-                "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                             "frac": achieved / hbm, "peak_source": src, "traffic": traffic,
-                             "kernel": "world_solve_kernel (SOR_LCP + integration)",
-                             "bytes_model": "236 B per row-iteration (rows x iterations of the launch)",
-                             "launch_ms_avg": kern_ms[2] / max(1, kern_steps),
-                             "traffic_source": "ncu dram bytes per row-iteration (profiles/) x rows x iters"},
+                "roofline": dict({"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                                  "frac": achieved / hbm, "peak_source": src, "traffic": traffic}, **dom),
                 "step_roofline": {"achieved": step_achieved, "frac": step_achieved / hbm,
                                   "bytes_model": "208*nb + 56*nc + 40*n_ball + m*(248 + 236*iters) per world"},
-                "kernel_share": {"world_collide_kernel": share[0], "world_setup_kernel": share[1],
-                                 "world_solve_kernel": share[2]},
+                "kernel_share": share_d,
                 "e2e": {"value": e2e, "unit": "world-steps/s", "h2d_bytes_per_step": nbt * 13 * 4,
                         "d2h_bytes_per_step": nbt * 13 * 4},
                 "gpu_launches": main["launches"], "clocks": clk}
@@ -706,7 +732,14 @@ def main():
     ap.add_argument("--exact-steps", type=int, default=100)
     ap.add_argument("--only-large", action="store_true",
                     help="print only the large-world measurement (for profiling)")
+    ap.add_argument("--step-kernels", default="auto", choices=["auto", "split", "fused"],
+                    help="one fused kernel per step, the collide / setup / solve kernels, or the "
+                         "autotuner's choice (under a profiler the autotuner's timings are distorted)")
+    ap.add_argument("--worlds", type=int, default=N_WORLDS,
+                    help="worlds of the batched workload (a smaller case for profiling; the "
+                         "benchmark configuration is 4096)")
     args = ap.parse_args()
+    _set_worlds(args.worlds)
     if args.impl == "reference":
         run_reference(args)
     elif args.only_adjoint or args.only_vehicles or args.only_large or args.only_exact:

@@ -141,15 +141,25 @@ int odegpuBatchRolloutBackward(odegpuBatchID b, const float* grad_state_final, f
 int odegpuBatchAdjointStatus(odegpuBatchID b, int* status);
 
 /* Launch shape of each kernel (no counterpart in the reference): kernel 0
- * collide, 1 setup, 2 solve, 3 adjoint; warps per block (one world per warp;
- * at most 4, 8, 8, 4) and the preferred shared-memory carveout in percent of
- * the unified L1/shared array (-1 = driver default). GetLaunchConfig writes
- * cfg[8] = {wpb, carveout} per kernel. Autotune times n_steps steps of every
- * candidate shape on the batch's current state (restored after each trial)
- * and keeps the fastest per kernel; the batch state, seeds and step index are
- * unchanged afterwards. */
+ * collide, 1 setup, 2 solve, 3 adjoint, 4 the fused step kernel; warps per
+ * block (one world per warp; at most 4, 8, 8, 4, 4) and the preferred
+ * shared-memory carveout in percent of the unified L1/shared array (-1 =
+ * driver default). GetLaunchConfig writes cfg[8] = {wpb, carveout} of
+ * kernels 0-3; GetStepKernels reports kernel 4.
+ * SetStepKernels(fused): a step is one launch of the fused step kernel
+ * (fused = 1: every warp runs collide, setup and solve of its world in turn,
+ * so short worlds do not wait at phase boundaries for the long ones) or the
+ * collide, setup and solve kernels (fused = 0, the default until Autotune
+ * picks). Both give the same results. With timing on (SetTiming), a fused
+ * step's time is reported in the collide entry of GetKernelTimes.
+ * Autotune times n_steps steps of every candidate shape on the batch's
+ * current state (restored after each trial), keeps the fastest per kernel and
+ * chooses fused or split steps by the faster step; the batch state, seeds and
+ * step index are unchanged afterwards. */
 int odegpuBatchSetLaunchConfig(odegpuBatchID b, int kernel, int warps_per_block, int smem_carveout);
 int odegpuBatchGetLaunchConfig(odegpuBatchID b, int* cfg);
+int odegpuBatchSetStepKernels(odegpuBatchID b, int fused);
+int odegpuBatchGetStepKernels(odegpuBatchID b, int* fused, int* warps_per_block, int* smem_carveout);
 int odegpuBatchAutotune(odegpuBatchID b, int n_steps);
 
 /* Instrumentation (no counterpart in the reference).

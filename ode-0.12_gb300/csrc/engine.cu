@@ -84,6 +84,41 @@ __global__ void __launch_bounds__(256) world_solve_kernel(BatchDev d, const int*
   world_solve(d, w, smem_raw + (size_t)(threadIdx.x >> 5) * kFwdSmemPerWarp, lane, opt);
 }
 
+// The three phases of a step in one launch: each warp runs collide, setup and
+// solve of its world back to back, handing contacts and rows over through
+// global memory as the separate kernels do (program order within the warp and
+// __syncwarp stand in for the kernel boundaries). Worlds do not wait for one
+// another between phases, so the short worlds of a batch fill the SMs while
+// the long ones are still sweeping, instead of every phase ending in a tail.
+constexpr int kStepSmemPerWarp =
+    kSmemPerWarp > kFwdSmemPerWarp ? (kSmemPerWarp > kCollideSmemPerWarp ? kSmemPerWarp : kCollideSmemPerWarp)
+                                   : (kFwdSmemPerWarp > kCollideSmemPerWarp ? kFwdSmemPerWarp : kCollideSmemPerWarp);
+__global__ void __launch_bounds__(128, 4) world_step_kernel(BatchDev d, const int* order, int first, int count,
+                                                            int step, StepOptions opt) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lane = threadIdx.x & 31;
+  const int w = slot_world(order, first, count, d.n_worlds);
+  if (w < 0) return;
+  unsigned char* base = smem_raw + (size_t)(threadIdx.x >> 5) * kStepSmemPerWarp;
+  // the separate kernels' handling of worlds above the on-chip limits
+  if (d.world[w].nb > kMaxB || d.world[w].ng > kMaxB + 8) {
+    if (lane == 0) {
+      atomicOr(&d.status[w], ST_TOO_LARGE);
+      d.ncontacts[w] = 0;
+      d.nrows[w] = 0;
+      d.nislands[w] = 0;
+    }
+    if (d.world[w].nb > kMaxB) return;
+    __syncwarp();
+  } else {
+    world_collide(d, w, step, carve_collide_smem(base), lane, opt);
+    __syncwarp();
+    world_setup(d, w, step, carve_smem(base), lane, opt);
+  }
+  __syncwarp();
+  world_solve(d, w, base, lane, opt);
+}
+
 __global__ void __launch_bounds__(128) world_exact_kernel(BatchDev d, ExactDev X, const int* order, int first,
                                                           int count, int step, StepOptions opt) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -174,10 +209,13 @@ struct odegpuBatch {
   int warps_per_block = 4;
   // per-kernel launch shape: warps per block and preferred shared-memory
   // carveout (percent of the unified L1/shared array, -1 = driver default)
-  // for the collide, setup, solve and adjoint kernels (odegpuBatchSetLaunchConfig
-  // / odegpuBatchAutotune)
-  int kwpb[4] = {4, 4, 4, 4};
-  int kcarve[4] = {-1, -1, -1, -1};
+  // for the collide, setup, solve, adjoint and fused step kernels
+  // (odegpuBatchSetLaunchConfig / odegpuBatchAutotune)
+  int kwpb[5] = {4, 4, 4, 4, 4};
+  int kcarve[5] = {-1, -1, -1, -1, -1};
+  // a step is one world_step_kernel launch (fused) or the collide, setup and
+  // solve kernels (odegpuBatchSetStepKernels / odegpuBatchAutotune)
+  bool fused = false;
   int step_counter = 0;
   cudaStream_t stream = nullptr;
   std::vector<WorldDesc> h_world;
@@ -357,11 +395,12 @@ struct odegpuBatch {
   // the carveout is a property of the kernel function: set it when it differs
   // from what the last launch of that kernel used (any batch)
   void apply_carveout(int k) {
-    static int current[4] = {-1, -1, -1, -1};
+    static int current[5] = {-1, -1, -1, -1, -1};
     if (current[k] == kcarve[k]) return;
     const void* fn = k == 0 ? (const void*)world_collide_kernel
                    : k == 1 ? (const void*)world_setup_kernel
-                   : k == 2 ? (const void*)world_solve_kernel : (const void*)adjoint_step_kernel;
+                   : k == 2 ? (const void*)world_solve_kernel
+                   : k == 3 ? (const void*)adjoint_step_kernel : (const void*)world_step_kernel;
     if (cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, kcarve[k]) == cudaSuccess)
       current[k] = kcarve[k];
     else
@@ -532,6 +571,24 @@ struct odegpuBatch {
       if (e != cudaSuccess) return fail(ODEGPU_E_CUDA, std::string("step launch: ") + cudaGetErrorString(e));
       return 0;
     }
+    if (fused) {
+      // one launch per step; with timing on, its time is recorded in the
+      // collide slot and the setup and solve slots stay empty
+      const int wf = single_world ? 1 : kwpb[4];
+      for (int s = 0; s < n_steps; ++s) {
+        mark(tm);
+        apply_carveout(4);
+        world_step_kernel<<<(count + wf - 1) / wf, wf * 32, (size_t)wf * kStepSmemPerWarp, stream>>>(
+            d, ord, first, count, step_counter + s, opt);
+        mark(tm);
+        mark(tm);
+        mark(tm);
+        launches += 1;
+      }
+      cudaError_t e = cudaGetLastError();
+      if (e != cudaSuccess) return fail(ODEGPU_E_CUDA, std::string("step launch: ") + cudaGetErrorString(e));
+      return 0;
+    }
     for (int s = 0; s < n_steps; ++s) {
       mark(tm);
       apply_carveout(0);
@@ -555,7 +612,7 @@ struct odegpuBatch {
 };
 
 // Largest block shapes (warps per block) the launch configuration accepts.
-constexpr int kMaxWpb[4] = {4, 8, 8, 4};
+constexpr int kMaxWpb[5] = {4, 8, 8, 4, 4};
 
 static int configure_kernels() {
   if (cudaFuncSetAttribute(world_collide_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -569,6 +626,9 @@ static int configure_kernels() {
     return -1;
   if (cudaFuncSetAttribute(adjoint_step_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)(kMaxWpb[3] * kAdjSmemPerWarp)) != cudaSuccess)
+    return -1;
+  if (cudaFuncSetAttribute(world_step_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)(kMaxWpb[4] * kStepSmemPerWarp)) != cudaSuccess)
     return -1;
   if (cudaFuncSetAttribute(world_exact_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)(kExactWarps * kSmemPerWarp)) != cudaSuccess)
@@ -1033,6 +1093,7 @@ int odegpuBatchCreate(const odegpuScene* sc, const odegpuBatchConfig* cfg, odegp
   }
   if (!rc && configure_kernels() != 0) rc = fail(ODEGPU_E_CUDA, "cannot configure shared memory");
   for (int k = 0; k < 3; ++k) B->kwpb[k] = std::min(B->warps_per_block, kMaxWpb[k]);
+  B->kwpb[4] = std::min(B->warps_per_block, kMaxWpb[4]);
   if (!rc && B->lw) rc = lw_setup(B, sc);
   if (rc) { delete B; return rc; }
   *out = B;
@@ -1184,12 +1245,26 @@ int odegpuBatchGetFeedback(odegpuBatchID b, double* out) {
 }
 
 int odegpuBatchSetLaunchConfig(odegpuBatchID b, int kernel, int warps_per_block, int smem_carveout) {
-  if (!b || kernel < 0 || kernel > 3) return fail(ODEGPU_E_ARG, "bad kernel index");
+  if (!b || kernel < 0 || kernel > 4) return fail(ODEGPU_E_ARG, "bad kernel index");
   if (warps_per_block < 1 || warps_per_block > kMaxWpb[kernel])
     return fail(ODEGPU_E_ARG, "warps per block out of range for this kernel");
   if (smem_carveout < -1 || smem_carveout > 100) return fail(ODEGPU_E_ARG, "carveout must be -1 or 0..100");
   b->kwpb[kernel] = warps_per_block;
   b->kcarve[kernel] = smem_carveout;
+  return 0;
+}
+
+int odegpuBatchSetStepKernels(odegpuBatchID b, int fused) {
+  if (!b || (fused != 0 && fused != 1)) return fail(ODEGPU_E_ARG, "bad arguments");
+  b->fused = fused != 0;
+  return 0;
+}
+
+int odegpuBatchGetStepKernels(odegpuBatchID b, int* fused, int* warps_per_block, int* smem_carveout) {
+  if (!b || !fused) return fail(ODEGPU_E_ARG, "bad arguments");
+  *fused = b->fused ? 1 : 0;
+  if (warps_per_block) *warps_per_block = b->kwpb[4];
+  if (smem_carveout) *smem_carveout = b->kcarve[4];
   return 0;
 }
 
@@ -1221,6 +1296,8 @@ int odegpuBatchAutotune(odegpuBatchID b, int n_steps) {
   int best_w[3] = {b->kwpb[0], b->kwpb[1], b->kwpb[2]}, best_c[3] = {b->kcarve[0], b->kcarve[1], b->kcarve[2]};
   StepOptions opt{1, nullptr, nullptr, nullptr, 0, 0};
   b->timing = true;
+  const bool saved_fused = b->fused;
+  b->fused = false;
   int rc = 0;
   for (int wi = 0; wi < 4 && !rc; ++wi) {
     for (int ci = 0; ci < 5 && !rc; ++ci) {
@@ -1247,6 +1324,33 @@ int odegpuBatchAutotune(odegpuBatchID b, int n_steps) {
     }
   }
   for (int k = 0; k < 3; ++k) { b->kwpb[k] = best_w[k]; b->kcarve[k] = best_c[k]; }
+  // the fused step kernel: its shapes against the best split step (the sum of
+  // the three kernels' best times)
+  double best_f = INFINITY;
+  int best_fw = b->kwpb[4], best_fc = b->kcarve[4];
+  b->fused = true;
+  for (int wi = 0; wi < 4 && !rc; ++wi) {
+    if (kWpb[wi] > kMaxWpb[4]) continue;
+    for (int ci = 0; ci < 5 && !rc; ++ci) {
+      b->kwpb[4] = kWpb[wi];
+      b->kcarve[4] = kCarve[ci];
+      if ((rc = restore())) break;
+      if ((rc = b->launch(0, b->n_worlds, 1, opt))) break;
+      b->ev_used = 0;
+      if ((rc = b->launch(0, b->n_worlds, n_steps, opt))) break;
+      if (cudaStreamSynchronize(b->stream) != cudaSuccess) { rc = fail(ODEGPU_E_CUDA, "autotune step"); break; }
+      double ms = 0.0;
+      for (size_t q = 0; q + 3 < b->ev_used; q += 4) {
+        float t = 0.f;
+        cudaEventElapsedTime(&t, b->ev_pool[q], b->ev_pool[q + 1]);
+        ms += t;
+      }
+      if (ms < best_f) { best_f = ms; best_fw = kWpb[wi]; best_fc = kCarve[ci]; }
+    }
+  }
+  b->kwpb[4] = best_fw;
+  b->kcarve[4] = best_fc;
+  b->fused = rc ? saved_fused : best_f < best[0] + best[1] + best[2];
   b->ev_used = 0;
   b->timing = saved_timing;
   if (!rc) rc = restore();
@@ -1687,7 +1791,7 @@ WorldCtx* ctx_create(int device) {
   c->B.device = device;
   c->B.n_worlds = 1;
   c->B.warps_per_block = 1;
-  for (int k = 0; k < 4; ++k) c->B.kwpb[k] = 1;
+  for (int k = 0; k < 5; ++k) c->B.kwpb[k] = 1;
   if (cudaStreamCreateWithFlags(&c->B.stream, cudaStreamNonBlocking) != cudaSuccess) {
     delete c;
     fail(ODEGPU_E_CUDA, "stream creation failed");

@@ -45,6 +45,8 @@ def _declare(L):
         "odegpuBatchSetFeedback": (i, [v, i]),
         "odegpuBatchSetLaunchConfig": (i, [v, i, i, i]),
         "odegpuBatchGetLaunchConfig": (i, [v, _P(i)]),
+        "odegpuBatchSetStepKernels": (i, [v, i]),
+        "odegpuBatchGetStepKernels": (i, [v, _P(i), _P(i), _P(i)]),
         "odegpuBatchAutotune": (i, [v, i]),
         "odegpuBatchGetFeedback": (i, [v, _P(d)]),
         "odegpuBatchRolloutForward": (i, [v, i, i]),

@@ -194,13 +194,24 @@ class Batch:
         return out[:self.nj_total]
 
     def set_launch_config(self, kernel, warps_per_block, smem_carveout=-1):
-        """kernel: 0 collide, 1 setup, 2 solve, 3 adjoint."""
+        """kernel: 0 collide, 1 setup, 2 solve, 3 adjoint, 4 fused step."""
         check(lib().odegpuBatchSetLaunchConfig(self.h, int(kernel), int(warps_per_block), int(smem_carveout)))
 
     def launch_config(self):
         cfg = (C.c_int * 8)()
         check(lib().odegpuBatchGetLaunchConfig(self.h, cfg))
         return [(cfg[2 * k], cfg[2 * k + 1]) for k in range(4)]
+
+    def set_step_kernels(self, fused=True):
+        """One fused kernel per step (collide, setup and solve of each world on
+        its warp) or the three separate kernels; the results are the same."""
+        check(lib().odegpuBatchSetStepKernels(self.h, 1 if fused else 0))
+
+    def step_kernels(self):
+        """(fused, warps per block, carveout) of the step launch."""
+        f, w, c = C.c_int(), C.c_int(), C.c_int()
+        check(lib().odegpuBatchGetStepKernels(self.h, C.byref(f), C.byref(w), C.byref(c)))
+        return bool(f.value), w.value, c.value
 
     def autotune(self, n_steps=4):
         """Pick each kernel's launch shape by timing candidates on the current state."""
