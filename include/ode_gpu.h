@@ -17,9 +17,9 @@
  *  - A world of up to 64 bodies whose joints and contacts cannot need more
  *    than 1024 constraint rows steps in one on-chip kernel per phase; a
  *    larger world (up to 65536 bodies) steps through the large-world
- *    pipeline of odegpu.h with the caller's contacts. dWorldStep and joint
- *    feedback are available on the first path only: for a larger world
- *    those calls return 0.
+ *    pipeline of odegpu.h with the caller's contacts, joint feedback
+ *    included. dWorldStep is available on the first path only: for a larger
+ *    world it returns 0.
  */
 #ifndef ODE_GPU_H
 #define ODE_GPU_H

@@ -187,7 +187,9 @@ int odegpuBatchWriteStateF32Async(odegpuBatchID b, const float* state);
  * dxQuickStepper at ode/src/quickstep.cpp:918-957): SetFeedback(1) makes
  * every following step compute, for every persistent joint, f1 t1 f2 t2 =
  * J^T lambda of its rows (f2 = t2 = 0 without a second body); GetFeedback
- * copies the last step's values to out[nj_total][12] (f1[3] t1[3] f2[3] t2[3]). */
+ * copies the last step's values to out[nj_total][12] (f1[3] t1[3] f2[3] t2[3]).
+ * Both steppers and both pipelines (worlds on one warp each, and the
+ * large-world pipeline) fill it. */
 int odegpuBatchSetFeedback(odegpuBatchID b, int on);
 int odegpuBatchGetFeedback(odegpuBatchID b, double* out);
 

@@ -479,7 +479,8 @@ struct odegpuBatch {
       lw_max_scan_kernel<<<1, kLwScanThreads, 0, stream>>>(L0.bfk, L0.nj);
       lw_info2_kernel<<<g(njall, 128), 128, 0, stream>>>(d, L0, step);
       lw_tmp1_kernel<<<g(nb, T), T, 0, stream>>>(d, L0);
-      lw_row_setup_kernel<<<g(R, T), T, 0, stream>>>(d, L0);
+      const bool fb = opt.jcopy && (opt.feedback || opt.contact_feedback);
+      lw_row_setup_kernel<<<g(R, T), T, 0, stream>>>(d, L0, fb ? opt.jcopy : nullptr);
       launches += 4;
       mark(tm);
       // SOR: initial order, then per reshuffle round the exact permutation,
@@ -526,6 +527,10 @@ struct odegpuBatch {
         if (e != cudaSuccess) return fail(ODEGPU_E_CUDA, std::string("sweep launch: ") + cudaGetErrorString(e));
         ++launches;
       }
+      if (fb) {
+        lw_feedback_kernel<<<g(njall, 128), 128, 0, stream>>>(d, L0, opt.jcopy, opt.feedback, opt.contact_feedback);
+        ++launches;
+      }
       lw_integrate_kernel<<<g(nb, T), T, 0, stream>>>(d, L0);
       ++launches;
       mark(tm);
@@ -536,9 +541,9 @@ struct odegpuBatch {
   }
 
   int launch(int first, int count, int n_steps, const StepOptions& opt_in, bool use_order = true) {
-    if (lw) return lw_launch(n_steps, opt_in);
     StepOptions opt = opt_in;
     if (feedback_on) { opt.jcopy = jcopy.p; opt.feedback = feedback.p; }
+    if (lw) return lw_launch(n_steps, opt);
     const BatchDev d = dev();
     const int* ord = (use_order && order.p) ? order.p : nullptr;
     cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
@@ -1219,7 +1224,6 @@ int odegpuBatchGetKernelTimes(odegpuBatchID b, double* ms, long long* n_steps) {
 }
 
 int odegpuBatchSetFeedback(odegpuBatchID b, int on) {
-  if (b && b->lw) return fail(ODEGPU_E_ARG, "not available for a large world (one world above the on-chip limits)");
   if (!b) return fail(ODEGPU_E_ARG, "null batch");
   OG_CUDA(cudaSetDevice(b->device));
   OG_CUDA(cudaStreamSynchronize(b->stream));
@@ -1868,8 +1872,6 @@ static int ctx_step_large(WorldCtx* c, HostWorld& hw) {
     return fail(ODEGPU_E_LIMIT, "world has " + std::to_string(nb) + " bodies; at most " +
                                     std::to_string(ODEGPU_MAX_BODIES_LARGE));
   if (hw.exact) return fail(ODEGPU_E_ARG, "dWorldStep is not available for a world above 64 bodies or 1024 rows");
-  if (hw.want_feedback)
-    return fail(ODEGPU_E_ARG, "joint feedback is not available for a world above 64 bodies or 1024 rows");
   WorldDesc D = hw.desc;
   D.body_off = D.geom_off = D.joint_off = D.contact_off = D.row_off = D.padj_off = 0;
   D.ng = 0;
@@ -1897,8 +1899,27 @@ static int ctx_step_large(WorldCtx* c, HostWorld& hw) {
     }
     c->lw_nb = nb; c->lw_njp = D.njp; c->lw_ccap = D.contact_cap;
   }
-  const StepOptions opt{0, nullptr, nullptr, nullptr, 1, 1};
+  StepOptions opt{0, nullptr, nullptr, nullptr, 1, 1};
+  if (hw.want_feedback) {
+    int rc = grow(B.jcopy, (size_t)D.row_cap * 12);
+    rc = rc ? rc : grow(B.feedback, (size_t)std::max(1, D.njp) * 12);
+    rc = rc ? rc : grow(c->contact_fb, (size_t)std::max(1, D.contact_cap) * 12);
+    if (rc) return rc;
+    opt.jcopy = B.jcopy.p;
+    opt.feedback = B.feedback.p;
+    opt.contact_feedback = c->contact_fb.p;
+  }
   if (int e = B.launch(0, 1, 1, opt, false)) return e;
+  if (hw.want_feedback) {
+    hw.feedback.resize((size_t)D.njp * 12);
+    hw.contact_feedback.resize((size_t)nc * 12);
+    if (!hw.feedback.empty())
+      OG_CUDA(cudaMemcpyAsync(hw.feedback.data(), B.feedback.p, hw.feedback.size() * sizeof(float),
+                              cudaMemcpyDeviceToHost, B.stream));
+    if (!hw.contact_feedback.empty())
+      OG_CUDA(cudaMemcpyAsync(hw.contact_feedback.data(), c->contact_fb.p,
+                              hw.contact_feedback.size() * sizeof(float), cudaMemcpyDeviceToHost, B.stream));
+  }
   return ctx_download(B, hw);
 }
 

@@ -601,11 +601,12 @@ __global__ void lw_tmp1_kernel(BatchDev d, LWDev L) {
   body_tmp1(d, D.body_off + b, 1.0f / D.dt, L.tmp1 + 6 * (size_t)b);
 }
 
-__global__ void lw_row_setup_kernel(BatchDev d, LWDev L) {
+// jcopy (optional): J of every row before scaling, kept for joint feedback
+__global__ void lw_row_setup_kernel(BatchDev d, LWDev L, float* jcopy) {
   const WorldDesc D = d.world[0];
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= d.nrows[0]) return;
-  row_setup(d, D, r, L.tmp1, 1.0f / D.dt, D.sor_w, nullptr, nullptr);
+  row_setup(d, D, r, L.tmp1, 1.0f / D.dt, D.sor_w, nullptr, jcopy);
 }
 
 // ---------------------------------------------------------------- SOR order
@@ -1123,6 +1124,40 @@ __global__ void __launch_bounds__(kLwSweepThreads) lw_sweep_kernel(BatchDev d, L
 }
 
 // ---------------------------------------------------------------- integration
+// Joint feedback (quickstep.cpp:918-957, Multiply1_12q1 :70-101), a thread per
+// island-ordered joint: f1 t1 = J1^T lambda and f2 t2 = J2^T lambda over the
+// joint's rows in order, J as getInfo2 produced it (jcopy); f2 = t2 = 0
+// without a second body. Persistent joints into feedback[joint][12], contact
+// joints into contact_feedback[contact][12] (either may be null).
+__global__ void lw_feedback_kernel(BatchDev d, LWDev L, const float* jcopy, float* feedback,
+                                   float* contact_feedback) {
+  const WorldDesc D = d.world[0];
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (d.nrows[0] == 0 || k >= *L.nj) return;
+  const int ord = L.jlist[k];
+  float* o;
+  int b2;
+  if (ord < D.njp) {
+    if (!feedback) return;
+    o = feedback + (size_t)(D.joint_off + ord) * 12;
+    b2 = d.joints[D.joint_off + ord].b2;
+  } else {
+    if (!contact_feedback) return;
+    o = contact_feedback + (size_t)(D.contact_off + ord - D.njp) * 12;
+    b2 = d.contacts[D.contact_off + ord - D.njp].b2;
+  }
+  float f[12];
+  for (int q = 0; q < 12; ++q) f[q] = 0.f;
+  for (int r = L.jm[k]; r < L.jm[k + 1]; ++r) {
+    const float s = L.lambda[r];
+    const float* J = jcopy + (size_t)(D.row_off + r) * 12;
+    for (int q = 0; q < 12; ++q) f[q] += J[q] * s;
+  }
+  if (b2 < 0)
+    for (int q = 6; q < 12; ++q) f[q] = 0.f;
+  for (int q = 0; q < 12; ++q) o[q] = f[q];
+}
+
 __global__ void lw_integrate_kernel(BatchDev d, LWDev L) {
   const WorldDesc D = d.world[0];
   const int b = blockIdx.x * blockDim.x + threadIdx.x;

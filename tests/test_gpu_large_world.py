@@ -47,6 +47,38 @@ def test_large_path_matches_warp_path(name):
     assert np.abs(a[0] - b[0]).max() < 1e-5, float(np.abs(a[0] - b[0]).max())
 
 
+@pytest.mark.parametrize("name", ["chains", "hinges"])
+def test_large_path_feedback_matches_warp_path(name):
+    """Joint feedback (quickstep.cpp:918-957) from the large-world pipeline
+    against the warp-per-world path, which the parity tests check against the
+    oracle: ball chains of the batched configuration and a hinge chain with
+    per-step torques touching a plane; 30 steps, the feedback of every step
+    within 1e-4 of its scale, and persistent joints only (as ODE's
+    dJointFeedback of persistent joints)."""
+    from odegpu.batch import Batch
+    sc = {
+        "chains": lambda: S.batched_worlds(n_worlds=1, seed=5, nmin=40, nmax=60),
+        "hinges": lambda: S.hinge_chains(n_worlds=1, links=12, seed=3, steps=30, plane_z=-1.0),
+    }[name]()
+    A = Batch(sc, large_world=False)
+    Lw = Batch(sc, large_world=True)
+    for B in (A, Lw):
+        B.set_feedback(True)
+    worst = 0.0
+    for _ in range(30):
+        A.step(1)
+        Lw.step(1)
+        fa, fl = A.feedback(), Lw.feedback()
+        scale = max(1.0, float(np.abs(fa).max()))
+        worst = max(worst, float(np.abs(fa - fl).max()) / scale)
+    assert sc.nj_total > 0
+    assert (A.status() == 0).all() and (Lw.status() == 0).all()
+    assert np.array_equal(A.counts()[0], Lw.counts()[0])
+    assert worst < 1e-4, worst
+    A.close()
+    Lw.close()
+
+
 POS_ATOL = 2e-5
 Q_ATOL = 2e-5
 VEL_ATOL = 5e-3

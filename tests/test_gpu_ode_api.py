@@ -549,3 +549,81 @@ def test_worlds_above_64_bodies_step_through_large_pipeline():
         U.player_input(chain, 0, 2, inp)
         with pytest.raises(subprocess.CalledProcessError):
             U.run_demo(exe, inp, "exact")
+
+
+def test_joint_feedback_above_64_bodies():
+    """dJointSetFeedback on an 80-link ball chain (above the on-chip kernel's
+    64 bodies, so dWorldQuickStep steps it through the large-world pipeline),
+    swinging from the environment: after each of five steps every joint's
+    feedback equals that of the batched path stepping the same world through
+    the same pipeline (which test_gpu_large_world.py checks against the
+    warp-per-world path), f2 = t2 = 0 for the joint to the environment, and
+    the top joint pulls the chain up."""
+    from odegpu._lib import lib
+    from odegpu.batch import Batch
+    L = lib()
+    f, v, i = C.c_float, C.c_void_p, C.c_int
+    L.dWorldCreate.restype = v
+    L.dWorldSetGravity.argtypes = [v, f, f, f]
+    L.dWorldSetCFM.argtypes = [v, f]
+    L.dBodyCreate.restype = v; L.dBodyCreate.argtypes = [v]
+    L.dBodySetPosition.argtypes = [v, f, f, f]
+    L.dBodySetLinearVel.argtypes = [v, f, f, f]
+    L.dBodyGetPosition.restype = C.POINTER(f); L.dBodyGetPosition.argtypes = [v]
+    L.dMassSetSphereTotal.argtypes = [C.POINTER(Mass), f, f]
+    L.dBodySetMass.argtypes = [v, C.POINTER(Mass)]
+    L.dJointCreateBall.restype = v; L.dJointCreateBall.argtypes = [v, v]
+    L.dJointAttach.argtypes = [v, v, v]
+    L.dJointSetBallAnchor.argtypes = [v, f, f, f]
+    L.dJointSetFeedback.argtypes = [v, C.POINTER(JointFeedback)]
+    L.dWorldQuickStep.restype = i; L.dWorldQuickStep.argtypes = [v, f]
+    L.dRandSetSeed.argtypes = [C.c_ulong]
+    L.dWorldDestroy.argtypes = [v]
+    n, m, r = 80, 2.0, 0.1
+    vx = [0.3 * np.sin(0.7 * k) for k in range(n)]
+    w = L.dWorldCreate()
+    L.dWorldSetGravity(w, 0.0, 0.0, -9.81)
+    L.dWorldSetCFM(w, 1e-5)
+    bodies, fbs = [], []
+    for k in range(n):
+        b = L.dBodyCreate(w)
+        L.dBodySetPosition(b, 0.0, 0.0, -0.5 - k)
+        L.dBodySetLinearVel(b, vx[k], 0.0, 0.0)
+        M = Mass()
+        L.dMassSetSphereTotal(C.byref(M), m, r)
+        L.dBodySetMass(b, C.byref(M))
+        bodies.append(b)
+    for k in range(n):
+        j = L.dJointCreateBall(w, None)
+        L.dJointAttach(j, bodies[k], bodies[k - 1] if k > 0 else None)
+        L.dJointSetBallAnchor(j, 0.0, 0.0, -float(k))
+        fb = JointFeedback()
+        L.dJointSetFeedback(j, C.byref(fb))
+        fbs.append(fb)
+    # the same world for the batched path
+    sb = S.SceneBuilder()
+    S._std_surface(sb)
+    ws = sb.new_world(cfm=1e-5, seed=0)
+    for k in range(n):
+        mm, I = S.sphere_mass_total(m, r)
+        sb.add_body(ws, (0.0, 0.0, -0.5 - k), mm, I, lvel=(vx[k], 0.0, 0.0))
+    for k in range(n):
+        sb.add_joint(ws, S.JOINT_BALL, k, k - 1 if k > 0 else -1, anchor=(0.0, 0.0, -float(k)),
+                     param=(0.2, 1e-5))
+    B = Batch(sb.build())
+    B.set_feedback(True)
+    L.dRandSetSeed(0)
+    for s in range(5):
+        assert L.dWorldQuickStep(w, 0.01) == 1
+        B.step(1)
+        ref = B.feedback()
+        got = np.array([list(fb.f1[:3]) + list(fb.t1[:3]) + list(fb.f2[:3]) + list(fb.t2[:3]) for fb in fbs])
+        scale = max(1.0, float(np.abs(ref).max()))
+        assert np.abs(got - ref).max() < 1e-4 * scale, (s, float(np.abs(got - ref).max()), scale)
+        assert np.all(got[0, 6:] == 0.0)
+        pos = np.array([L.dBodyGetPosition(b)[k] for b in bodies for k in range(3)]).reshape(n, 3)
+        assert np.abs(pos - B.state()[:, 0:3]).max() < 1e-5
+    assert got[0, 2] > 0.0
+    assert (B.status() == 0).all()
+    B.close()
+    L.dWorldDestroy(w)
