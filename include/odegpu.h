@@ -33,8 +33,10 @@ enum {
   ODEGPU_ST_ROW_OVERFLOW = 2,
   ODEGPU_ST_TOO_LARGE = 4,
   ODEGPU_ST_NONFINITE = 8,
-  /* a geom covered more than 10 x 10 heightfield samples (the collider's
-     buffer); that pair produced no contacts in the step */
+  /* a geom covered more heightfield samples than the collider holds (10 x 10
+     in the lane, or the world's workspace, at most 128 x 128, for worlds
+     whose geoms can cover more than 10 samples per axis); that pair produced
+     no contacts in the step */
   ODEGPU_ST_HF_ZONE = 32,
   /* large world: a geom had more than 64 candidate partners, or the
      candidate pairs exceeded the batch's pair capacity; pairs were dropped */
@@ -253,7 +255,7 @@ typedef struct {
   int geom;            /* world-local geom index of the nearest hit; -1: no hit;
                           -2: invalid ray (world / body out of range, length
                           negative or not finite); -3: a heightfield zone under
-                          the ray exceeds the collider's buffers */
+                          the ray exceeds the lane's 10 x 10 samples */
   float pos[3];        /* dContactGeom pos, normal, depth of dCollide(ray, geom) */
   float normal[3];
   float depth;

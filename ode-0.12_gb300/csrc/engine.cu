@@ -240,6 +240,7 @@ struct odegpuBatch {
   DBuf<float> rows;
   DBuf<float4> sweep;                // forward sweep buffers (sor_fwd.cuh)
   DBuf<unsigned char> fwd_scratch;
+  DBuf<unsigned char> hf_ws;          // heightfield zone workspaces (WorldDesc::hf_ws)
   DBuf<int> jlist, adj, adj_start, island_jstart, island_rstart, jrow, jm;
   DBuf<float> state_scratch;
   DBuf<odegpuRay> ray_in;          // odegpuBatchRayCast staging, grown on demand
@@ -314,6 +315,7 @@ struct odegpuBatch {
     d.joint_stop = n_ctrl_steps > 0 ? joint_stop.p : nullptr;
     d.step_counter_base = 0;
     d.contacts = contacts.p; d.rows = rows.p; d.sweep = sweep.p; d.fwd_scratch = fwd_scratch.p;
+    d.hf_ws = hf_ws.p;
     d.jlist = jlist.p; d.adj = adj.p;
     d.adj_start = adj_start.p; d.island_jstart = island_jstart.p; d.island_rstart = island_rstart.p;
     d.jrow = jrow.p; d.jm = jm.p;
@@ -458,6 +460,10 @@ struct odegpuBatch {
         scan(L0.own, nullptr, ng);
         lw_pairs_fill_kernel<<<g(ng, T), T, 0, stream>>>(d, L0);
         lw_narrow_kernel<<<g(L0.pair_cap, 128), 128, 0, stream>>>(d, L0);
+        if (D.hf_ws_side > 0) {
+          lw_hf_big_kernel<<<1, 32, 0, stream>>>(d, L0);
+          ++launches;
+        }
         scan(L0.pnc, L0.npairs, 0);
         lw_contacts_kernel<<<g(L0.pair_cap, T), T, 0, stream>>>(d, L0);
         launches += 3;
@@ -654,6 +660,25 @@ static float bound_radius(int type, const double* p) {
     default: return INFINITY;
   }
 }
+
+// Half-extent bound, under any rotation, of the axis-aligned box that the
+// reference computes for a geom (computeAABB: sphere.cpp:59-67, box.cpp:60-78,
+// capsule.cpp:60-74, cylinder.cpp:58-73, ray.cpp:56-89): sizes the
+// heightfield zones a geom can cover.
+static double aabb_half_bound(int type, const double* p) {
+  switch (type) {
+    case ODEGPU_GEOM_RAY: return 0.5 * p[0];
+    case ODEGPU_GEOM_SPHERE: return p[0];
+    case ODEGPU_GEOM_BOX: return 0.5 * std::sqrt(p[0] * p[0] + p[1] * p[1] + p[2] * p[2]);
+    case ODEGPU_GEOM_CAPSULE: return p[0] + 0.5 * p[1];
+    case ODEGPU_GEOM_CYLINDER: return std::sqrt(2.0 * p[0] * p[0] + 0.25 * p[1] * p[1]);
+    default: return 0.0;
+  }
+}
+// Samples per axis of the largest zone under a geom of that bound on a field
+// of sample spacing s: the floor and ceiling of the box's ends over the
+// spacing, each widened by one ulp (heightfield.cpp:1742-1760), plus one.
+static int hf_zone_side(double half, double s) { return (int)std::floor(2.0 * half / s + 3.0) + 1; }
 
 static int set_joint_stops(odegpuBatch* B, int n_ctrl, const double* js) {
   if (B->joint_stop.p) { cudaFree(B->joint_stop.p); B->joint_stop.p = nullptr; }
@@ -937,7 +962,7 @@ int odegpuBatchCreate(const odegpuScene* sc, const odegpuBatchConfig* cfg, odegp
   std::vector<DevJoint> joints(std::max(1, B->nj_total));
   std::vector<int> padj_start((size_t)NB + W);
   std::vector<int> padj;
-  long long contact_off = 0, row_off = 0;
+  long long contact_off = 0, row_off = 0, hf_ws_total = 0;
   int n_fwd_scratch = 0;
   for (int w = 0; w < W; ++w) {
     const odegpuWorldParams& P = sc->world[w];
@@ -975,6 +1000,30 @@ int odegpuBatchCreate(const odegpuScene* sc, const odegpuBatchConfig* cfg, odegp
     if (large) B->lw = new LargeWorld();
     row_off += D.row_cap;
     D.fwd_scratch = (!large && D.row_cap > kFwdRows) ? n_fwd_scratch++ : -1;
+    // a heightfield workspace for worlds whose geoms can cover more samples
+    // than the lane's arrays hold
+    {
+      double smin = INFINITY, half = 0.0;
+      for (int g = D.geom_off; g < D.geom_off + D.ng; ++g) {
+        const double* gp = sc->geom_param + ODEGPU_GEOM_NPARAM * (size_t)g;
+        if (gtype[g] == ODEGPU_GEOM_HEIGHTFIELD) {
+          const DevHeightfield& F = hfs[(int)gp[0]];
+          smin = std::min(smin, (double)std::min(F.sw, F.sd));
+        } else if (gbody[g] >= 0) {
+          half = std::max(half, aabb_half_bound(gtype[g], gp));
+        }
+      }
+      D.hf_ws_side = 0;
+      D.hf_ws = -1;
+      if (smin < INFINITY && half > 0.0) {
+        const int side = hf_zone_side(half, smin);
+        if (side > kHFZone) {
+          D.hf_ws_side = std::min(side, kHFBigZone);
+          D.hf_ws = hf_ws_total;
+          hf_ws_total += (og::hf_ws_bytes(D.hf_ws_side) + 255) & ~255LL;
+        }
+      }
+    }
     D.max_contacts = P.max_contacts;
     D.iterations = P.iterations;
     for (int k = 0; k < 3; ++k) D.gravity[k] = (float)P.gravity[k];
@@ -1077,6 +1126,7 @@ int odegpuBatchCreate(const odegpuScene* sc, const odegpuBatchConfig* cfg, odegp
   rc = rc ? rc : B->rows.alloc((size_t)row_off * kRowWords);
   rc = rc ? rc : B->sweep.alloc(((size_t)row_off + 32 * (size_t)W) * 8);
   rc = rc ? rc : B->fwd_scratch.alloc((size_t)std::max(1, n_fwd_scratch) * kFwdScratchPerWorld);
+  if (hf_ws_total > 0) rc = rc ? rc : B->hf_ws.alloc((size_t)hf_ws_total);
   rc = rc ? rc : B->jlist.alloc(jl_total);
   rc = rc ? rc : B->jrow.alloc(jl_total);
   rc = rc ? rc : B->jm.alloc(jl_total);
@@ -2003,10 +2053,10 @@ DevHeightfield make_dev_heightfield(int nx, int nz, double width, double depth, 
 }
 
 __global__ void collide_hf_kernel(DevHeightfield H, const float* heights, GeomView g, unsigned flags, Contact* out,
-                                  int* n) {
+                                  int* n, HFBig big) {
   if (threadIdx.x == 0 && blockIdx.x == 0) {
     Contact c[8];
-    int k = collide_heightfield(H, heights, g, flags, c, nullptr);
+    int k = collide_heightfield(H, heights, g, flags, c, nullptr, big);
     if (k < 0) k = -1;
     for (int i = 0; i < k; ++i) out[i] = c[i];
     *n = k;
@@ -2030,18 +2080,35 @@ void free_heights(float* dev) {
   if (dev) cudaFree(dev);
 }
 
+// dCollide(heightfield, g): the zone in the thread's arrays, or, when the geom
+// covers more samples than they hold, in a workspace allocated for the call
+// (up to kHFBigZone samples per axis).
 int collide_hf_gpu(const DevHeightfield& H, const float* d_heights, const GeomView& g, unsigned flags, Contact* out) {
+  const double gp[4] = {g.p[0], g.p[1], g.p[2], g.p[3]};
+  const int side = hf_zone_side(aabb_half_bound(g.type, gp), std::min(H.sw, H.sd));
+  HFBig big{nullptr, 0};
+  if (side > kHFZone) {
+    big.side = std::min(side, kHFBigZone);
+    OG_CUDA(cudaMalloc(&big.ws, (size_t)hf_ws_bytes(big.side)));
+  }
   Contact* d_c = nullptr;
-  OG_CUDA(cudaMalloc(&d_c, 8 * sizeof(Contact) + sizeof(int)));
+  if (cudaMalloc(&d_c, 8 * sizeof(Contact) + sizeof(int)) != cudaSuccess) {
+    cudaGetLastError();
+    if (big.ws) cudaFree(big.ws);
+    return fail(ODEGPU_E_NOMEM, "dCollide staging allocation failed");
+  }
   int* d_n = reinterpret_cast<int*>(d_c + 8);
-  collide_hf_kernel<<<1, 32>>>(H, d_heights, g, flags, d_c, d_n);
+  collide_hf_kernel<<<1, 32>>>(H, d_heights, g, flags, d_c, d_n, big);
   int n = 0;
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaMemcpy(&n, d_n, sizeof(int), cudaMemcpyDeviceToHost);
   if (e == cudaSuccess && n > 0) e = cudaMemcpy(out, d_c, n * sizeof(Contact), cudaMemcpyDeviceToHost);
   cudaFree(d_c);
+  if (big.ws) cudaFree(big.ws);
   if (e != cudaSuccess) return fail(ODEGPU_E_CUDA, cudaGetErrorString(e));
-  if (n < 0) return fail(ODEGPU_E_LIMIT, "the geom covers more than 10 x 10 heightfield samples");
+  if (n < 0)
+    return fail(ODEGPU_E_LIMIT, "the geom covers more than " + std::to_string(kHFBigZone) + " x " +
+                                    std::to_string(kHFBigZone) + " heightfield samples");
   return n;
 }
 

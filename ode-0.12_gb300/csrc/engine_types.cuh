@@ -107,6 +107,8 @@ struct WorldDesc {
   int max_contacts;
   int iterations;
   float gravity[3], erp, cfm, sor_w, max_vel, min_depth, dt;
+  int hf_ws_side;               // samples per axis of the world's heightfield workspace (0: none)
+  long long hf_ws;              // its byte offset in BatchDev::hf_ws
 };
 
 struct BatchDev {
@@ -155,6 +157,7 @@ struct BatchDev {
   float4* sweep;                       // per world (row_cap + 32) x 8 float4: the rows of the
                                        // current reshuffle round in execution order, quad-major
   unsigned char* fwd_scratch;          // row-indexed SOR arrays of worlds with a large row capacity
+  unsigned char* hf_ws;                // heightfield zone workspaces of worlds whose geoms need one
   int* jlist;                          // [njp + contact_cap per world] island order
   int* adj;                            // [2 * (njp + contact_cap) per world]
   int* adj_start;                      // [nb_total + n_worlds]

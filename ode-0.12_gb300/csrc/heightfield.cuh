@@ -11,8 +11,10 @@
 // if it lies over one of the plane's triangles (IsOnHeightfield2). Geoms
 // larger than 1.5 cells then test the remaining triangle vertices with the
 // geom's point-depth function. The edge pass is compiled out in the
-// reference and here. The zone is limited to kHFZone x kHFZone samples; a
-// larger one reports overflow and yields no contacts.
+// reference and here. Zones of up to kHFZone x kHFZone samples live in the
+// lane's local memory; a larger zone needs a workspace in global memory from
+// the caller (HFBig, up to kHFBigZone samples per axis), else it reports
+// overflow and yields no contacts.
 #pragma once
 #include "collide.cuh"
 #include "engine_types.cuh"
@@ -151,17 +153,99 @@ OG_D int geom_plane_collide(const GeomView& g, const GeomView& pl, unsigned flag
   return collide_capsule_plane(g, pl, flags, c);
 }
 
-// dCollideHeightfieldZone (heightfield.cpp:952-1676); g in heightfield space.
-// Returns the contact count, or -1 when the zone exceeds the lane buffers.
-OG_D int hf_zone(const DevHeightfield& H, const float* heights, int minX, int maxX, int minZ, int maxZ,
-                 const GeomView& g, const float* aabb, int max_contacts, unsigned flags, Contact* out,
-                 unsigned& kinds) {
-  kinds = 0u;
-  const int numX = (maxX - minX) + 1, numZ = (maxZ - minZ) + 1;
-  if (numX > kHFZone || numZ > kHFZone || numX < 1 || numZ < 1) return -1;
-  const float minO2 = aabb[2], maxO2 = aabb[3];
+// Working arrays of one zone (the reference's tempHeightBuffer,
+// tempTriangleBuffer and tempPlaneBuffer, heightfield.cpp:1120-1140). A
+// triangle's vertex indices are packed in a TV word, kTVBits bits each, with
+// its "up" flag above them; Idx holds triangle and plane indices.
+//   HFLocalZone: zones of up to kHFZone x kHFZone samples, in the lane's local
+//     memory (every zone of the workloads' geoms);
+//   HFGlobalZone: larger zones, up to kHFBigZone samples per axis, in a
+//     workspace in global memory that the caller owns.
+struct HFLocalZone {
+  using TV = unsigned;
+  using Idx = unsigned char;
+  static constexpr int kTVBits = 8;
   float vh[kHFZone * kHFZone];           // sample heights of the zone
   unsigned char vstate[kHFZone * kHFZone];
+  TV tv[kHFMaxTri];
+  float4 tp[kHFMaxTri];                  // plane (n, d)
+  float tmax[kHFMaxTri];                 // highest vertex
+  unsigned char tstate[kHFMaxTri];
+  Idx members[kHFMaxTri];                // triangles, grouped by plane
+  Idx pfirst[kHFMaxTri], pcount[kHFMaxTri];
+  float pmax[kHFMaxTri];
+  Idx porder[kHFMaxTri];                 // planes in sorted order
+};
+constexpr int kHFBigZone = 128;          // samples per axis of a global workspace, at most
+struct HFGlobalZone {
+  using TV = unsigned long long;
+  using Idx = unsigned short;
+  static constexpr int kTVBits = 16;
+  float* vh;
+  unsigned char* vstate;
+  TV* tv;
+  float4* tp;
+  float* tmax;
+  unsigned char* tstate;
+  Idx* members;
+  Idx* pfirst;
+  Idx* pcount;
+  float* pmax;
+  Idx* porder;
+};
+static_assert(kHFZone * kHFZone <= 256 && kHFMaxTri <= 255, "local zone indices are 8-bit");
+static_assert(kHFBigZone * kHFBigZone <= 65536 && 2 * (kHFBigZone - 1) * (kHFBigZone - 1) <= 65535,
+              "global zone indices are 16-bit");
+
+// Bytes of a global workspace for zones of up to side x side samples.
+OG_HD constexpr long long hf_ws_align(long long n) { return (n + 15) & ~15LL; }
+OG_HD constexpr long long hf_ws_bytes(int side) {
+  return hf_ws_align(4LL * side * side) + hf_ws_align(1LL * side * side) +
+         hf_ws_align(8LL * 2 * (side - 1) * (side - 1)) + hf_ws_align(16LL * 2 * (side - 1) * (side - 1)) +
+         hf_ws_align(4LL * 2 * (side - 1) * (side - 1)) + hf_ws_align(1LL * 2 * (side - 1) * (side - 1)) +
+         3 * hf_ws_align(2LL * 2 * (side - 1) * (side - 1)) + hf_ws_align(4LL * 2 * (side - 1) * (side - 1)) +
+         hf_ws_align(2LL * 2 * (side - 1) * (side - 1));
+}
+OG_D HFGlobalZone carve_hf_ws(unsigned char* p, int side) {
+  const long long S = (long long)side * side, T = 2LL * (side - 1) * (side - 1);
+  HFGlobalZone z;
+  z.vh = reinterpret_cast<float*>(p); p += hf_ws_align(4 * S);
+  z.vstate = p; p += hf_ws_align(S);
+  z.tv = reinterpret_cast<HFGlobalZone::TV*>(p); p += hf_ws_align(8 * T);
+  z.tp = reinterpret_cast<float4*>(p); p += hf_ws_align(16 * T);
+  z.tmax = reinterpret_cast<float*>(p); p += hf_ws_align(4 * T);
+  z.tstate = p; p += hf_ws_align(T);
+  z.members = reinterpret_cast<unsigned short*>(p); p += hf_ws_align(2 * T);
+  z.pfirst = reinterpret_cast<unsigned short*>(p); p += hf_ws_align(2 * T);
+  z.pcount = reinterpret_cast<unsigned short*>(p); p += hf_ws_align(2 * T);
+  z.pmax = reinterpret_cast<float*>(p); p += hf_ws_align(4 * T);
+  z.porder = reinterpret_cast<unsigned short*>(p);
+  return z;
+}
+
+// A workspace for zones above kHFZone x kHFZone samples: ws (16-byte aligned,
+// hf_ws_bytes(side) bytes) or null when the caller has none.
+struct HFBig {
+  unsigned char* ws;
+  int side;
+};
+
+// dCollideHeightfieldZone (heightfield.cpp:952-1676); g in heightfield space,
+// the zone's arrays in Z (which the caller has checked holds the zone).
+// Returns the contact count.
+template <class Z>
+OG_D int hf_zone(Z& z, const DevHeightfield& H, const float* heights, int minX, int maxX, int minZ, int maxZ,
+                 const GeomView& g, const float* aabb, int max_contacts, unsigned flags, Contact* out,
+                 unsigned& kinds) {
+  using TV = typename Z::TV;
+  using Idx = typename Z::Idx;
+  constexpr int kB = Z::kTVBits;
+  constexpr TV kM = (TV(1) << kB) - 1;
+  kinds = 0u;
+  const int numX = (maxX - minX) + 1, numZ = (maxZ - minZ) + 1;
+  const float minO2 = aabb[2], maxO2 = aabb[3];
+  float* vh = z.vh;
+  unsigned char* vstate = z.vstate;
   float maxY = -INFINITY, minY = INFINITY;
   for (int xl = 0; xl < numX; ++xl)
     for (int zl = 0; zl < numZ; ++zl) {
@@ -184,11 +268,11 @@ OG_D int hf_zone(const DevHeightfield& H, const float* heights, int minX, int ma
     if (xratio > 1.5f) further = true;
     else if ((aabb[5] - aabb[4]) * H.inv_sd > 1.5f) further = true;
   }
-  // triangles: vertex indices packed as i0 | i1 << 8 | i2 << 16 | up << 24
-  unsigned tv[kHFMaxTri];
-  float4 tp[kHFMaxTri];                  // plane (n, d)
-  float tmax[kHFMaxTri];                 // highest vertex
-  unsigned char tstate[kHFMaxTri];
+  // triangles: vertex indices packed as i0 | i1 << kB | i2 << 2kB | up << 3kB
+  TV* tv = z.tv;
+  float4* tp = z.tp;
+  float* tmax = z.tmax;
+  unsigned char* tstate = z.tstate;
   int numTri = 0;
   const int maxXl = maxX - minX, maxZl = maxZ - minZ;
   for (int xl = 0; xl < maxXl; ++xl) {
@@ -199,14 +283,14 @@ OG_D int hf_zone(const DevHeightfield& H, const float* heights, int minX, int ma
       const bool ac = ah > minO2, bc = bh > minO2, cc = ch > minO2, dc = dh > minO2;
       vstate[ia] = !ac; vstate[ib] = !bc; vstate[ic] = !cc; vstate[id] = !dc;
       if (ac || bc || cc) {
-        tv[numTri] = (unsigned)ia | ((unsigned)ib << 8) | ((unsigned)ic << 16) | (1u << 24);
+        tv[numTri] = (TV)ia | ((TV)ib << kB) | ((TV)ic << (2 * kB)) | (TV(1) << (3 * kB));
         float m = ah > bh ? ah : bh;
         tmax[numTri] = ch > m ? ch : m;
         tstate[numTri] = 0;
         ++numTri;
       }
       if (bc || cc || dc) {
-        tv[numTri] = (unsigned)id | ((unsigned)ib << 8) | ((unsigned)ic << 16);
+        tv[numTri] = (TV)id | ((TV)ib << kB) | ((TV)ic << (2 * kB));
         float m = dh > bh ? dh : bh;
         tmax[numTri] = ch > m ? ch : m;
         tstate[numTri] = 0;
@@ -227,29 +311,30 @@ OG_D int hf_zone(const DevHeightfield& H, const float* heights, int minX, int ma
   // pass 1: planes of the triangles
   for (int k = 0; k < numTri; ++k) {
     float v0[3], v1[3], v2[3];
-    vtx(tv[k] & 0xff, v0);
-    vtx((tv[k] >> 8) & 0xff, v1);
-    vtx((tv[k] >> 16) & 0xff, v2);
+    vtx((int)(tv[k] & kM), v0);
+    vtx((int)((tv[k] >> kB) & kM), v1);
+    vtx((int)((tv[k] >> (2 * kB)) & kM), v2);
     const float e1[3] = {v2[0] - v0[0], v2[1] - v0[1], v2[2] - v0[2]};
     const float e2[3] = {v1[0] - v0[0], v1[1] - v0[1], v1[2] - v0[2]};
     float n[3];
-    if (tv[k] >> 24) cross3(n, e1, e2);
+    if (tv[k] >> (3 * kB)) cross3(n, e1, e2);
     else cross3(n, e2, e1);
     const float il = 1.0f / sqrtf(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
     n[0] *= il; n[1] *= il; n[2] *= il;
     tp[k] = make_float4(n[0], n[1], n[2], dot3(n, v0));
   }
   // group by equal plane definition, in triangle order
-  unsigned char members[kHFMaxTri];      // triangles, grouped by plane
-  unsigned char pfirst[kHFMaxTri], pcount[kHFMaxTri];
-  float pmax[kHFMaxTri];
-  unsigned char porder[kHFMaxTri];       // planes in sorted order
+  Idx* members = z.members;             // triangles, grouped by plane
+  Idx* pfirst = z.pfirst;
+  Idx* pcount = z.pcount;
+  float* pmax = z.pmax;
+  Idx* porder = z.porder;               // planes in sorted order
   int numPlanes = 0, nmem = 0;
   for (int k = 0; k < numTri; ++k) {
     if (tstate[k]) continue;
     const float4 b = tp[k];
-    pfirst[numPlanes] = (unsigned char)nmem;
-    members[nmem++] = (unsigned char)k;
+    pfirst[numPlanes] = (Idx)nmem;
+    members[nmem++] = (Idx)k;
     int cnt = 1;
     float mx = tmax[k];
     for (int m = k + 1; m < numTri; ++m) {
@@ -257,16 +342,16 @@ OG_D int hf_zone(const DevHeightfield& H, const float* heights, int minX, int ma
       const float4 t = tp[m];
       if (fabsf(b.y - t.y) < kHFEps && fabsf(b.w - t.w) < kHFEps && fabsf(b.x - t.x) < kHFEps &&
           fabsf(b.z - t.z) < kHFEps) {
-        members[nmem++] = (unsigned char)m;
+        members[nmem++] = (Idx)m;
         ++cnt;
         tstate[m] = 1;
         if (tmax[m] > mx) mx = tmax[m];
       }
     }
     tstate[k] = 1;
-    pcount[numPlanes] = (unsigned char)cnt;
+    pcount[numPlanes] = (Idx)cnt;
     pmax[numPlanes] = mx;
-    porder[numPlanes] = (unsigned char)numPlanes;
+    porder[numPlanes] = (Idx)numPlanes;
     ++numPlanes;
   }
   // sortPlanes (heightfield.cpp:910-932) bubble-sorts the planes, swapping
@@ -275,7 +360,7 @@ OG_D int hf_zone(const DevHeightfield& H, const float* heights, int minX, int ma
   // and yields the same order whenever heights are equal or further apart
   // than dEpsilon; it needs far fewer passes.
   for (int i = 1; i < numPlanes; ++i) {
-    const unsigned char cur = porder[i];
+    const Idx cur = porder[i];
     const float key = pmax[cur];
     int j = i;
     while (j > 0 && (pmax[porder[j - 1]] - key) > kHFEps) {
@@ -298,11 +383,11 @@ OG_D int hf_zone(const DevHeightfield& H, const float* heights, int minX, int ma
     for (int i = 0; i < npc; ++i) {
       for (int bq = 0; bq < pcount[P]; ++bq) {
         const int t = members[pfirst[P] + bq];
-        const int i0 = tv[t] & 0xff;
+        const int i0 = (int)(tv[t] & kM);
         float corner[3];
         vtx(i0, corner);
         const int xl = i0 / numZ, zl = i0 - xl * numZ;
-        if (hf_on_triangle(H, corner, minX + xl, minZ + zl, pc[i].pos, (tv[t] >> 24) != 0)) {
+        if (hf_on_triangle(H, corner, minX + xl, minZ + zl, pc[i].pos, (tv[t] >> (3 * kB)) != 0)) {
           Contact& o = out[nc];
           for (int q = 0; q < 3; ++q) { o.pos[q] = pc[i].pos[q]; o.normal[q] = -pl.p[q]; }
           o.depth = pc[i].depth;
@@ -315,9 +400,9 @@ OG_D int hf_zone(const DevHeightfield& H, const float* heights, int minX, int ma
     for (int bq = 0; bq < pcount[P]; ++bq) {
       const int t = members[pfirst[P] + bq];
       if (did) {
-        vstate[tv[t] & 0xff] = 1;
-        vstate[(tv[t] >> 8) & 0xff] = 1;
-        vstate[(tv[t] >> 16) & 0xff] = 1;
+        vstate[tv[t] & kM] = 1;
+        vstate[(tv[t] >> kB) & kM] = 1;
+        vstate[(tv[t] >> (2 * kB)) & kM] = 1;
       } else {
         tstate[t] = 0;
       }
@@ -328,7 +413,7 @@ OG_D int hf_zone(const DevHeightfield& H, const float* heights, int minX, int ma
     for (int k = 0; k < numTri; ++k) {
       if (tstate[k]) continue;
       for (int i = 0; i < 3; ++i) {
-        const int vi = (tv[k] >> (8 * i)) & 0xff;
+        const int vi = (int)((tv[k] >> (kB * i)) & kM);
         if (vstate[vi]) continue;
         float v[3];
         vtx(vi, v);
@@ -369,9 +454,11 @@ OG_D int hf_zone(const DevHeightfield& H, const float* heights, int minX, int ma
 
 // dCollideHeightfield(hf, g): placeable heightfield, centred origin. Returns
 // the contact count (normals as the reference: pointing into the field), or
-// -1 when the zone under the geom exceeds the lane buffers.
+// -1 when the zone under the geom exceeds both the lane's arrays (kHFZone
+// samples per axis) and the workspace `big` (none by default).
 __device__ __noinline__ int collide_heightfield(const DevHeightfield& H, const float* heights, const GeomView& g,
-                                               unsigned flags, Contact* out, unsigned* kinds) {
+                                               unsigned flags, Contact* out, unsigned* kinds,
+                                               HFBig big = HFBig{nullptr, 0}) {
   const int maxc = (int)(flags & 0xffff);
   if (kinds) *kinds = 0u;
   if (maxc < 1) return 0;
@@ -403,8 +490,19 @@ __device__ __noinline__ int collide_heightfield(const DevHeightfield& H, const f
     nMinZ = nMinZ > 0 ? nMinZ : 0;
     nMaxZ = nMaxZ < H.nz - 1 ? nMaxZ : H.nz - 1;
   }
+  const int numX = nMaxX - nMinX + 1, numZ = nMaxZ - nMinZ + 1;
+  if (numX < 1 || numZ < 1) return -1;
   unsigned kd = 0u;
-  const int n = hf_zone(H, heights, nMinX, nMaxX, nMinZ, nMaxZ, g2, aabb, maxc, flags, out, kd);
+  int n;
+  if (numX <= kHFZone && numZ <= kHFZone) {
+    HFLocalZone z;
+    n = hf_zone(z, H, heights, nMinX, nMaxX, nMinZ, nMaxZ, g2, aabb, maxc, flags, out, kd);
+  } else if (big.ws && numX <= big.side && numZ <= big.side) {
+    HFGlobalZone z = carve_hf_ws(big.ws, big.side);
+    n = hf_zone(z, H, heights, nMinX, nMaxX, nMinZ, nMaxZ, g2, aabb, maxc, flags, out, kd);
+  } else {
+    return -1;
+  }
   if (kinds) *kinds = kd;
   for (int i = 0; i < n; ++i) {
     const float q[3] = {out[i].pos[0] - H.half_w, out[i].pos[1], out[i].pos[2] - H.half_d};

@@ -344,17 +344,13 @@ __global__ void __launch_bounds__(128) lw_narrow_kernel(BatchDev d, LWDev L) {
   Contact cc[8];
   int cnt = 0;
   if (vi.type == G_HEIGHTFIELD || vk.type == G_HEIGHTFIELD) {
-    const bool rev = vk.type == G_HEIGHTFIELD;
-    const GeomView& hv = rev ? vk : vi;
-    const GeomView& ov = rev ? vi : vk;
-    if (ov.type == G_SPHERE || ov.type == G_BOX || ov.type == G_CAPSULE || ov.type == G_CYLINDER) {
-      cnt = collide_heightfield(d.hfs[(int)hv.p[0]], d.hf_heights, ov, (unsigned)D.max_contacts, cc, nullptr);
-      if (cnt < 0) { atomicOr(&d.status[0], ST_HF_ZONE); cnt = 0; }
-      if (rev)
-        for (int c = 0; c < cnt; ++c) {
-          cc[c].normal[0] = -cc[c].normal[0]; cc[c].normal[1] = -cc[c].normal[1];
-          cc[c].normal[2] = -cc[c].normal[2];
-        }
+    cnt = collide_hf_pair(d, vi, vk, (unsigned)D.max_contacts, cc, nullptr, HFBig{nullptr, 0});
+    if (cnt < 0) {
+      // a zone beyond the thread's arrays: lw_hf_big_kernel collides it
+      // through the world's workspace (when it has one)
+      if (D.hf_ws_side > 0) { L.pnc[p] = -1; return; }
+      atomicOr(&d.status[0], ST_HF_ZONE);
+      cnt = 0;
     }
   } else {
     cnt = collide_primitive(vi, vk, (unsigned)D.max_contacts, cc);
@@ -362,6 +358,36 @@ __global__ void __launch_bounds__(128) lw_narrow_kernel(BatchDev d, LWDev L) {
   Contact* o = L.staged + (size_t)p * D.max_contacts;
   for (int c = 0; c < cnt; ++c) o[c] = cc[c];
   L.pnc[p] = cnt;
+}
+
+// The heightfield pairs lw_narrow_kernel left (count -1): one warp finds them
+// and collides them one at a time through the world's workspace, which they
+// share.
+__global__ void __launch_bounds__(32) lw_hf_big_kernel(BatchDev d, LWDev L) {
+  const WorldDesc D = d.world[0];
+  const int lane = threadIdx.x;
+  const int np = *L.npairs;
+  const HFBig big{d.hf_ws + D.hf_ws, D.hf_ws_side};
+  for (int base = 0; base < np; base += 32) {
+    const int p = base + lane;
+    unsigned todo = __ballot_sync(kFull, p < np && L.pnc[p] < 0);
+    while (todo) {
+      const int l = __ffs(todo) - 1;
+      todo &= todo - 1;
+      if (lane == l) {
+        GeomView vi, vk;
+        geom_view(d, D, L.pair_i[p], vi);
+        geom_view(d, D, L.pair_k[p], vk);
+        Contact cc[8];
+        int cnt = collide_hf_pair(d, vi, vk, (unsigned)D.max_contacts, cc, nullptr, big);
+        if (cnt < 0) { atomicOr(&d.status[0], ST_HF_ZONE); cnt = 0; }
+        Contact* o = L.staged + (size_t)p * D.max_contacts;
+        for (int c = 0; c < cnt; ++c) o[c] = cc[c];
+        L.pnc[p] = cnt;
+      }
+      __syncwarp();
+    }
+  }
 }
 
 // Contact joints in canonical order (dJointCreateContact + dJointAttach(body(g_i), body(g_k))).

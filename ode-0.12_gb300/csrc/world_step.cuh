@@ -143,6 +143,26 @@ OG_D void unrank_pair(int p, int ng, int& i, int& k) {
 // that the dCollide early-outs and a conservative bounding-sphere test cannot
 // reject; the colliders then run densely over those candidates and a warp
 // prefix scan writes the contacts in pair order. Returns the contact count.
+// dCollide(g_i, g_k) for a pair with a heightfield: the heightfield collider
+// runs with the field first and the normals are negated when the call was
+// reversed (collision_kernel.cpp:320-334). Returns the contact count, 0 for
+// geoms the heightfield has no collider for, or -1 when the zone under the
+// geom exceeds the lane's arrays and the workspace `big`.
+OG_D int collide_hf_pair(const BatchDev& d, const GeomView& vi, const GeomView& vk, unsigned flags, Contact* cc,
+                         unsigned* kinds, HFBig big) {
+  const bool rev = vk.type == G_HEIGHTFIELD;
+  const GeomView& hv = rev ? vk : vi;
+  const GeomView& ov = rev ? vi : vk;
+  if (!(ov.type == G_SPHERE || ov.type == G_BOX || ov.type == G_CAPSULE || ov.type == G_CYLINDER)) return 0;
+  const int cnt = collide_heightfield(d.hfs[(int)hv.p[0]], d.hf_heights, ov, flags, cc, kinds, big);
+  if (rev)
+    for (int c = 0; c < cnt; ++c) {
+      cc[c].normal[0] = -cc[c].normal[0]; cc[c].normal[1] = -cc[c].normal[1];
+      cc[c].normal[2] = -cc[c].normal[2];
+    }
+  return cnt;
+}
+
 OG_D int phase_collide(const BatchDev& d, const WorldDesc& D, int w, const WarpSmem& S, int lane) {
   const int ng = D.ng;
   const int npairs = ng * (ng - 1) / 2;
@@ -189,27 +209,33 @@ OG_D int phase_collide(const BatchDev& d, const WorldDesc& D, int w, const WarpS
       GeomView vi, vk;
       geom_view(d, D, i, vi);
       geom_view(d, D, k, vk);
-      if (vi.type == G_HEIGHTFIELD || vk.type == G_HEIGHTFIELD) {
-        // dCollide(gi, gk): the heightfield collider runs with the field first
-        // and the normals are negated when the call was reversed
-        const bool rev = vk.type == G_HEIGHTFIELD;
-        const GeomView& hv = rev ? vk : vi;
-        const GeomView& ov = rev ? vi : vk;
-        if (ov.type == G_SPHERE || ov.type == G_BOX || ov.type == G_CAPSULE || ov.type == G_CYLINDER) {
-          cnt = collide_heightfield(d.hfs[(int)hv.p[0]], d.hf_heights, ov, (unsigned)D.max_contacts, cc, &kinds);
-          if (cnt < 0) { atomicOr(&d.status[w], ST_HF_ZONE); cnt = 0; }
-          if (rev)
-            for (int c = 0; c < cnt; ++c) {
-              cc[c].normal[0] = -cc[c].normal[0]; cc[c].normal[1] = -cc[c].normal[1];
-              cc[c].normal[2] = -cc[c].normal[2];
-            }
-        }
-      } else {
+      if (vi.type == G_HEIGHTFIELD || vk.type == G_HEIGHTFIELD)
+        cnt = collide_hf_pair(d, vi, vk, (unsigned)D.max_contacts, cc, &kinds, HFBig{nullptr, 0});
+      else
         cnt = collide_primitive(vi, vk, (unsigned)D.max_contacts, cc);
-      }
       const int si = d.gsurf[gi], sk = d.gsurf[gk];
       surf = si > sk ? si : sk;
     }
+    // heightfield zones beyond the lane's arrays: one lane at a time through
+    // the world's workspace (worlds whose geoms can need one have it)
+    if (D.hf_ws_side > 0) {
+      unsigned big = __ballot_sync(kFull, cnt < 0);
+      while (big) {
+        const int l = __ffs(big) - 1;
+        big &= big - 1;
+        if (lane == l) {
+          int i, k;
+          unrank_pair(S.cand[ci], ng, i, k);
+          GeomView vi, vk;
+          geom_view(d, D, i, vi);
+          geom_view(d, D, k, vk);
+          cnt = collide_hf_pair(d, vi, vk, (unsigned)D.max_contacts, cc, &kinds,
+                                HFBig{d.hf_ws + D.hf_ws, D.hf_ws_side});
+        }
+        __syncwarp();
+      }
+    }
+    if (cnt < 0) { atomicOr(&d.status[w], ST_HF_ZONE); cnt = 0; }
     const int incl = warp_incl_scan(cnt, lane);
     const int excl = incl - cnt;
     const int total = __shfl_sync(kFull, incl, 31);

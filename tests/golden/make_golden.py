@@ -163,6 +163,68 @@ def make_hf_kats(n=150, seed=321):
         out=np.array([r[6] for r in recs]))
 
 
+def make_hf_big_kats(n=40, seed=909):
+    """dCollide(heightfield, geom) for geoms that cover more than 10 x 10
+    samples (zones of up to ~60 samples per axis): a seeded 96 x 80 fractal
+    field at 0.25 m spacing, spheres, boxes, capsules and cylinders of several
+    metres near its surface, random contact limits; the dDOUBLE build's
+    outputs (nc / out) and the dSINGLE build's (nc_s / out_s)."""
+    import ctypes as C
+    rng = np.random.Generator(np.random.PCG64(seed))
+    P = C.POINTER(C.c_double)
+    nx, nz, sp = 96, 80, 0.25
+    h = np.ascontiguousarray(S.fractal_heights(128, 0.4, seed=seed)[:nz, :nx])
+    Rh = np.array(S.HF_Z_UP)
+    pos_h = np.array([-0.7, 0.5, 0.1])
+    H = S.Heightfield()
+    H.nx, H.nz = nx, nz
+    H.width, H.depth = sp * (nx - 1), sp * (nz - 1)
+    H.scale, H.offset, H.thickness, H.wrap = 1.0, 0.0, 1.0, 0
+    H.heights = h.ctypes.data_as(P)
+    H.pos[:] = list(pos_h)
+    H.R[:] = list(Rh.ravel())
+    fd, fs = O.ref("d").ref_collide_hf, O.ref("s").ref_collide_hf
+    for f in (fd, fs):
+        f.restype = C.c_int
+        f.argtypes = [C.c_void_p, C.c_int, P, P, P, C.c_int, P]
+    recs = []
+    for t2 in (0, 1, 2, 3):
+        for _ in range(n):
+            if t2 == 0:
+                p2 = np.array([rng.uniform(1.3, 3.5), 0, 0, 0])
+                down = p2[0]
+            elif t2 == 1:
+                p2 = np.concatenate([rng.uniform(2.5, 8.0, 3), [0]])
+                down = 0.3 * np.linalg.norm(p2[:3])
+            elif t2 == 2:
+                p2 = np.array([rng.uniform(0.8, 1.5), rng.uniform(3.0, 8.0), 0, 0])
+                down = p2[0] + 0.2 * p2[1]
+            else:
+                p2 = np.array([rng.uniform(1.0, 2.5), rng.uniform(2.0, 5.0), 0, 0])
+                down = 0.5 * p2[0] + 0.3 * p2[1]
+            local = np.array([rng.uniform(-0.3, 0.3) * H.width, 0.0, rng.uniform(-0.3, 0.3) * H.depth])
+            ix = int(np.clip(round((local[0] + H.width / 2) / sp), 0, nx - 1))
+            iz = int(np.clip(round((local[2] + H.depth / 2) / sp), 0, nz - 1))
+            local[1] = h[iz, ix] + down + rng.uniform(-0.6, 0.3)
+            pos2 = Rh @ local + pos_h
+            R2 = rot(rng) if rng.uniform() < 0.8 else np.eye(3)
+            flags = int(rng.choice([1, 2, 4, 8]))
+            args = [np.ascontiguousarray(a, dtype=np.float64) for a in (p2, pos2, R2.ravel())]
+            res = []
+            for f in (fd, fs):
+                out = np.zeros((64, 9))
+                nc = f(C.byref(H), t2, *(a.ctypes.data_as(P) for a in args), flags, out.ctypes.data_as(P))
+                res.append((nc, out[:8]))
+            recs.append((t2, flags, p2, pos2, R2.ravel(), res[0][0], res[0][1], res[1][0], res[1][1]))
+    np.savez_compressed(
+        os.path.join(HERE, "hf_big_kats.npz"), heights=h, spacing=sp, hf_pos=pos_h, hf_R=Rh.ravel(),
+        t2=np.array([r[0] for r in recs]), flags=np.array([r[1] for r in recs]),
+        p2=np.array([r[2] for r in recs]), pos2=np.array([r[3] for r in recs]),
+        R2=np.array([r[4] for r in recs]), nc=np.array([r[5] for r in recs]),
+        out=np.array([r[6] for r in recs]), nc_s=np.array([r[7] for r in recs]),
+        out_s=np.array([r[8] for r in recs]))
+
+
 def frame_with_z(d):
     """A rotation whose third column is the unit vector d (a ray geom points
     along column 2 of its rotation, ode/src/ray.cpp:115-136)."""
@@ -481,6 +543,8 @@ if __name__ == "__main__":
                 add_single_outputs("cylinder_kats", hf_class=3)
             elif name.startswith("exact_"):
                 make_scene(name[len("exact_"):], exact=True)
+            elif name == "hf_big_kats":
+                make_hf_big_kats()
             elif name == "single_outputs":
                 add_single_outputs("collider_kats")
                 add_single_outputs("hf_kats")
@@ -500,6 +564,7 @@ if __name__ == "__main__":
     make_hf_kats()
     make_ray_kats()
     make_cylinder_kats()
+    make_hf_big_kats()
     add_single_outputs("collider_kats")
     add_single_outputs("hf_kats")
     add_single_outputs("ray_kats", hf_class=5)

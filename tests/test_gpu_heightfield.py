@@ -40,38 +40,64 @@ def _q_from_R(R):
     return q / np.linalg.norm(q)
 
 
-def test_heightfield_kats_on_gpu():
-    """Each golden dCollide(heightfield, geom) call as a world of its own (the
-    heightfield first in creation order, so the batch calls dCollide in the
-    same argument order); the contacts of the first step are the call's."""
-    from odegpu.batch import Batch
-    g = np.load(os.path.join(GOLDEN, "hf_kats.npz"))
+def _kat_scene(g, idx):
+    """The golden calls idx as worlds of their own: the heightfield first in
+    creation order (so the batch calls dCollide in the same argument order),
+    then a body carrying the call's geom."""
     h = g["heights"]
     sp = float(g["spacing"])
     b = S.SceneBuilder()
     surf = b.add_surface(0, 0.5)
     hf = b.add_heightfield(h, sp * (h.shape[1] - 1), sp * (h.shape[0] - 1), pos=g["hf_pos"],
                            R=np.asarray(g["hf_R"]).reshape(3, 3))
-    n = len(g["t2"])
-    for i in range(n):
+    for i in idx:
         w = b.new_world(max_contacts=int(g["flags"][i]), seed=1)
         b.add_geom(w, S.GEOM_HEIGHTFIELD, -1, (hf,), surf)
         bi = b.add_body(w, tuple(g["pos2"][i]), 1.0, np.eye(3) * 0.1, q=tuple(_q_from_R(g["R2"][i])))
         b.add_geom(w, int(g["t2"][i]), bi, tuple(g["p2"][i]), surf)
-    sc = b.build()
-    B = Batch(sc)
-    B.step(1)
-    assert (B.status() == 0).all(), B.status()
-    count_mism, worst = [], 0.0
-    for i in range(n):
-        c = B.contacts(i)
+    return b.build()
+
+
+def _compare_kats(g, idx, contacts_of, count_mism, scale=1.0):
+    worst = 0.0
+    for w, i in enumerate(idx):
+        c = contacts_of(w)
         nc = int(g["nc"][i])
         if len(c) != nc:
             count_mism.append((i, len(c), nc))
             continue
         if nc:
-            worst = max(worst, float(np.abs(c[:, :7] - g["out"][i][:nc, :7]).max()))
+            worst = max(worst, float(np.abs(c[:, :7] - g["out"][i][:nc, :7]).max()) / scale)
+    return worst
+
+
+@pytest.mark.parametrize("fixture", ["hf_kats", "hf_big_kats"])
+def test_heightfield_kats_on_gpu(fixture):
+    """Each golden dCollide(heightfield, geom) call as a world of its own; the
+    contacts of the first step are the call's. hf_big_kats holds geoms of
+    several metres on a 0.25 m field (zones of up to ~60 samples per axis,
+    beyond the lane's 10 x 10 arrays): those worlds collide through their
+    heightfield workspace, and a sample of them also through the large-world
+    pipeline (one world per batch). Records within 1e-4 (relative to the
+    coordinates' scale, up to ~12 m, for the large geoms)."""
+    from odegpu.batch import Batch
+    g = np.load(os.path.join(GOLDEN, f"{fixture}.npz"))
+    n = len(g["t2"])
+    idx = list(range(n))
+    B = Batch(_kat_scene(g, idx))
+    B.step(1)
+    assert (B.status() == 0).all(), B.status()
+    count_mism = []
+    scale = 1.0 if fixture == "hf_kats" else 12.0
+    worst = _compare_kats(g, idx, B.contacts, count_mism, scale)
     B.close()
+    if fixture == "hf_big_kats":
+        for i in range(0, n, 10):
+            Lw = Batch(_kat_scene(g, [i]), large_world=True)
+            Lw.step(1)
+            assert Lw.status()[0] == 0, (i, Lw.status())
+            worst = max(worst, _compare_kats(g, [i], Lw.contacts, count_mism, scale))
+            Lw.close()
     assert not count_mism, f"contact counts differ: {count_mism[:10]}"
     assert worst < ATOL, worst
     assert (g["nc"] > 0).sum() > n // 2

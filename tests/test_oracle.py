@@ -74,11 +74,14 @@ def hf_from_golden(g):
     return H, h
 
 
-def test_heightfield_kats_golden():
+@pytest.mark.parametrize("fixture", ["hf_kats", "hf_big_kats"])
+def test_heightfield_kats_golden(fixture):
     """dCollide(heightfield, sphere / box / capsule) on a placeable fractal
     field (dCollideHeightfield, ode/src/heightfield.cpp:1677-1853): contact
-    count and records bit-exact vs the reference."""
-    g = np.load(os.path.join(GOLDEN, "hf_kats.npz"))
+    count and records bit-exact vs the reference. hf_big_kats: geoms of
+    several metres (and cylinders) on a 0.25 m field, zones of up to ~60
+    samples per axis."""
+    g = np.load(os.path.join(GOLDEN, f"{fixture}.npz"))
     H, _h = hf_from_golden(g)
     L = O.oracle()
     f = L.oracle_collide_hf
