@@ -93,7 +93,7 @@ __global__ void __launch_bounds__(256) world_solve_kernel(BatchDev d, const int*
 constexpr int kStepSmemPerWarp =
     kSmemPerWarp > kFwdSmemPerWarp ? (kSmemPerWarp > kCollideSmemPerWarp ? kSmemPerWarp : kCollideSmemPerWarp)
                                    : (kFwdSmemPerWarp > kCollideSmemPerWarp ? kFwdSmemPerWarp : kCollideSmemPerWarp);
-__global__ void __launch_bounds__(128, 4) world_step_kernel(BatchDev d, const int* order, int first, int count,
+__global__ void __launch_bounds__(128, 3) world_step_kernel(BatchDev d, const int* order, int first, int count,
                                                             int step, StepOptions opt) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & 31;

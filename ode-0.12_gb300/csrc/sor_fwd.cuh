@@ -247,13 +247,16 @@ OG_D void fwd_row(const float4 (&rw)[8], bool active, const FwdSmem& S) {
 }
 
 // Rows of chunk c for this lane: from the row store (first iteration of the
-// round) or from the sweep buffer; returns whether the lane has a row.
-OG_D bool fwd_load(const float* rows, const float4* sweep, int capp, const FwdSmem& S, unsigned c, bool first,
-                   int lane, float4 (&rw)[8]) {
-  const bool active = lane <= (int)(c >> 11);
-  if (!active) return false;
-  const int slot = (int)(c & 0x7ffu) + lane;
-  if (first) {
+// round) or from the sweep buffer; returns whether the lane has a row. Lanes
+// past the chunk's end load the chunk's last row again (the same lines, no
+// divergent branch) and are masked out by fwd_row.
+template <bool kFirst>
+OG_D bool fwd_load(const float* rows, const float4* sweep, int capp, const FwdSmem& S, unsigned c, int lane,
+                   float4 (&rw)[8]) {
+  const int last = (int)(c >> 11);
+  const bool active = lane <= last;
+  const int slot = (int)(c & 0x7ffu) + (active ? lane : last);
+  if (kFirst) {
     const int r = S.exec[slot];
     const float4* src = reinterpret_cast<const float4*>(rows) + (size_t)r * 8;
 #pragma unroll
@@ -263,7 +266,7 @@ OG_D bool fwd_load(const float* rows, const float4* sweep, int capp, const FwdSm
 #pragma unroll
     for (int q = 0; q < 8; ++q) rw[q] = sweep[(size_t)q * capp + slot];
   }
-  return true;
+  return active;
 }
 // the first iteration's rows into the sweep buffer
 OG_D void fwd_keep(float4* sweep, int capp, unsigned c, bool active, int lane, const float4 (&rw)[8]) {
@@ -273,32 +276,38 @@ OG_D void fwd_keep(float4* sweep, int capp, unsigned c, bool active, int lane, c
   for (int q = 0; q < 8; ++q) sweep[(size_t)q * capp + slot] = rw[q];
 }
 
-// n_it iterations of one reshuffle round over the chunk list (S.chunk, rows
-// of the slots in S.exec).
-OG_D void fwd_sweep(const float* rows, float4* sweep, int capp, const FwdSmem& S, int nchunk, int n_it, int lane) {
-  for (int it = 0; it < n_it; ++it) {
-    const bool first = it == 0;
-    float4 ra[8], rb[8];
-    unsigned ca = S.chunk[0], cb = 0;
-    bool act_a = fwd_load(rows, sweep, capp, S, ca, first, lane, ra), act_b = false;
-    for (int k = 0; k < nchunk; k += 2) {
-      if (k + 1 < nchunk) {
-        cb = S.chunk[k + 1];
-        act_b = fwd_load(rows, sweep, capp, S, cb, first, lane, rb);
-      }
-      fwd_row(ra, act_a, S);
-      if (first) fwd_keep(sweep, capp, ca, act_a, lane, ra);
-      __syncwarp();
-      if (k + 1 >= nchunk) break;
-      if (k + 2 < nchunk) {
-        ca = S.chunk[k + 2];
-        act_a = fwd_load(rows, sweep, capp, S, ca, first, lane, ra);
-      }
-      fwd_row(rb, act_b, S);
-      if (first) fwd_keep(sweep, capp, cb, act_b, lane, rb);
-      __syncwarp();
+// One iteration over the chunk list (S.chunk, rows of the slots in S.exec);
+// the first iteration of a round reads the row store and fills the sweep
+// buffer, the others read the sweep buffer.
+template <bool kFirst>
+OG_D void fwd_iteration(const float* rows, float4* sweep, int capp, const FwdSmem& S, int nchunk, int lane) {
+  float4 ra[8], rb[8];
+  unsigned ca = S.chunk[0], cb = 0;
+  bool act_a = fwd_load<kFirst>(rows, sweep, capp, S, ca, lane, ra), act_b = false;
+  for (int k = 0; k < nchunk; k += 2) {
+    if (k + 1 < nchunk) {
+      cb = S.chunk[k + 1];
+      act_b = fwd_load<kFirst>(rows, sweep, capp, S, cb, lane, rb);
     }
+    fwd_row(ra, act_a, S);
+    if (kFirst) fwd_keep(sweep, capp, ca, act_a, lane, ra);
+    __syncwarp();
+    if (k + 1 >= nchunk) break;
+    if (k + 2 < nchunk) {
+      ca = S.chunk[k + 2];
+      act_a = fwd_load<kFirst>(rows, sweep, capp, S, ca, lane, ra);
+    }
+    fwd_row(rb, act_b, S);
+    if (kFirst) fwd_keep(sweep, capp, cb, act_b, lane, rb);
+    __syncwarp();
   }
+}
+
+// n_it iterations of one reshuffle round over the chunk list.
+OG_D void fwd_sweep(const float* rows, float4* sweep, int capp, const FwdSmem& S, int nchunk, int n_it, int lane) {
+  if (n_it < 1 || nchunk < 1) return;
+  fwd_iteration<true>(rows, sweep, capp, S, nchunk, lane);
+  for (int it = 1; it < n_it; ++it) fwd_iteration<false>(rows, sweep, capp, S, nchunk, lane);
 }
 
 // SOR over every island of the world (rows of island i start at world row
