@@ -136,9 +136,10 @@ OG_D int fwd_schedule(const FwdSmem& S, int nb, int M, int lane) {
       S.chunk[pos] = (uint16_t)lvl;
       add_u16_fwd(S.lstart, lvl, 1u);
     }
-    nlev = max(nlev, warp_max(pos < M ? lvl + 1 : 0));
+    if (pos < M) nlev = max(nlev, lvl + 1);
     __syncwarp();
   }
+  nlev = warp_max(nlev);
   // exclusive prefix over the level counts -> first slot of each level
   {
     int carry = 0;
@@ -357,30 +358,62 @@ OG_D unsigned fwd_sor_world(const float* rows, const int* rstart_g, int nb, int 
   }
   for (int it = 0; it < iters; it += 8) {
     const int round = it >> 3;
-    // the round's swap targets (dRandInt(q + 1) for step q of each island's
-    // shuffle), drawn lane-parallel: draw q of an island is the seed advanced
-    // by the island's stream offset + q; kept in exec
-    unsigned prefix = 0;
-    for (int ib = 0; ib < nisl; ib += 32) {
-      const int isl = ib + lane;
-      int m = 0;
-      if (isl < nisl) m = S.rstart[isl + 1] - S.rstart[isl];
-      const int draws = m > 0 ? n_shuffles * (m - 1) : 0;
-      const int incl = warp_incl_scan(draws, lane);
-      const unsigned first = prefix + (unsigned)(incl - draws) + (unsigned)(round * max(m - 1, 0));
-      for (int j = 0; j < 32 && ib + j < nisl; ++j) {
-        const int mj = __shfl_sync(kFull, m, j);
-        const unsigned fj = __shfl_sync(kFull, first, j);
-        const int r0 = S.rstart[ib + j];
-        if (1 + lane < mj) {
-          unsigned s = lcg_jump(seed, fj + 1u + (unsigned)lane);
-          for (int q = 1 + lane; q < mj; q += 32) {
-            S.exec[r0 + q] = (uint16_t)rand_int_from(s, q + 1);
-            s = kLcg32A * s + kLcg32C;
+    // the round's swap targets, dRandInt(q + 1) for step q = 1 .. m - 1 of
+    // each island's shuffle (quickstep.cpp:471-478). ODE draws them island by
+    // island, every round of an island before the next island, so draw q of
+    // island i in this round is the seed advanced by base_i + round (m_i - 1)
+    // + q, base_i the draws of the islands before it. The round's (island, q)
+    // entries are cut into one contiguous run per lane: a jump-ahead to the
+    // run's first entry, then one LCG step per entry. The island tables live
+    // in S.last and S.lstart until fwd_schedule claims them.
+    {
+      int* iex = S.last;                                        // entries before island i
+      unsigned* ist = reinterpret_cast<unsigned*>(S.lstart);    // seed before island i's round
+      int T = 0;
+      unsigned base = 0;
+      for (int ib = 0; ib < nisl; ib += 32) {
+        const int isl = ib + lane;
+        const int m = isl < nisl ? S.rstart[isl + 1] - S.rstart[isl] : 0;
+        const int e = m > 1 ? m - 1 : 0;
+        const int d = n_shuffles * e;
+        const int incl_e = warp_incl_scan(e, lane);
+        const int incl_d = warp_incl_scan(d, lane);
+        if (isl < nisl) {
+          iex[isl] = T + incl_e - e;
+          ist[isl] = lcg_jump(seed, base + (unsigned)(incl_d - d) + (unsigned)(round * e));
+        }
+        T += __shfl_sync(kFull, incl_e, 31);
+        base += (unsigned)__shfl_sync(kFull, incl_d, 31);
+      }
+      __syncwarp();
+      const int per = (T + 31) >> 5;
+      const int e0 = lane * per, e1 = min(T, e0 + per);
+      if (e0 < e1) {
+        // the island of entry e0: the last island whose first entry is <= e0
+        int lo = 0, hi = nisl - 1;
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (iex[mid] <= e0) lo = mid;
+          else hi = mid - 1;
+        }
+        int i = lo, r0 = S.rstart[i], m = S.rstart[i + 1] - r0, q = e0 - iex[i] + 1;
+        unsigned sd = lcg_jump(ist[i], (unsigned)q);
+        for (int e = e0;;) {
+          S.exec[r0 + q] = (uint16_t)rand_int_from(sd, q + 1);
+          if (++e >= e1) break;
+          if (++q < m) {
+            sd = lcg_next(sd);
+            continue;
           }
+          do {                       // the next island with draws
+            ++i;
+            r0 = S.rstart[i];
+            m = S.rstart[i + 1] - r0;
+          } while (m <= 1);
+          q = 1;
+          sd = lcg_next(ist[i]);
         }
       }
-      prefix += (unsigned)__shfl_sync(kFull, incl, 31);
     }
     __syncwarp();
     // the swaps themselves, one lane per island, in the reference's order
