@@ -13,6 +13,7 @@ namespace og {
 struct Info2 {
   float fps, erp;
   float* rows;   // first row of this joint
+  int fbase;     // its index in the world's row store: findex is stored absolute
   OG_D float& J1l(int r, int k) { return rows[r * kRowWords + k]; }
   OG_D float& J1a(int r, int k) { return rows[r * kRowWords + 3 + k]; }
   OG_D float& J2l(int r, int k) { return rows[r * kRowWords + 6 + k]; }
@@ -24,6 +25,8 @@ struct Info2 {
   OG_D float& lo(int r) { return rows[r * kRowWords + kRowLo]; }
   OG_D float& hi(int r) { return rows[r * kRowWords + kRowHi]; }
   OG_D int& findex(int r) { return reinterpret_cast<int*>(rows)[r * kRowWords + kRowFindex]; }
+  // findex of row r: row v of the same joint
+  OG_D void set_findex(int r, int v) { findex(r) = fbase + v; }
 };
 
 // Body state a joint reads: placement, orientation and velocities.
@@ -529,7 +532,7 @@ OG_D void contact_info2(const DevContact& ct, const DevSurface& S, int the_m, co
     if (S.mode & SURF_MOTION1) in.c(1) = S.motion1;
     in.lo(1) = -mu;
     in.hi(1) = mu;
-    if (S.mode & SURF_APPROX1_1) in.findex(1) = 0;
+    if (S.mode & SURF_APPROX1_1) in.set_findex(1, 0);
     if (S.mode & SURF_SLIP1) in.cfm(1) = S.slip1;
   }
   if (the_m >= 3) {
@@ -544,7 +547,7 @@ OG_D void contact_info2(const DevContact& ct, const DevSurface& S, int the_m, co
     if (S.mode & SURF_MOTION2) in.c(2) = S.motion2;
     if (S.mode & SURF_MU2) { in.lo(2) = -mu2; in.hi(2) = mu2; }
     else { in.lo(2) = -mu; in.hi(2) = mu; }
-    if (S.mode & SURF_APPROX1_2) in.findex(2) = 0;
+    if (S.mode & SURF_APPROX1_2) in.set_findex(2, 0);
     if (S.mode & SURF_SLIP2) in.cfm(2) = S.slip2;
   }
 }

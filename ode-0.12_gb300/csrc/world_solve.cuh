@@ -80,22 +80,25 @@ OG_D void assemble_joint_rows(const BatchDev& d, const WorldDesc& D, int ord, in
   float* rows = d.rows + (size_t)(D.row_off + r0) * kRowWords;
   int b1, b2;
   joint_bodies(d, D, ord, b1, b2);
+  // J zero, c = 0, cfm = the world's, lo / hi unbounded, findex -1 (the
+  // stepper's defaults before getInfo2, quickstep.cpp:716-745), in 16-byte
+  // stores; the iMJ words are written by the row setup
+  static_assert(kRowC == 24 && kRowFindex == 28 && kRowB1 == 29 && kRowB2 == 30 && kRowJoint == 31,
+                "row layout of the 16-byte stores");
   for (int r = 0; r < m; ++r) {
-    float* row = rows + r * kRowWords;
-    for (int q = 0; q < 12; ++q) row[q] = 0.f;
-    row[kRowC] = 0.f;
-    row[kRowCfm] = D.cfm;
-    row[kRowLo] = -INFINITY;
-    row[kRowHi] = INFINITY;
-    reinterpret_cast<int*>(row)[kRowFindex] = -1;
-    reinterpret_cast<int*>(row)[kRowB1] = b1;
-    reinterpret_cast<int*>(row)[kRowB2] = b2;
-    reinterpret_cast<int*>(row)[kRowJoint] = ord;
+    float4* row4 = reinterpret_cast<float4*>(rows + r * kRowWords);
+    const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+    row4[0] = z;
+    row4[1] = z;
+    row4[2] = z;
+    row4[6] = make_float4(0.f, D.cfm, -INFINITY, INFINITY);
+    reinterpret_cast<int4*>(row4)[7] = make_int4(-1, b1, b2, ord);
   }
   Info2 in;
   in.fps = h1;
   in.erp = erp;
   in.rows = rows;
+  in.fbase = r0;
   BodyRef B1, B2;
   load_body_ref(d, D.body_off + b1, B1);
   if (b2 >= 0) load_body_ref(d, D.body_off + b2, B2);
@@ -129,10 +132,6 @@ OG_D void assemble_joint_rows(const BatchDev& d, const WorldDesc& D, int ord, in
   } else {
     const DevContact& ct = d.contacts[D.contact_off + ord - D.njp];
     contact_info2(ct, d.surfaces[ct.surface], m, B1, pB2, D.min_depth, D.max_vel, in);
-  }
-  for (int r = 0; r < m; ++r) {
-    int* fi = reinterpret_cast<int*>(rows + r * kRowWords) + kRowFindex;
-    if (*fi != -1) *fi += r0;
   }
   if (dbg_rows)
     for (int r = 0; r < m; ++r) dbg_rows[(size_t)(D.row_off + r0 + r) * kRowWords + kDbgErp] = in.erp;

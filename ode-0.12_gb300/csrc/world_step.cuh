@@ -44,6 +44,8 @@ struct WarpSmem {
   uint8_t* jtag;      // [kMaxR]     joint tags for the island search
   // collide kernel
   uint16_t* cand;     // [kMaxPairs] candidate pairs that pass the bound test
+  float4* gpb;        // [kMaxB+8]   per geom: position (its body's, or its own when static), bound radius
+  int16_t* gbd;       // [kMaxB+8]   per geom: body, -1 static
 };
 constexpr int kMaxPairs = (kMaxB + 8) * (kMaxB + 7) / 2;   // geoms: bodies + a few static
 // Per-warp sizes are rounded up to 16 bytes so that every warp's slice (and
@@ -51,7 +53,7 @@ constexpr int kMaxPairs = (kMaxB + 8) * (kMaxB + 7) / 2;   // geoms: bodies + a 
 constexpr int align16(int n) { return (n + 15) & ~15; }
 constexpr int kSmemPerWarp = align16(kMaxB * 6 * 4 + (kMaxB + 1) * 4 + (kMaxB + 1) * 2 + 2 * kMaxR * 2 +
                                      kMaxR * 2 + kMaxR * 2 + kMaxB * 2 + kMaxB + kMaxR + 32);
-constexpr int kCollideSmemPerWarp = align16(kMaxPairs * 2 + 16);
+constexpr int kCollideSmemPerWarp = align16(kMaxPairs * 2 + 16) + align16((kMaxB + 8) * 16) + align16((kMaxB + 8) * 2);
 static_assert(kSmemPerWarp % 16 == 0 && kCollideSmemPerWarp % 16 == 0, "per-warp slices must stay aligned");
 static_assert(kMaxB * 6 * sizeof(float) >= 6 * kMaxB * sizeof(int), "the island phase borrows the tmp1 area");
 
@@ -74,6 +76,10 @@ OG_D WarpSmem carve_smem(unsigned char* base) {
 OG_D WarpSmem carve_collide_smem(unsigned char* base) {
   WarpSmem s{};
   s.cand = reinterpret_cast<uint16_t*>(base);
+  base += align16(kMaxPairs * 2 + 16);
+  s.gpb = reinterpret_cast<float4*>(base);
+  base += align16((kMaxB + 8) * 16);
+  s.gbd = reinterpret_cast<int16_t*>(base);
   return s;
 }
 
@@ -139,10 +145,6 @@ OG_D void unrank_pair(int p, int ng, int& i, int& k) {
   k = p - i * (2 * ng - i - 1) / 2 + i + 1;
 }
 
-// Phase 1: canonical pair loop. A first pass keeps, in pair order, the pairs
-// that the dCollide early-outs and a conservative bounding-sphere test cannot
-// reject; the colliders then run densely over those candidates and a warp
-// prefix scan writes the contacts in pair order. Returns the contact count.
 // dCollide(g_i, g_k) for a pair with a heightfield: the heightfield collider
 // runs with the field first and the normals are negated when the call was
 // reversed (collision_kernel.cpp:320-334). Returns the contact count, 0 for
@@ -163,9 +165,23 @@ OG_D int collide_hf_pair(const BatchDev& d, const GeomView& vi, const GeomView& 
   return cnt;
 }
 
+// Phase 1: canonical pair loop. A first pass keeps, in pair order, the pairs
+// that the dCollide early-outs and a conservative bounding-sphere test cannot
+// reject; the colliders then run densely over those candidates and a warp
+// prefix scan writes the contacts in pair order. Returns the contact count.
 OG_D int phase_collide(const BatchDev& d, const WorldDesc& D, int w, const WarpSmem& S, int lane) {
   const int ng = D.ng;
   const int npairs = ng * (ng - 1) / 2;
+  // the world's geoms for the candidate pass, staged once: body, position
+  // (a static geom's own) and bounding radius
+  for (int g = lane; g < ng; g += 32) {
+    const int gg = D.geom_off + g;
+    const int b = d.gbody[gg];
+    const float4 p = b >= 0 ? d.pos[D.body_off + b] : d.gpos[gg];
+    S.gpb[g] = make_float4(p.x, p.y, p.z, d.gbound[gg]);
+    S.gbd[g] = (int16_t)b;
+  }
+  __syncwarp();
   int ncand = 0;
   for (int base = 0; base < npairs; base += 32) {
     const int p = base + lane;
@@ -173,15 +189,13 @@ OG_D int phase_collide(const BatchDev& d, const WorldDesc& D, int w, const WarpS
     if (p < npairs) {
       int i, k;
       unrank_pair(p, ng, i, k);
-      const int gi = D.geom_off + i, gk = D.geom_off + k;
-      const int bi = d.gbody[gi], bk = d.gbody[gk];
+      const int bi = S.gbd[i], bk = S.gbd[k];
       keep = !((bi < 0 && bk < 0) || (bi == bk));
       if (keep) {
-        const float ri = d.gbound[gi], rk = d.gbound[gk];
-        if (isfinite(ri) && isfinite(rk)) {
-          const float4 pi4 = d.pos[D.body_off + bi], pk4 = d.pos[D.body_off + bk];
+        const float4 pi4 = S.gpb[i], pk4 = S.gpb[k];
+        if (isfinite(pi4.w) && isfinite(pk4.w)) {
           const float dx = pi4.x - pk4.x, dy = pi4.y - pk4.y, dz = pi4.z - pk4.z;
-          const float lim = (ri + rk) * 1.001f + 1e-5f;
+          const float lim = (pi4.w + pk4.w) * 1.001f + 1e-5f;
           if (dx * dx + dy * dy + dz * dz > lim * lim) keep = false;
         }
       }
