@@ -164,7 +164,7 @@ def solve_bytes(nr, iters=20):
     return float(np.sum(nr) * 236.0 * iters)
 
 
-SOLVE_PROFILE = os.path.join(ROOT, "profiles", "world_solve_kernel_batched_4096.txt")
+SOLVE_PROFILE = os.path.join(ROOT, "profiles", "world_solve_kernel_batched_512_settled.md")
 
 
 def solve_traffic_per_row_iter():
