@@ -654,7 +654,9 @@ def run_ours(args):
                 "window": {"rows_per_world_avg": main["rows"] / (args.steps * sc.n_worlds),
                            "bodies": int(nbt), "worlds_with_status": int((main["status"] != 0).sum()),
                            "launch_shape": {"collide": launch_cfg[0], "setup": launch_cfg[1],
-                                            "solve": launch_cfg[2], "fused_step": [fused_wpb, fused_carve],
+                                            "solve": launch_cfg[2],
+                                            "solve_registers": 128 if B.launch_config_ex(2)[2] else 168,
+                                            "fused_step": [fused_wpb, fused_carve],
                                             "step_kernels": "fused" if fused else "collide, setup, solve"},
                            "step_ms_min_median_max": [float(1e3 * times.min()), float(1e3 * np.median(times)),
                                                       float(1e3 * times.max())]},

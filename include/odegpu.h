@@ -160,6 +160,15 @@ int odegpuBatchAdjointStatus(odegpuBatchID b, int* status);
  * step index are unchanged afterwards. */
 int odegpuBatchSetLaunchConfig(odegpuBatchID b, int kernel, int warps_per_block, int smem_carveout);
 int odegpuBatchGetLaunchConfig(odegpuBatchID b, int* cfg);
+/* The same with a kernel variant: variant 1 of the solve kernel (2) caps it
+ * at 128 registers per thread, for 16 warps per SM instead of 12 (batches of
+ * small worlds gain from the occupancy, batches of large ones lose to the
+ * spills); every other kernel has variant 0 only. Autotune also picks the
+ * solve kernel's variant. */
+int odegpuBatchSetLaunchConfigEx(odegpuBatchID b, int kernel, int warps_per_block, int smem_carveout,
+                                 int variant);
+int odegpuBatchGetLaunchConfigEx(odegpuBatchID b, int kernel, int* warps_per_block, int* smem_carveout,
+                                 int* variant);
 int odegpuBatchSetStepKernels(odegpuBatchID b, int fused);
 int odegpuBatchGetStepKernels(odegpuBatchID b, int* fused, int* warps_per_block, int* smem_carveout);
 int odegpuBatchAutotune(odegpuBatchID b, int n_steps);

@@ -74,14 +74,28 @@ __global__ void __launch_bounds__(256) world_setup_kernel(BatchDev d, const int*
   world_setup(d, w, step, S, lane, opt);
 }
 
-__global__ void __launch_bounds__(256) world_solve_kernel(BatchDev d, const int* order, int first, int count,
-                                                          StepOptions opt) {
+// Two register budgets of the solve kernel: world_solve_kernel keeps its
+// working set in registers (168 per thread, 12 warps per SM),
+// world_solve_kernel_r128 is capped at 128 for 16 warps per SM at the price of
+// a few spills; batches of large worlds run faster on the first, batches of
+// small ones on the second (odegpuBatchSetLaunchConfigEx / odegpuBatchAutotune
+// pick).
+__device__ __forceinline__ void solve_kernel_body(const BatchDev& d, const int* order, int first, int count,
+                                                  const StepOptions& opt) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & 31;
   const int w = slot_world(order, first, count, d.n_worlds);
   if (w < 0) return;
   if (d.world[w].nb > kMaxB) return;
   world_solve(d, w, smem_raw + (size_t)(threadIdx.x >> 5) * kFwdSmemPerWarp, lane, opt);
+}
+__global__ void __launch_bounds__(256) world_solve_kernel(BatchDev d, const int* order, int first, int count,
+                                                          StepOptions opt) {
+  solve_kernel_body(d, order, first, count, opt);
+}
+__global__ void __launch_bounds__(256, 2) world_solve_kernel_r128(BatchDev d, const int* order, int first,
+                                                                  int count, StepOptions opt) {
+  solve_kernel_body(d, order, first, count, opt);
 }
 
 // The three phases of a step in one launch: each warp runs collide, setup and
@@ -216,6 +230,8 @@ struct odegpuBatch {
   // a step is one world_step_kernel launch (fused) or the collide, setup and
   // solve kernels (odegpuBatchSetStepKernels / odegpuBatchAutotune)
   bool fused = false;
+  // the solve kernel's register budget: 168 (false) or 128 (true) per thread
+  bool solve_lowreg = false;
   int step_counter = 0;
   cudaStream_t stream = nullptr;
   std::vector<WorldDesc> h_world;
@@ -397,14 +413,15 @@ struct odegpuBatch {
   // the carveout is a property of the kernel function: set it when it differs
   // from what the last launch of that kernel used (any batch)
   void apply_carveout(int k) {
-    static int current[5] = {-1, -1, -1, -1, -1};
-    if (current[k] == kcarve[k]) return;
+    static int current[6] = {-1, -1, -1, -1, -1, -1};   // slot 5: the 128-register solve kernel
+    const int slot = (k == 2 && solve_lowreg) ? 5 : k;
+    if (current[slot] == kcarve[k]) return;
     const void* fn = k == 0 ? (const void*)world_collide_kernel
                    : k == 1 ? (const void*)world_setup_kernel
-                   : k == 2 ? (const void*)world_solve_kernel
+                   : k == 2 ? (solve_lowreg ? (const void*)world_solve_kernel_r128 : (const void*)world_solve_kernel)
                    : k == 3 ? (const void*)adjoint_step_kernel : (const void*)world_step_kernel;
     if (cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, kcarve[k]) == cudaSuccess)
-      current[k] = kcarve[k];
+      current[slot] = kcarve[k];
     else
       cudaGetLastError();
   }
@@ -611,8 +628,12 @@ struct odegpuBatch {
           d, ord, first, count, step_counter + s, opt);
       mark(tm);
       apply_carveout(2);
-      world_solve_kernel<<<(count + w[2] - 1) / w[2], w[2] * 32, (size_t)w[2] * kFwdSmemPerWarp, stream>>>(
-          d, ord, first, count, opt);
+      if (solve_lowreg)
+        world_solve_kernel_r128<<<(count + w[2] - 1) / w[2], w[2] * 32, (size_t)w[2] * kFwdSmemPerWarp, stream>>>(
+            d, ord, first, count, opt);
+      else
+        world_solve_kernel<<<(count + w[2] - 1) / w[2], w[2] * 32, (size_t)w[2] * kFwdSmemPerWarp, stream>>>(
+            d, ord, first, count, opt);
       mark(tm);
       launches += 3;
     }
@@ -633,6 +654,9 @@ static int configure_kernels() {
                            (int)(kMaxWpb[1] * kSmemPerWarp)) != cudaSuccess)
     return -1;
   if (cudaFuncSetAttribute(world_solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)(kMaxWpb[2] * kFwdSmemPerWarp)) != cudaSuccess)
+    return -1;
+  if (cudaFuncSetAttribute(world_solve_kernel_r128, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)(kMaxWpb[2] * kFwdSmemPerWarp)) != cudaSuccess)
     return -1;
   if (cudaFuncSetAttribute(adjoint_step_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1308,6 +1332,24 @@ int odegpuBatchSetLaunchConfig(odegpuBatchID b, int kernel, int warps_per_block,
   return 0;
 }
 
+int odegpuBatchSetLaunchConfigEx(odegpuBatchID b, int kernel, int warps_per_block, int smem_carveout,
+                                 int variant) {
+  if (!b || (variant != 0 && !(kernel == 2 && variant == 1)))
+    return fail(ODEGPU_E_ARG, "variant 1 exists for the solve kernel (2) only");
+  if (int rc = odegpuBatchSetLaunchConfig(b, kernel, warps_per_block, smem_carveout)) return rc;
+  if (kernel == 2) b->solve_lowreg = variant == 1;
+  return 0;
+}
+
+int odegpuBatchGetLaunchConfigEx(odegpuBatchID b, int kernel, int* warps_per_block, int* smem_carveout,
+                                 int* variant) {
+  if (!b || kernel < 0 || kernel > 4) return fail(ODEGPU_E_ARG, "bad kernel index");
+  if (warps_per_block) *warps_per_block = b->kwpb[kernel];
+  if (smem_carveout) *smem_carveout = b->kcarve[kernel];
+  if (variant) *variant = (kernel == 2 && b->solve_lowreg) ? 1 : 0;
+  return 0;
+}
+
 int odegpuBatchSetStepKernels(odegpuBatchID b, int fused) {
   if (!b || (fused != 0 && fused != 1)) return fail(ODEGPU_E_ARG, "bad arguments");
   b->fused = fused != 0;
@@ -1350,14 +1392,19 @@ int odegpuBatchAutotune(odegpuBatchID b, int n_steps) {
   int best_w[3] = {b->kwpb[0], b->kwpb[1], b->kwpb[2]}, best_c[3] = {b->kcarve[0], b->kcarve[1], b->kcarve[2]};
   StepOptions opt{1, nullptr, nullptr, nullptr, 0, 0};
   b->timing = true;
-  const bool saved_fused = b->fused;
+  const bool saved_fused = b->fused, saved_lowreg = b->solve_lowreg;
   b->fused = false;
+  bool best_lowreg = saved_lowreg;
   int rc = 0;
+  // every shape of the three kernels with the 168-register solve kernel, then
+  // the solve kernel's shapes with its 128-register budget
+  for (int v = 0; v < 2 && !rc; ++v)
   for (int wi = 0; wi < 4 && !rc; ++wi) {
     for (int ci = 0; ci < 5 && !rc; ++ci) {
       bool tried[3];
+      b->solve_lowreg = v == 1;
       for (int k = 0; k < 3; ++k) {
-        tried[k] = kWpb[wi] <= kMaxWpb[k];
+        tried[k] = kWpb[wi] <= kMaxWpb[k] && (v == 0 || k == 2);
         b->kwpb[k] = tried[k] ? kWpb[wi] : best_w[k];
         b->kcarve[k] = tried[k] ? kCarve[ci] : best_c[k];
       }
@@ -1374,10 +1421,16 @@ int odegpuBatchAutotune(odegpuBatchID b, int n_steps) {
           ms[k] += t;
         }
       for (int k = 0; k < 3; ++k)
-        if (tried[k] && ms[k] < best[k]) { best[k] = ms[k]; best_w[k] = kWpb[wi]; best_c[k] = kCarve[ci]; }
+        if (tried[k] && ms[k] < best[k]) {
+          best[k] = ms[k];
+          best_w[k] = kWpb[wi];
+          best_c[k] = kCarve[ci];
+          if (k == 2) best_lowreg = v == 1;
+        }
     }
   }
   for (int k = 0; k < 3; ++k) { b->kwpb[k] = best_w[k]; b->kcarve[k] = best_c[k]; }
+  b->solve_lowreg = rc ? saved_lowreg : best_lowreg;
   // the fused step kernel: its shapes against the best split step (the sum of
   // the three kernels' best times)
   double best_f = INFINITY;

@@ -46,6 +46,8 @@ def _declare(L):
         "odegpuBatchSetLaunchConfig": (i, [v, i, i, i]),
         "odegpuBatchGetLaunchConfig": (i, [v, _P(i)]),
         "odegpuBatchSetStepKernels": (i, [v, i]),
+        "odegpuBatchSetLaunchConfigEx": (i, [v, i, i, i, i]),
+        "odegpuBatchGetLaunchConfigEx": (i, [v, i, _P(i), _P(i), _P(i)]),
         "odegpuBatchGetStepKernels": (i, [v, _P(i), _P(i), _P(i)]),
         "odegpuBatchAutotune": (i, [v, i]),
         "odegpuBatchGetFeedback": (i, [v, _P(d)]),

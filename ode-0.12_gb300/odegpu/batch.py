@@ -197,6 +197,18 @@ class Batch:
         """kernel: 0 collide, 1 setup, 2 solve, 3 adjoint, 4 fused step."""
         check(lib().odegpuBatchSetLaunchConfig(self.h, int(kernel), int(warps_per_block), int(smem_carveout)))
 
+    def set_launch_config_ex(self, kernel, warps_per_block, smem_carveout=-1, variant=0):
+        """As set_launch_config, with the kernel variant (1: the solve kernel
+        capped at 128 registers per thread for more warps per SM)."""
+        check(lib().odegpuBatchSetLaunchConfigEx(self.h, int(kernel), int(warps_per_block),
+                                                 int(smem_carveout), int(variant)))
+
+    def launch_config_ex(self, kernel):
+        """(warps per block, carveout, variant) of one kernel."""
+        w, c, v = C.c_int(), C.c_int(), C.c_int()
+        check(lib().odegpuBatchGetLaunchConfigEx(self.h, int(kernel), C.byref(w), C.byref(c), C.byref(v)))
+        return w.value, c.value, v.value
+
     def launch_config(self):
         cfg = (C.c_int * 8)()
         check(lib().odegpuBatchGetLaunchConfig(self.h, cfg))

@@ -199,6 +199,28 @@ def test_launch_modes_agree(batch_cls):
     assert np.array_equal(outs[0], outs[2])
 
 
+def test_solve_register_variants_agree(batch_cls):
+    """The solve kernel's two register budgets (168 per thread, or capped at
+    128) compile the same device code: 40 steps of a batch agree in contacts,
+    rows, islands and RNG state, and in state to FP32 rounding."""
+    sc = S.batched_worlds(n_worlds=64, seed=3)
+    outs = []
+    for variant in (0, 1):
+        B = batch_cls(sc)
+        w, c, _ = B.launch_config_ex(2)
+        B.set_launch_config_ex(2, w, c, variant)
+        assert B.launch_config_ex(2)[2] == variant
+        B.step(40)
+        outs.append((B.state(), B.seeds(), B.counts(), B.status()))
+        B.close()
+    (sa, ea, ca, ta), (sb, eb, cb, tb) = outs
+    assert (ta == 0).all() and (tb == 0).all()
+    for x, y in zip(ca, cb):
+        assert np.array_equal(x, y)
+    assert np.array_equal(ea, eb)
+    assert np.abs(sa - sb).max() < 1e-5, float(np.abs(sa - sb).max())
+
+
 def test_fused_step_matches_split_step(batch_cls):
     """The fused step kernel runs the split kernels' device code on one warp
     per world; compiled into another kernel, the arithmetic may contract into
