@@ -264,7 +264,9 @@ typedef struct {
   int geom;            /* world-local geom index of the nearest hit; -1: no hit;
                           -2: invalid ray (world / body out of range, length
                           negative or not finite); -3: a heightfield zone under
-                          the ray exceeds the lane's 10 x 10 samples */
+                          the ray exceeds the lane's 10 x 10 samples (the
+                          device entry only: the host entry casts such rays
+                          again with workspaces of up to 128 x 128 samples) */
   float pos[3];        /* dContactGeom pos, normal, depth of dCollide(ray, geom) */
   float normal[3];
   float depth;

@@ -261,6 +261,9 @@ struct odegpuBatch {
   DBuf<float> state_scratch;
   DBuf<odegpuRay> ray_in;          // odegpuBatchRayCast staging, grown on demand
   DBuf<odegpuRayHit> ray_out;
+  DBuf<unsigned char> ray_ws;      // heightfield workspaces of the second ray pass
+  DBuf<int> ray_list;              // rays of the second pass
+  double hf_min_spacing = 0.0;     // finest sample spacing of the batch's heightfields (0: none)
   bool exact = false;              // dWorldStep instead of dWorldQuickStep
   // dWorldStep scratch (world_exact.cuh). A step outside a graph sizes each
   // world's region by the rows its joints and this step's contacts can need
@@ -967,6 +970,10 @@ int odegpuBatchCreate(const odegpuScene* sc, const odegpuBatchConfig* cfg, odegp
       const DevHeightfield& D = hfs[(int)sc->geom_param[ODEGPU_GEOM_NPARAM * (size_t)g]];
       gpos[g] = make_float4(D.pos[0], D.pos[1], D.pos[2], 0.f);
     }
+  for (int i = 0; i < sc->n_heightfields; ++i) {
+    const double sp = std::min(hfs[i].sw, hfs[i].sd);
+    B->hf_min_spacing = B->hf_min_spacing > 0.0 ? std::min(B->hf_min_spacing, sp) : sp;
+  }
   std::vector<DevSurface> surf(std::max(1, sc->n_surfaces));
   for (int s = 0; s < sc->n_surfaces; ++s) {
     const odegpuSurface& S = sc->surfaces[s];
@@ -1744,7 +1751,8 @@ int odegpuBatchRayCastAsync(odegpuBatchID b, const odegpuRay* d_rays, int n, int
   OG_CUDA(cudaSetDevice(b->device));
   constexpr int kThreads = 128;   // 4 rays per block, one warp each
   const long long blocks = ((long long)n * 32 + kThreads - 1) / kThreads;
-  raycast_kernel<<<(unsigned)blocks, kThreads, 0, b->stream>>>(b->dev(), d_rays, n, (unsigned)flags, d_hits);
+  raycast_kernel<<<(unsigned)blocks, kThreads, 0, b->stream>>>(b->dev(), d_rays, nullptr, n, (unsigned)flags, d_hits,
+                                                                RayBig{nullptr, 0, 0});
   b->launches += 1;
   OG_CUDA(cudaGetLastError());
   return 0;
@@ -1772,6 +1780,36 @@ int odegpuBatchRayCast(odegpuBatchID b, const odegpuRay* rays, int n, int flags,
   OG_CUDA(cudaMemcpyAsync(hits, b->ray_out.p, (size_t)n * sizeof(odegpuRayHit), cudaMemcpyDeviceToHost,
                           b->stream));
   OG_CUDA(cudaStreamSynchronize(b->stream));
+  // rays whose heightfield zone exceeded the lane's arrays: cast again with
+  // a workspace per warp, sized by the longest of them on the finest field
+  std::vector<int> again;
+  for (int i = 0; i < n; ++i)
+    if (hits[i].geom == -3) again.push_back(i);
+  if (!again.empty() && b->hf_min_spacing > 0.0) {
+    double longest = 0.0;
+    for (int i : again) longest = std::max(longest, (double)rays[i].length);
+    const int side = std::min(kHFBigZone, hf_zone_side(0.5 * longest, b->hf_min_spacing));
+    const int warps = std::min<int>((int)again.size(), 256);
+    const long long stride = (hf_ws_bytes(side) + 255) & ~255LL;
+    auto grow_buf = [](auto& buf, size_t cnt) -> int {
+      if (buf.p && buf.n >= cnt) return 0;
+      if (buf.p) { cudaFree(buf.p); buf.p = nullptr; }
+      return buf.alloc(cnt);
+    };
+    if (int rc = grow_buf(b->ray_ws, (size_t)(stride * warps))) return rc;
+    if (int rc = grow_buf(b->ray_list, again.size())) return rc;
+    OG_CUDA(cudaMemcpyAsync(b->ray_list.p, again.data(), again.size() * sizeof(int), cudaMemcpyHostToDevice,
+                            b->stream));
+    constexpr int kThreads = 128;
+    raycast_kernel<<<(unsigned)((warps * 32 + kThreads - 1) / kThreads), kThreads, 0, b->stream>>>(
+        b->dev(), b->ray_in.p, b->ray_list.p, (int)again.size(), (unsigned)flags, b->ray_out.p,
+        RayBig{b->ray_ws.p, stride, side});
+    b->launches += 1;
+    OG_CUDA(cudaGetLastError());
+    OG_CUDA(cudaMemcpyAsync(hits, b->ray_out.p, (size_t)n * sizeof(odegpuRayHit), cudaMemcpyDeviceToHost,
+                            b->stream));
+    OG_CUDA(cudaStreamSynchronize(b->stream));
+  }
   int nhit = 0;
   for (int i = 0; i < n; ++i) nhit += hits[i].geom >= 0;
   return nhit;

@@ -275,7 +275,8 @@ def test_batch_ray_cast_vehicles_vs_oracle():
     """Vehicle worlds after 30 steps: body-attached suspension probes (the
     chassis' own geoms skipped) and world-frame rays at the cars, against the
     oracle's FP64 dCollide over every geom of the world: the same geom hit,
-    records within 2e-4 (rays of up to 2.5 m in FP32)."""
+    records within 2e-4 (rays of up to 2.5 m in FP32; 1e-3 for the rays of
+    10 to 30 m)."""
     from odegpu.batch import Batch
     sc = S.vehicles(n_worlds=6, steps=40, hf_samples=64)
     B = Batch(sc)
@@ -290,12 +291,31 @@ def test_batch_ray_cast_vehicles_vs_oracle():
         # every suspension probe hits the terrain or a wheel
         probes = hits[np.asarray(rays["body"]) == 0]
         assert (probes["geom"] >= 0).all(), probes
-    # a ray whose heightfield zone exceeds the collider's buffers is refused
-    # (geom -3) rather than answered from part of the zone
-    b0, _ = sc.world_bodies(0)
-    far = np.array([(0, -1, tuple(sc.body_pos[b0] + np.array([0, 0, 3.0])), (1.0, 0.3, -0.05), 30.0)],
-                   dtype=_ray_dtype())
-    assert B.ray_cast(far)["geom"][0] == -3
+    # rays whose heightfield zone exceeds the lane's 10 x 10 samples (10 to
+    # 30 m over the 0.5 m field): the host entry casts them again with a
+    # workspace per warp and answers them as the oracle does; the device
+    # entry, which has no workspace, refuses them (geom -3) rather than
+    # answering from part of the zone
+    import torch
+    from odegpu.batch import HIT_DTYPE
+    far = []
+    for w in range(sc.n_worlds):
+        b0, _ = sc.world_bodies(w)
+        for _ in range(6):
+            start = sc.body_pos[b0] + np.array([0, 0, 3.0]) + rng.normal(size=3)
+            aim = np.array([rng.uniform(-1, 1), rng.uniform(-1, 1), rng.uniform(-0.25, -0.02)])
+            far.append((w, -1, tuple(start), tuple(aim), float(rng.uniform(10.0, 30.0))))
+    far = np.array(far, dtype=_ray_dtype())
+    hits = B.ray_cast(far, flags=1)
+    assert (hits["geom"] != -3).all(), hits["geom"]
+    nhit = _compare(sc, state, far, hits, 1, 1e-3)
+    assert nhit > len(far) // 4, nhit
+    d_rays = torch.from_numpy(far.view(np.uint8).copy()).cuda()
+    d_hits = torch.zeros(len(far) * HIT_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+    torch.cuda.synchronize()
+    B.ray_cast_async(d_rays.data_ptr(), len(far), d_hits.data_ptr(), flags=1)
+    B.sync()
+    assert (d_hits.cpu().numpy().view(HIT_DTYPE)["geom"] == -3).any()
     B.close()
 
 
