@@ -112,13 +112,19 @@ OG_D void vjp_rar(const float* R, const float* A, const float* Mb, float* Rb) {
     }
 }
 
-// One 128-byte row with eight 16-byte loads (the row store is 128-byte aligned).
-OG_D void load_row_words(const float* row, float* J, float* iMJ, float& b, float& cfmA, float& lo, float& hi,
-                         int& f, int& b1, int& b2) {
-  const float4* r4 = reinterpret_cast<const float4*>(row);
-  float4 v[8];
+// A chunk's row for this lane (idle lanes past the chunk's end load its last
+// row again and are masked out): the row index and its eight 16-byte words.
+OG_D bool adj_chunk_row(const float* rows, const SorSmem& S, unsigned c, int lane, int& r, float4 (&v)[8]) {
+  const int last = (int)(c >> 11);
+  const bool active = lane <= last;
+  r = S.exec[(c & 0x7ffu) + (active ? lane : last)];
+  const float4* src = reinterpret_cast<const float4*>(rows + (size_t)r * kRowWords);
 #pragma unroll
-  for (int k = 0; k < 8; ++k) v[k] = r4[k];
+  for (int k = 0; k < 8; ++k) v[k] = src[k];
+  return active;
+}
+OG_D void unpack_row_words(const float4 (&v)[8], float* J, float* iMJ, float& b, float& cfmA, float& lo, float& hi,
+                           int& f, int& b1, int& b2) {
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     J[4 * k] = v[k].x; J[4 * k + 1] = v[k].y; J[4 * k + 2] = v[k].z; J[4 * k + 3] = v[k].w;
@@ -128,6 +134,39 @@ OG_D void load_row_words(const float* row, float* J, float* iMJ, float& b, float
   f = __float_as_int(v[7].x);
   b1 = __float_as_int(v[7].y);
   b2 = __float_as_int(v[7].z);
+}
+
+// One row update of the replayed sweep (the forward's arithmetic), recording
+// lambda before the update and the bound that clamped it, if any.
+OG_D void adj_replay_row(const float4 (&v)[8], int r, const SorSmem& S, float* lamT, unsigned char* codeT,
+                         size_t tap) {
+  float Jp[12], iMJ[12], bb, cfmA, lo, hi;
+  int f, b1, b2;
+  unpack_row_words(v, Jp, iMJ, bb, cfmA, lo, hi, f, b1, b2);
+  float* fc1 = S.fc + 6 * b1;
+  float* fc2 = S.fc + 6 * (b2 >= 0 ? b2 : kMaxB);
+  const float old = S.lambda[r];
+  lamT[tap + r] = old;
+  float delta = bb - old * cfmA;
+  delta -= (fc1[0] * Jp[0] + fc1[1] * Jp[1]) + (fc1[2] * Jp[2] + fc1[3] * Jp[3]) +
+           (fc1[4] * Jp[4] + fc1[5] * Jp[5]);
+  delta -= (fc2[0] * Jp[6] + fc2[1] * Jp[7]) + (fc2[2] * Jp[8] + fc2[3] * Jp[9]) +
+           (fc2[4] * Jp[10] + fc2[5] * Jp[11]);
+  float lo_act = lo, hi_act = hi;
+  if (f >= 0) {
+    hi_act = fabsf(hi * S.lambda[f]);
+    lo_act = -hi_act;
+  }
+  const float nl = old + delta;
+  unsigned char code = 0;
+  float lam_new = nl;
+  if (nl < lo_act) { code = 1; lam_new = lo_act; delta = lo_act - old; }
+  else if (nl > hi_act) { code = 2; lam_new = hi_act; delta = hi_act - old; }
+  codeT[tap + r] = code;
+  S.lambda[r] = lam_new;
+  for (int q = 0; q < 6; ++q) fc1[q] += delta * iMJ[q];
+  if (b2 >= 0)
+    for (int q = 0; q < 6; ++q) fc2[q] += delta * iMJ[6 + q];
 }
 
 // Derivative of the rows of persistent joint `ord` (rows r0..r0+m-1) with
@@ -732,8 +771,60 @@ OG_D void adj_shuffle(const int* rstart, int nisl, int n_shuffles, int round, un
   __syncwarp();
 }
 
+// One row of the sweep backwards: the row's state before its update in the
+// replayed sweep (lambda from the tape, fc by undoing the update), the
+// derivative through the update's clamp case, accumulated into the row's
+// record, d/dlambda and d/dfc.
+OG_D void adj_reverse_row(const float4 (&v)[8], int r, float old, unsigned char code, const SorSmem& S, float* fcb,
+                          float* lamb, float* rt0) {
+  float Jp[12], iMJ[12], bb, cfmA, lo, hi;
+  int f, b1, b2;
+  unpack_row_words(v, Jp, iMJ, bb, cfmA, lo, hi, f, b1, b2);
+  float4* rt4 = reinterpret_cast<float4*>(rt0 + r * kAdjRow);   // 112-byte records, 16-byte aligned
+  float acc[kAdjRow];
+#pragma unroll
+  for (int q = 0; q < 7; ++q) {
+    const float4 t = rt4[q];
+    acc[4 * q] = t.x; acc[4 * q + 1] = t.y; acc[4 * q + 2] = t.z; acc[4 * q + 3] = t.w;
+  }
+  const float dl = S.lambda[r] - old;
+  float* fc1 = S.fc + 6 * b1;
+  float* fb1 = fcb + 6 * b1;
+  float* fc2 = b2 >= 0 ? S.fc + 6 * b2 : nullptr;
+  float* fb2 = b2 >= 0 ? fcb + 6 * b2 : nullptr;
+  // fc before the update
+  for (int q = 0; q < 6; ++q) fc1[q] -= dl * iMJ[q];
+  if (fc2) for (int q = 0; q < 6; ++q) fc2[q] -= dl * iMJ[6 + q];
+  float dlb = 0.f;
+  for (int q = 0; q < 6; ++q) { dlb += iMJ[q] * fb1[q]; acc[kRiMJ + q] += dl * fb1[q]; }
+  if (fc2)
+    for (int q = 0; q < 6; ++q) { dlb += iMJ[6 + q] * fb2[q]; acc[kRiMJ + 6 + q] += dl * fb2[q]; }
+  const float lnb = lamb[r] + dlb;
+  float oldb = -dlb;
+  float ub = 0.f;
+  if (code == 0) {
+    ub = lnb;
+  } else if (f >= 0) {
+    const float lf = S.lambda[f];
+    const float dbound = (hi * lf >= 0.f) ? hi : -hi;   // d|hi lf| / dlf
+    lamb[f] += (code == 2 ? lnb : -lnb) * dbound;
+  }
+  // u = old + b' - old cfmA - J'.fc
+  oldb += ub * (1.f - cfmA);
+  acc[kRb] += ub;
+  acc[kRcfm] -= ub * old;
+  for (int q = 0; q < 6; ++q) { acc[kRJ + q] -= ub * fc1[q]; fb1[q] -= ub * Jp[q]; }
+  if (fc2)
+    for (int q = 0; q < 6; ++q) { acc[kRJ + 6 + q] -= ub * fc2[q]; fb2[q] -= ub * Jp[6 + q]; }
+#pragma unroll
+  for (int q = 0; q < 7; ++q)
+    rt4[q] = make_float4(acc[4 * q], acc[4 * q + 1], acc[4 * q + 2], acc[4 * q + 3]);
+  lamb[r] = oldb;
+  S.lambda[r] = old;
+}
+
 // One warp per world: the adjoint of one step (see the file comment).
-__global__ void __launch_bounds__(128) adjoint_step_kernel(BatchDev d, AdjDev a, int step) {
+__global__ void __launch_bounds__(128, 1) adjoint_step_kernel(BatchDev d, AdjDev a, int step) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & 31;
   const int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
@@ -790,38 +881,19 @@ __global__ void __launch_bounds__(128) adjoint_step_kernel(BatchDev d, AdjDev a,
         for (int i = lane; i < M; i += 32) seqT[(size_t)(it >> 3) * rc + i] = S.seq[i];
         nchunk = sor_schedule(rows, D.nb, S, M, lane);
       }
-      for (int k = 0; k < nchunk; ++k) {
-        const unsigned c = S.chunk[k];
-        if (lane <= (int)(c >> 11)) {
-          const int r = S.exec[(c & 0x7ffu) + lane];
-          float Jp[12], iMJ[12], bb, cfmA, lo, hi;
-          int f, b1, b2;
-          load_row_words(rows + (size_t)r * kRowWords, Jp, iMJ, bb, cfmA, lo, hi, f, b1, b2);
-          float* fc1 = S.fc + 6 * b1;
-          float* fc2 = S.fc + 6 * (b2 >= 0 ? b2 : kMaxB);
-          const float old = S.lambda[r];
-          lamT[(size_t)it * rc + r] = old;
-          float delta = bb - old * cfmA;
-          delta -= (fc1[0] * Jp[0] + fc1[1] * Jp[1]) + (fc1[2] * Jp[2] + fc1[3] * Jp[3]) +
-                   (fc1[4] * Jp[4] + fc1[5] * Jp[5]);
-          delta -= (fc2[0] * Jp[6] + fc2[1] * Jp[7]) + (fc2[2] * Jp[8] + fc2[3] * Jp[9]) +
-                   (fc2[4] * Jp[10] + fc2[5] * Jp[11]);
-          float lo_act = lo, hi_act = hi;
-          if (f >= 0) {
-            hi_act = fabsf(hi * S.lambda[f]);
-            lo_act = -hi_act;
-          }
-          const float nl = old + delta;
-          unsigned char code = 0;
-          float lam_new = nl;
-          if (nl < lo_act) { code = 1; lam_new = lo_act; delta = lo_act - old; }
-          else if (nl > hi_act) { code = 2; lam_new = hi_act; delta = hi_act - old; }
-          codeT[(size_t)it * rc + r] = code;
-          S.lambda[r] = lam_new;
-          for (int q = 0; q < 6; ++q) fc1[q] += delta * iMJ[q];
-          if (b2 >= 0)
-            for (int q = 0; q < 6; ++q) fc2[q] += delta * iMJ[6 + q];
-        }
+      // the next chunk's rows are loaded while a chunk updates (two register
+      // buffers used in turn)
+      const size_t tap = (size_t)it * rc;
+      float4 va[8], vb[8];
+      int ra = 0, rb = 0;
+      bool aa = nchunk > 0 && adj_chunk_row(rows, S, S.chunk[0], lane, ra, va), ab = false;
+      for (int k = 0; k < nchunk; k += 2) {
+        if (k + 1 < nchunk) ab = adj_chunk_row(rows, S, S.chunk[k + 1], lane, rb, vb);
+        if (aa) adj_replay_row(va, ra, S, lamT, codeT, tap);
+        __syncwarp();
+        if (k + 1 >= nchunk) break;
+        if (k + 2 < nchunk) aa = adj_chunk_row(rows, S, S.chunk[k + 2], lane, ra, va);
+        if (ab) adj_replay_row(vb, rb, S, lamT, codeT, tap);
         __syncwarp();
       }
     }
@@ -896,57 +968,34 @@ __global__ void __launch_bounds__(128) adjoint_step_kernel(BatchDev d, AdjDev a,
         __syncwarp();
         nchunk = sor_schedule(rows, D.nb, S, M, lane);
       }
-      for (int k = nchunk - 1; k >= 0; --k) {
-        const unsigned c = S.chunk[k];
-        if (lane <= (int)(c >> 11)) {
-          const int r = S.exec[(c & 0x7ffu) + lane];
-          float Jp[12], iMJ[12], bb, cfmA, lo, hi;
-          int f, b1, b2;
-          load_row_words(rows + (size_t)r * kRowWords, Jp, iMJ, bb, cfmA, lo, hi, f, b1, b2);
-          float4* rt4 = reinterpret_cast<float4*>(rt0 + r * kAdjRow);   // 112-byte records, 16-byte aligned
-          float acc[kAdjRow];
-#pragma unroll
-          for (int q = 0; q < 7; ++q) {
-            const float4 t = rt4[q];
-            acc[4 * q] = t.x; acc[4 * q + 1] = t.y; acc[4 * q + 2] = t.z; acc[4 * q + 3] = t.w;
-          }
-          const float old = lamT[(size_t)it * rc + r];
-          const unsigned char code = codeT[(size_t)it * rc + r];
-          const float dl = S.lambda[r] - old;
-          float* fc1 = S.fc + 6 * b1;
-          float* fb1 = fcb + 6 * b1;
-          float* fc2 = b2 >= 0 ? S.fc + 6 * b2 : nullptr;
-          float* fb2 = b2 >= 0 ? fcb + 6 * b2 : nullptr;
-          // fc before the update
-          for (int q = 0; q < 6; ++q) fc1[q] -= dl * iMJ[q];
-          if (fc2) for (int q = 0; q < 6; ++q) fc2[q] -= dl * iMJ[6 + q];
-          float dlb = 0.f;
-          for (int q = 0; q < 6; ++q) { dlb += iMJ[q] * fb1[q]; acc[kRiMJ + q] += dl * fb1[q]; }
-          if (fc2)
-            for (int q = 0; q < 6; ++q) { dlb += iMJ[6 + q] * fb2[q]; acc[kRiMJ + 6 + q] += dl * fb2[q]; }
-          const float lnb = lamb[r] + dlb;
-          float oldb = -dlb;
-          float ub = 0.f;
-          if (code == 0) {
-            ub = lnb;
-          } else if (f >= 0) {
-            const float lf = S.lambda[f];
-            const float dbound = (hi * lf >= 0.f) ? hi : -hi;   // d|hi lf| / dlf
-            lamb[f] += (code == 2 ? lnb : -lnb) * dbound;
-          }
-          // u = old + b' - old cfmA - J'.fc
-          oldb += ub * (1.f - cfmA);
-          acc[kRb] += ub;
-          acc[kRcfm] -= ub * old;
-          for (int q = 0; q < 6; ++q) { acc[kRJ + q] -= ub * fc1[q]; fb1[q] -= ub * Jp[q]; }
-          if (fc2)
-            for (int q = 0; q < 6; ++q) { acc[kRJ + 6 + q] -= ub * fc2[q]; fb2[q] -= ub * Jp[6 + q]; }
-#pragma unroll
-          for (int q = 0; q < 7; ++q)
-            rt4[q] = make_float4(acc[4 * q], acc[4 * q + 1], acc[4 * q + 2], acc[4 * q + 3]);
-          lamb[r] = oldb;
-          S.lambda[r] = old;
+      // the next chunk's rows and tape entries are loaded while a chunk is
+      // reversed (two register buffers used in turn)
+      const size_t tap = (size_t)it * rc;
+      float4 va[8], vb[8];
+      int ra = 0, rb = 0;
+      float oa = 0.f, ob = 0.f;
+      unsigned char ca = 0, cb = 0;
+      bool aa = false, ab = false;
+      if (nchunk > 0) {
+        aa = adj_chunk_row(rows, S, S.chunk[nchunk - 1], lane, ra, va);
+        oa = lamT[tap + ra];
+        ca = codeT[tap + ra];
+      }
+      for (int k = nchunk - 1; k >= 0; k -= 2) {
+        if (k - 1 >= 0) {
+          ab = adj_chunk_row(rows, S, S.chunk[k - 1], lane, rb, vb);
+          ob = lamT[tap + rb];
+          cb = codeT[tap + rb];
         }
+        if (aa) adj_reverse_row(va, ra, oa, ca, S, fcb, lamb, rt0);
+        __syncwarp();
+        if (k - 1 < 0) break;
+        if (k - 2 >= 0) {
+          aa = adj_chunk_row(rows, S, S.chunk[k - 2], lane, ra, va);
+          oa = lamT[tap + ra];
+          ca = codeT[tap + ra];
+        }
+        if (ab) adj_reverse_row(vb, rb, ob, cb, S, fcb, lamb, rt0);
         __syncwarp();
       }
     }
