@@ -175,6 +175,7 @@ struct HFLocalZone {
   Idx pfirst[kHFMaxTri], pcount[kHFMaxTri];
   float pmax[kHFMaxTri];
   Idx porder[kHFMaxTri];                 // planes in sorted order
+  Idx tord[kHFMaxTri], trank[kHFMaxTri]; // triangles by plane offset, and each one's place there
 };
 constexpr int kHFBigZone = 128;          // samples per axis of a global workspace, at most
 struct HFGlobalZone {
@@ -192,6 +193,8 @@ struct HFGlobalZone {
   Idx* pcount;
   float* pmax;
   Idx* porder;
+  Idx* tord;
+  Idx* trank;
 };
 static_assert(kHFZone * kHFZone <= 256 && kHFMaxTri <= 255, "local zone indices are 8-bit");
 static_assert(kHFBigZone * kHFBigZone <= 65536 && 2 * (kHFBigZone - 1) * (kHFBigZone - 1) <= 65535,
@@ -204,7 +207,7 @@ OG_HD constexpr long long hf_ws_bytes(int side) {
          hf_ws_align(8LL * 2 * (side - 1) * (side - 1)) + hf_ws_align(16LL * 2 * (side - 1) * (side - 1)) +
          hf_ws_align(4LL * 2 * (side - 1) * (side - 1)) + hf_ws_align(1LL * 2 * (side - 1) * (side - 1)) +
          3 * hf_ws_align(2LL * 2 * (side - 1) * (side - 1)) + hf_ws_align(4LL * 2 * (side - 1) * (side - 1)) +
-         hf_ws_align(2LL * 2 * (side - 1) * (side - 1));
+         3 * hf_ws_align(2LL * 2 * (side - 1) * (side - 1));
 }
 OG_D HFGlobalZone carve_hf_ws(unsigned char* p, int side) {
   const long long S = (long long)side * side, T = 2LL * (side - 1) * (side - 1);
@@ -219,7 +222,9 @@ OG_D HFGlobalZone carve_hf_ws(unsigned char* p, int side) {
   z.pfirst = reinterpret_cast<unsigned short*>(p); p += hf_ws_align(2 * T);
   z.pcount = reinterpret_cast<unsigned short*>(p); p += hf_ws_align(2 * T);
   z.pmax = reinterpret_cast<float*>(p); p += hf_ws_align(4 * T);
-  z.porder = reinterpret_cast<unsigned short*>(p);
+  z.porder = reinterpret_cast<unsigned short*>(p); p += hf_ws_align(2 * T);
+  z.tord = reinterpret_cast<unsigned short*>(p); p += hf_ws_align(2 * T);
+  z.trank = reinterpret_cast<unsigned short*>(p);
   return z;
 }
 
@@ -323,51 +328,103 @@ OG_D int hf_zone(Z& z, const DevHeightfield& H, const float* heights, int minX, 
     n[0] *= il; n[1] *= il; n[2] *= il;
     tp[k] = make_float4(n[0], n[1], n[2], dot3(n, v0));
   }
-  // group by equal plane definition, in triangle order
+  // group by equal plane definition, in triangle order: triangle k, when no
+  // earlier plane took it, leads a plane and takes every later untaken
+  // triangle whose plane matches within dEpsilon in all four components
+  // (heightfield.cpp:1395-1440). Those candidates lie within dEpsilon of k's
+  // offset, so they are found in a window of the triangles sorted by offset
+  // instead of by a scan of every later triangle; a leader's matches are then
+  // put back in triangle order.
   Idx* members = z.members;             // triangles, grouped by plane
   Idx* pfirst = z.pfirst;
   Idx* pcount = z.pcount;
   float* pmax = z.pmax;
   Idx* porder = z.porder;               // planes in sorted order
+  Idx* tord = z.tord;
+  Idx* trank = z.trank;
+  for (int k = 0; k < numTri; ++k) tord[k] = (Idx)k;
+  {
+    // Shell sort by offset (Ciura's gaps); the order among equal offsets does
+    // not matter: every one of them lies in the window
+    const int gaps[12] = {19930, 8858, 3937, 1750, 701, 301, 132, 57, 23, 10, 4, 1};
+    for (int gi = 0; gi < 12; ++gi) {
+      const int gap = gaps[gi];
+      for (int i = gap; i < numTri; ++i) {
+        const Idx cur = tord[i];
+        const float key = tp[cur].w;
+        int j = i;
+        while (j >= gap && tp[tord[j - gap]].w > key) {
+          tord[j] = tord[j - gap];
+          j -= gap;
+        }
+        tord[j] = cur;
+      }
+    }
+  }
+  for (int i = 0; i < numTri; ++i) trank[tord[i]] = (Idx)i;
   int numPlanes = 0, nmem = 0;
   for (int k = 0; k < numTri; ++k) {
     if (tstate[k]) continue;
     const float4 b = tp[k];
     pfirst[numPlanes] = (Idx)nmem;
     members[nmem++] = (Idx)k;
-    int cnt = 1;
-    float mx = tmax[k];
-    for (int m = k + 1; m < numTri; ++m) {
-      if (tstate[m]) continue;
+    const int first_match = nmem;
+    auto take = [&](int m) {
+      if (m <= k || tstate[m]) return;
       const float4 t = tp[m];
-      if (fabsf(b.y - t.y) < kHFEps && fabsf(b.w - t.w) < kHFEps && fabsf(b.x - t.x) < kHFEps &&
-          fabsf(b.z - t.z) < kHFEps) {
+      if (fabsf(b.y - t.y) < kHFEps && fabsf(b.x - t.x) < kHFEps && fabsf(b.z - t.z) < kHFEps)
         members[nmem++] = (Idx)m;
-        ++cnt;
-        tstate[m] = 1;
-        if (tmax[m] > mx) mx = tmax[m];
+    };
+    for (int j = (int)trank[k] - 1; j >= 0 && b.w - tp[tord[j]].w < kHFEps; --j) take(tord[j]);
+    for (int j = (int)trank[k] + 1; j < numTri && tp[tord[j]].w - b.w < kHFEps; ++j) take(tord[j]);
+    // the matches in triangle order (the reference appends them as it scans)
+    for (int i = first_match + 1; i < nmem; ++i) {
+      const Idx cur = members[i];
+      int j = i;
+      while (j > first_match && members[j - 1] > cur) {
+        members[j] = members[j - 1];
+        --j;
       }
+      members[j] = cur;
+    }
+    float mx = tmax[k];
+    for (int i = first_match; i < nmem; ++i) {
+      const int m = members[i];
+      tstate[m] = 1;
+      if (tmax[m] > mx) mx = tmax[m];
     }
     tstate[k] = 1;
-    pcount[numPlanes] = (Idx)cnt;
+    pcount[numPlanes] = (Idx)(nmem - first_match + 1);
     pmax[numPlanes] = mx;
     porder[numPlanes] = (Idx)numPlanes;
     ++numPlanes;
   }
   // sortPlanes (heightfield.cpp:910-932) bubble-sorts the planes, swapping
   // neighbours whose first height exceeds the second by more than dEpsilon.
-  // An insertion sort with the same neighbour test performs only such swaps
-  // and yields the same order whenever heights are equal or further apart
-  // than dEpsilon; it needs far fewer passes.
-  for (int i = 1; i < numPlanes; ++i) {
-    const Idx cur = porder[i];
-    const float key = pmax[cur];
-    int j = i;
-    while (j > 0 && (pmax[porder[j - 1]] - key) > kHFEps) {
-      porder[j] = porder[j - 1];
-      --j;
+  // A stable merge sort with the same test (the right head goes first only
+  // when the left head is higher by more than dEpsilon) yields the same order
+  // whenever heights are equal or further apart than dEpsilon, in
+  // O(n log n) comparisons.
+  {
+    Idx* src = porder;
+    Idx* dst = tord;                    // free once the planes are grouped
+    for (int width = 1; width < numPlanes; width *= 2) {
+      for (int lo = 0; lo < numPlanes; lo += 2 * width) {
+        const int mid = min(lo + width, numPlanes), hi = min(lo + 2 * width, numPlanes);
+        int i = lo, j = mid, o = lo;
+        while (i < mid && j < hi) {
+          if (pmax[src[i]] - pmax[src[j]] > kHFEps) dst[o++] = src[j++];
+          else dst[o++] = src[i++];
+        }
+        while (i < mid) dst[o++] = src[i++];
+        while (j < hi) dst[o++] = src[j++];
+      }
+      Idx* t = src;
+      src = dst;
+      dst = t;
     }
-    porder[j] = cur;
+    if (src != porder)
+      for (int i = 0; i < numPlanes; ++i) porder[i] = src[i];
   }
   int nc = 0;
   const unsigned plane_flags = (flags & ~0xffffu) | kHFMaxcPerCell;
