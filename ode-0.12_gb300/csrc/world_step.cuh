@@ -46,6 +46,7 @@ struct WarpSmem {
   uint16_t* cand;     // [kMaxPairs] candidate pairs that pass the bound test
   float4* gpb;        // [kMaxB+8]   per geom: position (its body's, or its own when static), bound radius
   int16_t* gbd;       // [kMaxB+8]   per geom: body, -1 static
+  unsigned long long* jmask;   // [kMaxB] per body: the bodies a persistent joint joins it to
 };
 constexpr int kMaxPairs = (kMaxB + 8) * (kMaxB + 7) / 2;   // geoms: bodies + a few static
 // Per-warp sizes are rounded up to 16 bytes so that every warp's slice (and
@@ -53,7 +54,8 @@ constexpr int kMaxPairs = (kMaxB + 8) * (kMaxB + 7) / 2;   // geoms: bodies + a 
 constexpr int align16(int n) { return (n + 15) & ~15; }
 constexpr int kSmemPerWarp = align16(kMaxB * 6 * 4 + (kMaxB + 1) * 4 + (kMaxB + 1) * 2 + 2 * kMaxR * 2 +
                                      kMaxR * 2 + kMaxR * 2 + kMaxB * 2 + kMaxB + kMaxR + 32);
-constexpr int kCollideSmemPerWarp = align16(kMaxPairs * 2 + 16) + align16((kMaxB + 8) * 16) + align16((kMaxB + 8) * 2);
+constexpr int kCollideSmemPerWarp = align16(kMaxPairs * 2 + 16) + align16((kMaxB + 8) * 16) + align16((kMaxB + 8) * 2) +
+                                    align16(kMaxB * 8);
 static_assert(kSmemPerWarp % 16 == 0 && kCollideSmemPerWarp % 16 == 0, "per-warp slices must stay aligned");
 static_assert(kMaxB * 6 * sizeof(float) >= 6 * kMaxB * sizeof(int), "the island phase borrows the tmp1 area");
 
@@ -80,6 +82,8 @@ OG_D WarpSmem carve_collide_smem(unsigned char* base) {
   s.gpb = reinterpret_cast<float4*>(base);
   base += align16((kMaxB + 8) * 16);
   s.gbd = reinterpret_cast<int16_t*>(base);
+  base += align16((kMaxB + 8) * 2);
+  s.jmask = reinterpret_cast<unsigned long long*>(base);
   return s;
 }
 
@@ -181,6 +185,18 @@ OG_D int phase_collide(const BatchDev& d, const WorldDesc& D, int w, const WarpS
     S.gpb[g] = make_float4(p.x, p.y, p.z, d.gbound[gg]);
     S.gbd[g] = (int16_t)b;
   }
+  // the pairs of bodies a persistent joint joins, as one bit mask per body:
+  // the near-callback's dAreConnectedExcluding(b1, b2, dJointTypeContact)
+  // test (ode/src/ode.cpp:1529-1537) becomes one shared-memory load
+  for (int b = lane; b < D.nb; b += 32) S.jmask[b] = 0ull;
+  __syncwarp();
+  for (int j = lane; j < D.njp; j += 32) {
+    const DevJoint& J = d.joints[D.joint_off + j];
+    if (J.b1 >= 0 && J.b2 >= 0) {
+      atomicOr(&S.jmask[J.b1], 1ull << J.b2);
+      atomicOr(&S.jmask[J.b2], 1ull << J.b1);
+    }
+  }
   __syncwarp();
   int ncand = 0;
   for (int base = 0; base < npairs; base += 32) {
@@ -199,7 +215,7 @@ OG_D int phase_collide(const BatchDev& d, const WorldDesc& D, int w, const WarpS
           if (dx * dx + dy * dy + dz * dz > lim * lim) keep = false;
         }
       }
-      if (keep && bi >= 0 && bk >= 0 && jointed(d, D, w, bi, bk)) keep = false;
+      if (keep && bi >= 0 && bk >= 0 && ((S.jmask[bi] >> bk) & 1ull)) keep = false;
     }
     const unsigned bal = __ballot_sync(kFull, keep);
     if (keep) S.cand[ncand + __popc(bal & ((1u << lane) - 1u))] = (uint16_t)p;
