@@ -199,12 +199,14 @@ OG_D int phase_collide(const BatchDev& d, const WorldDesc& D, int w, const WarpS
   }
   __syncwarp();
   int ncand = 0;
+  // this lane's pair (i, k) of the canonical order, advanced 32 pairs a round
+  int pi = 0, pk = 1;
+  if (lane < npairs) unrank_pair(lane, ng, pi, pk);
   for (int base = 0; base < npairs; base += 32) {
     const int p = base + lane;
     bool keep = false;
     if (p < npairs) {
-      int i, k;
-      unrank_pair(p, ng, i, k);
+      const int i = pi, k = pk;
       const int bi = S.gbd[i], bk = S.gbd[k];
       keep = !((bi < 0 && bk < 0) || (bi == bk));
       if (keep) {
@@ -216,6 +218,13 @@ OG_D int phase_collide(const BatchDev& d, const WorldDesc& D, int w, const WarpS
         }
       }
       if (keep && bi >= 0 && bk >= 0 && ((S.jmask[bi] >> bk) & 1ull)) keep = false;
+      // 32 pairs on: row i holds the pairs (i, i+1 .. ng-1)
+      pk += 32;
+      while (pk >= ng && pi < ng - 2) {
+        const int over = pk - ng;
+        ++pi;
+        pk = pi + 1 + over;
+      }
     }
     const unsigned bal = __ballot_sync(kFull, keep);
     if (keep) S.cand[ncand + __popc(bal & ((1u << lane) - 1u))] = (uint16_t)p;
