@@ -1,4 +1,6 @@
-// sor.cuh -- SOR_LCP (ode/src/quickstep.cpp:342-584) for one world, one warp.
+// sor.cuh -- the level schedule of SOR_LCP (ode/src/quickstep.cpp:342-584)
+// that the adjoint replays and reverses, one warp per world (the forward step
+// schedules with sor_fwd.cuh; any valid schedule gives the same sweep).
 //
 // The reference sweeps the rows strictly in order. Here the sweep order of an
 // iteration (the concatenation of every island's current order) is turned into
@@ -8,9 +10,7 @@
 // so they run in parallel, and every body still receives its updates in the
 // reference's sequence order; a friction row reads lambda[findex] at the same
 // point as in the reference because it shares its bodies with its normal row.
-// Rows are bucketed by level and each level is processed in chunks of 32 lanes,
-// with the next chunk's rows (one 128-byte line each) loaded while the current
-// chunk computes.
+// Rows are bucketed by level and each level is cut into chunks of 32 lanes.
 #pragma once
 #include "world_step.cuh"
 
@@ -155,154 +155,10 @@ OG_D int sor_schedule(const float* rows, int nb, const SorSmem& S, int M, int la
   }
 }
 
-// One projected Gauss-Seidel row update (quickstep.cpp:484-582) on row data
-// held in registers; fc and lambda live in shared memory. Written without
-// branches so the lanes of a chunk never diverge: a missing second body reads
-// the zero slot kMaxB (its J and iMJ halves are zero) and is not written back,
-// and the friction bound is selected rather than branched on.
-OG_D void sor_row(const float4 (&rw)[8], int r, const SorSmem& S) {
-  const float* J = reinterpret_cast<const float*>(&rw[0]);
-  const float* iMJ = reinterpret_cast<const float*>(&rw[3]);
-  const float bb = rw[6].x, Ad = rw[6].y, lo = rw[6].z, hi = rw[6].w;
-  const int findex = __float_as_int(rw[7].x);
-  const int b1 = __float_as_int(rw[7].y), b2 = __float_as_int(rw[7].z);
-  const bool two = b2 >= 0;
-  float* fc1 = S.fc + 6 * b1;
-  float* fc2 = S.fc + 6 * (two ? b2 : kMaxB);
-  const float old = S.lambda[r];
-  const float lf = S.lambda[findex >= 0 ? findex : kMaxR];
-  const float f10 = fc1[0], f11 = fc1[1], f12 = fc1[2], f13 = fc1[3], f14 = fc1[4], f15 = fc1[5];
-  const float f20 = fc2[0], f21 = fc2[1], f22 = fc2[2], f23 = fc2[3], f24 = fc2[4], f25 = fc2[5];
-  float delta = bb - old * Ad;
-  // the 6-term dot products are summed pairwise (shorter dependency chains
-  // than the reference's left-to-right sums; same terms)
-  delta -= (f10 * J[0] + f11 * J[1]) + (f12 * J[2] + f13 * J[3]) + (f14 * J[4] + f15 * J[5]);
-  delta -= (f20 * J[6] + f21 * J[7]) + (f22 * J[8] + f23 * J[9]) + (f24 * J[10] + f25 * J[11]);
-  const float hf = fabsf(hi * lf);
-  const float hi_act = findex >= 0 ? hf : hi;
-  const float lo_act = findex >= 0 ? -hf : lo;
-  const float nl = old + delta;
-  // the reference keeps delta when no bound is hit and uses bound - old otherwise
-  const bool clamped = (nl < lo_act) || (nl > hi_act);
-  const float lam = fminf(fmaxf(nl, lo_act), hi_act);
-  delta = clamped ? lam - old : delta;
-  S.lambda[r] = clamped ? lam : nl;
-  fc1[0] = f10 + delta * iMJ[0]; fc1[1] = f11 + delta * iMJ[1]; fc1[2] = f12 + delta * iMJ[2];
-  fc1[3] = f13 + delta * iMJ[3]; fc1[4] = f14 + delta * iMJ[4]; fc1[5] = f15 + delta * iMJ[5];
-  if (two) {
-    fc2[0] = f20 + delta * iMJ[6]; fc2[1] = f21 + delta * iMJ[7]; fc2[2] = f22 + delta * iMJ[8];
-    fc2[3] = f23 + delta * iMJ[9]; fc2[4] = f24 + delta * iMJ[10]; fc2[5] = f25 + delta * iMJ[11];
-  }
-}
-
-// Row data of an idle lane: no effect (zero J and iMJ, bounds 0, first body is
-// the zero slot, lambda slot kMaxR).
-OG_D void idle_row(float4 (&rw)[8]) {
-#pragma unroll
-  for (int q = 0; q < 7; ++q) rw[q] = make_float4(0.f, 0.f, 0.f, 0.f);
-  rw[7] = make_float4(__int_as_float(-1), __int_as_float(kMaxB), __int_as_float(-1), 0.f);
-}
-
 OG_D void load_row(const float* rows, int r, float4 (&rw)[8]) {
   const float4* src = reinterpret_cast<const float4*>(rows + (size_t)r * kRowWords);
 #pragma unroll
   for (int q = 0; q < 8; ++q) rw[q] = __ldg(src + q);
-}
-
-// SOR over every island of the world. island_rstart: [nisl+1] world rows.
-// Returns the RNG state after the step (the islands' shuffles consume ODE's
-// stream in island order, ceil(iters/8) * (m - 1) draws each).
-OG_D unsigned sor_world(const float* rows, const int* rstart, int nb, int M, int nisl, int iters,
-                        unsigned seed, const SorSmem& S, int lane) {
-  for (int i = lane; i < nb * 6; i += 32) S.fc[i] = 0.f;
-  if (lane < 6) S.fc[kMaxB * 6 + lane] = 0.f;
-  for (int i = lane; i < M; i += 32) S.lambda[i] = 0.f;
-  if (lane == 0) S.lambda[kMaxR] = 0.f;
-  const int n_shuffles = (iters + 7) / 8;
-  // initial order per island: findex == -1 rows first (ascending), the rest
-  // from the island's tail backwards (quickstep.cpp:405-425)
-  for (int isl = 0; isl < nisl; ++isl) {
-    const int rs = rstart[isl], re = rstart[isl + 1];
-    int negc = 0;
-    for (int base = rs; base < re; base += 32) {
-      const int r = base + lane;
-      bool neg = false;
-      if (r < re) neg = reinterpret_cast<const int*>(rows + (size_t)r * kRowWords)[kRowFindex] == -1;
-      const unsigned bal = __ballot_sync(kFull, neg && r < re);
-      const int negb = negc + __popc(bal & ((1u << lane) - 1u));
-      if (r < re) {
-        const int nonnegb = (r - rs) - negb;
-        const int p = neg ? rs + negb : re - 1 - nonnegb;
-        S.seq[p] = (uint16_t)r;
-      }
-      negc += __popc(bal);
-    }
-  }
-  __syncwarp();
-  unsigned total_draws = 0;
-  for (int isl = 0; isl < nisl; ++isl) {
-    const int m = rstart[isl + 1] - rstart[isl];
-    if (m > 0) total_draws += (unsigned)(n_shuffles * (m - 1));
-  }
-  int nchunk = 0;
-  for (int it = 0; it < iters; ++it) {
-    if ((it & 7) == 0) {
-      const int round = it >> 3;
-      unsigned prefix = 0;
-      for (int ib = 0; ib < nisl; ib += 32) {
-        const int isl = ib + lane;
-        int m = 0;
-        if (isl < nisl) m = rstart[isl + 1] - rstart[isl];
-        const int draws = m > 0 ? n_shuffles * (m - 1) : 0;
-        const int incl = warp_incl_scan(draws, lane);
-        if (isl < nisl && m > 1) {
-          unsigned s = lcg_jump(seed, prefix + (unsigned)(incl - draws) + (unsigned)(round * (m - 1)));
-          uint16_t* sq = S.seq + rstart[isl];
-          for (int q = 1; q < m; ++q) {
-            s = lcg_next(s);
-            const int sw = rand_int_from(s, q + 1);
-            const uint16_t t = sq[q];
-            sq[q] = sq[sw];
-            sq[sw] = t;
-          }
-        }
-        prefix += (unsigned)__shfl_sync(kFull, incl, 31);
-      }
-      __syncwarp();
-      nchunk = sor_schedule(rows, nb, S, M, lane);
-    }
-    // sweep: chunks in level order; the next chunk's rows are loaded while
-    // the current one computes (two register buffers used in turn). Idle lanes
-    // run a no-op row so the warp never diverges.
-    float4 ra[8], rb[8];
-    int r_a, r_b;
-    {
-      const unsigned c0 = S.chunk[0];
-      r_a = kMaxR;
-      if (lane <= (int)(c0 >> 11)) { r_a = S.exec[(c0 & 0x7ffu) + lane]; load_row(rows, r_a, ra); }
-      else idle_row(ra);
-    }
-    for (int k = 0; k < nchunk; k += 2) {
-      r_b = kMaxR;
-      if (k + 1 < nchunk) {
-        const unsigned c1 = S.chunk[k + 1];
-        if (lane <= (int)(c1 >> 11)) { r_b = S.exec[(c1 & 0x7ffu) + lane]; load_row(rows, r_b, rb); }
-        else idle_row(rb);
-      }
-      sor_row(ra, r_a, S);
-      __syncwarp();
-      if (k + 1 >= nchunk) break;
-      r_a = kMaxR;
-      if (k + 2 < nchunk) {
-        const unsigned c2 = S.chunk[k + 2];
-        if (lane <= (int)(c2 >> 11)) { r_a = S.exec[(c2 & 0x7ffu) + lane]; load_row(rows, r_a, ra); }
-        else idle_row(ra);
-      }
-      sor_row(rb, r_b, S);
-      __syncwarp();
-    }
-  }
-  return lcg_jump(seed, total_draws);
 }
 
 }  // namespace og
