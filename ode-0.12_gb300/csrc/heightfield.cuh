@@ -331,7 +331,7 @@ OG_D int hf_zone(Z& z, const DevHeightfield& H, const float* heights, int minX, 
   // group by equal plane definition, in triangle order: triangle k, when no
   // earlier plane took it, leads a plane and takes every later untaken
   // triangle whose plane matches within dEpsilon in all four components
-  // (heightfield.cpp:1395-1440). Those candidates lie within dEpsilon of k's
+  // (heightfield.cpp:1387-1440). Those candidates lie within dEpsilon of k's
   // offset, so they are found in a window of the triangles sorted by offset
   // instead of by a scan of every later triangle; a leader's matches are then
   // put back in triangle order.
