@@ -151,11 +151,16 @@ def test_rows_and_lambda_tap(batch_cls, name):
         # h it is the velocity change). 20 FP32 PGS iterations vs FP64.
         nbi = int(t["island_bodies"].sum())
         gfc = fc[sc.body_off[w] + t["body_of"][:nbi]]
-        np.testing.assert_allclose(gfc, t["cforce"][:nbi], rtol=2e-3, atol=0.2)
-        # lambda of clearly loaded rows (above 1% of the largest and 0.01 N s)
+        np.testing.assert_allclose(gfc, t["cforce"][:nbi], rtol=2e-3, atol=3e-2)
+        # lambda of clearly loaded rows (above 1% of the largest and 0.01 N s):
+        # where friction rows couple to their normal rows through the pyramid
+        # bounds (piles, the joint-type scene), 20 FP32 iterations leave up to
+        # ~1.7e-2 relative against FP64 (measured on GB300); joint chains and
+        # single-contact scenes agree to ~1e-4
         lam_o = t["lam"][:M]
         big = np.abs(lam_o) > max(1e-2 * np.abs(lam_o).max(), 1e-2)
-        np.testing.assert_allclose(lam[row_off[w]:row_off[w] + M][big], lam_o[big], rtol=2e-2)
+        lam_rtol = 2e-2 if name in ("batched", "mechanisms") else 1e-3
+        np.testing.assert_allclose(lam[row_off[w]:row_off[w] + M][big], lam_o[big], rtol=lam_rtol)
         checked += 1
     assert checked > 0
 
@@ -163,9 +168,10 @@ def test_rows_and_lambda_tap(batch_cls, name):
 def test_tower_trajectory_200_steps(batch_cls):
     """Non-chaotic stacks (golden fixture from the reference), 200 steps.
     Per world, the GPU's max position error against the FP64 reference must be
-    <= max(1e-4 * scene scale, 2 x the drift of the reference's own FP32 build
-    on the same scene); the stated target 1e-4 relative holds where FP32 ODE
-    itself reaches it."""
+    <= max(1e-4 * scene scale, 1.5 x the drift of the reference's own FP32
+    build on the same scene); the stated target 1e-4 relative holds where FP32
+    ODE itself reaches it (on GB300 the GPU's error equals the FP32 build's in
+    every world, 3e-8 to 7e-4 of the scale)."""
     import os
     g = dict(np.load(os.path.join(os.path.dirname(__file__), "golden", "tower.npz")))
     sc = S.Scene.from_arrays(g)
@@ -180,7 +186,7 @@ def test_tower_trajectory_200_steps(batch_cls):
         scale = np.abs(ref).max()
         err_gpu = np.abs(st[b0:b1, :3] - ref).max()
         err_s = np.abs(g[f"w{w}_final_s"][:, :3] - ref).max()
-        assert err_gpu <= max(1e-4 * scale, 2 * err_s), (w, err_gpu, err_s, scale)
+        assert err_gpu <= max(1e-4 * scale, 1.5 * err_s), (w, err_gpu, err_s, scale)
         n_tight += err_gpu <= 1e-4 * scale
     assert n_tight >= sc.n_worlds - 1
 
