@@ -327,7 +327,8 @@ void dNormalize4(dVector4 a);                                            /* :427
 void dPlaneSpace(const dVector3 n, dVector3 p, dVector3 q);              /* :462 */
 
 /* collision: include/ode/collision.h (space argument must be 0: spaces are
- * not on this path, pairs come from the caller) */
+ * not on this path, pairs come from the caller; dGeomGetSpace returns the
+ * handle given at creation) */
 int dCollide(dGeomID o1, dGeomID o2, int flags, dContactGeom* contact, int skip); /* :795 */
 dGeomID dCreateSphere(dSpaceID space, dReal radius);                     /* :924 */
 dGeomID dCreateBox(dSpaceID space, dReal lx, dReal ly, dReal lz);        /* :1002 */
@@ -372,17 +373,64 @@ void dGeomHeightfieldDataBuildDouble(dHeightfieldDataID d, const double* pHeight
 void dGeomDestroy(dGeomID g);                                            /* :68  */
 void dGeomSetData(dGeomID g, void* data);                                /* :78  */
 void* dGeomGetData(dGeomID g);                                           /* :87  */
+/* Placement. A geom on a body follows the body; with an offset it sits at
+ * body + offset, and dGeomGetPosition/Rotation and dCollide read that pose.
+ * dGeomSetBody(g, 0) keeps the geom where it was; dBodyDestroy detaches the
+ * body's geoms the same way. */
 void dGeomSetBody(dGeomID g, dBodyID body);                              /* :108 */
 dBodyID dGeomGetBody(dGeomID g);                                         /* :117 */
 void dGeomSetPosition(dGeomID g, dReal x, dReal y, dReal z);             /* :134 */
 void dGeomSetRotation(dGeomID g, const dMatrix3 R);                      /* :149 */
+void dGeomSetQuaternion(dGeomID g, const dQuaternion Q);                 /* :165 */
 const dReal* dGeomGetPosition(dGeomID g);                                /* :184 */
+void dGeomCopyPosition(dGeomID g, dVector3 pos);                         /* :194 */
 const dReal* dGeomGetRotation(dGeomID g);                                /* :213 */
+void dGeomCopyRotation(dGeomID g, dMatrix3 R);                           /* :229 */
+void dGeomGetQuaternion(dGeomID g, dQuaternion result);                  /* :245 */
+void dGeomGetAABB(dGeomID g, dReal aabb[6]);                             /* :264 */
+int dGeomIsSpace(dGeomID g);                                             /* :273 */
+dSpaceID dGeomGetSpace(dGeomID g);                                       /* :283 */
 int dGeomGetClass(dGeomID g);                                            /* :310 */
+/* Category / collide bits and the enabled flag are kept for the getters; they
+ * steer a space's pair search, and dCollide reads none of them. */
+void dGeomSetCategoryBits(dGeomID g, unsigned long bits);                /* :325 */
+void dGeomSetCollideBits(dGeomID g, unsigned long bits);                 /* :340 */
+unsigned long dGeomGetCategoryBits(dGeomID g);                           /* :351 */
+unsigned long dGeomGetCollideBits(dGeomID g);                            /* :362 */
+void dGeomEnable(dGeomID g);                                             /* :377 */
+void dGeomDisable(dGeomID g);                                            /* :392 */
+int dGeomIsEnabled(dGeomID g);                                           /* :408 */
+void dGeomGetRelPointPos(dGeomID g, dReal px, dReal py, dReal pz, dVector3 result);    /* :472 */
+void dGeomGetPosRelPoint(dGeomID g, dReal px, dReal py, dReal pz, dVector3 result);    /* :490 */
+void dGeomVectorToWorld(dGeomID g, dReal px, dReal py, dReal pz, dVector3 result);     /* :505 */
+void dGeomVectorFromWorld(dGeomID g, dReal px, dReal py, dReal pz, dVector3 result);   /* :520 */
+/* Offsets from the body: a geom without a body ignores the setters. */
+void dGeomSetOffsetPosition(dGeomID g, dReal x, dReal y, dReal z);       /* :545 */
+void dGeomSetOffsetRotation(dGeomID g, const dMatrix3 R);                /* :561 */
+void dGeomSetOffsetQuaternion(dGeomID g, const dQuaternion Q);           /* :577 */
+void dGeomSetOffsetWorldPosition(dGeomID g, dReal x, dReal y, dReal z);  /* :596 */
+void dGeomSetOffsetWorldRotation(dGeomID g, const dMatrix3 R);           /* :613 */
+void dGeomSetOffsetWorldQuaternion(dGeomID g, const dQuaternion Q);      /* :630 */
+void dGeomClearOffset(dGeomID g);                                        /* :646 */
+int dGeomIsOffset(dGeomID g);                                            /* :664 */
+const dReal* dGeomGetOffsetPosition(dGeomID g);                          /* :680 */
+void dGeomCopyOffsetPosition(dGeomID g, dVector3 pos);                   /* :693 */
+const dReal* dGeomGetOffsetRotation(dGeomID g);                          /* :710 */
+void dGeomCopyOffsetRotation(dGeomID g, dMatrix3 R);                     /* :724 */
+void dGeomGetOffsetQuaternion(dGeomID g, dQuaternion result);            /* :737 */
+/* class parameters and point depths */
+void dGeomSphereSetRadius(dGeomID g, dReal radius);                      /* :936 */
 dReal dGeomSphereGetRadius(dGeomID g);                                   /* :947 */
+dReal dGeomSpherePointDepth(dGeomID g, dReal x, dReal y, dReal z);       /* :964 */
+void dGeomBoxSetLengths(dGeomID g, dReal lx, dReal ly, dReal lz);        /* :1016 */
 void dGeomBoxGetLengths(dGeomID g, dVector3 result);                     /* :1028 */
+dReal dGeomBoxPointDepth(dGeomID g, dReal x, dReal y, dReal z);          /* :1043 */
+void dGeomPlaneSetParams(dGeomID g, dReal a, dReal b, dReal c, dReal d); /* :1047 */
 void dGeomPlaneGetParams(dGeomID g, dVector4 result);                    /* :1048 */
+dReal dGeomPlanePointDepth(dGeomID g, dReal x, dReal y, dReal z);        /* :1049 */
+void dGeomCapsuleSetParams(dGeomID g, dReal radius, dReal length);       /* :1052 */
 void dGeomCapsuleGetParams(dGeomID g, dReal* radius, dReal* length);     /* :1053 */
+dReal dGeomCapsulePointDepth(dGeomID g, dReal x, dReal y, dReal z);      /* :1054 */
 
 #ifdef __cplusplus
 }

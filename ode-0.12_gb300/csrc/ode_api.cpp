@@ -64,7 +64,11 @@ struct dxHeightfieldData {
   std::vector<float> heights;      // copied at build time (x fastest, then z)
   float* d_heights = nullptr;      // device copy
   bool built = false;
-  double min_height = -INFINITY, max_height = INFINITY;   // dGeomHeightfieldDataSetBounds
+  // m_fMinHeight / m_fMaxHeight (heightfield.cpp:86-87, :150-237, :845-850):
+  // the field's vertical extent after scale, offset and thickness, computed
+  // from the samples at build time or set by dGeomHeightfieldDataSetBounds;
+  // only dGeomGetAABB reads them
+  float hmin = 0, hmax = 0;
 };
 
 struct dxGeom {
@@ -76,6 +80,12 @@ struct dxGeom {
   int placeable;             // heightfield geoms: created placeable
   int ray_flags;             // ray geoms: kRay* below
   void* data;                // dGeomSetData
+  dSpaceID space;            // the space passed at creation (dGeomGetSpace)
+  unsigned long category_bits, collide_bits;   // ~0 at creation (collision_kernel.cpp:343-368)
+  int enabled;               // GEOM_ENABLED
+  int has_offset;            // offset_posr != 0: placed relative to its body
+  dReal opos[4], oR[12];     // the offset (body frame)
+  dReal fpos[4], fR[12];     // an offset geom's own final pose, recomputed on every read
 };
 
 // dxGeom::gflags bits of a ray (ode/src/collision_kernel.h: RAY_FIRSTCONTACT,
@@ -99,6 +109,7 @@ struct dxWorld {
 namespace {
 
 unsigned long g_seed = 0;   // ODE's global dRand state (ode/src/misc.cpp:31)
+std::vector<dxGeom*> g_geoms;   // live geoms, for dBodyDestroy's detach
 thread_local std::string g_err;
 
 void body_sync_R(dxBody* b) {
@@ -264,6 +275,9 @@ dBodyID dBodyCreate(dWorldID w) {
 }
 void dBodyDestroy(dBodyID b) {
   if (!b) return;
+  // the body's geoms are detached first, keeping their pose (ode.cpp:301-310)
+  for (dxGeom* g : g_geoms)
+    if (g->body == b) dGeomSetBody(g, nullptr);
   dxWorld* w = b->world;
   for (dxJoint* j : w->joints) {
     for (int i = 0; i < 2; ++i)
@@ -927,26 +941,32 @@ void dRandSetSeed(unsigned long s) { g_seed = s & 0xffffffffUL; }
 int dRandInt(int n) { return og::rand_int_from((unsigned)dRand(), n); }
 
 // ---------------------------------------------------------------- geoms + dCollide
-static dGeomID new_geom(int type, const double* p) {
+// dxGeom::dxGeom (collision_kernel.cpp:343-368): identity pose, enabled, all
+// category and collide bits set
+static dGeomID new_geom(dSpaceID space, int type, const double* p) {
   auto* g = new dxGeom();
   std::memset(g, 0, sizeof(*g));
   g->type = type;
   for (int k = 0; k < 4; ++k) g->p[k] = p[k];
   g->R[0] = g->R[5] = g->R[10] = 1;
+  g->space = space;
+  g->category_bits = g->collide_bits = ~0UL;
+  g->enabled = 1;
+  g_geoms.push_back(g);
   return g;
 }
-dGeomID dCreateSphere(dSpaceID, dReal r) { const double p[4] = {r, 0, 0, 0}; return new_geom(dSphereClass, p); }
-dGeomID dCreateBox(dSpaceID, dReal lx, dReal ly, dReal lz) {
+dGeomID dCreateSphere(dSpaceID s, dReal r) { const double p[4] = {r, 0, 0, 0}; return new_geom(s, dSphereClass, p); }
+dGeomID dCreateBox(dSpaceID s, dReal lx, dReal ly, dReal lz) {
   const double p[4] = {lx, ly, lz, 0};
-  return new_geom(dBoxClass, p);
+  return new_geom(s, dBoxClass, p);
 }
-dGeomID dCreateCapsule(dSpaceID, dReal r, dReal len) {
+dGeomID dCreateCapsule(dSpaceID s, dReal r, dReal len) {
   const double p[4] = {r, len, 0, 0};
-  return new_geom(dCapsuleClass, p);
+  return new_geom(s, dCapsuleClass, p);
 }
-dGeomID dCreateCylinder(dSpaceID, dReal r, dReal len) {
+dGeomID dCreateCylinder(dSpaceID s, dReal r, dReal len) {
   const double p[4] = {r, len, 0, 0};
-  return new_geom(dCylinderClass, p);
+  return new_geom(s, dCylinderClass, p);
 }
 void dGeomCylinderSetParams(dGeomID g, dReal r, dReal len) {
   if (g && g->type == dCylinderClass) { g->p[0] = r; g->p[1] = len; }
@@ -954,22 +974,32 @@ void dGeomCylinderSetParams(dGeomID g, dReal r, dReal len) {
 void dGeomCylinderGetParams(dGeomID g, dReal* r, dReal* l) {
   if (g && g->type == dCylinderClass) { *r = (dReal)g->p[0]; *l = (dReal)g->p[1]; }
 }
-dGeomID dCreatePlane(dSpaceID, dReal a, dReal b, dReal c, dReal d) {
-  // make_sure_plane_normal_has_unit_length (ode/src/plane.cpp:40-56)
-  double p[4] = {a, b, c, d};
-  double l = p[0] * p[0] + p[1] * p[1] + p[2] * p[2];
-  if (l > 0) { l = 1.0 / std::sqrt(l); for (int k = 0; k < 4; ++k) p[k] *= l; }
-  else { p[0] = 1; p[1] = p[2] = p[3] = 0; }
-  return new_geom(dPlaneClass, p);
+// make_sure_plane_normal_has_unit_length (ode/src/plane.cpp:49-65), in dReal
+// arithmetic as the dSINGLE build does it
+static void plane_params(double* p, dReal a, dReal b, dReal c, dReal d) {
+  dReal q[4] = {a, b, c, d};
+  dReal l = q[0] * q[0] + q[1] * q[1] + q[2] * q[2];
+  if (l > 0) { l = (dReal)1 / std::sqrt(l); for (int k = 0; k < 4; ++k) q[k] *= l; }
+  else { q[0] = 1; q[1] = q[2] = q[3] = 0; }
+  for (int k = 0; k < 4; ++k) p[k] = q[k];
 }
-void dGeomDestroy(dGeomID g) { delete g; }
+dGeomID dCreatePlane(dSpaceID s, dReal a, dReal b, dReal c, dReal d) {
+  double p[4];
+  plane_params(p, a, b, c, d);
+  return new_geom(s, dPlaneClass, p);
+}
+void dGeomDestroy(dGeomID g) {
+  if (!g) return;
+  g_geoms.erase(std::remove(g_geoms.begin(), g_geoms.end(), g), g_geoms.end());
+  delete g;
+}
 
 // Rays (ode/src/ray.cpp:49-194): the length is the class parameter; the start
 // is the geom's position and the direction column 2 of its rotation, so a ray
 // attached to a body follows that body.
-dGeomID dCreateRay(dSpaceID, dReal length) {
+dGeomID dCreateRay(dSpaceID s, dReal length) {
   const double p[4] = {length, 0, 0, 0};
-  return new_geom(dRayClass, p);
+  return new_geom(s, dRayClass, p);
 }
 void dGeomRaySetLength(dGeomID g, dReal length) {
   if (g && g->type == dRayClass) g->p[0] = length;
@@ -1024,12 +1054,27 @@ static bool hf_shape(dHeightfieldDataID d, dReal width, dReal depth, int widthSa
   d->heights.assign((size_t)widthSamples * depthSamples, 0.f);
   return true;
 }
+// dxHeightfieldData::ComputeHeightBounds (heightfield.cpp:150-237) over the
+// samples as dReal, then scale, offset and thickness
+static void hf_bounds(dHeightfieldDataID d) {
+  float lo = INFINITY, hi = -INFINITY;
+  for (const float h : d->heights) {
+    if (h < lo) lo = h;
+    if (h > hi) hi = h;
+  }
+  const float sc = (float)d->scale, of = (float)d->offset, th = (float)d->thickness;
+  lo *= sc; hi *= sc;
+  lo += of; hi += of;
+  lo -= th;
+  d->hmin = lo; d->hmax = hi;
+}
 void dGeomHeightfieldDataBuildSingle(dHeightfieldDataID d, const float* pHeightData, int, dReal width,
                                      dReal depth, int widthSamples, int depthSamples, dReal scale, dReal offset,
                                      dReal thickness, int bWrap) {
   if (!pHeightData || !hf_shape(d, width, depth, widthSamples, depthSamples, scale, offset, thickness, bWrap))
     return;
   for (size_t k = 0; k < d->heights.size(); ++k) d->heights[k] = pHeightData[k];
+  hf_bounds(d);
   d->built = og::upload_heights(d->heights, &d->d_heights) == 0;
 }
 void dGeomHeightfieldDataBuildDouble(dHeightfieldDataID d, const double* pHeightData, int, dReal width,
@@ -1038,6 +1083,7 @@ void dGeomHeightfieldDataBuildDouble(dHeightfieldDataID d, const double* pHeight
   if (!pHeightData || !hf_shape(d, width, depth, widthSamples, depthSamples, scale, offset, thickness, bWrap))
     return;
   for (size_t k = 0; k < d->heights.size(); ++k) d->heights[k] = (float)pHeightData[k];
+  hf_bounds(d);
   d->built = og::upload_heights(d->heights, &d->d_heights) == 0;
 }
 void dGeomHeightfieldDataBuildByte(dHeightfieldDataID d, const unsigned char* pHeightData, int, dReal width,
@@ -1046,6 +1092,7 @@ void dGeomHeightfieldDataBuildByte(dHeightfieldDataID d, const unsigned char* pH
   if (!pHeightData || !hf_shape(d, width, depth, widthSamples, depthSamples, scale, offset, thickness, bWrap))
     return;
   for (size_t k = 0; k < d->heights.size(); ++k) d->heights[k] = (float)pHeightData[k];
+  hf_bounds(d);
   d->built = og::upload_heights(d->heights, &d->d_heights) == 0;
 }
 void dGeomHeightfieldDataBuildShort(dHeightfieldDataID d, const short* pHeightData, int, dReal width, dReal depth,
@@ -1054,40 +1101,426 @@ void dGeomHeightfieldDataBuildShort(dHeightfieldDataID d, const short* pHeightDa
   if (!pHeightData || !hf_shape(d, width, depth, widthSamples, depthSamples, scale, offset, thickness, bWrap))
     return;
   for (size_t k = 0; k < d->heights.size(); ++k) d->heights[k] = (float)pHeightData[k];
+  hf_bounds(d);
   d->built = og::upload_heights(d->heights, &d->d_heights) == 0;
 }
-// The bounds tighten the field's bounding box, which only a space's early
-// rejection reads (heightfield.cpp:147-156); dCollide does not, so they are kept
-// for completeness only.
+// The bounds set the field's vertical extent in its bounding box
+// (heightfield.cpp:845-850), which dGeomGetAABB reports and only a space's
+// early rejection would read; dCollide does not.
 void dGeomHeightfieldDataSetBounds(dHeightfieldDataID d, dReal minHeight, dReal maxHeight) {
   if (!d) return;
-  d->min_height = minHeight;
-  d->max_height = maxHeight;
+  const float sc = (float)d->scale, of = (float)d->offset, th = (float)d->thickness;
+  d->hmin = minHeight * sc + of - th;
+  d->hmax = maxHeight * sc + of;
 }
-dGeomID dCreateHeightfield(dSpaceID, dHeightfieldDataID data, int bPlaceable) {
+dGeomID dCreateHeightfield(dSpaceID s, dHeightfieldDataID data, int bPlaceable) {
   const double p[4] = {0, 0, 0, 0};
-  dGeomID g = new_geom(dHeightfieldClass, p);
+  dGeomID g = new_geom(s, dHeightfieldClass, p);
   g->hf = data;
   g->placeable = bPlaceable;
   return g;
 }
-void dGeomSetBody(dGeomID g, dBodyID b) { g->body = b; }
+// ---------------------------------------------------------------- geom placement
+// A geom on a body reads the body's pose; with an offset it has its own final
+// pose, body.R * offset.pos + body.pos and body.R * offset.R
+// (dxGeom::computePosr, collision_kernel.cpp:454-465), recomputed on every read
+// so that it follows the body through the step. Planes and non-placeable
+// heightfields have no pose (GEOM_PLACEABLE clear).
+static bool geom_placeable(const dxGeom* g) {
+  return g->type != dPlaneClass && !(g->type == dHeightfieldClass && !g->placeable);
+}
+static void mul0_331(dReal* a, const dReal* R, const dReal* v) {   // a = R v
+  for (int i = 0; i < 3; ++i) a[i] = R[i * 4 + 0] * v[0] + R[i * 4 + 1] * v[1] + R[i * 4 + 2] * v[2];
+}
+static void mul1_331(dReal* a, const dReal* R, const dReal* v) {   // a = R^T v
+  for (int i = 0; i < 3; ++i) a[i] = R[0 * 4 + i] * v[0] + R[1 * 4 + i] * v[1] + R[2 * 4 + i] * v[2];
+}
+static void mul0_333(dReal* A, const dReal* B, const dReal* C) {   // A = B C, pads kept
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j)
+      A[i * 4 + j] = B[i * 4 + 0] * C[0 * 4 + j] + B[i * 4 + 1] * C[1 * 4 + j] + B[i * 4 + 2] * C[2 * 4 + j];
+}
+static void transpose33(dReal* T, const dReal* R) {   // matrixInvert (collision_kernel.cpp:417-426)
+  for (int k = 0; k < 12; ++k) T[k] = R[k];
+  std::swap(T[4], T[1]);
+  std::swap(T[2], T[8]);
+  std::swap(T[9], T[6]);
+}
+static void geom_recompute(dxGeom* g) {
+  if (!g->has_offset || !g->body) return;
+  mul0_331(g->fpos, g->body->R, g->opos);
+  for (int k = 0; k < 3; ++k) g->fpos[k] += g->body->pos[k];
+  mul0_333(g->fR, g->body->R, g->oR);
+}
+static dReal* geom_pos(dxGeom* g) {
+  geom_recompute(g);
+  return g->has_offset ? g->fpos : g->body ? g->body->pos : g->pos;
+}
+static dReal* geom_R(dxGeom* g) {
+  geom_recompute(g);
+  return g->has_offset ? g->fR : g->body ? g->body->R : g->R;
+}
+// getBodyPosr (collision_kernel.cpp:428-439): the body pose that puts the
+// offset geom at (fpos, fR)
+static void body_for_final(const dxGeom* g, const dReal* fpos, const dReal* fR, dReal* bpos, dReal* bR) {
+  dReal inv[12], wo[3];
+  transpose33(inv, g->oR);
+  for (int k = 0; k < 12; ++k) bR[k] = 0;
+  mul0_333(bR, fR, inv);
+  mul0_331(wo, bR, g->opos);
+  for (int k = 0; k < 3; ++k) bpos[k] = fpos[k] - wo[k];
+}
+// getWorldOffsetPosr (collision_kernel.cpp:441-452): the offset that puts the
+// geom at (fpos, fR) on its body as it stands
+static void offset_for_final(dxGeom* g, const dReal* fpos, const dReal* fR) {
+  dReal inv[12], wo[3];
+  transpose33(inv, g->body->R);
+  mul0_333(g->oR, inv, fR);
+  for (int k = 0; k < 3; ++k) wo[k] = fpos[k] - g->body->pos[k];
+  mul0_331(g->opos, inv, wo);
+}
+// dGeomCreateOffset (collision_kernel.cpp:1017-1034): a zero offset
+static bool geom_make_offset(dxGeom* g) {
+  if (!g || !g->body || !geom_placeable(g)) return false;
+  if (g->has_offset) return true;
+  g->has_offset = 1;
+  for (int k = 0; k < 4; ++k) g->opos[k] = 0;
+  for (int k = 0; k < 12; ++k) g->oR[k] = 0;
+  g->oR[0] = g->oR[5] = g->oR[10] = 1;
+  return true;
+}
+
+// dGeomSetBody (collision_kernel.cpp:507-546): attaching to another body drops
+// any offset; detaching keeps the geom where it was (its final pose, or the
+// body's) as its own
+void dGeomSetBody(dGeomID g, dBodyID b) {
+  if (!g) return;
+  if (b) {
+    if (g->body != b) {
+      g->has_offset = 0;
+      g->body = b;
+    }
+  } else if (g->body) {
+    const dReal* pos = geom_pos(g);
+    const dReal* R = geom_R(g);
+    for (int k = 0; k < 3; ++k) g->pos[k] = pos[k];
+    for (int k = 0; k < 12; ++k) g->R[k] = R[k];
+    g->has_offset = 0;
+    g->body = nullptr;
+  }
+}
 dBodyID dGeomGetBody(dGeomID g) { return g->body; }
+// dGeomSetPosition / SetRotation / SetQuaternion (collision_kernel.cpp:557-640):
+// an offset geom moves its body so that body + offset lands on the new pose
 void dGeomSetPosition(dGeomID g, dReal x, dReal y, dReal z) {
-  if (g->body) dBodySetPosition(g->body, x, y, z);
-  else { g->pos[0] = x; g->pos[1] = y; g->pos[2] = z; }
+  if (g->has_offset) {
+    dReal wo[3];
+    mul0_331(wo, g->body->R, g->opos);
+    dBodySetPosition(g->body, x - wo[0], y - wo[1], z - wo[2]);
+  } else if (g->body) {
+    dBodySetPosition(g->body, x, y, z);
+  } else {
+    g->pos[0] = x; g->pos[1] = y; g->pos[2] = z;
+  }
 }
 void dGeomSetRotation(dGeomID g, const dMatrix3 R) {
-  if (g->body) dBodySetRotation(g->body, R);
-  else for (int k = 0; k < 12; ++k) g->R[k] = R[k];
+  if (g->has_offset) {
+    dReal bpos[3], bR[12];
+    body_for_final(g, geom_pos(g), R, bpos, bR);
+    dBodySetRotation(g->body, bR);
+    dBodySetPosition(g->body, bpos[0], bpos[1], bpos[2]);
+  } else if (g->body) {
+    dBodySetRotation(g->body, R);
+  } else {
+    for (int k = 0; k < 12; ++k) g->R[k] = R[k];
+  }
 }
-const dReal* dGeomGetPosition(dGeomID g) { return g->body ? g->body->pos : g->pos; }
-const dReal* dGeomGetRotation(dGeomID g) { return g->body ? g->body->R : g->R; }
+void dGeomSetQuaternion(dGeomID g, const dQuaternion q) {
+  if (g->has_offset) {
+    dReal fR[12], bpos[3], bR[12];
+    dRfromQ(fR, q);
+    body_for_final(g, geom_pos(g), fR, bpos, bR);
+    dBodySetRotation(g->body, bR);
+    dBodySetPosition(g->body, bpos[0], bpos[1], bpos[2]);
+  }
+  // ODE 0.12 tests the body here with a plain `if`, so an offset geom's body
+  // then takes the quaternion itself as well (collision_kernel.cpp:630-633)
+  if (g->body) {
+    dBodySetQuaternion(g->body, q);
+  } else {
+    dRfromQ(g->R, q);
+  }
+}
+const dReal* dGeomGetPosition(dGeomID g) { return geom_pos(g); }
+const dReal* dGeomGetRotation(dGeomID g) { return geom_R(g); }
+void dGeomCopyPosition(dGeomID g, dVector3 pos) {   // :648-657
+  const dReal* p = geom_pos(g);
+  for (int k = 0; k < 3; ++k) pos[k] = p[k];
+}
+void dGeomCopyRotation(dGeomID g, dMatrix3 R) {   // :669-685, the pads left alone
+  const dReal* s = geom_R(g);
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 3; ++c) R[r * 4 + c] = s[r * 4 + c];
+}
+void dGeomGetQuaternion(dGeomID g, dQuaternion q) {   // :687-703
+  if (g->body && !g->has_offset) {
+    for (int k = 0; k < 4; ++k) q[k] = g->body->q[k];
+  } else {
+    dQfromR(q, geom_R(g));
+  }
+}
+
+// dGeomGetAABB (collision_kernel.cpp:705-711) with each class's computeAABB:
+// sphere.cpp:59-67, box.cpp:60-77, capsule.cpp:60-74, cylinder.cpp:59-76,
+// plane.cpp:80-107, ray.cpp:56-89, heightfield.cpp:475-600
+void dGeomGetAABB(dGeomID g, dReal aabb[6]) {
+  const float inf = INFINITY;
+  if (g->type == dPlaneClass) {
+    const dReal p[4] = {(dReal)g->p[0], (dReal)g->p[1], (dReal)g->p[2], (dReal)g->p[3]};
+    for (int k = 0; k < 6; ++k) aabb[k] = (k & 1) ? inf : -inf;
+    if (p[1] == 0 && p[2] == 0) {
+      aabb[0] = p[0] > 0 ? -inf : -p[3];
+      aabb[1] = p[0] > 0 ? p[3] : inf;
+    } else if (p[0] == 0 && p[2] == 0) {
+      aabb[2] = p[1] > 0 ? -inf : -p[3];
+      aabb[3] = p[1] > 0 ? p[3] : inf;
+    } else if (p[0] == 0 && p[1] == 0) {
+      aabb[4] = p[2] > 0 ? -inf : -p[3];
+      aabb[5] = p[2] > 0 ? p[3] : inf;
+    }
+    return;
+  }
+  if (g->type == dHeightfieldClass) {
+    const dxHeightfieldData* d = g->hf;
+    if (!d) { for (int k = 0; k < 6; ++k) aabb[k] = 0; return; }
+    const float hw = (dReal)d->width / (dReal)2, hd = (dReal)d->depth / (dReal)2;
+    if (d->wrap) {
+      for (int k = 0; k < 6; ++k) aabb[k] = (k & 1) ? inf : -inf;
+      if (!g->placeable) { aabb[2] = d->hmin; aabb[3] = d->hmax; }
+      return;
+    }
+    if (!g->placeable) {
+      aabb[0] = -hw; aabb[1] = hw;
+      aabb[2] = d->hmin; aabb[3] = d->hmax;
+      aabb[4] = -hd; aabb[5] = hd;
+      return;
+    }
+    const dReal* pos = geom_pos(g);
+    const dReal* R = geom_R(g);
+    dReal dx[6], dy[6], dz[6];
+    for (int i = 0; i < 3; ++i) {
+      const dReal ry = R[i * 4 + 1];
+      // an infinite bound times a zero entry counts as 0, not NaN
+      dy[i] = d->hmin != -inf ? ry * d->hmin : (ry ? ry * -inf : 0.f);
+      dy[i + 3] = d->hmax != inf ? ry * d->hmax : (ry ? ry * inf : 0.f);
+      dx[i] = R[i * 4 + 0] * -hw;
+      dx[i + 3] = R[i * 4 + 0] * hw;
+      dz[i] = R[i * 4 + 2] * -hd;
+      dz[i + 3] = R[i * 4 + 2] * hd;
+    }
+    for (int i = 0; i < 3; ++i) {
+      const dReal lo = std::min(std::min(std::min(dx[i], dx[i + 3]), std::min(dy[i], dy[i + 3])),
+                                std::min(dz[i], dz[i + 3]));
+      const dReal hi = std::max(std::max(std::max(dx[i], dx[i + 3]), std::max(dy[i], dy[i + 3])),
+                                std::max(dz[i], dz[i + 3]));
+      aabb[2 * i] = pos[i] + lo;
+      aabb[2 * i + 1] = pos[i] + hi;
+    }
+    return;
+  }
+  const dReal* pos = geom_pos(g);
+  const dReal* R = geom_R(g);
+  const dReal a = (dReal)g->p[0], b = (dReal)g->p[1], c = (dReal)g->p[2];
+  dReal ext[3];
+  switch (g->type) {
+    case dSphereClass:
+      for (int i = 0; i < 3; ++i) ext[i] = a;
+      break;
+    case dBoxClass:
+      for (int i = 0; i < 3; ++i)
+        ext[i] = (dReal)0.5 * (std::fabs(R[i * 4 + 0] * a) + std::fabs(R[i * 4 + 1] * b) + std::fabs(R[i * 4 + 2] * c));
+      break;
+    case dCapsuleClass:
+      for (int i = 0; i < 3; ++i) ext[i] = std::fabs(R[i * 4 + 2] * b) * (dReal)0.5 + a;
+      break;
+    case dCylinderClass:
+      for (int i = 0; i < 3; ++i)
+        ext[i] = std::fabs(R[i * 4 + 0] * a) + std::fabs(R[i * 4 + 1] * a) + (dReal)0.5 * std::fabs(R[i * 4 + 2] * b);
+      break;
+    case dRayClass:
+      for (int i = 0; i < 3; ++i) {
+        const dReal e = pos[i] + R[i * 4 + 2] * a;
+        aabb[2 * i] = pos[i] < e ? pos[i] : e;
+        aabb[2 * i + 1] = pos[i] < e ? e : pos[i];
+      }
+      return;
+    default:
+      for (int k = 0; k < 6; ++k) aabb[k] = 0;
+      return;
+  }
+  for (int i = 0; i < 3; ++i) {
+    aabb[2 * i] = pos[i] - ext[i];
+    aabb[2 * i + 1] = pos[i] + ext[i];
+  }
+}
+// No spaces on this path: a geom is never a space, and reports the space
+// handle it was created with (collision_kernel.cpp:714-726)
+int dGeomIsSpace(dGeomID) { return 0; }
+dSpaceID dGeomGetSpace(dGeomID g) { return g->space; }
 int dGeomGetClass(dGeomID g) { return g->type; }
+// Category / collide bits and the enabled flag (collision_kernel.cpp:735-782)
+// steer a space's pair search only; dCollide reads none of them.
+void dGeomSetCategoryBits(dGeomID g, unsigned long bits) { g->category_bits = bits; }
+void dGeomSetCollideBits(dGeomID g, unsigned long bits) { g->collide_bits = bits; }
+unsigned long dGeomGetCategoryBits(dGeomID g) { return g->category_bits; }
+unsigned long dGeomGetCollideBits(dGeomID g) { return g->collide_bits; }
+void dGeomEnable(dGeomID g) { g->enabled = 1; }
+void dGeomDisable(dGeomID g) { g->enabled = 0; }
+int dGeomIsEnabled(dGeomID g) { return g->enabled != 0; }
+// Geom-frame points and vectors (collision_kernel.cpp:784-874); a geom
+// without a pose passes them through
+void dGeomGetRelPointPos(dGeomID g, dReal px, dReal py, dReal pz, dVector3 result) {
+  if (!geom_placeable(g)) { result[0] = px; result[1] = py; result[2] = pz; return; }
+  const dReal* pos = geom_pos(g);
+  const dReal v[3] = {px, py, pz};
+  dReal a[3];
+  mul0_331(a, geom_R(g), v);
+  for (int k = 0; k < 3; ++k) result[k] = a[k] + pos[k];
+}
+void dGeomGetPosRelPoint(dGeomID g, dReal px, dReal py, dReal pz, dVector3 result) {
+  if (!geom_placeable(g)) { result[0] = px; result[1] = py; result[2] = pz; return; }
+  const dReal* pos = geom_pos(g);
+  const dReal v[3] = {px - pos[0], py - pos[1], pz - pos[2]};
+  mul1_331(result, geom_R(g), v);
+}
+void dGeomVectorToWorld(dGeomID g, dReal px, dReal py, dReal pz, dVector3 result) {
+  if (!geom_placeable(g)) { result[0] = px; result[1] = py; result[2] = pz; return; }
+  const dReal v[3] = {px, py, pz};
+  mul0_331(result, geom_R(g), v);
+}
+void dGeomVectorFromWorld(dGeomID g, dReal px, dReal py, dReal pz, dVector3 result) {
+  if (!geom_placeable(g)) { result[0] = px; result[1] = py; result[2] = pz; return; }
+  const dReal v[3] = {px, py, pz};
+  mul1_331(result, geom_R(g), v);
+}
+
+// Offsets from the body (collision_kernel.cpp:1036-1250). Setting one on a
+// geom without a body does nothing.
+void dGeomSetOffsetPosition(dGeomID g, dReal x, dReal y, dReal z) {
+  if (!geom_make_offset(g)) return;
+  g->opos[0] = x; g->opos[1] = y; g->opos[2] = z;
+}
+void dGeomSetOffsetRotation(dGeomID g, const dMatrix3 R) {
+  if (!geom_make_offset(g)) return;
+  for (int k = 0; k < 12; ++k) g->oR[k] = R[k];
+}
+void dGeomSetOffsetQuaternion(dGeomID g, const dQuaternion q) {
+  if (!geom_make_offset(g)) return;
+  dRfromQ(g->oR, q);
+}
+void dGeomSetOffsetWorldPosition(dGeomID g, dReal x, dReal y, dReal z) {
+  if (!geom_make_offset(g)) return;
+  dBodyGetPosRelPoint(g->body, x, y, z, g->opos);
+}
+void dGeomSetOffsetWorldRotation(dGeomID g, const dMatrix3 R) {
+  if (!geom_make_offset(g)) return;
+  dReal fpos[3];
+  const dReal* p = geom_pos(g);
+  for (int k = 0; k < 3; ++k) fpos[k] = p[k];
+  offset_for_final(g, fpos, R);
+}
+void dGeomSetOffsetWorldQuaternion(dGeomID g, const dQuaternion q) {
+  if (!geom_make_offset(g)) return;
+  dReal fpos[3], fR[12];
+  const dReal* p = geom_pos(g);
+  for (int k = 0; k < 3; ++k) fpos[k] = p[k];
+  dRfromQ(fR, q);
+  offset_for_final(g, fpos, fR);
+}
+void dGeomClearOffset(dGeomID g) { g->has_offset = 0; }
+int dGeomIsOffset(dGeomID g) { return g->has_offset ? 1 : 0; }
+static const dReal kZeroOffsetPos[4] = {0, 0, 0, 0};
+static const dReal kZeroOffsetR[12] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0};
+const dReal* dGeomGetOffsetPosition(dGeomID g) { return g->has_offset ? g->opos : kZeroOffsetPos; }
+void dGeomCopyOffsetPosition(dGeomID g, dVector3 pos) {
+  const dReal* p = dGeomGetOffsetPosition(g);
+  for (int k = 0; k < 3; ++k) pos[k] = p[k];
+}
+const dReal* dGeomGetOffsetRotation(dGeomID g) { return g->has_offset ? g->oR : kZeroOffsetR; }
+void dGeomCopyOffsetRotation(dGeomID g, dMatrix3 R) {
+  const dReal* s = dGeomGetOffsetRotation(g);
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 3; ++c) R[r * 4 + c] = s[r * 4 + c];
+}
+void dGeomGetOffsetQuaternion(dGeomID g, dQuaternion q) {
+  if (g->has_offset) {
+    dQfromR(q, g->oR);
+  } else {
+    q[0] = 1; q[1] = q[2] = q[3] = 0;
+  }
+}
+
+// ---------------------------------------------------------------- class parameters
+// Setters of sphere.cpp:76-84, box.cpp:86-96, plane.cpp:117-127,
+// capsule.cpp:83-92; the point depths of sphere.cpp:95-105, box.cpp:109-173,
+// plane.cpp:141-146, capsule.cpp:104-126, in dReal arithmetic.
 dReal dGeomSphereGetRadius(dGeomID g) { return (dReal)g->p[0]; }
+void dGeomSphereSetRadius(dGeomID g, dReal radius) {
+  if (g && g->type == dSphereClass) g->p[0] = radius;
+}
+dReal dGeomSpherePointDepth(dGeomID g, dReal x, dReal y, dReal z) {
+  const dReal* pos = geom_pos(g);
+  return (dReal)g->p[0] - std::sqrt((x - pos[0]) * (x - pos[0]) + (y - pos[1]) * (y - pos[1]) +
+                                    (z - pos[2]) * (z - pos[2]));
+}
 void dGeomBoxGetLengths(dGeomID g, dVector3 r) { for (int k = 0; k < 3; ++k) r[k] = (dReal)g->p[k]; }
+void dGeomBoxSetLengths(dGeomID g, dReal lx, dReal ly, dReal lz) {
+  if (g && g->type == dBoxClass) { g->p[0] = lx; g->p[1] = ly; g->p[2] = lz; }
+}
+dReal dGeomBoxPointDepth(dGeomID g, dReal x, dReal y, dReal z) {
+  const dReal* pos = geom_pos(g);
+  const dReal p[3] = {x - pos[0], y - pos[1], z - pos[2]};
+  dReal q[3], dist[6];
+  mul1_331(q, geom_R(g), p);
+  bool inside = true;
+  for (int i = 0; i < 3; ++i) {
+    const dReal side = (dReal)g->p[i] * (dReal)0.5;
+    dist[i] = side - q[i];
+    dist[i + 3] = side + q[i];
+    if (dist[i] < 0 || dist[i + 3] < 0) inside = false;
+  }
+  if (inside) {   // the nearest face
+    dReal m = (dReal)4294967295.0;
+    for (int i = 0; i < 6; ++i) if (dist[i] < m) m = dist[i];
+    return m;
+  }
+  dReal m = 0;   // outside: minus the largest face distance
+  for (int i = 0; i < 6; ++i) if (dist[i] > m) m = dist[i];
+  return -m;
+}
 void dGeomPlaneGetParams(dGeomID g, dVector4 r) { for (int k = 0; k < 4; ++k) r[k] = (dReal)g->p[k]; }
+void dGeomPlaneSetParams(dGeomID g, dReal a, dReal b, dReal c, dReal d) {
+  if (g && g->type == dPlaneClass) plane_params(g->p, a, b, c, d);
+}
+dReal dGeomPlanePointDepth(dGeomID g, dReal x, dReal y, dReal z) {
+  const dReal p[4] = {(dReal)g->p[0], (dReal)g->p[1], (dReal)g->p[2], (dReal)g->p[3]};
+  return p[3] - p[0] * x - p[1] * y - p[2] * z;
+}
 void dGeomCapsuleGetParams(dGeomID g, dReal* r, dReal* l) { *r = (dReal)g->p[0]; *l = (dReal)g->p[1]; }
+void dGeomCapsuleSetParams(dGeomID g, dReal radius, dReal length) {
+  if (g && g->type == dCapsuleClass) { g->p[0] = radius; g->p[1] = length; }
+}
+dReal dGeomCapsulePointDepth(dGeomID g, dReal x, dReal y, dReal z) {
+  const dReal* R = geom_R(g);
+  const dReal* pos = geom_pos(g);
+  const dReal a[3] = {x - pos[0], y - pos[1], z - pos[2]};
+  dReal beta = a[0] * R[2] + a[1] * R[6] + a[2] * R[10];
+  const dReal lz2 = (dReal)g->p[1] * (dReal)0.5;
+  if (beta < -lz2) beta = -lz2;
+  else if (beta > lz2) beta = lz2;
+  const dReal c[3] = {pos[0] + beta * R[2], pos[1] + beta * R[6], pos[2] + beta * R[10]};
+  return (dReal)g->p[0] - std::sqrt((x - c[0]) * (x - c[0]) + (y - c[1]) * (y - c[1]) + (z - c[2]) * (z - c[2]));
+}
 
 int dCollide(dGeomID o1, dGeomID o2, int flags, dContactGeom* contact, int skip) {
   // early-outs of ode/src/collision_kernel.cpp:292-311, then the collider on the GPU

@@ -1,0 +1,311 @@
+"""ODE's geom placement API on the host, against the reference's dSINGLE build:
+offsets from the body (ode/src/collision_kernel.cpp:1017-1250), the geom
+pose setters and getters with and without offsets (:507-703), bounding boxes
+of every class on this path (sphere.cpp:59-67, box.cpp:60-77,
+capsule.cpp:60-74, cylinder.cpp:59-76, plane.cpp:80-107, ray.cpp:56-89,
+heightfield.cpp:475-600), category / collide bits and the enabled flag
+(:735-782), geom-frame points (:784-874), the class setters and point depths,
+and dBodyDestroy's detach (ode.cpp:301-310). None of these calls reaches the
+GPU, so the same call sequence runs on both libraries here."""
+import ctypes as C
+import os
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+F, P, I, UL = C.c_float, C.c_void_p, C.c_int, C.c_ulong
+V4, M12 = F * 4, F * 12
+dSphereClass, dBoxClass, dCapsuleClass, dCylinderClass, dPlaneClass, dRayClass = 0, 1, 2, 3, 4, 5
+
+
+def _libs():
+    import oracle_lib as O
+    if not O.ref_available("s"):
+        pytest.skip("reference not built in this checkout")
+    ours = C.CDLL(os.path.join(ROOT, "ode-0.12_gb300", "libodegpu.so"))
+    ref = C.CDLL(os.path.join(ROOT, "oracle", "_ref", "libode_ref_s.so"))
+    for lib in (ours, ref):
+        for n in ("dWorldCreate", "dBodyCreate", "dCreateSphere", "dCreateBox", "dCreateCapsule", "dCreateCylinder",
+                  "dCreatePlane", "dCreateRay", "dGeomGetBody", "dGeomGetSpace", "dCreateHeightfield",
+                  "dGeomHeightfieldDataCreate"):
+            getattr(lib, n).restype = P
+        lib.dBodyCreate.argtypes = [P]
+        lib.dBodySetPosition.argtypes = [P, F, F, F]
+        lib.dBodySetRotation.argtypes = [P, P]
+        lib.dBodyDestroy.argtypes = [P]
+        lib.dBodyGetPosition.restype = lib.dBodyGetRotation.restype = C.POINTER(F)
+        lib.dBodyGetPosition.argtypes = lib.dBodyGetRotation.argtypes = [P]
+        lib.dRFromAxisAndAngle.argtypes = [P, F, F, F, F]
+        lib.dQFromAxisAndAngle.argtypes = [P, F, F, F, F]
+        lib.dCreateSphere.argtypes = [P, F]
+        lib.dCreateBox.argtypes = [P, F, F, F]
+        lib.dCreateCapsule.argtypes = lib.dCreateCylinder.argtypes = [P, F, F]
+        lib.dCreatePlane.argtypes = [P, F, F, F, F]
+        lib.dCreateRay.argtypes = [P, F]
+        for n in ("dGeomSetBody",):
+            getattr(lib, n).argtypes = [P, P]
+        for n in ("dGeomSetPosition", "dGeomSetOffsetPosition", "dGeomSetOffsetWorldPosition"):
+            getattr(lib, n).argtypes = [P, F, F, F]
+        for n in ("dGeomSetRotation", "dGeomSetQuaternion", "dGeomSetOffsetRotation", "dGeomSetOffsetQuaternion",
+                  "dGeomSetOffsetWorldRotation", "dGeomSetOffsetWorldQuaternion", "dGeomCopyPosition",
+                  "dGeomCopyRotation", "dGeomGetQuaternion", "dGeomGetAABB", "dGeomCopyOffsetPosition",
+                  "dGeomCopyOffsetRotation", "dGeomGetOffsetQuaternion"):
+            getattr(lib, n).argtypes = [P, P]
+        for n in ("dGeomGetPosition", "dGeomGetRotation", "dGeomGetOffsetPosition", "dGeomGetOffsetRotation"):
+            getattr(lib, n).restype = C.POINTER(F)
+            getattr(lib, n).argtypes = [P]
+        for n in ("dGeomClearOffset", "dGeomIsOffset", "dGeomIsSpace", "dGeomGetSpace", "dGeomEnable",
+                  "dGeomDisable", "dGeomIsEnabled", "dGeomDestroy", "dGeomGetCategoryBits", "dGeomGetCollideBits",
+                  "dGeomGetBody", "dGeomGetClass"):
+            getattr(lib, n).argtypes = [P]
+        lib.dGeomGetCategoryBits.restype = lib.dGeomGetCollideBits.restype = UL
+        lib.dGeomSetCategoryBits.argtypes = lib.dGeomSetCollideBits.argtypes = [P, UL]
+        for n in ("dGeomGetRelPointPos", "dGeomGetPosRelPoint", "dGeomVectorToWorld", "dGeomVectorFromWorld"):
+            getattr(lib, n).argtypes = [P, F, F, F, P]
+        for n in ("dGeomSpherePointDepth", "dGeomBoxPointDepth", "dGeomPlanePointDepth", "dGeomCapsulePointDepth"):
+            getattr(lib, n).restype = F
+            getattr(lib, n).argtypes = [P, F, F, F]
+        lib.dGeomSphereSetRadius.argtypes = [P, F]
+        lib.dGeomBoxSetLengths.argtypes = [P, F, F, F]
+        lib.dGeomPlaneSetParams.argtypes = [P, F, F, F, F]
+        lib.dGeomCapsuleSetParams.argtypes = [P, F, F]
+        lib.dGeomPlaneGetParams.argtypes = lib.dGeomBoxGetLengths.argtypes = [P, P]
+        lib.dGeomSphereGetRadius.restype = F
+        lib.dGeomSphereGetRadius.argtypes = [P]
+        lib.dGeomCapsuleGetParams.argtypes = [P, P, P]
+        lib.dGeomHeightfieldDataBuildSingle.argtypes = [P, P, I, F, F, I, I, F, F, F, I]
+        lib.dGeomHeightfieldDataSetBounds.argtypes = [P, F, F]
+        lib.dGeomHeightfieldDataDestroy.argtypes = [P]
+        lib.dCreateHeightfield.argtypes = [P, P, I]
+        lib.dWorldDestroy.argtypes = [P]
+    return ours, ref
+
+
+def _rot(lib, a):
+    R = M12()
+    lib.dRFromAxisAndAngle(R, *a)
+    return R
+
+
+def _quat(lib, a):
+    q = V4()
+    lib.dQFromAxisAndAngle(q, *a)
+    return q
+
+
+def _v3(p):
+    return [p[k] for k in range(3)]
+
+
+def _m9(p):
+    return [p[r * 4 + c] for r in range(3) for c in range(3)]
+
+
+def _out4(lib, fn, g):
+    r = V4()
+    fn(g, r)
+    return list(r)
+
+
+def _pose(lib, g):
+    return _v3(lib.dGeomGetPosition(g)) + _m9(lib.dGeomGetRotation(g))
+
+
+def _aabb(lib, g):
+    a = (F * 6)()
+    lib.dGeomGetAABB(g, a)
+    return list(a)
+
+
+def _points(lib, g, pts):
+    out = []
+    for name in ("dGeomGetRelPointPos", "dGeomGetPosRelPoint", "dGeomVectorToWorld", "dGeomVectorFromWorld"):
+        for p in pts:
+            r = V4()
+            getattr(lib, name)(g, *p, r)
+            out += list(r)[:3]
+    return out
+
+
+def _offset_sequence(lib, a):
+    """Offsets, the offset-aware setters and getters, then detach."""
+    out = []
+    w = lib.dWorldCreate()
+    b = lib.dBodyCreate(w)
+    lib.dBodySetPosition(b, *a[0:3])
+    lib.dBodySetRotation(b, _rot(lib, a[3:7]))
+    g = lib.dCreateBox(None, abs(a[7]) + 0.2, abs(a[8]) + 0.2, abs(a[9]) + 0.2)
+    lib.dGeomSetBody(g, b)
+    out += [lib.dGeomIsOffset(g)] + _pose(lib, g) + _out4(lib, lib.dGeomGetQuaternion, g)
+    lib.dGeomSetOffsetPosition(g, *a[10:13])
+    lib.dGeomSetOffsetRotation(g, _rot(lib, a[13:17]))
+    out += [lib.dGeomIsOffset(g)] + _pose(lib, g) + _out4(lib, lib.dGeomGetQuaternion, g)
+    out += _out4(lib, lib.dGeomCopyOffsetPosition, g)[:3] + _v3(lib.dGeomGetOffsetPosition(g))
+    out += _m9(lib.dGeomGetOffsetRotation(g)) + _out4(lib, lib.dGeomGetOffsetQuaternion, g)
+    out += _aabb(lib, g) + _points(lib, g, [a[17:20], a[20:23]])
+    out += [lib.dGeomBoxPointDepth(g, *p) for p in (a[0:3], a[17:20], a[20:23])]
+    pos = V4()
+    R = M12()
+    lib.dGeomCopyPosition(g, pos)
+    lib.dGeomCopyRotation(g, R)
+    out += list(pos)[:3] + _m9(R)
+    lib.dGeomSetOffsetQuaternion(g, _quat(lib, a[23:27]))
+    out += _pose(lib, g)
+    lib.dGeomSetOffsetWorldPosition(g, *a[27:30])
+    out += _pose(lib, g) + _v3(lib.dGeomGetOffsetPosition(g))
+    lib.dGeomSetOffsetWorldRotation(g, _rot(lib, a[30:34]))
+    out += _pose(lib, g) + _m9(lib.dGeomGetOffsetRotation(g))
+    lib.dGeomSetOffsetWorldQuaternion(g, _quat(lib, a[34:38]))
+    out += _pose(lib, g) + _m9(lib.dGeomGetOffsetRotation(g))
+    # the pose setters move the body so that body + offset lands on the pose
+    lib.dGeomSetPosition(g, *a[38:41])
+    out += _pose(lib, g) + _v3(lib.dBodyGetPosition(b)) + _m9(lib.dBodyGetRotation(b))
+    lib.dGeomSetRotation(g, _rot(lib, a[41:45]))
+    out += _pose(lib, g) + _v3(lib.dBodyGetPosition(b)) + _m9(lib.dBodyGetRotation(b))
+    lib.dGeomSetQuaternion(g, _quat(lib, a[45:49]))
+    out += _pose(lib, g) + _v3(lib.dBodyGetPosition(b)) + _m9(lib.dBodyGetRotation(b))
+    # moving the body moves the offset geom
+    lib.dBodySetPosition(b, *a[49:52])
+    out += _pose(lib, g) + _aabb(lib, g)
+    # detach keeps the final pose; a second geom keeps the body's
+    g2 = lib.dCreateSphere(None, 0.3)
+    lib.dGeomSetBody(g2, b)
+    lib.dGeomSetBody(g, None)
+    out += [lib.dGeomIsOffset(g), int(lib.dGeomGetBody(g) is None)] + _pose(lib, g)
+    lib.dBodySetPosition(b, 0.0, 0.0, 0.0)
+    out += _pose(lib, g)
+    # clearing an offset returns the geom to its body's pose
+    lib.dGeomSetBody(g, b)
+    lib.dGeomSetOffsetPosition(g, 0.5, -0.25, 1.0)
+    lib.dGeomClearOffset(g)
+    out += [lib.dGeomIsOffset(g)] + _pose(lib, g) + _out4(lib, lib.dGeomGetOffsetQuaternion, g)
+    out += _v3(lib.dGeomGetOffsetPosition(g)) + _m9(lib.dGeomGetOffsetRotation(g))
+    # dBodyDestroy detaches the body's geoms in place
+    lib.dBodySetPosition(b, *a[52:55])
+    lib.dGeomSetOffsetPosition(g, *a[55:58])
+    before = _pose(lib, g)
+    lib.dBodyDestroy(b)
+    out += before + [int(lib.dGeomGetBody(g) is None), int(lib.dGeomGetBody(g2) is None)]
+    out += _pose(lib, g) + _pose(lib, g2)
+    lib.dGeomDestroy(g)
+    lib.dGeomDestroy(g2)
+    lib.dWorldDestroy(w)
+    return np.array(out, dtype=np.float32)
+
+
+def _shape_sequence(lib, a):
+    """Free geoms of every class: AABBs, point depths, setters, bits."""
+    out = []
+    pts = [a[0:3], a[3:6], [0.0, 0.0, 0.0]]
+    geoms = [lib.dCreateSphere(None, abs(a[6]) + 0.1), lib.dCreateBox(None, abs(a[7]) + 0.1, abs(a[8]) + 0.1, 0.7),
+             lib.dCreateCapsule(None, abs(a[9]) + 0.1, abs(a[10]) + 0.2),
+             lib.dCreateCylinder(None, abs(a[11]) + 0.1, abs(a[12]) + 0.2), lib.dCreateRay(None, abs(a[13]) + 0.5)]
+    for i, g in enumerate(geoms):
+        lib.dGeomSetPosition(g, *a[14 + 3 * i:17 + 3 * i])
+        lib.dGeomSetQuaternion(g, _quat(lib, a[29 + 4 * i:33 + 4 * i]))
+        out += [lib.dGeomGetClass(g), lib.dGeomIsSpace(g), int(lib.dGeomGetSpace(g) is None)]
+        out += _pose(lib, g) + _out4(lib, lib.dGeomGetQuaternion, g) + _aabb(lib, g) + _points(lib, g, pts[:2])
+    sph, box, cap, cyl, ray = geoms
+    out += [lib.dGeomSpherePointDepth(sph, *p) for p in pts]
+    out += [lib.dGeomBoxPointDepth(box, *p) for p in pts]
+    out += [lib.dGeomCapsulePointDepth(cap, *p) for p in pts]
+    # setters
+    lib.dGeomSphereSetRadius(sph, 0.75)
+    lib.dGeomBoxSetLengths(box, 0.5, 1.5, 2.5)
+    lib.dGeomCapsuleSetParams(cap, 0.25, 1.75)
+    r, l = F(), F()
+    lib.dGeomCapsuleGetParams(cap, C.byref(r), C.byref(l))
+    out += [lib.dGeomSphereGetRadius(sph), r.value, l.value] + _out4(lib, lib.dGeomBoxGetLengths, box)[:3]
+    out += _aabb(lib, sph) + _aabb(lib, box) + _aabb(lib, cap)
+    out += [lib.dGeomSpherePointDepth(sph, *pts[0]), lib.dGeomBoxPointDepth(box, *pts[0]),
+            lib.dGeomCapsulePointDepth(cap, *pts[0])]
+    # planes: normalised parameters, half-space boxes along an axis
+    pl = lib.dCreatePlane(None, a[44], a[45], a[46], a[47])
+    out += _out4(lib, lib.dGeomPlaneGetParams, pl) + _aabb(lib, pl)
+    out += [lib.dGeomPlanePointDepth(pl, *p) for p in pts] + _points(lib, pl, pts[:1])
+    for prm in ((0.0, 0.0, -2.0, 0.5), (0.0, 3.0, 0.0, -1.0), (4.0, 0.0, 0.0, 2.0), (0.0, 0.0, 0.0, 1.0),
+                (a[48], a[49], 0.0, a[50])):
+        lib.dGeomPlaneSetParams(pl, *prm)
+        out += _out4(lib, lib.dGeomPlaneGetParams, pl) + _aabb(lib, pl)
+        out += [lib.dGeomPlanePointDepth(pl, *pts[0])]
+    # bits and the enabled flag
+    g = geoms[0]
+    out += [float(lib.dGeomGetCategoryBits(g) == C.c_ulong(-1).value),
+            float(lib.dGeomGetCollideBits(g) == C.c_ulong(-1).value), lib.dGeomIsEnabled(g)]
+    lib.dGeomSetCategoryBits(g, 0x5)
+    lib.dGeomSetCollideBits(g, 0xA0)
+    lib.dGeomDisable(g)
+    out += [lib.dGeomGetCategoryBits(g), lib.dGeomGetCollideBits(g), lib.dGeomIsEnabled(g)]
+    lib.dGeomEnable(g)
+    out += [lib.dGeomIsEnabled(g)]
+    for g in geoms + [pl]:
+        lib.dGeomDestroy(g)
+    return np.array(out, dtype=np.float32)
+
+
+def _heightfield_sequence(lib, a, heights, wrap):
+    out = []
+    d = lib.dGeomHeightfieldDataCreate()
+    h = np.ascontiguousarray(heights, dtype=np.float32)
+    nz, nx = h.shape
+    lib.dGeomHeightfieldDataBuildSingle(d, h.ctypes.data, 0, 6.0, 4.0, nx, nz, 1.5, -0.25, 0.5, wrap)
+    fixed = lib.dCreateHeightfield(None, d, 0)
+    placed = lib.dCreateHeightfield(None, d, 1)
+    lib.dGeomSetPosition(placed, *a[0:3])
+    lib.dGeomSetRotation(placed, _rot(lib, a[3:7]))
+    out += _aabb(lib, fixed) + _aabb(lib, placed) + _points(lib, fixed, [a[7:10]])
+    # new bounds reach boxes computed afterwards
+    lib.dGeomHeightfieldDataSetBounds(d, -2.0, 3.0)
+    for bp in (0, 1):
+        g = lib.dCreateHeightfield(None, d, bp)
+        if bp:
+            lib.dGeomSetPosition(g, *a[0:3])
+            lib.dGeomSetRotation(g, _rot(lib, a[3:7]))
+        out += _aabb(lib, g)
+        lib.dGeomDestroy(g)
+    lib.dGeomDestroy(fixed)
+    lib.dGeomDestroy(placed)
+    lib.dGeomHeightfieldDataDestroy(d)
+    return np.array(out, dtype=np.float32)
+
+
+def _close(x, y, rtol):
+    """Equal where both are infinite; within rtol * (1 + |y|) elsewhere."""
+    assert x.shape == y.shape
+    inf = np.isinf(y)
+    assert np.array_equal(np.isinf(x), inf) and np.array_equal(x[inf], y[inf]), (x[inf], y[inf])
+    err = np.abs(x[~inf] - y[~inf]) / (1.0 + np.abs(y[~inf]))
+    assert err.max(initial=0.0) <= rtol, (err.max(), int(np.argmax(err)))
+
+
+def test_geom_offsets_match_reference_fp32():
+    ours, ref = _libs()
+    rng = np.random.default_rng(41)
+    for _ in range(60):
+        a = [float(x) for x in rng.normal(size=58)]
+        x, y = _offset_sequence(ours, a), _offset_sequence(ref, a)
+        # within FP32 rounding: dBodySetRotation keeps a body's orientation
+        # through a quaternion formed in FP64 here and in FP32 in the
+        # reference (a few ulps of R), which every later pose inherits
+        _close(x, y, 2e-5)
+
+
+def test_geom_shapes_bits_and_bounds_match_reference_fp32():
+    ours, ref = _libs()
+    rng = np.random.default_rng(43)
+    for _ in range(60):
+        a = [float(x) for x in rng.normal(size=51)]
+        x, y = _shape_sequence(ours, a), _shape_sequence(ref, a)
+        _close(x, y, 2e-6)
+
+
+@pytest.mark.parametrize("wrap", [0, 1])
+def test_heightfield_bounds_match_reference_fp32(wrap):
+    ours, ref = _libs()
+    rng = np.random.default_rng(47 + wrap)
+    for _ in range(20):
+        a = [float(x) for x in rng.normal(size=10)]
+        heights = rng.normal(size=(5, 7)) * 2.0
+        x, y = _heightfield_sequence(ours, a, heights, wrap), _heightfield_sequence(ref, a, heights, wrap)
+        _close(x, y, 2e-6)

@@ -189,6 +189,83 @@ def test_dcollide_on_reference_kats():
     assert worst < 1e-3, worst
 
 
+def test_dcollide_with_offset_geoms():
+    """A geom placed on its body by an offset (ode/src/collision_kernel.cpp:
+    1036-1250) collides from its final pose, body.R * offset + body.pos
+    (dxGeom::computePosr, :454-465): dCollide of the offset geom equals dCollide
+    of a free geom put at that pose, bit for bit, and the pose follows the body
+    through a dWorldQuickStep."""
+    L = _api()
+    f, v = C.c_float, C.c_void_p
+    for n in ("dWorldCreate", "dBodyCreate"):
+        getattr(L, n).restype = v
+    L.dBodyCreate.argtypes = [v]
+    L.dWorldSetGravity.argtypes = [v, f, f, f]
+    L.dWorldQuickStep.argtypes = [v, f]
+    L.dWorldDestroy.argtypes = [v]
+    L.dBodySetPosition.argtypes = [v, f, f, f]
+    L.dBodySetRotation.argtypes = [v, C.POINTER(f)]
+    L.dBodySetAngularVel.argtypes = [v, f, f, f]
+    L.dBodyGetPosition.restype = L.dBodyGetRotation.restype = C.POINTER(f)
+    L.dBodyGetPosition.argtypes = L.dBodyGetRotation.argtypes = [v]
+    L.dRFromAxisAndAngle.argtypes = [C.POINTER(f), f, f, f, f]
+    L.dGeomSetBody.argtypes = [v, v]
+    L.dGeomSetOffsetPosition.argtypes = [v, f, f, f]
+    L.dGeomSetOffsetRotation.argtypes = [v, C.POINTER(f)]
+    L.dGeomGetPosition.restype = L.dGeomGetRotation.restype = C.POINTER(f)
+    L.dGeomGetPosition.argtypes = L.dGeomGetRotation.argtypes = [v]
+    M12 = f * 12
+
+    def rot(a):
+        R = M12()
+        L.dRFromAxisAndAngle(R, *a)
+        return R
+
+    def contacts(g1, g2):
+        out = (ContactGeom * 8)()
+        n = L.dCollide(g1, g2, 8, out, C.sizeof(ContactGeom))
+        return n, [list(out[c].pos[:3]) + list(out[c].normal[:3]) + [out[c].depth] for c in range(n)]
+
+    rng = np.random.default_rng(53)
+    hits = 0
+    for _ in range(40):
+        a = [float(x) for x in rng.normal(size=16)]
+        w = L.dWorldCreate()
+        L.dWorldSetGravity(w, 0.0, 0.0, -9.81)
+        b = L.dBodyCreate(w)
+        L.dBodySetPosition(b, *a[0:3])
+        L.dBodySetRotation(b, rot(a[3:7]))
+        L.dBodySetAngularVel(b, *a[13:16])
+        g = L.dCreateBox(None, 0.6, 0.4, 0.8)
+        L.dGeomSetBody(g, b)
+        L.dGeomSetOffsetPosition(g, 0.5 * a[7], 0.5 * a[8], 0.5 * a[9])
+        L.dGeomSetOffsetRotation(g, rot(a[9:13]))
+        gp = L.dGeomGetPosition(g)
+        s = L.dCreateSphere(None, 0.35)
+        L.dGeomSetPosition(s, gp[0] + 0.3 * a[10], gp[1] + 0.3 * a[11], gp[2] + 0.3 * a[12])
+        free = L.dCreateBox(None, 0.6, 0.4, 0.8)
+        L.dGeomSetPosition(free, gp[0], gp[1], gp[2])
+        gR = L.dGeomGetRotation(g)
+        L.dGeomSetRotation(free, M12(*[gR[k] for k in range(12)]))
+        n1, c1 = contacts(g, s)
+        n2, c2 = contacts(free, s)
+        assert n1 == n2 and c1 == c2, (n1, n2)
+        n3, c3 = contacts(s, g)
+        n4, c4 = contacts(s, free)
+        assert n3 == n4 and c3 == c4, (n3, n4)
+        hits += n1 > 0
+        assert L.dWorldQuickStep(w, 0.01) == 1
+        bp, bR = L.dBodyGetPosition(b), L.dBodyGetRotation(b)
+        Rb = np.array([[bR[r * 4 + c] for c in range(3)] for r in range(3)], dtype=np.float32)
+        want = Rb @ np.float32([0.5 * a[7], 0.5 * a[8], 0.5 * a[9]]) + np.float32([bp[0], bp[1], bp[2]])
+        gp = L.dGeomGetPosition(g)
+        assert np.allclose([gp[0], gp[1], gp[2]], want, atol=1e-5)
+        for h in (g, s, free):
+            L.dGeomDestroy(h)
+        L.dWorldDestroy(w)
+    assert hits >= 10, hits
+
+
 class JointFeedback(C.Structure):
     _fields_ = [("f1", C.c_float * 4), ("t1", C.c_float * 4), ("f2", C.c_float * 4), ("t2", C.c_float * 4)]
 
