@@ -85,9 +85,11 @@ typedef struct dJointFeedback {
   dVector3 f1, t1, f2, t2;
 } dJointFeedback;
 
-/* include/ode/collision.h:881-890 */
+/* include/ode/collision.h:881-899 */
 enum { dSphereClass = 0, dBoxClass, dCapsuleClass, dCylinderClass, dPlaneClass,
-       dRayClass, dConvexClass, dGeomTransformClass, dTriMeshClass, dHeightfieldClass };
+       dRayClass, dConvexClass, dGeomTransformClass, dTriMeshClass, dHeightfieldClass,
+       dFirstSpaceClass, dSimpleSpaceClass = dFirstSpaceClass, dHashSpaceClass,
+       dSweepAndPruneSpaceClass, dQuadTreeSpaceClass, dLastSpaceClass = dQuadTreeSpaceClass };
 
 /* include/ode/common.h:252-258 */
 typedef enum { dJointTypeNone = 0, dJointTypeBall, dJointTypeHinge, dJointTypeSlider,
@@ -326,9 +328,7 @@ void dNormalize3(dVector3 a);                                            /* :426
 void dNormalize4(dVector4 a);                                            /* :427 */
 void dPlaneSpace(const dVector3 n, dVector3 p, dVector3 q);              /* :462 */
 
-/* collision: include/ode/collision.h (space argument must be 0: spaces are
- * not on this path, pairs come from the caller; dGeomGetSpace returns the
- * handle given at creation) */
+/* collision: include/ode/collision.h */
 int dCollide(dGeomID o1, dGeomID o2, int flags, dContactGeom* contact, int skip); /* :795 */
 dGeomID dCreateSphere(dSpaceID space, dReal radius);                     /* :924 */
 dGeomID dCreateBox(dSpaceID space, dReal lx, dReal ly, dReal lz);        /* :1002 */
@@ -391,8 +391,8 @@ void dGeomGetAABB(dGeomID g, dReal aabb[6]);                             /* :264
 int dGeomIsSpace(dGeomID g);                                             /* :273 */
 dSpaceID dGeomGetSpace(dGeomID g);                                       /* :283 */
 int dGeomGetClass(dGeomID g);                                            /* :310 */
-/* Category / collide bits and the enabled flag are kept for the getters; they
- * steer a space's pair search, and dCollide reads none of them. */
+/* Category / collide bits and the enabled flag steer a space's pair search;
+ * dCollide reads none of them. */
 void dGeomSetCategoryBits(dGeomID g, unsigned long bits);                /* :325 */
 void dGeomSetCollideBits(dGeomID g, unsigned long bits);                 /* :340 */
 unsigned long dGeomGetCategoryBits(dGeomID g);                           /* :351 */
@@ -418,6 +418,32 @@ void dGeomCopyOffsetPosition(dGeomID g, dVector3 pos);                   /* :693
 const dReal* dGeomGetOffsetRotation(dGeomID g);                          /* :710 */
 void dGeomCopyOffsetRotation(dGeomID g, dMatrix3 R);                     /* :724 */
 void dGeomGetOffsetQuaternion(dGeomID g, dQuaternion result);            /* :737 */
+/* Spaces: include/ode/collision_space.h. Simple and hash spaces enumerate
+ * candidate pairs on the host in ODE's order (a geom that moves goes to the
+ * front of its space's list, as do the geoms of every body a step moves, in
+ * the step's island order), so a near-callback sees the pairs ODE would pass.
+ * Sweep-and-prune and quadtree spaces are not built. */
+typedef void dNearCallback(void* data, dGeomID o1, dGeomID o2);         /* collision_space.h:49 */
+dSpaceID dSimpleSpaceCreate(dSpaceID space);                             /* :52 */
+dSpaceID dHashSpaceCreate(dSpaceID space);                               /* :53 */
+void dSpaceDestroy(dSpaceID space);                                      /* :70 */
+void dHashSpaceSetLevels(dSpaceID space, int minlevel, int maxlevel);    /* :72 */
+void dHashSpaceGetLevels(dSpaceID space, int* minlevel, int* maxlevel);  /* :73 */
+void dSpaceSetCleanup(dSpaceID space, int mode);                         /* :75 */
+int dSpaceGetCleanup(dSpaceID space);                                    /* :76 */
+void dSpaceSetSublevel(dSpaceID space, int sublevel);                    /* :100 */
+int dSpaceGetSublevel(dSpaceID space);                                   /* :114 */
+void dSpaceSetManualCleanup(dSpaceID space, int mode);                   /* :133 */
+int dSpaceGetManualCleanup(dSpaceID space);                              /* :147 */
+void dSpaceAdd(dSpaceID space, dGeomID g);                               /* :149 */
+void dSpaceRemove(dSpaceID space, dGeomID g);                            /* :150 */
+int dSpaceQuery(dSpaceID space, dGeomID g);                              /* :151 */
+void dSpaceClean(dSpaceID space);                                        /* :152 */
+int dSpaceGetNumGeoms(dSpaceID space);                                   /* :153 */
+dGeomID dSpaceGetGeom(dSpaceID space, int i);                            /* :154 */
+int dSpaceGetClass(dSpaceID space);                                      /* :176 */
+void dSpaceCollide(dSpaceID space, void* data, dNearCallback* callback); /* collision.h:825 */
+void dSpaceCollide2(dGeomID space1, dGeomID space2, void* data, dNearCallback* callback);  /* collision.h:868 */
 /* class parameters and point depths */
 void dGeomSphereSetRadius(dGeomID g, dReal radius);                      /* :936 */
 dReal dGeomSphereGetRadius(dGeomID g);                                   /* :947 */

@@ -8,9 +8,11 @@
 // on the host. Setter arithmetic (anchors, axes, inertia inverse) is host FP64
 // as in host_setup.hpp.
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstring>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "ode_gpu.h"
@@ -33,6 +35,7 @@ struct dxBody {
   double invMass;
   int flags;   // ODEGPU_BODY_*
   void* data;  // dBodySetData
+  dxGeom* geom;   // the body's geoms, newest attached first (dxGeom::bodyAdd)
 };
 
 struct dxJoint {
@@ -80,13 +83,39 @@ struct dxGeom {
   int placeable;             // heightfield geoms: created placeable
   int ray_flags;             // ray geoms: kRay* below
   void* data;                // dGeomSetData
-  dSpaceID space;            // the space passed at creation (dGeomGetSpace)
   unsigned long category_bits, collide_bits;   // ~0 at creation (collision_kernel.cpp:343-368)
   int enabled;               // GEOM_ENABLED
+  int zero_sized;            // GEOM_ZERO_SIZED: a zero radius or side (sphere.cpp:55 and the like)
   int has_offset;            // offset_posr != 0: placed relative to its body
   dReal opos[4], oR[12];     // the offset (body frame)
   dReal fpos[4], fR[12];     // an offset geom's own final pose, recomputed on every read
+  dxGeom* body_next;         // next geom on the same body
+  // space membership (collision_kernel.h:150-171, collision_space.cpp:162-205):
+  // the parent space, the intrusive list link, and the GEOM_DIRTY /
+  // GEOM_AABB_BAD flags with the cached box they guard
+  dxSpace* space;
+  dxGeom* next;
+  dxGeom** tome;
+  int dirty, aabb_bad;
+  dReal aabb[6];
 };
+
+// dxSpace (collision_kernel.h:190-245): a geom of a space class holding the
+// list of its geoms, newest or most recently moved first
+struct dxSpace : dxGeom {
+  dxGeom* first;
+  int count;
+  int cleanup;          // destroy the geoms with the space (default 1)
+  int sublevel;         // dSpaceCollide2's nesting rule
+  int manual_cleanup;
+  int minlevel, maxlevel;   // hash space cell levels (-3, 10)
+};
+static bool is_space(const dxGeom* g) { return g->type >= dFirstSpaceClass && g->type <= dLastSpaceClass; }
+// every attached geom is notified when its body moves (ode.cpp:362-395, util.cpp:334-336)
+extern "C" {
+static void body_geoms_moved(dxBody* b);
+static void body_geoms_detach(dxBody* b);
+}
 
 // dxGeom::gflags bits of a ray (ode/src/collision_kernel.h: RAY_FIRSTCONTACT,
 // RAY_BACKFACECULL, RAY_CLOSEST_HIT). They steer the trimesh collider only, so
@@ -109,7 +138,6 @@ struct dxWorld {
 namespace {
 
 unsigned long g_seed = 0;   // ODE's global dRand state (ode/src/misc.cpp:31)
-std::vector<dxGeom*> g_geoms;   // live geoms, for dBodyDestroy's detach
 thread_local std::string g_err;
 
 void body_sync_R(dxBody* b) {
@@ -238,7 +266,10 @@ void dWorldDestroy(dWorldID w) {
   for (dxJoint* j : w->joints) j->world = nullptr;
   for (dxJoint* j : std::vector<dxJoint*>(w->joints))
     if (!j->group) delete j;
-  for (dxBody* b : w->bodies) delete b;
+  for (dxBody* b : w->bodies) {   // dBodyDestroy of each body (ode.cpp:1589-1594)
+    body_geoms_detach(b);
+    delete b;
+  }
   og::ctx_destroy(w->ctx);
   delete w;
 }
@@ -275,9 +306,7 @@ dBodyID dBodyCreate(dWorldID w) {
 }
 void dBodyDestroy(dBodyID b) {
   if (!b) return;
-  // the body's geoms are detached first, keeping their pose (ode.cpp:301-310)
-  for (dxGeom* g : g_geoms)
-    if (g->body == b) dGeomSetBody(g, nullptr);
+  body_geoms_detach(b);
   dxWorld* w = b->world;
   for (dxJoint* j : w->joints) {
     for (int i = 0; i < 2; ++i)
@@ -287,12 +316,16 @@ void dBodyDestroy(dBodyID b) {
   w->bodies.erase(std::remove(w->bodies.begin(), w->bodies.end(), b), w->bodies.end());
   delete b;
 }
-void dBodySetPosition(dBodyID b, dReal x, dReal y, dReal z) { b->pos[0] = x; b->pos[1] = y; b->pos[2] = z; }
+void dBodySetPosition(dBodyID b, dReal x, dReal y, dReal z) {
+  b->pos[0] = x; b->pos[1] = y; b->pos[2] = z;
+  body_geoms_moved(b);
+}
 void dBodySetQuaternion(dBodyID b, const dQuaternion q) {
   double qd[4] = {q[0], q[1], q[2], q[3]};
   og_host::normalize4(qd);
   for (int k = 0; k < 4; ++k) b->q[k] = (dReal)qd[k];
   body_sync_R(b);
+  body_geoms_moved(b);
 }
 void dBodySetRotation(dBodyID b, const dMatrix3 R) {
   // dQfromR (ode/src/rotation.cpp:258-307), then normalise as dBodySetRotation does
@@ -323,6 +356,7 @@ void dBodySetRotation(dBodyID b, const dMatrix3 R) {
   og_host::normalize4(q);
   for (int k = 0; k < 4; ++k) b->q[k] = (dReal)q[k];
   body_sync_R(b);
+  body_geoms_moved(b);
 }
 void dBodySetLinearVel(dBodyID b, dReal x, dReal y, dReal z) { b->lvel[0] = x; b->lvel[1] = y; b->lvel[2] = z; }
 void dBodySetAngularVel(dBodyID b, dReal x, dReal y, dReal z) { b->avel[0] = x; b->avel[1] = y; b->avel[2] = z; }
@@ -941,18 +975,89 @@ void dRandSetSeed(unsigned long s) { g_seed = s & 0xffffffffUL; }
 int dRandInt(int n) { return og::rand_int_from((unsigned)dRand(), n); }
 
 // ---------------------------------------------------------------- geoms + dCollide
-// dxGeom::dxGeom (collision_kernel.cpp:343-368): identity pose, enabled, all
-// category and collide bits set
+// ---------------------------------------------------------------- spaces (core)
+// The list discipline of collision_space.cpp:42-206: a geom joins its space at
+// the front; a clean geom that moves becomes dirty and goes to the front again,
+// and so do its parent spaces; dSpaceCollide cleans the dirty prefix (boxes
+// recomputed, flags cleared) and then visits pairs in list order. The order of
+// the near-callback's pairs, and with it the order of the contact joints a
+// program creates, follows from this.
+static void list_push_front(dxGeom** first, dxGeom* g) {   // dxGeom::spaceAdd
+  g->next = *first;
+  g->tome = first;
+  if (*first) (*first)->tome = &g->next;
+  *first = g;
+}
+static void list_unlink(dxGeom* g) {   // dxGeom::spaceRemove
+  if (g->next) g->next->tome = g->tome;
+  *g->tome = g->next;
+}
+// dGeomMoved (collision_space.cpp:47-74)
+static void geom_moved(dxGeom* g) {
+  dxSpace* parent = g->space;
+  while (parent && !g->dirty) {
+    g->dirty = g->aabb_bad = 1;
+    list_unlink(g);
+    list_push_front(&parent->first, g);
+    g = parent;
+    parent = parent->space;
+  }
+  for (; g; g = g->space) g->dirty = g->aabb_bad = 1;
+}
+// dxSpace::add / remove (collision_space.cpp:162-206)
+static void space_add(dxSpace* s, dxGeom* g) {
+  if (!s || !g || g->space) return;
+  g->space = s;
+  list_push_front(&s->first, g);
+  ++s->count;
+  g->dirty = g->aabb_bad = 1;
+  geom_moved(s);
+}
+static void space_remove(dxSpace* s, dxGeom* g) {
+  if (!s || !g || g->space != s) return;
+  list_unlink(g);
+  --s->count;
+  g->next = nullptr;
+  g->tome = nullptr;
+  g->space = nullptr;
+  geom_moved(s);
+}
+static void body_list_remove(dxGeom* g) {   // dxGeom::bodyRemove (collision_kernel.cpp:396-412)
+  if (!g->body) return;
+  for (dxGeom** l = &g->body->geom; *l; l = &(*l)->body_next)
+    if (*l == g) { *l = g->body_next; break; }
+  g->body = nullptr;
+  g->body_next = nullptr;
+}
+static void body_geoms_moved(dxBody* b) {
+  for (dxGeom* g = b->geom; g; g = g->body_next) geom_moved(g);
+}
+static void body_geoms_detach(dxBody* b) {   // dBodyDestroy (ode.cpp:301-310)
+  for (dxGeom *g = b->geom, *n; g; g = n) {
+    n = g->body_next;
+    dGeomSetBody(g, nullptr);
+  }
+}
+
+// dxGeom::dxGeom (collision_kernel.cpp:343-368): identity pose, enabled,
+// dirty, all category and collide bits set, then into the space if one is given
+static void init_geom(dxGeom* g, dSpaceID space, int type) {
+  g->type = type;
+  g->R[0] = g->R[5] = g->R[10] = 1;
+  g->category_bits = g->collide_bits = ~0UL;
+  g->enabled = 1;
+  g->dirty = g->aabb_bad = 1;
+  if (space) space_add(space, g);
+}
 static dGeomID new_geom(dSpaceID space, int type, const double* p) {
   auto* g = new dxGeom();
   std::memset(g, 0, sizeof(*g));
-  g->type = type;
   for (int k = 0; k < 4; ++k) g->p[k] = p[k];
-  g->R[0] = g->R[5] = g->R[10] = 1;
-  g->space = space;
-  g->category_bits = g->collide_bits = ~0UL;
-  g->enabled = 1;
-  g_geoms.push_back(g);
+  // GEOM_ZERO_SIZED (sphere.cpp:55, box.cpp:56, capsule.cpp:56, cylinder.cpp:55)
+  if (type == dSphereClass || type == dCapsuleClass) g->zero_sized = (dReal)p[0] == 0;
+  if (type == dBoxClass) g->zero_sized = (dReal)p[0] == 0 || (dReal)p[1] == 0 || (dReal)p[2] == 0;
+  if (type == dCylinderClass) g->zero_sized = (dReal)p[0] == 0 || (dReal)p[1] == 0;
+  init_geom(g, space, type);
   return g;
 }
 dGeomID dCreateSphere(dSpaceID s, dReal r) { const double p[4] = {r, 0, 0, 0}; return new_geom(s, dSphereClass, p); }
@@ -968,8 +1073,11 @@ dGeomID dCreateCylinder(dSpaceID s, dReal r, dReal len) {
   const double p[4] = {r, len, 0, 0};
   return new_geom(s, dCylinderClass, p);
 }
-void dGeomCylinderSetParams(dGeomID g, dReal r, dReal len) {
-  if (g && g->type == dCylinderClass) { g->p[0] = r; g->p[1] = len; }
+void dGeomCylinderSetParams(dGeomID g, dReal r, dReal len) {   // cylinder.cpp:84-93
+  if (!g || g->type != dCylinderClass) return;
+  g->p[0] = r; g->p[1] = len;
+  g->zero_sized = r == 0 || len == 0;
+  geom_moved(g);
 }
 void dGeomCylinderGetParams(dGeomID g, dReal* r, dReal* l) {
   if (g && g->type == dCylinderClass) { *r = (dReal)g->p[0]; *l = (dReal)g->p[1]; }
@@ -988,10 +1096,23 @@ dGeomID dCreatePlane(dSpaceID s, dReal a, dReal b, dReal c, dReal d) {
   plane_params(p, a, b, c, d);
   return new_geom(s, dPlaneClass, p);
 }
+// dGeomDestroy (collision_kernel.cpp:486-490 with ~dxGeom, :376-383): a space
+// first destroys (cleanup on) or releases its geoms (collision_space.cpp:96-113);
+// then the geom leaves its space and its body
 void dGeomDestroy(dGeomID g) {
   if (!g) return;
-  g_geoms.erase(std::remove(g_geoms.begin(), g_geoms.end(), g), g_geoms.end());
-  delete g;
+  if (is_space(g)) {
+    auto* sp = static_cast<dxSpace*>(g);
+    for (dxGeom *c = sp->first, *n; c; c = n) {
+      n = c->next;
+      if (sp->cleanup) dGeomDestroy(c);
+      else space_remove(sp, c);
+    }
+  }
+  if (g->space) space_remove(g->space, g);
+  body_list_remove(g);
+  if (is_space(g)) delete static_cast<dxSpace*>(g);
+  else delete g;
 }
 
 // Rays (ode/src/ray.cpp:49-194): the length is the class parameter; the start
@@ -1002,19 +1123,27 @@ dGeomID dCreateRay(dSpaceID s, dReal length) {
   return new_geom(s, dRayClass, p);
 }
 void dGeomRaySetLength(dGeomID g, dReal length) {
-  if (g && g->type == dRayClass) g->p[0] = length;
+  if (!g || g->type != dRayClass) return;
+  g->p[0] = length;
+  geom_moved(g);
 }
 dReal dGeomRayGetLength(dGeomID g) { return (g && g->type == dRayClass) ? (dReal)g->p[0] : 0; }
 void dGeomRaySet(dGeomID g, dReal px, dReal py, dReal pz, dReal dx, dReal dy, dReal dz) {
   // writes the placement the ray reads: a body's own when attached
   // (final_posr is the body's, ray.cpp:115-136), with the direction normalised
+  // An offset ray writes its own final pose, which the next read rebuilds
+  // from the body and the offset (ray.cpp:113-135 with dGeomMoved), so the
+  // call changes nothing there.
   if (!g || g->type != dRayClass) return;
-  double n[3] = {dx, dy, dz};
-  og_host::safe_normalize3(n);
-  dReal* pos = g->body ? g->body->pos : g->pos;
-  dReal* R = g->body ? g->body->R : g->R;
-  pos[0] = px; pos[1] = py; pos[2] = pz;
-  R[2] = (dReal)n[0]; R[6] = (dReal)n[1]; R[10] = (dReal)n[2];
+  if (!g->has_offset) {
+    double n[3] = {dx, dy, dz};
+    og_host::safe_normalize3(n);
+    dReal* pos = g->body ? g->body->pos : g->pos;
+    dReal* R = g->body ? g->body->R : g->R;
+    pos[0] = px; pos[1] = py; pos[2] = pz;
+    R[2] = (dReal)n[0]; R[6] = (dReal)n[1]; R[10] = (dReal)n[2];
+  }
+  geom_moved(g);
 }
 void dGeomRayGet(dGeomID g, dVector3 start, dVector3 dir) {
   if (!g || g->type != dRayClass) return;
@@ -1127,7 +1256,7 @@ dGeomID dCreateHeightfield(dSpaceID s, dHeightfieldDataID data, int bPlaceable) 
 // so that it follows the body through the step. Planes and non-placeable
 // heightfields have no pose (GEOM_PLACEABLE clear).
 static bool geom_placeable(const dxGeom* g) {
-  return g->type != dPlaneClass && !(g->type == dHeightfieldClass && !g->placeable);
+  return !is_space(g) && g->type != dPlaneClass && !(g->type == dHeightfieldClass && !g->placeable);
 }
 static void mul0_331(dReal* a, const dReal* R, const dReal* v) {   // a = R v
   for (int i = 0; i < 3; ++i) a[i] = R[i * 4 + 0] * v[0] + R[i * 4 + 1] * v[1] + R[i * 4 + 2] * v[2];
@@ -1194,19 +1323,23 @@ static bool geom_make_offset(dxGeom* g) {
 // any offset; detaching keeps the geom where it was (its final pose, or the
 // body's) as its own
 void dGeomSetBody(dGeomID g, dBodyID b) {
-  if (!g) return;
+  if (!g || !geom_placeable(g)) return;
   if (b) {
     if (g->body != b) {
       g->has_offset = 0;
+      body_list_remove(g);
       g->body = b;
+      g->body_next = b->geom;
+      b->geom = g;
     }
+    geom_moved(g);
   } else if (g->body) {
     const dReal* pos = geom_pos(g);
     const dReal* R = geom_R(g);
     for (int k = 0; k < 3; ++k) g->pos[k] = pos[k];
     for (int k = 0; k < 12; ++k) g->R[k] = R[k];
     g->has_offset = 0;
-    g->body = nullptr;
+    body_list_remove(g);
   }
 }
 dBodyID dGeomGetBody(dGeomID g) { return g->body; }
@@ -1221,6 +1354,7 @@ void dGeomSetPosition(dGeomID g, dReal x, dReal y, dReal z) {
     dBodySetPosition(g->body, x, y, z);
   } else {
     g->pos[0] = x; g->pos[1] = y; g->pos[2] = z;
+    geom_moved(g);
   }
 }
 void dGeomSetRotation(dGeomID g, const dMatrix3 R) {
@@ -1233,6 +1367,7 @@ void dGeomSetRotation(dGeomID g, const dMatrix3 R) {
     dBodySetRotation(g->body, R);
   } else {
     for (int k = 0; k < 12; ++k) g->R[k] = R[k];
+    geom_moved(g);
   }
 }
 void dGeomSetQuaternion(dGeomID g, const dQuaternion q) {
@@ -1249,6 +1384,7 @@ void dGeomSetQuaternion(dGeomID g, const dQuaternion q) {
     dBodySetQuaternion(g->body, q);
   } else {
     dRfromQ(g->R, q);
+    geom_moved(g);
   }
 }
 const dReal* dGeomGetPosition(dGeomID g) { return geom_pos(g); }
@@ -1270,11 +1406,27 @@ void dGeomGetQuaternion(dGeomID g, dQuaternion q) {   // :687-703
   }
 }
 
-// dGeomGetAABB (collision_kernel.cpp:705-711) with each class's computeAABB:
-// sphere.cpp:59-67, box.cpp:60-77, capsule.cpp:60-74, cylinder.cpp:59-76,
-// plane.cpp:80-107, ray.cpp:56-89, heightfield.cpp:475-600
-void dGeomGetAABB(dGeomID g, dReal aabb[6]) {
+// Each class's computeAABB: sphere.cpp:59-67, box.cpp:60-77,
+// capsule.cpp:60-74, cylinder.cpp:59-76, plane.cpp:80-107, ray.cpp:56-89,
+// heightfield.cpp:475-600, and a space's union of its geoms'
+// (collision_space.cpp:105-126)
+static void recompute_aabb(dxGeom* g);
+static void compute_aabb(dxGeom* g, dReal* aabb) {
   const float inf = INFINITY;
+  if (is_space(g)) {
+    const auto* sp = static_cast<const dxSpace*>(g);
+    if (!sp->first) {
+      for (int k = 0; k < 6; ++k) aabb[k] = 0;
+      return;
+    }
+    for (int k = 0; k < 6; ++k) aabb[k] = (k & 1) ? -inf : inf;
+    for (dxGeom* c = sp->first; c; c = c->next) {
+      recompute_aabb(c);
+      for (int k = 0; k < 6; k += 2) if (c->aabb[k] < aabb[k]) aabb[k] = c->aabb[k];
+      for (int k = 1; k < 6; k += 2) if (c->aabb[k] > aabb[k]) aabb[k] = c->aabb[k];
+    }
+    return;
+  }
   if (g->type == dPlaneClass) {
     const dReal p[4] = {(dReal)g->p[0], (dReal)g->p[1], (dReal)g->p[2], (dReal)g->p[3]};
     for (int k = 0; k < 6; ++k) aabb[k] = (k & 1) ? inf : -inf;
@@ -1363,9 +1515,19 @@ void dGeomGetAABB(dGeomID g, dReal aabb[6]) {
     aabb[2 * i + 1] = pos[i] + ext[i];
   }
 }
-// No spaces on this path: a geom is never a space, and reports the space
-// handle it was created with (collision_kernel.cpp:714-726)
-int dGeomIsSpace(dGeomID) { return 0; }
+// dxGeom::recomputeAABB (collision_kernel.h:151-157): the box is cached until
+// the geom moves
+static void recompute_aabb(dxGeom* g) {
+  if (!g->aabb_bad) return;
+  compute_aabb(g, g->aabb);
+  g->aabb_bad = 0;
+}
+void dGeomGetAABB(dGeomID g, dReal aabb[6]) {   // collision_kernel.cpp:705-711
+  recompute_aabb(g);
+  for (int k = 0; k < 6; ++k) aabb[k] = g->aabb[k];
+}
+// collision_kernel.cpp:714-726
+int dGeomIsSpace(dGeomID g) { return is_space(g) ? 1 : 0; }
 dSpaceID dGeomGetSpace(dGeomID g) { return g->space; }
 int dGeomGetClass(dGeomID g) { return g->type; }
 // Category / collide bits and the enabled flag (collision_kernel.cpp:735-782)
@@ -1409,18 +1571,22 @@ void dGeomVectorFromWorld(dGeomID g, dReal px, dReal py, dReal pz, dVector3 resu
 void dGeomSetOffsetPosition(dGeomID g, dReal x, dReal y, dReal z) {
   if (!geom_make_offset(g)) return;
   g->opos[0] = x; g->opos[1] = y; g->opos[2] = z;
+  geom_moved(g);
 }
 void dGeomSetOffsetRotation(dGeomID g, const dMatrix3 R) {
   if (!geom_make_offset(g)) return;
   for (int k = 0; k < 12; ++k) g->oR[k] = R[k];
+  geom_moved(g);
 }
 void dGeomSetOffsetQuaternion(dGeomID g, const dQuaternion q) {
   if (!geom_make_offset(g)) return;
   dRfromQ(g->oR, q);
+  geom_moved(g);
 }
 void dGeomSetOffsetWorldPosition(dGeomID g, dReal x, dReal y, dReal z) {
   if (!geom_make_offset(g)) return;
   dBodyGetPosRelPoint(g->body, x, y, z, g->opos);
+  geom_moved(g);
 }
 void dGeomSetOffsetWorldRotation(dGeomID g, const dMatrix3 R) {
   if (!geom_make_offset(g)) return;
@@ -1428,6 +1594,7 @@ void dGeomSetOffsetWorldRotation(dGeomID g, const dMatrix3 R) {
   const dReal* p = geom_pos(g);
   for (int k = 0; k < 3; ++k) fpos[k] = p[k];
   offset_for_final(g, fpos, R);
+  geom_moved(g);
 }
 void dGeomSetOffsetWorldQuaternion(dGeomID g, const dQuaternion q) {
   if (!geom_make_offset(g)) return;
@@ -1436,8 +1603,13 @@ void dGeomSetOffsetWorldQuaternion(dGeomID g, const dQuaternion q) {
   for (int k = 0; k < 3; ++k) fpos[k] = p[k];
   dRfromQ(fR, q);
   offset_for_final(g, fpos, fR);
+  geom_moved(g);
 }
-void dGeomClearOffset(dGeomID g) { g->has_offset = 0; }
+void dGeomClearOffset(dGeomID g) {
+  if (!g->has_offset) return;
+  g->has_offset = 0;
+  geom_moved(g);
+}
 int dGeomIsOffset(dGeomID g) { return g->has_offset ? 1 : 0; }
 static const dReal kZeroOffsetPos[4] = {0, 0, 0, 0};
 static const dReal kZeroOffsetR[12] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0};
@@ -1466,7 +1638,10 @@ void dGeomGetOffsetQuaternion(dGeomID g, dQuaternion q) {
 // plane.cpp:141-146, capsule.cpp:104-126, in dReal arithmetic.
 dReal dGeomSphereGetRadius(dGeomID g) { return (dReal)g->p[0]; }
 void dGeomSphereSetRadius(dGeomID g, dReal radius) {
-  if (g && g->type == dSphereClass) g->p[0] = radius;
+  if (!g || g->type != dSphereClass) return;
+  g->p[0] = radius;
+  g->zero_sized = radius == 0;
+  geom_moved(g);
 }
 dReal dGeomSpherePointDepth(dGeomID g, dReal x, dReal y, dReal z) {
   const dReal* pos = geom_pos(g);
@@ -1475,7 +1650,10 @@ dReal dGeomSpherePointDepth(dGeomID g, dReal x, dReal y, dReal z) {
 }
 void dGeomBoxGetLengths(dGeomID g, dVector3 r) { for (int k = 0; k < 3; ++k) r[k] = (dReal)g->p[k]; }
 void dGeomBoxSetLengths(dGeomID g, dReal lx, dReal ly, dReal lz) {
-  if (g && g->type == dBoxClass) { g->p[0] = lx; g->p[1] = ly; g->p[2] = lz; }
+  if (!g || g->type != dBoxClass) return;
+  g->p[0] = lx; g->p[1] = ly; g->p[2] = lz;
+  g->zero_sized = lx == 0 || ly == 0 || lz == 0;
+  geom_moved(g);
 }
 dReal dGeomBoxPointDepth(dGeomID g, dReal x, dReal y, dReal z) {
   const dReal* pos = geom_pos(g);
@@ -1500,7 +1678,9 @@ dReal dGeomBoxPointDepth(dGeomID g, dReal x, dReal y, dReal z) {
 }
 void dGeomPlaneGetParams(dGeomID g, dVector4 r) { for (int k = 0; k < 4; ++k) r[k] = (dReal)g->p[k]; }
 void dGeomPlaneSetParams(dGeomID g, dReal a, dReal b, dReal c, dReal d) {
-  if (g && g->type == dPlaneClass) plane_params(g->p, a, b, c, d);
+  if (!g || g->type != dPlaneClass) return;
+  plane_params(g->p, a, b, c, d);
+  geom_moved(g);
 }
 dReal dGeomPlanePointDepth(dGeomID g, dReal x, dReal y, dReal z) {
   const dReal p[4] = {(dReal)g->p[0], (dReal)g->p[1], (dReal)g->p[2], (dReal)g->p[3]};
@@ -1508,7 +1688,10 @@ dReal dGeomPlanePointDepth(dGeomID g, dReal x, dReal y, dReal z) {
 }
 void dGeomCapsuleGetParams(dGeomID g, dReal* r, dReal* l) { *r = (dReal)g->p[0]; *l = (dReal)g->p[1]; }
 void dGeomCapsuleSetParams(dGeomID g, dReal radius, dReal length) {
-  if (g && g->type == dCapsuleClass) { g->p[0] = radius; g->p[1] = length; }
+  if (!g || g->type != dCapsuleClass) return;
+  g->p[0] = radius; g->p[1] = length;
+  g->zero_sized = radius == 0;
+  geom_moved(g);
 }
 dReal dGeomCapsulePointDepth(dGeomID g, dReal x, dReal y, dReal z) {
   const dReal* R = geom_R(g);
@@ -1522,10 +1705,246 @@ dReal dGeomCapsulePointDepth(dGeomID g, dReal x, dReal y, dReal z) {
   return (dReal)g->p[0] - std::sqrt((x - c[0]) * (x - c[0]) + (y - c[1]) * (y - c[1]) + (z - c[2]) * (z - c[2]));
 }
 
+// ---------------------------------------------------------------- spaces (API)
+// Simple and hash spaces (collision_space.cpp:210-604) on the host: they only
+// enumerate candidate pairs for the caller's near-callback, which calls
+// dCollide. Sweep-and-prune and quadtree spaces are not built.
+static dSpaceID new_space(dSpaceID parent, int type) {
+  auto* sp = new dxSpace();
+  std::memset(static_cast<dxGeom*>(sp), 0, sizeof(dxGeom));
+  sp->first = nullptr;
+  sp->count = 0;
+  sp->cleanup = 1;
+  sp->sublevel = 0;
+  sp->manual_cleanup = 0;
+  sp->minlevel = -3;   // dxHashSpace::dxHashSpace (collision_space.cpp:385-390)
+  sp->maxlevel = 10;
+  init_geom(sp, parent, type);
+  return sp;
+}
+static bool geom_enabled(const dxGeom* g) { return g->enabled && !g->zero_sized; }   // GEOM_ENABLED
+// collideAABBs (collision_space_internal.h:48-82); every class on this path
+// keeps the default AABBTest, which always passes
+static void collide_aabbs(dxGeom* g1, dxGeom* g2, void* data, dNearCallback* cb) {
+  if (g1->body == g2->body && g1->body) return;
+  if (((g1->category_bits & g2->collide_bits) || (g2->category_bits & g1->collide_bits)) == 0) return;
+  const dReal* a = g1->aabb;
+  const dReal* b = g2->aabb;
+  if (a[0] > b[1] || a[1] < b[0] || a[2] > b[3] || a[3] < b[2] || a[4] > b[5] || a[5] < b[4]) return;
+  cb(data, g1, g2);
+}
+// cleanGeoms (collision_space.cpp:229-242, :390-402): boxes of the dirty
+// prefix, nested spaces first
+static void space_clean(dxSpace* sp) {
+  for (dxGeom* g = sp->first; g && g->dirty; g = g->next) {
+    if (is_space(g)) space_clean(static_cast<dxSpace*>(g));
+    recompute_aabb(g);
+    g->dirty = g->aabb_bad = 0;
+  }
+}
+// dxSimpleSpace::collide (collision_space.cpp:245-264): every pair in list order
+static void simple_collide(dxSpace* sp, void* data, dNearCallback* cb) {
+  space_clean(sp);
+  for (dxGeom* g1 = sp->first; g1; g1 = g1->next) {
+    if (!geom_enabled(g1)) continue;
+    for (dxGeom* g2 = g1->next; g2; g2 = g2->next)
+      if (geom_enabled(g2)) collide_aabbs(g1, g2, data, cb);
+  }
+}
+// collide2 of both space kinds (:267-283, :589-604): the geom against each member
+static void space_collide2(dxSpace* sp, void* data, dxGeom* geom, dNearCallback* cb) {
+  space_clean(sp);
+  recompute_aabb(geom);
+  for (dxGeom* g = sp->first; g; g = g->next)
+    if (geom_enabled(g)) collide_aabbs(g, geom, data, cb);
+}
+// findLevel (collision_space.cpp:325-347): the smallest cell level whose cell
+// is at least the box's largest side; boxes with an infinite side get none
+static int hash_level(const dReal* b) {
+  if (b[0] <= -INFINITY || b[1] >= INFINITY || b[2] <= -INFINITY || b[3] >= INFINITY || b[4] <= -INFINITY ||
+      b[5] >= INFINITY)
+    return INT_MAX;
+  dReal q = b[1] - b[0], q2 = b[3] - b[2];
+  if (q2 > q) q = q2;
+  q2 = b[5] - b[4];
+  if (q2 > q) q = q2;
+  int level = 0;
+  std::frexp(q, &level);
+  return level;
+}
+// getVirtualAddress (collision_space.cpp:354-357), int arithmetic widened to
+// unsigned long as there
+static unsigned long hash_cell(int level, int x, int y, int z) {
+  const int v = (int)((unsigned)level * 1000u + (unsigned)x * 100u + (unsigned)y * 10u + (unsigned)z);
+  return (unsigned long)(long)v;
+}
+// dxHashSpace::collide (collision_space.cpp:405-586): boxes binned into cells
+// of 2^level per level, cell buckets chained newest first, each pair tested
+// once through an n x n bit table, then the boxes too large for any level
+// against all the others and among themselves
+static void hash_collide(dxSpace* sp, void* data, dNearCallback* cb) {
+  static const long kPrime[31] = {1L, 2L, 3L, 7L, 13L, 31L, 61L, 127L, 251L, 509L, 1021L, 2039L, 4093L,
+                                  8191L, 16381L, 32749L, 65521L, 131071L, 262139L, 524287L, 1048573L,
+                                  2097143L, 4194301L, 8388593L, 16777213L, 33554393L, 67108859L,
+                                  134217689L, 268435399L, 536870909L, 1073741789L};   // largest prime < 2^i
+  if (sp->count < 2) return;
+  space_clean(sp);
+  struct Box { int next, level, db[6], index; dxGeom* g; };
+  std::vector<Box> box;
+  box.reserve(sp->count);
+  int first = -1, big = -1, n = 0, maxlevel = sp->minlevel - 1;
+  for (dxGeom* g = sp->first; g; g = g->next) {
+    if (!geom_enabled(g)) continue;
+    Box b{};
+    b.g = g;
+    int level = hash_level(g->aabb);
+    if (level < sp->minlevel) level = sp->minlevel;
+    const int id = (int)box.size();
+    if (level <= sp->maxlevel) {
+      b.next = first;
+      first = id;
+      b.level = level;
+      if (level > maxlevel) maxlevel = level;
+      const dReal cell = (dReal)std::ldexp(1.0, level);
+      for (int i = 0; i < 6; ++i) b.db[i] = (int)std::floor(g->aabb[i] / cell);
+      b.index = n++;
+    } else {
+      b.next = big;
+      big = id;
+    }
+    box.push_back(b);
+  }
+  const int rowsize = (n + 7) >> 3;
+  std::vector<unsigned char> tested((size_t)n * rowsize, 0);
+  int pi = 0;
+  while (pi < 31 && kPrime[pi] < 8L * n) ++pi;
+  if (pi >= 31) pi = 30;
+  const unsigned long sz = (unsigned long)kPrime[pi];
+  struct Node { int next, x, y, z, box; };
+  std::vector<int> table(sz, -1);
+  std::vector<Node> node;
+  for (int a = first; a >= 0; a = box[a].next) {
+    const Box& b = box[a];
+    for (int x = b.db[0]; x <= b.db[1]; ++x)
+      for (int y = b.db[2]; y <= b.db[3]; ++y)
+        for (int z = b.db[4]; z <= b.db[5]; ++z) {
+          const unsigned long h = hash_cell(b.level, x, y, z) % sz;
+          node.push_back({table[h], x, y, z, a});
+          table[h] = (int)node.size() - 1;
+        }
+  }
+  for (int a = first; a >= 0; a = box[a].next) {
+    int db[6];
+    for (int i = 0; i < 6; ++i) db[i] = box[a].db[i];
+    for (int level = box[a].level; level <= maxlevel; ++level) {
+      for (int x = db[0]; x <= db[1]; ++x)
+        for (int y = db[2]; y <= db[3]; ++y)
+          for (int z = db[4]; z <= db[5]; ++z) {
+            const unsigned long h = hash_cell(level, x, y, z) % sz;
+            for (int k = table[h]; k >= 0; k = node[k].next) {
+              const Node& nd = node[k];
+              if (nd.box == a) continue;
+              const Box& o = box[nd.box];
+              if (o.level != level || nd.x != x || nd.y != y || nd.z != z) continue;
+              const int ia = box[a].index, io = o.index;
+              const size_t bit = ia <= io ? (size_t)ia * rowsize + (io >> 3) : (size_t)io * rowsize + (ia >> 3);
+              const unsigned char mask = (unsigned char)(1u << ((ia <= io ? io : ia) & 7));
+              if ((tested[bit] & mask) == 0) collide_aabbs(box[a].g, o.g, data, cb);
+              tested[bit] |= mask;
+            }
+          }
+      for (int i = 0; i < 6; ++i) db[i] >>= 1;   // the cell one level up
+    }
+  }
+  for (int a = first; a >= 0; a = box[a].next)
+    for (int b = big; b >= 0; b = box[b].next) collide_aabbs(box[a].g, box[b].g, data, cb);
+  for (int a = big; a >= 0; a = box[a].next)
+    for (int b = box[a].next; b >= 0; b = box[b].next) collide_aabbs(box[a].g, box[b].g, data, cb);
+}
+static void space_collide(dxSpace* sp, void* data, dNearCallback* cb) {
+  if (sp->type == dHashSpaceClass) hash_collide(sp, data, cb);
+  else simple_collide(sp, data, cb);
+}
+
+dSpaceID dSimpleSpaceCreate(dSpaceID space) { return new_space(space, dSimpleSpaceClass); }
+dSpaceID dHashSpaceCreate(dSpaceID space) { return new_space(space, dHashSpaceClass); }
+void dHashSpaceSetLevels(dSpaceID space, int minlevel, int maxlevel) {
+  if (!space || space->type != dHashSpaceClass || minlevel > maxlevel) return;
+  space->minlevel = minlevel;
+  space->maxlevel = maxlevel;
+}
+void dHashSpaceGetLevels(dSpaceID space, int* minlevel, int* maxlevel) {
+  if (!space || space->type != dHashSpaceClass) return;
+  if (minlevel) *minlevel = space->minlevel;
+  if (maxlevel) *maxlevel = space->maxlevel;
+}
+void dSpaceDestroy(dSpaceID space) { dGeomDestroy(space); }
+void dSpaceSetCleanup(dSpaceID space, int mode) { space->cleanup = mode != 0; }
+int dSpaceGetCleanup(dSpaceID space) { return space->cleanup; }
+void dSpaceSetSublevel(dSpaceID space, int sublevel) { space->sublevel = sublevel; }
+int dSpaceGetSublevel(dSpaceID space) { return space->sublevel; }
+void dSpaceSetManualCleanup(dSpaceID space, int mode) { space->manual_cleanup = mode; }
+int dSpaceGetManualCleanup(dSpaceID space) { return space->manual_cleanup; }
+void dSpaceAdd(dSpaceID space, dGeomID g) { space_add(space, g); }
+void dSpaceRemove(dSpaceID space, dGeomID g) { space_remove(space, g); }
+int dSpaceQuery(dSpaceID space, dGeomID g) { return g && g->space == space ? 1 : 0; }
+void dSpaceClean(dSpaceID space) { space_clean(space); }
+int dSpaceGetNumGeoms(dSpaceID space) { return space->count; }
+dGeomID dSpaceGetGeom(dSpaceID space, int i) {   // dxSpace::getGeom (collision_space.cpp:131-149)
+  if (i < 0) return nullptr;
+  dxGeom* g = space->first;
+  for (int j = 0; j < i && g; ++j) g = g->next;
+  return g;
+}
+int dSpaceGetClass(dSpaceID space) { return space->type; }
+void dSpaceCollide(dSpaceID space, void* data, dNearCallback* callback) {   // collision_space.cpp:748-753
+  if (!space || !callback) return;
+  space_collide(space, data, callback);
+}
+namespace {
+struct SwapData { void* data; dNearCallback* cb; };
+void swap_callback(void* data, dGeomID g1, dGeomID g2) {   // collision_space.cpp:760-764
+  auto* d = static_cast<SwapData*>(data);
+  d->cb(d->data, g2, g1);
+}
+}  // namespace
+// dSpaceCollide2 (collision_space.cpp:767-834): a space against a geom, two
+// spaces by the smaller one's members (the deeper sublevel is taken as a
+// geom), or two geoms by their boxes alone
+void dSpaceCollide2(dGeomID g1, dGeomID g2, void* data, dNearCallback* callback) {
+  if (!g1 || !g2 || !callback) return;
+  dxSpace* s1 = is_space(g1) ? static_cast<dxSpace*>(g1) : nullptr;
+  dxSpace* s2 = is_space(g2) ? static_cast<dxSpace*>(g2) : nullptr;
+  if (s1 && s2 && s1->sublevel != s2->sublevel) {
+    if (s1->sublevel > s2->sublevel) s2 = nullptr;
+    else s1 = nullptr;
+  }
+  if (s1 && s2) {
+    if (s1 == s2) {
+      space_collide(s1, data, callback);
+    } else if (s1->count < s2->count) {
+      SwapData d{data, callback};
+      for (dxGeom* g = s1->first; g; g = g->next) space_collide2(s2, &d, g, swap_callback);
+    } else {
+      for (dxGeom* g = s2->first; g; g = g->next) space_collide2(s1, data, g, callback);
+    }
+  } else if (s1) {
+    space_collide2(s1, data, g2, callback);
+  } else if (s2) {
+    SwapData d{data, callback};
+    space_collide2(s2, &d, g1, swap_callback);
+  } else {
+    recompute_aabb(g1);
+    recompute_aabb(g2);
+    collide_aabbs(g1, g2, data, callback);
+  }
+}
+
 int dCollide(dGeomID o1, dGeomID o2, int flags, dContactGeom* contact, int skip) {
   // early-outs of ode/src/collision_kernel.cpp:292-311, then the collider on the GPU
   if (!o1 || !o2 || !contact || (flags & 0xffff) == 0) return 0;
   if (o1 == o2) return 0;
+  if (is_space(o1) || is_space(o2)) return 0;   // no collider takes a space
   if (o1->body == o2->body && o1->body) return 0;
   if (o1->type == dHeightfieldClass || o2->type == dHeightfieldClass) {
     // dCollideHeightfield runs with the field first; the reversed call
@@ -1639,9 +2058,13 @@ static int world_step(dWorldID w, dReal stepsize, bool exact) {
       }
     hw.flags[i] = b->flags;
   }
+  std::unordered_map<const dxBody*, int> body_index;
+  body_index.reserve((size_t)nb);
+  for (int i = 0; i < nb; ++i) body_index[w->bodies[i]] = i;
   auto index_of = [&](const dxBody* b) -> int {
     if (!b) return -1;
-    return (int)(std::find(w->bodies.begin(), w->bodies.end(), b) - w->bodies.begin());
+    const auto it = body_index.find(b);
+    return it == body_index.end() ? nb : it->second;
   };
   // joints: persistent first (creation order), then contacts (creation order)
   std::vector<dxJoint*> pj, cj;
@@ -1740,6 +2163,48 @@ static int world_step(dWorldID w, dReal stepsize, bool exact) {
     b->lvel[0] = hw.lvel[i].x; b->lvel[1] = hw.lvel[i].y; b->lvel[2] = hw.lvel[i].z;
     b->avel[0] = hw.avel[i].x; b->avel[1] = hw.avel[i].y; b->avel[2] = hw.avel[i].z;
     for (int k = 0; k < 4; ++k) b->facc[k] = b->tacc[k] = 0;
+  }
+  // Every stepped body notifies its geoms (dxStepBody, util.cpp:334-336),
+  // body by body in island order (quickstep.cpp:1004-1008, step.cpp:810-812),
+  // which moves them to the front of their spaces in that order. The islands
+  // are ODE's DFS (util.cpp:413-470): bodies newest first, each body's joints
+  // in list order, the bodies found pushed on a stack.
+  bool in_space = false;
+  for (dxBody* b : w->bodies)
+    for (dxGeom* g = b->geom; g && !in_space; g = g->body_next) in_space = g->space != nullptr;
+  if (!in_space) {
+    for (dxBody* b : w->bodies) body_geoms_moved(b);
+  } else {
+    const int nj = (int)(pj.size() + cj.size());
+    std::vector<int> jb(2 * (size_t)nj);
+    for (int k = 0; k < nj; ++k) {
+      const dxJoint* j = k < (int)pj.size() ? pj[k] : cj[k - pj.size()];
+      jb[2 * k] = index_of(j->body[0]);
+      jb[2 * k + 1] = index_of(j->body[1]);
+    }
+    std::vector<char> btag(nb, 0), jtag(nj, 0);
+    std::vector<int> stack;
+    for (int first = nb - 1; first >= 0; --first) {
+      if (btag[first]) continue;
+      btag[first] = 1;
+      int b = first;
+      for (;;) {
+        body_geoms_moved(w->bodies[b]);
+        for (int e = hw.padj_start[b]; e < hw.padj_start[b + 1]; ++e) {
+          const int k = hw.padj[e];
+          if (jtag[k]) continue;
+          jtag[k] = 1;
+          const int o = jb[2 * k] == b ? jb[2 * k + 1] : jb[2 * k];
+          if (o >= 0 && !btag[o]) {
+            btag[o] = 1;
+            stack.push_back(o);
+          }
+        }
+        if (stack.empty()) break;
+        b = stack.back();
+        stack.pop_back();
+      }
+    }
   }
   return hw.status == 0 ? 1 : 0;
 }

@@ -519,6 +519,21 @@ def make_tower():
     np.savez_compressed(os.path.join(HERE, "tower.npz"), **out)
 
 
+def make_space_order(seeds=range(8), n_steps=6):
+    """The reference's dSINGLE build through its public space API
+    (tests/space_program.py step_program): per step, the simple space's member
+    order and the near-callback's pairs, with the geoms of every stepped body
+    notified in island order by dWorldQuickStep and by dWorldStep."""
+    import ctypes as C
+    import space_program as SP
+    lib = SP.bind(C.CDLL(os.path.join(ROOT, "oracle", "_ref", "libode_ref_s.so")))
+    out = {"seeds": np.array(list(seeds)), "n_steps": np.int64(n_steps)}
+    for st in ("dWorldQuickStep", "dWorldStep"):
+        for s in seeds:
+            out[f"{st}_{s}"] = SP.step_program(lib, s, n_steps, st)
+    np.savez_compressed(os.path.join(HERE, "space_order.npz"), **out)
+
+
 def make_rng_kat():
     ref = O.ref("d")
     seeds = [0, 1, 12345, 0xdeadbeef, 0xffffffff]
@@ -545,6 +560,8 @@ if __name__ == "__main__":
                 make_scene(name[len("exact_"):], exact=True)
             elif name == "hf_big_kats":
                 make_hf_big_kats()
+            elif name == "space_order":
+                make_space_order()
             elif name == "single_outputs":
                 add_single_outputs("collider_kats")
                 add_single_outputs("hf_kats")
@@ -571,4 +588,5 @@ if __name__ == "__main__":
     add_single_outputs("cylinder_kats", hf_class=3)
     make_rng_kat()
     make_tower()
+    make_space_order()
     print("wrote collider_kats, rng_kat")

@@ -16,6 +16,7 @@ LIB = os.path.join(ROOT, "ode-0.12_gb300", "libodegpu.so")
 def declared(header):
     txt = open(os.path.join(ROOT, "include", header)).read()
     txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    txt = re.sub(r"typedef\s+\w+\s*\**\s*d\w+\s*\([^;]*;", "", txt)   # function types (dNearCallback)
     names = re.findall(r"\b(d[A-Z]\w+|odegpu[A-Z]\w+)\s*\(", txt)
     return sorted(set(names))
 

@@ -266,6 +266,23 @@ def test_dcollide_with_offset_geoms():
     assert hits >= 10, hits
 
 
+@pytest.mark.parametrize("stepper", ["dWorldQuickStep", "dWorldStep"])
+def test_space_order_after_steps_matches_reference(stepper):
+    """A simple space through world steps (tests/space_program.py
+    step_program): each step notifies every body's geoms in island order
+    (util.cpp:334-336 from quickstep.cpp:1004-1008 / step.cpp:810-812, islands
+    by util.cpp:413-470), which moves them to the front of the space. The space
+    order and the near-callback's pairs after every step equal the reference's
+    dSINGLE build's (tests/golden/space_order.npz), entry for entry."""
+    import space_program as SP
+    g = np.load(os.path.join(GOLDEN, "space_order.npz"))
+    L = SP.bind(C.CDLL(os.path.join(os.path.dirname(GOLDEN), "..", "ode-0.12_gb300", "libodegpu.so")))
+    for s in g["seeds"]:
+        got = SP.step_program(L, int(s), int(g["n_steps"]), stepper)
+        want = g[f"{stepper}_{s}"]
+        assert np.array_equal(got, want), (int(s), got[:40], want[:40])
+
+
 class JointFeedback(C.Structure):
     _fields_ = [("f1", C.c_float * 4), ("t1", C.c_float * 4), ("f2", C.c_float * 4), ("t2", C.c_float * 4)]
 
