@@ -135,6 +135,19 @@ void dWorldSetContactMaxCorrectingVel(dWorldID w, dReal vel);       /* :420 */
 dReal dWorldGetContactMaxCorrectingVel(dWorldID w);                 /* :427 */
 void dWorldSetContactSurfaceLayer(dWorldID w, dReal depth);         /* :440 */
 dReal dWorldGetContactSurfaceLayer(dWorldID w);                     /* :447 */
+/* Damping and the angular speed cap, applied by the step's body update on
+ * the GPU (ode/src/util.cpp:255-360) */
+dReal dWorldGetLinearDampingThreshold(dWorldID w);                  /* :635 */
+void dWorldSetLinearDampingThreshold(dWorldID w, dReal threshold);  /* :643 */
+dReal dWorldGetAngularDampingThreshold(dWorldID w);                 /* :649 */
+void dWorldSetAngularDampingThreshold(dWorldID w, dReal threshold); /* :657 */
+dReal dWorldGetLinearDamping(dWorldID w);                           /* :663 */
+void dWorldSetLinearDamping(dWorldID w, dReal scale);               /* :671 */
+dReal dWorldGetAngularDamping(dWorldID w);                          /* :677 */
+void dWorldSetAngularDamping(dWorldID w, dReal scale);              /* :685 */
+void dWorldSetDamping(dWorldID w, dReal linear_scale, dReal angular_scale);  /* :693 */
+dReal dWorldGetMaxAngularSpeed(dWorldID w);                         /* :702 */
+void dWorldSetMaxAngularSpeed(dWorldID w, dReal max_speed);         /* :710 */
 
 /* bodies: include/ode/objects.h */
 dBodyID dBodyCreate(dWorldID w);                                    /* :856 */
@@ -175,6 +188,27 @@ void dBodyVectorToWorld(dBodyID b, dReal px, dReal py, dReal pz, dVector3 result
 void dBodyVectorFromWorld(dBodyID b, dReal px, dReal py, dReal pz, dVector3 result); /* :1161 */
 void dBodySetData(dBodyID b, void* data);                           /* :873 */
 void* dBodyGetData(dBodyID b);                                      /* :880 */
+void dBodySetFiniteRotationMode(dBodyID b, int mode);               /* :1184 */
+void dBodySetFiniteRotationAxis(dBodyID b, dReal x, dReal y, dReal z);  /* :1202 */
+int dBodyGetFiniteRotationMode(dBodyID b);                          /* :1209 */
+void dBodyGetFiniteRotationAxis(dBodyID b, dVector3 result);        /* :1216 */
+/* The moved callback runs after each step for every body, in island order,
+ * once all bodies hold their new state (ODE runs it as each body is stepped). */
+void dBodySetMovedCallback(dBodyID b, void (*callback)(dBodyID));   /* :1316 */
+dGeomID dBodyGetFirstGeom(dBodyID b);                               /* :1328 */
+dGeomID dBodyGetNextGeom(dGeomID g);                                /* :1338 */
+void dBodySetDampingDefaults(dBodyID b);                            /* :1345 */
+dReal dBodyGetLinearDamping(dBodyID b);                             /* :1351 */
+void dBodySetLinearDamping(dBodyID b, dReal scale);                 /* :1361 */
+dReal dBodyGetAngularDamping(dBodyID b);                            /* :1369 */
+void dBodySetAngularDamping(dBodyID b, dReal scale);                /* :1379 */
+void dBodySetDamping(dBodyID b, dReal linear_scale, dReal angular_scale);  /* :1388 */
+dReal dBodyGetLinearDampingThreshold(dBodyID b);                    /* :1394 */
+void dBodySetLinearDampingThreshold(dBodyID b, dReal threshold);    /* :1402 */
+dReal dBodyGetAngularDampingThreshold(dBodyID b);                   /* :1408 */
+void dBodySetAngularDampingThreshold(dBodyID b, dReal threshold);   /* :1416 */
+dReal dBodyGetMaxAngularSpeed(dBodyID b);                           /* :1423 */
+void dBodySetMaxAngularSpeed(dBodyID b, dReal max_speed);           /* :1433 */
 int dBodyGetNumJoints(dBodyID b);                                   /* :1223 */
 void dBodyCopyPosition(dBodyID b, dVector3 pos);                    /* :943 */
 void dBodyCopyRotation(dBodyID b, dMatrix3 R);                      /* :961 */

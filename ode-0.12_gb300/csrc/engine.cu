@@ -242,6 +242,8 @@ struct odegpuBatch {
   DBuf<float4> pos, q, lvel, avel, facc, tacc;
   DBuf<float> mass, invMass, I, invI, invIw;
   DBuf<int> bflags;
+  DBuf<float4> bstep;          // dxStepBody options (kStepRec per body)
+  bool bstep_on = false;       // some body uses one
   DBuf<int> gtype, gbody, gsurf;
   DBuf<float4> gparam, gpos;
   DBuf<float> gbound;
@@ -323,6 +325,7 @@ struct odegpuBatch {
     d.nislands = nislands.p;
     d.pos = pos.p; d.q = q.p; d.lvel = lvel.p; d.avel = avel.p;
     d.mass = mass.p; d.invMass = invMass.p; d.I = I.p; d.invI = invI.p; d.bflags = bflags.p;
+    d.bstep = bstep_on ? bstep.p : nullptr;
     d.invIw = invIw.p; d.facc = facc.p; d.tacc = tacc.p;
     d.gtype = gtype.p; d.gbody = gbody.p; d.gparam = gparam.p; d.gbound = gbound.p; d.gpos = gpos.p;
     d.gsurf = gsurf.p; d.surfaces = surfaces.p;
@@ -1979,6 +1982,8 @@ static int ctx_upload(odegpuBatch& B, const HostWorld& hw, const WorldDesc& D) {
   rc = rc ? rc : put(B.invI, hw.invI, s);
   rc = rc ? rc : grow(B.invIw, 12 * (size_t)nb);
   rc = rc ? rc : put(B.bflags, hw.flags, s);
+  B.bstep_on = !hw.bstep.empty();
+  if (B.bstep_on) rc = rc ? rc : put(B.bstep, hw.bstep, s);
   rc = rc ? rc : put(B.joints, hw.joints, s);
   rc = rc ? rc : put(B.contacts, hw.contacts, s, (size_t)D.contact_cap);
   rc = rc ? rc : put(B.surfaces, hw.surfaces, s);

@@ -40,6 +40,7 @@ struct HostWorld {
   std::vector<float4> pos, q, lvel, avel, facc, tacc;
   std::vector<float> mass, invMass, I, invI;
   std::vector<int> flags;
+  std::vector<float4> bstep;          // dxStepBody options (kStepRec per body), empty when none used
   std::vector<DevJoint> joints;       // persistent joints with bodies attached
   std::vector<DevContact> contacts;   // contact joints, creation order
   std::vector<DevSurface> surfaces;   // one per contact

@@ -111,6 +111,13 @@ struct WorldDesc {
   long long hf_ws;              // its byte offset in BatchDev::hf_ws
 };
 
+// dxStepBody options of a body (ode/src/objects.h:38-47 flags, util.cpp:255-360):
+// record [0] = (flags as int bits, maximum angular speed, linear damping scale,
+// linear threshold squared), [1] = (angular scale, angular threshold squared,
+// finite rotation axis x, y), [2] = (axis z, 0, 0, 0)
+constexpr int kStepRec = 3;
+constexpr int kStepFiniteRot = 1, kStepFiniteAxis = 2, kStepLinDamp = 4, kStepAngDamp = 8, kStepMaxAng = 16;
+
 struct BatchDev {
   int n_worlds;
   const WorldDesc* world;
@@ -125,6 +132,9 @@ struct BatchDev {
   float *mass, *invMass;               // [nb_total]
   float *I, *invI;                     // [nb_total][9] body frame
   int* bflags;                         // [nb_total]
+  // per-body dxStepBody options, kStepRec float4 per body (kStep* above);
+  // null when no body of the batch uses one
+  const float4* bstep;
   float* invIw;                        // [nb_total][12] scratch: world-frame invI
   float4 *facc, *tacc;                 // [nb_total] scratch accumulators
 

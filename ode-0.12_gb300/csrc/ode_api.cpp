@@ -36,6 +36,13 @@ struct dxBody {
   int flags;   // ODEGPU_BODY_*
   void* data;  // dBodySetData
   dxGeom* geom;   // the body's geoms, newest attached first (dxGeom::bodyAdd)
+  // dxStepBody options (ode/src/objects.h:38-47, :118-147): og::kStep* flags,
+  // the angular speed cap, damping scales and squared thresholds, and the
+  // finite rotation axis (normalised, or zero)
+  int step_flags;
+  dReal max_angular_speed, lin_scale, lin_thr, ang_scale, ang_thr;
+  dReal frot_axis[4];
+  void (*moved_callback)(dxBody*);   // dBodySetMovedCallback
 };
 
 struct dxJoint {
@@ -128,6 +135,12 @@ struct dxWorld {
   int iterations = 20;
   double sor_w = 1.3;
   double max_vel = INFINITY, min_depth = 0;
+  // body defaults of dWorldCreate (ode/src/ode.cpp:1574-1579): no damping,
+  // thresholds 0.01 (kept squared), no angular speed cap
+  int body_step_flags = 0;
+  dReal lin_scale = 0, ang_scale = 0;
+  dReal lin_thr = (dReal)0.01 * (dReal)0.01, ang_thr = (dReal)0.01 * (dReal)0.01;
+  dReal max_angular_speed = INFINITY;
   std::vector<dxBody*> bodies;     // creation order
   std::vector<dxJoint*> joints;    // every live joint, creation order
   long long seq = 0;
@@ -288,6 +301,92 @@ dReal dWorldGetContactMaxCorrectingVel(dWorldID w) { return (dReal)w->max_vel; }
 void dWorldSetContactSurfaceLayer(dWorldID w, dReal d) { w->min_depth = d; }
 dReal dWorldGetContactSurfaceLayer(dWorldID w) { return (dReal)w->min_depth; }
 
+// Damping and the angular speed cap (ode/src/ode.cpp:1038-1118, :1930-2011):
+// a non-zero scale turns damping on, a finite cap turns the cap on, the
+// thresholds are kept squared; bodies take the world's values at creation or
+// from dBodySetDampingDefaults. dxStepBody applies them on the GPU.
+dReal dWorldGetLinearDampingThreshold(dWorldID w) { return std::sqrt(w->lin_thr); }
+void dWorldSetLinearDampingThreshold(dWorldID w, dReal t) { w->lin_thr = t * t; }
+dReal dWorldGetAngularDampingThreshold(dWorldID w) { return std::sqrt(w->ang_thr); }
+void dWorldSetAngularDampingThreshold(dWorldID w, dReal t) { w->ang_thr = t * t; }
+dReal dWorldGetLinearDamping(dWorldID w) { return w->lin_scale; }
+void dWorldSetLinearDamping(dWorldID w, dReal scale) {
+  w->body_step_flags = scale ? (w->body_step_flags | og::kStepLinDamp) : (w->body_step_flags & ~og::kStepLinDamp);
+  w->lin_scale = scale;
+}
+dReal dWorldGetAngularDamping(dWorldID w) { return w->ang_scale; }
+void dWorldSetAngularDamping(dWorldID w, dReal scale) {
+  w->body_step_flags = scale ? (w->body_step_flags | og::kStepAngDamp) : (w->body_step_flags & ~og::kStepAngDamp);
+  w->ang_scale = scale;
+}
+void dWorldSetDamping(dWorldID w, dReal linear_scale, dReal angular_scale) {
+  dWorldSetLinearDamping(w, linear_scale);
+  dWorldSetAngularDamping(w, angular_scale);
+}
+dReal dWorldGetMaxAngularSpeed(dWorldID w) { return w->max_angular_speed; }
+void dWorldSetMaxAngularSpeed(dWorldID w, dReal max_speed) {
+  w->body_step_flags = max_speed < INFINITY ? (w->body_step_flags | og::kStepMaxAng)
+                                            : (w->body_step_flags & ~og::kStepMaxAng);
+  w->max_angular_speed = max_speed;
+}
+void dBodySetDampingDefaults(dBodyID b) {
+  const dxWorld* w = b->world;
+  b->lin_scale = w->lin_scale; b->ang_scale = w->ang_scale;
+  b->lin_thr = w->lin_thr; b->ang_thr = w->ang_thr;
+  const int mask = og::kStepLinDamp | og::kStepAngDamp;
+  b->step_flags = (b->step_flags & ~mask) | (w->body_step_flags & mask);
+}
+dReal dBodyGetLinearDamping(dBodyID b) { return b->lin_scale; }
+void dBodySetLinearDamping(dBodyID b, dReal scale) {
+  b->step_flags = scale ? (b->step_flags | og::kStepLinDamp) : (b->step_flags & ~og::kStepLinDamp);
+  b->lin_scale = scale;
+}
+dReal dBodyGetAngularDamping(dBodyID b) { return b->ang_scale; }
+void dBodySetAngularDamping(dBodyID b, dReal scale) {
+  b->step_flags = scale ? (b->step_flags | og::kStepAngDamp) : (b->step_flags & ~og::kStepAngDamp);
+  b->ang_scale = scale;
+}
+void dBodySetDamping(dBodyID b, dReal linear_scale, dReal angular_scale) {
+  dBodySetLinearDamping(b, linear_scale);
+  dBodySetAngularDamping(b, angular_scale);
+}
+dReal dBodyGetLinearDampingThreshold(dBodyID b) { return std::sqrt(b->lin_thr); }
+void dBodySetLinearDampingThreshold(dBodyID b, dReal t) { b->lin_thr = t * t; }
+dReal dBodyGetAngularDampingThreshold(dBodyID b) { return std::sqrt(b->ang_thr); }
+void dBodySetAngularDampingThreshold(dBodyID b, dReal t) { b->ang_thr = t * t; }
+dReal dBodyGetMaxAngularSpeed(dBodyID b) { return b->max_angular_speed; }
+void dBodySetMaxAngularSpeed(dBodyID b, dReal max_speed) {
+  b->step_flags = max_speed < INFINITY ? (b->step_flags | og::kStepMaxAng) : (b->step_flags & ~og::kStepMaxAng);
+  b->max_angular_speed = max_speed;
+}
+// Finite rotation (ode/src/ode.cpp:767-806): the mode, and an axis that, when
+// non-zero, is normalised and limits the finite part to rotation about it
+void dBodySetFiniteRotationMode(dBodyID b, int mode) {
+  b->step_flags &= ~(og::kStepFiniteRot | og::kStepFiniteAxis);
+  if (mode) {
+    b->step_flags |= og::kStepFiniteRot;
+    if (b->frot_axis[0] != 0 || b->frot_axis[1] != 0 || b->frot_axis[2] != 0) b->step_flags |= og::kStepFiniteAxis;
+  }
+}
+void dBodySetFiniteRotationAxis(dBodyID b, dReal x, dReal y, dReal z) {
+  b->frot_axis[0] = x; b->frot_axis[1] = y; b->frot_axis[2] = z;
+  if (x != 0 || y != 0 || z != 0) {
+    dNormalize3(b->frot_axis);
+    b->step_flags |= og::kStepFiniteAxis;
+  } else {
+    b->step_flags &= ~og::kStepFiniteAxis;
+  }
+}
+int dBodyGetFiniteRotationMode(dBodyID b) { return (b->step_flags & og::kStepFiniteRot) != 0; }
+void dBodyGetFiniteRotationAxis(dBodyID b, dVector3 result) {
+  for (int k = 0; k < 3; ++k) result[k] = b->frot_axis[k];
+}
+// Called after each step for every body, in island order, once all bodies
+// have their new state (ODE calls it as each body is stepped).
+void dBodySetMovedCallback(dBodyID b, void (*callback)(dBodyID)) { b->moved_callback = callback; }
+dGeomID dBodyGetFirstGeom(dBodyID b) { return b->geom; }        // ode.cpp:1122-1133
+dGeomID dBodyGetNextGeom(dGeomID g) { return g->body_next; }
+
 // ---------------------------------------------------------------- bodies
 dBodyID dBodyCreate(dWorldID w) {
   // dBodyCreate defaults (ode/src/ode.cpp:248-294): unit mass and inertia,
@@ -302,6 +401,9 @@ dBodyID dBodyCreate(dWorldID w) {
   b->invMass = 1;
   b->flags = ODEGPU_BODY_GYROSCOPIC;
   w->bodies.push_back(b);
+  dBodySetDampingDefaults(b);   // ode.cpp:285-288
+  b->step_flags |= w->body_step_flags & og::kStepMaxAng;
+  b->max_angular_speed = w->max_angular_speed;
   return b;
 }
 void dBodyDestroy(dBodyID b) {
@@ -2058,6 +2160,25 @@ static int world_step(dWorldID w, dReal stepsize, bool exact) {
       }
     hw.flags[i] = b->flags;
   }
+  // dxStepBody options, uploaded only when some body uses one. The finite
+  // axis flag without the mode has no effect (util.cpp:272-276).
+  bool any_step = false;
+  for (const dxBody* b : w->bodies) any_step |= b->step_flags != 0;
+  hw.bstep.clear();
+  if (any_step) {
+    hw.bstep.resize((size_t)og::kStepRec * nb);
+    for (int i = 0; i < nb; ++i) {
+      const dxBody* b = w->bodies[i];
+      float4* r = &hw.bstep[(size_t)og::kStepRec * i];
+      int fl = b->step_flags;
+      if (!(fl & og::kStepFiniteRot)) fl &= ~og::kStepFiniteAxis;
+      float flf;
+      std::memcpy(&flf, &fl, sizeof(fl));
+      r[0] = make_float4(flf, b->max_angular_speed, b->lin_scale, b->lin_thr);
+      r[1] = make_float4(b->ang_scale, b->ang_thr, b->frot_axis[0], b->frot_axis[1]);
+      r[2] = make_float4(b->frot_axis[2], 0.f, 0.f, 0.f);
+    }
+  }
   std::unordered_map<const dxBody*, int> body_index;
   body_index.reserve((size_t)nb);
   for (int i = 0; i < nb; ++i) body_index[w->bodies[i]] = i;
@@ -2164,15 +2285,23 @@ static int world_step(dWorldID w, dReal stepsize, bool exact) {
     b->avel[0] = hw.avel[i].x; b->avel[1] = hw.avel[i].y; b->avel[2] = hw.avel[i].z;
     for (int k = 0; k < 4; ++k) b->facc[k] = b->tacc[k] = 0;
   }
-  // Every stepped body notifies its geoms (dxStepBody, util.cpp:334-336),
-  // body by body in island order (quickstep.cpp:1004-1008, step.cpp:810-812),
-  // which moves them to the front of their spaces in that order. The islands
+  // Every stepped body notifies its geoms and then its moved callback
+  // (dxStepBody, util.cpp:334-340), body by body in island order
+  // (quickstep.cpp:1004-1008, step.cpp:810-812), which moves the geoms to the
+  // front of their spaces in that order. The islands
   // are ODE's DFS (util.cpp:413-470): bodies newest first, each body's joints
   // in list order, the bodies found pushed on a stack.
-  bool in_space = false;
-  for (dxBody* b : w->bodies)
-    for (dxGeom* g = b->geom; g && !in_space; g = g->body_next) in_space = g->space != nullptr;
-  if (!in_space) {
+  bool in_order = false;   // geoms in a space, or a moved callback: the order is visible
+  for (dxBody* b : w->bodies) {
+    in_order |= b->moved_callback != nullptr;
+    for (dxGeom* g = b->geom; g && !in_order; g = g->body_next) in_order = g->space != nullptr;
+  }
+  auto moved = [&](int i) {
+    dxBody* b = w->bodies[i];
+    body_geoms_moved(b);
+    if (b->moved_callback) b->moved_callback(b);
+  };
+  if (!in_order) {
     for (dxBody* b : w->bodies) body_geoms_moved(b);
   } else {
     const int nj = (int)(pj.size() + cj.size());
@@ -2189,7 +2318,7 @@ static int world_step(dWorldID w, dReal stepsize, bool exact) {
       btag[first] = 1;
       int b = first;
       for (;;) {
-        body_geoms_moved(w->bodies[b]);
+        moved(b);
         for (int e = hw.padj_start[b]; e < hw.padj_start[b + 1]; ++e) {
           const int k = hw.padj[e];
           if (jtag[k]) continue;

@@ -734,23 +734,7 @@ OG_D bool integrate_exact_body(const BatchDev& d, const WorldDesc& D, int gb, co
   float r3[3];
   mul0_331(r3, d.invIw + 12 * gb, data);
   av.x += r3[0]; av.y += r3[1]; av.z += r3[2];
-  float4 p = d.pos[gb];
-  p.x += h * lv.x; p.y += h * lv.y; p.z += h * lv.z;
-  const float4 q4 = d.q[gb];
-  float q[4] = {q4.x, q4.y, q4.z, q4.w};
-  float dq[4];
-  dq[0] = 0.5f * (-av.x * q[1] - av.y * q[2] - av.z * q[3]);
-  dq[1] = 0.5f * (av.x * q[0] + av.y * q[3] - av.z * q[2]);
-  dq[2] = 0.5f * (-av.x * q[3] + av.y * q[0] + av.z * q[1]);
-  dq[3] = 0.5f * (av.x * q[2] - av.y * q[1] + av.z * q[0]);
-  for (int j = 0; j < 4; j++) q[j] += h * dq[j];
-  normalize4(q);
-  d.pos[gb] = p;
-  d.q[gb] = make_float4(q[0], q[1], q[2], q[3]);
-  d.lvel[gb] = lv;
-  d.avel[gb] = av;
-  return !(isfinite(p.x) && isfinite(p.y) && isfinite(p.z) && isfinite(lv.x) && isfinite(lv.y) &&
-           isfinite(lv.z) && isfinite(av.x) && isfinite(av.y) && isfinite(av.z));
+  return step_body(d, gb, h, lv, av);
 }
 
 OG_D float dot6(const float* u, const float* v) {

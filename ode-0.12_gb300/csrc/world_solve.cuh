@@ -366,6 +366,89 @@ OG_D void phase_feedback(const BatchDev& d, const WorldDesc& D, int w, const flo
   }
 }
 
+// sinc for the finite rotation (util.cpp:242-248): the two-term Taylor series
+// below 1e-4 (compared in double there, as here)
+OG_D float step_sinc(float x) {
+  return fabs((double)x) < 1.0e-4 ? 1.0f - x * x * 0.166666666666666666667f : sinf(x) / x;
+}
+// q += hq * dWtoDQ(w, q) (rotation.cpp dWtoDQ)
+OG_D void add_wq(float q[4], float wx, float wy, float wz, float hq) {
+  float dq[4];
+  dq[0] = 0.5f * (-wx * q[1] - wy * q[2] - wz * q[3]);
+  dq[1] = 0.5f * (wx * q[0] + wy * q[3] - wz * q[2]);
+  dq[2] = 0.5f * (-wx * q[3] + wy * q[0] + wz * q[1]);
+  dq[3] = 0.5f * (wx * q[2] - wy * q[1] + wz * q[0]);
+  for (int j = 0; j < 4; j++) q[j] += hq * dq[j];
+}
+// dxStepBody (util.cpp:255-360) after the velocity update: the angular speed
+// cap, the position, the rotation (infinitesimal, or finite about w or about
+// the body's axis, with the reference's halved h for the remainder about the
+// axis), normalisation, then the velocity damping. Writes the body back;
+// returns true when the new state is not finite.
+OG_D bool step_body(const BatchDev& d, int gb, float h, float4 lv, float4 av) {
+  const float4* bs = d.bstep ? d.bstep + (size_t)kStepRec * gb : nullptr;
+  const int fl = bs ? __float_as_int(bs[0].x) : 0;
+  if (fl & kStepMaxAng) {
+    const float mx = bs[0].y;
+    const float a2 = av.x * av.x + av.y * av.y + av.z * av.z;
+    if (a2 > mx * mx) {
+      const float c = mx / sqrtf(a2);
+      av.x *= c; av.y *= c; av.z *= c;
+    }
+  }
+  float4 p = d.pos[gb];
+  p.x += h * lv.x; p.y += h * lv.y; p.z += h * lv.z;
+  const float4 q4 = d.q[gb];
+  float q[4] = {q4.x, q4.y, q4.z, q4.w};
+  if (fl & kStepFiniteRot) {
+    float r[4], irv[3] = {0.f, 0.f, 0.f};
+    const float hh = h * 0.5f;
+    if (fl & kStepFiniteAxis) {
+      const float ax = bs[1].z, ay = bs[1].w, az = bs[2].x;
+      const float k = ax * av.x + ay * av.y + az * av.z;
+      const float frv[3] = {ax * k, ay * k, az * k};
+      irv[0] = av.x - frv[0]; irv[1] = av.y - frv[1]; irv[2] = av.z - frv[2];
+      const float theta = k * hh;
+      r[0] = cosf(theta);
+      const float sn = step_sinc(theta) * hh;
+      r[1] = frv[0] * sn; r[2] = frv[1] * sn; r[3] = frv[2] * sn;
+    } else {
+      const float wlen = sqrtf(av.x * av.x + av.y * av.y + av.z * av.z);
+      const float theta = wlen * hh;
+      r[0] = cosf(theta);
+      const float sn = step_sinc(theta) * hh;
+      r[1] = av.x * sn; r[2] = av.y * sn; r[3] = av.z * sn;
+    }
+    const float q2[4] = {r[0] * q[0] - r[1] * q[1] - r[2] * q[2] - r[3] * q[3],   // dQMultiply0
+                         r[0] * q[1] + r[1] * q[0] + r[2] * q[3] - r[3] * q[2],
+                         r[0] * q[2] + r[2] * q[0] + r[3] * q[1] - r[1] * q[3],
+                         r[0] * q[3] + r[3] * q[0] + r[1] * q[2] - r[2] * q[1]};
+    for (int j = 0; j < 4; j++) q[j] = q2[j];
+    if (fl & kStepFiniteAxis) add_wq(q, irv[0], irv[1], irv[2], hh);
+  } else {
+    add_wq(q, av.x, av.y, av.z, h);
+  }
+  normalize4(q);
+  if (fl & kStepLinDamp) {
+    if (lv.x * lv.x + lv.y * lv.y + lv.z * lv.z > bs[0].w) {
+      const float k = 1.f - bs[0].z;
+      lv.x *= k; lv.y *= k; lv.z *= k;
+    }
+  }
+  if (fl & kStepAngDamp) {
+    if (av.x * av.x + av.y * av.y + av.z * av.z > bs[1].y) {
+      const float k = 1.f - bs[1].x;
+      av.x *= k; av.y *= k; av.z *= k;
+    }
+  }
+  d.pos[gb] = p;
+  d.q[gb] = make_float4(q[0], q[1], q[2], q[3]);
+  d.lvel[gb] = lv;
+  d.avel[gb] = av;
+  return !(isfinite(p.x) && isfinite(p.y) && isfinite(p.z) && isfinite(lv.x) && isfinite(lv.y) &&
+           isfinite(lv.z) && isfinite(av.x) && isfinite(av.y) && isfinite(av.z));
+}
+
 // Phase 7 for one body (global index gb): velocity update from the
 // constraint forces cforce[6] (null: none) and the external forces, then
 // dxStepBody (quickstep.cpp:905-916, :960-975, :1001-1021; util.cpp:255-360).
@@ -389,25 +472,7 @@ OG_D bool integrate_body(const BatchDev& d, const WorldDesc& D, int gb, const fl
     mul0_331(r3, d.invIw + 12 * gb, t3);
     av.x = av.x + r3[0]; av.y = av.y + r3[1]; av.z = av.z + r3[2];
   }
-  float4 p = d.pos[gb];
-  p.x += h * lv.x; p.y += h * lv.y; p.z += h * lv.z;
-  const float4 q4 = d.q[gb];
-  float q[4] = {q4.x, q4.y, q4.z, q4.w};
-  float dq[4];
-  dq[0] = 0.5f * (-av.x * q[1] - av.y * q[2] - av.z * q[3]);
-  dq[1] = 0.5f * (av.x * q[0] + av.y * q[3] - av.z * q[2]);
-  dq[2] = 0.5f * (-av.x * q[3] + av.y * q[0] + av.z * q[1]);
-  dq[3] = 0.5f * (av.x * q[2] - av.y * q[1] + av.z * q[0]);
-  for (int j = 0; j < 4; j++) q[j] += h * dq[j];
-  normalize4(q);
-  d.pos[gb] = p;
-  d.q[gb] = make_float4(q[0], q[1], q[2], q[3]);
-  d.lvel[gb] = lv;
-  d.avel[gb] = av;
-  if (!(isfinite(p.x) && isfinite(p.y) && isfinite(p.z) && isfinite(lv.x) && isfinite(lv.y) &&
-        isfinite(lv.z) && isfinite(av.x) && isfinite(av.y) && isfinite(av.z)))
-    return true;
-  return false;
+  return step_body(d, gb, h, lv, av);
 }
 OG_D void phase_integrate(const BatchDev& d, const WorldDesc& D, int w, const float* cforce, int lane,
                           bool have_rows) {

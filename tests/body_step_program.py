@@ -1,0 +1,139 @@
+"""A seeded program over ODE's body-update options (damping, the angular speed
+cap, finite rotation with and without an axis, moved callbacks), run through
+ctypes on libodegpu or on the reference's dSINGLE build. Bodies spin and fall
+without contacts, some joined by a ball joint, so the trajectories are smooth
+and the two libraries agree to FP32 rounding. Returns the getters' answers
+and the body states after each step."""
+import ctypes as C
+
+import numpy as np
+
+F, P, I = C.c_float, C.c_void_p, C.c_int
+MOVED = C.CFUNCTYPE(None, P)
+
+
+def bind(lib):
+    for n in ("dWorldCreate", "dBodyCreate", "dJointCreateBall", "dBodyGetFirstGeom", "dBodyGetNextGeom",
+              "dCreateSphere"):
+        getattr(lib, n).restype = P
+    lib.dInitODE2.argtypes = [C.c_uint]
+    lib.dBodyCreate.argtypes = [P]
+    for n in ("dBodySetPosition", "dBodySetLinearVel", "dBodySetAngularVel", "dBodySetFiniteRotationAxis",
+              "dWorldSetGravity"):
+        getattr(lib, n).argtypes = [P, F, F, F]
+    for n in ("dWorldSetLinearDamping", "dWorldSetAngularDamping", "dWorldSetLinearDampingThreshold",
+              "dWorldSetAngularDampingThreshold", "dWorldSetMaxAngularSpeed", "dBodySetLinearDamping",
+              "dBodySetAngularDamping", "dBodySetLinearDampingThreshold", "dBodySetAngularDampingThreshold",
+              "dBodySetMaxAngularSpeed"):
+        getattr(lib, n).argtypes = [P, F]
+    lib.dWorldSetDamping.argtypes = lib.dBodySetDamping.argtypes = [P, F, F]
+    for n in ("dWorldGetLinearDamping", "dWorldGetAngularDamping", "dWorldGetLinearDampingThreshold",
+              "dWorldGetAngularDampingThreshold", "dWorldGetMaxAngularSpeed", "dBodyGetLinearDamping",
+              "dBodyGetAngularDamping", "dBodyGetLinearDampingThreshold", "dBodyGetAngularDampingThreshold",
+              "dBodyGetMaxAngularSpeed"):
+        getattr(lib, n).restype = F
+        getattr(lib, n).argtypes = [P]
+    lib.dBodySetFiniteRotationMode.argtypes = [P, I]
+    lib.dBodyGetFiniteRotationMode.argtypes = [P]
+    lib.dBodyGetFiniteRotationAxis.argtypes = [P, P]
+    lib.dBodySetDampingDefaults.argtypes = [P]
+    lib.dBodySetMovedCallback.argtypes = [P, MOVED]
+    lib.dBodyGetFirstGeom.argtypes = [P]
+    lib.dBodyGetNextGeom.argtypes = [P]
+    lib.dCreateSphere.argtypes = [P, F]
+    lib.dGeomSetBody.argtypes = [P, P]
+    lib.dBodySetMass.argtypes = [P, P]
+    lib.dMassSetBox.argtypes = [P, F, F, F, F]
+    for n in ("dBodyGetPosition", "dBodyGetQuaternion", "dBodyGetLinearVel", "dBodyGetAngularVel"):
+        getattr(lib, n).restype = C.POINTER(F)
+        getattr(lib, n).argtypes = [P]
+    lib.dJointCreateBall.argtypes = [P, P]
+    lib.dJointAttach.argtypes = [P, P, P]
+    lib.dJointSetBallAnchor.argtypes = [P, F, F, F]
+    lib.dWorldQuickStep.argtypes = lib.dWorldStep.argtypes = [P, F]
+    lib.dWorldDestroy.argtypes = [P]
+    return lib
+
+
+class Mass(C.Structure):
+    _fields_ = [("mass", F), ("c", F * 4), ("I", F * 12)]
+
+
+def state(lib, b):
+    out = []
+    for n, k in (("dBodyGetPosition", 3), ("dBodyGetQuaternion", 4), ("dBodyGetLinearVel", 3),
+                 ("dBodyGetAngularVel", 3)):
+        p = getattr(lib, n)(b)
+        out += [p[i] for i in range(k)]
+    return out
+
+
+def program(lib, seed, n_steps=30, stepper="dWorldQuickStep"):
+    """Returns (getters, states [n_steps][nb][13], moved-callback order)."""
+    rng = np.random.default_rng(seed)
+    lib.dInitODE2(0)
+    w = lib.dWorldCreate()
+    lib.dWorldSetGravity(w, 0.0, 0.0, -9.81)
+    getters = []
+    # world defaults, then the world's damping (bodies created afterwards take it)
+    getters += [lib.dWorldGetLinearDamping(w), lib.dWorldGetAngularDampingThreshold(w),
+                lib.dWorldGetMaxAngularSpeed(w)]
+    lib.dWorldSetDamping(w, 0.01, 0.02)
+    lib.dWorldSetLinearDampingThreshold(w, 0.5)
+    lib.dWorldSetAngularDampingThreshold(w, 0.25)
+    lib.dWorldSetMaxAngularSpeed(w, 12.0)
+    bodies = []
+    for k in range(8):
+        b = lib.dBodyCreate(w)
+        m = Mass()
+        lib.dMassSetBox(C.byref(m), 1.0, *(float(x) for x in rng.uniform(0.2, 1.0, 3)))
+        lib.dBodySetMass(b, C.byref(m))
+        lib.dBodySetPosition(b, float(2 * k), 0.0, 5.0)
+        lib.dBodySetLinearVel(b, *(float(x) for x in rng.normal(0, 2, 3)))
+        lib.dBodySetAngularVel(b, *(float(x) for x in rng.normal(0, 8, 3)))
+        bodies.append(b)
+    b = bodies
+    # per-body options over the world's
+    lib.dBodySetDamping(b[1], 0.0, 0.0)                 # damping off
+    lib.dBodySetLinearDamping(b[2], 0.05)
+    lib.dBodySetAngularDampingThreshold(b[2], 100.0)    # above its speed: no angular damping
+    lib.dBodySetMaxAngularSpeed(b[3], float("inf"))     # cap off
+    lib.dBodySetMaxAngularSpeed(b[4], 3.0)
+    for bb in b[5:]:                                    # fast spin, uncapped: finite rotation shows
+        lib.dBodySetMaxAngularSpeed(bb, float("inf"))
+        lib.dBodySetAngularVel(bb, *(float(x) for x in rng.normal(0, 25, 3)))
+    lib.dBodySetFiniteRotationMode(b[5], 1)             # finite about w
+    lib.dBodySetFiniteRotationAxis(b[6], 0.0, 0.0, 2.0) # axis first (normalised), then the mode
+    lib.dBodySetFiniteRotationMode(b[6], 1)
+    lib.dBodySetFiniteRotationMode(b[7], 1)
+    lib.dBodySetFiniteRotationAxis(b[7], *(float(x) for x in rng.normal(size=3)))
+    lib.dBodySetLinearDamping(b[0], 0.03)
+    lib.dBodySetDampingDefaults(b[0])                   # back to the world's
+    ax = (F * 4)()
+    for bb in b:
+        lib.dBodyGetFiniteRotationAxis(bb, ax)
+        getters += [lib.dBodyGetLinearDamping(bb), lib.dBodyGetAngularDamping(bb),
+                    lib.dBodyGetLinearDampingThreshold(bb), lib.dBodyGetAngularDampingThreshold(bb),
+                    lib.dBodyGetMaxAngularSpeed(bb), lib.dBodyGetFiniteRotationMode(bb)] + list(ax)[:3]
+    # two bodies joined by a ball joint form one island
+    j = lib.dJointCreateBall(w, None)
+    lib.dJointAttach(j, b[3], b[4])
+    lib.dJointSetBallAnchor(j, 7.0, 0.0, 5.0)
+    # body geom lists and moved callbacks
+    g1, g2 = lib.dCreateSphere(None, 0.1), lib.dCreateSphere(None, 0.2)
+    lib.dGeomSetBody(g1, b[2])
+    lib.dGeomSetBody(g2, b[2])
+    getters += [int(lib.dBodyGetFirstGeom(b[2]) == g2), int(lib.dBodyGetNextGeom(g2) == g1),
+                int(lib.dBodyGetNextGeom(g1) is None), int(lib.dBodyGetFirstGeom(b[0]) is None)]
+    ix = {bb: k for k, bb in enumerate(b)}
+    moved = []
+    cb = MOVED(lambda p: moved.append(ix.get(p, -1)))
+    for bb in b:
+        lib.dBodySetMovedCallback(bb, cb)
+    states = []
+    for _ in range(n_steps):
+        getattr(lib, stepper)(w, 0.01)
+        states.append([state(lib, bb) for bb in b])
+    lib.dWorldDestroy(w)
+    return (np.array(getters, dtype=np.float64), np.array(states, dtype=np.float64),
+            np.array(moved, dtype=np.int64))

@@ -534,6 +534,22 @@ def make_space_order(seeds=range(8), n_steps=6):
     np.savez_compressed(os.path.join(HERE, "space_order.npz"), **out)
 
 
+def make_body_step_options(seeds=(1, 2, 3), n_steps=30):
+    """The reference's dSINGLE build through its public API
+    (tests/body_step_program.py): damping, the angular speed cap and finite
+    rotation over a smooth 30-step flight, the getters, and the moved
+    callbacks' order, for dWorldQuickStep and dWorldStep."""
+    import ctypes as C
+    import body_step_program as BP
+    lib = BP.bind(C.CDLL(os.path.join(ROOT, "oracle", "_ref", "libode_ref_s.so")))
+    out = {"seeds": np.array(seeds), "n_steps": np.int64(n_steps)}
+    for st in ("dWorldQuickStep", "dWorldStep"):
+        for s in seeds:
+            g, x, m = BP.program(lib, s, n_steps, st)
+            out[f"{st}_{s}_getters"], out[f"{st}_{s}_states"], out[f"{st}_{s}_moved"] = g, x, m
+    np.savez_compressed(os.path.join(HERE, "body_step_options.npz"), **out)
+
+
 def make_rng_kat():
     ref = O.ref("d")
     seeds = [0, 1, 12345, 0xdeadbeef, 0xffffffff]
@@ -562,6 +578,8 @@ if __name__ == "__main__":
                 make_hf_big_kats()
             elif name == "space_order":
                 make_space_order()
+            elif name == "body_step_options":
+                make_body_step_options()
             elif name == "single_outputs":
                 add_single_outputs("collider_kats")
                 add_single_outputs("hf_kats")
@@ -589,4 +607,5 @@ if __name__ == "__main__":
     make_rng_kat()
     make_tower()
     make_space_order()
+    make_body_step_options()
     print("wrote collider_kats, rng_kat")

@@ -283,6 +283,29 @@ def test_space_order_after_steps_matches_reference(stepper):
         assert np.array_equal(got, want), (int(s), got[:40], want[:40])
 
 
+@pytest.mark.parametrize("stepper", ["dWorldQuickStep", "dWorldStep"])
+def test_body_step_options_match_reference(stepper):
+    """Damping, the angular speed cap and finite rotation (with and without an
+    axis) in the step's body update on the GPU (dxStepBody,
+    ode/src/util.cpp:255-360) against the reference's dSINGLE build over 30
+    steps of spinning, falling bodies (tests/body_step_program.py,
+    tests/golden/body_step_options.npz): states within 1e-4 (1 + |x|), the
+    moved callbacks in the reference's island order, the getters exact. Each
+    option changes the states by far more than the tolerance (damping by a
+    few percent of the velocities per step, the cap from 8 to 3 rad/s, finite
+    against infinitesimal rotation by about 1e-3 per step at 25 rad/s)."""
+    import body_step_program as BP
+    g = np.load(os.path.join(GOLDEN, "body_step_options.npz"))
+    L = BP.bind(C.CDLL(os.path.join(os.path.dirname(GOLDEN), "..", "ode-0.12_gb300", "libodegpu.so")))
+    for s in g["seeds"]:
+        got_g, got_x, got_m = BP.program(L, int(s), int(g["n_steps"]), stepper)
+        want_x = g[f"{stepper}_{s}_states"]
+        assert np.array_equal(got_g, g[f"{stepper}_{s}_getters"])
+        assert np.array_equal(got_m, g[f"{stepper}_{s}_moved"])
+        err = np.abs(got_x - want_x) / (1.0 + np.abs(want_x))
+        assert err.max() <= 1e-4, (int(s), float(err.max()), np.unravel_index(np.argmax(err), err.shape))
+
+
 class JointFeedback(C.Structure):
     _fields_ = [("f1", C.c_float * 4), ("t1", C.c_float * 4), ("f2", C.c_float * 4), ("t2", C.c_float * 4)]
 
