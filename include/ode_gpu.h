@@ -246,12 +246,15 @@ int dConnectingJointList(dBodyID b1, dBodyID b2, dJointID* out);         /* :294
 void dJointSetFeedback(dJointID j, dJointFeedback* f);                   /* :1770 */
 dJointFeedback* dJointGetFeedback(dJointID j);                           /* :1776 */
 void dJointSetBallAnchor(dJointID j, dReal x, dReal y, dReal z);         /* :1785 */
+void dJointSetBallAnchor2(dJointID j, dReal x, dReal y, dReal z);        /* :1791 */
 void dJointSetBallParam(dJointID j, int parameter, dReal value);         /* :1797 */
 void dJointGetBallAnchor(dJointID j, dVector3 result);                   /* :2351 */
 void dJointGetBallAnchor2(dJointID j, dVector3 result);                  /* :2363 */
 dReal dJointGetBallParam(dJointID j, int parameter);                     /* :2369 */
 void dJointSetHingeAnchor(dJointID j, dReal x, dReal y, dReal z);        /* :1803 */
 void dJointSetHingeAxis(dJointID j, dReal x, dReal y, dReal z);          /* :1811 */
+void dJointSetHingeAnchorDelta(dJointID j, dReal x, dReal y, dReal z, dReal dx, dReal dy, dReal dz);  /* :1805 */
+void dJointSetHingeAxisOffset(dJointID j, dReal x, dReal y, dReal z, dReal angle);  /* :1841 */
 void dJointGetHingeAnchor(dJointID j, dVector3 result);                  /* :2378 */
 void dJointGetHingeAnchor2(dJointID j, dVector3 result);                 /* :2388 */
 void dJointGetHingeAxis(dJointID j, dVector3 result);                    /* :2394 */
@@ -271,7 +274,10 @@ void dJointSetHinge2Param(dJointID j, int parameter, dReal value);       /* :190
 dReal dJointGetHinge2Param(dJointID j, int parameter);                   /* :2487 */
 void dJointAddHinge2Torques(dJointID j, dReal torque1, dReal torque2);   /* :1916 */
 dReal dJointGetHinge2Angle1(dJointID j);                                 /* :2493 */
+dReal dJointGetHinge2Angle1Rate(dJointID j);                             /* :2499 */
+dReal dJointGetHinge2Angle2Rate(dJointID j);                             /* :2505 */
 void dJointSetSliderAxis(dJointID j, dReal x, dReal y, dReal z);         /* :1863 */
+void dJointSetSliderAxisDelta(dJointID j, dReal x, dReal y, dReal z, dReal dx, dReal dy, dReal dz);  /* :1868 */
 void dJointSetSliderParam(dJointID j, int parameter, dReal value);       /* :1874 */
 void dJointAddSliderForce(dJointID j, dReal force);                      /* :1884 */
 dReal dJointGetSliderPosition(dJointID j);                               /* :2433 */
@@ -281,6 +287,8 @@ dReal dJointGetSliderParam(dJointID j, int parameter);                   /* :245
 void dJointSetUniversalAnchor(dJointID j, dReal x, dReal y, dReal z);    /* :1922 */
 void dJointSetUniversalAxis1(dJointID j, dReal x, dReal y, dReal z);     /* :1928 */
 void dJointSetUniversalAxis2(dJointID j, dReal x, dReal y, dReal z);     /* :1973 */
+void dJointSetUniversalAxis1Offset(dJointID j, dReal x, dReal y, dReal z, dReal offset1, dReal offset2);  /* :1966 */
+void dJointSetUniversalAxis2Offset(dJointID j, dReal x, dReal y, dReal z, dReal offset1, dReal offset2);  /* :2013 */
 void dJointSetUniversalParam(dJointID j, int parameter, dReal value);    /* :2020 */
 void dJointAddUniversalTorques(dJointID j, dReal torque1, dReal torque2);/* :2028 */
 void dJointGetUniversalAnchor(dJointID j, dVector3 result);              /* :2513 */
@@ -291,6 +299,8 @@ dReal dJointGetUniversalParam(dJointID j, int parameter);                /* :254
 void dJointGetUniversalAngles(dJointID j, dReal* angle1, dReal* angle2); /* :2560 */
 dReal dJointGetUniversalAngle1(dJointID j);                              /* :2566 */
 dReal dJointGetUniversalAngle2(dJointID j);                              /* :2572 */
+dReal dJointGetUniversalAngle1Rate(dJointID j);                          /* :2578 */
+dReal dJointGetUniversalAngle2Rate(dJointID j);                          /* :2584 */
 void dJointSetFixed(dJointID j);                                         /* :2247 */
 void dJointSetFixedParam(dJointID j, int parameter, dReal value);        /* :2254 */
 dReal dJointGetFixedParam(dJointID j, int parameter);                    /* :2934 */

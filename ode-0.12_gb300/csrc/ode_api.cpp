@@ -933,6 +933,155 @@ dReal dJointGetUniversalAngle2(dJointID j) {
   JB jb(j);
   return (dReal)(j->reverse ? -og_host::universal_angle1(j->h, jb.B) : og_host::universal_angle2(j->h, jb.B));
 }
+// Angle rates (ode/src/joints/hinge2.cpp:357-390, universal.cpp:682-726): the
+// world axis dotted with the bodies' angular velocities. The hinge2 rates read
+// the bodies as attached, without the reversal the angles apply.
+static double joint_rate(const dxJoint* j, const double* ax) {
+  const dReal* w0 = j->body[0]->avel;
+  double rate = ax[0] * w0[0] + ax[1] * w0[1] + ax[2] * w0[2];
+  if (j->body[1]) {
+    const dReal* w1 = j->body[1]->avel;
+    rate -= ax[0] * w1[0] + ax[1] * w1[1] + ax[2] * w1[2];
+  }
+  return rate;
+}
+static void body_axis(const dxBody* b, const double* axis, double* out) {   // R axis
+  double R[12];
+  for (int k = 0; k < 12; ++k) R[k] = b->R[k];
+  og_host::mul0_331(out, R, axis);
+}
+static void axis2_world(const dxJoint* j, double* out) {   // getAxis2 (joint.cpp)
+  if (j->body[1]) body_axis(j->body[1], j->h.axis2, out);
+  else for (int k = 0; k < 3; ++k) out[k] = j->h.axis2[k];
+}
+dReal dJointGetHinge2Angle1Rate(dJointID j) {
+  if (!j->body[0]) return 0;
+  double ax[3];
+  body_axis(j->body[0], j->h.axis1, ax);
+  return (dReal)joint_rate(j, ax);
+}
+dReal dJointGetHinge2Angle2Rate(dJointID j) {
+  if (!j->body[0] || !j->body[1]) return 0;
+  double ax[3];
+  body_axis(j->body[1], j->h.axis2, ax);
+  return (dReal)joint_rate(j, ax);
+}
+dReal dJointGetUniversalAngle1Rate(dJointID j) {
+  if (!j->body[0]) return 0;
+  double ax[3];
+  if (j->reverse) axis2_world(j, ax);
+  else body_axis(j->body[0], j->h.axis1, ax);
+  return (dReal)joint_rate(j, ax);
+}
+dReal dJointGetUniversalAngle2Rate(dJointID j) {
+  if (!j->body[0]) return 0;
+  double ax[3];
+  if (j->reverse) body_axis(j->body[0], j->h.axis1, ax);
+  else axis2_world(j, ax);
+  return (dReal)joint_rate(j, ax);
+}
+// dQFromAxisAndAngle (rotation.cpp:169-189) in FP64, for the setters below
+static void q_from_axis_angle(double* q, double ax, double ay, double az, double angle) {
+  double l = ax * ax + ay * ay + az * az;
+  if (l > 0) {
+    angle *= 0.5;
+    q[0] = std::cos(angle);
+    l = std::sin(angle) / std::sqrt(l);
+    q[1] = ax * l; q[2] = ay * l; q[3] = az * l;
+  } else {
+    q[0] = 1; q[1] = q[2] = q[3] = 0;
+  }
+}
+// dJointSetUniversalAxis1Offset / Axis2Offset (universal.cpp:418-556): set the
+// axis, then the relative rotations that make the current pose read the given
+// angles. As in the reference: the second offset is composed with
+// dQMultiply1, and on a reversed joint Axis2Offset's swap leaves offset2 as
+// given (offset1 = -offset2 is assigned first).
+static void universal_offset_qrels(dxJoint* j, const double* a1, const double* a2, double off1, double off2) {
+  JB jb(j);
+  double qa[4], R[12] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0}, qc[4], qo[4];
+  q_from_axis_angle(qa, a1[0], a1[1], a1[2], off1);
+  og_host::r_from_2axes(R, a1[0], a1[1], a1[2], a2[0], a2[1], a2[2]);
+  og_host::q_from_r(qc, R);
+  og_host::qmul0(qo, qa, qc);
+  og_host::qmul1(j->h.qrel, jb.B[0].q, qo);
+  q_from_axis_angle(qa, a2[0], a2[1], a2[2], off2);
+  og_host::r_from_2axes(R, a2[0], a2[1], a2[2], a1[0], a1[1], a1[2]);
+  og_host::q_from_r(qc, R);
+  og_host::qmul1(qo, qa, qc);
+  if (j->body[1]) og_host::qmul1(j->h.qrel2, jb.B[1].q, qo);
+  else for (int k = 0; k < 4; ++k) j->h.qrel2[k] = qc[k];
+}
+void dJointSetUniversalAxis1Offset(dJointID j, dReal x, dReal y, dReal z, dReal offset1, dReal offset2) {
+  JB jb(j);
+  if (j->reverse) {
+    og_host::set_axes(j->h, jb.B, x, y, z, nullptr, j->h.axis2);
+    offset1 = -offset1;
+    offset2 = -offset2;
+  } else {
+    og_host::set_axes(j->h, jb.B, x, y, z, j->h.axis1, nullptr);
+  }
+  og_host::universal_qrels(j->h, jb.B);
+  if (!j->body[0]) return;
+  double ax2[3];
+  axis2_world(j, ax2);
+  const double a1[3] = {x, y, z};
+  universal_offset_qrels(j, a1, ax2, offset1, offset2);
+}
+void dJointSetUniversalAxis2Offset(dJointID j, dReal x, dReal y, dReal z, dReal offset1, dReal offset2) {
+  JB jb(j);
+  if (j->reverse) {
+    og_host::set_axes(j->h, jb.B, x, y, z, j->h.axis1, nullptr);
+    offset1 = -offset2;
+    offset2 = -offset1;
+  } else {
+    og_host::set_axes(j->h, jb.B, x, y, z, nullptr, j->h.axis2);
+  }
+  og_host::universal_qrels(j->h, jb.B);
+  if (!j->body[0]) return;
+  double ax1[3], ax2[3];
+  og_host::universal_axes(j->h, jb.B, ax1, ax2);
+  universal_offset_qrels(j, ax1, ax2, offset1, offset2);
+}
+// dJointSetBallAnchor2 (ball.cpp:79-88): body 2's anchor as given, untransformed
+void dJointSetBallAnchor2(dJointID j, dReal x, dReal y, dReal z) {
+  j->h.anchor2[0] = x; j->h.anchor2[1] = y; j->h.anchor2[2] = z; j->h.anchor2[3] = 0;
+}
+// dJointSetHingeAnchorDelta (hinge.cpp:163-199): as dJointSetHingeAnchor, but
+// a hinge to the environment keeps anchor + delta as its fixed point
+void dJointSetHingeAnchorDelta(dJointID j, dReal x, dReal y, dReal z, dReal dx, dReal dy, dReal dz) {
+  JB jb(j);
+  og_host::set_anchors(j->h, jb.B, x, y, z, j->h.anchor1, j->h.anchor2);
+  if (j->body[0] && !j->body[1]) {
+    const dReal p[3] = {x + dx, y + dy, z + dz};
+    for (int k = 0; k < 3; ++k) j->h.anchor2[k] = p[k];
+  }
+  j->h.anchor1[3] = j->h.anchor2[3] = 0;
+  og_host::hinge_qrel(j->h, jb.B);
+}
+// dJointSetHingeAxisOffset (hinge.cpp:213-230): the axis, then the relative
+// rotation turned so that the current pose reads the given angle
+void dJointSetHingeAxisOffset(dJointID j, dReal x, dReal y, dReal z, dReal dangle) {
+  JB jb(j);
+  og_host::set_axes(j->h, jb.B, x, y, z, j->h.axis1, j->h.axis2);
+  og_host::hinge_qrel(j->h, jb.B);
+  if (j->reverse) dangle = -dangle;
+  double qa[4], qo[4];
+  q_from_axis_angle(qa, x, y, z, dangle);
+  og_host::qmul3(qo, qa, j->h.qrel);
+  for (int k = 0; k < 4; ++k) j->h.qrel[k] = qo[k];
+}
+// dJointSetSliderAxisDelta (slider.cpp:243-262): as dJointSetSliderAxis, with
+// a slider to the environment moving its reference point by the delta
+void dJointSetSliderAxisDelta(dJointID j, dReal x, dReal y, dReal z, dReal dx, dReal dy, dReal dz) {
+  JB jb(j);
+  og_host::set_axes(j->h, jb.B, x, y, z, j->h.axis1, nullptr);
+  og_host::slider_offset(j->h, jb.B);
+  if (!j->body[1]) {
+    j->h.offset[0] += dx; j->h.offset[1] += dy; j->h.offset[2] += dz;
+  }
+  og_host::initial_qrel(j->h, jb.B);
+}
 void dJointAddUniversalTorques(dJointID j, dReal t1, dReal t2) {
   // :729-754
   if (j->reverse) { const dReal tmp = t1; t1 = -t2; t2 = -tmp; }
