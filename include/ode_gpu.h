@@ -24,6 +24,8 @@
 #ifndef ODE_GPU_H
 #define ODE_GPU_H
 
+#include <stddef.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -112,6 +114,29 @@ enum {
 void dInitODE(void);
 int dInitODE2(unsigned int uiInitFlags);
 void dCloseODE(void);
+/* include/ode/odeinit.h:177-204 and objects.h:157-289: per-thread data and
+ * step working memory are the GPU path's own, so these accept and return 1 */
+int dAllocateODEDataForThread(unsigned int uiAllocateFlags);             /* odeinit.h:177 */
+void dCleanupODEAllDataForThread(void);                                  /* odeinit.h:204 */
+typedef struct {
+  unsigned struct_size;
+  float reserve_factor;
+  unsigned reserve_minimum;
+} dWorldStepReserveInfo;                                                 /* objects.h:201-207 */
+typedef struct {
+  unsigned struct_size;
+  void* (*alloc_block)(size_t block_size);
+  void* (*shrink_block)(void* block_pointer, size_t block_current_size, size_t block_smaller_size);
+  void (*free_block)(void* block_pointer, size_t block_current_size);
+} dWorldStepMemoryFunctionsInfo;                                         /* objects.h:256-263 */
+#define dWORLDSTEP_RESERVEFACTOR_DEFAULT 1.2f
+#define dWORLDSTEP_RESERVESIZE_DEFAULT 65536U
+int dWorldUseSharedWorkingMemory(dWorldID w, dWorldID from_world);      /* objects.h:157 */
+void dWorldCleanupWorkingMemory(dWorldID w);                             /* objects.h:180 */
+int dWorldSetStepMemoryReservationPolicy(dWorldID w, const dWorldStepReserveInfo* policyinfo);  /* objects.h:234 */
+int dWorldSetStepMemoryManager(dWorldID w, const dWorldStepMemoryFunctionsInfo* memfuncs);       /* objects.h:289 */
+const char* dGetConfiguration(void);                                     /* common.h:404 */
+int dCheckConfiguration(const char* token);                              /* common.h:414 */
 
 /* world: include/ode/objects.h */
 dWorldID dWorldCreate(void);                                        /* :54  */
@@ -411,6 +436,12 @@ void dGeomHeightfieldDataBuildShort(dHeightfieldDataID d, const short* pHeightDa
                                     dReal width, dReal depth, int widthSamples, int depthSamples,
                                     dReal scale, dReal offset, dReal thickness, int bWrap);  /* :1311 */
 void dGeomHeightfieldDataSetBounds(dHeightfieldDataID d, dReal minHeight, dReal maxHeight);  /* :1433 */
+typedef dReal dHeightfieldGetHeight(void* p_user_data, int x, int z);  /* collision.h:1121 */
+void dGeomHeightfieldDataBuildCallback(dHeightfieldDataID d, void* pUserData, dHeightfieldGetHeight* pCallback,
+                                       dReal width, dReal depth, int widthSamples, int depthSamples,
+                                       dReal scale, dReal offset, dReal thickness, int bWrap);  /* :1215 */
+void dGeomHeightfieldSetHeightfieldData(dGeomID g, dHeightfieldDataID d);   /* :1447 */
+dHeightfieldDataID dGeomHeightfieldGetHeightfieldData(dGeomID g);          /* :1459 */
 void dGeomHeightfieldDataBuildDouble(dHeightfieldDataID d, const double* pHeightData, int bCopyHeightData,
                                      dReal width, dReal depth, int widthSamples, int depthSamples,
                                      dReal scale, dReal offset, dReal thickness, int bWrap);  /* :1411 */

@@ -271,6 +271,34 @@ extern "C" {
 void dInitODE(void) {}
 int dInitODE2(unsigned int) { return 1; }
 void dCloseODE(void) {}
+// Per-thread data and step working memory (odeinit.cpp:515-530,
+// objects.h:157-289): the GPU path keeps its own device buffers per world, so
+// these accept their arguments and have nothing to do.
+int dAllocateODEDataForThread(unsigned int) { return 1; }
+void dCleanupODEAllDataForThread(void) {}
+int dWorldUseSharedWorkingMemory(dWorldID w, dWorldID) { return w ? 1 : 0; }
+void dWorldCleanupWorkingMemory(dWorldID) {}
+int dWorldSetStepMemoryReservationPolicy(dWorldID w, const dWorldStepReserveInfo* info) {
+  if (!w) return 0;
+  return !info || (info->struct_size >= sizeof(*info) && info->reserve_factor >= 1.0f) ? 1 : 0;
+}
+int dWorldSetStepMemoryManager(dWorldID w, const dWorldStepMemoryFunctionsInfo* mem) {
+  if (!w) return 0;
+  return !mem || mem->struct_size >= sizeof(*mem) ? 1 : 0;
+}
+// dGetConfiguration / dCheckConfiguration (ode.cpp:2176-2275): the tokens of a
+// single-precision build without debug checks or trimesh; a token matches
+// whole words only, and an empty or spaced token is reported present
+const char* dGetConfiguration(void) { return "ODE ODE_EXT_no_debug ODE_single_precision"; }
+int dCheckConfiguration(const char* extension) {
+  if (!extension || *extension == '\0' || std::strchr(extension, ' ')) return 1;
+  const std::string cfg = dGetConfiguration(), tok = extension;
+  for (size_t at = cfg.find(tok); at != std::string::npos; at = cfg.find(tok, at + tok.size())) {
+    const size_t end = at + tok.size();
+    if ((at == 0 || cfg[at - 1] == ' ') && (end == cfg.size() || cfg[end] == ' ')) return 1;
+  }
+  return 0;
+}
 
 // ---------------------------------------------------------------- world
 dWorldID dWorldCreate(void) { return new dxWorld(); }
@@ -1475,6 +1503,21 @@ void dGeomHeightfieldDataBuildByte(dHeightfieldDataID d, const unsigned char* pH
   hf_bounds(d);
   d->built = og::upload_heights(d->heights, &d->d_heights) == 0;
 }
+// dGeomHeightfieldDataBuildCallback (heightfield.cpp:676-697): the callback
+// is sampled here once for every sample and the field is then used like a
+// built one (ODE calls it for the cells each collision touches, so a callback
+// whose answers change later is not followed). Its bounds are infinite until
+// dGeomHeightfieldDataSetBounds.
+void dGeomHeightfieldDataBuildCallback(dHeightfieldDataID d, void* pUserData, dHeightfieldGetHeight* pCallback,
+                                       dReal width, dReal depth, int widthSamples, int depthSamples, dReal scale,
+                                       dReal offset, dReal thickness, int bWrap) {
+  if (!pCallback || !hf_shape(d, width, depth, widthSamples, depthSamples, scale, offset, thickness, bWrap)) return;
+  for (int z = 0; z < depthSamples; ++z)
+    for (int x = 0; x < widthSamples; ++x) d->heights[(size_t)z * widthSamples + x] = pCallback(pUserData, x, z);
+  d->hmin = -INFINITY;
+  d->hmax = INFINITY;
+  d->built = og::upload_heights(d->heights, &d->d_heights) == 0;
+}
 void dGeomHeightfieldDataBuildShort(dHeightfieldDataID d, const short* pHeightData, int, dReal width, dReal depth,
                                     int widthSamples, int depthSamples, dReal scale, dReal offset, dReal thickness,
                                     int bWrap) {
@@ -1493,6 +1536,10 @@ void dGeomHeightfieldDataSetBounds(dHeightfieldDataID d, dReal minHeight, dReal 
   d->hmin = minHeight * sc + of - th;
   d->hmax = maxHeight * sc + of;
 }
+// As in ODE 0.12 (heightfield.cpp:869-880), the setter stores the handle as
+// the geom's user data and leaves the field it collides with unchanged.
+void dGeomHeightfieldSetHeightfieldData(dGeomID g, dHeightfieldDataID d) { g->data = d; }
+dHeightfieldDataID dGeomHeightfieldGetHeightfieldData(dGeomID g) { return g->hf; }
 dGeomID dCreateHeightfield(dSpaceID s, dHeightfieldDataID data, int bPlaceable) {
   const double p[4] = {0, 0, 0, 0};
   dGeomID g = new_geom(s, dHeightfieldClass, p);

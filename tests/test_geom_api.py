@@ -309,3 +309,85 @@ def test_heightfield_bounds_match_reference_fp32(wrap):
         heights = rng.normal(size=(5, 7)) * 2.0
         x, y = _heightfield_sequence(ours, a, heights, wrap), _heightfield_sequence(ref, a, heights, wrap)
         _close(x, y, 2e-6)
+
+
+def test_heightfield_callback_bounds_and_data_handles_match_reference():
+    """dGeomHeightfieldDataBuildCallback (heightfield.cpp:676-697): infinite
+    vertical bounds until dGeomHeightfieldDataSetBounds, and ODE 0.12's
+    dGeomHeightfieldSetHeightfieldData, which stores the handle as the geom's
+    user data (:869-880); the callback is asked for every sample here."""
+    ours, ref = _libs()
+    HCB = C.CFUNCTYPE(F, P, I, I)
+    calls = []
+
+    def height(_, x, z):
+        calls.append((x, z))
+        return F(0.25 * x - 0.5 * z + 0.125 * x * z).value
+
+    cb = HCB(height)
+    outs = []
+    for lib in (ours, ref):
+        lib.dGeomHeightfieldDataBuildCallback.argtypes = [P, P, HCB, F, F, I, I, F, F, F, I]
+        lib.dGeomHeightfieldSetHeightfieldData.argtypes = [P, P]
+        lib.dGeomHeightfieldGetHeightfieldData.restype = P
+        lib.dGeomHeightfieldGetHeightfieldData.argtypes = [P]
+        lib.dGeomGetData.restype = P
+        lib.dGeomGetData.argtypes = [P]
+        out = []
+        for wrap in (0, 1):
+            d = lib.dGeomHeightfieldDataCreate()
+            lib.dGeomHeightfieldDataBuildCallback(d, None, cb, 6.0, 4.0, 7, 5, 1.5, -0.25, 0.5, wrap)
+            g = lib.dCreateHeightfield(None, d, 0)
+            out += _aabb(lib, g)
+            lib.dGeomHeightfieldDataSetBounds(d, -1.0, 2.0)
+            g2 = lib.dCreateHeightfield(None, d, 0)
+            out += _aabb(lib, g2)
+            d2 = lib.dGeomHeightfieldDataCreate()
+            lib.dGeomHeightfieldSetHeightfieldData(g2, d2)
+            out += [float(lib.dGeomHeightfieldGetHeightfieldData(g2) == d), float(lib.dGeomGetData(g2) == d2)]
+            for h in (g, g2):
+                lib.dGeomDestroy(h)
+            lib.dGeomHeightfieldDataDestroy(d)
+            lib.dGeomHeightfieldDataDestroy(d2)
+        outs.append(np.array(out, dtype=np.float32))
+    assert np.array_equal(outs[0], outs[1]), outs
+    assert (6, 4) in calls   # every sample was read here
+
+
+def test_configuration_and_working_memory_calls():
+    """dCheckConfiguration's whole-token match (ode.cpp:2241-2275) agrees with
+    the reference on tokens both builds share, and the working-memory calls
+    accept what the reference accepts (objects.h:157-289)."""
+    ours, ref = _libs()
+    tokens = [b"ODE", b"ODE_single_precision", b"ODE_single", b"single_precision", b"ODE_double_precision",
+              b"", b"a b", b"ODE_EXT_trimesh", b"ODE_EXT_opcode"]
+    for lib in (ours, ref):
+        lib.dCheckConfiguration.argtypes = [C.c_char_p]
+        lib.dGetConfiguration.restype = C.c_char_p
+    for t in tokens:
+        assert ours.dCheckConfiguration(t) == ref.dCheckConfiguration(t), t
+    assert b"ODE_single_precision" in ours.dGetConfiguration()
+
+    class Reserve(C.Structure):
+        _fields_ = [("struct_size", C.c_uint), ("reserve_factor", F), ("reserve_minimum", C.c_uint)]
+
+    for lib in (ours, ref):
+        lib.dWorldSetStepMemoryReservationPolicy.argtypes = [P, P]
+        lib.dWorldUseSharedWorkingMemory.argtypes = [P, P]
+        lib.dWorldCleanupWorkingMemory.argtypes = [P]
+        lib.dAllocateODEDataForThread.argtypes = [C.c_uint]
+        lib.dWorldCreate.restype = P
+        lib.dWorldDestroy.argtypes = [P]
+    got = []
+    for lib in (ours, ref):
+        lib.dInitODE2(0)
+        w = lib.dWorldCreate()
+        good, bad = Reserve(C.sizeof(Reserve), 1.5, 4096), Reserve(C.sizeof(Reserve), 0.5, 4096)
+        got.append([lib.dWorldSetStepMemoryReservationPolicy(w, C.byref(good)),
+                    lib.dWorldSetStepMemoryReservationPolicy(w, None), lib.dAllocateODEDataForThread(0xffffffff)])
+        lib.dWorldCleanupWorkingMemory(w)
+        lib.dWorldDestroy(w)
+    assert got[0] == got[1] == [1, 1, 1], got
+    w = ours.dWorldCreate()
+    assert ours.dWorldSetStepMemoryReservationPolicy(w, C.byref(bad)) == 0
+    ours.dWorldDestroy(w)

@@ -375,8 +375,10 @@ def test_joint_feedback_through_ode_api(stepper):
 
 
 @pytest.mark.parametrize("fixture", ["hf_kats", "hf_big_kats"])
-def test_dcollide_heightfield_through_ode_api(fixture):
-    """dGeomHeightfieldDataBuildDouble + dCreateHeightfield (placeable) +
+@pytest.mark.parametrize("build", ["double", "callback"])
+def test_dcollide_heightfield_through_ode_api(fixture, build):
+    """dGeomHeightfieldDataBuildDouble (or BuildCallback over the same
+    samples) + dCreateHeightfield (placeable) +
     dCollide on the reference's golden heightfield calls, in both argument
     orders (the reversed call negates the normals): counts exact, records
     within 1e-4 (of the coordinates' scale, ~12 m, for hf_big_kats, whose
@@ -394,8 +396,15 @@ def test_dcollide_heightfield_through_ode_api(fixture):
     sp = float(g["spacing"])
     nz, nx = h.shape
     hd = L.dGeomHeightfieldDataCreate()
-    L.dGeomHeightfieldDataBuildDouble(hd, h.ctypes.data_as(C.POINTER(C.c_double)), 1, sp * (nx - 1),
-                                      sp * (nz - 1), nx, nz, 1.0, 0.0, 1.0, 0)
+    # the same samples through dGeomHeightfieldDataBuildCallback (sampled at build)
+    HCB = C.CFUNCTYPE(f, v, i, i)
+    cb = HCB(lambda _, x, z: float(h[z, x]))
+    if build == "double":
+        L.dGeomHeightfieldDataBuildDouble(hd, h.ctypes.data_as(C.POINTER(C.c_double)), 1, sp * (nx - 1),
+                                          sp * (nz - 1), nx, nz, 1.0, 0.0, 1.0, 0)
+    else:
+        L.dGeomHeightfieldDataBuildCallback.argtypes = [v, v, HCB, f, f, i, i, f, f, f, i]
+        L.dGeomHeightfieldDataBuildCallback(hd, None, cb, sp * (nx - 1), sp * (nz - 1), nx, nz, 1.0, 0.0, 1.0, 0)
     hg = L.dCreateHeightfield(None, hd, 1)
     L.dGeomSetPosition(hg, *[float(x) for x in g["hf_pos"]])
     Rh = g["hf_R"]
