@@ -213,6 +213,13 @@ void dBodyVectorToWorld(dBodyID b, dReal px, dReal py, dReal pz, dVector3 result
 void dBodyVectorFromWorld(dBodyID b, dReal px, dReal py, dReal pz, dVector3 result); /* :1161 */
 void dBodySetData(dBodyID b, void* data);                           /* :873 */
 void* dBodyGetData(dBodyID b);                                      /* :880 */
+/* Manual enabling only: automatic disabling is not built. A step moves the
+ * enabled bodies and those an enabled joint connects to them (enabling them,
+ * as ODE's island walk does); other disabled bodies keep their state and
+ * their accumulated forces. */
+void dBodyEnable(dBodyID b);                                        /* :1269 */
+void dBodyDisable(dBodyID b);                                       /* :1278 */
+int dBodyIsEnabled(dBodyID b);                                      /* :1285 */
 void dBodySetFiniteRotationMode(dBodyID b, int mode);               /* :1184 */
 void dBodySetFiniteRotationAxis(dBodyID b, dReal x, dReal y, dReal z);  /* :1202 */
 int dBodyGetFiniteRotationMode(dBodyID b);                          /* :1209 */
@@ -253,6 +260,7 @@ dJointID dJointCreateHinge2(dWorldID w, dJointGroupID g);                /* :157
 dJointID dJointCreateSlider(dWorldID w, dJointGroupID g);                /* :1554 */
 dJointID dJointCreateUniversal(dWorldID w, dJointGroupID g);             /* :1578 */
 dJointID dJointCreateFixed(dWorldID w, dJointGroupID g);                 /* :1611 */
+dJointID dJointCreateNull(dWorldID w, dJointGroupID g);                  /* :1613 */
 void dJointDestroy(dJointID j);                                          /* :1647 */
 void dJointSetData(dJointID j, void* data);                              /* :1722 */
 void* dJointGetData(dJointID j);                                         /* :1728 */

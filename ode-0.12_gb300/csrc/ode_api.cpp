@@ -43,6 +43,7 @@ struct dxBody {
   dReal max_angular_speed, lin_scale, lin_thr, ang_scale, ang_thr;
   dReal frot_axis[4];
   void (*moved_callback)(dxBody*);   // dBodySetMovedCallback
+  int disabled;                      // dBodyDisable (no auto-disable on this path)
 };
 
 struct dxJoint {
@@ -412,6 +413,12 @@ void dBodyGetFiniteRotationAxis(dBodyID b, dVector3 result) {
 // Called after each step for every body, in island order, once all bodies
 // have their new state (ODE calls it as each body is stepped).
 void dBodySetMovedCallback(dBodyID b, void (*callback)(dBodyID)) { b->moved_callback = callback; }
+// dBodyEnable / Disable / IsEnabled (ode.cpp:854-875); automatic disabling
+// is not built, so a body only changes state here or when a step's island
+// walk reaches it
+void dBodyEnable(dBodyID b) { b->disabled = 0; }
+void dBodyDisable(dBodyID b) { b->disabled = 1; }
+int dBodyIsEnabled(dBodyID b) { return b->disabled ? 0 : 1; }
 dGeomID dBodyGetFirstGeom(dBodyID b) { return b->geom; }        // ode.cpp:1122-1133
 dGeomID dBodyGetNextGeom(dGeomID g) { return g->body_next; }
 
@@ -593,6 +600,9 @@ dJointID dJointCreateSlider(dWorldID w, dJointGroupID g) { return new_joint(w, g
 dJointID dJointCreateUniversal(dWorldID w, dJointGroupID g) { return new_joint(w, g, dJointTypeUniversal); }
 dJointID dJointCreateFixed(dWorldID w, dJointGroupID g) { return new_joint(w, g, dJointTypeFixed); }
 dJointID dJointCreateAMotor(dWorldID w, dJointGroupID g) { return new_joint(w, g, dJointTypeAMotor); }
+// dJointCreateNull (ode.cpp:1250-1254, joints/null.cpp): no rows, but it joins
+// its bodies into one island like any joint
+dJointID dJointCreateNull(dWorldID w, dJointGroupID g) { return new_joint(w, g, dJointTypeNull); }
 dJointID dJointCreateContact(dWorldID w, dJointGroupID g, const dContact* c) {
   dxJoint* j = new_joint(w, g, dJointTypeContact);
   j->contact = *c;   // dJointCreateContact copies the contact (ode/src/ode.cpp:1201-1208)
@@ -2332,7 +2342,37 @@ static int world_step(dWorldID w, dReal stepsize, bool exact) {
     if (!w->ctx) return 0;
   }
   og::HostWorld& hw = w->hw;
-  const int nb = (int)w->bodies.size();
+  // The bodies this step moves (util.cpp:413-470): every enabled body and
+  // whatever an enabled joint connects to one, which the island walk enables
+  // again; a disabled body reached by none stays as it is, forces included.
+  std::vector<dxBody*> sb;
+  {
+    std::unordered_map<const dxBody*, std::vector<dxBody*>> nbr;
+    for (const dxJoint* j : w->joints)
+      if (j->body[0] && j->body[1] && !j->disabled) {
+        nbr[j->body[0]].push_back(j->body[1]);
+        nbr[j->body[1]].push_back(j->body[0]);
+      }
+    std::unordered_map<const dxBody*, char> reached;
+    std::vector<dxBody*> stack;
+    for (dxBody* b : w->bodies)
+      if (!b->disabled && !reached[b]) {
+        reached[b] = 1;
+        stack.push_back(b);
+        while (!stack.empty()) {
+          dxBody* c = stack.back();
+          stack.pop_back();
+          c->disabled = 0;
+          const auto it = nbr.find(c);
+          if (it == nbr.end()) continue;
+          for (dxBody* o : it->second)
+            if (!reached[o]) { reached[o] = 1; stack.push_back(o); }
+        }
+      }
+    for (dxBody* b : w->bodies)
+      if (!b->disabled) sb.push_back(b);
+  }
+  const int nb = (int)sb.size();
   if (nb == 0) return 1;
   if (nb > ODEGPU_MAX_BODIES_LARGE) return 0;
   hw.pos.resize(nb); hw.q.resize(nb); hw.lvel.resize(nb); hw.avel.resize(nb);
@@ -2340,7 +2380,7 @@ static int world_step(dWorldID w, dReal stepsize, bool exact) {
   hw.mass.resize(nb); hw.invMass.resize(nb); hw.I.resize(9 * (size_t)nb); hw.invI.resize(9 * (size_t)nb);
   hw.flags.resize(nb);
   for (int i = 0; i < nb; ++i) {
-    dxBody* b = w->bodies[i];
+    dxBody* b = sb[i];
     hw.pos[i] = make_float4(b->pos[0], b->pos[1], b->pos[2], 0.f);
     hw.q[i] = make_float4(b->q[0], b->q[1], b->q[2], b->q[3]);
     hw.lvel[i] = make_float4(b->lvel[0], b->lvel[1], b->lvel[2], 0.f);
@@ -2359,12 +2399,12 @@ static int world_step(dWorldID w, dReal stepsize, bool exact) {
   // dxStepBody options, uploaded only when some body uses one. The finite
   // axis flag without the mode has no effect (util.cpp:272-276).
   bool any_step = false;
-  for (const dxBody* b : w->bodies) any_step |= b->step_flags != 0;
+  for (const dxBody* b : sb) any_step |= b->step_flags != 0;
   hw.bstep.clear();
   if (any_step) {
     hw.bstep.resize((size_t)og::kStepRec * nb);
     for (int i = 0; i < nb; ++i) {
-      const dxBody* b = w->bodies[i];
+      const dxBody* b = sb[i];
       float4* r = &hw.bstep[(size_t)og::kStepRec * i];
       int fl = b->step_flags;
       if (!(fl & og::kStepFiniteRot)) fl &= ~og::kStepFiniteAxis;
@@ -2377,7 +2417,7 @@ static int world_step(dWorldID w, dReal stepsize, bool exact) {
   }
   std::unordered_map<const dxBody*, int> body_index;
   body_index.reserve((size_t)nb);
-  for (int i = 0; i < nb; ++i) body_index[w->bodies[i]] = i;
+  for (int i = 0; i < nb; ++i) body_index[sb[i]] = i;
   auto index_of = [&](const dxBody* b) -> int {
     if (!b) return -1;
     const auto it = body_index.find(b);
@@ -2388,7 +2428,7 @@ static int world_step(dWorldID w, dReal stepsize, bool exact) {
   for (dxJoint* j : w->joints) {
     // unattached and disabled joints take no part (util.cpp:435-467, 500-510):
     // they neither join islands nor add rows
-    if (!j->body[0] || j->disabled) continue;
+    if (!j->body[0] || j->disabled || j->body[0]->disabled) continue;
     (j->type == dJointTypeContact ? cj : pj).push_back(j);
   }
   hw.joints.resize(pj.size());
@@ -2473,7 +2513,7 @@ static int world_step(dWorldID w, dReal stepsize, bool exact) {
     for (size_t k = 0; k < cj.size(); ++k) fill(cj[k], hw.contact_feedback.data() + 12 * k);
   }
   for (int i = 0; i < nb; ++i) {
-    dxBody* b = w->bodies[i];
+    dxBody* b = sb[i];
     b->pos[0] = hw.pos[i].x; b->pos[1] = hw.pos[i].y; b->pos[2] = hw.pos[i].z;
     b->q[0] = hw.q[i].x; b->q[1] = hw.q[i].y; b->q[2] = hw.q[i].z; b->q[3] = hw.q[i].w;
     body_sync_R(b);
@@ -2488,17 +2528,17 @@ static int world_step(dWorldID w, dReal stepsize, bool exact) {
   // are ODE's DFS (util.cpp:413-470): bodies newest first, each body's joints
   // in list order, the bodies found pushed on a stack.
   bool in_order = false;   // geoms in a space, or a moved callback: the order is visible
-  for (dxBody* b : w->bodies) {
+  for (dxBody* b : sb) {
     in_order |= b->moved_callback != nullptr;
     for (dxGeom* g = b->geom; g && !in_order; g = g->body_next) in_order = g->space != nullptr;
   }
   auto moved = [&](int i) {
-    dxBody* b = w->bodies[i];
+    dxBody* b = sb[i];
     body_geoms_moved(b);
     if (b->moved_callback) b->moved_callback(b);
   };
   if (!in_order) {
-    for (dxBody* b : w->bodies) body_geoms_moved(b);
+    for (dxBody* b : sb) body_geoms_moved(b);
   } else {
     const int nj = (int)(pj.size() + cj.size());
     std::vector<int> jb(2 * (size_t)nj);

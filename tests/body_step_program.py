@@ -137,3 +137,98 @@ def program(lib, seed, n_steps=30, stepper="dWorldQuickStep"):
     lib.dWorldDestroy(w)
     return (np.array(getters, dtype=np.float64), np.array(states, dtype=np.float64),
             np.array(moved, dtype=np.int64))
+
+
+class Surface(C.Structure):
+    _fields_ = [("mode", I), ("mu", F), ("mu2", F), ("bounce", F), ("bounce_vel", F), ("soft_erp", F),
+                ("soft_cfm", F), ("motion1", F), ("motion2", F), ("motionN", F), ("slip1", F), ("slip2", F)]
+
+
+class ContactGeom(C.Structure):
+    _fields_ = [("pos", F * 4), ("normal", F * 4), ("depth", F), ("g1", P), ("g2", P), ("side1", I),
+                ("side2", I)]
+
+
+class Contact(C.Structure):
+    _fields_ = [("surface", Surface), ("geom", ContactGeom), ("fdir1", F * 4)]
+
+
+def bind_islands(lib):
+    bind(lib)
+    for n in ("dJointCreateNull", "dJointGroupCreate", "dJointCreateContact"):
+        getattr(lib, n).restype = P
+    lib.dJointCreateNull.argtypes = [P, P]
+    lib.dJointGroupCreate.argtypes = [I]
+    lib.dJointCreateContact.argtypes = [P, P, P]
+    lib.dJointGroupEmpty.argtypes = lib.dJointGroupDestroy.argtypes = [P]
+    lib.dBodyEnable.argtypes = lib.dBodyDisable.argtypes = lib.dBodyIsEnabled.argtypes = [P]
+    lib.dRandSetSeed.argtypes = [C.c_ulong]
+    lib.dRandGetSeed.restype = C.c_ulong
+    lib.dBodySetForce.argtypes = [P, F, F, F]
+    lib.dBodyGetForce.restype = C.POINTER(F)
+    lib.dBodyGetForce.argtypes = [P]
+    return lib
+
+
+def island_program(lib, seed, n_steps=12, stepper="dWorldQuickStep"):
+    """Boxes resting on ground contacts (depth 0.01, friction), linked by ball
+    and null joints, some disabled: a null joint merges two islands, a
+    disabled body joined to an enabled one is woken, disabled bodies joined
+    only to each other or to the ground stay put with their forces kept.
+    Returns per step the RNG seed (its draws follow every island's row count),
+    the enabled flags, the states and the moved-callback order."""
+    rng = np.random.default_rng(seed)
+    lib.dInitODE2(0)
+    lib.dRandSetSeed(1234 + seed)
+    w = lib.dWorldCreate()
+    lib.dWorldSetGravity(w, 0.0, 0.0, -9.81)
+    b = []
+    for k in range(9):
+        bb = lib.dBodyCreate(w)
+        m = Mass()
+        lib.dMassSetBox(C.byref(m), 1.0, 0.5, 0.5, 0.5)
+        lib.dBodySetMass(bb, C.byref(m))
+        lib.dBodySetPosition(bb, float(k), 0.0, 0.25 + 0.01 * float(rng.random()))
+        lib.dBodySetLinearVel(bb, *(float(x) for x in rng.normal(0, 0.2, 3)))
+        b.append(bb)
+    order = [int(x) for x in rng.permutation(9)]
+    links = [("ball", 0, 1), ("null", 2, 3), ("null", 4, 6), ("ball", 7, 8), ("null", 3, 0)]
+    for kind, i, k in links:
+        j = (lib.dJointCreateBall if kind == "ball" else lib.dJointCreateNull)(w, None)
+        lib.dJointAttach(j, b[i], b[k])
+        if kind == "ball":
+            lib.dJointSetBallAnchor(j, 0.5 * (i + k), 0.0, 0.25)
+    lib.dBodyDisable(b[6])          # joined to b4 by a null joint: woken
+    lib.dBodyDisable(b[7])          # joined only to b8 ...
+    lib.dBodyDisable(b[8])          # ... both disabled: they stay
+    lib.dBodyDisable(b[5])          # a ground contact only: stays
+    lib.dBodySetForce(b[5], 1.0, 2.0, 3.0)
+    grp = lib.dJointGroupCreate(0)
+    ix = {bb: k for k, bb in enumerate(b)}
+    moved = []
+    cb = MOVED(lambda p: moved.append(ix.get(p, -1)))
+    for bb in b:
+        lib.dBodySetMovedCallback(bb, cb)
+    seeds, flags, states = [], [], []
+    for _ in range(n_steps):
+        lib.dJointGroupEmpty(grp)
+        for k in order:           # ground contacts, created in a shuffled order
+            c = Contact()
+            c.surface.mode = 0
+            c.surface.mu = 0.5
+            p = lib.dBodyGetPosition(b[k])
+            c.geom.pos[0], c.geom.pos[1], c.geom.pos[2] = p[0], p[1], 0.0
+            c.geom.normal[2] = 1.0
+            c.geom.depth = 0.01
+            j = lib.dJointCreateContact(w, grp, C.byref(c))
+            lib.dJointAttach(j, b[k], None)
+        getattr(lib, stepper)(w, 0.01)
+        seeds.append(lib.dRandGetSeed())
+        flags.append([lib.dBodyIsEnabled(bb) for bb in b])
+        states.append([state(lib, bb) for bb in b])
+    f5 = lib.dBodyGetForce(b[5])
+    kept = [f5[0], f5[1], f5[2]]
+    lib.dJointGroupDestroy(grp)
+    lib.dWorldDestroy(w)
+    return (np.array(seeds, dtype=np.int64), np.array(flags, dtype=np.int64), np.array(states, dtype=np.float64),
+            np.array(moved, dtype=np.int64), np.array(kept, dtype=np.float64))

@@ -538,7 +538,8 @@ def make_body_step_options(seeds=(1, 2, 3), n_steps=30):
     """The reference's dSINGLE build through its public API
     (tests/body_step_program.py): damping, the angular speed cap and finite
     rotation over a smooth 30-step flight, the getters, and the moved
-    callbacks' order, for dWorldQuickStep and dWorldStep."""
+    callbacks' order, for dWorldQuickStep and dWorldStep; and the island
+    program (null joints, disabled bodies): RNG seeds, enabled flags, states."""
     import ctypes as C
     import body_step_program as BP
     lib = BP.bind(C.CDLL(os.path.join(ROOT, "oracle", "_ref", "libode_ref_s.so")))
@@ -547,6 +548,11 @@ def make_body_step_options(seeds=(1, 2, 3), n_steps=30):
         for s in seeds:
             g, x, m = BP.program(lib, s, n_steps, st)
             out[f"{st}_{s}_getters"], out[f"{st}_{s}_states"], out[f"{st}_{s}_moved"] = g, x, m
+    for st in ("dWorldQuickStep", "dWorldStep"):
+        for s in seeds:
+            r = BP.island_program(BP.bind_islands(lib), s, 12, st)
+            for k, v in zip(("seeds", "enabled", "states", "moved", "kept_force"), r):
+                out[f"islands_{st}_{s}_{k}"] = v
     np.savez_compressed(os.path.join(HERE, "body_step_options.npz"), **out)
 
 

@@ -306,6 +306,31 @@ def test_body_step_options_match_reference(stepper):
         assert err.max() <= 1e-4, (int(s), float(err.max()), np.unravel_index(np.argmax(err), err.shape))
 
 
+@pytest.mark.parametrize("stepper", ["dWorldQuickStep", "dWorldStep"])
+def test_disabled_bodies_and_null_joints_match_reference(stepper):
+    """Islands with null joints (ode/src/joints/null.cpp: no rows, one island)
+    and disabled bodies (util.cpp:413-470: reached ones are woken, the rest are
+    not stepped and keep their forces) against the reference's dSINGLE build
+    over 12 steps of boxes on ground contacts (tests/body_step_program.py
+    island_program): the RNG seed after every step exactly (SOR's shuffle
+    draws follow each island's row count, so a wrongly merged or split island
+    changes it), the enabled flags, the moved-callback order and the kept
+    forces exactly, states within 1e-4 (1 + |x|)."""
+    import body_step_program as BP
+    g = np.load(os.path.join(GOLDEN, "body_step_options.npz"))
+    L = BP.bind_islands(C.CDLL(os.path.join(os.path.dirname(GOLDEN), "..", "ode-0.12_gb300", "libodegpu.so")))
+    for s in g["seeds"]:
+        seeds, flags, states, moved, kept = BP.island_program(L, int(s), 12, stepper)
+        pre = f"islands_{stepper}_{s}_"
+        assert np.array_equal(seeds, g[pre + "seeds"]), (int(s), seeds, g[pre + "seeds"])
+        assert np.array_equal(flags, g[pre + "enabled"])
+        assert np.array_equal(moved, g[pre + "moved"])
+        assert np.array_equal(kept, g[pre + "kept_force"])
+        want = g[pre + "states"]
+        err = np.abs(states - want) / (1.0 + np.abs(want))
+        assert err.max() <= 1e-4, (int(s), float(err.max()))
+
+
 class JointFeedback(C.Structure):
     _fields_ = [("f1", C.c_float * 4), ("t1", C.c_float * 4), ("f2", C.c_float * 4), ("t2", C.c_float * 4)]
 
