@@ -18,7 +18,10 @@ enum {
   SURF_SOFT_CFM = 0x010, SURF_MOTION1 = 0x020, SURF_MOTION2 = 0x040, SURF_MOTIONN = 0x080,
   SURF_SLIP1 = 0x100, SURF_SLIP2 = 0x200, SURF_APPROX1_1 = 0x1000, SURF_APPROX1_2 = 0x2000
 };
-enum { BODY_GYROSCOPIC = 1, BODY_NO_GRAVITY = 2 };
+// BODY_WOKEN: disabled when the step began and joined by an enabled joint to
+// an enabled body, so the step's island walk enables it; it never starts an
+// island (ode/src/util.cpp:420-423 skips disabled bodies as starts)
+enum { BODY_GYROSCOPIC = 1, BODY_NO_GRAVITY = 2, BODY_WOKEN = 4 };
 
 // Per-world status bits (odegpuBatchStatus).
 enum {

@@ -499,7 +499,7 @@ OG_D void lw_walk(const LWDev& L, const int* astart, int* stack, unsigned char* 
                   int nb, int& jc_out, int& ni_out) {
   int jc = 0, ni = 0;
   for (int bb = nb - 1; bb >= 0; --bb) {
-    if (flags[bb] & 1) continue;
+    if (flags[bb] & 5) continue;   // walked, or woken by this step (4): not a start
     flags[bb] = 1;
     const int jstart = jc;
     int sp = 0, b = bb;
@@ -541,14 +541,14 @@ __global__ void __launch_bounds__(32) lw_islands_kernel(BatchDev d, LWDev L, int
     short* other = reinterpret_cast<short*>(flags + ((nb + 16) & ~15));
     for (int b = lane; b <= nb; b += 32) astart[b] = L.acount[b];
     for (int e = lane; e < E; e += 32) other[e] = (short)L.adj_other[e];
-    for (int b = lane; b < nb; b += 32) flags[b] = 0;
+    for (int b = lane; b < nb; b += 32) flags[b] = (d.bflags[b] & BODY_WOKEN) ? 4 : 0;
     __syncwarp();
     if (lane == 0) {
       atomicAdd(&L.stats[LWS_WALK_COPY_NS], lw_now() - t_start);
       lw_walk<short>(L, astart, stack, flags, other, nb, jc, ni);
     }
   } else {
-    for (int b = lane; b < nb; b += 32) L.bflag[b] = 0;
+    for (int b = lane; b < nb; b += 32) L.bflag[b] = (d.bflags[b] & BODY_WOKEN) ? 4 : 0;
     __syncwarp();
     if (lane == 0) lw_walk<int>(L, L.acount, L.stack, L.bflag, L.adj_other, nb, jc, ni);
   }

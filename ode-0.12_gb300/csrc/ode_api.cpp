@@ -2345,7 +2345,7 @@ static int world_step(dWorldID w, dReal stepsize, bool exact) {
   // The bodies this step moves (util.cpp:413-470): every enabled body and
   // whatever an enabled joint connects to one, which the island walk enables
   // again; a disabled body reached by none stays as it is, forces included.
-  std::vector<dxBody*> sb;
+  std::vector<dxBody*> sb, woken;
   {
     std::unordered_map<const dxBody*, std::vector<dxBody*>> nbr;
     for (const dxJoint* j : w->joints)
@@ -2362,6 +2362,7 @@ static int world_step(dWorldID w, dReal stepsize, bool exact) {
         while (!stack.empty()) {
           dxBody* c = stack.back();
           stack.pop_back();
+          if (c->disabled) woken.push_back(c);
           c->disabled = 0;
           const auto it = nbr.find(c);
           if (it == nbr.end()) continue;
@@ -2395,6 +2396,11 @@ static int world_step(dWorldID w, dReal stepsize, bool exact) {
         hw.invI[9 * (size_t)i + r * 3 + c] = (float)b->invI[r * 3 + c];
       }
     hw.flags[i] = b->flags;
+  }
+  if (!woken.empty()) {   // woken this step: never an island start
+    std::unordered_map<const dxBody*, int> slot;
+    for (int i = 0; i < nb; ++i) slot[sb[i]] = i;
+    for (const dxBody* b : woken) hw.flags[slot[b]] |= og::BODY_WOKEN;
   }
   // dxStepBody options, uploaded only when some body uses one. The finite
   // axis flag without the mode has no effect (util.cpp:272-276).
@@ -2550,7 +2556,7 @@ static int world_step(dWorldID w, dReal stepsize, bool exact) {
     std::vector<char> btag(nb, 0), jtag(nj, 0);
     std::vector<int> stack;
     for (int first = nb - 1; first >= 0; --first) {
-      if (btag[first]) continue;
+      if (btag[first] || (hw.flags[first] & og::BODY_WOKEN)) continue;
       btag[first] = 1;
       int b = first;
       for (;;) {

@@ -417,7 +417,15 @@ OG_D int phase_islands(const BatchDev& d, const WorldDesc& D, int w, int nc, int
     __syncwarp();
     if (!__any_sync(kFull, changed)) break;
   }
-  for (int b = lane; b < nb; b += 32) atomicAdd(&bcnt[lab[b]], 1);
+  // a component's island starts at its newest body that was enabled when the
+  // step began (S.cnt is free again: by label, -1 for none)
+  int* rt = S.cnt;
+  for (int b = lane; b < nb; b += 32) rt[b] = -1;
+  __syncwarp();
+  for (int b = lane; b < nb; b += 32) {
+    atomicAdd(&bcnt[lab[b]], 1);
+    if (!(d.bflags[D.body_off + b] & BODY_WOKEN)) atomicMax(&rt[lab[b]], b);
+  }
   for (int j = lane; j < nj_all; j += 32)
     if (S.jb1[j] >= 0) atomicAdd(&jcnt[lab[S.jb1[j]]], 1);
   __syncwarp();
@@ -425,8 +433,9 @@ OG_D int phase_islands(const BatchDev& d, const WorldDesc& D, int w, int nc, int
   int jcount = 0, nisl = 0, scarry = 0;
   for (int base = 0; base < nb; base += 32) {
     const int b = nb - 1 - (base + lane);
-    const bool isl = b >= 0 && lab[b] == b && jcnt[b] > 0;
-    const int jn = isl ? jcnt[b] : 0, bn = isl ? bcnt[b] : 0;
+    const int l = b >= 0 ? lab[b] : 0;
+    const bool isl = b >= 0 && (rt[l] >= 0 ? rt[l] : l) == b && jcnt[l] > 0;
+    const int jn = isl ? jcnt[l] : 0, bn = isl ? bcnt[l] : 0;
     const int ji = warp_incl_scan(jn, lane), bi = warp_incl_scan(bn, lane);
     const unsigned bal = __ballot_sync(kFull, isl);
     if (isl) {
