@@ -173,6 +173,35 @@ void dWorldSetAngularDamping(dWorldID w, dReal scale);              /* :685 */
 void dWorldSetDamping(dWorldID w, dReal linear_scale, dReal angular_scale);  /* :693 */
 dReal dWorldGetMaxAngularSpeed(dWorldID w);                         /* :702 */
 void dWorldSetMaxAngularSpeed(dWorldID w, dReal max_speed);         /* :710 */
+/* Auto-disable, checked on the host at the start of every step
+ * (ode/src/util.cpp:98-230); a disabled body is left out of the step until an
+ * enabled joint connects it to an enabled body. dWorldGetAutoDisableFlag
+ * returns ODE 0.12's raw flag bit (16) when set. */
+dReal dWorldGetAutoDisableLinearThreshold(dWorldID w);              /* :487 */
+void dWorldSetAutoDisableLinearThreshold(dWorldID w, dReal linear_threshold);    /* :494 */
+dReal dWorldGetAutoDisableAngularThreshold(dWorldID w);             /* :501 */
+void dWorldSetAutoDisableAngularThreshold(dWorldID w, dReal angular_threshold);  /* :508 */
+int dWorldGetAutoDisableAverageSamplesCount(dWorldID w);            /* :543 */
+void dWorldSetAutoDisableAverageSamplesCount(dWorldID w, unsigned int average_samples_count);  /* :551 */
+int dWorldGetAutoDisableSteps(dWorldID w);                          /* :558 */
+void dWorldSetAutoDisableSteps(dWorldID w, int steps);              /* :565 */
+dReal dWorldGetAutoDisableTime(dWorldID w);                         /* :572 */
+void dWorldSetAutoDisableTime(dWorldID w, dReal time);              /* :579 */
+int dWorldGetAutoDisableFlag(dWorldID w);                           /* :586 */
+void dWorldSetAutoDisableFlag(dWorldID w, int do_auto_disable);     /* :593 */
+dReal dBodyGetAutoDisableLinearThreshold(dBodyID b);                /* :753 */
+void dBodySetAutoDisableLinearThreshold(dBodyID b, dReal linear_average_threshold);   /* :760 */
+dReal dBodyGetAutoDisableAngularThreshold(dBodyID b);               /* :767 */
+void dBodySetAutoDisableAngularThreshold(dBodyID b, dReal angular_average_threshold); /* :774 */
+int dBodyGetAutoDisableAverageSamplesCount(dBodyID b);              /* :781 */
+void dBodySetAutoDisableAverageSamplesCount(dBodyID b, unsigned int average_samples_count);  /* :788 */
+int dBodyGetAutoDisableSteps(dBodyID b);                            /* :796 */
+void dBodySetAutoDisableSteps(dBodyID b, int steps);                /* :803 */
+dReal dBodyGetAutoDisableTime(dBodyID b);                           /* :810 */
+void dBodySetAutoDisableTime(dBodyID b, dReal time);                /* :817 */
+int dBodyGetAutoDisableFlag(dBodyID b);                             /* :824 */
+void dBodySetAutoDisableFlag(dBodyID b, int do_auto_disable);       /* :831 */
+void dBodySetAutoDisableDefaults(dBodyID b);                        /* :839 */
 
 /* bodies: include/ode/objects.h */
 dBodyID dBodyCreate(dWorldID w);                                    /* :856 */
@@ -213,10 +242,9 @@ void dBodyVectorToWorld(dBodyID b, dReal px, dReal py, dReal pz, dVector3 result
 void dBodyVectorFromWorld(dBodyID b, dReal px, dReal py, dReal pz, dVector3 result); /* :1161 */
 void dBodySetData(dBodyID b, void* data);                           /* :873 */
 void* dBodyGetData(dBodyID b);                                      /* :880 */
-/* Manual enabling only: automatic disabling is not built. A step moves the
- * enabled bodies and those an enabled joint connects to them (enabling them,
- * as ODE's island walk does); other disabled bodies keep their state and
- * their accumulated forces. */
+/* A step moves the enabled bodies and those an enabled joint connects to
+ * them (enabling them, as ODE's island walk does); other disabled bodies keep
+ * their state and their accumulated forces. */
 void dBodyEnable(dBodyID b);                                        /* :1269 */
 void dBodyDisable(dBodyID b);                                       /* :1278 */
 int dBodyIsEnabled(dBodyID b);                                      /* :1285 */

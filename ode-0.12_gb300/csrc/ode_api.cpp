@@ -43,7 +43,13 @@ struct dxBody {
   dReal max_angular_speed, lin_scale, lin_thr, ang_scale, ang_thr;
   dReal frot_axis[4];
   void (*moved_callback)(dxBody*);   // dBodySetMovedCallback
-  int disabled;                      // dBodyDisable (no auto-disable on this path)
+  int disabled;                      // dBodyDisable, or auto-disabled
+  // auto-disable (ode/src/objects.h dxAutoDisable, util.cpp:98-230): the
+  // parameters, the idle countdowns and the velocity sample ring
+  int auto_disable, adis_steps, adis_stepsleft, avg_ready;
+  unsigned adis_samples, avg_counter;
+  dReal adis_time, adis_lin_thr, adis_ang_thr, adis_timeleft;
+  dReal (*avg_buf)[6];
 };
 
 struct dxJoint {
@@ -142,6 +148,11 @@ struct dxWorld {
   dReal lin_scale = 0, ang_scale = 0;
   dReal lin_thr = (dReal)0.01 * (dReal)0.01, ang_thr = (dReal)0.01 * (dReal)0.01;
   dReal max_angular_speed = INFINITY;
+  // auto-disable defaults of dWorldCreate (ode/src/ode.cpp:1560-1566)
+  int auto_disable = 0, adis_steps = 10;
+  unsigned adis_samples = 1;
+  dReal adis_time = 0;
+  dReal adis_lin_thr = (dReal)0.01 * (dReal)0.01, adis_ang_thr = (dReal)0.01 * (dReal)0.01;
   std::vector<dxBody*> bodies;     // creation order
   std::vector<dxJoint*> joints;    // every live joint, creation order
   long long seq = 0;
@@ -310,6 +321,7 @@ void dWorldDestroy(dWorldID w) {
     if (!j->group) delete j;
   for (dxBody* b : w->bodies) {   // dBodyDestroy of each body (ode.cpp:1589-1594)
     body_geoms_detach(b);
+    delete[] b->avg_buf;
     delete b;
   }
   og::ctx_destroy(w->ctx);
@@ -412,11 +424,65 @@ void dBodyGetFiniteRotationAxis(dBodyID b, dVector3 result) {
 }
 // Called after each step for every body, in island order, once all bodies
 // have their new state (ODE calls it as each body is stepped).
+// Auto-disable parameters (ode/src/ode.cpp:900-1010, :1843-1927): thresholds
+// kept squared; a body takes the world's at creation or from
+// dBodySetAutoDisableDefaults; turning a body's flag off also enables it and
+// resets its countdowns and samples to the world's.
+dReal dWorldGetAutoDisableLinearThreshold(dWorldID w) { return std::sqrt(w->adis_lin_thr); }
+void dWorldSetAutoDisableLinearThreshold(dWorldID w, dReal t) { w->adis_lin_thr = t * t; }
+dReal dWorldGetAutoDisableAngularThreshold(dWorldID w) { return std::sqrt(w->adis_ang_thr); }
+void dWorldSetAutoDisableAngularThreshold(dWorldID w, dReal t) { w->adis_ang_thr = t * t; }
+int dWorldGetAutoDisableAverageSamplesCount(dWorldID w) { return (int)w->adis_samples; }
+void dWorldSetAutoDisableAverageSamplesCount(dWorldID w, unsigned int n) { w->adis_samples = n; }
+int dWorldGetAutoDisableSteps(dWorldID w) { return w->adis_steps; }
+void dWorldSetAutoDisableSteps(dWorldID w, int steps) { w->adis_steps = steps; }
+dReal dWorldGetAutoDisableTime(dWorldID w) { return w->adis_time; }
+void dWorldSetAutoDisableTime(dWorldID w, dReal time) { w->adis_time = time; }
+// the raw flag bit, as ODE 0.12 returns it (ode.cpp:1913-1917)
+int dWorldGetAutoDisableFlag(dWorldID w) { return w->auto_disable ? 16 : 0; }
+void dWorldSetAutoDisableFlag(dWorldID w, int do_auto_disable) { w->auto_disable = do_auto_disable != 0; }
+dReal dBodyGetAutoDisableLinearThreshold(dBodyID b) { return std::sqrt(b->adis_lin_thr); }
+void dBodySetAutoDisableLinearThreshold(dBodyID b, dReal t) { b->adis_lin_thr = t * t; }
+dReal dBodyGetAutoDisableAngularThreshold(dBodyID b) { return std::sqrt(b->adis_ang_thr); }
+void dBodySetAutoDisableAngularThreshold(dBodyID b, dReal t) { b->adis_ang_thr = t * t; }
+int dBodyGetAutoDisableAverageSamplesCount(dBodyID b) { return (int)b->adis_samples; }
+void dBodySetAutoDisableAverageSamplesCount(dBodyID b, unsigned int n) {
+  b->adis_samples = n;
+  delete[] b->avg_buf;
+  b->avg_buf = n > 0 ? new dReal[n][6] : nullptr;
+  b->avg_counter = 0;
+  b->avg_ready = 0;
+}
+int dBodyGetAutoDisableSteps(dBodyID b) { return b->adis_steps; }
+void dBodySetAutoDisableSteps(dBodyID b, int steps) { b->adis_steps = steps; }
+dReal dBodyGetAutoDisableTime(dBodyID b) { return b->adis_time; }
+void dBodySetAutoDisableTime(dBodyID b, dReal time) { b->adis_time = time; }
+int dBodyGetAutoDisableFlag(dBodyID b) { return b->auto_disable ? 1 : 0; }
+void dBodySetAutoDisableFlag(dBodyID b, int do_auto_disable) {
+  if (!do_auto_disable) {
+    b->auto_disable = 0;
+    b->disabled = 0;
+    b->adis_steps = b->world->adis_steps;
+    b->adis_time = b->world->adis_time;
+    dBodySetAutoDisableAverageSamplesCount(b, b->world->adis_samples);
+  } else {
+    b->auto_disable = 1;
+  }
+}
+void dBodySetAutoDisableDefaults(dBodyID b) {
+  const dxWorld* w = b->world;
+  b->adis_steps = w->adis_steps; b->adis_time = w->adis_time; b->adis_samples = w->adis_samples;
+  b->adis_lin_thr = w->adis_lin_thr; b->adis_ang_thr = w->adis_ang_thr;
+  dBodySetAutoDisableFlag(b, w->auto_disable);
+}
 void dBodySetMovedCallback(dBodyID b, void (*callback)(dBodyID)) { b->moved_callback = callback; }
-// dBodyEnable / Disable / IsEnabled (ode.cpp:854-875); automatic disabling
-// is not built, so a body only changes state here or when a step's island
-// walk reaches it
-void dBodyEnable(dBodyID b) { b->disabled = 0; }
+// dBodyEnable / Disable / IsEnabled (ode.cpp:854-875); a body also changes
+// state when a step's auto-disable check or island walk reaches it
+void dBodyEnable(dBodyID b) {
+  b->disabled = 0;
+  b->adis_stepsleft = b->adis_steps;
+  b->adis_timeleft = b->adis_time;
+}
 void dBodyDisable(dBodyID b) { b->disabled = 1; }
 int dBodyIsEnabled(dBodyID b) { return b->disabled ? 0 : 1; }
 dGeomID dBodyGetFirstGeom(dBodyID b) { return b->geom; }        // ode.cpp:1122-1133
@@ -436,6 +502,11 @@ dBodyID dBodyCreate(dWorldID w) {
   b->invMass = 1;
   b->flags = ODEGPU_BODY_GYROSCOPIC;
   w->bodies.push_back(b);
+  // auto-disable state (ode.cpp:270-279)
+  dBodySetAutoDisableDefaults(b);
+  b->adis_stepsleft = b->adis_steps;
+  b->adis_timeleft = b->adis_time;
+  dBodySetAutoDisableAverageSamplesCount(b, b->adis_samples);
   dBodySetDampingDefaults(b);   // ode.cpp:285-288
   b->step_flags |= w->body_step_flags & og::kStepMaxAng;
   b->max_angular_speed = w->max_angular_speed;
@@ -451,6 +522,7 @@ void dBodyDestroy(dBodyID b) {
     if (!j->body[0] && j->body[1]) { j->body[0] = j->body[1]; j->body[1] = nullptr; j->reverse = 1; }
   }
   w->bodies.erase(std::remove(w->bodies.begin(), w->bodies.end(), b), w->bodies.end());
+  delete[] b->avg_buf;
   delete b;
 }
 void dBodySetPosition(dBodyID b, dReal x, dReal y, dReal z) {
@@ -2335,8 +2407,56 @@ int dWorldQuickStep(dWorldID w, dReal stepsize) { return world_step(w, stepsize,
 // of ode/src/step.cpp and its Dantzig LCP on the GPU (world_exact.cuh)
 int dWorldStep(dWorldID w, dReal stepsize) { return world_step(w, stepsize, true); }
 
+// dInternalHandleAutoDisabling (ode/src/util.cpp:98-230), the first thing a
+// step does: each enabled, auto-disabling body with a joint (no freezing in
+// mid-air) samples its velocities into its ring; once the ring is full, an
+// average below both thresholds counts the body idle, and idle for the steps
+// and the time asked disables it and zeroes its velocities.
+static void handle_auto_disabling(dxWorld* w, dReal stepsize) {
+  bool any = false;
+  for (const dxBody* b : w->bodies) any |= b->auto_disable && !b->disabled;
+  if (!any) return;
+  std::unordered_map<const dxBody*, char> jointed;
+  for (const dxJoint* j : w->joints)
+    for (int s = 0; s < 2; ++s)
+      if (j->body[s]) jointed[j->body[s]] = 1;
+  for (dxBody* b : w->bodies) {
+    if (!jointed.count(b) || !b->auto_disable || b->disabled || b->adis_samples == 0) continue;
+    if (b->avg_counter >= b->adis_samples) { b->avg_ready = 0; b->avg_counter = 0; }
+    dReal* smp = b->avg_buf[b->avg_counter];
+    for (int k = 0; k < 3; ++k) { smp[k] = b->lvel[k]; smp[3 + k] = b->avel[k]; }
+    if (++b->avg_counter >= b->adis_samples) { b->avg_counter = 0; b->avg_ready = 1; }
+    int idle = 0;
+    if (b->avg_ready) {
+      idle = 1;
+      dReal al[3], aa[3];
+      for (int k = 0; k < 3; ++k) { al[k] = b->avg_buf[0][k]; aa[k] = b->avg_buf[0][3 + k]; }
+      if (b->adis_samples > 1) {
+        for (unsigned i = 1; i < b->adis_samples; ++i)
+          for (int k = 0; k < 3; ++k) { al[k] += b->avg_buf[i][k]; aa[k] += b->avg_buf[i][3 + k]; }
+        const dReal r1 = (dReal)1.0 / (dReal)b->adis_samples;
+        for (int k = 0; k < 3; ++k) { al[k] *= r1; aa[k] *= r1; }
+      }
+      if (al[0] * al[0] + al[1] * al[1] + al[2] * al[2] > b->adis_lin_thr) idle = 0;
+      else if (aa[0] * aa[0] + aa[1] * aa[1] + aa[2] * aa[2] > b->adis_ang_thr) idle = 0;
+    }
+    if (idle) {
+      b->adis_stepsleft--;
+      b->adis_timeleft -= stepsize;
+    } else {
+      b->adis_stepsleft = b->adis_steps;
+      b->adis_timeleft = b->adis_time;
+    }
+    if (b->adis_stepsleft <= 0 && b->adis_timeleft <= 0) {
+      b->disabled = 1;
+      for (int k = 0; k < 3; ++k) b->lvel[k] = b->avel[k] = 0;
+    }
+  }
+}
+
 static int world_step(dWorldID w, dReal stepsize, bool exact) {
   if (!w || !(stepsize > 0)) return 0;
+  handle_auto_disabling(w, stepsize);
   if (!w->ctx) {
     w->ctx = og::ctx_create(0);
     if (!w->ctx) return 0;
