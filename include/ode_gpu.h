@@ -245,6 +245,9 @@ void* dBodyGetData(dBodyID b);                                      /* :880 */
 /* A step moves the enabled bodies and those an enabled joint connects to
  * them (enabling them, as ODE's island walk does); other disabled bodies keep
  * their state and their accumulated forces. */
+void dBodySetDynamic(dBodyID b);                                    /* :1241 */
+void dBodySetKinematic(dBodyID b);                                  /* :1255 */
+int dBodyIsKinematic(dBodyID b);                                    /* :1262 */
 void dBodyEnable(dBodyID b);                                        /* :1269 */
 void dBodyDisable(dBodyID b);                                       /* :1278 */
 int dBodyIsEnabled(dBodyID b);                                      /* :1285 */
@@ -432,6 +435,13 @@ int dSafeNormalize4(dVector4 a);                                         /* :425
 void dNormalize3(dVector3 a);                                            /* :426 */
 void dNormalize4(dVector4 a);                                            /* :427 */
 void dPlaneSpace(const dVector3 n, dVector3 p, dVector3 q);              /* :462 */
+void dOrthogonalizeR(dMatrix3 m);                                        /* :464 */
+/* include/ode/misc.h: matrices with rows padded to a multiple of 4 */
+void dMakeRandomVector(dReal* A, int n, dReal range);                    /* misc.h:65 */
+void dMakeRandomMatrix(dReal* A, int n, int m, dReal range);             /* :68 */
+void dClearUpperTriangle(dReal* A, int n);                               /* :71 */
+dReal dMaxDifference(const dReal* A, const dReal* B, int n, int m);      /* :74 */
+dReal dMaxDifferenceLowerTriangle(const dReal* A, const dReal* B, int n);  /* :78 */
 
 /* collision: include/ode/collision.h */
 int dCollide(dGeomID o1, dGeomID o2, int flags, dContactGeom* contact, int skip); /* :795 */
@@ -500,6 +510,7 @@ void dGeomCopyRotation(dGeomID g, dMatrix3 R);                           /* :229
 void dGeomGetQuaternion(dGeomID g, dQuaternion result);                  /* :245 */
 void dGeomGetAABB(dGeomID g, dReal aabb[6]);                             /* :264 */
 int dGeomIsSpace(dGeomID g);                                             /* :273 */
+void dInfiniteAABB(dGeomID g, dReal aabb[6]);                            /* :1481 */
 dSpaceID dGeomGetSpace(dGeomID g);                                       /* :283 */
 int dGeomGetClass(dGeomID g);                                            /* :310 */
 /* Category / collide bits and the enabled flag steer a space's pair search;

@@ -574,6 +574,18 @@ const dReal* dBodyGetRotation(dBodyID b) { return b->R; }
 const dReal* dBodyGetQuaternion(dBodyID b) { return b->q; }
 const dReal* dBodyGetLinearVel(dBodyID b) { return b->lvel; }
 const dReal* dBodyGetAngularVel(dBodyID b) { return b->avel; }
+// Kinematic bodies (ode/src/ode.cpp:834-852): zero inverse mass and inertia,
+// so forces and constraints do not move them; dBodySetDynamic restores both
+// from the body's mass.
+void dBodySetKinematic(dBodyID b) {
+  for (int k = 0; k < 9; ++k) b->invI[k] = 0;
+  b->invMass = 0;
+}
+int dBodyIsKinematic(dBodyID b) { return b->invMass == 0; }
+void dBodySetDynamic(dBodyID b) {
+  const dMass m = b->mass;
+  dBodySetMass(b, &m);
+}
 void dBodySetMass(dBodyID b, const dMass* m) {
   // dBodySetMass (ode/src/ode.cpp:492-509): invI through a Cholesky inverse
   b->mass = *m;
@@ -1907,6 +1919,9 @@ void dGeomGetAABB(dGeomID g, dReal aabb[6]) {   // collision_kernel.cpp:705-711
   for (int k = 0; k < 6; ++k) aabb[k] = g->aabb[k];
 }
 // collision_kernel.cpp:714-726
+void dInfiniteAABB(dGeomID, dReal aabb[6]) {   // collision_util.cpp:457-465
+  for (int k = 0; k < 6; ++k) aabb[k] = (k & 1) ? INFINITY : -INFINITY;
+}
 int dGeomIsSpace(dGeomID g) { return is_space(g) ? 1 : 0; }
 dSpaceID dGeomGetSpace(dGeomID g) { return g->space; }
 int dGeomGetClass(dGeomID g) { return g->type; }
@@ -3107,6 +3122,60 @@ void dWorldImpulseToForce(dWorldID, dReal stepsize, dReal ix, dReal iy, dReal iz
 }
 // misc.cpp:57-60
 dReal dRandReal(void) { return (dReal)dRand() / (dReal)0xffffffffUL; }
+
+// Matrix helpers of ode/src/misc.cpp:139-195 over row-padded matrices
+// (rows of dPAD(columns) entries, include/ode/common.h:136)
+static int pad4(int a) { return a > 1 ? ((a - 1) | 3) + 1 : a; }
+void dMakeRandomVector(dReal* A, int n, dReal range) {
+  for (int i = 0; i < n; ++i) A[i] = (dRandReal() * (dReal)2.0 - (dReal)1.0) * range;
+}
+void dMakeRandomMatrix(dReal* A, int n, int m, dReal range) {
+  const int skip = pad4(m);
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < m; ++j) A[(size_t)i * skip + j] = (dRandReal() * (dReal)2.0 - (dReal)1.0) * range;
+}
+void dClearUpperTriangle(dReal* A, int n) {
+  const int skip = pad4(n);
+  for (int i = 0; i < n; ++i)
+    for (int j = i + 1; j < n; ++j) A[(size_t)i * skip + j] = 0;
+}
+dReal dMaxDifference(const dReal* A, const dReal* B, int n, int m) {
+  const int skip = pad4(m);
+  dReal mx = 0;
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < m; ++j) {
+      const dReal d = std::fabs(A[(size_t)i * skip + j] - B[(size_t)i * skip + j]);
+      if (d > mx) mx = d;
+    }
+  return mx;
+}
+dReal dMaxDifferenceLowerTriangle(const dReal* A, const dReal* B, int n) {
+  const int skip = pad4(n);
+  dReal mx = 0;
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j <= i; ++j) {
+      const dReal d = std::fabs(A[(size_t)i * skip + j] - B[(size_t)i * skip + j]);
+      if (d > mx) mx = d;
+    }
+  return mx;
+}
+// dOrthogonalizeR (ode/src/odemath.cpp:187-211): rows 0 and 1 normalised
+// (row 1 first made orthogonal to row 0 by a Gram-Schmidt step), row 2 their
+// cross product, so the result is a rotation and never a reflection
+void dOrthogonalizeR(dMatrix3 m) {
+  if (m[0] * m[0] + m[1] * m[1] + m[2] * m[2] != 1) dSafeNormalize3(m);
+  const dReal proj = m[0] * m[4] + m[1] * m[5] + m[2] * m[6];
+  if (proj != 0) {
+    m[4] -= proj * m[0];
+    m[5] -= proj * m[1];
+    m[6] -= proj * m[2];
+  }
+  if (m[4] * m[4] + m[5] * m[5] + m[6] * m[6] != 1) dSafeNormalize3(m + 4);
+  m[8] = m[1] * m[6] - m[2] * m[5];
+  m[9] = m[2] * m[4] - m[0] * m[6];
+  m[10] = m[0] * m[5] - m[1] * m[4];
+  m[3] = m[7] = m[11] = 0;
+}
 // the pre-0.9 names of the capsule mass functions (mass.cpp:544-553)
 void dMassSetCappedCylinder(dMass* m, dReal density, int direction, dReal radius, dReal length) {
   dMassSetCapsule(m, density, direction, radius, length);

@@ -390,3 +390,76 @@ def test_mass_check_matches_reference():
         else:
             m.I[0] = float("nan")
         assert ours.dMassCheck(C.byref(m)) == ref.dMassCheck(C.byref(m)), field
+
+
+def test_matrix_helpers_kinematic_bodies_and_orthogonalize_match_reference():
+    """dMakeRandomVector / Matrix, dClearUpperTriangle, dMaxDifference[LowerTriangle]
+    (ode/src/misc.cpp:139-195), dOrthogonalizeR (odemath.cpp:187-211),
+    dInfiniteAABB and dBodySetKinematic / SetDynamic / IsKinematic
+    (ode.cpp:834-852) against the reference's dSINGLE build, bit for bit."""
+    import ctypes as C
+    import numpy as np
+    import oracle_lib as O
+    if not O.ref_available("s"):
+        pytest.skip("reference not built in this checkout")
+    F, P = C.c_float, C.c_void_p
+    outs = []
+    for path in (os.path.join(ROOT, "ode-0.12_gb300", "libodegpu.so"),
+                 os.path.join(ROOT, "oracle", "_ref", "libode_ref_s.so")):
+        lib = C.CDLL(path)
+        lib.dRandSetSeed.argtypes = [C.c_ulong]
+        lib.dMakeRandomVector.argtypes = [P, C.c_int, F]
+        lib.dMakeRandomMatrix.argtypes = [P, C.c_int, C.c_int, F]
+        lib.dClearUpperTriangle.argtypes = [P, C.c_int]
+        lib.dMaxDifference.restype = lib.dMaxDifferenceLowerTriangle.restype = F
+        lib.dMaxDifference.argtypes = [P, P, C.c_int, C.c_int]
+        lib.dMaxDifferenceLowerTriangle.argtypes = [P, P, C.c_int]
+        lib.dOrthogonalizeR.argtypes = [P]
+        lib.dInfiniteAABB.argtypes = [P, P]
+        lib.dWorldCreate.restype = lib.dBodyCreate.restype = P
+        lib.dBodyCreate.argtypes = [P]
+        for n in ("dBodySetKinematic", "dBodySetDynamic", "dBodyIsKinematic", "dBodySetMass", "dBodyGetMass"):
+            getattr(lib, n).argtypes = [P] if n not in ("dBodySetMass", "dBodyGetMass") else [P, P]
+        lib.dMassSetBox.argtypes = [P, F, F, F, F]
+        lib.dWorldDestroy.argtypes = [P]
+        lib.dRandSetSeed(77)
+        out = []
+        v = (F * 7)()
+        lib.dMakeRandomVector(v, 7, 2.5)
+        out += list(v)
+        a, b = (F * 24)(), (F * 24)()   # 3 x 5, rows padded to 8
+        lib.dMakeRandomMatrix(a, 3, 5, 1.5)
+        lib.dMakeRandomMatrix(b, 3, 5, 1.5)
+        out += [lib.dMaxDifference(a, b, 3, 5)]
+        sq, sq2 = (F * 40)(), (F * 40)()   # 5 x 5, rows padded to 8
+        lib.dMakeRandomMatrix(sq, 5, 5, 1.0)
+        lib.dMakeRandomMatrix(sq2, 5, 5, 1.0)
+        out += [lib.dMaxDifferenceLowerTriangle(sq, sq2, 5)]
+        lib.dClearUpperTriangle(sq, 5)
+        out += list(sq)
+        rng = np.random.default_rng(5)
+        for _ in range(20):
+            m = (F * 12)(*rng.normal(size=12).astype(np.float32))
+            lib.dOrthogonalizeR(m)
+            out += list(m)
+        box = (F * 6)()
+        lib.dInfiniteAABB(None, box)
+        out += list(box)
+        w = lib.dWorldCreate()
+        bd = lib.dBodyCreate(w)
+
+        class Mass(C.Structure):
+            _fields_ = [("mass", F), ("c", F * 4), ("I", F * 12)]
+
+        m = Mass()
+        lib.dMassSetBox(C.byref(m), 2.0, 0.3, 0.4, 0.5)
+        lib.dBodySetMass(bd, C.byref(m))
+        out += [lib.dBodyIsKinematic(bd)]
+        lib.dBodySetKinematic(bd)
+        out += [lib.dBodyIsKinematic(bd)]
+        lib.dBodySetDynamic(bd)
+        out += [lib.dBodyIsKinematic(bd)]
+        lib.dWorldDestroy(w)
+        outs.append(np.array(out, dtype=np.float32))
+    assert np.array_equal(outs[0], outs[1]), \
+        np.flatnonzero(outs[0] != outs[1])
