@@ -445,6 +445,10 @@ dReal dMaxDifferenceLowerTriangle(const dReal* A, const dReal* B, int n);  /* :7
 
 /* collision: include/ode/collision.h */
 int dCollide(dGeomID o1, dGeomID o2, int flags, dContactGeom* contact, int skip); /* :795 */
+/* A caller's collider for a class pair runs on the host in place of the
+ * built-in one; dCloseODE drops the overrides. */
+typedef int dColliderFn(dGeomID o1, dGeomID o2, int flags, dContactGeom* contact, int skip);  /* :1488 */
+void dSetColliderOverride(int i, int j, dColliderFn* fn);                /* :1514 */
 dGeomID dCreateSphere(dSpaceID space, dReal radius);                     /* :924 */
 dGeomID dCreateBox(dSpaceID space, dReal lx, dReal ly, dReal lz);        /* :1002 */
 dGeomID dCreatePlane(dSpaceID space, dReal a, dReal b, dReal c, dReal d); /* :1046 */

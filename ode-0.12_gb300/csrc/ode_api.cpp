@@ -280,9 +280,25 @@ void joint_anchor(const dxJoint* j, bool second, dVector3 r) {
 
 extern "C" {
 
+// Collider overrides (dSetColliderOverride, collision_kernel.cpp:275-285):
+// a caller's function for a class pair, called on the host in place of the
+// built-in collider; (i, j) calls it as given and (j, i) with the geoms
+// swapped, so for i == j the swapped entry is the one that stays
+namespace {
+constexpr int kGeomClasses = 18;   // dGeomNumClasses of ODE 0.12
+struct ColliderOverride { dColliderFn* fn; int reverse; int set; };
+ColliderOverride g_override[kGeomClasses][kGeomClasses];
+}  // namespace
+void dSetColliderOverride(int i, int j, dColliderFn* fn) {
+  if (i < 0 || j < 0 || i >= kGeomClasses || j >= kGeomClasses) return;
+  g_override[i][j] = {fn, 0, 1};
+  g_override[j][i] = {fn, 1, 1};
+}
 void dInitODE(void) {}
 int dInitODE2(unsigned int) { return 1; }
-void dCloseODE(void) {}
+// dCloseODE drops the overrides, as the reference's next initialisation
+// rebuilds its collider table (collision_kernel.cpp:167-273)
+void dCloseODE(void) { std::memset(g_override, 0, sizeof(g_override)); }
 // Per-thread data and step working memory (odeinit.cpp:515-530,
 // objects.h:157-289): the GPU path keeps its own device buffers per world, so
 // these accept their arguments and have nothing to do.
@@ -2339,8 +2355,24 @@ int dCollide(dGeomID o1, dGeomID o2, int flags, dContactGeom* contact, int skip)
   // early-outs of ode/src/collision_kernel.cpp:292-311, then the collider on the GPU
   if (!o1 || !o2 || !contact || (flags & 0xffff) == 0) return 0;
   if (o1 == o2) return 0;
-  if (is_space(o1) || is_space(o2)) return 0;   // no collider takes a space
   if (o1->body == o2->body && o1->body) return 0;
+  if (o1->type >= 0 && o1->type < kGeomClasses && o2->type >= 0 && o2->type < kGeomClasses &&
+      g_override[o1->type][o2->type].set) {
+    // the caller's collider (collision_kernel.cpp:313-336); a reversed entry
+    // swaps the geoms and then flips normals, geoms and sides back
+    const ColliderOverride& ov = g_override[o1->type][o2->type];
+    if (!ov.fn) return 0;
+    if (!ov.reverse) return ov.fn(o1, o2, flags, contact, skip);
+    const int n = ov.fn(o2, o1, flags, contact, skip);
+    for (int i = 0; i < n; ++i) {
+      dContactGeom* c = (dContactGeom*)((char*)contact + (size_t)i * skip);
+      for (int k = 0; k < 3; ++k) c->normal[k] = -c->normal[k];
+      std::swap(c->g1, c->g2);
+      std::swap(c->side1, c->side2);
+    }
+    return n;
+  }
+  if (is_space(o1) || is_space(o2)) return 0;   // no collider takes a space
   if (o1->type == dHeightfieldClass || o2->type == dHeightfieldClass) {
     // dCollideHeightfield runs with the field first; the reversed call
     // negates the normals (ode/src/collision_kernel.cpp:319-335)

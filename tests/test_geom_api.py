@@ -391,3 +391,59 @@ def test_configuration_and_working_memory_calls():
     w = ours.dWorldCreate()
     assert ours.dWorldSetStepMemoryReservationPolicy(w, C.byref(bad)) == 0
     ours.dWorldDestroy(w)
+
+
+def test_collider_override_matches_reference():
+    """dSetColliderOverride (collision_kernel.cpp:275-336): the caller's
+    collider runs in place of the built-in one, as given for (i, j) and with
+    the geoms swapped and normals, geoms and sides flipped back for (j, i), so
+    an override of a class with itself takes the swapped form; a null
+    override leaves the pair without contacts. dCloseODE then dInitODE2 give
+    the built-in colliders back."""
+    ours, ref = _libs()
+
+    class CG(C.Structure):
+        _fields_ = [("pos", F * 4), ("normal", F * 4), ("depth", F), ("g1", P), ("g2", P), ("side1", I),
+                    ("side2", I)]
+
+    CB = C.CFUNCTYPE(I, P, P, I, P, I)
+
+    def fake(o1, o2, flags, contact, skip):
+        n = min(2, flags & 0xffff)
+        for i in range(n):
+            c = CG.from_address(contact + i * skip)
+            c.pos[0], c.pos[1], c.pos[2] = 1.0 + i, 2.0, 3.0
+            c.normal[0], c.normal[1], c.normal[2] = 0.6, 0.0, 0.8
+            c.depth = 0.25 * (i + 1)
+            c.g1, c.g2 = o1, o2
+            c.side1, c.side2 = 7, 9 + i
+        return n
+
+    cb = CB(fake)
+    outs = []
+    for lib in (ours, ref):
+        lib.dInitODE2.argtypes = [C.c_uint]
+        lib.dInitODE2(0)
+        lib.dSetColliderOverride.argtypes = [I, I, P]
+        lib.dCollide.argtypes = [P, P, I, P, I]
+        lib.dSetColliderOverride(dSphereClass, dBoxClass, C.cast(cb, P))
+        lib.dSetColliderOverride(dSphereClass, dSphereClass, C.cast(cb, P))
+        lib.dSetColliderOverride(dBoxClass, dBoxClass, None)
+        s1, s2 = lib.dCreateSphere(None, 0.5), lib.dCreateSphere(None, 0.5)
+        b1, b2 = lib.dCreateBox(None, 1.0, 1.0, 1.0), lib.dCreateBox(None, 1.0, 1.0, 1.0)
+        ids = {s1: 0, s2: 1, b1: 2, b2: 3, None: -1}
+        out = []
+        for o1, o2, nmax in ((s1, b1, 4), (b1, s1, 4), (s1, s2, 1), (b1, b2, 4)):
+            buf = (CG * 4)()
+            n = lib.dCollide(o1, o2, nmax, buf, C.sizeof(CG))
+            out += [n]
+            for i in range(n):
+                c = buf[i]
+                out += list(c.pos)[:3] + list(c.normal)[:3] + [c.depth, ids[c.g1], ids[c.g2], c.side1, c.side2]
+        for g in (s1, s2, b1, b2):
+            lib.dGeomDestroy(g)
+        lib.dCloseODE()
+        lib.dInitODE2(0)
+        outs.append(np.array(out, dtype=np.float32))
+    assert np.array_equal(outs[0], outs[1]), (outs[0], outs[1])
+    assert outs[0][0] == 2 and outs[0][-1] == 0
