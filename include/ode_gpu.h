@@ -515,6 +515,10 @@ void dGeomGetQuaternion(dGeomID g, dQuaternion result);                  /* :245
 void dGeomGetAABB(dGeomID g, dReal aabb[6]);                             /* :264 */
 int dGeomIsSpace(dGeomID g);                                             /* :273 */
 void dInfiniteAABB(dGeomID g, dReal aabb[6]);                            /* :1481 */
+void dClosestLineSegmentPoints(const dVector3 a1, const dVector3 a2, const dVector3 b1, const dVector3 b2,
+                               dVector3 cp1, dVector3 cp2);              /* :1466 */
+int dBoxTouchesBox(const dVector3 p1, const dMatrix3 R1, const dVector3 side1, const dVector3 p2,
+                   const dMatrix3 R2, const dVector3 side2);             /* :1470 */
 dSpaceID dGeomGetSpace(dGeomID g);                                       /* :283 */
 int dGeomGetClass(dGeomID g);                                            /* :310 */
 /* Category / collide bits and the enabled flag steer a space's pair search;

@@ -2208,6 +2208,13 @@ int collide_hf_gpu(const DevHeightfield& H, const float* d_heights, const GeomVi
   return n;
 }
 
+// dClosestLineSegmentPoints for the ODE API: the colliders' own routine, run
+// on the host (it is __host__ __device__)
+void closest_segment_points_host(const float* a1, const float* a2, const float* b1, const float* b2, float* cp1,
+                                 float* cp2) {
+  closest_segment_points(a1, a2, b1, b2, cp1, cp2);
+}
+
 int collide_pair_gpu(const GeomView& a, const GeomView& b, unsigned flags, Contact* out) {
   Contact* d_c = nullptr;
   int* d_n = nullptr;

@@ -59,6 +59,10 @@ void ctx_destroy(WorldCtx* c);
 // Uploads hw, runs one world step on the GPU, writes the new body state (pos,
 // q, lvel, avel) and the RNG state back into hw. Returns 0 or an ODEGPU_E code.
 int ctx_step(WorldCtx* c, HostWorld& hw);
+// The colliders' closest points of two segments (host side of a
+// __host__ __device__ routine), for dClosestLineSegmentPoints.
+void closest_segment_points_host(const float* a1, const float* a2, const float* b1, const float* b2, float* cp1,
+                                 float* cp2);
 // One dCollide on the GPU. Returns the contact count (<= 8) or a negative code.
 int collide_pair_gpu(const GeomView& a, const GeomView& b, unsigned flags, Contact* out);
 // Heightfields for the ODE API: the dxHeightfieldData caches, the device copy

@@ -1935,6 +1935,45 @@ void dGeomGetAABB(dGeomID g, dReal aabb[6]) {   // collision_kernel.cpp:705-711
   for (int k = 0; k < 6; ++k) aabb[k] = g->aabb[k];
 }
 // collision_kernel.cpp:714-726
+// dClosestLineSegmentPoints (collision_util.cpp:109-209)
+void dClosestLineSegmentPoints(const dVector3 a1, const dVector3 a2, const dVector3 b1, const dVector3 b2,
+                               dVector3 cp1, dVector3 cp2) {
+  og::closest_segment_points_host(a1, a2, b1, b2, cp1, cp2);
+}
+// dBoxTouchesBox (collision_util.cpp:388-449): the fifteen separating axes
+// of two boxes (the three faces of each, the nine edge pairs) after
+// Gottschalk, Lin and Manocha's OBB tree test, in box 1's frame, with
+// R = R1' R2 and Q = |R|
+int dBoxTouchesBox(const dVector3 p1, const dMatrix3 R1, const dVector3 side1, const dVector3 p2,
+                   const dMatrix3 R2, const dVector3 side2) {
+  const dReal p[3] = {p2[0] - p1[0], p2[1] - p1[1], p2[2] - p1[2]};
+  dReal pp[3], A[3], B[3], R[3][3], Q[3][3];
+  for (int i = 0; i < 3; ++i) {
+    pp[i] = R1[i] * p[0] + R1[4 + i] * p[1] + R1[8 + i] * p[2];
+    A[i] = side1[i] * (dReal)0.5;
+    B[i] = side2[i] * (dReal)0.5;
+  }
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      R[i][j] = R1[i] * R2[j] + R1[4 + i] * R2[4 + j] + R1[8 + i] * R2[8 + j];
+      Q[i][j] = std::fabs(R[i][j]);
+    }
+  for (int i = 0; i < 3; ++i)   // box 1's faces
+    if (std::fabs(pp[i]) > A[i] + B[0] * Q[i][0] + B[1] * Q[i][1] + B[2] * Q[i][2]) return 0;
+  for (int j = 0; j < 3; ++j) {   // box 2's faces
+    const dReal d = R2[j] * p[0] + R2[4 + j] * p[1] + R2[8 + j] * p[2];
+    if (std::fabs(d) > A[0] * Q[0][j] + A[1] * Q[1][j] + A[2] * Q[2][j] + B[j]) return 0;
+  }
+  for (int i = 0; i < 3; ++i) {   // edge i of box 1 against edge j of box 2
+    const int a = (i + 1) % 3, b = (i + 2) % 3, m = a < b ? a : b, n = a < b ? b : a;
+    for (int j = 0; j < 3; ++j) {
+      const int k = j == 0 ? 1 : 0, l = j == 2 ? 1 : 2;
+      if (std::fabs(pp[b] * R[a][j] - pp[a] * R[b][j]) > A[m] * Q[n][j] + A[n] * Q[m][j] + B[k] * Q[i][l] + B[l] * Q[i][k])
+        return 0;
+    }
+  }
+  return 1;
+}
 void dInfiniteAABB(dGeomID, dReal aabb[6]) {   // collision_util.cpp:457-465
   for (int k = 0; k < 6; ++k) aabb[k] = (k & 1) ? INFINITY : -INFINITY;
 }

@@ -463,3 +463,48 @@ def test_matrix_helpers_kinematic_bodies_and_orthogonalize_match_reference():
         outs.append(np.array(out, dtype=np.float32))
     assert np.array_equal(outs[0], outs[1]), \
         np.flatnonzero(outs[0] != outs[1])
+
+
+def test_closest_segment_points_and_box_touches_box_match_reference():
+    """dClosestLineSegmentPoints (ode/src/collision_util.cpp:109-209, the
+    colliders' own host-and-device routine) and dBoxTouchesBox (:388-449) on
+    seeded segments and box pairs near contact, against the reference's
+    dSINGLE build: points bit for bit, the boolean exactly."""
+    import ctypes as C
+    import numpy as np
+    import oracle_lib as O
+    if not O.ref_available("s"):
+        pytest.skip("reference not built in this checkout")
+    F, P = C.c_float, C.c_void_p
+    V4, M12 = F * 4, F * 12
+    libs = [C.CDLL(os.path.join(ROOT, "ode-0.12_gb300", "libodegpu.so")),
+            C.CDLL(os.path.join(ROOT, "oracle", "_ref", "libode_ref_s.so"))]
+    for lib in libs:
+        lib.dClosestLineSegmentPoints.argtypes = [P] * 6
+        lib.dBoxTouchesBox.argtypes = [P] * 6
+        lib.dRFromAxisAndAngle.argtypes = [P, F, F, F, F]
+    rng = np.random.default_rng(13)
+    touches = 0
+    for k in range(3000):
+        pts = rng.normal(size=(4, 3)).astype(np.float32)
+        if k % 10 == 0:
+            pts[1] = pts[0]                 # a degenerate segment
+        if k % 10 == 1:
+            pts[3] = pts[2] + (pts[1] - pts[0])   # parallel segments
+        ax = [float(x) for x in rng.normal(size=8)]
+        s1, s2 = rng.uniform(0.2, 1.5, 3), rng.uniform(0.2, 1.5, 3)
+        p2 = rng.normal(size=3) * 1.2
+        res = []
+        for lib in libs:
+            v = [V4(*pts[i], 0.0) for i in range(4)]
+            c1, c2 = V4(), V4()
+            lib.dClosestLineSegmentPoints(v[0], v[1], v[2], v[3], c1, c2)
+            R1, R2 = M12(), M12()
+            lib.dRFromAxisAndAngle(R1, *ax[:4])
+            lib.dRFromAxisAndAngle(R2, *ax[4:])
+            t = lib.dBoxTouchesBox(V4(0.1, -0.2, 0.3, 0), R1, V4(*s1, 0), V4(*p2, 0), R2, V4(*s2, 0))
+            res.append((list(c1)[:3] + list(c2)[:3], t))
+        assert res[0][0] == res[1][0], (k, res)
+        assert res[0][1] == res[1][1], (k, res)
+        touches += res[0][1]
+    assert 300 < touches < 2700, touches
