@@ -232,3 +232,52 @@ def island_program(lib, seed, n_steps=12, stepper="dWorldQuickStep"):
     lib.dWorldDestroy(w)
     return (np.array(seeds, dtype=np.int64), np.array(flags, dtype=np.int64), np.array(states, dtype=np.float64),
             np.array(moved, dtype=np.int64), np.array(kept, dtype=np.float64))
+
+
+def kinematic_program(lib, seed, n_steps=20, stepper="dWorldQuickStep"):
+    """A kinematic box (ode.cpp:834-852: zero inverse mass and inertia) moving
+    and spinning at set velocities, a dynamic box hanging on it by a ball
+    joint under gravity, and a second dynamic box on a ground contact. The
+    kinematic body keeps its velocities and moves by them; the others follow.
+    Returns the IsKinematic answers and the states after each step."""
+    rng = np.random.default_rng(seed)
+    lib.dInitODE2(0)
+    for n in ("dBodySetKinematic", "dBodySetDynamic", "dBodyIsKinematic"):
+        getattr(lib, n).argtypes = [P]
+    w = lib.dWorldCreate()
+    lib.dWorldSetGravity(w, 0.0, 0.0, -9.81)
+    b = []
+    for k in range(3):
+        bb = lib.dBodyCreate(w)
+        m = Mass()
+        lib.dMassSetBox(C.byref(m), 1.0, *(float(x) for x in rng.uniform(0.3, 0.8, 3)))
+        lib.dBodySetMass(bb, C.byref(m))
+        lib.dBodySetPosition(bb, float(k), 0.0, 1.0 + 0.5 * k)
+        b.append(bb)
+    got = [lib.dBodyIsKinematic(b[0])]
+    lib.dBodySetKinematic(b[0])
+    lib.dBodySetLinearVel(b[0], 1.0, 0.2, 0.0)
+    lib.dBodySetAngularVel(b[0], 0.0, 0.0, 0.5)
+    lib.dBodySetKinematic(b[2])
+    lib.dBodySetDynamic(b[2])                  # back to its mass
+    got += [lib.dBodyIsKinematic(b[0]), lib.dBodyIsKinematic(b[2])]
+    j = lib.dJointCreateBall(w, None)
+    lib.dJointAttach(j, b[0], b[1])
+    lib.dJointSetBallAnchor(j, 0.5, 0.0, 1.25)
+    grp = lib.dJointGroupCreate(0)
+    states = []
+    for _ in range(n_steps):
+        lib.dJointGroupEmpty(grp)
+        c = Contact()
+        c.surface.mu = 0.5
+        p = lib.dBodyGetPosition(b[2])
+        c.geom.pos[0], c.geom.pos[1], c.geom.pos[2] = p[0], p[1], p[2] - 0.2
+        c.geom.normal[2] = 1.0
+        c.geom.depth = 0.02
+        jc = lib.dJointCreateContact(w, grp, C.byref(c))
+        lib.dJointAttach(jc, b[2], b[0])       # a contact with the kinematic body too
+        getattr(lib, stepper)(w, 0.01)
+        states.append([state(lib, bb) for bb in b])
+    lib.dJointGroupDestroy(grp)
+    lib.dWorldDestroy(w)
+    return np.array(got, dtype=np.int64), np.array(states, dtype=np.float64)

@@ -553,6 +553,10 @@ def make_body_step_options(seeds=(1, 2, 3), n_steps=30):
             r = BP.island_program(BP.bind_islands(lib), s, 12, st)
             for k, v in zip(("seeds", "enabled", "states", "moved", "kept_force"), r):
                 out[f"islands_{st}_{s}_{k}"] = v
+    for st in ("dWorldQuickStep", "dWorldStep"):
+        for s in seeds:
+            k, x = BP.kinematic_program(BP.bind_islands(lib), s, 20, st)
+            out[f"kinematic_{st}_{s}_flags"], out[f"kinematic_{st}_{s}_states"] = k, x
     np.savez_compressed(os.path.join(HERE, "body_step_options.npz"), **out)
 
 

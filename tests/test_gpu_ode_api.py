@@ -331,6 +331,25 @@ def test_disabled_bodies_and_null_joints_match_reference(stepper):
         assert err.max() <= 1e-4, (int(s), float(err.max()))
 
 
+@pytest.mark.parametrize("stepper", ["dWorldQuickStep", "dWorldStep"])
+def test_kinematic_bodies_match_reference(stepper):
+    """A kinematic body (zero inverse mass and inertia, ode.cpp:834-852) in a
+    ball joint and a contact, stepped on the GPU, against the reference's
+    dSINGLE build over 20 steps (tests/body_step_program.py
+    kinematic_program): the kinematic body moves by its set velocities
+    untouched by gravity or constraints, the others follow; states within
+    1e-4 (1 + |x|), IsKinematic answers exactly."""
+    import body_step_program as BP
+    g = np.load(os.path.join(GOLDEN, "body_step_options.npz"))
+    L = BP.bind_islands(C.CDLL(os.path.join(os.path.dirname(GOLDEN), "..", "ode-0.12_gb300", "libodegpu.so")))
+    for s in g["seeds"]:
+        flags, states = BP.kinematic_program(L, int(s), 20, stepper)
+        assert np.array_equal(flags, g[f"kinematic_{stepper}_{s}_flags"])
+        want = g[f"kinematic_{stepper}_{s}_states"]
+        err = np.abs(states - want) / (1.0 + np.abs(want))
+        assert err.max() <= 1e-4, (int(s), float(err.max()), np.unravel_index(np.argmax(err), err.shape))
+
+
 class JointFeedback(C.Structure):
     _fields_ = [("f1", C.c_float * 4), ("t1", C.c_float * 4), ("f2", C.c_float * 4), ("t2", C.c_float * 4)]
 
