@@ -20,6 +20,13 @@
  *    pipeline of odegpu.h with the caller's contacts, joint feedback
  *    included. dWorldStep is available on the first path only: for a larger
  *    world it returns 0.
+ *  - Spaces, geom placement, auto-disable and the other bookkeeping run on
+ *    the host as in ODE (same pair order, same island order); moved
+ *    callbacks run after the whole step rather than body by body, and a
+ *    heightfield's height callback is sampled once when the data is built.
+ *  - Not built: sweep-and-prune and quadtree spaces, trimesh, convex, geom
+ *    transforms, user geom classes, and the LMotor, PR, PU, piston and
+ *    plane-2D joints.
  */
 #ifndef ODE_GPU_H
 #define ODE_GPU_H
