@@ -25,8 +25,7 @@
  *    callbacks run after the whole step rather than body by body, and a
  *    heightfield's height callback is sampled once when the data is built.
  *  - Not built: sweep-and-prune and quadtree spaces, trimesh, convex, geom
- *    transforms, user geom classes, and the LMotor, PR, PU, piston and
- *    plane-2D joints.
+ *    transforms, and the LMotor, PR, PU, piston and plane-2D joints.
  */
 #ifndef ODE_GPU_H
 #define ODE_GPU_H
@@ -456,6 +455,22 @@ int dCollide(dGeomID o1, dGeomID o2, int flags, dContactGeom* contact, int skip)
  * built-in one; dCloseODE drops the overrides. */
 typedef int dColliderFn(dGeomID o1, dGeomID o2, int flags, dContactGeom* contact, int skip);  /* :1488 */
 void dSetColliderOverride(int i, int j, dColliderFn* fn);                /* :1514 */
+/* User geom classes (at most four): their colliders, boxes and box tests are
+ * the caller's host functions. */
+typedef void dGetAABBFn(dGeomID g, dReal aabb[6]);                       /* :1487 */
+typedef dColliderFn* dGetColliderFnFn(int num);                          /* :1490 */
+typedef void dGeomDtorFn(dGeomID o);                                     /* :1491 */
+typedef int dAABBTestFn(dGeomID o1, dGeomID o2, dReal aabb[6]);          /* :1492 */
+typedef struct dGeomClass {
+  int bytes;
+  dGetColliderFnFn* collider;
+  dGetAABBFn* aabb;
+  dAABBTestFn* aabb_test;
+  dGeomDtorFn* dtor;
+} dGeomClass;                                                            /* :1494-1500 */
+int dCreateGeomClass(const dGeomClass* classptr);                        /* :1502 */
+void* dGeomGetClassData(dGeomID g);                                      /* :1503 */
+dGeomID dCreateGeom(int classnum);                                       /* :1504 */
 dGeomID dCreateSphere(dSpaceID space, dReal radius);                     /* :924 */
 dGeomID dCreateBox(dSpaceID space, dReal lx, dReal ly, dReal lz);        /* :1002 */
 dGeomID dCreatePlane(dSpaceID space, dReal a, dReal b, dReal c, dReal d); /* :1046 */

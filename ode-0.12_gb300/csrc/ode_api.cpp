@@ -10,6 +10,7 @@
 #include <algorithm>
 #include <climits>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <unordered_map>
@@ -104,6 +105,7 @@ struct dxGeom {
   dReal opos[4], oR[12];     // the offset (body frame)
   dReal fpos[4], fR[12];     // an offset geom's own final pose, recomputed on every read
   dxGeom* body_next;         // next geom on the same body
+  void* class_data;          // a user class's zeroed block (dGeomGetClassData)
   // space membership (collision_kernel.h:150-171, collision_space.cpp:162-205):
   // the parent space, the intrusive list link, and the GEOM_DIRTY /
   // GEOM_AABB_BAD flags with the cached box they guard
@@ -129,6 +131,7 @@ static bool is_space(const dxGeom* g) { return g->type >= dFirstSpaceClass && g-
 extern "C" {
 static void body_geoms_moved(dxBody* b);
 static void body_geoms_detach(dxBody* b);
+static const dGeomClass* user_class_of(const dxGeom* g);
 }
 
 // dxGeom::gflags bits of a ray (ode/src/collision_kernel.h: RAY_FIRSTCONTACT,
@@ -280,25 +283,54 @@ void joint_anchor(const dxJoint* j, bool second, dVector3 r) {
 
 extern "C" {
 
-// Collider overrides (dSetColliderOverride, collision_kernel.cpp:275-285):
-// a caller's function for a class pair, called on the host in place of the
-// built-in collider; (i, j) calls it as given and (j, i) with the geoms
-// swapped, so for i == j the swapped entry is the one that stays
+// The collider table of collision_kernel.cpp:142-285 for what the caller can
+// change in it: every class pair starts on the built-in colliders (the GPU);
+// a user geom class routes its pairs that hold no collider yet to a
+// first-call resolution through the class's collider getter;
+// dSetColliderOverride puts the caller's function in, over what was there.
+// Setting (i, j) also sets (j, i) with the geoms swapped, so for an override
+// of i == j the swapped entry is the one that stays.
 namespace {
-constexpr int kGeomClasses = 18;   // dGeomNumClasses of ODE 0.12
-struct ColliderOverride { dColliderFn* fn; int reverse; int set; };
-ColliderOverride g_override[kGeomClasses][kGeomClasses];
+constexpr int kGeomClasses = 18;                 // dGeomNumClasses of ODE 0.12
+constexpr int kFirstUserClass = 14, kMaxUserClasses = 4;
+enum { kColliderBuiltin = 0, kColliderUser = 1, kColliderFn = 2 };
+struct ColliderEntry { int kind; dColliderFn* fn; int reverse; };
+ColliderEntry g_colliders[kGeomClasses][kGeomClasses];
+dGeomClass g_user_classes[kMaxUserClasses];
+int g_num_user_classes = 0;
+void set_collider(int i, int j, int kind, dColliderFn* fn) {   // setCollider
+  g_colliders[i][j] = {kind, fn, 0};
+  g_colliders[j][i] = {kind, fn, 1};
+}
+bool is_user_class(int t) { return t >= kFirstUserClass && t < kFirstUserClass + g_num_user_classes; }
 }  // namespace
 void dSetColliderOverride(int i, int j, dColliderFn* fn) {
   if (i < 0 || j < 0 || i >= kGeomClasses || j >= kGeomClasses) return;
-  g_override[i][j] = {fn, 0, 1};
-  g_override[j][i] = {fn, 1, 1};
+  set_collider(i, j, kColliderFn, fn);
+}
+// dCreateGeomClass (collision_kernel.cpp:975-990): at most four classes
+int dCreateGeomClass(const dGeomClass* c) {
+  if (!c || c->bytes < 0 || !c->collider || !c->aabb || g_num_user_classes >= kMaxUserClasses) return -1;
+  g_user_classes[g_num_user_classes] = *c;
+  const int cls = kFirstUserClass + g_num_user_classes;
+  // setAllColliders (:162-166) through setCollider (:148-159), which writes
+  // only entries that hold no collider yet
+  auto empty = [](const ColliderEntry& e) { return e.kind == kColliderBuiltin || (e.kind == kColliderFn && !e.fn); };
+  for (int j = 0; j < kGeomClasses; ++j) {
+    if (empty(g_colliders[cls][j])) g_colliders[cls][j] = {kColliderUser, nullptr, 0};
+    if (empty(g_colliders[j][cls])) g_colliders[j][cls] = {kColliderUser, nullptr, 1};
+  }
+  ++g_num_user_classes;
+  return cls;
 }
 void dInitODE(void) {}
 int dInitODE2(unsigned int) { return 1; }
-// dCloseODE drops the overrides, as the reference's next initialisation
-// rebuilds its collider table (collision_kernel.cpp:167-273)
-void dCloseODE(void) { std::memset(g_override, 0, sizeof(g_override)); }
+// dCloseODE forgets the user classes and the caller's colliders, as the
+// reference's does (odeinit.cpp:360-361)
+void dCloseODE(void) {
+  std::memset(g_colliders, 0, sizeof(g_colliders));
+  g_num_user_classes = 0;
+}
 // Per-thread data and step working memory (odeinit.cpp:515-530,
 // objects.h:157-289): the GPU path keeps its own device buffers per world, so
 // these accept their arguments and have nothing to do.
@@ -1498,6 +1530,10 @@ void dGeomDestroy(dGeomID g) {
       else space_remove(sp, c);
     }
   }
+  if (const dGeomClass* uc = user_class_of(g)) {   // ~dxUserGeom: the class's destructor, then its block
+    if (uc->dtor) uc->dtor(g);
+    std::free(g->class_data);
+  }
   if (g->space) space_remove(g->space, g);
   body_list_remove(g);
   if (is_space(g)) delete static_cast<dxSpace*>(g);
@@ -1821,6 +1857,10 @@ void dGeomGetQuaternion(dGeomID g, dQuaternion q) {   // :687-703
 static void recompute_aabb(dxGeom* g);
 static void compute_aabb(dxGeom* g, dReal* aabb) {
   const float inf = INFINITY;
+  if (const dGeomClass* uc = user_class_of(g)) {
+    uc->aabb(g, aabb);
+    return;
+  }
   if (is_space(g)) {
     const auto* sp = static_cast<const dxSpace*>(g);
     if (!sp->first) {
@@ -2155,6 +2195,22 @@ dReal dGeomCapsulePointDepth(dGeomID g, dReal x, dReal y, dReal z) {
   return (dReal)g->p[0] - std::sqrt((x - c[0]) * (x - c[0]) + (y - c[1]) * (y - c[1]) + (z - c[2]) * (z - c[2]));
 }
 
+// User geoms (collision_kernel.cpp:900-938, :993-1012): placeable, in no
+// space, with a zeroed block of the class's size; the class gives the box, an
+// optional box test for space pairs and a destructor
+dGeomID dCreateGeom(int classnum) {
+  if (!is_user_class(classnum)) return nullptr;
+  const double p[4] = {0, 0, 0, 0};
+  dGeomID g = new_geom(nullptr, classnum, p);
+  const int bytes = g_user_classes[classnum - kFirstUserClass].bytes;
+  g->class_data = std::calloc(1, bytes > 0 ? (size_t)bytes : 1);
+  return g;
+}
+void* dGeomGetClassData(dGeomID g) { return g && is_user_class(g->type) ? g->class_data : nullptr; }
+static const dGeomClass* user_class_of(const dxGeom* g) {
+  return is_user_class(g->type) ? &g_user_classes[g->type - kFirstUserClass] : nullptr;
+}
+
 // ---------------------------------------------------------------- spaces (API)
 // Simple and hash spaces (collision_space.cpp:210-604) on the host: they only
 // enumerate candidate pairs for the caller's near-callback, which calls
@@ -2173,14 +2229,18 @@ static dSpaceID new_space(dSpaceID parent, int type) {
   return sp;
 }
 static bool geom_enabled(const dxGeom* g) { return g->enabled && !g->zero_sized; }   // GEOM_ENABLED
-// collideAABBs (collision_space_internal.h:48-82); every class on this path
-// keeps the default AABBTest, which always passes
+// collideAABBs (collision_space_internal.h:48-82)
 static void collide_aabbs(dxGeom* g1, dxGeom* g2, void* data, dNearCallback* cb) {
   if (g1->body == g2->body && g1->body) return;
   if (((g1->category_bits & g2->collide_bits) || (g2->category_bits & g1->collide_bits)) == 0) return;
   const dReal* a = g1->aabb;
   const dReal* b = g2->aabb;
   if (a[0] > b[1] || a[1] < b[0] || a[2] > b[3] || a[3] < b[2] || a[4] > b[5] || a[5] < b[4]) return;
+  // a user class may prove the boxes apart (dxUserGeom::AABBTest)
+  const dGeomClass* u1 = user_class_of(g1);
+  const dGeomClass* u2 = user_class_of(g2);
+  if (u1 && u1->aabb_test && u1->aabb_test(g1, g2, g2->aabb) == 0) return;
+  if (u2 && u2->aabb_test && u2->aabb_test(g2, g1, g1->aabb) == 0) return;
   cb(data, g1, g2);
 }
 // cleanGeoms (collision_space.cpp:229-242, :390-402): boxes of the dirty
@@ -2396,19 +2456,39 @@ int dCollide(dGeomID o1, dGeomID o2, int flags, dContactGeom* contact, int skip)
   if (o1 == o2) return 0;
   if (o1->body == o2->body && o1->body) return 0;
   if (o1->type >= 0 && o1->type < kGeomClasses && o2->type >= 0 && o2->type < kGeomClasses &&
-      g_override[o1->type][o2->type].set) {
-    // the caller's collider (collision_kernel.cpp:313-336); a reversed entry
-    // swaps the geoms and then flips normals, geoms and sides back
-    const ColliderOverride& ov = g_override[o1->type][o2->type];
-    if (!ov.fn) return 0;
-    if (!ov.reverse) return ov.fn(o1, o2, flags, contact, skip);
-    const int n = ov.fn(o2, o1, flags, contact, skip);
-    for (int i = 0; i < n; ++i) {
-      dContactGeom* c = (dContactGeom*)((char*)contact + (size_t)i * skip);
-      for (int k = 0; k < 3; ++k) c->normal[k] = -c->normal[k];
-      std::swap(c->g1, c->g2);
-      std::swap(c->side1, c->side2);
+      g_colliders[o1->type][o2->type].kind != kColliderBuiltin) {
+    // a caller's collider or a user class (collision_kernel.cpp:313-336); a
+    // reversed entry swaps the geoms and then flips normals, geoms and sides
+    // back
+    const ColliderEntry e = g_colliders[o1->type][o2->type];
+    dxGeom* a = e.reverse ? o2 : o1;
+    dxGeom* b = e.reverse ? o1 : o2;
+    int n;
+    if (e.kind == kColliderUser) {
+      // dCollideUserGeomWithGeom (:940-972): the user geom's class names the
+      // collider for the other class, or else the other user class for it;
+      // the answer is kept in the table and the pair goes round again
+      const int t1 = a->type, t2 = b->type;
+      dColliderFn* fn = g_user_classes[t1 - kFirstUserClass].collider(t2);
+      int rev = 0;
+      if (!fn && is_user_class(t2)) {
+        fn = g_user_classes[t2 - kFirstUserClass].collider(t1);
+        rev = 1;
+      }
+      g_colliders[t1][t2] = {kColliderFn, fn, rev};
+      g_colliders[t2][t1] = {kColliderFn, fn, !rev};
+      n = dCollide(a, b, flags, contact, skip);
+    } else {
+      if (!e.fn) return 0;
+      n = e.fn(a, b, flags, contact, skip);
     }
+    if (e.reverse)
+      for (int i = 0; i < n; ++i) {
+        dContactGeom* c = (dContactGeom*)((char*)contact + (size_t)i * skip);
+        for (int k = 0; k < 3; ++k) c->normal[k] = -c->normal[k];
+        std::swap(c->g1, c->g2);
+        std::swap(c->side1, c->side2);
+      }
     return n;
   }
   if (is_space(o1) || is_space(o2)) return 0;   // no collider takes a space

@@ -447,3 +447,111 @@ def test_collider_override_matches_reference():
         outs.append(np.array(out, dtype=np.float32))
     assert np.array_equal(outs[0], outs[1]), (outs[0], outs[1])
     assert outs[0][0] == 2 and outs[0][-1] == 0
+
+
+def test_user_geom_classes_match_reference():
+    """dCreateGeomClass / dCreateGeom / dGeomGetClassData (collision_kernel.cpp:
+    900-1012): the class's collider getter resolved on a pair's first
+    dCollide, from the other user class when the first has none, the caller's
+    box and box test used by a space's pair search, the destructor on
+    dGeomDestroy, all as in the reference's dSINGLE build."""
+    ours, ref = _libs()
+
+    class CG(C.Structure):
+        _fields_ = [("pos", F * 4), ("normal", F * 4), ("depth", F), ("g1", P), ("g2", P), ("side1", I),
+                    ("side2", I)]
+
+    FN = C.CFUNCTYPE(I, P, P, I, P, I)
+    GET = C.CFUNCTYPE(P, I)
+    AABB = C.CFUNCTYPE(None, P, C.POINTER(F))
+    TEST = C.CFUNCTYPE(I, P, P, C.POINTER(F))
+    DTOR = C.CFUNCTYPE(None, P)
+
+    class GeomClass(C.Structure):
+        _fields_ = [("bytes", I), ("collider", GET), ("aabb", AABB), ("aabb_test", TEST), ("dtor", DTOR)]
+
+    outs = []
+    for lib in (ours, ref):
+        lib.dInitODE2.argtypes = [C.c_uint]
+        lib.dInitODE2(0)
+        for n in ("dCreateGeomClass",):
+            getattr(lib, n).argtypes = [P]
+        lib.dCreateGeom.restype = lib.dGeomGetClassData.restype = P
+        lib.dCreateGeom.argtypes = [I]
+        lib.dGeomGetClassData.argtypes = [P]
+        lib.dCollide.argtypes = [P, P, I, P, I]
+        lib.dSimpleSpaceCreate.restype = P
+        lib.dSimpleSpaceCreate.argtypes = [P]
+        lib.dSpaceAdd.argtypes = [P, P]
+        NEAR = C.CFUNCTYPE(None, P, P, P)
+        lib.dSpaceCollide.argtypes = [P, P, NEAR]
+        lib.dSpaceDestroy.argtypes = [P]
+        ids, log = {}, []
+
+        def mk_fn(tag):
+            def fn(o1, o2, flags, contact, skip):
+                log.append((tag, ids[o1], ids[o2]))
+                c = CG.from_address(contact)
+                c.pos[0], c.pos[1], c.pos[2] = float(tag), 0.5, 0.25
+                c.normal[0], c.normal[1], c.normal[2] = 0.0, 0.6, 0.8
+                c.depth = 0.125
+                c.g1, c.g2, c.side1, c.side2 = o1, o2, 3, 4
+                return 1
+            return fn
+
+        fn_sphere, fn_self = FN(mk_fn(1)), FN(mk_fn(2))
+        keep = [fn_sphere, fn_self]
+
+        def getter(num):
+            log.append(("get", num))
+            if num == dSphereClass:
+                return C.cast(fn_sphere, P).value
+            if num >= 14:
+                return C.cast(fn_self, P).value
+            return None
+
+        def aabb(g, out):
+            p = lib.dGeomGetPosition(g)
+            r = C.cast(lib.dGeomGetClassData(g), C.POINTER(F))[0]
+            for k in range(3):
+                out[2 * k], out[2 * k + 1] = p[k] - r, p[k] + r
+
+        def test(g1, g2, box):
+            return 0 if lib.dGeomGetClass(g2) == dBoxClass else 1
+
+        def dtor(g):
+            log.append(("dtor", ids[g]))
+
+        gc = GeomClass(8, GET(getter), AABB(aabb), TEST(test), DTOR(dtor))
+        keep += [gc]
+        cls = lib.dCreateGeomClass(C.byref(gc))
+        sp = lib.dSimpleSpaceCreate(None)
+        u1, u2 = lib.dCreateGeom(cls), lib.dCreateGeom(cls)
+        s = lib.dCreateSphere(sp, 0.5)
+        b = lib.dCreateBox(sp, 1.0, 1.0, 1.0)
+        for k, g in enumerate((u1, u2, s, b)):
+            ids[g] = k
+        for g, pos, r in ((u1, (0.0, 0.0, 0.0), 0.6), (u2, (0.8, 0.0, 0.0), 0.5)):
+            C.cast(lib.dGeomGetClassData(g), C.POINTER(F))[0] = r
+            lib.dGeomSetPosition(g, *pos)
+            lib.dSpaceAdd(sp, g)
+        lib.dGeomSetPosition(s, 0.3, 0.3, 0.0)
+        lib.dGeomSetPosition(b, -0.4, 0.0, 0.2)
+        out = [cls, lib.dGeomGetClass(u1)]
+        for o1, o2 in ((u1, s), (s, u1), (u1, u2), (u2, u1), (u1, b), (b, u2)):
+            buf = (CG * 2)()
+            n = lib.dCollide(o1, o2, 2, buf, C.sizeof(CG))
+            out += [n] + ([] if n == 0 else list(buf[0].pos)[:3] + list(buf[0].normal)[:3] +
+                          [ids[buf[0].g1], ids[buf[0].g2], buf[0].side1, buf[0].side2])
+        out += _aabb(lib, u1)
+        pairs = []
+        near = NEAR(lambda d, a, c: pairs.append((ids[a], ids[c])))
+        lib.dSpaceCollide(sp, None, near)
+        out += [x for pr in pairs for x in pr]
+        lib.dGeomDestroy(u1)
+        lib.dSpaceDestroy(sp)
+        lib.dCloseODE()
+        lib.dInitODE2(0)
+        outs.append((np.array(out, dtype=np.float32), log))
+    assert np.array_equal(outs[0][0], outs[1][0]), (outs[0][0], outs[1][0])
+    assert outs[0][1] == outs[1][1], (outs[0][1], outs[1][1])
