@@ -31,6 +31,7 @@
 #define ODE_GPU_H
 
 #include <stddef.h>
+#include <stdio.h>
 
 #ifdef __cplusplus
 extern "C" {
@@ -443,6 +444,7 @@ void dNormalize4(dVector4 a);                                            /* :427
 void dPlaneSpace(const dVector3 n, dVector3 p, dVector3 q);              /* :462 */
 void dOrthogonalizeR(dMatrix3 m);                                        /* :464 */
 /* include/ode/misc.h: matrices with rows padded to a multiple of 4 */
+void dPrintMatrix(const dReal* A, int n, int m, const char* fmt, FILE* f);  /* misc.h:61 */
 void dMakeRandomVector(dReal* A, int n, dReal range);                    /* misc.h:65 */
 void dMakeRandomMatrix(dReal* A, int n, int m, dReal range);             /* :68 */
 void dClearUpperTriangle(dReal* A, int n);                               /* :71 */
@@ -537,6 +539,8 @@ void dGeomGetQuaternion(dGeomID g, dQuaternion result);                  /* :245
 void dGeomGetAABB(dGeomID g, dReal aabb[6]);                             /* :264 */
 int dGeomIsSpace(dGeomID g);                                             /* :273 */
 void dInfiniteAABB(dGeomID g, dReal aabb[6]);                            /* :1481 */
+enum { dGeomCommonControlClass = 0, dGeomColliderControlClass = 1 };     /* :412-415 */
+int dGeomLowLevelControl(dGeomID g, int controlClass, int controlCode, void* dataValue, int* dataSize);  /* :460 */
 void dClosestLineSegmentPoints(const dVector3 a1, const dVector3 a2, const dVector3 b1, const dVector3 b2,
                                dVector3 cp1, dVector3 cp2);              /* :1466 */
 int dBoxTouchesBox(const dVector3 p1, const dMatrix3 R1, const dVector3 side1, const dVector3 p2,

@@ -10,6 +10,7 @@
 #include <algorithm>
 #include <climits>
 #include <cmath>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <string>
@@ -2017,6 +2018,13 @@ int dBoxTouchesBox(const dVector3 p1, const dMatrix3 R1, const dVector3 side1, c
 void dInfiniteAABB(dGeomID, dReal aabb[6]) {   // collision_util.cpp:457-465
   for (int k = 0; k < 6; ++k) aabb[k] = (k & 1) ? INFINITY : -INFINITY;
 }
+// dGeomLowLevelControl (collision_kernel.cpp:877-889): only trimeshes take
+// controls in ODE 0.12; every class here answers none
+int dGeomLowLevelControl(dGeomID g, int, int, void*, int* dataSize) {
+  if (!g || !dataSize) return 0;
+  *dataSize = 0;
+  return 0;
+}
 int dGeomIsSpace(dGeomID g) { return is_space(g) ? 1 : 0; }
 dSpaceID dGeomGetSpace(dGeomID g) { return g->space; }
 int dGeomGetClass(dGeomID g) { return g->type; }
@@ -3277,6 +3285,13 @@ dReal dRandReal(void) { return (dReal)dRand() / (dReal)0xffffffffUL; }
 // Matrix helpers of ode/src/misc.cpp:139-195 over row-padded matrices
 // (rows of dPAD(columns) entries, include/ode/common.h:136)
 static int pad4(int a) { return a > 1 ? ((a - 1) | 3) + 1 : a; }
+void dPrintMatrix(const dReal* A, int n, int m, const char* fmt, FILE* f) {   // misc.cpp:128-136
+  const int skip = pad4(m);
+  for (int i = 0; i < n; ++i) {
+    for (int j = 0; j < m; ++j) std::fprintf(f, fmt, A[(size_t)i * skip + j]);
+    std::fprintf(f, "\n");
+  }
+}
 void dMakeRandomVector(dReal* A, int n, dReal range) {
   for (int i = 0; i < n; ++i) A[i] = (dRandReal() * (dReal)2.0 - (dReal)1.0) * range;
 }

@@ -508,3 +508,29 @@ def test_closest_segment_points_and_box_touches_box_match_reference():
         assert res[0][1] == res[1][1], (k, res)
         touches += res[0][1]
     assert 300 < touches < 2700, touches
+
+
+def test_print_matrix_writes_what_the_reference_writes(tmp_path):
+    """dPrintMatrix (ode/src/misc.cpp:128-136): padded rows, the caller's
+    format, one line per row, byte for byte as the reference's."""
+    import ctypes as C
+    import oracle_lib as O
+    if not O.ref_available("s"):
+        pytest.skip("reference not built in this checkout")
+    libc = C.CDLL(None)
+    libc.fopen.restype = C.c_void_p
+    libc.fopen.argtypes = [C.c_char_p, C.c_char_p]
+    libc.fclose.argtypes = [C.c_void_p]
+    A = (C.c_float * 16)(*[0.5 * k - 2.25 for k in range(16)])   # 2 rows padded to 8
+    texts = []
+    for name, path in (("ours", os.path.join(ROOT, "ode-0.12_gb300", "libodegpu.so")),
+                       ("ref", os.path.join(ROOT, "oracle", "_ref", "libode_ref_s.so"))):
+        lib = C.CDLL(path)
+        lib.dPrintMatrix.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_char_p, C.c_void_p]
+        out = str(tmp_path / f"{name}.txt")
+        f = libc.fopen(out.encode(), b"w")
+        lib.dPrintMatrix(A, 3, 3, b"%10.4f ", f)
+        lib.dPrintMatrix(A, 2, 5, b"%g,", f)
+        libc.fclose(f)
+        texts.append(open(out).read())
+    assert texts[0] == texts[1] and texts[0].count("\n") == 5, texts
