@@ -24,8 +24,8 @@
  *    the host as in ODE (same pair order, same island order); moved
  *    callbacks run after the whole step rather than body by body, and a
  *    heightfield's height callback is sampled once when the data is built.
- *  - Not built: sweep-and-prune and quadtree spaces, trimesh, convex, geom
- *    transforms, and the LMotor, PR, PU, piston and plane-2D joints.
+ *  - Not built: sweep-and-prune and quadtree spaces, trimesh, convex, and
+ *    the LMotor, PR, PU, piston and plane-2D joints.
  */
 #ifndef ODE_GPU_H
 #define ODE_GPU_H
@@ -473,6 +473,14 @@ typedef struct dGeomClass {
 int dCreateGeomClass(const dGeomClass* classptr);                        /* :1502 */
 void* dGeomGetClassData(dGeomID g);                                      /* :1503 */
 dGeomID dCreateGeom(int classnum);                                       /* :1504 */
+/* Geom transforms: the wrapped geom collides at the transform's pose. */
+dGeomID dCreateGeomTransform(dSpaceID space);                            /* :1086 */
+void dGeomTransformSetGeom(dGeomID g, dGeomID obj);                      /* :1087 */
+dGeomID dGeomTransformGetGeom(dGeomID g);                                /* :1088 */
+void dGeomTransformSetCleanup(dGeomID g, int mode);                      /* :1089 */
+int dGeomTransformGetCleanup(dGeomID g);                                 /* :1090 */
+void dGeomTransformSetInfo(dGeomID g, int mode);                         /* :1091 */
+int dGeomTransformGetInfo(dGeomID g);                                    /* :1092 */
 dGeomID dCreateSphere(dSpaceID space, dReal radius);                     /* :924 */
 dGeomID dCreateBox(dSpaceID space, dReal lx, dReal ly, dReal lz);        /* :1002 */
 dGeomID dCreatePlane(dSpaceID space, dReal a, dReal b, dReal c, dReal d); /* :1046 */

@@ -107,6 +107,12 @@ struct dxGeom {
   dReal fpos[4], fR[12];     // an offset geom's own final pose, recomputed on every read
   dxGeom* body_next;         // next geom on the same body
   void* class_data;          // a user class's zeroed block (dGeomGetClassData)
+  // geom transforms (collision_transform.cpp): the wrapped geom, its
+  // cleanup and info modes, and its final pose as last computed
+  dxGeom* tobj;
+  int tcleanup, tinfo;
+  dReal tpos[4], tR[12];
+  const dReal *ovr_pos, *ovr_R;   // set while a transform collides or boxes this geom
   // space membership (collision_kernel.h:150-171, collision_space.cpp:162-205):
   // the parent space, the intrusive list link, and the GEOM_DIRTY /
   // GEOM_AABB_BAD flags with the cached box they guard
@@ -294,7 +300,7 @@ extern "C" {
 namespace {
 constexpr int kGeomClasses = 18;                 // dGeomNumClasses of ODE 0.12
 constexpr int kFirstUserClass = 14, kMaxUserClasses = 4;
-enum { kColliderBuiltin = 0, kColliderUser = 1, kColliderFn = 2 };
+enum { kColliderBuiltin = 0, kColliderUser = 1, kColliderFn = 2, kColliderTransform = 3 };
 struct ColliderEntry { int kind; dColliderFn* fn; int reverse; };
 ColliderEntry g_colliders[kGeomClasses][kGeomClasses];
 dGeomClass g_user_classes[kMaxUserClasses];
@@ -304,14 +310,29 @@ void set_collider(int i, int j, int kind, dColliderFn* fn) {   // setCollider
   g_colliders[j][i] = {kind, fn, 1};
 }
 bool is_user_class(int t) { return t >= kFirstUserClass && t < kFirstUserClass + g_num_user_classes; }
+// dInitColliders (collision_kernel.cpp:167-268) for the entries that are not
+// the GPU's: a geom transform pairs with every class through its own
+// collider, (T, T) unswapped
+bool g_colliders_ready = false;
+void colliders_init() {
+  if (g_colliders_ready) return;
+  g_colliders_ready = true;
+  const int T = dGeomTransformClass;
+  for (int j = 0; j < kGeomClasses; ++j) {
+    if (g_colliders[T][j].kind == kColliderBuiltin) g_colliders[T][j] = {kColliderTransform, nullptr, 0};
+    if (g_colliders[j][T].kind == kColliderBuiltin) g_colliders[j][T] = {kColliderTransform, nullptr, 1};
+  }
+}
 }  // namespace
 void dSetColliderOverride(int i, int j, dColliderFn* fn) {
   if (i < 0 || j < 0 || i >= kGeomClasses || j >= kGeomClasses) return;
+  colliders_init();
   set_collider(i, j, kColliderFn, fn);
 }
 // dCreateGeomClass (collision_kernel.cpp:975-990): at most four classes
 int dCreateGeomClass(const dGeomClass* c) {
   if (!c || c->bytes < 0 || !c->collider || !c->aabb || g_num_user_classes >= kMaxUserClasses) return -1;
+  colliders_init();
   g_user_classes[g_num_user_classes] = *c;
   const int cls = kFirstUserClass + g_num_user_classes;
   // setAllColliders (:162-166) through setCollider (:148-159), which writes
@@ -324,13 +345,17 @@ int dCreateGeomClass(const dGeomClass* c) {
   ++g_num_user_classes;
   return cls;
 }
-void dInitODE(void) {}
-int dInitODE2(unsigned int) { return 1; }
+void dInitODE(void) { colliders_init(); }
+int dInitODE2(unsigned int) {
+  colliders_init();
+  return 1;
+}
 // dCloseODE forgets the user classes and the caller's colliders, as the
 // reference's does (odeinit.cpp:360-361)
 void dCloseODE(void) {
   std::memset(g_colliders, 0, sizeof(g_colliders));
   g_num_user_classes = 0;
+  g_colliders_ready = false;
 }
 // Per-thread data and step working memory (odeinit.cpp:515-530,
 // objects.h:157-289): the GPU path keeps its own device buffers per world, so
@@ -1531,6 +1556,7 @@ void dGeomDestroy(dGeomID g) {
       else space_remove(sp, c);
     }
   }
+  if (g->type == dGeomTransformClass && g->tobj && g->tcleanup) dGeomDestroy(g->tobj);   // ~dxGeomTransform
   if (const dGeomClass* uc = user_class_of(g)) {   // ~dxUserGeom: the class's destructor, then its block
     if (uc->dtor) uc->dtor(g);
     std::free(g->class_data);
@@ -1727,12 +1753,24 @@ static void geom_recompute(dxGeom* g) {
   mul0_333(g->fR, g->body->R, g->oR);
 }
 static dReal* geom_pos(dxGeom* g) {
+  if (g->ovr_pos) return const_cast<dReal*>(g->ovr_pos);
   geom_recompute(g);
   return g->has_offset ? g->fpos : g->body ? g->body->pos : g->pos;
 }
 static dReal* geom_R(dxGeom* g) {
+  if (g->ovr_R) return const_cast<dReal*>(g->ovr_R);
   geom_recompute(g);
   return g->has_offset ? g->fR : g->body ? g->body->R : g->R;
+}
+// dxGeomTransform::computeFinalTx (collision_transform.cpp:94-102): the
+// wrapped geom's own pose carried by the transform's
+static void transform_final(dxGeom* tr) {
+  const dReal* R = geom_R(tr);
+  const dReal* P = geom_pos(tr);
+  const dReal* op = geom_pos(tr->tobj);
+  mul0_331(tr->tpos, R, op);
+  for (int k = 0; k < 3; ++k) tr->tpos[k] += P[k];
+  mul0_333(tr->tR, R, geom_R(tr->tobj));
 }
 // getBodyPosr (collision_kernel.cpp:428-439): the body pose that puts the
 // offset geom at (fpos, fR)
@@ -1860,6 +1898,23 @@ static void compute_aabb(dxGeom* g, dReal* aabb) {
   const float inf = INFINITY;
   if (const dGeomClass* uc = user_class_of(g)) {
     uc->aabb(g, aabb);
+    return;
+  }
+  if (g->type == dGeomTransformClass) {
+    // dxGeomTransform::computeAABB (collision_transform.cpp:78-92): the
+    // wrapped geom's box at the carried pose, written into the wrapped geom's
+    // box as well (its cached box flag untouched), as the reference does
+    if (!g->tobj) {
+      for (int k = 0; k < 6; ++k) aabb[k] = 0;
+      return;
+    }
+    transform_final(g);
+    dxGeom* o = g->tobj;
+    o->ovr_pos = g->tpos;
+    o->ovr_R = g->tR;
+    compute_aabb(o, o->aabb);
+    o->ovr_pos = o->ovr_R = nullptr;
+    for (int k = 0; k < 6; ++k) aabb[k] = o->aabb[k];
     return;
   }
   if (is_space(g)) {
@@ -2219,6 +2274,23 @@ static const dGeomClass* user_class_of(const dxGeom* g) {
   return is_user_class(g->type) ? &g_user_classes[g->type - kFirstUserClass] : nullptr;
 }
 
+// Geom transforms (collision_transform.cpp:153-209): a placeable geom that
+// carries another one (not in a space, not on a body) at its own pose
+dGeomID dCreateGeomTransform(dSpaceID space) {
+  const double p[4] = {0, 0, 0, 0};
+  return new_geom(space, dGeomTransformClass, p);
+}
+void dGeomTransformSetGeom(dGeomID g, dGeomID obj) {
+  if (!g || g->type != dGeomTransformClass) return;
+  if (g->tobj && g->tcleanup) dGeomDestroy(g->tobj);
+  g->tobj = obj;
+}
+dGeomID dGeomTransformGetGeom(dGeomID g) { return g && g->type == dGeomTransformClass ? g->tobj : nullptr; }
+void dGeomTransformSetCleanup(dGeomID g, int mode) { if (g && g->type == dGeomTransformClass) g->tcleanup = mode; }
+int dGeomTransformGetCleanup(dGeomID g) { return g && g->type == dGeomTransformClass ? g->tcleanup : 0; }
+void dGeomTransformSetInfo(dGeomID g, int mode) { if (g && g->type == dGeomTransformClass) g->tinfo = mode; }
+int dGeomTransformGetInfo(dGeomID g) { return g && g->type == dGeomTransformClass ? g->tinfo : 0; }
+
 // ---------------------------------------------------------------- spaces (API)
 // Simple and hash spaces (collision_space.cpp:210-604) on the host: they only
 // enumerate candidate pairs for the caller's near-callback, which calls
@@ -2463,6 +2535,7 @@ int dCollide(dGeomID o1, dGeomID o2, int flags, dContactGeom* contact, int skip)
   if (!o1 || !o2 || !contact || (flags & 0xffff) == 0) return 0;
   if (o1 == o2) return 0;
   if (o1->body == o2->body && o1->body) return 0;
+  colliders_init();
   if (o1->type >= 0 && o1->type < kGeomClasses && o2->type >= 0 && o2->type < kGeomClasses &&
       g_colliders[o1->type][o2->type].kind != kColliderBuiltin) {
     // a caller's collider or a user class (collision_kernel.cpp:313-336); a
@@ -2486,6 +2559,23 @@ int dCollide(dGeomID o1, dGeomID o2, int flags, dContactGeom* contact, int skip)
       g_colliders[t1][t2] = {kColliderFn, fn, rev};
       g_colliders[t2][t1] = {kColliderFn, fn, !rev};
       n = dCollide(a, b, flags, contact, skip);
+    } else if (e.kind == kColliderTransform) {
+      // dCollideTransform (collision_transform.cpp:105-150): the wrapped geom
+      // collides at the carried pose (the one of the last box, while the
+      // transform's box is valid) and with the transform's body; in info
+      // mode the contacts name the transform
+      dxGeom* o = a->tobj;
+      if (!o) return 0;
+      if (a->aabb_bad) transform_final(a);
+      dxBody* body_bak = o->body;
+      o->ovr_pos = a->tpos;
+      o->ovr_R = a->tR;
+      o->body = a->body;
+      n = dCollide(o, b, flags, contact, skip);
+      if (a->tinfo)
+        for (int i = 0; i < n; ++i) ((dContactGeom*)((char*)contact + (size_t)i * skip))->g1 = a;
+      o->ovr_pos = o->ovr_R = nullptr;
+      o->body = body_bak;
     } else {
       if (!e.fn) return 0;
       n = e.fn(a, b, flags, contact, skip);

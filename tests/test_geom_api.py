@@ -555,3 +555,125 @@ def test_user_geom_classes_match_reference():
         outs.append((np.array(out, dtype=np.float32), log))
     assert np.array_equal(outs[0][0], outs[1][0]), (outs[0][0], outs[1][0])
     assert outs[0][1] == outs[1][1], (outs[0][1], outs[1][1])
+
+
+def test_geom_transform_matches_reference():
+    """dCreateGeomTransform and its calls (collision_transform.cpp:38-209): the
+    wrapped geom's box at the carried pose, collisions with the wrapped geom
+    at that pose and with the transform's body (both argument orders, info
+    mode naming the transform), space pairs, cleanup on destroy. The wrapped
+    geom is of a user class, so its collider is the test's own host code and
+    records the pose it sees; against the reference's dSINGLE build."""
+    ours, ref = _libs()
+
+    class CG(C.Structure):
+        _fields_ = [("pos", F * 4), ("normal", F * 4), ("depth", F), ("g1", P), ("g2", P), ("side1", I),
+                    ("side2", I)]
+
+    FN = C.CFUNCTYPE(I, P, P, I, P, I)
+    GET = C.CFUNCTYPE(P, I)
+    AABB = C.CFUNCTYPE(None, P, C.POINTER(F))
+    DTOR = C.CFUNCTYPE(None, P)
+
+    class GeomClass(C.Structure):
+        _fields_ = [("bytes", I), ("collider", GET), ("aabb", AABB), ("aabb_test", P), ("dtor", DTOR)]
+
+    outs = []
+    for lib in (ours, ref):
+        lib.dInitODE2.argtypes = [C.c_uint]
+        lib.dInitODE2(0)
+        lib.dCreateGeomClass.argtypes = [P]
+        lib.dCreateGeom.restype = lib.dGeomGetClassData.restype = lib.dCreateGeomTransform.restype = P
+        lib.dGeomTransformGetGeom.restype = P
+        lib.dCreateGeom.argtypes = [I]
+        lib.dGeomGetClassData.argtypes = lib.dGeomTransformGetGeom.argtypes = [P]
+        lib.dCreateGeomTransform.argtypes = [P]
+        lib.dGeomTransformSetGeom.argtypes = [P, P]
+        for n in ("dGeomTransformSetCleanup", "dGeomTransformSetInfo"):
+            getattr(lib, n).argtypes = [P, I]
+        lib.dGeomTransformGetCleanup.argtypes = lib.dGeomTransformGetInfo.argtypes = [P]
+        lib.dCollide.argtypes = [P, P, I, P, I]
+        lib.dSimpleSpaceCreate.restype = P
+        lib.dSimpleSpaceCreate.argtypes = [P]
+        NEAR = C.CFUNCTYPE(None, P, P, P)
+        lib.dSpaceCollide.argtypes = [P, P, NEAR]
+        lib.dSpaceDestroy.argtypes = [P]
+        ids, log = {}, []
+
+        def coll(o1, o2, flags, contact, skip):
+            p = lib.dGeomGetPosition(o1)
+            R = lib.dGeomGetRotation(o1)
+            log.append(("coll", ids.get(o1, -1), ids.get(o2, -1), p[0], p[1], p[2], R[0], R[1], R[5]))
+            c = CG.from_address(contact)
+            c.pos[0], c.pos[1], c.pos[2] = p[0], p[1], p[2]
+            c.normal[2] = 1.0
+            c.depth = 0.1
+            c.g1, c.g2 = o1, o2
+            return 1
+
+        fn = FN(coll)
+
+        def getter(num):
+            return C.cast(fn, P).value if num == dSphereClass else None
+
+        def aabb(g, out):
+            p = lib.dGeomGetPosition(g)
+            for k in range(3):
+                out[2 * k], out[2 * k + 1] = p[k] - 0.4, p[k] + 0.4
+
+        def dtor(g):
+            log.append(("dtor", ids.get(g, -1)))
+
+        gc = GeomClass(4, GET(getter), AABB(aabb), None, DTOR(dtor))
+        cls = lib.dCreateGeomClass(C.byref(gc))
+        w = lib.dWorldCreate()
+        body = lib.dBodyCreate(w)
+        lib.dBodySetPosition(body, 0.5, -0.25, 1.0)
+        lib.dBodySetRotation(body, _rot(lib, [0.2, 0.9, -0.3, 0.7]))
+        sp = lib.dSimpleSpaceCreate(None)
+        tr = lib.dCreateGeomTransform(sp)
+        u = lib.dCreateGeom(cls)
+        s = lib.dCreateSphere(sp, 0.5)
+        s2 = lib.dCreateSphere(None, 0.3)
+        for k, g in enumerate((tr, u, s, s2)):
+            ids[g] = k
+        out = [lib.dGeomTransformGetCleanup(tr), lib.dGeomTransformGetInfo(tr),
+               int(lib.dGeomTransformGetGeom(tr) is None)] + _aabb(lib, tr)
+        lib.dGeomTransformSetGeom(tr, u)
+        lib.dGeomTransformSetCleanup(tr, 1)
+        lib.dGeomSetPosition(u, 0.25, 0.0, -0.5)
+        lib.dGeomSetRotation(u, _rot(lib, [1.0, 0.0, 0.5, 0.3]))
+        lib.dGeomSetPosition(tr, 1.0, 2.0, 3.0)
+        lib.dGeomSetRotation(tr, _rot(lib, [0.0, 1.0, 1.0, 0.8]))
+        lib.dGeomSetPosition(s, 1.2, 2.1, 2.6)
+        out += _aabb(lib, tr) + _pose(lib, tr)
+        for info in (0, 1):
+            lib.dGeomTransformSetInfo(tr, info)
+            for o1, o2 in ((tr, s), (s, tr)):
+                buf = (CG * 2)()
+                n = lib.dCollide(o1, o2, 2, buf, C.sizeof(CG))
+                out += [n] + list(buf[0].pos)[:3] + list(buf[0].normal)[:3] + [ids[buf[0].g1], ids[buf[0].g2]]
+        pairs = []
+        near = NEAR(lambda d, a, b: pairs.append((ids[a], ids[b])))
+        lib.dSpaceCollide(sp, None, near)
+        out += [x for pr in pairs for x in pr]
+        # on a body: the wrapped geom takes the body for the same-body rule
+        lib.dGeomSetBody(tr, body)
+        lib.dGeomSetBody(s2, body)
+        buf = (CG * 2)()
+        out += [lib.dCollide(tr, s2, 2, buf, C.sizeof(CG))] + _aabb(lib, tr)
+        lib.dGeomSetBody(s2, None)
+        lib.dGeomSetPosition(s2, 1.0, -0.2, 0.9)
+        out += [lib.dCollide(tr, s2, 2, buf, C.sizeof(CG))] + list(buf[0].pos)[:3]
+        lib.dGeomDestroy(tr)            # cleanup on: the user geom goes too
+        lib.dSpaceDestroy(sp)
+        lib.dGeomDestroy(s2)
+        lib.dWorldDestroy(w)
+        lib.dCloseODE()
+        lib.dInitODE2(0)
+        outs.append((np.array(out, dtype=np.float64), log))
+    _close(outs[0][0].astype(np.float32), outs[1][0].astype(np.float32), 2e-6)
+    la, lb = outs[0][1], outs[1][1]
+    assert [x[:3] for x in la] == [x[:3] for x in lb], (la, lb)
+    _close(np.array([x[3:] for x in la if x[0] == "coll"], dtype=np.float32),
+           np.array([x[3:] for x in lb if x[0] == "coll"], dtype=np.float32), 2e-6)
