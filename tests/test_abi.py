@@ -534,3 +534,25 @@ def test_print_matrix_writes_what_the_reference_writes(tmp_path):
         libc.fclose(f)
         texts.append(open(out).read())
     assert texts[0] == texts[1] and texts[0].count("\n") == 5, texts
+
+
+def test_space_demo_builds_both_ways_and_pairs_agree():
+    """tests/c_api/space_stack_demo.c, an ODE program in the shape of ODE's
+    demos (hash space, near-callback with dCollide and contact joints,
+    auto-disable, damping), compiles unchanged against include/ode_gpu.h and
+    against the reference. Its first dSpaceCollide comes before any step and
+    needs no GPU, so both builds must print the same pairs for it; the
+    reference build runs to the end."""
+    import c_api_util as U
+    if not U.ref_demo_available():
+        pytest.skip("reference not built in this checkout")
+    src = os.path.join(ROOT, "tests", "c_api", "space_stack_demo.c")
+    with tempfile.TemporaryDirectory() as d:
+        ours = U.build_gpu_demo(os.path.join(d, "ours"), src=src)
+        ref = U.build_ref_demo(os.path.join(d, "ref"), src=src)
+        r = subprocess.run([ref, "24", "30", "7"], capture_output=True, text=True, check=True)
+        o = subprocess.run([ours, "24", "30", "7"], capture_output=True, text=True)
+    ref_lines, our_lines = r.stdout.splitlines(), o.stdout.splitlines()
+    assert ref_lines[0].startswith("pairs") and int(ref_lines[0].split()[1]) >= 8, ref_lines[0]
+    assert our_lines[0] == ref_lines[0]
+    assert len(ref_lines) == 2 * 30 + 24
