@@ -24,7 +24,7 @@
  *    the host as in ODE (same pair order, same island order); moved
  *    callbacks run after the whole step rather than body by body, and a
  *    heightfield's height callback is sampled once when the data is built.
- *  - Not built: sweep-and-prune and quadtree spaces, trimesh, convex, and
+ *  - Not built: sweep-and-prune spaces, trimesh, convex, and
  *    the LMotor, PR, PU, piston and plane-2D joints.
  */
 #ifndef ODE_GPU_H
@@ -586,10 +586,14 @@ void dGeomGetOffsetQuaternion(dGeomID g, dQuaternion result);            /* :737
  * candidate pairs on the host in ODE's order (a geom that moves goes to the
  * front of its space's list, as do the geoms of every body a step moves, in
  * the step's island order), so a near-callback sees the pairs ODE would pass.
- * Sweep-and-prune and quadtree spaces are not built. */
+ * Sweep-and-prune spaces are not built. */
 typedef void dNearCallback(void* data, dGeomID o1, dGeomID o2);         /* collision_space.h:49 */
 dSpaceID dSimpleSpaceCreate(dSpaceID space);                             /* :52 */
 dSpaceID dHashSpaceCreate(dSpaceID space);                               /* :53 */
+/* A quadtree over x and y. As in ODE 0.12, dSpaceGetGeom does not enumerate
+ * it (returns 0), its box stays infinite, and destroying it does not destroy
+ * its geoms (here they are released from it). */
+dSpaceID dQuadTreeSpaceCreate(dSpaceID space, const dVector3 Center, const dVector3 Extents, int Depth);  /* :54 */
 void dSpaceDestroy(dSpaceID space);                                      /* :70 */
 void dHashSpaceSetLevels(dSpaceID space, int minlevel, int maxlevel);    /* :72 */
 void dHashSpaceGetLevels(dSpaceID space, int* minlevel, int* maxlevel);  /* :73 */

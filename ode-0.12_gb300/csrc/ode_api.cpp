@@ -113,6 +113,7 @@ struct dxGeom {
   int tcleanup, tinfo;
   dReal tpos[4], tR[12];
   const dReal *ovr_pos, *ovr_R;   // set while a transform collides or boxes this geom
+  int qblock;                     // quadtree space: the block holding this geom
   // space membership (collision_kernel.h:150-171, collision_space.cpp:162-205):
   // the parent space, the intrusive list link, and the GEOM_DIRTY /
   // GEOM_AABB_BAD flags with the cached box they guard
@@ -132,6 +133,21 @@ struct dxSpace : dxGeom {
   int sublevel;         // dSpaceCollide2's nesting rule
   int manual_cleanup;
   int minlevel, maxlevel;   // hash space cell levels (-3, 10)
+  struct QuadTree* qt;      // quadtree space: its blocks and dirty list
+};
+// dxQuadTreeSpace (collision_quadtreespace.cpp:46-160, :334-392): a fixed tree
+// of blocks split in two along x and along y per level; a geom lives in the
+// smallest block whose half-open box holds its box (the root when none), in
+// that block's list (newest first); geoms that moved wait in a dirty list
+// and are re-seated when the space is cleaned
+struct QuadBlock {
+  dReal minx, maxx, miny, maxy;
+  dxGeom* first;
+  int count, parent, children;   // children: index of the first of four, or -1
+};
+struct QuadTree {
+  std::vector<QuadBlock> blocks;
+  std::vector<dxGeom*> dirty;
 };
 static bool is_space(const dxGeom* g) { return g->type >= dFirstSpaceClass && g->type <= dLastSpaceClass; }
 // every attached geom is notified when its body moves (ode.cpp:362-395, util.cpp:334-336)
@@ -1444,16 +1460,66 @@ static void geom_moved(dxGeom* g) {
   dxSpace* parent = g->space;
   while (parent && !g->dirty) {
     g->dirty = g->aabb_bad = 1;
-    list_unlink(g);
-    list_push_front(&parent->first, g);
+    if (parent->qt) {
+      parent->qt->dirty.push_back(g);   // dxQuadTreeSpace::dirty
+    } else {
+      list_unlink(g);
+      list_push_front(&parent->first, g);
+    }
     g = parent;
     parent = parent->space;
   }
   for (; g; g = g->space) g->dirty = g->aabb_bad = 1;
 }
-// dxSpace::add / remove (collision_space.cpp:162-206)
+// Block::Inside / GetBlock / GetBlockChild / AddObject / DelObject
+// (collision_quadtreespace.cpp:251-331)
+static bool quad_inside(const QuadBlock& b, const dReal* a) {
+  return a[0] >= b.minx && a[1] < b.maxx && a[2] >= b.miny && a[3] < b.maxy;
+}
+static int quad_block_child(const QuadTree& q, int b, const dReal* a) {
+  for (;;) {
+    const int c = q.blocks[b].children;
+    if (c < 0) return b;
+    int next = -1;
+    for (int i = 0; i < 4 && next < 0; ++i)
+      if (quad_inside(q.blocks[c + i], a)) next = c + i;
+    if (next < 0) return b;
+    b = next;
+  }
+}
+static int quad_block(const QuadTree& q, int b, const dReal* a) {
+  for (;;) {
+    if (quad_inside(q.blocks[b], a)) return quad_block_child(q, b, a);
+    if (q.blocks[b].parent < 0) return b;
+    b = q.blocks[b].parent;
+  }
+}
+static void quad_add(QuadTree& q, int b, dxGeom* g) {
+  g->next = q.blocks[b].first;
+  q.blocks[b].first = g;
+  g->qblock = b;
+  for (int k = b; k >= 0; k = q.blocks[k].parent) ++q.blocks[k].count;
+}
+static void quad_del(QuadTree& q, dxGeom* g) {
+  const int b = g->qblock;
+  for (dxGeom** l = &q.blocks[b].first; *l; l = &(*l)->next)
+    if (*l == g) { *l = g->next; break; }
+  g->qblock = -1;
+  for (int k = b; k >= 0; k = q.blocks[k].parent) --q.blocks[k].count;
+}
+
+// dxSpace::add / remove (collision_space.cpp:162-206, quadtree :485-532)
 static void space_add(dxSpace* s, dxGeom* g) {
   if (!s || !g || g->space) return;
+  if (s->qt) {
+    g->dirty = g->aabb_bad = 1;
+    s->qt->dirty.push_back(g);
+    g->space = s;
+    quad_add(*s->qt, quad_block(*s->qt, 0, g->aabb), g);   // by the box it has now
+    ++s->count;
+    geom_moved(s);
+    return;
+  }
   g->space = s;
   list_push_front(&s->first, g);
   ++s->count;
@@ -1462,6 +1528,16 @@ static void space_add(dxSpace* s, dxGeom* g) {
 }
 static void space_remove(dxSpace* s, dxGeom* g) {
   if (!s || !g || g->space != s) return;
+  if (s->qt) {
+    quad_del(*s->qt, g);
+    --s->count;
+    auto& d = s->qt->dirty;
+    d.erase(std::remove(d.begin(), d.end(), g), d.end());
+    g->next = nullptr;
+    g->space = nullptr;
+    geom_moved(s);
+    return;
+  }
   list_unlink(g);
   --s->count;
   g->next = nullptr;
@@ -1554,6 +1630,20 @@ void dGeomDestroy(dGeomID g) {
       n = c->next;
       if (sp->cleanup) dGeomDestroy(c);
       else space_remove(sp, c);
+    }
+    if (sp->qt) {
+      // ODE 0.12's space destructor walks the base list, which a quadtree
+      // space leaves empty, so its geoms are neither destroyed nor released
+      // there; here they are released
+      for (QuadBlock& b : sp->qt->blocks)
+        for (dxGeom *c = b.first, *n; c; c = n) {
+          n = c->next;
+          c->next = nullptr;
+          c->qblock = -1;
+          c->space = nullptr;
+        }
+      delete sp->qt;
+      sp->qt = nullptr;
     }
   }
   if (g->type == dGeomTransformClass && g->tobj && g->tcleanup) dGeomDestroy(g->tobj);   // ~dxGeomTransform
@@ -1919,6 +2009,10 @@ static void compute_aabb(dxGeom* g, dReal* aabb) {
   }
   if (is_space(g)) {
     const auto* sp = static_cast<const dxSpace*>(g);
+    if (sp->qt) {   // a quadtree space keeps the infinite box it starts with (:387-391, :538-540)
+      for (int k = 0; k < 6; ++k) aabb[k] = (k & 1) ? inf : -inf;
+      return;
+    }
     if (!sp->first) {
       for (int k = 0; k < 6; ++k) aabb[k] = 0;
       return;
@@ -2326,6 +2420,22 @@ static void collide_aabbs(dxGeom* g1, dxGeom* g2, void* data, dNearCallback* cb)
 // cleanGeoms (collision_space.cpp:229-242, :390-402): boxes of the dirty
 // prefix, nested spaces first
 static void space_clean(dxSpace* sp) {
+  if (sp->qt) {   // dxQuadTreeSpace::cleanGeoms (:542-559): boxes, then each geom to its block
+    QuadTree& q = *sp->qt;
+    for (size_t i = 0; i < q.dirty.size(); ++i) {
+      dxGeom* g = q.dirty[i];
+      if (is_space(g)) space_clean(static_cast<dxSpace*>(g));
+      recompute_aabb(g);
+      g->dirty = g->aabb_bad = 0;
+      const int nb = quad_block(q, g->qblock, g->aabb);
+      if (nb != g->qblock) {
+        quad_del(q, g);
+        quad_add(q, nb, g);
+      }
+    }
+    q.dirty.clear();
+    return;
+  }
   for (dxGeom* g = sp->first; g && g->dirty; g = g->next) {
     if (is_space(g)) space_clean(static_cast<dxSpace*>(g));
     recompute_aabb(g);
@@ -2342,7 +2452,12 @@ static void simple_collide(dxSpace* sp, void* data, dNearCallback* cb) {
   }
 }
 // collide2 of both space kinds (:267-283, :589-604): the geom against each member
+static void quad_collide2(dxSpace* sp, void* data, dxGeom* geom, dNearCallback* cb);
 static void space_collide2(dxSpace* sp, void* data, dxGeom* geom, dNearCallback* cb) {
+  if (sp->qt) {
+    quad_collide2(sp, data, geom, cb);
+    return;
+  }
   space_clean(sp);
   recompute_aabb(geom);
   for (dxGeom* g = sp->first; g; g = g->next)
@@ -2451,13 +2566,79 @@ static void hash_collide(dxSpace* sp, void* data, dNearCallback* cb) {
   for (int a = big; a >= 0; a = box[a].next)
     for (int b = box[a].next; b >= 0; b = box[b].next) collide_aabbs(box[a].g, box[b].g, data, cb);
 }
+// Block::Collide (collision_quadtreespace.cpp:177-238): each enabled geom of
+// a block against the later ones in its list and, through the children whose
+// box its box reaches (every child holding one geom is visited), against the
+// geoms below; then the children holding two or more geoms in turn
+static void quad_collide_geom(const QuadTree& q, int b, dxGeom* g1, dxGeom* g2, void* data, dNearCallback* cb) {
+  for (; g2; g2 = g2->next)
+    if (geom_enabled(g2)) collide_aabbs(g1, g2, data, cb);
+  const int c = q.blocks[b].children;
+  if (c < 0) return;
+  for (int i = 0; i < 4; ++i) {
+    const QuadBlock& ch = q.blocks[c + i];
+    if (ch.count == 0) continue;
+    if (ch.count != 1 && (g1->aabb[0] >= ch.maxx || g1->aabb[1] < ch.minx || g1->aabb[2] >= ch.maxy ||
+                          g1->aabb[3] < ch.miny))
+      continue;
+    quad_collide_geom(q, c + i, g1, ch.first, data, cb);
+  }
+}
+static void quad_collide_block(const QuadTree& q, int b, void* data, dNearCallback* cb) {
+  for (dxGeom* g = q.blocks[b].first; g; g = g->next)
+    if (geom_enabled(g)) quad_collide_geom(q, b, g, g->next, data, cb);
+  const int c = q.blocks[b].children;
+  if (c < 0) return;
+  for (int i = 0; i < 4; ++i)
+    if (q.blocks[c + i].count > 1) quad_collide_block(q, c + i, data, cb);
+}
 static void space_collide(dxSpace* sp, void* data, dNearCallback* cb) {
-  if (sp->type == dHashSpaceClass) hash_collide(sp, data, cb);
-  else simple_collide(sp, data, cb);
+  if (sp->qt) {
+    space_clean(sp);
+    quad_collide_block(*sp->qt, 0, data, cb);
+  } else if (sp->type == dHashSpaceClass) {
+    hash_collide(sp, data, cb);
+  } else {
+    simple_collide(sp, data, cb);
+  }
 }
 
 dSpaceID dSimpleSpaceCreate(dSpaceID space) { return new_space(space, dSimpleSpaceClass); }
 dSpaceID dHashSpaceCreate(dSpaceID space) { return new_space(space, dHashSpaceClass); }
+// dQuadTreeSpaceCreate (collision_quadtreespace.cpp:362-392, :134-175): the
+// root spans center +- extents on x and y, its upper edges nudged up to the
+// next float so that they are inside; depth levels of four children each
+static void quad_build(QuadTree& q, int b, dReal minx, dReal maxx, dReal miny, dReal maxy, int parent, int depth) {
+  q.blocks[b] = {minx, maxx, miny, maxy, nullptr, 0, parent, -1};
+  if (depth <= 0) return;
+  const int c = (int)q.blocks.size();
+  q.blocks[b].children = c;
+  q.blocks.resize(q.blocks.size() + 4);
+  const dReal ex = (maxx - minx) / 2, ey = (maxy - miny) / 2;
+  dReal right_x = minx;
+  int k = 0;
+  for (int i = 0; i < 2; ++i) {
+    const dReal left_x = right_x;
+    right_x = i != 1 ? left_x + ex : maxx;
+    dReal right_y = miny;
+    for (int j = 0; j < 2; ++j) {
+      const dReal left_y = right_y;
+      right_y = j != 1 ? left_y + ey : maxy;
+      quad_build(q, c + k++, left_x, right_x, left_y, right_y, b, depth - 1);
+    }
+  }
+}
+dSpaceID dQuadTreeSpaceCreate(dSpaceID space, const dVector3 Center, const dVector3 Extents, int Depth) {
+  auto* q = new QuadTree();
+  q->blocks.resize(1);
+  quad_build(*q, 0, Center[0] - Extents[0], std::nextafter((dReal)(Center[0] + Extents[0]), (dReal)INFINITY),
+             Center[1] - Extents[1], std::nextafter((dReal)(Center[1] + Extents[1]), (dReal)INFINITY), -1,
+             Depth < 0 ? 0 : Depth);
+  dSpaceID sp = new_space(nullptr, dQuadTreeSpaceClass);
+  sp->qt = q;
+  if (space) space_add(space, sp);
+  return sp;
+}
 void dHashSpaceSetLevels(dSpaceID space, int minlevel, int maxlevel) {
   if (!space || space->type != dHashSpaceClass || minlevel > maxlevel) return;
   space->minlevel = minlevel;
@@ -2481,7 +2662,8 @@ int dSpaceQuery(dSpaceID space, dGeomID g) { return g && g->space == space ? 1 :
 void dSpaceClean(dSpaceID space) { space_clean(space); }
 int dSpaceGetNumGeoms(dSpaceID space) { return space->count; }
 dGeomID dSpaceGetGeom(dSpaceID space, int i) {   // dxSpace::getGeom (collision_space.cpp:131-149)
-  if (i < 0) return nullptr;
+  // ODE 0.12 leaves the quadtree's enumeration unimplemented (:412-483)
+  if (i < 0 || space->qt) return nullptr;
   dxGeom* g = space->first;
   for (int j = 0; j < i && g; ++j) g = g->next;
   return g;
@@ -2498,6 +2680,24 @@ void swap_callback(void* data, dGeomID g1, dGeomID g2) {   // collision_space.cp
   d->cb(d->data, g2, g1);
 }
 }  // namespace
+// dxQuadTreeSpace::collide2 (collision_quadtreespace.cpp:585-611): a member
+// against its block and the blocks below, with the pair swapped, then the
+// blocks above; any other geom against the whole tree, swapped
+static void quad_collide2(dxSpace* sp, void* data, dxGeom* g2, dNearCallback* cb) {
+  space_clean(sp);
+  recompute_aabb(g2);
+  const QuadTree& q = *sp->qt;
+  SwapData d{data, cb};
+  if (g2->space == sp) {
+    int b = g2->qblock;
+    quad_collide_geom(q, b, g2, q.blocks[b].first, &d, swap_callback);
+    while ((b = q.blocks[b].parent) >= 0)
+      for (dxGeom* g1 = q.blocks[b].first; g1; g1 = g1->next)
+        if (geom_enabled(g1)) collide_aabbs(g1, g2, data, cb);
+  } else {
+    quad_collide_geom(q, 0, g2, q.blocks[0].first, &d, swap_callback);
+  }
+}
 // dSpaceCollide2 (collision_space.cpp:767-834): a space against a geom, two
 // spaces by the smaller one's members (the deeper sublevel is taken as a
 // geom), or two geoms by their boxes alone

@@ -249,3 +249,104 @@ def step_program(lib, seed, n_steps=6, stepper="dWorldQuickStep"):
     lib.dSpaceDestroy(sp)
     lib.dWorldDestroy(w)
     return np.array(rec, dtype=np.int64)
+
+
+def quad_program(lib, seed, n_ops=60):
+    """Random edits between collides in a quadtree space (center 0, extents 4,
+    depth 3) holding geoms of every class, a nested simple space, geoms on
+    bodies and free ones, moves (re-seated in their blocks when the space is
+    cleaned), disabling, bits, removal and re-adding. ODE 0.12 does not
+    enumerate a quadtree's geoms, so only the near-callback's pairs and the
+    counts are recorded."""
+    rng = np.random.default_rng(seed)
+    ids = _Ids()
+    rec = []
+    pairs = []
+    cb = NEAR(lambda d, a, b: pairs.append((ids(a), ids(b))))
+    lib.dInitODE2(0)
+    lib.dQuadTreeSpaceCreate.restype = P
+    lib.dQuadTreeSpaceCreate.argtypes = [P, P, P, I]
+    w = lib.dWorldCreate()
+    center, extents = (F * 4)(0.0, 0.0, 0.0, 0.0), (F * 4)(4.0, 4.0, 4.0, 0.0)
+    top = ids.add(lib.dQuadTreeSpaceCreate(None, center, extents, 3))
+    sub = ids.add(lib.dSimpleSpaceCreate(top))
+    bodies = []
+    for _ in range(4):
+        b = lib.dBodyCreate(w)
+        lib.dBodySetPosition(b, *(rng.uniform(-3, 3, 3)))
+        bodies.append(b)
+    geoms = []
+
+    def make(space):
+        c = int(rng.integers(0, 6))
+        if c == 0:
+            g = lib.dCreateSphere(space, float(rng.uniform(0.1, 0.6)))
+        elif c == 1:
+            g = lib.dCreateBox(space, *(rng.uniform(0.1, 1.0, 3)))
+        elif c == 2:
+            g = lib.dCreateCapsule(space, float(rng.uniform(0.1, 0.4)), float(rng.uniform(0.2, 1.2)))
+        elif c == 3:
+            g = lib.dCreateCylinder(space, float(rng.uniform(0.1, 0.4)), float(rng.uniform(0.2, 1.2)))
+        elif c == 4:
+            g = lib.dCreateRay(space, float(rng.uniform(0.5, 2.5)))
+        else:
+            g = lib.dCreatePlane(space, 0.0, 0.0, 1.0, float(rng.uniform(-3, 0)))
+        ids.add(g)
+        if c != 5:
+            if rng.random() < 0.4:
+                lib.dGeomSetBody(g, bodies[int(rng.integers(0, len(bodies)))])
+            else:
+                lib.dGeomSetPosition(g, *(rng.uniform(-5, 5, 3)))
+                lib.dGeomSetQuaternion(g, _quat(rng.normal(size=4)))
+        geoms.append((g, c))
+
+    for _ in range(16):
+        make(top if rng.random() < 0.8 else sub)
+    removed = []
+    for _ in range(n_ops):
+        op = int(rng.integers(0, 11))
+        g, c = geoms[int(rng.integers(0, len(geoms)))]
+        if op == 0:
+            lib.dBodySetPosition(bodies[int(rng.integers(0, len(bodies)))], *(rng.uniform(-5, 5, 3)))
+        elif op == 1 and c != 5:
+            lib.dGeomSetPosition(g, *(rng.uniform(-5, 5, 3)))
+        elif op == 2:
+            (lib.dGeomDisable if rng.random() < 0.5 else lib.dGeomEnable)(g)
+        elif op == 3:
+            lib.dGeomSetCategoryBits(g, int(rng.integers(0, 8)))
+            lib.dGeomSetCollideBits(g, int(rng.integers(0, 8)))
+        elif op == 4:
+            sp = lib.dGeomGetSpace(g)
+            if sp is not None:
+                lib.dSpaceRemove(sp, g)
+                removed.append(g)
+        elif op == 5 and removed:
+            lib.dSpaceAdd(top if rng.random() < 0.7 else sub, removed.pop(0))
+        elif op == 6:
+            make(top if rng.random() < 0.8 else sub)
+        elif op in (7, 8):
+            pairs.clear()
+            lib.dSpaceCollide(top, None, cb)
+            rec += [len(pairs)] + [x for pr in pairs for x in pr]
+        elif op == 9:
+            pairs.clear()
+            lib.dSpaceCollide2(top, g, None, cb)
+            lib.dSpaceCollide2(g, top, None, cb)
+            lib.dSpaceCollide2(sub, top, None, cb)
+            rec += [len(pairs)] + [x for pr in pairs for x in pr]
+        elif op == 10 and c != 5:
+            lib.dGeomGetPosition(g)   # see ops_program: keeps the reference clear of its offset crash
+            lib.dGeomSetBody(g, bodies[int(rng.integers(0, len(bodies)))] if rng.random() < 0.7 else None)
+        rec += [lib.dSpaceGetNumGeoms(top), lib.dSpaceGetNumGeoms(sub)]
+    pairs.clear()
+    lib.dSpaceCollide(top, None, cb)
+    rec += [len(pairs)] + [x for pr in pairs for x in pr]
+    # (dSpaceGetGeom is left out: ODE 0.12 aborts in it for a quadtree)
+    rec += [lib.dSpaceGetClass(top), lib.dSpaceQuery(top, sub)]
+    box = (F * 6)()
+    lib.dGeomGetAABB(top, box)
+    rec += [float(x) for x in box]
+    for g in removed:
+        lib.dGeomDestroy(g)
+    lib.dWorldDestroy(w)
+    return np.array(rec, dtype=np.float64)

@@ -53,3 +53,28 @@ def test_space_order_fixture_prefix_without_gpu():
         n0 = int(np.argmax(want == -9)) + 1
         n1 = n0 + 1 + 2 * int(want[n0])
         assert want[n0] > 0 and np.array_equal(got[:n1], want[:n1])
+
+
+def test_quadtree_space_pairs_match_reference():
+    """dQuadTreeSpaceCreate (ode/src/collision_quadtreespace.cpp): the pairs of
+    dSpaceCollide and dSpaceCollide2 over seeded programs of edits
+    (tests/space_program.py quad_program) equal the reference's dSINGLE
+    build's entry for entry, with ODE 0.12's missing enumeration and
+    infinite box."""
+    ours, ref = _libs()
+    n = 0
+    for seed in range(40):
+        a, b = SP.quad_program(ours, seed), SP.quad_program(ref, seed)
+        m = min(len(a), len(b))
+        assert a.shape == b.shape and np.array_equal(a, b), (seed, int(np.argmax(a[:m] != b[:m])))
+        n += len(a)
+    assert n > 4000
+    # ODE 0.12 does not enumerate a quadtree (its getGeom aborts); here it answers 0
+    ours.dQuadTreeSpaceCreate.restype = C.c_void_p
+    ours.dQuadTreeSpaceCreate.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
+    v = (C.c_float * 4)(0, 0, 0, 0)
+    e = (C.c_float * 4)(1, 1, 1, 0)
+    q = ours.dQuadTreeSpaceCreate(None, v, e, 2)
+    ours.dCreateSphere(q, 0.2)
+    assert ours.dSpaceGetNumGeoms(q) == 1 and ours.dSpaceGetGeom(q, 0) is None
+    ours.dSpaceDestroy(q)
