@@ -24,7 +24,7 @@
  *    the host as in ODE (same pair order, same island order); moved
  *    callbacks run after the whole step rather than body by body, and a
  *    heightfield's height callback is sampled once when the data is built.
- *  - Not built: sweep-and-prune spaces, trimesh, convex, and
+ *  - Not built: trimesh, convex, and
  *    the LMotor, PR, PU, piston and plane-2D joints.
  */
 #ifndef ODE_GPU_H
@@ -585,8 +585,7 @@ void dGeomGetOffsetQuaternion(dGeomID g, dQuaternion result);            /* :737
 /* Spaces: include/ode/collision_space.h. Simple and hash spaces enumerate
  * candidate pairs on the host in ODE's order (a geom that moves goes to the
  * front of its space's list, as do the geoms of every body a step moves, in
- * the step's island order), so a near-callback sees the pairs ODE would pass.
- * Sweep-and-prune spaces are not built. */
+ * the step's island order), so a near-callback sees the pairs ODE would pass. */
 typedef void dNearCallback(void* data, dGeomID o1, dGeomID o2);         /* collision_space.h:49 */
 dSpaceID dSimpleSpaceCreate(dSpaceID space);                             /* :52 */
 dSpaceID dHashSpaceCreate(dSpaceID space);                               /* :53 */
@@ -594,6 +593,11 @@ dSpaceID dHashSpaceCreate(dSpaceID space);                               /* :53 
  * it (returns 0), its box stays infinite, and destroying it does not destroy
  * its geoms (here they are released from it). */
 dSpaceID dQuadTreeSpaceCreate(dSpaceID space, const dVector3 Center, const dVector3 Extents, int Depth);  /* :54 */
+/* Sweep and prune along the first axis of axisorder (collision_space.h:56-66) */
+enum { dSAP_AXES_XYZ = 0 | (1 << 2) | (2 << 4), dSAP_AXES_XZY = 0 | (2 << 2) | (1 << 4),
+       dSAP_AXES_YXZ = 1 | (0 << 2) | (2 << 4), dSAP_AXES_YZX = 1 | (2 << 2) | (0 << 4),
+       dSAP_AXES_ZXY = 2 | (0 << 2) | (1 << 4), dSAP_AXES_ZYX = 2 | (1 << 2) | (0 << 4) };
+dSpaceID dSweepAndPruneSpaceCreate(dSpaceID space, int axisorder);       /* :66 */
 void dSpaceDestroy(dSpaceID space);                                      /* :70 */
 void dHashSpaceSetLevels(dSpaceID space, int minlevel, int maxlevel);    /* :72 */
 void dHashSpaceGetLevels(dSpaceID space, int* minlevel, int* maxlevel);  /* :73 */

@@ -8,7 +8,9 @@
 // on the host. Setter arithmetic (anchors, axes, inertia inverse) is host FP64
 // as in host_setup.hpp.
 #include <algorithm>
+#include <cfloat>
 #include <climits>
+#include <cstdint>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -114,6 +116,7 @@ struct dxGeom {
   dReal tpos[4], tR[12];
   const dReal *ovr_pos, *ovr_R;   // set while a transform collides or boxes this geom
   int qblock;                     // quadtree space: the block holding this geom
+  int sap_dirty, sap_clean;       // sweep-and-prune space: slots in its lists (-1: none)
   // space membership (collision_kernel.h:150-171, collision_space.cpp:162-205):
   // the parent space, the intrusive list link, and the GEOM_DIRTY /
   // GEOM_AABB_BAD flags with the cached box they guard
@@ -134,6 +137,30 @@ struct dxSpace : dxGeom {
   int manual_cleanup;
   int minlevel, maxlevel;   // hash space cell levels (-3, 10)
   struct QuadTree* qt;      // quadtree space: its blocks and dirty list
+  struct SapSpace* sap;     // sweep-and-prune space: its lists and sort state
+};
+// OPCODE's radix sort of floats as ODE 0.12 keeps it (collision_sapspace.cpp:
+// 54-131, :592-820): four byte passes from the least significant, a pass
+// skipped when every key has the first key's byte, negatives laid out in
+// reverse in the top pass; when the keys are already in order along the
+// previous result (or, with no valid result, in index order) that order is
+// returned as it is. The order of equal keys follows from all of this.
+struct RadixSorter {
+  std::vector<uint32_t> buf;   // two rank lists
+  size_t size = 0, used = 0, primary = 0;   // primary: offset of the current list
+  bool valid = false;
+  uint32_t* ranks1() { return buf.data() + primary; }
+  uint32_t* ranks2() { return buf.data() + (primary == 0 ? size : 0); }
+  void swap() { primary = primary == 0 ? size : 0; }
+  const uint32_t* sort(const float* keys, uint32_t nb);
+};
+// dxSAPSpace (collision_sapspace.cpp:135-520): geoms in a dirty list and a
+// clean list, each geom knowing its slot; removal moves the last one in
+struct SapSpace {
+  std::vector<dxGeom*> dirty, geoms, tmp, tmp_inf;
+  std::vector<float> pos;
+  RadixSorter sorter;
+  int ax0, ax1, ax2;
 };
 // dxQuadTreeSpace (collision_quadtreespace.cpp:46-160, :334-392): a fixed tree
 // of blocks split in two along x and along y per level; a geom lives in the
@@ -1455,6 +1482,19 @@ static void list_unlink(dxGeom* g) {   // dxGeom::spaceRemove
   if (g->next) g->next->tome = g->tome;
   *g->tome = g->next;
 }
+// dxSAPSpace::dirty (collision_sapspace.cpp:363-387): from the clean list
+// (the last one takes its slot) to the end of the dirty list
+static void sap_dirty(SapSpace& S, dxGeom* g) {
+  if (g->sap_dirty >= 0) return;
+  const int gi = g->sap_clean;
+  dxGeom* last = S.geoms.back();
+  S.geoms[gi] = last;
+  last->sap_clean = gi;
+  S.geoms.pop_back();
+  g->sap_clean = -1;
+  g->sap_dirty = (int)S.dirty.size();
+  S.dirty.push_back(g);
+}
 // dGeomMoved (collision_space.cpp:47-74)
 static void geom_moved(dxGeom* g) {
   dxSpace* parent = g->space;
@@ -1462,6 +1502,8 @@ static void geom_moved(dxGeom* g) {
     g->dirty = g->aabb_bad = 1;
     if (parent->qt) {
       parent->qt->dirty.push_back(g);   // dxQuadTreeSpace::dirty
+    } else if (parent->sap) {
+      sap_dirty(*parent->sap, g);
     } else {
       list_unlink(g);
       list_push_front(&parent->first, g);
@@ -1511,6 +1553,16 @@ static void quad_del(QuadTree& q, dxGeom* g) {
 // dxSpace::add / remove (collision_space.cpp:162-206, quadtree :485-532)
 static void space_add(dxSpace* s, dxGeom* g) {
   if (!s || !g || g->space) return;
+  if (s->sap) {   // dxSAPSpace::add (:303-320)
+    g->dirty = g->aabb_bad = 1;
+    g->sap_dirty = (int)s->sap->dirty.size();
+    g->sap_clean = -1;
+    s->sap->dirty.push_back(g);
+    g->space = s;
+    ++s->count;
+    geom_moved(s);
+    return;
+  }
   if (s->qt) {
     g->dirty = g->aabb_bad = 1;
     s->qt->dirty.push_back(g);
@@ -1528,6 +1580,25 @@ static void space_add(dxSpace* s, dxGeom* g) {
 }
 static void space_remove(dxSpace* s, dxGeom* g) {
   if (!s || !g || g->space != s) return;
+  if (s->sap) {   // dxSAPSpace::remove (:322-361)
+    SapSpace& S = *s->sap;
+    if (g->sap_dirty >= 0) {
+      dxGeom* last = S.dirty.back();
+      S.dirty[g->sap_dirty] = last;
+      last->sap_dirty = g->sap_dirty;
+      S.dirty.pop_back();
+    } else {
+      dxGeom* last = S.geoms.back();
+      S.geoms[g->sap_clean] = last;
+      last->sap_clean = g->sap_clean;
+      S.geoms.pop_back();
+    }
+    g->sap_dirty = g->sap_clean = -1;
+    --s->count;
+    g->space = nullptr;
+    geom_moved(s);
+    return;
+  }
   if (s->qt) {
     quad_del(*s->qt, g);
     --s->count;
@@ -1630,6 +1701,17 @@ void dGeomDestroy(dGeomID g) {
       n = c->next;
       if (sp->cleanup) dGeomDestroy(c);
       else space_remove(sp, c);
+    }
+    if (sp->sap) {
+      // ~dxSAPSpace (:278-291): the first of each list until it is empty
+      SapSpace& S = *sp->sap;
+      for (std::vector<dxGeom*>* l : {&S.dirty, &S.geoms})
+        while (!l->empty()) {
+          if (sp->cleanup) dGeomDestroy((*l)[0]);
+          else space_remove(sp, (*l)[0]);
+        }
+      delete sp->sap;
+      sp->sap = nullptr;
     }
     if (sp->qt) {
       // ODE 0.12's space destructor walks the base list, which a quadtree
@@ -2009,7 +2091,7 @@ static void compute_aabb(dxGeom* g, dReal* aabb) {
   }
   if (is_space(g)) {
     const auto* sp = static_cast<const dxSpace*>(g);
-    if (sp->qt) {   // a quadtree space keeps the infinite box it starts with (:387-391, :538-540)
+    if (sp->qt || sp->sap) {   // these keep the infinite box they start with (quadtree :387-391, SAP :265-271)
       for (int k = 0; k < 6; ++k) aabb[k] = (k & 1) ? inf : -inf;
       return;
     }
@@ -2420,6 +2502,19 @@ static void collide_aabbs(dxGeom* g1, dxGeom* g2, void* data, dNearCallback* cb)
 // cleanGeoms (collision_space.cpp:229-242, :390-402): boxes of the dirty
 // prefix, nested spaces first
 static void space_clean(dxSpace* sp) {
+  if (sp->sap) {   // dxSAPSpace::cleanGeoms (:394-423): the dirty list onto the clean one
+    SapSpace& S = *sp->sap;
+    for (dxGeom* g : S.dirty) {
+      if (is_space(g)) space_clean(static_cast<dxSpace*>(g));
+      recompute_aabb(g);
+      g->dirty = g->aabb_bad = 0;
+      g->sap_dirty = -1;
+      g->sap_clean = (int)S.geoms.size();
+      S.geoms.push_back(g);
+    }
+    S.dirty.clear();
+    return;
+  }
   if (sp->qt) {   // dxQuadTreeSpace::cleanGeoms (:542-559): boxes, then each geom to its block
     QuadTree& q = *sp->qt;
     for (size_t i = 0; i < q.dirty.size(); ++i) {
@@ -2456,6 +2551,15 @@ static void quad_collide2(dxSpace* sp, void* data, dxGeom* geom, dNearCallback* 
 static void space_collide2(dxSpace* sp, void* data, dxGeom* geom, dNearCallback* cb) {
   if (sp->qt) {
     quad_collide2(sp, data, geom, cb);
+    return;
+  }
+  if (sp->sap) {   // dxSAPSpace::collide2 (:498-519): every clean member, boxes tested
+    space_clean(sp);
+    recompute_aabb(geom);
+    for (size_t i = 0; i < sp->sap->geoms.size(); ++i) {
+      dxGeom* g = sp->sap->geoms[i];
+      if (geom_enabled(g)) collide_aabbs(g, geom, data, cb);
+    }
     return;
   }
   space_clean(sp);
@@ -2592,8 +2696,164 @@ static void quad_collide_block(const QuadTree& q, int b, void* data, dNearCallba
   for (int i = 0; i < 4; ++i)
     if (q.blocks[c + i].count > 1) quad_collide_block(q, c + i, data, cb);
 }
+const uint32_t* RadixSorter::sort(const float* keys, uint32_t nb) {
+  if (nb != used) {   // ReallocateRanksIfNecessary
+    if (nb > size) {
+      buf.assign(2 * (size_t)nb, 0);
+      size = nb;
+      primary = 0;
+    }
+    valid = false;
+    used = nb;
+  }
+  uint32_t hist[4][256] = {};
+  auto byte_of = [&](uint32_t i, int pass) {
+    uint32_t v;
+    std::memcpy(&v, keys + i, 4);
+    return (v >> (8 * pass)) & 0xffu;
+  };
+  // histograms, and the already-sorted test along the previous order
+  bool sorted = true;
+  uint32_t k = 0;
+  if (!valid) {
+    for (; k < nb; ++k) {
+      if (k > 0 && keys[k] < keys[k - 1]) { sorted = false; break; }
+      for (int pass = 0; pass < 4; ++pass) ++hist[pass][byte_of(k, pass)];
+    }
+    if (sorted) {
+      for (uint32_t i = 0; i < nb; ++i) ranks1()[i] = i;
+      return ranks1();
+    }
+  } else {
+    const uint32_t* r = ranks1();
+    for (; k < nb; ++k) {
+      if (k > 0 && keys[r[k]] < keys[r[k - 1]]) { sorted = false; break; }
+      for (int pass = 0; pass < 4; ++pass) ++hist[pass][byte_of(k, pass)];
+    }
+    if (sorted) return ranks1();
+  }
+  for (; k < nb; ++k)
+    for (int pass = 0; pass < 4; ++pass) ++hist[pass][byte_of(k, pass)];
+  uint32_t negatives = 0;
+  for (int i = 128; i < 256; ++i) negatives += hist[3][i];
+  for (int pass = 0; pass < 4; ++pass) {
+    const uint32_t* count = hist[pass];
+    const uint32_t unique = byte_of(0, pass);
+    const bool perform = count[unique] != nb;
+    if (pass != 3) {
+      if (!perform) continue;
+      uint32_t* out = ranks2();
+      uint32_t* link[256];
+      link[0] = out;
+      for (int i = 1; i < 256; ++i) link[i] = link[i - 1] + count[i - 1];
+      if (!valid) {
+        for (uint32_t i = 0; i < nb; ++i) *link[byte_of(i, pass)]++ = i;
+        valid = true;
+      } else {
+        const uint32_t* in = ranks1();
+        for (uint32_t i = 0; i < nb; ++i) *link[byte_of(in[i], pass)]++ = in[i];
+      }
+      swap();
+    } else if (perform) {
+      uint32_t* out = ranks2();
+      uint32_t* link[256];
+      link[0] = out + negatives;   // positives after the negatives
+      for (int i = 1; i < 128; ++i) link[i] = link[i - 1] + count[i - 1];
+      link[255] = out;             // negatives in reverse
+      for (int i = 0; i < 127; ++i) link[254 - i] = link[255 - i] + count[255 - i];
+      for (int i = 128; i < 256; ++i) link[i] += count[i];
+      if (!valid) {
+        for (uint32_t i = 0; i < nb; ++i) {
+          const uint32_t radix = byte_of(i, 3);
+          if (radix < 128) *link[radix]++ = i;
+          else *(--link[radix]) = i;
+        }
+        valid = true;
+      } else {
+        const uint32_t* in = ranks1();
+        for (uint32_t i = 0; i < nb; ++i) {
+          const uint32_t radix = byte_of(in[i], 3);
+          if (radix < 128) *link[radix]++ = in[i];
+          else *(--link[radix]) = in[i];
+        }
+      }
+      swap();
+    } else if (unique >= 128) {   // all negative: the order reversed
+      uint32_t* out = ranks2();
+      if (!valid) {
+        for (uint32_t i = 0; i < nb; ++i) out[i] = nb - i - 1;
+        valid = true;
+      } else {
+        const uint32_t* in = ranks1();
+        for (uint32_t i = 0; i < nb; ++i) out[i] = in[nb - i - 1];
+      }
+      swap();
+    }
+  }
+  return ranks1();
+}
+// collideGeomsNoAABBs (collision_sapspace.cpp:234-257): collideAABBs without
+// the box overlap test, which the sweep has done
+static void sap_collide_pair(dxGeom* g1, dxGeom* g2, void* data, dNearCallback* cb) {
+  if (g1->body == g2->body && g1->body) return;
+  if (((g1->category_bits & g2->collide_bits) || (g2->category_bits & g1->collide_bits)) == 0) return;
+  const dGeomClass* u1 = user_class_of(g1);
+  const dGeomClass* u2 = user_class_of(g2);
+  if (u1 && u1->aabb_test && u1->aabb_test(g1, g2, g2->aabb) == 0) return;
+  if (u2 && u2->aabb_test && u2->aabb_test(g2, g1, g1->aabb) == 0) return;
+  cb(data, g1, g2);
+}
+// dxSAPSpace::collide and BoxPruning (collision_sapspace.cpp:425-496,
+// :521-575): enabled geoms split by an infinite upper bound on the first
+// axis; the finite ones sorted by their lower bound on it and swept, each
+// against the ones that start before it ends, kept when the other two axes
+// overlap; then the infinite ones against each other and against the rest
+static void sap_collide(dxSpace* sp, void* data, dNearCallback* cb) {
+  space_clean(sp);
+  SapSpace& S = *sp->sap;
+  S.tmp.clear();
+  S.tmp_inf.clear();
+  for (dxGeom* g : S.geoms) {
+    if (!geom_enabled(g)) continue;
+    (g->aabb[S.ax0 + 1] == INFINITY ? S.tmp_inf : S.tmp).push_back(g);
+  }
+  std::vector<std::pair<uint32_t, uint32_t>> overlap;
+  const uint32_t n = (uint32_t)S.tmp.size();
+  if (n > 0) {
+    S.pos.resize(n + 1);
+    for (uint32_t i = 0; i < n; ++i) S.pos[i] = (float)S.tmp[i]->aabb[S.ax0];
+    S.pos[n] = FLT_MAX;
+    const uint32_t count = n + 1;
+    const uint32_t* sorted = S.sorter.sort(S.pos.data(), count);
+    const uint32_t* last = sorted + count;
+    const uint32_t* running = sorted;
+    while (running < last && sorted < last) {
+      const uint32_t id0 = *sorted++;
+      while (S.pos[*running++] < S.pos[id0]) {
+      }
+      if (running < last) {
+        const uint32_t* running2 = running;
+        const dReal* a0 = S.tmp[id0]->aabb;
+        const dReal max0 = a0[S.ax0 + 1], max1 = a0[S.ax1 + 1], max2 = a0[S.ax2 + 1];
+        uint32_t id1;
+        while (S.pos[id1 = *running2++] <= max0) {
+          const dReal* a1 = S.tmp[id1]->aabb;
+          if (max1 >= a1[S.ax1] && a1[S.ax1 + 1] >= a0[S.ax1] && max2 >= a1[S.ax2] && a1[S.ax2 + 1] >= a0[S.ax2])
+            overlap.push_back({id0, id1});
+        }
+      }
+    }
+  }
+  for (const auto& pr : overlap) sap_collide_pair(S.tmp[pr.first], S.tmp[pr.second], data, cb);
+  for (size_t m = 0; m < S.tmp_inf.size(); ++m) {
+    for (size_t k = m + 1; k < S.tmp_inf.size(); ++k) sap_collide_pair(S.tmp_inf[m], S.tmp_inf[k], data, cb);
+    for (dxGeom* g2 : S.tmp) sap_collide_pair(S.tmp_inf[m], g2, data, cb);
+  }
+}
 static void space_collide(dxSpace* sp, void* data, dNearCallback* cb) {
-  if (sp->qt) {
+  if (sp->sap) {
+    sap_collide(sp, data, cb);
+  } else if (sp->qt) {
     space_clean(sp);
     quad_collide_block(*sp->qt, 0, data, cb);
   } else if (sp->type == dHashSpaceClass) {
@@ -2627,6 +2887,18 @@ static void quad_build(QuadTree& q, int b, dReal minx, dReal maxx, dReal miny, d
       quad_build(q, c + k++, left_x, right_x, left_y, right_y, b, depth - 1);
     }
   }
+}
+// dSweepAndPruneSpaceCreate (collision_sapspace.cpp:210-213, :261-276): the
+// sweep axis and the two test axes from the axis order's three 2-bit fields
+dSpaceID dSweepAndPruneSpaceCreate(dSpaceID space, int axisorder) {
+  auto* S = new SapSpace();
+  S->ax0 = (axisorder & 3) << 1;
+  S->ax1 = ((axisorder >> 2) & 3) << 1;
+  S->ax2 = ((axisorder >> 4) & 3) << 1;
+  dSpaceID sp = new_space(nullptr, dSweepAndPruneSpaceClass);
+  sp->sap = S;
+  if (space) space_add(space, sp);
+  return sp;
 }
 dSpaceID dQuadTreeSpaceCreate(dSpaceID space, const dVector3 Center, const dVector3 Extents, int Depth) {
   auto* q = new QuadTree();
@@ -2664,6 +2936,11 @@ int dSpaceGetNumGeoms(dSpaceID space) { return space->count; }
 dGeomID dSpaceGetGeom(dSpaceID space, int i) {   // dxSpace::getGeom (collision_space.cpp:131-149)
   // ODE 0.12 leaves the quadtree's enumeration unimplemented (:412-483)
   if (i < 0 || space->qt) return nullptr;
+  if (space->sap) {   // dxSAPSpace::getGeom (:293-301): the dirty list, then the clean one
+    const int nd = (int)space->sap->dirty.size();
+    if (i < nd) return space->sap->dirty[i];
+    return i - nd < (int)space->sap->geoms.size() ? space->sap->geoms[i - nd] : nullptr;
+  }
   dxGeom* g = space->first;
   for (int j = 0; j < i && g; ++j) g = g->next;
   return g;

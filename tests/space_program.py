@@ -94,7 +94,13 @@ def ops_program(lib, seed, kind="hash", n_ops=60):
     cb = NEAR(lambda d, a, b: pairs.append((ids(a), ids(b))))
     lib.dInitODE2(0)
     w = lib.dWorldCreate()
-    top = ids.add((lib.dHashSpaceCreate if kind == "hash" else lib.dSimpleSpaceCreate)(None))
+    if kind == "sap":
+        lib.dSweepAndPruneSpaceCreate.restype = P
+        lib.dSweepAndPruneSpaceCreate.argtypes = [P, I]
+        axes = [0 | (1 << 2) | (2 << 4), 2 | (1 << 2) | (0 << 4), 1 | (2 << 2) | (0 << 4)][seed % 3]
+        top = ids.add(lib.dSweepAndPruneSpaceCreate(None, axes))
+    else:
+        top = ids.add((lib.dHashSpaceCreate if kind == "hash" else lib.dSimpleSpaceCreate)(None))
     if kind == "hash":
         lib.dHashSpaceSetLevels(top, int(rng.integers(-4, 0)), int(rng.integers(1, 6)))
     sub = ids.add(lib.dSimpleSpaceCreate(top))
@@ -350,3 +356,37 @@ def quad_program(lib, seed, n_ops=60):
         lib.dGeomDestroy(g)
     lib.dWorldDestroy(w)
     return np.array(rec, dtype=np.float64)
+
+
+def sap_tie_program(lib, seed, n_rounds=12):
+    """A sweep-and-prune space where many boxes share their lower bound on the
+    sweep axis, negative ones included, collided again and again while a few
+    move: the order of equal keys out of the radix sort, which depends on the
+    previous sorts, sets the pair order."""
+    rng = np.random.default_rng(seed)
+    ids = _Ids()
+    pairs = []
+    cb = NEAR(lambda d, a, b: pairs.append((ids(a), ids(b))))
+    lib.dInitODE2(0)
+    lib.dSweepAndPruneSpaceCreate.restype = P
+    lib.dSweepAndPruneSpaceCreate.argtypes = [P, I]
+    sp = ids.add(lib.dSweepAndPruneSpaceCreate(None, 0 | (1 << 2) | (2 << 4)))
+    xs = [-2.5, -1.0, -0.25, 0.0, 0.5, 1.75]
+    geoms = []
+    for _ in range(30):
+        g = ids.add(lib.dCreateBox(sp, 1.0, float(rng.uniform(0.2, 1.0)), float(rng.uniform(0.2, 1.0))))
+        lib.dGeomSetPosition(g, float(rng.choice(xs)), float(rng.uniform(-1, 1)), float(rng.uniform(-1, 1)))
+        geoms.append(g)
+    rec = []
+    for _ in range(n_rounds):
+        for g in rng.choice(len(geoms), size=3, replace=False):
+            lib.dGeomSetPosition(geoms[int(g)], float(rng.choice(xs)), float(rng.uniform(-1, 1)),
+                                 float(rng.uniform(-1, 1)))
+        pairs.clear()
+        lib.dSpaceCollide(sp, None, cb)
+        rec += [len(pairs)] + [x for pr in pairs for x in pr] + _order(lib, ids, sp)
+        pairs.clear()
+        lib.dSpaceCollide(sp, None, cb)   # again with nothing moved: the previous order is kept
+        rec += [len(pairs)] + [x for pr in pairs for x in pr]
+    lib.dSpaceDestroy(sp)
+    return np.array(rec, dtype=np.int64)

@@ -24,7 +24,7 @@ def _libs():
     return ours, ref
 
 
-@pytest.mark.parametrize("kind", ["simple", "hash"])
+@pytest.mark.parametrize("kind", ["simple", "hash", "sap"])
 def test_space_pairs_and_orders_match_reference(kind):
     ours, ref = _libs()
     n_pairs = 0
@@ -78,3 +78,16 @@ def test_quadtree_space_pairs_match_reference():
     ours.dCreateSphere(q, 0.2)
     assert ours.dSpaceGetNumGeoms(q) == 1 and ours.dSpaceGetGeom(q, 0) is None
     ours.dSpaceDestroy(q)
+
+
+def test_sap_space_tie_order_matches_reference():
+    """Sweep and prune (ode/src/collision_sapspace.cpp) with many equal sort
+    keys, negative ones included, over repeated collides: the radix sort's
+    order of equal keys and its reuse of the previous order give the
+    reference's pairs entry for entry."""
+    ours, ref = _libs()
+    for seed in range(10):
+        a, b = SP.sap_tie_program(ours, seed), SP.sap_tie_program(ref, seed)
+        m = min(len(a), len(b))
+        assert a.shape == b.shape and np.array_equal(a, b), (seed, int(np.argmax(a[:m] != b[:m])))
+        assert len(a) > 500
