@@ -551,6 +551,9 @@ enum { dGeomCommonControlClass = 0, dGeomColliderControlClass = 1 };     /* :412
 int dGeomLowLevelControl(dGeomID g, int controlClass, int controlCode, void* dataValue, int* dataSize);  /* :460 */
 void dClosestLineSegmentPoints(const dVector3 a1, const dVector3 a2, const dVector3 b1, const dVector3 b2,
                                dVector3 cp1, dVector3 cp2);              /* :1466 */
+int dBoxBox(const dVector3 p1, const dMatrix3 R1, const dVector3 side1, const dVector3 p2, const dMatrix3 R2,
+            const dVector3 side2, dVector3 normal, dReal* depth, int* return_code, int flags,
+            dContactGeom* contact, int skip);                           /* :1475 */
 int dBoxTouchesBox(const dVector3 p1, const dMatrix3 R1, const dVector3 side1, const dVector3 p2,
                    const dMatrix3 R2, const dVector3 side2);             /* :1470 */
 dSpaceID dGeomGetSpace(dGeomID g);                                       /* :283 */

@@ -209,9 +209,12 @@ OG_HD void cull_points(int n, const float p[], int m, int i0, int iret[]) {
 
 // dBoxBox (ode/src/box.cpp:331-713): separating-axis test over 15 axes (1.05
 // fudge on the edge axes), then edge-edge or face clipping + culling.
+// depth_out / code_out (for the ODE API's dBoxBox): the deepest penetration
+// once the normal is known, and the contact's code on the paths that make
+// contacts, as box.cpp:461, :501, :710 set them.
 OG_HD int box_box(const float* p1, const float* R1, const float* side1, const float* p2,
                   const float* R2, const float* side2, float* normal, unsigned flags,
-                  Contact* contact) {
+                  Contact* contact, float* depth_out = nullptr, int* code_out = nullptr) {
   const float fudge_factor = 1.05f;
   float p[3], pp[3], normalC[3] = {0.f, 0.f, 0.f};
   const float* normalR = nullptr;
@@ -278,6 +281,7 @@ OG_HD int box_box(const float* p1, const float* R1, const float* side1, const fl
     mul0_331(normal, R1, normalC);
   }
   if (invert_normal) { normal[0] = -normal[0]; normal[1] = -normal[1]; normal[2] = -normal[2]; }
+  if (depth_out) *depth_out = -s;
   const float depth = -s;
   int i, j;
   if (code > 6) {
@@ -299,6 +303,7 @@ OG_HD int box_box(const float* p1, const float* R1, const float* side1, const fl
     for (i = 0; i < 3; i++) pb[i] += ub[i] * beta;
     for (i = 0; i < 3; i++) contact[0].pos[i] = 0.5f * (pa[i] + pb[i]);
     contact[0].depth = depth;
+    if (code_out) *code_out = code;
     return 1;
   }
   const float *Ra, *Rb, *pa, *pb, *Sa, *Sb;
@@ -385,6 +390,7 @@ OG_HD int box_box(const float* p1, const float* R1, const float* side1, const fl
     }
     cnum = maxc;
   }
+  if (code_out) *code_out = code;
   return cnum;
 }
 

@@ -2215,6 +2215,13 @@ void closest_segment_points_host(const float* a1, const float* a2, const float* 
   closest_segment_points(a1, a2, b1, b2, cp1, cp2);
 }
 
+// dBoxBox for the ODE API: the box-box collider run on the host (it is
+// __host__ __device__), with its normal, depth and code
+int box_box_host(const float* p1, const float* R1, const float* side1, const float* p2, const float* R2,
+                 const float* side2, float* normal, float* depth, int* code, unsigned flags, Contact* out) {
+  return box_box(p1, R1, side1, p2, R2, side2, normal, flags, out, depth, code);
+}
+
 int collide_pair_gpu(const GeomView& a, const GeomView& b, unsigned flags, Contact* out) {
   Contact* d_c = nullptr;
   int* d_n = nullptr;

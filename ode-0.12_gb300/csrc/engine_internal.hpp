@@ -63,6 +63,9 @@ int ctx_step(WorldCtx* c, HostWorld& hw);
 // __host__ __device__ routine), for dClosestLineSegmentPoints.
 void closest_segment_points_host(const float* a1, const float* a2, const float* b1, const float* b2, float* cp1,
                                  float* cp2);
+// The box-box collider on the host, for dBoxBox (at most 8 contacts).
+int box_box_host(const float* p1, const float* R1, const float* side1, const float* p2, const float* R2,
+                 const float* side2, float* normal, float* depth, int* code, unsigned flags, Contact* out);
 // One dCollide on the GPU. Returns the contact count (<= 8) or a negative code.
 int collide_pair_gpu(const GeomView& a, const GeomView& b, unsigned flags, Contact* out);
 // Heightfields for the ODE API: the dxHeightfieldData caches, the device copy

@@ -2212,6 +2212,24 @@ void dClosestLineSegmentPoints(const dVector3 a1, const dVector3 a2, const dVect
                                dVector3 cp1, dVector3 cp2) {
   og::closest_segment_points_host(a1, a2, b1, b2, cp1, cp2);
 }
+// dBoxBox (box.cpp:331-713): the box-box collider itself, returning the
+// normal, the deepest penetration and the contact code with its contacts'
+// positions and depths (at most 8; the caller fills the rest of each record)
+int dBoxBox(const dVector3 p1, const dMatrix3 R1, const dVector3 side1, const dVector3 p2, const dMatrix3 R2,
+            const dVector3 side2, dVector3 normal, dReal* depth, int* return_code, int flags, dContactGeom* contact,
+            int skip) {
+  if ((flags & 0xffff) == 0) return 0;
+  unsigned f = (unsigned)flags;
+  if ((f & 0xffff) > 8) f = (f & ~0xffffu) | 8u;
+  og::Contact out[8];
+  const int n = og::box_box_host(p1, R1, side1, p2, R2, side2, normal, depth, return_code, f, out);
+  for (int i = 0; i < n; ++i) {
+    dContactGeom* c = (dContactGeom*)((char*)contact + (size_t)i * skip);
+    for (int k = 0; k < 3; ++k) c->pos[k] = out[i].pos[k];
+    c->depth = out[i].depth;
+  }
+  return n;
+}
 // dBoxTouchesBox (collision_util.cpp:388-449): the fifteen separating axes
 // of two boxes (the three faces of each, the nine edge pairs) after
 // Gottschalk, Lin and Manocha's OBB tree test, in box 1's frame, with
