@@ -386,6 +386,7 @@ int dJointGetAMotorNumAxes(dJointID j);                                  /* :284
 void dJointGetAMotorAxis(dJointID j, int anum, dVector3 result);         /* :2851 */
 int dJointGetAMotorAxisRel(dJointID j, int anum);                        /* :2869 */
 dReal dJointGetAMotorAngle(dJointID j, int anum);                        /* :2879 */
+dReal dJointGetAMotorAngleRate(dJointID j, int anum);                    /* :2889, 0 (unimplemented in ODE 0.12) */
 dReal dJointGetAMotorParam(dJointID j, int parameter);                   /* :2895 */
 int dJointGetAMotorMode(dJointID j);                                     /* :2910 */
 int dAreConnectedExcluding(dBodyID b1, dBodyID b2, int joint_type);      /* :2968 */

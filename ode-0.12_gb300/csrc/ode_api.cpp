@@ -1398,6 +1398,9 @@ void dJointGetAMotorAxis(dJointID j, int anum, dVector3 r) {
   else if (H.am_rel[anum] == 2) world_axis2(j, H.am_axis[anum], r);
   else for (int k = 0; k < 3; ++k) r[k] = (dReal)H.am_axis[anum][k];
 }
+// ODE 0.12 leaves this unimplemented (amotor.cpp:445-451 stops in dDebug);
+// here it answers 0
+dReal dJointGetAMotorAngleRate(dJointID, int) { return 0; }
 dReal dJointGetAMotorAngle(dJointID j, int anum) {
   // user mode: the angle set; Euler mode: the angles of the bodies' current
   // placement (the reference returns those its last getInfo1 computed)
